@@ -1,0 +1,129 @@
+/*
+ * femoracle — CPU restatement of the solve path of PARALLEL_FEM_CODES.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the GPU
+ * library (libfemgpu): tests, the smoke entry point and the CPU-baseline
+ * leg of the benchmark call it; the product path never does.
+ *
+ * Every function restates one reference routine with single-rank
+ * (NPROC = 1) semantics: neq_bef = 0 and NEQ = neq, so every vector has
+ * NEQ + 1 slots and slot NEQ is the Dirichlet sink that must read 0.
+ * The restatement is pinned against the reference's own C compiled from
+ * its sources (oracle/ref_harness) by tests/test_oracle_pin.py.
+ *
+ * Element blocks are stored as the reference stores them: element e owns
+ * S*S doubles, row-major, at A[e*S*S] (ebe_assembly.c:9-17), and the
+ * element->equation map lm[e*S + k] (Fill_LM.c).
+ */
+#ifndef FEMORACLE_H
+#define FEMORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- mesh (Mesh_Generator/Structured_Mesh/meshGenerator.c:113-177) ---- */
+int  or_mesh_structured(int M, int N, double x0, double y0, double x1, double y1,
+                        int left_tilt, double *x, double *y, int *ien);
+
+/* ---- numbering and connectivity ---- */
+/* Fill_LM for NDOF dofs per node (01_SS_.../Fill_LM.c:3-27, 03_Euler_.../Fill_LM.c:3-31).
+ * type[node*ndof+k] == 0 marks a Dirichlet dof; invp[node*ndof+k] its equation. */
+void or_fill_lm(int nel, int ndof, const int *ien, const int *type, const int *invp,
+                int NEQ, int *lm);
+
+/* Adjacency of the free dofs of 1-dof meshes, sorted rows without duplicates
+ * (Permutation_of_LM.c:21-49 + insertNode/mount_IA_JA :78-143).
+ * IA has NEQ+1 entries; JA must hold up to nel*9 entries. Returns nnz. */
+int  or_lm_adjacency(int nel, const int *ien, const int *type, const int *invp,
+                     int NEQ, int *IA, int *JA);
+
+/* Reverse Cuthill-McKee (00_CommonFiles/Reordering/symrcm.c:4-237). */
+void or_symrcm(int n, const int *IA, const int *JA, int *perm);
+
+/* Permutation_of_LM: adjacency + RCM + inverse (Permutation_of_LM.c:8-76).
+ * Perm and invPerm have NEQ+1 entries; Perm[NEQ] = invPerm[NEQ] = NEQ.
+ * bandwidth[0..1] receives MATRIX_bandwidth before and after (may be NULL). */
+int  or_permutation_of_lm(int nel, const int *ien, const int *type, const int *invp,
+                          int NEQ, int *Perm, int *invPerm, int *bandwidth);
+
+/* MATRIX_bandwidth with the reference's stray ';' (reordering.c:215-236). */
+int  or_matrix_bandwidth(int n, const int *IA, const int *JA);
+
+/* ---- BLAS-1 (00_CommonFiles/BLAS_Operations) ---- */
+double or_ddot(int n, const double *x, const double *y);
+
+/* ---- EBE matvec ---- */
+/* ebemv: 3x3 blocks through the local RCM permutation (EBE/ebemv.c:4-64). */
+void or_ebemv3_perm(int nel, const int *lm, const double *A, const int *Perm,
+                    const int *invPerm, int NEQ, const double *P, double *Q);
+/* ebemvNDOF3 / ebemvNDOF4 / ebemv without permutation, S = 3, 9 or 12
+ * (EBE/ebemvNDOF3.c:3-92, EBE/ebemvNDOF4.c:4-121). Q is zeroed first. */
+void or_ebemv(int nel, int S, const int *lm, const double *A, int NEQ,
+              const double *P, double *Q);
+
+/* ---- preconditioners ---- */
+/* Diag_precond_EBE_setup: Diag accumulates (never zeroed, as in the
+ * reference), invDiag = 1/Diag, F *= invDiag (EBE/Diag_precond_EBE_setup.c:3-32). */
+void or_diag_setup(int nel, int S, const int *lm, const double *A, int NEQ,
+                   double *Diag, double *invDiag, double *F);
+void or_diag_apply(int n, const double *invDiag, const double *p, double *z);
+
+/* Nodal block-diagonal (B = NDOF = 3 or 4): gather the B x B diagonal blocks
+ * of every element node (EBE/BlockDiag_precond_EBE_setup.c:57-80,
+ * EBE/BlockDiagDOF3_precond_EBE_setup.c), invert with the reference's
+ * closed-form cofactors (matrix_Inverse :90-147, DOF3_matrix_Inverse :84-124),
+ * then F <- B^-1 F.  Id[node*B+k] is the equation of dof k (NEQ = sink).
+ * ref_quirks != 0 reproduces the reference's 4x4 inverse term for entry 14. */
+void or_blockdiag_setup(int nnodes, int nel, int B, const int *ien, const double *A,
+                        const int *Id, int NEQ, int ref_quirks,
+                        double *BlockDiag, double *invBlockDiag, double *F);
+void or_blockdiag_apply(int nnodes, int B, const int *Id, int NEQ,
+                        const double *invBlockDiag, double *p, double *z);
+
+/* ---- GMRES (Solvers_and_Preconditioners/pgmres.c:5-200) ---- */
+typedef int (*or_mv_fn)(void *ctx, double *P, double *Q);      /* Q = A P, vectors NEQ+1 */
+typedef int (*or_pc_fn)(void *ctx, double *p, double *z);      /* owned slice, may alias */
+int or_pgmres(int NEQ, int kmax, int lmax, double tol,
+              or_mv_fn mv, or_pc_fn precond, void *ctx,
+              double *B, double *X, int *iterations);
+
+/* ---- steady SUPG/CAU transport (01_SS_Transport_Equation) ---- */
+typedef struct {
+    double k;            /* Condutivity() for kx and ky                      */
+    double gamma;        /* Reaction()                                       */
+    double beta[2];      /* Velocity(): constant field                       */
+    double f;            /* Font(): constant source                          */
+    const double *upresc;/* Dirichlet value per node (read where type == 0)  */
+    int cau;             /* 1: CAU shock capture, 0: none                    */
+} or_transport_problem;
+
+/* Build_K_F_SUPG + CAU_ShockCapture + h_shock_2sqrtArea + F_assembly +
+ * ebe_assembly (Build_K_F_SUPG.c:4-187).  u is the current solution of the
+ * free dofs (length neq).  A receives 9 doubles per element, f neq doubles. */
+void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
+                       const int *type, const int *invp, const int *ien, int neq,
+                       const or_transport_problem *prob, const double *u,
+                       double *A, double *f);
+
+/* Steady transport Process loop (01_SS_.../Process.c:6-93) with EBE storage,
+ * ebemv with local RCM, Diag preconditioner and GMRES.  U has NEQ+1 slots and
+ * holds the result.  Returns the number of nonlinear iterations. */
+int or_transport_process(int nnodes, int nel, const double *x, const double *y,
+                         const int *type, const int *invp, const int *ien, int neq,
+                         const or_transport_problem *prob,
+                         double solver_tol, double nonlinear_tol, int kmax, int lmax,
+                         int max_nonlinear, double *U, int *gmres_iterations);
+
+/* One linear solve of an assembled EBE system with Diag preconditioning:
+ * setup (accumulating Diag as the reference does), then pgmres.  With
+ * Perm == NULL the unpermuted matvec is used.  Returns GMRES iterations. */
+int or_ebe_diag_solve(int nel, int S, const int *lm, const double *A, int NEQ,
+                      const int *Perm, const int *invPerm,
+                      double *Diag, double *invDiag, double *F,
+                      int kmax, int lmax, double tol, double *X);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

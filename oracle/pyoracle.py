@@ -1,0 +1,310 @@
+"""ctypes bindings of the oracle (CPU restatement) and of the reference build.
+
+TEST INFRASTRUCTURE ONLY: used by tests/, __graft_entry__.smoke() and the
+cpu_baseline / reference legs of bench.py.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libfemoracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref_sst.so")
+REF_SRC = "/root/reference"
+
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_c_int, _c_dbl = ctypes.c_int, ctypes.c_double
+
+
+def build(ref: bool | None = None) -> None:
+    """Compile the restatement, and the reference build when its sources exist."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref is None:
+        ref = os.path.isdir(REF_SRC)
+    if ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build(ref=False)
+        L = ctypes.CDLL(ORACLE_SO)
+        L.or_mesh_structured.argtypes = [_c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _f64p, _f64p, _i32p]
+        L.or_fill_lm.argtypes = [_c_int, _c_int, _i32p, _i32p, _i32p, _c_int, _i32p]
+        L.or_fill_lm.restype = None
+        L.or_lm_adjacency.argtypes = [_c_int, _i32p, _i32p, _i32p, _c_int, _i32p, _i32p]
+        L.or_symrcm.argtypes = [_c_int, _i32p, _i32p, _i32p]
+        L.or_symrcm.restype = None
+        L.or_permutation_of_lm.argtypes = [_c_int, _i32p, _i32p, _i32p, _c_int, _i32p, _i32p, _i32p]
+        L.or_ddot.argtypes = [_c_int, _f64p, _f64p]
+        L.or_ddot.restype = _c_dbl
+        L.or_ebemv3_perm.argtypes = [_c_int, _i32p, _f64p, _i32p, _i32p, _c_int, _f64p, _f64p]
+        L.or_ebemv3_perm.restype = None
+        L.or_ebemv.argtypes = [_c_int, _c_int, _i32p, _f64p, _c_int, _f64p, _f64p]
+        L.or_ebemv.restype = None
+        L.or_diag_setup.argtypes = [_c_int, _c_int, _i32p, _f64p, _c_int, _f64p, _f64p, _f64p]
+        L.or_diag_setup.restype = None
+        L.or_blockdiag_setup.argtypes = [_c_int, _c_int, _c_int, _i32p, _f64p, _i32p, _c_int, _c_int, _f64p, _f64p, _f64p]
+        L.or_blockdiag_setup.restype = None
+        L.or_blockdiag_apply.argtypes = [_c_int, _c_int, _i32p, _c_int, _f64p, _f64p, _f64p]
+        L.or_blockdiag_apply.restype = None
+        L.or_build_k_f_supg.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                        ctypes.c_void_p, _f64p, _f64p, _f64p]
+        L.or_build_k_f_supg.restype = None
+        L.or_transport_process.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                           ctypes.c_void_p, _c_dbl, _c_dbl, _c_int, _c_int, _c_int,
+                                           _f64p, ctypes.POINTER(_c_int)]
+        L.or_ebe_diag_solve.argtypes = [_c_int, _c_int, _i32p, _f64p, _c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        _f64p, _f64p, _f64p, _c_int, _c_int, _c_dbl, _f64p]
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def ref():
+    """The reference's own C (oracle/_ref), or None where it was not built."""
+    global _ref
+    if _ref is None and ref_available():
+        R = ctypes.CDLL(REF_SO)
+        R.fr_sst_connectivity.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                          _i32p, _i32p, _i32p, _i32p]
+        R.fr_sst_build.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                   _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_dbl, _f64p, _f64p, _f64p]
+        R.fr_sst_build.restype = None
+        R.fr_sst_process.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                     _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_dbl, _c_dbl, _c_dbl,
+                                     _c_int, _c_int, _f64p, ctypes.POINTER(_c_int)]
+        R.fr_ebemv.argtypes = [_c_int, _c_int, _i32p, _f64p, _i32p, _i32p, _f64p, _f64p]
+        R.fr_ebemv.restype = None
+        R.fr_diag_pgmres.argtypes = [_c_int, _c_int, _i32p, _f64p, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p,
+                                     _c_int, _c_int, _c_dbl]
+        R.fr_symrcm.argtypes = [_c_int, _c_int, _i32p, _i32p, _i32p]
+        R.fr_symrcm.restype = None
+        R.fr_sst_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
+        R.fr_sst_layout.restype = None
+        _ref = R
+    return _ref
+
+
+# ---------------------------------------------------------------- helpers
+class _Problem(ctypes.Structure):
+    _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl),
+                ("upresc", ctypes.POINTER(_c_dbl)), ("cau", _c_int)]
+
+
+def _mesh_args(m):
+    return (m.nnodes, m.nel, np.ascontiguousarray(m.x), np.ascontiguousarray(m.y),
+            np.ascontiguousarray(m.type, dtype=np.int32), np.ascontiguousarray(m.invp, dtype=np.int32),
+            np.ascontiguousarray(m.ien, dtype=np.int32).reshape(-1), m.neq)
+
+
+def _problem_struct(p):
+    up = np.ascontiguousarray(p.upresc, dtype=np.float64)
+    s = _Problem(p.k, p.gamma, (_c_dbl * 2)(*p.beta), p.f,
+                 up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(p.cau))
+    return s, up
+
+
+def fill_lm(mesh) -> np.ndarray:
+    S = 3 * mesh.ndof
+    lm = np.empty(mesh.nel * S, dtype=np.int32)
+    lib().or_fill_lm(mesh.nel, mesh.ndof, np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1),
+                     mesh.type, mesh.invp, mesh.neq, lm)
+    return lm.reshape(mesh.nel, S)
+
+
+def permutation_of_lm(mesh):
+    """(Perm, invPerm, bandwidth[2]) of the local RCM (Permutation_of_LM.c)."""
+    n = mesh.neq
+    perm = np.empty(n + 1, dtype=np.int32)
+    inv = np.empty(n + 1, dtype=np.int32)
+    band = np.zeros(2, dtype=np.int32)
+    lib().or_permutation_of_lm(mesh.nel, np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1),
+                               mesh.type, mesh.invp, n, perm, inv, band)
+    return perm, inv, band
+
+
+def adjacency(mesh):
+    n = mesh.neq
+    IA = np.empty(n + 1, dtype=np.int32)
+    JA = np.empty(mesh.nel * 9 + 1, dtype=np.int32)
+    nnz = lib().or_lm_adjacency(mesh.nel, np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1),
+                                mesh.type, mesh.invp, n, IA, JA)
+    return IA, JA[:nnz].copy()
+
+
+def symrcm(IA, JA) -> np.ndarray:
+    n = IA.shape[0] - 1
+    p = np.empty(max(n, 1), dtype=np.int32)
+    lib().or_symrcm(n, np.ascontiguousarray(IA, dtype=np.int32), np.ascontiguousarray(JA, dtype=np.int32), p)
+    return p[:n]
+
+
+def build_k_f_supg(prob, u=None):
+    m = prob.mesh
+    if u is None:
+        u = np.zeros(m.neq, dtype=np.float64)
+    A = np.empty(m.nel * 9, dtype=np.float64)
+    F = np.empty(m.neq + 1, dtype=np.float64)
+    s, keep = _problem_struct(prob)
+    lib().or_build_k_f_supg(*_mesh_args(m), ctypes.byref(s), np.ascontiguousarray(u, dtype=np.float64), A, F)
+    F[m.neq] = 0.0
+    return A.reshape(m.nel, 9), F
+
+
+def ebemv3_perm(lm, A, perm, inv, P):
+    nel = lm.shape[0]
+    n = perm.shape[0] - 1
+    Q = np.zeros(n + 1, dtype=np.float64)
+    lib().or_ebemv3_perm(nel, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1),
+                         np.ascontiguousarray(A, dtype=np.float64).reshape(-1), perm, inv, n,
+                         np.ascontiguousarray(P, dtype=np.float64), Q)
+    return Q
+
+
+def ebemv(lm, A, NEQ, P):
+    nel, S = lm.shape
+    Q = np.zeros(NEQ + 1, dtype=np.float64)
+    lib().or_ebemv(nel, S, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1),
+                   np.ascontiguousarray(A, dtype=np.float64).reshape(-1), NEQ,
+                   np.ascontiguousarray(P, dtype=np.float64), Q)
+    return Q
+
+
+def diag_setup(lm, A, NEQ, F, Diag=None):
+    nel, S = lm.shape
+    Diag = np.zeros(NEQ + 1) if Diag is None else Diag
+    invDiag = np.zeros(NEQ + 1)
+    F = np.array(F, dtype=np.float64, copy=True)
+    lib().or_diag_setup(nel, S, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1),
+                        np.ascontiguousarray(A, dtype=np.float64).reshape(-1), NEQ, Diag, invDiag, F)
+    return Diag, invDiag, F
+
+
+def blockdiag_setup(mesh, A, F, ref_quirks=True):
+    """Nodal block-diagonal setup; returns (BlockDiag, invBlockDiag, Id, F')."""
+    B = mesh.ndof
+    Id = np.where(mesh.type == 0, mesh.neq, mesh.invp).astype(np.int32)
+    bd = np.zeros(mesh.nnodes * B * B)
+    ibd = np.zeros(mesh.nnodes * B * B)
+    F = np.array(F, dtype=np.float64, copy=True)
+    lib().or_blockdiag_setup(mesh.nnodes, mesh.nel, B, np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1),
+                             np.ascontiguousarray(A, dtype=np.float64).reshape(-1), Id, mesh.neq,
+                             int(ref_quirks), bd, ibd, F)
+    return bd, ibd, Id, F
+
+
+def blockdiag_apply(mesh, ibd, Id, p):
+    p = np.array(p, dtype=np.float64, copy=True)
+    z = np.zeros_like(p)
+    lib().or_blockdiag_apply(mesh.nnodes, mesh.ndof, Id, mesh.neq, ibd, p, z)
+    return z
+
+
+def ebe_diag_solve(lm, A, NEQ, F, perm=None, inv=None, Diag=None, kmax=30, lmax=1000, tol=1e-10):
+    """Diag setup + pgmres; returns (X, iterations, Diag, invDiag, F')."""
+    nel, S = lm.shape
+    Diag = np.zeros(NEQ + 1) if Diag is None else Diag
+    invDiag = np.zeros(NEQ + 1)
+    F = np.array(F, dtype=np.float64, copy=True)
+    X = np.zeros(NEQ + 1)
+    pp = perm.ctypes.data if perm is not None else None
+    ip = inv.ctypes.data if inv is not None else None
+    it = lib().or_ebe_diag_solve(nel, S, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1),
+                                 np.ascontiguousarray(A, dtype=np.float64).reshape(-1), NEQ,
+                                 pp, ip, Diag, invDiag, F, kmax, lmax, tol, X)
+    return X, it, Diag, invDiag, F
+
+
+def transport_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=1000):
+    """Steady transport Process loop; returns (U[neq], nonlinear its, GMRES its)."""
+    m = prob.mesh
+    U = np.zeros(m.neq + 1)
+    its = _c_int(0)
+    s, keep = _problem_struct(prob)
+    nl = lib().or_transport_process(*_mesh_args(m), ctypes.byref(s), solver_tol, nonlinear_tol,
+                                    kmax, lmax, max_nonlinear, U, ctypes.byref(its))
+    return U[:m.neq].copy(), nl, its.value
+
+
+# ------------------------------------------------------- reference build
+def ref_connectivity(mesh):
+    R = ref()
+    n = mesh.neq
+    lm = np.empty(mesh.nel * 3, dtype=np.int32)
+    perm = np.empty(n + 1, dtype=np.int32)
+    inv = np.empty(n + 1, dtype=np.int32)
+    band = np.zeros(2, dtype=np.int32)
+    nnz = R.fr_sst_connectivity(*_mesh_args(mesh), lm, perm, inv, band)
+    return lm.reshape(mesh.nel, 3), perm, inv, band, nnz
+
+
+def ref_build(prob, u=None):
+    m = prob.mesh
+    if u is None:
+        u = np.zeros(m.neq)
+    A = np.empty(m.nel * 9)
+    F = np.empty(m.neq + 1)
+    F[m.neq] = 0.0
+    ref().fr_sst_build(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f,
+                       prob.upmode, prob.upval, np.ascontiguousarray(u, dtype=np.float64), A, F)
+    return A.reshape(m.nel, 9), F
+
+
+def ref_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000):
+    m = prob.mesh
+    U = np.zeros(m.neq + 1)
+    its = _c_int(0)
+    ref().fr_sst_process(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f,
+                         prob.upmode, prob.upval, solver_tol, nonlinear_tol, kmax, lmax, U, ctypes.byref(its))
+    return U[:m.neq].copy(), its.value
+
+
+def ref_ebemv(lm, A, perm, inv, P):
+    nel = lm.shape[0]
+    n = perm.shape[0] - 1
+    Q = np.zeros(n + 1)
+    ref().fr_ebemv(nel, n, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1),
+                   np.ascontiguousarray(A, dtype=np.float64).reshape(-1), perm, inv,
+                   np.ascontiguousarray(P, dtype=np.float64), Q)
+    return Q
+
+
+def ref_diag_pgmres(lm, A, perm, inv, F, kmax=30, lmax=1000, tol=1e-10, Diag=None):
+    nel = lm.shape[0]
+    n = perm.shape[0] - 1
+    Diag = np.zeros(n + 1) if Diag is None else Diag
+    invDiag = np.zeros(n + 1)
+    F = np.array(F, dtype=np.float64, copy=True)
+    X = np.zeros(n + 1)
+    it = ref().fr_diag_pgmres(nel, n, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1),
+                              np.ascontiguousarray(A, dtype=np.float64).reshape(-1), perm, inv,
+                              Diag, invDiag, F, X, kmax, lmax, tol)
+    return X, it, Diag, invDiag, F
+
+
+def ref_symrcm(IA, JA):
+    n = IA.shape[0] - 1
+    p = np.empty(max(n, 1), dtype=np.int32)
+    ref().fr_symrcm(n, int(IA[-1]), np.array(IA, dtype=np.int32), np.array(JA, dtype=np.int32), p)
+    return p[:n]
+
+
+def ref_layout():
+    out = np.zeros(64, dtype=np.int64)
+    ref().fr_sst_layout(out)
+    return out

@@ -1,0 +1,302 @@
+/*
+ * Checker harness around the reference's own steady-transport solve path,
+ * compiled from the reference sources by oracle/Makefile (target "ref").
+ *
+ * The reference's Preprocess needs partition files and at least two MPI
+ * ranks, so this harness fills the reference's structs directly for one
+ * rank (neq_bef = 0, NEQ = neq) and then calls the reference's own
+ * Fill_LM, Permutation_of_LM, Build_K_F_SUPG, Diag_precond_EBE_setup,
+ * ebemv, pgmres and Process.  setProblem is supplied here: it installs a
+ * synthetic problem (constant conductivity, reaction, velocity, source,
+ * and a Dirichlet rule) in place of the reference's problem directories.
+ *
+ * Used only by tests and the CPU-baseline leg of the benchmark.
+ */
+#include "SSTranspEquation.h"
+#include "solvers.h"
+#include "preconditioners.h"
+#include "matvec.h"
+#include "reordering.h"
+
+/* ---- synthetic problem (replaces the reference's setProblem.c) ---- */
+static double g_k, g_gamma, g_bx, g_by, g_f, g_upval, g_xmin, g_ymin;
+static int g_upmode;
+
+static double syn_k(void) { return g_k; }
+static double syn_gamma(void) { return g_gamma; }
+static double syn_font(double X, double Y, double k, double gm, double bx, double by)
+{ (void)X; (void)Y; (void)k; (void)gm; (void)bx; (void)by; return g_f; }
+static void syn_vel(double X, double Y, double B[2]) { (void)X; (void)Y; B[0] = g_bx; B[1] = g_by; }
+/* mode 0: 1 on the inflow edges x = xmin or y = ymin, 0 elsewhere;
+ * mode 1: the constant g_upval everywhere. */
+static double syn_upresc(double X, double Y)
+{
+    if (g_upmode == 1) return g_upval;
+    return (X <= g_xmin + 1e-12 || Y <= g_ymin + 1e-12) ? 1.0 : 0.0;
+}
+
+int setProblem(ParametersType *P, FemFunctionsType *F)
+{
+    (void)P;
+    F->Condutivity = syn_k;
+    F->Font = syn_font;
+    F->Reaction = syn_gamma;
+    F->Velocity = syn_vel;
+    F->upresc = syn_upresc;
+    return 0;
+}
+
+/* ---- single-rank struct set-up (what Preprocess.c:120-370 leaves behind) ---- */
+typedef struct {
+    ParametersType P;
+    MatrixDataType M;
+    FemStructsType S;
+    FemFunctionsType F;
+    FemOtherFunctionsType O;
+} fr_sst;
+
+static void fr_setup(fr_sst *c, int nnodes, int nel, const double *x, const double *y,
+                     const int *type, const int *invp, const int *ien, int neq,
+                     double solver_tol, double nl_tol, int kmax, int lmax)
+{
+    int I;
+    memset(c, 0, sizeof(*c));
+    strcpy(c->P.ProblemTitle, "SYNTH");
+    strcpy(c->P.Solver, "GMRES");
+    strcpy(c->P.Preconditioner, "Diag");
+    strcpy(c->P.Scaling, "NOT");
+    strcpy(c->P.reordering, "SYMRCM");
+    strcpy(c->P.MatrixVectorProductScheme, "EBE");
+    strcpy(c->P.StabilizationForm, "SUPG");
+    strcpy(c->P.ShockCapture, "CAU");
+    strcpy(c->P.h_Shock, "2sqrtArea");
+    c->P.SolverTolerance = solver_tol;
+    c->P.NonLinearTolerance = nl_tol;
+    c->P.LinearMaxIter = lmax;
+    c->P.KrylovBasisVectorsQuantity = kmax;
+    c->P.nnodes = c->P.nNodes = nnodes;
+    c->P.nel = c->P.nEl = nel;
+    c->P.neq = neq;
+    c->P.neq_bef = 0;
+    c->P.NEQ = neq;
+    c->P.RANK = 0;
+    c->P.NPROC = 1;
+
+    NodeType *Node = calloc((size_t)nnodes, sizeof(NodeType));
+    ElementType *El = calloc((size_t)nel, sizeof(ElementType));
+    for (I = 0; I < nnodes; I++) {
+        Node[I].x = x[I];
+        Node[I].y = y[I];
+        Node[I].Type = type[I];
+        Node[I].Send = 1;
+        Node[I].invP_id = type[I] == 0 ? -1 : invp[I];
+    }
+    for (I = 0; I < nel; I++) {
+        El[I].Vertex[0] = ien[3*I];
+        El[I].Vertex[1] = ien[3*I+1];
+        El[I].Vertex[2] = ien[3*I+2];
+    }
+    double *F = calloc((size_t)neq + 1, sizeof(double));
+    double *U = calloc((size_t)neq + 1, sizeof(double));
+    int **lm = calloc((size_t)nel, sizeof(int *));
+    int *lmaux = calloc((size_t)nel * 3, sizeof(int));
+    for (I = 0; I < nel; I++) lm[I] = &lmaux[3*I];
+    c->S.Node = Node;
+    c->S.Element = El;
+    c->S.lm = lm;
+    c->S.lmaux = lmaux;
+    c->S.F = F;
+    c->S.U = U;
+    c->S.f = F;
+    c->S.u = U;
+    Fill_LM(&c->P, lm, Node, El);
+
+    int *Perm = calloc((size_t)neq + 1, sizeof(int));
+    int *invPerm = calloc((size_t)neq + 1, sizeof(int));
+    Permutation_of_LM(&c->P, &c->S, Perm, invPerm);
+    double **K = calloc((size_t)nel, sizeof(double *));
+    double *Kaux = calloc((size_t)nel * 9, sizeof(double));
+    for (I = 0; I < nel; I++) K[I] = &Kaux[9*I];
+    c->M.A = K;
+    c->M.Aaux = Kaux;
+    c->M.Perm = Perm;
+    c->M.invPerm = invPerm;
+    c->M.Diag = calloc((size_t)neq + 1, sizeof(double));
+    c->M.invDiag = calloc((size_t)neq + 1, sizeof(double));
+    c->S.delta_old = calloc((size_t)nel + 1, sizeof(double));
+    c->S.Re_old = calloc((size_t)nel + 1, sizeof(double));
+}
+
+static void fr_free(fr_sst *c)
+{
+    free(c->S.Node); free(c->S.Element); free(c->S.lm); free(c->S.lmaux);
+    free(c->S.F); free(c->S.U);
+    free(c->M.A); free(c->M.Aaux); free(c->M.Perm); free(c->M.invPerm);
+    free(c->M.Diag); free(c->M.invDiag);
+    free(c->S.delta_old); free(c->S.Re_old);
+}
+
+static void fr_problem(double k, double gamma, double bx, double by, double f,
+                       int upmode, double upval, const double *x, const double *y, int nnodes)
+{
+    int I;
+    g_k = k; g_gamma = gamma; g_bx = bx; g_by = by; g_f = f;
+    g_upmode = upmode; g_upval = upval;
+    g_xmin = x[0]; g_ymin = y[0];
+    for (I = 1; I < nnodes; I++) {
+        if (x[I] < g_xmin) g_xmin = x[I];
+        if (y[I] < g_ymin) g_ymin = y[I];
+    }
+}
+
+/* Connectivity and local RCM exactly as the reference computes them. */
+int fr_sst_connectivity(int nnodes, int nel, const double *x, const double *y,
+                        const int *type, const int *invp, const int *ien, int neq,
+                        int *lm_out, int *Perm_out, int *invPerm_out, int *band_out)
+{
+    fr_sst c;
+    fr_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, 1e-10, 1e-3, 30, 10);
+    memcpy(lm_out, c.S.lmaux, sizeof(int) * 3 * (size_t)nel);
+    memcpy(Perm_out, c.M.Perm, sizeof(int) * ((size_t)neq + 1));
+    memcpy(invPerm_out, c.M.invPerm, sizeof(int) * ((size_t)neq + 1));
+    band_out[0] = c.P.bandwidth_bef;
+    band_out[1] = c.P.bandwidth_aft;
+    fr_free(&c);
+    return c.P.nnzero;
+}
+
+/* One Build_K_F_SUPG call at the free-dof state u. */
+void fr_sst_build(int nnodes, int nel, const double *x, const double *y,
+                  const int *type, const int *invp, const int *ien, int neq,
+                  double k, double gamma, double bx, double by, double f,
+                  int upmode, double upval, const double *u, double *A_out, double *F_out)
+{
+    fr_sst c;
+    fr_problem(k, gamma, bx, by, f, upmode, upval, x, y, nnodes);
+    fr_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, 1e-10, 1e-3, 30, 10);
+    setProblem(&c.P, &c.F);
+    setMatrixVectorProductType(&c.P, &c.F);
+    setSolver(&c.P, &c.O);
+    setScaling(&c.P, &c.F);
+    setPreconditioner(&c.P, &c.F);
+    setStabilizationForm(&c.P, &c.F, &c.O);
+    memcpy(c.S.u, u, sizeof(double) * (size_t)neq);
+    Build_K_F_SUPG(&c.P, &c.M, &c.S, &c.F);
+    memcpy(A_out, c.M.Aaux, sizeof(double) * 9 * (size_t)nel);
+    memcpy(F_out, c.S.F, sizeof(double) * (size_t)neq);
+    fr_free(&c);
+}
+
+/* The whole steady-transport Process loop of the reference. */
+int fr_sst_process(int nnodes, int nel, const double *x, const double *y,
+                   const int *type, const int *invp, const int *ien, int neq,
+                   double k, double gamma, double bx, double by, double f,
+                   int upmode, double upval, double solver_tol, double nl_tol,
+                   int kmax, int lmax, double *U_out, int *gmres_iterations)
+{
+    fr_sst c;
+    fr_problem(k, gamma, bx, by, f, upmode, upval, x, y, nnodes);
+    fr_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, solver_tol, nl_tol, kmax, lmax);
+    c.P.iterations = 0;
+    /* Process.c allocates, installs and frees its own delta_old / Re_old */
+    free(c.S.delta_old); free(c.S.Re_old);
+    Process(0, 1, &c.P, &c.M, &c.S, &c.F, &c.O);
+    c.S.delta_old = c.S.Re_old = NULL;
+    memcpy(U_out, c.S.U, sizeof(double) * (size_t)neq);
+    *gmres_iterations = c.P.iterations;
+    fr_free(&c);
+    return 0;
+}
+
+/* ebemv on caller-provided blocks (row-major 3x3 per element). */
+void fr_ebemv(int nel, int NEQ, const int *lm, const double *A, const int *Perm,
+              const int *invPerm, const double *P, double *Q)
+{
+    ParametersType Pm; MatrixDataType M; FemStructsType S;
+    int I;
+    memset(&Pm, 0, sizeof Pm); memset(&M, 0, sizeof M); memset(&S, 0, sizeof S);
+    Pm.NEQ = NEQ; Pm.neq = NEQ; Pm.nel = nel; Pm.NPROC = 1;
+    int **l = calloc((size_t)nel, sizeof(int *));
+    double **a = calloc((size_t)nel, sizeof(double *));
+    for (I = 0; I < nel; I++) { l[I] = (int *)&lm[3*I]; a[I] = (double *)&A[9*I]; }
+    S.lm = l; M.A = a; M.Perm = (int *)Perm; M.invPerm = (int *)invPerm;
+    double *Pc = calloc((size_t)NEQ + 1, sizeof(double));
+    memcpy(Pc, P, sizeof(double) * ((size_t)NEQ + 1));
+    ebemv(&Pm, &M, &S, Pc, Q);
+    free(Pc); free(l); free(a);
+}
+
+/* Diag_precond_EBE_setup followed by pgmres (mv = ebemv, precond =
+ * Diag_precond), as Process.c:59-76 sequences them.  F is preconditioned
+ * in place; Diag accumulates across calls on the same array. */
+int fr_diag_pgmres(int nel, int NEQ, const int *lm, const double *A, const int *Perm,
+                   const int *invPerm, double *Diag, double *invDiag, double *F,
+                   double *X, int kmax, int lmax, double tol)
+{
+    ParametersType Pm; MatrixDataType M; FemStructsType S; FemFunctionsType Fn;
+    int I;
+    memset(&Pm, 0, sizeof Pm); memset(&M, 0, sizeof M);
+    memset(&S, 0, sizeof S); memset(&Fn, 0, sizeof Fn);
+    Pm.NEQ = NEQ; Pm.neq = NEQ; Pm.nel = nel; Pm.NPROC = 1;
+    Pm.KrylovBasisVectorsQuantity = kmax; Pm.LinearMaxIter = lmax;
+    Pm.SolverTolerance = tol; Pm.iterations = 0;
+    int **l = calloc((size_t)nel, sizeof(int *));
+    double **a = calloc((size_t)nel, sizeof(double *));
+    for (I = 0; I < nel; I++) { l[I] = (int *)&lm[3*I]; a[I] = (double *)&A[9*I]; }
+    S.lm = l; M.A = a; M.Perm = (int *)Perm; M.invPerm = (int *)invPerm;
+    M.Diag = Diag; M.invDiag = invDiag;
+    Fn.mv = ebemv; Fn.precond = Diag_precond; Fn.precondR = NO_precond;
+    Diag_precond_EBE_setup(&Pm, &M, &S, 1, F);
+    pgmres(&Pm, &M, &S, &Fn, F, X);
+    free(l); free(a);
+    return Pm.iterations;
+}
+
+/* REORDERING_SYMRCM on a caller CSR pattern (not modified). */
+void fr_symrcm(int n, int nnz, int *IA, int *JA, int *perm)
+{
+    REORDERING_SYMRCM(n, nnz, JA, IA, perm);
+}
+
+/* Layout pin: offsets of the fields the GPU drop-in reads. */
+#include <stddef.h>
+void fr_sst_layout(long *out)
+{
+    out[0] = (long)sizeof(ParametersType);
+    out[1] = (long)offsetof(ParametersType, SolverTolerance);
+    out[2] = (long)offsetof(ParametersType, KrylovBasisVectorsQuantity);
+    out[3] = (long)offsetof(ParametersType, nnodes);
+    out[4] = (long)offsetof(ParametersType, nel);
+    out[5] = (long)offsetof(ParametersType, neq);
+    out[6] = (long)offsetof(ParametersType, neq_bef);
+    out[7] = (long)offsetof(ParametersType, NEQ);
+    out[8] = (long)offsetof(ParametersType, LinearMaxIter);
+    out[9] = (long)offsetof(ParametersType, iterations);
+    out[10] = (long)offsetof(ParametersType, RANK);
+    out[11] = (long)offsetof(ParametersType, NPROC);
+    out[12] = (long)sizeof(MatrixDataType);
+    out[13] = (long)offsetof(MatrixDataType, A);
+    out[14] = (long)offsetof(MatrixDataType, Aaux);
+    out[15] = (long)offsetof(MatrixDataType, Diag);
+    out[16] = (long)offsetof(MatrixDataType, invDiag);
+    out[17] = (long)offsetof(MatrixDataType, Perm);
+    out[18] = (long)offsetof(MatrixDataType, invPerm);
+    out[19] = (long)sizeof(FemStructsType);
+    out[20] = (long)offsetof(FemStructsType, lm);
+    out[21] = (long)offsetof(FemStructsType, lmaux);
+    out[22] = (long)offsetof(FemStructsType, Node);
+    out[23] = (long)offsetof(FemStructsType, Element);
+    out[24] = (long)sizeof(FemFunctionsType);
+    out[25] = (long)offsetof(FemFunctionsType, mv);
+    out[26] = (long)offsetof(FemFunctionsType, precond);
+    out[27] = (long)offsetof(FemFunctionsType, precondR);
+    out[28] = (long)offsetof(FemFunctionsType, precond_setup);
+    out[29] = (long)sizeof(NodeType);
+    out[30] = (long)sizeof(ElementType);
+    out[31] = (long)offsetof(MatrixDataType, AA);
+    out[32] = (long)offsetof(MatrixDataType, JA);
+    out[33] = (long)offsetof(MatrixDataType, IA);
+    out[34] = (long)offsetof(ParametersType, MatrixVectorProductScheme);
+    out[35] = (long)offsetof(ParametersType, Preconditioner);
+    out[36] = (long)offsetof(ParametersType, nnzero);
+}

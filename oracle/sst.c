@@ -1,0 +1,157 @@
+/*
+ * femoracle: steady SUPG/CAU convection-diffusion-reaction on P1 triangles.
+ * TEST INFRASTRUCTURE ONLY (see femoracle.h).
+ *
+ * Restates 01_SS_Transport_Equation/2D/01_CommonFiles/Build_K_F_SUPG.c with
+ * CAU_ShockCapture.c, h_shock_2sqrtArea.c, F_assembly.c, ebe_assembly.c and
+ * the Process.c fixed-point loop.  The element formulas are those of the
+ * reference, term for term, so that the element blocks agree to the last bit
+ * when both are compiled without floating-point contraction.
+ */
+#include "femoracle.h"
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+/* CAU_ShockCapture (CAU_ShockCapture.c:3-31). */
+static double cau(double kx, double ky, double bx, double by, double gamma,
+                  double ue1, double ue2, double ue3, double ueb, double feb,
+                  double y23, double y31, double y12, double x32, double x13, double x21,
+                  double invArea, double h)
+{
+    double third = 1. / 3.;
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = bgu + gamma*ueb - feb;
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    double bxp = bgu*gx/(ng*ng);
+    double byp = bgu*gy/(ng*ng);
+    double kp = bxp*bxp*kx + byp*byp*ky;
+    double nbp = sqrt(bxp*bxp + byp*byp);
+    double Pe = 0.5*h*nbp*nbp*nbp/kp;
+    if (ng > 0) {
+        if (third*Pe < 0.7) return 0.5*h*third*Pe*fabs(Ru)/ng;
+        return 0.5*h*0.7*fabs(Ru)/ng;
+    }
+    return 0;
+}
+
+void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
+                       const int *type, const int *invp, const int *ien, int neq,
+                       const or_transport_problem *prob, const double *u,
+                       double *A, double *F)
+{
+    const double third = 1.0/3.0, sixth = 1.0/6.0, twelfth = 1.0/12.0;
+    double kx = prob->k, ky = prob->k, gamma = prob->gamma;
+    double *U = malloc(sizeof(double) * (size_t)nnodes);
+    int J, E;
+    memset(A, 0, sizeof(double) * 9 * (size_t)nel);
+    for (J = 0; J < neq; J++) F[J] = 0;
+    for (J = 0; J < nnodes; J++)
+        U[J] = type[J] == 0 ? prob->upresc[J] : u[invp[J]];
+
+    for (E = 0; E < nel; E++) {
+        int J1 = ien[3*E], J2 = ien[3*E+1], J3 = ien[3*E+2];
+        double X0 = x[J1], X1 = x[J2], X2 = x[J3];
+        double Y0 = y[J1], Y1 = y[J2], Y2 = y[J3];
+        double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+        double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+        double TwoA = x21*y31 - x13*y12;
+        double Area = 0.5*TwoA;
+        double invArea = 1.0/Area;
+        double h = sqrt(fabs(TwoA));
+        double bx = prob->beta[0], by = prob->beta[1];
+        double norm = sqrt(bx*bx + by*by);
+        double tau = norm > 0 ? 0.5*h/norm : 0;
+        double fe1 = prob->f, fe2 = prob->f, fe3 = prob->f;
+        double feb = third*(fe1 + fe2 + fe3);
+        double ue1 = U[J1], ue2 = U[J2], ue3 = U[J3];
+        double ueb = third*(ue1 + ue2 + ue3);
+        double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+        double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+        double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+        double C11 = sixth*(bx*y23 + by*x32);
+        double C12 = sixth*(bx*y31 + by*x13);
+        double C13 = sixth*(bx*y12 + by*x21);
+        double R11 = sixth*(gamma*Area);
+        double R12 = twelfth*(gamma*Area);
+        double Cpg12 = 0.25*invArea*tau*(y23*(bx*bx*y31 + bx*by*x13) + x32*(bx*by*y31 + by*by*x13));
+        double Cpg13 = 0.25*invArea*tau*(y23*(bx*bx*y12 + bx*by*x21) + x32*(bx*by*y12 + by*by*x21));
+        double Cpg23 = 0.25*invArea*tau*(y31*(bx*bx*y12 + bx*by*x21) + x13*(bx*by*y12 + by*by*x21));
+        double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
+        double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
+        double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
+        double hs = sqrt(fabs(2*Area));
+        double Eu = prob->cau ? cau(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb,
+                                    y23, y31, y12, x32, x13, x21, invArea, hs) : 0.0;
+        double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
+        double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
+        double Csc23 = Eu*0.25*invArea*(y31*y12 + x13*x21);
+        double ke[3][3];
+        ke[0][0] = -(D12 + D13) + C11 - (Cpg12 + Cpg13) + R11 + Rpg11 - (Csc12 + Csc13);
+        ke[0][1] = D12 + C12 + Cpg12 + R12 + Rpg11 + Csc12;
+        ke[0][2] = D13 + C13 + Cpg13 + R12 + Rpg11 + Csc13;
+        ke[1][0] = D12 + C11 + Cpg12 + R12 + Rpg21 + Csc12;
+        ke[1][1] = -(D12 + D23) + C12 - (Cpg12 + Cpg23) + R11 + Rpg21 - (Csc12 + Csc23);
+        ke[1][2] = D23 + C13 + Cpg23 + R12 + Rpg21 + Csc23;
+        ke[2][0] = D13 + C11 + Cpg13 + R12 + Rpg31 + Csc13;
+        ke[2][1] = D23 + C12 + Cpg23 + R12 + Rpg31 + Csc23;
+        ke[2][2] = -(D13 + D23) + C13 - (Cpg13 + Cpg23) + R11 + Rpg31 - (Csc13 + Csc23);
+        double Fe1 = Area*twelfth*(2*fe1 + fe2 + fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y23 + by*x32);
+        double Fe2 = Area*twelfth*(fe1 + 2*fe2 + fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y31 + by*x13);
+        double Fe3 = Area*twelfth*(fe1 + fe2 + 2*fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y12 + by*x21);
+        /* F_assembly (F_assembly.c:3-28): Dirichlet lifting per free vertex */
+        const int V[3] = { J1, J2, J3 };
+        const double Fe[3] = { Fe1, Fe2, Fe3 };
+        for (int a = 0; a < 3; a++) {
+            if (type[V[a]] != 1) continue;
+            F[invp[V[a]]] += Fe[a];
+            for (int b = 0; b < 3; b++)
+                if (b != a && type[V[b]] == 0)
+                    F[invp[V[a]]] -= ke[a][b] * prob->upresc[V[b]];
+        }
+        /* ebe_assembly (ebe_assembly.c:3-19) */
+        double *Ae = A + 9L * E;
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) Ae[3*r + c] = ke[r][c];
+    }
+    free(U);
+}
+
+int or_transport_process(int nnodes, int nel, const double *x, const double *y,
+                         const int *type, const int *invp, const int *ien, int neq,
+                         const or_transport_problem *prob,
+                         double solver_tol, double nonlinear_tol, int kmax, int lmax,
+                         int max_nonlinear, double *U, int *gmres_iterations)
+{
+    int NEQ = neq, it = 0, i;
+    int *lm = malloc(sizeof(int) * 3 * (size_t)nel);
+    int *Perm = malloc(sizeof(int) * ((size_t)NEQ + 1));
+    int *invPerm = malloc(sizeof(int) * ((size_t)NEQ + 1));
+    double *A = malloc(sizeof(double) * 9 * (size_t)nel);
+    double *F = calloc((size_t)NEQ + 1, sizeof(double));
+    double *Diag = calloc((size_t)NEQ + 1, sizeof(double));
+    double *invDiag = calloc((size_t)NEQ + 1, sizeof(double));
+    double *uold = calloc((size_t)NEQ + 1, sizeof(double));
+    double normdiff = nonlinear_tol + 1, normu = 1.0 / nonlinear_tol;
+
+    or_fill_lm(nel, 1, ien, type, invp, NEQ, lm);
+    or_permutation_of_lm(nel, ien, type, invp, NEQ, Perm, invPerm, NULL);
+    if (gmres_iterations) *gmres_iterations = 0;
+    /* Process.c:37-86 */
+    while (normdiff > nonlinear_tol * normu && it < max_nonlinear) {
+        it++;
+        memcpy(uold, U, sizeof(double) * neq);
+        or_build_k_f_supg(nnodes, nel, x, y, type, invp, ien, neq, prob, U, A, F);
+        int gi = or_ebe_diag_solve(nel, 3, lm, A, NEQ, Perm, invPerm, Diag, invDiag, F,
+                                   kmax, lmax, solver_tol, U);
+        if (gmres_iterations) *gmres_iterations += gi;
+        for (i = 0; i < neq; i++) uold[i] += -1 * U[i];
+        normdiff = sqrt(or_ddot(neq, uold, uold));
+        normu = sqrt(or_ddot(neq, U, U));
+    }
+    free(lm); free(Perm); free(invPerm); free(A); free(F);
+    free(Diag); free(invDiag); free(uold);
+    return it;
+}

@@ -1,0 +1,124 @@
+"""Synthetic meshes and problems for the solve path (seeded, numpy only).
+
+The reference reads meshes written by Mesh_Generator/Structured_Mesh/
+meshGenerator.c (node order row by row, two triangles per quad, see
+meshGenerator.c:113-177) and partitioned by Parallel_Preprocess.  The
+single-GPU path needs no partitioning: a mesh here is one domain whose free
+dofs are numbered in node order (node-major, dof-minor for NDOF > 1), which
+is what Parallel_Preprocess produces for one rank before the local RCM of
+Permutation_of_LM.c.
+
+All problems are synthetic and seeded; no dataset is involved.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+
+@dataclasses.dataclass
+class Mesh:
+    x: np.ndarray          # float64[nnodes]
+    y: np.ndarray          # float64[nnodes]
+    ien: np.ndarray        # int32[nel, 3]  (Element[e].Vertex)
+    ndof: int
+    type: np.ndarray       # int32[nnodes*ndof]  0 = Dirichlet, 1 = free (Node.Type)
+    invp: np.ndarray       # int32[nnodes*ndof]  equation of a free dof, -1 otherwise (Node.invP_id)
+    neq: int
+
+    @property
+    def nnodes(self) -> int:
+        return int(self.x.shape[0])
+
+    @property
+    def nel(self) -> int:
+        return int(self.ien.shape[0])
+
+
+def structured_mesh(M: int, N: int, x0=0.0, y0=0.0, x1=1.0, y1=1.0, left=False):
+    """Node coordinates and connectivity of an M x N structured rectangle
+    (meshGenerator.c:113-177, "right" or "left" diagonal)."""
+    nx = M + 1
+    i = np.arange(M + 1, dtype=np.float64)
+    j = np.arange(N + 1, dtype=np.float64)
+    hx = (x1 - x0) / M
+    hy = (y1 - y0) / N
+    X = np.tile(x0 + i * hx, N + 1)
+    Y = np.repeat(y0 + j * hy, M + 1)
+    jj, ii = np.meshgrid(np.arange(N), np.arange(M), indexing="ij")
+    a = (jj * nx + ii).reshape(-1).astype(np.int64)
+    ien = np.empty((2 * M * N, 3), dtype=np.int32)
+    if not left:
+        ien[0::2] = np.stack([a, a + 1, a + nx + 1], axis=1)
+        ien[1::2] = np.stack([a, a + nx + 1, a + nx], axis=1)
+    else:
+        ien[0::2] = np.stack([a, a + 1, a + nx], axis=1)
+        ien[1::2] = np.stack([a + 1, a + nx + 1, a + nx], axis=1)
+    return X, Y, ien
+
+
+def number_dofs(type_: np.ndarray) -> tuple[np.ndarray, int]:
+    """Sequential equation numbers for the free dofs (type != 0)."""
+    free = type_ != 0
+    invp = np.full(type_.shape, -1, dtype=np.int32)
+    invp[free] = np.arange(int(free.sum()), dtype=np.int32)
+    return invp, int(free.sum())
+
+
+def boundary_mask(x, y, tol=1e-12):
+    x0, x1, y0, y1 = x.min(), x.max(), y.min(), y.max()
+    return (np.abs(x - x0) < tol) | (np.abs(x - x1) < tol) | (np.abs(y - y0) < tol) | (np.abs(y - y1) < tol)
+
+
+@dataclasses.dataclass
+class TransportProblem:
+    """Steady SUPG/CAU convection-diffusion-reaction data (the FemFunctions
+    callbacks Condutivity, Reaction, Velocity, Font, upresc of
+    01_SS_Transport_Equation/2D/01_CommonFiles/SSTranspEquation.h:140-146),
+    with a constant velocity field, conductivity, reaction and source."""
+    mesh: Mesh
+    k: float
+    gamma: float
+    beta: tuple[float, float]
+    f: float
+    upresc: np.ndarray     # float64[nnodes], Dirichlet value (read where type == 0)
+    upmode: int = 0        # 0: 1 on inflow edges x=xmin, y=ymin, else 0;  1: constant
+    upval: float = 0.0
+    cau: bool = True
+
+
+def transport_problem(n_nodes_side: int, angle_deg=30.0, k=1e-6, gamma=0.0, f=0.0,
+                      left=False, upmode=0, upval=1.0, cau=True) -> TransportProblem:
+    """Unit square with n x n nodes, every boundary node Dirichlet.
+    upmode 0: u = 1 on x = 0 and y = 0, u = 0 on the rest of the boundary
+    (the steady transport workload: 129 x 129 nodes, beta = (cos 30, sin 30),
+    k = 1e-6).  upmode 1: u = upval on the whole boundary (the TESTE problem of
+    01_SS_Transport_Equation/2D/TESTE, exact solution u = upval when f = 0,
+    gamma = 0)."""
+    M = n_nodes_side - 1
+    X, Y, ien = structured_mesh(M, M, left=left)
+    bnd = boundary_mask(X, Y)
+    type_ = np.where(bnd, 0, 1).astype(np.int32)
+    invp, neq = number_dofs(type_)
+    mesh = Mesh(X, Y, ien, 1, type_, invp, neq)
+    if upmode == 0:
+        up = np.where((X <= X.min() + 1e-12) | (Y <= Y.min() + 1e-12), 1.0, 0.0)
+    else:
+        up = np.full_like(X, upval)
+    a = math.radians(angle_deg)
+    return TransportProblem(mesh, float(k), float(gamma), (math.cos(a), math.sin(a)),
+                            float(f), up.astype(np.float64), upmode, float(upval), cau)
+
+
+def batch_transport_problems(count=256, seed=4, nmin=33, nmax=513, cau=True):
+    """The batched transport workload: count independent steady SUPG problems,
+    mesh N x N nodes with N uniform in [nmin, nmax], velocity angle uniform in
+    [0, 360), conductivity log-uniform in [1e-8, 1e-2] (numpy PCG64, seeded)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = rng.integers(nmin, nmax + 1, size=count)
+    angles = rng.uniform(0.0, 360.0, size=count)
+    ks = 10.0 ** rng.uniform(-8.0, -2.0, size=count)
+    return [transport_problem(int(n), float(a), float(kk), cau=cau)
+            for n, a, kk in zip(ns, angles, ks)]
