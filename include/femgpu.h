@@ -1,0 +1,178 @@
+/*
+ * femgpu — GB300 (sm_103a) solve path for 2-D stabilised P1 finite elements.
+ *
+ * Plain C ABI: opaque handles, host pointers and sizes, integer status codes.
+ * No function exits the process; every call returns FG_OK or an error code
+ * whose text fg_last_error() gives.
+ *
+ * Numbering.  Host-facing calls use the reference's equation numbering:
+ * equations 0..n-1 of the free dofs (Node.invP_id), and every vector has
+ * n + 1 slots, slot n being the Dirichlet sink that reads as 0
+ * (01_SS_Transport_Equation/2D/01_CommonFiles/Preprocess.c:288-296 with one
+ * rank: neq_bef = 0, NEQ = neq).  Element blocks are row-major S x S per
+ * element, S = 3 * ndof (ebe_assembly.c:3-19), and lm is Fill_LM's map.
+ * Internally the library renumbers the dofs (local reverse Cuthill-McKee,
+ * as Permutation_of_LM.c does for ebemv) and colours the elements.
+ */
+#ifndef FEMGPU_H
+#define FEMGPU_H
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ---- */
+enum {
+    FG_OK = 0,
+    FG_ERR_ARG = 1,        /* invalid argument or size                         */
+    FG_ERR_CUDA = 2,       /* CUDA runtime error (text in fg_last_error)       */
+    FG_ERR_NOMEM = 3,      /* device or host allocation failed                 */
+    FG_ERR_STATE = 4,      /* call out of order (e.g. solve before blocks)     */
+    FG_ERR_BREAKDOWN = 5,  /* zero pivot / non-finite value in the solve       */
+    FG_ERR_NOTCONV = 6,    /* iteration limit reached before the tolerance     */
+    FG_ERR_UNSUPPORTED = 7 /* option not available for this system             */
+};
+
+/* Text of the last error on the calling thread (never NULL). */
+const char *fg_last_error(void);
+/* Library version, major*10000 + minor*100 + patch. */
+int fg_version(void);
+/* Select the CUDA device for handles created afterwards on this thread. */
+int fg_set_device(int device);
+
+/* ---- system: mesh connectivity, element blocks, preconditioner ---- */
+typedef struct fg_system fg_system;
+
+enum { FG_REORDER_NONE = 0, FG_REORDER_RCM = 1 };
+
+/* Create a system from the mesh.
+ *   ien[nel*3]         element vertices (Element[e].Vertex)
+ *   type[nnodes*ndof]  0 = Dirichlet dof, otherwise free (Node.Type)
+ *   invp[nnodes*ndof]  equation of each free dof, 0..neq-1 (Node.invP_id)
+ * Builds lm (Fill_LM.c), the local RCM numbering (Permutation_of_LM.c, when
+ * reorder == FG_REORDER_RCM and ndof == 1), a greedy element colouring and
+ * the dof/node incidence lists, and uploads the connectivity.
+ * Replaces Preprocess.c:288-340 (lm, Perm, invPerm, A allocation). */
+int fg_system_create(fg_system **out, int nnodes, int nel, int ndof,
+                     const int *ien, const int *type, const int *invp, int neq,
+                     int reorder);
+
+/* Host-only set-up products of a mesh (no device needed): lm[nel*3*ndof]
+ * (Fill_LM), Perm/invPerm[neq+1] (Permutation_of_LM with SYMRCM),
+ * colour[nel] (greedy element colouring; -1 for an element without a free
+ * dof), and into info: ncolours, bandwidths, nnz.  Any output may be NULL. */
+typedef struct fg_system_info fg_system_info;
+int fg_mesh_analyze(int nnodes, int nel, int ndof, const int *ien, const int *type,
+                    const int *invp, int neq, int reorder, int *lm, int *Perm,
+                    int *invPerm, int *colour, fg_system_info *info);
+int fg_system_destroy(fg_system *s);
+
+struct fg_system_info {
+    int n, nel, ndof, S, nnodes, ncolours;
+    int bandwidth_before, bandwidth_after;  /* MATRIX_bandwidth of the dof graph */
+    int nnz;                                /* entries of the dof adjacency      */
+    size_t device_bytes;                    /* device memory held by the system  */
+};
+int fg_system_get_info(const fg_system *s, fg_system_info *info);
+
+/* Copies of the set-up products, in the reference's numbering:
+ * lm[nel*S]; Perm[n+1], invPerm[n+1] (Permutation_of_LM.c:56-72);
+ * colour[nel] (greedy element colouring over the free dofs). */
+int fg_system_get_lm(const fg_system *s, int *lm);
+int fg_system_get_perm(const fg_system *s, int *Perm, int *invPerm);
+int fg_system_get_colours(const fg_system *s, int *colour);
+
+/* Upload element blocks A[nel][S][S] (row-major, ebe_assembly.c) from host
+ * memory; keeps an FP64 and an FP32 copy on the device. */
+int fg_set_blocks(fg_system *s, const double *A);
+/* Download the element blocks (row-major, reference element order). */
+int fg_get_blocks(const fg_system *s, double *A);
+
+/* Q = A P (ebemv / ebemvNDOF3 / ebemvNDOF4 on the GPU).  P and Q are host
+ * vectors of n+1 entries; Q[n] is returned as 0.  precision: 64 or 32. */
+int fg_matvec(fg_system *s, const double *P, double *Q, int precision);
+
+/* ---- preconditioners (Solvers_and_Preconditioners/preconditioners.h) ---- */
+enum { FG_PRECOND_NONE = 0, FG_PRECOND_DIAG = 1, FG_PRECOND_BLOCKDIAG = 2 };
+enum {
+    FG_SETUP_ACCUMULATE = 1, /* Diag += new diagonal, as Diag_precond_EBE_setup
+                                does across nonlinear iterations              */
+    FG_SETUP_REF_QUIRKS = 2  /* 4x4 block inverse with the reference's entry-14
+                                term (BlockDiag_precond_EBE_setup.c:142)      */
+};
+/* Build the preconditioner from the current blocks and, when F is not NULL,
+ * precondition F in place (n+1 host entries), as the *_EBE_setup routines
+ * do.  The right-hand side the solver receives is then M^-1 F. */
+int fg_precond_setup(fg_system *s, int kind, int flags, double *F);
+/* z = M^-1 p for host vectors of n+1 entries (p == z allowed). */
+int fg_precond_apply(fg_system *s, const double *p, double *z);
+/* Diagonal used by the Diag preconditioner (n+1 entries, host). */
+int fg_get_diag(const fg_system *s, double *Diag);
+int fg_set_diag(fg_system *s, const double *Diag);
+
+/* ---- GMRES (Solvers_and_Preconditioners/pgmres.c:5-200) ---- */
+enum { FG_PREC_FP64 = 64, FG_PREC_MIXED = 32 };
+typedef struct {
+    int kmax;            /* KrylovBasisVectorsQuantity (k-1 Arnoldi steps/cycle) */
+    int lmax;            /* LinearMaxIter: restart cycles                         */
+    double tol;          /* SolverTolerance                                       */
+    int precision;       /* FG_PREC_FP64: the reference's method, all FP64;
+                            FG_PREC_MIXED: FP32 Arnoldi (blocks, basis, M^-1)
+                            inside FP64 refinement: each cycle restarts from the
+                            FP64 residual, stops when the true relative residual
+                            ||F - A X|| / ||F|| <= tol                            */
+    double inner_tol;    /* mixed: relative decrease per FP32 cycle (0 = 1e-5)    */
+} fg_solver_opts;
+
+typedef struct {
+    int iterations;      /* Arnoldi steps (Parameters->iterations increment)   */
+    int cycles;          /* restart cycles                                     */
+    int converged;       /* 1 when the stopping test was met                   */
+    int status;          /* FG_OK / FG_ERR_NOTCONV / FG_ERR_BREAKDOWN          */
+    double rho;          /* last preconditioned residual estimate              */
+    double eps;          /* tol * ||M^-1 F|| (FP64) or tol (mixed)             */
+    double true_rel_residual; /* ||F - A X||_2 / ||F||_2, FP64 on the device   */
+    double seconds;      /* wall time of the solve on the device stream        */
+} fg_solve_stats;
+
+/* Solve (M^-1 A) X = B with B = M^-1 F already preconditioned (as the
+ * reference's precond_setup leaves F).  X0 = 0.  F_true (optional, n+1,
+ * unpreconditioned) is used for the true residual; NULL: B is used with M.
+ * B, X, F_true are host vectors of n+1 entries. */
+int fg_solve(fg_system *s, const fg_solver_opts *opts, const double *B, double *X,
+             const double *F_true, fg_solve_stats *stats);
+
+/* ---- steady SUPG/CAU transport assembly on the device ---- */
+typedef struct {
+    double k;            /* Condutivity(), used for kx and ky         */
+    double gamma;        /* Reaction()                                */
+    double beta[2];      /* Velocity() (constant field)               */
+    double f;            /* Font() (constant source)                  */
+    int cau;             /* 1: CAU shock capture (CAU_ShockCapture.c) */
+} fg_transport_coeffs;
+
+/* Set node coordinates (x, y) and Dirichlet values upresc[nnodes]. */
+int fg_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc);
+/* Build_K_F_SUPG on the device at the free-dof state u (host, n entries,
+ * NULL = 0): element blocks stay on the device; F (host, n+1) receives the
+ * right-hand side when not NULL. */
+int fg_transport_assemble(fg_system *s, const fg_transport_coeffs *c, const double *u, double *F);
+/* Steady transport Process loop (Process.c:6-93) on the device: assemble,
+ * Diag setup (accumulating, as the reference), GMRES, until
+ * ||u - u_old|| <= nonlinear_tol * ||u||.  U (host, n entries) holds the
+ * solution. */
+typedef struct {
+    int nonlinear_iterations;
+    int gmres_iterations;
+    double seconds;
+    double true_rel_residual;  /* of the last linear solve */
+} fg_process_stats;
+int fg_transport_process(fg_system *s, const fg_transport_coeffs *c,
+                         const fg_solver_opts *opts, double nonlinear_tol,
+                         int max_nonlinear, double *U, fg_process_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

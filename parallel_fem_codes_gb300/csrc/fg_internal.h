@@ -1,0 +1,101 @@
+// Internal declarations shared by the host set-up code and the CUDA
+// translation units of libfemgpu.  Not part of the public ABI.
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace fg {
+
+// ------------------------------------------------------------ error text
+void set_error(const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define FG_CUDA(call)                                                        \
+    do {                                                                     \
+        cudaError_t fg_e_ = (call);                                          \
+        if (fg_e_ != cudaSuccess) return ::fg::cuda_fail(fg_e_, #call);      \
+    } while (0)
+
+// ------------------------------------------------------------ host topology
+// Everything the device layout needs, computed once per mesh on the host.
+struct Topology {
+    int nnodes = 0, nel = 0, ndof = 1, S = 3, n = 0;
+    std::vector<int> ien;        // nel*3, reference element order
+    std::vector<int> type;       // nnodes*ndof
+    std::vector<int> invp;       // nnodes*ndof, reference equation numbers
+    std::vector<int> lm;         // nel*S, reference numbering (Fill_LM), sink = n
+    std::vector<int> perm, iperm;// n+1: internal dof i holds reference dof perm[i]
+    int band_before = 0, band_after = 0, nnz = 0;
+    std::vector<int> colour;     // nel, reference element order
+    int ncol = 0;
+    std::vector<int> eorder;     // internal element position -> reference element
+    std::vector<int> epos;       // reference element -> internal position
+    std::vector<int> cptr;       // ncol+1, internal element ranges per colour
+    // dof incidence (internal dofs; entries pos*16 + local row), ordered by
+    // reference element index, for order-faithful gathers
+    std::vector<int> dinc_ptr, dinc;
+    // node incidence (entries pos*4 + vertex), ordered by reference element
+    std::vector<int> ninc_ptr, ninc;
+    std::vector<int> node_dof;   // nnodes*ndof: internal dof or n (sink)
+};
+
+int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
+                   const int *type, const int *invp, int neq, int reorder);
+
+// Reverse Cuthill-McKee with the tie-breaking of the reference
+// (00_CommonFiles/Reordering/symrcm.c); IA/JA row-sorted, symmetric or not.
+void symrcm(int n, const int *IA, const int *JA, int *perm);
+int matrix_bandwidth(int n, const int *IA, const int *JA);
+
+// ------------------------------------------------------------ device layout
+constexpr int kMaxColours = 64;
+constexpr int kElemChunk = 1024;   // elements per matvec work item
+constexpr int kMaxParts = 256;     // dof parts (reduction partials) per system
+constexpr int kPartMin = 2048;     // minimum dofs per part
+constexpr int kThreads = 256;
+
+struct SysState {
+    int live;          // system still being solved
+    int in_cycle;      // Arnoldi continues in the current cycle
+    int steps;         // Arnoldi steps in the current cycle
+    int cycles;        // completed cycles
+    int iterations;    // total Arnoldi steps
+    int converged;
+    int status;        // FG_OK / FG_ERR_*
+    int first;         // next cycle is the first
+    double rho, eps, normb, r0, target, true_res, fnorm, hn;
+};
+
+// Per-system descriptor read by every kernel (device memory).
+struct SysDev {
+    int n, n_pad, nel, nel_pad, S, ndof, ncol, nparts, nnodes;
+    int kmax, lmax, mixed, precond;
+    double tol, inner_tol;
+    const int *lm;             // [S][nel_pad] internal dofs
+    const double *A64;         // [S*S][nel_pad]
+    const float *A32;
+    const double *invd64;      // n_pad
+    const float *invd32;
+    const int *node_dof;       // [nnodes][ndof]
+    const double *ibd64;       // [nnodes][ndof*ndof]
+    const float *ibd32;
+    double *x, *b, *ftrue, *r64, *t64, *u64;  // FP64 vectors (n_pad)
+    void *V;                   // kmax vectors of T, stride n_pad
+    void *w, *t;               // T vectors
+    double *H;                 // (kmax+1) x kmax, H[j*kmax + i]
+    double *g, *cs, *sn, *hbuf;// kmax+1 each
+    double *part;              // nparts x kPartStride
+    unsigned *counter;         // 4 counters (one per reduction kernel kind)
+    SysState *st;
+};
+constexpr int kPartStride = 64;    // doubles per part (>= kmax + 2, kmax <= 60)
+
+struct EChunk { int sys, e0, e1; };
+struct DChunk { int sys, part, d0, d1; };
+struct NChunk { int sys, n0, n1; };
+
+}  // namespace fg

@@ -1,0 +1,998 @@
+// EBE matvec and the batched restarted GMRES engine (sm_103a).
+//
+// Method (00_CommonFiles/Solvers_and_Preconditioners/pgmres.c:5-200):
+// restarted, left-preconditioned GMRES(kmax) with X0 = 0, at most kmax-1
+// Arnoldi steps per cycle (pgmres.c:159), Givens rotations (:120-155),
+// back-substitution (:163-171) and X += V y (:173-175).  The reference's
+// modified Gram-Schmidt with one MPI_Allreduce per dot becomes classical
+// Gram-Schmidt with reorthogonalisation (CGS2): three streaming passes over
+// the basis per step, each ending in a deterministic device-wide reduction
+// (fixed part order, "last part reduces"), instead of 2(i+1) dependent
+// reductions.
+//
+// Work decomposition.  A batch holds any number of systems.  Element work
+// is cut into chunks per colour, dof work into parts per system; every
+// kernel walks its chunk table with a grid-stride loop and skips systems
+// that are not active.  A system's partial sums depend only on its own
+// parts, so a result is bit-identical whether the system is solved alone
+// or inside a batch.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "system.h"
+
+namespace fg {
+
+// ---------------------------------------------------------------- helpers
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename T> __device__ __forceinline__ T ldst(const T *p) { return __ldcs(p); }
+
+// Gate of a kernel: 0 = system live, 1 = inside an Arnoldi cycle, < 0 = always.
+__device__ __forceinline__ bool gated(const SysDev &D, int gate)
+{
+    if (gate < 0) return true;
+    return gate == 0 ? D.st->live != 0 : D.st->in_cycle != 0;
+}
+
+// Last-part election: returns true in the CTA that completed the final part
+// of system D for counter slot `slot` (all threads of the CTA agree).
+__device__ __forceinline__ bool last_part(const SysDev &D, int slot)
+{
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        unsigned prev = atomicAdd(&D.counter[slot], 1u);
+        s_last = (prev == (unsigned)D.nparts - 1u);
+        if (s_last) D.counter[slot] = 0u;
+    }
+    __syncthreads();
+    if (s_last) __threadfence();
+    return s_last != 0;
+}
+
+// Deterministic sum over parts of slots [0, nv): warp w reduces slots
+// w, w+8, ...; lane l adds parts l, l+32, ... in order, then a fixed
+// butterfly.  Results to out[] (shared or global).
+__device__ __forceinline__ void reduce_parts(const SysDev &D, int nv, double *out)
+{
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int j = warp; j < nv; j += kThreads / 32) {
+        double s = 0.0;
+        for (int p = lane; p < D.nparts; p += 32) s += __ldcg(&D.part[p * kPartStride + j]);
+        s = warp_sum(s);
+        if (lane == 0) out[j] = s;
+    }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------- EBE matvec
+// y[lm] += A_e x[lm] for the elements of one colour.  A and lm are SoA
+// ([entry][element]), so lane-consecutive elements read consecutive
+// addresses; x gathers and y updates hit L2.  Elements of one colour share
+// no free dof, so the scatter needs no atomics and the summation order is
+// fixed (colour by colour).  The sink (index n) is never written.
+// in_sel: 0 = x (FP64), 1 = V[step] (T), 2 = aux (TX); out_sel: 0 = t64,
+// 1 = t, 2 = aux.
+template <int S, typename TA, typename TX, typename TY>
+__global__ void __launch_bounds__(kThreads)
+k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const int *__restrict__ nch,
+         int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out)
+{
+    const int total = *nch;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const EChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!gated(D, gate)) continue;
+        const TX *X = in_sel == 0 ? (const TX *)D.x
+                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+        TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
+        const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
+        const size_t ld = (size_t)D.nel_pad;
+        const int n = D.n;
+        for (int e = k.e0 + threadIdx.x; e < k.e1; e += blockDim.x) {
+            int idx[S];
+            TA xv[S];
+#pragma unroll
+            for (int a = 0; a < S; ++a) idx[a] = __ldcs(D.lm + a * ld + e);
+#pragma unroll
+            for (int a = 0; a < S; ++a) xv[a] = (TA)X[idx[a]];
+#pragma unroll
+            for (int r = 0; r < S; ++r) {
+                TA acc = ldst(A + (size_t)(r * S) * ld + e) * xv[0];
+#pragma unroll
+                for (int q = 1; q < S; ++q) acc += ldst(A + (size_t)(r * S + q) * ld + e) * xv[q];
+                if (idx[r] != n) Y[idx[r]] += (TY)acc;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- block-diagonal apply
+// z[dofs of node] = invB(node) * p[dofs of node] (BlockDiag_precond.c:3-29,
+// BlockDiagDOF3_precond.c:3-27); dofs that are Dirichlet read 0 and are not
+// written.  sel: 0 = t64 -> u64 (FP64), 1 = t -> w (T), 2 = aux.
+template <int B, typename T>
+__global__ void __launch_bounds__(kThreads)
+k_blockdiag(const SysDev *__restrict__ sys, const NChunk *__restrict__ ch, const int *__restrict__ nch,
+            int gate, int sel, const T *aux_in, T *aux_out)
+{
+    const int total = *nch;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const NChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!gated(D, gate)) continue;
+        const T *P = sel == 0 ? (const T *)D.t64 : sel == 1 ? (const T *)D.t : aux_in;
+        T *Z = sel == 0 ? (T *)D.u64 : sel == 1 ? (T *)D.w : aux_out;
+        const T *M = sizeof(T) == 8 ? (const T *)D.ibd64 : (const T *)D.ibd32;
+        for (int nd = k.n0 + threadIdx.x; nd < k.n1; nd += blockDim.x) {
+            int id[B];
+            T v[B];
+#pragma unroll
+            for (int a = 0; a < B; ++a) {
+                id[a] = D.node_dof[nd * B + a];
+                v[a] = id[a] == D.n ? (T)0 : P[id[a]];
+            }
+            const T *m = M + (size_t)nd * B * B;
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                T s = m[r * B] * v[0];
+#pragma unroll
+                for (int q = 1; q < B; ++q) s += m[r * B + q] * v[q];
+                if (id[r] != D.n) Z[id[r]] = s;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- cycle start
+// FP64: u = M^-1 (A x) (t64 holds A x; for the block-diagonal case u64
+// already holds M^-1 t64), r = b - u (pgmres.c:64-75), partial ||r||^2,
+// true residual s = F - A x, partial ||s||^2, and on the first cycle ||b||^2
+// and ||F||^2.  t64 is cleared for the next use.
+__global__ void __launch_bounds__(kThreads)
+k_start(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch)
+{
+    __shared__ double red[4][kThreads / 32];
+    __shared__ double tot[4];
+    const int total = *nch;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!D.st->live) continue;
+        const bool first = D.st->first != 0;
+        const bool has_f = D.ftrue != nullptr;
+        double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) {
+            double t = D.t64[d];
+            double u = D.precond == FG_PRECOND_DIAG ? t * D.invd64[d]
+                     : D.precond == FG_PRECOND_BLOCKDIAG ? D.u64[d] : t;
+            double bd = D.b[d];
+            double r = -1.0 * (u + -1.0 * bd);
+            D.r64[d] = r;
+            D.t64[d] = 0.0;
+            a0 += r * r;
+            if (has_f) {
+                double s = D.ftrue[d] - t;
+                a1 += s * s;
+                if (first) a3 += D.ftrue[d] * D.ftrue[d];
+            }
+            if (first) a2 += bd * bd;
+        }
+        a0 = warp_sum(a0); a1 = warp_sum(a1); a2 = warp_sum(a2); a3 = warp_sum(a3);
+        if (lane == 0) { red[0][warp] = a0; red[1][warp] = a1; red[2][warp] = a2; red[3][warp] = a3; }
+        __syncthreads();
+        if (threadIdx.x < 4) {
+            double s = 0;
+            for (int w = 0; w < kThreads / 32; ++w) s += red[threadIdx.x][w];
+            D.part[k.part * kPartStride + threadIdx.x] = s;
+        }
+        if (last_part(D, 0)) {
+            reduce_parts(D, 4, tot);
+            if (threadIdx.x == 0) {
+                SysState *st = D.st;
+                double r0 = sqrt(tot[0]);
+                if (st->first) {
+                    st->normb = sqrt(tot[2]);
+                    st->fnorm = sqrt(tot[3]);
+                    st->eps = D.mixed ? D.tol : D.tol * st->normb;
+                    st->first = 0;
+                }
+                double rel_true = has_f ? (st->fnorm > 0 ? sqrt(tot[1]) / st->fnorm : sqrt(tot[1])) : NAN;
+                double rel_pre = st->normb > 0 ? r0 / st->normb : r0;
+                st->true_res = rel_true;
+                st->r0 = r0;
+                st->steps = 0;
+                bool stop = false;
+                if (!(r0 > 0.0)) {                      // exact (or empty) right-hand side
+                    stop = true;
+                    st->converged = (r0 == 0.0);
+                    if (!(r0 == 0.0)) st->status = FG_ERR_BREAKDOWN;
+                    st->rho = r0;
+                } else if (D.mixed) {
+                    double m = has_f ? rel_true : rel_pre;
+                    if (m <= D.tol) { stop = true; st->converged = 1; }
+                    else if (st->cycles >= D.lmax) { stop = true; st->status = FG_ERR_NOTCONV; }
+                    st->target = D.inner_tol * r0;
+                }
+                if (stop) { st->live = 0; st->in_cycle = 0; }
+                else {
+                    st->in_cycle = 1;
+                    D.g[0] = r0;                        // e[0] = ||r||
+                    st->rho = r0;
+                }
+            }
+        }
+    }
+}
+
+// v0 = r * (1 / ||r||) (pgmres.c:78-81)
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_scale_v0(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch)
+{
+    const int total = *nch;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!D.st->in_cycle) continue;
+        const double sc = 1.0 / D.st->r0;
+        T *V0 = (T *)D.V;
+        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) V0[d] = (T)(sc * D.r64[d]);
+    }
+}
+
+// ---------------------------------------------------------------- Arnoldi step
+// Dof parts are walked in sub-tiles of kThreads*4 dofs; within a sub-tile
+// the dot products accumulate in T, across sub-tiles and warps in FP64.
+constexpr int kSub = kThreads * 4;
+
+// pass 1: w = M^-1 t (t cleared), h1_j = <v_j, w>, j = 0..i
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_dots1(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
+{
+    __shared__ double red[kPartStride][kThreads / 32];
+    __shared__ double tot[kPartStride];
+    const int total = *nch;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!D.st->in_cycle) continue;
+        T *w = (T *)D.w, *t = (T *)D.t;
+        const T *V = (const T *)D.V;
+        const T *invd = sizeof(T) == 8 ? (const T *)D.invd64 : (const T *)D.invd32;
+        for (int j = threadIdx.x; j <= i * (kThreads / 32) + (kThreads / 32 - 1); j += blockDim.x)
+            (&red[0][0])[j] = 0.0;
+        __syncthreads();
+        for (int base = k.d0; base < k.d1; base += kSub) {
+            T wv[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                int d = base + threadIdx.x + q * kThreads;
+                T v = 0;
+                if (d < k.d1) {
+                    if (D.precond == FG_PRECOND_BLOCKDIAG) v = w[d];
+                    else {
+                        T tv = t[d];
+                        v = D.precond == FG_PRECOND_DIAG ? tv * invd[d] : tv;
+                        w[d] = v;
+                    }
+                    t[d] = (T)0;
+                }
+                wv[q] = v;
+            }
+            for (int j = 0; j <= i; ++j) {
+                const T *vj = V + (size_t)j * D.n_pad;
+                T a = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int d = base + threadIdx.x + q * kThreads;
+                    if (d < k.d1) a += vj[d] * wv[q];
+                }
+                a = warp_sum(a);
+                if (lane == 0) red[j][warp] += (double)a;
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+            double s = 0;
+            for (int w8 = 0; w8 < kThreads / 32; ++w8) s += red[j][w8];
+            D.part[k.part * kPartStride + j] = s;
+        }
+        if (last_part(D, 1)) {
+            reduce_parts(D, i + 1, tot);
+            for (int j = threadIdx.x; j <= i; j += blockDim.x) D.H[j * D.kmax + i] = tot[j];
+        }
+    }
+}
+
+// pass 2: w -= sum_j h1_j v_j ; h2_j = <v_j, w>
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_orth1(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
+{
+    __shared__ double red[kPartStride][kThreads / 32];
+    __shared__ double tot[kPartStride];
+    __shared__ T hs[kPartStride];
+    const int total = *nch;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!D.st->in_cycle) continue;
+        T *w = (T *)D.w;
+        const T *V = (const T *)D.V;
+        for (int j = threadIdx.x; j <= i; j += blockDim.x) hs[j] = (T)D.H[j * D.kmax + i];
+        for (int j = threadIdx.x; j <= i * (kThreads / 32) + (kThreads / 32 - 1); j += blockDim.x)
+            (&red[0][0])[j] = 0.0;
+        __syncthreads();
+        for (int base = k.d0; base < k.d1; base += kSub) {
+            T wv[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                int d = base + threadIdx.x + q * kThreads;
+                wv[q] = d < k.d1 ? w[d] : (T)0;
+            }
+            for (int j = 0; j <= i; ++j) {
+                const T *vj = V + (size_t)j * D.n_pad;
+                const T h = hs[j];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int d = base + threadIdx.x + q * kThreads;
+                    if (d < k.d1) wv[q] -= h * vj[d];
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                int d = base + threadIdx.x + q * kThreads;
+                if (d < k.d1) w[d] = wv[q];
+            }
+            for (int j = 0; j <= i; ++j) {
+                const T *vj = V + (size_t)j * D.n_pad;
+                T a = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int d = base + threadIdx.x + q * kThreads;
+                    if (d < k.d1) a += vj[d] * wv[q];
+                }
+                a = warp_sum(a);
+                if (lane == 0) red[j][warp] += (double)a;
+            }
+        }
+        __syncthreads();
+        for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+            double s = 0;
+            for (int w8 = 0; w8 < kThreads / 32; ++w8) s += red[j][w8];
+            D.part[k.part * kPartStride + j] = s;
+        }
+        if (last_part(D, 2)) {
+            reduce_parts(D, i + 1, tot);
+            for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+                D.hbuf[j] = tot[j];
+                D.H[j * D.kmax + i] += tot[j];
+            }
+        }
+    }
+}
+
+// pass 3: w -= sum_j h2_j v_j ; ||w||; then, in the last part, the Givens
+// rotations of column i and the residual estimate (pgmres.c:111-157).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_orth2(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
+{
+    __shared__ double red[kThreads / 32];
+    __shared__ double tot[1];
+    __shared__ T hs[kPartStride];
+    const int total = *nch;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!D.st->in_cycle) continue;
+        T *w = (T *)D.w;
+        const T *V = (const T *)D.V;
+        for (int j = threadIdx.x; j <= i; j += blockDim.x) hs[j] = (T)D.hbuf[j];
+        __syncthreads();
+        double acc = 0.0;
+        for (int base = k.d0; base < k.d1; base += kSub) {
+            T wv[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                int d = base + threadIdx.x + q * kThreads;
+                wv[q] = d < k.d1 ? w[d] : (T)0;
+            }
+            for (int j = 0; j <= i; ++j) {
+                const T *vj = V + (size_t)j * D.n_pad;
+                const T h = hs[j];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int d = base + threadIdx.x + q * kThreads;
+                    if (d < k.d1) wv[q] -= h * vj[d];
+                }
+            }
+            T a = 0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                int d = base + threadIdx.x + q * kThreads;
+                if (d < k.d1) { w[d] = wv[q]; a += wv[q] * wv[q]; }
+            }
+            acc += (double)a;
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) red[warp] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0;
+            for (int w8 = 0; w8 < kThreads / 32; ++w8) s += red[w8];
+            D.part[k.part * kPartStride] = s;
+        }
+        if (last_part(D, 3)) {
+            reduce_parts(D, 1, tot);
+            if (threadIdx.x == 0) {
+                SysState *st = D.st;
+                const int km = D.kmax;
+                double *H = D.H, *cs = D.cs, *sn = D.sn, *g = D.g;
+                double hn = sqrt(tot[0]);
+                st->hn = hn;
+                H[(i + 1) * km + i] = hn;
+                for (int j = 0; j <= i - 1; ++j) {
+                    double h1 = cs[j] * H[j * km + i] + sn[j] * H[(j + 1) * km + i];
+                    double h2 = -sn[j] * H[j * km + i] + cs[j] * H[(j + 1) * km + i];
+                    H[j * km + i] = h1;
+                    H[(j + 1) * km + i] = h2;
+                }
+                double r = sqrt(H[i * km + i] * H[i * km + i] + H[(i + 1) * km + i] * H[(i + 1) * km + i]);
+                cs[i] = H[i * km + i] / r;
+                sn[i] = H[(i + 1) * km + i] / r;
+                H[i * km + i] = r;
+                H[(i + 1) * km + i] = 0.0;
+                g[i + 1] = -sn[i] * g[i];
+                g[i] = cs[i] * g[i];
+                st->rho = fabs(g[i + 1]);
+                st->steps = i + 1;
+                st->iterations += 1;
+                double target = D.mixed ? st->target : st->eps;
+                if (!(r > 0.0) || !isfinite(st->rho)) {
+                    st->status = FG_ERR_BREAKDOWN;
+                    st->in_cycle = 0;
+                    if (!(r > 0.0)) st->steps = i;     // column i unusable
+                } else if (!(st->rho > target) || i + 1 >= D.kmax - 1 || !(hn > 0.0)) {
+                    st->in_cycle = 0;
+                }
+            }
+        }
+    }
+}
+
+// v_{i+1} = w * (1 / h_{i+1,i}) (pgmres.c:117)
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_normalize(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
+{
+    const int total = *nch;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!D.st->in_cycle) continue;
+        const T sc = (T)(1.0 / D.st->hn);
+        const T *w = (const T *)D.w;
+        T *v = (T *)D.V + (size_t)(i + 1) * D.n_pad;
+        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) v[d] = sc * w[d];
+    }
+}
+
+// ---------------------------------------------------------------- cycle end
+// y from the triangular system (pgmres.c:163-171), computed redundantly by
+// every CTA from the same data; x += V y (:173-175).  The last part does the
+// restart bookkeeping (:177-179).
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_update(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch)
+{
+    __shared__ double y[kPartStride];
+    const int total = *nch;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!D.st->live) continue;
+        const int m = D.st->steps;
+        const int km = D.kmax;
+        __syncthreads();
+        if (threadIdx.x == 0 && m > 0) {
+            int i = m - 1;
+            y[i] = D.g[i] / D.H[i * km + i];
+            for (int j = i - 1; j >= 0; --j) {
+                double s = 0.0;
+                for (int q = j + 1; q <= i; ++q) s = s + D.H[j * km + q] * y[q];
+                y[j] = (D.g[j] - s) / D.H[j * km + j];
+            }
+        }
+        __syncthreads();
+        const T *V = (const T *)D.V;
+        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) {
+            double xv = D.x[d];
+            for (int j = 0; j < m; ++j) xv = xv + (double)V[(size_t)j * D.n_pad + d] * y[j];
+            D.x[d] = xv;
+        }
+        if (last_part(D, 4)) {
+            if (threadIdx.x == 0) {
+                SysState *st = D.st;
+                st->cycles += 1;
+                st->in_cycle = 0;
+                if (st->status == FG_ERR_BREAKDOWN) { st->live = 0; }
+                else if (!D.mixed) {
+                    if (!(st->rho > st->eps)) { st->converged = 1; st->live = 0; }
+                    else if (st->cycles >= D.lmax) { st->status = FG_ERR_NOTCONV; st->live = 0; }
+                }
+            }
+        }
+    }
+}
+
+// final true residual: t64 holds A x
+__global__ void __launch_bounds__(kThreads)
+k_final(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch)
+{
+    __shared__ double red[kThreads / 32];
+    __shared__ double tot[1];
+    const int total = *nch;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        double a = 0;
+        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) {
+            double t = D.t64[d];
+            D.t64[d] = 0.0;
+            if (D.ftrue) { double s = D.ftrue[d] - t; a += s * s; }
+        }
+        a = warp_sum(a);
+        if (lane == 0) red[warp] = a;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double s = 0;
+            for (int w8 = 0; w8 < kThreads / 32; ++w8) s += red[w8];
+            D.part[k.part * kPartStride] = s;
+        }
+        if (last_part(D, 5)) {
+            reduce_parts(D, 1, tot);
+            if (threadIdx.x == 0) {
+                SysState *st = D.st;
+                st->true_res = D.ftrue ? (st->fnorm > 0 ? sqrt(tot[0]) / st->fnorm : sqrt(tot[0])) : NAN;
+            }
+        }
+    }
+}
+
+__global__ void k_init_state(const SysDev *__restrict__ sys, int nsys)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nsys) return;
+    SysState *st = sys[s].st;
+    memset(st, 0, sizeof(SysState));
+    st->live = 1;
+    st->first = 1;
+    st->status = FG_OK;
+    for (int c = 0; c < 8; ++c) sys[s].counter[c] = 0u;
+}
+
+// live flags of all systems into one array (one small copy per cycle)
+__global__ void k_live(const SysDev *__restrict__ sys, int nsys, int *out)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nsys) out[s] = sys[s].st->live;
+}
+
+// ---------------------------------------------------------------- host side
+int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+namespace {
+
+struct MvLaunch {
+    template <typename TA, typename TX, typename TY>
+    static void go(int S, dim3 g, cudaStream_t st, const SysDev *sys, const EChunk *ch, const int *nch,
+                   int gate, int in_sel, int out_sel, int step, const TX *ai, TY *ao)
+    {
+        switch (S) {
+        case 3: k_ebe_mv<3, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao); break;
+        case 6: k_ebe_mv<6, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao); break;
+        case 9: k_ebe_mv<9, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao); break;
+        case 12: k_ebe_mv<12, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao); break;
+        }
+    }
+};
+
+template <typename T>
+void launch_blockdiag(int B, dim3 g, cudaStream_t st, const SysDev *sys, const NChunk *ch, const int *nch,
+                      int gate, int sel, const T *ai, T *ao)
+{
+    switch (B) {
+    case 2: k_blockdiag<2, T><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, sel, ai, ao); break;
+    case 3: k_blockdiag<3, T><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, sel, ai, ao); break;
+    case 4: k_blockdiag<4, T><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, sel, ai, ao); break;
+    }
+}
+
+inline dim3 grid_for(int nchunks)
+{
+    int cap = 8 * sm_count();
+    return dim3((unsigned)std::max(1, std::min(nchunks, cap)));
+}
+
+int elem_chunk(int cnt)
+{
+    int per = cnt / (256 * 2 * sm_count());
+    return 256 * std::max(1, std::min(8, per));
+}
+
+int parts_for(int n)
+{
+    int p = (n + 511) / 512;
+    return std::max(1, std::min(kMaxParts, p));
+}
+
+}  // namespace
+
+// Chunk tables of one batch (device copies + host counts).
+struct Plan {
+    int nsys = 0, ncol = 0, S = 3, B = 1;
+    std::vector<int> ech_off;      // ncol+1 offsets into echunks
+    int n_dch = 0, n_nch = 0;
+    DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
+};
+
+static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig &cfg, std::vector<SysDev> &hs,
+                      cudaStream_t st)
+{
+    P.nsys = (int)mem.size();
+    P.S = mem[0].s->topo.S;
+    P.B = mem[0].s->topo.ndof;
+    P.ncol = 0;
+    for (auto &m : mem) {
+        if (m.s->topo.S != P.S) { set_error("a batch must hold systems of one block size"); return FG_ERR_ARG; }
+        P.ncol = std::max(P.ncol, m.s->topo.ncol);
+    }
+    std::vector<EChunk> ech;
+    P.ech_off.assign(P.ncol + 1, 0);
+    for (int c = 0; c < P.ncol; ++c) {
+        for (int s = 0; s < P.nsys; ++s) {
+            const Topology &t = mem[s].s->topo;
+            if (c >= t.ncol) continue;
+            int e0 = t.cptr[c], e1 = t.cptr[c + 1];
+            int cs = elem_chunk(e1 - e0);
+            for (int e = e0; e < e1; e += cs) ech.push_back({s, e, std::min(e + cs, e1)});
+        }
+        P.ech_off[c + 1] = (int)ech.size();
+    }
+    std::vector<DChunk> dch;
+    std::vector<NChunk> nch;
+    for (int s = 0; s < P.nsys; ++s) {
+        int n = mem[s].s->topo.n;
+        int np = hs[s].nparts;
+        for (int p = 0; p < np; ++p) {
+            int d0 = (int)((long long)n * p / np), d1 = (int)((long long)n * (p + 1) / np);
+            dch.push_back({s, p, d0, d1});
+        }
+        int nn = mem[s].s->topo.nnodes;
+        for (int a = 0; a < nn; a += 1024) nch.push_back({s, a, std::min(a + 1024, nn)});
+    }
+    P.n_dch = (int)dch.size();
+    P.n_nch = (int)nch.size();
+    std::vector<int> ecounts(P.ncol);
+    for (int c = 0; c < P.ncol; ++c) ecounts[c] = P.ech_off[c + 1] - P.ech_off[c];
+    int r;
+    if ((r = P.sysdev.alloc(sizeof(SysDev) * hs.size())) ||
+        (r = P.echunks.alloc(sizeof(EChunk) * std::max<size_t>(1, ech.size()))) ||
+        (r = P.ecount.alloc(sizeof(int) * std::max(1, P.ncol))) ||
+        (r = P.dchunks.alloc(sizeof(DChunk) * std::max<size_t>(1, dch.size()))) ||
+        (r = P.dcount.alloc(sizeof(int))) ||
+        (r = P.nchunks.alloc(sizeof(NChunk) * std::max<size_t>(1, nch.size()))) ||
+        (r = P.ncount.alloc(sizeof(int))) ||
+        (r = P.live.alloc(sizeof(int) * P.nsys)))
+        return r;
+    FG_CUDA(cudaMemcpyAsync(P.sysdev.p, hs.data(), sizeof(SysDev) * hs.size(), cudaMemcpyHostToDevice, st));
+    if (!ech.empty())
+        FG_CUDA(cudaMemcpyAsync(P.echunks.p, ech.data(), sizeof(EChunk) * ech.size(), cudaMemcpyHostToDevice, st));
+    if (P.ncol)
+        FG_CUDA(cudaMemcpyAsync(P.ecount.p, ecounts.data(), sizeof(int) * P.ncol, cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(P.dchunks.p, dch.data(), sizeof(DChunk) * dch.size(), cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(P.dcount.p, &P.n_dch, sizeof(int), cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(P.nchunks.p, nch.data(), sizeof(NChunk) * nch.size(), cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemcpyAsync(P.ncount.p, &P.n_nch, sizeof(int), cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaStreamSynchronize(st));   // host vectors above go out of scope
+    return FG_OK;
+}
+
+// Enqueue the matvec over all colours: mode 0 (x -> t64, FP64, gate live)
+// or mode 1 (V[step] -> t, T, gate in_cycle).
+template <typename T>
+static void enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
+{
+    const SysDev *sys = P.sysdev.as<SysDev>();
+    for (int c = 0; c < P.ncol; ++c) {
+        int cnt = P.ech_off[c + 1] - P.ech_off[c];
+        if (!cnt) continue;
+        const EChunk *ch = P.echunks.as<EChunk>() + P.ech_off[c];
+        const int *nc = P.ecount.as<int>() + c;
+        if (mode == 0)
+            MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, ch, nc, 0, 0, 0, 0, nullptr, nullptr);
+        else
+            MvLaunch::go<T, T, T>(P.S, grid_for(cnt), st, sys, ch, nc, 1, 1, 1, step, nullptr, nullptr);
+    }
+}
+
+template <typename T>
+static void enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
+{
+    const SysDev *sys = P.sysdev.as<SysDev>();
+    const DChunk *dc = P.dchunks.as<DChunk>();
+    const int *nd = P.dcount.as<int>();
+    dim3 gd = grid_for(P.n_dch), gn = grid_for(P.n_nch);
+    const bool bd = cfg.precond == FG_PRECOND_BLOCKDIAG;
+    enqueue_matvec<T>(P, 0, 0, st);
+    if (bd) launch_blockdiag<double>(P.B, gn, st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 0, 0, nullptr, nullptr);
+    k_start<<<gd, kThreads, 0, st>>>(sys, dc, nd);
+    k_scale_v0<T><<<gd, kThreads, 0, st>>>(sys, dc, nd);
+    for (int i = 0; i < cfg.kmax - 1; ++i) {
+        enqueue_matvec<T>(P, 1, i, st);
+        if (bd) launch_blockdiag<T>(P.B, gn, st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 1, 1, nullptr, nullptr);
+        k_dots1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        k_orth1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        k_orth2<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        k_normalize<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+    }
+    k_update<T><<<gd, kThreads, 0, st>>>(sys, dc, nd);
+    k_live<<<(P.nsys + 255) / 256, 256, 0, st>>>(sys, P.nsys, P.live.as<int>());
+}
+
+static int ensure_workspace(fg_system *s, int kmax, int mixed)
+{
+    Workspace &w = s->ws;
+    if (w.kmax >= kmax && w.mixed == mixed) return FG_OK;
+    w.kmax = 0;
+    w.mixed = -1;
+    size_t np = (size_t)s->n_pad;
+    size_t ts = mixed ? sizeof(float) : sizeof(double);
+    int r;
+    if ((r = w.V.alloc(ts * np * kmax)) || (r = w.w.alloc(ts * np)) || (r = w.t.alloc(ts * np)) ||
+        (r = w.x.alloc(8 * np)) || (r = w.b.alloc(8 * np)) || (r = w.ftrue.alloc(8 * np)) ||
+        (r = w.r64.alloc(8 * np)) || (r = w.t64.alloc(8 * np)) || (r = w.u64.alloc(8 * np)) ||
+        (r = w.small.alloc(8 * ((size_t)(kmax + 1) * kmax + 4 * (kmax + 1)))) ||
+        (r = w.part.alloc(8 * (size_t)kMaxParts * kPartStride)) ||
+        (r = w.counter.alloc(sizeof(unsigned) * 8)) || (r = w.state.alloc(sizeof(SysState))))
+        return r;
+    w.kmax = kmax;
+    w.mixed = mixed;
+    return FG_OK;
+}
+
+static SysDev make_desc(fg_system *s, const SolveConfig &cfg, bool has_f)
+{
+    const Topology &t = s->topo;
+    Workspace &w = s->ws;
+    SysDev D{};
+    D.n = t.n; D.n_pad = s->n_pad; D.nel = t.nel; D.nel_pad = s->nel_pad; D.S = t.S; D.ndof = t.ndof;
+    D.ncol = t.ncol; D.nparts = parts_for(t.n); D.nnodes = t.nnodes;
+    D.kmax = cfg.kmax; D.lmax = cfg.lmax; D.mixed = cfg.mixed; D.precond = cfg.precond;
+    D.tol = cfg.tol; D.inner_tol = cfg.inner_tol;
+    D.lm = s->lm.as<int>(); D.A64 = s->A64.as<double>(); D.A32 = s->A32.as<float>();
+    D.invd64 = s->invd64.as<double>(); D.invd32 = s->invd32.as<float>();
+    D.node_dof = s->node_dof.as<int>(); D.ibd64 = s->ibd64.as<double>(); D.ibd32 = s->ibd32.as<float>();
+    D.x = w.x.as<double>(); D.b = w.b.as<double>(); D.ftrue = has_f ? w.ftrue.as<double>() : nullptr;
+    D.r64 = w.r64.as<double>(); D.t64 = w.t64.as<double>(); D.u64 = w.u64.as<double>();
+    D.V = w.V.p; D.w = w.w.p; D.t = w.t.p;
+    double *sm = w.small.as<double>();
+    D.H = sm;
+    D.g = sm + (size_t)(cfg.kmax + 1) * cfg.kmax;
+    D.cs = D.g + (cfg.kmax + 1);
+    D.sn = D.cs + (cfg.kmax + 1);
+    D.hbuf = D.sn + (cfg.kmax + 1);
+    D.part = w.part.as<double>();
+    D.counter = w.counter.as<unsigned>();
+    D.st = w.state.as<SysState>();
+    return D;
+}
+
+int solve_batch(std::vector<BatchMember> &mem, const SolveConfig &cfg, fg_solve_stats *stats, cudaStream_t st)
+{
+    if (mem.empty()) return FG_OK;
+    if (cfg.kmax < 2 || cfg.kmax > kPartStride - 4) { set_error("kmax must be in [2, 60]"); return FG_ERR_ARG; }
+    if (cfg.lmax < 1) { set_error("lmax must be >= 1"); return FG_ERR_ARG; }
+    for (auto &m : mem) {
+        fg_system *s = m.s;
+        if (!s->blocks_ok) { set_error("solve before element blocks were set"); return FG_ERR_STATE; }
+        if (cfg.precond != FG_PRECOND_NONE && s->precond != cfg.precond) {
+            set_error("solve with a preconditioner that was not set up"); return FG_ERR_STATE;
+        }
+        if (cfg.precond == FG_PRECOND_BLOCKDIAG && s->topo.ndof < 2) {
+            set_error("block-diagonal preconditioner needs ndof >= 2"); return FG_ERR_UNSUPPORTED;
+        }
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<SysDev> hs;
+    hs.reserve(mem.size());
+    for (auto &m : mem) {
+        fg_system *s = m.s;
+        int r = ensure_workspace(s, cfg.kmax, cfg.mixed);
+        if (r) return r;
+        Workspace &w = s->ws;
+        size_t vb = 8 * (size_t)s->n_pad;
+        FG_CUDA(cudaMemsetAsync(w.x.p, 0, vb, st));
+        FG_CUDA(cudaMemsetAsync(w.t64.p, 0, vb, st));
+        FG_CUDA(cudaMemsetAsync(w.t.p, 0, (cfg.mixed ? 4 : 8) * (size_t)s->n_pad, st));
+        FG_CUDA(cudaMemsetAsync(w.V.p, 0, (cfg.mixed ? 4 : 8) * (size_t)s->n_pad * cfg.kmax, st));
+        FG_CUDA(cudaMemsetAsync(w.small.p, 0, w.small.bytes, st));
+        if (cfg.device_io) {
+            FG_CUDA(cudaMemcpyAsync(w.b.p, m.B, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToDevice, st));
+            if (m.Ftrue) FG_CUDA(cudaMemcpyAsync(w.ftrue.p, m.Ftrue, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToDevice, st));
+        } else {
+            // host vectors in reference numbering -> staging (r64) -> internal
+            size_t hb = 8 * (size_t)(s->topo.n + 1);
+            FG_CUDA(cudaMemcpyAsync(w.r64.p, m.B, hb, cudaMemcpyHostToDevice, st));
+            if ((r = permute_in(s, w.r64.as<double>(), w.b.as<double>(), st))) return r;
+            if (m.Ftrue) {
+                FG_CUDA(cudaMemcpyAsync(w.u64.p, m.Ftrue, hb, cudaMemcpyHostToDevice, st));
+                if ((r = permute_in(s, w.u64.as<double>(), w.ftrue.as<double>(), st))) return r;
+            }
+        }
+        hs.push_back(make_desc(s, cfg, m.Ftrue != nullptr));
+    }
+    Plan P;
+    int r = build_plan(P, mem, cfg, hs, st);
+    if (r) return r;
+    const int nsys = P.nsys;
+    k_init_state<<<(nsys + 127) / 128, 128, 0, st>>>(P.sysdev.as<SysDev>(), nsys);
+    FG_CUDA(cudaGetLastError());
+
+    // one restart cycle as a CUDA graph, replayed until no system is live
+    cudaGraphExec_t exec = nullptr;
+    if (cfg.use_graph) {
+        cudaGraph_t graph = nullptr;
+        FG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        if (cfg.mixed) enqueue_cycle<float>(P, cfg, st);
+        else enqueue_cycle<double>(P, cfg, st);
+        cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
+        ce = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+    }
+    std::vector<int> live(nsys, 1);
+    int *h_live = nullptr;
+    FG_CUDA(cudaMallocHost(&h_live, sizeof(int) * nsys));
+    int guard = cfg.lmax + 2;
+    int rc = FG_OK;
+    for (int cyc = 0; cyc < guard; ++cyc) {
+        cudaError_t ce;
+        if (exec) ce = cudaGraphLaunch(exec, st);
+        else {
+            if (cfg.mixed) enqueue_cycle<float>(P, cfg, st);
+            else enqueue_cycle<double>(P, cfg, st);
+            ce = cudaGetLastError();
+        }
+        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_live, P.live.p, sizeof(int) * nsys, cudaMemcpyDeviceToHost, st);
+        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+        if (ce != cudaSuccess) { rc = cuda_fail(ce, "GMRES cycle"); break; }
+        int any = 0;
+        for (int s = 0; s < nsys; ++s) any |= h_live[s];
+        if (!any) break;
+    }
+    cudaFreeHost(h_live);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (rc) return rc;
+    // final true residual for every system
+    {
+        const SysDev *sys = P.sysdev.as<SysDev>();
+        for (int c = 0; c < P.ncol; ++c) {
+            int cnt = P.ech_off[c + 1] - P.ech_off[c];
+            if (!cnt) continue;
+            MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, P.echunks.as<EChunk>() + P.ech_off[c],
+                                                 P.ecount.as<int>() + c, -1, 0, 0, 0, nullptr, nullptr);
+        }
+        k_final<<<grid_for(P.n_dch), kThreads, 0, st>>>(sys, P.dchunks.as<DChunk>(), P.dcount.as<int>());
+        FG_CUDA(cudaGetLastError());
+    }
+    // results
+    for (int s = 0; s < nsys; ++s) {
+        BatchMember &m = mem[s];
+        fg_system *sy = m.s;
+        if (m.X) {
+            if (cfg.device_io) {
+                FG_CUDA(cudaMemcpyAsync(m.X, sy->ws.x.p, 8 * (size_t)(sy->topo.n + 1), cudaMemcpyDeviceToDevice, st));
+            } else {
+                if ((r = permute_out(sy, sy->ws.x.as<double>(), sy->ws.r64.as<double>(), st))) return r;
+                FG_CUDA(cudaMemcpyAsync(m.X, sy->ws.r64.p, 8 * (size_t)(sy->topo.n + 1), cudaMemcpyDeviceToHost, st));
+            }
+        }
+    }
+    std::vector<SysState> sts(nsys);
+    for (int s = 0; s < nsys; ++s)
+        FG_CUDA(cudaMemcpyAsync(&sts[s], mem[s].s->ws.state.p, sizeof(SysState), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    int worst = FG_OK;
+    for (int s = 0; s < nsys; ++s) {
+        if (!stats) break;
+        fg_solve_stats &o = stats[s];
+        o.iterations = sts[s].iterations;
+        o.cycles = sts[s].cycles;
+        o.converged = sts[s].converged;
+        o.status = sts[s].status;
+        o.rho = sts[s].rho;
+        o.eps = sts[s].eps;
+        o.true_rel_residual = sts[s].true_res;
+        o.seconds = secs;
+        if (o.status != FG_OK && worst == FG_OK) worst = o.status;
+    }
+    return FG_OK;
+}
+
+// Single matvec on device vectors (internal numbering, FP64 in/out).
+int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaStream_t st)
+{
+    if (!s->blocks_ok) { set_error("matvec before element blocks were set"); return FG_ERR_STATE; }
+    const Topology &t = s->topo;
+    SysDev D{};
+    D.n = t.n; D.n_pad = s->n_pad; D.nel = t.nel; D.nel_pad = s->nel_pad; D.S = t.S;
+    D.lm = s->lm.as<int>(); D.A64 = s->A64.as<double>(); D.A32 = s->A32.as<float>();
+    DevMem sd, ch, cnt;
+    std::vector<EChunk> ech;
+    std::vector<int> off(t.ncol + 1, 0), counts(t.ncol);
+    for (int c = 0; c < t.ncol; ++c) {
+        int e0 = t.cptr[c], e1 = t.cptr[c + 1], cs = elem_chunk(e1 - e0);
+        for (int e = e0; e < e1; e += cs) ech.push_back({0, e, std::min(e + cs, e1)});
+        off[c + 1] = (int)ech.size();
+        counts[c] = off[c + 1] - off[c];
+    }
+    int r;
+    if ((r = sd.alloc(sizeof(SysDev))) || (r = ch.alloc(sizeof(EChunk) * std::max<size_t>(1, ech.size()))) ||
+        (r = cnt.alloc(sizeof(int) * std::max(1, t.ncol))))
+        return r;
+    FG_CUDA(cudaMemcpyAsync(sd.p, &D, sizeof(SysDev), cudaMemcpyHostToDevice, st));
+    if (!ech.empty()) FG_CUDA(cudaMemcpyAsync(ch.p, ech.data(), sizeof(EChunk) * ech.size(), cudaMemcpyHostToDevice, st));
+    if (t.ncol) FG_CUDA(cudaMemcpyAsync(cnt.p, counts.data(), sizeof(int) * t.ncol, cudaMemcpyHostToDevice, st));
+    FG_CUDA(cudaMemsetAsync(y, 0, 8 * (size_t)(t.n + 1), st));
+    for (int c = 0; c < t.ncol; ++c) {
+        if (!counts[c]) continue;
+        const EChunk *cp = ch.as<EChunk>() + off[c];
+        const int *np = cnt.as<int>() + c;
+        if (precision == 32)
+            MvLaunch::go<float, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y);
+        else
+            MvLaunch::go<double, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y);
+    }
+    FG_CUDA(cudaGetLastError());
+    FG_CUDA(cudaStreamSynchronize(st));
+    return FG_OK;
+}
+
+}  // namespace fg

@@ -1,0 +1,421 @@
+// Set-up kernels: block layout, Diag and nodal block-diagonal
+// preconditioner set-up, SUPG/CAU transport assembly, renumbering.
+//
+// This translation unit is compiled with -fmad=false: every product and sum
+// is rounded as written, in the order the reference writes it, so the
+// element blocks, right-hand side, diagonal and block inverses agree with
+// the reference's C to the last bit (sqrt and division are correctly
+// rounded in both).
+#include <algorithm>
+#include <cmath>
+
+#include "system.h"
+
+namespace fg {
+
+// ---------------------------------------------------------------- renumbering
+__global__ void k_permute(const int *__restrict__ map, const double *__restrict__ src, double *__restrict__ dst,
+                          int n, int gather)
+{
+    // gather: dst[i] = src[map[i]]   (map = perm: internal <- reference)
+    // scatter: dst[map[i]] = src[i]  (map = perm: reference <- internal)
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        if (gather) dst[i] = src[map[i]];
+        else dst[map[i]] = src[i];
+    }
+    if (i == 0) dst[n] = 0.0;
+}
+
+int permute_in(fg_system *s, const double *ref_dev, double *int_dev, cudaStream_t st)
+{
+    int n = s->topo.n;
+    k_permute<<<(n + 255) / 256 + 1, 256, 0, st>>>(s->perm.as<int>(), ref_dev, int_dev, n, 1);
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+}
+
+int permute_out(fg_system *s, const double *int_dev, double *ref_dev, cudaStream_t st)
+{
+    int n = s->topo.n;
+    k_permute<<<(n + 255) / 256 + 1, 256, 0, st>>>(s->perm.as<int>(), int_dev, ref_dev, n, 0);
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+}
+
+// ---------------------------------------------------------------- blocks
+// Host layout (reference element order, row-major S x S) -> SoA in the
+// internal element order: A64[k][pos] = raw[eorder[pos]][k].
+__global__ void k_blocks_in(const double *__restrict__ raw, const int *__restrict__ eorder, double *__restrict__ A64,
+                            float *__restrict__ A32, int nel, int ld, int SS)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const double *src = raw + (size_t)eorder[pos] * SS;
+    for (int k = 0; k < SS; ++k) {
+        double v = src[k];
+        A64[(size_t)k * ld + pos] = v;
+        A32[(size_t)k * ld + pos] = (float)v;
+    }
+}
+
+__global__ void k_blocks_out(double *__restrict__ raw, const int *__restrict__ eorder, const double *__restrict__ A64,
+                             int nel, int ld, int SS)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    double *dst = raw + (size_t)eorder[pos] * SS;
+    for (int k = 0; k < SS; ++k) dst[k] = A64[(size_t)k * ld + pos];
+}
+
+__global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, size_t n)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+int convert_blocks(fg_system *s, cudaStream_t st)
+{
+    size_t n = (size_t)s->topo.S * s->topo.S * s->nel_pad;
+    k_to_f32<<<std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 8 * sm_count())), 256, 0, st>>>(
+        s->A64.as<double>(), s->A32.as<float>(), n);
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+}
+
+int upload_blocks_raw(fg_system *s, const double *raw_dev, cudaStream_t st)
+{
+    int nel = s->topo.nel;
+    if (nel > 0)
+        k_blocks_in<<<(nel + 255) / 256, 256, 0, st>>>(raw_dev, s->eorder.as<int>(), s->A64.as<double>(),
+                                                      s->A32.as<float>(), nel, s->nel_pad, s->topo.S * s->topo.S);
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+}
+
+int download_blocks_raw(const fg_system *s, double *raw_dev, cudaStream_t st)
+{
+    int nel = s->topo.nel;
+    if (nel > 0)
+        k_blocks_out<<<(nel + 255) / 256, 256, 0, st>>>(raw_dev, s->eorder.as<int>(), s->A64.as<double>(), nel,
+                                                       s->nel_pad, s->topo.S * s->topo.S);
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+}
+
+// ---------------------------------------------------------------- Diag
+// Diag_precond_EBE_setup (EBE/Diag_precond_EBE_setup.c:3-32), one thread
+// per dof, gathering the element diagonals in reference element order so
+// the sum is the reference's; accumulate keeps the previous Diag as the
+// reference does across nonlinear iterations.
+__global__ void k_diag_setup(const int *__restrict__ dptr, const int *__restrict__ dinc, const double *__restrict__ A64,
+                             int ld, int S, int n, int accumulate, double *__restrict__ diag,
+                             double *__restrict__ invd64, float *__restrict__ invd32, double *__restrict__ F)
+{
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    double s = accumulate ? diag[d] : 0.0;
+    for (int q = dptr[d]; q < dptr[d + 1]; ++q) {
+        int pos = dinc[q] >> 4, r = dinc[q] & 15;
+        s += A64[(size_t)(r * S + r) * ld + pos];
+    }
+    diag[d] = s;
+    double inv = 1.0 / s;
+    invd64[d] = inv;
+    invd32[d] = (float)inv;
+    if (F) F[d] *= inv;
+}
+
+// ---------------------------------------------------------------- block diagonal
+// Nodal B x B diagonal blocks (EBE/BlockDiag_precond_EBE_setup.c:70-80,
+// EBE/BlockDiagDOF3_precond_EBE_setup.c:66-76) and their closed-form
+// inverses (matrix_Inverse :90-147, DOF3_matrix_Inverse :84-124).
+__device__ void inv4(const double *B, double *R, bool quirk)
+{
+    double a=B[0],b=B[1],c=B[2],d=B[3],e=B[4],f=B[5],g=B[6],h=B[7];
+    double i=B[8],j=B[9],k=B[10],l=B[11],m=B[12],n=B[13],o=B[14],p=B[15];
+    double det = (a*f*k*p - a*f*l*o - a*g*j*p + a*g*l*n + a*h*j*o - a*h*k*n
+                 -b*e*k*p + b*e*l*o + b*g*i*p - b*g*l*m - b*h*i*o + b*h*k*m +
+                 c*(e*j*p - e*l*n - f*i*p + f*l*m + h*i*n - h*j*m) +
+                 d*(-e*j*o + e*k*n + f*i*o - f*k*m - g*i*n + g*j*m));
+    double q = 1.0 / det;
+    R[0]  = q*(-h*k*n + g*l*n + h*j*o - f*l*o - g*j*p + f*k*p);
+    R[1]  = q*(d*k*n - c*l*n - d*j*o + b*l*o + c*j*p - b*k*p);
+    R[2]  = q*(-d*g*n + c*h*n + d*f*o - b*h*o - c*f*p + b*g*p);
+    R[3]  = q*(d*g*j - c*h*j - d*f*k + b*h*k + c*f*l - b*g*l);
+    R[4]  = q*(h*k*m - g*l*m - h*i*o + e*l*o + g*i*p - e*k*p);
+    R[5]  = q*(-d*k*m + c*l*m + d*i*o - a*l*o - c*i*p + a*k*p);
+    R[6]  = q*(d*g*m - c*h*m - d*e*o + a*h*o + c*e*p - a*g*p);
+    R[7]  = q*(-d*g*i + c*h*i + d*e*k - a*h*k - c*e*l + a*g*l);
+    R[8]  = q*(-h*j*m + f*l*m + h*i*n - e*l*n - f*i*p + e*j*p);
+    R[9]  = q*(d*j*m - b*l*m - d*i*n + a*l*n + b*i*p - a*j*p);
+    R[10] = q*(-d*f*m + b*h*m + d*e*n - a*h*n - b*e*p + a*f*p);
+    R[11] = q*(d*f*i - b*h*i - d*e*j + a*h*j + b*e*l - a*f*l);
+    R[12] = q*(g*j*m - f*k*m - g*i*n + e*k*n + f*i*o - e*j*o);
+    R[13] = q*(-c*j*m + b*k*m + c*i*n - a*k*n - b*i*o + a*j*o);
+    // the reference writes c*j*m in entry 14 where the cofactor has c*f*m
+    R[14] = q*((quirk ? c*j*m : c*f*m) - b*g*m - c*e*n + a*g*n + b*e*o - a*f*o);
+    R[15] = q*(-c*f*i + b*g*i + c*e*j - a*g*j - b*e*k + a*f*k);
+}
+
+__device__ void inv3(const double *B, double *R)
+{
+    double a=B[0],b=B[1],c=B[2],d=B[3],e=B[4],f=B[5],g=B[6],h=B[7],i=B[8];
+    double det = a*e*i - a*f*h - b*d*i + b*f*g + c*d*h - c*e*g;
+    double q = 1.0 / det;
+    R[0] = q*(e*i - f*h); R[1] = q*(c*h - b*i); R[2] = q*(b*f - c*e);
+    R[3] = q*(f*g - d*i); R[4] = q*(a*i - c*g); R[5] = q*(c*d - a*f);
+    R[6] = q*(d*h - e*g); R[7] = q*(b*g - a*h); R[8] = q*(a*e - b*d);
+}
+
+__device__ void inv2(const double *B, double *R)
+{
+    double det = B[0] * B[3] - B[1] * B[2];
+    double q = 1.0 / det;
+    R[0] = q * B[3]; R[1] = -q * B[1]; R[2] = -q * B[2]; R[3] = q * B[0];
+}
+
+template <int B>
+__global__ void k_blockdiag_setup(const int *__restrict__ nptr, const int *__restrict__ ninc, const double *__restrict__ A64,
+                                  int ld, int nnodes, int quirk, double *__restrict__ bd, double *__restrict__ ibd64,
+                                  float *__restrict__ ibd32)
+{
+    int nd = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nd >= nnodes) return;
+    const int S = 3 * B;
+    double blk[B * B], inv[B * B];
+    for (int q = 0; q < B * B; ++q) blk[q] = 0.0;
+    for (int q = nptr[nd]; q < nptr[nd + 1]; ++q) {
+        int pos = ninc[q] >> 2, v = ninc[q] & 3;
+        for (int r = 0; r < B; ++r)
+            for (int c = 0; c < B; ++c) blk[r * B + c] += A64[(size_t)((B * v + r) * S + B * v + c) * ld + pos];
+    }
+    if (B == 4) inv4(blk, inv, quirk != 0);
+    else if (B == 3) inv3(blk, inv);
+    else inv2(blk, inv);
+    for (int q = 0; q < B * B; ++q) {
+        bd[(size_t)nd * B * B + q] = blk[q];
+        ibd64[(size_t)nd * B * B + q] = inv[q];
+        ibd32[(size_t)nd * B * B + q] = (float)inv[q];
+    }
+}
+
+// F <- B^-1 F per node (BlockDiag_precond.c:12-26), Dirichlet dofs read 0
+template <int B>
+__global__ void k_blockdiag_apply64(const int *__restrict__ node_dof, const double *__restrict__ ibd, int nnodes, int n,
+                                    const double *__restrict__ p, double *__restrict__ z)
+{
+    int nd = blockIdx.x * blockDim.x + threadIdx.x;
+    if (nd >= nnodes) return;
+    int id[B];
+    double v[B];
+    for (int a = 0; a < B; ++a) { id[a] = node_dof[nd * B + a]; v[a] = id[a] == n ? 0.0 : p[id[a]]; }
+    const double *m = ibd + (size_t)nd * B * B;
+    for (int r = 0; r < B; ++r) {
+        double s = m[r * B] * v[0];
+        for (int q = 1; q < B; ++q) s += m[r * B + q] * v[q];
+        if (id[r] != n) z[id[r]] = s;
+    }
+}
+
+int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (kind == FG_PRECOND_NONE) { s->precond = kind; return FG_OK; }
+    if (!s->blocks_ok) { set_error("preconditioner set-up before element blocks were set"); return FG_ERR_STATE; }
+    if (kind == FG_PRECOND_DIAG) {
+        if (t.n > 0)
+            k_diag_setup<<<(t.n + 255) / 256, 256, 0, st>>>(s->dinc_ptr.as<int>(), s->dinc.as<int>(), s->A64.as<double>(),
+                                                           s->nel_pad, t.S, t.n, (flags & FG_SETUP_ACCUMULATE) ? 1 : 0,
+                                                           s->diag.as<double>(), s->invd64.as<double>(),
+                                                           s->invd32.as<float>(), F_dev);
+        FG_CUDA(cudaGetLastError());
+        s->precond = kind;
+        return FG_OK;
+    }
+    if (kind == FG_PRECOND_BLOCKDIAG) {
+        int B = t.ndof;
+        if (B < 2) { set_error("block-diagonal preconditioner needs ndof >= 2"); return FG_ERR_UNSUPPORTED; }
+        int g = (t.nnodes + 127) / 128;
+        int q = (flags & FG_SETUP_REF_QUIRKS) ? 1 : 0;
+        const int *np = s->ninc_ptr.as<int>(), *ni = s->ninc.as<int>();
+        double *bd = s->bd.as<double>(), *i64 = s->ibd64.as<double>();
+        float *i32 = s->ibd32.as<float>();
+        if (B == 4) k_blockdiag_setup<4><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32);
+        else if (B == 3) k_blockdiag_setup<3><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32);
+        else k_blockdiag_setup<2><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32);
+        FG_CUDA(cudaGetLastError());
+        s->precond = kind;
+        if (F_dev) {
+            if (B == 4) k_blockdiag_apply64<4><<<g, 128, 0, st>>>(s->node_dof.as<int>(), i64, t.nnodes, t.n, F_dev, F_dev);
+            else if (B == 3) k_blockdiag_apply64<3><<<g, 128, 0, st>>>(s->node_dof.as<int>(), i64, t.nnodes, t.n, F_dev, F_dev);
+            else k_blockdiag_apply64<2><<<g, 128, 0, st>>>(s->node_dof.as<int>(), i64, t.nnodes, t.n, F_dev, F_dev);
+            FG_CUDA(cudaGetLastError());
+        }
+        return FG_OK;
+    }
+    set_error("unknown preconditioner kind");
+    return FG_ERR_ARG;
+}
+
+__global__ void k_diag_apply(const double *__restrict__ invd, int n, const double *p, double *z)
+{
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d < n) z[d] = p[d] * invd[d];
+    if (d == n) z[n] = 0.0;
+}
+
+int precond_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (s->precond == FG_PRECOND_DIAG) {
+        k_diag_apply<<<(t.n + 256) / 256, 256, 0, st>>>(s->invd64.as<double>(), t.n, p, z);
+    } else if (s->precond == FG_PRECOND_BLOCKDIAG) {
+        int g = (t.nnodes + 127) / 128, B = t.ndof;
+        if (p != z) FG_CUDA(cudaMemcpyAsync(z, p, 8 * (size_t)(t.n + 1), cudaMemcpyDeviceToDevice, st));
+        // in place is safe: each node reads its own dofs before writing them
+        if (B == 4) k_blockdiag_apply64<4><<<g, 128, 0, st>>>(s->node_dof.as<int>(), s->ibd64.as<double>(), t.nnodes, t.n, z, z);
+        else if (B == 3) k_blockdiag_apply64<3><<<g, 128, 0, st>>>(s->node_dof.as<int>(), s->ibd64.as<double>(), t.nnodes, t.n, z, z);
+        else k_blockdiag_apply64<2><<<g, 128, 0, st>>>(s->node_dof.as<int>(), s->ibd64.as<double>(), t.nnodes, t.n, z, z);
+    } else if (p != z) {
+        FG_CUDA(cudaMemcpyAsync(z, p, 8 * (size_t)(t.n + 1), cudaMemcpyDeviceToDevice, st));
+    }
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+}
+
+// ---------------------------------------------------------------- SUPG/CAU transport
+// Build_K_F_SUPG.c:47-177 with CAU_ShockCapture.c:3-31 and
+// h_shock_2sqrtArea.c, one thread per element (internal order).  Writes the
+// 3x3 block (ebe_assembly.c) into the SoA layout and the element load
+// vector Fe; the Dirichlet lifting is applied in k_transport_F.
+__device__ double cau_eu(double kx, double ky, double bx, double by, double gamma, double ue1, double ue2, double ue3,
+                         double ueb, double feb, double y23, double y31, double y12, double x32, double x13,
+                         double x21, double invArea, double h)
+{
+    double third = 1. / 3.;
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = bgu + gamma*ueb - feb;
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    double bxp = bgu*gx/(ng*ng);
+    double byp = bgu*gy/(ng*ng);
+    double kp = bxp*bxp*kx + byp*byp*ky;
+    double nbp = sqrt(bxp*bxp + byp*byp);
+    double Pe = 0.5*h*nbp*nbp*nbp/kp;
+    if (ng > 0) {
+        if (third*Pe < 0.7) return 0.5*h*third*Pe*fabs(Ru)/ng;
+        return 0.5*h*0.7*fabs(Ru)/ng;
+    }
+    return 0;
+}
+
+__global__ void k_transport_elem(int nel, int ld, const int *__restrict__ gien, const double *__restrict__ gx,
+                                 const double *__restrict__ gy, const int *__restrict__ gtype,
+                                 const int *__restrict__ node_dof, const double *__restrict__ up,
+                                 const double *__restrict__ u, fg_transport_coeffs cf,
+                                 double *__restrict__ A64, double *__restrict__ Fe)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const double third = 1.0/3.0, sixth = 1.0/6.0, twelfth = 1.0/12.0;
+    const double kx = cf.k, ky = cf.k, gamma = cf.gamma;
+    int J1 = gien[pos], J2 = gien[ld + pos], J3 = gien[2 * (size_t)ld + pos];
+    double X0 = gx[J1], X1 = gx[J2], X2 = gx[J3];
+    double Y0 = gy[J1], Y1 = gy[J2], Y2 = gy[J3];
+    double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+    double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+    double TwoA = x21*y31 - x13*y12;
+    double Area = 0.5*TwoA;
+    double invArea = 1.0/Area;
+    double h = sqrt(fabs(TwoA));
+    double bx = cf.beta[0], by = cf.beta[1];
+    double norm = sqrt(bx*bx + by*by);
+    double tau = norm > 0 ? 0.5*h/norm : 0;
+    double fe1 = cf.f, fe2 = cf.f, fe3 = cf.f;
+    double feb = third*(fe1 + fe2 + fe3);
+    double ue1 = gtype[J1] == 0 ? up[J1] : u[node_dof[J1]];
+    double ue2 = gtype[J2] == 0 ? up[J2] : u[node_dof[J2]];
+    double ue3 = gtype[J3] == 0 ? up[J3] : u[node_dof[J3]];
+    double ueb = third*(ue1 + ue2 + ue3);
+    double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+    double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+    double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+    double C11 = sixth*(bx*y23 + by*x32);
+    double C12 = sixth*(bx*y31 + by*x13);
+    double C13 = sixth*(bx*y12 + by*x21);
+    double R11 = sixth*(gamma*Area);
+    double R12 = twelfth*(gamma*Area);
+    double Cpg12 = 0.25*invArea*tau*(y23*(bx*bx*y31 + bx*by*x13) + x32*(bx*by*y31 + by*by*x13));
+    double Cpg13 = 0.25*invArea*tau*(y23*(bx*bx*y12 + bx*by*x21) + x32*(bx*by*y12 + by*by*x21));
+    double Cpg23 = 0.25*invArea*tau*(y31*(bx*bx*y12 + bx*by*x21) + x13*(bx*by*y12 + by*by*x21));
+    double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
+    double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
+    double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
+    double hs = sqrt(fabs(2*Area));
+    double Eu = cf.cau ? cau_eu(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31, y12, x32, x13, x21,
+                                invArea, hs) : 0.0;
+    double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
+    double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
+    double Csc23 = Eu*0.25*invArea*(y31*y12 + x13*x21);
+    double *a = A64 + pos;
+    a[0 * ld] = -(D12 + D13) + C11 - (Cpg12 + Cpg13) + R11 + Rpg11 - (Csc12 + Csc13);
+    a[1 * ld] = D12 + C12 + Cpg12 + R12 + Rpg11 + Csc12;
+    a[2 * ld] = D13 + C13 + Cpg13 + R12 + Rpg11 + Csc13;
+    a[3 * ld] = D12 + C11 + Cpg12 + R12 + Rpg21 + Csc12;
+    a[4 * ld] = -(D12 + D23) + C12 - (Cpg12 + Cpg23) + R11 + Rpg21 - (Csc12 + Csc23);
+    a[5 * ld] = D23 + C13 + Cpg23 + R12 + Rpg21 + Csc23;
+    a[6 * ld] = D13 + C11 + Cpg13 + R12 + Rpg31 + Csc13;
+    a[7 * ld] = D23 + C12 + Cpg23 + R12 + Rpg31 + Csc23;
+    a[8 * ld] = -(D13 + D23) + C13 - (Cpg13 + Cpg23) + R11 + Rpg31 - (Csc13 + Csc23);
+    Fe[pos] = Area*twelfth*(2*fe1 + fe2 + fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y23 + by*x32);
+    Fe[ld + pos] = Area*twelfth*(fe1 + 2*fe2 + fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y31 + by*x13);
+    Fe[2 * (size_t)ld + pos] = Area*twelfth*(fe1 + fe2 + 2*fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y12 + by*x21);
+}
+
+// F_assembly (F_assembly.c:3-28) as a gather per free dof, in reference
+// element order: F += Fe_a, then F -= ke[a][b] * upresc(b) for the
+// Dirichlet vertices b of the element in vertex order.
+__global__ void k_transport_F(int n, int ld, const int *__restrict__ dptr, const int *__restrict__ dinc,
+                              const int *__restrict__ gien, const int *__restrict__ gtype,
+                              const double *__restrict__ up, const double *__restrict__ A64,
+                              const double *__restrict__ Fe, double *__restrict__ F)
+{
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d > n) return;
+    if (d == n) { F[n] = 0.0; return; }
+    double s = 0.0;
+    for (int q = dptr[d]; q < dptr[d + 1]; ++q) {
+        int pos = dinc[q] >> 4, a = dinc[q] & 15;
+        s += Fe[(size_t)a * ld + pos];
+        for (int b = 0; b < 3; ++b) {
+            if (b == a) continue;
+            int nb = gien[(size_t)b * ld + pos];
+            if (gtype[nb] == 0) s -= A64[(size_t)(a * 3 + b) * ld + pos] * up[nb];
+        }
+    }
+    F[d] = s;
+}
+
+int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c, const double *u_dev, double *F_dev,
+                              cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (t.ndof != 1) { set_error("transport assembly needs ndof == 1"); return FG_ERR_UNSUPPORTED; }
+    if (!s->geometry_ok) { set_error("transport assembly before fg_set_geometry"); return FG_ERR_STATE; }
+    if (t.nel > 0)
+        k_transport_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(), s->gx.as<double>(),
+                                                             s->gy.as<double>(), s->gtype.as<int>(), s->node_dof.as<int>(),
+                                                             s->gup.as<double>(), u_dev, *c, s->A64.as<double>(),
+                                                             s->Fe.as<double>());
+    FG_CUDA(cudaGetLastError());
+    k_transport_F<<<(t.n + 256) / 256, 256, 0, st>>>(t.n, s->nel_pad, s->dinc_ptr.as<int>(), s->dinc.as<int>(),
+                                                    s->gien.as<int>(), s->gtype.as<int>(), s->gup.as<double>(),
+                                                    s->A64.as<double>(), s->Fe.as<double>(), F_dev);
+    FG_CUDA(cudaGetLastError());
+    s->blocks_ok = true;
+    return convert_blocks(s, st);
+}
+
+}  // namespace fg

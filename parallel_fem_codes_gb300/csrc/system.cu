@@ -1,0 +1,425 @@
+// fg_system lifecycle and the public C ABI (include/femgpu.h).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "system.h"
+
+namespace fg {
+
+static thread_local std::string g_err = "no error";
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+int cuda_fail(cudaError_t e, const char *what)
+{
+    g_err = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    if (e == cudaErrorMemoryAllocation) return FG_ERR_NOMEM;
+    return FG_ERR_CUDA;
+}
+
+int DevMem::alloc(size_t b)
+{
+    if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+    if (b == 0) b = 16;
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e != cudaSuccess) { p = nullptr; return cuda_fail(e, "cudaMalloc"); }
+    bytes = b;
+    e = cudaMemset(p, 0, b);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+    return FG_OK;
+}
+
+int upload_blocks_raw(fg_system *s, const double *raw_dev, cudaStream_t st);
+int download_blocks_raw(const fg_system *s, double *raw_dev, cudaStream_t st);
+
+template <class T>
+static int upload(DevMem &m, const std::vector<T> &v)
+{
+    int r = m.alloc(sizeof(T) * std::max<size_t>(v.size(), 1));
+    if (r) return r;
+    if (!v.empty()) FG_CUDA(cudaMemcpy(m.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    return FG_OK;
+}
+
+// staging vector on the device for host <-> reference-numbered transfers
+static int stage(fg_system *s, DevMem &m, size_t bytes)
+{
+    if (m.bytes >= bytes) return FG_OK;
+    return m.alloc(bytes);
+}
+
+}  // namespace fg
+
+using namespace fg;
+
+fg_system::~fg_system()
+{
+    if (stream) cudaStreamDestroy(stream);
+    if (h_vec) cudaFreeHost(h_vec);
+}
+
+size_t fg_system::bytes() const
+{
+    const DevMem *all[] = {&lm, &A64, &A32, &dinc_ptr, &dinc, &ninc_ptr, &ninc, &node_dof, &eorder, &perm,
+                           &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
+                           &ginvp, &Fe, &F64, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
+                           &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
+    size_t b = 0;
+    for (auto *m : all) b += m->bytes;
+    return b;
+}
+
+// dot product in the summation order of BLAS_Operations/ddot.c:10-16
+static double ddot5(int n, const double *x, const double *y)
+{
+    long i, m = n - 4;
+    double s = 0.0;
+    for (i = 0; i < m; i += 5)
+        s += x[i] * y[i] + x[i + 1] * y[i + 1] + x[i + 2] * y[i + 2] + x[i + 3] * y[i + 3] + x[i + 4] * y[i + 4];
+    for (; i < n; i++) s += x[i] * y[i];
+    return s;
+}
+
+extern "C" {
+
+const char *fg_last_error(void) { return g_err.c_str(); }
+
+int fg_version(void) { return 10000; }
+
+int fg_set_device(int device)
+{
+    FG_CUDA(cudaSetDevice(device));
+    return FG_OK;
+}
+
+int fg_system_create(fg_system **out, int nnodes, int nel, int ndof, const int *ien, const int *type,
+                     const int *invp, int neq, int reorder)
+{
+    if (!out) { set_error("fg_system_create: out is NULL"); return FG_ERR_ARG; }
+    *out = nullptr;
+    fg_system *s = new (std::nothrow) fg_system();
+    if (!s) { set_error("host allocation failed"); return FG_ERR_NOMEM; }
+    int r = build_topology(s->topo, nnodes, nel, ndof, ien, type, invp, neq, reorder);
+    if (r) { delete s; return r; }
+    const Topology &t = s->topo;
+    cudaGetDevice(&s->device);
+    cudaError_t ce = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) { delete s; return cuda_fail(ce, "cudaStreamCreate"); }
+    s->n_pad = ((t.n + 1) + 31) / 32 * 32;
+    s->nel_pad = std::max(32, (t.nel + 31) / 32 * 32);
+    const int S = t.S;
+    std::vector<int> lm_soa((size_t)S * s->nel_pad, t.n);
+    for (int p = 0; p < t.nel; ++p) {
+        int e = t.eorder[p];
+        for (int a = 0; a < S; ++a) lm_soa[(size_t)a * s->nel_pad + p] = t.iperm[t.lm[(size_t)e * S + a]];
+    }
+    std::vector<int> gien((size_t)3 * s->nel_pad, 0);
+    for (int p = 0; p < t.nel; ++p)
+        for (int v = 0; v < 3; ++v) gien[(size_t)v * s->nel_pad + p] = t.ien[3 * (size_t)t.eorder[p] + v];
+    std::vector<int> perm(t.perm.begin(), t.perm.end());
+    size_t SS = (size_t)S * S * s->nel_pad;
+    if ((r = upload(s->lm, lm_soa)) || (r = upload(s->dinc_ptr, t.dinc_ptr)) || (r = upload(s->dinc, t.dinc)) ||
+        (r = upload(s->ninc_ptr, t.ninc_ptr)) || (r = upload(s->ninc, t.ninc)) ||
+        (r = upload(s->node_dof, t.node_dof)) || (r = upload(s->eorder, t.eorder)) || (r = upload(s->perm, perm)) ||
+        (r = upload(s->gien, gien)) || (r = s->A64.alloc(8 * SS)) || (r = s->A32.alloc(4 * SS)) ||
+        (r = s->diag.alloc(8 * (size_t)s->n_pad)) || (r = s->invd64.alloc(8 * (size_t)s->n_pad)) ||
+        (r = s->invd32.alloc(4 * (size_t)s->n_pad))) {
+        delete s;
+        return r;
+    }
+    if (t.ndof > 1) {
+        size_t nb = (size_t)t.nnodes * t.ndof * t.ndof;
+        if ((r = s->bd.alloc(8 * nb)) || (r = s->ibd64.alloc(8 * nb)) || (r = s->ibd32.alloc(4 * nb))) {
+            delete s;
+            return r;
+        }
+    }
+    ce = cudaMallocHost(&s->h_vec, sizeof(double) * 2 * (size_t)(t.n + 1));
+    if (ce != cudaSuccess) { delete s; return cuda_fail(ce, "cudaMallocHost"); }
+    *out = s;
+    return FG_OK;
+}
+
+int fg_mesh_analyze(int nnodes, int nel, int ndof, const int *ien, const int *type, const int *invp, int neq,
+                    int reorder, int *lm, int *Perm, int *invPerm, int *colour, fg_system_info *info)
+{
+    Topology t;
+    int r = build_topology(t, nnodes, nel, ndof, ien, type, invp, neq, reorder);
+    if (r) return r;
+    if (lm) std::memcpy(lm, t.lm.data(), sizeof(int) * t.lm.size());
+    if (Perm) std::memcpy(Perm, t.perm.data(), sizeof(int) * t.perm.size());
+    if (invPerm) std::memcpy(invPerm, t.iperm.data(), sizeof(int) * t.iperm.size());
+    if (colour) std::memcpy(colour, t.colour.data(), sizeof(int) * t.colour.size());
+    if (info) {
+        info->n = t.n; info->nel = t.nel; info->ndof = t.ndof; info->S = t.S; info->nnodes = t.nnodes;
+        info->ncolours = t.ncol; info->bandwidth_before = t.band_before; info->bandwidth_after = t.band_after;
+        info->nnz = t.nnz; info->device_bytes = 0;
+    }
+    return FG_OK;
+}
+
+int fg_system_destroy(fg_system *s)
+{
+    if (s) {
+        cudaStreamSynchronize(s->stream);
+        delete s;
+    }
+    return FG_OK;
+}
+
+int fg_system_get_info(const fg_system *s, fg_system_info *info)
+{
+    if (!s || !info) { set_error("NULL argument"); return FG_ERR_ARG; }
+    const Topology &t = s->topo;
+    info->n = t.n; info->nel = t.nel; info->ndof = t.ndof; info->S = t.S; info->nnodes = t.nnodes;
+    info->ncolours = t.ncol; info->bandwidth_before = t.band_before; info->bandwidth_after = t.band_after;
+    info->nnz = t.nnz; info->device_bytes = s->bytes();
+    return FG_OK;
+}
+
+int fg_system_get_lm(const fg_system *s, int *lm)
+{
+    if (!s || !lm) { set_error("NULL argument"); return FG_ERR_ARG; }
+    std::memcpy(lm, s->topo.lm.data(), sizeof(int) * s->topo.lm.size());
+    return FG_OK;
+}
+
+int fg_system_get_perm(const fg_system *s, int *Perm, int *invPerm)
+{
+    if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (Perm) std::memcpy(Perm, s->topo.perm.data(), sizeof(int) * s->topo.perm.size());
+    if (invPerm) std::memcpy(invPerm, s->topo.iperm.data(), sizeof(int) * s->topo.iperm.size());
+    return FG_OK;
+}
+
+int fg_system_get_colours(const fg_system *s, int *colour)
+{
+    if (!s || !colour) { set_error("NULL argument"); return FG_ERR_ARG; }
+    std::memcpy(colour, s->topo.colour.data(), sizeof(int) * s->topo.colour.size());
+    return FG_OK;
+}
+
+int fg_set_blocks(fg_system *s, const double *A)
+{
+    if (!s || (!A && s->topo.nel)) { set_error("NULL argument"); return FG_ERR_ARG; }
+    size_t bytes = sizeof(double) * (size_t)s->topo.nel * s->topo.S * s->topo.S;
+    int r = stage(s, s->F64, std::max<size_t>(bytes, 8 * (size_t)s->n_pad));
+    if (r) return r;
+    if (bytes) FG_CUDA(cudaMemcpyAsync(s->F64.p, A, bytes, cudaMemcpyHostToDevice, s->stream));
+    if ((r = upload_blocks_raw(s, s->F64.as<double>(), s->stream))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    s->blocks_ok = true;
+    return FG_OK;
+}
+
+int fg_get_blocks(const fg_system *s, double *A)
+{
+    if (!s || !A) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (!s->blocks_ok) { set_error("no element blocks"); return FG_ERR_STATE; }
+    fg_system *m = const_cast<fg_system *>(s);
+    size_t bytes = sizeof(double) * (size_t)s->topo.nel * s->topo.S * s->topo.S;
+    int r = stage(m, m->F64, std::max<size_t>(bytes, 8 * (size_t)s->n_pad));
+    if (r) return r;
+    if ((r = download_blocks_raw(s, m->F64.as<double>(), s->stream))) return r;
+    if (bytes) FG_CUDA(cudaMemcpyAsync(A, m->F64.p, bytes, cudaMemcpyDeviceToHost, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+// host vector (reference numbering, n+1) -> device internal numbering
+static int vec_in(fg_system *s, const double *h, double *d_int, double *d_tmp)
+{
+    FG_CUDA(cudaMemcpyAsync(d_tmp, h, 8 * (size_t)(s->topo.n + 1), cudaMemcpyHostToDevice, s->stream));
+    return permute_in(s, d_tmp, d_int, s->stream);
+}
+
+static int vec_out(fg_system *s, const double *d_int, double *h, double *d_tmp)
+{
+    int r = permute_out(s, d_int, d_tmp, s->stream);
+    if (r) return r;
+    FG_CUDA(cudaMemcpyAsync(h, d_tmp, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToHost, s->stream));
+    return FG_OK;
+}
+
+static int ensure_io(fg_system *s)
+{
+    int r;
+    if ((r = stage(s, s->ws.r64, 8 * (size_t)s->n_pad))) return r;
+    if ((r = stage(s, s->ws.t64, 8 * (size_t)s->n_pad))) return r;
+    if ((r = stage(s, s->ws.u64, 8 * (size_t)s->n_pad))) return r;
+    return FG_OK;
+}
+
+int fg_matvec(fg_system *s, const double *P, double *Q, int precision)
+{
+    if (!s || !P || !Q) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = vec_in(s, P, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
+    if ((r = matvec_device(s, s->ws.t64.as<double>(), s->ws.u64.as<double>(), precision, s->stream))) return r;
+    if ((r = vec_out(s, s->ws.u64.as<double>(), Q, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_precond_setup(fg_system *s, int kind, int flags, double *F)
+{
+    if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    double *fd = nullptr;
+    if (F) {
+        if ((r = vec_in(s, F, s->ws.u64.as<double>(), s->ws.r64.as<double>()))) return r;
+        fd = s->ws.u64.as<double>();
+    }
+    if ((r = precond_setup_device(s, kind, flags, fd, s->stream))) return r;
+    if (F) {
+        if ((r = vec_out(s, fd, F, s->ws.r64.as<double>()))) return r;
+    }
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_precond_apply(fg_system *s, const double *p, double *z)
+{
+    if (!s || !p || !z) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = vec_in(s, p, s->ws.u64.as<double>(), s->ws.r64.as<double>()))) return r;
+    if ((r = precond_apply_device(s, s->ws.u64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
+    if ((r = vec_out(s, s->ws.u64.as<double>(), z, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_get_diag(const fg_system *s, double *Diag)
+{
+    if (!s || !Diag) { set_error("NULL argument"); return FG_ERR_ARG; }
+    fg_system *m = const_cast<fg_system *>(s);
+    int r = ensure_io(m);
+    if (r) return r;
+    if ((r = vec_out(m, m->diag.as<double>(), Diag, m->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_set_diag(fg_system *s, const double *Diag)
+{
+    if (!s || !Diag) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = vec_in(s, Diag, s->diag.as<double>(), s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_solve(fg_system *s, const fg_solver_opts *o, const double *B, double *X, const double *F_true,
+             fg_solve_stats *stats)
+{
+    if (!s || !o || !B || !X) { set_error("NULL argument"); return FG_ERR_ARG; }
+    SolveConfig cfg;
+    cfg.kmax = o->kmax; cfg.lmax = o->lmax; cfg.tol = o->tol;
+    cfg.mixed = o->precision == FG_PREC_MIXED ? 1 : 0;
+    if (o->precision != FG_PREC_MIXED && o->precision != FG_PREC_FP64) {
+        set_error("precision must be FG_PREC_FP64 or FG_PREC_MIXED"); return FG_ERR_ARG;
+    }
+    cfg.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
+    cfg.precond = s->precond;
+    std::vector<BatchMember> mem{{s, B, F_true, X}};
+    fg_solve_stats st{};
+    int r = solve_batch(mem, cfg, &st, s->stream);
+    if (stats) *stats = st;
+    return r;
+}
+
+int fg_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc)
+{
+    if (!s || !x || !y || !upresc) { set_error("NULL argument"); return FG_ERR_ARG; }
+    const Topology &t = s->topo;
+    std::vector<double> vx(x, x + t.nnodes), vy(y, y + t.nnodes), vu(upresc, upresc + t.nnodes);
+    std::vector<int> ty(t.nnodes);
+    for (int i = 0; i < t.nnodes; ++i) ty[i] = t.type[(size_t)i * t.ndof];
+    int r;
+    if ((r = upload(s->gx, vx)) || (r = upload(s->gy, vy)) || (r = upload(s->gup, vu)) || (r = upload(s->gtype, ty)) ||
+        (r = s->Fe.alloc(8 * (size_t)3 * s->nel_pad)))
+        return r;
+    s->geometry_ok = true;
+    return FG_OK;
+}
+
+int fg_transport_assemble(fg_system *s, const fg_transport_coeffs *c, const double *u, double *F)
+{
+    if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if (u) {
+        // u has n entries: stage it as an n+1 vector with the sink at 0
+        std::memcpy(s->h_vec, u, 8 * (size_t)s->topo.n);
+        s->h_vec[s->topo.n] = 0.0;
+        if ((r = vec_in(s, s->h_vec, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
+    } else {
+        FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    }
+    if ((r = transport_assemble_device(s, c, s->ws.t64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
+    if (F) {
+        if ((r = vec_out(s, s->ws.u64.as<double>(), F, s->ws.r64.as<double>()))) return r;
+    }
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_transport_process(fg_system *s, const fg_transport_coeffs *c, const fg_solver_opts *o, double nonlinear_tol,
+                         int max_nonlinear, double *U, fg_process_stats *stats)
+{
+    if (!s || !c || !o || !U) { set_error("NULL argument"); return FG_ERR_ARG; }
+    const int n = s->topo.n;
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> F(n + 1), Fp(n + 1), X(n + 1, 0.0), uold(n);
+    std::memset(U, 0, sizeof(double) * n);
+    double normdiff = nonlinear_tol + 1, normu = 1.0 / nonlinear_tol;
+    int it = 0, gmres = 0, r;
+    double last_res = NAN;
+    // a fresh run starts from a zero diagonal (Preprocess.c:292 callocs it)
+    FG_CUDA(cudaMemsetAsync(s->diag.p, 0, s->diag.bytes, s->stream));
+    // Process.c:37-86
+    while (normdiff > nonlinear_tol * normu && it < max_nonlinear) {
+        ++it;
+        std::memcpy(uold.data(), U, sizeof(double) * n);
+        if ((r = fg_transport_assemble(s, c, U, F.data()))) return r;
+        Fp = F;
+        if ((r = fg_precond_setup(s, FG_PRECOND_DIAG, FG_SETUP_ACCUMULATE, Fp.data()))) return r;
+        fg_solve_stats st{};
+        r = fg_solve(s, o, Fp.data(), X.data(), F.data(), &st);
+        if (r) return r;
+        gmres += st.iterations;
+        last_res = st.true_rel_residual;
+        for (int i = 0; i < n; ++i) {
+            U[i] = X[i];
+            uold[i] += -1 * U[i];
+        }
+        normdiff = std::sqrt(ddot5(n, uold.data(), uold.data()));
+        normu = std::sqrt(ddot5(n, U, U));
+    }
+    if (stats) {
+        stats->nonlinear_iterations = it;
+        stats->gmres_iterations = gmres;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        stats->true_rel_residual = last_res;
+    }
+    return FG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+// The fg_system object and the batched Krylov engine (internal).
+#pragma once
+#include <memory>
+#include <vector>
+
+#include "fg_internal.h"
+#include "../../include/femgpu.h"
+
+namespace fg {
+
+// Device allocation owned by a system or a batch.
+struct DevMem {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevMem() = default;
+    DevMem(const DevMem &) = delete;
+    DevMem &operator=(const DevMem &) = delete;
+    ~DevMem() { if (p) cudaFree(p); }
+    int alloc(size_t b);     // zero-filled
+    template <class T> T *as() const { return static_cast<T *>(p); }
+};
+
+// Solver workspace of one system (kept resident between solves).
+struct Workspace {
+    int kmax = 0, mixed = -1;
+    DevMem V, w, t, x, b, ftrue, r64, t64, u64, small, part, counter, state;
+};
+
+}  // namespace fg
+
+struct fg_system {
+    fg::Topology topo;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int n_pad = 0, nel_pad = 0;
+    // connectivity and blocks, internal numbering / element order, SoA
+    fg::DevMem lm, A64, A32;
+    fg::DevMem dinc_ptr, dinc, ninc_ptr, ninc, node_dof, eorder, perm;
+    // preconditioners
+    fg::DevMem diag, invd64, invd32, bd, ibd64, ibd32;
+    int precond = FG_PRECOND_NONE;
+    bool blocks_ok = false;
+    // geometry (device assembly)
+    fg::DevMem gx, gy, gup, gien, gtype, ginvp, Fe, F64;
+    bool geometry_ok = false;
+    // host staging (pinned)
+    double *h_vec = nullptr;   // 2*(n+1) doubles
+    fg::Workspace ws;
+    size_t bytes() const;
+    ~fg_system();
+};
+
+namespace fg {
+
+// A set of systems solved together: one graph launch per restart cycle
+// advances every live member; members stop independently.
+struct BatchMember {
+    fg_system *s;
+    const double *B;       // host or device, see solve_batch
+    const double *Ftrue;
+    double *X;
+};
+
+struct SolveConfig {
+    int kmax = 30, lmax = 1000;
+    double tol = 1e-10, inner_tol = 1e-5;
+    int mixed = 0;         // 0: FP64 reference method; 1: FP32 Arnoldi in FP64 refinement
+    int precond = FG_PRECOND_DIAG;
+    int device_io = 0;     // B/X/Ftrue are device pointers in internal numbering
+    int use_graph = 1;
+};
+
+// Solve every member; stats[i] receives the result of member i.
+int solve_batch(std::vector<BatchMember> &members, const SolveConfig &cfg,
+                fg_solve_stats *stats, cudaStream_t stream);
+
+// Matvec on device vectors in internal numbering (precision 64 or 32).
+int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaStream_t st);
+
+// Set-up kernels (setup.cu)
+int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaStream_t st);
+int precond_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st);
+int convert_blocks(fg_system *s, cudaStream_t st);
+int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c,
+                              const double *u_dev, double *F_dev, cudaStream_t st);
+// Gathers / scatters between reference and internal numbering (n+1 vectors)
+int permute_in(fg_system *s, const double *ref_dev, double *int_dev, cudaStream_t st);
+int permute_out(fg_system *s, const double *int_dev, double *ref_dev, cudaStream_t st);
+
+int sm_count();
+
+}  // namespace fg

@@ -1,0 +1,343 @@
+// Host-side set-up of a mesh for the device: Fill_LM, local reverse
+// Cuthill-McKee numbering, greedy element colouring, incidence lists.
+// Runs once per mesh; everything per-iteration runs on the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+
+#include "fg_internal.h"
+#include "../../include/femgpu.h"
+
+namespace fg {
+
+// ---------------------------------------------------------------- RCM
+// Reverse Cuthill-McKee as 00_CommonFiles/Reordering/symrcm.c computes it
+// (the permutation is part of the connectivity contract, so the order of
+// every choice matters):
+//  * degrees of the symmetrised pattern (calc_degrees, symrcm.c:307-350);
+//  * neighbours visited in ascending index order, the union of row i of the
+//    pattern and of its transpose (symrcm.c:136-199);
+//  * unvisited neighbours go through a binary min-heap keyed on degree alone
+//    with strict comparisons (H_insert/H_remove_min/H_heapify_min,
+//    symrcm.c:508-567) before entering the BFS queue;
+//  * each component starts at the node returned by the repeated-BFS
+//    pseudo-peripheral search from its lowest unvisited index
+//    (find_starting_node, symrcm.c:352-483);
+//  * the Cuthill-McKee order is reversed at the end (symrcm.c:232-236).
+namespace {
+struct Cand { int id, deg, dist; };
+
+struct MinHeap {
+    std::vector<Cand> h;
+    void push(Cand v) {
+        size_t i = h.size();
+        h.push_back(v);
+        while (i > 0) {
+            size_t p = (i - 1) / 2;
+            if (h[i].deg < h[p].deg) { std::swap(h[i], h[p]); i = p; } else break;
+        }
+    }
+    Cand pop() {
+        Cand top = h[0];
+        h[0] = h.back();
+        h.pop_back();
+        size_t n = h.size(), j = 0;
+        for (;;) {
+            size_t l = 2 * j + 1, r = 2 * j + 2, m = j;
+            if (l < n && h[l].deg < h[j].deg) m = l;
+            if (r < n && h[r].deg < h[m].deg) m = r;
+            if (m == j) break;
+            std::swap(h[j], h[m]);
+            j = m;
+        }
+        return top;
+    }
+};
+
+struct Graph {
+    int n;
+    const int *IA, *JA;
+    std::vector<int> IT, JT, D;
+    // ascending distinct neighbours of i (row i of A merged with row i of A^T)
+    template <class F> void for_neighbours(int i, F &&f) const {
+        int j1 = IA[i], e1 = IA[i + 1], j2 = IT[i], e2 = IT[i + 1];
+        while (j1 < e1 || j2 < e2) {
+            int r;
+            if (j1 == e1) r = JT[j2++];
+            else if (j2 == e2) r = JA[j1++];
+            else {
+                int a = JA[j1], b = JT[j2];
+                if (a <= b) { r = a; ++j1; if (a == b) ++j2; }
+                else { r = b; ++j2; }
+            }
+            f(r);
+        }
+    }
+};
+
+int pseudo_peripheral(const Graph &g, int start, std::vector<int> &seen, std::vector<Cand> &Q)
+{
+    Cand x{start, g.D[start], 0};
+    int max_dist = 0;
+    std::fill(seen.begin(), seen.end(), 0);
+    size_t qh = 0;
+    Q.clear();
+    Q.push_back(x);
+    seen[start] = 1;
+    for (;;) {
+        while (qh < Q.size()) {
+            Cand v = Q[qh++];
+            if (v.dist > x.dist || (v.id != x.id && v.deg > x.deg)) x = v;
+            g.for_neighbours(v.id, [&](int r) {
+                if (!seen[r]) { Q.push_back({r, g.D[r], v.dist + 1}); seen[r] = 1; }
+            });
+        }
+        if (max_dist < x.dist) {
+            max_dist = x.dist;
+            std::fill(seen.begin(), seen.end(), 0);
+            seen[x.id] = 1;
+            x.dist = 0;
+            Q.clear();
+            qh = 0;
+            Q.push_back(x);
+        } else break;
+    }
+    return x.id;
+}
+}  // namespace
+
+void symrcm(int n, const int *IA, const int *JA, int *perm)
+{
+    Graph g{n, IA, JA, {}, {}, {}};
+    int nnz = IA[n];
+    g.IT.assign(n + 1, 0);
+    g.JT.assign(std::max(nnz, 1), 0);
+    for (int k = 0; k < nnz; ++k) g.IT[JA[k] + 1]++;
+    for (int i = 0; i < n; ++i) g.IT[i + 1] += g.IT[i];
+    {
+        std::vector<int> w(g.IT.begin(), g.IT.end());
+        for (int i = 0; i < n; ++i)
+            for (int k = IA[i]; k < IA[i + 1]; ++k) g.JT[w[JA[k]]++] = i;
+    }
+    g.D.assign(n, 0);
+    int max_deg = 0;
+    for (int i = 0; i < n; ++i)
+        for (int k = IA[i]; k < IA[i + 1]; ++k) {
+            int r = JA[k];
+            max_deg = std::max(max_deg, ++g.D[r]);
+            if (r != i) {
+                bool found = false;
+                for (int l = IA[r]; l < IA[r + 1]; ++l) {
+                    if (JA[l] == i) { found = true; break; }
+                    if (JA[l] > i) break;
+                }
+                if (!found) max_deg = std::max(max_deg, ++g.D[i]);
+            }
+        }
+    if (max_deg == 0) {
+        for (int i = 0; i < n; ++i) perm[i] = i;
+        return;
+    }
+    std::vector<int> visit(n, 0), seen(n, 0);
+    std::vector<Cand> Q, Q2;
+    Q.reserve(n);
+    Q2.reserve(n);
+    MinHeap heap;
+    size_t qh = 0;
+    int c = 0;
+    while (c < n) {
+        int i = 0;
+        while (i < n && visit[i]) ++i;
+        Cand root{pseudo_peripheral(g, i, seen, Q2), 0, 0};
+        root.deg = g.D[root.id];
+        visit[root.id] = 1;
+        Q.push_back(root);
+        while (qh < Q.size()) {
+            Cand v = Q[qh++];
+            perm[c++] = v.id;
+            g.for_neighbours(v.id, [&](int r) {
+                if (!visit[r]) { heap.push({r, g.D[r], v.dist + 1}); visit[r] = 1; }
+            });
+            while (!heap.h.empty()) Q.push_back(heap.pop());
+        }
+    }
+    std::reverse(perm, perm + n);
+}
+
+// MATRIX_bandwidth (reordering.c:215-236); the right band is taken from the
+// last row only, as the reference's stray ';' makes it.
+int matrix_bandwidth(int n, const int *IA, const int *JA)
+{
+    int bl = 0, br = 0;
+    for (int i = 0; i < n; ++i) {
+        if (std::fabs(double(i - JA[IA[i]])) > bl) bl = i - JA[IA[i]];
+        br = JA[IA[i + 1] - 1] - i;
+    }
+    return std::max(bl, br);
+}
+
+// ---------------------------------------------------------------- topology
+int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
+                   const int *type, const int *invp, int neq, int reorder)
+{
+    if (nnodes <= 0 || nel < 0 || ndof < 1 || ndof > 4 || neq < 0 || !ien || !type || !invp) {
+        set_error("fg_system_create: invalid mesh arguments");
+        return FG_ERR_ARG;
+    }
+    const int S = 3 * ndof, n = neq;
+    t.nnodes = nnodes; t.nel = nel; t.ndof = ndof; t.S = S; t.n = n;
+    t.ien.assign(ien, ien + (size_t)nel * 3);
+    t.type.assign(type, type + (size_t)nnodes * ndof);
+    t.invp.assign(invp, invp + (size_t)nnodes * ndof);
+    for (size_t k = 0; k < t.ien.size(); ++k)
+        if (t.ien[k] < 0 || t.ien[k] >= nnodes) { set_error("ien entry out of range"); return FG_ERR_ARG; }
+    for (size_t d = 0; d < t.type.size(); ++d)
+        if (t.type[d] != 0 && (t.invp[d] < 0 || t.invp[d] >= n)) {
+            set_error("invp of a free dof out of range"); return FG_ERR_ARG;
+        }
+
+    // Fill_LM (01_SS_.../Fill_LM.c:3-27; 03_Euler_.../Fill_LM.c:3-31)
+    t.lm.resize((size_t)nel * S);
+    for (int e = 0; e < nel; ++e)
+        for (int v = 0; v < 3; ++v)
+            for (int k = 0; k < ndof; ++k) {
+                int d = t.ien[3 * e + v] * ndof + k;
+                t.lm[(size_t)e * S + ndof * v + k] = t.type[d] == 0 ? n : t.invp[d];
+            }
+
+    // dof adjacency (row-sorted, duplicate-free), Permutation_of_LM.c:21-49
+    std::vector<int> IA(n + 1, 0), JA;
+    {
+        std::vector<int> cnt(n + 1, 0);
+        for (int e = 0; e < nel; ++e)
+            for (int a = 0; a < S; ++a) {
+                int ra = t.lm[(size_t)e * S + a];
+                if (ra == n) continue;
+                for (int b = 0; b < S; ++b)
+                    if (t.lm[(size_t)e * S + b] != n) cnt[ra]++;
+            }
+        std::vector<int> start(n + 1, 0);
+        for (int r = 0; r < n; ++r) start[r + 1] = start[r] + cnt[r];
+        std::vector<int> tmp(std::max(start[n], 1));
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (int e = 0; e < nel; ++e)
+            for (int a = 0; a < S; ++a) {
+                int ra = t.lm[(size_t)e * S + a];
+                if (ra == n) continue;
+                for (int b = 0; b < S; ++b) {
+                    int rb = t.lm[(size_t)e * S + b];
+                    if (rb != n) tmp[start[ra] + cnt[ra]++] = rb;
+                }
+            }
+        JA.reserve(start[n]);
+        for (int r = 0; r < n; ++r) {
+            std::sort(tmp.begin() + start[r], tmp.begin() + start[r + 1]);
+            IA[r] = (int)JA.size();
+            for (int k = start[r]; k < start[r + 1]; ++k)
+                if (k == start[r] || tmp[k] != tmp[k - 1]) JA.push_back(tmp[k]);
+        }
+        IA[n] = (int)JA.size();
+    }
+    t.nnz = IA[n];
+    t.perm.resize(n + 1);
+    t.iperm.resize(n + 1);
+    t.band_before = n > 0 ? matrix_bandwidth(n, IA.data(), JA.data()) : 0;
+    if (reorder == FG_REORDER_RCM && n > 0) symrcm(n, IA.data(), JA.data(), t.perm.data());
+    else std::iota(t.perm.begin(), t.perm.begin() + n, 0);
+    t.perm[n] = n;
+    for (int i = 0; i < n; ++i) t.iperm[t.perm[i]] = i;
+    t.iperm[n] = n;
+    t.band_after = t.band_before;
+    if (n > 0 && reorder == FG_REORDER_RCM) {
+        std::vector<int> IB(n + 1, 0), JB(t.nnz);
+        for (int i = 0; i < n; ++i) IB[i + 1] = IB[i] + IA[t.perm[i] + 1] - IA[t.perm[i]];
+        for (int i = 0; i < n; ++i) {
+            int o = IB[i];
+            for (int k = IA[t.perm[i]]; k < IA[t.perm[i] + 1]; ++k) JB[o++] = t.iperm[JA[k]];
+            std::sort(JB.begin() + IB[i], JB.begin() + IB[i + 1]);
+        }
+        t.band_after = matrix_bandwidth(n, IB.data(), JB.data());
+    }
+
+    // greedy element colouring over the free dofs, in reference element order:
+    // the smallest colour no earlier element sharing a free dof holds
+    t.colour.assign(nel, 0);
+    std::vector<uint64_t> used(n + 1, 0);
+    std::vector<char> has_free(nel, 0);
+    t.ncol = 0;
+    for (int e = 0; e < nel; ++e) {
+        uint64_t forb = 0;
+        for (int a = 0; a < S; ++a) {
+            int r = t.lm[(size_t)e * S + a];
+            if (r != n) { forb |= used[r]; has_free[e] = 1; }
+        }
+        if (!has_free[e]) { t.colour[e] = -1; continue; }
+        if (forb == ~0ull) { set_error("element colouring needs more than 64 colours"); return FG_ERR_UNSUPPORTED; }
+        int c = __builtin_ctzll(~forb);
+        t.colour[e] = c;
+        t.ncol = std::max(t.ncol, c + 1);
+        for (int a = 0; a < S; ++a) {
+            int r = t.lm[(size_t)e * S + a];
+            if (r != n) used[r] |= 1ull << c;
+        }
+    }
+    // internal element order: by colour, then by the smallest internal dof
+    // (gather locality), then by reference index; elements without a free
+    // dof go last and are skipped by the matvec
+    std::vector<int> key(nel);
+    for (int e = 0; e < nel; ++e) {
+        int m = n;
+        for (int a = 0; a < S; ++a) m = std::min(m, t.iperm[t.lm[(size_t)e * S + a]]);
+        key[e] = m;
+    }
+    t.eorder.resize(nel);
+    std::iota(t.eorder.begin(), t.eorder.end(), 0);
+    std::stable_sort(t.eorder.begin(), t.eorder.end(), [&](int a, int b) {
+        int ca = t.colour[a] < 0 ? 1 << 30 : t.colour[a];
+        int cb = t.colour[b] < 0 ? 1 << 30 : t.colour[b];
+        if (ca != cb) return ca < cb;
+        return key[a] < key[b];
+    });
+    t.epos.resize(nel);
+    for (int p = 0; p < nel; ++p) t.epos[t.eorder[p]] = p;
+    t.cptr.assign(t.ncol + 1, 0);
+    for (int e = 0; e < nel; ++e)
+        if (t.colour[e] >= 0) t.cptr[t.colour[e] + 1]++;
+    for (int c = 0; c < t.ncol; ++c) t.cptr[c + 1] += t.cptr[c];
+
+    // dof incidence: (pos, local row) per internal dof, reference element order
+    t.dinc_ptr.assign(n + 1, 0);
+    for (int e = 0; e < nel; ++e)
+        for (int a = 0; a < S; ++a) {
+            int r = t.lm[(size_t)e * S + a];
+            if (r != n) t.dinc_ptr[t.iperm[r] + 1]++;
+        }
+    for (int i = 0; i < n; ++i) t.dinc_ptr[i + 1] += t.dinc_ptr[i];
+    t.dinc.resize(std::max(t.dinc_ptr[n], 1));
+    {
+        std::vector<int> fill(t.dinc_ptr.begin(), t.dinc_ptr.end() - 1);
+        for (int e = 0; e < nel; ++e)
+            for (int a = 0; a < S; ++a) {
+                int r = t.lm[(size_t)e * S + a];
+                if (r != n) t.dinc[fill[t.iperm[r]]++] = t.epos[e] * 16 + a;
+            }
+    }
+    // node incidence (pos, vertex), reference element order
+    t.ninc_ptr.assign(nnodes + 1, 0);
+    for (int e = 0; e < nel; ++e)
+        for (int v = 0; v < 3; ++v) t.ninc_ptr[t.ien[3 * e + v] + 1]++;
+    for (int i = 0; i < nnodes; ++i) t.ninc_ptr[i + 1] += t.ninc_ptr[i];
+    t.ninc.resize(std::max(t.ninc_ptr[nnodes], 1));
+    {
+        std::vector<int> fill(t.ninc_ptr.begin(), t.ninc_ptr.end() - 1);
+        for (int e = 0; e < nel; ++e)
+            for (int v = 0; v < 3; ++v) t.ninc[fill[t.ien[3 * e + v]]++] = t.epos[e] * 4 + v;
+    }
+    t.node_dof.resize((size_t)nnodes * ndof);
+    for (size_t d = 0; d < t.node_dof.size(); ++d)
+        t.node_dof[d] = t.type[d] == 0 ? n : t.iperm[t.invp[d]];
+    return FG_OK;
+}
+
+}  // namespace fg

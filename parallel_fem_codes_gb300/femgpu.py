@@ -1,0 +1,261 @@
+"""ctypes binding of libfemgpu (include/femgpu.h) and a thin object layer.
+
+The library is loaded from the package's in-tree build
+(parallel_fem_codes_gb300/_lib/libfemgpu.so).  There is no fallback: if the
+library is missing or a call fails, an exception says why.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FG_OK = 0
+FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG = 0, 1, 2
+FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
+FG_PREC_FP64, FG_PREC_MIXED = 64, 32
+FG_REORDER_NONE, FG_REORDER_RCM = 0, 1
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE",
+          5: "ERR_BREAKDOWN", 6: "ERR_NOTCONV", 7: "ERR_UNSUPPORTED"}
+
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_vp = ctypes.c_void_p
+_c_int, _c_dbl = ctypes.c_int, ctypes.c_double
+
+
+class FemGpuError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SystemInfo(ctypes.Structure):
+    _fields_ = [("n", _c_int), ("nel", _c_int), ("ndof", _c_int), ("S", _c_int), ("nnodes", _c_int),
+                ("ncolours", _c_int), ("bandwidth_before", _c_int), ("bandwidth_after", _c_int),
+                ("nnz", _c_int), ("device_bytes", ctypes.c_size_t)]
+
+
+class SolverOpts(ctypes.Structure):
+    _fields_ = [("kmax", _c_int), ("lmax", _c_int), ("tol", _c_dbl), ("precision", _c_int),
+                ("inner_tol", _c_dbl)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iterations", _c_int), ("cycles", _c_int), ("converged", _c_int), ("status", _c_int),
+                ("rho", _c_dbl), ("eps", _c_dbl), ("true_rel_residual", _c_dbl), ("seconds", _c_dbl)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class TransportCoeffs(ctypes.Structure):
+    _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl), ("cau", _c_int)]
+
+
+class ProcessStats(ctypes.Structure):
+    _fields_ = [("nonlinear_iterations", _c_int), ("gmres_iterations", _c_int), ("seconds", _c_dbl),
+                ("true_rel_residual", _c_dbl)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def lib(build_if_missing: bool = True):
+    """The loaded libfemgpu; builds it in-tree first when it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise FemGpuError(7, f"libfemgpu is not built ({path}); run __graft_entry__.build()")
+        _build.build()
+    L = ctypes.CDLL(path)
+    L.fg_last_error.restype = ctypes.c_char_p
+    L.fg_system_create.argtypes = [ctypes.POINTER(_vp), _c_int, _c_int, _c_int, _i32p, _i32p, _i32p, _c_int, _c_int]
+    L.fg_system_destroy.argtypes = [_vp]
+    L.fg_mesh_analyze.argtypes = [_c_int, _c_int, _c_int, _i32p, _i32p, _i32p, _c_int, _c_int,
+                                  _vp, _vp, _vp, _vp, ctypes.POINTER(SystemInfo)]
+    L.fg_system_get_info.argtypes = [_vp, ctypes.POINTER(SystemInfo)]
+    L.fg_system_get_lm.argtypes = [_vp, _i32p]
+    L.fg_system_get_perm.argtypes = [_vp, _i32p, _i32p]
+    L.fg_system_get_colours.argtypes = [_vp, _i32p]
+    L.fg_set_blocks.argtypes = [_vp, _f64p]
+    L.fg_get_blocks.argtypes = [_vp, _f64p]
+    L.fg_matvec.argtypes = [_vp, _f64p, _f64p, _c_int]
+    L.fg_precond_setup.argtypes = [_vp, _c_int, _c_int, _vp]
+    L.fg_precond_apply.argtypes = [_vp, _f64p, _f64p]
+    L.fg_get_diag.argtypes = [_vp, _f64p]
+    L.fg_set_diag.argtypes = [_vp, _f64p]
+    L.fg_solve.argtypes = [_vp, ctypes.POINTER(SolverOpts), _f64p, _f64p, _vp, ctypes.POINTER(SolveStats)]
+    L.fg_set_geometry.argtypes = [_vp, _f64p, _f64p, _f64p]
+    L.fg_transport_assemble.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), _vp, _vp]
+    L.fg_transport_process.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), ctypes.POINTER(SolverOpts), _c_dbl,
+                                       _c_int, _f64p, ctypes.POINTER(ProcessStats)]
+    _lib = L
+    return L
+
+
+def check(code: int) -> None:
+    if code != FG_OK:
+        raise FemGpuError(code, lib().fg_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def mesh_analyze(mesh, reorder: bool = True) -> dict:
+    """Host-only set-up products (no GPU): lm, Perm, invPerm, colour, info."""
+    S = 3 * mesh.ndof
+    lm = np.empty(mesh.nel * S, dtype=np.int32)
+    perm = np.empty(mesh.neq + 1, dtype=np.int32)
+    inv = np.empty(mesh.neq + 1, dtype=np.int32)
+    col = np.empty(max(mesh.nel, 1), dtype=np.int32)
+    info = SystemInfo()
+    check(lib().fg_mesh_analyze(mesh.nnodes, mesh.nel, mesh.ndof,
+                                np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1),
+                                np.ascontiguousarray(mesh.type, dtype=np.int32),
+                                np.ascontiguousarray(mesh.invp, dtype=np.int32), mesh.neq,
+                                FG_REORDER_RCM if reorder else FG_REORDER_NONE,
+                                lm.ctypes.data, perm.ctypes.data, inv.ctypes.data, col.ctypes.data,
+                                ctypes.byref(info)))
+    return {"lm": lm.reshape(mesh.nel, S), "perm": perm, "invperm": inv, "colour": col[:mesh.nel],
+            "info": {k: getattr(info, k) for k, _ in info._fields_}}
+
+
+@dataclasses.dataclass
+class SolveResult:
+    x: np.ndarray
+    stats: dict
+
+
+class System:
+    """One EBE linear system on the GPU: mesh connectivity, element blocks,
+    preconditioner and resident solver state."""
+
+    def __init__(self, mesh, reorder: bool = True):
+        self.mesh = mesh
+        h = _vp()
+        check(lib().fg_system_create(ctypes.byref(h), mesh.nnodes, mesh.nel, mesh.ndof,
+                                     np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1),
+                                     np.ascontiguousarray(mesh.type, dtype=np.int32),
+                                     np.ascontiguousarray(mesh.invp, dtype=np.int32), mesh.neq,
+                                     FG_REORDER_RCM if reorder else FG_REORDER_NONE))
+        self._h = h
+        self.n = mesh.neq
+        self.S = 3 * mesh.ndof
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fg_system_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        i = SystemInfo()
+        check(lib().fg_system_get_info(self._h, ctypes.byref(i)))
+        return {k: getattr(i, k) for k, _ in i._fields_}
+
+    def lm(self):
+        out = np.empty(self.mesh.nel * self.S, dtype=np.int32)
+        check(lib().fg_system_get_lm(self._h, out))
+        return out.reshape(self.mesh.nel, self.S)
+
+    def perm(self):
+        p = np.empty(self.n + 1, dtype=np.int32)
+        q = np.empty(self.n + 1, dtype=np.int32)
+        check(lib().fg_system_get_perm(self._h, p, q))
+        return p, q
+
+    def colours(self):
+        c = np.empty(self.mesh.nel, dtype=np.int32)
+        check(lib().fg_system_get_colours(self._h, c))
+        return c
+
+    def set_blocks(self, A):
+        check(lib().fg_set_blocks(self._h, np.ascontiguousarray(A, dtype=np.float64).reshape(-1)))
+
+    def get_blocks(self):
+        A = np.empty(self.mesh.nel * self.S * self.S)
+        check(lib().fg_get_blocks(self._h, A))
+        return A.reshape(self.mesh.nel, self.S * self.S)
+
+    def matvec(self, P, precision=64):
+        P = np.ascontiguousarray(P, dtype=np.float64)
+        Q = np.empty(self.n + 1)
+        check(lib().fg_matvec(self._h, P, Q, precision))
+        return Q
+
+    def precond_setup(self, kind=FG_PRECOND_DIAG, flags=0, F=None):
+        Fc = None if F is None else np.array(F, dtype=np.float64, copy=True)
+        check(lib().fg_precond_setup(self._h, kind, flags, _ptr(Fc)))
+        return Fc
+
+    def precond_apply(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        z = np.empty(self.n + 1)
+        check(lib().fg_precond_apply(self._h, p, z))
+        return z
+
+    def diag(self):
+        d = np.empty(self.n + 1)
+        check(lib().fg_get_diag(self._h, d))
+        return d
+
+    def solve(self, B, kmax=30, lmax=1000, tol=1e-10, precision=FG_PREC_FP64, inner_tol=0.0, F_true=None):
+        B = np.ascontiguousarray(B, dtype=np.float64)
+        X = np.zeros(self.n + 1)
+        o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+        st = SolveStats()
+        Ft = None if F_true is None else np.ascontiguousarray(F_true, dtype=np.float64)
+        check(lib().fg_solve(self._h, ctypes.byref(o), B, X, _ptr(Ft), ctypes.byref(st)))
+        return SolveResult(X, st.as_dict())
+
+    # ---- transport assembly
+    def set_geometry(self, x, y, upresc):
+        check(lib().fg_set_geometry(self._h, np.ascontiguousarray(x, dtype=np.float64),
+                                    np.ascontiguousarray(y, dtype=np.float64),
+                                    np.ascontiguousarray(upresc, dtype=np.float64)))
+
+    def transport_assemble(self, prob, u=None):
+        c = TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau))
+        F = np.empty(self.n + 1)
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        check(lib().fg_transport_assemble(self._h, ctypes.byref(c), _ptr(uu), F.ctypes.data))
+        return F
+
+    def transport_process(self, prob, kmax=30, lmax=1000, tol=1e-10, nonlinear_tol=1e-3, max_nonlinear=1000,
+                          precision=FG_PREC_FP64):
+        c = TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau))
+        o = SolverOpts(kmax, lmax, tol, precision, 0.0)
+        U = np.zeros(self.n)
+        st = ProcessStats()
+        check(lib().fg_transport_process(self._h, ctypes.byref(c), ctypes.byref(o), nonlinear_tol, max_nonlinear,
+                                         U, ctypes.byref(st)))
+        return U, {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def transport_system(prob, reorder=True) -> System:
+    """A System with the geometry and Dirichlet data of a transport problem."""
+    s = System(prob.mesh, reorder=reorder)
+    s.set_geometry(prob.mesh.x, prob.mesh.y, prob.upresc)
+    return s

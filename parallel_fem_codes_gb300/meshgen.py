@@ -122,3 +122,33 @@ def batch_transport_problems(count=256, seed=4, nmin=33, nmax=513, cau=True):
     ks = 10.0 ** rng.uniform(-8.0, -2.0, size=count)
     return [transport_problem(int(n), float(a), float(kk), cau=cau)
             for n, a, kk in zip(ns, angles, ks)]
+
+
+def multi_dof_mesh(n_nodes_side: int, ndof: int, seed: int = 0, dirichlet=None, jitter: float = 0.0):
+    """Structured unit-square mesh with ndof dofs per node (the Euler layout
+    (rho, rho u, rho v, E) for ndof = 4 and the Navier-Stokes layout (u, v, p)
+    for ndof = 3).  dirichlet(k) -> bool mask over nodes for dof k; default:
+    every boundary dof Dirichlet except the last dof of each node."""
+    M = n_nodes_side - 1
+    X, Y, ien = structured_mesh(M, M)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    bnd = boundary_mask(X, Y)
+    if jitter:
+        h = 1.0 / M
+        X = X + np.where(bnd, 0.0, rng.uniform(-jitter * h, jitter * h, X.shape))
+        Y = Y + np.where(bnd, 0.0, rng.uniform(-jitter * h, jitter * h, Y.shape))
+    type_ = np.ones((X.shape[0], ndof), dtype=np.int32)
+    for k in range(ndof):
+        mask = dirichlet(k, X, Y, bnd) if dirichlet is not None else (bnd if k < ndof - 1 else np.zeros_like(bnd))
+        type_[mask, k] = 0
+    type_ = type_.reshape(-1)
+    invp, neq = number_dofs(type_)
+    return Mesh(X, Y, ien, ndof, type_, invp, neq)
+
+
+def random_blocks(nel: int, S: int, seed: int = 0, dominance: float = 4.0):
+    """Random nonsymmetric element blocks with a dominant diagonal (float64[nel, S*S])."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    A = rng.uniform(-1.0, 1.0, size=(nel, S, S))
+    A[:, np.arange(S), np.arange(S)] += dominance
+    return A.reshape(nel, S * S)
