@@ -1,0 +1,369 @@
+"""Benchmark: batched steady SUPG transport solves at relative residual 1e-10.
+
+Workload (one step): 256 independent steady SUPG/CAU convection-diffusion
+problems, structured N x N node meshes with N uniform in [33, 513] (seed 4),
+velocity angle uniform in [0, 360), conductivity log-uniform in
+[1e-8, 1e-2]; each is assembled on the device (SUPG + CAU at u = 0),
+Diag-preconditioned and solved to true relative residual 1e-10 with FP32
+GMRES(30) cycles inside FP64 iterative refinement, all instances in one
+batch (one graph launch per restart cycle).  The plain method for
+comparison is the reference's FP64 GMRES(30) run one instance at a time on
+the same GPU.
+
+Output: one JSON line (rank 0).  `value` is solves/s with the meshes
+resident in HBM; `e2e` is the same metric through the host-buffer C ABI
+(element blocks and right-hand sides copied in, solutions copied out, every
+step).  `--impl reference` times the reference's CPU implementation of the
+path (the oracle port where the reference's own build is absent) on the
+host cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s + p50/p99 latency @1e-10 resid: served mixed vs plain FP64 GMRES"
+WORKLOAD = ("batched steady SUPG/CAU transport: 256 instances, NxN nodes N~U[33,513] (seed 4), "
+            "angle~U[0,360), k~logU[1e-8,1e-2]; Diag-preconditioned GMRES(30), FP32 inner + FP64 "
+            "refinement to true rel. residual 1e-10")
+KMAX, TOL = 30, 1e-10
+
+
+# ------------------------------------------------------------------ CPU legs
+def _cpu_solve(args):
+    """One instance on the host: assembly, Diag set-up and FP64 GMRES(30)
+    (the reference's method), by the oracle port or the reference's own C."""
+    idx, count, seed, use_ref = args
+    sys.path.insert(0, ROOT)
+    import oracle as O
+    from parallel_fem_codes_gb300 import meshgen as G
+    p = G.batch_transport_problems(count, seed)[idx]
+    t0 = time.perf_counter()
+    m = p.mesh
+    if use_ref and O.ref_available():
+        lm, perm, inv, _, _ = O.ref_connectivity(m)
+        A, F = O.ref_build(p)
+        X, it, *_ = O.ref_diag_pgmres(lm, A, perm, inv, F, kmax=KMAX, lmax=100000, tol=TOL)
+    else:
+        lm = O.fill_lm(m)
+        perm, inv, _ = O.permutation_of_lm(m)
+        A, F = O.build_k_f_supg(p)
+        X, it, *_ = O.ebe_diag_solve(lm, A, m.neq, F, perm, inv, kmax=KMAX, lmax=100000, tol=TOL)
+    return idx, time.perf_counter() - t0, it, m.nel
+
+
+def cpu_sample_indices(problem_nel, budget_nel):
+    """First instances (in workload order) whose element count sums to ~budget."""
+    out, tot = [], 0
+    for i, ne in enumerate(problem_nel):
+        if tot >= budget_nel:
+            break
+        out.append(i)
+        tot += ne
+    return out
+
+
+def run_cpu(pool, count, seed, idxs, use_ref):
+    t0 = time.perf_counter()
+    res = pool.map(_cpu_solve, [(i, count, seed, use_ref) for i in idxs])
+    wall = time.perf_counter() - t0
+    return wall, res
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self, dev=0):
+        try:
+            rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
+        except OSError:
+            return None
+        rows = [[c.strip() for c in r] for r in rows if len(r) >= 9 and r[0].strip() == str(dev)]
+        if not rows:
+            return None
+        sm = [float(r[1].split()[0]) for r in rows if r[1].split()[0].replace(".", "").isdigit()]
+        mx = [float(r[2].split()[0]) for r in rows if r[2].split()[0].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ helpers
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def pct(v, q):
+    return float(np.percentile(np.asarray(v, dtype=np.float64), q)) if len(v) else None
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args, rank, ws, dist):
+    if rank != 0:
+        return 0
+    from parallel_fem_codes_gb300 import meshgen as G
+    import oracle as O
+    O.build(ref=None)
+    probs = G.batch_transport_problems(args.count, args.seed)
+    nel = [p.mesh.nel for p in probs]
+    idxs = cpu_sample_indices(nel, args.cpu_budget)
+    cores = os.cpu_count() or 1
+    use_ref = O.ref_available()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(cores, len(idxs))) as pool:
+        for _ in range(args.warmup):
+            run_cpu(pool, args.count, args.seed, idxs[:1], use_ref)
+        walls = []
+        for _ in range(args.steps):
+            w, res = run_cpu(pool, args.count, args.seed, idxs, use_ref)
+            walls.append(w)
+    lat = [r[1] for r in res]
+    value = len(idxs) / statistics.median(walls)
+    kind = "reference" if use_ref else "port"
+    sample = (f"first {len(idxs)} of {args.count} instances ({sum(nel[i] for i in idxs)} elements, "
+              f"workload mean {np.mean(nel):.0f} elements/instance), one process per instance, "
+              f"FP64 GMRES(30) with Diag, tol 1e-10")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(walls),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "instances": args.count, "seed": args.seed},
+            "latency_ms": {"p50": 1e3 * pct(lat, 50), "p99": 1e3 * pct(lat, 99)},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": min(cores, len(idxs)), "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ------------------------------------------------------------------ our arm
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--count", type=int, default=256)
+    ap.add_argument("--seed", type=int, default=4)
+    ap.add_argument("--cpu-budget", type=int, default=400_000, help="elements in the CPU sample")
+    ap.add_argument("--plain-count", type=int, default=0, help="instances in the plain FP64 leg (0 = all)")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    rank, ws, dist = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, rank, ws, dist)
+
+    # spawn the CPU pool before the first GPU call
+    cores = os.cpu_count() or 1
+    pool = None
+    if rank == 0 and not args.no_cpu:
+        pool = mp.get_context("spawn").Pool(cores)
+
+    import torch
+    from parallel_fem_codes_gb300 import femgpu as fg, meshgen as G
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    fg.lib(build_if_missing=False)
+    probs = G.batch_transport_problems(args.count, args.seed + 1000 * rank)
+    t0 = time.perf_counter()
+    systems = [fg.transport_system(p) for p in probs]
+    setup_s = time.perf_counter() - t0
+    nel_total = sum(p.mesh.nel for p in probs)
+    n_total = sum(p.mesh.neq for p in probs)
+    stream = torch.cuda.ExternalStream(systems[0].stream)
+
+    def served_step():
+        for s, p in zip(systems, probs):
+            s.transport_prepare(p)
+        return fg.solve_resident(systems, kmax=KMAX, lmax=10000, tol=TOL, precision=fg.FG_PREC_MIXED)
+
+    for _ in range(args.warmup):
+        st = served_step()
+    barrier(dist)
+    torch.cuda.synchronize()
+    clk = ClockSampler(os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "",
+                                    f"clocks_rank{rank}.csv"))
+    l0 = fg.launch_count()
+    times = []
+    with clk:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        for _ in range(args.steps):
+            e0.record(stream)
+            st = served_step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+    torch.cuda.synchronize()
+    barrier(dist)
+    launches = (fg.launch_count() - l0) / args.steps
+    step_s = reduce_max(dist, sum(times) / len(times))
+    value = ws * args.count / step_s
+    conv = all(s["converged"] == 1 for s in st)
+    worst_res = max(s["true_rel_residual"] for s in st)
+    iters = [s["iterations"] for s in st]
+    clocks = clk.summary(dev)
+
+    # error of the mixed solutions against the FP64 solve (same GPU, per instance)
+    xs_mixed = [s.solution() for s in systems[: min(8, len(systems))]]
+
+    # plain FP64 GMRES, one instance at a time (latency distribution)
+    nplain = args.count if args.plain_count <= 0 else min(args.plain_count, args.count)
+    plain_lat, plain_iters, plain_err = [], [], []
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    for i in range(nplain):
+        s, p = systems[i], probs[i]
+        s.transport_prepare(p)
+        e0.record(stream)
+        r = fg.solve_resident([s], kmax=KMAX, lmax=100000, tol=TOL, precision=fg.FG_PREC_FP64)
+        e1.record(stream)
+        e1.synchronize()
+        plain_lat.append(e0.elapsed_time(e1) / 1e3)
+        plain_iters.append(r[0]["iterations"])
+        if i < len(xs_mixed):
+            x64 = s.solution()
+            plain_err.append(float(np.linalg.norm(xs_mixed[i] - x64) / max(np.linalg.norm(x64), 1e-300)))
+    plain_value = nplain / sum(plain_lat)
+
+    # roofline: the batched FP32 EBE matvec alone
+    ms_mv, bytes_mv = fg.bench_matvec(systems, precision=32, reps=20)
+    peak, peak_kind = peaks()
+    achieved = bytes_mv / (ms_mv * 1e-3) / 1e9
+
+    # e2e through the host-buffer C ABI: blocks + F in, X out, every step
+    e2e = None
+    if not args.no_e2e:
+        As, Fs = [], []
+        for s, p in zip(systems, probs):
+            Fs.append(s.transport_assemble(p))
+            As.append(s.get_blocks())
+        h2d = sum(a.nbytes for a in As) + 2 * sum(f.nbytes for f in Fs)
+        d2h = 2 * sum(f.nbytes for f in Fs)
+
+        def e2e_step():
+            Bs = []
+            for s, A, F in zip(systems, As, Fs):
+                s.set_blocks(A)
+                Bs.append(s.precond_setup(fg.FG_PRECOND_DIAG, 0, F))
+            return fg.solve_batch(systems, Bs, Fs, kmax=KMAX, lmax=10000, tol=TOL, precision=fg.FG_PREC_MIXED)
+
+        e2e_step()
+        et = []
+        for _ in range(max(1, args.steps)):
+            e0.record(stream)
+            xs, st2 = e2e_step()
+            e1.record(stream)
+            e1.synchronize()
+            et.append(e0.elapsed_time(e1) / 1e3)
+        e2e_s = reduce_max(dist, sum(et) / len(et))
+        e2e = {"value": ws * args.count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+
+    cpu = None
+    if pool is not None:
+        nel = [p.mesh.nel for p in probs]
+        idxs = cpu_sample_indices(nel, args.cpu_budget)
+        wall, res = run_cpu(pool, args.count, args.seed, idxs, False)
+        pool.close()
+        cpu = {"value": len(idxs) / wall, "unit": "solves/s", "cores": min(cores, len(idxs)), "kind": "port",
+               "sample": (f"first {len(idxs)} of {args.count} instances ({sum(nel[i] for i in idxs)} elements; "
+                          f"workload mean {np.mean(nel):.0f}/instance), one process per instance, oracle port "
+                          f"of the reference's FP64 GMRES(30)+Diag, tol 1e-10")}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "instances": args.count, "elements": nel_total, "dofs": n_total,
+                       "kmax": KMAX, "tol": TOL, "l2": "inputs larger than L2 (per-step working set >1 GB)"},
+            "latency_ms": {"p50": 1e3 * step_s, "p99": 1e3 * step_s,
+                           "note": "synchronous batch: every instance completes at the end of the step"},
+            "plain_fp64": {"solves_per_s": plain_value, "instances": nplain, "p50_ms": 1e3 * pct(plain_lat, 50),
+                           "p99_ms": 1e3 * pct(plain_lat, 99), "iterations_mean": float(np.mean(plain_iters))},
+            "speedup_vs_plain_fp64": value / plain_value,
+            "mixed": {"converged_all": conv, "worst_true_rel_residual": worst_res,
+                      "iterations_mean": float(np.mean(iters)),
+                      "rel_err_vs_fp64_max": max(plain_err) if plain_err else None},
+            "clocks": clocks, "gpu_launches": launches, "e2e": e2e,
+            "roofline": {"bound": "hbm", "kernel": "k_ebe_mv<3,float> (all colours, batched)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_source": peak_kind, "traffic": None, "ms_per_matvec": ms_mv,
+                         "bytes_per_matvec": bytes_mv},
+            "cpu_baseline": cpu, "setup_s": setup_s,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -143,6 +143,39 @@ typedef struct {
 int fg_solve(fg_system *s, const fg_solver_opts *opts, const double *B, double *X,
              const double *F_true, fg_solve_stats *stats);
 
+/* Solve many systems together (same block size and preconditioner kind):
+ * one CUDA-graph launch per restart cycle advances every member, members
+ * stop independently, and each result is bit-identical to solving that
+ * system alone.  B[i], X[i], F_true[i] are host vectors of system i
+ * (F_true may be NULL, or F_true[i] NULL).  stats has count entries. */
+int fg_solve_batch(fg_system *const *systems, int count, const fg_solver_opts *opts,
+                   const double *const *B, double *const *X, const double *const *F_true,
+                   fg_solve_stats *stats);
+
+/* Device-resident variant: each system solves with the right-hand side its
+ * last fg_transport_prepare left on the device; the solution stays on the
+ * device (fg_get_solution copies it out). */
+int fg_solve_resident(fg_system *const *systems, int count, const fg_solver_opts *opts,
+                      fg_solve_stats *stats);
+int fg_get_solution(const fg_system *s, double *X);
+
+/* Kernel launches issued by this library so far (direct launches plus the
+ * kernel nodes of every graph launch), for launch accounting. */
+long long fg_launch_count(void);
+
+/* The CUDA stream (cudaStream_t) a system's work runs on, for callers that
+ * record events or order their own work around it. */
+void *fg_system_stream(const fg_system *s);
+
+/* Time the batched EBE matvec of these systems alone: reps back-to-back
+ * matvecs (all colours) of V[0] into the Arnoldi work vector, in FP64
+ * (precision 64) or FP32 (32), timed with CUDA events on the first
+ * system's stream.  *ms_per_matvec receives the mean; *bytes the
+ * algorithmic bytes of one matvec: nel*(S*S*w + S*4) + 2*n*w summed over
+ * the systems.  Requires a previous solve (workspace) on every system. */
+int fg_bench_matvec(fg_system *const *systems, int count, int precision, int reps,
+                    double *ms_per_matvec, double *bytes);
+
 /* ---- steady SUPG/CAU transport assembly on the device ---- */
 typedef struct {
     double k;            /* Condutivity(), used for kx and ky         */
@@ -158,6 +191,10 @@ int fg_set_geometry(fg_system *s, const double *x, const double *y, const double
  * NULL = 0): element blocks stay on the device; F (host, n+1) receives the
  * right-hand side when not NULL. */
 int fg_transport_assemble(fg_system *s, const fg_transport_coeffs *c, const double *u, double *F);
+/* Assemble at u (host, n entries, NULL = 0) and set up a fresh Diag
+ * preconditioner, keeping F and M^-1 F on the device as the system's
+ * resident right-hand side for fg_solve_resident.  Nothing is copied back. */
+int fg_transport_prepare(fg_system *s, const fg_transport_coeffs *c, const double *u);
 /* Steady transport Process loop (Process.c:6-93) on the device: assemble,
  * Diag setup (accumulating, as the reference), GMRES, until
  * ||u - u_old|| <= nonlinear_tol * ||u||.  U (host, n entries) holds the

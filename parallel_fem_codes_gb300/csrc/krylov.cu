@@ -17,6 +17,7 @@
 // parts, so a result is bit-identical whether the system is solved alone
 // or inside a batch.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -735,9 +736,10 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
 // Enqueue the matvec over all colours: mode 0 (x -> t64, FP64, gate live)
 // or mode 1 (V[step] -> t, T, gate in_cycle).
 template <typename T>
-static void enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
+static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
 {
     const SysDev *sys = P.sysdev.as<SysDev>();
+    int k = 0;
     for (int c = 0; c < P.ncol; ++c) {
         int cnt = P.ech_off[c + 1] - P.ech_off[c];
         if (!cnt) continue;
@@ -746,32 +748,38 @@ static void enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
         if (mode == 0)
             MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, ch, nc, 0, 0, 0, 0, nullptr, nullptr);
         else
-            MvLaunch::go<T, T, T>(P.S, grid_for(cnt), st, sys, ch, nc, 1, 1, 1, step, nullptr, nullptr);
+            MvLaunch::go<T, T, T>(P.S, grid_for(cnt), st, sys, ch, nc, mode == 2 ? -1 : 1, 1, 1, step, nullptr, nullptr);
+        ++k;
     }
+    return k;
 }
 
+// One restart cycle for every member; returns the number of kernels.
 template <typename T>
-static void enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
+static int enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
 {
     const SysDev *sys = P.sysdev.as<SysDev>();
     const DChunk *dc = P.dchunks.as<DChunk>();
     const int *nd = P.dcount.as<int>();
     dim3 gd = grid_for(P.n_dch), gn = grid_for(P.n_nch);
     const bool bd = cfg.precond == FG_PRECOND_BLOCKDIAG;
-    enqueue_matvec<T>(P, 0, 0, st);
-    if (bd) launch_blockdiag<double>(P.B, gn, st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 0, 0, nullptr, nullptr);
+    int k = enqueue_matvec<T>(P, 0, 0, st);
+    if (bd) { launch_blockdiag<double>(P.B, gn, st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 0, 0, nullptr, nullptr); ++k; }
     k_start<<<gd, kThreads, 0, st>>>(sys, dc, nd);
     k_scale_v0<T><<<gd, kThreads, 0, st>>>(sys, dc, nd);
+    k += 2;
     for (int i = 0; i < cfg.kmax - 1; ++i) {
-        enqueue_matvec<T>(P, 1, i, st);
-        if (bd) launch_blockdiag<T>(P.B, gn, st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 1, 1, nullptr, nullptr);
+        k += enqueue_matvec<T>(P, 1, i, st);
+        if (bd) { launch_blockdiag<T>(P.B, gn, st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 1, 1, nullptr, nullptr); ++k; }
         k_dots1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
         k_orth1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
         k_orth2<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
         k_normalize<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        k += 4;
     }
     k_update<T><<<gd, kThreads, 0, st>>>(sys, dc, nd);
     k_live<<<(P.nsys + 255) / 256, 256, 0, st>>>(sys, P.nsys, P.live.as<int>());
+    return k + 2;
 }
 
 static int ensure_workspace(fg_system *s, int kmax, int mixed)
@@ -872,14 +880,15 @@ int solve_batch(std::vector<BatchMember> &mem, const SolveConfig &cfg, fg_solve_
     const int nsys = P.nsys;
     k_init_state<<<(nsys + 127) / 128, 128, 0, st>>>(P.sysdev.as<SysDev>(), nsys);
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    int graph_nodes = 0;
 
     // one restart cycle as a CUDA graph, replayed until no system is live
     cudaGraphExec_t exec = nullptr;
     if (cfg.use_graph) {
         cudaGraph_t graph = nullptr;
         FG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        if (cfg.mixed) enqueue_cycle<float>(P, cfg, st);
-        else enqueue_cycle<double>(P, cfg, st);
+        graph_nodes = cfg.mixed ? enqueue_cycle<float>(P, cfg, st) : enqueue_cycle<double>(P, cfg, st);
         cudaError_t ce = cudaStreamEndCapture(st, &graph);
         if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
         ce = cudaGraphInstantiate(&exec, graph, 0);
@@ -893,10 +902,11 @@ int solve_batch(std::vector<BatchMember> &mem, const SolveConfig &cfg, fg_solve_
     int rc = FG_OK;
     for (int cyc = 0; cyc < guard; ++cyc) {
         cudaError_t ce;
-        if (exec) ce = cudaGraphLaunch(exec, st);
-        else {
-            if (cfg.mixed) enqueue_cycle<float>(P, cfg, st);
-            else enqueue_cycle<double>(P, cfg, st);
+        if (exec) {
+            ce = cudaGraphLaunch(exec, st);
+            count_launches(graph_nodes);
+        } else {
+            count_launches(cfg.mixed ? enqueue_cycle<float>(P, cfg, st) : enqueue_cycle<double>(P, cfg, st));
             ce = cudaGetLastError();
         }
         if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_live, P.live.p, sizeof(int) * nsys, cudaMemcpyDeviceToHost, st);
@@ -920,6 +930,7 @@ int solve_batch(std::vector<BatchMember> &mem, const SolveConfig &cfg, fg_solve_
         }
         k_final<<<grid_for(P.n_dch), kThreads, 0, st>>>(sys, P.dchunks.as<DChunk>(), P.dcount.as<int>());
         FG_CUDA(cudaGetLastError());
+        count_launches(P.ncol + 1);
     }
     // results
     for (int s = 0; s < nsys; ++s) {
@@ -991,8 +1002,64 @@ int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaS
             MvLaunch::go<double, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y);
     }
     FG_CUDA(cudaGetLastError());
+    count_launches(t.ncol);
     FG_CUDA(cudaStreamSynchronize(st));
     return FG_OK;
 }
+
+// The batched matvec alone, timed with CUDA events (fg_bench_matvec).
+int bench_matvec(std::vector<fg_system *> &systems, int precision, int reps, double *ms, double *bytes)
+{
+    if (systems.empty() || reps < 1) { set_error("empty batch or reps < 1"); return FG_ERR_ARG; }
+    SolveConfig cfg;
+    cfg.mixed = precision == 32 ? 1 : 0;
+    cfg.kmax = 2;
+    std::vector<BatchMember> mem;
+    std::vector<SysDev> hs;
+    double b = 0;
+    const double w = cfg.mixed ? 4.0 : 8.0;
+    for (auto *s : systems) {
+        if (!s->blocks_ok) { set_error("matvec before element blocks were set"); return FG_ERR_STATE; }
+        int kk = std::max(2, s->ws.kmax);
+        int r = ensure_workspace(s, kk, cfg.mixed);
+        if (r) return r;
+        cfg.kmax = kk;
+        mem.push_back({s, nullptr, nullptr, nullptr});
+        hs.push_back(make_desc(s, cfg, false));
+        const Topology &t = s->topo;
+        b += (double)t.nel * (t.S * t.S * w + t.S * 4.0) + 2.0 * t.n * w;
+    }
+    cudaStream_t st = systems[0]->stream;
+    Plan P;
+    int r = build_plan(P, mem, cfg, hs, st);
+    if (r) return r;
+    cudaEvent_t e0, e1;
+    FG_CUDA(cudaEventCreate(&e0));
+    FG_CUDA(cudaEventCreate(&e1));
+    auto run = [&](int n) {
+        for (int i = 0; i < n; ++i)
+            count_launches(cfg.mixed ? enqueue_matvec<float>(P, 2, 0, st) : enqueue_matvec<double>(P, 2, 0, st));
+    };
+    run(2);  // warm-up
+    cudaEventRecord(e0, st);
+    run(reps);
+    cudaEventRecord(e1, st);
+    cudaError_t ce = cudaEventSynchronize(e1);
+    float t = 0;
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (ce != cudaSuccess) return cuda_fail(ce, "bench_matvec");
+    for (auto *s : systems)
+        FG_CUDA(cudaMemsetAsync(s->ws.t.p, 0, s->ws.t.bytes, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    *ms = t / reps;
+    *bytes = b;
+    return FG_OK;
+}
+
+static std::atomic<long long> g_launches{0};
+void count_launches(long long n) { g_launches += n; }
+long long launch_total() { return g_launches.load(); }
 
 }  // namespace fg

@@ -32,6 +32,7 @@ int permute_in(fg_system *s, const double *ref_dev, double *int_dev, cudaStream_
     int n = s->topo.n;
     k_permute<<<(n + 255) / 256 + 1, 256, 0, st>>>(s->perm.as<int>(), ref_dev, int_dev, n, 1);
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
     return FG_OK;
 }
 
@@ -40,6 +41,7 @@ int permute_out(fg_system *s, const double *int_dev, double *ref_dev, cudaStream
     int n = s->topo.n;
     k_permute<<<(n + 255) / 256 + 1, 256, 0, st>>>(s->perm.as<int>(), int_dev, ref_dev, n, 0);
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
     return FG_OK;
 }
 
@@ -80,6 +82,7 @@ int convert_blocks(fg_system *s, cudaStream_t st)
     k_to_f32<<<std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 8 * sm_count())), 256, 0, st>>>(
         s->A64.as<double>(), s->A32.as<float>(), n);
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
     return FG_OK;
 }
 
@@ -90,6 +93,7 @@ int upload_blocks_raw(fg_system *s, const double *raw_dev, cudaStream_t st)
         k_blocks_in<<<(nel + 255) / 256, 256, 0, st>>>(raw_dev, s->eorder.as<int>(), s->A64.as<double>(),
                                                       s->A32.as<float>(), nel, s->nel_pad, s->topo.S * s->topo.S);
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
     return FG_OK;
 }
 
@@ -100,6 +104,7 @@ int download_blocks_raw(const fg_system *s, double *raw_dev, cudaStream_t st)
         k_blocks_out<<<(nel + 255) / 256, 256, 0, st>>>(raw_dev, s->eorder.as<int>(), s->A64.as<double>(), nel,
                                                        s->nel_pad, s->topo.S * s->topo.S);
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
     return FG_OK;
 }
 
@@ -230,6 +235,7 @@ int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaS
                                                            s->diag.as<double>(), s->invd64.as<double>(),
                                                            s->invd32.as<float>(), F_dev);
         FG_CUDA(cudaGetLastError());
+    count_launches(1);
         s->precond = kind;
         return FG_OK;
     }
@@ -245,12 +251,14 @@ int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaS
         else if (B == 3) k_blockdiag_setup<3><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32);
         else k_blockdiag_setup<2><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32);
         FG_CUDA(cudaGetLastError());
+    count_launches(1);
         s->precond = kind;
         if (F_dev) {
             if (B == 4) k_blockdiag_apply64<4><<<g, 128, 0, st>>>(s->node_dof.as<int>(), i64, t.nnodes, t.n, F_dev, F_dev);
             else if (B == 3) k_blockdiag_apply64<3><<<g, 128, 0, st>>>(s->node_dof.as<int>(), i64, t.nnodes, t.n, F_dev, F_dev);
             else k_blockdiag_apply64<2><<<g, 128, 0, st>>>(s->node_dof.as<int>(), i64, t.nnodes, t.n, F_dev, F_dev);
             FG_CUDA(cudaGetLastError());
+    count_launches(1);
         }
         return FG_OK;
     }
@@ -281,6 +289,7 @@ int precond_apply_device(fg_system *s, const double *p, double *z, cudaStream_t 
         FG_CUDA(cudaMemcpyAsync(z, p, 8 * (size_t)(t.n + 1), cudaMemcpyDeviceToDevice, st));
     }
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
     return FG_OK;
 }
 
@@ -410,10 +419,12 @@ int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c, const 
                                                              s->gup.as<double>(), u_dev, *c, s->A64.as<double>(),
                                                              s->Fe.as<double>());
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
     k_transport_F<<<(t.n + 256) / 256, 256, 0, st>>>(t.n, s->nel_pad, s->dinc_ptr.as<int>(), s->dinc.as<int>(),
                                                     s->gien.as<int>(), s->gtype.as<int>(), s->gup.as<double>(),
                                                     s->A64.as<double>(), s->Fe.as<double>(), F_dev);
     FG_CUDA(cudaGetLastError());
+    count_launches(1);
     s->blocks_ok = true;
     return convert_blocks(s, st);
 }

@@ -342,6 +342,104 @@ int fg_solve(fg_system *s, const fg_solver_opts *o, const double *B, double *X, 
     return r;
 }
 
+static int batch_config(fg_system *const *systems, int count, const fg_solver_opts *o, SolveConfig &cfg)
+{
+    if (!systems || count < 1 || !o) { set_error("NULL argument or empty batch"); return FG_ERR_ARG; }
+    if (o->precision != FG_PREC_MIXED && o->precision != FG_PREC_FP64) {
+        set_error("precision must be FG_PREC_FP64 or FG_PREC_MIXED"); return FG_ERR_ARG;
+    }
+    cfg.kmax = o->kmax; cfg.lmax = o->lmax; cfg.tol = o->tol;
+    cfg.mixed = o->precision == FG_PREC_MIXED ? 1 : 0;
+    cfg.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
+    for (int i = 0; i < count; ++i) {
+        if (!systems[i]) { set_error("NULL system in batch"); return FG_ERR_ARG; }
+        if (systems[i]->device != systems[0]->device) { set_error("batch spans devices"); return FG_ERR_ARG; }
+        // the batch runs on the first member's stream: finish each member's own work first
+        if (i > 0) FG_CUDA(cudaStreamSynchronize(systems[i]->stream));
+    }
+    cfg.precond = systems[0]->precond;
+    return FG_OK;
+}
+
+int fg_solve_batch(fg_system *const *systems, int count, const fg_solver_opts *o, const double *const *B,
+                   double *const *X, const double *const *F_true, fg_solve_stats *stats)
+{
+    SolveConfig cfg;
+    int r = batch_config(systems, count, o, cfg);
+    if (r) return r;
+    if (!B || !X) { set_error("NULL B or X"); return FG_ERR_ARG; }
+    std::vector<BatchMember> mem;
+    for (int i = 0; i < count; ++i) {
+        if (!B[i] || !X[i]) { set_error("NULL B[i] or X[i]"); return FG_ERR_ARG; }
+        mem.push_back({systems[i], B[i], F_true ? F_true[i] : nullptr, X[i]});
+    }
+    std::vector<fg_solve_stats> st(count);
+    r = solve_batch(mem, cfg, st.data(), systems[0]->stream);
+    if (stats) std::memcpy(stats, st.data(), sizeof(fg_solve_stats) * count);
+    return r;
+}
+
+int fg_solve_resident(fg_system *const *systems, int count, const fg_solver_opts *o, fg_solve_stats *stats)
+{
+    SolveConfig cfg;
+    int r = batch_config(systems, count, o, cfg);
+    if (r) return r;
+    cfg.device_io = 1;
+    std::vector<BatchMember> mem;
+    for (int i = 0; i < count; ++i) {
+        if (!systems[i]->rhs_ok) { set_error("fg_solve_resident before fg_transport_prepare"); return FG_ERR_STATE; }
+        mem.push_back({systems[i], systems[i]->rhs_b.as<double>(), systems[i]->rhs_f.as<double>(), nullptr});
+    }
+    std::vector<fg_solve_stats> st(count);
+    r = solve_batch(mem, cfg, st.data(), systems[0]->stream);
+    if (stats) std::memcpy(stats, st.data(), sizeof(fg_solve_stats) * count);
+    return r;
+}
+
+int fg_get_solution(const fg_system *s, double *X)
+{
+    if (!s || !X) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (!s->ws.x.p) { set_error("no solution on the device"); return FG_ERR_STATE; }
+    fg_system *m = const_cast<fg_system *>(s);
+    int r = vec_out(m, m->ws.x.as<double>(), X, m->ws.r64.as<double>());
+    if (r) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+long long fg_launch_count(void) { return launch_total(); }
+
+void *fg_system_stream(const fg_system *s) { return s ? (void *)s->stream : nullptr; }
+
+int fg_bench_matvec(fg_system *const *systems, int count, int precision, int reps, double *ms, double *bytes)
+{
+    if (!systems || count < 1 || !ms || !bytes) { set_error("NULL argument"); return FG_ERR_ARG; }
+    std::vector<fg_system *> v(systems, systems + count);
+    for (int i = 1; i < count; ++i) FG_CUDA(cudaStreamSynchronize(systems[i]->stream));
+    return bench_matvec(v, precision, reps, ms, bytes);
+}
+
+int fg_transport_prepare(fg_system *s, const fg_transport_coeffs *c, const double *u)
+{
+    if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = stage(s, s->rhs_f, 8 * (size_t)s->n_pad)) || (r = stage(s, s->rhs_b, 8 * (size_t)s->n_pad))) return r;
+    if (u) {
+        std::memcpy(s->h_vec, u, 8 * (size_t)s->topo.n);
+        s->h_vec[s->topo.n] = 0.0;
+        if ((r = vec_in(s, s->h_vec, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
+    } else {
+        FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, 8 * (size_t)s->n_pad, s->stream));
+    }
+    if ((r = transport_assemble_device(s, c, s->ws.t64.as<double>(), s->rhs_f.as<double>(), s->stream))) return r;
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, 8 * (size_t)s->n_pad, s->stream));
+    FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, 8 * (size_t)s->n_pad, cudaMemcpyDeviceToDevice, s->stream));
+    if ((r = precond_setup_device(s, FG_PRECOND_DIAG, 0, s->rhs_b.as<double>(), s->stream))) return r;
+    s->rhs_ok = true;
+    return FG_OK;
+}
+
 int fg_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc)
 {
     if (!s || !x || !y || !upresc) { set_error("NULL argument"); return FG_ERR_ARG; }

@@ -43,6 +43,9 @@ struct fg_system {
     // geometry (device assembly)
     fg::DevMem gx, gy, gup, gien, gtype, ginvp, Fe, F64;
     bool geometry_ok = false;
+    // resident right-hand side (internal numbering): F and M^-1 F
+    fg::DevMem rhs_f, rhs_b;
+    bool rhs_ok = false;
     // host staging (pinned)
     double *h_vec = nullptr;   // 2*(n+1) doubles
     fg::Workspace ws;
@@ -74,6 +77,8 @@ struct SolveConfig {
 int solve_batch(std::vector<BatchMember> &members, const SolveConfig &cfg,
                 fg_solve_stats *stats, cudaStream_t stream);
 
+int bench_matvec(std::vector<fg_system *> &systems, int precision, int reps, double *ms, double *bytes);
+
 // Matvec on device vectors in internal numbering (precision 64 or 32).
 int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaStream_t st);
 
@@ -88,5 +93,9 @@ int permute_in(fg_system *s, const double *ref_dev, double *int_dev, cudaStream_
 int permute_out(fg_system *s, const double *int_dev, double *ref_dev, cudaStream_t st);
 
 int sm_count();
+
+// launch accounting (fg_launch_count)
+void count_launches(long long n);
+long long launch_total();
 
 }  // namespace fg

@@ -99,6 +99,14 @@ def lib(build_if_missing: bool = True):
     L.fg_solve.argtypes = [_vp, ctypes.POINTER(SolverOpts), _f64p, _f64p, _vp, ctypes.POINTER(SolveStats)]
     L.fg_set_geometry.argtypes = [_vp, _f64p, _f64p, _f64p]
     L.fg_transport_assemble.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), _vp, _vp]
+    L.fg_solve_batch.argtypes = [_vp, _c_int, ctypes.POINTER(SolverOpts), _vp, _vp, _vp, _vp]
+    L.fg_solve_resident.argtypes = [_vp, _c_int, ctypes.POINTER(SolverOpts), _vp]
+    L.fg_get_solution.argtypes = [_vp, _f64p]
+    L.fg_launch_count.restype = ctypes.c_longlong
+    L.fg_system_stream.argtypes = [_vp]
+    L.fg_system_stream.restype = _vp
+    L.fg_bench_matvec.argtypes = [_vp, _c_int, _c_int, _c_int, ctypes.POINTER(_c_dbl), ctypes.POINTER(_c_dbl)]
+    L.fg_transport_prepare.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), _vp]
     L.fg_transport_process.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), ctypes.POINTER(SolverOpts), _c_dbl,
                                        _c_int, _f64p, ctypes.POINTER(ProcessStats)]
     _lib = L
@@ -169,6 +177,11 @@ class System:
     @property
     def handle(self):
         return self._h
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of this system's work, as an integer handle."""
+        return int(lib().fg_system_stream(self._h) or 0)
 
     def info(self) -> dict:
         i = SystemInfo()
@@ -243,6 +256,15 @@ class System:
         check(lib().fg_transport_assemble(self._h, ctypes.byref(c), _ptr(uu), F.ctypes.data))
         return F
 
+    def transport_prepare(self, prob, u=None):
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        check(lib().fg_transport_prepare(self._h, ctypes.byref(_coeffs(prob)), _ptr(uu)))
+
+    def solution(self):
+        X = np.empty(self.n + 1)
+        check(lib().fg_get_solution(self._h, X))
+        return X
+
     def transport_process(self, prob, kmax=30, lmax=1000, tol=1e-10, nonlinear_tol=1e-3, max_nonlinear=1000,
                           precision=FG_PREC_FP64):
         c = TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau))
@@ -252,6 +274,52 @@ class System:
         check(lib().fg_transport_process(self._h, ctypes.byref(c), ctypes.byref(o), nonlinear_tol, max_nonlinear,
                                          U, ctypes.byref(st)))
         return U, {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def _coeffs(prob):
+    return TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau))
+
+
+def launch_count() -> int:
+    return int(lib().fg_launch_count())
+
+
+def solve_batch(systems, Bs, F_trues=None, kmax=30, lmax=1000, tol=1e-10, precision=FG_PREC_FP64, inner_tol=0.0):
+    """Solve systems together (host vectors); returns (list of X, list of stats)."""
+    n = len(systems)
+    H = (_vp * n)(*[s.handle for s in systems])
+    Bs = [np.ascontiguousarray(b, dtype=np.float64) for b in Bs]
+    Xs = [np.zeros(s.n + 1) for s in systems]
+    Bp = (_vp * n)(*[b.ctypes.data for b in Bs])
+    Xp = (_vp * n)(*[x.ctypes.data for x in Xs])
+    Fp = None
+    if F_trues is not None:
+        F_trues = [np.ascontiguousarray(f, dtype=np.float64) for f in F_trues]
+        Fp = (_vp * n)(*[f.ctypes.data for f in F_trues])
+    st = (SolveStats * n)()
+    o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+    check(lib().fg_solve_batch(ctypes.cast(H, _vp), n, ctypes.byref(o), ctypes.cast(Bp, _vp), ctypes.cast(Xp, _vp),
+                               None if Fp is None else ctypes.cast(Fp, _vp), ctypes.cast(st, _vp)))
+    return Xs, [s.as_dict() for s in st]
+
+
+def solve_resident(systems, kmax=30, lmax=1000, tol=1e-10, precision=FG_PREC_FP64, inner_tol=0.0):
+    """Solve systems with their device-resident right-hand sides; returns stats."""
+    n = len(systems)
+    H = (_vp * n)(*[s.handle for s in systems])
+    st = (SolveStats * n)()
+    o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+    check(lib().fg_solve_resident(ctypes.cast(H, _vp), n, ctypes.byref(o), ctypes.cast(st, _vp)))
+    return [s.as_dict() for s in st]
+
+
+def bench_matvec(systems, precision=32, reps=20):
+    """(ms per batched matvec, algorithmic bytes per matvec) timed with CUDA events."""
+    n = len(systems)
+    H = (_vp * n)(*[s.handle for s in systems])
+    ms, b = _c_dbl(), _c_dbl()
+    check(lib().fg_bench_matvec(ctypes.cast(H, _vp), n, precision, reps, ctypes.byref(ms), ctypes.byref(b)))
+    return ms.value, b.value
 
 
 def transport_system(prob, reorder=True) -> System:
