@@ -54,7 +54,7 @@ int matrix_bandwidth(int n, const int *IA, const int *JA);
 // ------------------------------------------------------------ device layout
 constexpr int kMaxColours = 64;
 constexpr int kElemChunk = 1024;   // elements per matvec work item
-constexpr int kMaxParts = 256;     // dof parts (reduction partials) per system
+constexpr int kMaxParts = 1024;    // dof parts (reduction partials) per system
 constexpr int kPartMin = 2048;     // minimum dofs per part
 constexpr int kThreads = 256;
 
@@ -87,7 +87,7 @@ struct SysDev {
     void *V;                   // kmax vectors of T, stride n_pad
     void *w, *t;               // T vectors
     double *H;                 // (kmax+1) x kmax, H[j*kmax + i]
-    double *g, *cs, *sn, *hbuf;// kmax+1 each
+    double *g, *cs, *sn, *hbuf, *y;  // kmax+1 each
     double *part;              // nparts x kPartStride
     unsigned *counter;         // 4 counters (one per reduction kernel kind)
     SysState *st;

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <type_traits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -42,6 +43,7 @@ __device__ __forceinline__ float warp_sum(float v)
 }
 
 template <typename T> __device__ __forceinline__ T ldst(const T *p) { return __ldcs(p); }
+
 
 // Gate of a kernel: 0 = system live, 1 = inside an Arnoldi cycle, < 0 = always.
 __device__ __forceinline__ bool gated(const SysDev &D, int gate)
@@ -106,19 +108,55 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
         const int n = D.n;
-        for (int e = k.e0 + threadIdx.x; e < k.e1; e += blockDim.x) {
-            int idx[S];
-            TA xv[S];
+        if constexpr (S == 3) {
+            // 3x3 blocks: lanes take consecutive elements (their dofs are
+            // neighbours, so gathers and updates share cache sectors) and each
+            // thread keeps two elements' loads in flight before the first
+            // gather.
+            constexpr int U = 2;
+            const int stride = blockDim.x * U;
+            for (int e0 = k.e0 + threadIdx.x; e0 < k.e1; e0 += stride) {
+                int idx[U][3];
+                TA av[U][9], xv[U][3];
 #pragma unroll
-            for (int a = 0; a < S; ++a) idx[a] = __ldcs(D.lm + a * ld + e);
+                for (int u = 0; u < U; ++u) {
+                    const int e = min(e0 + u * (int)blockDim.x, k.e1 - 1);
 #pragma unroll
-            for (int a = 0; a < S; ++a) xv[a] = (TA)X[idx[a]];
+                    for (int a = 0; a < 3; ++a) idx[u][a] = __ldcs(D.lm + a * ld + e);
 #pragma unroll
-            for (int r = 0; r < S; ++r) {
-                TA acc = ldst(A + (size_t)(r * S) * ld + e) * xv[0];
+                    for (int m = 0; m < 9; ++m) av[u][m] = ldst(A + m * ld + e);
+                }
 #pragma unroll
-                for (int q = 1; q < S; ++q) acc += ldst(A + (size_t)(r * S + q) * ld + e) * xv[q];
-                if (idx[r] != n) Y[idx[r]] += (TY)acc;
+                for (int u = 0; u < U; ++u)
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) xv[u][a] = (TA)X[idx[u][a]];
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (e0 + u * (int)blockDim.x >= k.e1) break;
+#pragma unroll
+                    for (int r = 0; r < 3; ++r) {
+                        TA acc = av[u][3 * r] * xv[u][0];
+                        acc += av[u][3 * r + 1] * xv[u][1];
+                        acc += av[u][3 * r + 2] * xv[u][2];
+                        if (idx[u][r] != n) Y[idx[u][r]] += (TY)acc;
+                    }
+                }
+            }
+        } else {
+            for (int e = k.e0 + threadIdx.x; e < k.e1; e += blockDim.x) {
+                int idx[S];
+                TA xv[S];
+#pragma unroll
+                for (int a = 0; a < S; ++a) idx[a] = __ldcs(D.lm + a * ld + e);
+#pragma unroll
+                for (int a = 0; a < S; ++a) xv[a] = (TA)X[idx[a]];
+#pragma unroll
+                for (int r = 0; r < S; ++r) {
+                    TA acc = ldst(A + (size_t)(r * S) * ld + e) * xv[0];
+#pragma unroll
+                    for (int q = 1; q < S; ++q) acc += ldst(A + (size_t)(r * S + q) * ld + e) * xv[q];
+                    if (idx[r] != n) Y[idx[r]] += (TY)acc;
+                }
             }
         }
     }
@@ -259,295 +297,7 @@ k_scale_v0(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const 
     }
 }
 
-// ---------------------------------------------------------------- Arnoldi step
-// Dof parts are walked in sub-tiles of kThreads*4 dofs; within a sub-tile
-// the dot products accumulate in T, across sub-tiles and warps in FP64.
-constexpr int kSub = kThreads * 4;
-
-// pass 1: w = M^-1 t (t cleared), h1_j = <v_j, w>, j = 0..i
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-k_dots1(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
-{
-    __shared__ double red[kPartStride][kThreads / 32];
-    __shared__ double tot[kPartStride];
-    const int total = *nch;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = blockIdx.x; c < total; c += gridDim.x) {
-        const DChunk k = ch[c];
-        const SysDev &D = sys[k.sys];
-        if (!D.st->in_cycle) continue;
-        T *w = (T *)D.w, *t = (T *)D.t;
-        const T *V = (const T *)D.V;
-        const T *invd = sizeof(T) == 8 ? (const T *)D.invd64 : (const T *)D.invd32;
-        for (int j = threadIdx.x; j <= i * (kThreads / 32) + (kThreads / 32 - 1); j += blockDim.x)
-            (&red[0][0])[j] = 0.0;
-        __syncthreads();
-        for (int base = k.d0; base < k.d1; base += kSub) {
-            T wv[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                int d = base + threadIdx.x + q * kThreads;
-                T v = 0;
-                if (d < k.d1) {
-                    if (D.precond == FG_PRECOND_BLOCKDIAG) v = w[d];
-                    else {
-                        T tv = t[d];
-                        v = D.precond == FG_PRECOND_DIAG ? tv * invd[d] : tv;
-                        w[d] = v;
-                    }
-                    t[d] = (T)0;
-                }
-                wv[q] = v;
-            }
-            for (int j = 0; j <= i; ++j) {
-                const T *vj = V + (size_t)j * D.n_pad;
-                T a = 0;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    int d = base + threadIdx.x + q * kThreads;
-                    if (d < k.d1) a += vj[d] * wv[q];
-                }
-                a = warp_sum(a);
-                if (lane == 0) red[j][warp] += (double)a;
-            }
-        }
-        __syncthreads();
-        for (int j = threadIdx.x; j <= i; j += blockDim.x) {
-            double s = 0;
-            for (int w8 = 0; w8 < kThreads / 32; ++w8) s += red[j][w8];
-            D.part[k.part * kPartStride + j] = s;
-        }
-        if (last_part(D, 1)) {
-            reduce_parts(D, i + 1, tot);
-            for (int j = threadIdx.x; j <= i; j += blockDim.x) D.H[j * D.kmax + i] = tot[j];
-        }
-    }
-}
-
-// pass 2: w -= sum_j h1_j v_j ; h2_j = <v_j, w>
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-k_orth1(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
-{
-    __shared__ double red[kPartStride][kThreads / 32];
-    __shared__ double tot[kPartStride];
-    __shared__ T hs[kPartStride];
-    const int total = *nch;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = blockIdx.x; c < total; c += gridDim.x) {
-        const DChunk k = ch[c];
-        const SysDev &D = sys[k.sys];
-        if (!D.st->in_cycle) continue;
-        T *w = (T *)D.w;
-        const T *V = (const T *)D.V;
-        for (int j = threadIdx.x; j <= i; j += blockDim.x) hs[j] = (T)D.H[j * D.kmax + i];
-        for (int j = threadIdx.x; j <= i * (kThreads / 32) + (kThreads / 32 - 1); j += blockDim.x)
-            (&red[0][0])[j] = 0.0;
-        __syncthreads();
-        for (int base = k.d0; base < k.d1; base += kSub) {
-            T wv[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                int d = base + threadIdx.x + q * kThreads;
-                wv[q] = d < k.d1 ? w[d] : (T)0;
-            }
-            for (int j = 0; j <= i; ++j) {
-                const T *vj = V + (size_t)j * D.n_pad;
-                const T h = hs[j];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    int d = base + threadIdx.x + q * kThreads;
-                    if (d < k.d1) wv[q] -= h * vj[d];
-                }
-            }
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                int d = base + threadIdx.x + q * kThreads;
-                if (d < k.d1) w[d] = wv[q];
-            }
-            for (int j = 0; j <= i; ++j) {
-                const T *vj = V + (size_t)j * D.n_pad;
-                T a = 0;
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    int d = base + threadIdx.x + q * kThreads;
-                    if (d < k.d1) a += vj[d] * wv[q];
-                }
-                a = warp_sum(a);
-                if (lane == 0) red[j][warp] += (double)a;
-            }
-        }
-        __syncthreads();
-        for (int j = threadIdx.x; j <= i; j += blockDim.x) {
-            double s = 0;
-            for (int w8 = 0; w8 < kThreads / 32; ++w8) s += red[j][w8];
-            D.part[k.part * kPartStride + j] = s;
-        }
-        if (last_part(D, 2)) {
-            reduce_parts(D, i + 1, tot);
-            for (int j = threadIdx.x; j <= i; j += blockDim.x) {
-                D.hbuf[j] = tot[j];
-                D.H[j * D.kmax + i] += tot[j];
-            }
-        }
-    }
-}
-
-// pass 3: w -= sum_j h2_j v_j ; ||w||; then, in the last part, the Givens
-// rotations of column i and the residual estimate (pgmres.c:111-157).
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-k_orth2(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
-{
-    __shared__ double red[kThreads / 32];
-    __shared__ double tot[1];
-    __shared__ T hs[kPartStride];
-    const int total = *nch;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = blockIdx.x; c < total; c += gridDim.x) {
-        const DChunk k = ch[c];
-        const SysDev &D = sys[k.sys];
-        if (!D.st->in_cycle) continue;
-        T *w = (T *)D.w;
-        const T *V = (const T *)D.V;
-        for (int j = threadIdx.x; j <= i; j += blockDim.x) hs[j] = (T)D.hbuf[j];
-        __syncthreads();
-        double acc = 0.0;
-        for (int base = k.d0; base < k.d1; base += kSub) {
-            T wv[4];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                int d = base + threadIdx.x + q * kThreads;
-                wv[q] = d < k.d1 ? w[d] : (T)0;
-            }
-            for (int j = 0; j <= i; ++j) {
-                const T *vj = V + (size_t)j * D.n_pad;
-                const T h = hs[j];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    int d = base + threadIdx.x + q * kThreads;
-                    if (d < k.d1) wv[q] -= h * vj[d];
-                }
-            }
-            T a = 0;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                int d = base + threadIdx.x + q * kThreads;
-                if (d < k.d1) { w[d] = wv[q]; a += wv[q] * wv[q]; }
-            }
-            acc += (double)a;
-        }
-        acc = warp_sum(acc);
-        if (lane == 0) red[warp] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double s = 0;
-            for (int w8 = 0; w8 < kThreads / 32; ++w8) s += red[w8];
-            D.part[k.part * kPartStride] = s;
-        }
-        if (last_part(D, 3)) {
-            reduce_parts(D, 1, tot);
-            if (threadIdx.x == 0) {
-                SysState *st = D.st;
-                const int km = D.kmax;
-                double *H = D.H, *cs = D.cs, *sn = D.sn, *g = D.g;
-                double hn = sqrt(tot[0]);
-                st->hn = hn;
-                H[(i + 1) * km + i] = hn;
-                for (int j = 0; j <= i - 1; ++j) {
-                    double h1 = cs[j] * H[j * km + i] + sn[j] * H[(j + 1) * km + i];
-                    double h2 = -sn[j] * H[j * km + i] + cs[j] * H[(j + 1) * km + i];
-                    H[j * km + i] = h1;
-                    H[(j + 1) * km + i] = h2;
-                }
-                double r = sqrt(H[i * km + i] * H[i * km + i] + H[(i + 1) * km + i] * H[(i + 1) * km + i]);
-                cs[i] = H[i * km + i] / r;
-                sn[i] = H[(i + 1) * km + i] / r;
-                H[i * km + i] = r;
-                H[(i + 1) * km + i] = 0.0;
-                g[i + 1] = -sn[i] * g[i];
-                g[i] = cs[i] * g[i];
-                st->rho = fabs(g[i + 1]);
-                st->steps = i + 1;
-                st->iterations += 1;
-                double target = D.mixed ? st->target : st->eps;
-                if (!(r > 0.0) || !isfinite(st->rho)) {
-                    st->status = FG_ERR_BREAKDOWN;
-                    st->in_cycle = 0;
-                    if (!(r > 0.0)) st->steps = i;     // column i unusable
-                } else if (!(st->rho > target) || i + 1 >= D.kmax - 1 || !(hn > 0.0)) {
-                    st->in_cycle = 0;
-                }
-            }
-        }
-    }
-}
-
-// v_{i+1} = w * (1 / h_{i+1,i}) (pgmres.c:117)
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-k_normalize(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
-{
-    const int total = *nch;
-    for (int c = blockIdx.x; c < total; c += gridDim.x) {
-        const DChunk k = ch[c];
-        const SysDev &D = sys[k.sys];
-        if (!D.st->in_cycle) continue;
-        const T sc = (T)(1.0 / D.st->hn);
-        const T *w = (const T *)D.w;
-        T *v = (T *)D.V + (size_t)(i + 1) * D.n_pad;
-        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) v[d] = sc * w[d];
-    }
-}
-
-// ---------------------------------------------------------------- cycle end
-// y from the triangular system (pgmres.c:163-171), computed redundantly by
-// every CTA from the same data; x += V y (:173-175).  The last part does the
-// restart bookkeeping (:177-179).
-template <typename T>
-__global__ void __launch_bounds__(kThreads)
-k_update(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch)
-{
-    __shared__ double y[kPartStride];
-    const int total = *nch;
-    for (int c = blockIdx.x; c < total; c += gridDim.x) {
-        const DChunk k = ch[c];
-        const SysDev &D = sys[k.sys];
-        if (!D.st->live) continue;
-        const int m = D.st->steps;
-        const int km = D.kmax;
-        __syncthreads();
-        if (threadIdx.x == 0 && m > 0) {
-            int i = m - 1;
-            y[i] = D.g[i] / D.H[i * km + i];
-            for (int j = i - 1; j >= 0; --j) {
-                double s = 0.0;
-                for (int q = j + 1; q <= i; ++q) s = s + D.H[j * km + q] * y[q];
-                y[j] = (D.g[j] - s) / D.H[j * km + j];
-            }
-        }
-        __syncthreads();
-        const T *V = (const T *)D.V;
-        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) {
-            double xv = D.x[d];
-            for (int j = 0; j < m; ++j) xv = xv + (double)V[(size_t)j * D.n_pad + d] * y[j];
-            D.x[d] = xv;
-        }
-        if (last_part(D, 4)) {
-            if (threadIdx.x == 0) {
-                SysState *st = D.st;
-                st->cycles += 1;
-                st->in_cycle = 0;
-                if (st->status == FG_ERR_BREAKDOWN) { st->live = 0; }
-                else if (!D.mixed) {
-                    if (!(st->rho > st->eps)) { st->converged = 1; st->live = 0; }
-                    else if (st->cycles >= D.lmax) { st->status = FG_ERR_NOTCONV; st->live = 0; }
-                }
-            }
-        }
-    }
-}
+#include "arnoldi.cuh"
 
 // final true residual: t64 holds A x
 __global__ void __launch_bounds__(kThreads)
@@ -657,7 +407,7 @@ int elem_chunk(int cnt)
 
 int parts_for(int n)
 {
-    int p = (n + 511) / 512;
+    int p = (n + kPartMin - 1) / kPartMin;
     return std::max(1, std::min(kMaxParts, p));
 }
 
@@ -699,8 +449,10 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     for (int s = 0; s < P.nsys; ++s) {
         int n = mem[s].s->topo.n;
         int np = hs[s].nparts;
+        // part boundaries on multiples of 4 dofs (16-byte packs in FP32 and FP64)
         for (int p = 0; p < np; ++p) {
-            int d0 = (int)((long long)n * p / np), d1 = (int)((long long)n * (p + 1) / np);
+            int d0 = (int)((long long)n * p / np) & ~3;
+            int d1 = p + 1 == np ? n : (int)((long long)n * (p + 1) / np) & ~3;
             dch.push_back({s, p, d0, d1});
         }
         int nn = mem[s].s->topo.nnodes;
@@ -794,7 +546,7 @@ static int ensure_workspace(fg_system *s, int kmax, int mixed)
     if ((r = w.V.alloc(ts * np * kmax)) || (r = w.w.alloc(ts * np)) || (r = w.t.alloc(ts * np)) ||
         (r = w.x.alloc(8 * np)) || (r = w.b.alloc(8 * np)) || (r = w.ftrue.alloc(8 * np)) ||
         (r = w.r64.alloc(8 * np)) || (r = w.t64.alloc(8 * np)) || (r = w.u64.alloc(8 * np)) ||
-        (r = w.small.alloc(8 * ((size_t)(kmax + 1) * kmax + 4 * (kmax + 1)))) ||
+        (r = w.small.alloc(8 * ((size_t)(kmax + 1) * kmax + 5 * (kmax + 1)))) ||
         (r = w.part.alloc(8 * (size_t)kMaxParts * kPartStride)) ||
         (r = w.counter.alloc(sizeof(unsigned) * 8)) || (r = w.state.alloc(sizeof(SysState))))
         return r;
@@ -824,6 +576,7 @@ static SysDev make_desc(fg_system *s, const SolveConfig &cfg, bool has_f)
     D.cs = D.g + (cfg.kmax + 1);
     D.sn = D.cs + (cfg.kmax + 1);
     D.hbuf = D.sn + (cfg.kmax + 1);
+    D.y = D.hbuf + (cfg.kmax + 1);
     D.part = w.part.as<double>();
     D.counter = w.counter.as<unsigned>();
     D.st = w.state.as<SysState>();
