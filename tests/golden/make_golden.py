@@ -1,0 +1,54 @@
+"""Generate the golden fixtures from the reference's own C (checker build).
+
+Run here, where the reference sources are present:
+    make -C oracle ref REF=/root/reference && python tests/golden/make_golden.py
+It writes tests/golden/sst_*.npz: mesh, connectivity (lm, Perm, invPerm,
+bandwidths), element blocks and right-hand side at u = 0, one Diag +
+GMRES(30) solve, and the full CAU Process loop (solution and GMRES
+iterations), all computed by the reference's Fill_LM, Permutation_of_LM,
+Build_K_F_SUPG, Diag_precond_EBE_setup, pgmres and Process.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+import oracle as O  # noqa: E402
+from parallel_fem_codes_gb300 import meshgen as G  # noqa: E402
+
+CASES = {
+    # name: (nodes per side, angle, conductivity, gamma, f, upmode, upval)
+    "sst_17_adv": (17, 30.0, 1e-6, 0.0, 0.0, 0, 1.0),
+    "sst_12_mixed": (12, 200.0, 1e-3, 0.5, 1.0, 0, 1.0),
+    "sst_9_teste": (9, 0.0, 1.0, 0.0, 0.0, 1, 10.0),
+}
+
+
+def main():
+    if not O.ref_available():
+        raise SystemExit("build the reference first: make -C oracle ref REF=/root/reference")
+    for name, (n, ang, k, gm, f, upm, upv) in CASES.items():
+        p = G.transport_problem(n, angle_deg=ang, k=k, gamma=gm, f=f, upmode=upm, upval=upv)
+        if name == "sst_9_teste":
+            p.beta = (0.0, 0.0)
+        m = p.mesh
+        lm, perm, inv, band, nnz = O.ref_connectivity(m)
+        A, F = O.ref_build(p)
+        X, it, Diag, invDiag, Fp = O.ref_diag_pgmres(lm, A, perm, inv, F, kmax=30, lmax=1000, tol=1e-10)
+        U, its = O.ref_process(p, 1e-10, 1e-3, 30, 1000)
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            x=m.x, y=m.y, ien=m.ien, type=m.type, invp=m.invp, neq=m.neq, upresc=p.upresc,
+            k=p.k, gamma=p.gamma, beta=np.array(p.beta), f=p.f, upmode=p.upmode, upval=p.upval,
+            lm=lm, perm=perm, invperm=inv, band=band, nnz=nnz, A=A, F=F[: m.neq],
+            Fp=Fp[: m.neq], Diag=Diag[: m.neq], X=X[: m.neq], gmres_its=it,
+            U=U, process_its=its)
+        print(name, "neq", m.neq, "gmres", it, "process gmres", its)
+
+
+if __name__ == "__main__":
+    main()
