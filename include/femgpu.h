@@ -93,6 +93,22 @@ int fg_get_blocks(const fg_system *s, double *A);
  * vectors of n+1 entries; Q[n] is returned as 0.  precision: 64 or 32. */
 int fg_matvec(fg_system *s, const double *P, double *Q, int precision);
 
+/* Q = A P like fg_matvec, on DEVICE vectors the caller owns (n+1 entries
+ * each, reference numbering, Q[n] returned as 0), without allocating any
+ * memory.  No counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc after their set-up phase (their device memory
+ * belongs to another allocator, or their loop must not pay cudaMalloc's
+ * implicit synchronisation).  The scratch it needs comes from one fixed
+ * array of about 33 MiB compiled into the library and held on every GPU
+ * that loads it; systems with more than 2,097,151 equations or more than
+ * 65,536 colour chunks of 1024 elements are rejected with FG_ERR_ARG.
+ * The first call on a device looks up the array's device address, so make
+ * that first call before starting any stream capture.  The work is queued
+ * on the system's stream (fg_system_stream) and the call returns without
+ * waiting for it.  All calls share the array: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
+int fg_matvec_noalloc(fg_system *s, const double *P_dev, double *Q_dev, int precision);
+
 /* ---- preconditioners (Solvers_and_Preconditioners/preconditioners.h) ---- */
 enum { FG_PRECOND_NONE = 0, FG_PRECOND_DIAG = 1, FG_PRECOND_BLOCKDIAG = 2 };
 enum {

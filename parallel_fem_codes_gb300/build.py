@@ -22,6 +22,7 @@ UNITS = [
     ("system.cu", []),
     ("krylov.cu", []),
     ("setup.cu", ["-fmad=false"]),
+    ("noalloc.cu", []),
 ]
 
 

@@ -811,6 +811,26 @@ int bench_matvec(std::vector<fg_system *> &systems, int precision, int reps, dou
     return FG_OK;
 }
 
+// Colour-by-colour matvec y += A x from a caller-placed descriptor and chunk
+// table (device memory the caller owns); used by fg_matvec_noalloc.
+int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const EChunk *ch_dev, const int *counts_dev,
+                          const int *off_host, int ncol, const double *x, double *y, cudaStream_t st)
+{
+    for (int c = 0; c < ncol; ++c) {
+        int cnt = off_host[c + 1] - off_host[c];
+        if (!cnt) continue;
+        const EChunk *cp = ch_dev + off_host[c];
+        const int *np = counts_dev + c;
+        if (precision == 32)
+            MvLaunch::go<float, double, double>(S, grid_for(cnt), st, sys_dev, cp, np, -1, 2, 2, 0, x, y);
+        else
+            MvLaunch::go<double, double, double>(S, grid_for(cnt), st, sys_dev, cp, np, -1, 2, 2, 0, x, y);
+        count_launches(1);
+    }
+    FG_CUDA(cudaGetLastError());
+    return FG_OK;
+}
+
 static std::atomic<long long> g_launches{0};
 void count_launches(long long n) { g_launches += n; }
 long long launch_total() { return g_launches.load(); }

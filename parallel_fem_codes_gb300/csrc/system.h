@@ -78,6 +78,8 @@ int solve_batch(std::vector<BatchMember> &members, const SolveConfig &cfg,
                 fg_solve_stats *stats, cudaStream_t stream);
 
 int bench_matvec(std::vector<fg_system *> &systems, int precision, int reps, double *ms, double *bytes);
+int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const EChunk *ch_dev, const int *counts_dev,
+                          const int *off_host, int ncol, const double *x, double *y, cudaStream_t st);
 
 // Matvec on device vectors in internal numbering (precision 64 or 32).
 int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaStream_t st);
