@@ -225,6 +225,41 @@ int fg_transport_process(fg_system *s, const fg_transport_coeffs *c,
                          const fg_solver_opts *opts, double nonlinear_tol,
                          int max_nonlinear, double *U, fg_process_stats *stats);
 
+/* ---- request server: continuous batching of transport solves ----
+ * A worker thread owns one batch.  Requests (a system whose geometry is set,
+ * with transport coefficients) wait in a FIFO; between restart cycles the
+ * worker admits waiting requests while the Krylov workspace of the admitted
+ * ones fits the HBM budget and the active count is below max_active,
+ * assembles them on the device (SUPG/CAU at u = 0, fresh Diag), and every
+ * cycle advances all admitted solves together; a solve leaves the batch as
+ * soon as it converges.  Meshes and Krylov state stay on the device.  A
+ * result is bit-identical to solving the same system alone. */
+typedef struct fg_server fg_server;
+typedef struct {
+    int kmax, lmax;
+    double tol;
+    int precision;            /* FG_PREC_MIXED or FG_PREC_FP64          */
+    double inner_tol;
+    size_t hbm_budget_bytes;  /* 0: 80% of the free device memory       */
+    int max_active;           /* 0: no limit                            */
+} fg_server_opts;
+typedef struct {
+    unsigned long long tag;
+    fg_solve_stats stats;
+    double t_submit, t_admit, t_done;  /* seconds on the server's clock */
+} fg_server_result;
+int fg_server_create(fg_server **out, const fg_server_opts *opts);
+/* Queue a request; thread-safe.  The system must not be in use elsewhere
+ * until its result has been polled. */
+int fg_server_submit(fg_server *sv, fg_system *s, const fg_transport_coeffs *c, unsigned long long tag);
+/* Move up to max finished results into out; *count receives how many. */
+int fg_server_poll(fg_server *sv, fg_server_result *out, int max, int *count);
+/* Block until at least n results are waiting to be polled, or timeout_s. */
+int fg_server_wait(fg_server *sv, int n, double timeout_s);
+/* Seconds since the server was created (the clock of the results). */
+double fg_server_now(const fg_server *sv);
+int fg_server_destroy(fg_server *sv);
+
 #ifdef __cplusplus
 }
 #endif

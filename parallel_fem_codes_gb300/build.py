@@ -23,6 +23,7 @@ UNITS = [
     ("krylov.cu", []),
     ("setup.cu", ["-fmad=false"]),
     ("noalloc.cu", []),
+    ("server.cu", []),
 ]
 
 

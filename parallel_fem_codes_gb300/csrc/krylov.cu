@@ -583,140 +583,216 @@ static SysDev make_desc(fg_system *s, const SolveConfig &cfg, bool has_f)
     return D;
 }
 
-int solve_batch(std::vector<BatchMember> &mem, const SolveConfig &cfg, fg_solve_stats *stats, cudaStream_t st)
+int validate_member(fg_system *s, const SolveConfig &cfg)
 {
-    if (mem.empty()) return FG_OK;
     if (cfg.kmax < 2 || cfg.kmax > kPartStride - 4) { set_error("kmax must be in [2, 60]"); return FG_ERR_ARG; }
     if (cfg.lmax < 1) { set_error("lmax must be >= 1"); return FG_ERR_ARG; }
-    for (auto &m : mem) {
-        fg_system *s = m.s;
-        if (!s->blocks_ok) { set_error("solve before element blocks were set"); return FG_ERR_STATE; }
-        if (cfg.precond != FG_PRECOND_NONE && s->precond != cfg.precond) {
-            set_error("solve with a preconditioner that was not set up"); return FG_ERR_STATE;
-        }
-        if (cfg.precond == FG_PRECOND_BLOCKDIAG && s->topo.ndof < 2) {
-            set_error("block-diagonal preconditioner needs ndof >= 2"); return FG_ERR_UNSUPPORTED;
-        }
+    if (!s->blocks_ok) { set_error("solve before element blocks were set"); return FG_ERR_STATE; }
+    if (cfg.precond != FG_PRECOND_NONE && s->precond != cfg.precond) {
+        set_error("solve with a preconditioner that was not set up"); return FG_ERR_STATE;
     }
-    auto t0 = std::chrono::steady_clock::now();
-    std::vector<SysDev> hs;
-    hs.reserve(mem.size());
-    for (auto &m : mem) {
-        fg_system *s = m.s;
-        int r = ensure_workspace(s, cfg.kmax, cfg.mixed);
-        if (r) return r;
-        Workspace &w = s->ws;
-        size_t vb = 8 * (size_t)s->n_pad;
-        FG_CUDA(cudaMemsetAsync(w.x.p, 0, vb, st));
-        FG_CUDA(cudaMemsetAsync(w.t64.p, 0, vb, st));
-        FG_CUDA(cudaMemsetAsync(w.t.p, 0, (cfg.mixed ? 4 : 8) * (size_t)s->n_pad, st));
-        FG_CUDA(cudaMemsetAsync(w.V.p, 0, (cfg.mixed ? 4 : 8) * (size_t)s->n_pad * cfg.kmax, st));
-        FG_CUDA(cudaMemsetAsync(w.small.p, 0, w.small.bytes, st));
-        if (cfg.device_io) {
-            FG_CUDA(cudaMemcpyAsync(w.b.p, m.B, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToDevice, st));
-            if (m.Ftrue) FG_CUDA(cudaMemcpyAsync(w.ftrue.p, m.Ftrue, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToDevice, st));
-        } else {
-            // host vectors in reference numbering -> staging (r64) -> internal
-            size_t hb = 8 * (size_t)(s->topo.n + 1);
-            FG_CUDA(cudaMemcpyAsync(w.r64.p, m.B, hb, cudaMemcpyHostToDevice, st));
-            if ((r = permute_in(s, w.r64.as<double>(), w.b.as<double>(), st))) return r;
-            if (m.Ftrue) {
-                FG_CUDA(cudaMemcpyAsync(w.u64.p, m.Ftrue, hb, cudaMemcpyHostToDevice, st));
-                if ((r = permute_in(s, w.u64.as<double>(), w.ftrue.as<double>(), st))) return r;
-            }
-        }
-        hs.push_back(make_desc(s, cfg, m.Ftrue != nullptr));
+    if (cfg.precond == FG_PRECOND_BLOCKDIAG && s->topo.ndof < 2) {
+        set_error("block-diagonal preconditioner needs ndof >= 2"); return FG_ERR_UNSUPPORTED;
     }
-    Plan P;
-    int r = build_plan(P, mem, cfg, hs, st);
-    if (r) return r;
-    const int nsys = P.nsys;
-    k_init_state<<<(nsys + 127) / 128, 128, 0, st>>>(P.sysdev.as<SysDev>(), nsys);
-    FG_CUDA(cudaGetLastError());
-    count_launches(1);
-    int graph_nodes = 0;
+    return FG_OK;
+}
 
-    // one restart cycle as a CUDA graph, replayed until no system is live
-    cudaGraphExec_t exec = nullptr;
-    if (cfg.use_graph) {
+size_t workspace_bytes(const fg_system *s, int kmax, int mixed)
+{
+    size_t np = (size_t)s->n_pad, ts = mixed ? 4 : 8;
+    return ts * np * (kmax + 2) + 8 * np * 6 + 8 * ((size_t)(kmax + 1) * kmax + 5 * (kmax + 1)) +
+           8 * (size_t)kMaxParts * kPartStride + 256;
+}
+
+BatchRun::BatchRun(const SolveConfig &c, cudaStream_t s) : cfg(c), st(s) {}
+
+BatchRun::~BatchRun()
+{
+    if (exec) cudaGraphExecDestroy(exec);
+    if (h_live) cudaFreeHost(h_live);
+}
+
+// Workspace, cleared vectors and right-hand side of a new member (queued on
+// the batch stream); the member joins at the next commit().
+int BatchRun::stage(const BatchMember &m)
+{
+    fg_system *s = m.s;
+    int r = validate_member(s, cfg);
+    if (r) return r;
+    if ((r = ensure_workspace(s, cfg.kmax, cfg.mixed))) return r;
+    Workspace &w = s->ws;
+    size_t vb = 8 * (size_t)s->n_pad;
+    FG_CUDA(cudaMemsetAsync(w.x.p, 0, vb, st));
+    FG_CUDA(cudaMemsetAsync(w.t64.p, 0, vb, st));
+    FG_CUDA(cudaMemsetAsync(w.t.p, 0, (cfg.mixed ? 4 : 8) * (size_t)s->n_pad, st));
+    FG_CUDA(cudaMemsetAsync(w.V.p, 0, (cfg.mixed ? 4 : 8) * (size_t)s->n_pad * cfg.kmax, st));
+    FG_CUDA(cudaMemsetAsync(w.small.p, 0, w.small.bytes, st));
+    if (cfg.device_io) {
+        FG_CUDA(cudaMemcpyAsync(w.b.p, m.B, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToDevice, st));
+        if (m.Ftrue) FG_CUDA(cudaMemcpyAsync(w.ftrue.p, m.Ftrue, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToDevice, st));
+    } else {
+        // host vectors in reference numbering -> staging -> internal numbering
+        size_t hb = 8 * (size_t)(s->topo.n + 1);
+        FG_CUDA(cudaMemcpyAsync(w.r64.p, m.B, hb, cudaMemcpyHostToDevice, st));
+        if ((r = permute_in(s, w.r64.as<double>(), w.b.as<double>(), st))) return r;
+        if (m.Ftrue) {
+            FG_CUDA(cudaMemcpyAsync(w.u64.p, m.Ftrue, hb, cudaMemcpyHostToDevice, st));
+            if ((r = permute_in(s, w.u64.as<double>(), w.ftrue.as<double>(), st))) return r;
+        }
+    }
+    mem.push_back(m);
+    hs.push_back(make_desc(s, cfg, m.Ftrue != nullptr));
+    ++pending;
+    return FG_OK;
+}
+
+// Rebuild the work tables for the current members and initialise the state
+// of the members staged since the last commit.
+int BatchRun::commit()
+{
+    if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+    if (mem.empty()) { pending = 0; return FG_OK; }
+    P = std::make_unique<Plan>();
+    int r = build_plan(*P, mem, cfg, hs, st);
+    if (r) return r;
+    if (pending > 0) {
+        int first = (int)mem.size() - pending;
+        k_init_state<<<(pending + 127) / 128, 128, 0, st>>>(P->sysdev.as<SysDev>() + first, pending);
+        FG_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
+    pending = 0;
+    if ((int)live_cap < (int)mem.size()) {
+        if (h_live) cudaFreeHost(h_live);
+        live_cap = std::max<size_t>(mem.size(), 2 * live_cap);
+        FG_CUDA(cudaMallocHost(&h_live, sizeof(int) * live_cap));
+    }
+    return FG_OK;
+}
+
+// One restart cycle of every member; live[i] tells whether member i goes on.
+int BatchRun::cycle(bool use_graph, std::vector<int> &live)
+{
+    live.assign(mem.size(), 0);
+    if (mem.empty()) return FG_OK;
+    const Plan &Pl = *P;
+    cudaError_t ce = cudaSuccess;
+    if (use_graph && !exec) {
         cudaGraph_t graph = nullptr;
         FG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        graph_nodes = cfg.mixed ? enqueue_cycle<float>(P, cfg, st) : enqueue_cycle<double>(P, cfg, st);
-        cudaError_t ce = cudaStreamEndCapture(st, &graph);
+        graph_nodes = cfg.mixed ? enqueue_cycle<float>(Pl, cfg, st) : enqueue_cycle<double>(Pl, cfg, st);
+        ce = cudaStreamEndCapture(st, &graph);
         if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
         ce = cudaGraphInstantiate(&exec, graph, 0);
         cudaGraphDestroy(graph);
-        if (ce != cudaSuccess) return cuda_fail(ce, "cudaGraphInstantiate");
+        if (ce != cudaSuccess) { exec = nullptr; return cuda_fail(ce, "cudaGraphInstantiate"); }
     }
-    std::vector<int> live(nsys, 1);
-    int *h_live = nullptr;
-    FG_CUDA(cudaMallocHost(&h_live, sizeof(int) * nsys));
-    int guard = cfg.lmax + 2;
-    int rc = FG_OK;
-    for (int cyc = 0; cyc < guard; ++cyc) {
-        cudaError_t ce;
-        if (exec) {
-            ce = cudaGraphLaunch(exec, st);
-            count_launches(graph_nodes);
-        } else {
-            count_launches(cfg.mixed ? enqueue_cycle<float>(P, cfg, st) : enqueue_cycle<double>(P, cfg, st));
-            ce = cudaGetLastError();
-        }
-        if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_live, P.live.p, sizeof(int) * nsys, cudaMemcpyDeviceToHost, st);
-        if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
-        if (ce != cudaSuccess) { rc = cuda_fail(ce, "GMRES cycle"); break; }
+    if (use_graph) {
+        ce = cudaGraphLaunch(exec, st);
+        count_launches(graph_nodes);
+    } else {
+        count_launches(cfg.mixed ? enqueue_cycle<float>(Pl, cfg, st) : enqueue_cycle<double>(Pl, cfg, st));
+        ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_live, Pl.live.p, sizeof(int) * mem.size(), cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "GMRES cycle");
+    for (size_t i = 0; i < mem.size(); ++i) live[i] = h_live[i];
+    return FG_OK;
+}
+
+// True residual of the listed members' current x (FP64), then their state.
+int BatchRun::finish(const std::vector<int> &idx, std::vector<SysState> &out)
+{
+    out.assign(idx.size(), SysState{});
+    if (idx.empty()) return FG_OK;
+    std::vector<BatchMember> sub;
+    std::vector<SysDev> shs;
+    for (int i : idx) { sub.push_back(mem[i]); shs.push_back(hs[i]); }
+    Plan F;
+    int r = build_plan(F, sub, cfg, shs, st);
+    if (r) return r;
+    const SysDev *sys = F.sysdev.as<SysDev>();
+    for (int c = 0; c < F.ncol; ++c) {
+        int cnt = F.ech_off[c + 1] - F.ech_off[c];
+        if (!cnt) continue;
+        MvLaunch::go<double, double, double>(F.S, grid_for(cnt), st, sys, F.echunks.as<EChunk>() + F.ech_off[c],
+                                             F.ecount.as<int>() + c, -1, 0, 0, 0, nullptr, nullptr);
+        count_launches(1);
+    }
+    k_final<<<grid_for(F.n_dch), kThreads, 0, st>>>(sys, F.dchunks.as<DChunk>(), F.dcount.as<int>());
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    for (size_t q = 0; q < idx.size(); ++q)
+        FG_CUDA(cudaMemcpyAsync(&out[q], sub[q].s->ws.state.p, sizeof(SysState), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    return FG_OK;
+}
+
+// Drop members (indices ascending or not); the tables are rebuilt at the
+// next commit().
+void BatchRun::remove(std::vector<int> idx)
+{
+    std::sort(idx.rbegin(), idx.rend());
+    for (int i : idx) {
+        mem.erase(mem.begin() + i);
+        hs.erase(hs.begin() + i);
+    }
+    if (exec) { cudaGraphExecDestroy(exec); exec = nullptr; }
+    P.reset();
+}
+
+void fill_stats(const SysState &s, double secs, fg_solve_stats &o)
+{
+    o.iterations = s.iterations;
+    o.cycles = s.cycles;
+    o.converged = s.converged;
+    o.status = s.status;
+    o.rho = s.rho;
+    o.eps = s.eps;
+    o.true_rel_residual = s.true_res;
+    o.seconds = secs;
+}
+
+int solve_batch(std::vector<BatchMember> &mem, const SolveConfig &cfg, fg_solve_stats *stats, cudaStream_t st)
+{
+    if (mem.empty()) return FG_OK;
+    for (auto &m : mem) {
+        int r = validate_member(m.s, cfg);
+        if (r) return r;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    BatchRun run(cfg, st);
+    int r;
+    for (auto &m : mem)
+        if ((r = run.stage(m))) return r;
+    if ((r = run.commit())) return r;
+    std::vector<int> live;
+    for (int cyc = 0; cyc < cfg.lmax + 2; ++cyc) {
+        if ((r = run.cycle(cfg.use_graph != 0, live))) return r;
         int any = 0;
-        for (int s = 0; s < nsys; ++s) any |= h_live[s];
+        for (int v : live) any |= v;
         if (!any) break;
     }
-    cudaFreeHost(h_live);
-    if (exec) cudaGraphExecDestroy(exec);
-    if (rc) return rc;
-    // final true residual for every system
-    {
-        const SysDev *sys = P.sysdev.as<SysDev>();
-        for (int c = 0; c < P.ncol; ++c) {
-            int cnt = P.ech_off[c + 1] - P.ech_off[c];
-            if (!cnt) continue;
-            MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, P.echunks.as<EChunk>() + P.ech_off[c],
-                                                 P.ecount.as<int>() + c, -1, 0, 0, 0, nullptr, nullptr);
-        }
-        k_final<<<grid_for(P.n_dch), kThreads, 0, st>>>(sys, P.dchunks.as<DChunk>(), P.dcount.as<int>());
-        FG_CUDA(cudaGetLastError());
-        count_launches(P.ncol + 1);
-    }
-    // results
-    for (int s = 0; s < nsys; ++s) {
-        BatchMember &m = mem[s];
+    std::vector<int> all(mem.size());
+    for (size_t i = 0; i < all.size(); ++i) all[i] = (int)i;
+    std::vector<SysState> sts;
+    if ((r = run.finish(all, sts))) return r;
+    for (size_t i = 0; i < mem.size(); ++i) {
+        BatchMember &m = mem[i];
         fg_system *sy = m.s;
-        if (m.X) {
-            if (cfg.device_io) {
-                FG_CUDA(cudaMemcpyAsync(m.X, sy->ws.x.p, 8 * (size_t)(sy->topo.n + 1), cudaMemcpyDeviceToDevice, st));
-            } else {
-                if ((r = permute_out(sy, sy->ws.x.as<double>(), sy->ws.r64.as<double>(), st))) return r;
-                FG_CUDA(cudaMemcpyAsync(m.X, sy->ws.r64.p, 8 * (size_t)(sy->topo.n + 1), cudaMemcpyDeviceToHost, st));
-            }
+        if (!m.X) continue;
+        if (cfg.device_io) {
+            FG_CUDA(cudaMemcpyAsync(m.X, sy->ws.x.p, 8 * (size_t)(sy->topo.n + 1), cudaMemcpyDeviceToDevice, st));
+        } else {
+            if ((r = permute_out(sy, sy->ws.x.as<double>(), sy->ws.r64.as<double>(), st))) return r;
+            FG_CUDA(cudaMemcpyAsync(m.X, sy->ws.r64.p, 8 * (size_t)(sy->topo.n + 1), cudaMemcpyDeviceToHost, st));
         }
     }
-    std::vector<SysState> sts(nsys);
-    for (int s = 0; s < nsys; ++s)
-        FG_CUDA(cudaMemcpyAsync(&sts[s], mem[s].s->ws.state.p, sizeof(SysState), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    int worst = FG_OK;
-    for (int s = 0; s < nsys; ++s) {
-        if (!stats) break;
-        fg_solve_stats &o = stats[s];
-        o.iterations = sts[s].iterations;
-        o.cycles = sts[s].cycles;
-        o.converged = sts[s].converged;
-        o.status = sts[s].status;
-        o.rho = sts[s].rho;
-        o.eps = sts[s].eps;
-        o.true_rel_residual = sts[s].true_res;
-        o.seconds = secs;
-        if (o.status != FG_OK && worst == FG_OK) worst = o.status;
-    }
+    if (stats)
+        for (size_t i = 0; i < mem.size(); ++i) fill_stats(sts[i], secs, stats[i]);
     return FG_OK;
 }
 

@@ -73,6 +73,39 @@ struct SolveConfig {
     int use_graph = 1;
 };
 
+struct Plan;
+
+// A steppable batch: members are staged and committed between restart
+// cycles, each cycle advances every live member, finished members are
+// removed.  solve_batch and the request server are built on it.
+class BatchRun {
+public:
+    BatchRun(const SolveConfig &cfg, cudaStream_t st);
+    ~BatchRun();
+    int stage(const BatchMember &m);
+    int commit();
+    int cycle(bool use_graph, std::vector<int> &live);
+    int finish(const std::vector<int> &idx, std::vector<SysState> &out);
+    void remove(std::vector<int> idx);
+    size_t size() const { return mem.size(); }
+    const BatchMember &member(size_t i) const { return mem[i]; }
+    SolveConfig cfg;
+    cudaStream_t st;
+private:
+    std::vector<BatchMember> mem;
+    std::vector<SysDev> hs;
+    std::unique_ptr<Plan> P;
+    int pending = 0;
+    cudaGraphExec_t exec = nullptr;
+    int graph_nodes = 0;
+    int *h_live = nullptr;
+    size_t live_cap = 0;
+};
+
+int validate_member(fg_system *s, const SolveConfig &cfg);
+size_t workspace_bytes(const fg_system *s, int kmax, int mixed);
+void fill_stats(const SysState &s, double secs, fg_solve_stats &o);
+
 // Solve every member; stats[i] receives the result of member i.
 int solve_batch(std::vector<BatchMember> &members, const SolveConfig &cfg,
                 fg_solve_stats *stats, cudaStream_t stream);

@@ -62,6 +62,20 @@ class ProcessStats(ctypes.Structure):
                 ("true_rel_residual", _c_dbl)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("kmax", _c_int), ("lmax", _c_int), ("tol", _c_dbl), ("precision", _c_int),
+                ("inner_tol", _c_dbl), ("hbm_budget_bytes", ctypes.c_size_t), ("max_active", _c_int)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("tag", ctypes.c_ulonglong), ("stats", SolveStats), ("t_submit", _c_dbl), ("t_admit", _c_dbl),
+                ("t_done", _c_dbl)]
+
+    def as_dict(self):
+        return {"tag": self.tag, **self.stats.as_dict(), "t_submit": self.t_submit, "t_admit": self.t_admit,
+                "t_done": self.t_done}
+
+
 _lib = None
 
 
@@ -109,6 +123,13 @@ def lib(build_if_missing: bool = True):
     L.fg_transport_prepare.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), _vp]
     L.fg_transport_process.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), ctypes.POINTER(SolverOpts), _c_dbl,
                                        _c_int, _f64p, ctypes.POINTER(ProcessStats)]
+    L.fg_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerOpts)]
+    L.fg_server_submit.argtypes = [_vp, _vp, ctypes.POINTER(TransportCoeffs), ctypes.c_ulonglong]
+    L.fg_server_poll.argtypes = [_vp, _vp, _c_int, ctypes.POINTER(_c_int)]
+    L.fg_server_wait.argtypes = [_vp, _c_int, _c_dbl]
+    L.fg_server_now.argtypes = [_vp]
+    L.fg_server_now.restype = _c_dbl
+    L.fg_server_destroy.argtypes = [_vp]
     _lib = L
     return L
 
@@ -320,6 +341,50 @@ def bench_matvec(systems, precision=32, reps=20):
     ms, b = _c_dbl(), _c_dbl()
     check(lib().fg_bench_matvec(ctypes.cast(H, _vp), n, precision, reps, ctypes.byref(ms), ctypes.byref(b)))
     return ms.value, b.value
+
+
+class Server:
+    """Continuous-batching request server (fg_server_*): submit transport
+    requests at any time, poll finished results with their timestamps."""
+
+    def __init__(self, kmax=30, lmax=10000, tol=1e-10, precision=FG_PREC_MIXED, inner_tol=0.0,
+                 hbm_budget_bytes=0, max_active=0):
+        h = _vp()
+        o = ServerOpts(kmax, lmax, tol, precision, inner_tol, hbm_budget_bytes, max_active)
+        check(lib().fg_server_create(ctypes.byref(h), ctypes.byref(o)))
+        self._h = h
+        self._keep = {}
+
+    def submit(self, system, prob, tag):
+        c = _coeffs(prob)
+        self._keep[tag] = system
+        check(lib().fg_server_submit(self._h, system.handle, ctypes.byref(c), tag))
+
+    def now(self) -> float:
+        return float(lib().fg_server_now(self._h))
+
+    def wait(self, n, timeout=60.0):
+        check(lib().fg_server_wait(self._h, n, timeout))
+
+    def poll(self, max_results=4096):
+        buf = (ServerResult * max_results)()
+        cnt = _c_int(0)
+        check(lib().fg_server_poll(self._h, ctypes.cast(buf, _vp), max_results, ctypes.byref(cnt)))
+        out = [buf[i].as_dict() for i in range(cnt.value)]
+        for r in out:
+            self._keep.pop(r["tag"], None)
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().fg_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def transport_system(prob, reorder=True) -> System:
