@@ -101,7 +101,7 @@ int fg_matvec(fg_system *s, const double *P, double *Q, int precision);
  * implicit synchronisation).  The scratch it needs comes from one fixed
  * array of about 33 MiB compiled into the library and held on every GPU
  * that loads it; systems with more than 2,097,151 equations or more than
- * 65,536 colour chunks of 1024 elements are rejected with FG_ERR_ARG.
+ * 65,536 element patches of 1024 elements are rejected with FG_ERR_ARG.
  * The first call on a device looks up the array's device address, so make
  * that first call before starting any stream capture.  The work is queued
  * on the system's stream (fg_system_stream) and the call returns without

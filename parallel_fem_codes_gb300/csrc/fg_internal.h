@@ -41,7 +41,21 @@ struct Topology {
     // node incidence (entries pos*4 + vertex), ordered by reference element
     std::vector<int> ninc_ptr, ninc;
     std::vector<int> node_dof;   // nnodes*ndof: internal dof or n (sink)
+    // patch layout of the matvec: the elements with a free dof, in internal
+    // order, cut into patches of at most kPatchElems; inside a patch the
+    // elements are grouped by a local colouring
+    int npatch = 0, npcol = 0, maxdof = 0, nel_active = 0;
+    std::vector<int> pt_elem;    // npatch+1 element offsets (internal positions)
+    std::vector<int> pt_dof;     // npatch+1 offsets into dofs
+    std::vector<unsigned short> pt_col;  // npatch * kPatchColStride local colour offsets
+    std::vector<int> dofs;       // patch-local dof -> internal dof, bit 31 = shared with another patch
+    std::vector<unsigned short> lm16;    // nel*S local indices (internal order), 0xFFFF = sink
+    std::vector<int> pc_ptr, pc_list;    // patches grouped by patch colour
 };
+
+constexpr int kPatchElems = 1024;      // elements per matvec patch
+constexpr int kPatchMaxLocalColours = 16;
+constexpr int kPatchColStride = kPatchMaxLocalColours + 1;
 
 int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
                    const int *type, const int *invp, int neq, int reorder);
@@ -76,6 +90,10 @@ struct SysDev {
     int kmax, lmax, mixed, precond;
     double tol, inner_tol;
     const int *lm;             // [S][nel_pad] internal dofs
+    const unsigned short *lm16;// [S][nel_pad] patch-local indices (0xFFFF = sink)
+    const int *pt_elem, *pt_dof, *dofs;
+    const unsigned short *pt_col;
+    int maxdof;
     const double *A64;         // [S*S][nel_pad]
     const float *A32;
     const double *invd64;      // n_pad

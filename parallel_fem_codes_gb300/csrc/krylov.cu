@@ -11,7 +11,8 @@
 // reductions.
 //
 // Work decomposition.  A batch holds any number of systems.  Element work
-// is cut into chunks per colour, dof work into parts per system; every
+// is cut into patches (grouped by patch colour), dof work into parts per
+// system; every
 // kernel walks its chunk table with a grid-stride loop and skips systems
 // that are not active.  A system's partial sums depend only on its own
 // parts, so a result is bit-identical whether the system is solved alone
@@ -85,11 +86,17 @@ __device__ __forceinline__ void reduce_parts(const SysDev &D, int nv, double *ou
 }
 
 // ---------------------------------------------------------------- EBE matvec
-// y[lm] += A_e x[lm] for the elements of one colour.  A and lm are SoA
-// ([entry][element]), so lane-consecutive elements read consecutive
-// addresses; x gathers and y updates hit L2.  Elements of one colour share
-// no free dof, so the scatter needs no atomics and the summation order is
-// fixed (colour by colour).  The sink (index n) is never written.
+// y[lm] += A_e x[lm] by patches.  A patch is up to kPatchElems consecutive
+// elements (internal order: sorted by their smallest dof, so a patch covers
+// a compact band of dofs).  One CTA per patch: it gathers the patch's x
+// entries into shared memory, accumulates the element rows into a
+// shared-memory y local colour by local colour (elements of one local
+// colour share no dof, so no atomics and a fixed summation order), and
+// writes each dof once: a plain store for dofs only this patch touches, an
+// update for dofs shared with other patches.  Patches that share a dof have
+// different patch colours and run in different launches, so the updates do
+// not race.  A and lm16 are SoA ([entry][element]); lane-consecutive
+// elements read consecutive addresses.  The sink (index n) is never written.
 // in_sel: 0 = x (FP64), 1 = V[step] (T), 2 = aux (TX); out_sel: 0 = t64,
 // 1 = t, 2 = aux.
 template <int S, typename TA, typename TX, typename TY>
@@ -97,6 +104,12 @@ __global__ void __launch_bounds__(kThreads)
 k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const int *__restrict__ nch,
          int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out)
 {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr unsigned short kSink = 0xFFFF;
+    // S = 3: every thread preloads its (up to) kPatchElems / kThreads
+    // elements' blocks before the colour passes, so a whole patch of loads
+    // is in flight at once; larger blocks are loaded inside the passes.
+    constexpr int E = S == 3 ? kPatchElems / kThreads : 1;
     const int total = *nch;
     for (int c = blockIdx.x; c < total; c += gridDim.x) {
         const EChunk k = ch[c];
@@ -107,57 +120,75 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
-        const int n = D.n;
+        TA *xs = reinterpret_cast<TA *>(smem_raw);
+        TA *ys = xs + D.maxdof;
+        const int p = k.e0;
+        const int pe0 = D.pt_elem[p], pne = D.pt_elem[p + 1] - pe0;
+        const int pd0 = D.pt_dof[p], pnd = D.pt_dof[p + 1] - pd0;
+        const unsigned short *pc = D.pt_col + (size_t)p * kPatchColStride;
+
+        TA av[E][S == 3 ? 9 : 1];
+        unsigned short li[E][S == 3 ? 3 : 1];
         if constexpr (S == 3) {
-            // 3x3 blocks: lanes take consecutive elements (their dofs are
-            // neighbours, so gathers and updates share cache sectors) and each
-            // thread keeps two elements' loads in flight before the first
-            // gather.
-            constexpr int U = 2;
-            const int stride = blockDim.x * U;
-            for (int e0 = k.e0 + threadIdx.x; e0 < k.e1; e0 += stride) {
-                int idx[U][3];
-                TA av[U][9], xv[U][3];
 #pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    const int e = min(e0 + u * (int)blockDim.x, k.e1 - 1);
+            for (int u = 0; u < E; ++u) {
+                const int q = min(threadIdx.x + u * kThreads, pne - 1);
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) idx[u][a] = __ldcs(D.lm + a * ld + e);
+                for (int a = 0; a < 3; ++a) li[u][a] = __ldcs(D.lm16 + a * ld + pe0 + q);
 #pragma unroll
-                    for (int m = 0; m < 9; ++m) av[u][m] = ldst(A + m * ld + e);
-                }
+                for (int m = 0; m < 9; ++m) av[u][m] = ldst(A + m * ld + pe0 + q);
+            }
+        }
+        __syncthreads();                      // the previous patch is done with xs / ys
+        for (int j = threadIdx.x; j < pnd; j += blockDim.x) {
+            xs[j] = (TA)X[D.dofs[pd0 + j] & 0x7fffffff];
+            ys[j] = (TA)0;
+        }
+        __syncthreads();
+        for (int col = 0; col < kPatchMaxLocalColours; ++col) {
+            const int cs = pc[col], ce = pc[col + 1];
+            if (cs >= ce) break;
+            if constexpr (S == 3) {
 #pragma unroll
-                for (int u = 0; u < U; ++u)
+                for (int u = 0; u < E; ++u) {
+                    const int q = threadIdx.x + u * kThreads;
+                    if (q < cs || q >= ce) continue;
+                    TA xv[3];
 #pragma unroll
-                    for (int a = 0; a < 3; ++a) xv[u][a] = (TA)X[idx[u][a]];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    if (e0 + u * (int)blockDim.x >= k.e1) break;
+                    for (int a = 0; a < 3; ++a) xv[a] = li[u][a] == kSink ? (TA)0 : xs[li[u][a]];
 #pragma unroll
                     for (int r = 0; r < 3; ++r) {
-                        TA acc = av[u][3 * r] * xv[u][0];
-                        acc += av[u][3 * r + 1] * xv[u][1];
-                        acc += av[u][3 * r + 2] * xv[u][2];
-                        if (idx[u][r] != n) Y[idx[u][r]] += (TY)acc;
+                        TA acc = av[u][3 * r] * xv[0];
+                        acc += av[u][3 * r + 1] * xv[1];
+                        acc += av[u][3 * r + 2] * xv[2];
+                        if (li[u][r] != kSink) ys[li[u][r]] += acc;
+                    }
+                }
+            } else {
+                for (int q = cs + threadIdx.x; q < ce; q += blockDim.x) {
+                    unsigned short l[S];
+                    TA xv[S];
+#pragma unroll
+                    for (int a = 0; a < S; ++a) {
+                        l[a] = __ldcs(D.lm16 + a * ld + pe0 + q);
+                        xv[a] = l[a] == kSink ? (TA)0 : xs[l[a]];
+                    }
+#pragma unroll
+                    for (int r = 0; r < S; ++r) {
+                        TA acc = ldst(A + (size_t)(r * S) * ld + pe0 + q) * xv[0];
+#pragma unroll
+                        for (int m = 1; m < S; ++m) acc += ldst(A + (size_t)(r * S + m) * ld + pe0 + q) * xv[m];
+                        if (l[r] != kSink) ys[l[r]] += acc;
                     }
                 }
             }
-        } else {
-            for (int e = k.e0 + threadIdx.x; e < k.e1; e += blockDim.x) {
-                int idx[S];
-                TA xv[S];
-#pragma unroll
-                for (int a = 0; a < S; ++a) idx[a] = __ldcs(D.lm + a * ld + e);
-#pragma unroll
-                for (int a = 0; a < S; ++a) xv[a] = (TA)X[idx[a]];
-#pragma unroll
-                for (int r = 0; r < S; ++r) {
-                    TA acc = ldst(A + (size_t)(r * S) * ld + e) * xv[0];
-#pragma unroll
-                    for (int q = 1; q < S; ++q) acc += ldst(A + (size_t)(r * S + q) * ld + e) * xv[q];
-                    if (idx[r] != n) Y[idx[r]] += (TY)acc;
-                }
-            }
+            __syncthreads();
+        }
+        for (int j = threadIdx.x; j < pnd; j += blockDim.x) {
+            const int dd = D.dofs[pd0 + j];
+            const int d = dd & 0x7fffffff;
+            if (dd < 0) Y[d] += (TY)ys[j];
+            else Y[d] = (TY)ys[j];
         }
     }
 }
@@ -369,16 +400,25 @@ int sm_count()
 namespace {
 
 struct MvLaunch {
+    // smem: bytes of dynamic shared memory (2 * max patch dofs * sizeof(TA))
     template <typename TA, typename TX, typename TY>
     static void go(int S, dim3 g, cudaStream_t st, const SysDev *sys, const EChunk *ch, const int *nch,
-                   int gate, int in_sel, int out_sel, int step, const TX *ai, TY *ao)
+                   int gate, int in_sel, int out_sel, int step, const TX *ai, TY *ao, size_t smem)
     {
         switch (S) {
-        case 3: k_ebe_mv<3, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao); break;
-        case 6: k_ebe_mv<6, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao); break;
-        case 9: k_ebe_mv<9, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao); break;
-        case 12: k_ebe_mv<12, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao); break;
+        case 3: run<3, TA, TX, TY>(g, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, smem); break;
+        case 6: run<6, TA, TX, TY>(g, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, smem); break;
+        case 9: run<9, TA, TX, TY>(g, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, smem); break;
+        case 12: run<12, TA, TX, TY>(g, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, smem); break;
         }
+    }
+    template <int S, typename TA, typename TX, typename TY>
+    static void run(dim3 g, cudaStream_t st, const SysDev *sys, const EChunk *ch, const int *nch, int gate,
+                    int in_sel, int out_sel, int step, const TX *ai, TY *ao, size_t smem)
+    {
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_ebe_mv<S, TA, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_ebe_mv<S, TA, TX, TY><<<g, kThreads, smem, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao);
     }
 };
 
@@ -399,12 +439,6 @@ inline dim3 grid_for(int nchunks)
     return dim3((unsigned)std::max(1, std::min(nchunks, cap)));
 }
 
-int elem_chunk(int cnt)
-{
-    int per = cnt / (256 * 2 * sm_count());
-    return 256 * std::max(1, std::min(8, per));
-}
-
 int parts_for(int n)
 {
     int p = (n + kPartMin - 1) / kPartMin;
@@ -415,7 +449,8 @@ int parts_for(int n)
 
 // Chunk tables of one batch (device copies + host counts).
 struct Plan {
-    int nsys = 0, ncol = 0, S = 3, B = 1;
+    int nsys = 0, ncol = 0, S = 3, B = 1, maxdof = 1;   // ncol: patch colours
+    size_t smem(int w) const { return 2 * (size_t)maxdof * w; }
     std::vector<int> ech_off;      // ncol+1 offsets into echunks
     int n_dch = 0, n_nch = 0;
     DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
@@ -428,19 +463,20 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     P.S = mem[0].s->topo.S;
     P.B = mem[0].s->topo.ndof;
     P.ncol = 0;
+    P.maxdof = 1;
     for (auto &m : mem) {
         if (m.s->topo.S != P.S) { set_error("a batch must hold systems of one block size"); return FG_ERR_ARG; }
-        P.ncol = std::max(P.ncol, m.s->topo.ncol);
+        P.ncol = std::max(P.ncol, m.s->topo.npcol);
+        P.maxdof = std::max(P.maxdof, m.s->topo.maxdof);
     }
+    // matvec work items: one per patch, grouped by patch colour
     std::vector<EChunk> ech;
     P.ech_off.assign(P.ncol + 1, 0);
     for (int c = 0; c < P.ncol; ++c) {
         for (int s = 0; s < P.nsys; ++s) {
             const Topology &t = mem[s].s->topo;
-            if (c >= t.ncol) continue;
-            int e0 = t.cptr[c], e1 = t.cptr[c + 1];
-            int cs = elem_chunk(e1 - e0);
-            for (int e = e0; e < e1; e += cs) ech.push_back({s, e, std::min(e + cs, e1)});
+            if (c >= t.npcol) continue;
+            for (int q = t.pc_ptr[c]; q < t.pc_ptr[c + 1]; ++q) ech.push_back({s, t.pc_list[q], 0});
         }
         P.ech_off[c + 1] = (int)ech.size();
     }
@@ -498,9 +534,11 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
         const EChunk *ch = P.echunks.as<EChunk>() + P.ech_off[c];
         const int *nc = P.ecount.as<int>() + c;
         if (mode == 0)
-            MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, ch, nc, 0, 0, 0, 0, nullptr, nullptr);
+            MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, ch, nc, 0, 0, 0, 0, nullptr, nullptr,
+                                                 P.smem(8));
         else
-            MvLaunch::go<T, T, T>(P.S, grid_for(cnt), st, sys, ch, nc, mode == 2 ? -1 : 1, 1, 1, step, nullptr, nullptr);
+            MvLaunch::go<T, T, T>(P.S, grid_for(cnt), st, sys, ch, nc, mode == 2 ? -1 : 1, 1, 1, step, nullptr,
+                                  nullptr, P.smem(sizeof(T)));
         ++k;
     }
     return k;
@@ -565,6 +603,7 @@ static SysDev make_desc(fg_system *s, const SolveConfig &cfg, bool has_f)
     D.kmax = cfg.kmax; D.lmax = cfg.lmax; D.mixed = cfg.mixed; D.precond = cfg.precond;
     D.tol = cfg.tol; D.inner_tol = cfg.inner_tol;
     D.lm = s->lm.as<int>(); D.A64 = s->A64.as<double>(); D.A32 = s->A32.as<float>();
+    set_patch_fields(D, s);
     D.invd64 = s->invd64.as<double>(); D.invd32 = s->invd32.as<float>();
     D.node_dof = s->node_dof.as<int>(); D.ibd64 = s->ibd64.as<double>(); D.ibd32 = s->ibd32.as<float>();
     D.x = w.x.as<double>(); D.b = w.b.as<double>(); D.ftrue = has_f ? w.ftrue.as<double>() : nullptr;
@@ -717,7 +756,7 @@ int BatchRun::finish(const std::vector<int> &idx, std::vector<SysState> &out)
         int cnt = F.ech_off[c + 1] - F.ech_off[c];
         if (!cnt) continue;
         MvLaunch::go<double, double, double>(F.S, grid_for(cnt), st, sys, F.echunks.as<EChunk>() + F.ech_off[c],
-                                             F.ecount.as<int>() + c, -1, 0, 0, 0, nullptr, nullptr);
+                                             F.ecount.as<int>() + c, -1, 0, 0, 0, nullptr, nullptr, F.smem(8));
         count_launches(1);
     }
     k_final<<<grid_for(F.n_dch), kThreads, 0, st>>>(sys, F.dchunks.as<DChunk>(), F.dcount.as<int>());
@@ -804,34 +843,35 @@ int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaS
     SysDev D{};
     D.n = t.n; D.n_pad = s->n_pad; D.nel = t.nel; D.nel_pad = s->nel_pad; D.S = t.S;
     D.lm = s->lm.as<int>(); D.A64 = s->A64.as<double>(); D.A32 = s->A32.as<float>();
+    set_patch_fields(D, s);
     DevMem sd, ch, cnt;
     std::vector<EChunk> ech;
-    std::vector<int> off(t.ncol + 1, 0), counts(t.ncol);
-    for (int c = 0; c < t.ncol; ++c) {
-        int e0 = t.cptr[c], e1 = t.cptr[c + 1], cs = elem_chunk(e1 - e0);
-        for (int e = e0; e < e1; e += cs) ech.push_back({0, e, std::min(e + cs, e1)});
+    std::vector<int> off(t.npcol + 1, 0), counts(t.npcol);
+    for (int c = 0; c < t.npcol; ++c) {
+        for (int q = t.pc_ptr[c]; q < t.pc_ptr[c + 1]; ++q) ech.push_back({0, t.pc_list[q], 0});
         off[c + 1] = (int)ech.size();
         counts[c] = off[c + 1] - off[c];
     }
     int r;
     if ((r = sd.alloc(sizeof(SysDev))) || (r = ch.alloc(sizeof(EChunk) * std::max<size_t>(1, ech.size()))) ||
-        (r = cnt.alloc(sizeof(int) * std::max(1, t.ncol))))
+        (r = cnt.alloc(sizeof(int) * std::max(1, t.npcol))))
         return r;
     FG_CUDA(cudaMemcpyAsync(sd.p, &D, sizeof(SysDev), cudaMemcpyHostToDevice, st));
     if (!ech.empty()) FG_CUDA(cudaMemcpyAsync(ch.p, ech.data(), sizeof(EChunk) * ech.size(), cudaMemcpyHostToDevice, st));
-    if (t.ncol) FG_CUDA(cudaMemcpyAsync(cnt.p, counts.data(), sizeof(int) * t.ncol, cudaMemcpyHostToDevice, st));
+    if (t.npcol) FG_CUDA(cudaMemcpyAsync(cnt.p, counts.data(), sizeof(int) * t.npcol, cudaMemcpyHostToDevice, st));
     FG_CUDA(cudaMemsetAsync(y, 0, 8 * (size_t)(t.n + 1), st));
-    for (int c = 0; c < t.ncol; ++c) {
+    const size_t smem = 2 * (size_t)D.maxdof * (precision == 32 ? 4 : 8);
+    for (int c = 0; c < t.npcol; ++c) {
         if (!counts[c]) continue;
         const EChunk *cp = ch.as<EChunk>() + off[c];
         const int *np = cnt.as<int>() + c;
         if (precision == 32)
-            MvLaunch::go<float, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y);
+            MvLaunch::go<float, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y, smem);
         else
-            MvLaunch::go<double, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y);
+            MvLaunch::go<double, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y, smem);
     }
     FG_CUDA(cudaGetLastError());
-    count_launches(t.ncol);
+    count_launches(t.npcol);
     FG_CUDA(cudaStreamSynchronize(st));
     return FG_OK;
 }
@@ -890,17 +930,18 @@ int bench_matvec(std::vector<fg_system *> &systems, int precision, int reps, dou
 // Colour-by-colour matvec y += A x from a caller-placed descriptor and chunk
 // table (device memory the caller owns); used by fg_matvec_noalloc.
 int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const EChunk *ch_dev, const int *counts_dev,
-                          const int *off_host, int ncol, const double *x, double *y, cudaStream_t st)
+                          const int *off_host, int ncol, int maxdof, const double *x, double *y, cudaStream_t st)
 {
+    const size_t smem = 2 * (size_t)std::max(1, maxdof) * (precision == 32 ? 4 : 8);
     for (int c = 0; c < ncol; ++c) {
         int cnt = off_host[c + 1] - off_host[c];
         if (!cnt) continue;
         const EChunk *cp = ch_dev + off_host[c];
         const int *np = counts_dev + c;
         if (precision == 32)
-            MvLaunch::go<float, double, double>(S, grid_for(cnt), st, sys_dev, cp, np, -1, 2, 2, 0, x, y);
+            MvLaunch::go<float, double, double>(S, grid_for(cnt), st, sys_dev, cp, np, -1, 2, 2, 0, x, y, smem);
         else
-            MvLaunch::go<double, double, double>(S, grid_for(cnt), st, sys_dev, cp, np, -1, 2, 2, 0, x, y);
+            MvLaunch::go<double, double, double>(S, grid_for(cnt), st, sys_dev, cp, np, -1, 2, 2, 0, x, y, smem);
         count_launches(1);
     }
     FG_CUDA(cudaGetLastError());

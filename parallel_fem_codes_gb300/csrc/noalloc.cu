@@ -11,11 +11,11 @@
 //
 // Scratch.  g_noalloc_scratch is a file-scope __device__ array of
 // kNoAllocBytes (about 33 MiB).  Every GPU that loads this library holds it
-// until the process exits.  It stores the system descriptor, the colour
-// chunk table and two renumbering vectors of at most kNoAllocMaxEq entries,
+// until the process exits.  It stores the system descriptor, the matvec
+// work-item table and two renumbering vectors of at most kNoAllocMaxEq entries,
 // so the entry point accepts systems with n + 1 <= kNoAllocMaxEq equations
-// (including the Dirichlet sink) and at most kNoAllocMaxChunks colour
-// chunks, and rejects larger ones with FG_ERR_ARG.
+// (including the Dirichlet sink) and at most kNoAllocMaxChunks element
+// patches of kPatchElems elements, and rejects larger ones with FG_ERR_ARG.
 //
 // Host code cannot use the array's name as a device address (in host code
 // it names a host-side stand-in): the device address is looked up once per
@@ -35,8 +35,7 @@
 namespace fg {
 
 constexpr int kNoAllocMaxEq = 1 << 21;       // n + 1 <= 2,097,152
-constexpr int kNoAllocMaxChunks = 1 << 16;   // colour chunks per system
-constexpr int kNoAllocChunk = 1024;          // elements per chunk
+constexpr int kNoAllocMaxChunks = 1 << 16;   // element patches (matvec work items) per system
 constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 constexpr size_t kOffDesc = 0;
 constexpr size_t kOffCounts = align256(sizeof(SysDev));
@@ -105,19 +104,17 @@ extern "C" int fg_matvec_noalloc(fg_system *s, const double *P_dev, double *Q_de
     FG_CUDA(cudaGetDevice(&dev));
     if (dev != s->device) { set_error("fg_matvec_noalloc: the system's device is not the current device"); return FG_ERR_ARG; }
 
-    // colour chunk table on the host
+    // matvec work items (one per patch of elements, grouped by patch colour)
     int off[kMaxColours + 1] = {0};
     int counts[kMaxColours] = {0};
     int nch = 0;
-    for (int c = 0; c < t.ncol; ++c) {
-        for (int e = t.cptr[c]; e < t.cptr[c + 1]; e += kNoAllocChunk) {
-            if (nch >= kNoAllocMaxChunks) {
-                set_error("fg_matvec_noalloc: system needs more than " + std::to_string(kNoAllocMaxChunks) +
-                          " colour chunks, the fixed scratch holds no more");
-                return FG_ERR_ARG;
-            }
-            t_chunks[nch++] = {0, e, std::min(e + kNoAllocChunk, t.cptr[c + 1])};
-        }
+    if (t.npatch > kNoAllocMaxChunks || t.npcol > kMaxColours) {
+        set_error("fg_matvec_noalloc: system has more than " + std::to_string(kNoAllocMaxChunks) +
+                  " element patches, the fixed scratch holds no more");
+        return FG_ERR_ARG;
+    }
+    for (int c = 0; c < t.npcol; ++c) {
+        for (int q = t.pc_ptr[c]; q < t.pc_ptr[c + 1]; ++q) t_chunks[nch++] = {0, t.pc_list[q], 0};
         off[c + 1] = nch;
         counts[c] = off[c + 1] - off[c];
     }
@@ -128,6 +125,7 @@ extern "C" int fg_matvec_noalloc(fg_system *s, const double *P_dev, double *Q_de
     SysDev D{};
     D.n = t.n; D.n_pad = s->n_pad; D.nel = t.nel; D.nel_pad = s->nel_pad; D.S = t.S;
     D.lm = s->lm.as<int>(); D.A64 = s->A64.as<double>(); D.A32 = s->A32.as<float>();
+    set_patch_fields(D, s);
     SysDev *d_desc = reinterpret_cast<SysDev *>(base + kOffDesc);
     int *d_counts = reinterpret_cast<int *>(base + kOffCounts);
     EChunk *d_chunks = reinterpret_cast<EChunk *>(base + kOffChunks);
@@ -135,13 +133,14 @@ extern "C" int fg_matvec_noalloc(fg_system *s, const double *P_dev, double *Q_de
     double *d_y = reinterpret_cast<double *>(base + kOffY);
     cudaStream_t st = s->stream;
     FG_CUDA(cudaMemcpyAsync(d_desc, &D, sizeof(SysDev), cudaMemcpyHostToDevice, st));
-    if (t.ncol) FG_CUDA(cudaMemcpyAsync(d_counts, counts, sizeof(int) * t.ncol, cudaMemcpyHostToDevice, st));
+    if (t.npcol) FG_CUDA(cudaMemcpyAsync(d_counts, counts, sizeof(int) * t.npcol, cudaMemcpyHostToDevice, st));
     if (nch) FG_CUDA(cudaMemcpyAsync(d_chunks, t_chunks, sizeof(EChunk) * nch, cudaMemcpyHostToDevice, st));
     // x (reference numbering) -> internal numbering; y starts at zero
     k_na_gather<<<(t.n + 256) / 256, 256, 0, st>>>(s->perm.as<int>(), P_dev, d_x, t.n);
     FG_CUDA(cudaGetLastError());
     FG_CUDA(cudaMemsetAsync(d_y, 0, sizeof(double) * (size_t)(t.n + 1), st));
-    if ((r = launch_matvec_colours(t.S, precision, d_desc, d_chunks, d_counts, off, t.ncol, d_x, d_y, st))) return r;
+    if ((r = launch_matvec_colours(t.S, precision, d_desc, d_chunks, d_counts, off, t.npcol, t.maxdof, d_x, d_y, st)))
+        return r;
     k_na_scatter<<<(t.n + 256) / 256, 256, 0, st>>>(s->perm.as<int>(), d_y, Q_dev, t.n);
     FG_CUDA(cudaGetLastError());
     count_launches(2);

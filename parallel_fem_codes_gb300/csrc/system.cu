@@ -64,6 +64,7 @@ fg_system::~fg_system()
 size_t fg_system::bytes() const
 {
     const DevMem *all[] = {&lm, &A64, &A32, &dinc_ptr, &dinc, &ninc_ptr, &ninc, &node_dof, &eorder, &perm,
+                           &lm16, &pt_elem, &pt_dof, &pt_col, &pdofs, &rhs_f, &rhs_b,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
                            &ginvp, &Fe, &F64, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
                            &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
@@ -120,6 +121,14 @@ int fg_system_create(fg_system **out, int nnodes, int nel, int ndof, const int *
     for (int p = 0; p < t.nel; ++p)
         for (int v = 0; v < 3; ++v) gien[(size_t)v * s->nel_pad + p] = t.ien[3 * (size_t)t.eorder[p] + v];
     std::vector<int> perm(t.perm.begin(), t.perm.end());
+    std::vector<unsigned short> lm16((size_t)S * s->nel_pad, (unsigned short)0xFFFF);
+    for (int p = 0; p < t.nel; ++p)
+        for (int a = 0; a < S; ++a) lm16[(size_t)a * s->nel_pad + p] = t.lm16[(size_t)p * S + a];
+    if ((r = upload(s->lm16, lm16)) || (r = upload(s->pt_elem, t.pt_elem)) || (r = upload(s->pt_dof, t.pt_dof)) ||
+        (r = upload(s->pt_col, t.pt_col)) || (r = upload(s->pdofs, t.dofs))) {
+        delete s;
+        return r;
+    }
     size_t SS = (size_t)S * S * s->nel_pad;
     if ((r = upload(s->lm, lm_soa)) || (r = upload(s->dinc_ptr, t.dinc_ptr)) || (r = upload(s->dinc, t.dinc)) ||
         (r = upload(s->ninc_ptr, t.ninc_ptr)) || (r = upload(s->ninc, t.ninc)) ||

@@ -36,6 +36,7 @@ struct fg_system {
     // connectivity and blocks, internal numbering / element order, SoA
     fg::DevMem lm, A64, A32;
     fg::DevMem dinc_ptr, dinc, ninc_ptr, ninc, node_dof, eorder, perm;
+    fg::DevMem lm16, pt_elem, pt_dof, pt_col, pdofs;   // matvec patch layout
     // preconditioners
     fg::DevMem diag, invd64, invd32, bd, ibd64, ibd32;
     int precond = FG_PRECOND_NONE;
@@ -54,6 +55,17 @@ struct fg_system {
 };
 
 namespace fg {
+
+// Patch-layout pointers of a system's descriptor (matvec).
+inline void set_patch_fields(SysDev &D, const fg_system *s)
+{
+    D.lm16 = s->lm16.as<unsigned short>();
+    D.pt_elem = s->pt_elem.as<int>();
+    D.pt_dof = s->pt_dof.as<int>();
+    D.pt_col = s->pt_col.as<unsigned short>();
+    D.dofs = s->pdofs.as<int>();
+    D.maxdof = std::max(1, s->topo.maxdof);
+}
 
 // A set of systems solved together: one graph launch per restart cycle
 // advances every live member; members stop independently.
@@ -112,7 +124,7 @@ int solve_batch(std::vector<BatchMember> &members, const SolveConfig &cfg,
 
 int bench_matvec(std::vector<fg_system *> &systems, int precision, int reps, double *ms, double *bytes);
 int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const EChunk *ch_dev, const int *counts_dev,
-                          const int *off_host, int ncol, const double *x, double *y, cudaStream_t st);
+                          const int *off_host, int ncol, int maxdof, const double *x, double *y, cudaStream_t st);
 
 // Matvec on device vectors in internal numbering (precision 64 or 32).
 int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaStream_t st);

@@ -282,29 +282,127 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
             if (r != n) used[r] |= 1ull << c;
         }
     }
-    // internal element order: by colour, then by the smallest internal dof
-    // (gather locality), then by reference index; elements without a free
-    // dof go last and are skipped by the matvec
+    // internal element order (the patch layout of the matvec): elements with
+    // a free dof sorted by their smallest internal dof (stable), cut into
+    // patches of kPatchElems consecutive elements; inside each patch the
+    // elements are grouped by a greedy local colouring so that the patch's
+    // shared-memory accumulation needs no atomics.  Elements without a free
+    // dof go last and are skipped by the matvec.
     std::vector<int> key(nel);
     for (int e = 0; e < nel; ++e) {
         int m = n;
         for (int a = 0; a < S; ++a) m = std::min(m, t.iperm[t.lm[(size_t)e * S + a]]);
         key[e] = m;
     }
-    t.eorder.resize(nel);
-    std::iota(t.eorder.begin(), t.eorder.end(), 0);
-    std::stable_sort(t.eorder.begin(), t.eorder.end(), [&](int a, int b) {
-        int ca = t.colour[a] < 0 ? 1 << 30 : t.colour[a];
-        int cb = t.colour[b] < 0 ? 1 << 30 : t.colour[b];
-        if (ca != cb) return ca < cb;
-        return key[a] < key[b];
+    std::vector<int> sorted(nel);
+    std::iota(sorted.begin(), sorted.end(), 0);
+    std::stable_sort(sorted.begin(), sorted.end(), [&](int a, int b) {
+        int ka = has_free[a] ? key[a] : n + 1, kb = has_free[b] ? key[b] : n + 1;
+        return ka < kb;
     });
+    int nact = 0;
+    for (int e = 0; e < nel; ++e) nact += has_free[e] ? 1 : 0;
+    t.nel_active = nact;
+    t.npatch = (nact + kPatchElems - 1) / kPatchElems;
+    t.eorder.resize(nel);
+    t.pt_elem.assign(t.npatch + 1, 0);
+    t.pt_dof.assign(t.npatch + 1, 0);
+    t.pt_col.assign((size_t)t.npatch * kPatchColStride, 0);
+    t.dofs.clear();
+    t.maxdof = 0;
+    std::vector<int> local(n + 1, -1), owner_count(n + 1, 0);
+    std::vector<uint32_t> lmask;   // per local dof: local colours used
+    for (int p = 0; p < t.npatch; ++p) {
+        const int b = p * kPatchElems, e = std::min(nact, b + kPatchElems);
+        t.pt_elem[p] = b;
+        // local dofs of the patch, ascending internal index
+        std::vector<int> pd;
+        for (int q = b; q < e; ++q)
+            for (int a = 0; a < S; ++a) {
+                int r = t.lm[(size_t)sorted[q] * S + a];
+                if (r != n && local[t.iperm[r]] < 0) { local[t.iperm[r]] = 0; pd.push_back(t.iperm[r]); }
+            }
+        std::sort(pd.begin(), pd.end());
+        for (size_t j = 0; j < pd.size(); ++j) { local[pd[j]] = (int)j; owner_count[pd[j]]++; }
+        // greedy local colouring in patch order
+        lmask.assign(pd.size(), 0u);
+        std::vector<int> lcol(e - b);
+        int ncl = 0;
+        for (int q = b; q < e; ++q) {
+            uint32_t forb = 0;
+            for (int a = 0; a < S; ++a) {
+                int r = t.lm[(size_t)sorted[q] * S + a];
+                if (r != n) forb |= lmask[local[t.iperm[r]]];
+            }
+            if ((forb & 0xFFFFu) == 0xFFFFu) {
+                set_error("patch colouring needs more than 16 local colours"); return FG_ERR_UNSUPPORTED;
+            }
+            int c = __builtin_ctz(~forb);
+            lcol[q - b] = c;
+            ncl = std::max(ncl, c + 1);
+            for (int a = 0; a < S; ++a) {
+                int r = t.lm[(size_t)sorted[q] * S + a];
+                if (r != n) lmask[local[t.iperm[r]]] |= 1u << c;
+            }
+        }
+        // elements of the patch grouped by local colour (stable)
+        std::vector<int> idx(e - b);
+        std::iota(idx.begin(), idx.end(), 0);
+        std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return lcol[x] < lcol[y]; });
+        unsigned short *pc = &t.pt_col[(size_t)p * kPatchColStride];
+        for (int c = 0, k = 0; c <= kPatchMaxLocalColours; ++c) {
+            while (k < (int)idx.size() && lcol[idx[k]] < c) ++k;
+            pc[c] = (unsigned short)k;     // first element of local colour c
+        }
+        for (int k = 0; k < (int)idx.size(); ++k) t.eorder[b + k] = sorted[b + idx[k]];
+        t.pt_dof[p] = (int)t.dofs.size();
+        for (int d : pd) t.dofs.push_back(d);
+        t.maxdof = std::max(t.maxdof, (int)pd.size());
+        for (int d : pd) local[d] = -1;
+    }
+    t.pt_elem[t.npatch] = nact;
+    t.pt_dof[t.npatch] = (int)t.dofs.size();
+    for (int q = nact; q < nel; ++q) t.eorder[q] = sorted[q];
+    for (auto &d : t.dofs)
+        if (owner_count[d] > 1) d |= (int)0x80000000u;
     t.epos.resize(nel);
     for (int p = 0; p < nel; ++p) t.epos[t.eorder[p]] = p;
+    // patch-local element maps (internal element order)
+    t.lm16.assign((size_t)nel * S, 0xFFFF);
+    for (int p = 0; p < t.npatch; ++p) {
+        const int b = t.pt_elem[p], e = t.pt_elem[p + 1];
+        for (int j = t.pt_dof[p]; j < t.pt_dof[p + 1]; ++j) local[t.dofs[j] & 0x7fffffff] = j - t.pt_dof[p];
+        for (int q = b; q < e; ++q)
+            for (int a = 0; a < S; ++a) {
+                int r = t.lm[(size_t)t.eorder[q] * S + a];
+                t.lm16[(size_t)q * S + a] = r == n ? (unsigned short)0xFFFF : (unsigned short)local[t.iperm[r]];
+            }
+        for (int j = t.pt_dof[p]; j < t.pt_dof[p + 1]; ++j) local[t.dofs[j] & 0x7fffffff] = -1;
+    }
+    // patch colouring: patches that share a dof get different colours
+    {
+        std::vector<uint32_t> used(n + 1, 0u);
+        std::vector<int> pcol(t.npatch, 0);
+        t.npcol = 0;
+        for (int p = 0; p < t.npatch; ++p) {
+            uint32_t forb = 0;
+            for (int j = t.pt_dof[p]; j < t.pt_dof[p + 1]; ++j)
+                if (t.dofs[j] < 0) forb |= used[t.dofs[j] & 0x7fffffff];
+            if (forb == 0xFFFFFFFFu) { set_error("patch colouring needs more than 32 colours"); return FG_ERR_UNSUPPORTED; }
+            int c = __builtin_ctz(~forb);
+            pcol[p] = c;
+            t.npcol = std::max(t.npcol, c + 1);
+            for (int j = t.pt_dof[p]; j < t.pt_dof[p + 1]; ++j)
+                if (t.dofs[j] < 0) used[t.dofs[j] & 0x7fffffff] |= 1u << c;
+        }
+        t.pc_ptr.assign(t.npcol + 1, 0);
+        for (int p = 0; p < t.npatch; ++p) t.pc_ptr[pcol[p] + 1]++;
+        for (int c = 0; c < t.npcol; ++c) t.pc_ptr[c + 1] += t.pc_ptr[c];
+        t.pc_list.assign(t.npatch, 0);
+        std::vector<int> fill(t.pc_ptr.begin(), t.pc_ptr.end() - 1);
+        for (int p = 0; p < t.npatch; ++p) t.pc_list[fill[pcol[p]]++] = p;
+    }
     t.cptr.assign(t.ncol + 1, 0);
-    for (int e = 0; e < nel; ++e)
-        if (t.colour[e] >= 0) t.cptr[t.colour[e] + 1]++;
-    for (int c = 0; c < t.ncol; ++c) t.cptr[c + 1] += t.cptr[c];
 
     // dof incidence: (pos, local row) per internal dof, reference element order
     t.dinc_ptr.assign(n + 1, 0);
