@@ -13,6 +13,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT, "libfemgpu.so")
+COMPAT_SST = os.path.join(OUT, "libfemgpu_sst.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, extra flags); setup.cu is rounded exactly as written (no FMA
@@ -50,13 +51,19 @@ def build(force: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s, _ in UNITS]
     hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     hdrs.append(os.path.join(os.path.dirname(PKG), "include", "femgpu.h"))
-    if not force and os.path.exists(LIB):
-        t = os.path.getmtime(LIB)
+    srcs += [os.path.join(PKG, "compat", f) for f in os.listdir(os.path.join(PKG, "compat"))]
+    if not force and os.path.exists(LIB) and os.path.exists(COMPAT_SST):
+        t = min(os.path.getmtime(LIB), os.path.getmtime(COMPAT_SST))
         if all(os.path.getmtime(f) < t for f in srcs + hdrs + [__file__]):
             return LIB
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(lambda u: _compile(*u), UNITS))
     subprocess.run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"], check=True)
+    # drop-in shim with the reference's entry-point names (steady transport)
+    cc = os.environ.get("CC", "gcc")
+    subprocess.run([cc, "-O2", "-fPIC", "-shared", "-std=gnu99", "-Wall", "-o", COMPAT_SST,
+                    os.path.join(PKG, "compat", "compat_sst.c"), "-L" + OUT, "-lfemgpu",
+                    "-Wl,-rpath,$ORIGIN"], check=True)
     return LIB
 
 

@@ -1,0 +1,214 @@
+/*
+ * Drop-in shim for the steady-transport driver: the reference's solve-path
+ * entry points, with the reference's names and signatures, running on the
+ * GPU through libfemgpu.  Linking this library instead of
+ * pgmres.c, ebemv.c, Diag_precond.c, EBE/Diag_precond_EBE_setup.c,
+ * NO_precond.c and NO_precond_setup.c leaves every driver file unchanged.
+ *
+ * One rank only (NPROC = 1): neq_bef = 0, NEQ = neq, vectors of NEQ + 1.
+ * The GPU system of a MatrixDataType is created on first use from the
+ * driver's Node/Element arrays and cached in a small table keyed by the
+ * MatrixDataType pointer (the reference's structs have no room for it).
+ *
+ * Errors: the reference prints and stops (mycalloc.c:10-13,
+ * setPreconditioner.c:66-69).  The shim prints the library's message and
+ * calls exit(1) the same way, unless FEMGPU_COMPAT_NO_EXIT is set in the
+ * environment, in which case it returns the non-zero status instead.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "femgpu_ref_sst.h"
+#include "../../include/femgpu.h"
+
+#define FGC_MAX_SYSTEMS 64
+
+static struct {
+    const MatrixDataType *key;
+    fg_system *sys;
+    int nel, neq;
+} g_tab[FGC_MAX_SYSTEMS];
+
+static int fgc_fail(int rc, const char *where)
+{
+    fprintf(stderr, "femgpu (%s): %s\n", where, fg_last_error());
+    if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
+    return rc;
+}
+
+/* GPU system of this driver state (created on first use). */
+static fg_system *fgc_system(ParametersType *P, MatrixDataType *M, FemStructsType *S)
+{
+    int i, free_slot = -1;
+    for (i = 0; i < FGC_MAX_SYSTEMS; i++) {
+        if (g_tab[i].key == M && g_tab[i].nel == P->nel && g_tab[i].neq == P->neq) return g_tab[i].sys;
+        if (!g_tab[i].key && free_slot < 0) free_slot = i;
+    }
+    if (P->NPROC > 1 || P->neq_bef != 0) {
+        fprintf(stderr, "femgpu: the GPU solve path replaces the MPI decomposition (one rank only)\n");
+        if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
+        return NULL;
+    }
+    if (free_slot < 0) { fprintf(stderr, "femgpu: too many systems\n"); return NULL; }
+    int nn = P->nnodes, ne = P->nel;
+    int *type = malloc(sizeof(int) * (size_t)nn), *invp = malloc(sizeof(int) * (size_t)nn);
+    int *ien = malloc(sizeof(int) * 3 * (size_t)ne);
+    for (i = 0; i < nn; i++) {
+        type[i] = S->Node[i].Type == 0 ? 0 : 1;
+        invp[i] = S->Node[i].Type == 0 ? -1 : S->Node[i].invP_id;
+    }
+    for (i = 0; i < ne; i++) {
+        ien[3 * i] = S->Element[i].Vertex[0];
+        ien[3 * i + 1] = S->Element[i].Vertex[1];
+        ien[3 * i + 2] = S->Element[i].Vertex[2];
+    }
+    fg_system *sys = NULL;
+    int reorder = strcasecmp(P->reordering, "NOT") == 0 ? FG_REORDER_NONE : FG_REORDER_RCM;
+    int rc = fg_system_create(&sys, nn, ne, 1, ien, type, invp, P->neq, reorder);
+    free(type); free(invp); free(ien);
+    if (rc) { fgc_fail(rc, "system set-up"); return NULL; }
+    g_tab[free_slot].key = M;
+    g_tab[free_slot].sys = sys;
+    g_tab[free_slot].nel = ne;
+    g_tab[free_slot].neq = P->neq;
+    return sys;
+}
+
+/* Element blocks as Build_K_F_SUPG left them: nel rows of 9 in Aaux
+ * (Preprocess.c:331-340 allocates A as row pointers into Aaux). */
+static int fgc_upload_blocks(fg_system *sys, MatrixDataType *M)
+{
+    int rc = fg_set_blocks(sys, M->Aaux);
+    return rc ? fgc_fail(rc, "element blocks") : 0;
+}
+
+int NO_precond(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    (void)P; (void)M; (void)S; (void)p; (void)z;
+    return 0;
+}
+
+int NO_precond_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
+{
+    (void)tag; (void)F;
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    if (fgc_upload_blocks(sys, M)) return 1;
+    int rc = fg_precond_setup(sys, FG_PRECOND_NONE, 0, NULL);
+    return rc ? fgc_fail(rc, "NO_precond_setup") : 0;
+}
+
+/* Diag_precond_EBE_setup (EBE/Diag_precond_EBE_setup.c:3-32): Diag keeps
+ * accumulating in MatrixData->Diag across calls, as in the reference;
+ * invDiag is filled and F is preconditioned in place. */
+int Diag_precond_EBE_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
+{
+    (void)tag;
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    if (fgc_upload_blocks(sys, M)) return 1;
+    int rc = fg_set_diag(sys, M->Diag);
+    if (!rc) rc = fg_precond_setup(sys, FG_PRECOND_DIAG, FG_SETUP_ACCUMULATE, F);
+    if (!rc) rc = fg_get_diag(sys, M->Diag);
+    if (rc) return fgc_fail(rc, "Diag_precond_EBE_setup");
+    for (int i = 0; i < P->NEQ; i++) M->invDiag[i] = 1.0 / M->Diag[i];
+    return 0;
+}
+
+/* Diag_precond (Diag_precond.c:3-15), on the owned slice (p may be z). */
+int Diag_precond(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    double keep = p[P->neq];
+    p[P->neq] = 0.0;
+    int rc = fg_precond_apply(sys, p, z);
+    if (z != p) p[P->neq] = keep;
+    return rc ? fgc_fail(rc, "Diag_precond") : 0;
+}
+
+/* ebemv (EBE/ebemv.c:4-64): Q = A P over NEQ + 1 entries; Q[NEQ] = 0. */
+int ebemv(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *Pv, double *Qv)
+{
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    if (fgc_upload_blocks(sys, M)) return 1;
+    Pv[P->NEQ] = 0.0;
+    int rc = fg_matvec(sys, Pv, Qv, 64);
+    return rc ? fgc_fail(rc, "ebemv") : 0;
+}
+
+/* pgmres (Solvers_and_Preconditioners/pgmres.c:5-200): the whole restarted
+ * GMRES on the GPU when mv is this shim's ebemv and the preconditioner pair
+ * is this shim's Diag_precond or NO_precond (the configurations the
+ * steady-transport driver installs with EBE storage); the blocks and the
+ * preconditioner were set up by the *_setup call that precedes every solve
+ * (Process.c:59-76).  Parameters->iterations grows by the Arnoldi steps. */
+int pgmres(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctionsType *Fn, double *B, double *X)
+{
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    if (Fn->mv != ebemv || Fn->precondR != NO_precond ||
+        (Fn->precond != Diag_precond && Fn->precond != NO_precond)) {
+        fprintf(stderr, "femgpu: pgmres supports mv = ebemv with Diag or no preconditioning on the GPU\n");
+        if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
+        return 1;
+    }
+    fg_solver_opts o;
+    o.kmax = P->KrylovBasisVectorsQuantity;
+    o.lmax = P->LinearMaxIter;
+    o.tol = P->SolverTolerance;
+    o.precision = FG_PREC_FP64;
+    o.inner_tol = 0.0;
+    fg_solve_stats st;
+    memset(&st, 0, sizeof st);
+    int rc = fg_solve(sys, &o, B, X, NULL, &st);
+    if (rc) return fgc_fail(rc, "pgmres");
+    P->iterations += st.iterations;
+    return 0;
+}
+
+/* Field offsets of the restated structs (layout pin, compared with the
+ * reference's own header by the tests). */
+#include <stddef.h>
+void fgc_sst_layout(long *out)
+{
+    out[0] = (long)sizeof(ParametersType);
+    out[1] = (long)offsetof(ParametersType, SolverTolerance);
+    out[2] = (long)offsetof(ParametersType, KrylovBasisVectorsQuantity);
+    out[3] = (long)offsetof(ParametersType, nnodes);
+    out[4] = (long)offsetof(ParametersType, nel);
+    out[5] = (long)offsetof(ParametersType, neq);
+    out[6] = (long)offsetof(ParametersType, neq_bef);
+    out[7] = (long)offsetof(ParametersType, NEQ);
+    out[8] = (long)offsetof(ParametersType, LinearMaxIter);
+    out[9] = (long)offsetof(ParametersType, iterations);
+    out[10] = (long)offsetof(ParametersType, RANK);
+    out[11] = (long)offsetof(ParametersType, NPROC);
+    out[12] = (long)sizeof(MatrixDataType);
+    out[13] = (long)offsetof(MatrixDataType, A);
+    out[14] = (long)offsetof(MatrixDataType, Aaux);
+    out[15] = (long)offsetof(MatrixDataType, Diag);
+    out[16] = (long)offsetof(MatrixDataType, invDiag);
+    out[17] = (long)offsetof(MatrixDataType, Perm);
+    out[18] = (long)offsetof(MatrixDataType, invPerm);
+    out[19] = (long)sizeof(FemStructsType);
+    out[20] = (long)offsetof(FemStructsType, lm);
+    out[21] = (long)offsetof(FemStructsType, lmaux);
+    out[22] = (long)offsetof(FemStructsType, Node);
+    out[23] = (long)offsetof(FemStructsType, Element);
+    out[24] = (long)sizeof(FemFunctionsType);
+    out[25] = (long)offsetof(FemFunctionsType, mv);
+    out[26] = (long)offsetof(FemFunctionsType, precond);
+    out[27] = (long)offsetof(FemFunctionsType, precondR);
+    out[28] = (long)offsetof(FemFunctionsType, precond_setup);
+    out[29] = (long)sizeof(NodeType);
+    out[30] = (long)sizeof(ElementType);
+    out[31] = (long)offsetof(MatrixDataType, AA);
+    out[32] = (long)offsetof(MatrixDataType, JA);
+    out[33] = (long)offsetof(MatrixDataType, IA);
+    out[34] = (long)offsetof(ParametersType, MatrixVectorProductScheme);
+    out[35] = (long)offsetof(ParametersType, Preconditioner);
+    out[36] = (long)offsetof(ParametersType, nnzero);
+}

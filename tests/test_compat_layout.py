@@ -1,0 +1,30 @@
+"""The drop-in shim's restated struct layout equals the reference's (its
+own header compiled by oracle/Makefile), and the shim exports the
+reference's entry-point names.  CPU only."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle as O
+from parallel_fem_codes_gb300 import refapi
+
+
+def test_shim_exports_reference_names():
+    L = refapi.shim()
+    for name in ("pgmres", "ebemv", "Diag_precond", "Diag_precond_EBE_setup", "NO_precond", "NO_precond_setup"):
+        assert hasattr(L, name), name
+
+
+def test_python_mirror_matches_shim_header():
+    out = np.zeros(64, dtype=np.int64)
+    refapi.shim().fgc_sst_layout(out)
+    assert list(out[:37]) == refapi.layout_offsets()
+
+
+@pytest.mark.skipif(not O.ref_available(), reason="reference build (oracle/_ref) not present")
+def test_shim_layout_matches_reference_header():
+    ours = np.zeros(64, dtype=np.int64)
+    refapi.shim().fgc_sst_layout(ours)
+    theirs = O.ref_layout()
+    assert np.array_equal(ours[:37], theirs[:37])
