@@ -31,7 +31,8 @@ enum {
     FG_ERR_STATE = 4,      /* call out of order (e.g. solve before blocks)     */
     FG_ERR_BREAKDOWN = 5,  /* zero pivot / non-finite value in the solve       */
     FG_ERR_NOTCONV = 6,    /* iteration limit reached before the tolerance     */
-    FG_ERR_UNSUPPORTED = 7 /* option not available for this system             */
+    FG_ERR_UNSUPPORTED = 7, /* option not available for this system            */
+    FG_ERR_TIMEOUT = 8     /* a bounded device-side wait ran out               */
 };
 
 /* Text of the last error on the calling thread (never NULL). */
@@ -109,8 +110,21 @@ int fg_matvec(fg_system *s, const double *P, double *Q, int precision);
  * GPU race and must be serialised by the caller. */
 int fg_matvec_noalloc(fg_system *s, const double *P_dev, double *Q_dev, int precision);
 
+/* ---- assembled CSR operator (MatrixVectorProductScheme "CSR") ----
+ * FG_OP_CSR builds, once, the CSR pattern of the free dofs in the local RCM
+ * numbering (csr_Initialization.c:5-434) and from then on assembles the CSR
+ * values from the element blocks on the device (csr_assembly.c:3-54, sums
+ * in element order) whenever blocks change; matvecs and solves use the CSR
+ * form (csrmv.c:4-65).  FG_OP_EBE (default) uses the element blocks. */
+enum { FG_OP_EBE = 0, FG_OP_CSR = 1 };
+int fg_set_operator(fg_system *s, int op);
+/* CSR values in the reference's CSR layout: IA[n+1], JA[nnz], AA[nnz]
+ * (internal numbering = the reference's renumbered equations), any NULL. */
+int fg_get_csr(const fg_system *s, int *nnz, int *IA, int *JA, double *AA);
+
 /* ---- preconditioners (Solvers_and_Preconditioners/preconditioners.h) ---- */
-enum { FG_PRECOND_NONE = 0, FG_PRECOND_DIAG = 1, FG_PRECOND_BLOCKDIAG = 2 };
+enum { FG_PRECOND_NONE = 0, FG_PRECOND_DIAG = 1, FG_PRECOND_BLOCKDIAG = 2,
+       FG_PRECOND_ILU0 = 3  /* ILU(0) of the assembled CSR operator (fg_set_operator) */ };
 enum {
     FG_SETUP_ACCUMULATE = 1, /* Diag += new diagonal, as Diag_precond_EBE_setup
                                 does across nonlinear iterations              */

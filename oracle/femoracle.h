@@ -123,6 +123,16 @@ int or_ebe_diag_solve(int nel, int S, const int *lm, const double *A, int NEQ,
                       double *Diag, double *invDiag, double *F,
                       int kmax, int lmax, double tol, double *X);
 
+/* ---- assembled CSR path and ILU(0) (oracle/csr_ilu.c) ---- */
+int  or_csr_pattern(int nel, const int *ien, const int *type, const int *invp, int NEQ,
+                    const int *Perm, const int *invPerm, int *IA, int *JA);
+void or_csr_assemble(int nel, int S, const int *lm, const double *A, int NEQ,
+                     const int *IA, const int *JA, double *AA);
+void or_csrmv(int n, const int *IA, const int *JA, const double *AA, const double *P, double *Q);
+int  or_ilu0_factor(int n, const int *IA, const int *JA, const double *AA, double *LU, double *D);
+void or_ilu0_apply(int n, const int *IA, const int *JA, const double *LU, const double *D,
+                   const double *y, double *x);
+
 #ifdef __cplusplus
 }
 #endif

@@ -308,3 +308,75 @@ def ref_layout():
     out = np.zeros(64, dtype=np.int64)
     ref().fr_sst_layout(out)
     return out
+
+
+# ------------------------------------------------------- CSR path and ILU(0)
+def csr_pattern(mesh, perm, inv):
+    """CSR pattern of the free dofs in the RCM numbering of csr_Initialization."""
+    L = lib()
+    L.or_csr_pattern.argtypes = [_c_int, _i32p, _i32p, _i32p, _c_int, _i32p, _i32p, _i32p, _i32p]
+    n = mesh.neq
+    IA = np.empty(n + 1, dtype=np.int32)
+    JA = np.empty(mesh.nel * 9 * mesh.ndof ** 2 + 1, dtype=np.int32)
+    nnz = L.or_csr_pattern(mesh.nel, np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1),
+                           mesh.type, mesh.invp, n, perm, inv, IA, JA)
+    return IA, JA[:nnz].copy()
+
+
+def csr_assemble(lm_new, A, NEQ, IA, JA):
+    L = lib()
+    L.or_csr_assemble.argtypes = [_c_int, _c_int, _i32p, _f64p, _c_int, _i32p, _i32p, _f64p]
+    L.or_csr_assemble.restype = None
+    nel, S = lm_new.shape
+    AA = np.zeros(JA.shape[0])
+    L.or_csr_assemble(nel, S, np.ascontiguousarray(lm_new, dtype=np.int32).reshape(-1),
+                      np.ascontiguousarray(A, dtype=np.float64).reshape(-1), NEQ, IA, JA, AA)
+    return AA
+
+
+def csrmv(IA, JA, AA, P):
+    L = lib()
+    L.or_csrmv.argtypes = [_c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+    L.or_csrmv.restype = None
+    n = IA.shape[0] - 1
+    Q = np.zeros(n + 1)
+    L.or_csrmv(n, IA, JA, AA, np.ascontiguousarray(P, dtype=np.float64), Q)
+    return Q
+
+
+def ilu0(IA, JA, AA):
+    L = lib()
+    L.or_ilu0_factor.argtypes = [_c_int, _i32p, _i32p, _f64p, _f64p, _f64p]
+    n = IA.shape[0] - 1
+    LU = np.zeros_like(AA)
+    D = np.zeros(n)
+    rc = L.or_ilu0_factor(n, IA, JA, AA, LU, D)
+    return rc, LU, D
+
+
+def ilu0_apply(IA, JA, LU, D, y):
+    L = lib()
+    L.or_ilu0_apply.argtypes = [_c_int, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p]
+    L.or_ilu0_apply.restype = None
+    n = IA.shape[0] - 1
+    x = np.zeros(n + 1)
+    L.or_ilu0_apply(n, IA, JA, LU, D, np.ascontiguousarray(y, dtype=np.float64), x)
+    return x
+
+
+def ref_csr(prob, A, P):
+    """The reference's csr_Initialization + csr_assembly + csrmv + ILU(0)."""
+    R = ref()
+    R.fr_sst_csr.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _f64p, _c_int,
+                             _i32p, _i32p, _f64p, _i32p, _f64p, _f64p, _f64p]
+    m = prob.mesh
+    nmax = m.nel * 9 + 1
+    IA = np.empty(m.neq + 1, dtype=np.int32)
+    JA = np.empty(nmax, dtype=np.int32)
+    AA = np.empty(nmax)
+    invp = np.empty(m.nnodes, dtype=np.int32)
+    Q = np.zeros(m.neq + 1)
+    z = np.zeros(m.neq + 1)
+    nnz = R.fr_sst_csr(*_mesh_args(m), np.ascontiguousarray(A, dtype=np.float64).reshape(-1), nmax, IA, JA, AA,
+                       invp, np.ascontiguousarray(P, dtype=np.float64), Q, z)
+    return IA, JA[:nnz].copy(), AA[:nnz].copy(), invp, Q, z

@@ -300,3 +300,51 @@ void fr_sst_layout(long *out)
     out[35] = (long)offsetof(ParametersType, Preconditioner);
     out[36] = (long)offsetof(ParametersType, nnzero);
 }
+
+/* ---- assembled CSR path: csr_Initialization + csr_assembly + csrmv +
+ * ILUp_precond_setup (ILU0) + ILUp_precond, one rank ---- */
+void csr_Initialization(ParametersType *, MatrixDataType *, FemStructsType *);
+
+/* Build the CSR structure the reference's way (renumbering the nodes by
+ * RCM), assemble the given element blocks through csr_assembly, and return
+ * IA/JA/AA, the new node numbering, and ILU(0) applied to P (z) together
+ * with csrmv of P (Q).  Arrays: IA[neq+1], JA/AA[nnz_max], invp_out[nnodes]. */
+int fr_sst_csr(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+               const int *ien, int neq, const double *A, int nnz_max, int *IA_out, int *JA_out,
+               double *AA_out, int *invp_out, const double *P, double *Q, double *z)
+{
+    fr_sst c;
+    int I;
+    fr_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, 1e-10, 1e-3, 30, 10);
+    strcpy(c.P.MatrixVectorProductScheme, "CSR");
+    strcpy(c.P.Preconditioner, "ILU0");
+    csr_Initialization(&c.P, &c.M, &c.S);
+    int nnz = c.P.nnzero;
+    if (nnz > nnz_max) { fr_free(&c); return -1; }
+    c.M.AA = calloc((size_t)nnz + 1, sizeof(double));
+    c.M.AA_bef = calloc(1, sizeof(double));
+    c.M.AA_aft = calloc(1, sizeof(double));
+    double ke[3][3];
+    int r, q;
+    for (I = 0; I < nel; I++) {
+        for (r = 0; r < 3; r++)
+            for (q = 0; q < 3; q++) ke[r][q] = A[9 * I + 3 * r + q];
+        csr_assembly(&c.P, &c.M, &c.S, I, ke);
+    }
+    memcpy(IA_out, c.M.IA, sizeof(int) * ((size_t)neq + 1));
+    memcpy(JA_out, c.M.JA, sizeof(int) * (size_t)nnz);
+    memcpy(AA_out, c.M.AA, sizeof(double) * (size_t)nnz);
+    for (I = 0; I < nnodes; I++) invp_out[I] = c.S.Node[I].invP_id;
+    double *Pc = calloc((size_t)neq + 1, sizeof(double));
+    memcpy(Pc, P, sizeof(double) * (size_t)neq);
+    c.P.neqaux_bef = c.P.neqaux_aft = 0;
+    csrmv(&c.P, &c.M, &c.S, Pc, Q);
+    /* ILU(0): set-up (factorises and applies to F), then one apply */
+    double *F = calloc((size_t)neq + 1, sizeof(double));
+    ILUp_precond_setup(&c.P, &c.M, &c.S, 1, F);
+    memcpy(z, P, sizeof(double) * (size_t)neq);
+    ILUp_precond(&c.P, &c.M, &c.S, z, z);
+    free(Pc); free(F);
+    fr_free(&c);
+    return nnz;
+}

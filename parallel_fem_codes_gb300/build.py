@@ -25,6 +25,7 @@ UNITS = [
     ("setup.cu", ["-fmad=false"]),
     ("noalloc.cu", []),
     ("server.cu", []),
+    ("ilu.cu", ["-fmad=false"]),
 ]
 
 

@@ -53,6 +53,16 @@ struct Topology {
     std::vector<int> pc_ptr, pc_list;    // patches grouped by patch colour
 };
 
+// Assembled CSR form of a system (csr_Initialization.c), rows and columns
+// in the internal (RCM) numbering, which is the reference's CSR numbering.
+struct CsrTopology {
+    int n = 0, nnz = 0;
+    std::vector<int> ia, ja, diag;       // diag[i]: slot of the diagonal of row i
+    std::vector<int> inc_ptr, inc;       // slot -> contributions pos*256 + a*16 + b, reference element order
+    std::vector<int> fwd_chunks, bwd_chunks;  // row chunk starts in solve order (32 rows each)
+};
+int build_csr(const Topology &t, CsrTopology &c);
+
 constexpr int kPatchElems = 1024;      // elements per matvec patch
 constexpr int kPatchMaxLocalColours = 16;
 constexpr int kPatchColStride = kPatchMaxLocalColours + 1;
@@ -94,6 +104,12 @@ struct SysDev {
     const int *pt_elem, *pt_dof, *dofs;
     const unsigned short *pt_col;
     int maxdof;
+    // assembled CSR operator and ILU(0) (op == 1)
+    int op, csr_w;
+    const int *csr_ia, *csr_ja, *csr_diag;
+    const double *AA64, *LU64, *dinv64;
+    const float *AA32, *LU32, *dinv32;
+    int *ilu_flag;             // per-row ready flags of the sync-free solves
     const double *A64;         // [S*S][nel_pad]
     const float *A32;
     const double *invd64;      // n_pad

@@ -193,6 +193,40 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
     }
 }
 
+// ---------------------------------------------------------------- CSR SpMV
+// y = A x for the assembled operator (csrmv.c:57-62), W lanes per row
+// (W = 4, 8 or 32 from the mean row length; rows of P1 transport hold ~7
+// entries, rows of the 4-dof Euler system ~30): lanes stride the row,
+// shuffle-reduce, one lane stores.  Works on dof parts like the Krylov
+// kernels; same in/out selection as k_ebe_mv.
+template <int W, typename TA, typename TX, typename TY>
+__global__ void __launch_bounds__(kThreads)
+k_csr_mv(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch,
+         int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out)
+{
+    const int total = *nch;
+    const int sub = threadIdx.x % W, grp = threadIdx.x / W, ngrp = blockDim.x / W;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!gated(D, gate)) continue;
+        const TX *X = in_sel == 0 ? (const TX *)D.x
+                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+        TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
+        const TA *AA = sizeof(TA) == 8 ? (const TA *)D.AA64 : (const TA *)D.AA32;
+        for (int base = k.d0; base < k.d1; base += ngrp) {
+            const int row = base + grp;
+            TA s = 0;
+            if (row < k.d1)
+                for (int q = D.csr_ia[row] + sub; q < D.csr_ia[row + 1]; q += W)
+                    s += ldst(AA + q) * (TA)X[__ldcs(D.csr_ja + q)];
+#pragma unroll
+            for (int o = W / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, W);
+            if (row < k.d1 && sub == 0) Y[row] = (TY)s;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- block-diagonal apply
 // z[dofs of node] = invB(node) * p[dofs of node] (BlockDiag_precond.c:3-29,
 // BlockDiagDOF3_precond.c:3-27); dofs that are Dirichlet read 0 and are not
@@ -252,7 +286,7 @@ k_start(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
         for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) {
             double t = D.t64[d];
             double u = D.precond == FG_PRECOND_DIAG ? t * D.invd64[d]
-                     : D.precond == FG_PRECOND_BLOCKDIAG ? D.u64[d] : t;
+                     : (D.precond == FG_PRECOND_BLOCKDIAG || D.precond == FG_PRECOND_ILU0) ? D.u64[d] : t;
             double bd = D.b[d];
             double r = -1.0 * (u + -1.0 * bd);
             D.r64[d] = r;
@@ -450,10 +484,13 @@ int parts_for(int n)
 // Chunk tables of one batch (device copies + host counts).
 struct Plan {
     int nsys = 0, ncol = 0, S = 3, B = 1, maxdof = 1;   // ncol: patch colours
+    int op = FG_OP_EBE, csr_w = 4, precond = FG_PRECOND_NONE;
     size_t smem(int w) const { return 2 * (size_t)maxdof * w; }
     std::vector<int> ech_off;      // ncol+1 offsets into echunks
-    int n_dch = 0, n_nch = 0;
+    int n_dch = 0, n_nch = 0, n_ilu = 0;
+    size_t flag_bytes = 0;
     DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
+    DevMem ilu_fwd, ilu_bwd, ilu_flags, ilu_ctr;   // sync-free ILU(0) substitutions
 };
 
 static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig &cfg, std::vector<SysDev> &hs,
@@ -496,6 +533,35 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     }
     P.n_dch = (int)dch.size();
     P.n_nch = (int)nch.size();
+    P.op = mem[0].s->op;
+    P.precond = cfg.precond;
+    P.csr_w = 4;
+    for (auto &m : mem) {
+        if (m.s->op != P.op) { set_error("a batch must use one operator kind"); return FG_ERR_ARG; }
+        P.csr_w = std::max(P.csr_w, m.s->csr_w);
+    }
+    // ILU(0) substitutions: 32-row items, rows ascending (forward) or
+    // descending (backward) within each system, systems interleaved
+    std::vector<int2> fwd, bwd;
+    if (cfg.precond == FG_PRECOND_ILU0) {
+        std::vector<size_t> off(P.nsys + 1, 0);
+        for (int s = 0; s < P.nsys; ++s) off[s + 1] = off[s] + (size_t)mem[s].s->topo.n + 1;
+        P.flag_bytes = 4 * off[P.nsys];
+        int r0;
+        if ((r0 = P.ilu_flags.alloc(std::max<size_t>(P.flag_bytes, 4))) || (r0 = P.ilu_ctr.alloc(64))) return r0;
+        for (int s = 0; s < P.nsys; ++s) hs[s].ilu_flag = P.ilu_flags.as<int>() + off[s];
+        int maxch = 0;
+        for (int s = 0; s < P.nsys; ++s) maxch = std::max(maxch, (mem[s].s->topo.n + 31) / 32);
+        for (int q = 0; q < maxch; ++q)
+            for (int s = 0; s < P.nsys; ++s) {
+                int nch_s = (mem[s].s->topo.n + 31) / 32;
+                if (q < nch_s) {
+                    fwd.push_back(make_int2(s, q * 32));
+                    bwd.push_back(make_int2(s, (nch_s - 1 - q) * 32));
+                }
+            }
+        P.n_ilu = (int)fwd.size();
+    }
     std::vector<int> ecounts(P.ncol);
     for (int c = 0; c < P.ncol; ++c) ecounts[c] = P.ech_off[c + 1] - P.ech_off[c];
     int r;
@@ -506,8 +572,14 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
         (r = P.dcount.alloc(sizeof(int))) ||
         (r = P.nchunks.alloc(sizeof(NChunk) * std::max<size_t>(1, nch.size()))) ||
         (r = P.ncount.alloc(sizeof(int))) ||
-        (r = P.live.alloc(sizeof(int) * P.nsys)))
+        (r = P.live.alloc(sizeof(int) * P.nsys)) ||
+        (r = P.ilu_fwd.alloc(sizeof(int2) * std::max<size_t>(1, fwd.size()))) ||
+        (r = P.ilu_bwd.alloc(sizeof(int2) * std::max<size_t>(1, bwd.size()))))
         return r;
+    if (!fwd.empty()) {
+        FG_CUDA(cudaMemcpyAsync(P.ilu_fwd.p, fwd.data(), sizeof(int2) * fwd.size(), cudaMemcpyHostToDevice, st));
+        FG_CUDA(cudaMemcpyAsync(P.ilu_bwd.p, bwd.data(), sizeof(int2) * bwd.size(), cudaMemcpyHostToDevice, st));
+    }
     FG_CUDA(cudaMemcpyAsync(P.sysdev.p, hs.data(), sizeof(SysDev) * hs.size(), cudaMemcpyHostToDevice, st));
     if (!ech.empty())
         FG_CUDA(cudaMemcpyAsync(P.echunks.p, ech.data(), sizeof(EChunk) * ech.size(), cudaMemcpyHostToDevice, st));
@@ -523,9 +595,35 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
 
 // Enqueue the matvec over all colours: mode 0 (x -> t64, FP64, gate live)
 // or mode 1 (V[step] -> t, T, gate in_cycle).
+template <typename TA, typename TX, typename TY>
+static void launch_csr_mv(const Plan &P, cudaStream_t st, int gate, int in_sel, int out_sel, int step)
+{
+    const SysDev *sys = P.sysdev.as<SysDev>();
+    dim3 g = grid_for(P.n_dch);
+    const DChunk *dc = P.dchunks.as<DChunk>();
+    const int *nd = P.dcount.as<int>();
+    if (P.csr_w == 4)
+        k_csr_mv<4, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, dc, nd, gate, in_sel, out_sel, step, nullptr, nullptr);
+    else if (P.csr_w == 8)
+        k_csr_mv<8, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, dc, nd, gate, in_sel, out_sel, step, nullptr, nullptr);
+    else
+        k_csr_mv<32, TA, TX, TY><<<g, kThreads, 0, st>>>(sys, dc, nd, gate, in_sel, out_sel, step, nullptr, nullptr);
+}
+
+// Enqueue the matvec: mode 0 (x -> t64, FP64, gate live), mode 1 (V[step]
+// -> t, T, gate in_cycle), mode 2 (V[0] -> t, T, every member), mode 3
+// (x -> t64, FP64, every member).  Returns the number of kernels.
 template <typename T>
 static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
 {
+    const bool f64 = mode == 0 || mode == 3;
+    const int gate = mode == 0 ? 0 : mode == 1 ? 1 : -1;
+    const int sel = f64 ? 0 : 1;
+    if (P.op == FG_OP_CSR) {
+        if (f64) launch_csr_mv<double, double, double>(P, st, gate, sel, sel, step);
+        else launch_csr_mv<T, T, T>(P, st, gate, sel, sel, step);
+        return 1;
+    }
     const SysDev *sys = P.sysdev.as<SysDev>();
     int k = 0;
     for (int c = 0; c < P.ncol; ++c) {
@@ -533,15 +631,41 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
         if (!cnt) continue;
         const EChunk *ch = P.echunks.as<EChunk>() + P.ech_off[c];
         const int *nc = P.ecount.as<int>() + c;
-        if (mode == 0)
-            MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, ch, nc, 0, 0, 0, 0, nullptr, nullptr,
+        if (f64)
+            MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, ch, nc, gate, 0, 0, 0, nullptr, nullptr,
                                                  P.smem(8));
         else
-            MvLaunch::go<T, T, T>(P.S, grid_for(cnt), st, sys, ch, nc, mode == 2 ? -1 : 1, 1, 1, step, nullptr,
-                                  nullptr, P.smem(sizeof(T)));
+            MvLaunch::go<T, T, T>(P.S, grid_for(cnt), st, sys, ch, nc, gate, 1, 1, step, nullptr, nullptr,
+                                  P.smem(sizeof(T)));
         ++k;
     }
     return k;
+}
+
+// M^-1 applied after a matvec: sel 0 (t64 -> u64, FP64) or 1 (t -> w, T).
+template <typename T>
+static int enqueue_precond(const Plan &P, int sel, cudaStream_t st)
+{
+    const SysDev *sys = P.sysdev.as<SysDev>();
+    if (P.precond == FG_PRECOND_BLOCKDIAG) {
+        if (sel == 0)
+            launch_blockdiag<double>(P.B, grid_for(P.n_nch), st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 0,
+                                     0, nullptr, nullptr);
+        else
+            launch_blockdiag<T>(P.B, grid_for(P.n_nch), st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 1, 1,
+                                nullptr, nullptr);
+        return 1;
+    }
+    if (P.precond == FG_PRECOND_ILU0) {
+        int *ctr = P.ilu_ctr.as<int>(), *err = ctr + 4;
+        const int fp32 = sel == 1 && sizeof(T) == 4;
+        launch_ilu_solve(sys, P.ilu_fwd.as<int2>(), P.n_ilu, P.ilu_flags.as<int>(), P.flag_bytes, ctr, err, sel, 0,
+                         fp32, st);
+        launch_ilu_solve(sys, P.ilu_bwd.as<int2>(), P.n_ilu, P.ilu_flags.as<int>(), P.flag_bytes, ctr, err, sel, 1,
+                         fp32, st);
+        return 2;
+    }
+    return 0;
 }
 
 // One restart cycle for every member; returns the number of kernels.
@@ -551,16 +675,15 @@ static int enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
     const SysDev *sys = P.sysdev.as<SysDev>();
     const DChunk *dc = P.dchunks.as<DChunk>();
     const int *nd = P.dcount.as<int>();
-    dim3 gd = grid_for(P.n_dch), gn = grid_for(P.n_nch);
-    const bool bd = cfg.precond == FG_PRECOND_BLOCKDIAG;
+    dim3 gd = grid_for(P.n_dch);
     int k = enqueue_matvec<T>(P, 0, 0, st);
-    if (bd) { launch_blockdiag<double>(P.B, gn, st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 0, 0, nullptr, nullptr); ++k; }
+    k += enqueue_precond<T>(P, 0, st);
     k_start<<<gd, kThreads, 0, st>>>(sys, dc, nd);
     k_scale_v0<T><<<gd, kThreads, 0, st>>>(sys, dc, nd);
     k += 2;
     for (int i = 0; i < cfg.kmax - 1; ++i) {
         k += enqueue_matvec<T>(P, 1, i, st);
-        if (bd) { launch_blockdiag<T>(P.B, gn, st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 1, 1, nullptr, nullptr); ++k; }
+        k += enqueue_precond<T>(P, 1, st);
         k_dots1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
         k_orth1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
         k_orth2<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
@@ -633,6 +756,10 @@ int validate_member(fg_system *s, const SolveConfig &cfg)
     if (cfg.precond == FG_PRECOND_BLOCKDIAG && s->topo.ndof < 2) {
         set_error("block-diagonal preconditioner needs ndof >= 2"); return FG_ERR_UNSUPPORTED;
     }
+    if (s->op == FG_OP_CSR && !s->csr_ok) { set_error("CSR operator selected but not set up"); return FG_ERR_STATE; }
+    if (cfg.precond == FG_PRECOND_ILU0 && s->op != FG_OP_CSR) {
+        set_error("ILU(0) needs the CSR operator (fg_set_operator(FG_OP_CSR))"); return FG_ERR_STATE;
+    }
     return FG_OK;
 }
 
@@ -659,6 +786,7 @@ int BatchRun::stage(const BatchMember &m)
     int r = validate_member(s, cfg);
     if (r) return r;
     if ((r = ensure_workspace(s, cfg.kmax, cfg.mixed))) return r;
+    if (s->op == FG_OP_CSR && (r = csr_refresh(s, st))) return r;
     Workspace &w = s->ws;
     size_t vb = 8 * (size_t)s->n_pad;
     FG_CUDA(cudaMemsetAsync(w.x.p, 0, vb, st));
@@ -752,13 +880,7 @@ int BatchRun::finish(const std::vector<int> &idx, std::vector<SysState> &out)
     int r = build_plan(F, sub, cfg, shs, st);
     if (r) return r;
     const SysDev *sys = F.sysdev.as<SysDev>();
-    for (int c = 0; c < F.ncol; ++c) {
-        int cnt = F.ech_off[c + 1] - F.ech_off[c];
-        if (!cnt) continue;
-        MvLaunch::go<double, double, double>(F.S, grid_for(cnt), st, sys, F.echunks.as<EChunk>() + F.ech_off[c],
-                                             F.ecount.as<int>() + c, -1, 0, 0, 0, nullptr, nullptr, F.smem(8));
-        count_launches(1);
-    }
+    count_launches(enqueue_matvec<double>(F, 3, 0, st));
     k_final<<<grid_for(F.n_dch), kThreads, 0, st>>>(sys, F.dchunks.as<DChunk>(), F.dcount.as<int>());
     FG_CUDA(cudaGetLastError());
     count_launches(1);
@@ -860,6 +982,33 @@ int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaS
     if (!ech.empty()) FG_CUDA(cudaMemcpyAsync(ch.p, ech.data(), sizeof(EChunk) * ech.size(), cudaMemcpyHostToDevice, st));
     if (t.npcol) FG_CUDA(cudaMemcpyAsync(cnt.p, counts.data(), sizeof(int) * t.npcol, cudaMemcpyHostToDevice, st));
     FG_CUDA(cudaMemsetAsync(y, 0, 8 * (size_t)(t.n + 1), st));
+    if (s->op == FG_OP_CSR) {
+        if ((r = csr_refresh(s, st))) return r;
+        std::vector<DChunk> dch;
+        for (int d = 0; d < t.n; d += 2048) dch.push_back({0, 0, d, std::min(d + 2048, t.n)});
+        DevMem dc, dn;
+        int nd = (int)dch.size();
+        if ((r = dc.alloc(sizeof(DChunk) * std::max<size_t>(1, dch.size()))) || (r = dn.alloc(sizeof(int)))) return r;
+        if (nd) FG_CUDA(cudaMemcpyAsync(dc.p, dch.data(), sizeof(DChunk) * nd, cudaMemcpyHostToDevice, st));
+        FG_CUDA(cudaMemcpyAsync(dn.p, &nd, sizeof(int), cudaMemcpyHostToDevice, st));
+        dim3 g = grid_for(std::max(nd, 1));
+        const SysDev *sdp = sd.as<SysDev>();
+        const DChunk *dcp = dc.as<DChunk>();
+        const int *dnp = dn.as<int>();
+        if (precision == 32) {
+            if (s->csr_w == 4) k_csr_mv<4, float, double, double><<<g, kThreads, 0, st>>>(sdp, dcp, dnp, -1, 2, 2, 0, x, y);
+            else if (s->csr_w == 8) k_csr_mv<8, float, double, double><<<g, kThreads, 0, st>>>(sdp, dcp, dnp, -1, 2, 2, 0, x, y);
+            else k_csr_mv<32, float, double, double><<<g, kThreads, 0, st>>>(sdp, dcp, dnp, -1, 2, 2, 0, x, y);
+        } else {
+            if (s->csr_w == 4) k_csr_mv<4, double, double, double><<<g, kThreads, 0, st>>>(sdp, dcp, dnp, -1, 2, 2, 0, x, y);
+            else if (s->csr_w == 8) k_csr_mv<8, double, double, double><<<g, kThreads, 0, st>>>(sdp, dcp, dnp, -1, 2, 2, 0, x, y);
+            else k_csr_mv<32, double, double, double><<<g, kThreads, 0, st>>>(sdp, dcp, dnp, -1, 2, 2, 0, x, y);
+        }
+        FG_CUDA(cudaGetLastError());
+        count_launches(1);
+        FG_CUDA(cudaStreamSynchronize(st));
+        return FG_OK;
+    }
     const size_t smem = 2 * (size_t)D.maxdof * (precision == 32 ? 4 : 8);
     for (int c = 0; c < t.npcol; ++c) {
         if (!counts[c]) continue;

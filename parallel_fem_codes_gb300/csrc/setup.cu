@@ -227,6 +227,7 @@ int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaS
 {
     const Topology &t = s->topo;
     if (kind == FG_PRECOND_NONE) { s->precond = kind; return FG_OK; }
+    if (kind == FG_PRECOND_ILU0) return ilu0_setup_device(s, F_dev, st);
     if (!s->blocks_ok) { set_error("preconditioner set-up before element blocks were set"); return FG_ERR_STATE; }
     if (kind == FG_PRECOND_DIAG) {
         if (t.n > 0)
@@ -276,6 +277,7 @@ __global__ void k_diag_apply(const double *__restrict__ invd, int n, const doubl
 int precond_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st)
 {
     const Topology &t = s->topo;
+    if (s->precond == FG_PRECOND_ILU0) return ilu0_apply_device(s, p, z, st);
     if (s->precond == FG_PRECOND_DIAG) {
         k_diag_apply<<<(t.n + 256) / 256, 256, 0, st>>>(s->invd64.as<double>(), t.n, p, z);
     } else if (s->precond == FG_PRECOND_BLOCKDIAG) {
@@ -426,6 +428,7 @@ int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c, const 
     FG_CUDA(cudaGetLastError());
     count_launches(1);
     s->blocks_ok = true;
+    s->csr_dirty = true;
     return convert_blocks(s, st);
 }
 

@@ -65,6 +65,8 @@ size_t fg_system::bytes() const
 {
     const DevMem *all[] = {&lm, &A64, &A32, &dinc_ptr, &dinc, &ninc_ptr, &ninc, &node_dof, &eorder, &perm,
                            &lm16, &pt_elem, &pt_dof, &pt_col, &pdofs, &rhs_f, &rhs_b,
+                           &csr_ia, &csr_ja, &csr_diag, &csr_inc_ptr, &csr_inc, &AA64, &AA32, &LU64, &LU32,
+                           &dinv64, &dinv32, &ilu_flags, &ilu_ctr,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
                            &ginvp, &Fe, &F64, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
                            &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
@@ -221,6 +223,7 @@ int fg_set_blocks(fg_system *s, const double *A)
     if ((r = upload_blocks_raw(s, s->F64.as<double>(), s->stream))) return r;
     FG_CUDA(cudaStreamSynchronize(s->stream));
     s->blocks_ok = true;
+    s->csr_dirty = true;
     return FG_OK;
 }
 
@@ -417,6 +420,34 @@ int fg_get_solution(const fg_system *s, double *X)
 }
 
 long long fg_launch_count(void) { return launch_total(); }
+
+int fg_set_operator(fg_system *s, int op)
+{
+    if (!s || (op != FG_OP_EBE && op != FG_OP_CSR)) { set_error("invalid operator"); return FG_ERR_ARG; }
+    if (op == FG_OP_CSR) {
+        int r = csr_setup(s);
+        if (r) return r;
+        if (s->blocks_ok && (r = csr_refresh(s, s->stream))) return r;
+        FG_CUDA(cudaStreamSynchronize(s->stream));
+    }
+    s->op = op;
+    return FG_OK;
+}
+
+int fg_get_csr(const fg_system *s, int *nnz, int *IA, int *JA, double *AA)
+{
+    if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (!s->csr_ok) { set_error("no CSR operator (fg_set_operator(FG_OP_CSR))"); return FG_ERR_STATE; }
+    fg_system *m = const_cast<fg_system *>(s);
+    int r = csr_refresh(m, s->stream);
+    if (r) return r;
+    if (nnz) *nnz = s->csr_nnz;
+    if (IA) FG_CUDA(cudaMemcpyAsync(IA, s->csr_ia.p, sizeof(int) * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToHost, s->stream));
+    if (JA) FG_CUDA(cudaMemcpyAsync(JA, s->csr_ja.p, sizeof(int) * (size_t)s->csr_nnz, cudaMemcpyDeviceToHost, s->stream));
+    if (AA) FG_CUDA(cudaMemcpyAsync(AA, s->AA64.p, sizeof(double) * (size_t)s->csr_nnz, cudaMemcpyDeviceToHost, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
 
 void *fg_system_stream(const fg_system *s) { return s ? (void *)s->stream : nullptr; }
 

@@ -47,6 +47,12 @@ struct fg_system {
     // resident right-hand side (internal numbering): F and M^-1 F
     fg::DevMem rhs_f, rhs_b;
     bool rhs_ok = false;
+    // assembled CSR operator and ILU(0)
+    int op = FG_OP_EBE;
+    bool csr_ok = false, csr_dirty = true;
+    int csr_nnz = 0, csr_w = 4;
+    fg::DevMem csr_ia, csr_ja, csr_diag, csr_inc_ptr, csr_inc, AA64, AA32, LU64, LU32, dinv64, dinv32, ilu_flags,
+        ilu_ctr;
     // host staging (pinned)
     double *h_vec = nullptr;   // 2*(n+1) doubles
     fg::Workspace ws;
@@ -56,9 +62,29 @@ struct fg_system {
 
 namespace fg {
 
+// CSR / ILU(0) (ilu.cu)
+int csr_setup(fg_system *s);
+int csr_refresh(fg_system *s, cudaStream_t st);
+int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st);
+int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st);
+int launch_ilu_solve(const SysDev *sys, const int2 *items, int nitems, int *flags, size_t flag_bytes, int *counter,
+                     int *err, int sel, int backward, int fp32, cudaStream_t st);
+
 // Patch-layout pointers of a system's descriptor (matvec).
 inline void set_patch_fields(SysDev &D, const fg_system *s)
 {
+    D.op = s->op;
+    D.csr_w = s->csr_w;
+    D.csr_ia = s->csr_ia.as<int>();
+    D.csr_ja = s->csr_ja.as<int>();
+    D.csr_diag = s->csr_diag.as<int>();
+    D.AA64 = s->AA64.as<double>();
+    D.AA32 = s->AA32.as<float>();
+    D.LU64 = s->LU64.as<double>();
+    D.LU32 = s->LU32.as<float>();
+    D.dinv64 = s->dinv64.as<double>();
+    D.dinv32 = s->dinv32.as<float>();
+    D.ilu_flag = nullptr;
     D.lm16 = s->lm16.as<unsigned short>();
     D.pt_elem = s->pt_elem.as<int>();
     D.pt_dof = s->pt_dof.as<int>();

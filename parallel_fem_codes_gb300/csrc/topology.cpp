@@ -439,3 +439,72 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
 }
 
 }  // namespace fg
+
+namespace fg {
+
+// Assembled CSR form (csr_Initialization.c:5-434): pattern of the free dofs
+// in the internal numbering (the reference renumbers its equations by the
+// same RCM, csr_Initialization.c:408-463), rows sorted, the diagonal slot of
+// each row, and for every slot the element contributions in reference
+// element order (csr_assembly.c sums them in that order).
+int build_csr(const Topology &t, CsrTopology &c)
+{
+    const int n = t.n, S = t.S;
+    c.n = n;
+    c.ia.assign(n + 1, 0);
+    std::vector<std::vector<int>> rows(n);
+    for (int e = 0; e < t.nel; ++e)
+        for (int a = 0; a < S; ++a) {
+            int r = t.lm[(size_t)e * S + a];
+            if (r == n) continue;
+            for (int b = 0; b < S; ++b) {
+                int q = t.lm[(size_t)e * S + b];
+                if (q != n) rows[t.iperm[r]].push_back(t.iperm[q]);
+            }
+        }
+    for (int i = 0; i < n; ++i) {
+        auto &v = rows[i];
+        std::sort(v.begin(), v.end());
+        v.erase(std::unique(v.begin(), v.end()), v.end());
+        c.ia[i + 1] = c.ia[i] + (int)v.size();
+    }
+    c.nnz = c.ia[n];
+    c.ja.resize(std::max(c.nnz, 1));
+    c.diag.assign(n, -1);
+    for (int i = 0; i < n; ++i) {
+        std::copy(rows[i].begin(), rows[i].end(), c.ja.begin() + c.ia[i]);
+        for (int k = c.ia[i]; k < c.ia[i + 1]; ++k)
+            if (c.ja[k] == i) c.diag[i] = k;
+        if (c.diag[i] < 0) { set_error("CSR row without a diagonal entry"); return FG_ERR_ARG; }
+        std::vector<int>().swap(rows[i]);
+    }
+    auto slot = [&](int r, int q) {
+        const int *b = c.ja.data() + c.ia[r], *e = c.ja.data() + c.ia[r + 1];
+        return (int)(std::lower_bound(b, e, q) - c.ja.data());
+    };
+    c.inc_ptr.assign(c.nnz + 1, 0);
+    for (int e = 0; e < t.nel; ++e)
+        for (int a = 0; a < S; ++a) {
+            int r = t.lm[(size_t)e * S + a];
+            if (r == n) continue;
+            for (int b = 0; b < S; ++b) {
+                int q = t.lm[(size_t)e * S + b];
+                if (q != n) c.inc_ptr[slot(t.iperm[r], t.iperm[q]) + 1]++;
+            }
+        }
+    for (int k = 0; k < c.nnz; ++k) c.inc_ptr[k + 1] += c.inc_ptr[k];
+    c.inc.resize(std::max(c.inc_ptr[c.nnz], 1));
+    std::vector<int> fill(c.inc_ptr.begin(), c.inc_ptr.end() - 1);
+    for (int e = 0; e < t.nel; ++e)
+        for (int a = 0; a < S; ++a) {
+            int r = t.lm[(size_t)e * S + a];
+            if (r == n) continue;
+            for (int b = 0; b < S; ++b) {
+                int q = t.lm[(size_t)e * S + b];
+                if (q != n) c.inc[fill[slot(t.iperm[r], t.iperm[q])]++] = t.epos[e] * 256 + a * 16 + b;
+            }
+        }
+    return FG_OK;
+}
+
+}  // namespace fg

@@ -15,12 +15,13 @@ import numpy as np
 from . import build as _build
 
 FG_OK = 0
-FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG = 0, 1, 2
+FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG, FG_PRECOND_ILU0 = 0, 1, 2, 3
+FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED = 64, 32
 FG_REORDER_NONE, FG_REORDER_RCM = 0, 1
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE",
-          5: "ERR_BREAKDOWN", 6: "ERR_NOTCONV", 7: "ERR_UNSUPPORTED"}
+          5: "ERR_BREAKDOWN", 6: "ERR_NOTCONV", 7: "ERR_UNSUPPORTED", 8: "ERR_TIMEOUT"}
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -117,6 +118,8 @@ def lib(build_if_missing: bool = True):
     L.fg_solve_resident.argtypes = [_vp, _c_int, ctypes.POINTER(SolverOpts), _vp]
     L.fg_get_solution.argtypes = [_vp, _f64p]
     L.fg_launch_count.restype = ctypes.c_longlong
+    L.fg_set_operator.argtypes = [_vp, _c_int]
+    L.fg_get_csr.argtypes = [_vp, ctypes.POINTER(_c_int), _vp, _vp, _vp]
     L.fg_system_stream.argtypes = [_vp]
     L.fg_system_stream.restype = _vp
     L.fg_bench_matvec.argtypes = [_vp, _c_int, _c_int, _c_int, ctypes.POINTER(_c_dbl), ctypes.POINTER(_c_dbl)]
@@ -224,6 +227,19 @@ class System:
         c = np.empty(self.mesh.nel, dtype=np.int32)
         check(lib().fg_system_get_colours(self._h, c))
         return c
+
+    def set_operator(self, op):
+        check(lib().fg_set_operator(self._h, op))
+
+    def csr(self):
+        """(IA, JA, AA) of the assembled operator in the internal (RCM) numbering."""
+        nnz = _c_int(0)
+        check(lib().fg_get_csr(self._h, ctypes.byref(nnz), None, None, None))
+        IA = np.empty(self.n + 1, dtype=np.int32)
+        JA = np.empty(max(nnz.value, 1), dtype=np.int32)
+        AA = np.empty(max(nnz.value, 1))
+        check(lib().fg_get_csr(self._h, None, IA.ctypes.data, JA.ctypes.data, AA.ctypes.data))
+        return IA, JA[:nnz.value], AA[:nnz.value]
 
     def set_blocks(self, A):
         check(lib().fg_set_blocks(self._h, np.ascontiguousarray(A, dtype=np.float64).reshape(-1)))
