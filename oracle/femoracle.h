@@ -123,6 +123,29 @@ int or_ebe_diag_solve(int nel, int S, const int *lm, const double *A, int NEQ,
                       double *Diag, double *invDiag, double *F,
                       int kmax, int lmax, double tol, double *X);
 
+/* ---- steady Navier-Stokes, SUPG/PSPG/LSIC (04_SS_NavierStokes_Equations) ---- */
+typedef struct {
+    double reynolds;       /* ReynoldsNumber (density 1, viscosity 1/Re)             */
+    const double *upresc;  /* [3*nnodes] prescribed u, v, p (read where type == 0)   */
+    const double *f1, *f2; /* [nnodes] body force at the nodes (NULL = 0)            */
+} or_ns_problem;
+
+/* Build_K_F_SUPG_PSPG (Picard tangent) + eval_U + ebe_assembly.  u holds the
+ * free dofs (neq); A receives 81 doubles per element (row-major), F the
+ * residual (NEQ+1 slots, sink 0). */
+void or_build_ns(int nnodes, int nel, const double *x, const double *y, const int *type,
+                 const int *invp, const int *ien, int neq, const or_ns_problem *prob,
+                 const double *u, double *A, double *F);
+
+/* Picard loop of 04_SS_NavierStokes_Equations/2D/01_CommonFiles/Process.c:6-62
+ * with EBE 9x9 blocks, BlockDiagDOF3 and GMRES: build, set up, solve for the
+ * increment s, u += s, until ||s|| / ||u|| <= nonlinear_tol.  Returns the
+ * number of nonlinear iterations; *last_delta receives ||s|| / ||u||. */
+int or_ns_process(int nnodes, int nel, const double *x, const double *y, const int *type,
+                  const int *invp, const int *ien, int neq, const or_ns_problem *prob,
+                  double solver_tol, double nonlinear_tol, int kmax, int lmax, int max_nonlinear,
+                  double *u, int *gmres_iterations, double *last_delta);
+
 /* ---- assembled CSR path and ILU(0) (oracle/csr_ilu.c) ---- */
 int  or_csr_pattern(int nel, const int *ien, const int *type, const int *invp, int NEQ,
                     const int *Perm, const int *invPerm, int *IA, int *JA);

@@ -14,6 +14,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libfemoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_sst.so")
+REF_NS_SO = os.path.join(HERE, "_ref", "libref_ns.so")
 REF_SRC = "/root/reference"
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -67,6 +68,12 @@ def lib():
                                            _f64p, ctypes.POINTER(_c_int)]
         L.or_ebe_diag_solve.argtypes = [_c_int, _c_int, _i32p, _f64p, _c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         _f64p, _f64p, _f64p, _c_int, _c_int, _c_dbl, _f64p]
+        L.or_build_ns.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                  ctypes.c_void_p, _f64p, _f64p, _f64p]
+        L.or_build_ns.restype = None
+        L.or_ns_process.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                    ctypes.c_void_p, _c_dbl, _c_dbl, _c_int, _c_int, _c_int,
+                                    _f64p, ctypes.POINTER(_c_int), ctypes.POINTER(_c_dbl)]
         _lib = L
     return _lib
 
@@ -100,7 +107,104 @@ def ref():
     return _ref
 
 
+_ref_ns = None
+
+
+def ref_ns():
+    """The reference's steady Navier-Stokes driver (oracle/_ref), or None."""
+    global _ref_ns
+    if _ref_ns is None and os.path.exists(REF_NS_SO):
+        R = ctypes.CDLL(REF_NS_SO)
+        mesh = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int]
+        R.fr_ns_lm.argtypes = mesh + [_i32p]
+        R.fr_ns_lm.restype = None
+        R.fr_ns_build.argtypes = mesh + [_c_dbl, _f64p, _c_int, _f64p, _f64p, _f64p]
+        R.fr_ns_build.restype = None
+        R.fr_ns_blockdiag.argtypes = mesh + [_f64p, _f64p, _f64p]
+        R.fr_ns_blockdiag.restype = None
+        R.fr_ns_ebemv.argtypes = mesh + [_f64p, _f64p, _f64p]
+        R.fr_ns_ebemv.restype = None
+        R.fr_ns_process.argtypes = mesh + [_c_dbl, _f64p, _c_int, _c_dbl, _c_dbl, _c_int, _c_int, _c_int,
+                                           _f64p, ctypes.POINTER(_c_int)]
+        _ref_ns = R
+    return _ref_ns
+
+
 # ---------------------------------------------------------------- helpers
+class _NSProblem(ctypes.Structure):
+    _fields_ = [("reynolds", _c_dbl), ("upresc", ctypes.POINTER(_c_dbl)),
+                ("f1", ctypes.POINTER(_c_dbl)), ("f2", ctypes.POINTER(_c_dbl))]
+
+
+def _ns_struct(p):
+    keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (p.upresc, p.f1, p.f2)]
+    P = ctypes.POINTER(_c_dbl)
+    s = _NSProblem(p.reynolds, keep[0].ctypes.data_as(P), keep[1].ctypes.data_as(P), keep[2].ctypes.data_as(P))
+    return s, keep
+
+
+def build_ns(prob, u=None):
+    """Build_K_F_SUPG_PSPG at the free-dof state u; returns (A[nel, 81], F[neq+1])."""
+    m = prob.mesh
+    u = np.zeros(m.neq) if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    A = np.empty(m.nel * 81)
+    F = np.empty(m.neq + 1)
+    s, keep = _ns_struct(prob)
+    lib().or_build_ns(*_mesh_args(m), ctypes.byref(s), u, A, F)
+    return A.reshape(m.nel, 81), F
+
+
+def ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=100):
+    """Picard loop; returns (u[neq], nonlinear its, GMRES its, last ||s||/||u||)."""
+    m = prob.mesh
+    u = np.zeros(m.neq + 1)
+    its, last = _c_int(0), _c_dbl(0.0)
+    s, keep = _ns_struct(prob)
+    nl = lib().or_ns_process(*_mesh_args(m), ctypes.byref(s), solver_tol, nonlinear_tol, kmax, lmax,
+                             max_nonlinear, u, ctypes.byref(its), ctypes.byref(last))
+    return u[:m.neq].copy(), nl, its.value, last.value
+
+
+def ref_ns_lm(mesh):
+    lm = np.empty(mesh.nel * 9, dtype=np.int32)
+    ref_ns().fr_ns_lm(*_mesh_args(mesh), lm)
+    return lm.reshape(mesh.nel, 9)
+
+
+def ref_ns_build(prob, u=None):
+    m = prob.mesh
+    u = np.zeros(m.neq) if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    A = np.empty(m.nel * 81)
+    F = np.empty(m.neq + 1)
+    ref_ns().fr_ns_build(*_mesh_args(m), prob.reynolds, np.ascontiguousarray(prob.coef.reshape(-1)),
+                         int(prob.lid), u, A, F)
+    return A.reshape(m.nel, 81), F
+
+
+def ref_ns_blockdiag(mesh, A, F):
+    F = np.array(F, dtype=np.float64, copy=True)
+    inv = np.empty(mesh.nnodes * 9)
+    ref_ns().fr_ns_blockdiag(*_mesh_args(mesh), np.ascontiguousarray(A, dtype=np.float64).reshape(-1), F, inv)
+    return inv, F
+
+
+def ref_ns_ebemv(mesh, A, P):
+    Q = np.zeros(mesh.neq + 1)
+    ref_ns().fr_ns_ebemv(*_mesh_args(mesh), np.ascontiguousarray(A, dtype=np.float64).reshape(-1),
+                         np.ascontiguousarray(P, dtype=np.float64), Q)
+    return Q
+
+
+def ref_ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=100):
+    m = prob.mesh
+    u = np.zeros(m.neq + 1)
+    its = _c_int(0)
+    ref_ns().fr_ns_process(*_mesh_args(m), prob.reynolds, np.ascontiguousarray(prob.coef.reshape(-1)),
+                           int(prob.lid), solver_tol, nonlinear_tol, kmax, lmax, max_nonlinear, u,
+                           ctypes.byref(its))
+    return u[:m.neq].copy(), its.value
+
+
 class _Problem(ctypes.Structure):
     _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl),
                 ("upresc", ctypes.POINTER(_c_dbl)), ("cau", _c_int)]

@@ -152,3 +152,67 @@ def random_blocks(nel: int, S: int, seed: int = 0, dominance: float = 4.0):
     A = rng.uniform(-1.0, 1.0, size=(nel, S, S))
     A[:, np.arange(S), np.arange(S)] += dominance
     return A.reshape(nel, S * S)
+
+
+@dataclasses.dataclass
+class NSProblem:
+    """Steady incompressible Navier-Stokes data (the FemFunctions callbacks
+    v1presc, v2presc, ppresc, f1ext, f2ext of
+    04_SS_NavierStokes_Equations/2D/01_CommonFiles/SSNavierStokesEquations.h:153-157)
+    evaluated at the nodes.  Each field is the affine function
+    coef[k, 0] + coef[k, 1] x + coef[k, 2] y (k: v1, v2, p, f1, f2); with
+    lid = True, v1 is the lid-driven-cavity rule of CAVITY_v1presc.c
+    (1 where |y - 1| <= 1e-15, else 0)."""
+    mesh: Mesh
+    reynolds: float
+    coef: np.ndarray       # float64[5, 3]
+    lid: bool
+    upresc: np.ndarray     # float64[nnodes*3]  prescribed u, v, p (read where type == 0)
+    f1: np.ndarray         # float64[nnodes]
+    f2: np.ndarray         # float64[nnodes]
+
+
+def _ns_fields(mesh: Mesh, coef: np.ndarray, lid: bool):
+    x, y = mesh.x, mesh.y
+    val = [coef[k, 0] + coef[k, 1] * x + coef[k, 2] * y for k in range(5)]
+    if lid:
+        val[0] = np.where(np.abs(y - 1.0) <= 1e-15, 1.0, 0.0)
+    up = np.stack(val[:3], axis=1).reshape(-1).astype(np.float64)
+    return up, val[3].astype(np.float64), val[4].astype(np.float64)
+
+
+def ns_problem(mesh: Mesh, reynolds: float, coef=None, lid=False) -> NSProblem:
+    coef = np.zeros((5, 3)) if coef is None else np.asarray(coef, dtype=np.float64).reshape(5, 3)
+    up, f1, f2 = _ns_fields(mesh, coef, lid)
+    return NSProblem(mesh, float(reynolds), coef, bool(lid), up, f1, f2)
+
+
+def cavity_problem(n_nodes_side: int, reynolds=1000.0, jitter=0.0, seed=3) -> NSProblem:
+    """Lid-driven cavity on the unit square with n x n nodes (the CAVITY set-up:
+    marks of Mesh_Generator/Structured_Mesh/meshGenerator.c:333-343, velocity
+    prescribed on the whole boundary, u = 1 on the lid y = 1, pressure pinned at
+    the centre node; n must be odd so that the centre is a node).  Interior
+    nodes other than the centre are moved uniformly by up to jitter*h in x and
+    y (numpy PCG64, seeded)."""
+    if n_nodes_side % 2 == 0:
+        raise ValueError("the cavity needs an odd number of nodes per side (pressure pin at the centre)")
+    M = n_nodes_side - 1
+    X, Y, ien = structured_mesh(M, M)
+    bnd = boundary_mask(X, Y)
+    centre = (np.abs(X - 0.5) <= 1e-15) & (np.abs(Y - 0.5) <= 1e-15)
+    if jitter:
+        rng = np.random.Generator(np.random.PCG64(seed))
+        h = 1.0 / M
+        keep = bnd | centre
+        dx = rng.uniform(-jitter * h, jitter * h, X.shape)
+        dy = rng.uniform(-jitter * h, jitter * h, Y.shape)
+        X = X + np.where(keep, 0.0, dx)
+        Y = Y + np.where(keep, 0.0, dy)
+    type_ = np.ones((X.shape[0], 3), dtype=np.int32)
+    type_[bnd, 0] = 0
+    type_[bnd, 1] = 0
+    type_[centre, 2] = 0
+    type_ = type_.reshape(-1)
+    invp, neq = number_dofs(type_)
+    mesh = Mesh(X, Y, ien, 3, type_, invp, neq)
+    return ns_problem(mesh, reynolds, lid=True)

@@ -6,7 +6,10 @@ It writes tests/golden/sst_*.npz: mesh, connectivity (lm, Perm, invPerm,
 bandwidths), element blocks and right-hand side at u = 0, one Diag +
 GMRES(30) solve, and the full CAU Process loop (solution and GMRES
 iterations), all computed by the reference's Fill_LM, Permutation_of_LM,
-Build_K_F_SUPG, Diag_precond_EBE_setup, pgmres and Process.
+Build_K_F_SUPG, Diag_precond_EBE_setup, pgmres and Process; and
+tests/golden/ns_*.npz: the steady Navier-Stokes driver's Fill_LM,
+Build_K_F_SUPG_PSPG at a state u, BlockDiagDOF3_precond_EBE_setup,
+ebemvNDOF3 and (cavity) the Picard Process loop.
 """
 import os
 import sys
@@ -48,6 +51,33 @@ def main():
             Fp=Fp[: m.neq], Diag=Diag[: m.neq], X=X[: m.neq], gmres_its=it,
             U=U, process_its=its)
         print(name, "neq", m.neq, "gmres", it, "process gmres", its)
+    for name, (prob, seed, process) in ns_cases().items():
+        m = prob.mesh
+        rng = np.random.Generator(np.random.PCG64(seed))
+        u = rng.standard_normal(m.neq) if seed else np.zeros(m.neq)
+        lm = O.ref_ns_lm(m)
+        A, F = O.ref_ns_build(prob, u)
+        inv, Fp = O.ref_ns_blockdiag(m, A, F)
+        P = rng.standard_normal(m.neq + 1)
+        P[m.neq] = 0.0
+        Q = O.ref_ns_ebemv(m, A, P)
+        extra = {}
+        if process:
+            U, its = O.ref_ns_process(prob, 1e-10, 1e-6, 30, 1000, 30)
+            extra = dict(U=U, process_its=its)
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            x=m.x, y=m.y, ien=m.ien, type=m.type, invp=m.invp, neq=m.neq, reynolds=prob.reynolds,
+            coef=prob.coef, lid=int(prob.lid), u=u, lm=lm, A=A, F=F, inv=inv, Fp=Fp, P=P, Q=Q, **extra)
+        print(name, "neq", m.neq, extra.get("process_its"))
+
+
+def ns_cases():
+    """name: (problem, seed of the state u (0: u = 0), run the Process loop)."""
+    cav = G.cavity_problem(9, reynolds=100.0)
+    mesh = G.multi_dof_mesh(9, 3, seed=2, jitter=0.2)
+    aff = G.ns_problem(mesh, 50.0, np.random.Generator(np.random.PCG64(5)).standard_normal((5, 3)))
+    return {"ns_9_cavity": (cav, 0, True), "ns_9_affine": (aff, 6, False)}
 
 
 if __name__ == "__main__":
