@@ -234,10 +234,40 @@ typedef struct {
     int gmres_iterations;
     double seconds;
     double true_rel_residual;  /* of the last linear solve */
+    double nonlinear_residual; /* the loop's last stopping quantity */
 } fg_process_stats;
 int fg_transport_process(fg_system *s, const fg_transport_coeffs *c,
                          const fg_solver_opts *opts, double nonlinear_tol,
                          int max_nonlinear, double *U, fg_process_stats *stats);
+
+/* ---- steady incompressible Navier-Stokes, SUPG/PSPG/LSIC (NDOF = 3) ----
+ * Replaces Build_K_F_SUPG_PSPG.c:8-669 (with eval_U.c:3-35 and
+ * ebe_assembly.c) and the Picard loop of
+ * 04_SS_NavierStokes_Equations/2D/01_CommonFiles/Process.c:6-62 for a system
+ * created with ndof = 3 (dofs u, v, p per node). */
+typedef struct {
+    double reynolds;   /* ReynoldsNumber: density 1, viscosity 1/Re          */
+    int precond;       /* FG_PRECOND_BLOCKDIAG (BlockDiagDOF3), FG_PRECOND_DIAG
+                          (accumulating, as Diag_precond_EBE_setup.c) or
+                          FG_PRECOND_NONE                                     */
+} fg_ns_coeffs;
+
+/* Node coordinates, the prescribed (u, v, p) of every node (upresc[3*node+k],
+ * read where dof k of the node is Dirichlet: v1presc/v2presc/ppresc at the
+ * node) and the body force at the nodes (f1ext/f2ext; NULL = 0). */
+int fg_ns_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc,
+                       const double *f1, const double *f2);
+/* Build_K_F_SUPG_PSPG at the free-dof state u (host, n entries, NULL = 0):
+ * the 9x9 Picard tangent stays on the device; F (host, n+1) receives the
+ * residual when not NULL. */
+int fg_ns_assemble(fg_system *s, const fg_ns_coeffs *c, const double *u, double *F);
+/* Picard loop: assemble at u, preconditioner set-up, GMRES for the increment
+ * s, u += s, until ||s|| / ||u|| <= nonlinear_tol or max_nonlinear
+ * iterations.  u (host, n entries) is the initial state on entry (the
+ * reference starts from 0) and the solution on return; the state stays on the
+ * device between iterations. */
+int fg_ns_process(fg_system *s, const fg_ns_coeffs *c, const fg_solver_opts *opts, double nonlinear_tol,
+                  int max_nonlinear, double *u, fg_process_stats *stats);
 
 /* ---- request server: continuous batching of transport solves ----
  * A worker thread owns one batch.  Requests (a system whose geometry is set,

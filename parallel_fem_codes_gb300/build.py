@@ -26,6 +26,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("server.cu", []),
     ("ilu.cu", ["-fmad=false"]),
+    ("ns.cu", ["-fmad=false"]),
 ]
 
 

@@ -68,7 +68,7 @@ size_t fg_system::bytes() const
                            &csr_ia, &csr_ja, &csr_diag, &csr_inc_ptr, &csr_inc, &AA64, &AA32, &LU64, &LU32,
                            &dinv64, &dinv32, &ilu_flags, &ilu_ctr,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
-                           &ginvp, &Fe, &F64, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
+                           &ginvp, &Fe, &F64, &gf1, &gf2, &ns_u, &ns_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
                            &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
     size_t b = 0;
     for (auto *m : all) b += m->bytes;
@@ -556,6 +556,111 @@ int fg_transport_process(fg_system *s, const fg_transport_coeffs *c, const fg_so
         stats->gmres_iterations = gmres;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         stats->true_rel_residual = last_res;
+        stats->nonlinear_residual = normdiff / normu;
+    }
+    return FG_OK;
+}
+
+int fg_ns_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc, const double *f1,
+                       const double *f2)
+{
+    if (!s || !x || !y || !upresc) { set_error("NULL argument"); return FG_ERR_ARG; }
+    const Topology &t = s->topo;
+    if (t.ndof != 3) { set_error("Navier-Stokes geometry needs a system with ndof == 3"); return FG_ERR_UNSUPPORTED; }
+    const size_t nn = (size_t)t.nnodes;
+    std::vector<double> vx(x, x + nn), vy(y, y + nn), vu(upresc, upresc + 3 * nn);
+    std::vector<double> v1 = f1 ? std::vector<double>(f1, f1 + nn) : std::vector<double>(nn, 0.0);
+    std::vector<double> v2 = f2 ? std::vector<double>(f2, f2 + nn) : std::vector<double>(nn, 0.0);
+    int r;
+    if ((r = upload(s->gx, vx)) || (r = upload(s->gy, vy)) || (r = upload(s->gup, vu)) || (r = upload(s->gf1, v1)) ||
+        (r = upload(s->gf2, v2)) || (r = s->Fe.alloc(8 * (size_t)9 * s->nel_pad)))
+        return r;
+    s->ns_geometry_ok = true;
+    return FG_OK;
+}
+
+int fg_ns_assemble(fg_system *s, const fg_ns_coeffs *c, const double *u, double *F)
+{
+    if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if (u) {
+        std::memcpy(s->h_vec, u, 8 * (size_t)s->topo.n);
+        s->h_vec[s->topo.n] = 0.0;
+        if ((r = vec_in(s, s->h_vec, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
+    } else {
+        FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    }
+    if ((r = ns_assemble_device(s, c->reynolds, s->ws.t64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
+    if (F) {
+        if ((r = vec_out(s, s->ws.u64.as<double>(), F, s->ws.r64.as<double>()))) return r;
+    }
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+// Process.c:6-62 of the Navier-Stokes driver with the state, the residual and
+// the increment kept on the device: per iteration one assembly, one
+// preconditioner set-up on the residual, one batched-engine solve and one
+// update kernel; only the two norms come back to the host.
+int fg_ns_process(fg_system *s, const fg_ns_coeffs *c, const fg_solver_opts *o, double nonlinear_tol,
+                  int max_nonlinear, double *u, fg_process_stats *stats)
+{
+    if (!s || !c || !o || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (c->precond != FG_PRECOND_NONE && c->precond != FG_PRECOND_DIAG && c->precond != FG_PRECOND_BLOCKDIAG) {
+        set_error("Navier-Stokes preconditioner must be NONE, DIAG or BLOCKDIAG");
+        return FG_ERR_ARG;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    const int n = s->topo.n;
+    fg_system *one[1] = {s};
+    SolveConfig cfg;
+    int r = batch_config(one, 1, o, cfg);
+    if (r) return r;
+    cfg.device_io = 1;
+    if ((r = ensure_io(s)) || (r = stage(s, s->rhs_f, 8 * (size_t)s->n_pad)) ||
+        (r = stage(s, s->rhs_b, 8 * (size_t)s->n_pad)) || (r = stage(s, s->ns_u, 8 * (size_t)s->n_pad)) ||
+        (r = stage(s, s->ns_part, ns_update_scratch_bytes())))
+        return r;
+    std::memcpy(s->h_vec, u, 8 * (size_t)n);
+    s->h_vec[n] = 0.0;
+    FG_CUDA(cudaMemsetAsync(s->ns_u.p, 0, s->ns_u.bytes, s->stream));
+    if ((r = vec_in(s, s->h_vec, s->ns_u.as<double>(), s->ws.r64.as<double>()))) return r;
+    // a fresh run starts from a zero diagonal (Preprocess.c:316 callocs it)
+    if (c->precond == FG_PRECOND_DIAG) FG_CUDA(cudaMemsetAsync(s->diag.p, 0, s->diag.bytes, s->stream));
+    double *part = s->ns_part.as<double>(), *norms = part + (s->ns_part.bytes / 8 - 2);
+    double delta = nonlinear_tol + 1.0, last_res = NAN;
+    int it = 0, gmres = 0;
+    while (delta > nonlinear_tol && it < max_nonlinear) {
+        ++it;
+        if ((r = ns_assemble_device(s, c->reynolds, s->ns_u.as<double>(), s->rhs_f.as<double>(), s->stream))) return r;
+        FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, 8 * (size_t)s->n_pad, cudaMemcpyDeviceToDevice, s->stream));
+        int flags = c->precond == FG_PRECOND_DIAG ? FG_SETUP_ACCUMULATE : 0;
+        if ((r = precond_setup_device(s, c->precond, flags, s->rhs_b.as<double>(), s->stream))) return r;
+        s->rhs_ok = true;
+        cfg.precond = s->precond;
+        std::vector<BatchMember> mem{{s, s->rhs_b.as<double>(), s->rhs_f.as<double>(), nullptr}};
+        fg_solve_stats st{};
+        if ((r = solve_batch(mem, cfg, &st, s->stream))) return r;
+        gmres += st.iterations;
+        last_res = st.true_rel_residual;
+        if ((r = ns_update_device(s, s->ns_u.as<double>(), s->ws.x.as<double>(), part, norms, s->stream))) return r;
+        FG_CUDA(cudaMemcpyAsync(s->h_vec, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+        FG_CUDA(cudaStreamSynchronize(s->stream));
+        delta = std::sqrt(s->h_vec[0]) / std::sqrt(s->h_vec[1]);
+    }
+    if ((r = vec_out(s, s->ns_u.as<double>(), s->h_vec, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    std::memcpy(u, s->h_vec, 8 * (size_t)n);
+    if (stats) {
+        stats->nonlinear_iterations = it;
+        stats->gmres_iterations = gmres;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        stats->true_rel_residual = last_res;
+        stats->nonlinear_residual = delta;
     }
     return FG_OK;
 }

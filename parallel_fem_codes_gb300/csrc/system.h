@@ -44,6 +44,9 @@ struct fg_system {
     // geometry (device assembly)
     fg::DevMem gx, gy, gup, gien, gtype, ginvp, Fe, F64;
     bool geometry_ok = false;
+    // Navier-Stokes: nodal body force, Picard state and norm scratch (gup holds 3 values per node)
+    fg::DevMem gf1, gf2, ns_u, ns_part;
+    bool ns_geometry_ok = false;
     // resident right-hand side (internal numbering): F and M^-1 F
     fg::DevMem rhs_f, rhs_b;
     bool rhs_ok = false;
@@ -154,6 +157,11 @@ int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const ECh
 
 // Matvec on device vectors in internal numbering (precision 64 or 32).
 int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaStream_t st);
+
+// Navier-Stokes (ns.cu)
+int ns_assemble_device(fg_system *s, double reynolds, const double *u_dev, double *F_dev, cudaStream_t st);
+int ns_update_device(fg_system *s, double *u_dev, const double *s_dev, double *part, double *out, cudaStream_t st);
+size_t ns_update_scratch_bytes();
 
 // Set-up kernels (setup.cu)
 int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaStream_t st);

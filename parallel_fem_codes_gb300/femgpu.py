@@ -60,7 +60,11 @@ class TransportCoeffs(ctypes.Structure):
 
 class ProcessStats(ctypes.Structure):
     _fields_ = [("nonlinear_iterations", _c_int), ("gmres_iterations", _c_int), ("seconds", _c_dbl),
-                ("true_rel_residual", _c_dbl)]
+                ("true_rel_residual", _c_dbl), ("nonlinear_residual", _c_dbl)]
+
+
+class NSCoeffs(ctypes.Structure):
+    _fields_ = [("reynolds", _c_dbl), ("precond", _c_int)]
 
 
 class ServerOpts(ctypes.Structure):
@@ -126,6 +130,10 @@ def lib(build_if_missing: bool = True):
     L.fg_transport_prepare.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), _vp]
     L.fg_transport_process.argtypes = [_vp, ctypes.POINTER(TransportCoeffs), ctypes.POINTER(SolverOpts), _c_dbl,
                                        _c_int, _f64p, ctypes.POINTER(ProcessStats)]
+    L.fg_ns_set_geometry.argtypes = [_vp, _f64p, _f64p, _f64p, _vp, _vp]
+    L.fg_ns_assemble.argtypes = [_vp, ctypes.POINTER(NSCoeffs), _vp, _vp]
+    L.fg_ns_process.argtypes = [_vp, ctypes.POINTER(NSCoeffs), ctypes.POINTER(SolverOpts), _c_dbl, _c_int, _f64p,
+                                ctypes.POINTER(ProcessStats)]
     L.fg_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerOpts)]
     L.fg_server_submit.argtypes = [_vp, _vp, ctypes.POINTER(TransportCoeffs), ctypes.c_ulonglong]
     L.fg_server_poll.argtypes = [_vp, _vp, _c_int, ctypes.POINTER(_c_int)]
@@ -311,6 +319,42 @@ class System:
         check(lib().fg_transport_process(self._h, ctypes.byref(c), ctypes.byref(o), nonlinear_tol, max_nonlinear,
                                          U, ctypes.byref(st)))
         return U, {k: getattr(st, k) for k, _ in st._fields_}
+
+    # ---- steady Navier-Stokes (ndof = 3)
+    def ns_set_geometry(self, prob):
+        f1 = np.ascontiguousarray(prob.f1, dtype=np.float64)
+        f2 = np.ascontiguousarray(prob.f2, dtype=np.float64)
+        check(lib().fg_ns_set_geometry(self._h, np.ascontiguousarray(self.mesh.x, dtype=np.float64),
+                                       np.ascontiguousarray(self.mesh.y, dtype=np.float64),
+                                       np.ascontiguousarray(prob.upresc, dtype=np.float64),
+                                       f1.ctypes.data, f2.ctypes.data))
+
+    def ns_assemble(self, prob, u=None):
+        """Build_K_F_SUPG_PSPG at u (free dofs, reference numbering); returns F (n+1)."""
+        c = NSCoeffs(prob.reynolds, FG_PRECOND_BLOCKDIAG)
+        F = np.empty(self.n + 1)
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        check(lib().fg_ns_assemble(self._h, ctypes.byref(c), _ptr(uu), F.ctypes.data))
+        return F
+
+    def ns_process(self, prob, u0=None, kmax=30, lmax=1000, tol=1e-10, nonlinear_tol=1e-3, max_nonlinear=100,
+                   precision=FG_PREC_FP64, inner_tol=0.0, precond=FG_PRECOND_BLOCKDIAG):
+        """Picard loop from u0 (default 0); returns (u[n], stats)."""
+        c = NSCoeffs(prob.reynolds, precond)
+        o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+        u = np.zeros(self.n) if u0 is None else np.array(u0, dtype=np.float64, copy=True)
+        st = ProcessStats()
+        check(lib().fg_ns_process(self._h, ctypes.byref(c), ctypes.byref(o), nonlinear_tol, max_nonlinear, u,
+                                  ctypes.byref(st)))
+        return u, {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def ns_system(prob) -> System:
+    """A System (ndof = 3, node-order numbering) with the geometry, prescribed
+    values and body force of a Navier-Stokes problem."""
+    s = System(prob.mesh, reorder=False)
+    s.ns_set_geometry(prob)
+    return s
 
 
 def _coeffs(prob):
