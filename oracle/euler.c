@@ -1,0 +1,357 @@
+/*
+ * Compressible Euler, SUPG + CAU on P1 triangles with conservative
+ * variables (rho, rho u, rho v, rho E): CPU restatement of
+ * 03_Euler_Equations/2D/01_CommonFiles/Build_M_K_F_SUPG.c:6-1057 with
+ * Ax_Ay_calculations.c:3-98, Delta_CAU.c:4-84, eval_U_dU.c:3-59 and
+ * ebe_assembly.c, and of the predictor/multicorrector time loop of
+ * 00_CommonFiles/Time_Integration/Predictor_Old.c:6-134 with the stop tests
+ * of Criteria.c:3-80.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker of the GPU library).
+ *
+ * The reference writes every product of the Jacobians (AxAx, AxAy, AyAx,
+ * AyAy) and the convection blocks (b_i Ax + c_i Ay)/6 term by term, leaving
+ * out the terms that multiply a structural zero of Ax and Ay.  Here they are
+ * formed as plain 4x4 products and sums over k = 0..3: the extra terms are
+ * exact zeros, and adding an exact zero leaves a sum unchanged, so every
+ * entry rounds exactly as the reference's.  The one entry the reference
+ * never sets, Ay[0][3] (Ax_Ay_calculations.c:33-36 sets Ay[0][0] twice), is
+ * a structural zero it never reads; it is set to 0 here.
+ * pow(x, 2) is kept where the reference uses it (tau, speed of sound).
+ */
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "femoracle.h"
+
+/* Jacobians of the Euler fluxes at the barycentric state Ub
+ * (Ax_Ay_calculations.c: dimensionless :3-48, dimensional :50-98). */
+static void eu_jacobians(double gamma, double mach, int dimensionless, const double Ub[4],
+                         double Ax[4][4], double Ay[4][4])
+{
+    double v1 = Ub[1] / Ub[0], v2 = Ub[2] / Ub[0], E = Ub[3] / Ub[0];
+    memset(Ax, 0, 16 * sizeof(double));
+    memset(Ay, 0, 16 * sizeof(double));
+    Ax[0][1] = 1.0;
+    Ay[0][2] = 1.0;
+    Ax[1][1] = (3.0 - gamma) * v1;
+    Ax[1][2] = -(gamma - 1.0) * v2;
+    Ax[2][0] = -v1 * v2;
+    Ax[2][1] = v2;
+    Ax[2][2] = v1;
+    Ax[3][3] = gamma * v1;
+    Ay[2][1] = -(gamma - 1.0) * v1;
+    Ay[2][2] = (3.0 - gamma) * v2;
+    Ay[3][3] = gamma * v2;
+    if (dimensionless) {
+        double nv = v1 * v1 + v2 * v2, e2 = mach * mach;
+        Ax[1][0] = -(v1 * v1) + ((gamma - 1) * nv * 0.5);
+        Ax[1][3] = (gamma - 1.0) / e2;
+        Ax[3][0] = -v1 * (gamma * E - ((gamma - 1.0) * e2 * nv));
+        Ax[3][1] = gamma * E - (gamma - 1.0) * e2 * (0.5 * nv + v1 * v1);
+        Ax[3][2] = -(gamma - 1.0) * e2 * v1 * v2;
+        Ay[2][0] = -(v2 * v2) + (((gamma - 1.0) * nv * 0.5));
+        Ay[3][0] = -v2 * (gamma * E - (gamma - 1.0) * e2 * nv);
+        Ay[3][2] = gamma * E - (gamma - 1.0) * e2 * (0.5 * nv + v2 * v2);
+    } else {
+        double rho = Ub[0], nU = (Ub[1] * Ub[1]) + (Ub[2] * Ub[2]);
+        Ax[1][0] = -(v1 * v1) + (((gamma - 1) * nU * 0.5) / (rho * rho));
+        Ax[1][3] = gamma - 1.0;
+        Ax[3][0] = (-gamma * v1 * E) + ((gamma - 1.0) * v1 * (nU / (rho * rho)));
+        Ax[3][1] = (gamma * E) - ((gamma - 1.0) * 0.5 * ((nU / (rho * rho)) + (2.0 * v1 * v1)));
+        Ax[3][2] = -((gamma - 1.0) * v1 * v2);
+        Ay[2][0] = -(v2 * v2) + (((gamma - 1.0) * nU * 0.5) / (rho * rho));
+        Ay[3][0] = (-gamma * v2 * E) + (((gamma - 1.0) * v2 * nU) / (rho * rho));
+        Ay[3][2] = (gamma * E) - ((gamma - 1.0) * 0.5 * ((nU / (rho * rho)) + (2.0 * v2 * v2)));
+    }
+    Ay[1][0] = Ax[2][0];
+    Ay[1][1] = v2;
+    Ay[1][2] = v1;
+    Ay[2][3] = Ax[1][3];
+    Ay[3][1] = Ax[3][2];
+}
+
+/* P = X Y, sums over k in ascending order */
+static void mul4(double X[4][4], double Y[4][4], double P[4][4])
+{
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) {
+            double s = X[r][0] * Y[0][c];
+            for (int k = 1; k < 4; k++) s += X[r][k] * Y[k][c];
+            P[r][c] = s;
+        }
+}
+
+/* w^T A0^-1 w with the symmetric expansion of Delta_CAU.c:37-63 */
+static double a0_norm2(double A0[4][4], const double w[4])
+{
+    return w[0] * (A0[0][0] * w[0] + 2.0 * A0[0][1] * w[1] + 2.0 * A0[0][2] * w[2] + 2.0 * A0[0][3] * w[3]) +
+           w[1] * (A0[1][1] * w[1] + 2.0 * A0[1][2] * w[2] + 2.0 * A0[1][3] * w[3]) +
+           w[2] * (A0[2][2] * w[2] + 2.0 * A0[2][3] * w[3]) +
+           w[3] * A0[3][3] * w[3];
+}
+
+/* CAU shock-capturing coefficient (Delta_CAU.c:4-84) */
+static double eu_delta_cau(double tolerance, const double gx[4], const double gy[4], double Ax[4][4],
+                           double Ay[4][4], double A0[4][4], const double dUb[4], const double b[3],
+                           const double c[3], double twoArea)
+{
+    double Agx[4], Agy[4], kx[4], ky[4], L[4];
+    for (int r = 0; r < 4; r++) {
+        double sx = Ax[r][0] * gx[0], sy = Ay[r][0] * gy[0];
+        for (int k = 1; k < 4; k++) { sx += Ax[r][k] * gx[k]; sy += Ay[r][k] * gy[k]; }
+        Agx[r] = sx;
+        Agy[r] = sy;
+    }
+    for (int i = 0; i < 4; i++) {
+        kx[i] = (b[0] * gx[i] + c[0] * gy[i]) / twoArea;
+        ky[i] = (b[1] * gx[i] + c[1] * gy[i]) / twoArea;
+    }
+    double nk = sqrt(a0_norm2(A0, kx) + a0_norm2(A0, ky));
+    for (int i = 0; i < 4; i++) L[i] = dUb[i] + Agx[i] + Agy[i];
+    double nL = sqrt(a0_norm2(A0, L));
+    double ng = sqrt(a0_norm2(A0, gx) + a0_norm2(A0, gy));
+    return ng >= tolerance ? nL / nk : 0.0;
+}
+
+/* One element: Ae = Me + alpha dt Ke (12x12, row-major) and Re = -Me dUe - Ke Ue. */
+static void eu_element(const or_euler_problem *pb, const double X[3], const double Y[3], const double Ue[12],
+                       const double dUe[12], double Ae[144], double Re[12])
+{
+    const double third = 1.0 / 3.0, sixth = 1.0 / 6.0;
+    const double gamma = pb->gamma, alpha = pb->alpha, dt = pb->dt;
+    double b[3] = {Y[1] - Y[2], Y[2] - Y[0], Y[0] - Y[1]};
+    double c[3] = {X[2] - X[1], X[0] - X[2], X[1] - X[0]};
+    double twoArea = fabs(c[2] * b[1] - c[1] * b[2]);
+    double Area = 0.5 * twoArea;
+    double Ub[4], dUb[4], gx[4], gy[4];
+    int i, j, r, q;
+    for (i = 0; i < 4; i++) {
+        Ub[i] = (Ue[i] + Ue[i + 4] + Ue[i + 8]) * third;
+        dUb[i] = (dUe[i] + dUe[i + 4] + dUe[i + 8]) * third;
+    }
+    for (i = 0; i < 4; i++) {
+        gx[i] = (Ue[i] * b[0] + Ue[i + 4] * b[1] + Ue[i + 8] * b[2]) / twoArea;
+        gy[i] = (Ue[i] * c[0] + Ue[i + 4] * c[1] + Ue[i + 8] * c[2]) / twoArea;
+    }
+    double v1 = Ub[1] / Ub[0], v2 = Ub[2] / Ub[0], E = Ub[3] / Ub[0];
+    double nU = (Ub[1] * Ub[1]) + (Ub[2] * Ub[2]);
+    double Ax[4][4], Ay[4][4];
+    eu_jacobians(gamma, pb->mach, pb->dimensionless, Ub, Ax, Ay);
+
+    /* inverse Riemannian metric A0^-1 in entropy variables (:131-158) */
+    double rho_i = Ub[3] - ((nU * 0.5) / Ub[0]);
+    double V2 = Ub[1] / rho_i, V3 = Ub[2] / rho_i, V4 = (-Ub[0]) / rho_i;
+    double re = -1.0 / (rho_i * V4);
+    double k1 = (V2 * V2 + V3 * V3) * 0.5 / V4;
+    double A0[4][4];
+    A0[0][0] = re * (k1 * k1 + gamma);
+    A0[0][1] = re * (k1 * V2);
+    A0[0][2] = re * (k1 * V3);
+    A0[0][3] = re * ((k1 + 1.0) * V4);
+    A0[1][1] = re * (V2 * V2 - V4);
+    A0[1][2] = re * (V2 * V3);
+    A0[1][3] = re * (V2 * V4);
+    A0[2][2] = re * (V3 * V3 - V4);
+    A0[2][3] = re * (V3 * V4);
+    A0[3][3] = re * V4 * V4;
+    A0[1][0] = A0[0][1]; A0[2][0] = A0[0][2]; A0[3][0] = A0[0][3];
+    A0[2][1] = A0[1][2]; A0[3][1] = A0[1][3]; A0[3][2] = A0[2][3];
+
+    /* AiAj products (:160-234) */
+    double Axx[4][4], Axy[4][4], Ayx[4][4], Ayy[4][4];
+    mul4(Ax, Ax, Axx);
+    mul4(Ax, Ay, Axy);
+    mul4(Ay, Ax, Ayx);
+    mul4(Ay, Ay, Ayy);
+
+    double delta = eu_delta_cau(pb->tolerance, gx, gy, Ax, Ay, A0, dUb, b, c, twoArea);
+
+    /* SUPG tau (:240-269) */
+    double betax = 2.0 * (gx[0] * Ub[0] + gx[1] * Ub[1] + gx[2] * Ub[2] + gx[3] * Ub[3]);
+    double betay = 2.0 * (gy[0] * Ub[0] + gy[1] * Ub[1] + gy[2] * Ub[2] + gy[3] * Ub[3]);
+    double betaxy = sqrt(betax * betax + betay * betay);
+    if (betaxy != 0.0) { betax = betax / betaxy; betay = betay / betaxy; }
+    double h = sqrt(twoArea);
+    double avb = fabs(v1 * betax + v2 * betay);
+    double cs = sqrt(gamma * (gamma - 1.0) * (E - 0.5 * (pow(v1, 2) + pow(v2, 2))));
+    double CFL = ((cs + avb) * dt) / h;
+    double psi = (2.0 * alpha * CFL) * (1.0 / (1.0 + 2.0 * alpha * CFL));
+    double tau_d = delta / pow((cs + avb), 2);
+    double tau_a = h / (2.0 * (cs + avb));
+    double tau_t = (2.0 / (3.0 * (1.0 + 2.0 * alpha * CFL))) * tau_a;
+    double tau = tau_t + psi * (tau_a - tau_d);
+    if (tau < 0.0) tau = 0.0;
+
+    /* convection blocks C_i = (b_i Ax + c_i Ay)/6 (Galerkin, :277-334) and
+     * the SUPG blocks a_i^x = b_i AxAx + c_i AyAx, a_i^y = b_i AxAy + c_i AyAy (:610-733) */
+    double C[3][4][4], ax[3][4][4], ay[3][4][4];
+    for (i = 0; i < 3; i++)
+        for (r = 0; r < 4; r++)
+            for (q = 0; q < 4; q++) {
+                C[i][r][q] = (b[i] * Ax[r][q] + c[i] * Ay[r][q]) * sixth;
+                ax[i][r][q] = b[i] * Axx[r][q] + c[i] * Ayx[r][q];
+                ay[i][r][q] = b[i] * Axy[r][q] + c[i] * Ayy[r][q];
+            }
+    double Mg1 = Area * sixth, Mg2 = Area / 12.0;
+    double t4a = tau / (4 * Area);
+    double d4a = delta / (4.0 * Area);
+    double Kcau[3][3];
+    for (i = 0; i < 3; i++)
+        for (j = i + 1; j < 3; j++)
+            Kcau[i][j] = Kcau[j][i] = d4a * (b[i] * b[j] + c[i] * c[j]);
+
+    /* blocks (row node i, column node j) of Me (:349-561) and Ke (:770-1030) */
+    double Me[12][12], Ke[12][12];
+    for (i = 0; i < 3; i++) {
+        int o1 = i == 0 ? 1 : 0, o2 = i == 2 ? 1 : 2;       /* the other two nodes, ascending */
+        for (j = 0; j < 3; j++)
+            for (r = 0; r < 4; r++)
+                for (q = 0; q < 4; q++) {
+                    double mpg = C[i][r][q] * tau;
+                    Me[4 * i + r][4 * j + q] = r == q ? (i == j ? Mg1 : Mg2) + mpg : mpg;
+                    double kg = C[j][r][q];
+                    if (i == j) {
+                        double p1 = t4a * (b[o1] * ax[i][r][q] + c[o1] * ay[i][r][q]);
+                        double p2 = t4a * (b[o2] * ax[i][r][q] + c[o2] * ay[i][r][q]);
+                        double k = kg - (p1 + p2);
+                        Ke[4 * i + r][4 * j + q] = r == q ? k - (Kcau[i][o1] + Kcau[i][o2]) : k;
+                    } else {
+                        double p = t4a * (b[j] * ax[i][r][q] + c[j] * ay[i][r][q]);
+                        Ke[4 * i + r][4 * j + q] = r == q ? kg + p + Kcau[i][j] : kg + p;
+                    }
+                }
+    }
+    /* local residual and the matrix of the corrector (:1033-1047) */
+    double adt = alpha * dt;
+    for (r = 0; r < 12; r++) {
+        double m = 0, k = 0;
+        for (q = 0; q < 12; q++) {
+            m += Me[r][q] * dUe[q];
+            k += Ke[r][q] * Ue[q];
+            Ae[12 * r + q] = Me[r][q] + adt * Ke[r][q];
+        }
+        Re[r] = -m - k;
+    }
+}
+
+void or_build_euler(int nnodes, int nel, const double *x, const double *y, const int *type,
+                    const int *invp, const int *ien, int neq, const or_euler_problem *prob,
+                    const double *u, const double *du, double *A, double *R)
+{
+    int E, v, k, NEQ = neq;
+    size_t nn = (size_t)(nnodes ? nnodes : 1);
+    double *U = malloc(sizeof(double) * 4 * nn), *dU = malloc(sizeof(double) * 4 * nn);
+    /* eval_U_dU.c:3-59 */
+    for (v = 0; v < nnodes; v++)
+        for (k = 0; k < 4; k++) {
+            long d = 4L * v + k;
+            if (type[d] > 0) { U[d] = u[invp[d]]; dU[d] = du[invp[d]]; }
+            else { U[d] = prob->upresc[d]; dU[d] = 0.0; }
+        }
+    memset(R, 0, sizeof(double) * ((size_t)NEQ + 1));
+    for (E = 0; E < nel; E++) {
+        double X[3], Y[3], Ue[12], dUe[12], Re[12];
+        int lm[12];
+        for (v = 0; v < 3; v++) {
+            int J = ien[3 * E + v];
+            X[v] = x[J]; Y[v] = y[J];
+            for (k = 0; k < 4; k++) {
+                long d = 4L * J + k;
+                Ue[4 * v + k] = U[d];
+                dUe[4 * v + k] = dU[d];
+                lm[4 * v + k] = type[d] == 0 ? NEQ : invp[d];
+            }
+        }
+        eu_element(prob, X, Y, Ue, dUe, A + 144L * E, Re);
+        for (k = 0; k < 12; k++) R[lm[k]] += Re[k];
+        R[NEQ] = 0;
+    }
+    free(U); free(dU);
+}
+
+/* ---- Predictor_Old with EBE 12x12 blocks and BlockDiag (4x4) ---- */
+typedef struct {
+    int nel, nnodes, NEQ;
+    const int *lm, *Id;
+    const double *A, *inv;
+} eu_ctx;
+
+static int eu_mv_cb(void *p, double *P, double *Q)
+{
+    eu_ctx *c = (eu_ctx *)p;
+    or_ebemv(c->nel, 12, c->lm, c->A, c->NEQ, P, Q);
+    return 0;
+}
+
+static int eu_pc_cb(void *p, double *x, double *z)
+{
+    eu_ctx *c = (eu_ctx *)p;
+    or_blockdiag_apply(c->nnodes, 4, c->Id, c->NEQ, c->inv, x, z);
+    return 0;
+}
+
+static void axpy_ref(int n, double a, const double *x, double *y)
+{
+    /* daxpy.c: y += a x, unrolled by 4 (same rounding as the plain loop) */
+    for (int i = 0; i < n; i++) y[i] += a * x[i];
+}
+
+int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, const int *type,
+                       const int *invp, const int *ien, int neq, const or_euler_problem *prob,
+                       const or_time_opts *to, double solver_tol, int kmax, int lmax,
+                       double *u, double *a, or_time_stats *st)
+{
+    int NEQ = neq, i;
+    size_t ne = (size_t)(nel ? nel : 1), nn = (size_t)(nnodes ? nnodes : 1);
+    int *lm = malloc(sizeof(int) * 12 * ne), *Id = malloc(sizeof(int) * 4 * nn);
+    double *A = malloc(sizeof(double) * 144 * ne);
+    double *R = calloc((size_t)NEQ + 1, sizeof(double));
+    double *Da = calloc((size_t)NEQ + 1, sizeof(double));
+    double *u_old = calloc((size_t)NEQ + 1, sizeof(double));
+    double *bd = malloc(sizeof(double) * 16 * nn), *inv = malloc(sizeof(double) * 16 * nn);
+    double *diff = calloc((size_t)NEQ + 1, sizeof(double));
+    or_fill_lm(nel, 4, ien, type, invp, NEQ, lm);
+    for (i = 0; i < 4 * nnodes; i++) Id[i] = type[i] == 0 ? NEQ : invp[i];
+    eu_ctx ctx = { nel, nnodes, NEQ, lm, Id, A, inv };
+    double dt = prob->dt, alpha = prob->alpha, t = 0.0;
+    int steps = 0, corr = 0, gmres = 0, stop_time;
+    memset(a, 0, sizeof(double) * (size_t)neq);
+    do {
+        int it = 0, stop;
+        steps++;
+        t += dt;
+        memcpy(u_old, u, sizeof(double) * (size_t)neq);
+        axpy_ref(neq, (1.0 - alpha) * dt, a, u);              /* prediction */
+        memset(a, 0, sizeof(double) * (size_t)neq);
+        do {                                                   /* multicorrection */
+            int gi = 0;
+            it++;
+            or_build_euler(nnodes, nel, x, y, type, invp, ien, neq, prob, u, a, A, R);
+            or_blockdiag_setup(nnodes, nel, 4, ien, A, Id, NEQ, 1, bd, inv, R);
+            or_pgmres(NEQ, kmax, lmax, solver_tol, eu_mv_cb, eu_pc_cb, &ctx, R, Da, &gi);
+            gmres += gi;
+            axpy_ref(neq, 1, Da, a);
+            axpy_ref(neq, alpha * dt, Da, u);
+            double norm_a = sqrt(or_ddot(neq, a, a));
+            double norm_Da = sqrt(or_ddot(neq, Da, Da));
+            /* Criteria.c:25-41 */
+            if (to->stop_by_norm) stop = norm_Da < to->correction_tol * norm_a || it >= to->max_corrections;
+            else stop = it >= to->max_corrections;
+        } while (!stop);
+        corr += it;
+        /* Criteria.c:44-80 */
+        if (to->steady_state) {
+            for (i = 0; i < neq; i++) diff[i] = u[i] - u_old[i];
+            double nd = sqrt(or_ddot(neq, diff, diff)), nu = sqrt(or_ddot(neq, u, u));
+            stop_time = to->time_tol * nu > nd || fabs(to->final_time - t) < dt;
+        } else {
+            stop_time = to->final_time - t < 1e-10;
+        }
+        if (to->max_steps > 0 && steps >= to->max_steps) stop_time = 1;
+    } while (!stop_time);
+    if (st) { st->steps = steps; st->corrections = corr; st->gmres_iterations = gmres; st->t = t; }
+    free(lm); free(Id); free(A); free(R); free(Da); free(u_old); free(bd); free(inv); free(diff);
+    return steps;
+}

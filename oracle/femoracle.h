@@ -146,6 +146,47 @@ int or_ns_process(int nnodes, int nel, const double *x, const double *y, const i
                   double solver_tol, double nonlinear_tol, int kmax, int lmax, int max_nonlinear,
                   double *u, int *gmres_iterations, double *last_delta);
 
+/* ---- compressible Euler, SUPG + CAU (03_Euler_Equations) ---- */
+typedef struct {
+    double gamma;          /* FemFunctions->gamma (constant)                          */
+    double mach;           /* Parameters->Mach (dimensionless Jacobians)               */
+    int dimensionless;     /* 1: dimensionless_Ax_Ay_calculations, 0: dimensional      */
+    double tolerance;      /* StabilizationTolerance (CAU switch on |grad U|)          */
+    double alpha, dt;      /* Alpha_Build, DeltaT_Build                                */
+    const double *upresc;  /* [4*nnodes] prescribed rho, rho u, rho v, rho E           */
+} or_euler_problem;
+
+/* Build_M_K_F_SUPG + Delta_CAU + eval_U_dU + ebe_assembly: A receives the
+ * 144 entries of Me + alpha dt Ke per element, R the residual -M dU - K U
+ * (NEQ+1 slots, sink 0).  u, du: free dofs (neq). */
+void or_build_euler(int nnodes, int nel, const double *x, const double *y, const int *type,
+                    const int *invp, const int *ien, int neq, const or_euler_problem *prob,
+                    const double *u, const double *du, double *A, double *R);
+
+/* Stop tests of 00_CommonFiles/Time_Integration/Criteria.c */
+typedef struct {
+    int stop_by_norm;      /* 0: StopByIterations, 1: StopByNorm                      */
+    int max_corrections;   /* NonLinearMaxIter                                          */
+    double correction_tol; /* NonLinearTolerance                                        */
+    int steady_state;      /* 0: StopByTime, 1: StopBySteadyState                      */
+    double final_time;     /* FinalTime                                                 */
+    double time_tol;       /* TimeIntegrationTolerance                                  */
+    int max_steps;         /* bound on the time steps (0: none; not in the reference)   */
+} or_time_opts;
+
+typedef struct {
+    int steps, corrections, gmres_iterations;
+    double t;
+} or_time_stats;
+
+/* Predictor_Old.c:6-134 with EBE 12x12 blocks, BlockDiag (4x4, the
+ * reference's inverse) and GMRES.  u: initial state on entry (the
+ * problem's InitialSolution), final state on return; a: du/dt on return. */
+int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, const int *type,
+                       const int *invp, const int *ien, int neq, const or_euler_problem *prob,
+                       const or_time_opts *to, double solver_tol, int kmax, int lmax,
+                       double *u, double *a, or_time_stats *st);
+
 /* ---- assembled CSR path and ILU(0) (oracle/csr_ilu.c) ---- */
 int  or_csr_pattern(int nel, const int *ien, const int *type, const int *invp, int NEQ,
                     const int *Perm, const int *invPerm, int *IA, int *JA);

@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libfemoracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_sst.so")
 REF_NS_SO = os.path.join(HERE, "_ref", "libref_ns.so")
+REF_EU_SO = os.path.join(HERE, "_ref", "libref_euler.so")
 REF_SRC = "/root/reference"
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -74,6 +75,12 @@ def lib():
         L.or_ns_process.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
                                     ctypes.c_void_p, _c_dbl, _c_dbl, _c_int, _c_int, _c_int,
                                     _f64p, ctypes.POINTER(_c_int), ctypes.POINTER(_c_dbl)]
+        L.or_build_euler.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                     ctypes.c_void_p, _f64p, _f64p, _f64p, _f64p]
+        L.or_build_euler.restype = None
+        L.or_euler_predictor.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                         ctypes.c_void_p, ctypes.c_void_p, _c_dbl, _c_int, _c_int,
+                                         _f64p, _f64p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -130,7 +137,123 @@ def ref_ns():
     return _ref_ns
 
 
+_ref_eu = None
+
+
+def ref_euler():
+    """The reference's Euler driver (oracle/_ref), or None."""
+    global _ref_eu
+    if _ref_eu is None and os.path.exists(REF_EU_SO):
+        R = ctypes.CDLL(REF_EU_SO)
+        mesh = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int]
+        R.fr_eu_lm.argtypes = mesh + [_i32p]
+        R.fr_eu_lm.restype = None
+        R.fr_eu_build.argtypes = mesh + [_f64p, _f64p, _c_int, _f64p, _f64p, _f64p, _f64p]
+        R.fr_eu_build.restype = None
+        R.fr_eu_blockdiag.argtypes = mesh + [_f64p, _f64p, _f64p]
+        R.fr_eu_blockdiag.restype = None
+        R.fr_eu_ebemv.argtypes = mesh + [_f64p, _f64p, _f64p]
+        R.fr_eu_ebemv.restype = None
+        R.fr_eu_predictor.argtypes = mesh + [_f64p, _f64p, _c_int, _f64p, _f64p, _c_int, _c_int, _c_dbl,
+                                             _f64p, ctypes.POINTER(_c_dbl)]
+        _ref_eu = R
+    return _ref_eu
+
+
 # ---------------------------------------------------------------- helpers
+class _EulerProblem(ctypes.Structure):
+    _fields_ = [("gamma", _c_dbl), ("mach", _c_dbl), ("dimensionless", _c_int), ("tolerance", _c_dbl),
+                ("alpha", _c_dbl), ("dt", _c_dbl), ("upresc", ctypes.POINTER(_c_dbl))]
+
+
+class TimeOpts(ctypes.Structure):
+    """or_time_opts: the stop tests of Criteria.c."""
+    _fields_ = [("stop_by_norm", _c_int), ("max_corrections", _c_int), ("correction_tol", _c_dbl),
+                ("steady_state", _c_int), ("final_time", _c_dbl), ("time_tol", _c_dbl), ("max_steps", _c_int)]
+
+    def as_array(self):
+        return np.array([self.stop_by_norm, self.max_corrections, self.correction_tol, self.steady_state,
+                         self.final_time, self.time_tol], dtype=np.float64)
+
+
+class _TimeStats(ctypes.Structure):
+    _fields_ = [("steps", _c_int), ("corrections", _c_int), ("gmres_iterations", _c_int), ("t", _c_dbl)]
+
+
+def _eu_struct(p):
+    up = np.ascontiguousarray(p.upresc, dtype=np.float64)
+    s = _EulerProblem(p.gamma, p.mach, int(p.dimensionless), p.tolerance, p.alpha, p.dt,
+                      up.ctypes.data_as(ctypes.POINTER(_c_dbl)))
+    return s, up
+
+
+def build_euler(prob, u=None, du=None):
+    """Build_M_K_F_SUPG at (u, du); returns (A[nel, 144], R[neq+1])."""
+    m = prob.mesh
+    u = prob.initial_state() if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    du = np.zeros(m.neq) if du is None else np.ascontiguousarray(du, dtype=np.float64)
+    A = np.empty(m.nel * 144)
+    R = np.empty(m.neq + 1)
+    s, keep = _eu_struct(prob)
+    lib().or_build_euler(*_mesh_args(m), ctypes.byref(s), u, du, A, R)
+    return A.reshape(m.nel, 144), R
+
+
+def euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000, u0=None):
+    """Predictor_Old loop; returns (u[neq], a[neq], stats dict)."""
+    m = prob.mesh
+    u = np.zeros(m.neq + 1)
+    u[:m.neq] = prob.initial_state() if u0 is None else u0
+    a = np.zeros(m.neq + 1)
+    st = _TimeStats()
+    s, keep = _eu_struct(prob)
+    lib().or_euler_predictor(*_mesh_args(m), ctypes.byref(s), ctypes.byref(topts), tol, kmax, lmax, u, a,
+                             ctypes.byref(st))
+    return u[:m.neq].copy(), a[:m.neq].copy(), {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def ref_euler_lm(mesh):
+    lm = np.empty(mesh.nel * 12, dtype=np.int32)
+    ref_euler().fr_eu_lm(*_mesh_args(mesh), lm)
+    return lm.reshape(mesh.nel, 12)
+
+
+def ref_euler_build(prob, u=None, du=None):
+    m = prob.mesh
+    u = prob.initial_state() if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    du = np.zeros(m.neq) if du is None else np.ascontiguousarray(du, dtype=np.float64)
+    A = np.empty(m.nel * 144)
+    R = np.empty(m.neq + 1)
+    ref_euler().fr_eu_build(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
+                            int(prob.wall), u, du, A, R)
+    return A.reshape(m.nel, 144), R
+
+
+def ref_euler_blockdiag(mesh, A, F):
+    F = np.array(F, dtype=np.float64, copy=True)
+    inv = np.empty(mesh.nnodes * 16)
+    ref_euler().fr_eu_blockdiag(*_mesh_args(mesh), np.ascontiguousarray(A, dtype=np.float64).reshape(-1), F, inv)
+    return inv, F
+
+
+def ref_euler_ebemv(mesh, A, P):
+    Q = np.zeros(mesh.neq + 1)
+    ref_euler().fr_eu_ebemv(*_mesh_args(mesh), np.ascontiguousarray(A, dtype=np.float64).reshape(-1),
+                            np.ascontiguousarray(P, dtype=np.float64), Q)
+    return Q
+
+
+def ref_euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000):
+    """The reference's Predictor_Old; returns (u[neq], GMRES iterations, final t)."""
+    m = prob.mesh
+    u = np.zeros(m.neq + 1)
+    t = _c_dbl(0.0)
+    its = ref_euler().fr_eu_predictor(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
+                                      int(prob.wall), np.ascontiguousarray(prob.init), topts.as_array(),
+                                      kmax, lmax, tol, u, ctypes.byref(t))
+    return u[:m.neq].copy(), its, t.value
+
+
 class _NSProblem(ctypes.Structure):
     _fields_ = [("reynolds", _c_dbl), ("upresc", ctypes.POINTER(_c_dbl)),
                 ("f1", ctypes.POINTER(_c_dbl)), ("f2", ctypes.POINTER(_c_dbl))]

@@ -1,0 +1,257 @@
+/*
+ * Checker harness around the reference's own compressible Euler solve path
+ * (03_Euler_Equations/2D/01_CommonFiles with 00_CommonFiles/Time_Integration),
+ * compiled from the reference sources by oracle/Makefile (target "ref").
+ *
+ * The structs are filled for one rank (neq_bef = 0, NEQ = neq, EBE storage)
+ * and the reference's own Fill_LM, Build_M_K_F_SUPG (with Delta_CAU and
+ * Ax_Ay_calculations), BlockDiag_precond_EBE_setup, ebemvNDOF4, pgmres and
+ * Predictor_Old are called.  The function pointers are installed as the
+ * reference's set* functions install them for StabilizationForm "SUPG",
+ * ShockCapture "CAU", TimeIntegration "Predictor1", Preconditioner
+ * "BlockDiag", MatrixVectorProductScheme "EBE" (setStabilizationForm.c and
+ * set_BC_no_penetrability.c are not linked: they pull in the CYLINDER and
+ * NACA0012 problem directories).  setProblem is supplied here: gamma is a
+ * constant, each prescribed field is a0 + a1 x + a2 y, optionally with the
+ * OBLIQUO wall rule for v2 (0 where |y| <= 1e-15 and x > 0,
+ * OBLIQUO/OBLIQUO_v2presc.c), and the initial solution sets every free dof
+ * k to a constant (as OBLIQUO_InitialSolution.c does).
+ *
+ * Used only by tests.
+ */
+#include "EulerEquations.h"
+#include "solvers.h"
+#include "preconditioners.h"
+#include "matvec.h"
+#include "time_integration.h"
+
+/* ---- synthetic problem (replaces the reference's setProblem.c) ---- */
+static double g_gamma, g_c[4][3], g_init[4];
+static int g_wall;
+
+static double syn_gamma(double X, double Y) { (void)X; (void)Y; return g_gamma; }
+static double syn_cv(double X, double Y) { (void)X; (void)Y; return 716.5; }
+static double affine(int k, double X, double Y) { return g_c[k][0] + g_c[k][1] * X + g_c[k][2] * Y; }
+static double syn_rho(double X, double Y) { return affine(0, X, Y); }
+static double syn_v1(double X, double Y) { return affine(1, X, Y); }
+static double syn_v2(double X, double Y)
+{
+    if (g_wall && fabs(Y) <= 1e-15 && fabs(X) > 0) return 0.0;
+    return affine(2, X, Y);
+}
+static double syn_e(double X, double Y) { return affine(3, X, Y); }
+static int syn_init(ParametersType *P, NodeType *Node, double *u)
+{
+    int I, k;
+    for (I = 0; I < P->nnodes; I++)
+        for (k = 0; k < 4; k++)
+            if (Node[I].Type[k] != 0) u[Node[I].invP_id[k]] = g_init[k];
+    return 0;
+}
+
+int setProblem(ParametersType *P, FemFunctionsType *F)
+{
+    (void)P;
+    F->gamma = syn_gamma;
+    F->cv = syn_cv;
+    F->rhopresc = syn_rho;
+    F->v1presc = syn_v1;
+    F->v2presc = syn_v2;
+    F->epresc = syn_e;
+    F->InitialSolution = syn_init;
+    return 0;
+}
+
+typedef struct {
+    ParametersType P;
+    MatrixDataType M;
+    FemStructsType S;
+    FemFunctionsType F;
+    FemOtherFunctionsType O;
+    AuxBuildStructuresType Aux;
+} fr_eu;
+
+static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const double *y, const int *type,
+                        const int *invp, const int *ien, int neq, const double *prm)
+{
+    int I, k;
+    memset(c, 0, sizeof(*c));
+    strcpy(c->P.ProblemTitle, "SYNTH");
+    strcpy(c->P.Solver, "GMRES");
+    strcpy(c->P.TimeIntegration, "Predictor1");
+    strcpy(c->P.MatrixVectorProductScheme, "EBE");
+    strcpy(c->P.StabilizationForm, "SUPG");
+    strcpy(c->P.ShockCapture, "CAU");
+    strcpy(c->P.Preconditioner, "BlockDiag");
+    strcpy(c->P.Scaling, "NOT");
+    strcpy(c->P.reordering, "NOT");
+    /* prm: gamma, mach, dimensionless, tolerance, alpha, dt */
+    g_gamma = prm[0];
+    c->P.Mach = prm[1];
+    strcpy(c->P.Dimensionless, prm[2] != 0.0 ? "YES" : "NO");
+    c->P.StabilizationTolerance = prm[3];
+    c->P.Alpha = c->P.Alpha_Build = prm[4];
+    c->P.DeltaT = c->P.DeltaT_Build = prm[5];
+    c->P.nnodes = c->P.nNodes = nnodes;
+    c->P.nel = c->P.nEl = nel;
+    c->P.neq = neq;
+    c->P.neq_bef = 0;
+    c->P.NEQ = neq;
+    c->P.RANK = 0;
+    c->P.NPROC = 1;
+    NodeType *Node = calloc((size_t)nnodes, sizeof(NodeType));
+    ElementType *El = calloc((size_t)nel, sizeof(ElementType));
+    for (I = 0; I < nnodes; I++) {
+        Node[I].x = x[I];
+        Node[I].y = y[I];
+        for (k = 0; k < NDOF; k++) {
+            Node[I].Type[k] = type[NDOF * I + k];
+            Node[I].Send[k] = 1;
+            Node[I].invP_id[k] = type[NDOF * I + k] == 0 ? -1 : invp[NDOF * I + k];
+        }
+    }
+    for (I = 0; I < nel; I++) {
+        El[I].Vertex[0] = ien[3 * I];
+        El[I].Vertex[1] = ien[3 * I + 1];
+        El[I].Vertex[2] = ien[3 * I + 2];
+        El[I].Type = -1;
+    }
+    c->S.Node = Node;
+    c->S.Element = El;
+    c->S.F = calloc((size_t)neq + 1, sizeof(double));
+    c->S.U = calloc((size_t)neq + 1, sizeof(double));
+    c->S.f = c->S.F;
+    c->S.u = c->S.U;
+    c->S.lm = calloc((size_t)nel, sizeof(int *));
+    c->S.lmaux = calloc((size_t)nel * 12, sizeof(int));
+    for (I = 0; I < nel; I++) c->S.lm[I] = &c->S.lmaux[12 * I];
+    Fill_LM(&c->P, c->S.lm, Node, El);
+    c->M.A = calloc((size_t)nel, sizeof(double *));
+    c->M.Aaux = calloc((size_t)nel * 144, sizeof(double));
+    for (I = 0; I < nel; I++) c->M.A[I] = &c->M.Aaux[144 * I];
+    c->M.Diag = calloc((size_t)neq + 1, sizeof(double));
+    c->M.invDiag = calloc((size_t)neq + 1, sizeof(double));
+    c->Aux.tolerance = prm[3];
+    c->S.AuxBuild = &c->Aux;
+    c->S.delta_old = calloc((size_t)nel + 1, sizeof(double));
+    /* setProblem / setMatrixVectorProductType / setSolver / setPreconditioner /
+     * setDimensionlessness as Process.c:9-16 runs them; SUPG + CAU as
+     * setStabilizationForm.c installs them */
+    setProblem(&c->P, &c->F);
+    setMatrixVectorProductType(&c->P, &c->F);
+    setSolver(&c->P, &c->O);
+    setPreconditioner(&c->P, &c->F);
+    setDimensionlessness(&c->P, &c->F);
+    c->O.Build = Build_M_K_F_SUPG;
+    c->F.ShockCapture = Delta_CAU;
+}
+
+static void fr_eu_free(fr_eu *c)
+{
+    free(c->S.Node); free(c->S.Element); free(c->S.F); free(c->S.U);
+    free(c->S.lm); free(c->S.lmaux); free(c->M.A); free(c->M.Aaux);
+    free(c->M.Diag); free(c->M.invDiag); free(c->S.delta_old);
+    if (c->M.Id) { free(c->M.Id[0]); free(c->M.Id); }
+    if (c->M.BlockDiag) { free(c->M.BlockDiag[0]); free(c->M.BlockDiag); }
+    if (c->M.invBlockDiag) { free(c->M.invBlockDiag[0]); free(c->M.invBlockDiag); }
+}
+
+static void fr_eu_problem(const double *coef, int wall, const double *init)
+{
+    memcpy(g_c, coef, sizeof g_c);
+    g_wall = wall;
+    if (init) memcpy(g_init, init, sizeof g_init);
+}
+
+void fr_eu_lm(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+              const int *ien, int neq, int *lm_out)
+{
+    fr_eu c;
+    double prm[6] = {1.4, 1.0, 0.0, 0.0, 0.5, 1.0};
+    fr_eu_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, prm);
+    memcpy(lm_out, c.S.lmaux, sizeof(int) * 12 * (size_t)nel);
+    fr_eu_free(&c);
+}
+
+/* One Build_M_K_F_SUPG call at (u, du) (A: 144 per element, R: NEQ+1). */
+void fr_eu_build(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                 const int *ien, int neq, const double *prm, const double *coef, int wall, const double *u,
+                 const double *du, double *A_out, double *R_out)
+{
+    fr_eu c;
+    fr_eu_problem(coef, wall, NULL);
+    fr_eu_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, prm);
+    double *dus = calloc((size_t)neq + 1, sizeof(double));
+    memcpy(c.S.u, u, sizeof(double) * (size_t)neq);
+    memcpy(dus, du, sizeof(double) * (size_t)neq);
+    c.S.du = dus;
+    Build_M_K_F_SUPG(&c.P, &c.M, &c.S, &c.F);
+    memcpy(A_out, c.M.Aaux, sizeof(double) * 144 * (size_t)nel);
+    memcpy(R_out, c.S.F, sizeof(double) * ((size_t)neq + 1));
+    free(dus);
+    fr_eu_free(&c);
+}
+
+/* BlockDiag_precond_EBE_setup (first call) on caller blocks; F in place. */
+void fr_eu_blockdiag(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                     const int *ien, int neq, const double *A, double *F, double *inv_out)
+{
+    fr_eu c;
+    int I;
+    double prm[6] = {1.4, 1.0, 0.0, 0.0, 0.5, 1.0};
+    fr_eu_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, prm);
+    memcpy(c.M.Aaux, A, sizeof(double) * 144 * (size_t)nel);
+    BlockDiag_precond_EBE_setup(&c.P, &c.M, &c.S, 1, F);
+    for (I = 0; I < nnodes; I++) memcpy(inv_out + 16L * I, c.M.invBlockDiag[I], 16 * sizeof(double));
+    fr_eu_free(&c);
+}
+
+void fr_eu_ebemv(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                 const int *ien, int neq, const double *A, const double *P, double *Q)
+{
+    fr_eu c;
+    double prm[6] = {1.4, 1.0, 0.0, 0.0, 0.5, 1.0};
+    fr_eu_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, prm);
+    memcpy(c.M.Aaux, A, sizeof(double) * 144 * (size_t)nel);
+    double *Pc = calloc((size_t)neq + 1, sizeof(double));
+    memcpy(Pc, P, sizeof(double) * ((size_t)neq + 1));
+    ebemvNDOF4(&c.P, &c.M, &c.S, Pc, Q);
+    free(Pc);
+    fr_eu_free(&c);
+}
+
+/* The predictor/multicorrector time loop of the reference.
+ * topt: stop_by_norm, max_corrections, correction_tol, steady_state,
+ *       final_time, time_tol; solver: kmax, lmax, tol. */
+int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                    const int *ien, int neq, const double *prm, const double *coef, int wall,
+                    const double *init, const double *topt, int kmax, int lmax, double tol, double *u_out,
+                    double *t_out)
+{
+    fr_eu c;
+    fr_eu_problem(coef, wall, init);
+    fr_eu_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, prm);
+    strcpy(c.P.StopMulticorrection, topt[0] != 0.0 ? "NORM" : "ITERATION");
+    c.P.NonLinearMaxIter = (int)topt[1];
+    c.P.NonLinearTolerance = topt[2];
+    strcpy(c.P.StopAtSteadyState, topt[3] != 0.0 ? "YES" : "NO");
+    c.P.FinalTime = topt[4];
+    c.P.TimeIntegrationTolerance = topt[5];
+    c.P.KrylovBasisVectorsQuantity = kmax;
+    c.P.LinearMaxIter = lmax;
+    c.P.SolverTolerance = tol;
+    c.P.iterations = 0;
+    setStopCriteria(&c.P, &c.F);
+    /* Predictor_Old installs and frees its own du, uB, delta_old and AuxBuild */
+    free(c.S.delta_old);
+    c.S.delta_old = NULL;
+    Predictor_Old(&c.P, &c.M, &c.S, &c.F, &c.O);
+    c.S.delta_old = NULL;
+    c.S.du = c.S.uB = NULL;
+    c.S.AuxBuild = NULL;
+    memcpy(u_out, c.S.u, sizeof(double) * (size_t)neq);
+    *t_out = c.P.CurrentTime;
+    int its = c.P.iterations;
+    fr_eu_free(&c);
+    return its;
+}

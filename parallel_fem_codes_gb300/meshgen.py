@@ -216,3 +216,100 @@ def cavity_problem(n_nodes_side: int, reynolds=1000.0, jitter=0.0, seed=3) -> NS
     invp, neq = number_dofs(type_)
     mesh = Mesh(X, Y, ien, 3, type_, invp, neq)
     return ns_problem(mesh, reynolds, lid=True)
+
+
+@dataclasses.dataclass
+class EulerProblem:
+    """Compressible Euler data in conservative variables (rho, rho u, rho v,
+    rho E): the FemFunctions callbacks gamma, rhopresc, v1presc, v2presc,
+    epresc and InitialSolution of
+    03_Euler_Equations/2D/01_CommonFiles/EulerEquations.h:171-177 and the
+    Parameters the SUPG build reads.  Each prescribed field k is
+    coef[k, 0] + coef[k, 1] x + coef[k, 2] y; wall = True adds the OBLIQUO
+    wall rule for v2 (0 where |y| <= 1e-15 and x > 0,
+    OBLIQUO/OBLIQUO_v2presc.c).  init[k] is the initial value of every free
+    dof k (OBLIQUO_InitialSolution.c)."""
+    mesh: Mesh
+    gamma: float
+    mach: float
+    dimensionless: bool
+    tolerance: float       # StabilizationTolerance
+    alpha: float
+    dt: float
+    coef: np.ndarray       # float64[4, 3]
+    wall: bool
+    init: np.ndarray       # float64[4]
+    upresc: np.ndarray     # float64[nnodes*4]
+
+    def initial_state(self) -> np.ndarray:
+        """Free-dof vector of the initial solution (length neq)."""
+        m = self.mesh
+        u = np.zeros(m.neq)
+        t = m.type.reshape(-1, 4)
+        ip = m.invp.reshape(-1, 4)
+        for k in range(4):
+            free = t[:, k] != 0
+            u[ip[free, k]] = self.init[k]
+        return u
+
+    def params(self) -> np.ndarray:
+        return np.array([self.gamma, self.mach, 1.0 if self.dimensionless else 0.0, self.tolerance,
+                         self.alpha, self.dt], dtype=np.float64)
+
+
+def _euler_presc(mesh: Mesh, coef: np.ndarray, wall: bool) -> np.ndarray:
+    x, y = mesh.x, mesh.y
+    val = [coef[k, 0] + coef[k, 1] * x + coef[k, 2] * y for k in range(4)]
+    if wall:
+        val[2] = np.where((np.abs(y) <= 1e-15) & (np.abs(x) > 0), 0.0, val[2])
+    return np.stack(val, axis=1).reshape(-1).astype(np.float64)
+
+
+def euler_problem(mesh: Mesh, gamma=1.4, mach=2.0, dimensionless=True, tolerance=1e-8, alpha=0.5, dt=1e-3,
+                  coef=None, wall=False, init=(1.0, 0.0, 0.0, 1.0)) -> EulerProblem:
+    coef = np.zeros((4, 3)) if coef is None else np.asarray(coef, dtype=np.float64).reshape(4, 3)
+    return EulerProblem(mesh, float(gamma), float(mach), bool(dimensionless), float(tolerance), float(alpha),
+                        float(dt), coef, bool(wall), np.asarray(init, dtype=np.float64),
+                        _euler_presc(mesh, coef, wall))
+
+
+def euler_dt(mesh: Mesh, gamma: float, state, cfl=0.5) -> float:
+    """cfl * min_e h_e / (|v| + c) for the uniform state (rho, rho u, rho v,
+    rho E), with h_e = sqrt(2 Area_e) and the sound speed
+    c = sqrt(gamma (gamma - 1) (E - |v|^2 / 2)) as Build_M_K_F_SUPG.c:256-259
+    computes them."""
+    rho, mu, mv, E = state
+    v1, v2 = mu / rho, mv / rho
+    v = math.hypot(v1, v2)
+    c = math.sqrt(gamma * (gamma - 1.0) * (E / rho - 0.5 * (v1 * v1 + v2 * v2)))
+    x, y, ien = mesh.x, mesh.y, mesh.ien
+    x1, x2, x3 = x[ien[:, 0]], x[ien[:, 1]], x[ien[:, 2]]
+    y1, y2, y3 = y[ien[:, 0]], y[ien[:, 1]], y[ien[:, 2]]
+    two_a = np.abs((x2 - x1) * (y3 - y1) - (x1 - x3) * (y1 - y2))
+    return float(cfl * np.sqrt(two_a).min() / (v + c))
+
+
+def obliquo_problem(n_nodes_side: int, mach=2.0, dimensionless=True, alpha=0.5, tolerance=1e-8, dt=None):
+    """The oblique-shock set-up OBLIQUO on the unit square with n x n nodes:
+    marks of Mesh_Generator/Structured_Mesh/meshGenerator.c:231-241 (bottom
+    wall y = 0: rho v prescribed; inflow x = 0 and top y = 1: everything
+    prescribed; elsewhere free), inflow (rho, rho u, rho v, rho E) =
+    (1, 0.98481, -0.17365, 0.94643) at 10 degrees (OBLIQUO_*presc.c), the
+    same initial state, gamma = 1.4.  dt defaults to 0.5 min h / (|v| + c)
+    of the initial state."""
+    M = n_nodes_side - 1
+    X, Y, ien = structured_mesh(M, M)
+    bottom = np.abs(Y) <= 1e-15
+    inflow = (np.abs(X) <= 1e-15) | (np.abs(Y - 1.0) <= 1e-15)
+    type_ = np.ones((X.shape[0], 4), dtype=np.int32)
+    type_[bottom, 2] = 0
+    type_[inflow & ~bottom, :] = 0
+    type_ = type_.reshape(-1)
+    invp, neq = number_dofs(type_)
+    mesh = Mesh(X, Y, ien, 4, type_, invp, neq)
+    state = (1.0, 0.98481, -0.17365, 0.94643)
+    coef = np.zeros((4, 3))
+    coef[:, 0] = state
+    if dt is None:
+        dt = euler_dt(mesh, 1.4, state, 0.5)
+    return euler_problem(mesh, 1.4, mach, dimensionless, tolerance, alpha, dt, coef, True, state)

@@ -9,7 +9,9 @@ iterations), all computed by the reference's Fill_LM, Permutation_of_LM,
 Build_K_F_SUPG, Diag_precond_EBE_setup, pgmres and Process; and
 tests/golden/ns_*.npz: the steady Navier-Stokes driver's Fill_LM,
 Build_K_F_SUPG_PSPG at a state u, BlockDiagDOF3_precond_EBE_setup,
-ebemvNDOF3 and (cavity) the Picard Process loop.
+ebemvNDOF3 and (cavity) the Picard Process loop; and tests/golden/eu_*.npz:
+the Euler driver's Fill_LM, Build_M_K_F_SUPG at a state (u, du),
+BlockDiag_precond_EBE_setup, ebemvNDOF4 and the Predictor_Old time loop.
 """
 import os
 import sys
@@ -72,6 +74,36 @@ def main():
         print(name, "neq", m.neq, extra.get("process_its"))
 
 
+def euler_cases():
+    """name: (problem, seed of the perturbation of (u, du), time options)."""
+    p9 = G.obliquo_problem(9)
+    p7 = G.obliquo_problem(7, dimensionless=False)
+    return {"eu_9_obliquo": (p9, 3, O.TimeOpts(0, 2, 1e-3, 0, 4 * p9.dt, 1e-6, 0)),
+            "eu_7_dimensional": (p7, 4, O.TimeOpts(1, 4, 1e-2, 1, 20 * p7.dt, 1e-2, 0))}
+
+
+def write_euler():
+    for name, (prob, seed, to) in euler_cases().items():
+        m = prob.mesh
+        rng = np.random.Generator(np.random.PCG64(seed))
+        u0 = prob.initial_state()
+        u = u0 * (1.0 + 0.05 * rng.standard_normal(m.neq))
+        du = 0.01 * rng.standard_normal(m.neq)
+        lm = O.ref_euler_lm(m)
+        A, R = O.ref_euler_build(prob, u, du)
+        inv, Rp = O.ref_euler_blockdiag(m, A, R)
+        P = rng.standard_normal(m.neq + 1)
+        P[m.neq] = 0.0
+        Q = O.ref_euler_ebemv(m, A, P)
+        U, its, t = O.ref_euler_predictor(prob, to, 1e-10, 25, 1000)
+        np.savez_compressed(
+            os.path.join(HERE, name + ".npz"),
+            x=m.x, y=m.y, ien=m.ien, type=m.type, invp=m.invp, neq=m.neq, params=prob.params(),
+            coef=prob.coef, wall=int(prob.wall), init=prob.init, topts=to.as_array(), u=u, du=du, lm=lm,
+            A=A, R=R, inv=inv, Rp=Rp, P=P, Q=Q, U=U, gmres_its=its, t=t)
+        print(name, "neq", m.neq, "gmres", its, "t", t)
+
+
 def ns_cases():
     """name: (problem, seed of the state u (0: u = 0), run the Process loop)."""
     cav = G.cavity_problem(9, reynolds=100.0)
@@ -82,3 +114,4 @@ def ns_cases():
 
 if __name__ == "__main__":
     main()
+    write_euler()

@@ -1,0 +1,97 @@
+"""The Euler oracle (oracle/euler.c) against the golden fixtures generated
+from the reference's own C (03_Euler_Equations driver: Fill_LM,
+Build_M_K_F_SUPG with Delta_CAU and both Jacobian forms,
+BlockDiag_precond_EBE_setup, ebemvNDOF4, Predictor_Old with the Criteria.c
+stop tests), and against the reference build itself where it is present.
+Everything is bit-exact, including the time loop."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from parallel_fem_codes_gb300 import meshgen as G
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "eu_*.npz")))
+
+
+def problem_from(g):
+    m = G.Mesh(g["x"], g["y"], g["ien"], 4, g["type"], g["invp"], int(g["neq"]))
+    gm, mach, dl, tol, alpha, dt = [float(v) for v in g["params"]]
+    return G.euler_problem(m, gm, mach, bool(dl), tol, alpha, dt, g["coef"], bool(g["wall"]), g["init"])
+
+
+def topts_from(g):
+    a = g["topts"]
+    return O.TimeOpts(int(a[0]), int(a[1]), float(a[2]), int(a[3]), float(a[4]), float(a[5]), 0)
+
+
+@pytest.fixture(scope="module", params=GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def case(request, oracle_lib):
+    g = dict(np.load(request.param))
+    return g, problem_from(g)
+
+
+def test_golden_present():
+    assert len(GOLDEN) >= 2
+
+
+def test_fill_lm(case):
+    g, p = case
+    assert np.array_equal(O.fill_lm(p.mesh).reshape(-1), g["lm"].reshape(-1))
+
+
+def test_build_bit_exact(case):
+    g, p = case
+    A, R = O.build_euler(p, g["u"], g["du"])
+    assert np.array_equal(A, g["A"])
+    assert np.array_equal(R, g["R"])
+
+
+def test_blockdiag_4x4_bit_exact(case):
+    g, p = case
+    bd, ibd, Id, Rp = O.blockdiag_setup(p.mesh, g["A"], g["R"], ref_quirks=True)
+    assert np.array_equal(ibd, g["inv"])
+    assert np.array_equal(Rp, g["Rp"])
+
+
+def test_ebemv_ndof4_bit_exact(case):
+    g, p = case
+    Q = O.ebemv(O.fill_lm(p.mesh), g["A"], p.mesh.neq, g["P"])
+    assert np.array_equal(Q, g["Q"])
+
+
+def test_predictor_bit_exact(case):
+    g, p = case
+    u, a, st = O.euler_predictor(p, topts_from(g), tol=1e-10, kmax=25, lmax=1000)
+    assert st["gmres_iterations"] == int(g["gmres_its"])
+    assert st["t"] == float(g["t"])
+    assert np.array_equal(u, g["U"])
+
+
+def test_obliquo_layout():
+    p = G.obliquo_problem(9)
+    m = p.mesh
+    t = m.type.reshape(-1, 4)
+    bottom = np.abs(m.y) <= 1e-15
+    inflow = ((np.abs(m.x) <= 1e-15) | (np.abs(m.y - 1.0) <= 1e-15)) & ~bottom
+    assert np.all(t[bottom] == [1, 1, 0, 1])
+    assert np.all(t[inflow] == 0)
+    assert np.all(t[~bottom & ~inflow] == 1)
+    up = p.upresc.reshape(-1, 4)
+    assert np.all(up[bottom & (m.x > 0), 2] == 0.0)
+    assert up[0, 2] == -0.17365                       # the corner keeps the inflow value
+    assert np.array_equal(p.initial_state()[m.invp.reshape(-1, 4)[t[:, 0] != 0, 0]], np.ones(int((t[:, 0] != 0).sum())))
+
+
+@pytest.mark.skipif(O.ref_euler() is None, reason="reference build absent (oracle/_ref)")
+@pytest.mark.parametrize("n,dimless", [(15, True), (10, False)])
+def test_against_reference_build(n, dimless):
+    p = G.obliquo_problem(n, dimensionless=dimless)
+    rng = np.random.default_rng(n)
+    u = p.initial_state() * (1.0 + 0.1 * rng.standard_normal(p.mesh.neq))
+    du = 0.05 * rng.standard_normal(p.mesh.neq)
+    A, R = O.build_euler(p, u, du)
+    Ar, Rr = O.ref_euler_build(p, u, du)
+    assert np.array_equal(A, Ar) and np.array_equal(R, Rr)
