@@ -269,6 +269,61 @@ int fg_ns_assemble(fg_system *s, const fg_ns_coeffs *c, const double *u, double 
 int fg_ns_process(fg_system *s, const fg_ns_coeffs *c, const fg_solver_opts *opts, double nonlinear_tol,
                   int max_nonlinear, double *u, fg_process_stats *stats);
 
+/* ---- compressible Euler, SUPG + CAU, conservative variables (NDOF = 4) ----
+ * Replaces Build_M_K_F_SUPG.c:6-1057 (with Delta_CAU.c, Ax_Ay_calculations.c,
+ * eval_U_dU.c and ebe_assembly.c) of 03_Euler_Equations/2D/01_CommonFiles and
+ * the predictor/multicorrector loop of
+ * 00_CommonFiles/Time_Integration/Predictor_Old.c:6-134 with the stop tests
+ * of Criteria.c, for a system created with ndof = 4 (rho, rho u, rho v, rho E
+ * per node). */
+typedef struct {
+    double gamma;      /* FemFunctions->gamma (a constant)                        */
+    double mach;       /* Parameters->Mach, used by the dimensionless Jacobians   */
+    int dimensionless; /* 1: dimensionless_Ax_Ay_calculations; 0: dimensional    */
+    double tolerance;  /* StabilizationTolerance: CAU is off below this |grad U|  */
+    double alpha;      /* Alpha (time integration)                                */
+    double dt;         /* DeltaT                                                  */
+} fg_euler_coeffs;
+
+/* Node coordinates and the prescribed (rho, rho u, rho v, rho E) of every node
+ * (upresc[4*node+k], read where dof k of the node is Dirichlet). */
+int fg_euler_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc);
+/* Build_M_K_F_SUPG at the free-dof state u and its time derivative du (host,
+ * n entries each; NULL = 0): the 12x12 blocks Me + alpha dt Ke stay on the
+ * device; R (host, n+1) receives -Me dU - Ke U when not NULL. */
+int fg_euler_assemble(fg_system *s, const fg_euler_coeffs *c, const double *u, const double *du, double *R);
+
+/* Time loop controls (Criteria.c) and the preconditioner of each correction. */
+typedef struct {
+    int stop_by_norm;      /* 0: StopByIterations; 1: StopByNorm                  */
+    int max_corrections;   /* NonLinearMaxIter                                     */
+    double correction_tol; /* NonLinearTolerance (StopByNorm)                      */
+    int steady_state;      /* 0: StopByTime; 1: StopBySteadyState                  */
+    double final_time;     /* FinalTime                                            */
+    double time_tol;       /* TimeIntegrationTolerance (StopBySteadyState)         */
+    int max_steps;         /* bound on the steps, 0 = none (not in the reference)  */
+    int precond;           /* FG_PRECOND_BLOCKDIAG, FG_PRECOND_DIAG or NONE        */
+    int setup_flags;       /* FG_SETUP_REF_QUIRKS: the reference's 4x4 inverse     */
+} fg_time_opts;
+
+typedef struct {
+    int steps;
+    int corrections;
+    int gmres_iterations;
+    double t;                  /* time reached                                    */
+    double seconds;
+    double true_rel_residual;  /* of the last linear solve                        */
+} fg_time_stats;
+
+/* Predictor_Old: per step t += dt, u += (1 - alpha) dt a, a = 0, then
+ * corrections (assemble at (u, a), preconditioner set-up on R, GMRES for Da,
+ * a += Da, u += alpha dt Da) until the correction stop test, until the time
+ * stop test.  u (host, n) is the initial state on entry (the problem's
+ * InitialSolution) and the final state on return; a (host, n, may be NULL)
+ * receives du/dt.  The state stays on the device for the whole loop. */
+int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *opts,
+                       const fg_time_opts *t, double *u, double *a, fg_time_stats *stats);
+
 /* ---- request server: continuous batching of transport solves ----
  * A worker thread owns one batch.  Requests (a system whose geometry is set,
  * with transport coefficients) wait in a FIFO; between restart cycles the

@@ -27,6 +27,7 @@ UNITS = [
     ("server.cu", []),
     ("ilu.cu", ["-fmad=false"]),
     ("ns.cu", ["-fmad=false"]),
+    ("euler.cu", ["-fmad=false"]),
 ]
 
 

@@ -1,0 +1,258 @@
+// Compressible Euler on the device: the SUPG + CAU element build of
+// 03_Euler_Equations/2D/01_CommonFiles/Build_M_K_F_SUPG.c:6-1057 with
+// Ax_Ay_calculations.c, Delta_CAU.c, eval_U_dU.c and ebe_assembly.c.
+//
+// k_euler_elem is one thread per element (internal element order).  It
+// gathers the nodal state (rho, rho u, rho v, rho E) and its time derivative
+// (prescribed values and zero for Dirichlet dofs), forms the barycentric
+// Jacobians Ax, Ay, the metric A0^-1, the CAU coefficient and the SUPG tau,
+// and then writes the 12x12 block Me + alpha dt Ke row by row together with
+// the element residual -Me dUe - Ke Ue.  The entries of Me and Ke are formed
+// on the fly from Ax and Ay (the rows of the products AxAx, AxAy, AyAx, AyAy
+// are recomputed per block row), which keeps about 80 doubles live instead
+// of the reference's ~600 named temporaries.
+//
+// Bit-exactness: the reference writes the Jacobian products and the blocks
+// (b_i Ax + c_i Ay)/6 term by term without the terms that multiply a
+// structural zero of Ax or Ay; here they are plain 4x4 products and sums over
+// k = 0..3, whose extra terms are exact zeros (adding an exact zero leaves a
+// sum unchanged).  Ay[0][3], which the reference never sets and never reads,
+// is 0.  Every other expression keeps the reference's order and association;
+// the unit is compiled with -fmad=false.  pow(x, 2) is evaluated as x * x
+// (pow's result for an exponent of 2 is the correctly rounded square).
+#include "system.h"
+
+namespace fg {
+
+__device__ __forceinline__ void eu_jacobians(const fg_euler_coeffs &cf, const double Ub[4], double Ax[4][4],
+                                             double Ay[4][4])
+{
+    const double gamma = cf.gamma;
+    const double v1 = Ub[1] / Ub[0], v2 = Ub[2] / Ub[0], E = Ub[3] / Ub[0];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { Ax[r][q] = 0.0; Ay[r][q] = 0.0; }
+    Ax[0][1] = 1.0;
+    Ay[0][2] = 1.0;
+    Ax[1][1] = (3.0 - gamma) * v1;
+    Ax[1][2] = -(gamma - 1.0) * v2;
+    Ax[2][0] = -v1 * v2;
+    Ax[2][1] = v2;
+    Ax[2][2] = v1;
+    Ax[3][3] = gamma * v1;
+    Ay[2][1] = -(gamma - 1.0) * v1;
+    Ay[2][2] = (3.0 - gamma) * v2;
+    Ay[3][3] = gamma * v2;
+    if (cf.dimensionless) {
+        const double nv = v1 * v1 + v2 * v2, e2 = cf.mach * cf.mach;
+        Ax[1][0] = -(v1 * v1) + ((gamma - 1) * nv * 0.5);
+        Ax[1][3] = (gamma - 1.0) / e2;
+        Ax[3][0] = -v1 * (gamma * E - ((gamma - 1.0) * e2 * nv));
+        Ax[3][1] = gamma * E - (gamma - 1.0) * e2 * (0.5 * nv + v1 * v1);
+        Ax[3][2] = -(gamma - 1.0) * e2 * v1 * v2;
+        Ay[2][0] = -(v2 * v2) + (((gamma - 1.0) * nv * 0.5));
+        Ay[3][0] = -v2 * (gamma * E - (gamma - 1.0) * e2 * nv);
+        Ay[3][2] = gamma * E - (gamma - 1.0) * e2 * (0.5 * nv + v2 * v2);
+    } else {
+        const double rho = Ub[0], nU = (Ub[1] * Ub[1]) + (Ub[2] * Ub[2]);
+        Ax[1][0] = -(v1 * v1) + (((gamma - 1) * nU * 0.5) / (rho * rho));
+        Ax[1][3] = gamma - 1.0;
+        Ax[3][0] = (-gamma * v1 * E) + ((gamma - 1.0) * v1 * (nU / (rho * rho)));
+        Ax[3][1] = (gamma * E) - ((gamma - 1.0) * 0.5 * ((nU / (rho * rho)) + (2.0 * v1 * v1)));
+        Ax[3][2] = -((gamma - 1.0) * v1 * v2);
+        Ay[2][0] = -(v2 * v2) + (((gamma - 1.0) * nU * 0.5) / (rho * rho));
+        Ay[3][0] = (-gamma * v2 * E) + (((gamma - 1.0) * v2 * nU) / (rho * rho));
+        Ay[3][2] = (gamma * E) - ((gamma - 1.0) * 0.5 * ((nU / (rho * rho)) + (2.0 * v2 * v2)));
+    }
+    Ay[1][0] = Ax[2][0];
+    Ay[1][1] = v2;
+    Ay[1][2] = v1;
+    Ay[2][3] = Ax[1][3];
+    Ay[3][1] = Ax[3][2];
+}
+
+// w^T A0^-1 w, symmetric expansion of Delta_CAU.c:37-63 (A0 upper triangle)
+__device__ __forceinline__ double a0_norm2(const double A0[10], const double w[4])
+{
+    // A0: 00 01 02 03 11 12 13 22 23 33
+    return w[0] * (A0[0] * w[0] + 2.0 * A0[1] * w[1] + 2.0 * A0[2] * w[2] + 2.0 * A0[3] * w[3]) +
+           w[1] * (A0[4] * w[1] + 2.0 * A0[5] * w[2] + 2.0 * A0[6] * w[3]) +
+           w[2] * (A0[7] * w[2] + 2.0 * A0[8] * w[3]) +
+           w[3] * A0[9] * w[3];
+}
+
+__global__ void __launch_bounds__(128) k_euler_elem(int nel, int ld, int n, const int *__restrict__ gien,
+                                                    const double *__restrict__ gx, const double *__restrict__ gy,
+                                                    const int *__restrict__ node_dof, const double *__restrict__ up,
+                                                    const double *__restrict__ u, const double *__restrict__ du,
+                                                    fg_euler_coeffs cf, double *__restrict__ A64,
+                                                    double *__restrict__ Fe)
+{
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const double third = 1.0 / 3.0, sixth = 1.0 / 6.0;
+    const double gamma = cf.gamma;
+    double X[3], Y[3], Ue[12], dUe[12];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const int J = gien[(size_t)v * ld + pos];
+        X[v] = gx[J];
+        Y[v] = gy[J];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int d = node_dof[4 * J + k];
+            const bool dir = d == n;
+            Ue[4 * v + k] = dir ? up[4 * J + k] : u[d];
+            dUe[4 * v + k] = dir ? 0.0 : du[d];
+        }
+    }
+    const double b[3] = {Y[1] - Y[2], Y[2] - Y[0], Y[0] - Y[1]};
+    const double c[3] = {X[2] - X[1], X[0] - X[2], X[1] - X[0]};
+    const double twoArea = fabs(c[2] * b[1] - c[1] * b[2]);
+    const double Area = 0.5 * twoArea;
+    double Ub[4], dUb[4], gxu[4], gyu[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        Ub[i] = (Ue[i] + Ue[i + 4] + Ue[i + 8]) * third;
+        dUb[i] = (dUe[i] + dUe[i + 4] + dUe[i + 8]) * third;
+        gxu[i] = (Ue[i] * b[0] + Ue[i + 4] * b[1] + Ue[i + 8] * b[2]) / twoArea;
+        gyu[i] = (Ue[i] * c[0] + Ue[i + 4] * c[1] + Ue[i + 8] * c[2]) / twoArea;
+    }
+    const double v1 = Ub[1] / Ub[0], v2 = Ub[2] / Ub[0], E = Ub[3] / Ub[0];
+    const double nU = (Ub[1] * Ub[1]) + (Ub[2] * Ub[2]);
+    double Ax[4][4], Ay[4][4];
+    eu_jacobians(cf, Ub, Ax, Ay);
+
+    // A0^-1 (Build_M_K_F_SUPG.c:131-158), upper triangle
+    double delta;
+    {
+        const double rho_i = Ub[3] - ((nU * 0.5) / Ub[0]);
+        const double V2 = Ub[1] / rho_i, V3 = Ub[2] / rho_i, V4 = (-Ub[0]) / rho_i;
+        const double re = -1.0 / (rho_i * V4);
+        const double k1 = (V2 * V2 + V3 * V3) * 0.5 / V4;
+        const double A0[10] = {re * (k1 * k1 + gamma), re * (k1 * V2),      re * (k1 * V3), re * ((k1 + 1.0) * V4),
+                               re * (V2 * V2 - V4),    re * (V2 * V3),      re * (V2 * V4), re * (V3 * V3 - V4),
+                               re * (V3 * V4),         re * V4 * V4};
+        // CAU (Delta_CAU.c:4-84)
+        double kx[4], ky[4], L[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            double sx = Ax[r][0] * gxu[0], sy = Ay[r][0] * gyu[0];
+#pragma unroll
+            for (int k = 1; k < 4; ++k) { sx += Ax[r][k] * gxu[k]; sy += Ay[r][k] * gyu[k]; }
+            L[r] = dUb[r] + sx + sy;
+            kx[r] = (b[0] * gxu[r] + c[0] * gyu[r]) / twoArea;
+            ky[r] = (b[1] * gxu[r] + c[1] * gyu[r]) / twoArea;
+        }
+        const double nk = sqrt(a0_norm2(A0, kx) + a0_norm2(A0, ky));
+        const double nL = sqrt(a0_norm2(A0, L));
+        const double ng = sqrt(a0_norm2(A0, gxu) + a0_norm2(A0, gyu));
+        delta = ng >= cf.tolerance ? nL / nk : 0.0;
+    }
+
+    // SUPG tau (:240-269)
+    double tau;
+    {
+        double betax = 2.0 * (gxu[0] * Ub[0] + gxu[1] * Ub[1] + gxu[2] * Ub[2] + gxu[3] * Ub[3]);
+        double betay = 2.0 * (gyu[0] * Ub[0] + gyu[1] * Ub[1] + gyu[2] * Ub[2] + gyu[3] * Ub[3]);
+        const double betaxy = sqrt(betax * betax + betay * betay);
+        if (betaxy != 0.0) { betax = betax / betaxy; betay = betay / betaxy; }
+        const double h = sqrt(twoArea);
+        const double avb = fabs(v1 * betax + v2 * betay);
+        const double cs = sqrt(gamma * (gamma - 1.0) * (E - 0.5 * (v1 * v1 + v2 * v2)));
+        const double CFL = ((cs + avb) * cf.dt) / h;
+        const double psi = (2.0 * cf.alpha * CFL) * (1.0 / (1.0 + 2.0 * cf.alpha * CFL));
+        const double cv = cs + avb;
+        const double tau_d = delta / (cv * cv);
+        const double tau_a = h / (2.0 * (cs + avb));
+        const double tau_t = (2.0 / (3.0 * (1.0 + 2.0 * cf.alpha * CFL))) * tau_a;
+        tau = tau_t + psi * (tau_a - tau_d);
+        if (tau < 0.0) tau = 0.0;
+    }
+
+    const double Mg1 = Area * sixth, Mg2 = Area / 12.0;
+    const double t4a = tau / (4 * Area);
+    const double d4a = delta / (4.0 * Area);
+    const double Kc01 = d4a * (b[0] * b[1] + c[0] * c[1]);
+    const double Kc02 = d4a * (b[0] * b[2] + c[0] * c[2]);
+    const double Kc12 = d4a * (b[1] * b[2] + c[1] * c[2]);
+    const double adt = cf.alpha * cf.dt;
+    double *a = A64 + pos;
+    double *fe = Fe + pos;
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) {
+        const int o1 = i == 0 ? 1 : 0, o2 = i == 2 ? 1 : 2;     // the other two nodes, ascending
+        const double kcd = i == 0 ? Kc01 + Kc02 : i == 1 ? Kc01 + Kc12 : Kc02 + Kc12;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            // row r of AxAx, AxAy, AyAx, AyAy (sums over k ascending)
+            double pxx[4], pxy[4], pyx[4], pyy[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                double s1 = Ax[r][0] * Ax[0][q], s2 = Ax[r][0] * Ay[0][q];
+                double s3 = Ay[r][0] * Ax[0][q], s4 = Ay[r][0] * Ay[0][q];
+#pragma unroll
+                for (int k = 1; k < 4; ++k) {
+                    s1 += Ax[r][k] * Ax[k][q];
+                    s2 += Ax[r][k] * Ay[k][q];
+                    s3 += Ay[r][k] * Ax[k][q];
+                    s4 += Ay[r][k] * Ay[k][q];
+                }
+                pxx[q] = s1; pxy[q] = s2; pyx[q] = s3; pyy[q] = s4;
+            }
+            const int R = 4 * i + r;
+            double m = 0, k = 0;
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const double kij = j == i ? 0.0 : (i + j == 1 ? Kc01 : i + j == 2 ? Kc02 : Kc12);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const double Ci = (b[i] * Ax[r][q] + c[i] * Ay[r][q]) * sixth;
+                    const double mpg = Ci * tau;
+                    const double Me = r == q ? (i == j ? Mg1 : Mg2) + mpg : mpg;
+                    const double kg = (b[j] * Ax[r][q] + c[j] * Ay[r][q]) * sixth;
+                    const double ax = b[i] * pxx[q] + c[i] * pyx[q];
+                    const double ay = b[i] * pxy[q] + c[i] * pyy[q];
+                    double Ke;
+                    if (i == j) {
+                        const double p1 = t4a * (b[o1] * ax + c[o1] * ay);
+                        const double p2 = t4a * (b[o2] * ax + c[o2] * ay);
+                        const double kk = kg - (p1 + p2);
+                        Ke = r == q ? kk - kcd : kk;
+                    } else {
+                        const double p = t4a * (b[j] * ax + c[j] * ay);
+                        Ke = r == q ? kg + p + kij : kg + p;
+                    }
+                    const int Q = 4 * j + q;
+                    m += Me * dUe[Q];
+                    k += Ke * Ue[Q];
+                    a[(size_t)(R * 12 + Q) * ld] = Me + adt * Ke;
+                }
+            }
+            fe[(size_t)R * ld] = -m - k;
+        }
+    }
+}
+
+int euler_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
+                          double *R_dev, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (t.ndof != 4) { set_error("Euler assembly needs ndof == 4"); return FG_ERR_UNSUPPORTED; }
+    if (!s->eu_geometry_ok) { set_error("Euler assembly before fg_euler_set_geometry"); return FG_ERR_STATE; }
+    if (t.nel > 0)
+        k_euler_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(),
+                                                         s->gx.as<double>(), s->gy.as<double>(),
+                                                         s->node_dof.as<int>(), s->gup.as<double>(), u_dev, du_dev,
+                                                         *c, s->A64.as<double>(), s->Fe.as<double>());
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    int r = gather_residual(s, s->Fe.as<double>(), R_dev, st);
+    if (r) return r;
+    s->blocks_ok = true;
+    s->csr_dirty = true;
+    return convert_blocks(s, st);
+}
+
+}  // namespace fg

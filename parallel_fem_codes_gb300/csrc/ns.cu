@@ -7,9 +7,10 @@
 // k_ns_elem is one thread per element (internal element order): gather the
 // three nodes' coordinates and (u, v, p) (free dofs from the state vector,
 // Dirichlet dofs from the prescribed values), form the 9x9 tangent straight
-// into the SoA block array and the element residual into Fe.  k_ns_F sums
-// the element residuals of every free dof in reference element order, as
-// the reference's F[lm] += Res loop does, so F is bit-identical.
+// into the SoA block array and the element residual into Fe.
+// k_elem_residual (shared with the Euler build) sums the element residuals
+// of every free dof in reference element order, as the reference's
+// F[lm] += Res loop does, so F is bit-identical.
 //
 // Every entry is the same sum of the same products, associated the same way,
 // as in the reference, written per pair of element nodes (i, j): with
@@ -168,9 +169,9 @@ __global__ void __launch_bounds__(128) k_ns_elem(int nel, int ld, int n, const i
 }
 
 // F[d] = sum of the element residual entries of dof d in reference element
-// order (Build_K_F_SUPG_PSPG.c:652-656); F[n] = 0.
-__global__ void k_ns_F(int n, int ld, const int *__restrict__ dptr, const int *__restrict__ dinc,
-                       const double *__restrict__ Fe, double *__restrict__ F)
+// order, as the builds' F[lm] += Res loops add them; F[n] = 0.
+__global__ void k_elem_residual(int n, int ld, const int *__restrict__ dptr, const int *__restrict__ dinc,
+                                const double *__restrict__ Fe, double *__restrict__ F)
 {
     const int d = blockIdx.x * blockDim.x + threadIdx.x;
     if (d > n) return;
@@ -181,6 +182,16 @@ __global__ void k_ns_F(int n, int ld, const int *__restrict__ dptr, const int *_
         s += Fe[(size_t)a * ld + pos];
     }
     F[d] = s;
+}
+
+int gather_residual(fg_system *s, const double *Fe, double *F, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    k_elem_residual<<<(t.n + 256) / 256, 256, 0, st>>>(t.n, s->nel_pad, s->dinc_ptr.as<int>(), s->dinc.as<int>(), Fe,
+                                                      F);
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    return FG_OK;
 }
 
 int ns_assemble_device(fg_system *s, double reynolds, const double *u_dev, double *F_dev, cudaStream_t st)
@@ -195,47 +206,75 @@ int ns_assemble_device(fg_system *s, double reynolds, const double *u_dev, doubl
                                                       s->gf1.as<double>(), s->gf2.as<double>(), u_dev, reynolds,
                                                       s->A64.as<double>(), s->Fe.as<double>());
     FG_CUDA(cudaGetLastError());
-    k_ns_F<<<(t.n + 256) / 256, 256, 0, st>>>(t.n, s->nel_pad, s->dinc_ptr.as<int>(), s->dinc.as<int>(),
-                                             s->Fe.as<double>(), F_dev);
-    FG_CUDA(cudaGetLastError());
-    count_launches(2);
+    count_launches(1);
+    int r = gather_residual(s, s->Fe.as<double>(), F_dev, st);
+    if (r) return r;
     s->blocks_ok = true;
     s->csr_dirty = true;
     return convert_blocks(s, st);
 }
 
-// ---------------------------------------------------------------- Picard update
-// u += s over the free dofs and the two squared norms ||s||^2, ||u||^2:
-// per-CTA partial sums, then one CTA adds them in a fixed order.
+// ---------------------------------------------------------------- state updates
+// The BLAS-1 steps of the nonlinear and time loops (daxpy, and the norms
+// their stop tests take), on the device.  Norms are per-CTA partial sums of
+// squares added by one CTA in a fixed order: deterministic for a given n.
+// Compiled without FMA contraction, like the reference's y += a * x.
 constexpr int kNormBlocks = 1024;
 
-__global__ void k_ns_update(int n, double *__restrict__ u, const double *__restrict__ s, double *__restrict__ part)
+static int norm_blocks(int n) { return std::max(1, std::min(kNormBlocks, (n + 255) / 256)); }
+
+__device__ __forceinline__ void block_sums(double a, double b, double *part)
 {
     __shared__ double sh[2][8];
-    double ss = 0.0, uu = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const double v = u[i] + 1 * s[i];
-        u[i] = v;
-        ss += s[i] * s[i];
-        uu += v * v;
-    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        ss += __shfl_down_sync(0xffffffffu, ss, o);
-        uu += __shfl_down_sync(0xffffffffu, uu, o);
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
     }
     const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) { sh[0][w] = ss; sh[1][w] = uu; }
+    if ((threadIdx.x & 31) == 0) { sh[0][w] = a; sh[1][w] = b; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { a += sh[0][k]; b += sh[1][k]; }
-        part[2 * blockIdx.x] = a;
-        part[2 * blockIdx.x + 1] = b;
+        double x = 0.0, y = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) { x += sh[0][k]; y += sh[1][k]; }
+        part[2 * blockIdx.x] = x;
+        part[2 * blockIdx.x + 1] = y;
     }
 }
 
-__global__ void k_ns_norms(const double *__restrict__ part, int nb, double *__restrict__ out)
+// y += a x; partial sums of x^2 and of the updated y^2
+__global__ void __launch_bounds__(256) k_axpy_sq(int n, double a, const double *__restrict__ x,
+                                                 double *__restrict__ y, double *__restrict__ part)
+{
+    double xx = 0.0, yy = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double xi = x[i], v = y[i] + a * xi;
+        y[i] = v;
+        xx += xi * xi;
+        yy += v * v;
+    }
+    block_sums(xx, yy, part);
+}
+
+// partial sums of (u - v)^2 and u^2
+__global__ void __launch_bounds__(256) k_diff_sq(int n, const double *__restrict__ u, const double *__restrict__ v,
+                                                 double *__restrict__ part)
+{
+    double dd = 0.0, uu = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double d = u[i] - v[i];
+        dd += d * d;
+        uu += u[i] * u[i];
+    }
+    block_sums(dd, uu, part);
+}
+
+__global__ void k_axpy(int n, double a, const double *__restrict__ x, double *__restrict__ y)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] += a * x[i];
+}
+
+__global__ void k_sum_parts(const double *__restrict__ part, int nb, double *__restrict__ out)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double a = 0.0, b = 0.0;
@@ -244,17 +283,34 @@ __global__ void k_ns_norms(const double *__restrict__ part, int nb, double *__re
     out[1] = b;
 }
 
-int ns_update_device(fg_system *s, double *u_dev, const double *s_dev, double *part, double *out, cudaStream_t st)
+int axpy_norms_device(int n, double a, const double *x, double *y, double *part, double *out, cudaStream_t st)
 {
-    const int n = s->topo.n;
-    const int nb = std::max(1, std::min(kNormBlocks, (n + 255) / 256));
-    k_ns_update<<<nb, 256, 0, st>>>(n, u_dev, s_dev, part);
-    k_ns_norms<<<1, 32, 0, st>>>(part, nb, out);
+    const int nb = norm_blocks(n);
+    k_axpy_sq<<<nb, 256, 0, st>>>(n, a, x, y, part);
+    k_sum_parts<<<1, 32, 0, st>>>(part, nb, out);
     FG_CUDA(cudaGetLastError());
     count_launches(2);
     return FG_OK;
 }
 
-size_t ns_update_scratch_bytes() { return sizeof(double) * (2 * kNormBlocks + 2); }
+int diff_norms_device(int n, const double *u, const double *v, double *part, double *out, cudaStream_t st)
+{
+    const int nb = norm_blocks(n);
+    k_diff_sq<<<nb, 256, 0, st>>>(n, u, v, part);
+    k_sum_parts<<<1, 32, 0, st>>>(part, nb, out);
+    FG_CUDA(cudaGetLastError());
+    count_launches(2);
+    return FG_OK;
+}
+
+int axpy_device(int n, double a, const double *x, double *y, cudaStream_t st)
+{
+    k_axpy<<<norm_blocks(n), 256, 0, st>>>(n, a, x, y);
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    return FG_OK;
+}
+
+size_t norm_scratch_bytes() { return sizeof(double) * (2 * kNormBlocks + 2); }
 
 }  // namespace fg

@@ -68,7 +68,7 @@ size_t fg_system::bytes() const
                            &csr_ia, &csr_ja, &csr_diag, &csr_inc_ptr, &csr_inc, &AA64, &AA32, &LU64, &LU32,
                            &dinv64, &dinv32, &ilu_flags, &ilu_ctr,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
-                           &ginvp, &Fe, &F64, &gf1, &gf2, &ns_u, &ns_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
+                           &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
                            &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
     size_t b = 0;
     for (auto *m : all) b += m->bytes;
@@ -253,6 +253,22 @@ static int vec_out(fg_system *s, const double *d_int, double *h, double *d_tmp)
     int r = permute_out(s, d_int, d_tmp, s->stream);
     if (r) return r;
     FG_CUDA(cudaMemcpyAsync(h, d_tmp, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToHost, s->stream));
+    return FG_OK;
+}
+
+// host state (n entries, reference numbering, NULL = 0) -> device internal numbering
+static int state_in(fg_system *s, const double *h, double *d)
+{
+    if (!h) {
+        FG_CUDA(cudaMemsetAsync(d, 0, 8 * (size_t)s->n_pad, s->stream));
+        return FG_OK;
+    }
+    std::memcpy(s->h_vec, h, 8 * (size_t)s->topo.n);
+    s->h_vec[s->topo.n] = 0.0;
+    int r = vec_in(s, s->h_vec, d, s->ws.r64.as<double>());
+    if (r) return r;
+    // the pinned staging buffer is reused by the next transfer
+    FG_CUDA(cudaStreamSynchronize(s->stream));
     return FG_OK;
 }
 
@@ -465,13 +481,7 @@ int fg_transport_prepare(fg_system *s, const fg_transport_coeffs *c, const doubl
     int r = ensure_io(s);
     if (r) return r;
     if ((r = stage(s, s->rhs_f, 8 * (size_t)s->n_pad)) || (r = stage(s, s->rhs_b, 8 * (size_t)s->n_pad))) return r;
-    if (u) {
-        std::memcpy(s->h_vec, u, 8 * (size_t)s->topo.n);
-        s->h_vec[s->topo.n] = 0.0;
-        if ((r = vec_in(s, s->h_vec, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
-    } else {
-        FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, 8 * (size_t)s->n_pad, s->stream));
-    }
+    if ((r = state_in(s, u, s->ws.t64.as<double>()))) return r;
     if ((r = transport_assemble_device(s, c, s->ws.t64.as<double>(), s->rhs_f.as<double>(), s->stream))) return r;
     FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, 8 * (size_t)s->n_pad, s->stream));
     FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, 8 * (size_t)s->n_pad, cudaMemcpyDeviceToDevice, s->stream));
@@ -500,14 +510,7 @@ int fg_transport_assemble(fg_system *s, const fg_transport_coeffs *c, const doub
     if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
     int r = ensure_io(s);
     if (r) return r;
-    if (u) {
-        // u has n entries: stage it as an n+1 vector with the sink at 0
-        std::memcpy(s->h_vec, u, 8 * (size_t)s->topo.n);
-        s->h_vec[s->topo.n] = 0.0;
-        if ((r = vec_in(s, s->h_vec, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
-    } else {
-        FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
-    }
+    if ((r = state_in(s, u, s->ws.t64.as<double>()))) return r;
     if ((r = transport_assemble_device(s, c, s->ws.t64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
     if (F) {
         if ((r = vec_out(s, s->ws.u64.as<double>(), F, s->ws.r64.as<double>()))) return r;
@@ -584,13 +587,7 @@ int fg_ns_assemble(fg_system *s, const fg_ns_coeffs *c, const double *u, double 
     if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
     int r = ensure_io(s);
     if (r) return r;
-    if (u) {
-        std::memcpy(s->h_vec, u, 8 * (size_t)s->topo.n);
-        s->h_vec[s->topo.n] = 0.0;
-        if ((r = vec_in(s, s->h_vec, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
-    } else {
-        FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
-    }
+    if ((r = state_in(s, u, s->ws.t64.as<double>()))) return r;
     if ((r = ns_assemble_device(s, c->reynolds, s->ws.t64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
     if (F) {
         if ((r = vec_out(s, s->ws.u64.as<double>(), F, s->ws.r64.as<double>()))) return r;
@@ -622,21 +619,19 @@ int fg_ns_process(fg_system *s, const fg_ns_coeffs *c, const fg_solver_opts *o, 
     if (r) return r;
     cfg.device_io = 1;
     if ((r = ensure_io(s)) || (r = stage(s, s->rhs_f, 8 * (size_t)s->n_pad)) ||
-        (r = stage(s, s->rhs_b, 8 * (size_t)s->n_pad)) || (r = stage(s, s->ns_u, 8 * (size_t)s->n_pad)) ||
-        (r = stage(s, s->ns_part, ns_update_scratch_bytes())))
+        (r = stage(s, s->rhs_b, 8 * (size_t)s->n_pad)) || (r = stage(s, s->state_u, 8 * (size_t)s->n_pad)) ||
+        (r = stage(s, s->norm_part, norm_scratch_bytes())))
         return r;
-    std::memcpy(s->h_vec, u, 8 * (size_t)n);
-    s->h_vec[n] = 0.0;
-    FG_CUDA(cudaMemsetAsync(s->ns_u.p, 0, s->ns_u.bytes, s->stream));
-    if ((r = vec_in(s, s->h_vec, s->ns_u.as<double>(), s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaMemsetAsync(s->state_u.p, 0, s->state_u.bytes, s->stream));
+    if ((r = state_in(s, u, s->state_u.as<double>()))) return r;
     // a fresh run starts from a zero diagonal (Preprocess.c:316 callocs it)
     if (c->precond == FG_PRECOND_DIAG) FG_CUDA(cudaMemsetAsync(s->diag.p, 0, s->diag.bytes, s->stream));
-    double *part = s->ns_part.as<double>(), *norms = part + (s->ns_part.bytes / 8 - 2);
+    double *part = s->norm_part.as<double>(), *norms = part + (s->norm_part.bytes / 8 - 2);
     double delta = nonlinear_tol + 1.0, last_res = NAN;
     int it = 0, gmres = 0;
     while (delta > nonlinear_tol && it < max_nonlinear) {
         ++it;
-        if ((r = ns_assemble_device(s, c->reynolds, s->ns_u.as<double>(), s->rhs_f.as<double>(), s->stream))) return r;
+        if ((r = ns_assemble_device(s, c->reynolds, s->state_u.as<double>(), s->rhs_f.as<double>(), s->stream))) return r;
         FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, 8 * (size_t)s->n_pad, cudaMemcpyDeviceToDevice, s->stream));
         int flags = c->precond == FG_PRECOND_DIAG ? FG_SETUP_ACCUMULATE : 0;
         if ((r = precond_setup_device(s, c->precond, flags, s->rhs_b.as<double>(), s->stream))) return r;
@@ -647,12 +642,13 @@ int fg_ns_process(fg_system *s, const fg_ns_coeffs *c, const fg_solver_opts *o, 
         if ((r = solve_batch(mem, cfg, &st, s->stream))) return r;
         gmres += st.iterations;
         last_res = st.true_rel_residual;
-        if ((r = ns_update_device(s, s->ns_u.as<double>(), s->ws.x.as<double>(), part, norms, s->stream))) return r;
+        if ((r = axpy_norms_device(n, 1, s->ws.x.as<double>(), s->state_u.as<double>(), part, norms, s->stream)))
+            return r;
         FG_CUDA(cudaMemcpyAsync(s->h_vec, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
         FG_CUDA(cudaStreamSynchronize(s->stream));
         delta = std::sqrt(s->h_vec[0]) / std::sqrt(s->h_vec[1]);
     }
-    if ((r = vec_out(s, s->ns_u.as<double>(), s->h_vec, s->ws.r64.as<double>()))) return r;
+    if ((r = vec_out(s, s->state_u.as<double>(), s->h_vec, s->ws.r64.as<double>()))) return r;
     FG_CUDA(cudaStreamSynchronize(s->stream));
     std::memcpy(u, s->h_vec, 8 * (size_t)n);
     if (stats) {
@@ -661,6 +657,138 @@ int fg_ns_process(fg_system *s, const fg_ns_coeffs *c, const fg_solver_opts *o, 
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         stats->true_rel_residual = last_res;
         stats->nonlinear_residual = delta;
+    }
+    return FG_OK;
+}
+
+int fg_euler_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc)
+{
+    if (!s || !x || !y || !upresc) { set_error("NULL argument"); return FG_ERR_ARG; }
+    const Topology &t = s->topo;
+    if (t.ndof != 4) { set_error("Euler geometry needs a system with ndof == 4"); return FG_ERR_UNSUPPORTED; }
+    const size_t nn = (size_t)t.nnodes;
+    std::vector<double> vx(x, x + nn), vy(y, y + nn), vu(upresc, upresc + 4 * nn);
+    int r;
+    if ((r = upload(s->gx, vx)) || (r = upload(s->gy, vy)) || (r = upload(s->gup, vu)) ||
+        (r = s->Fe.alloc(8 * (size_t)12 * s->nel_pad)))
+        return r;
+    s->eu_geometry_ok = true;
+    return FG_OK;
+}
+
+int fg_euler_assemble(fg_system *s, const fg_euler_coeffs *c, const double *u, const double *du, double *R)
+{
+    if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = stage(s, s->state_a, 8 * (size_t)s->n_pad))) return r;
+    if ((r = state_in(s, u, s->ws.t64.as<double>())) || (r = state_in(s, du, s->state_a.as<double>()))) return r;
+    if ((r = euler_assemble_device(s, c, s->ws.t64.as<double>(), s->state_a.as<double>(), s->ws.u64.as<double>(),
+                                   s->stream)))
+        return r;
+    if (R && (r = vec_out(s, s->ws.u64.as<double>(), R, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+// Predictor_Old.c:6-134 with the state (u, a, u_old), the residual and the
+// increment kept on the device; per correction one assembly, one
+// preconditioner set-up, one batched-engine solve and two update kernels.
+// Only the norms the stop tests read come back to the host.
+int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *o, const fg_time_opts *to,
+                       double *u, double *a, fg_time_stats *stats)
+{
+    if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (to->precond != FG_PRECOND_NONE && to->precond != FG_PRECOND_DIAG && to->precond != FG_PRECOND_BLOCKDIAG) {
+        set_error("Euler preconditioner must be NONE, DIAG or BLOCKDIAG");
+        return FG_ERR_ARG;
+    }
+    if (to->max_corrections < 1 || !(c->dt > 0)) { set_error("max_corrections >= 1 and dt > 0 required"); return FG_ERR_ARG; }
+    auto t0 = std::chrono::steady_clock::now();
+    const int n = s->topo.n;
+    fg_system *one[1] = {s};
+    SolveConfig cfg;
+    int r = batch_config(one, 1, o, cfg);
+    if (r) return r;
+    cfg.device_io = 1;
+    const size_t vb = 8 * (size_t)s->n_pad;
+    if ((r = ensure_io(s)) || (r = stage(s, s->rhs_f, vb)) || (r = stage(s, s->rhs_b, vb)) ||
+        (r = stage(s, s->state_u, vb)) || (r = stage(s, s->state_a, vb)) || (r = stage(s, s->state_old, vb)) ||
+        (r = stage(s, s->norm_part, norm_scratch_bytes())))
+        return r;
+    double *du = s->state_u.as<double>(), *da = s->state_a.as<double>(), *dold = s->state_old.as<double>();
+    FG_CUDA(cudaMemsetAsync(s->state_u.p, 0, vb, s->stream));
+    if ((r = state_in(s, u, du))) return r;
+    FG_CUDA(cudaMemsetAsync(da, 0, vb, s->stream));
+    if (to->precond == FG_PRECOND_DIAG) FG_CUDA(cudaMemsetAsync(s->diag.p, 0, s->diag.bytes, s->stream));
+    double *part = s->norm_part.as<double>(), *norms = part + (s->norm_part.bytes / 8 - 2);
+    const double dt = c->dt, alpha = c->alpha;
+    double t = 0.0, last_res = NAN;
+    int steps = 0, corr = 0, gmres = 0;
+    bool stop_time = false;
+    do {
+        ++steps;
+        t += dt;
+        FG_CUDA(cudaMemcpyAsync(dold, du, 8 * (size_t)n, cudaMemcpyDeviceToDevice, s->stream));
+        if ((r = axpy_device(n, (1.0 - alpha) * dt, da, du, s->stream))) return r;      // prediction
+        FG_CUDA(cudaMemsetAsync(da, 0, 8 * (size_t)n, s->stream));
+        int it = 0;
+        bool stop = false;
+        do {                                                                          // multicorrection
+            ++it;
+            if ((r = euler_assemble_device(s, c, du, da, s->rhs_f.as<double>(), s->stream))) return r;
+            FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, vb, cudaMemcpyDeviceToDevice, s->stream));
+            int flags = to->setup_flags | (to->precond == FG_PRECOND_DIAG ? FG_SETUP_ACCUMULATE : 0);
+            if ((r = precond_setup_device(s, to->precond, flags, s->rhs_b.as<double>(), s->stream))) return r;
+            s->rhs_ok = true;
+            cfg.precond = s->precond;
+            std::vector<BatchMember> mem{{s, s->rhs_b.as<double>(), s->rhs_f.as<double>(), nullptr}};
+            fg_solve_stats st{};
+            if ((r = solve_batch(mem, cfg, &st, s->stream))) return r;
+            gmres += st.iterations;
+            last_res = st.true_rel_residual;
+            const double *Da = s->ws.x.as<double>();
+            if ((r = axpy_norms_device(n, 1, Da, da, part, norms, s->stream))) return r;   // a += Da
+            if ((r = axpy_device(n, alpha * dt, Da, du, s->stream))) return r;           // u += alpha dt Da
+            if (to->stop_by_norm) {
+                FG_CUDA(cudaMemcpyAsync(s->h_vec, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+                FG_CUDA(cudaStreamSynchronize(s->stream));
+                const double norm_Da = std::sqrt(s->h_vec[0]), norm_a = std::sqrt(s->h_vec[1]);
+                stop = norm_Da < to->correction_tol * norm_a || it >= to->max_corrections;
+            } else {
+                stop = it >= to->max_corrections;
+            }
+        } while (!stop);
+        corr += it;
+        if (to->steady_state) {
+            if ((r = diff_norms_device(n, du, dold, part, norms, s->stream))) return r;
+            FG_CUDA(cudaMemcpyAsync(s->h_vec, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+            FG_CUDA(cudaStreamSynchronize(s->stream));
+            const double nd = std::sqrt(s->h_vec[0]), nu = std::sqrt(s->h_vec[1]);
+            stop_time = to->time_tol * nu > nd || std::fabs(to->final_time - t) < dt;
+        } else {
+            stop_time = to->final_time - t < 1e-10;
+        }
+        if (to->max_steps > 0 && steps >= to->max_steps) stop_time = true;
+    } while (!stop_time);
+    if ((r = vec_out(s, du, s->h_vec, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    std::memcpy(u, s->h_vec, 8 * (size_t)n);
+    if (a) {
+        if ((r = vec_out(s, da, s->h_vec, s->ws.r64.as<double>()))) return r;
+        FG_CUDA(cudaStreamSynchronize(s->stream));
+        std::memcpy(a, s->h_vec, 8 * (size_t)n);
+    }
+    if (stats) {
+        stats->steps = steps;
+        stats->corrections = corr;
+        stats->gmres_iterations = gmres;
+        stats->t = t;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        stats->true_rel_residual = last_res;
     }
     return FG_OK;
 }

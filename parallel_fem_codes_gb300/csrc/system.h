@@ -44,9 +44,10 @@ struct fg_system {
     // geometry (device assembly)
     fg::DevMem gx, gy, gup, gien, gtype, ginvp, Fe, F64;
     bool geometry_ok = false;
-    // Navier-Stokes: nodal body force, Picard state and norm scratch (gup holds 3 values per node)
-    fg::DevMem gf1, gf2, ns_u, ns_part;
-    bool ns_geometry_ok = false;
+    // Navier-Stokes / Euler: nodal body force (gup holds ndof values per node),
+    // state of the nonlinear and time loops (internal numbering) and norm scratch
+    fg::DevMem gf1, gf2, state_u, state_a, state_old, norm_part;
+    bool ns_geometry_ok = false, eu_geometry_ok = false;
     // resident right-hand side (internal numbering): F and M^-1 F
     fg::DevMem rhs_f, rhs_b;
     bool rhs_ok = false;
@@ -158,10 +159,18 @@ int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const ECh
 // Matvec on device vectors in internal numbering (precision 64 or 32).
 int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaStream_t st);
 
-// Navier-Stokes (ns.cu)
+// Navier-Stokes (ns.cu), residual gather and the loops' BLAS-1 steps
 int ns_assemble_device(fg_system *s, double reynolds, const double *u_dev, double *F_dev, cudaStream_t st);
-int ns_update_device(fg_system *s, double *u_dev, const double *s_dev, double *part, double *out, cudaStream_t st);
-size_t ns_update_scratch_bytes();
+int gather_residual(fg_system *s, const double *Fe, double *F, cudaStream_t st);
+// y += a x, out[0] = sum x^2, out[1] = sum y^2 (after the update)
+int axpy_norms_device(int n, double a, const double *x, double *y, double *part, double *out, cudaStream_t st);
+// out[0] = sum (u - v)^2, out[1] = sum u^2
+int diff_norms_device(int n, const double *u, const double *v, double *part, double *out, cudaStream_t st);
+int axpy_device(int n, double a, const double *x, double *y, cudaStream_t st);
+size_t norm_scratch_bytes();
+// Euler (euler.cu)
+int euler_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
+                          double *R_dev, cudaStream_t st);
 
 // Set-up kernels (setup.cu)
 int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaStream_t st);

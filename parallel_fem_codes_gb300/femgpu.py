@@ -67,6 +67,22 @@ class NSCoeffs(ctypes.Structure):
     _fields_ = [("reynolds", _c_dbl), ("precond", _c_int)]
 
 
+class EulerCoeffs(ctypes.Structure):
+    _fields_ = [("gamma", _c_dbl), ("mach", _c_dbl), ("dimensionless", _c_int), ("tolerance", _c_dbl),
+                ("alpha", _c_dbl), ("dt", _c_dbl)]
+
+
+class TimeOpts(ctypes.Structure):
+    _fields_ = [("stop_by_norm", _c_int), ("max_corrections", _c_int), ("correction_tol", _c_dbl),
+                ("steady_state", _c_int), ("final_time", _c_dbl), ("time_tol", _c_dbl), ("max_steps", _c_int),
+                ("precond", _c_int), ("setup_flags", _c_int)]
+
+
+class TimeStats(ctypes.Structure):
+    _fields_ = [("steps", _c_int), ("corrections", _c_int), ("gmres_iterations", _c_int), ("t", _c_dbl),
+                ("seconds", _c_dbl), ("true_rel_residual", _c_dbl)]
+
+
 class ServerOpts(ctypes.Structure):
     _fields_ = [("kmax", _c_int), ("lmax", _c_int), ("tol", _c_dbl), ("precision", _c_int),
                 ("inner_tol", _c_dbl), ("hbm_budget_bytes", ctypes.c_size_t), ("max_active", _c_int)]
@@ -134,6 +150,10 @@ def lib(build_if_missing: bool = True):
     L.fg_ns_assemble.argtypes = [_vp, ctypes.POINTER(NSCoeffs), _vp, _vp]
     L.fg_ns_process.argtypes = [_vp, ctypes.POINTER(NSCoeffs), ctypes.POINTER(SolverOpts), _c_dbl, _c_int, _f64p,
                                 ctypes.POINTER(ProcessStats)]
+    L.fg_euler_set_geometry.argtypes = [_vp, _f64p, _f64p, _f64p]
+    L.fg_euler_assemble.argtypes = [_vp, ctypes.POINTER(EulerCoeffs), _vp, _vp, _vp]
+    L.fg_euler_predictor.argtypes = [_vp, ctypes.POINTER(EulerCoeffs), ctypes.POINTER(SolverOpts),
+                                     ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
     L.fg_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerOpts)]
     L.fg_server_submit.argtypes = [_vp, _vp, ctypes.POINTER(TransportCoeffs), ctypes.c_ulonglong]
     L.fg_server_poll.argtypes = [_vp, _vp, _c_int, ctypes.POINTER(_c_int)]
@@ -347,6 +367,56 @@ class System:
         check(lib().fg_ns_process(self._h, ctypes.byref(c), ctypes.byref(o), nonlinear_tol, max_nonlinear, u,
                                   ctypes.byref(st)))
         return u, {k: getattr(st, k) for k, _ in st._fields_}
+
+    # ---- compressible Euler (ndof = 4)
+    def euler_set_geometry(self, prob):
+        check(lib().fg_euler_set_geometry(self._h, np.ascontiguousarray(self.mesh.x, dtype=np.float64),
+                                          np.ascontiguousarray(self.mesh.y, dtype=np.float64),
+                                          np.ascontiguousarray(prob.upresc, dtype=np.float64)))
+
+    def euler_assemble(self, prob, u=None, du=None):
+        """Build_M_K_F_SUPG at (u, du) (free dofs, reference numbering); returns R (n+1)."""
+        c = euler_coeffs(prob)
+        R = np.empty(self.n + 1)
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        dd = None if du is None else np.ascontiguousarray(du, dtype=np.float64)
+        check(lib().fg_euler_assemble(self._h, ctypes.byref(c), _ptr(uu), _ptr(dd), R.ctypes.data))
+        return R
+
+    def euler_predictor(self, prob, topts, u0=None, kmax=25, lmax=1000, tol=1e-10, precision=FG_PREC_FP64,
+                        inner_tol=0.0):
+        """Predictor_Old from u0 (default: the problem's initial state); returns (u, a, stats)."""
+        c = euler_coeffs(prob)
+        o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+        u = prob.initial_state() if u0 is None else np.array(u0, dtype=np.float64, copy=True)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        a = np.zeros(self.n)
+        st = TimeStats()
+        check(lib().fg_euler_predictor(self._h, ctypes.byref(c), ctypes.byref(o), ctypes.byref(topts), u,
+                                       a.ctypes.data, ctypes.byref(st)))
+        return u, a, {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def euler_coeffs(prob) -> EulerCoeffs:
+    return EulerCoeffs(prob.gamma, prob.mach, int(prob.dimensionless), prob.tolerance, prob.alpha, prob.dt)
+
+
+def time_opts(stop_by_norm=0, max_corrections=2, correction_tol=1e-3, steady_state=0, final_time=0.0,
+              time_tol=1e-6, max_steps=0, precond=None, setup_flags=None) -> TimeOpts:
+    """Criteria.c controls; the preconditioner defaults to the reference's
+    BlockDiag with its 4x4 inverse (FG_SETUP_REF_QUIRKS)."""
+    precond = FG_PRECOND_BLOCKDIAG if precond is None else precond
+    setup_flags = FG_SETUP_REF_QUIRKS if setup_flags is None else setup_flags
+    return TimeOpts(stop_by_norm, max_corrections, correction_tol, steady_state, final_time, time_tol, max_steps,
+                    precond, setup_flags)
+
+
+def euler_system(prob) -> System:
+    """A System (ndof = 4, node-order numbering) with the geometry and
+    prescribed values of an Euler problem."""
+    s = System(prob.mesh, reorder=False)
+    s.euler_set_geometry(prob)
+    return s
 
 
 def ns_system(prob) -> System:
