@@ -295,3 +295,38 @@ int or_ebe_diag_solve(int nel, int S, const int *lm, const double *A, int NEQ,
     or_pgmres(NEQ, kmax, lmax, tol, ebe_mv_cb, diag_pc_cb, &c, F, X, &it);
     return it;
 }
+
+/* ---- EBE + nodal block-diagonal solve helper (NS / Euler drivers) ---- */
+typedef struct {
+    int nel, S, NEQ, nnodes, B;
+    const int *lm, *Id;
+    const double *A, *inv;
+} blk_ctx;
+
+static int blk_mv_cb(void *p, double *P, double *Q)
+{
+    blk_ctx *c = (blk_ctx *)p;
+    or_ebemv(c->nel, c->S, c->lm, c->A, c->NEQ, P, Q);
+    return 0;
+}
+
+static int blk_pc_cb(void *p, double *x, double *z)
+{
+    blk_ctx *c = (blk_ctx *)p;
+    or_blockdiag_apply(c->nnodes, c->B, c->Id, c->NEQ, c->inv, x, z);
+    return 0;
+}
+
+int or_ebe_block_solve(int nnodes, int nel, int B, const int *ien, const int *lm, const double *A,
+                       const int *Id, int NEQ, int ref_quirks, double *F, int kmax, int lmax,
+                       double tol, double *X)
+{
+    double *bd = malloc(sizeof(double) * (size_t)B * B * (nnodes ? nnodes : 1));
+    double *inv = malloc(sizeof(double) * (size_t)B * B * (nnodes ? nnodes : 1));
+    blk_ctx c = { nel, 3 * B, NEQ, nnodes, B, lm, Id, A, inv };
+    int it = 0;
+    or_blockdiag_setup(nnodes, nel, B, ien, A, Id, NEQ, ref_quirks, bd, inv, F);
+    or_pgmres(NEQ, kmax, lmax, tol, blk_mv_cb, blk_pc_cb, &c, F, X, &it);
+    free(bd); free(inv);
+    return it;
+}

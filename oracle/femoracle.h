@@ -88,6 +88,13 @@ int or_pgmres(int NEQ, int kmax, int lmax, double tol,
               or_mv_fn mv, or_pc_fn precond, void *ctx,
               double *B, double *X, int *iterations);
 
+/* One linear solve of an assembled EBE system (S = 3B) with the nodal
+ * block-diagonal preconditioner: set-up (F preconditioned in place), then
+ * pgmres.  Returns GMRES iterations. */
+int or_ebe_block_solve(int nnodes, int nel, int B, const int *ien, const int *lm, const double *A,
+                       const int *Id, int NEQ, int ref_quirks, double *F, int kmax, int lmax,
+                       double tol, double *X);
+
 /* ---- steady SUPG/CAU transport (01_SS_Transport_Equation) ---- */
 typedef struct {
     double k;            /* Condutivity() for kx and ky                      */

@@ -69,6 +69,8 @@ def lib():
                                            _f64p, ctypes.POINTER(_c_int)]
         L.or_ebe_diag_solve.argtypes = [_c_int, _c_int, _i32p, _f64p, _c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         _f64p, _f64p, _f64p, _c_int, _c_int, _c_dbl, _f64p]
+        L.or_ebe_block_solve.argtypes = [_c_int, _c_int, _c_int, _i32p, _i32p, _f64p, _i32p, _c_int, _c_int,
+                                         _f64p, _c_int, _c_int, _c_dbl, _f64p]
         L.or_build_ns.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
                                   ctypes.c_void_p, _f64p, _f64p, _f64p]
         L.or_build_ns.restype = None
@@ -133,6 +135,8 @@ def ref_ns():
         R.fr_ns_ebemv.restype = None
         R.fr_ns_process.argtypes = mesh + [_c_dbl, _f64p, _c_int, _c_dbl, _c_dbl, _c_int, _c_int, _c_int,
                                            _f64p, ctypes.POINTER(_c_int)]
+        R.fr_ns_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
+        R.fr_ns_layout.restype = None
         _ref_ns = R
     return _ref_ns
 
@@ -156,6 +160,8 @@ def ref_euler():
         R.fr_eu_ebemv.restype = None
         R.fr_eu_predictor.argtypes = mesh + [_f64p, _f64p, _c_int, _f64p, _f64p, _c_int, _c_int, _c_dbl,
                                              _f64p, ctypes.POINTER(_c_dbl)]
+        R.fr_eu_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
+        R.fr_eu_layout.restype = None
         _ref_eu = R
     return _ref_eu
 
@@ -455,6 +461,20 @@ def ebe_diag_solve(lm, A, NEQ, F, perm=None, inv=None, Diag=None, kmax=30, lmax=
                                  np.ascontiguousarray(A, dtype=np.float64).reshape(-1), NEQ,
                                  pp, ip, Diag, invDiag, F, kmax, lmax, tol, X)
     return X, it, Diag, invDiag, F
+
+
+def ebe_block_solve(mesh, A, F, kmax=30, lmax=1000, tol=1e-10, ref_quirks=True):
+    """Nodal block-diagonal set-up + pgmres on EBE blocks; returns (X, iterations, F')."""
+    B = mesh.ndof
+    Id = np.where(mesh.type == 0, mesh.neq, mesh.invp).astype(np.int32)
+    F = np.array(F, dtype=np.float64, copy=True)
+    X = np.zeros(mesh.neq + 1)
+    lm = fill_lm(mesh)
+    it = lib().or_ebe_block_solve(mesh.nnodes, mesh.nel, B, np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1),
+                                  np.ascontiguousarray(lm, dtype=np.int32).reshape(-1),
+                                  np.ascontiguousarray(A, dtype=np.float64).reshape(-1), Id, mesh.neq,
+                                  int(ref_quirks), F, kmax, lmax, tol, X)
+    return X, it, F
 
 
 def transport_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=1000):

@@ -211,3 +211,42 @@ int fr_ns_process(int nnodes, int nel, const double *x, const double *y, const i
     fr_ns_free(&c);
     return 0;
 }
+
+/* Layout pin: the same sizes and offsets the drop-in shim reports for its
+ * restated structs (parallel_fem_codes_gb300/compat/compat_block.c). */
+#include <stddef.h>
+void fr_ns_layout(long *out)
+{
+    int i = 0;
+    out[i++] = (long)sizeof(ParametersType);
+    out[i++] = (long)offsetof(ParametersType, SolverTolerance);
+    out[i++] = (long)offsetof(ParametersType, KrylovBasisVectorsQuantity);
+    out[i++] = (long)offsetof(ParametersType, nnodes);
+    out[i++] = (long)offsetof(ParametersType, nel);
+    out[i++] = (long)offsetof(ParametersType, neq);
+    out[i++] = (long)offsetof(ParametersType, neq_bef);
+    out[i++] = (long)offsetof(ParametersType, NEQ);
+    out[i++] = (long)offsetof(ParametersType, iterations);
+    out[i++] = (long)offsetof(ParametersType, RANK);
+    out[i++] = (long)offsetof(ParametersType, NPROC);
+    out[i++] = (long)offsetof(ParametersType, LinearMaxIter);
+    out[i++] = (long)offsetof(ParametersType, PardisoVariables);
+    out[i++] = (long)sizeof(MatrixDataType);
+    out[i++] = (long)offsetof(MatrixDataType, Aaux);
+    out[i++] = (long)offsetof(MatrixDataType, Diag);
+    out[i++] = (long)offsetof(MatrixDataType, invDiag);
+    out[i++] = (long)offsetof(MatrixDataType, Id);
+    out[i++] = (long)offsetof(MatrixDataType, A_SPIKE);
+    out[i++] = (long)sizeof(FemStructsType);
+    out[i++] = (long)offsetof(FemStructsType, Node);
+    out[i++] = (long)offsetof(FemStructsType, Element);
+    out[i++] = (long)offsetof(FemStructsType, IdRecv_aft);
+    out[i++] = (long)sizeof(FemFunctionsType);
+    out[i++] = (long)offsetof(FemFunctionsType, mv);
+    out[i++] = (long)offsetof(FemFunctionsType, precond);
+    out[i++] = (long)offsetof(FemFunctionsType, precondR);
+    out[i++] = (long)offsetof(FemFunctionsType, precond_setup);
+    out[i++] = (long)sizeof(NodeType);
+    out[i++] = (long)offsetof(NodeType, invP_id);
+    out[i++] = (long)sizeof(ElementType);
+}

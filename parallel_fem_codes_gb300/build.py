@@ -14,6 +14,9 @@ CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT, "libfemgpu.so")
 COMPAT_SST = os.path.join(OUT, "libfemgpu_sst.so")
+COMPAT_NS = os.path.join(OUT, "libfemgpu_ns.so")
+COMPAT_EULER = os.path.join(OUT, "libfemgpu_euler.so")
+COMPAT = [COMPAT_SST, COMPAT_NS, COMPAT_EULER]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, extra flags); setup.cu is rounded exactly as written (no FMA
@@ -55,18 +58,22 @@ def build(force: bool = False) -> str:
     hdrs = [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh"))]
     hdrs.append(os.path.join(os.path.dirname(PKG), "include", "femgpu.h"))
     srcs += [os.path.join(PKG, "compat", f) for f in os.listdir(os.path.join(PKG, "compat"))]
-    if not force and os.path.exists(LIB) and os.path.exists(COMPAT_SST):
-        t = min(os.path.getmtime(LIB), os.path.getmtime(COMPAT_SST))
+    if not force and all(os.path.exists(f) for f in [LIB] + COMPAT):
+        t = min(os.path.getmtime(f) for f in [LIB] + COMPAT)
         if all(os.path.getmtime(f) < t for f in srcs + hdrs + [__file__]):
             return LIB
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(lambda u: _compile(*u), UNITS))
     subprocess.run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"], check=True)
-    # drop-in shim with the reference's entry-point names (steady transport)
+    # drop-in shims with the reference's entry-point names: steady transport,
+    # steady Navier-Stokes and Euler drivers (one per struct layout)
     cc = os.environ.get("CC", "gcc")
-    subprocess.run([cc, "-O2", "-fPIC", "-shared", "-std=gnu99", "-Wall", "-o", COMPAT_SST,
-                    os.path.join(PKG, "compat", "compat_sst.c"), "-L" + OUT, "-lfemgpu",
-                    "-Wl,-rpath,$ORIGIN"], check=True)
+    shims = [(COMPAT_SST, "compat_sst.c", []), (COMPAT_NS, "compat_block.c", ["-DFGC_NS"]),
+             (COMPAT_EULER, "compat_block.c", ["-DFGC_EULER"])]
+    for out, src, defs in shims:
+        subprocess.run([cc, "-O2", "-fPIC", "-shared", "-std=gnu99", "-Wall", *defs, "-o", out,
+                        os.path.join(PKG, "compat", src), "-L" + OUT, "-lfemgpu", "-Wl,-rpath,$ORIGIN"],
+                       check=True)
     return LIB
 
 

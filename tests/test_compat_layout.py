@@ -28,3 +28,33 @@ def test_shim_layout_matches_reference_header():
     refapi.shim().fgc_sst_layout(ours)
     theirs = O.ref_layout()
     assert np.array_equal(ours[:37], theirs[:37])
+
+
+@pytest.mark.parametrize("kind,names", [
+    ("ns", ("pgmres", "ebemvNDOF3", "BlockDiagDOF3_precond", "BlockDiagDOF3_precond_EBE_setup", "Diag_precond",
+            "Diag_precond_EBE_setup", "NO_precond", "NO_precond_setup")),
+    ("euler", ("pgmres", "ebemvNDOF4", "BlockDiag_precond", "BlockDiag_precond_EBE_setup", "Diag_precond",
+               "Diag_precond_EBE_setup", "NO_precond", "NO_precond_setup"))])
+def test_block_shims_export_reference_names(kind, names):
+    L = refapi.block_shim(kind)
+    for name in names:
+        assert hasattr(L, name), name
+
+
+@pytest.mark.parametrize("kind", ["ns", "euler"])
+def test_block_python_mirror_matches_shim_header(kind):
+    out = np.zeros(64, dtype=np.int64)
+    getattr(refapi.block_shim(kind), refapi._KINDS[kind]["layout"])(out)
+    assert list(out[:31]) == refapi.block_layout_offsets(kind)
+
+
+@pytest.mark.parametrize("kind", ["ns", "euler"])
+def test_block_shim_layout_matches_reference_header(kind):
+    R = O.ref_ns() if kind == "ns" else O.ref_euler()
+    if R is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    theirs = np.zeros(64, dtype=np.int64)
+    (R.fr_ns_layout if kind == "ns" else R.fr_eu_layout)(theirs)
+    ours = np.zeros(64, dtype=np.int64)
+    getattr(refapi.block_shim(kind), refapi._KINDS[kind]["layout"])(ours)
+    assert np.array_equal(ours[:31], theirs[:31])
