@@ -206,6 +206,75 @@ def run_reference(args, rank, ws, dist):
 
 
 # ------------------------------------------------------------------ our arm
+# ------------------------------------------------------------------ other drivers
+def euler_leg(fg, G, n=513, steps=20, corrections=2, kmax=25):
+    """Euler OBLIQUO on n x n nodes (Mach 2, dimensionless, dt = 0.5 min h /
+    (|v| + c)), `steps` time steps of Predictor_Old with `corrections`
+    corrections each (StopMulticorrection = ITERATION), GMRES(kmax) with the
+    reference's 4x4 BlockDiag, FP64 and mixed precision; plus the 12x12 EBE
+    matvec roofline on the same system."""
+    p = G.obliquo_problem(n)
+    t0 = time.perf_counter()
+    s = fg.euler_system(p)
+    setup_s = time.perf_counter() - t0
+    s.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1), kmax=kmax)     # warm-up
+    out = {"workload": f"Euler OBLIQUO {n}x{n} nodes, {p.mesh.nel} elements, {p.mesh.neq} dofs, "
+                       f"{steps} steps x {corrections} corrections, GMRES({kmax}), BlockDiag, tol 1e-10",
+           "setup_s": setup_s}
+    us = {}
+    for name, prec in (("fp64", fg.FG_PREC_FP64), ("mixed", fg.FG_PREC_MIXED)):
+        to = fg.time_opts(0, corrections, 1e-3, 0, steps * p.dt, 1e-6, max_steps=steps)
+        t0 = time.perf_counter()
+        u, a, st = s.euler_predictor(p, to, kmax=kmax, tol=1e-10, precision=prec)
+        wall = time.perf_counter() - t0
+        us[name] = u
+        out[name] = {"seconds": wall, "steps": st["steps"], "corrections": st["corrections"],
+                     "gmres_iterations": st["gmres_iterations"], "steps_per_s": st["steps"] / wall,
+                     "ms_per_correction": 1e3 * wall / st["corrections"],
+                     "last_true_rel_residual": st["true_rel_residual"]}
+    out["mixed_rel_diff_vs_fp64"] = float(np.linalg.norm(us["mixed"] - us["fp64"]) / np.linalg.norm(us["fp64"]))
+    out["matvec"] = _matvec_roofline(fg, s)
+    return out
+
+
+def ns_leg(fg, G, n=1025, reynolds=1000.0, kmax=50, cycles=20):
+    """Navier-Stokes CAVITY on n x n nodes (interior jittered by 0.2 h, seed 3),
+    Re = 1000: one Picard step (device assembly, BlockDiagDOF3, GMRES(kmax)),
+    the linear solve capped at `cycles` restart cycles (at this size and
+    Reynolds number BlockDiagDOF3-GMRES needs far more to reach 1e-10), FP64
+    and mixed; reported as Arnoldi iterations per second, plus the 9x9 EBE
+    matvec roofline."""
+    p = G.cavity_problem(n, reynolds=reynolds, jitter=0.2)
+    t0 = time.perf_counter()
+    s = fg.ns_system(p)
+    setup_s = time.perf_counter() - t0
+    s.ns_process(p, kmax=kmax, lmax=1, max_nonlinear=1)                                       # warm-up
+    out = {"workload": f"NS CAVITY {n}x{n} nodes (jitter 0.2h), Re={reynolds:g}, {p.mesh.nel} elements, "
+                       f"{p.mesh.neq} dofs; one Picard step, GMRES({kmax}) capped at {cycles} cycles, BlockDiagDOF3",
+           "setup_s": setup_s}
+    for name, prec in (("fp64", fg.FG_PREC_FP64), ("mixed", fg.FG_PREC_MIXED)):
+        t0 = time.perf_counter()
+        u, st = s.ns_process(p, kmax=kmax, lmax=cycles, tol=1e-10, max_nonlinear=1, precision=prec)
+        wall = time.perf_counter() - t0
+        out[name] = {"seconds": wall, "gmres_iterations": st["gmres_iterations"],
+                     "iterations_per_s": st["gmres_iterations"] / wall,
+                     "dof_iterations_per_s": p.mesh.neq * st["gmres_iterations"] / wall,
+                     "true_rel_residual": st["true_rel_residual"]}
+    out["matvec"] = _matvec_roofline(fg, s)
+    return out
+
+
+def _matvec_roofline(fg, s):
+    peak, kind = peaks()
+    r = {}
+    for prec in (64, 32):
+        ms, b = fg.bench_matvec([s], precision=prec, reps=20)
+        gbs = b / (ms * 1e-3) / 1e9
+        r[f"fp{prec}"] = {"ms": ms, "bytes": b, "GB_per_s": gbs, "frac": gbs / peak}
+    r["peak"], r["peak_source"] = peak, kind
+    return r
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -218,6 +287,9 @@ def main():
     ap.add_argument("--plain-count", type=int, default=0, help="instances in the plain FP64 leg (0 = all)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-legs", action="store_true", help="skip the Euler and Navier-Stokes legs")
+    ap.add_argument("--euler-n", type=int, default=513, help="nodes per side of the Euler leg")
+    ap.add_argument("--ns-n", type=int, default=1025, help="nodes per side of the Navier-Stokes leg (odd)")
     args = ap.parse_args()
     rank, ws, dist = dist_setup()
     if args.impl == "reference":
@@ -366,6 +438,10 @@ def main():
         e2e = {"value": ws * args.count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
 
+    legs = None
+    if not args.no_legs and rank == 0:
+        legs = {"euler_obliquo": euler_leg(fg, G, n=args.euler_n), "ns_cavity": ns_leg(fg, G, n=args.ns_n)}
+
     cpu = None
     if pool is not None:
         nel = [p.mesh.nel for p in probs]
@@ -398,7 +474,7 @@ def main():
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind, "traffic": None, "ms_per_matvec": ms_mv,
                          "bytes_per_matvec": bytes_mv},
-            "cpu_baseline": cpu, "setup_s": setup_s,
+            "cpu_baseline": cpu, "setup_s": setup_s, "legs": legs,
         }
         print(json.dumps(line), flush=True)
     return 0
