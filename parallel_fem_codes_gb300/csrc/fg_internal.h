@@ -63,7 +63,45 @@ struct CsrTopology {
 };
 int build_csr(const Topology &t, CsrTopology &c);
 
-constexpr int kPatchElems = 1024;      // elements per matvec patch
+constexpr int kPatchElems = 1024;      // largest matvec patch (3x3 blocks)
+// Elements per matvec patch for S x S blocks (a multiple of 32).  The
+// matvec stages every element's S products of a patch in shared memory, so
+// larger blocks use smaller patches (a single large mesh then also gets
+// more patches, enough to fill the GPU).
+// (FG_MV_PE3 ... FG_MV_PE12: compile-time tuning constants.)
+#ifndef FG_MV_PE3
+#define FG_MV_PE3 1024
+#endif
+#ifndef FG_MV_PE6
+#define FG_MV_PE6 256
+#endif
+#ifndef FG_MV_PE9
+#define FG_MV_PE9 256
+#endif
+#ifndef FG_MV_PE12
+#define FG_MV_PE12 256
+#endif
+__host__ __device__ constexpr int patch_elems(int S)
+{
+    return S <= 3 ? FG_MV_PE3 : S <= 6 ? FG_MV_PE6 : S <= 9 ? FG_MV_PE9 : FG_MV_PE12;
+}
+__host__ __device__ constexpr int round4(int v) { return (v + 3) & ~3; }
+// Shared-memory layout of one matvec CTA (bytes): x and y of the patch's
+// dofs (round4(maxdof) each), the staged products [S][PE] and the staged
+// 16-bit local indices [S][PE].
+struct MvSmem {
+    size_t xs, ys, ye, ls, total;
+    __host__ __device__ MvSmem(int S, int maxdof, int w)
+    {
+        const size_t PE = patch_elems(S), md = round4(maxdof > 0 ? maxdof : 1);
+        xs = 0;
+        ys = md * w;
+        ye = 2 * md * w;
+        ls = ye + (size_t)S * PE * w;
+        total = ls + (size_t)S * PE * 2;
+    }
+};
+inline size_t mv_smem_bytes(int S, int maxdof, int w) { return MvSmem(S, maxdof, w).total; }
 constexpr int kPatchMaxLocalColours = 16;
 constexpr int kPatchColStride = kPatchMaxLocalColours + 1;
 

@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "system.h"
 
@@ -86,30 +87,43 @@ __device__ __forceinline__ void reduce_parts(const SysDev &D, int nv, double *ou
 }
 
 // ---------------------------------------------------------------- EBE matvec
-// y[lm] += A_e x[lm] by patches.  A patch is up to kPatchElems consecutive
-// elements (internal order: sorted by their smallest dof, so a patch covers
-// a compact band of dofs).  One CTA per patch: it gathers the patch's x
-// entries into shared memory, accumulates the element rows into a
-// shared-memory y local colour by local colour (elements of one local
-// colour share no dof, so no atomics and a fixed summation order), and
-// writes each dof once: a plain store for dofs only this patch touches, an
-// update for dofs shared with other patches.  Patches that share a dof have
-// different patch colours and run in different launches, so the updates do
-// not race.  A and lm16 are SoA ([entry][element]); lane-consecutive
-// elements read consecutive addresses.  The sink (index n) is never written.
+// y[lm] += A_e x[lm] by patches.  A patch is up to patch_elems(S)
+// consecutive elements (internal order: sorted by their smallest dof, so a
+// patch covers a compact band of dofs).  The CTAs loop over the patches of
+// their launch (one launch per patch colour); per patch:
+//  1. x of the patch's dofs is gathered into shared memory;
+//  2. the element products A_e x_e are formed and staged in shared memory
+//     with the elements' local indices, one thread per element (S = 3: each
+//     thread loads its four elements' blocks at once, before step 1, so a
+//     whole patch of loads is in flight); A and lm16 are SoA
+//     [entry][element], so lane-consecutive elements read consecutive
+//     addresses;
+//  3. the staged rows are added into a shared-memory y local colour by local
+//     colour (elements of one local colour share no dof: no atomics, a fixed
+//     summation order), then each dof is written once: a plain store for
+//     dofs only this patch touches, an update for dofs shared with other
+//     patches (patches sharing a dof have different patch colours and run
+//     in different launches, so the updates do not race).
+// The patch sizes (patch_elems) and this kernel shape were chosen by a
+// measured sweep: an L2 prefetch of the next patch, one thread per block
+// row with small patches, and a two-stage bulk-copy pipeline through shared
+// memory were all slower.  The sink (index n) is never written.
 // in_sel: 0 = x (FP64), 1 = V[step] (T), 2 = aux (TX); out_sel: 0 = t64,
 // 1 = t, 2 = aux.
 template <int S, typename TA, typename TX, typename TY>
 __global__ void __launch_bounds__(kThreads)
 k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const int *__restrict__ nch,
-         int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out)
+         int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out, int maxdof)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr unsigned short kSink = 0xFFFF;
-    // S = 3: every thread preloads its (up to) kPatchElems / kThreads
-    // elements' blocks before the colour passes, so a whole patch of loads
-    // is in flight at once; larger blocks are loaded inside the passes.
-    constexpr int E = S == 3 ? kPatchElems / kThreads : 1;
+    constexpr int PE = patch_elems(S);
+    constexpr int E = S == 3 ? PE / kThreads : 1;        // S = 3: elements per thread
+    const MvSmem L(S, maxdof, (int)sizeof(TA));
+    TA *xs = reinterpret_cast<TA *>(smem_raw + L.xs);
+    TA *ys = reinterpret_cast<TA *>(smem_raw + L.ys);
+    TA *ye = reinterpret_cast<TA *>(smem_raw + L.ye);
+    unsigned short *ls = reinterpret_cast<unsigned short *>(smem_raw + L.ls);
     const int total = *nch;
     for (int c = blockIdx.x; c < total; c += gridDim.x) {
         const EChunk k = ch[c];
@@ -120,8 +134,6 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
-        TA *xs = reinterpret_cast<TA *>(smem_raw);
-        TA *ys = xs + D.maxdof;
         const int p = k.e0;
         const int pe0 = D.pt_elem[p], pne = D.pt_elem[p + 1] - pe0;
         const int pd0 = D.pt_dof[p], pnd = D.pt_dof[p + 1] - pd0;
@@ -139,54 +151,65 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
                 for (int m = 0; m < 9; ++m) av[u][m] = ldst(A + m * ld + pe0 + q);
             }
         }
-        __syncthreads();                      // the previous patch is done with xs / ys
-        for (int j = threadIdx.x; j < pnd; j += blockDim.x) {
+        __syncthreads();                      // the previous patch is done with shared memory
+        for (int j = threadIdx.x; j < pnd; j += kThreads) {
             xs[j] = (TA)X[D.dofs[pd0 + j] & 0x7fffffff];
             ys[j] = (TA)0;
+        }
+        __syncthreads();
+        if constexpr (S == 3) {
+#pragma unroll
+            for (int u = 0; u < E; ++u) {
+                const int q = threadIdx.x + u * kThreads;
+                if (q >= pne) continue;
+                TA xv[3];
+#pragma unroll
+                for (int a = 0; a < 3; ++a) xv[a] = li[u][a] == kSink ? (TA)0 : xs[li[u][a]];
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    TA acc = av[u][3 * r] * xv[0];
+                    acc += av[u][3 * r + 1] * xv[1];
+                    acc += av[u][3 * r + 2] * xv[2];
+                    ye[r * PE + q] = acc;
+                    ls[r * PE + q] = li[u][r];
+                }
+            }
+        } else {
+            for (int q = threadIdx.x; q < pne; q += kThreads) {
+                unsigned short l[S];
+                TA xv[S];
+#pragma unroll
+                for (int a = 0; a < S; ++a) {
+                    l[a] = __ldcs(D.lm16 + a * ld + pe0 + q);
+                    xv[a] = l[a] == kSink ? (TA)0 : xs[l[a]];
+                }
+#pragma unroll
+                for (int r = 0; r < S; ++r) {
+                    TA acc = ldst(A + (size_t)(r * S) * ld + pe0 + q) * xv[0];
+#pragma unroll
+                    for (int m = 1; m < S; ++m) acc += ldst(A + (size_t)(r * S + m) * ld + pe0 + q) * xv[m];
+                    ye[r * PE + q] = acc;
+                    ls[r * PE + q] = l[r];
+                }
+            }
         }
         __syncthreads();
         for (int col = 0; col < kPatchMaxLocalColours; ++col) {
             const int cs = pc[col], ce = pc[col + 1];
             if (cs >= ce) break;
-            if constexpr (S == 3) {
+            for (int q = cs + threadIdx.x; q < ce; q += kThreads) {
 #pragma unroll
-                for (int u = 0; u < E; ++u) {
-                    const int q = threadIdx.x + u * kThreads;
-                    if (q < cs || q >= ce) continue;
-                    TA xv[3];
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) xv[a] = li[u][a] == kSink ? (TA)0 : xs[li[u][a]];
-#pragma unroll
-                    for (int r = 0; r < 3; ++r) {
-                        TA acc = av[u][3 * r] * xv[0];
-                        acc += av[u][3 * r + 1] * xv[1];
-                        acc += av[u][3 * r + 2] * xv[2];
-                        if (li[u][r] != kSink) ys[li[u][r]] += acc;
-                    }
-                }
-            } else {
-                for (int q = cs + threadIdx.x; q < ce; q += blockDim.x) {
-                    unsigned short l[S];
-                    TA xv[S];
-#pragma unroll
-                    for (int a = 0; a < S; ++a) {
-                        l[a] = __ldcs(D.lm16 + a * ld + pe0 + q);
-                        xv[a] = l[a] == kSink ? (TA)0 : xs[l[a]];
-                    }
-#pragma unroll
-                    for (int r = 0; r < S; ++r) {
-                        TA acc = ldst(A + (size_t)(r * S) * ld + pe0 + q) * xv[0];
-#pragma unroll
-                        for (int m = 1; m < S; ++m) acc += ldst(A + (size_t)(r * S + m) * ld + pe0 + q) * xv[m];
-                        if (l[r] != kSink) ys[l[r]] += acc;
-                    }
+                for (int r = 0; r < S; ++r) {
+                    const unsigned short l = ls[r * PE + q];
+                    if (l != kSink) ys[l] += ye[r * PE + q];
                 }
             }
             __syncthreads();
         }
-        for (int j = threadIdx.x; j < pnd; j += blockDim.x) {
+        for (int j = threadIdx.x; j < pnd; j += kThreads) {
             const int dd = D.dofs[pd0 + j];
             const int d = dd & 0x7fffffff;
+            if (d == D.n) continue;                       // dof-list padding
             if (dd < 0) Y[d] += (TY)ys[j];
             else Y[d] = (TY)ys[j];
         }
@@ -434,25 +457,47 @@ int sm_count()
 namespace {
 
 struct MvLaunch {
-    // smem: bytes of dynamic shared memory (2 * max patch dofs * sizeof(TA))
+    // Persistent CTAs: as many as fit on the GPU (their dynamic shared memory,
+    // mv_smem_bytes, decides how many per SM), at most one per patch.
     template <typename TA, typename TX, typename TY>
-    static void go(int S, dim3 g, cudaStream_t st, const SysDev *sys, const EChunk *ch, const int *nch,
-                   int gate, int in_sel, int out_sel, int step, const TX *ai, TY *ao, size_t smem)
+    static void go(int S, int nitems, cudaStream_t st, const SysDev *sys, const EChunk *ch, const int *nch,
+                   int gate, int in_sel, int out_sel, int step, const TX *ai, TY *ao, int maxdof)
     {
         switch (S) {
-        case 3: run<3, TA, TX, TY>(g, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, smem); break;
-        case 6: run<6, TA, TX, TY>(g, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, smem); break;
-        case 9: run<9, TA, TX, TY>(g, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, smem); break;
-        case 12: run<12, TA, TX, TY>(g, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, smem); break;
+        case 3: run<3, TA, TX, TY>(nitems, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof); break;
+        case 6: run<6, TA, TX, TY>(nitems, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof); break;
+        case 9: run<9, TA, TX, TY>(nitems, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof); break;
+        case 12: run<12, TA, TX, TY>(nitems, st, sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof); break;
         }
     }
     template <int S, typename TA, typename TX, typename TY>
-    static void run(dim3 g, cudaStream_t st, const SysDev *sys, const EChunk *ch, const int *nch, int gate,
-                    int in_sel, int out_sel, int step, const TX *ai, TY *ao, size_t smem)
+    static void run(int nitems, cudaStream_t st, const SysDev *sys, const EChunk *ch, const int *nch, int gate,
+                    int in_sel, int out_sel, int step, const TX *ai, TY *ao, int maxdof)
     {
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(k_ebe_mv<S, TA, TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_ebe_mv<S, TA, TX, TY><<<g, kThreads, smem, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao);
+        const size_t smem = mv_smem_bytes(S, maxdof, sizeof(TA));
+        auto kern = k_ebe_mv<S, TA, TX, TY>;
+        // the attribute and the occupancy are cached per instantiation
+        // (last shared-memory size seen); they are host-side queries only
+        static std::mutex mu;
+        static size_t set_bytes = 0, occ_bytes = 0;
+        static int occ_cached = 1;
+        int occ;
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (smem > set_bytes) {
+                cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                set_bytes = smem;
+            }
+            if (smem != occ_bytes) {
+                int o = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kThreads, smem);
+                occ_cached = std::max(o, 1);
+                occ_bytes = smem;
+            }
+            occ = occ_cached;
+        }
+        const int g = std::max(1, std::min(nitems, occ * sm_count()));
+        kern<<<g, kThreads, smem, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof);
     }
 };
 
@@ -485,7 +530,6 @@ int parts_for(int n)
 struct Plan {
     int nsys = 0, ncol = 0, S = 3, B = 1, maxdof = 1;   // ncol: patch colours
     int op = FG_OP_EBE, csr_w = 4, precond = FG_PRECOND_NONE;
-    size_t smem(int w) const { return 2 * (size_t)maxdof * w; }
     std::vector<int> ech_off;      // ncol+1 offsets into echunks
     int n_dch = 0, n_nch = 0, n_ilu = 0;
     size_t flag_bytes = 0;
@@ -632,11 +676,10 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
         const EChunk *ch = P.echunks.as<EChunk>() + P.ech_off[c];
         const int *nc = P.ecount.as<int>() + c;
         if (f64)
-            MvLaunch::go<double, double, double>(P.S, grid_for(cnt), st, sys, ch, nc, gate, 0, 0, 0, nullptr, nullptr,
-                                                 P.smem(8));
+            MvLaunch::go<double, double, double>(P.S, cnt, st, sys, ch, nc, gate, 0, 0, 0, nullptr, nullptr,
+                                                 P.maxdof);
         else
-            MvLaunch::go<T, T, T>(P.S, grid_for(cnt), st, sys, ch, nc, gate, 1, 1, step, nullptr, nullptr,
-                                  P.smem(sizeof(T)));
+            MvLaunch::go<T, T, T>(P.S, cnt, st, sys, ch, nc, gate, 1, 1, step, nullptr, nullptr, P.maxdof);
         ++k;
     }
     return k;
@@ -1009,15 +1052,14 @@ int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaS
         FG_CUDA(cudaStreamSynchronize(st));
         return FG_OK;
     }
-    const size_t smem = 2 * (size_t)D.maxdof * (precision == 32 ? 4 : 8);
     for (int c = 0; c < t.npcol; ++c) {
         if (!counts[c]) continue;
         const EChunk *cp = ch.as<EChunk>() + off[c];
         const int *np = cnt.as<int>() + c;
         if (precision == 32)
-            MvLaunch::go<float, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y, smem);
+            MvLaunch::go<float, double, double>(t.S, counts[c], st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y, D.maxdof);
         else
-            MvLaunch::go<double, double, double>(t.S, grid_for(counts[c]), st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y, smem);
+            MvLaunch::go<double, double, double>(t.S, counts[c], st, sd.as<SysDev>(), cp, np, -1, 2, 2, 0, x, y, D.maxdof);
     }
     FG_CUDA(cudaGetLastError());
     count_launches(t.npcol);
@@ -1081,16 +1123,15 @@ int bench_matvec(std::vector<fg_system *> &systems, int precision, int reps, dou
 int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const EChunk *ch_dev, const int *counts_dev,
                           const int *off_host, int ncol, int maxdof, const double *x, double *y, cudaStream_t st)
 {
-    const size_t smem = 2 * (size_t)std::max(1, maxdof) * (precision == 32 ? 4 : 8);
     for (int c = 0; c < ncol; ++c) {
         int cnt = off_host[c + 1] - off_host[c];
         if (!cnt) continue;
         const EChunk *cp = ch_dev + off_host[c];
         const int *np = counts_dev + c;
         if (precision == 32)
-            MvLaunch::go<float, double, double>(S, grid_for(cnt), st, sys_dev, cp, np, -1, 2, 2, 0, x, y, smem);
+            MvLaunch::go<float, double, double>(S, cnt, st, sys_dev, cp, np, -1, 2, 2, 0, x, y, maxdof);
         else
-            MvLaunch::go<double, double, double>(S, grid_for(cnt), st, sys_dev, cp, np, -1, 2, 2, 0, x, y, smem);
+            MvLaunch::go<double, double, double>(S, cnt, st, sys_dev, cp, np, -1, 2, 2, 0, x, y, maxdof);
         count_launches(1);
     }
     FG_CUDA(cudaGetLastError());

@@ -284,7 +284,7 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
     }
     // internal element order (the patch layout of the matvec): elements with
     // a free dof sorted by their smallest internal dof (stable), cut into
-    // patches of kPatchElems consecutive elements; inside each patch the
+    // patches of patch_elems(S) consecutive elements; inside each patch the
     // elements are grouped by a greedy local colouring so that the patch's
     // shared-memory accumulation needs no atomics.  Elements without a free
     // dof go last and are skipped by the matvec.
@@ -303,25 +303,34 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
     int nact = 0;
     for (int e = 0; e < nel; ++e) nact += has_free[e] ? 1 : 0;
     t.nel_active = nact;
-    t.npatch = (nact + kPatchElems - 1) / kPatchElems;
+    // A patch takes up to PE elements; it closes early, only at a multiple of
+    // 16 elements (every patch starts 16-element aligned: aligned vector
+    // loads of its rows), when 16 more elements could push its dof count
+    // past the cap that bounds the matvec's shared memory.
+    const int PE = patch_elems(S), dof_cap = S == 3 ? 1536 : PE * S;
     t.eorder.resize(nel);
-    t.pt_elem.assign(t.npatch + 1, 0);
-    t.pt_dof.assign(t.npatch + 1, 0);
-    t.pt_col.assign((size_t)t.npatch * kPatchColStride, 0);
+    t.pt_elem.clear();
+    t.pt_dof.clear();
+    t.pt_col.clear();
     t.dofs.clear();
     t.maxdof = 0;
     std::vector<int> local(n + 1, -1), owner_count(n + 1, 0);
     std::vector<uint32_t> lmask;   // per local dof: local colours used
-    for (int p = 0; p < t.npatch; ++p) {
-        const int b = p * kPatchElems, e = std::min(nact, b + kPatchElems);
-        t.pt_elem[p] = b;
+    for (int b = 0, p = 0; b < nact; ++p) {
         // local dofs of the patch, ascending internal index
         std::vector<int> pd;
-        for (int q = b; q < e; ++q)
+        int e = b;
+        while (e < nact && e - b < PE) {
+            if ((e - b) % 16 == 0 && (int)pd.size() + 16 * S > dof_cap) break;
             for (int a = 0; a < S; ++a) {
-                int r = t.lm[(size_t)sorted[q] * S + a];
+                int r = t.lm[(size_t)sorted[e] * S + a];
                 if (r != n && local[t.iperm[r]] < 0) { local[t.iperm[r]] = 0; pd.push_back(t.iperm[r]); }
             }
+            ++e;
+        }
+        t.pt_elem.push_back(b);
+        t.pt_col.resize((size_t)(p + 1) * kPatchColStride, 0);
+        t.pt_dof.push_back(0);
         std::sort(pd.begin(), pd.end());
         for (size_t j = 0; j < pd.size(); ++j) { local[pd[j]] = (int)j; owner_count[pd[j]]++; }
         // greedy local colouring in patch order
@@ -355,13 +364,18 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
             pc[c] = (unsigned short)k;     // first element of local colour c
         }
         for (int k = 0; k < (int)idx.size(); ++k) t.eorder[b + k] = sorted[b + idx[k]];
+        // each patch's dof list starts on a 16-byte boundary
+        while (t.dofs.size() % 4) t.dofs.push_back(n);
         t.pt_dof[p] = (int)t.dofs.size();
         for (int d : pd) t.dofs.push_back(d);
         t.maxdof = std::max(t.maxdof, (int)pd.size());
         for (int d : pd) local[d] = -1;
+        b = e;
     }
-    t.pt_elem[t.npatch] = nact;
-    t.pt_dof[t.npatch] = (int)t.dofs.size();
+    t.npatch = (int)t.pt_elem.size();
+    t.pt_elem.push_back(nact);
+    while (t.dofs.size() % 4) t.dofs.push_back(n);
+    t.pt_dof.push_back((int)t.dofs.size());
     for (int q = nact; q < nel; ++q) t.eorder[q] = sorted[q];
     for (auto &d : t.dofs)
         if (owner_count[d] > 1) d |= (int)0x80000000u;
