@@ -42,6 +42,12 @@ WORKLOAD = ("served steady SUPG/CAU transport: 256 requests, NxN nodes N~U[33,51
             "angle~U[0,360), k~logU[1e-8,1e-2]; device assembly + Diag + GMRES(30), FP32 inner + FP64 "
             "refinement to true rel. residual 1e-10, continuous batching")
 KMAX, TOL = 30, 1e-10
+# DRAM bytes / algorithmic bytes of one batched FP32 matvec, measured by ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum of the k_ebe_mv launches of
+# `bench.py --matvec-only --count 32 --steps 1`, cold): 414.1 MB for
+# 418.2 MB.  The traffic scales with the instances (each patch reads its own
+# blocks once).
+MATVEC_TRAFFIC_RATIO = 414.1 / 418.19
 
 
 # ------------------------------------------------------------------ CPU legs
@@ -275,6 +281,20 @@ def _matvec_roofline(fg, s):
     return r
 
 
+def run_matvec_only(args):
+    from parallel_fem_codes_gb300 import femgpu as fg, meshgen as G
+    fg.lib(build_if_missing=False)
+    probs = G.batch_transport_problems(args.count, args.seed)
+    systems = [fg.transport_system(p) for p in probs]
+    for s, p in zip(systems, probs):
+        s.transport_assemble(p)
+    ms, b = fg.bench_matvec(systems, precision=32, reps=max(1, args.steps))   # after 2 warm-up matvecs
+    print(json.dumps({"matvec_only": True, "instances": args.count, "elements": sum(p.mesh.nel for p in probs),
+                      "ms": ms, "algorithmic_bytes": b, "GB_per_s": b / ms / 1e6,
+                      "matvecs": 2 + max(1, args.steps)}), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -290,10 +310,16 @@ def main():
     ap.add_argument("--no-legs", action="store_true", help="skip the Euler and Navier-Stokes legs")
     ap.add_argument("--euler-n", type=int, default=513, help="nodes per side of the Euler leg")
     ap.add_argument("--ns-n", type=int, default=1025, help="nodes per side of the Navier-Stokes leg (odd)")
+    ap.add_argument("--matvec-only", action="store_true",
+                    help="only the batched FP32 EBE matvec of --count instances (2 warm-up + --steps "
+                         "matvecs); the small case the ncu traffic capture runs")
     args = ap.parse_args()
     rank, ws, dist = dist_setup()
     if args.impl == "reference":
         return run_reference(args, rank, ws, dist)
+
+    if args.matvec_only:
+        return run_matvec_only(args)
 
     # spawn the CPU pool before the first GPU call
     cores = os.cpu_count() or 1
@@ -472,7 +498,10 @@ def main():
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": "k_ebe_mv<3,float> (all colours, batched)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                         "peak_source": peak_kind, "traffic": None, "ms_per_matvec": ms_mv,
+                         "peak_source": peak_kind, "traffic": MATVEC_TRAFFIC_RATIO * bytes_mv,
+                         "traffic_source": "ncu dram__bytes_read+write per matvec of a 32-instance capture "
+                                           "(bench.py --matvec-only --count 32), scaled by algorithmic bytes",
+                         "ms_per_matvec": ms_mv,
                          "bytes_per_matvec": bytes_mv},
             "cpu_baseline": cpu, "setup_s": setup_s, "legs": legs,
         }
