@@ -124,7 +124,18 @@ int fg_get_csr(const fg_system *s, int *nnz, int *IA, int *JA, double *AA);
 
 /* ---- preconditioners (Solvers_and_Preconditioners/preconditioners.h) ---- */
 enum { FG_PRECOND_NONE = 0, FG_PRECOND_DIAG = 1, FG_PRECOND_BLOCKDIAG = 2,
-       FG_PRECOND_ILU0 = 3  /* ILU(0) of the assembled CSR operator (fg_set_operator) */ };
+       FG_PRECOND_ILU0 = 3, /* ILU(0) of the assembled CSR operator (fg_set_operator) */
+       FG_PRECOND_SPIKE = 4 /* truncated SPIKE of the CSR operator (fg_set_spike)   */ };
+/* Truncated SPIKE ("SPIKEk", CSR/SPIKE_precond_setup.c:10-312 and
+ * CSR/SPIKE_precond.c:8-158).  The reference's P MPI ranks become `parts`
+ * row blocks of the CSR operator on one GPU (at most n / 2k, so every block
+ * keeps 2k rows); each block is factorised by banded LU without pivoting
+ * (the reference calls PARDISO) and neighbours are coupled through k x k
+ * corner blocks and one 2k x 2k reduced system per interface.  k in
+ * [1, 64] (default 16), parts in [1, 65536] (default 16).  Takes effect at
+ * the next fg_precond_setup(FG_PRECOND_SPIKE); systems whose band factors
+ * would exceed 8 GiB are rejected there with FG_ERR_UNSUPPORTED. */
+int fg_set_spike(fg_system *s, int k, int parts);
 enum {
     FG_SETUP_ACCUMULATE = 1, /* Diag += new diagonal, as Diag_precond_EBE_setup
                                 does across nonlinear iterations              */

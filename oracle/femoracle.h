@@ -204,6 +204,14 @@ int  or_ilu0_factor(int n, const int *IA, const int *JA, const double *AA, doubl
 void or_ilu0_apply(int n, const int *IA, const int *JA, const double *LU, const double *D,
                    const double *y, double *x);
 
+/* truncated SPIKE over CSR row blocks (spike.c) */
+typedef struct or_spike or_spike;
+int  or_spike_blocks(int n, int k, int parts);
+or_spike *or_spike_setup(int n, const int *IA, const int *JA, const double *AA, int k, int parts, int *err);
+void or_spike_apply(const or_spike *sp, const double *f, double *y);
+int  or_spike_info(const or_spike *sp, int *k, int *bs, int *kl, int *ku);
+void or_spike_free(or_spike *sp);
+
 #ifdef __cplusplus
 }
 #endif

@@ -627,3 +627,45 @@ def ref_csr(prob, A, P):
     nnz = R.fr_sst_csr(*_mesh_args(m), np.ascontiguousarray(A, dtype=np.float64).reshape(-1), nmax, IA, JA, AA,
                        invp, np.ascontiguousarray(P, dtype=np.float64), Q, z)
     return IA, JA[:nnz].copy(), AA[:nnz].copy(), invp, Q, z
+
+
+class Spike:
+    """Truncated SPIKE (oracle/spike.c) of a CSR matrix (IA, JA, AA, 0-based,
+    internal numbering): `apply(f)` returns M^-1 f for n-entry f."""
+
+    def __init__(self, IA, JA, AA, k, parts):
+        L = lib()
+        L.or_spike_setup.argtypes = [_c_int, _i32p, _i32p, _f64p, _c_int, _c_int, ctypes.POINTER(ctypes.c_int)]
+        L.or_spike_setup.restype = ctypes.c_void_p
+        L.or_spike_apply.argtypes = [ctypes.c_void_p, _f64p, _f64p]
+        L.or_spike_apply.restype = None
+        L.or_spike_info.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), _i32p, _i32p, _i32p]
+        L.or_spike_free.argtypes = [ctypes.c_void_p]
+        L.or_spike_free.restype = None
+        self._L = L
+        self.n = int(IA.shape[0]) - 1
+        err = ctypes.c_int(0)
+        self._h = L.or_spike_setup(self.n, np.ascontiguousarray(IA, dtype=np.int32),
+                                   np.ascontiguousarray(JA, dtype=np.int32),
+                                   np.ascontiguousarray(AA, dtype=np.float64), int(k), int(parts), ctypes.byref(err))
+        self.err = err.value
+        if not self._h:
+            raise ValueError("or_spike_setup rejected its arguments")
+        kk = ctypes.c_int(0)
+        nb = L.or_spike_blocks(self.n, int(k), int(parts))
+        self.bs = np.zeros(nb + 1, np.int32)
+        self.kl = np.zeros(nb, np.int32)
+        self.ku = np.zeros(nb, np.int32)
+        P = L.or_spike_info(self._h, ctypes.byref(kk), self.bs, self.kl, self.ku)
+        self.P, self.k = P, kk.value
+
+    def apply(self, f):
+        f = np.ascontiguousarray(f[: self.n], dtype=np.float64)
+        y = np.zeros(self.n)
+        self._L.or_spike_apply(self._h, f, y)
+        return y
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._L.or_spike_free(self._h)
+            self._h = None

@@ -29,6 +29,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("server.cu", []),
     ("ilu.cu", ["-fmad=false"]),
+    ("spike.cu", ["-fmad=false"]),
     ("ns.cu", ["-fmad=false"]),
     ("euler.cu", ["-fmad=false"]),
 ]

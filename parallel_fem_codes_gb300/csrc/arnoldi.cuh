@@ -127,7 +127,7 @@ k_dots1(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
 #pragma unroll
         for (int c = 0; c < N; ++c) zero.v[c] = (T)0;
         for (int q = k.d0 + threadIdx.x * N; q < k.d1; q += blockDim.x * N) {
-            if (D.precond != FG_PRECOND_BLOCKDIAG && D.precond != FG_PRECOND_ILU0) {
+            if (!precond_separate(D.precond)) {
                 auto tv = ld_pk(t + q);
                 if (D.precond == FG_PRECOND_DIAG) {
                     auto iv = ld_pk(invd + q);

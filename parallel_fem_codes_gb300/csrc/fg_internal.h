@@ -148,6 +148,15 @@ struct SysDev {
     const double *AA64, *LU64, *dinv64;
     const float *AA32, *LU32, *dinv32;
     int *ilu_flag;             // per-row ready flags of the sync-free solves
+    // truncated SPIKE (precond == FG_PRECOND_SPIKE): sp_P row blocks of the
+    // CSR operator, coupling size sp_k; band LU factors, k x k corner
+    // couplings, LU of the 2k x 2k reduced systems; FP64 apply scratch
+    int sp_k, sp_P, sp_smem_rows;
+    const int *sp_bs, *sp_bl, *sp_bu;
+    const long long *sp_boff;
+    const double *sp_band, *sp_B, *sp_C, *sp_S;
+    const int *sp_piv;
+    double *sp_g, *sp_h, *sp_x;
     const double *A64;         // [S*S][nel_pad]
     const float *A32;
     const double *invd64;      // n_pad
@@ -165,6 +174,10 @@ struct SysDev {
     SysState *st;
 };
 constexpr int kPartStride = 64;    // doubles per part (>= kmax + 2, kmax <= 60)
+
+// Preconditioners applied by kernels of their own between the matvec and
+// the Arnoldi pass (the others are fused into the vector kernels).
+__host__ __device__ constexpr bool precond_separate(int p) { return p >= 2; }
 
 struct EChunk { int sys, e0, e1; };
 struct DChunk { int sys, part, d0, d1; };

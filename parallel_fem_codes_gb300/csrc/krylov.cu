@@ -309,7 +309,7 @@ k_start(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
         for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) {
             double t = D.t64[d];
             double u = D.precond == FG_PRECOND_DIAG ? t * D.invd64[d]
-                     : (D.precond == FG_PRECOND_BLOCKDIAG || D.precond == FG_PRECOND_ILU0) ? D.u64[d] : t;
+                     : precond_separate(D.precond) ? D.u64[d] : t;
             double bd = D.b[d];
             double r = -1.0 * (u + -1.0 * bd);
             D.r64[d] = r;
@@ -531,10 +531,11 @@ struct Plan {
     int nsys = 0, ncol = 0, S = 3, B = 1, maxdof = 1;   // ncol: patch colours
     int op = FG_OP_EBE, csr_w = 4, precond = FG_PRECOND_NONE;
     std::vector<int> ech_off;      // ncol+1 offsets into echunks
-    int n_dch = 0, n_nch = 0, n_ilu = 0;
+    int n_dch = 0, n_nch = 0, n_ilu = 0, n_spb = 0, n_spi = 0;
     size_t flag_bytes = 0;
     DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
     DevMem ilu_fwd, ilu_bwd, ilu_flags, ilu_ctr;   // sync-free ILU(0) substitutions
+    DevMem sp_blocks, sp_ifaces;                   // SPIKE (system, block) and (system, interface) items
 };
 
 static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig &cfg, std::vector<SysDev> &hs,
@@ -606,6 +607,16 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
             }
         P.n_ilu = (int)fwd.size();
     }
+    // SPIKE: one CTA per block and per interface of every member
+    std::vector<int2> spb, spi;
+    if (cfg.precond == FG_PRECOND_SPIKE)
+        for (int s = 0; s < P.nsys; ++s) {
+            const int np = mem[s].s->sp_P;
+            for (int q = 0; q < np; ++q) spb.push_back(make_int2(s, q));
+            for (int q = 0; q + 1 < np; ++q) spi.push_back(make_int2(s, q));
+        }
+    P.n_spb = (int)spb.size();
+    P.n_spi = (int)spi.size();
     std::vector<int> ecounts(P.ncol);
     for (int c = 0; c < P.ncol; ++c) ecounts[c] = P.ech_off[c + 1] - P.ech_off[c];
     int r;
@@ -618,8 +629,14 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
         (r = P.ncount.alloc(sizeof(int))) ||
         (r = P.live.alloc(sizeof(int) * P.nsys)) ||
         (r = P.ilu_fwd.alloc(sizeof(int2) * std::max<size_t>(1, fwd.size()))) ||
-        (r = P.ilu_bwd.alloc(sizeof(int2) * std::max<size_t>(1, bwd.size()))))
+        (r = P.ilu_bwd.alloc(sizeof(int2) * std::max<size_t>(1, bwd.size()))) ||
+        (r = P.sp_blocks.alloc(sizeof(int2) * std::max<size_t>(1, spb.size()))) ||
+        (r = P.sp_ifaces.alloc(sizeof(int2) * std::max<size_t>(1, spi.size()))))
         return r;
+    if (!spb.empty())
+        FG_CUDA(cudaMemcpyAsync(P.sp_blocks.p, spb.data(), sizeof(int2) * spb.size(), cudaMemcpyHostToDevice, st));
+    if (!spi.empty())
+        FG_CUDA(cudaMemcpyAsync(P.sp_ifaces.p, spi.data(), sizeof(int2) * spi.size(), cudaMemcpyHostToDevice, st));
     if (!fwd.empty()) {
         FG_CUDA(cudaMemcpyAsync(P.ilu_fwd.p, fwd.data(), sizeof(int2) * fwd.size(), cudaMemcpyHostToDevice, st));
         FG_CUDA(cudaMemcpyAsync(P.ilu_bwd.p, bwd.data(), sizeof(int2) * bwd.size(), cudaMemcpyHostToDevice, st));
@@ -707,6 +724,11 @@ static int enqueue_precond(const Plan &P, int sel, cudaStream_t st)
         launch_ilu_solve(sys, P.ilu_bwd.as<int2>(), P.n_ilu, P.ilu_flags.as<int>(), P.flag_bytes, ctr, err, sel, 1,
                          fp32, st);
         return 2;
+    }
+    if (P.precond == FG_PRECOND_SPIKE) {
+        const int fp32 = sel == 1 && sizeof(T) == 4;
+        launch_spike_apply(sys, P.sp_blocks.as<int2>(), P.n_spb, P.sp_ifaces.as<int2>(), P.n_spi, sel, fp32, st);
+        return P.n_spi > 0 ? 3 : 1;
     }
     return 0;
 }
@@ -802,6 +824,9 @@ int validate_member(fg_system *s, const SolveConfig &cfg)
     if (s->op == FG_OP_CSR && !s->csr_ok) { set_error("CSR operator selected but not set up"); return FG_ERR_STATE; }
     if (cfg.precond == FG_PRECOND_ILU0 && s->op != FG_OP_CSR) {
         set_error("ILU(0) needs the CSR operator (fg_set_operator(FG_OP_CSR))"); return FG_ERR_STATE;
+    }
+    if (cfg.precond == FG_PRECOND_SPIKE && (s->op != FG_OP_CSR || !s->sp_ready)) {
+        set_error("SPIKE needs the CSR operator and its set-up (fg_precond_setup)"); return FG_ERR_STATE;
     }
     return FG_OK;
 }

@@ -228,6 +228,7 @@ int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaS
     const Topology &t = s->topo;
     if (kind == FG_PRECOND_NONE) { s->precond = kind; return FG_OK; }
     if (kind == FG_PRECOND_ILU0) return ilu0_setup_device(s, F_dev, st);
+    if (kind == FG_PRECOND_SPIKE) return spike_setup_device(s, F_dev, st);
     if (!s->blocks_ok) { set_error("preconditioner set-up before element blocks were set"); return FG_ERR_STATE; }
     if (kind == FG_PRECOND_DIAG) {
         if (t.n > 0)
@@ -278,6 +279,7 @@ int precond_apply_device(fg_system *s, const double *p, double *z, cudaStream_t 
 {
     const Topology &t = s->topo;
     if (s->precond == FG_PRECOND_ILU0) return ilu0_apply_device(s, p, z, st);
+    if (s->precond == FG_PRECOND_SPIKE) return spike_apply_device(s, p, z, st);
     if (s->precond == FG_PRECOND_DIAG) {
         k_diag_apply<<<(t.n + 256) / 256, 256, 0, st>>>(s->invd64.as<double>(), t.n, p, z);
     } else if (s->precond == FG_PRECOND_BLOCKDIAG) {

@@ -66,7 +66,8 @@ size_t fg_system::bytes() const
     const DevMem *all[] = {&lm, &A64, &A32, &dinc_ptr, &dinc, &ninc_ptr, &ninc, &node_dof, &eorder, &perm,
                            &lm16, &pt_elem, &pt_dof, &pt_col, &pdofs, &rhs_f, &rhs_b,
                            &csr_ia, &csr_ja, &csr_diag, &csr_inc_ptr, &csr_inc, &AA64, &AA32, &LU64, &LU32,
-                           &dinv64, &dinv32, &ilu_flags, &ilu_ctr,
+                           &dinv64, &dinv32, &ilu_flags, &ilu_ctr, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
+                           &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
                            &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
                            &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
@@ -447,6 +448,20 @@ int fg_set_operator(fg_system *s, int op)
         FG_CUDA(cudaStreamSynchronize(s->stream));
     }
     s->op = op;
+    return FG_OK;
+}
+
+int fg_set_spike(fg_system *s, int k, int parts)
+{
+    if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (k < 1 || k > kSpikeMaxK) { set_error("SPIKE coupling size k must be in [1, 64]"); return FG_ERR_ARG; }
+    if (parts < 1 || parts > 65536) { set_error("SPIKE block count must be in [1, 65536]"); return FG_ERR_ARG; }
+    if (k != s->sp_k || parts != s->sp_parts) {
+        s->sp_k = k;
+        s->sp_parts = parts;
+        s->sp_ready = false;
+        if (s->precond == FG_PRECOND_SPIKE) s->precond = FG_PRECOND_NONE;   // set up again
+    }
     return FG_OK;
 }
 

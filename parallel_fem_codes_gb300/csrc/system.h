@@ -57,6 +57,12 @@ struct fg_system {
     int csr_nnz = 0, csr_w = 4;
     fg::DevMem csr_ia, csr_ja, csr_diag, csr_inc_ptr, csr_inc, AA64, AA32, LU64, LU32, dinv64, dinv32, ilu_flags,
         ilu_ctr;
+    // truncated SPIKE over row blocks of the CSR operator
+    int sp_k = 16, sp_parts = 16, sp_P = 0, sp_maxm = 0;
+    bool sp_ready = false;
+    std::vector<int> sp_bs_host;
+    fg::DevMem sp_bs, sp_bl, sp_bu, sp_boff, sp_band, sp_B, sp_C, sp_S, sp_piv, sp_g, sp_h, sp_x, sp_tw, sp_err,
+        sp_items, sp_sysdev;
     // host staging (pinned)
     double *h_vec = nullptr;   // 2*(n+1) doubles
     fg::Workspace ws;
@@ -74,6 +80,17 @@ int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st)
 int launch_ilu_solve(const SysDev *sys, const int2 *items, int nitems, int *flags, size_t flag_bytes, int *counter,
                      int *err, int sel, int backward, int fp32, cudaStream_t st);
 
+// Truncated SPIKE (spike.cu)
+constexpr int kSpikeMaxK = 64;                 // largest coupling size
+constexpr int kSpikeSmemRows = 6144;           // blocks up to this many rows solve in shared memory
+int spike_setup_device(fg_system *s, double *F_dev, cudaStream_t st);
+int spike_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st);
+// One engine apply over a batch: blocks / interfaces are (system, index)
+// items; sel 0 (t64 -> u64, FP64, gate live) or 1 (t -> w, T, gate in_cycle).
+int launch_spike_apply(const SysDev *sys, const int2 *blocks, int nblocks, const int2 *ifaces, int nifaces, int sel,
+                       int fp32, cudaStream_t st);
+void set_spike_fields(SysDev &D, const fg_system *s);
+
 // Patch-layout pointers of a system's descriptor (matvec).
 inline void set_patch_fields(SysDev &D, const fg_system *s)
 {
@@ -89,6 +106,7 @@ inline void set_patch_fields(SysDev &D, const fg_system *s)
     D.dinv64 = s->dinv64.as<double>();
     D.dinv32 = s->dinv32.as<float>();
     D.ilu_flag = nullptr;
+    set_spike_fields(D, s);
     D.lm16 = s->lm16.as<unsigned short>();
     D.pt_elem = s->pt_elem.as<int>();
     D.pt_dof = s->pt_dof.as<int>();

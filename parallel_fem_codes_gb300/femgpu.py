@@ -15,7 +15,7 @@ import numpy as np
 from . import build as _build
 
 FG_OK = 0
-FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG, FG_PRECOND_ILU0 = 0, 1, 2, 3
+FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG, FG_PRECOND_ILU0, FG_PRECOND_SPIKE = 0, 1, 2, 3, 4
 FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED = 64, 32
@@ -139,6 +139,7 @@ def lib(build_if_missing: bool = True):
     L.fg_get_solution.argtypes = [_vp, _f64p]
     L.fg_launch_count.restype = ctypes.c_longlong
     L.fg_set_operator.argtypes = [_vp, _c_int]
+    L.fg_set_spike.argtypes = [_vp, _c_int, _c_int]
     L.fg_get_csr.argtypes = [_vp, ctypes.POINTER(_c_int), _vp, _vp, _vp]
     L.fg_system_stream.argtypes = [_vp]
     L.fg_system_stream.restype = _vp
@@ -258,6 +259,10 @@ class System:
 
     def set_operator(self, op):
         check(lib().fg_set_operator(self._h, op))
+
+    def set_spike(self, k=16, parts=16):
+        """Coupling size and block count of the SPIKE preconditioner."""
+        check(lib().fg_set_spike(self._h, int(k), int(parts)))
 
     def csr(self):
         """(IA, JA, AA) of the assembled operator in the internal (RCM) numbering."""
