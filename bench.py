@@ -240,6 +240,30 @@ def euler_leg(fg, G, n=513, steps=20, corrections=2, kmax=25):
                      "last_true_rel_residual": st["true_rel_residual"]}
     out["mixed_rel_diff_vs_fp64"] = float(np.linalg.norm(us["mixed"] - us["fp64"]) / np.linalg.norm(us["fp64"]))
     out["matvec"] = _matvec_roofline(fg, s)
+    # the reference's second configuration of this problem: CSR operator on the
+    # RCM numbering with ILU(0) (MatrixVectorProductScheme "CSR", "ILU0")
+    t0 = time.perf_counter()
+    sc = fg.euler_system(p, reorder=True)
+    sc.set_operator(fg.FG_OP_CSR)
+    ilu = {"setup_s": time.perf_counter() - t0}
+    sc.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1, precond=fg.FG_PRECOND_ILU0,
+                                       setup_flags=0), kmax=kmax)                                  # warm-up
+    isteps = min(steps, 5)            # the ILU(0) substitutions are latency-bound: fewer steps
+    ilu["steps_timed"] = isteps
+    u_bd, _, _ = s.euler_predictor(p, fg.time_opts(0, corrections, 1e-3, 0, isteps * p.dt, 1e-6, max_steps=isteps),
+                                   kmax=kmax, tol=1e-10)
+    for name, prec in (("fp64", fg.FG_PREC_FP64), ("mixed", fg.FG_PREC_MIXED)):
+        to = fg.time_opts(0, corrections, 1e-3, 0, isteps * p.dt, 1e-6, max_steps=isteps, precond=fg.FG_PRECOND_ILU0,
+                          setup_flags=0)
+        t0 = time.perf_counter()
+        u, a, st = sc.euler_predictor(p, to, kmax=kmax, tol=1e-10, precision=prec)
+        wall = time.perf_counter() - t0
+        ilu[name] = {"seconds": wall, "steps": st["steps"], "corrections": st["corrections"],
+                     "gmres_iterations": st["gmres_iterations"], "steps_per_s": st["steps"] / wall,
+                     "ms_per_correction": 1e3 * wall / st["corrections"],
+                     "last_true_rel_residual": st["true_rel_residual"],
+                     "rel_diff_vs_blockdiag_fp64": float(np.linalg.norm(u - u_bd) / np.linalg.norm(u_bd))}
+    out["csr_ilu0_rcm"] = ilu
     return out
 
 

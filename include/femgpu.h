@@ -259,8 +259,9 @@ int fg_transport_process(fg_system *s, const fg_transport_coeffs *c,
 typedef struct {
     double reynolds;   /* ReynoldsNumber: density 1, viscosity 1/Re          */
     int precond;       /* FG_PRECOND_BLOCKDIAG (BlockDiagDOF3), FG_PRECOND_DIAG
-                          (accumulating, as Diag_precond_EBE_setup.c) or
-                          FG_PRECOND_NONE                                     */
+                          (accumulating, as Diag_precond_EBE_setup.c),
+                          FG_PRECOND_NONE, or FG_PRECOND_ILU0 / _SPIKE on a
+                          system switched to FG_OP_CSR                        */
 } fg_ns_coeffs;
 
 /* Node coordinates, the prescribed (u, v, p) of every node (upresc[3*node+k],
@@ -313,7 +314,8 @@ typedef struct {
     double final_time;     /* FinalTime                                            */
     double time_tol;       /* TimeIntegrationTolerance (StopBySteadyState)         */
     int max_steps;         /* bound on the steps, 0 = none (not in the reference)  */
-    int precond;           /* FG_PRECOND_BLOCKDIAG, FG_PRECOND_DIAG or NONE        */
+    int precond;           /* FG_PRECOND_BLOCKDIAG, FG_PRECOND_DIAG or NONE; ILU0 or
+                              SPIKE on a system switched to FG_OP_CSR            */
     int setup_flags;       /* FG_SETUP_REF_QUIRKS: the reference's 4x4 inverse     */
 } fg_time_opts;
 

@@ -148,6 +148,8 @@ struct SysDev {
     const double *AA64, *LU64, *dinv64;
     const float *AA32, *LU32, *dinv32;
     int *ilu_flag;             // per-row ready flags of the sync-free solves
+    const int *ilu_ford, *ilu_bord;      // rows in forward / backward level order
+    const int2 *ilu_fpass, *ilu_bpass;   // passes (start, rows) of those orders
     // truncated SPIKE (precond == FG_PRECOND_SPIKE): sp_P row blocks of the
     // CSR operator, coupling size sp_k; band LU factors, k x k corner
     // couplings, LU of the 2k x 2k reduced systems; FP64 apply scratch

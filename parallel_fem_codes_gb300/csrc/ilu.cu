@@ -11,12 +11,19 @@
 //   CSR/ILUp_precond.c:4-47.
 //
 // Rows of a triangular factor depend on earlier (forward) or later
-// (backward) rows, so these kernels are "sync-free": each warp claims the
-// next chunk of 32 rows from an atomic counter, in solve order, and each
-// lane waits on the ready flags of the rows its own row reads.  A row only
-// waits on rows claimed before it, by warps already running, so the wait
-// always ends; it is still bounded (kSpinLimit polls), and a wait that runs
-// out records FG_ERR_TIMEOUT instead of hanging.
+// (backward) rows.  The set-up sorts the rows once by dependency level
+// (level of a row = 1 + the largest level of the rows it reads; separately
+// for L and for U) and cuts every level into passes of 32/G rows.  The
+// kernels are "sync-free" over that order: each warp claims the next pass
+// from an atomic counter, G lanes take each row of the pass, and lanes wait
+// on the ready flags of the rows their entries read.  The rows of one pass
+// are of one level and never read each other, so no lane waits for a row
+// of its own warp, and every row waited for belongs to a pass claimed
+// earlier by a running warp: the waits always end.  They are still bounded
+// (kSpinLimit polls); a wait that runs out records FG_ERR_TIMEOUT.  Level
+// order keeps the critical path at the depth of the dependency graph: in
+// plain row order a warp that works through a run of rows turns the chain
+// row i -> row i-1 of a CSR matrix into a chain of the whole matrix.
 //
 // Compiled with -fmad=false: the factorisation and the FP64 substitutions
 // round exactly as the reference's C.
@@ -63,32 +70,67 @@ __global__ void k_csr_assemble(int nnz, const int *__restrict__ inc_ptr, const i
 }
 
 // ---------------------------------------------------------------- rows
-template <typename T>
+// A row of a substitution is handled by a group of G lanes (G = 4 ... 32,
+// from the longest L or U part of the system): each lane waits for the row
+// its entry reads and forms that entry's product, so the waits and loads of
+// a row overlap; the products are then subtracted one by one in column
+// order (every lane of the group repeats the same subtractions), which
+// rounds exactly as the sequential loop of ILUp_precond.c.  The first lane
+// of the group stores the row and raises its flag.
+template <typename T, int G>
 __device__ __forceinline__ void fwd_row(int i, const int *ia, const int *ja, const int *dg, const T *LU,
                                         const T *in, T *out, int *flag, int *err)
 {
+    const int gl = threadIdx.x & (G - 1), gb = (threadIdx.x & 31) & ~(G - 1);
+    const unsigned gm = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << gb;
+    const int b = ia[i], d = dg[i];
     T v = in[i];
-    for (int k = ia[i]; k < dg[i]; ++k) {
-        int j = ja[k];
-        if (!wait_ready(flag + j, err)) break;
-        v -= out[j] * LU[k];
+    for (int base = b; base < d; base += G) {
+        const int k = base + gl;
+        T p = (T)0;
+        if (k < d) {
+            const int j = ja[k];
+            if (wait_ready(flag + j, err)) p = out[j] * LU[k];
+        }
+        const int cnt = min(G, d - base);
+#pragma unroll
+        for (int t = 0; t < G; ++t) {
+            const T pt = __shfl_sync(gm, p, gb + t);
+            if (t < cnt) v = v - pt;
+        }
     }
-    out[i] = v;
-    set_ready(flag + i);
+    if (gl == 0) {
+        out[i] = v;
+        set_ready(flag + i);
+    }
 }
 
-template <typename T>
+template <typename T, int G>
 __device__ __forceinline__ void bwd_row(int i, const int *ia, const int *ja, const int *dg, const T *LU,
                                         const T *dinv, T *x, int *flag, int *err)
 {
+    const int gl = threadIdx.x & (G - 1), gb = (threadIdx.x & 31) & ~(G - 1);
+    const unsigned gm = (G == 32 ? 0xffffffffu : ((1u << G) - 1u)) << gb;
+    const int b = dg[i] + 1, e = ia[i + 1];
     T v = x[i];
-    for (int k = dg[i] + 1; k < ia[i + 1]; ++k) {
-        int j = ja[k];
-        if (!wait_ready(flag + j, err)) break;
-        v -= x[j] * LU[k];
+    for (int base = b; base < e; base += G) {
+        const int k = base + gl;
+        T p = (T)0;
+        if (k < e) {
+            const int j = ja[k];
+            if (wait_ready(flag + j, err)) p = x[j] * LU[k];
+        }
+        const int cnt = min(G, e - base);
+#pragma unroll
+        for (int t = 0; t < G; ++t) {
+            const T pt = __shfl_sync(gm, p, gb + t);
+            if (t < cnt) v = v - pt;
+        }
     }
-    x[i] = v * dinv[i];
-    set_ready(flag + i);
+    if (gl == 0) {
+        x[i] = v * dinv[i];
+        set_ready(flag + i);
+    }
 }
 
 __device__ __forceinline__ int claim(int *counter)
@@ -98,96 +140,216 @@ __device__ __forceinline__ int claim(int *counter)
     return __shfl_sync(0xffffffffu, c, 0);
 }
 
-// ILU(0) factorisation of one system.  chunks: ascending row starts.
-__global__ void k_ilu0_factor(int n, const int *__restrict__ ia, const int *__restrict__ ja, const int *__restrict__ dg,
-                              const double *__restrict__ AA, double *LU, double *dinv, int *flag, int *counter,
-                              int nchunks, int *err)
+// ILU(0) factorisation of one system: a warp per row, rows claimed one at
+// a time in forward level order (the factorisation of a row reads the rows
+// of its L part, as the forward substitution does).  The lanes wait for the rows the
+// L part reads all at once, then stage the row and the U parts of those
+// rows (with each entry's position in the row) in shared memory; the
+// elimination then runs over the L entries in column order inside shared
+// memory, updating each entry in the same order as the IKJ loop of
+// ILUp_precond_setup.c:73-168, so results are bit-identical to it.  Rows
+// longer than kFacRow, with more than 32 L entries or more than kFacPairs
+// U entries to read take the same loop on one lane, reading global memory.
+constexpr int kFacRow = 64, kFacPairs = 448, kFacWarps = 4;
+
+struct FacSm {
+    int col[kFacRow];
+    double val[kFacRow];
+    double dinv[32];
+    int u0[32], ustart[33];
+    short pos[kFacPairs];
+    double uval[kFacPairs];
+};
+
+__device__ __forceinline__ int row_pos(const int *col, int len, int c)
 {
+    int lo = 0, hi = len - 1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        if (col[mid] == c) return mid;
+        if (col[mid] < c) lo = mid + 1; else hi = mid - 1;
+    }
+    return -1;
+}
+
+// One lane, global memory (long rows).
+__device__ void fac_row_seq(int i, const int *__restrict__ ia, const int *__restrict__ ja, const int *__restrict__ dg,
+                            const double *__restrict__ AA, double *LU, double *dinv, int *flag, int *err)
+{
+    const int b = ia[i], e = ia[i + 1];
+    for (int k = b; k < e; ++k) LU[k] = k == dg[i] ? 0.0 : AA[k];
+    double piv = AA[dg[i]];
+    for (int k = b; k < dg[i]; ++k) {
+        const int jrow = ja[k];
+        if (!wait_ready(flag + jrow, err)) break;
+        LU[k] = LU[k] * dinv[jrow];
+        const double lk = LU[k];
+        for (int m = dg[jrow] + 1; m < ia[jrow + 1]; ++m) {
+            const int col = ja[m];
+            int lo = b, hi = e - 1, pos = -1;
+            while (lo <= hi) {
+                int mid = (lo + hi) >> 1;
+                if (ja[mid] == col) { pos = mid; break; }
+                if (ja[mid] < col) lo = mid + 1; else hi = mid - 1;
+            }
+            if (pos < 0) continue;
+            if (col == i) piv = piv - lk * LU[m];
+            else LU[pos] = LU[pos] - lk * LU[m];
+        }
+    }
+    if (piv == 0.0) atomicExch(err, FG_ERR_BREAKDOWN);
+    dinv[i] = 1.0 / piv;
+}
+
+__global__ void __launch_bounds__(32 * kFacWarps)
+k_ilu0_factor(int n, const int *__restrict__ ord, const int *__restrict__ ia, const int *__restrict__ ja,
+              const int *__restrict__ dg, const double *__restrict__ AA, double *LU, double *dinv, int *flag,
+              int *counter, int *err)
+{
+    __shared__ FacSm sm_all[kFacWarps];
+    FacSm &S = sm_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     for (;;) {
-        int c = claim(counter);
-        if (c >= nchunks) break;
-        int i = c * 32 + lane;
-        if (i >= n) continue;
-        const int b = ia[i], e = ia[i + 1];
-        for (int k = b; k < e; ++k) LU[k] = k == dg[i] ? 0.0 : AA[k];
-        double piv = AA[dg[i]];
-        for (int k = b; k < dg[i]; ++k) {
-            const int jrow = ja[k];
-            if (!wait_ready(flag + jrow, err)) break;
-            LU[k] *= dinv[jrow];
-            const double lk = LU[k];
-            for (int m = dg[jrow] + 1; m < ia[jrow + 1]; ++m) {
-                const int col = ja[m];
-                // column of row jrow's U part inside row i's pattern?
-                int lo = b, hi = e - 1, pos = -1;
-                while (lo <= hi) {
-                    int mid = (lo + hi) >> 1;
-                    if (ja[mid] == col) { pos = mid; break; }
-                    if (ja[mid] < col) lo = mid + 1; else hi = mid - 1;
-                }
-                if (pos < 0) continue;
-                if (col == i) piv -= lk * LU[m];
-                else LU[pos] -= lk * LU[m];
+        const int c = claim(counter);
+        if (c >= n) break;
+        {
+            const int i = ord[c];
+            const int b = ia[i], e = ia[i + 1], d = dg[i], len = e - b, nL = d - b;
+            int u0 = 0, ulen = 0;
+            double dj = 0.0;
+            if (nL <= 32 && lane < nL) {
+                const int jrow = ja[b + lane];
+                wait_ready(flag + jrow, err);
+                u0 = dg[jrow] + 1;
+                ulen = ia[jrow + 1] - u0;
+                dj = dinv[jrow];
             }
+            int scan = ulen;                       // inclusive scan of the U lengths
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, scan, o);
+                if (lane >= o) scan += t;
+            }
+            const int total = __shfl_sync(0xffffffffu, scan, 31);
+            if (len > kFacRow || nL > 32 || total > kFacPairs) {
+                if (lane == 0) fac_row_seq(i, ia, ja, dg, AA, LU, dinv, flag, err);
+                __syncwarp();
+            } else {
+                for (int t = lane; t < len; t += 32) {
+                    S.col[t] = ja[b + t];
+                    S.val[t] = AA[b + t];          // the diagonal slot carries the pivot
+                }
+                if (lane < nL) {
+                    S.dinv[lane] = dj;
+                    S.u0[lane] = u0;
+                    S.ustart[lane] = scan - ulen;
+                }
+                if (lane == 0) S.ustart[nL] = total;
+                __syncwarp();
+#pragma unroll 2
+                for (int q = 0; q < (kFacPairs + 31) / 32; ++q) {
+                    const int p = lane + 32 * q;
+                    if (p < total) {
+                        int lo = 0, hi = nL - 1;       // entry l with ustart[l] <= p < ustart[l+1]
+                        while (lo < hi) {
+                            const int mid = (lo + hi + 1) >> 1;
+                            if (S.ustart[mid] <= p) lo = mid; else hi = mid - 1;
+                        }
+                        const int m = S.u0[lo] + (p - S.ustart[lo]);
+                        S.pos[p] = (short)row_pos(S.col, len, ja[m]);
+                        S.uval[p] = __ldcg(LU + m);   // another lane waited for this row: read from L2
+                    }
+                }
+                __syncwarp();
+                for (int l = 0; l < nL; ++l) {
+                    if (lane == 0) S.val[l] = S.val[l] * S.dinv[l];
+                    __syncwarp();
+                    const double lk = S.val[l];
+                    for (int p = S.ustart[l] + lane; p < S.ustart[l + 1]; p += 32) {
+                        const int ps = S.pos[p];
+                        if (ps >= 0) S.val[ps] = S.val[ps] - lk * S.uval[p];
+                    }
+                    __syncwarp();
+                }
+                for (int t = lane; t < len; t += 32) LU[b + t] = t == nL ? 0.0 : S.val[t];
+                if (lane == 0) {
+                    const double piv = S.val[nL];
+                    if (piv == 0.0) atomicExch(err, FG_ERR_BREAKDOWN);
+                    dinv[i] = 1.0 / piv;
+                }
+                __syncwarp();
+            }
+            if (lane == 0) {
+                __threadfence();
+                set_ready(flag + i);
+            }
+            __syncwarp();
         }
-        if (piv == 0.0) atomicExch(err, FG_ERR_BREAKDOWN);
-        dinv[i] = 1.0 / piv;
-        set_ready(flag + i);
     }
+}
+
+// Rows of pass p (start and count in the level order `ord`) for this
+// lane's group; a pass longer than 32/G rows (a batch running systems with
+// fewer lanes per row) is taken in several rounds, all of one level.
+template <int G, typename F>
+__device__ __forceinline__ void for_pass_rows(const int *ord, int2 p, F &&row)
+{
+    const int g = (threadIdx.x & 31) / G;
+    for (int r0 = 0; r0 < p.y; r0 += 32 / G)
+        if (r0 + g < p.y) row(ord[p.x + r0 + g]);
 }
 
 // Substitutions of one system (set-up path: F <- U^-1 L^-1 F, FP64).
-__global__ void k_ilu_fwd1(int n, const int *ia, const int *ja, const int *dg, const double *LU, const double *in,
-                           double *out, int *flag, int *counter, int nchunks, int *err)
+template <int G>
+__global__ void k_ilu_fwd1(const int *ord, const int2 *passes, int npass, const int *ia, const int *ja, const int *dg,
+                           const double *LU, const double *in, double *out, int *flag, int *counter, int *err)
 {
-    const int lane = threadIdx.x & 31;
     for (;;) {
-        int c = claim(counter);
-        if (c >= nchunks) break;
-        int i = c * 32 + lane;
-        if (i < n) fwd_row<double>(i, ia, ja, dg, LU, in, out, flag, err);
+        const int c = claim(counter);
+        if (c >= npass) break;
+        for_pass_rows<G>(ord, passes[c], [&](int i) { fwd_row<double, G>(i, ia, ja, dg, LU, in, out, flag, err); });
     }
 }
 
-__global__ void k_ilu_bwd1(int n, const int *ia, const int *ja, const int *dg, const double *LU, const double *dinv,
-                           double *x, int *flag, int *counter, int nchunks, int *err)
+template <int G>
+__global__ void k_ilu_bwd1(const int *ord, const int2 *passes, int npass, const int *ia, const int *ja, const int *dg,
+                           const double *LU, const double *dinv, double *x, int *flag, int *counter, int *err)
 {
-    const int lane = threadIdx.x & 31;
     for (;;) {
-        int c = claim(counter);
-        if (c >= nchunks) break;
-        int i = (nchunks - 1 - c) * 32 + lane;       // chunks from the last row down
-        if (i < n) bwd_row<double>(i, ia, ja, dg, LU, dinv, x, flag, err);
+        const int c = claim(counter);
+        if (c >= npass) break;
+        for_pass_rows<G>(ord, passes[c], [&](int i) { bwd_row<double, G>(i, ia, ja, dg, LU, dinv, x, flag, err); });
     }
 }
 
-// Engine substitutions over a batch.  items: (system, first row) in solve
-// order (ascending rows per system for fwd, descending for bwd); sel 0:
-// FP64 t64 -> u64 (cycle start, gate live), sel 1: t -> w (Arnoldi, gate
-// in cycle).  The flags of every system were cleared before the launch.
-template <typename T>
+// Engine substitutions over a batch.  items: (system, pass) in solve order
+// (the passes of every system interleaved, each system's in its level
+// order); sel 0: FP64 t64 -> u64 (cycle start, gate live), sel 1: t -> w
+// (Arnoldi, gate in cycle).  The flags of every system were cleared before
+// the launch.
+template <typename T, int G>
 __global__ void k_ilu_solve(const SysDev *__restrict__ sys, const int2 *__restrict__ items, int nitems,
                             int *counter, int sel, int backward, int *err)
 {
-    const int lane = threadIdx.x & 31;
     for (;;) {
-        int c = claim(counter);
+        const int c = claim(counter);
         if (c >= nitems) break;
         const int2 it = items[c];
         const SysDev &D = sys[it.x];
         if (sel == 0 ? !D.st->live : !D.st->in_cycle) continue;
-        const int i = it.y + lane;
-        if (i >= D.n) continue;
         const T *LU = sizeof(T) == 8 ? (const T *)D.LU64 : (const T *)D.LU32;
         if (!backward) {
             const T *in = sel == 0 ? (const T *)D.t64 : (const T *)D.t;
             T *out = sel == 0 ? (T *)D.u64 : (T *)D.w;
-            fwd_row<T>(i, D.csr_ia, D.csr_ja, D.csr_diag, LU, in, out, D.ilu_flag, err);
+            for_pass_rows<G>(D.ilu_ford, D.ilu_fpass[it.y], [&](int i) {
+                fwd_row<T, G>(i, D.csr_ia, D.csr_ja, D.csr_diag, LU, in, out, D.ilu_flag, err);
+            });
         } else {
             T *x = sel == 0 ? (T *)D.u64 : (T *)D.w;
             const T *dinv = sizeof(T) == 8 ? (const T *)D.dinv64 : (const T *)D.dinv32;
-            bwd_row<T>(i, D.csr_ia, D.csr_ja, D.csr_diag, LU, dinv, x, D.ilu_flag, err);
+            for_pass_rows<G>(D.ilu_bord, D.ilu_bpass[it.y], [&](int i) {
+                bwd_row<T, G>(i, D.csr_ia, D.csr_ja, D.csr_diag, LU, dinv, x, D.ilu_flag, err);
+            });
         }
     }
 }
@@ -202,6 +364,61 @@ __global__ void k_f64_to_f32(const double *a, float *b, int n)
 static int warps_grid()
 {
     return 4 * sm_count();   // 256-thread CTAs: 8 warps each
+}
+
+// Level order of the rows for the forward (L) or backward (U) dependency
+// graph and its passes of at most `rows` rows, each inside one level.
+static void ilu_schedule(const CsrTopology &c, bool backward, int rows, std::vector<int> &order,
+                         std::vector<int2> &passes)
+{
+    const int n = c.n;
+    std::vector<int> lev(n, 0);
+    int top = 0;
+    for (int t = 0; t < n; ++t) {
+        const int i = backward ? n - 1 - t : t;
+        const int k0 = backward ? c.diag[i] + 1 : c.ia[i], k1 = backward ? c.ia[i + 1] : c.diag[i];
+        int l = 0;
+        for (int k = k0; k < k1; ++k) l = std::max(l, lev[c.ja[k]] + 1);
+        lev[i] = l;
+        top = std::max(top, l);
+    }
+    std::vector<int> start(top + 2, 0);
+    for (int i = 0; i < n; ++i) ++start[lev[i] + 1];
+    for (int l = 0; l <= top; ++l) start[l + 1] += start[l];
+    order.assign(n, 0);
+    std::vector<int> pos(start.begin(), start.end() - 1);
+    for (int i = 0; i < n; ++i) order[pos[lev[i]]++] = i;
+    passes.clear();
+    for (int l = 0; l <= top && n > 0; ++l)
+        for (int p = start[l]; p < start[l + 1]; p += rows) passes.push_back(make_int2(p, std::min(rows, start[l + 1] - p)));
+}
+
+// One substitution of one system on its flags and counter (cleared here).
+static int sweep1(fg_system *s, bool backward, const double *in, double *x, cudaStream_t st)
+{
+    const int n = s->topo.n;
+    int *flag = s->ilu_flags.as<int>(), *ctr = s->ilu_ctr.as<int>(), *err = ctr + 4;
+    const int *ia = s->csr_ia.as<int>(), *ja = s->csr_ja.as<int>(), *dg = s->csr_diag.as<int>();
+    const double *LU = s->LU64.as<double>(), *dinv = s->dinv64.as<double>();
+    const int *ord = backward ? s->ilu_bord.as<int>() : s->ilu_ford.as<int>();
+    const int2 *ps = backward ? s->ilu_bpass.as<int2>() : s->ilu_fpass.as<int2>();
+    const int np = backward ? s->ilu_nbpass : s->ilu_nfpass;
+    FG_CUDA(cudaMemsetAsync(flag, 0, 4 * (size_t)(n + 1), st));
+    FG_CUDA(cudaMemsetAsync(ctr, 0, 4, st));
+    const int g = warps_grid();
+#define FG_SWEEP1(G)                                                                                      \
+    (backward ? k_ilu_bwd1<G><<<g, 256, 0, st>>>(ord, ps, np, ia, ja, dg, LU, dinv, x, flag, ctr, err)     \
+              : k_ilu_fwd1<G><<<g, 256, 0, st>>>(ord, ps, np, ia, ja, dg, LU, in, x, flag, ctr, err))
+    switch (s->ilu_g) {
+    case 4: FG_SWEEP1(4); break;
+    case 8: FG_SWEEP1(8); break;
+    case 16: FG_SWEEP1(16); break;
+    default: FG_SWEEP1(32); break;
+    }
+#undef FG_SWEEP1
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    return FG_OK;
 }
 
 int csr_setup(fg_system *s)
@@ -224,6 +441,27 @@ int csr_setup(fg_system *s)
         (r = s->ilu_ctr.alloc(64)))
         return r;
     s->csr_nnz = c.nnz;
+    // substitution schedule: lanes per row from the longest L or U part
+    int longest = 1;
+    for (int i = 0; i < c.n; ++i) longest = std::max({longest, c.diag[i] - c.ia[i], c.ia[i + 1] - c.diag[i] - 1});
+    s->ilu_g = longest <= 4 ? 4 : longest <= 8 ? 8 : longest <= 16 ? 16 : 32;
+    {
+        std::vector<int> fo, bo;
+        std::vector<int2> fp, bp;
+        ilu_schedule(c, false, 32 / s->ilu_g, fo, fp);
+        ilu_schedule(c, true, 32 / s->ilu_g, bo, bp);
+        auto up2 = [](DevMem &m, const std::vector<int2> &v) -> int {
+            int rr = m.alloc(sizeof(int2) * std::max<size_t>(v.size(), 1));
+            if (rr) return rr;
+            if (!v.empty()) FG_CUDA(cudaMemcpy(m.p, v.data(), sizeof(int2) * v.size(), cudaMemcpyHostToDevice));
+            return FG_OK;
+        };
+        if ((r = up(s->ilu_ford, fo)) || (r = up(s->ilu_bord, bo)) || (r = up2(s->ilu_fpass, fp)) ||
+            (r = up2(s->ilu_bpass, bp)))
+            return r;
+        s->ilu_nfpass = (int)fp.size();
+        s->ilu_nbpass = (int)bp.size();
+    }
     double avg = c.n ? (double)c.nnz / c.n : 1.0;
     s->csr_w = avg <= 8 ? 4 : avg <= 16 ? 8 : 32;
     s->csr_ok = true;
@@ -253,14 +491,15 @@ int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st)
     int r;
     if (!s->csr_ok) { set_error("ILU(0) needs the CSR operator (fg_set_operator(FG_OP_CSR))"); return FG_ERR_STATE; }
     if ((r = csr_refresh(s, st))) return r;
-    const int n = s->topo.n, nch = (n + 31) / 32;
+    const int n = s->topo.n;
     int *flag = s->ilu_flags.as<int>(), *ctr = s->ilu_ctr.as<int>(), *err = ctr + 4;
     FG_CUDA(cudaMemsetAsync(s->ilu_ctr.p, 0, s->ilu_ctr.bytes, st));
     FG_CUDA(cudaMemsetAsync(flag, 0, 4 * (size_t)(n + 1), st));
     if (n > 0)
-        k_ilu0_factor<<<warps_grid(), 256, 0, st>>>(n, s->csr_ia.as<int>(), s->csr_ja.as<int>(), s->csr_diag.as<int>(),
-                                                    s->AA64.as<double>(), s->LU64.as<double>(), s->dinv64.as<double>(),
-                                                    flag, ctr, nch, err);
+        k_ilu0_factor<<<8 * sm_count(), 32 * kFacWarps, 0, st>>>(n, s->ilu_ford.as<int>(), s->csr_ia.as<int>(),
+                                                                 s->csr_ja.as<int>(), s->csr_diag.as<int>(),
+                                                                 s->AA64.as<double>(), s->LU64.as<double>(),
+                                                                 s->dinv64.as<double>(), flag, ctr, err);
     FG_CUDA(cudaGetLastError());
     k_f64_to_f32<<<(std::max(s->csr_nnz, 1) + 255) / 256, 256, 0, st>>>(s->LU64.as<double>(), s->LU32.as<float>(),
                                                                        s->csr_nnz);
@@ -269,19 +508,10 @@ int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st)
     count_launches(3);
     if (F_dev && n > 0) {
         double *tmp = s->ws.t64.as<double>();   // F_dev is ws.u64 when called from fg_precond_setup
-        FG_CUDA(cudaMemsetAsync(flag, 0, 4 * (size_t)(n + 1), st));
-        FG_CUDA(cudaMemsetAsync(ctr, 0, 4, st));
-        k_ilu_fwd1<<<warps_grid(), 256, 0, st>>>(n, s->csr_ia.as<int>(), s->csr_ja.as<int>(), s->csr_diag.as<int>(),
-                                                 s->LU64.as<double>(), F_dev, tmp, flag, ctr, nch, err);
-        FG_CUDA(cudaMemsetAsync(flag, 0, 4 * (size_t)(n + 1), st));
-        FG_CUDA(cudaMemsetAsync(ctr, 0, 4, st));
-        k_ilu_bwd1<<<warps_grid(), 256, 0, st>>>(n, s->csr_ia.as<int>(), s->csr_ja.as<int>(), s->csr_diag.as<int>(),
-                                                 s->LU64.as<double>(), s->dinv64.as<double>(), tmp, flag, ctr, nch,
-                                                 err);
-        FG_CUDA(cudaGetLastError());
+        int r2;
+        if ((r2 = sweep1(s, false, F_dev, tmp, st)) || (r2 = sweep1(s, true, nullptr, tmp, st))) return r2;
         FG_CUDA(cudaMemcpyAsync(F_dev, tmp, 8 * (size_t)n, cudaMemcpyDeviceToDevice, st));
         FG_CUDA(cudaMemsetAsync(tmp, 0, 8 * (size_t)s->n_pad, st));
-        count_launches(2);
     }
     int herr = 0;
     FG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -295,20 +525,13 @@ int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st)
 // z = U^-1 L^-1 p of one system (FP64, internal numbering; p may be z).
 int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st)
 {
-    const int n = s->topo.n, nch = (n + 31) / 32;
+    const int n = s->topo.n;
     if (s->precond != FG_PRECOND_ILU0) { set_error("ILU(0) not set up"); return FG_ERR_STATE; }
-    int *flag = s->ilu_flags.as<int>(), *ctr = s->ilu_ctr.as<int>(), *err = ctr + 4;
+    int *ctr = s->ilu_ctr.as<int>(), *err = ctr + 4;
     double *tmp = s->ws.t64.as<double>();
     FG_CUDA(cudaMemsetAsync(s->ilu_ctr.p, 0, s->ilu_ctr.bytes, st));
-    FG_CUDA(cudaMemsetAsync(flag, 0, 4 * (size_t)(n + 1), st));
-    k_ilu_fwd1<<<warps_grid(), 256, 0, st>>>(n, s->csr_ia.as<int>(), s->csr_ja.as<int>(), s->csr_diag.as<int>(),
-                                             s->LU64.as<double>(), p, tmp, flag, ctr, nch, err);
-    FG_CUDA(cudaMemsetAsync(flag, 0, 4 * (size_t)(n + 1), st));
-    FG_CUDA(cudaMemsetAsync(ctr, 0, 4, st));
-    k_ilu_bwd1<<<warps_grid(), 256, 0, st>>>(n, s->csr_ia.as<int>(), s->csr_ja.as<int>(), s->csr_diag.as<int>(),
-                                             s->LU64.as<double>(), s->dinv64.as<double>(), tmp, flag, ctr, nch, err);
-    FG_CUDA(cudaGetLastError());
-    count_launches(2);
+    int r;
+    if ((r = sweep1(s, false, p, tmp, st)) || (r = sweep1(s, true, nullptr, tmp, st))) return r;
     FG_CUDA(cudaMemcpyAsync(z, tmp, 8 * (size_t)n, cudaMemcpyDeviceToDevice, st));
     FG_CUDA(cudaMemsetAsync(z + n, 0, 8, st));
     FG_CUDA(cudaMemsetAsync(tmp, 0, 8 * (size_t)s->n_pad, st));
@@ -321,14 +544,28 @@ int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st)
 
 // One sync-free substitution over a batch (engine; flags cleared here).
 int launch_ilu_solve(const SysDev *sys, const int2 *items, int nitems, int *flags, size_t flag_bytes, int *counter,
-                     int *err, int sel, int backward, int fp32, cudaStream_t st)
+                     int *err, int sel, int backward, int fp32, int lanes, cudaStream_t st)
 {
     FG_CUDA(cudaMemsetAsync(flags, 0, flag_bytes, st));
     FG_CUDA(cudaMemsetAsync(counter, 0, sizeof(int), st));
-    if (fp32)
-        k_ilu_solve<float><<<warps_grid(), 256, 0, st>>>(sys, items, nitems, counter, sel, backward, err);
-    else
-        k_ilu_solve<double><<<warps_grid(), 256, 0, st>>>(sys, items, nitems, counter, sel, backward, err);
+    const int g = warps_grid();
+#define FG_SOLVE(T, G) k_ilu_solve<T, G><<<g, 256, 0, st>>>(sys, items, nitems, counter, sel, backward, err)
+    if (fp32) {
+        switch (lanes) {
+        case 4: FG_SOLVE(float, 4); break;
+        case 8: FG_SOLVE(float, 8); break;
+        case 16: FG_SOLVE(float, 16); break;
+        default: FG_SOLVE(float, 32); break;
+        }
+    } else {
+        switch (lanes) {
+        case 4: FG_SOLVE(double, 4); break;
+        case 8: FG_SOLVE(double, 8); break;
+        case 16: FG_SOLVE(double, 16); break;
+        default: FG_SOLVE(double, 32); break;
+        }
+    }
+#undef FG_SOLVE
     FG_CUDA(cudaGetLastError());
     count_launches(1);
     return FG_OK;

@@ -529,9 +529,9 @@ int parts_for(int n)
 // Chunk tables of one batch (device copies + host counts).
 struct Plan {
     int nsys = 0, ncol = 0, S = 3, B = 1, maxdof = 1;   // ncol: patch colours
-    int op = FG_OP_EBE, csr_w = 4, precond = FG_PRECOND_NONE;
+    int op = FG_OP_EBE, csr_w = 4, precond = FG_PRECOND_NONE, ilu_g = 4;
     std::vector<int> ech_off;      // ncol+1 offsets into echunks
-    int n_dch = 0, n_nch = 0, n_ilu = 0, n_spb = 0, n_spi = 0;
+    int n_dch = 0, n_nch = 0, n_ilu = 0, n_ilub = 0, n_spb = 0, n_spi = 0;
     size_t flag_bytes = 0;
     DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
     DevMem ilu_fwd, ilu_bwd, ilu_flags, ilu_ctr;   // sync-free ILU(0) substitutions
@@ -585,8 +585,8 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
         if (m.s->op != P.op) { set_error("a batch must use one operator kind"); return FG_ERR_ARG; }
         P.csr_w = std::max(P.csr_w, m.s->csr_w);
     }
-    // ILU(0) substitutions: 32-row items, rows ascending (forward) or
-    // descending (backward) within each system, systems interleaved
+    // ILU(0) substitutions: one item per pass of a system's level order
+    // (forward and backward lists), systems interleaved
     std::vector<int2> fwd, bwd;
     if (cfg.precond == FG_PRECOND_ILU0) {
         std::vector<size_t> off(P.nsys + 1, 0);
@@ -595,17 +595,18 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
         int r0;
         if ((r0 = P.ilu_flags.alloc(std::max<size_t>(P.flag_bytes, 4))) || (r0 = P.ilu_ctr.alloc(64))) return r0;
         for (int s = 0; s < P.nsys; ++s) hs[s].ilu_flag = P.ilu_flags.as<int>() + off[s];
-        int maxch = 0;
-        for (int s = 0; s < P.nsys; ++s) maxch = std::max(maxch, (mem[s].s->topo.n + 31) / 32);
-        for (int q = 0; q < maxch; ++q)
+        int maxp = 0;
+        for (int s = 0; s < P.nsys; ++s) {
+            maxp = std::max({maxp, mem[s].s->ilu_nfpass, mem[s].s->ilu_nbpass});
+            P.ilu_g = std::max(P.ilu_g, mem[s].s->ilu_g);
+        }
+        for (int q = 0; q < maxp; ++q)
             for (int s = 0; s < P.nsys; ++s) {
-                int nch_s = (mem[s].s->topo.n + 31) / 32;
-                if (q < nch_s) {
-                    fwd.push_back(make_int2(s, q * 32));
-                    bwd.push_back(make_int2(s, (nch_s - 1 - q) * 32));
-                }
+                if (q < mem[s].s->ilu_nfpass) fwd.push_back(make_int2(s, q));
+                if (q < mem[s].s->ilu_nbpass) bwd.push_back(make_int2(s, q));
             }
         P.n_ilu = (int)fwd.size();
+        P.n_ilub = (int)bwd.size();
     }
     // SPIKE: one CTA per block and per interface of every member
     std::vector<int2> spb, spi;
@@ -720,9 +721,9 @@ static int enqueue_precond(const Plan &P, int sel, cudaStream_t st)
         int *ctr = P.ilu_ctr.as<int>(), *err = ctr + 4;
         const int fp32 = sel == 1 && sizeof(T) == 4;
         launch_ilu_solve(sys, P.ilu_fwd.as<int2>(), P.n_ilu, P.ilu_flags.as<int>(), P.flag_bytes, ctr, err, sel, 0,
-                         fp32, st);
-        launch_ilu_solve(sys, P.ilu_bwd.as<int2>(), P.n_ilu, P.ilu_flags.as<int>(), P.flag_bytes, ctr, err, sel, 1,
-                         fp32, st);
+                         fp32, P.ilu_g, st);
+        launch_ilu_solve(sys, P.ilu_bwd.as<int2>(), P.n_ilub, P.ilu_flags.as<int>(), P.flag_bytes, ctr, err, sel, 1,
+                         fp32, P.ilu_g, st);
         return 2;
     }
     if (P.precond == FG_PRECOND_SPIKE) {

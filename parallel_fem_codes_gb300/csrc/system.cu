@@ -66,7 +66,7 @@ size_t fg_system::bytes() const
     const DevMem *all[] = {&lm, &A64, &A32, &dinc_ptr, &dinc, &ninc_ptr, &ninc, &node_dof, &eorder, &perm,
                            &lm16, &pt_elem, &pt_dof, &pt_col, &pdofs, &rhs_f, &rhs_b,
                            &csr_ia, &csr_ja, &csr_diag, &csr_inc_ptr, &csr_inc, &AA64, &AA32, &LU64, &LU32,
-                           &dinv64, &dinv32, &ilu_flags, &ilu_ctr, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
+                           &dinv64, &dinv32, &ilu_flags, &ilu_ctr, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
                            &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
                            &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
@@ -622,8 +622,8 @@ int fg_ns_process(fg_system *s, const fg_ns_coeffs *c, const fg_solver_opts *o, 
                   int max_nonlinear, double *u, fg_process_stats *stats)
 {
     if (!s || !c || !o || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
-    if (c->precond != FG_PRECOND_NONE && c->precond != FG_PRECOND_DIAG && c->precond != FG_PRECOND_BLOCKDIAG) {
-        set_error("Navier-Stokes preconditioner must be NONE, DIAG or BLOCKDIAG");
+    if (c->precond < FG_PRECOND_NONE || c->precond > FG_PRECOND_SPIKE) {
+        set_error("Navier-Stokes preconditioner must be NONE, DIAG, BLOCKDIAG, ILU0 or SPIKE");
         return FG_ERR_ARG;
     }
     auto t0 = std::chrono::steady_clock::now();
@@ -717,8 +717,8 @@ int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_o
                        double *u, double *a, fg_time_stats *stats)
 {
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
-    if (to->precond != FG_PRECOND_NONE && to->precond != FG_PRECOND_DIAG && to->precond != FG_PRECOND_BLOCKDIAG) {
-        set_error("Euler preconditioner must be NONE, DIAG or BLOCKDIAG");
+    if (to->precond < FG_PRECOND_NONE || to->precond > FG_PRECOND_SPIKE) {
+        set_error("Euler preconditioner must be NONE, DIAG, BLOCKDIAG, ILU0 or SPIKE");
         return FG_ERR_ARG;
     }
     if (to->max_corrections < 1 || !(c->dt > 0)) { set_error("max_corrections >= 1 and dt > 0 required"); return FG_ERR_ARG; }

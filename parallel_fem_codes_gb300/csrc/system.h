@@ -55,6 +55,10 @@ struct fg_system {
     int op = FG_OP_EBE;
     bool csr_ok = false, csr_dirty = true;
     int csr_nnz = 0, csr_w = 4;
+    // ILU(0) schedule: rows in level order (forward / backward) and their
+    // passes; ilu_g lanes per row
+    int ilu_g = 32, ilu_nfpass = 0, ilu_nbpass = 0;
+    fg::DevMem ilu_ford, ilu_bord, ilu_fpass, ilu_bpass;
     fg::DevMem csr_ia, csr_ja, csr_diag, csr_inc_ptr, csr_inc, AA64, AA32, LU64, LU32, dinv64, dinv32, ilu_flags,
         ilu_ctr;
     // truncated SPIKE over row blocks of the CSR operator
@@ -78,7 +82,7 @@ int csr_refresh(fg_system *s, cudaStream_t st);
 int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st);
 int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st);
 int launch_ilu_solve(const SysDev *sys, const int2 *items, int nitems, int *flags, size_t flag_bytes, int *counter,
-                     int *err, int sel, int backward, int fp32, cudaStream_t st);
+                     int *err, int sel, int backward, int fp32, int lanes, cudaStream_t st);
 
 // Truncated SPIKE (spike.cu)
 constexpr int kSpikeMaxK = 64;                 // largest coupling size
@@ -106,6 +110,10 @@ inline void set_patch_fields(SysDev &D, const fg_system *s)
     D.dinv64 = s->dinv64.as<double>();
     D.dinv32 = s->dinv32.as<float>();
     D.ilu_flag = nullptr;
+    D.ilu_ford = s->ilu_ford.as<int>();
+    D.ilu_bord = s->ilu_bord.as<int>();
+    D.ilu_fpass = s->ilu_fpass.as<int2>();
+    D.ilu_bpass = s->ilu_bpass.as<int2>();
     set_spike_fields(D, s);
     D.lm16 = s->lm16.as<unsigned short>();
     D.pt_elem = s->pt_elem.as<int>();

@@ -416,18 +416,20 @@ def time_opts(stop_by_norm=0, max_corrections=2, correction_tol=1e-3, steady_sta
                     precond, setup_flags)
 
 
-def euler_system(prob) -> System:
-    """A System (ndof = 4, node-order numbering) with the geometry and
-    prescribed values of an Euler problem."""
-    s = System(prob.mesh, reorder=False)
+def euler_system(prob, reorder=False) -> System:
+    """A System (ndof = 4; node-order numbering, or RCM with reorder=True,
+    as the CSR/ILU(0) configuration uses) with the geometry and prescribed
+    values of an Euler problem."""
+    s = System(prob.mesh, reorder=reorder)
     s.euler_set_geometry(prob)
     return s
 
 
-def ns_system(prob) -> System:
-    """A System (ndof = 3, node-order numbering) with the geometry, prescribed
-    values and body force of a Navier-Stokes problem."""
-    s = System(prob.mesh, reorder=False)
+def ns_system(prob, reorder=False) -> System:
+    """A System (ndof = 3; node-order numbering, or RCM with reorder=True)
+    with the geometry, prescribed values and body force of a Navier-Stokes
+    problem."""
+    s = System(prob.mesh, reorder=reorder)
     s.ns_set_geometry(prob)
     return s
 

@@ -103,6 +103,26 @@ def test_euler_predictor_mixed(fg):
     assert rel(ug, uo) < 1e-7
 
 
+@pytest.mark.parametrize("precond", ["ilu0", "spike"])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_euler_predictor_csr_rcm(fg, precond, precision):
+    """The CSR operator on the RCM numbering with ILU(0) (the reference's
+    "CSR" + "ILU0" configuration) or SPIKE inside the time loop reaches the
+    same states as the oracle's BlockDiag run."""
+    p = G.obliquo_problem(17)
+    to_o = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt, 1e-6, 0)
+    uo, ao, sto = O.euler_predictor(p, to_o, tol=1e-10, kmax=25)
+    s = fg.euler_system(p, reorder=True)
+    s.set_operator(fg.FG_OP_CSR)
+    kind = fg.FG_PRECOND_ILU0 if precond == "ilu0" else fg.FG_PRECOND_SPIKE
+    if precond == "spike":
+        s.set_spike(16, 4)
+    to = fg.time_opts(0, 2, 1e-3, 0, 3 * p.dt, 1e-6, precond=kind, setup_flags=0)
+    ug, ag, st = s.euler_predictor(p, to, kmax=25, tol=1e-10, precision=precision)
+    assert st["steps"] == 3 and st["true_rel_residual"] <= 1e-9
+    assert rel(ug, uo) < 1e-7
+
+
 def test_euler_rejects_wrong_ndof(fg):
     p = G.transport_problem(9)
     s = fg.System(p.mesh)

@@ -94,6 +94,23 @@ def test_ns_process_fp64(fg):
     assert rel(ug, uo) < 1e-7
 
 
+@pytest.mark.parametrize("precond", ["ilu0", "spike"])
+def test_ns_process_csr_rcm(fg, precond):
+    """The Picard loop on the CSR operator in the RCM numbering with ILU(0)
+    or SPIKE reaches the oracle's (BlockDiagDOF3) solution."""
+    p = G.cavity_problem(17, reynolds=100.0)
+    uo, nl_o, its_o, last_o = O.ns_process(p, 1e-10, 1e-6, 30, 1000, 40)
+    s = fg.ns_system(p, reorder=True)
+    s.set_operator(fg.FG_OP_CSR)
+    kind = fg.FG_PRECOND_ILU0 if precond == "ilu0" else fg.FG_PRECOND_SPIKE
+    if precond == "spike":
+        s.set_spike(12, 4)
+    ug, st = s.ns_process(p, kmax=30, tol=1e-10, nonlinear_tol=1e-6, max_nonlinear=40, precond=kind)
+    assert abs(st["nonlinear_iterations"] - nl_o) <= 1
+    assert st["nonlinear_residual"] <= 1e-6
+    assert rel(ug, uo) < 1e-7
+
+
 def test_ns_process_mixed(fg):
     p = G.cavity_problem(17, reynolds=100.0, jitter=0.2)
     uo, nl_o, its_o, last_o = O.ns_process(p, 1e-10, 1e-6, 30, 1000, 40)
