@@ -147,7 +147,7 @@ struct SysDev {
     const int *csr_ia, *csr_ja, *csr_diag;
     const double *AA64, *LU64, *dinv64;
     const float *AA32, *LU32, *dinv32;
-    int *ilu_flag;             // per-row ready flags of the sync-free solves
+    void *ilu_tmp;             // forward-substitution output (T, n_pad)
     const int *ilu_ford, *ilu_bord;      // rows in forward / backward level order
     const int2 *ilu_fpass, *ilu_bpass;   // passes (start, rows) of those orders
     // truncated SPIKE (precond == FG_PRECOND_SPIKE): sp_P row blocks of the

@@ -532,9 +532,8 @@ struct Plan {
     int op = FG_OP_EBE, csr_w = 4, precond = FG_PRECOND_NONE, ilu_g = 4;
     std::vector<int> ech_off;      // ncol+1 offsets into echunks
     int n_dch = 0, n_nch = 0, n_ilu = 0, n_ilub = 0, n_spb = 0, n_spi = 0;
-    size_t flag_bytes = 0;
     DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
-    DevMem ilu_fwd, ilu_bwd, ilu_flags, ilu_ctr;   // sync-free ILU(0) substitutions
+    DevMem ilu_fwd, ilu_bwd, ilu_ctr;              // sync-free ILU(0) substitutions
     DevMem sp_blocks, sp_ifaces;                   // SPIKE (system, block) and (system, interface) items
 };
 
@@ -589,12 +588,8 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     // (forward and backward lists), systems interleaved
     std::vector<int2> fwd, bwd;
     if (cfg.precond == FG_PRECOND_ILU0) {
-        std::vector<size_t> off(P.nsys + 1, 0);
-        for (int s = 0; s < P.nsys; ++s) off[s + 1] = off[s] + (size_t)mem[s].s->topo.n + 1;
-        P.flag_bytes = 4 * off[P.nsys];
         int r0;
-        if ((r0 = P.ilu_flags.alloc(std::max<size_t>(P.flag_bytes, 4))) || (r0 = P.ilu_ctr.alloc(64))) return r0;
-        for (int s = 0; s < P.nsys; ++s) hs[s].ilu_flag = P.ilu_flags.as<int>() + off[s];
+        if ((r0 = P.ilu_ctr.alloc(64))) return r0;
         int maxp = 0;
         for (int s = 0; s < P.nsys; ++s) {
             maxp = std::max({maxp, mem[s].s->ilu_nfpass, mem[s].s->ilu_nbpass});
@@ -720,11 +715,10 @@ static int enqueue_precond(const Plan &P, int sel, cudaStream_t st)
     if (P.precond == FG_PRECOND_ILU0) {
         int *ctr = P.ilu_ctr.as<int>(), *err = ctr + 4;
         const int fp32 = sel == 1 && sizeof(T) == 4;
-        launch_ilu_solve(sys, P.ilu_fwd.as<int2>(), P.n_ilu, P.ilu_flags.as<int>(), P.flag_bytes, ctr, err, sel, 0,
-                         fp32, P.ilu_g, st);
-        launch_ilu_solve(sys, P.ilu_bwd.as<int2>(), P.n_ilub, P.ilu_flags.as<int>(), P.flag_bytes, ctr, err, sel, 1,
-                         fp32, P.ilu_g, st);
-        return 2;
+        launch_ilu_pending(sys, P.dchunks.as<DChunk>(), P.dcount.as<int>(), P.n_dch, sel, fp32, st);
+        launch_ilu_solve(sys, P.ilu_fwd.as<int2>(), P.n_ilu, ctr, err, sel, 0, fp32, P.ilu_g, st);
+        launch_ilu_solve(sys, P.ilu_bwd.as<int2>(), P.n_ilub, ctr, err, sel, 1, fp32, P.ilu_g, st);
+        return 3;
     }
     if (P.precond == FG_PRECOND_SPIKE) {
         const int fp32 = sel == 1 && sizeof(T) == 4;

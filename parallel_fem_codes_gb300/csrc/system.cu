@@ -66,7 +66,7 @@ size_t fg_system::bytes() const
     const DevMem *all[] = {&lm, &A64, &A32, &dinc_ptr, &dinc, &ninc_ptr, &ninc, &node_dof, &eorder, &perm,
                            &lm16, &pt_elem, &pt_dof, &pt_col, &pdofs, &rhs_f, &rhs_b,
                            &csr_ia, &csr_ja, &csr_diag, &csr_inc_ptr, &csr_inc, &AA64, &AA32, &LU64, &LU32,
-                           &dinv64, &dinv32, &ilu_flags, &ilu_ctr, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
+                           &dinv64, &dinv32, &ilu_flags, &ilu_ctr, &ilu_tmp, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
                            &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
                            &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,

@@ -60,7 +60,7 @@ struct fg_system {
     int ilu_g = 32, ilu_nfpass = 0, ilu_nbpass = 0;
     fg::DevMem ilu_ford, ilu_bord, ilu_fpass, ilu_bpass;
     fg::DevMem csr_ia, csr_ja, csr_diag, csr_inc_ptr, csr_inc, AA64, AA32, LU64, LU32, dinv64, dinv32, ilu_flags,
-        ilu_ctr;
+        ilu_ctr, ilu_tmp;   // ilu_tmp: output of the forward substitution (n_pad doubles)
     // truncated SPIKE over row blocks of the CSR operator
     int sp_k = 16, sp_parts = 16, sp_P = 0, sp_maxm = 0;
     bool sp_ready = false;
@@ -81,8 +81,10 @@ int csr_setup(fg_system *s);
 int csr_refresh(fg_system *s, cudaStream_t st);
 int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st);
 int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st);
-int launch_ilu_solve(const SysDev *sys, const int2 *items, int nitems, int *flags, size_t flag_bytes, int *counter,
-                     int *err, int sel, int backward, int fp32, int lanes, cudaStream_t st);
+int launch_ilu_pending(const SysDev *sys, const DChunk *ch, const int *nch, int n_dch, int sel, int fp32,
+                       cudaStream_t st);
+int launch_ilu_solve(const SysDev *sys, const int2 *items, int nitems, int *counter, int *err, int sel, int backward,
+                     int fp32, int lanes, cudaStream_t st);
 
 // Truncated SPIKE (spike.cu)
 constexpr int kSpikeMaxK = 64;                 // largest coupling size
@@ -109,7 +111,7 @@ inline void set_patch_fields(SysDev &D, const fg_system *s)
     D.LU32 = s->LU32.as<float>();
     D.dinv64 = s->dinv64.as<double>();
     D.dinv32 = s->dinv32.as<float>();
-    D.ilu_flag = nullptr;
+    D.ilu_tmp = s->ilu_tmp.p;
     D.ilu_ford = s->ilu_ford.as<int>();
     D.ilu_bord = s->ilu_bord.as<int>();
     D.ilu_fpass = s->ilu_fpass.as<int2>();
