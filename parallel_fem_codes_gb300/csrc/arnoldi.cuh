@@ -62,6 +62,45 @@ __device__ __forceinline__ void part_dots(const SysDev &D, const DChunk &k, int 
     }
 }
 
+// dots of V[0..i] with w and with v = V[i] over a part, in one sweep of the
+// basis: warp-per-j, <V[j], w> to out[j] and <V[j], v> to out[i + 1 + j]
+template <typename T>
+__device__ __forceinline__ void part_dots2(const SysDev &D, const DChunk &k, int i, const T *__restrict__ w,
+                                           double *out)
+{
+    constexpr int N = Pk<T>::N;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const T *V = (const T *)D.V;
+    const T *vi = V + (size_t)i * D.n_pad;
+    for (int j = warp; j <= i; j += kThreads / 32) {
+        const T *vj = V + (size_t)j * D.n_pad;
+        T a0 = 0, a1 = 0, b0 = 0, b1 = 0;
+        int q = k.d0 + lane * N;
+        for (; q + 32 * N < k.d1; q += 2 * 32 * N) {
+            auto v0 = ld_pk(vj + q), v1 = ld_pk(vj + q + 32 * N);
+            auto w0 = ld_pk(w + q), w1 = ld_pk(w + q + 32 * N);
+            auto u0 = ld_pk(vi + q), u1 = ld_pk(vi + q + 32 * N);
+#pragma unroll
+            for (int c = 0; c < N; ++c) {
+                a0 += v0.v[c] * w0.v[c];
+                a1 += v1.v[c] * w1.v[c];
+                b0 += v0.v[c] * u0.v[c];
+                b1 += v1.v[c] * u1.v[c];
+            }
+        }
+        for (; q < k.d1; q += 32 * N) {
+            auto v0 = ld_pk(vj + q), w0 = ld_pk(w + q), u0 = ld_pk(vi + q);
+#pragma unroll
+            for (int c = 0; c < N; ++c) {
+                a0 += v0.v[c] * w0.v[c];
+                b0 += v0.v[c] * u0.v[c];
+            }
+        }
+        double sa = warp_sum((double)(a0 + a1)), sb = warp_sum((double)(b0 + b1));
+        if (lane == 0) { out[j] = sa; out[i + 1 + j] = sb; }
+    }
+}
+
 // w[d] -= sum_{j<=i} h[j] V[j][d] for the dofs of the part (a pack per
 // thread, four basis vectors in flight); returns this thread's sum of the
 // new w^2 when want_norm.  Entries past n stay zero.
@@ -145,6 +184,65 @@ k_dots1(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
         if (last_part(D, 1)) {
             reduce_parts(D, i + 1, tot);
             for (int j = threadIdx.x; j <= i; j += blockDim.x) D.H[j * D.kmax + i] = tot[j];
+        }
+    }
+}
+
+// Mixed-precision pass 1 (classical Gram-Schmidt with a Gram correction):
+// w = M^-1 t (t cleared), s = V^T w and the new column g = V^T v_i of the
+// basis' Gram matrix G = V^T V in one sweep.  The last part forms
+// c = s + (s - G s): the coefficients of the two classical passes of CGS2
+// (h1 = s, h2 = V^T (w - V s) = s - G s) with the second one taken from G
+// instead of a second sweep over the basis; c becomes column i of H and
+// the update that k_orth2 applies.  Used when 2 (kmax) <= kPartStride.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+k_dots1g(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
+{
+    __shared__ double red[kPartStride];
+    __shared__ double tot[kPartStride];
+    const int total = *nch;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const DChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!D.st->in_cycle) continue;
+        T *w = (T *)D.w, *t = (T *)D.t;
+        const T *invd = sizeof(T) == 8 ? (const T *)D.invd64 : (const T *)D.invd32;
+        constexpr int N = Pk<T>::N;
+        typename Pk<T>::type zero;
+#pragma unroll
+        for (int c = 0; c < N; ++c) zero.v[c] = (T)0;
+        for (int q = k.d0 + threadIdx.x * N; q < k.d1; q += blockDim.x * N) {
+            if (!precond_separate(D.precond)) {
+                auto tv = ld_pk(t + q);
+                if (D.precond == FG_PRECOND_DIAG) {
+                    auto iv = ld_pk(invd + q);
+#pragma unroll
+                    for (int c = 0; c < N; ++c) tv.v[c] *= iv.v[c];
+                }
+                st_pk(w + q, tv);
+            }
+            st_pk(t + q, zero);
+        }
+        __syncthreads();
+        part_dots2<T>(D, k, i, w, red);
+        __syncthreads();
+        for (int j = threadIdx.x; j < 2 * (i + 1); j += blockDim.x) D.part[k.part * kPartStride + j] = red[j];
+        if (last_part(D, 1)) {
+            reduce_parts(D, 2 * (i + 1), tot);
+            const int km = D.kmax;
+            for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+                D.G[j * km + i] = tot[i + 1 + j];
+                D.G[i * km + j] = tot[i + 1 + j];
+            }
+            __syncthreads();
+            for (int j = threadIdx.x; j <= i; j += blockDim.x) {
+                double gs = 0.0;
+                for (int l = 0; l <= i; ++l) gs += D.G[j * km + l] * tot[l];
+                const double cj = tot[j] + (tot[j] - gs);
+                D.H[j * km + i] = cj;
+                D.hbuf[j] = cj;
+            }
         }
     }
 }

@@ -171,6 +171,7 @@ struct SysDev {
     void *w, *t;               // T vectors
     double *H;                 // (kmax+1) x kmax, H[j*kmax + i]
     double *g, *cs, *sn, *hbuf, *y;  // kmax+1 each
+    double *G;                 // kmax x kmax Gram matrix of the basis (mixed precision)
     double *part;              // nparts x kPartStride
     unsigned *counter;         // 4 counters (one per reduction kernel kind)
     SysState *st;

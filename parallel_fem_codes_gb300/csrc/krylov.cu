@@ -736,6 +736,9 @@ static int enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
     const DChunk *dc = P.dchunks.as<DChunk>();
     const int *nd = P.dcount.as<int>();
     dim3 gd = grid_for(P.n_dch);
+    // mixed precision: one sweep fewer per step (Gram-corrected CGS); the
+    // FP64 reference method keeps two full classical passes
+    const bool gram = cfg.mixed && 2 * cfg.kmax <= kPartStride;
     int k = enqueue_matvec<T>(P, 0, 0, st);
     k += enqueue_precond<T>(P, 0, st);
     k_start<<<gd, kThreads, 0, st>>>(sys, dc, nd);
@@ -744,11 +747,16 @@ static int enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
     for (int i = 0; i < cfg.kmax - 1; ++i) {
         k += enqueue_matvec<T>(P, 1, i, st);
         k += enqueue_precond<T>(P, 1, st);
-        k_dots1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
-        k_orth1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        if (gram) {
+            k_dots1g<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        } else {
+            k_dots1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+            k_orth1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+            ++k;
+        }
         k_orth2<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
         k_normalize<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
-        k += 4;
+        k += 3;
     }
     k_update<T><<<gd, kThreads, 0, st>>>(sys, dc, nd);
     k_live<<<(P.nsys + 255) / 256, 256, 0, st>>>(sys, P.nsys, P.live.as<int>());
@@ -767,7 +775,7 @@ static int ensure_workspace(fg_system *s, int kmax, int mixed)
     if ((r = w.V.alloc(ts * np * kmax)) || (r = w.w.alloc(ts * np)) || (r = w.t.alloc(ts * np)) ||
         (r = w.x.alloc(8 * np)) || (r = w.b.alloc(8 * np)) || (r = w.ftrue.alloc(8 * np)) ||
         (r = w.r64.alloc(8 * np)) || (r = w.t64.alloc(8 * np)) || (r = w.u64.alloc(8 * np)) ||
-        (r = w.small.alloc(8 * ((size_t)(kmax + 1) * kmax + 5 * (kmax + 1)))) ||
+        (r = w.small.alloc(8 * ((size_t)(kmax + 1) * kmax + 5 * (kmax + 1) + (size_t)kmax * kmax))) ||
         (r = w.part.alloc(8 * (size_t)kMaxParts * kPartStride)) ||
         (r = w.counter.alloc(sizeof(unsigned) * 8)) || (r = w.state.alloc(sizeof(SysState))))
         return r;
@@ -799,6 +807,7 @@ static SysDev make_desc(fg_system *s, const SolveConfig &cfg, bool has_f)
     D.sn = D.cs + (cfg.kmax + 1);
     D.hbuf = D.sn + (cfg.kmax + 1);
     D.y = D.hbuf + (cfg.kmax + 1);
+    D.G = D.y + (cfg.kmax + 1);
     D.part = w.part.as<double>();
     D.counter = w.counter.as<unsigned>();
     D.st = w.state.as<SysState>();
@@ -829,7 +838,8 @@ int validate_member(fg_system *s, const SolveConfig &cfg)
 size_t workspace_bytes(const fg_system *s, int kmax, int mixed)
 {
     size_t np = (size_t)s->n_pad, ts = mixed ? 4 : 8;
-    return ts * np * (kmax + 2) + 8 * np * 6 + 8 * ((size_t)(kmax + 1) * kmax + 5 * (kmax + 1)) +
+    return ts * np * (kmax + 2) + 8 * np * 6 +
+           8 * ((size_t)(kmax + 1) * kmax + 5 * (kmax + 1) + (size_t)kmax * kmax) +
            8 * (size_t)kMaxParts * kPartStride + 256;
 }
 
