@@ -101,9 +101,13 @@ __device__ __forceinline__ void reduce_parts(const SysDev &D, int nv, double *ou
 //  3. the staged rows are added into a shared-memory y local colour by local
 //     colour (elements of one local colour share no dof: no atomics, a fixed
 //     summation order), then each dof is written once: a plain store for
-//     dofs only this patch touches, an update for dofs shared with other
-//     patches (patches sharing a dof have different patch colours and run
-//     in different launches, so the updates do not race).
+//     dofs only this patch touches, a reduction store (red.add) for dofs
+//     shared with other patches (patches sharing a dof have different patch
+//     colours and run in different launches, so the updates apply in launch
+//     order, as read-modify-writes would).
+// For 3x3 blocks each thread loads its entries of the patch's dof list
+// with the element data, so the x gather costs one dependent round trip and
+// the write-back none.
 // The patch sizes (patch_elems) and this kernel shape were chosen by a
 // measured sweep: an L2 prefetch of the next patch, one thread per block
 // row with small patches, and a two-stage bulk-copy pipeline through shared
@@ -111,7 +115,7 @@ __device__ __forceinline__ void reduce_parts(const SysDev &D, int nv, double *ou
 // in_sel: 0 = x (FP64), 1 = V[step] (T), 2 = aux (TX); out_sel: 0 = t64,
 // 1 = t, 2 = aux.
 template <int S, typename TA, typename TX, typename TY>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, S == 3 ? (sizeof(TA) == 4 ? 3 : 2) : (sizeof(TA) == 4 ? 4 : 3))
 k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const int *__restrict__ nch,
          int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out, int maxdof)
 {
@@ -119,6 +123,7 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
     constexpr unsigned short kSink = 0xFFFF;
     constexpr int PE = patch_elems(S);
     constexpr int E = S == 3 ? PE / kThreads : 1;        // S = 3: elements per thread
+    constexpr int DMAX = S == 3 ? 1536 / kThreads : 1;  // S = 3: patch dofs per thread (the patch cap)
     const MvSmem L(S, maxdof, (int)sizeof(TA));
     TA *xs = reinterpret_cast<TA *>(smem_raw + L.xs);
     TA *ys = reinterpret_cast<TA *>(smem_raw + L.ys);
@@ -141,6 +146,14 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
 
         TA av[E][S == 3 ? 9 : 1];
         unsigned short li[E][S == 3 ? 3 : 1];
+        int dv[DMAX];                         // S = 3: this thread's entries of the patch's dof list
+        if constexpr (S == 3) {
+#pragma unroll
+            for (int u = 0; u < DMAX; ++u) {
+                const int j = threadIdx.x + u * kThreads;
+                dv[u] = j < pnd ? __ldg(D.dofs + pd0 + j) : 0;
+            }
+        }
         if constexpr (S == 3) {
 #pragma unroll
             for (int u = 0; u < E; ++u) {
@@ -152,9 +165,20 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
             }
         }
         __syncthreads();                      // the previous patch is done with shared memory
-        for (int j = threadIdx.x; j < pnd; j += kThreads) {
-            xs[j] = (TA)X[D.dofs[pd0 + j] & 0x7fffffff];
-            ys[j] = (TA)0;
+        if constexpr (S == 3) {
+#pragma unroll
+            for (int u = 0; u < DMAX; ++u) {
+                const int j = threadIdx.x + u * kThreads;
+                if (j < pnd) {
+                    xs[j] = (TA)X[dv[u] & 0x7fffffff];
+                    ys[j] = (TA)0;
+                }
+            }
+        } else {
+            for (int j = threadIdx.x; j < pnd; j += kThreads) {
+                xs[j] = (TA)X[D.dofs[pd0 + j] & 0x7fffffff];
+                ys[j] = (TA)0;
+            }
         }
         __syncthreads();
         if constexpr (S == 3) {
@@ -206,12 +230,23 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
             }
             __syncthreads();
         }
-        for (int j = threadIdx.x; j < pnd; j += kThreads) {
-            const int dd = D.dofs[pd0 + j];
+        // a dof shared with other patches takes a reduction store (no round
+        // trip); the patches of one launch share no dof, so each update is
+        // Y[d] + v in launch order, as a read-modify-write would be
+        auto put = [&](int j, int dd) {
             const int d = dd & 0x7fffffff;
-            if (d == D.n) continue;                       // dof-list padding
-            if (dd < 0) Y[d] += (TY)ys[j];
+            if (d == D.n) return;                         // dof-list padding
+            if (dd < 0) atomicAdd(Y + d, (TY)ys[j]);
             else Y[d] = (TY)ys[j];
+        };
+        if constexpr (S == 3) {
+#pragma unroll
+            for (int u = 0; u < DMAX; ++u) {
+                const int j = threadIdx.x + u * kThreads;
+                if (j < pnd) put(j, dv[u]);
+            }
+        } else {
+            for (int j = threadIdx.x; j < pnd; j += kThreads) put(j, D.dofs[pd0 + j]);
         }
     }
 }
