@@ -51,6 +51,12 @@ struct Topology {
     std::vector<int> dofs;       // patch-local dof -> internal dof, bit 31 = shared with another patch
     std::vector<unsigned short> lm16;    // nel*S local indices (internal order), 0xFFFF = sink
     std::vector<int> pc_ptr, pc_list;    // patches grouped by patch colour
+    // per-patch incidence lists: for patch p, at incl[pt_inc[p]] the list
+    // starts (pnd + 1 entries) of each local dof, then the staged product
+    // positions (row * patch_elems(S) + element) that add into it, in
+    // element order; both parts padded to 8 entries (16-byte copies)
+    std::vector<int> pt_inc;
+    std::vector<unsigned short> incl;
 };
 
 // Assembled CSR form of a system (csr_Initialization.c), rows and columns
@@ -86,19 +92,29 @@ __host__ __device__ constexpr int patch_elems(int S)
     return S <= 3 ? FG_MV_PE3 : S <= 6 ? FG_MV_PE6 : S <= 9 ? FG_MV_PE9 : FG_MV_PE12;
 }
 __host__ __device__ constexpr int round4(int v) { return (v + 3) & ~3; }
-// Shared-memory layout of one matvec CTA (bytes): x and y of the patch's
-// dofs (round4(maxdof) each), the staged products [S][PE] and the staged
-// 16-bit local indices [S][PE].
+// Shared-memory layout of one matvec CTA (bytes).  S x S blocks, S > 3: x
+// and y of the patch's dofs (round4(maxdof) each), the staged products
+// [S][PE] and the staged 16-bit local indices [S][PE].  3x3 blocks: x, the
+// staged products and the patch's incidence lists (ic: up to maxdof + 8 +
+// 3 PE 16-bit entries, 16-byte aligned).
 struct MvSmem {
-    size_t xs, ys, ye, ls, total;
+    size_t xs, ys, ye, ls, ic, total;
     __host__ __device__ MvSmem(int S, int maxdof, int w)
     {
         const size_t PE = patch_elems(S), md = round4(maxdof > 0 ? maxdof : 1);
         xs = 0;
-        ys = md * w;
-        ye = 2 * md * w;
-        ls = ye + (size_t)S * PE * w;
-        total = ls + (size_t)S * PE * 2;
+        if (S == 3) {
+            ys = ls = 0;
+            ye = md * w;
+            ic = (ye + (size_t)S * PE * w + 15) / 16 * 16;
+            total = ic + 2 * ((md + 8 + (size_t)S * PE + 7) / 8 * 8);
+        } else {
+            ys = md * w;
+            ye = 2 * md * w;
+            ls = ye + (size_t)S * PE * w;
+            ic = 0;
+            total = ls + (size_t)S * PE * 2;
+        }
     }
 };
 inline size_t mv_smem_bytes(int S, int maxdof, int w) { return MvSmem(S, maxdof, w).total; }
@@ -141,6 +157,8 @@ struct SysDev {
     const unsigned short *lm16;// [S][nel_pad] patch-local indices (0xFFFF = sink)
     const int *pt_elem, *pt_dof, *dofs;
     const unsigned short *pt_col;
+    const int *pt_inc;                 // per-patch incidence lists (3x3 matvec)
+    const unsigned short *incl;
     int maxdof;
     // assembled CSR operator and ILU(0) (op == 1)
     int op, csr_w;

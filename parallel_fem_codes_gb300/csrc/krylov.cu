@@ -251,6 +251,113 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
     }
 }
 
+// 16-byte asynchronous copy global -> shared (cp.async, L2 only) and its wait.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// The 3x3 matvec: per patch, the dof list, element blocks and local
+// indices are loaded into registers (one round trip), x of the patch's dofs
+// is gathered into shared memory while the patch's incidence lists arrive
+// there by asynchronous copies, the element products are staged in shared
+// memory, and then the thread that gathered a dof sums the products that add
+// into it, in the fixed order of its incidence list, and writes it: a plain
+// store for a dof only this patch touches, a reduction store (red.add) for
+// one shared with other patches (those run in other launches, so the updates
+// apply in launch order).  Two barriers per patch; every thread sums whole
+// dofs, so no shared-memory y and no colour passes.
+template <typename TA, typename TX, typename TY>
+__global__ void __launch_bounds__(kThreads, sizeof(TA) == 4 ? 3 : 2)
+k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const int *__restrict__ nch,
+          int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out, int maxdof)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr unsigned short kSink = 0xFFFF;
+    constexpr int PE = patch_elems(3);
+    constexpr int E = PE / kThreads;        // elements per thread
+    constexpr int DMAX = 1536 / kThreads;   // patch dofs per thread (the patch cap)
+    const MvSmem L(3, maxdof, (int)sizeof(TA));
+    TA *xs = reinterpret_cast<TA *>(smem_raw + L.xs);
+    TA *ye = reinterpret_cast<TA *>(smem_raw + L.ye);
+    unsigned short *ic = reinterpret_cast<unsigned short *>(smem_raw + L.ic);
+    const int total = *nch;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const EChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!gated(D, gate)) continue;
+        const TX *X = in_sel == 0 ? (const TX *)D.x
+                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+        TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
+        const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
+        const size_t ld = (size_t)D.nel_pad;
+        const int p = k.e0;
+        const int pe0 = D.pt_elem[p], pne = D.pt_elem[p + 1] - pe0;
+        const int pd0 = D.pt_dof[p], pnd = D.pt_dof[p + 1] - pd0;
+        const int i0 = D.pt_inc[p], ni = D.pt_inc[p + 1] - i0;
+        const int head = (pnd + 1 + 7) & ~7;
+        int dv[DMAX];
+#pragma unroll
+        for (int u = 0; u < DMAX; ++u) {
+            const int j = threadIdx.x + u * kThreads;
+            dv[u] = j < pnd ? __ldg(D.dofs + pd0 + j) : 0;
+        }
+        TA av[E][9];
+        unsigned short li[E][3];
+#pragma unroll
+        for (int u = 0; u < E; ++u) {
+            const int q = min(threadIdx.x + u * kThreads, pne - 1);
+#pragma unroll
+            for (int a = 0; a < 3; ++a) li[u][a] = __ldcs(D.lm16 + a * ld + pe0 + q);
+#pragma unroll
+            for (int m = 0; m < 9; ++m) av[u][m] = ldst(A + m * ld + pe0 + q);
+        }
+        __syncthreads();                      // the previous patch is done with shared memory
+        for (int t = threadIdx.x; t < ni / 8; t += kThreads) cp_async16(ic + 8 * t, D.incl + i0 + 8 * t);
+#pragma unroll
+        for (int u = 0; u < DMAX; ++u) {
+            const int j = threadIdx.x + u * kThreads;
+            if (j < pnd) xs[j] = (TA)X[dv[u] & 0x7fffffff];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < E; ++u) {
+            const int q = threadIdx.x + u * kThreads;
+            if (q >= pne) continue;
+            TA xv[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) xv[a] = li[u][a] == kSink ? (TA)0 : xs[li[u][a]];
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                TA acc = av[u][3 * r] * xv[0];
+                acc += av[u][3 * r + 1] * xv[1];
+                acc += av[u][3 * r + 2] * xv[2];
+                ye[r * PE + q] = acc;
+            }
+        }
+        cp_async_wait_all();
+        __syncthreads();
+#pragma unroll
+        for (int u = 0; u < DMAX; ++u) {
+            const int j = threadIdx.x + u * kThreads;
+            const int dd = dv[u];
+            const int d = dd & 0x7fffffff;
+            if (j >= pnd || d == D.n) continue;           // dof-list padding
+            const int e0 = ic[j], e1 = ic[j + 1];
+            TA v = (TA)0;
+            for (int e = e0; e < e1; ++e) v += ye[ic[head + e]];
+            if (dd < 0) atomicAdd(Y + d, (TY)v);          // shared dof: reduction store
+            else Y[d] = (TY)v;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- CSR SpMV
 // y = A x for the assembled operator (csrmv.c:57-62), W lanes per row
 // (W = 4, 8 or 32 from the mean row length; rows of P1 transport hold ~7
@@ -510,7 +617,7 @@ struct MvLaunch {
                     int in_sel, int out_sel, int step, const TX *ai, TY *ao, int maxdof)
     {
         const size_t smem = mv_smem_bytes(S, maxdof, sizeof(TA));
-        auto kern = k_ebe_mv<S, TA, TX, TY>;
+        auto kern = S == 3 ? k_ebe_mv3<TA, TX, TY> : k_ebe_mv<S, TA, TX, TY>;
         // the attribute and the occupancy are cached per instantiation
         // (last shared-memory size seen); they are host-side queries only
         static std::mutex mu;

@@ -36,7 +36,7 @@ struct fg_system {
     // connectivity and blocks, internal numbering / element order, SoA
     fg::DevMem lm, A64, A32;
     fg::DevMem dinc_ptr, dinc, ninc_ptr, ninc, node_dof, eorder, perm;
-    fg::DevMem lm16, pt_elem, pt_dof, pt_col, pdofs;   // matvec patch layout
+    fg::DevMem lm16, pt_elem, pt_dof, pt_col, pdofs, pt_inc, incl;   // matvec patch layout
     // preconditioners
     fg::DevMem diag, invd64, invd32, bd, ibd64, ibd32;
     int precond = FG_PRECOND_NONE;
@@ -122,6 +122,8 @@ inline void set_patch_fields(SysDev &D, const fg_system *s)
     D.pt_dof = s->pt_dof.as<int>();
     D.pt_col = s->pt_col.as<unsigned short>();
     D.dofs = s->pdofs.as<int>();
+    D.pt_inc = s->pt_inc.as<int>();
+    D.incl = s->incl.as<unsigned short>();
     D.maxdof = std::max(1, s->topo.maxdof);
 }
 

@@ -393,6 +393,35 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
             }
         for (int j = t.pt_dof[p]; j < t.pt_dof[p + 1]; ++j) local[t.dofs[j] & 0x7fffffff] = -1;
     }
+    // incidence lists of the patches (summation of the staged products by dof)
+    {
+        const int PEs = patch_elems(S);
+        t.pt_inc.assign(t.npatch + 1, 0);
+        t.incl.clear();
+        std::vector<int> cnt;
+        for (int p = 0; p < t.npatch; ++p) {
+            const int b = t.pt_elem[p], e = t.pt_elem[p + 1], nd = t.pt_dof[p + 1] - t.pt_dof[p];
+            t.pt_inc[p] = (int)t.incl.size();
+            cnt.assign(nd + 1, 0);
+            for (int q = b; q < e; ++q)
+                for (int a = 0; a < S; ++a) {
+                    const unsigned short l = t.lm16[(size_t)q * S + a];
+                    if (l != 0xFFFF) cnt[l + 1]++;
+                }
+            for (int j = 0; j < nd; ++j) cnt[j + 1] += cnt[j];
+            const size_t base = t.incl.size(), head = ((size_t)nd + 1 + 7) / 8 * 8;
+            const size_t body = ((size_t)cnt[nd] + 7) / 8 * 8;
+            t.incl.resize(base + head + body, 0);
+            for (int j = 0; j <= nd; ++j) t.incl[base + j] = (unsigned short)cnt[j];
+            std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+            for (int q = b; q < e; ++q)
+                for (int a = 0; a < S; ++a) {
+                    const unsigned short l = t.lm16[(size_t)q * S + a];
+                    if (l != 0xFFFF) t.incl[base + head + fill[l]++] = (unsigned short)(a * PEs + (q - b));
+                }
+        }
+        t.pt_inc[t.npatch] = (int)t.incl.size();
+    }
     // patch colouring: patches that share a dof get different colours
     {
         std::vector<uint32_t> used(n + 1, 0u);
