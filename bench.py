@@ -43,11 +43,13 @@ WORKLOAD = ("served steady SUPG/CAU transport: 256 requests, NxN nodes N~U[33,51
             "refinement to true rel. residual 1e-10, continuous batching")
 KMAX, TOL = 30, 1e-10
 # DRAM bytes / algorithmic bytes of one batched FP32 matvec, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum of the k_ebe_mv launches of
-# `bench.py --matvec-only --count 32 --steps 1`, cold): 414.1 MB for
-# 418.2 MB.  The traffic scales with the instances (each patch reads its own
-# blocks once).
-MATVEC_TRAFFIC_RATIO = 414.1 / 418.19
+# (dram__bytes_read.sum + dram__bytes_write.sum of the two k_ebe_mv3
+# launches of one matvec of `bench.py --matvec-only --count 32 --steps 1`,
+# cold): 475.7 MB for 418.2 MB algorithmic; the difference is the patches'
+# incidence lists (16-bit index data, ~7 B per element), which the
+# algorithmic count leaves out.  The traffic scales with the instances (each
+# patch reads its own blocks once).
+MATVEC_TRAFFIC_RATIO = 475.7 / 418.19
 
 
 # ------------------------------------------------------------------ CPU legs
@@ -520,7 +522,7 @@ def main():
                       "iterations_mean": float(np.mean(iters)),
                       "rel_err_vs_fp64_max": max(plain_err) if plain_err else None},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e,
-            "roofline": {"bound": "hbm", "kernel": "k_ebe_mv<3,float> (all colours, batched)",
+            "roofline": {"bound": "hbm", "kernel": "k_ebe_mv3<float> (all patch colours, batched)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind, "traffic": MATVEC_TRAFFIC_RATIO * bytes_mv,
                          "traffic_source": "ncu dram__bytes_read+write per matvec of a 32-instance capture "
