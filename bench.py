@@ -296,6 +296,66 @@ def ns_leg(fg, G, n=1025, reynolds=1000.0, kmax=50, cycles=20):
     return out
 
 
+def c5_leg(fg, G, count=96, rates=(10, 30, 100, 300, 1000, 2000), seed=5):
+    """Mixed serving: Poisson arrivals at each rate of `count` requests, 70%
+    steady SUPG/CAU transport and 30% 10-step Euler OBLIQUO loops
+    (Predictor_Old, 2 corrections per step), elements log-uniform in
+    [1e3, 2e6] (angle, conductivity as the batched transport workload), all
+    mixed precision to 1e-10; transport requests are batched continuously,
+    Euler loops run beside them.  Reports per rate the throughput (requests
+    / makespan) and p50/p99 latency (done - submit) per kind."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    kinds = rng.random(count) < 0.3
+    elems = np.exp(rng.uniform(np.log(1e3), np.log(2e6), size=count))
+    sides = np.maximum(9, (1 + np.sqrt(elems / 2)).astype(int))
+    angles = rng.uniform(0.0, 360.0, size=count)
+    kappa = np.exp(rng.uniform(np.log(1e-8), np.log(1e-2), size=count))
+    reqs = []
+    t0 = time.perf_counter()
+    for i in range(count):
+        if kinds[i]:
+            pr = G.obliquo_problem(int(sides[i]))
+            to = fg.time_opts(0, 2, 1e-3, 0, 10 * pr.dt, 1e-6, max_steps=10)
+            reqs.append(("euler", fg.euler_system(pr), pr, to))
+        else:
+            pr = G.transport_problem(int(sides[i]), angle_deg=float(angles[i]), k=float(kappa[i]))
+            reqs.append(("transport", fg.transport_system(pr), pr, None))
+    setup_s = time.perf_counter() - t0
+
+    def one(rate):
+        sv = fg.Server(kmax=KMAX, lmax=10000, tol=TOL, precision=fg.FG_PREC_MIXED)
+        gaps = rng.exponential(1.0 / rate, size=count) if rate else np.zeros(count)
+        arrive = np.cumsum(gaps) - gaps[0]
+        t_start = sv.now()
+        for i, (kind, sy, pr, to) in enumerate(reqs):
+            delay = arrive[i] - (sv.now() - t_start)
+            if delay > 0:
+                time.sleep(delay)
+            if kind == "euler":
+                sv.submit_euler(sy, pr, to, i)
+            else:
+                sv.submit(sy, pr, i)
+        sv.wait(count, timeout=900)
+        res = sv.poll(count + 16)
+        sv.close()
+        t_end = max(r["t_done"] for r in res)
+        out = {"rate_req_per_s": rate, "requests_per_s": count / (t_end - t_start),
+               "converged_all": all(r["true_rel_residual"] <= TOL for r in res)}
+        for kind in ("transport", "euler"):
+            lat = [r["t_done"] - r["t_submit"] for r in res if reqs[r["tag"]][0] == kind]
+            if lat:
+                out[kind] = {"n": len(lat), "p50_ms": 1e3 * pct(lat, 50), "p99_ms": 1e3 * pct(lat, 99)}
+        return out
+
+    one(0)                                                                   # warm-up, all at once
+    out = {"workload": f"{count} requests: 70% steady transport, 30% 10-step Euler OBLIQUO (2 corrections/step), "
+                       f"elements logU[1e3, 2e6] (seed {seed}), mixed precision to 1e-10; Poisson arrivals",
+           "transport_requests": int((~kinds).sum()), "euler_requests": int(kinds.sum()),
+           "elements_total": int(sum(2 * (int(n) - 1) ** 2 for n in sides)), "setup_s": setup_s,
+           "rates": [one(r) for r in rates]}
+    return out
+
+
 def _matvec_roofline(fg, s):
     peak, kind = peaks()
     r = {}
@@ -336,6 +396,7 @@ def main():
     ap.add_argument("--no-legs", action="store_true", help="skip the Euler and Navier-Stokes legs")
     ap.add_argument("--euler-n", type=int, default=513, help="nodes per side of the Euler leg")
     ap.add_argument("--ns-n", type=int, default=1025, help="nodes per side of the Navier-Stokes leg (odd)")
+    ap.add_argument("--c5-count", type=int, default=96, help="requests per rate of the mixed serving leg")
     ap.add_argument("--matvec-only", action="store_true",
                     help="only the batched FP32 EBE matvec of --count instances (2 warm-up + --steps "
                          "matvecs); the small case the ncu traffic capture runs")
@@ -492,7 +553,8 @@ def main():
 
     legs = None
     if not args.no_legs and rank == 0:
-        legs = {"euler_obliquo": euler_leg(fg, G, n=args.euler_n), "ns_cavity": ns_leg(fg, G, n=args.ns_n)}
+        legs = {"euler_obliquo": euler_leg(fg, G, n=args.euler_n), "ns_cavity": ns_leg(fg, G, n=args.ns_n),
+                "served_mixed_c5": c5_leg(fg, G, count=args.c5_count)}
 
     cpu = None
     if pool is not None:

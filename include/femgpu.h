@@ -364,6 +364,15 @@ int fg_server_create(fg_server **out, const fg_server_opts *opts);
 /* Queue a request; thread-safe.  The system must not be in use elsewhere
  * until its result has been polled. */
 int fg_server_submit(fg_server *sv, fg_system *s, const fg_transport_coeffs *c, unsigned long long tag);
+/* Queue an Euler time loop (fg_euler_predictor with the server's kmax,
+ * lmax, tol, precision and inner_tol); thread-safe.  u (host, n) is the
+ * initial state and receives the final state; it and the system stay the
+ * caller's but must not be touched until the result has been polled.  In
+ * the result, stats.iterations counts the GMRES iterations of the loop,
+ * stats.cycles its corrections.  Euler loops run one at a time, beside the
+ * transport batch, on the system's own stream. */
+int fg_server_submit_euler(fg_server *sv, fg_system *s, const fg_euler_coeffs *c, const fg_time_opts *t,
+                           double *u, unsigned long long tag);
 /* Move up to max finished results into out; *count receives how many. */
 int fg_server_poll(fg_server *sv, fg_server_result *out, int max, int *count);
 /* Block until at least n results are waiting to be polled, or timeout_s. */

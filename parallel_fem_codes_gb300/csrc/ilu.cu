@@ -488,7 +488,7 @@ int csr_setup(fg_system *s)
     auto up = [](DevMem &m, const std::vector<int> &v) -> int {
         int rr = m.alloc(sizeof(int) * std::max<size_t>(v.size(), 1));
         if (rr) return rr;
-        if (!v.empty()) FG_CUDA(cudaMemcpy(m.p, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice));
+        if (!v.empty()) return h2d(m.p, v.data(), sizeof(int) * v.size());
         return FG_OK;
     };
     size_t nz = (size_t)std::max(c.nnz, 1), n1 = (size_t)c.n + 1;
@@ -511,7 +511,7 @@ int csr_setup(fg_system *s)
         auto up2 = [](DevMem &m, const std::vector<int2> &v) -> int {
             int rr = m.alloc(sizeof(int2) * std::max<size_t>(v.size(), 1));
             if (rr) return rr;
-            if (!v.empty()) FG_CUDA(cudaMemcpy(m.p, v.data(), sizeof(int2) * v.size(), cudaMemcpyHostToDevice));
+            if (!v.empty()) return h2d(m.p, v.data(), sizeof(int2) * v.size());
             return FG_OK;
         };
         if ((r = up(s->ilu_ford, fo)) || (r = up(s->ilu_bord, bo)) || (r = up2(s->ilu_fpass, fp)) ||

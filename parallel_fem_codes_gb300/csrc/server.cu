@@ -1,12 +1,20 @@
-// Request server: continuous batching of steady transport solves.
+// Request server: continuous batching of steady transport solves, and
+// Euler time loops beside them.
 //
-// One worker thread owns a BatchRun.  Between restart cycles it admits
+// Transport: one worker thread owns a BatchRun.  Between restart cycles it admits
 // waiting requests (FIFO) while their Krylov workspace fits the HBM budget,
 // assembles each admitted system on the device, and runs one cycle for all
 // admitted solves; converged solves leave the batch immediately and their
 // results are published with submit / admit / done times.  Because every
 // system's reductions use only its own parts, a result does not depend on
 // which other requests shared its cycles.
+//
+// Euler: a second worker thread takes Euler requests (a system with Euler
+// geometry, coefficients, time-stepping controls and a host state) in FIFO
+// order and runs each request's Predictor_Old loop (fg_euler_predictor: the
+// loop's assembly, preconditioner set-up and solves stay on the device, on
+// the system's own stream), so Euler loops overlap with the transport
+// batch on the GPU.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -29,6 +37,15 @@ struct Request {
     size_t bytes;
 };
 
+struct EulerRequest {
+    fg_system *s;
+    fg_euler_coeffs c;
+    fg_time_opts t;
+    double *u;
+    unsigned long long tag;
+    double t_submit;
+};
+
 }  // namespace fg
 
 using namespace fg;
@@ -42,6 +59,8 @@ struct fg_server {
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
     std::deque<Request> queue;
+    std::deque<EulerRequest> queue_eu;
+    std::condition_variable cv_work_eu;
     std::vector<fg_server_result> done;
     std::vector<Request> active;   // parallel to the batch members
     std::set<fg_system *> busy;
@@ -49,10 +68,11 @@ struct fg_server {
     bool stop = false;
     int error = FG_OK;
     std::string error_text;
-    std::thread worker;
+    std::thread worker, worker_eu;
 
     double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
     void run();
+    void run_euler();
     void fail(int code)
     {
         std::lock_guard<std::mutex> l(mu);
@@ -133,6 +153,43 @@ void fg_server::run()
     }
 }
 
+void fg_server::run_euler()
+{
+    cudaSetDevice(device);
+    fg_solver_opts so{cfg.kmax, cfg.lmax, cfg.tol, cfg.mixed ? FG_PREC_MIXED : FG_PREC_FP64, o.inner_tol};
+    for (;;) {
+        EulerRequest r;
+        {
+            std::unique_lock<std::mutex> l(mu);
+            cv_work_eu.wait(l, [&] { return stop || !queue_eu.empty(); });
+            if (stop) { queue_eu.clear(); return; }
+            r = queue_eu.front();
+            queue_eu.pop_front();
+        }
+        const double t_admit = now();
+        fg_time_stats ts{};
+        int rc = fg_euler_predictor(r.s, &r.c, &so, &r.t, r.u, nullptr, &ts);
+        if (rc != FG_OK) { fail(rc); return; }
+        const double t = now();
+        std::lock_guard<std::mutex> l(mu);
+        fg_server_result res{};
+        res.tag = r.tag;
+        res.stats.iterations = ts.gmres_iterations;
+        res.stats.cycles = ts.corrections;
+        res.stats.converged = ts.true_rel_residual <= cfg.tol ? 1 : 0;
+        res.stats.status = FG_OK;
+        res.stats.eps = cfg.tol;
+        res.stats.true_rel_residual = ts.true_rel_residual;
+        res.stats.seconds = t - t_admit;
+        res.t_submit = r.t_submit;
+        res.t_admit = t_admit;
+        res.t_done = t;
+        done.push_back(res);
+        busy.erase(r.s);
+        cv_done.notify_all();
+    }
+}
+
 extern "C" {
 
 int fg_server_create(fg_server **out, const fg_server_opts *opts)
@@ -165,6 +222,7 @@ int fg_server_create(fg_server **out, const fg_server_opts *opts)
     }
     sv->t0 = std::chrono::steady_clock::now();
     sv->worker = std::thread([sv] { sv->run(); });
+    sv->worker_eu = std::thread([sv] { sv->run_euler(); });
     *out = sv;
     return FG_OK;
 }
@@ -183,6 +241,28 @@ int fg_server_submit(fg_server *sv, fg_system *s, const fg_transport_coeffs *c, 
         sv->queue.push_back(r);
     }
     sv->cv_work.notify_one();
+    return FG_OK;
+}
+
+int fg_server_submit_euler(fg_server *sv, fg_system *s, const fg_euler_coeffs *c, const fg_time_opts *t,
+                           double *u, unsigned long long tag)
+{
+    if (!sv || !s || !c || !t || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (!s->eu_geometry_ok || s->topo.ndof != 4) {
+        set_error("fg_server_submit_euler: the system has no Euler geometry (fg_euler_set_geometry)");
+        return FG_ERR_STATE;
+    }
+    if (s->device != sv->device) { set_error("fg_server_submit_euler: system on another device"); return FG_ERR_ARG; }
+    EulerRequest r{s, *c, *t, u, tag, sv->now()};
+    {
+        std::lock_guard<std::mutex> l(sv->mu);
+        if (sv->error) { set_error(sv->error_text); return sv->error; }
+        if (sv->stop) { set_error("server is stopping"); return FG_ERR_STATE; }
+        if (sv->busy.count(s)) { set_error("fg_server_submit_euler: the system is in use by another request"); return FG_ERR_STATE; }
+        sv->busy.insert(s);
+        sv->queue_eu.push_back(r);
+    }
+    sv->cv_work_eu.notify_one();
     return FG_OK;
 }
 
@@ -218,7 +298,9 @@ int fg_server_destroy(fg_server *sv)
         sv->stop = true;
     }
     sv->cv_work.notify_all();
+    sv->cv_work_eu.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
+    if (sv->worker_eu.joinable()) sv->worker_eu.join();
     cudaStreamSynchronize(sv->st);
     cudaStreamDestroy(sv->st);
     delete sv;

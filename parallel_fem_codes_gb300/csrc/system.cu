@@ -20,6 +20,10 @@ int cuda_fail(cudaError_t e, const char *what)
     return FG_ERR_CUDA;
 }
 
+// The zero fill runs on the legacy default stream, which the library's
+// non-blocking streams are not ordered after, and cudaMemset returns before
+// it is done: wait for it, or a copy queued next on another stream could
+// land first and be zeroed.
 int DevMem::alloc(size_t b)
 {
     if (p) { cudaFree(p); p = nullptr; bytes = 0; }
@@ -28,7 +32,19 @@ int DevMem::alloc(size_t b)
     if (e != cudaSuccess) { p = nullptr; return cuda_fail(e, "cudaMalloc"); }
     bytes = b;
     e = cudaMemset(p, 0, b);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
+    return FG_OK;
+}
+
+// Host -> device copy that has landed when it returns (cudaMemcpy from
+// pageable memory may return before its DMA completes, on the legacy
+// stream).
+int h2d(void *dst, const void *src, size_t bytes)
+{
+    cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy");
     return FG_OK;
 }
 
@@ -40,7 +56,7 @@ static int upload(DevMem &m, const std::vector<T> &v)
 {
     int r = m.alloc(sizeof(T) * std::max<size_t>(v.size(), 1));
     if (r) return r;
-    if (!v.empty()) FG_CUDA(cudaMemcpy(m.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice));
+    if (!v.empty()) return h2d(m.p, v.data(), sizeof(T) * v.size());
     return FG_OK;
 }
 

@@ -16,7 +16,7 @@ struct DevMem {
     DevMem(const DevMem &) = delete;
     DevMem &operator=(const DevMem &) = delete;
     ~DevMem() { if (p) cudaFree(p); }
-    int alloc(size_t b);     // zero-filled
+    int alloc(size_t b);     // zero-filled (the fill has completed on return)
     template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
@@ -75,6 +75,9 @@ struct fg_system {
 };
 
 namespace fg {
+
+// Host -> device copy, complete on return.
+int h2d(void *dst, const void *src, size_t bytes);
 
 // CSR / ILU(0) (ilu.cu)
 int csr_setup(fg_system *s);

@@ -157,6 +157,8 @@ def lib(build_if_missing: bool = True):
                                      ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
     L.fg_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerOpts)]
     L.fg_server_submit.argtypes = [_vp, _vp, ctypes.POINTER(TransportCoeffs), ctypes.c_ulonglong]
+    L.fg_server_submit_euler.argtypes = [_vp, _vp, ctypes.POINTER(EulerCoeffs), ctypes.POINTER(TimeOpts), _f64p,
+                                         ctypes.c_ulonglong]
     L.fg_server_poll.argtypes = [_vp, _vp, _c_int, ctypes.POINTER(_c_int)]
     L.fg_server_wait.argtypes = [_vp, _c_int, _c_dbl]
     L.fg_server_now.argtypes = [_vp]
@@ -482,7 +484,8 @@ def bench_matvec(systems, precision=32, reps=20):
 
 class Server:
     """Continuous-batching request server (fg_server_*): submit transport
-    requests at any time, poll finished results with their timestamps."""
+    requests and Euler time loops at any time, poll finished results with
+    their timestamps (Euler results carry the final state as "u")."""
 
     def __init__(self, kmax=30, lmax=10000, tol=1e-10, precision=FG_PREC_MIXED, inner_tol=0.0,
                  hbm_budget_bytes=0, max_active=0):
@@ -497,6 +500,13 @@ class Server:
         self._keep[tag] = system
         check(lib().fg_server_submit(self._h, system.handle, ctypes.byref(c), tag))
 
+    def submit_euler(self, system, prob, topts, tag, u0=None):
+        c = euler_coeffs(prob)
+        u = prob.initial_state() if u0 is None else np.array(u0, dtype=np.float64, copy=True)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        self._keep[tag] = (system, u, topts)
+        check(lib().fg_server_submit_euler(self._h, system.handle, ctypes.byref(c), ctypes.byref(topts), u, tag))
+
     def now(self) -> float:
         return float(lib().fg_server_now(self._h))
 
@@ -509,7 +519,9 @@ class Server:
         check(lib().fg_server_poll(self._h, ctypes.cast(buf, _vp), max_results, ctypes.byref(cnt)))
         out = [buf[i].as_dict() for i in range(cnt.value)]
         for r in out:
-            self._keep.pop(r["tag"], None)
+            kept = self._keep.pop(r["tag"], None)
+            if isinstance(kept, tuple):
+                r["u"] = kept[1]
         return out
 
     def close(self):

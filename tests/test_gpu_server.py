@@ -65,3 +65,52 @@ def test_server_admission_respects_budget(fg):
     assert len(res) == 4
     for a, b in zip(res, res[1:]):
         assert b["t_admit"] >= a["t_done"]      # one at a time
+
+
+def test_served_mixed_transport_and_euler(fg):
+    """Euler time loops served beside transport solves: each Euler result
+    equals the same loop run alone through fg_euler_predictor (the loop is
+    deterministic), transport results are unchanged, and Euler loops overlap
+    with the transport batch in time."""
+    tprobs = [G.transport_problem(n, angle_deg=a, k=1e-5) for n, a in [(129, 30.0), (65, 200.0), (97, 300.0)]]
+    eprobs = [G.obliquo_problem(n) for n in (33, 17)]
+    topts = [fg.time_opts(0, 2, 1e-3, 0, 4 * p.dt, 1e-6, max_steps=4) for p in eprobs]
+    solo_u = []
+    for p, to in zip(eprobs, topts):
+        s = fg.euler_system(p)
+        u, a, st = s.euler_predictor(p, to, kmax=30, lmax=10000, tol=1e-10, precision=fg.FG_PREC_MIXED)
+        solo_u.append((u, st))
+    solo_t = []
+    for p in tprobs:
+        s = fg.transport_system(p)
+        s.transport_prepare(p)
+        solo_t.append(fg.solve_resident([s], precision=fg.FG_PREC_MIXED)[0])
+    tsys = [fg.transport_system(p) for p in tprobs]
+    esys = [fg.euler_system(p) for p in eprobs]
+    sv = fg.Server(precision=fg.FG_PREC_MIXED)
+    sv.submit_euler(esys[0], eprobs[0], topts[0], 100)
+    for i, (s, p) in enumerate(zip(tsys, tprobs)):
+        sv.submit(s, p, i)
+    sv.submit_euler(esys[1], eprobs[1], topts[1], 101)
+    sv.wait(5, timeout=120)
+    res = {r["tag"]: r for r in sv.poll()}
+    sv.close()
+    assert sorted(res) == [0, 1, 2, 100, 101]
+    for k, (u0, st0) in zip((100, 101), solo_u):
+        assert np.array_equal(res[k]["u"], u0)
+        assert res[k]["iterations"] == st0["gmres_iterations"]
+        assert res[k]["cycles"] == st0["corrections"]
+        assert res[k]["true_rel_residual"] <= 1e-10
+    for i in range(3):
+        assert res[i]["iterations"] == solo_t[i]["iterations"]
+    e0 = res[100]
+    assert any(res[i]["t_admit"] < e0["t_done"] and e0["t_admit"] < res[i]["t_done"] for i in range(3))
+
+
+def test_server_euler_rejects_transport_system(fg):
+    p = G.transport_problem(9)
+    s = fg.transport_system(p)
+    sv = fg.Server()
+    with pytest.raises(fg.FemGpuError):
+        sv.submit_euler(s, G.obliquo_problem(9), fg.time_opts(0, 1, 1e-3, 0, 1.0, 1e-6, max_steps=1), 7)
+    sv.close()
