@@ -51,8 +51,10 @@ enum { FG_REORDER_NONE = 0, FG_REORDER_RCM = 1 };
  *   ien[nel*3]         element vertices (Element[e].Vertex)
  *   type[nnodes*ndof]  0 = Dirichlet dof, otherwise free (Node.Type)
  *   invp[nnodes*ndof]  equation of each free dof, 0..neq-1 (Node.invP_id)
- * Builds lm (Fill_LM.c), the local RCM numbering (Permutation_of_LM.c, when
- * reorder == FG_REORDER_RCM and ndof == 1), a greedy element colouring and
+ * Builds lm (Fill_LM.c), the local RCM numbering of the dof graph
+ * (Permutation_of_LM.c, when reorder == FG_REORDER_RCM; the reference's
+ * drivers use it for ndof == 1 and node order otherwise), a greedy element
+ * colouring and
  * the dof/node incidence lists, and uploads the connectivity.
  * Replaces Preprocess.c:288-340 (lm, Perm, invPerm, A allocation). */
 int fg_system_create(fg_system **out, int nnodes, int nel, int ndof,
