@@ -3,7 +3,17 @@
  * entry points, with the reference's names and signatures, running on the
  * GPU through libfemgpu.  Linking this library instead of
  * pgmres.c, ebemv.c, Diag_precond.c, EBE/Diag_precond_EBE_setup.c,
- * NO_precond.c and NO_precond_setup.c leaves every driver file unchanged.
+ * NO_precond.c and NO_precond_setup.c (EBE storage) or csr_assembly.c,
+ * csrmv.c, CSR/ILUp_precond*.c and CSR/SPIKE_precond*.c (MatrixVector-
+ * ProductScheme "CSR" with "ILU0" or "SPIKEk") leaves every driver file
+ * unchanged.
+ *
+ * CSR storage: the shim's csr_assembly keeps each element's 3x3 block (the
+ * library assembles its CSR values from the blocks, in csr_assembly.c's
+ * element order), so MatrixData->AA is not filled; every consumer of AA on
+ * the solve path (csrmv, the ILU and SPIKE set-ups and applies, pgmres) is
+ * in this shim.  SPIKE's row-block count (the reference's rank count) is
+ * FEMGPU_SPIKE_BLOCKS (default 16).
  *
  * One rank only (NPROC = 1): neq_bef = 0, NEQ = neq, vectors of NEQ + 1.
  * The GPU system of a MatrixDataType is created on first use from the
@@ -28,7 +38,16 @@ static struct {
     const MatrixDataType *key;
     fg_system *sys;
     int nel, neq;
+    double *blocks;     /* CSR storage: element blocks captured by csr_assembly */
+    int csr;            /* the system runs on the CSR operator */
 } g_tab[FGC_MAX_SYSTEMS];
+
+static int fgc_slot(const MatrixDataType *M)
+{
+    for (int i = 0; i < FGC_MAX_SYSTEMS; i++)
+        if (g_tab[i].key == M) return i;
+    return -1;
+}
 
 static int fgc_fail(int rc, const char *where)
 {
@@ -72,6 +91,12 @@ static fg_system *fgc_system(ParametersType *P, MatrixDataType *M, FemStructsTyp
     g_tab[free_slot].sys = sys;
     g_tab[free_slot].nel = ne;
     g_tab[free_slot].neq = P->neq;
+    g_tab[free_slot].blocks = NULL;
+    g_tab[free_slot].csr = 0;
+    if (strcasecmp(P->MatrixVectorProductScheme, "CSR") == 0) {
+        g_tab[free_slot].blocks = calloc((size_t)ne * 9, sizeof(double));
+        if (!g_tab[free_slot].blocks) { fgc_fail(FG_ERR_NOMEM, "CSR block buffer"); return NULL; }
+    }
     return sys;
 }
 
@@ -79,7 +104,13 @@ static fg_system *fgc_system(ParametersType *P, MatrixDataType *M, FemStructsTyp
  * (Preprocess.c:331-340 allocates A as row pointers into Aaux). */
 static int fgc_upload_blocks(fg_system *sys, MatrixDataType *M)
 {
-    int rc = fg_set_blocks(sys, M->Aaux);
+    int i = fgc_slot(M);
+    const double *blk = i >= 0 && g_tab[i].blocks ? g_tab[i].blocks : M->Aaux;
+    int rc = fg_set_blocks(sys, blk);
+    if (!rc && i >= 0 && g_tab[i].blocks && !g_tab[i].csr) {
+        rc = fg_set_operator(sys, FG_OP_CSR);
+        if (!rc) g_tab[i].csr = 1;
+    }
     return rc ? fgc_fail(rc, "element blocks") : 0;
 }
 
@@ -139,19 +170,98 @@ int ebemv(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *Pv, d
     return rc ? fgc_fail(rc, "ebemv") : 0;
 }
 
+/* csr_assembly (csr_assembly.c:3-54): the element's block is kept; the
+ * library sums the blocks into its CSR values in element order when a
+ * CSR consumer below runs. */
+void csr_assembly(ParametersType *P, MatrixDataType *M, FemStructsType *S, int E, double ke[3][3])
+{
+    if (!fgc_system(P, M, S)) return;
+    int i = fgc_slot(M);
+    if (i < 0 || !g_tab[i].blocks || E < 0 || E >= g_tab[i].nel) return;
+    double *b = g_tab[i].blocks + (size_t)E * 9;
+    for (int a = 0; a < 3; a++)
+        for (int c = 0; c < 3; c++) b[3 * a + c] = ke[a][c];
+}
+
+/* csrmv (MatrixVector_Operations/CSR/csrmv.c:4-65): Q = A P, Q[NEQ] = 0. */
+int csrmv(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *Pv, double *Qv)
+{
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    if (fgc_upload_blocks(sys, M)) return 1;
+    Pv[P->NEQ] = 0.0;
+    int rc = fg_matvec(sys, Pv, Qv, 64);
+    return rc ? fgc_fail(rc, "csrmv") : 0;
+}
+
+/* ILUp_precond_setup (CSR/ILUp_precond_setup.c:8-168) for "ILU0": ILU(0)
+ * of the CSR operator, F preconditioned in place.  ILU(p > 0) is not on the
+ * GPU and is refused. */
+int ILUp_precond_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
+{
+    (void)tag;
+    if (atoi(&P->Preconditioner[3]) != 0) {
+        fprintf(stderr, "femgpu: only ILU(0) runs on the GPU (Preconditioner \"%s\")\n", P->Preconditioner);
+        if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
+        return 1;
+    }
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    if (fgc_upload_blocks(sys, M)) return 1;
+    int rc = fg_precond_setup(sys, FG_PRECOND_ILU0, 0, F);
+    return rc ? fgc_fail(rc, "ILUp_precond_setup") : 0;
+}
+
+/* ILUp_precond (CSR/ILUp_precond.c:4-47): z = (LU)^-1 p (p may be z). */
+int ILUp_precond(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    return Diag_precond(P, M, S, p, z);
+}
+
+/* SPIKE_precond_setup (CSR/SPIKE_precond_setup.c:10-312): k from the
+ * "SPIKEk" string as the reference reads it (:54), the row blocks from
+ * FEMGPU_SPIKE_BLOCKS; F preconditioned in place.  k_SPIKE_block_size
+ * receives k, as in the reference. */
+int SPIKE_precond_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
+{
+    (void)tag;
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    int k = atoi(&P->Preconditioner[5]);
+    const char *e = getenv("FEMGPU_SPIKE_BLOCKS");
+    int parts = e ? atoi(e) : 16;
+    int rc = fg_set_spike(sys, k, parts);
+    if (rc) return fgc_fail(rc, "SPIKE_precond_setup");
+    if (fgc_upload_blocks(sys, M)) return 1;
+    rc = fg_precond_setup(sys, FG_PRECOND_SPIKE, 0, F);
+    if (rc) return fgc_fail(rc, "SPIKE_precond_setup");
+    P->k_SPIKE_block_size = k;
+    return 0;
+}
+
+/* SPIKE_precond (CSR/SPIKE_precond.c:8-158): z = M^-1 p (p may be z). */
+int SPIKE_precond(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    return Diag_precond(P, M, S, p, z);
+}
+
 /* pgmres (Solvers_and_Preconditioners/pgmres.c:5-200): the whole restarted
- * GMRES on the GPU when mv is this shim's ebemv and the preconditioner pair
- * is this shim's Diag_precond or NO_precond (the configurations the
- * steady-transport driver installs with EBE storage); the blocks and the
+ * GMRES on the GPU when mv is this shim's ebemv with its Diag_precond or
+ * NO_precond, or its csrmv with its ILUp_precond, SPIKE_precond or
+ * NO_precond (the configurations the steady-transport driver installs,
+ * setPreconditioner.c:6-65); the blocks and the
  * preconditioner were set up by the *_setup call that precedes every solve
  * (Process.c:59-76).  Parameters->iterations grows by the Arnoldi steps. */
 int pgmres(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctionsType *Fn, double *B, double *X)
 {
     fg_system *sys = fgc_system(P, M, S);
     if (!sys) return 1;
-    if (Fn->mv != ebemv || Fn->precondR != NO_precond ||
-        (Fn->precond != Diag_precond && Fn->precond != NO_precond)) {
-        fprintf(stderr, "femgpu: pgmres supports mv = ebemv with Diag or no preconditioning on the GPU\n");
+    const int ebe_ok = Fn->mv == ebemv && (Fn->precond == Diag_precond || Fn->precond == NO_precond);
+    const int csr_ok = Fn->mv == csrmv && (Fn->precond == ILUp_precond || Fn->precond == SPIKE_precond ||
+                                           Fn->precond == NO_precond);
+    if (Fn->precondR != NO_precond || !(ebe_ok || csr_ok)) {
+        fprintf(stderr, "femgpu: pgmres supports mv = ebemv with Diag or no preconditioning, or mv = csrmv with "
+                        "ILU(0), SPIKE or no preconditioning, on the GPU\n");
         if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
         return 1;
     }

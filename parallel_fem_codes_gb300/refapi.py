@@ -92,9 +92,11 @@ def shim():
         L = ctypes.CDLL(_build.COMPAT_SST)
         for name in ("pgmres",):
             getattr(L, name).argtypes = [ctypes.c_void_p] * 6
-        for name in ("ebemv", "Diag_precond", "NO_precond"):
+        for name in ("ebemv", "Diag_precond", "NO_precond", "csrmv", "ILUp_precond", "SPIKE_precond"):
             getattr(L, name).argtypes = [ctypes.c_void_p] * 5
-        for name in ("Diag_precond_EBE_setup", "NO_precond_setup"):
+        L.csr_assembly.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_int, ctypes.c_void_p]
+        L.csr_assembly.restype = None
+        for name in ("Diag_precond_EBE_setup", "NO_precond_setup", "ILUp_precond_setup", "SPIKE_precond_setup"):
             getattr(L, name).argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, c_int, ctypes.c_void_p]
         L.fgc_sst_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
         L.fgc_sst_layout.restype = None
@@ -107,15 +109,16 @@ def _addr(lib, name):
 
 
 class DriverState:
-    """The structs Preprocess.c fills for one rank (EBE storage, Diag
-    preconditioning, GMRES), holding numpy arrays the driver owns."""
+    """The structs Preprocess.c fills for one rank (EBE or CSR storage;
+    Diag, ILU0, SPIKEk or no preconditioning; GMRES), holding numpy arrays
+    the driver owns."""
 
-    def __init__(self, mesh, kmax=30, lmax=1000, tol=1e-10, precond="Diag"):
+    def __init__(self, mesh, kmax=30, lmax=1000, tol=1e-10, precond="Diag", scheme="EBE"):
         L = shim()
         n, nel, nn = mesh.neq, mesh.nel, mesh.nnodes
         self.P = ParametersType()
         for k, v in (("Solver", b"GMRES"), ("Preconditioner", precond.encode()), ("Scaling", b"NOT"),
-                     ("reordering", b"SYMRCM"), ("MatrixVectorProductScheme", b"EBE")):
+                     ("reordering", b"SYMRCM"), ("MatrixVectorProductScheme", scheme.encode())):
             setattr(self.P, k, v)
         self.P.SolverTolerance, self.P.KrylovBasisVectorsQuantity, self.P.LinearMaxIter = tol, kmax, lmax
         self.P.nnodes = self.P.nNodes = nn
@@ -145,10 +148,14 @@ class DriverState:
         self.S.Node = ctypes.cast(self.nodes, ctypes.POINTER(NodeType))
         self.S.Element = ctypes.cast(self.elems, ctypes.POINTER(ElementType))
         self.Fn = FemFunctionsType()
-        self.Fn.mv = _addr(L, "ebemv")
-        self.Fn.precond = _addr(L, "Diag_precond" if precond == "Diag" else "NO_precond")
+        kind = "Diag" if precond == "Diag" else "ILUp" if precond.startswith("ILU") else \
+            "SPIKE" if precond.startswith("SPIKE") else "NO"
+        self.Fn.mv = _addr(L, "csrmv" if scheme == "CSR" else "ebemv")
+        self.Fn.assembly = _addr(L, "csr_assembly") if scheme == "CSR" else None
+        self.Fn.precond = _addr(L, kind + "_precond")
         self.Fn.precondR = _addr(L, "NO_precond")
-        self.setup = getattr(L, "Diag_precond_EBE_setup" if precond == "Diag" else "NO_precond_setup")
+        self.setup = getattr(L, {"Diag": "Diag_precond_EBE_setup", "ILUp": "ILUp_precond_setup",
+                                 "SPIKE": "SPIKE_precond_setup", "NO": "NO_precond_setup"}[kind])
 
     def ptrs(self):
         return (ctypes.addressof(self.P), ctypes.addressof(self.M), ctypes.addressof(self.S))
@@ -168,6 +175,19 @@ class DriverState:
         Pv = np.array(P, dtype=np.float64, copy=True)
         Q = np.zeros_like(Pv)
         rc = shim().ebemv(*self.ptrs(), Pv.ctypes.data, Q.ctypes.data)
+        return rc, Q
+
+    def csr_assembly(self, A):
+        """What Build_K_F_SUPG does with CSR storage: one call per element."""
+        L = shim()
+        A = np.ascontiguousarray(A, dtype=np.float64).reshape(-1, 9)
+        for e in range(A.shape[0]):
+            L.csr_assembly(*self.ptrs(), e, A[e].ctypes.data)
+
+    def csrmv(self, P):
+        Pv = np.array(P, dtype=np.float64, copy=True)
+        Q = np.zeros_like(Pv)
+        rc = shim().csrmv(*self.ptrs(), Pv.ctypes.data, Q.ctypes.data)
         return rc, Q
 
 
