@@ -63,41 +63,50 @@ __device__ __forceinline__ void part_dots(const SysDev &D, const DChunk &k, int 
 }
 
 // dots of V[0..i] with w and with v = V[i] over a part, in one sweep of the
-// basis: warp-per-j, <V[j], w> to out[j] and <V[j], v> to out[i + 1 + j]
+// basis: warp w takes j = w, w+8, w+16, w+24 (i < 32) together, so each pack
+// of w and v is loaded once per warp whatever the number of its vectors;
+// <V[j], w> to out[j], <V[j], v> to out[i + 1 + j]
 template <typename T>
 __device__ __forceinline__ void part_dots2(const SysDev &D, const DChunk &k, int i, const T *__restrict__ w,
                                            double *out)
 {
     constexpr int N = Pk<T>::N;
+    constexpr int NW = kThreads / 32;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const T *V = (const T *)D.V;
     const T *vi = V + (size_t)i * D.n_pad;
-    for (int j = warp; j <= i; j += kThreads / 32) {
-        const T *vj = V + (size_t)j * D.n_pad;
-        T a0 = 0, a1 = 0, b0 = 0, b1 = 0;
-        int q = k.d0 + lane * N;
-        for (; q + 32 * N < k.d1; q += 2 * 32 * N) {
-            auto v0 = ld_pk(vj + q), v1 = ld_pk(vj + q + 32 * N);
-            auto w0 = ld_pk(w + q), w1 = ld_pk(w + q + 32 * N);
-            auto u0 = ld_pk(vi + q), u1 = ld_pk(vi + q + 32 * N);
+    const int nj = warp <= i ? (i - warp) / NW + 1 : 0;   // vectors of this warp (<= 4)
+    if (nj == 0) return;
+    const T *vj[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) vj[u] = V + (size_t)min(warp + NW * u, i) * D.n_pad;
+    T a[4], b[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) a[u] = b[u] = (T)0;
+    for (int q = k.d0 + lane * N; q < k.d1; q += 32 * N) {
+        const auto w0 = ld_pk(w + q), u0 = ld_pk(vi + q);
+        typename Pk<T>::type v0[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (u < nj) v0[u] = ld_pk(vj[u] + q);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (u >= nj) break;
 #pragma unroll
             for (int c = 0; c < N; ++c) {
-                a0 += v0.v[c] * w0.v[c];
-                a1 += v1.v[c] * w1.v[c];
-                b0 += v0.v[c] * u0.v[c];
-                b1 += v1.v[c] * u1.v[c];
+                a[u] += v0[u].v[c] * w0.v[c];
+                b[u] += v0[u].v[c] * u0.v[c];
             }
         }
-        for (; q < k.d1; q += 32 * N) {
-            auto v0 = ld_pk(vj + q), w0 = ld_pk(w + q), u0 = ld_pk(vi + q);
+    }
 #pragma unroll
-            for (int c = 0; c < N; ++c) {
-                a0 += v0.v[c] * w0.v[c];
-                b0 += v0.v[c] * u0.v[c];
-            }
+    for (int u = 0; u < 4; ++u) {
+        if (u >= nj) break;
+        const double sa = warp_sum((double)a[u]), sb = warp_sum((double)b[u]);
+        if (lane == 0) {
+            out[warp + NW * u] = sa;
+            out[i + 1 + warp + NW * u] = sb;
         }
-        double sa = warp_sum((double)(a0 + a1)), sb = warp_sum((double)(b0 + b1));
-        if (lane == 0) { out[j] = sa; out[i + 1 + j] = sb; }
     }
 }
 
@@ -194,7 +203,7 @@ k_dots1(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
 // c = s + (s - G s): the coefficients of the two classical passes of CGS2
 // (h1 = s, h2 = V^T (w - V s) = s - G s) with the second one taken from G
 // instead of a second sweep over the basis; c becomes column i of H and
-// the update that k_orth2 applies.  Used when 2 (kmax) <= kPartStride.
+// the update that k_orth2 applies.  Used when kmax <= 32.
 template <typename T>
 __global__ void __launch_bounds__(kThreads)
 k_dots1g(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)

@@ -880,7 +880,7 @@ static int enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
     dim3 gd = grid_for(P.n_dch);
     // mixed precision: one sweep fewer per step (Gram-corrected CGS); the
     // FP64 reference method keeps two full classical passes
-    const bool gram = cfg.mixed && 2 * cfg.kmax <= kPartStride;
+    const bool gram = cfg.mixed && cfg.kmax <= 32;   // 2 (i + 1) partial sums fit a part slot
     int k = enqueue_matvec<T>(P, 0, 0, st);
     k += enqueue_precond<T>(P, 0, st);
     k_start<<<gd, kThreads, 0, st>>>(sys, dc, nd);
