@@ -339,6 +339,28 @@ typedef struct {
 int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *opts,
                        const fg_time_opts *t, double *u, double *a, fg_time_stats *stats);
 
+/* ---- transient SUPG/CAU transport (02_Transport_Equation) ----
+ * Replaces Build_M_K_R_SUPG.c:6-252 (with CAU_ShockCapture.c:3-33,
+ * h_shock_2sqrtArea.c, eval_U_dU.c and ebe_assembly.c) for a system with
+ * ndof = 1 and the geometry of fg_set_geometry: the blocks become
+ * Ae = me + alpha dt ke (SUPG mass and the steady operator of
+ * fg_transport_assemble), R = F - me du - ke u, accumulated in the
+ * reference's element order (bit-identical). */
+typedef struct {
+    fg_transport_coeffs c;  /* conductivity, reaction, velocity, source, CAU */
+    double alpha;           /* Alpha (Alpha_Build)                          */
+    double dt;              /* DeltaT (DeltaT_Build)                         */
+} fg_tt_coeffs;
+/* One build at (u, du) (free dofs, reference numbering, host; NULL = 0);
+ * R (host, n+1, may be NULL) receives the residual. */
+int fg_tt_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, const double *du, double *R);
+/* Predictor_Old (Time_Integration/Predictor_Old.c:6-134, Criteria.c) with
+ * this build, as fg_euler_predictor runs it: state, residual and increment
+ * on the device; t->precond FG_PRECOND_DIAG (accumulating, the reference's
+ * Diag_precond_EBE_setup) or any other kind this system supports. */
+int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *opts, const fg_time_opts *t,
+                    double *u, double *a, fg_time_stats *stats);
+
 /* ---- request server: continuous batching of transport solves ----
  * A worker thread owns one batch.  Requests (a system whose geometry is set,
  * with transport coefficients) wait in a FIFO; between restart cycles the

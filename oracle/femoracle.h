@@ -194,6 +194,20 @@ int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, co
                        const or_time_opts *to, double solver_tol, int kmax, int lmax,
                        double *u, double *a, or_time_stats *st);
 
+/* ---- transient SUPG/CAU transport (02_Transport_Equation, oracle/tt.c) ----
+ * Build_M_K_R_SUPG: A receives Ae = me + alpha dt ke (9 per element), R the
+ * residual F - me du - ke u (NEQ + 1 entries, R[NEQ] = 0); u, du: free dofs. */
+void or_build_tt(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                 const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
+                 const double *u, const double *du, double *A, double *R);
+/* Predictor_Old with Build_M_K_R_SUPG, ebemv on the local RCM numbering,
+ * accumulating Diag and GMRES.  u: initial state in, final state out; a
+ * (neq) receives du/dt. */
+int or_tt_predictor(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                    const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
+                    const or_time_opts *to, double solver_tol, int kmax, int lmax, double *u, double *a,
+                    or_time_stats *st);
+
 /* ---- assembled CSR path and ILU(0) (oracle/csr_ilu.c) ---- */
 int  or_csr_pattern(int nel, const int *ien, const int *type, const int *invp, int NEQ,
                     const int *Perm, const int *invPerm, int *IA, int *JA);

@@ -83,6 +83,12 @@ def lib():
         L.or_euler_predictor.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, _c_dbl, _c_int, _c_int,
                                          _f64p, _f64p, ctypes.c_void_p]
+        L.or_build_tt.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, ctypes.c_void_p,
+                                  _c_dbl, _c_dbl, _f64p, _f64p, _f64p, _f64p]
+        L.or_build_tt.restype = None
+        L.or_tt_predictor.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                      ctypes.c_void_p, _c_dbl, _c_dbl, ctypes.c_void_p, _c_dbl, _c_int, _c_int,
+                                      _f64p, _f64p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -397,6 +403,33 @@ def build_k_f_supg(prob, u=None):
     lib().or_build_k_f_supg(*_mesh_args(m), ctypes.byref(s), np.ascontiguousarray(u, dtype=np.float64), A, F)
     F[m.neq] = 0.0
     return A.reshape(m.nel, 9), F
+
+
+def build_tt(prob, alpha, dt, u=None, du=None):
+    """Build_M_K_R_SUPG (transient transport) at (u, du); returns
+    (A[nel, 9] = me + alpha dt ke, R[neq+1])."""
+    m = prob.mesh
+    u = np.zeros(m.neq) if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    du = np.zeros(m.neq) if du is None else np.ascontiguousarray(du, dtype=np.float64)
+    A = np.empty(m.nel * 9)
+    R = np.empty(m.neq + 1)
+    s, keep = _problem_struct(prob)
+    lib().or_build_tt(*_mesh_args(m), ctypes.byref(s), float(alpha), float(dt), u, du, A, R)
+    return A.reshape(m.nel, 9), R
+
+
+def tt_predictor(prob, alpha, dt, topts: TimeOpts, tol=1e-10, kmax=30, lmax=1000, u0=None):
+    """Predictor_Old with the transient transport build; returns (u, a, stats)."""
+    m = prob.mesh
+    u = np.zeros(m.neq + 1)
+    if u0 is not None:
+        u[:m.neq] = u0
+    a = np.zeros(m.neq + 1)
+    st = _TimeStats()
+    s, keep = _problem_struct(prob)
+    lib().or_tt_predictor(*_mesh_args(m), ctypes.byref(s), float(alpha), float(dt), ctypes.byref(topts), tol, kmax,
+                          lmax, u, a, ctypes.byref(st))
+    return u[:m.neq].copy(), a[:m.neq].copy(), {k: getattr(st, k) for k, _ in st._fields_}
 
 
 def ebemv3_perm(lm, A, perm, inv, P):

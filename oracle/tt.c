@@ -1,0 +1,212 @@
+/*
+ * femoracle: transient SUPG/CAU convection-diffusion-reaction on P1
+ * triangles.  TEST INFRASTRUCTURE ONLY (see femoracle.h).
+ *
+ * Restates 02_Transport_Equation/2D/01_CommonFiles/Build_M_K_R_SUPG.c:6-252
+ * (SUPG mass, diffusion, convection, reaction, SUPG and CAU terms; the block
+ * Ae = me + alpha dt ke stored per element as ebe_assembly does; the
+ * residual R = F - me du - ke u accumulated element by element), with
+ * CAU_ShockCapture.c:3-33 (residual including du), h_shock_2sqrtArea.c and
+ * eval_U_dU.c, and the Predictor_Old.c:6-134 time loop with Diag
+ * preconditioning (accumulating, Diag_precond_EBE_setup.c) and GMRES.  The
+ * element formulas are the reference's, term for term, so blocks and
+ * residual agree to the last bit when both are compiled without
+ * floating-point contraction.
+ */
+#include "femoracle.h"
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* CAU_ShockCapture of the transient driver: Ru includes du/dt. */
+static double tt_cau(double kx, double ky, double bx, double by, double gamma, double ue1, double ue2,
+                     double ue3, double ueb, double dueb, double feb, double y23, double y31, double y12,
+                     double x32, double x13, double x21, double invArea, double h)
+{
+    double third = 1. / 3.;
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = dueb + bgu + gamma*ueb - feb;
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    double bxp = bgu*gx/(ng*ng);
+    double byp = bgu*gy/(ng*ng);
+    double kp = bxp*bxp*kx + byp*byp*ky;
+    double nbp = sqrt(bxp*bxp + byp*byp);
+    double Pe = 0.5*h*nbp*nbp*nbp/kp;
+    if (ng > 0) {
+        if (third*Pe < 0.7) return 0.5*h*third*Pe*fabs(Ru)/ng;
+        return 0.5*h*0.7*fabs(Ru)/ng;
+    }
+    return 0;
+}
+
+void or_build_tt(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                 const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
+                 const double *u, const double *du, double *A, double *R)
+{
+    const double third = 1.0/3.0, sixth = 1.0/6.0, twelfth = 1.0/12.0;
+    const double kx = prob->k, ky = prob->k, gamma = prob->gamma;
+    double *U = malloc(sizeof(double) * (size_t)(nnodes ? nnodes : 1));
+    double *dU = malloc(sizeof(double) * (size_t)(nnodes ? nnodes : 1));
+    int J, E;
+    for (J = 0; J <= neq; J++) R[J] = 0;
+    for (J = 0; J < nnodes; J++) {          /* eval_U_dU.c:3-22 */
+        U[J] = type[J] == 0 ? prob->upresc[J] : u[invp[J]];
+        dU[J] = type[J] == 0 ? 0.0 : du[invp[J]];
+    }
+    for (E = 0; E < nel; E++) {
+        int J1 = ien[3*E], J2 = ien[3*E+1], J3 = ien[3*E+2];
+        double X0 = x[J1], X1 = x[J2], X2 = x[J3];
+        double Y0 = y[J1], Y1 = y[J2], Y2 = y[J3];
+        double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+        double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+        double TwoA = x21*y31 - x13*y12;
+        double Area = 0.5*TwoA;
+        double invArea = 1.0/Area;
+        double h = sqrt(fabs(TwoA));
+        double bx = prob->beta[0], by = prob->beta[1];
+        double norm = sqrt(bx*bx + by*by);
+        double tau = norm > 0 ? 0.5*h/norm : 0;
+        double fe1 = prob->f, fe2 = prob->f, fe3 = prob->f;
+        double feb = third*(fe1 + fe2 + fe3);
+        double ue[3] = { U[J1], U[J2], U[J3] }, due[3] = { dU[J1], dU[J2], dU[J3] };
+        double ueb = third*(ue[0] + ue[1] + ue[2]);
+        double dueb = third*(due[0] + due[1] + due[2]);
+        double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+        double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+        double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+        double C11 = sixth*(bx*y23 + by*x32);
+        double C12 = sixth*(bx*y31 + by*x13);
+        double C13 = sixth*(bx*y12 + by*x21);
+        double R11 = sixth*(gamma*Area);
+        double R12 = twelfth*(gamma*Area);
+        double Cpg12 = 0.25*invArea*tau*(y23*(bx*bx*y31 + bx*by*x13) + x32*(bx*by*y31 + by*by*x13));
+        double Cpg13 = 0.25*invArea*tau*(y23*(bx*bx*y12 + bx*by*x21) + x32*(bx*by*y12 + by*by*x21));
+        double Cpg23 = 0.25*invArea*tau*(y31*(bx*bx*y12 + bx*by*x21) + x13*(bx*by*y12 + by*by*x21));
+        double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
+        double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
+        double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
+        double hs = sqrt(fabs(2*Area));
+        double Eu = prob->cau ? tt_cau(kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb,
+                                       y23, y31, y12, x32, x13, x21, invArea, hs) : 0.0;
+        double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
+        double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
+        double Csc23 = Eu*0.25*invArea*(y31*y12 + x13*x21);
+        double me[3][3], ke[3][3];
+        me[0][0] = sixth*Area + tau*C11;
+        me[0][1] = twelfth*Area + tau*C11;
+        me[0][2] = twelfth*Area + tau*C11;
+        me[1][0] = twelfth*Area + tau*C12;
+        me[1][1] = sixth*Area + tau*C12;
+        me[1][2] = twelfth*Area + tau*C12;
+        me[2][0] = twelfth*Area + tau*C13;
+        me[2][1] = twelfth*Area + tau*C13;
+        me[2][2] = sixth*Area + tau*C13;
+        ke[0][0] = -(D12 + D13) + C11 - (Cpg12 + Cpg13) + R11 + Rpg11 - (Csc12 + Csc13);
+        ke[0][1] = D12 + C12 + Cpg12 + R12 + Rpg11 + Csc12;
+        ke[0][2] = D13 + C13 + Cpg13 + R12 + Rpg11 + Csc13;
+        ke[1][0] = D12 + C11 + Cpg12 + R12 + Rpg21 + Csc12;
+        ke[1][1] = -(D12 + D23) + C12 - (Cpg12 + Cpg23) + R11 + Rpg21 - (Csc12 + Csc23);
+        ke[1][2] = D23 + C13 + Cpg23 + R12 + Rpg21 + Csc23;
+        ke[2][0] = D13 + C11 + Cpg13 + R12 + Rpg31 + Csc13;
+        ke[2][1] = D23 + C12 + Cpg23 + R12 + Rpg31 + Csc23;
+        ke[2][2] = -(D13 + D23) + C13 - (Cpg13 + Cpg23) + R11 + Rpg31 - (Csc13 + Csc23);
+        /* lm of the element (Fill_LM.c): equation or the sink neq */
+        int lm[3];
+        lm[0] = type[J1] == 0 ? neq : invp[J1];
+        lm[1] = type[J2] == 0 ? neq : invp[J2];
+        lm[2] = type[J3] == 0 ? neq : invp[J3];
+        R[lm[0]] += Area*twelfth*(2*fe1 + fe2 + fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y23 + by*x32);
+        R[lm[1]] += Area*twelfth*(fe1 + 2*fe2 + fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y31 + by*x13);
+        R[lm[2]] += Area*twelfth*(fe1 + fe2 + 2*fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y12 + by*x21);
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) R[lm[i]] -= me[i][j]*due[j] + ke[i][j]*ue[j];
+        R[neq] = 0;
+        double *Ae = A + 9L * E;
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++) Ae[3*i + j] = me[i][j] + alpha*dt*ke[i][j];
+    }
+    free(U);
+    free(dU);
+}
+
+typedef struct {
+    int nel, NEQ;
+    const int *lm, *Perm, *invPerm;
+    const double *A, *invDiag;
+} tt_ctx;
+
+static int tt_mv_cb(void *p, double *P, double *Q)
+{
+    tt_ctx *c = (tt_ctx *)p;
+    or_ebemv3_perm(c->nel, c->lm, c->A, c->Perm, c->invPerm, c->NEQ, P, Q);
+    return 0;
+}
+
+static int tt_pc_cb(void *p, double *x, double *z)
+{
+    tt_ctx *c = (tt_ctx *)p;
+    or_diag_apply(c->NEQ, c->invDiag, x, z);
+    return 0;
+}
+
+int or_tt_predictor(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                    const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
+                    const or_time_opts *to, double solver_tol, int kmax, int lmax, double *u, double *a,
+                    or_time_stats *st)
+{
+    const int NEQ = neq;
+    size_t ne = (size_t)(nel ? nel : 1);
+    int *lm = malloc(sizeof(int) * 3 * ne);
+    int *Perm = malloc(sizeof(int) * ((size_t)NEQ + 1)), *invPerm = malloc(sizeof(int) * ((size_t)NEQ + 1));
+    double *A = malloc(sizeof(double) * 9 * ne);
+    double *R = calloc((size_t)NEQ + 1, sizeof(double));
+    double *Da = calloc((size_t)NEQ + 1, sizeof(double));
+    double *u_old = calloc((size_t)NEQ + 1, sizeof(double));
+    double *Diag = calloc((size_t)NEQ + 1, sizeof(double)), *invDiag = calloc((size_t)NEQ + 1, sizeof(double));
+    double *diff = calloc((size_t)NEQ + 1, sizeof(double));
+    or_fill_lm(nel, 1, ien, type, invp, NEQ, lm);
+    or_permutation_of_lm(nel, ien, type, invp, NEQ, Perm, invPerm, NULL);
+    tt_ctx ctx = { nel, NEQ, lm, Perm, invPerm, A, invDiag };
+    double t = 0.0;
+    int steps = 0, corr = 0, gmres = 0, stop_time, i;
+    memset(a, 0, sizeof(double) * (size_t)neq);
+    do {
+        int it = 0, stop;
+        steps++;
+        t += dt;
+        memcpy(u_old, u, sizeof(double) * (size_t)neq);
+        for (i = 0; i < neq; i++) u[i] += (1.0 - alpha) * dt * a[i];     /* prediction */
+        memset(a, 0, sizeof(double) * (size_t)neq);
+        do {                                                            /* multicorrection */
+            int gi = 0;
+            it++;
+            or_build_tt(nnodes, nel, x, y, type, invp, ien, neq, prob, alpha, dt, u, a, A, R);
+            or_diag_setup(nel, 3, lm, A, NEQ, Diag, invDiag, R);
+            or_pgmres(NEQ, kmax, lmax, solver_tol, tt_mv_cb, tt_pc_cb, &ctx, R, Da, &gi);
+            gmres += gi;
+            for (i = 0; i < neq; i++) a[i] += 1 * Da[i];
+            for (i = 0; i < neq; i++) u[i] += alpha * dt * Da[i];
+            double norm_a = sqrt(or_ddot(neq, a, a));
+            double norm_Da = sqrt(or_ddot(neq, Da, Da));
+            /* Criteria.c:25-41 */
+            if (to->stop_by_norm) stop = norm_Da < to->correction_tol * norm_a || it >= to->max_corrections;
+            else stop = it >= to->max_corrections;
+        } while (!stop);
+        corr += it;
+        /* Criteria.c:44-80 */
+        if (to->steady_state) {
+            for (i = 0; i < neq; i++) diff[i] = u[i] - u_old[i];
+            double nd = sqrt(or_ddot(neq, diff, diff)), nu = sqrt(or_ddot(neq, u, u));
+            stop_time = to->time_tol * nu > nd || fabs(to->final_time - t) < dt;
+        } else {
+            stop_time = to->final_time - t < 1e-10;
+        }
+        if (to->max_steps > 0 && steps >= to->max_steps) stop_time = 1;
+    } while (!stop_time);
+    if (st) { st->steps = steps; st->corrections = corr; st->gmres_iterations = gmres; st->t = t; }
+    free(lm); free(Perm); free(invPerm); free(A); free(R); free(Da); free(u_old); free(Diag); free(invDiag);
+    free(diff);
+    return steps;
+}

@@ -411,6 +411,163 @@ __global__ void k_transport_F(int n, int ld, const int *__restrict__ dptr, const
     F[d] = s;
 }
 
+// ---------------------------------------------------------------- transient SUPG/CAU transport
+// Build_M_K_R_SUPG.c:6-252 (02_Transport_Equation) with its
+// CAU_ShockCapture.c:3-33 (the residual includes du/dt), h_shock_2sqrtArea.c
+// and eval_U_dU.c, one thread per element (internal order).  Writes the block
+// Ae = me + alpha dt ke into the SoA layout and, per element row a, the four
+// terms the reference applies to R[lm[a]] in order: + Fe_a, then
+// - (me[a][b] du_b + ke[a][b] u_b) for b = 0, 1, 2 (Rt[(4 a + k) ld + pos]).
+__device__ double tt_cau_eu(double kx, double ky, double bx, double by, double gamma, double ue1, double ue2,
+                            double ue3, double ueb, double dueb, double feb, double y23, double y31, double y12,
+                            double x32, double x13, double x21, double invArea, double h)
+{
+    double third = 1. / 3.;
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = dueb + bgu + gamma*ueb - feb;
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    double bxp = bgu*gx/(ng*ng);
+    double byp = bgu*gy/(ng*ng);
+    double kp = bxp*bxp*kx + byp*byp*ky;
+    double nbp = sqrt(bxp*bxp + byp*byp);
+    double Pe = 0.5*h*nbp*nbp*nbp/kp;
+    if (ng > 0) {
+        if (third*Pe < 0.7) return 0.5*h*third*Pe*fabs(Ru)/ng;
+        return 0.5*h*0.7*fabs(Ru)/ng;
+    }
+    return 0;
+}
+
+__global__ void k_tt_elem(int nel, int ld, const int *__restrict__ gien, const double *__restrict__ gx,
+                          const double *__restrict__ gy, const int *__restrict__ gtype,
+                          const int *__restrict__ node_dof, const double *__restrict__ up,
+                          const double *__restrict__ u, const double *__restrict__ du, fg_tt_coeffs tc,
+                          double *__restrict__ A64, double *__restrict__ Rt)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const fg_transport_coeffs &cf = tc.c;
+    const double third = 1.0/3.0, sixth = 1.0/6.0, twelfth = 1.0/12.0;
+    const double kx = cf.k, ky = cf.k, gamma = cf.gamma;
+    int J1 = gien[pos], J2 = gien[ld + pos], J3 = gien[2 * (size_t)ld + pos];
+    double X0 = gx[J1], X1 = gx[J2], X2 = gx[J3];
+    double Y0 = gy[J1], Y1 = gy[J2], Y2 = gy[J3];
+    double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+    double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+    double TwoA = x21*y31 - x13*y12;
+    double Area = 0.5*TwoA;
+    double invArea = 1.0/Area;
+    double h = sqrt(fabs(TwoA));
+    double bx = cf.beta[0], by = cf.beta[1];
+    double norm = sqrt(bx*bx + by*by);
+    double tau = norm > 0 ? 0.5*h/norm : 0;
+    double fe1 = cf.f, fe2 = cf.f, fe3 = cf.f;
+    double feb = third*(fe1 + fe2 + fe3);
+    const int J[3] = {J1, J2, J3};
+    double ue[3], due[3];
+    for (int a = 0; a < 3; ++a) {
+        const bool fixed = gtype[J[a]] == 0;
+        ue[a] = fixed ? up[J[a]] : u[node_dof[J[a]]];
+        due[a] = fixed ? 0.0 : du[node_dof[J[a]]];
+    }
+    double ueb = third*(ue[0] + ue[1] + ue[2]);
+    double dueb = third*(due[0] + due[1] + due[2]);
+    double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+    double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+    double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+    double C11 = sixth*(bx*y23 + by*x32);
+    double C12 = sixth*(bx*y31 + by*x13);
+    double C13 = sixth*(bx*y12 + by*x21);
+    double R11 = sixth*(gamma*Area);
+    double R12 = twelfth*(gamma*Area);
+    double Cpg12 = 0.25*invArea*tau*(y23*(bx*bx*y31 + bx*by*x13) + x32*(bx*by*y31 + by*by*x13));
+    double Cpg13 = 0.25*invArea*tau*(y23*(bx*bx*y12 + bx*by*x21) + x32*(bx*by*y12 + by*by*x21));
+    double Cpg23 = 0.25*invArea*tau*(y31*(bx*bx*y12 + bx*by*x21) + x13*(bx*by*y12 + by*by*x21));
+    double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
+    double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
+    double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
+    double hs = sqrt(fabs(2*Area));
+    double Eu = cf.cau ? tt_cau_eu(kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb, y23, y31, y12, x32,
+                                   x13, x21, invArea, hs) : 0.0;
+    double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
+    double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
+    double Csc23 = Eu*0.25*invArea*(y31*y12 + x13*x21);
+    double me[3][3], ke[3][3];
+    me[0][0] = sixth*Area + tau*C11;
+    me[0][1] = twelfth*Area + tau*C11;
+    me[0][2] = twelfth*Area + tau*C11;
+    me[1][0] = twelfth*Area + tau*C12;
+    me[1][1] = sixth*Area + tau*C12;
+    me[1][2] = twelfth*Area + tau*C12;
+    me[2][0] = twelfth*Area + tau*C13;
+    me[2][1] = twelfth*Area + tau*C13;
+    me[2][2] = sixth*Area + tau*C13;
+    ke[0][0] = -(D12 + D13) + C11 - (Cpg12 + Cpg13) + R11 + Rpg11 - (Csc12 + Csc13);
+    ke[0][1] = D12 + C12 + Cpg12 + R12 + Rpg11 + Csc12;
+    ke[0][2] = D13 + C13 + Cpg13 + R12 + Rpg11 + Csc13;
+    ke[1][0] = D12 + C11 + Cpg12 + R12 + Rpg21 + Csc12;
+    ke[1][1] = -(D12 + D23) + C12 - (Cpg12 + Cpg23) + R11 + Rpg21 - (Csc12 + Csc23);
+    ke[1][2] = D23 + C13 + Cpg23 + R12 + Rpg21 + Csc23;
+    ke[2][0] = D13 + C11 + Cpg13 + R12 + Rpg31 + Csc13;
+    ke[2][1] = D23 + C12 + Cpg23 + R12 + Rpg31 + Csc23;
+    ke[2][2] = -(D13 + D23) + C13 - (Cpg13 + Cpg23) + R11 + Rpg31 - (Csc13 + Csc23);
+    const double adt = tc.alpha*tc.dt;
+    double *A = A64 + pos;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) A[(size_t)(3 * a + b) * ld] = me[a][b] + adt*ke[a][b];
+    const double Fe[3] = {Area*twelfth*(2*fe1 + fe2 + fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y23 + by*x32),
+                          Area*twelfth*(fe1 + 2*fe2 + fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y31 + by*x13),
+                          Area*twelfth*(fe1 + fe2 + 2*fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y12 + by*x21)};
+    for (int a = 0; a < 3; ++a) {
+        Rt[(size_t)(4 * a) * ld + pos] = Fe[a];
+        for (int b = 0; b < 3; ++b) Rt[(size_t)(4 * a + 1 + b) * ld + pos] = me[a][b]*due[b] + ke[a][b]*ue[b];
+    }
+}
+
+// R[d]: the element terms of dof d in reference element order, applied as
+// the reference applies them (R += Fe, then three subtractions); R[n] = 0.
+__global__ void k_tt_R(int n, int ld, const int *__restrict__ dptr, const int *__restrict__ dinc,
+                       const double *__restrict__ Rt, double *__restrict__ R)
+{
+    int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d > n) return;
+    if (d == n) { R[n] = 0.0; return; }
+    double s = 0.0;
+    for (int q = dptr[d]; q < dptr[d + 1]; ++q) {
+        const int pos = dinc[q] >> 4, a = dinc[q] & 15;
+        s += Rt[(size_t)(4 * a) * ld + pos];
+        s -= Rt[(size_t)(4 * a + 1) * ld + pos];
+        s -= Rt[(size_t)(4 * a + 2) * ld + pos];
+        s -= Rt[(size_t)(4 * a + 3) * ld + pos];
+    }
+    R[d] = s;
+}
+
+int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev, const double *du_dev, double *R_dev,
+                       cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (t.ndof != 1) { set_error("transient transport assembly needs ndof == 1"); return FG_ERR_UNSUPPORTED; }
+    if (!s->geometry_ok) { set_error("transient transport assembly before fg_set_geometry"); return FG_ERR_STATE; }
+    int r;
+    if (s->Fe.bytes < 8 * (size_t)12 * s->nel_pad && (r = s->Fe.alloc(8 * (size_t)12 * s->nel_pad))) return r;
+    if (t.nel > 0)
+        k_tt_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(), s->gx.as<double>(),
+                                                      s->gy.as<double>(), s->gtype.as<int>(), s->node_dof.as<int>(),
+                                                      s->gup.as<double>(), u_dev, du_dev, *c, s->A64.as<double>(),
+                                                      s->Fe.as<double>());
+    FG_CUDA(cudaGetLastError());
+    k_tt_R<<<(t.n + 256) / 256, 256, 0, st>>>(t.n, s->nel_pad, s->dinc_ptr.as<int>(), s->dinc.as<int>(),
+                                             s->Fe.as<double>(), R_dev);
+    FG_CUDA(cudaGetLastError());
+    count_launches(2);
+    s->blocks_ok = true;
+    s->csr_dirty = true;
+    return convert_blocks(s, st);
+}
+
 int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c, const double *u_dev, double *F_dev,
                               cudaStream_t st)
 {

@@ -726,19 +726,25 @@ int fg_euler_assemble(fg_system *s, const fg_euler_coeffs *c, const double *u, c
     return FG_OK;
 }
 
+}  // extern "C"
+
+namespace fg {
+
 // Predictor_Old.c:6-134 with the state (u, a, u_old), the residual and the
-// increment kept on the device; per correction one assembly, one
-// preconditioner set-up, one batched-engine solve and two update kernels.
-// Only the norms the stop tests read come back to the host.
-int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *o, const fg_time_opts *to,
-                       double *u, double *a, fg_time_stats *stats)
+// increment kept on the device; per correction one assembly (`assemble(u,
+// a, R)` on the device, internal numbering), one preconditioner set-up, one
+// batched-engine solve and two update kernels.  Only the norms the stop
+// tests read come back to the host.  Shared by the Euler and the transient
+// transport drivers (the reference shares Predictor_Old between them).
+template <class Assemble>
+static int predictor_old(fg_system *s, double dt, double alpha, Assemble &&assemble, const fg_solver_opts *o,
+                         const fg_time_opts *to, double *u, double *a, fg_time_stats *stats)
 {
-    if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
     if (to->precond < FG_PRECOND_NONE || to->precond > FG_PRECOND_SPIKE) {
-        set_error("Euler preconditioner must be NONE, DIAG, BLOCKDIAG, ILU0 or SPIKE");
+        set_error("time-loop preconditioner must be NONE, DIAG, BLOCKDIAG, ILU0 or SPIKE");
         return FG_ERR_ARG;
     }
-    if (to->max_corrections < 1 || !(c->dt > 0)) { set_error("max_corrections >= 1 and dt > 0 required"); return FG_ERR_ARG; }
+    if (to->max_corrections < 1 || !(dt > 0)) { set_error("max_corrections >= 1 and dt > 0 required"); return FG_ERR_ARG; }
     auto t0 = std::chrono::steady_clock::now();
     const int n = s->topo.n;
     fg_system *one[1] = {s};
@@ -757,7 +763,6 @@ int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_o
     FG_CUDA(cudaMemsetAsync(da, 0, vb, s->stream));
     if (to->precond == FG_PRECOND_DIAG) FG_CUDA(cudaMemsetAsync(s->diag.p, 0, s->diag.bytes, s->stream));
     double *part = s->norm_part.as<double>(), *norms = part + (s->norm_part.bytes / 8 - 2);
-    const double dt = c->dt, alpha = c->alpha;
     double t = 0.0, last_res = NAN;
     int steps = 0, corr = 0, gmres = 0;
     bool stop_time = false;
@@ -771,7 +776,7 @@ int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_o
         bool stop = false;
         do {                                                                          // multicorrection
             ++it;
-            if ((r = euler_assemble_device(s, c, du, da, s->rhs_f.as<double>(), s->stream))) return r;
+            if ((r = assemble(du, da, s->rhs_f.as<double>()))) return r;
             FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, vb, cudaMemcpyDeviceToDevice, s->stream));
             int flags = to->setup_flags | (to->precond == FG_PRECOND_DIAG ? FG_SETUP_ACCUMULATE : 0);
             if ((r = precond_setup_device(s, to->precond, flags, s->rhs_b.as<double>(), s->stream))) return r;
@@ -823,6 +828,51 @@ int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_o
         stats->true_rel_residual = last_res;
     }
     return FG_OK;
+}
+
+
+}  // namespace fg
+
+extern "C" {
+
+int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *o, const fg_time_opts *to,
+                       double *u, double *a, fg_time_stats *stats)
+{
+    if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
+    return predictor_old(s, c->dt, c->alpha,
+                         [&](const double *du, const double *da, double *R) {
+                             return euler_assemble_device(s, c, du, da, R, s->stream);
+                         },
+                         o, to, u, a, stats);
+}
+
+int fg_tt_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, const double *du, double *R)
+{
+    if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = stage(s, s->state_a, 8 * (size_t)s->n_pad))) return r;
+    if ((r = state_in(s, u, s->ws.t64.as<double>())) || (r = state_in(s, du, s->state_a.as<double>()))) return r;
+    if ((r = tt_assemble_device(s, c, s->ws.t64.as<double>(), s->state_a.as<double>(), s->ws.u64.as<double>(),
+                                s->stream)))
+        return r;
+    if (R && (r = vec_out(s, s->ws.u64.as<double>(), R, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o, const fg_time_opts *to, double *u,
+                    double *a, fg_time_stats *stats)
+{
+    if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
+    return predictor_old(s, c->dt, c->alpha,
+                         [&](const double *du, const double *da, double *R) {
+                             return tt_assemble_device(s, c, du, da, R, s->stream);
+                         },
+                         o, to, u, a, stats);
 }
 
 }  // extern "C"

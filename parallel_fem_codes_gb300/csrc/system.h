@@ -201,6 +201,9 @@ int axpy_norms_device(int n, double a, const double *x, double *y, double *part,
 int diff_norms_device(int n, const double *u, const double *v, double *part, double *out, cudaStream_t st);
 int axpy_device(int n, double a, const double *x, double *y, cudaStream_t st);
 size_t norm_scratch_bytes();
+// Transient transport (setup.cu)
+int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev, const double *du_dev, double *R_dev,
+                       cudaStream_t st);
 // Euler (euler.cu)
 int euler_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
                           double *R_dev, cudaStream_t st);

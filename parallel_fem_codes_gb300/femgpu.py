@@ -58,6 +58,11 @@ class TransportCoeffs(ctypes.Structure):
     _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl), ("cau", _c_int)]
 
 
+class TTCoeffs(ctypes.Structure):
+    """fg_tt_coeffs: transport coefficients plus Alpha and DeltaT."""
+    _fields_ = [("c", TransportCoeffs), ("alpha", _c_dbl), ("dt", _c_dbl)]
+
+
 class ProcessStats(ctypes.Structure):
     _fields_ = [("nonlinear_iterations", _c_int), ("gmres_iterations", _c_int), ("seconds", _c_dbl),
                 ("true_rel_residual", _c_dbl), ("nonlinear_residual", _c_dbl)]
@@ -155,6 +160,9 @@ def lib(build_if_missing: bool = True):
     L.fg_euler_assemble.argtypes = [_vp, ctypes.POINTER(EulerCoeffs), _vp, _vp, _vp]
     L.fg_euler_predictor.argtypes = [_vp, ctypes.POINTER(EulerCoeffs), ctypes.POINTER(SolverOpts),
                                      ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
+    L.fg_tt_assemble.argtypes = [_vp, ctypes.POINTER(TTCoeffs), _vp, _vp, _vp]
+    L.fg_tt_predictor.argtypes = [_vp, ctypes.POINTER(TTCoeffs), ctypes.POINTER(SolverOpts),
+                                  ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
     L.fg_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerOpts)]
     L.fg_server_submit.argtypes = [_vp, _vp, ctypes.POINTER(TransportCoeffs), ctypes.c_ulonglong]
     L.fg_server_submit_euler.argtypes = [_vp, _vp, ctypes.POINTER(EulerCoeffs), ctypes.POINTER(TimeOpts), _f64p,
@@ -375,6 +383,29 @@ class System:
                                   ctypes.byref(st)))
         return u, {k: getattr(st, k) for k, _ in st._fields_}
 
+    # ---- transient transport (ndof = 1, geometry from set_geometry)
+    def tt_assemble(self, prob, alpha, dt, u=None, du=None):
+        """Build_M_K_R_SUPG at (u, du); returns R (n+1); blocks stay on the device."""
+        c = tt_coeffs(prob, alpha, dt)
+        R = np.empty(self.n + 1)
+        uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
+        dd = None if du is None else np.ascontiguousarray(du, dtype=np.float64)
+        check(lib().fg_tt_assemble(self._h, ctypes.byref(c), _ptr(uu), _ptr(dd), R.ctypes.data))
+        return R
+
+    def tt_predictor(self, prob, alpha, dt, topts, u0=None, kmax=30, lmax=1000, tol=1e-10,
+                     precision=FG_PREC_FP64, inner_tol=0.0):
+        """Predictor_Old with the transient transport build; returns (u, a, stats)."""
+        c = tt_coeffs(prob, alpha, dt)
+        o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+        u = np.zeros(self.n) if u0 is None else np.array(u0, dtype=np.float64, copy=True)
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        a = np.zeros(self.n)
+        st = TimeStats()
+        check(lib().fg_tt_predictor(self._h, ctypes.byref(c), ctypes.byref(o), ctypes.byref(topts), u,
+                                    a.ctypes.data, ctypes.byref(st)))
+        return u, a, {k: getattr(st, k) for k, _ in st._fields_}
+
     # ---- compressible Euler (ndof = 4)
     def euler_set_geometry(self, prob):
         check(lib().fg_euler_set_geometry(self._h, np.ascontiguousarray(self.mesh.x, dtype=np.float64),
@@ -402,6 +433,11 @@ class System:
         check(lib().fg_euler_predictor(self._h, ctypes.byref(c), ctypes.byref(o), ctypes.byref(topts), u,
                                        a.ctypes.data, ctypes.byref(st)))
         return u, a, {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def tt_coeffs(prob, alpha, dt) -> TTCoeffs:
+    """Transient transport coefficients of a transport problem."""
+    return TTCoeffs(_coeffs(prob), float(alpha), float(dt))
 
 
 def euler_coeffs(prob) -> EulerCoeffs:

@@ -1,0 +1,70 @@
+"""The transient transport restatement (oracle/tt.c: Build_M_K_R_SUPG.c and
+the Predictor_Old loop with Diag).  The reference's transient driver does
+not compile here (TranspEquation.h:8 includes an MPI header by absolute
+path), so the restatement is pinned through the steady build, which is
+pinned bit-exactly against the reference (tests/test_oracle_golden.py and
+the reference build): the stiffness part of the transient block equals the
+steady block, the load part of the transient residual equals the steady
+right-hand side, and the time loop keeps exact constant solutions and
+reaches the steady solution."""
+import numpy as np
+import pytest
+
+import oracle as O
+from parallel_fem_codes_gb300 import meshgen as G
+
+
+def test_stiffness_part_equals_steady_block():
+    p = G.transport_problem(17, angle_deg=35.0, k=1e-3, gamma=0.2, f=0.5)
+    u = np.random.default_rng(0).random(p.mesh.neq)
+    K, _ = O.build_k_f_supg(p, u)
+    A1, _ = O.build_tt(p, 0.5, 2.0, u=u)        # me + 1 * ke
+    A2, _ = O.build_tt(p, 0.5, 4.0, u=u)        # me + 2 * ke
+    scale = np.abs(K).max()
+    assert np.abs((A2 - A1) - K).max() <= 1e-13 * scale
+    # the mass part (A1 - K) is the consistent P1 mass plus the SUPG term
+    me = 2 * A1 - A2
+    assert np.all(np.abs(me).max(axis=1) > 0)
+
+
+def test_load_part_equals_steady_rhs():
+    """u = 0, du = 0, zero Dirichlet data: R is the SUPG load, which the
+    steady build assembles the same way (no lifting when the data are 0)."""
+    p = G.transport_problem(17, angle_deg=10.0, k=1e-4, f=1.0, upmode=1, upval=0.0)
+    _, F = O.build_k_f_supg(p)
+    _, R = O.build_tt(p, 0.5, 0.1)
+    assert np.array_equal(R[:-1], F[:-1]) and R[-1] == 0.0
+
+
+def test_residual_of_du_is_mass_times_du():
+    """Linear in du: R(u, du) - R(u, 0) = -me du, with the element order of
+    the reference's accumulation (checked to rounding)."""
+    p = G.transport_problem(9, angle_deg=60.0, k=1e-2, cau=False)
+    rng = np.random.default_rng(3)
+    u = rng.random(p.mesh.neq)
+    du = rng.random(p.mesh.neq)
+    _, R0 = O.build_tt(p, 0.5, 0.1, u=u)
+    _, R1 = O.build_tt(p, 0.5, 0.1, u=u, du=du)
+    A1, _ = O.build_tt(p, 0.5, 2.0, u=u)
+    A2, _ = O.build_tt(p, 0.5, 4.0, u=u)
+    me = 2 * A1 - A2
+    lm = O.fill_lm(p.mesh)
+    Mdu = O.ebemv(lm, me, p.mesh.neq, np.append(du, 0.0))
+    assert np.abs((R0 - R1)[:-1] - Mdu[:-1]).max() <= 1e-12 * np.abs(Mdu).max()
+
+
+def test_constant_state_is_kept():
+    """u = c everywhere with f = gamma c is a steady solution (TESTE)."""
+    c, gamma = 2.5, 0.3
+    p = G.transport_problem(17, angle_deg=30.0, k=1e-3, gamma=gamma, f=gamma * c, upmode=1, upval=c)
+    u0 = np.full(p.mesh.neq, c)
+    u, a, st = O.tt_predictor(p, 0.5, 0.01, O.TimeOpts(0, 2, 1e-3, 0, 0.05, 1e-6, 0), u0=u0)
+    assert st["steps"] == 5
+    assert np.abs(u - c).max() <= 1e-10 and np.abs(a).max() <= 1e-8
+
+
+def test_reaches_the_steady_solution():
+    p = G.transport_problem(17, angle_deg=30.0, k=1e-2, cau=False)
+    Us, nl, its = O.transport_process(p, 1e-12, 1e-3, 30, 1000)
+    u, a, st = O.tt_predictor(p, 0.5, 0.05, O.TimeOpts(1, 5, 1e-6, 1, 1e3, 1e-9, 0), tol=1e-12)
+    assert np.linalg.norm(u - Us[: p.mesh.neq]) / np.linalg.norm(Us[: p.mesh.neq]) < 1e-6
