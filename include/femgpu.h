@@ -61,6 +61,23 @@ int fg_system_create(fg_system **out, int nnodes, int nel, int ndof,
                      const int *ien, const int *type, const int *invp, int neq,
                      int reorder);
 
+/* ---- mesh files (host only, no device needed) ----
+ * fg_mesh_read: a global mesh file as Mesh_Generator/Structured_Mesh/
+ * meshGenerator.c:184-209 writes it (per node x, y and one free(1)/
+ * prescribed(0) flag per dof; elements v0 v1 v2, with a trailing tag when
+ * ndof > 1); equations numbered over the free dofs in node order.
+ * fg_mesh_read_rank: a one-rank partition file as SST/Preprocess.c:127-168
+ * reads it (per node x, y and per dof Type [Send invP_id]); the file's
+ * invP_id numbering is kept.  Call once with NULL arrays for the sizes in
+ * *info, then with x, y[nnodes], type, invp[nnodes*ndof], ien[nel*3]; the
+ * arrays feed fg_system_create.  Replaces the partitioner's one-rank output
+ * (Parallel_Preprocess) for single-GPU runs. */
+typedef struct { int nnodes, nel, neq; } fg_mesh_info;
+int fg_mesh_read(const char *path, int ndof, fg_mesh_info *info, double *x, double *y, int *type, int *invp,
+                 int *ien);
+int fg_mesh_read_rank(const char *path, int ndof, fg_mesh_info *info, double *x, double *y, int *type, int *invp,
+                      int *ien);
+
 /* Host-only set-up products of a mesh (no device needed): lm[nel*3*ndof]
  * (Fill_LM), Perm/invPerm[neq+1] (Permutation_of_LM with SYMRCM),
  * colour[nel] (greedy element colouring; -1 for an element without a free

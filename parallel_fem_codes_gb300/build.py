@@ -23,6 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # contraction) so assembly and preconditioner set-up match the reference.
 UNITS = [
     ("topology.cpp", []),
+    ("meshio.cpp", []),
     ("system.cu", []),
     ("krylov.cu", []),
     ("setup.cu", ["-fmad=false"]),

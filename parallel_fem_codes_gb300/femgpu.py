@@ -63,6 +63,10 @@ class TTCoeffs(ctypes.Structure):
     _fields_ = [("c", TransportCoeffs), ("alpha", _c_dbl), ("dt", _c_dbl)]
 
 
+class MeshInfo(ctypes.Structure):
+    _fields_ = [("nnodes", _c_int), ("nel", _c_int), ("neq", _c_int)]
+
+
 class ProcessStats(ctypes.Structure):
     _fields_ = [("nonlinear_iterations", _c_int), ("gmres_iterations", _c_int), ("seconds", _c_dbl),
                 ("true_rel_residual", _c_dbl), ("nonlinear_residual", _c_dbl)]
@@ -160,6 +164,8 @@ def lib(build_if_missing: bool = True):
     L.fg_euler_assemble.argtypes = [_vp, ctypes.POINTER(EulerCoeffs), _vp, _vp, _vp]
     L.fg_euler_predictor.argtypes = [_vp, ctypes.POINTER(EulerCoeffs), ctypes.POINTER(SolverOpts),
                                      ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
+    for name in ("fg_mesh_read", "fg_mesh_read_rank"):
+        getattr(L, name).argtypes = [ctypes.c_char_p, _c_int, ctypes.POINTER(MeshInfo), _vp, _vp, _vp, _vp, _vp]
     L.fg_tt_assemble.argtypes = [_vp, ctypes.POINTER(TTCoeffs), _vp, _vp, _vp]
     L.fg_tt_predictor.argtypes = [_vp, ctypes.POINTER(TTCoeffs), ctypes.POINTER(SolverOpts),
                                   ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
@@ -183,6 +189,24 @@ def check(code: int) -> None:
 
 def _ptr(a):
     return None if a is None else a.ctypes.data
+
+
+def read_mesh(path, ndof=1, rank_file=False):
+    """A mesh file of the reference through the library's reader: a global
+    mesh as the structured mesh generator writes it, or (rank_file=True) a
+    one-rank partition file.  Returns a meshgen.Mesh."""
+    from . import meshgen
+    fn = lib().fg_mesh_read_rank if rank_file else lib().fg_mesh_read
+    info = MeshInfo()
+    p = os.fsencode(path)
+    check(fn(p, ndof, ctypes.byref(info), None, None, None, None, None))
+    x, y = np.empty(info.nnodes), np.empty(info.nnodes)
+    t = np.empty(info.nnodes * ndof, dtype=np.int32)
+    iv = np.empty(info.nnodes * ndof, dtype=np.int32)
+    ien = np.empty(info.nel * 3, dtype=np.int32)
+    check(fn(p, ndof, ctypes.byref(info), x.ctypes.data, y.ctypes.data, t.ctypes.data, iv.ctypes.data,
+             ien.ctypes.data))
+    return meshgen.Mesh(x=x, y=y, ien=ien.reshape(-1, 3), ndof=ndof, type=t, invp=iv, neq=info.neq)
 
 
 def mesh_analyze(mesh, reorder: bool = True) -> dict:

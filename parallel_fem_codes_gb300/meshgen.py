@@ -313,3 +313,22 @@ def obliquo_problem(n_nodes_side: int, mach=2.0, dimensionless=True, alpha=0.5, 
     if dt is None:
         dt = euler_dt(mesh, 1.4, state, 0.5)
     return euler_problem(mesh, 1.4, mach, dimensionless, tolerance, alpha, dt, coef, True, state)
+
+
+def write_rank_file(mesh: Mesh, path: str) -> None:
+    """A one-rank partition file (the format SST/Preprocess.c:127-168 reads):
+    per node x, y and per dof Type [Send invP_id] (Send = 1: nothing to
+    exchange), then the elements."""
+    with open(path, "w") as f:
+        f.write(f"{mesh.nnodes}\n")
+        for i in range(mesh.nnodes):
+            f.write(f"{mesh.x[i]:.14f}\t{mesh.y[i]:.14f}\t")
+            for k in range(mesh.ndof):
+                q = i * mesh.ndof + k
+                t = int(mesh.type[q])
+                f.write(f"{t}\t" if t == 0 else f"{t}\t1\t{int(mesh.invp[q])}\t")
+            f.write("\n")
+        f.write(f"{mesh.nel}\n")
+        for e in range(mesh.nel):
+            f.write(" ".join(str(int(v)) for v in mesh.ien[e]) + "\n")
+
