@@ -161,6 +161,18 @@ enum {
     FG_SETUP_REF_QUIRKS = 2  /* 4x4 block inverse with the reference's entry-14
                                 term (BlockDiag_precond_EBE_setup.c:142)      */
 };
+/* ---- diagonal scaling (Solvers_and_Preconditioners/scaling.c) ----
+ * FG_SCALE_LEFT: Left_scaling_EBE (:10-42): the accumulating Diag set-up on
+ * F (F /= Diag), then every block row times 1/Diag of its equation.
+ * FG_SCALE_LEFTRIGHT: LeftRight_scaling_EBE (:92-121): entries times
+ * sqrt(1/Diag_I 1/Diag_J), F = (F / Diag) sqrt(Diag); solve, then
+ * fg_unscale (Left_unscaling, :187-196: X *= sqrt(1/Diag)).  F: host n+1,
+ * in place, may be NULL.  The system's preconditioner becomes
+ * FG_PRECOND_NONE (set another one up afterwards if wanted). */
+enum { FG_SCALE_LEFT = 1, FG_SCALE_LEFTRIGHT = 2 };
+int fg_scale(fg_system *s, int kind, double *F);
+int fg_unscale(fg_system *s, double *X);
+
 /* Build the preconditioner from the current blocks and, when F is not NULL,
  * precondition F in place (n+1 host entries), as the *_EBE_setup routines
  * do.  The right-hand side the solver receives is then M^-1 F. */

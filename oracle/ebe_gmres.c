@@ -82,6 +82,40 @@ void or_diag_setup(int nel, int S, const int *lm, const double *A, int NEQ,
     for (I = 0; I < NEQ; I++) F[I] *= invDiag[I];
 }
 
+/* Left_scaling_EBE (Solvers_and_Preconditioners/scaling.c:10-42): the
+ * accumulating Diag set-up on F, invDiag[NEQ] = invDiag[NEQ-1] (the
+ * value the last rank broadcasts for the sink), then every block row
+ * times invDiag of its equation.  One rank. */
+void or_scale_left(int nel, int S, const int *lm, double *A, int NEQ, double *Diag, double *invDiag, double *F)
+{
+    int E, I, J;
+    or_diag_setup(nel, S, lm, A, NEQ, Diag, invDiag, F);
+    invDiag[NEQ] = invDiag[NEQ - 1];
+    for (E = 0; E < nel; E++)
+        for (I = 0; I < S; I++)
+            for (J = 0; J < S; J++) A[(long)S*S*E + S*I + J] *= invDiag[lm[(long)S*E + I]];
+}
+
+/* LeftRight_scaling_EBE (scaling.c:92-121): A_IJ *= sqrt(invDiag_I
+ * invDiag_J), F = (F / d) * sqrt(d); the solution is unscaled by
+ * Left_unscaling (scaling.c:187-196): x *= sqrt(invDiag). */
+void or_scale_leftright(int nel, int S, const int *lm, double *A, int NEQ, double *Diag, double *invDiag, double *F)
+{
+    int E, I, J;
+    or_diag_setup(nel, S, lm, A, NEQ, Diag, invDiag, F);
+    invDiag[NEQ] = invDiag[NEQ - 1];
+    for (E = 0; E < nel; E++)
+        for (I = 0; I < S; I++)
+            for (J = 0; J < S; J++)
+                A[(long)S*S*E + S*I + J] *= sqrt(invDiag[lm[(long)S*E + I]] * invDiag[lm[(long)S*E + J]]);
+    for (I = 0; I < NEQ; I++) F[I] *= sqrt(Diag[I]);
+}
+
+void or_unscale(int NEQ, const double *invDiag, double *x)
+{
+    for (int I = 0; I < NEQ; I++) x[I] *= sqrt(invDiag[I]);
+}
+
 /* Diag_precond (Solvers_and_Preconditioners/Diag_precond.c:3-15). */
 void or_diag_apply(int n, const double *invDiag, const double *p, double *z)
 {

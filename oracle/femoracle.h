@@ -68,6 +68,11 @@ void or_ebemv(int nel, int S, const int *lm, const double *A, int NEQ,
 void or_diag_setup(int nel, int S, const int *lm, const double *A, int NEQ,
                    double *Diag, double *invDiag, double *F);
 void or_diag_apply(int n, const double *invDiag, const double *p, double *z);
+/* Left / LeftRight scaling of an EBE system (scaling.c:10-42, 92-121) on
+ * the accumulating Diag; or_unscale is Left_unscaling (scaling.c:187-196). */
+void or_scale_left(int nel, int S, const int *lm, double *A, int NEQ, double *Diag, double *invDiag, double *F);
+void or_scale_leftright(int nel, int S, const int *lm, double *A, int NEQ, double *Diag, double *invDiag, double *F);
+void or_unscale(int NEQ, const double *invDiag, double *x);
 
 /* Nodal block-diagonal (B = NDOF = 3 or 4): gather the B x B diagonal blocks
  * of every element node (EBE/BlockDiag_precond_EBE_setup.c:57-80,

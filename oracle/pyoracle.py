@@ -702,3 +702,29 @@ class Spike:
         if getattr(self, "_h", None):
             self._L.or_spike_free(self._h)
             self._h = None
+
+
+def scale(lm, A, NEQ, F, kind, Diag=None):
+    """Left ("Left") or LeftRight ("LeftRight") scaling of an EBE system;
+    returns (A scaled, F scaled, Diag, invDiag[NEQ+1])."""
+    L = lib()
+    fn = L.or_scale_left if kind == "Left" else L.or_scale_leftright
+    fn.argtypes = [_c_int, _c_int, _i32p, _f64p, _c_int, _f64p, _f64p, _f64p]
+    fn.restype = None
+    nel, S = lm.shape
+    A = np.array(A, dtype=np.float64, copy=True).reshape(-1)
+    F = np.array(F, dtype=np.float64, copy=True)
+    D = np.zeros(NEQ + 1) if Diag is None else np.array(Diag, dtype=np.float64, copy=True)
+    inv = np.zeros(NEQ + 1)
+    fn(nel, S, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1), A, NEQ, D, inv, F)
+    return A.reshape(nel, S * S), F, D, inv
+
+
+def unscale(invDiag, x):
+    L = lib()
+    L.or_unscale.argtypes = [_c_int, _f64p, _f64p]
+    L.or_unscale.restype = None
+    x = np.array(x, dtype=np.float64, copy=True)
+    L.or_unscale(invDiag.shape[0] - 1, np.ascontiguousarray(invDiag, dtype=np.float64), x)
+    return x
+

@@ -268,6 +268,69 @@ int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaS
     return FG_ERR_ARG;
 }
 
+// ---------------------------------------------------------------- diagonal scaling
+// Left_scaling_EBE / LeftRight_scaling_EBE (scaling.c:10-42, 92-121) on the
+// blocks of the internal element order: row I of element e times invDiag of
+// its equation (left), or entry (I, J) times sqrt(invDiag_I invDiag_J)
+// (left-right); the sink n reads invDiag[n], which the caller set to the
+// reference's invDiag[NEQ] = invDiag[NEQ - 1].
+__global__ void k_scale_blocks(int nel, int ld, int S, const int *__restrict__ lm, const double *__restrict__ invd,
+                               int both, double *__restrict__ A64)
+{
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    for (int I = 0; I < S; ++I) {
+        const double dI = invd[lm[(size_t)I * ld + pos]];
+        for (int J = 0; J < S; ++J) {
+            double &a = A64[(size_t)(I * S + J) * ld + pos];
+            if (both) a *= sqrt(dI * invd[lm[(size_t)J * ld + pos]]);
+            else a *= dI;
+        }
+    }
+}
+
+// x[i] *= sqrt(v[i]) for i < n (F of the left-right scaling with v = Diag;
+// Left_unscaling, scaling.c:187-196, with v = invDiag)
+__global__ void k_mul_sqrt(int n, const double *__restrict__ v, double *__restrict__ x)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] *= sqrt(v[i]);
+}
+
+int scale_device(fg_system *s, int kind, double *F_dev, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (!s->blocks_ok) { set_error("scaling before element blocks were set"); return FG_ERR_STATE; }
+    if (kind != FG_SCALE_LEFT && kind != FG_SCALE_LEFTRIGHT) { set_error("unknown scaling"); return FG_ERR_ARG; }
+    int r;
+    if ((r = precond_setup_device(s, FG_PRECOND_DIAG, FG_SETUP_ACCUMULATE, F_dev, st))) return r;
+    double *invd = s->invd64.as<double>();
+    if (t.n > 0)                                      // invDiag[NEQ] = invDiag[NEQ - 1] (reference numbering)
+        FG_CUDA(cudaMemcpyAsync(invd + t.n, invd + t.iperm[t.n - 1], sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (t.nel > 0)
+        k_scale_blocks<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, t.S, s->lm.as<int>(), invd,
+                                                           kind == FG_SCALE_LEFTRIGHT, s->A64.as<double>());
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    if (kind == FG_SCALE_LEFTRIGHT && F_dev && t.n > 0) {
+        k_mul_sqrt<<<(t.n + 255) / 256, 256, 0, st>>>(t.n, s->diag.as<double>(), F_dev);
+        FG_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
+    s->precond = FG_PRECOND_NONE;                    // the scaled system is solved as it stands
+    s->csr_dirty = true;
+    return convert_blocks(s, st);
+}
+
+int unscale_device(fg_system *s, double *x_dev, cudaStream_t st)
+{
+    const int n = s->topo.n;
+    if (n > 0) k_mul_sqrt<<<(n + 255) / 256, 256, 0, st>>>(n, s->invd64.as<double>(), x_dev);
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    return FG_OK;
+}
+
 __global__ void k_diag_apply(const double *__restrict__ invd, int n, const double *p, double *z)
 {
     int d = blockIdx.x * blockDim.x + threadIdx.x;

@@ -334,6 +334,38 @@ int fg_precond_setup(fg_system *s, int kind, int flags, double *F)
     return FG_OK;
 }
 
+int fg_scale(fg_system *s, int kind, double *F)
+{
+    if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    double *fd = nullptr;
+    if (F) {
+        if ((r = vec_in(s, F, s->ws.u64.as<double>(), s->ws.r64.as<double>()))) return r;
+        fd = s->ws.u64.as<double>();
+    }
+    if ((r = scale_device(s, kind, fd, s->stream))) return r;
+    if (F && (r = vec_out(s, fd, F, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_unscale(fg_system *s, double *X)
+{
+    if (!s || !X) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = vec_in(s, X, s->ws.u64.as<double>(), s->ws.r64.as<double>()))) return r;
+    if ((r = unscale_device(s, s->ws.u64.as<double>(), s->stream))) return r;
+    if ((r = vec_out(s, s->ws.u64.as<double>(), X, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
 int fg_precond_apply(fg_system *s, const double *p, double *z)
 {
     if (!s || !p || !z) { set_error("NULL argument"); return FG_ERR_ARG; }

@@ -212,6 +212,9 @@ int euler_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *
 int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaStream_t st);
 int precond_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st);
 int convert_blocks(fg_system *s, cudaStream_t st);
+// Left / left-right diagonal scaling of the blocks and F (internal numbering)
+int scale_device(fg_system *s, int kind, double *F_dev, cudaStream_t st);
+int unscale_device(fg_system *s, double *x_dev, cudaStream_t st);
 int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c,
                               const double *u_dev, double *F_dev, cudaStream_t st);
 // Gathers / scatters between reference and internal numbering (n+1 vectors)

@@ -16,6 +16,7 @@ from . import build as _build
 
 FG_OK = 0
 FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG, FG_PRECOND_ILU0, FG_PRECOND_SPIKE = 0, 1, 2, 3, 4
+FG_SCALE_LEFT, FG_SCALE_LEFTRIGHT = 1, 2
 FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED = 64, 32
@@ -166,6 +167,8 @@ def lib(build_if_missing: bool = True):
                                      ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
     for name in ("fg_mesh_read", "fg_mesh_read_rank"):
         getattr(L, name).argtypes = [ctypes.c_char_p, _c_int, ctypes.POINTER(MeshInfo), _vp, _vp, _vp, _vp, _vp]
+    L.fg_scale.argtypes = [_vp, _c_int, _vp]
+    L.fg_unscale.argtypes = [_vp, _vp]
     L.fg_tt_assemble.argtypes = [_vp, ctypes.POINTER(TTCoeffs), _vp, _vp, _vp]
     L.fg_tt_predictor.argtypes = [_vp, ctypes.POINTER(TTCoeffs), ctypes.POINTER(SolverOpts),
                                   ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
@@ -326,6 +329,17 @@ class System:
         Fc = None if F is None else np.array(F, dtype=np.float64, copy=True)
         check(lib().fg_precond_setup(self._h, kind, flags, _ptr(Fc)))
         return Fc
+
+    def scale(self, kind, F=None):
+        """Left or left-right diagonal scaling of the blocks; returns scaled F."""
+        Fc = None if F is None else np.array(F, dtype=np.float64, copy=True)
+        check(lib().fg_scale(self._h, kind, _ptr(Fc)))
+        return Fc
+
+    def unscale(self, X):
+        Xc = np.array(X, dtype=np.float64, copy=True)
+        check(lib().fg_unscale(self._h, Xc.ctypes.data))
+        return Xc
 
     def precond_apply(self, p):
         p = np.ascontiguousarray(p, dtype=np.float64)
