@@ -78,6 +78,19 @@ int fg_mesh_read(const char *path, int ndof, fg_mesh_info *info, double *x, doub
 int fg_mesh_read_rank(const char *path, int ndof, fg_mesh_info *info, double *x, double *y, int *type, int *invp,
                       int *ien);
 
+/* Paraview output (the drivers' 01_CommonFiles/Paraview_Output.c): an ASCII
+ * VTK UnstructuredGrid of the triangles with the fields as point data, in
+ * order.  values are node-major [nnodes*ncomp], ncomp 1..3 (a 2-component
+ * field is written with a third component 0).  z lifts the points (the
+ * transport drivers write (x, y, u)); NULL writes z = 0.  Host only. */
+typedef struct {
+    const char *name;
+    int ncomp;
+    const double *values;
+} fg_vtu_field;
+int fg_write_vtu(const char *path, int nnodes, int nel, const double *x, const double *y, const int *ien,
+                 int nfields, const fg_vtu_field *fields, const double *z);
+
 /* Host-only set-up products of a mesh (no device needed): lm[nel*3*ndof]
  * (Fill_LM), Perm/invPerm[neq+1] (Permutation_of_LM with SYMRCM),
  * colour[nel] (greedy element colouring; -1 for an element without a free

@@ -132,4 +132,65 @@ int fg_mesh_read_rank(const char *path, int ndof, fg_mesh_info *info, double *x,
     return r ? r : deliver(m, info, x, y, type, invp, ien);
 }
 
+// Paraview output, one writer for the drivers' Paraview_Output.c files:
+//   SST  01_CommonFiles/Paraview_Output.c:22-111   "solucao", points (x, y, u)
+//   Euler 01_CommonFiles/Paraview_Output.c:61-114  Density, Temperature, Pressure
+//   NS   01_CommonFiles/Paraview_Output.c:83-134   Velocity (3 components), Pressure
+// an ASCII VTK UnstructuredGrid of the triangles (cell type 5, offsets 3(e+1))
+// with the given point data in order; z lifts the points (the transport
+// drivers' 3-D view) or is NULL for z = 0.  A 2-component field is written
+// with a third component 0, as the NS writer writes the velocity.
+int fg_write_vtu(const char *path, int nnodes, int nel, const double *x, const double *y, const int *ien,
+                 int nfields, const fg_vtu_field *fields, const double *z)
+{
+    if (!path || !x || !y || !ien || (nfields > 0 && !fields)) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (nnodes < 0 || nel < 0 || nfields < 0) { set_error("invalid sizes"); return FG_ERR_ARG; }
+    for (int k = 0; k < nfields; ++k)
+        if (!fields[k].name || !fields[k].values || fields[k].ncomp < 1 || fields[k].ncomp > 3) {
+            set_error("field " + std::to_string(k) + ": a name, values and 1..3 components are required");
+            return FG_ERR_ARG;
+        }
+    for (size_t q = 0; q < (size_t)nel * 3; ++q)
+        if (ien[q] < 0 || ien[q] >= nnodes) { set_error("element vertex out of range"); return FG_ERR_ARG; }
+    FILE *f = std::fopen(path, "w");
+    if (!f) { set_error(std::string("cannot open ") + path + " for writing"); return FG_ERR_ARG; }
+    std::fprintf(f, "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"BigEndian\">\n");
+    std::fprintf(f, "\t<UnstructuredGrid>\n");
+    std::fprintf(f, "\t\t<Piece NumberOfPoints=\"%d\" NumberOfCells=\"%d\">\n", nnodes, nel);
+    std::fprintf(f, "\t\t\t<PointData Scalars=\"scalars\">\n");
+    for (int k = 0; k < nfields; ++k) {
+        const fg_vtu_field &fd = fields[k];
+        const int nc = fd.ncomp;
+        if (nc == 1) {
+            std::fprintf(f, "\t\t\t\t<DataArray type=\"Float32\" Name=\"%s\" Format=\"ascii\">\n", fd.name);
+            for (int i = 0; i < nnodes; ++i) std::fprintf(f, "\t\t\t\t   %.12f\n", fd.values[i]);
+        } else {
+            std::fprintf(f, "\t\t\t\t<DataArray type=\"Float32\" Name=\"%s\" NumberOfComponents=\"3\" Format=\"ascii\">\n",
+                         fd.name);
+            for (int i = 0; i < nnodes; ++i) {
+                const double *v = fd.values + (size_t)i * nc;
+                std::fprintf(f, "\t\t\t\t   %.12f   %.12f   %.12f\n", v[0], v[1], nc == 3 ? v[2] : 0.0);
+            }
+        }
+        std::fprintf(f, "\t\t\t\t</DataArray>\n");
+    }
+    std::fprintf(f, "\t\t\t</PointData>\n\t\t\t<Points>\n");
+    std::fprintf(f, "\t\t\t\t<DataArray type=\"Float32\" NumberOfComponents=\"3\" Format=\"ascii\">\n");
+    for (int i = 0; i < nnodes; ++i)
+        std::fprintf(f, "\t\t\t\t   %.12f\t%.12f\t%.12f\n", x[i], y[i], z ? z[i] : 0.0);
+    std::fprintf(f, "\t\t\t\t</DataArray>\n\t\t\t</Points>\n\t\t\t<Cells>\n");
+    std::fprintf(f, "\t\t\t\t<DataArray type=\"Int32\" Name=\"connectivity\" Format=\"ascii\">\n");
+    for (int e = 0; e < nel; ++e)
+        std::fprintf(f, "\t\t\t\t   %d\t%d\t%d\n", ien[3 * (size_t)e], ien[3 * (size_t)e + 1], ien[3 * (size_t)e + 2]);
+    std::fprintf(f, "\t\t\t\t</DataArray>\n\t\t\t\t<DataArray type=\"Int32\" Name=\"offsets\" Format=\"ascii\">\n");
+    for (int e = 0; e < nel; ++e) std::fprintf(f, "\t\t\t\t   %d\n", (e + 1) * 3);
+    std::fprintf(f, "\t\t\t\t</DataArray>\n\t\t\t\t<DataArray type=\"Int32\" Name=\"types\" Format=\"ascii\">\n");
+    for (int e = 0; e < nel; ++e) std::fprintf(f, "\t\t\t\t   %d\n", 5);
+    std::fprintf(f, "\t\t\t\t</DataArray>\n\t\t\t</Cells>\n\t\t</Piece>\n\t</UnstructuredGrid>\n</VTKFile>\n");
+    const bool ok = std::ferror(f) == 0;
+    std::fclose(f);
+    if (!ok) { set_error(std::string("write error on ") + path); return FG_ERR_ARG; }
+    return FG_OK;
+}
+
 }  // extern "C"

@@ -167,6 +167,7 @@ def lib(build_if_missing: bool = True):
                                      ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
     for name in ("fg_mesh_read", "fg_mesh_read_rank"):
         getattr(L, name).argtypes = [ctypes.c_char_p, _c_int, ctypes.POINTER(MeshInfo), _vp, _vp, _vp, _vp, _vp]
+    L.fg_write_vtu.argtypes = [ctypes.c_char_p, _c_int, _c_int, _vp, _vp, _vp, _c_int, _vp, _vp]
     L.fg_scale.argtypes = [_vp, _c_int, _vp]
     L.fg_unscale.argtypes = [_vp, _vp]
     L.fg_tt_assemble.argtypes = [_vp, ctypes.POINTER(TTCoeffs), _vp, _vp, _vp]
@@ -210,6 +211,60 @@ def read_mesh(path, ndof=1, rank_file=False):
     check(fn(p, ndof, ctypes.byref(info), x.ctypes.data, y.ctypes.data, t.ctypes.data, iv.ctypes.data,
              ien.ctypes.data))
     return meshgen.Mesh(x=x, y=y, ien=ien.reshape(-1, 3), ndof=ndof, type=t, invp=iv, neq=info.neq)
+
+
+class _VtuField(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char_p), ("ncomp", ctypes.c_int), ("values", ctypes.c_void_p)]
+
+
+def write_vtu(path, mesh, fields, z=None):
+    """Paraview output: `fields` maps a name to node values (nnodes) or
+    (nnodes, ncomp) with ncomp <= 3, written in order; `z` lifts the points."""
+    keep = []
+    arr = (_VtuField * max(len(fields), 1))()
+    for k, (name, vals) in enumerate(fields.items()):
+        v = np.ascontiguousarray(vals, dtype=np.float64)
+        if v.shape[0] != mesh.nnodes:
+            raise ValueError(f"field {name}: {v.shape[0]} values for {mesh.nnodes} nodes")
+        keep.append(v)
+        arr[k] = _VtuField(name.encode(), 1 if v.ndim == 1 else v.shape[1], v.ctypes.data)
+    x = np.ascontiguousarray(mesh.x, dtype=np.float64)
+    y = np.ascontiguousarray(mesh.y, dtype=np.float64)
+    ien = np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1)
+    zz = None if z is None else np.ascontiguousarray(z, dtype=np.float64)
+    check(lib().fg_write_vtu(os.fsencode(path), mesh.nnodes, mesh.nel, x.ctypes.data, y.ctypes.data, ien.ctypes.data,
+                             len(fields), ctypes.addressof(arr), None if zz is None else zz.ctypes.data))
+
+
+def node_values(mesh, u, upresc):
+    """Per-node dof values (nnodes x ndof, squeezed for ndof = 1): free dofs
+    from the solution u (invP_id numbering), prescribed ones from upresc, as
+    every Paraview_Output.c gathers them before writing."""
+    u = np.asarray(u, dtype=np.float64)
+    up = np.asarray(upresc, dtype=np.float64).reshape(-1)
+    v = np.where(mesh.type > 0, u[np.maximum(mesh.invp, 0)], up)
+    return v if mesh.ndof == 1 else v.reshape(mesh.nnodes, mesh.ndof)
+
+
+def write_transport_vtu(path, prob, u):
+    """SST / transient transport output: "solucao" with points lifted by u."""
+    v = node_values(prob.mesh, u, prob.upresc)
+    write_vtu(path, prob.mesh, {"solucao": v}, z=v)
+
+
+def write_euler_vtu(path, prob, U, cv=716.5):
+    """Euler output: Density, Temperature, Pressure from the conserved
+    variables (rho, rho u, rho v, rho E); cv is the problem's cv(x, y)."""
+    V = node_values(prob.mesh, U, prob.upresc)
+    rho, m1, m2, e = V[:, 0], V[:, 1], V[:, 2], V[:, 3]
+    aux = e - (m1 * m1 + m2 * m2) / (2.0 * rho)
+    write_vtu(path, prob.mesh, {"Density": rho, "Temperature": aux / (rho * cv), "Pressure": (prob.gamma - 1) * aux})
+
+
+def write_ns_vtu(path, prob, U):
+    """Navier-Stokes output: Velocity (u, v, 0) and Pressure."""
+    V = node_values(prob.mesh, U, prob.upresc)
+    write_vtu(path, prob.mesh, {"Velocity": V[:, :2], "Pressure": V[:, 2]})
 
 
 def mesh_analyze(mesh, reorder: bool = True) -> dict:

@@ -63,3 +63,65 @@ def test_rank_file_of_another_rank_is_refused(fg, tmp_path):
         fg.read_mesh(path, rank_file=True)
     with pytest.raises(fg.FemGpuError):
         fg.read_mesh(str(tmp_path / "missing.dat"))
+
+
+def _vtu_arrays(path):
+    import xml.etree.ElementTree as ET
+    piece = ET.parse(path).getroot().find("UnstructuredGrid/Piece")
+    pd = {d.get("Name"): np.array(d.text.split(), dtype=float) for d in piece.find("PointData")}
+    pts = np.array(piece.find("Points/DataArray").text.split(), dtype=float).reshape(-1, 3)
+    cells = {d.get("Name"): np.array(d.text.split(), dtype=int) for d in piece.find("Cells")}
+    return piece, pd, pts, cells
+
+
+def test_vtu_transport_output(fg, tmp_path):
+    p = G.transport_problem(9)
+    m = p.mesh
+    u = np.linspace(0.1, 0.9, m.neq)
+    path = str(tmp_path / "out.vtu")
+    fg.write_transport_vtu(path, p, u)
+    piece, pd, pts, cells = _vtu_arrays(path)
+    assert int(piece.get("NumberOfPoints")) == m.nnodes and int(piece.get("NumberOfCells")) == m.nel
+    # free nodes from u through invP_id, prescribed ones from upresc (Paraview_Output.c:30-35)
+    want = np.array([u[m.invp[i]] if m.type[i] > 0 else p.upresc[i] for i in range(m.nnodes)])
+    assert np.allclose(pd["solucao"], want, atol=1e-12)
+    assert np.allclose(pts[:, 0], m.x) and np.allclose(pts[:, 1], m.y) and np.allclose(pts[:, 2], want)
+    assert np.array_equal(cells["connectivity"].reshape(-1, 3), m.ien)
+    assert np.array_equal(cells["offsets"], 3 * np.arange(1, m.nel + 1))
+    assert np.all(cells["types"] == 5)
+    # the reference's line layout: one value per line, %.12f
+    lines = open(path).read().splitlines()
+    assert lines[0] == '<VTKFile type="UnstructuredGrid" version="0.1" byte_order="BigEndian">'
+    assert lines[5] == "\t\t\t\t   %.12f" % want[0]
+
+
+def test_vtu_euler_ns_output(fg, tmp_path):
+    ep = G.obliquo_problem(9)
+    m = ep.mesh
+    U = ep.initial_state()
+    fg.write_euler_vtu(str(tmp_path / "e.vtu"), ep, U)
+    _, pd, pts, _ = _vtu_arrays(str(tmp_path / "e.vtu"))
+    assert list(pd) == ["Density", "Temperature", "Pressure"]
+    V = fg.node_values(m, U, ep.upresc)
+    aux = V[:, 3] - (V[:, 1] ** 2 + V[:, 2] ** 2) / (2 * V[:, 0])
+    assert np.allclose(pd["Density"], V[:, 0], atol=1e-12)
+    assert np.allclose(pd["Pressure"], (ep.gamma - 1) * aux, atol=1e-11)
+    assert np.allclose(pd["Temperature"], aux / (V[:, 0] * 716.5), atol=1e-12)
+    assert np.all(pts[:, 2] == 0)
+    npb = G.cavity_problem(7)
+    U = np.arange(npb.mesh.neq, dtype=float) * 1e-3
+    fg.write_ns_vtu(str(tmp_path / "n.vtu"), npb, U)
+    _, pd, _, _ = _vtu_arrays(str(tmp_path / "n.vtu"))
+    V = fg.node_values(npb.mesh, U, npb.upresc)
+    vel = pd["Velocity"].reshape(-1, 3)
+    assert np.allclose(vel[:, :2], V[:, :2], atol=1e-12) and np.all(vel[:, 2] == 0)
+    assert np.allclose(pd["Pressure"], V[:, 2], atol=1e-12)
+
+
+def test_vtu_rejects_bad_input(fg, tmp_path):
+    p = G.transport_problem(5)
+    with pytest.raises(Exception):
+        fg.write_vtu(str(tmp_path / "x.vtu"), p.mesh, {"a": np.zeros(3)})
+    bad = G.Mesh(p.mesh.x, p.mesh.y, p.mesh.ien + 1000, 1, p.mesh.type, p.mesh.invp, p.mesh.neq)
+    with pytest.raises(Exception):
+        fg.write_vtu(str(tmp_path / "x.vtu"), bad, {"a": np.zeros(p.mesh.nnodes)})
