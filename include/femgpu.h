@@ -361,7 +361,24 @@ typedef struct {
     int precond;           /* FG_PRECOND_BLOCKDIAG, FG_PRECOND_DIAG or NONE; ILU0 or
                               SPIKE on a system switched to FG_OP_CSR            */
     int setup_flags;       /* FG_SETUP_REF_QUIRKS: the reference's 4x4 inverse     */
+    int scheme;            /* FG_TIME_PREDICTOR (0), FG_TIME_BDF, FG_TIME_TRBDF2    */
 } fg_time_opts;
+
+/* TimeIntegration of the drivers (setStabilizationForm.c):
+ *   FG_TIME_PREDICTOR  "Predictor1"        Predictor_Old.c
+ *   FG_TIME_BDF        "Predictor1_BDF"    Predictor_Old_BDF.c: one BDF1 step
+ *                      (no prediction, u += alpha dt Da), then BDF2 steps
+ *                      u = 4/3 u^n - 1/3 u^{n-1}, u += 2/3 dt Da; the Build
+ *                      keeps Alpha_Build = alpha, and the steady-state test
+ *                      compares with the initial state, as the reference does
+ *   FG_TIME_TRBDF2     Predictor_New_TRBDF2.c without its bubble unknowns:
+ *                      per step a TR stage (alpha 1/2 over lambda dt,
+ *                      lambda = 2 - sqrt 2) and a BDF2 stage (alpha
+ *                      1/(2 - lambda) over (1 - lambda) dt, prediction
+ *                      A u - B u_old).  "Predictor1_TRBDF2"
+ *                      (Predictor_Old_TRBDF2.c) solves against a right-hand
+ *                      side that nothing fills and is not restated. */
+enum { FG_TIME_PREDICTOR = 0, FG_TIME_BDF = 1, FG_TIME_TRBDF2 = 2 };
 
 typedef struct {
     int steps;
@@ -372,7 +389,8 @@ typedef struct {
     double true_rel_residual;  /* of the last linear solve                        */
 } fg_time_stats;
 
-/* Predictor_Old: per step t += dt, u += (1 - alpha) dt a, a = 0, then
+/* Predictor_Old (t->scheme FG_TIME_PREDICTOR; BDF and TR-BDF2 above): per
+ * step t += dt, u += (1 - alpha) dt a, a = 0, then
  * corrections (assemble at (u, a), preconditioner set-up on R, GMRES for Da,
  * a += Da, u += alpha dt Da) until the correction stop test, until the time
  * stop test.  u (host, n) is the initial state on entry (the problem's

@@ -292,10 +292,30 @@ static int eu_pc_cb(void *p, double *x, double *z)
     return 0;
 }
 
-static void axpy_ref(int n, double a, const double *x, double *y)
+typedef struct {
+    eu_ctx mv;
+    int nnodes, nel, neq;
+    const double *x, *y;
+    const int *type, *invp, *ien;
+    const or_euler_problem *prob;
+    double *R, *bd;
+    double solver_tol;
+    int kmax, lmax;
+} eu_loop;
+
+/* one correction: Build_M_K_F_SUPG at Alpha_Build / DeltaT_Build,
+ * BlockDiag_precond_EBE_setup on R, pgmres for Da */
+static int eu_correct(void *p, double alpha_b, double dt_b, const double *u, const double *a, double *Da, int *gi)
 {
-    /* daxpy.c: y += a x, unrolled by 4 (same rounding as the plain loop) */
-    for (int i = 0; i < n; i++) y[i] += a * x[i];
+    eu_loop *c = (eu_loop *)p;
+    or_euler_problem pb = *c->prob;
+    pb.alpha = alpha_b;
+    pb.dt = dt_b;
+    or_build_euler(c->nnodes, c->nel, c->x, c->y, c->type, c->invp, c->ien, c->neq, &pb, u, a,
+                   (double *)c->mv.A, c->R);
+    or_blockdiag_setup(c->nnodes, c->nel, 4, c->ien, c->mv.A, c->mv.Id, c->neq, 1, c->bd, (double *)c->mv.inv, c->R);
+    or_pgmres(c->neq, c->kmax, c->lmax, c->solver_tol, eu_mv_cb, eu_pc_cb, &c->mv, c->R, Da, gi);
+    return 0;
 }
 
 int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, const int *type,
@@ -308,50 +328,12 @@ int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, co
     int *lm = malloc(sizeof(int) * 12 * ne), *Id = malloc(sizeof(int) * 4 * nn);
     double *A = malloc(sizeof(double) * 144 * ne);
     double *R = calloc((size_t)NEQ + 1, sizeof(double));
-    double *Da = calloc((size_t)NEQ + 1, sizeof(double));
-    double *u_old = calloc((size_t)NEQ + 1, sizeof(double));
     double *bd = malloc(sizeof(double) * 16 * nn), *inv = malloc(sizeof(double) * 16 * nn);
-    double *diff = calloc((size_t)NEQ + 1, sizeof(double));
     or_fill_lm(nel, 4, ien, type, invp, NEQ, lm);
     for (i = 0; i < 4 * nnodes; i++) Id[i] = type[i] == 0 ? NEQ : invp[i];
-    eu_ctx ctx = { nel, nnodes, NEQ, lm, Id, A, inv };
-    double dt = prob->dt, alpha = prob->alpha, t = 0.0;
-    int steps = 0, corr = 0, gmres = 0, stop_time;
-    memset(a, 0, sizeof(double) * (size_t)neq);
-    do {
-        int it = 0, stop;
-        steps++;
-        t += dt;
-        memcpy(u_old, u, sizeof(double) * (size_t)neq);
-        axpy_ref(neq, (1.0 - alpha) * dt, a, u);              /* prediction */
-        memset(a, 0, sizeof(double) * (size_t)neq);
-        do {                                                   /* multicorrection */
-            int gi = 0;
-            it++;
-            or_build_euler(nnodes, nel, x, y, type, invp, ien, neq, prob, u, a, A, R);
-            or_blockdiag_setup(nnodes, nel, 4, ien, A, Id, NEQ, 1, bd, inv, R);
-            or_pgmres(NEQ, kmax, lmax, solver_tol, eu_mv_cb, eu_pc_cb, &ctx, R, Da, &gi);
-            gmres += gi;
-            axpy_ref(neq, 1, Da, a);
-            axpy_ref(neq, alpha * dt, Da, u);
-            double norm_a = sqrt(or_ddot(neq, a, a));
-            double norm_Da = sqrt(or_ddot(neq, Da, Da));
-            /* Criteria.c:25-41 */
-            if (to->stop_by_norm) stop = norm_Da < to->correction_tol * norm_a || it >= to->max_corrections;
-            else stop = it >= to->max_corrections;
-        } while (!stop);
-        corr += it;
-        /* Criteria.c:44-80 */
-        if (to->steady_state) {
-            for (i = 0; i < neq; i++) diff[i] = u[i] - u_old[i];
-            double nd = sqrt(or_ddot(neq, diff, diff)), nu = sqrt(or_ddot(neq, u, u));
-            stop_time = to->time_tol * nu > nd || fabs(to->final_time - t) < dt;
-        } else {
-            stop_time = to->final_time - t < 1e-10;
-        }
-        if (to->max_steps > 0 && steps >= to->max_steps) stop_time = 1;
-    } while (!stop_time);
-    if (st) { st->steps = steps; st->corrections = corr; st->gmres_iterations = gmres; st->t = t; }
-    free(lm); free(Id); free(A); free(R); free(Da); free(u_old); free(bd); free(inv); free(diff);
+    eu_loop c = { { nel, nnodes, NEQ, lm, Id, A, inv }, nnodes, nel, neq, x, y, type, invp, ien, prob, R, bd,
+                  solver_tol, kmax, lmax };
+    int steps = or_time_integrate(neq, prob->alpha, prob->dt, to, eu_correct, &c, u, a, st);
+    free(lm); free(Id); free(A); free(R); free(bd); free(inv);
     return steps;
 }

@@ -184,12 +184,27 @@ typedef struct {
     double final_time;     /* FinalTime                                                 */
     double time_tol;       /* TimeIntegrationTolerance                                  */
     int max_steps;         /* bound on the time steps (0: none; not in the reference)   */
+    int scheme;            /* OR_TIME_PREDICTOR, OR_TIME_BDF or OR_TIME_TRBDF2          */
 } or_time_opts;
+
+enum { OR_TIME_PREDICTOR = 0, OR_TIME_BDF = 1, OR_TIME_TRBDF2 = 2 };
 
 typedef struct {
     int steps, corrections, gmres_iterations;
     double t;
 } or_time_stats;
+
+/* One correction of a time loop (oracle/time_loop.c): Build at (u, a) with
+ * Alpha_Build = alpha_b and DeltaT_Build = dt_b, preconditioner set-up on
+ * the residual, GMRES for Da (neq + 1 entries); *gmres receives the
+ * iterations.  Non-zero return aborts the loop. */
+typedef int (*or_correction_fn)(void *ctx, double alpha_b, double dt_b, const double *u, const double *a,
+                                double *Da, int *gmres);
+/* Predictor_Old, Predictor_Old_BDF or (bubble-free) Predictor_New_TRBDF2 by
+ * to->scheme; u: initial state in, final state out; a: du/dt out.  Returns
+ * the steps (a TR-BDF2 step is its TR and BDF2 stages), -1 on failure. */
+int or_time_integrate(int neq, double alpha, double dt, const or_time_opts *to, or_correction_fn correct,
+                      void *ctx, double *u, double *a, or_time_stats *st);
 
 /* Predictor_Old.c:6-134 with EBE 12x12 blocks, BlockDiag (4x4, the
  * reference's inverse) and GMRES.  u: initial state on entry (the

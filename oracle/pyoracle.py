@@ -181,11 +181,12 @@ class _EulerProblem(ctypes.Structure):
 class TimeOpts(ctypes.Structure):
     """or_time_opts: the stop tests of Criteria.c."""
     _fields_ = [("stop_by_norm", _c_int), ("max_corrections", _c_int), ("correction_tol", _c_dbl),
-                ("steady_state", _c_int), ("final_time", _c_dbl), ("time_tol", _c_dbl), ("max_steps", _c_int)]
+                ("steady_state", _c_int), ("final_time", _c_dbl), ("time_tol", _c_dbl), ("max_steps", _c_int),
+                ("scheme", _c_int)]
 
     def as_array(self):
         return np.array([self.stop_by_norm, self.max_corrections, self.correction_tol, self.steady_state,
-                         self.final_time, self.time_tol], dtype=np.float64)
+                         self.final_time, self.time_tol, self.scheme], dtype=np.float64)
 
 
 class _TimeStats(ctypes.Structure):

@@ -6,7 +6,8 @@
  * The structs are filled for one rank (neq_bef = 0, NEQ = neq, EBE storage)
  * and the reference's own Fill_LM, Build_M_K_F_SUPG (with Delta_CAU and
  * Ax_Ay_calculations), BlockDiag_precond_EBE_setup, ebemvNDOF4, pgmres and
- * Predictor_Old are called.  The function pointers are installed as the
+ * the time loops (Predictor_Old, Predictor_Old_BDF, or Predictor_New_TRBDF2
+ * run with the SUPG builder, where its bubble unknowns stay zero) are called.  The function pointers are installed as the
  * reference's set* functions install them for StabilizationForm "SUPG",
  * ShockCapture "CAU", TimeIntegration "Predictor1", Preconditioner
  * "BlockDiag", MatrixVectorProductScheme "EBE" (setStabilizationForm.c and
@@ -220,9 +221,10 @@ void fr_eu_ebemv(int nnodes, int nel, const double *x, const double *y, const in
     fr_eu_free(&c);
 }
 
-/* The predictor/multicorrector time loop of the reference.
+/* The predictor/multicorrector time loops of the reference.
  * topt: stop_by_norm, max_corrections, correction_tol, steady_state,
- *       final_time, time_tol; solver: kmax, lmax, tol. */
+ *       final_time, time_tol, scheme (0 Predictor_Old, 1 Predictor_Old_BDF,
+ *       2 Predictor_New_TRBDF2); solver: kmax, lmax, tol. */
 int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
                     const int *ien, int neq, const double *prm, const double *coef, int wall,
                     const double *init, const double *topt, int kmax, int lmax, double tol, double *u_out,
@@ -242,12 +244,17 @@ int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const
     c.P.SolverTolerance = tol;
     c.P.iterations = 0;
     setStopCriteria(&c.P, &c.F);
-    /* Predictor_Old installs and frees its own du, uB, delta_old and AuxBuild */
+    /* the loops install and free their own du, uB, duB, delta_old and AuxBuild */
     free(c.S.delta_old);
     c.S.delta_old = NULL;
-    Predictor_Old(&c.P, &c.M, &c.S, &c.F, &c.O);
+    if (topt[6] == 1.0)
+        Predictor_Old_BDF(&c.P, &c.M, &c.S, &c.F, &c.O);
+    else if (topt[6] == 2.0)
+        Predictor_New_TRBDF2(&c.P, &c.M, &c.S, &c.F, &c.O);
+    else
+        Predictor_Old(&c.P, &c.M, &c.S, &c.F, &c.O);
     c.S.delta_old = NULL;
-    c.S.du = c.S.uB = NULL;
+    c.S.du = c.S.uB = c.S.duB = NULL;
     c.S.AuxBuild = NULL;
     memcpy(u_out, c.S.u, sizeof(double) * (size_t)neq);
     *t_out = c.P.CurrentTime;

@@ -151,6 +151,29 @@ static int tt_pc_cb(void *p, double *x, double *z)
     return 0;
 }
 
+typedef struct {
+    tt_ctx mv;
+    int nnodes, nel, neq;
+    const double *x, *y;
+    const int *type, *invp, *ien;
+    const or_transport_problem *prob;
+    double *R, *Diag;
+    double solver_tol;
+    int kmax, lmax;
+} tt_loop;
+
+/* one correction: Build_M_K_R_SUPG at Alpha_Build / DeltaT_Build, the
+ * accumulating Diag_precond_EBE_setup on R, pgmres for Da */
+static int tt_correct(void *p, double alpha_b, double dt_b, const double *u, const double *a, double *Da, int *gi)
+{
+    tt_loop *c = (tt_loop *)p;
+    or_build_tt(c->nnodes, c->nel, c->x, c->y, c->type, c->invp, c->ien, c->neq, c->prob, alpha_b, dt_b, u, a,
+                (double *)c->mv.A, c->R);
+    or_diag_setup(c->nel, 3, c->mv.lm, c->mv.A, c->neq, c->Diag, (double *)c->mv.invDiag, c->R);
+    or_pgmres(c->neq, c->kmax, c->lmax, c->solver_tol, tt_mv_cb, tt_pc_cb, &c->mv, c->R, Da, gi);
+    return 0;
+}
+
 int or_tt_predictor(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
                     const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
                     const or_time_opts *to, double solver_tol, int kmax, int lmax, double *u, double *a,
@@ -162,51 +185,12 @@ int or_tt_predictor(int nnodes, int nel, const double *x, const double *y, const
     int *Perm = malloc(sizeof(int) * ((size_t)NEQ + 1)), *invPerm = malloc(sizeof(int) * ((size_t)NEQ + 1));
     double *A = malloc(sizeof(double) * 9 * ne);
     double *R = calloc((size_t)NEQ + 1, sizeof(double));
-    double *Da = calloc((size_t)NEQ + 1, sizeof(double));
-    double *u_old = calloc((size_t)NEQ + 1, sizeof(double));
     double *Diag = calloc((size_t)NEQ + 1, sizeof(double)), *invDiag = calloc((size_t)NEQ + 1, sizeof(double));
-    double *diff = calloc((size_t)NEQ + 1, sizeof(double));
     or_fill_lm(nel, 1, ien, type, invp, NEQ, lm);
     or_permutation_of_lm(nel, ien, type, invp, NEQ, Perm, invPerm, NULL);
-    tt_ctx ctx = { nel, NEQ, lm, Perm, invPerm, A, invDiag };
-    double t = 0.0;
-    int steps = 0, corr = 0, gmres = 0, stop_time, i;
-    memset(a, 0, sizeof(double) * (size_t)neq);
-    do {
-        int it = 0, stop;
-        steps++;
-        t += dt;
-        memcpy(u_old, u, sizeof(double) * (size_t)neq);
-        for (i = 0; i < neq; i++) u[i] += (1.0 - alpha) * dt * a[i];     /* prediction */
-        memset(a, 0, sizeof(double) * (size_t)neq);
-        do {                                                            /* multicorrection */
-            int gi = 0;
-            it++;
-            or_build_tt(nnodes, nel, x, y, type, invp, ien, neq, prob, alpha, dt, u, a, A, R);
-            or_diag_setup(nel, 3, lm, A, NEQ, Diag, invDiag, R);
-            or_pgmres(NEQ, kmax, lmax, solver_tol, tt_mv_cb, tt_pc_cb, &ctx, R, Da, &gi);
-            gmres += gi;
-            for (i = 0; i < neq; i++) a[i] += 1 * Da[i];
-            for (i = 0; i < neq; i++) u[i] += alpha * dt * Da[i];
-            double norm_a = sqrt(or_ddot(neq, a, a));
-            double norm_Da = sqrt(or_ddot(neq, Da, Da));
-            /* Criteria.c:25-41 */
-            if (to->stop_by_norm) stop = norm_Da < to->correction_tol * norm_a || it >= to->max_corrections;
-            else stop = it >= to->max_corrections;
-        } while (!stop);
-        corr += it;
-        /* Criteria.c:44-80 */
-        if (to->steady_state) {
-            for (i = 0; i < neq; i++) diff[i] = u[i] - u_old[i];
-            double nd = sqrt(or_ddot(neq, diff, diff)), nu = sqrt(or_ddot(neq, u, u));
-            stop_time = to->time_tol * nu > nd || fabs(to->final_time - t) < dt;
-        } else {
-            stop_time = to->final_time - t < 1e-10;
-        }
-        if (to->max_steps > 0 && steps >= to->max_steps) stop_time = 1;
-    } while (!stop_time);
-    if (st) { st->steps = steps; st->corrections = corr; st->gmres_iterations = gmres; st->t = t; }
-    free(lm); free(Perm); free(invPerm); free(A); free(R); free(Da); free(u_old); free(Diag); free(invDiag);
-    free(diff);
+    tt_loop c = { { nel, NEQ, lm, Perm, invPerm, A, invDiag }, nnodes, nel, neq, x, y, type, invp, ien, prob, R,
+                  Diag, solver_tol, kmax, lmax };
+    int steps = or_time_integrate(neq, alpha, dt, to, tt_correct, &c, u, a, st);
+    free(lm); free(Perm); free(invPerm); free(A); free(R); free(Diag); free(invDiag);
     return steps;
 }

@@ -274,6 +274,14 @@ __global__ void k_axpy(int n, double a, const double *__restrict__ x, double *__
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) y[i] += a * x[i];
 }
 
+// y = c1 x1 - c2 x2, each product rounded (the BDF2 and TR-BDF2 predictions)
+// (y may be x1: each entry is read before it is written by the same thread)
+__global__ void k_lincomb(int n, double c1, const double *x1, double c2, const double *__restrict__ x2, double *y)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        y[i] = c1 * x1[i] - c2 * x2[i];
+}
+
 __global__ void k_sum_parts(const double *__restrict__ part, int nb, double *__restrict__ out)
 {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -300,6 +308,14 @@ int diff_norms_device(int n, const double *u, const double *v, double *part, dou
     k_sum_parts<<<1, 32, 0, st>>>(part, nb, out);
     FG_CUDA(cudaGetLastError());
     count_launches(2);
+    return FG_OK;
+}
+
+int lincomb_device(int n, double c1, const double *x1, double c2, const double *x2, double *y, cudaStream_t st)
+{
+    k_lincomb<<<norm_blocks(n), 256, 0, st>>>(n, c1, x1, c2, x2, y);
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
     return FG_OK;
 }
 

@@ -85,7 +85,7 @@ size_t fg_system::bytes() const
                            &dinv64, &dinv32, &ilu_flags, &ilu_ctr, &ilu_tmp, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
                            &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
-                           &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
+                           &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &state_u1, &state_u2, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
                            &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
     size_t b = 0;
     for (auto *m : all) b += m->bytes;
@@ -762,21 +762,34 @@ int fg_euler_assemble(fg_system *s, const fg_euler_coeffs *c, const double *u, c
 
 namespace fg {
 
-// Predictor_Old.c:6-134 with the state (u, a, u_old), the residual and the
-// increment kept on the device; per correction one assembly (`assemble(u,
-// a, R)` on the device, internal numbering), one preconditioner set-up, one
-// batched-engine solve and two update kernels.  Only the norms the stop
-// tests read come back to the host.  Shared by the Euler and the transient
-// transport drivers (the reference shares Predictor_Old between them).
+// The time loops of 00_CommonFiles/Time_Integration with the state (u, a,
+// u_old, and u^{n-1}, u^n for BDF2), the residual and the increment kept on
+// the device; per correction one assembly (`assemble(alpha_b, dt_b, u, a,
+// R)` on the device, internal numbering, with the Alpha_Build / DeltaT_Build
+// of the stage), one preconditioner set-up, one batched-engine solve and two
+// update kernels.  Only the norms the stop tests read come back to the host.
+// Shared by the Euler and the transient transport drivers (the reference
+// shares its predictors between them).
+//   FG_TIME_PREDICTOR  Predictor_Old.c:53-126
+//   FG_TIME_BDF        Predictor_Old_BDF.c:44-150 (BDF1 start, then BDF2; the
+//                      Build keeps Alpha_Build = alpha; u_old stays the
+//                      initial state for the steady-state test)
+//   FG_TIME_TRBDF2     Predictor_New_TRBDF2.c:55-190 without the bubble
+//                      unknowns (TR stage alpha 1/2 over lambda dt, BDF2
+//                      stage alpha 1/(2 - lambda) over (1 - lambda) dt)
 template <class Assemble>
-static int predictor_old(fg_system *s, double dt, double alpha, Assemble &&assemble, const fg_solver_opts *o,
-                         const fg_time_opts *to, double *u, double *a, fg_time_stats *stats)
+static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble, const fg_solver_opts *o,
+                     const fg_time_opts *to, double *u, double *a, fg_time_stats *stats)
 {
     if (to->precond < FG_PRECOND_NONE || to->precond > FG_PRECOND_SPIKE) {
         set_error("time-loop preconditioner must be NONE, DIAG, BLOCKDIAG, ILU0 or SPIKE");
         return FG_ERR_ARG;
     }
     if (to->max_corrections < 1 || !(dt > 0)) { set_error("max_corrections >= 1 and dt > 0 required"); return FG_ERR_ARG; }
+    if (to->scheme < FG_TIME_PREDICTOR || to->scheme > FG_TIME_TRBDF2) {
+        set_error("time scheme must be FG_TIME_PREDICTOR, FG_TIME_BDF or FG_TIME_TRBDF2");
+        return FG_ERR_ARG;
+    }
     auto t0 = std::chrono::steady_clock::now();
     const int n = s->topo.n;
     fg_system *one[1] = {s};
@@ -784,11 +797,12 @@ static int predictor_old(fg_system *s, double dt, double alpha, Assemble &&assem
     int r = batch_config(one, 1, o, cfg);
     if (r) return r;
     cfg.device_io = 1;
-    const size_t vb = 8 * (size_t)s->n_pad;
+    const size_t vb = 8 * (size_t)s->n_pad, nb = 8 * (size_t)n;
     if ((r = ensure_io(s)) || (r = stage(s, s->rhs_f, vb)) || (r = stage(s, s->rhs_b, vb)) ||
         (r = stage(s, s->state_u, vb)) || (r = stage(s, s->state_a, vb)) || (r = stage(s, s->state_old, vb)) ||
         (r = stage(s, s->norm_part, norm_scratch_bytes())))
         return r;
+    if (to->scheme == FG_TIME_BDF && ((r = stage(s, s->state_u1, vb)) || (r = stage(s, s->state_u2, vb)))) return r;
     double *du = s->state_u.as<double>(), *da = s->state_a.as<double>(), *dold = s->state_old.as<double>();
     FG_CUDA(cudaMemsetAsync(s->state_u.p, 0, vb, s->stream));
     if ((r = state_in(s, u, du))) return r;
@@ -797,31 +811,28 @@ static int predictor_old(fg_system *s, double dt, double alpha, Assemble &&assem
     double *part = s->norm_part.as<double>(), *norms = part + (s->norm_part.bytes / 8 - 2);
     double t = 0.0, last_res = NAN;
     int steps = 0, corr = 0, gmres = 0;
-    bool stop_time = false;
-    do {
-        ++steps;
-        t += dt;
-        FG_CUDA(cudaMemcpyAsync(dold, du, 8 * (size_t)n, cudaMemcpyDeviceToDevice, s->stream));
-        if ((r = axpy_device(n, (1.0 - alpha) * dt, da, du, s->stream))) return r;      // prediction
-        FG_CUDA(cudaMemsetAsync(da, 0, 8 * (size_t)n, s->stream));
-        int it = 0;
+
+    // the multicorrection of every scheme: a += Da, u += coef Da until the
+    // correction stop test (Criteria.c:25-41)
+    auto multicorrect = [&](double ab, double db, double coef) -> int {
+        int it = 0, rr;
         bool stop = false;
-        do {                                                                          // multicorrection
+        do {
             ++it;
-            if ((r = assemble(du, da, s->rhs_f.as<double>()))) return r;
+            if ((rr = assemble(ab, db, du, da, s->rhs_f.as<double>()))) return rr;
             FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, vb, cudaMemcpyDeviceToDevice, s->stream));
             int flags = to->setup_flags | (to->precond == FG_PRECOND_DIAG ? FG_SETUP_ACCUMULATE : 0);
-            if ((r = precond_setup_device(s, to->precond, flags, s->rhs_b.as<double>(), s->stream))) return r;
+            if ((rr = precond_setup_device(s, to->precond, flags, s->rhs_b.as<double>(), s->stream))) return rr;
             s->rhs_ok = true;
             cfg.precond = s->precond;
             std::vector<BatchMember> mem{{s, s->rhs_b.as<double>(), s->rhs_f.as<double>(), nullptr}};
             fg_solve_stats st{};
-            if ((r = solve_batch(mem, cfg, &st, s->stream))) return r;
+            if ((rr = solve_batch(mem, cfg, &st, s->stream))) return rr;
             gmres += st.iterations;
             last_res = st.true_rel_residual;
             const double *Da = s->ws.x.as<double>();
-            if ((r = axpy_norms_device(n, 1, Da, da, part, norms, s->stream))) return r;   // a += Da
-            if ((r = axpy_device(n, alpha * dt, Da, du, s->stream))) return r;           // u += alpha dt Da
+            if ((rr = axpy_norms_device(n, 1, Da, da, part, norms, s->stream))) return rr;   // a += Da
+            if ((rr = axpy_device(n, coef, Da, du, s->stream))) return rr;                 // u += coef Da
             if (to->stop_by_norm) {
                 FG_CUDA(cudaMemcpyAsync(s->h_vec, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
                 FG_CUDA(cudaStreamSynchronize(s->stream));
@@ -832,17 +843,73 @@ static int predictor_old(fg_system *s, double dt, double alpha, Assemble &&assem
             }
         } while (!stop);
         corr += it;
+        return FG_OK;
+    };
+    // Criteria.c:44-80 with the DeltaT in force, plus the optional step bound
+    auto time_stop = [&](double dt_now, bool &stop_time) -> int {
         if (to->steady_state) {
-            if ((r = diff_norms_device(n, du, dold, part, norms, s->stream))) return r;
+            int rr = diff_norms_device(n, du, dold, part, norms, s->stream);
+            if (rr) return rr;
             FG_CUDA(cudaMemcpyAsync(s->h_vec, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
             FG_CUDA(cudaStreamSynchronize(s->stream));
             const double nd = std::sqrt(s->h_vec[0]), nu = std::sqrt(s->h_vec[1]);
-            stop_time = to->time_tol * nu > nd || std::fabs(to->final_time - t) < dt;
+            stop_time = to->time_tol * nu > nd || std::fabs(to->final_time - t) < dt_now;
         } else {
             stop_time = to->final_time - t < 1e-10;
         }
         if (to->max_steps > 0 && steps >= to->max_steps) stop_time = true;
-    } while (!stop_time);
+        return FG_OK;
+    };
+    auto copy = [&](double *dst, const double *src) -> int {
+        FG_CUDA(cudaMemcpyAsync(dst, src, nb, cudaMemcpyDeviceToDevice, s->stream));
+        return FG_OK;
+    };
+    bool stop_time = false;
+    if (to->scheme == FG_TIME_PREDICTOR) {
+        do {
+            ++steps;
+            t += dt;
+            if ((r = copy(dold, du))) return r;
+            if ((r = axpy_device(n, (1.0 - alpha) * dt, da, du, s->stream))) return r;      // prediction
+            FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+            if ((r = multicorrect(alpha, dt, alpha * dt)) || (r = time_stop(dt, stop_time))) return r;
+        } while (!stop_time);
+    } else if (to->scheme == FG_TIME_BDF) {
+        const double four_thirds = 4.0 / 3.0, two_thirds = 2.0 / 3.0, one_third = 1.0 / 3.0;
+        double *u1 = s->state_u1.as<double>(), *u2 = s->state_u2.as<double>();
+        ++steps;                                                                          // BDF1 start
+        t += dt;
+        if ((r = copy(dold, du)) || (r = copy(u1, du))) return r;
+        FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+        if ((r = multicorrect(alpha, dt, alpha * dt)) || (r = copy(u2, du))) return r;
+        do {                                                                              // BDF2 steps
+            ++steps;
+            t += dt;
+            if ((r = lincomb_device(n, four_thirds, u2, one_third, u1, du, s->stream))) return r;
+            FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+            if ((r = multicorrect(alpha, dt, two_thirds * dt))) return r;
+            if ((r = copy(u1, u2)) || (r = copy(u2, du)) || (r = time_stop(dt, stop_time))) return r;
+        } while (!stop_time);
+    } else {
+        const double lambda = 2.0 - std::sqrt(2.0);
+        const double A = 1.0 / (lambda * (2.0 - lambda));
+        const double B = (1.0 - lambda) * (1.0 - lambda) / (lambda * (2.0 - lambda));
+        const double dtTR = lambda * dt, dtBDF2 = (1.0 - lambda) * dt;
+        const double aTR = 0.5, aBDF2 = 1.0 / (2.0 - lambda);
+        if ((r = copy(dold, du))) return r;
+        do {
+            ++steps;
+            t += dtTR;                                                                    // TR stage
+            if ((r = axpy_device(n, aTR * dtTR, da, du, s->stream))) return r;
+            FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+            if ((r = multicorrect(aTR, dtTR, aTR * dtTR))) return r;
+            t += dtBDF2;                                                                  // BDF2 stage
+            if ((r = lincomb_device(n, A, du, B, dold, du, s->stream))) return r;
+            FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+            if ((r = multicorrect(aBDF2, dtBDF2, aBDF2 * dtBDF2))) return r;
+            if ((r = copy(dold, du)) || (r = time_stop(dtBDF2, stop_time))) return r;
+        } while (!stop_time);
+    }
     if ((r = vec_out(s, du, s->h_vec, s->ws.r64.as<double>()))) return r;
     FG_CUDA(cudaStreamSynchronize(s->stream));
     std::memcpy(u, s->h_vec, 8 * (size_t)n);
@@ -871,11 +938,14 @@ int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_o
                        double *u, double *a, fg_time_stats *stats)
 {
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
-    return predictor_old(s, c->dt, c->alpha,
-                         [&](const double *du, const double *da, double *R) {
-                             return euler_assemble_device(s, c, du, da, R, s->stream);
-                         },
-                         o, to, u, a, stats);
+    return time_loop(s, c->dt, c->alpha,
+                     [&](double ab, double db, const double *du, const double *da, double *R) {
+                         fg_euler_coeffs cc = *c;
+                         cc.alpha = ab;
+                         cc.dt = db;
+                         return euler_assemble_device(s, &cc, du, da, R, s->stream);
+                     },
+                     o, to, u, a, stats);
 }
 
 int fg_tt_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, const double *du, double *R)
@@ -900,11 +970,14 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
                     double *a, fg_time_stats *stats)
 {
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
-    return predictor_old(s, c->dt, c->alpha,
-                         [&](const double *du, const double *da, double *R) {
-                             return tt_assemble_device(s, c, du, da, R, s->stream);
-                         },
-                         o, to, u, a, stats);
+    return time_loop(s, c->dt, c->alpha,
+                     [&](double ab, double db, const double *du, const double *da, double *R) {
+                         fg_tt_coeffs cc = *c;
+                         cc.alpha = ab;
+                         cc.dt = db;
+                         return tt_assemble_device(s, &cc, du, da, R, s->stream);
+                     },
+                     o, to, u, a, stats);
 }
 
 }  // extern "C"

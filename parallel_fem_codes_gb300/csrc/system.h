@@ -47,6 +47,7 @@ struct fg_system {
     // Navier-Stokes / Euler: nodal body force (gup holds ndof values per node),
     // state of the nonlinear and time loops (internal numbering) and norm scratch
     fg::DevMem gf1, gf2, state_u, state_a, state_old, norm_part;
+    fg::DevMem state_u1, state_u2;     // u^{n-1}, u^n of the BDF2 steps
     bool ns_geometry_ok = false, eu_geometry_ok = false;
     // resident right-hand side (internal numbering): F and M^-1 F
     fg::DevMem rhs_f, rhs_b;
@@ -200,6 +201,7 @@ int axpy_norms_device(int n, double a, const double *x, double *y, double *part,
 // out[0] = sum (u - v)^2, out[1] = sum u^2
 int diff_norms_device(int n, const double *u, const double *v, double *part, double *out, cudaStream_t st);
 int axpy_device(int n, double a, const double *x, double *y, cudaStream_t st);
+int lincomb_device(int n, double c1, const double *x1, double c2, const double *x2, double *y, cudaStream_t st);
 size_t norm_scratch_bytes();
 // Transient transport (setup.cu)
 int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev, const double *du_dev, double *R_dev,

@@ -20,6 +20,7 @@ FG_SCALE_LEFT, FG_SCALE_LEFTRIGHT = 1, 2
 FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED = 64, 32
+FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 = 0, 1, 2
 FG_REORDER_NONE, FG_REORDER_RCM = 0, 1
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE",
           5: "ERR_BREAKDOWN", 6: "ERR_NOTCONV", 7: "ERR_UNSUPPORTED", 8: "ERR_TIMEOUT"}
@@ -85,7 +86,7 @@ class EulerCoeffs(ctypes.Structure):
 class TimeOpts(ctypes.Structure):
     _fields_ = [("stop_by_norm", _c_int), ("max_corrections", _c_int), ("correction_tol", _c_dbl),
                 ("steady_state", _c_int), ("final_time", _c_dbl), ("time_tol", _c_dbl), ("max_steps", _c_int),
-                ("precond", _c_int), ("setup_flags", _c_int)]
+                ("precond", _c_int), ("setup_flags", _c_int), ("scheme", _c_int)]
 
 
 class TimeStats(ctypes.Structure):
@@ -538,13 +539,14 @@ def euler_coeffs(prob) -> EulerCoeffs:
 
 
 def time_opts(stop_by_norm=0, max_corrections=2, correction_tol=1e-3, steady_state=0, final_time=0.0,
-              time_tol=1e-6, max_steps=0, precond=None, setup_flags=None) -> TimeOpts:
-    """Criteria.c controls; the preconditioner defaults to the reference's
-    BlockDiag with its 4x4 inverse (FG_SETUP_REF_QUIRKS)."""
+              time_tol=1e-6, max_steps=0, precond=None, setup_flags=None, scheme=0) -> TimeOpts:
+    """Criteria.c controls and the TimeIntegration scheme (FG_TIME_*); the
+    preconditioner defaults to the reference's BlockDiag with its 4x4
+    inverse (FG_SETUP_REF_QUIRKS)."""
     precond = FG_PRECOND_BLOCKDIAG if precond is None else precond
     setup_flags = FG_SETUP_REF_QUIRKS if setup_flags is None else setup_flags
     return TimeOpts(stop_by_norm, max_corrections, correction_tol, steady_state, final_time, time_tol, max_steps,
-                    precond, setup_flags)
+                    precond, setup_flags, scheme)
 
 
 def euler_system(prob, reorder=False) -> System:

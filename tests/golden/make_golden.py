@@ -11,7 +11,10 @@ tests/golden/ns_*.npz: the steady Navier-Stokes driver's Fill_LM,
 Build_K_F_SUPG_PSPG at a state u, BlockDiagDOF3_precond_EBE_setup,
 ebemvNDOF3 and (cavity) the Picard Process loop; and tests/golden/eu_*.npz:
 the Euler driver's Fill_LM, Build_M_K_F_SUPG at a state (u, du),
-BlockDiag_precond_EBE_setup, ebemvNDOF4 and the Predictor_Old time loop.
+BlockDiag_precond_EBE_setup, ebemvNDOF4 and the Predictor_Old time loop;
+and tests/golden/time_schemes_euler.npz: the final states of Predictor_Old_BDF and
+of Predictor_New_TRBDF2 (run with Build_M_K_F_SUPG, its bubble unknowns
+zero) on the Euler cases.
 """
 import os
 import sys
@@ -112,6 +115,19 @@ def ns_cases():
     return {"ns_9_cavity": (cav, 0, True), "ns_9_affine": (aff, 6, False)}
 
 
+def write_euler_schemes():
+    out = {}
+    for name, (prob, seed, to) in euler_cases().items():
+        for scheme in (1, 2):
+            to.scheme = scheme
+            U, its, t = O.ref_euler_predictor(prob, to, 1e-10, 25, 1000)
+            key = f"{name}_s{scheme}"
+            out[key + "_U"], out[key + "_its"], out[key + "_t"] = U, its, t
+            print(key, "gmres", its, "t", t)
+    np.savez_compressed(os.path.join(HERE, "time_schemes_euler.npz"), **out)
+
+
 if __name__ == "__main__":
     main()
     write_euler()
+    write_euler_schemes()

@@ -128,3 +128,19 @@ def test_euler_rejects_wrong_ndof(fg):
     s = fg.System(p.mesh)
     with pytest.raises(fg.FemGpuError):
         s.euler_set_geometry(G.obliquo_problem(9))
+
+
+@pytest.mark.parametrize("scheme", [1, 2], ids=["bdf", "trbdf2"])
+@pytest.mark.parametrize("steady", [0, 1])
+def test_euler_time_schemes(fg, scheme, steady):
+    """Predictor_Old_BDF and the TR-BDF2 loop on the device against the
+    oracle (itself bit-exact with the reference's loops)."""
+    p = G.obliquo_problem(17, dimensionless=not steady)
+    args = (1, 4, 1e-2, 1, 40 * p.dt, 1e-2) if steady else (0, 2, 1e-3, 0, 4 * p.dt, 1e-6)
+    to_o = O.TimeOpts(*args, 0, scheme)
+    uo, ao, sto = O.euler_predictor(p, to_o, tol=1e-10, kmax=25)
+    s = fg.euler_system(p)
+    ug, ag, st = s.euler_predictor(p, fg.time_opts(*args, scheme=scheme), kmax=25, tol=1e-10)
+    assert st["steps"] == sto["steps"]
+    assert st["t"] == sto["t"]
+    assert rel(ug, uo) < 1e-7

@@ -62,3 +62,18 @@ def test_tt_predictor_steady_stop(fg):
                                                           setup_flags=0), tol=1e-12)
     assert st["steps"] == sto["steps"]
     assert rel(ug, uo) < 1e-8
+
+
+@pytest.mark.parametrize("scheme", [1, 2], ids=["bdf", "trbdf2"])
+def test_tt_time_schemes(fg, scheme):
+    """The BDF and TR-BDF2 loops drive the transient transport build too
+    (the reference shares its predictors between the drivers)."""
+    p = G.transport_problem(33, angle_deg=30.0, k=1e-3, f=0.0)
+    to_o = O.TimeOpts(0, 2, 1e-3, 0, 6 * 0.02, 1e-6, 0, scheme)
+    uo, ao, sto = O.tt_predictor(p, 0.5, 0.02, to_o, tol=1e-10, kmax=30)
+    s = fg.transport_system(p)
+    to = fg.time_opts(0, 2, 1e-3, 0, 6 * 0.02, 1e-6, precond=fg.FG_PRECOND_DIAG, setup_flags=0, scheme=scheme)
+    ug, ag, st = s.tt_predictor(p, 0.5, 0.02, to, kmax=30, tol=1e-10)
+    assert st["steps"] == sto["steps"] and st["t"] == sto["t"]
+    assert st["corrections"] == sto["corrections"]
+    assert rel(ug, uo) < 1e-8

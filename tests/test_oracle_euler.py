@@ -70,6 +70,40 @@ def test_predictor_bit_exact(case):
     assert np.array_equal(u, g["U"])
 
 
+SCHEMES = os.path.join(os.path.dirname(__file__), "golden", "time_schemes_euler.npz")
+
+
+@pytest.mark.parametrize("name", ["eu_9_obliquo", "eu_7_dimensional"])
+@pytest.mark.parametrize("scheme", [1, 2], ids=["bdf", "trbdf2"])
+def test_time_schemes_bit_exact(name, scheme, oracle_lib):
+    """Predictor_Old_BDF and (bubble-free) Predictor_New_TRBDF2 against the
+    reference's own loops run by the golden generator."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")))
+    p = problem_from(g)
+    gs = np.load(SCHEMES)
+    to = topts_from(g)
+    to.scheme = scheme
+    u, a, st = O.euler_predictor(p, to, tol=1e-10, kmax=25, lmax=1000)
+    key = f"{name}_s{scheme}"
+    assert st["gmres_iterations"] == int(gs[key + "_its"])
+    assert st["t"] == float(gs[key + "_t"])
+    assert np.array_equal(u, gs[key + "_U"])
+
+
+@pytest.mark.parametrize("scheme", [0, 1, 2])
+def test_time_schemes_against_reference_build(scheme, oracle_lib):
+    """The same against the reference build itself, on a third case, where
+    the reference sources were compiled (oracle/_ref)."""
+    if O.ref_euler() is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    p = G.obliquo_problem(11)
+    to = O.TimeOpts(1, 3, 1e-2, 0, 3 * p.dt, 1e-6, 0, scheme)
+    U, its, t = O.ref_euler_predictor(p, to, 1e-10, 25, 1000)
+    u, a, st = O.euler_predictor(p, to, tol=1e-10, kmax=25, lmax=1000)
+    assert st["gmres_iterations"] == its and st["t"] == t
+    assert np.array_equal(u, U)
+
+
 def test_obliquo_layout():
     p = G.obliquo_problem(9)
     m = p.mesh
