@@ -306,7 +306,12 @@ typedef struct {
                           (accumulating, as Diag_precond_EBE_setup.c),
                           FG_PRECOND_NONE, or FG_PRECOND_ILU0 / _SPIKE on a
                           system switched to FG_OP_CSR                        */
+    int form;          /* StabilizationForm (setStabilizationForm.c):
+                          FG_NS_SUPG_PSPG (0) Build_K_F_SUPG_PSPG.c, or
+                          FG_NS_VMS_DCDD Build_K_F_VMS_DCDD.c:8-716 (LSIC and
+                          the condensed bubble; its source term is 0)         */
 } fg_ns_coeffs;
+enum { FG_NS_SUPG_PSPG = 0, FG_NS_VMS_DCDD = 1 };
 
 /* Node coordinates, the prescribed (u, v, p) of every node (upresc[3*node+k],
  * read where dof k of the node is Dirichlet: v1presc/v2presc/ppresc at the

@@ -140,6 +140,7 @@ typedef struct {
     double reynolds;       /* ReynoldsNumber (density 1, viscosity 1/Re)             */
     const double *upresc;  /* [3*nnodes] prescribed u, v, p (read where type == 0)   */
     const double *f1, *f2; /* [nnodes] body force at the nodes (NULL = 0)            */
+    int form;              /* 0: SUPG-PSPG, 1: VMS-DCDD (StabilizationForm)           */
 } or_ns_problem;
 
 /* Build_K_F_SUPG_PSPG (Picard tangent) + eval_U + ebe_assembly.  u holds the
@@ -148,6 +149,11 @@ typedef struct {
 void or_build_ns(int nnodes, int nel, const double *x, const double *y, const int *type,
                  const int *invp, const int *ien, int neq, const or_ns_problem *prob,
                  const double *u, double *A, double *F);
+
+/* Build_K_F_VMS_DCDD (oracle/ns_vms.c); or_build_ns calls it for form 1. */
+void or_build_ns_vms(int nnodes, int nel, const double *x, const double *y, const int *type,
+                     const int *invp, const int *ien, int neq, const or_ns_problem *prob,
+                     const double *u, double *A, double *F);
 
 /* Picard loop of 04_SS_NavierStokes_Equations/2D/01_CommonFiles/Process.c:6-62
  * with EBE 9x9 blocks, BlockDiagDOF3 and GMRES: build, set up, solve for the

@@ -157,6 +157,10 @@ void or_build_ns(int nnodes, int nel, const double *x, const double *y, const in
                  const double *u, double *A, double *F)
 {
     int E, v, k, NEQ = neq;
+    if (prob->form == 1) {       /* StabilizationForm "VMS-DCDD" (setStabilizationForm.c) */
+        or_build_ns_vms(nnodes, nel, x, y, type, invp, ien, neq, prob, u, A, F);
+        return;
+    }
     double *U = malloc(sizeof(double) * 3 * (size_t)(nnodes ? nnodes : 1));
     /* eval_U.c:3-35: free dofs from u, prescribed ones from the problem */
     for (v = 0; v < nnodes; v++)

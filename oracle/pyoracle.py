@@ -141,6 +141,8 @@ def ref_ns():
         R.fr_ns_ebemv.restype = None
         R.fr_ns_process.argtypes = mesh + [_c_dbl, _f64p, _c_int, _c_dbl, _c_dbl, _c_int, _c_int, _c_int,
                                            _f64p, ctypes.POINTER(_c_int)]
+        R.fr_ns_set_form.argtypes = [_c_int]
+        R.fr_ns_set_form.restype = None
         R.fr_ns_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
         R.fr_ns_layout.restype = None
         _ref_ns = R
@@ -269,33 +271,35 @@ def ref_euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000):
 
 class _NSProblem(ctypes.Structure):
     _fields_ = [("reynolds", _c_dbl), ("upresc", ctypes.POINTER(_c_dbl)),
-                ("f1", ctypes.POINTER(_c_dbl)), ("f2", ctypes.POINTER(_c_dbl))]
+                ("f1", ctypes.POINTER(_c_dbl)), ("f2", ctypes.POINTER(_c_dbl)), ("form", _c_int)]
 
 
-def _ns_struct(p):
+def _ns_struct(p, form=0):
     keep = [np.ascontiguousarray(a, dtype=np.float64) for a in (p.upresc, p.f1, p.f2)]
     P = ctypes.POINTER(_c_dbl)
-    s = _NSProblem(p.reynolds, keep[0].ctypes.data_as(P), keep[1].ctypes.data_as(P), keep[2].ctypes.data_as(P))
+    s = _NSProblem(p.reynolds, keep[0].ctypes.data_as(P), keep[1].ctypes.data_as(P), keep[2].ctypes.data_as(P),
+                   form)
     return s, keep
 
 
-def build_ns(prob, u=None):
-    """Build_K_F_SUPG_PSPG at the free-dof state u; returns (A[nel, 81], F[neq+1])."""
+def build_ns(prob, u=None, form=0):
+    """Build_K_F_SUPG_PSPG (form 0) or Build_K_F_VMS_DCDD (form 1) at the
+    free-dof state u; returns (A[nel, 81], F[neq+1])."""
     m = prob.mesh
     u = np.zeros(m.neq) if u is None else np.ascontiguousarray(u, dtype=np.float64)
     A = np.empty(m.nel * 81)
     F = np.empty(m.neq + 1)
-    s, keep = _ns_struct(prob)
+    s, keep = _ns_struct(prob, form)
     lib().or_build_ns(*_mesh_args(m), ctypes.byref(s), u, A, F)
     return A.reshape(m.nel, 81), F
 
 
-def ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=100):
+def ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=100, form=0):
     """Picard loop; returns (u[neq], nonlinear its, GMRES its, last ||s||/||u||)."""
     m = prob.mesh
     u = np.zeros(m.neq + 1)
     its, last = _c_int(0), _c_dbl(0.0)
-    s, keep = _ns_struct(prob)
+    s, keep = _ns_struct(prob, form)
     nl = lib().or_ns_process(*_mesh_args(m), ctypes.byref(s), solver_tol, nonlinear_tol, kmax, lmax,
                              max_nonlinear, u, ctypes.byref(its), ctypes.byref(last))
     return u[:m.neq].copy(), nl, its.value, last.value
@@ -307,8 +311,9 @@ def ref_ns_lm(mesh):
     return lm.reshape(mesh.nel, 9)
 
 
-def ref_ns_build(prob, u=None):
+def ref_ns_build(prob, u=None, form=0):
     m = prob.mesh
+    ref_ns().fr_ns_set_form(form)
     u = np.zeros(m.neq) if u is None else np.ascontiguousarray(u, dtype=np.float64)
     A = np.empty(m.nel * 81)
     F = np.empty(m.neq + 1)
@@ -331,8 +336,9 @@ def ref_ns_ebemv(mesh, A, P):
     return Q
 
 
-def ref_ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=100):
+def ref_ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=100, form=0):
     m = prob.mesh
+    ref_ns().fr_ns_set_form(form)
     u = np.zeros(m.neq + 1)
     its = _c_int(0)
     ref_ns().fr_ns_process(*_mesh_args(m), prob.reynolds, np.ascontiguousarray(prob.coef.reshape(-1)),

@@ -54,6 +54,11 @@ typedef struct {
     FemOtherFunctionsType O;
 } fr_ns;
 
+static int g_form;  /* 0: "SUPG-PSPG", 1: "VMS-DCDD" */
+
+/* StabilizationForm of the following builds and Process runs. */
+void fr_ns_set_form(int form) { g_form = form; }
+
 static void fr_ns_setup(fr_ns *c, int nnodes, int nel, const double *x, const double *y,
                         const int *type, const int *invp, const int *ien, int neq, double Re,
                         double solver_tol, double nl_tol, int kmax, int lmax, int max_nl)
@@ -65,7 +70,7 @@ static void fr_ns_setup(fr_ns *c, int nnodes, int nel, const double *x, const do
     strcpy(c->P.Preconditioner, "BlockDiag");
     strcpy(c->P.reordering, "NOT");
     strcpy(c->P.MatrixVectorProductScheme, "EBE");
-    strcpy(c->P.StabilizationForm, "SUPG-PSPG");
+    strcpy(c->P.StabilizationForm, g_form ? "VMS-DCDD" : "SUPG-PSPG");
     c->P.ReynoldsNumber = Re;
     c->P.SolverTolerance = solver_tol;
     c->P.NonLinearTolerance = nl_tol;
@@ -147,7 +152,8 @@ void fr_ns_lm(int nnodes, int nel, const double *x, const double *y, const int *
     fr_ns_free(&c);
 }
 
-/* One Build_K_F_SUPG_PSPG call at the free-dof state u (A: 81 per element). */
+/* One build (Build_K_F_SUPG_PSPG or Build_K_F_VMS_DCDD by the form) at the
+ * free-dof state u (A: 81 per element). */
 void fr_ns_build(int nnodes, int nel, const double *x, const double *y, const int *type,
                  const int *invp, const int *ien, int neq, double Re, const double *coef, int lid,
                  const double *u, double *A_out, double *F_out)
@@ -161,7 +167,7 @@ void fr_ns_build(int nnodes, int nel, const double *x, const double *y, const in
     setPreconditioner(&c.P, &c.F);
     setStabilizationForm(&c.P, &c.F, &c.O);
     memcpy(c.S.u, u, sizeof(double) * (size_t)neq);
-    Build_K_F_SUPG_PSPG(&c.P, &c.M, &c.S, &c.F);
+    c.O.Build(&c.P, &c.M, &c.S, &c.F);
     memcpy(A_out, c.M.Aaux, sizeof(double) * 81 * (size_t)nel);
     memcpy(F_out, c.S.F, sizeof(double) * ((size_t)neq + 1));
     fr_ns_free(&c);

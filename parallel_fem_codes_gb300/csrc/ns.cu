@@ -194,13 +194,189 @@ int gather_residual(fg_system *s, const double *Fe, double *F, cudaStream_t st)
     return FG_OK;
 }
 
-int ns_assemble_device(fg_system *s, double reynolds, const double *u_dev, double *F_dev, cudaStream_t st)
+// ---------------------------------------------------------------- VMS-DCDD
+// Build_K_F_VMS_DCDD.c:8-716 (StabilizationForm "VMS-DCDD"): Galerkin + LSIC
+// with the bubble enrichment condensed through the 2x2 inverse W of K_BB.
+// With velocity dofs r = 2 i + d and g_r = b_i (d = 0) or c_i (d = 1):
+//   Ndelta(r, s) = (NhB_i W[d][e]) NBh_j,   NBh_i = 9/40 (ux b_i + uy c_i) = -NhB_i
+//   Gdelta(r, k) = (NhB_i W[d][0]) GB0_k + (NhB_i W[d][1]) GB1_k,  GB = -9/40 (b; c)
+//   Gphi(k, m)   = GB0_m (GB0_k W00 + GB1_k W01) + GB1_m (GB0_k W01 + GB1_k W11)
+// evaluated on the fly, each associated as the reference writes it.  The
+// reference's own choices are kept: the tangent holds Ndelta only in the
+// same-direction blocks and from the upper triangle, with a plus sign at
+// (node 2 x, node 1 x) (:645); the pressure block takes the upper triangle
+// of Gphi; the residual uses the full matrices; delta = 0 and the source is
+// 0 (:289, :388-394), so the residual is 0 - (...).
+struct VmsElem {
+    double g[6];                  // b0 c0 b1 c1 b2 c2
+    double A, invArea, visc, ux, uy, duxdx, duxdy, duydx, duydy, duxduy, p;
+    double C[3], NBh[3], W00, W01, W11, ks, kv;
+};
+
+__device__ __forceinline__ double vms_gb(const VmsElem &e, int k, int d) { return -(9.0 / 40.0) * e.g[2 * k + d]; }
+__device__ __forceinline__ double vms_w(const VmsElem &e, int d, int f)
+{
+    return d != f ? e.W01 : (d ? e.W11 : e.W00);
+}
+__device__ __forceinline__ double vms_nd(const VmsElem &e, int r, int s)
+{
+    return -e.NBh[r >> 1] * vms_w(e, r & 1, s & 1) * e.NBh[s >> 1];
+}
+__device__ __forceinline__ double vms_gd(const VmsElem &e, int r, int k)
+{
+    const double nh = -e.NBh[r >> 1];
+    return nh * vms_w(e, r & 1, 0) * vms_gb(e, k, 0) + nh * vms_w(e, r & 1, 1) * vms_gb(e, k, 1);
+}
+__device__ __forceinline__ double vms_gphi(const VmsElem &e, int k, int m)
+{
+    const double g0k = vms_gb(e, k, 0), g1k = vms_gb(e, k, 1);
+    return vms_gb(e, m, 0) * (g0k * e.W00 + g1k * e.W01) + vms_gb(e, m, 1) * (g0k * e.W01 + g1k * e.W11);
+}
+
+__global__ void __launch_bounds__(128) k_ns_vms_elem(int nel, int ld, int n, const int *__restrict__ gien,
+                                                     const double *__restrict__ gx, const double *__restrict__ gy,
+                                                     const int *__restrict__ node_dof, const double *__restrict__ up,
+                                                     const double *__restrict__ u, double Re,
+                                                     double *__restrict__ A64, double *__restrict__ Fe)
+{
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const double third = 1.0 / 3.0, sixth = 1.0 / 6.0, nf = 9.0 / 40.0;
+    double X[3], Y[3], Ue[9];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const int J = gien[(size_t)v * ld + pos];
+        X[v] = gx[J];
+        Y[v] = gy[J];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int d = node_dof[3 * J + k];
+            Ue[3 * v + k] = d == n ? up[3 * J + k] : u[d];
+        }
+    }
+    VmsElem e;
+    double *g = e.g;
+    g[0] = Y[1] - Y[2]; g[2] = Y[2] - Y[0]; g[4] = Y[0] - Y[1];
+    g[1] = X[2] - X[1]; g[3] = X[0] - X[2]; g[5] = X[1] - X[0];
+    const double TwoA = fabs(g[5] * g[2] - g[3] * g[4]);
+    e.A = 0.5 * TwoA;
+    e.invArea = 1.0 / e.A;
+    const double hi = 0.5 * e.invArea;
+    e.ux = third * (Ue[0] + Ue[3] + Ue[6]);
+    e.uy = third * (Ue[1] + Ue[4] + Ue[7]);
+    e.duxdx = hi * (Ue[0] * g[0] + Ue[3] * g[2] + Ue[6] * g[4]);
+    e.duxdy = hi * (Ue[0] * g[1] + Ue[3] * g[3] + Ue[6] * g[5]);
+    e.duydx = hi * (Ue[1] * g[0] + Ue[4] * g[2] + Ue[7] * g[4]);
+    e.duydy = hi * (Ue[1] * g[1] + Ue[4] * g[3] + Ue[7] * g[5]);
+    e.duxduy = Ue[0] * g[0] + Ue[1] * g[1] + Ue[3] * g[2] + Ue[4] * g[3] + Ue[6] * g[4] + Ue[7] * g[5];
+    e.p = third * (Ue[2] + Ue[5] + Ue[8]);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        e.C[i] = hi * (e.ux * g[2 * i] + e.uy * g[2 * i + 1]);
+        e.NBh[i] = nf * (e.ux * g[2 * i] + e.uy * g[2 * i + 1]);
+    }
+    const double h = sqrt(4 * e.A / 3.14159265359);      // PI of the reference's header
+    e.visc = 1. / Re;
+    const double unorm = sqrt(e.ux * e.ux + e.uy * e.uy);
+    const double tau_l = 0.5 * h * unorm;
+    e.ks = tau_l * 0.25 * e.invArea;
+    e.kv = e.visc * 0.25 * e.invArea;
+    const double Ab = g[0] * g[0] + g[2] * g[2] + g[4] * g[4] + g[0] * g[2] + g[0] * g[4] + g[2] * g[4];
+    const double Bc = g[1] * g[1] + g[3] * g[3] + g[5] * g[5] + g[1] * g[3] + g[1] * g[5] + g[3] * g[5];
+    const double Cbc = g[0] * g[1] + g[2] * g[3] + g[4] * g[5];
+    const double delta = 0.0, visc = e.visc;
+    const double tv = 2 * visc + delta, vd = visc + delta;
+    const double D = (tv * tv + vd * vd) * Ab * Bc + tv * vd * (Ab * Ab + Bc * Bc) - visc * visc * Cbc * Cbc / 4.0;
+    e.W00 = 40.0 * e.A / (81.0 * D) * (tv * Bc + vd * Ab);
+    e.W01 = -40.0 * e.A / (81.0 * D) * (visc * Cbc / 2.0);
+    e.W11 = 40.0 * e.A / (81.0 * D) * (tv * Ab + vd * Bc);
+    double *a = A64 + pos;
+    // tangent (:577-665)
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        const int row = 3 * (r >> 1) + (r & 1);
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2) {
+            const int col = 3 * (s2 >> 1) + (s2 & 1);
+            const int lo = r < s2 ? r : s2, hi2 = r < s2 ? s2 : r;
+            const int pl = lo & ~1, pu = hi2 & ~1;
+            double kvis;
+            if (!(lo & 1) && !(hi2 & 1)) kvis = e.kv * (2 * g[pl] * g[pu] + g[pl + 1] * g[pu + 1]);
+            else if ((lo & 1) && (hi2 & 1)) kvis = e.kv * (g[pl] * g[pu] + 2 * g[pl + 1] * g[pu + 1]);
+            else if (!(lo & 1)) kvis = e.kv * (g[pl + 1] * g[pu]);
+            else kvis = e.kv * (g[pl] * g[pu + 1]);
+            const double kls = e.ks * g[s2] * g[r];
+            double v;
+            if ((r & 1) == (s2 & 1)) {
+                const double N = third * e.A * e.C[s2 >> 1];
+                v = (r == 4 && s2 == 2) ? N + vms_nd(e, lo, hi2) + kvis + kls : N - vms_nd(e, lo, hi2) + kvis + kls;
+            } else {
+                v = kvis + kls;
+            }
+            a[(size_t)(row * 9 + col) * ld] = v;
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) a[(size_t)(row * 9 + 3 * k + 2) * ld] = -(sixth * g[r] - vms_gd(e, r, k));
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int row = 3 * k + 2;
+#pragma unroll
+        for (int s2 = 0; s2 < 6; ++s2)
+            a[(size_t)(row * 9 + 3 * (s2 >> 1) + (s2 & 1)) * ld] = sixth * g[s2] - vms_gd(e, s2, k);
+#pragma unroll
+        for (int m = 0; m < 3; ++m) a[(size_t)(row * 9 + 3 * m + 2) * ld] = k <= m ? vms_gphi(e, k, m) : vms_gphi(e, m, k);
+    }
+    // residual (:316-342, :532-573)
+    const double uv[6] = {Ue[0], Ue[1], Ue[3], Ue[4], Ue[6], Ue[7]}, pv[3] = {Ue[2], Ue[5], Ue[8]};
+    const double advx = e.duxdx * e.ux + e.duxdy * e.uy, advy = e.duydx * e.ux + e.duydy * e.uy;
+    const double sym = e.duxdy + e.duydx;
+    const double GTv = third * e.A * (e.duxdx + e.duydy);
+    double *fe = Fe + pos;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double Ndv[2], Gdv[2];
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            const int r = 2 * i + d;
+            double sN = vms_nd(e, r, 0) * uv[0];
+#pragma unroll
+            for (int s2 = 1; s2 < 6; ++s2) sN += vms_nd(e, r, s2) * uv[s2];
+            Ndv[d] = sN;
+            Gdv[d] = vms_gd(e, r, 0) * pv[0] + vms_gd(e, r, 1) * pv[1] + vms_gd(e, r, 2) * pv[2];
+        }
+        double Nphiv = -vms_gd(e, 0, i) * uv[0];
+#pragma unroll
+        for (int s2 = 1; s2 < 6; ++s2) Nphiv += -vms_gd(e, s2, i) * uv[s2];
+        const double Gphiv = vms_gphi(e, i, 0) * pv[0] + vms_gphi(e, i, 1) * pv[1] + vms_gphi(e, i, 2) * pv[2];
+        const double b = g[2 * i], c = g[2 * i + 1];
+        const double Nvx = third * e.A * advx, Nvy = third * e.A * advy;
+        const double Kvx = 0.5 * visc * (2 * b * e.duxdx + c * sym);
+        const double Kvy = 0.5 * visc * (2 * c * e.duydy + b * sym);
+        const double Ksx = e.ks * b * e.duxduy, Ksy = e.ks * c * e.duxduy;
+        const double Gvx = 0.5 * e.p * b, Gvy = 0.5 * e.p * c;
+        fe[(size_t)(3 * i + 0) * ld] = 0.0 - (Nvx - Ndv[0] + Kvx + Ksx - (Gvx - Gdv[0]));
+        fe[(size_t)(3 * i + 1) * ld] = 0.0 - (Nvy - Ndv[1] + Kvy + Ksy - (Gvy - Gdv[1]));
+        fe[(size_t)(3 * i + 2) * ld] = 0.0 - (GTv - Nphiv + Gphiv);
+    }
+}
+
+int ns_assemble_device(fg_system *s, double reynolds, int form, const double *u_dev, double *F_dev, cudaStream_t st)
 {
     const Topology &t = s->topo;
     if (t.ndof != 3) { set_error("Navier-Stokes assembly needs ndof == 3"); return FG_ERR_UNSUPPORTED; }
     if (!s->ns_geometry_ok) { set_error("Navier-Stokes assembly before fg_ns_set_geometry"); return FG_ERR_STATE; }
     if (!(reynolds > 0)) { set_error("Reynolds number must be positive"); return FG_ERR_ARG; }
-    if (t.nel > 0)
+    if (form != FG_NS_SUPG_PSPG && form != FG_NS_VMS_DCDD) {
+        set_error("Navier-Stokes form must be FG_NS_SUPG_PSPG or FG_NS_VMS_DCDD");
+        return FG_ERR_ARG;
+    }
+    if (t.nel > 0 && form == FG_NS_VMS_DCDD)
+        k_ns_vms_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(),
+                                                          s->gx.as<double>(), s->gy.as<double>(),
+                                                          s->node_dof.as<int>(), s->gup.as<double>(), u_dev, reynolds,
+                                                          s->A64.as<double>(), s->Fe.as<double>());
+    else if (t.nel > 0)
         k_ns_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(), s->gx.as<double>(),
                                                       s->gy.as<double>(), s->node_dof.as<int>(), s->gup.as<double>(),
                                                       s->gf1.as<double>(), s->gf2.as<double>(), u_dev, reynolds,

@@ -652,7 +652,7 @@ int fg_ns_assemble(fg_system *s, const fg_ns_coeffs *c, const double *u, double 
     int r = ensure_io(s);
     if (r) return r;
     if ((r = state_in(s, u, s->ws.t64.as<double>()))) return r;
-    if ((r = ns_assemble_device(s, c->reynolds, s->ws.t64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
+    if ((r = ns_assemble_device(s, c->reynolds, c->form, s->ws.t64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
     if (F) {
         if ((r = vec_out(s, s->ws.u64.as<double>(), F, s->ws.r64.as<double>()))) return r;
     }
@@ -695,7 +695,7 @@ int fg_ns_process(fg_system *s, const fg_ns_coeffs *c, const fg_solver_opts *o, 
     int it = 0, gmres = 0;
     while (delta > nonlinear_tol && it < max_nonlinear) {
         ++it;
-        if ((r = ns_assemble_device(s, c->reynolds, s->state_u.as<double>(), s->rhs_f.as<double>(), s->stream))) return r;
+        if ((r = ns_assemble_device(s, c->reynolds, c->form, s->state_u.as<double>(), s->rhs_f.as<double>(), s->stream))) return r;
         FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, 8 * (size_t)s->n_pad, cudaMemcpyDeviceToDevice, s->stream));
         int flags = c->precond == FG_PRECOND_DIAG ? FG_SETUP_ACCUMULATE : 0;
         if ((r = precond_setup_device(s, c->precond, flags, s->rhs_b.as<double>(), s->stream))) return r;

@@ -194,7 +194,7 @@ int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const ECh
 int matvec_device(fg_system *s, const double *x, double *y, int precision, cudaStream_t st);
 
 // Navier-Stokes (ns.cu), residual gather and the loops' BLAS-1 steps
-int ns_assemble_device(fg_system *s, double reynolds, const double *u_dev, double *F_dev, cudaStream_t st);
+int ns_assemble_device(fg_system *s, double reynolds, int form, const double *u_dev, double *F_dev, cudaStream_t st);
 int gather_residual(fg_system *s, const double *Fe, double *F, cudaStream_t st);
 // y += a x, out[0] = sum x^2, out[1] = sum y^2 (after the update)
 int axpy_norms_device(int n, double a, const double *x, double *y, double *part, double *out, cudaStream_t st);

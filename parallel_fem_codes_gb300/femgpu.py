@@ -21,6 +21,7 @@ FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED = 64, 32
 FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 = 0, 1, 2
+FG_NS_SUPG_PSPG, FG_NS_VMS_DCDD = 0, 1
 FG_REORDER_NONE, FG_REORDER_RCM = 0, 1
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE",
           5: "ERR_BREAKDOWN", 6: "ERR_NOTCONV", 7: "ERR_UNSUPPORTED", 8: "ERR_TIMEOUT"}
@@ -75,7 +76,7 @@ class ProcessStats(ctypes.Structure):
 
 
 class NSCoeffs(ctypes.Structure):
-    _fields_ = [("reynolds", _c_dbl), ("precond", _c_int)]
+    _fields_ = [("reynolds", _c_dbl), ("precond", _c_int), ("form", _c_int)]
 
 
 class EulerCoeffs(ctypes.Structure):
@@ -458,18 +459,19 @@ class System:
                                        np.ascontiguousarray(prob.upresc, dtype=np.float64),
                                        f1.ctypes.data, f2.ctypes.data))
 
-    def ns_assemble(self, prob, u=None):
-        """Build_K_F_SUPG_PSPG at u (free dofs, reference numbering); returns F (n+1)."""
-        c = NSCoeffs(prob.reynolds, FG_PRECOND_BLOCKDIAG)
+    def ns_assemble(self, prob, u=None, form=FG_NS_SUPG_PSPG):
+        """Build_K_F_SUPG_PSPG (or Build_K_F_VMS_DCDD with form=FG_NS_VMS_DCDD)
+        at u (free dofs, reference numbering); returns F (n+1)."""
+        c = NSCoeffs(prob.reynolds, FG_PRECOND_BLOCKDIAG, form)
         F = np.empty(self.n + 1)
         uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
         check(lib().fg_ns_assemble(self._h, ctypes.byref(c), _ptr(uu), F.ctypes.data))
         return F
 
     def ns_process(self, prob, u0=None, kmax=30, lmax=1000, tol=1e-10, nonlinear_tol=1e-3, max_nonlinear=100,
-                   precision=FG_PREC_FP64, inner_tol=0.0, precond=FG_PRECOND_BLOCKDIAG):
+                   precision=FG_PREC_FP64, inner_tol=0.0, precond=FG_PRECOND_BLOCKDIAG, form=FG_NS_SUPG_PSPG):
         """Picard loop from u0 (default 0); returns (u[n], stats)."""
-        c = NSCoeffs(prob.reynolds, precond)
+        c = NSCoeffs(prob.reynolds, precond, form)
         o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
         u = np.zeros(self.n) if u0 is None else np.array(u0, dtype=np.float64, copy=True)
         st = ProcessStats()

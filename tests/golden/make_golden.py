@@ -14,7 +14,9 @@ the Euler driver's Fill_LM, Build_M_K_F_SUPG at a state (u, du),
 BlockDiag_precond_EBE_setup, ebemvNDOF4 and the Predictor_Old time loop;
 and tests/golden/time_schemes_euler.npz: the final states of Predictor_Old_BDF and
 of Predictor_New_TRBDF2 (run with Build_M_K_F_SUPG, its bubble unknowns
-zero) on the Euler cases.
+zero) on the Euler cases; and tests/golden/vms_ns.npz: Build_K_F_VMS_DCDD
+(blocks and residual at a state u) and its Picard Process loop on the NS
+cases.
 """
 import os
 import sys
@@ -127,7 +129,22 @@ def write_euler_schemes():
     np.savez_compressed(os.path.join(HERE, "time_schemes_euler.npz"), **out)
 
 
+def write_ns_vms():
+    out = {}
+    for name, (prob, seed, run) in ns_cases().items():
+        m = prob.mesh
+        u = np.random.Generator(np.random.PCG64(seed + 11)).standard_normal(m.neq)
+        A, F = O.ref_ns_build(prob, u, form=1)
+        out[name + "_u"], out[name + "_A"], out[name + "_F"] = u, A, F
+        if run:
+            U, its = O.ref_ns_process(prob, 1e-10, 1e-3, 30, 1000, 20, form=1)
+            out[name + "_U"], out[name + "_its"] = U, its
+            print(name, "VMS-DCDD gmres", its)
+    np.savez_compressed(os.path.join(HERE, "vms_ns.npz"), **out)
+
+
 if __name__ == "__main__":
     main()
     write_euler()
     write_euler_schemes()
+    write_ns_vms()

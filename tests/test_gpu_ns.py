@@ -137,3 +137,25 @@ def test_ns_rejects_scalar_system(fg):
     s = fg.System(p.mesh)
     with pytest.raises(fg.FemGpuError):
         s.ns_set_geometry(G.ns_problem(G.multi_dof_mesh(9, 3), 10.0))
+
+
+@pytest.mark.parametrize("case", ["cavity33_jitter", "affine13"])
+def test_ns_vms_dcdd_assembly_bit_exact(fg, case):
+    """Build_K_F_VMS_DCDD on the device against the oracle (pinned to the
+    reference's build): blocks and residual bit-identical."""
+    p = G.cavity_problem(33, reynolds=400.0, jitter=0.2) if case == "cavity33_jitter" else _affine()
+    u = np.random.default_rng(9).standard_normal(p.mesh.neq)
+    A, F = O.build_ns(p, u, form=1)
+    s = fg.ns_system(p)
+    assert np.array_equal(s.ns_assemble(p, u, form=fg.FG_NS_VMS_DCDD), F)
+    assert np.array_equal(s.get_blocks(), A)
+
+
+def test_ns_vms_dcdd_process(fg):
+    p = G.cavity_problem(17, reynolds=100.0)
+    uo, nl_o, its_o, last_o = O.ns_process(p, 1e-10, 1e-6, 30, 1000, 40, form=1)
+    s = fg.ns_system(p)
+    ug, st = s.ns_process(p, kmax=30, tol=1e-10, nonlinear_tol=1e-6, max_nonlinear=40, form=fg.FG_NS_VMS_DCDD)
+    assert abs(st["nonlinear_iterations"] - nl_o) <= 1
+    assert st["nonlinear_residual"] <= 1e-6
+    assert rel(ug, uo) < 1e-7

@@ -93,3 +93,32 @@ def test_against_reference_build(n, jitter, re):
     inv, Fp = O.ref_ns_blockdiag(p.mesh, A, F)
     bd, ibd, Id, Fq = O.blockdiag_setup(p.mesh, A, F)
     assert np.array_equal(ibd, inv) and np.array_equal(Fq, Fp)
+
+
+VMS = os.path.join(os.path.dirname(__file__), "golden", "vms_ns.npz")
+
+
+@pytest.mark.parametrize("name", ["ns_9_cavity", "ns_9_affine"])
+def test_vms_dcdd_bit_exact(name, oracle_lib):
+    """Build_K_F_VMS_DCDD (StabilizationForm "VMS-DCDD") and, for the cavity,
+    its Picard loop: the restatement against the reference's own build."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")))
+    p = _problem(g)
+    v = np.load(VMS)
+    A, F = O.build_ns(p, v[name + "_u"], form=1)
+    assert np.array_equal(A, v[name + "_A"])
+    assert np.array_equal(F, v[name + "_F"])
+    if name + "_U" in v:
+        U, nl, its, last = O.ns_process(p, 1e-10, 1e-3, 30, 1000, 20, form=1)
+        assert its == int(v[name + "_its"])
+        assert np.array_equal(U, v[name + "_U"])
+
+
+def test_vms_dcdd_against_reference_build(oracle_lib):
+    if O.ref_ns() is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    p = G.cavity_problem(13, reynolds=1000.0, jitter=0.2, seed=5)
+    u = np.random.default_rng(13).standard_normal(p.mesh.neq)
+    A0, F0 = O.ref_ns_build(p, u, form=1)
+    A1, F1 = O.build_ns(p, u, form=1)
+    assert np.array_equal(A0, A1) and np.array_equal(F0, F1)
