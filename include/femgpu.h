@@ -267,8 +267,15 @@ typedef struct {
     double gamma;        /* Reaction()                                */
     double beta[2];      /* Velocity() (constant field)               */
     double f;            /* Font() (constant source)                  */
-    int cau;             /* 1: CAU shock capture (CAU_ShockCapture.c) */
+    int cau;             /* ShockCapture: 1 "CAU" (CAU_ShockCapture.c),
+                            2 "CAUDD" (CAU_DD_ShockCapture.c, DD form
+                            only), 0 none                             */
+    int form;            /* StabilizationForm: FG_TRANSPORT_SUPG (0)
+                            Build_K_F_SUPG.c, or FG_TRANSPORT_DD
+                            Build_K_F_DD.c:4-178 (steady builds only) */
 } fg_transport_coeffs;
+enum { FG_TRANSPORT_SUPG = 0, FG_TRANSPORT_DD = 1 };
+enum { FG_SHOCK_NONE = 0, FG_SHOCK_CAU = 1, FG_SHOCK_CAUDD = 2 };
 
 /* Set node coordinates (x, y) and Dirichlet values upresc[nnodes]. */
 int fg_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc);

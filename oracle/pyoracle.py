@@ -118,6 +118,8 @@ def ref():
         R.fr_symrcm.restype = None
         R.fr_sst_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
         R.fr_sst_layout.restype = None
+        R.fr_sst_set_form.argtypes = [_c_int, _c_int]
+        R.fr_sst_set_form.restype = None
         _ref = R
     return _ref
 
@@ -349,7 +351,7 @@ def ref_ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=100
 
 class _Problem(ctypes.Structure):
     _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl),
-                ("upresc", ctypes.POINTER(_c_dbl)), ("cau", _c_int)]
+                ("upresc", ctypes.POINTER(_c_dbl)), ("cau", _c_int), ("form", _c_int)]
 
 
 def _mesh_args(m):
@@ -361,7 +363,7 @@ def _mesh_args(m):
 def _problem_struct(p):
     up = np.ascontiguousarray(p.upresc, dtype=np.float64)
     s = _Problem(p.k, p.gamma, (_c_dbl * 2)(*p.beta), p.f,
-                 up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(p.cau))
+                 up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(p.cau), int(getattr(p, "form", 0)))
     return s, up
 
 
@@ -540,6 +542,12 @@ def ref_connectivity(mesh):
     return lm.reshape(mesh.nel, 3), perm, inv, band, nnz
 
 
+def _ref_form(prob):
+    """StabilizationForm / ShockCapture of the reference run: "SUPG" or "DD",
+    "CAU" (cau 1, and the reference's stand-in for cau 0) or "CAUDD"."""
+    ref().fr_sst_set_form(int(getattr(prob, "form", 0)), 2 if int(prob.cau) == 2 else 1)
+
+
 def ref_build(prob, u=None):
     m = prob.mesh
     if u is None:
@@ -547,6 +555,7 @@ def ref_build(prob, u=None):
     A = np.empty(m.nel * 9)
     F = np.empty(m.neq + 1)
     F[m.neq] = 0.0
+    _ref_form(prob)
     ref().fr_sst_build(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f,
                        prob.upmode, prob.upval, np.ascontiguousarray(u, dtype=np.float64), A, F)
     return A.reshape(m.nel, 9), F
@@ -556,6 +565,7 @@ def ref_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000):
     m = prob.mesh
     U = np.zeros(m.neq + 1)
     its = _c_int(0)
+    _ref_form(prob)
     ref().fr_sst_process(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f,
                          prob.upmode, prob.upval, solver_tol, nonlinear_tol, kmax, lmax, U, ctypes.byref(its))
     return U[:m.neq].copy(), its.value

@@ -55,6 +55,15 @@ typedef struct {
     FemOtherFunctionsType O;
 } fr_sst;
 
+static int g_form, g_shock = 1;  /* StabilizationForm 0 "SUPG" / 1 "DD"; ShockCapture 1 "CAU" / 2 "CAUDD" */
+
+/* Stabilisation of the following builds and Process runs. */
+void fr_sst_set_form(int form, int shock)
+{
+    g_form = form;
+    g_shock = shock;
+}
+
 static void fr_setup(fr_sst *c, int nnodes, int nel, const double *x, const double *y,
                      const int *type, const int *invp, const int *ien, int neq,
                      double solver_tol, double nl_tol, int kmax, int lmax)
@@ -67,8 +76,8 @@ static void fr_setup(fr_sst *c, int nnodes, int nel, const double *x, const doub
     strcpy(c->P.Scaling, "NOT");
     strcpy(c->P.reordering, "SYMRCM");
     strcpy(c->P.MatrixVectorProductScheme, "EBE");
-    strcpy(c->P.StabilizationForm, "SUPG");
-    strcpy(c->P.ShockCapture, "CAU");
+    strcpy(c->P.StabilizationForm, g_form ? "DD" : "SUPG");
+    strcpy(c->P.ShockCapture, g_shock == 2 ? "CAUDD" : "CAU");
     strcpy(c->P.h_Shock, "2sqrtArea");
     c->P.SolverTolerance = solver_tol;
     c->P.NonLinearTolerance = nl_tol;
@@ -165,7 +174,7 @@ int fr_sst_connectivity(int nnodes, int nel, const double *x, const double *y,
     return c.P.nnzero;
 }
 
-/* One Build_K_F_SUPG call at the free-dof state u. */
+/* One build (Build_K_F_SUPG or Build_K_F_DD by the form) at the free-dof state u. */
 void fr_sst_build(int nnodes, int nel, const double *x, const double *y,
                   const int *type, const int *invp, const int *ien, int neq,
                   double k, double gamma, double bx, double by, double f,
@@ -181,7 +190,7 @@ void fr_sst_build(int nnodes, int nel, const double *x, const double *y,
     setPreconditioner(&c.P, &c.F);
     setStabilizationForm(&c.P, &c.F, &c.O);
     memcpy(c.S.u, u, sizeof(double) * (size_t)neq);
-    Build_K_F_SUPG(&c.P, &c.M, &c.S, &c.F);
+    c.O.Build_K_F(&c.P, &c.M, &c.S, &c.F);
     memcpy(A_out, c.M.Aaux, sizeof(double) * 9 * (size_t)nel);
     memcpy(F_out, c.S.F, sizeof(double) * (size_t)neq);
     fr_free(&c);

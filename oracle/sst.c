@@ -4,9 +4,11 @@
  *
  * Restates 01_SS_Transport_Equation/2D/01_CommonFiles/Build_K_F_SUPG.c with
  * CAU_ShockCapture.c, h_shock_2sqrtArea.c, F_assembly.c, ebe_assembly.c and
- * the Process.c fixed-point loop.  The element formulas are those of the
- * reference, term for term, so that the element blocks agree to the last bit
- * when both are compiled without floating-point contraction.
+ * the Process.c fixed-point loop, and (form 1, StabilizationForm "DD")
+ * Build_K_F_DD.c:4-178 with CAU_DD_ShockCapture.c:3-22.  The element
+ * formulas are those of the reference, term for term, so that the element
+ * blocks agree to the last bit when both are compiled without
+ * floating-point contraction.
  */
 #include "femoracle.h"
 #include <stdlib.h>
@@ -37,6 +39,74 @@ static double cau(double kx, double ky, double bx, double by, double gamma,
     return 0;
 }
 
+/* CAU_DD_ShockCapture (CAU_DD_ShockCapture.c:3-22): 0.5 h |R(u)| / |grad u|. */
+static double cau_dd(double bx, double by, double gamma, double ue1, double ue2, double ue3, double ueb,
+                     double feb, double y23, double y31, double y12, double x32, double x13, double x21,
+                     double invArea, double h)
+{
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = bgu + gamma*ueb - feb;
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    return ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0;
+}
+
+/* Build_K_F_DD.c:54-164: Galerkin + dynamic diffusion with the bubble
+ * (KBB, KhB, KBh, FB) condensed into the 3x3 block and the load. */
+static void dd_element(double kx, double ky, double bx, double by, double gamma, const double fe[3],
+                       const double ue[3], int shock, const double X[3], const double Y[3], double ke[3][3],
+                       double Fe[3])
+{
+    const double third = 1.0/3.0, sixth = 1.0/6.0, seventh = 1.0/7.0, twelfth = 1.0/12.0;
+    const double t320 = 3./20.0, n920 = 9./20.0, n940 = 9./40.0;
+    double y23 = Y[1] - Y[2], y31 = Y[2] - Y[0], y12 = Y[0] - Y[1];
+    double x32 = X[2] - X[1], x13 = X[0] - X[2], x21 = X[1] - X[0];
+    double TwoA = x21*y31 - x13*y12;
+    double Area = 0.5*TwoA;
+    double invArea = 1.0/Area;
+    double feb = third*(fe[0] + fe[1] + fe[2]);
+    double ueb = third*(ue[0] + ue[1] + ue[2]);
+    double a[3] = { bx*y23 + by*x32, bx*y31 + by*x13, bx*y12 + by*x21 };
+    double C12 = y23*y31 + x32*x13, C13 = y23*y12 + x32*x21, C23 = y31*y12 + x13*x21;
+    double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+    double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+    double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+    double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
+    double h = sqrt(fabs(2*Area));                          /* h_shock_2sqrtArea */
+    double Eu = 0.0;
+    if (shock == 2)
+        Eu = cau_dd(bx, by, gamma, ue[0], ue[1], ue[2], ueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
+    else if (shock == 1)
+        Eu = cau(kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
+    double K12 = 0.25*Eu*invArea*C12, K13 = 0.25*Eu*invArea*C13, K23 = 0.25*Eu*invArea*C23;
+    double Khh[3][3];
+    Khh[0][0] = -(D12 + D13) + sixth*a[0] + R11 -(K12 + K13);
+    Khh[0][1] =          D12 + sixth*a[1] + R12 + K12;
+    Khh[0][2] =          D13 + sixth*a[2] + R12 + K13;
+    Khh[1][0] =          D12 + sixth*a[0] + R12 + K12;
+    Khh[1][1] = -(D12 + D23) + sixth*a[1] + R11 -(K12 + K23);
+    Khh[1][2] =          D23 + sixth*a[2] + R12 + K23;
+    Khh[2][0] =          D13 + sixth*a[0] + R12 + K13;
+    Khh[2][1] =          D23 + sixth*a[1] + R12 + K23;
+    Khh[2][2] = -(D13 + D23) + sixth*a[2] + R11 -(K13 + K23);
+    double KhB[3], KBh[3];
+    KhB[0] = n920*(0.5*a[0] + a[1] + a[2]) + t320*gamma*Area;
+    KhB[1] = n920*(a[0] + 0.5*a[1] + a[2]) + t320*gamma*Area;
+    KhB[2] = n920*(a[0] + a[1] + 0.5*a[2]) + t320*gamma*Area;
+    for (int i = 0; i < 3; i++) KBh[i] = n940*a[i] + t320*gamma*Area;
+    double KBB = -9*n940*(D12 + D13 + D23) + seventh*t320*(a[0] + a[1] + a[2]) + 9*seventh*n940*Area
+               - Eu*invArea*(C12 + C13 + C23)/360.;
+    double invKBB = 1.0/KBB;
+    double Fh[3] = { twelfth*Area*(2*fe[0] + fe[1] + fe[2]), twelfth*Area*(fe[0] + 2*fe[1] + fe[2]),
+                     twelfth*Area*(fe[0] + fe[1] + 2*fe[2]) };
+    double FB = t320*Area*(fe[0] + fe[1] + fe[2]);
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j < 3; j++) ke[i][j] = Khh[i][j] - invKBB*KhB[i]*KBh[j];
+        Fe[i] = Fh[i] - invKBB*KhB[i]*FB;
+    }
+}
+
 void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
                        const int *type, const int *invp, const int *ien, int neq,
                        const or_transport_problem *prob, const double *u,
@@ -53,6 +123,23 @@ void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
 
     for (E = 0; E < nel; E++) {
         int J1 = ien[3*E], J2 = ien[3*E+1], J3 = ien[3*E+2];
+        if (prob->form == 1) {                   /* StabilizationForm "DD" */
+            const double Xv[3] = { x[J1], x[J2], x[J3] }, Yv[3] = { y[J1], y[J2], y[J3] };
+            const double fv[3] = { prob->f, prob->f, prob->f }, uv[3] = { U[J1], U[J2], U[J3] };
+            double ke[3][3], Fe[3];
+            dd_element(kx, ky, prob->beta[0], prob->beta[1], gamma, fv, uv, prob->cau, Xv, Yv, ke, Fe);
+            const int V[3] = { J1, J2, J3 };
+            for (int a = 0; a < 3; a++) {        /* F_assembly.c:3-28 */
+                if (type[V[a]] != 1) continue;
+                F[invp[V[a]]] += Fe[a];
+                for (int b = 0; b < 3; b++)
+                    if (b != a && type[V[b]] == 0) F[invp[V[a]]] -= ke[a][b] * prob->upresc[V[b]];
+            }
+            double *Ae = A + 9L * E;
+            for (int r = 0; r < 3; r++)
+                for (int c = 0; c < 3; c++) Ae[3*r + c] = ke[r][c];
+            continue;
+        }
         double X0 = x[J1], X1 = x[J2], X2 = x[J3];
         double Y0 = y[J1], Y1 = y[J2], Y2 = y[J3];
         double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;

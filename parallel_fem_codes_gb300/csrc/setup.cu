@@ -450,6 +450,90 @@ __global__ void k_transport_elem(int nel, int ld, const int *__restrict__ gien, 
     Fe[2 * (size_t)ld + pos] = Area*twelfth*(fe1 + fe2 + 2*fe3) + sixth*tau*(fe1+fe2+fe3)*(bx*y12 + by*x21);
 }
 
+// CAU_DD_ShockCapture.c:3-22: 0.5 h |R(u)| / |grad u| (0 below 1e-10)
+__device__ double cau_dd_eu(double bx, double by, double gamma, double ue1, double ue2, double ue3, double ueb,
+                            double feb, double y23, double y31, double y12, double x32, double x13, double x21,
+                            double invArea, double h)
+{
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = bgu + gamma*ueb - feb;
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    return ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0.0;
+}
+
+// Build_K_F_DD.c:54-164 (StabilizationForm "DD"): Galerkin with dynamic
+// diffusion, the element bubble (KBB, KhB, KBh, FB) condensed into the 3x3
+// block and the load: ke = Khh - KhB KBh / KBB, Fe = Fh - KhB FB / KBB, each
+// term associated as the reference writes it (note R11 = (gamma/6) Area
+// here, against gamma Area / 6 in the SUPG build).
+__global__ void k_transport_dd_elem(int nel, int ld, const int *__restrict__ gien, const double *__restrict__ gx,
+                                    const double *__restrict__ gy, const int *__restrict__ gtype,
+                                    const int *__restrict__ node_dof, const double *__restrict__ up,
+                                    const double *__restrict__ u, fg_transport_coeffs cf,
+                                    double *__restrict__ A64, double *__restrict__ Fe)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const double third = 1.0/3.0, sixth = 1.0/6.0, seventh = 1.0/7.0, twelfth = 1.0/12.0;
+    const double t320 = 3./20.0, n920 = 9./20.0, n940 = 9./40.0;
+    const double kx = cf.k, ky = cf.k, gamma = cf.gamma, bx = cf.beta[0], by = cf.beta[1];
+    int J1 = gien[pos], J2 = gien[ld + pos], J3 = gien[2 * (size_t)ld + pos];
+    double X0 = gx[J1], X1 = gx[J2], X2 = gx[J3];
+    double Y0 = gy[J1], Y1 = gy[J2], Y2 = gy[J3];
+    double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+    double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+    double TwoA = x21*y31 - x13*y12;
+    double Area = 0.5*TwoA;
+    double invArea = 1.0/Area;
+    double fe1 = cf.f, fe2 = cf.f, fe3 = cf.f;
+    double feb = third*(fe1 + fe2 + fe3);
+    double ue1 = gtype[J1] == 0 ? up[J1] : u[node_dof[J1]];
+    double ue2 = gtype[J2] == 0 ? up[J2] : u[node_dof[J2]];
+    double ue3 = gtype[J3] == 0 ? up[J3] : u[node_dof[J3]];
+    double ueb = third*(ue1 + ue2 + ue3);
+    double a1 = bx*y23 + by*x32, a2 = bx*y31 + by*x13, a3 = bx*y12 + by*x21;
+    double C12 = y23*y31 + x32*x13, C13 = y23*y12 + x32*x21, C23 = y31*y12 + x13*x21;
+    double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+    double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+    double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+    double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
+    double h = sqrt(fabs(2*Area));
+    double Eu = 0.0;
+    if (cf.cau == 2)
+        Eu = cau_dd_eu(bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
+    else if (cf.cau == 1)
+        Eu = cau_eu(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
+    double K12 = 0.25*Eu*invArea*C12, K13 = 0.25*Eu*invArea*C13, K23 = 0.25*Eu*invArea*C23;
+    double Khh[9];
+    Khh[0] = -(D12 + D13) + sixth*a1 + R11 -(K12 + K13);
+    Khh[1] =          D12 + sixth*a2 + R12 + K12;
+    Khh[2] =          D13 + sixth*a3 + R12 + K13;
+    Khh[3] =          D12 + sixth*a1 + R12 + K12;
+    Khh[4] = -(D12 + D23) + sixth*a2 + R11 -(K12 + K23);
+    Khh[5] =          D23 + sixth*a3 + R12 + K23;
+    Khh[6] =          D13 + sixth*a1 + R12 + K13;
+    Khh[7] =          D23 + sixth*a2 + R12 + K23;
+    Khh[8] = -(D13 + D23) + sixth*a3 + R11 -(K13 + K23);
+    const double KhB[3] = {n920*(0.5*a1 + a2 + a3) + t320*gamma*Area, n920*(a1 + 0.5*a2 + a3) + t320*gamma*Area,
+                           n920*(a1 + a2 + 0.5*a3) + t320*gamma*Area};
+    const double KBh[3] = {n940*a1 + t320*gamma*Area, n940*a2 + t320*gamma*Area, n940*a3 + t320*gamma*Area};
+    double KBB = -9*n940*(D12 + D13 + D23) + seventh*t320*(a1 + a2 + a3) + 9*seventh*n940*Area
+               - Eu*invArea*(C12 + C13 + C23)/360.;
+    double invKBB = 1.0/KBB;
+    const double Fh[3] = {twelfth*Area*(2*fe1 + fe2 + fe3), twelfth*Area*(fe1 + 2*fe2 + fe3),
+                          twelfth*Area*(fe1 + fe2 + 2*fe3)};
+    double FB = t320*Area*(fe1 + fe2 + fe3);
+    double *a = A64 + pos;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) a[(size_t)(3 * i + j) * ld] = Khh[3 * i + j] - invKBB*KhB[i]*KBh[j];
+        Fe[(size_t)i * ld + pos] = Fh[i] - invKBB*KhB[i]*FB;
+    }
+}
+
 // F_assembly (F_assembly.c:3-28) as a gather per free dof, in reference
 // element order: F += Fe_a, then F -= ke[a][b] * upresc(b) for the
 // Dirichlet vertices b of the element in vertex order.
@@ -614,6 +698,10 @@ int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev,
     const Topology &t = s->topo;
     if (t.ndof != 1) { set_error("transient transport assembly needs ndof == 1"); return FG_ERR_UNSUPPORTED; }
     if (!s->geometry_ok) { set_error("transient transport assembly before fg_set_geometry"); return FG_ERR_STATE; }
+    if (c->c.form != FG_TRANSPORT_SUPG || c->c.cau < FG_SHOCK_NONE || c->c.cau > FG_SHOCK_CAU) {
+        set_error("transient transport builds the SUPG form with CAU or no shock capture");
+        return FG_ERR_UNSUPPORTED;
+    }
     int r;
     if (s->Fe.bytes < 8 * (size_t)12 * s->nel_pad && (r = s->Fe.alloc(8 * (size_t)12 * s->nel_pad))) return r;
     if (t.nel > 0)
@@ -637,7 +725,21 @@ int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c, const 
     const Topology &t = s->topo;
     if (t.ndof != 1) { set_error("transport assembly needs ndof == 1"); return FG_ERR_UNSUPPORTED; }
     if (!s->geometry_ok) { set_error("transport assembly before fg_set_geometry"); return FG_ERR_STATE; }
-    if (t.nel > 0)
+    if (c->form != FG_TRANSPORT_SUPG && c->form != FG_TRANSPORT_DD) {
+        set_error("transport form must be FG_TRANSPORT_SUPG or FG_TRANSPORT_DD");
+        return FG_ERR_ARG;
+    }
+    if (c->cau < FG_SHOCK_NONE || c->cau > FG_SHOCK_CAUDD || (c->cau == FG_SHOCK_CAUDD && c->form != FG_TRANSPORT_DD)) {
+        set_error("shock capture must be NONE or CAU, or CAUDD with the DD form");
+        return FG_ERR_ARG;
+    }
+    if (t.nel > 0 && c->form == FG_TRANSPORT_DD)
+        k_transport_dd_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(),
+                                                                s->gx.as<double>(), s->gy.as<double>(),
+                                                                s->gtype.as<int>(), s->node_dof.as<int>(),
+                                                                s->gup.as<double>(), u_dev, *c, s->A64.as<double>(),
+                                                                s->Fe.as<double>());
+    else if (t.nel > 0)
         k_transport_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(), s->gx.as<double>(),
                                                              s->gy.as<double>(), s->gtype.as<int>(), s->node_dof.as<int>(),
                                                              s->gup.as<double>(), u_dev, *c, s->A64.as<double>(),

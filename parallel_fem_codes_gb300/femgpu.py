@@ -22,6 +22,8 @@ FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED = 64, 32
 FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 = 0, 1, 2
 FG_NS_SUPG_PSPG, FG_NS_VMS_DCDD = 0, 1
+FG_TRANSPORT_SUPG, FG_TRANSPORT_DD = 0, 1
+FG_SHOCK_NONE, FG_SHOCK_CAU, FG_SHOCK_CAUDD = 0, 1, 2
 FG_REORDER_NONE, FG_REORDER_RCM = 0, 1
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE",
           5: "ERR_BREAKDOWN", 6: "ERR_NOTCONV", 7: "ERR_UNSUPPORTED", 8: "ERR_TIMEOUT"}
@@ -58,7 +60,8 @@ class SolveStats(ctypes.Structure):
 
 
 class TransportCoeffs(ctypes.Structure):
-    _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl), ("cau", _c_int)]
+    _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl), ("cau", _c_int),
+                ("form", _c_int)]
 
 
 class TTCoeffs(ctypes.Structure):
@@ -425,7 +428,7 @@ class System:
                                     np.ascontiguousarray(upresc, dtype=np.float64)))
 
     def transport_assemble(self, prob, u=None):
-        c = TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau))
+        c = _coeffs(prob)
         F = np.empty(self.n + 1)
         uu = None if u is None else np.ascontiguousarray(u, dtype=np.float64)
         check(lib().fg_transport_assemble(self._h, ctypes.byref(c), _ptr(uu), F.ctypes.data))
@@ -442,7 +445,7 @@ class System:
 
     def transport_process(self, prob, kmax=30, lmax=1000, tol=1e-10, nonlinear_tol=1e-3, max_nonlinear=1000,
                           precision=FG_PREC_FP64):
-        c = TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau))
+        c = _coeffs(prob)
         o = SolverOpts(kmax, lmax, tol, precision, 0.0)
         U = np.zeros(self.n)
         st = ProcessStats()
@@ -570,7 +573,8 @@ def ns_system(prob, reorder=False) -> System:
 
 
 def _coeffs(prob):
-    return TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau))
+    return TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau),
+                           int(getattr(prob, "form", 0)))
 
 
 def launch_count() -> int:

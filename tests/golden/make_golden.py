@@ -16,7 +16,9 @@ and tests/golden/time_schemes_euler.npz: the final states of Predictor_Old_BDF a
 of Predictor_New_TRBDF2 (run with Build_M_K_F_SUPG, its bubble unknowns
 zero) on the Euler cases; and tests/golden/vms_ns.npz: Build_K_F_VMS_DCDD
 (blocks and residual at a state u) and its Picard Process loop on the NS
-cases.
+cases; and tests/golden/dd_sst.npz: the steady transport driver's
+Build_K_F_DD with CAUDD and with CAU (blocks and F at a state u) and its
+Process loop on the transport cases.
 """
 import os
 import sys
@@ -143,8 +145,27 @@ def write_ns_vms():
     np.savez_compressed(os.path.join(HERE, "vms_ns.npz"), **out)
 
 
+def write_sst_dd():
+    out = {}
+    for name, (n, ang, k, gm, f, upm, upv) in CASES.items():
+        if name == "sst_9_teste":
+            continue
+        for shock in (1, 2):
+            p = G.transport_problem(n, angle_deg=ang, k=k, gamma=gm, f=f, upmode=upm, upval=upv, cau=shock)
+            p.form = 1
+            u = np.random.Generator(np.random.PCG64(n + shock)).random(p.mesh.neq)
+            A, F = O.ref_build(p, u)
+            U, its = O.ref_process(p, 1e-10, 1e-3, 30, 1000)
+            key = f"{name}_c{shock}"
+            out[key + "_u"], out[key + "_A"], out[key + "_F"] = u, A, F[: p.mesh.neq]
+            out[key + "_U"], out[key + "_its"] = U, its
+            print(key, "DD process gmres", its)
+    np.savez_compressed(os.path.join(HERE, "dd_sst.npz"), **out)
+
+
 if __name__ == "__main__":
     main()
     write_euler()
     write_euler_schemes()
     write_ns_vms()
+    write_sst_dd()

@@ -162,3 +162,35 @@ def test_teste_exact_solution(fg):
     s = fg.transport_system(p)
     U, st = s.transport_process(p, 30, 1000, 1e-12, 1e-6)
     assert np.max(np.abs(U - 10.0)) < 1e-9
+
+
+@pytest.mark.parametrize("shock", [1, 2], ids=["cau", "caudd"])
+def test_dd_assembly_bit_exact(fg, shock):
+    """Build_K_F_DD (StabilizationForm "DD") on the device against the
+    oracle, which is bit-exact with the reference's build."""
+    p = G.transport_problem(33, angle_deg=110.0, k=1e-4, gamma=0.2, f=0.5, cau=shock)
+    p.form = fg.FG_TRANSPORT_DD
+    m = p.mesh
+    s = fg.transport_system(p)
+    for u in (None, np.random.default_rng(5).random(m.neq)):
+        A0, F0 = O.build_k_f_supg(p, u)
+        F = s.transport_assemble(p, u)
+        assert np.array_equal(s.get_blocks(), A0)
+        assert np.array_equal(F[:-1], F0[:-1])
+
+
+def test_dd_process_matches_oracle(fg):
+    p = G.transport_problem(33, cau=2)
+    p.form = fg.FG_TRANSPORT_DD
+    U0, nl0, it0 = O.transport_process(p, 1e-10, 1e-3, 30, 1000)
+    s = fg.transport_system(p)
+    U, st = s.transport_process(p, 30, 1000, 1e-10, 1e-3)
+    assert st["nonlinear_iterations"] == nl0
+    assert rel(U, U0) <= 1e-9
+
+
+def test_caudd_needs_dd_form(fg):
+    p = G.transport_problem(9, cau=2)
+    s = fg.transport_system(p)
+    with pytest.raises(Exception):
+        s.transport_assemble(p)

@@ -117,3 +117,35 @@ def test_structured_mesh_matches_generator_order(oracle_lib):
         O.lib().or_mesh_structured(M, M, 0.0, 0.0, 1.0, 1.0, left, x, y, ien)
         X, Y, I = G.structured_mesh(M, M, left=bool(left))
         assert np.array_equal(X, x) and np.array_equal(Y, y) and np.array_equal(I.reshape(-1), ien)
+
+
+DD = os.path.join(os.path.dirname(__file__), "golden", "dd_sst.npz")
+
+
+@pytest.mark.parametrize("name", ["sst_17_adv", "sst_12_mixed"])
+@pytest.mark.parametrize("shock", [1, 2], ids=["cau", "caudd"])
+def test_dd_bit_exact(name, shock, oracle_lib):
+    """StabilizationForm "DD" (Build_K_F_DD with CAU or CAUDD): blocks, F and
+    the whole Process loop against the reference's own run."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")))
+    p = _problem(g)
+    p.form, p.cau = 1, shock
+    d = np.load(DD)
+    key = f"{name}_c{shock}"
+    A, F = O.build_k_f_supg(p, d[key + "_u"])
+    assert np.array_equal(A, d[key + "_A"])
+    assert np.array_equal(F[: p.mesh.neq], d[key + "_F"])
+    U, nl, its = O.transport_process(p, 1e-10, 1e-3, 30, 1000)
+    assert its == int(d[key + "_its"])
+    assert np.array_equal(U, d[key + "_U"])
+
+
+def test_dd_against_reference_build(oracle_lib):
+    if not O.ref_available():
+        pytest.skip("reference build (oracle/_ref) not present")
+    p = G.transport_problem(21, angle_deg=110.0, k=1e-4, gamma=0.2, f=0.5, cau=2)
+    p.form = 1
+    u = np.random.default_rng(21).random(p.mesh.neq)
+    A0, F0 = O.ref_build(p, u)
+    A1, F1 = O.build_k_f_supg(p, u)
+    assert np.array_equal(A0, A1) and np.array_equal(F0[:-1], F1[:-1])
