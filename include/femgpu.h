@@ -269,13 +269,19 @@ typedef struct {
     double f;            /* Font() (constant source)                  */
     int cau;             /* ShockCapture: 1 "CAU" (CAU_ShockCapture.c),
                             2 "CAUDD" (CAU_DD_ShockCapture.c, DD form
-                            only), 0 none                             */
+                            only), 3 "YZBeta" (YZBeta_ShockCapture.c:
+                            per-element state kept on the device
+                            across builds, zeroed when a Process run
+                            starts), 0 none                           */
     int form;            /* StabilizationForm: FG_TRANSPORT_SUPG (0)
                             Build_K_F_SUPG.c, or FG_TRANSPORT_DD
                             Build_K_F_DD.c:4-178 (steady builds only) */
+    int h_shock;         /* h_Shock: FG_HSHOCK_2SQRTAREA (0), _OPTION1
+                            (h_shock_Option1.c), _OPTION2 (steady)    */
 } fg_transport_coeffs;
 enum { FG_TRANSPORT_SUPG = 0, FG_TRANSPORT_DD = 1 };
-enum { FG_SHOCK_NONE = 0, FG_SHOCK_CAU = 1, FG_SHOCK_CAUDD = 2 };
+enum { FG_SHOCK_NONE = 0, FG_SHOCK_CAU = 1, FG_SHOCK_CAUDD = 2, FG_SHOCK_YZBETA = 3 };
+enum { FG_HSHOCK_2SQRTAREA = 0, FG_HSHOCK_OPTION1 = 1, FG_HSHOCK_OPTION2 = 2 };
 
 /* Set node coordinates (x, y) and Dirichlet values upresc[nnodes]. */
 int fg_set_geometry(fg_system *s, const double *x, const double *y, const double *upresc);

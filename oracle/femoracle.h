@@ -107,8 +107,10 @@ typedef struct {
     double beta[2];      /* Velocity(): constant field                       */
     double f;            /* Font(): constant source                          */
     const double *upresc;/* Dirichlet value per node (read where type == 0)  */
-    int cau;             /* 1: CAU, 2: CAUDD (DD form only), 0: none        */
+    int cau;             /* 1: CAU, 2: CAUDD (DD form only), 3: YZBeta, 0: none */
     int form;            /* 0: SUPG, 1: DD (StabilizationForm)               */
+    int h_shock;         /* 0: 2sqrtArea, 1: Option1, 2: Option2             */
+    double *Re_old, *delta_old; /* [nel] YZBeta state, NULL: fresh zeros    */
 } or_transport_problem;
 
 /* Build_K_F_SUPG + CAU_ShockCapture + h_shock_2sqrtArea + F_assembly +

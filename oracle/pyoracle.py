@@ -118,7 +118,7 @@ def ref():
         R.fr_symrcm.restype = None
         R.fr_sst_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
         R.fr_sst_layout.restype = None
-        R.fr_sst_set_form.argtypes = [_c_int, _c_int]
+        R.fr_sst_set_form.argtypes = [_c_int, _c_int, _c_int]
         R.fr_sst_set_form.restype = None
         _ref = R
     return _ref
@@ -351,7 +351,8 @@ def ref_ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=100
 
 class _Problem(ctypes.Structure):
     _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl),
-                ("upresc", ctypes.POINTER(_c_dbl)), ("cau", _c_int), ("form", _c_int)]
+                ("upresc", ctypes.POINTER(_c_dbl)), ("cau", _c_int), ("form", _c_int), ("h_shock", _c_int),
+                ("Re_old", ctypes.c_void_p), ("delta_old", ctypes.c_void_p)]
 
 
 def _mesh_args(m):
@@ -363,7 +364,8 @@ def _mesh_args(m):
 def _problem_struct(p):
     up = np.ascontiguousarray(p.upresc, dtype=np.float64)
     s = _Problem(p.k, p.gamma, (_c_dbl * 2)(*p.beta), p.f,
-                 up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(p.cau), int(getattr(p, "form", 0)))
+                 up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(p.cau), int(getattr(p, "form", 0)),
+                 int(getattr(p, "h_shock", 0)), None, None)
     return s, up
 
 
@@ -545,7 +547,8 @@ def ref_connectivity(mesh):
 def _ref_form(prob):
     """StabilizationForm / ShockCapture of the reference run: "SUPG" or "DD",
     "CAU" (cau 1, and the reference's stand-in for cau 0) or "CAUDD"."""
-    ref().fr_sst_set_form(int(getattr(prob, "form", 0)), 2 if int(prob.cau) == 2 else 1)
+    ref().fr_sst_set_form(int(getattr(prob, "form", 0)), int(prob.cau) if int(prob.cau) in (2, 3) else 1,
+                          int(getattr(prob, "h_shock", 0)))
 
 
 def ref_build(prob, u=None):

@@ -55,13 +55,16 @@ typedef struct {
     FemOtherFunctionsType O;
 } fr_sst;
 
-static int g_form, g_shock = 1;  /* StabilizationForm 0 "SUPG" / 1 "DD"; ShockCapture 1 "CAU" / 2 "CAUDD" */
+/* StabilizationForm 0 "SUPG" / 1 "DD"; ShockCapture 1 "CAU" / 2 "CAUDD" /
+ * 3 "YZBeta"; h_Shock 0 "2sqrtArea" / 1 "Option1" / 2 "Option2" */
+static int g_form, g_shock = 1, g_hshock;
 
 /* Stabilisation of the following builds and Process runs. */
-void fr_sst_set_form(int form, int shock)
+void fr_sst_set_form(int form, int shock, int hshock)
 {
     g_form = form;
     g_shock = shock;
+    g_hshock = hshock;
 }
 
 static void fr_setup(fr_sst *c, int nnodes, int nel, const double *x, const double *y,
@@ -77,8 +80,8 @@ static void fr_setup(fr_sst *c, int nnodes, int nel, const double *x, const doub
     strcpy(c->P.reordering, "SYMRCM");
     strcpy(c->P.MatrixVectorProductScheme, "EBE");
     strcpy(c->P.StabilizationForm, g_form ? "DD" : "SUPG");
-    strcpy(c->P.ShockCapture, g_shock == 2 ? "CAUDD" : "CAU");
-    strcpy(c->P.h_Shock, "2sqrtArea");
+    strcpy(c->P.ShockCapture, g_shock == 3 ? "YZBeta" : g_shock == 2 ? "CAUDD" : "CAU");
+    strcpy(c->P.h_Shock, g_hshock == 2 ? "Option2" : g_hshock == 1 ? "Option1" : "2sqrtArea");
     c->P.SolverTolerance = solver_tol;
     c->P.NonLinearTolerance = nl_tol;
     c->P.LinearMaxIter = lmax;

@@ -39,6 +39,52 @@ static double cau(double kx, double ky, double bx, double by, double gamma,
     return 0;
 }
 
+/* YZBeta_ShockCapture (YZBeta_ShockCapture.c:3-36): YZ-beta with beta = 1
+ * and 2, relaxed against the element's previous value (w = 1/2, or 0 when
+ * |R(u)| moved by less than 20%); Re_old / delta_old carry the state. */
+static double yzbeta(double *Re_old, double *delta_old, int e, double bx, double by, double gamma,
+                     double ue1, double ue2, double ue3, double ueb, double feb, double y23, double y31, double y12,
+                     double x32, double x13, double x21, double invArea, double h)
+{
+    double w = 0.5, Eu;
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = bgu + gamma*ueb - feb;
+    double nRu = fabs(Ru);
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    double nu = fabs(ueb);
+    if (nu >= 1e-12 && ng >= 1e-12) Eu = 0.25*h*nRu/ng + 0.125*h*h*nRu/nu;
+    else Eu = 0;
+    if (fabs(nRu - Re_old[e])/nRu < 0.2) w = 0.;
+    Eu = w*Eu + (1.0 - w)*delta_old[e];
+    Re_old[e] = nRu;
+    delta_old[e] = Eu;
+    return Eu;
+}
+
+/* h_shock_calculation: 2sqrtArea (0, h_shock_2sqrtArea.c), Option1 (1,
+ * h_shock_Option1.c:3-19, from grad u) or Option2 (2, h_shock_Option2.c:3-16,
+ * from the velocity). */
+static double h_shock(int opt, double bx, double by, double u1, double u2, double u3, double y23, double y31,
+                      double y12, double x32, double x13, double x21, double Area)
+{
+    if (opt == 1) {
+        double P1 = fabs(u1*y23*y23 + u2*y31*y23 + u3*y12*y23 + u1*x32*x32 + u2*x13*x32 + u3*x21*x32);
+        double P2 = fabs(u1*y23*y31 + u2*y31*y31 + u3*y12*y31 + u1*x32*x13 + u2*x13*x13 + u3*x21*x13);
+        double P3 = fabs(u1*y23*y12 + u2*y31*y12 + u3*y12*y12 + u1*x32*x21 + u2*x13*x21 + u3*x21*x21);
+        double a1 = y23*u1 + y31*u2 + y12*u3, a2 = x32*u1 + x13*u2 + x21*u3;
+        double ng = sqrt(a1*a1 + a2*a2);
+        return P1 + P2 + P3 >= 1e-12 ? 4*Area*ng/(P1 + P2 + P3) : 0;
+    }
+    if (opt == 2) {
+        double P1 = fabs(bx*y23 + by*x32), P2 = fabs(bx*y31 + by*x13), P3 = fabs(bx*y12 + by*x21);
+        double nb = sqrt(bx*bx + by*by);
+        return P1 + P2 + P3 >= 1e-12 ? 4*Area*nb/(P1 + P2 + P3) : 0;
+    }
+    return sqrt(fabs(2*Area));
+}
+
 /* CAU_DD_ShockCapture (CAU_DD_ShockCapture.c:3-22): 0.5 h |R(u)| / |grad u|. */
 static double cau_dd(double bx, double by, double gamma, double ue1, double ue2, double ue3, double ueb,
                      double feb, double y23, double y31, double y12, double x32, double x13, double x21,
@@ -55,8 +101,8 @@ static double cau_dd(double bx, double by, double gamma, double ue1, double ue2,
 /* Build_K_F_DD.c:54-164: Galerkin + dynamic diffusion with the bubble
  * (KBB, KhB, KBh, FB) condensed into the 3x3 block and the load. */
 static void dd_element(double kx, double ky, double bx, double by, double gamma, const double fe[3],
-                       const double ue[3], int shock, const double X[3], const double Y[3], double ke[3][3],
-                       double Fe[3])
+                       const double ue[3], int shock, int hopt, double *Re_old, double *delta_old, int e,
+                       const double X[3], const double Y[3], double ke[3][3], double Fe[3])
 {
     const double third = 1.0/3.0, sixth = 1.0/6.0, seventh = 1.0/7.0, twelfth = 1.0/12.0;
     const double t320 = 3./20.0, n920 = 9./20.0, n940 = 9./40.0;
@@ -73,9 +119,12 @@ static void dd_element(double kx, double ky, double bx, double by, double gamma,
     double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
     double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
     double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
-    double h = sqrt(fabs(2*Area));                          /* h_shock_2sqrtArea */
+    double h = h_shock(hopt, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
     double Eu = 0.0;
-    if (shock == 2)
+    if (shock == 3)
+        Eu = yzbeta(Re_old, delta_old, e, bx, by, gamma, ue[0], ue[1], ue[2], ueb, feb, y23, y31, y12, x32, x13,
+                    x21, invArea, h);
+    else if (shock == 2)
         Eu = cau_dd(bx, by, gamma, ue[0], ue[1], ue[2], ueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
     else if (shock == 1)
         Eu = cau(kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
@@ -116,6 +165,14 @@ void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
     double kx = prob->k, ky = prob->k, gamma = prob->gamma;
     double *U = malloc(sizeof(double) * (size_t)nnodes);
     int J, E;
+    /* the shock-capture state of Process.c:16-17 (fresh zeros when the
+       caller keeps none, as for a single build) */
+    double *Re_old = prob->Re_old, *delta_old = prob->delta_old, *own = NULL;
+    if (!Re_old || !delta_old) {
+        own = calloc(2 * (size_t)(nel ? nel : 1), sizeof(double));
+        Re_old = own;
+        delta_old = own + (nel ? nel : 1);
+    }
     memset(A, 0, sizeof(double) * 9 * (size_t)nel);
     for (J = 0; J < neq; J++) F[J] = 0;
     for (J = 0; J < nnodes; J++)
@@ -127,7 +184,8 @@ void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
             const double Xv[3] = { x[J1], x[J2], x[J3] }, Yv[3] = { y[J1], y[J2], y[J3] };
             const double fv[3] = { prob->f, prob->f, prob->f }, uv[3] = { U[J1], U[J2], U[J3] };
             double ke[3][3], Fe[3];
-            dd_element(kx, ky, prob->beta[0], prob->beta[1], gamma, fv, uv, prob->cau, Xv, Yv, ke, Fe);
+            dd_element(kx, ky, prob->beta[0], prob->beta[1], gamma, fv, uv, prob->cau, prob->h_shock, Re_old,
+                       delta_old, E, Xv, Yv, ke, Fe);
             const int V[3] = { J1, J2, J3 };
             for (int a = 0; a < 3; a++) {        /* F_assembly.c:3-28 */
                 if (type[V[a]] != 1) continue;
@@ -169,8 +227,10 @@ void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
         double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
         double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
         double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
-        double hs = sqrt(fabs(2*Area));
-        double Eu = prob->cau ? cau(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb,
+        double hs = h_shock(prob->h_shock, bx, by, ue1, ue2, ue3, y23, y31, y12, x32, x13, x21, Area);
+        double Eu = prob->cau == 3 ? yzbeta(Re_old, delta_old, E, bx, by, gamma, ue1, ue2, ue3, ueb, feb,
+                                            y23, y31, y12, x32, x13, x21, invArea, hs)
+                  : prob->cau ? cau(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb,
                                     y23, y31, y12, x32, x13, x21, invArea, hs) : 0.0;
         double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
         double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
@@ -204,6 +264,7 @@ void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
             for (int c = 0; c < 3; c++) Ae[3*r + c] = ke[r][c];
     }
     free(U);
+    free(own);
 }
 
 int or_transport_process(int nnodes, int nel, const double *x, const double *y,
@@ -226,6 +287,12 @@ int or_transport_process(int nnodes, int nel, const double *x, const double *y,
     or_fill_lm(nel, 1, ien, type, invp, NEQ, lm);
     or_permutation_of_lm(nel, ien, type, invp, NEQ, Perm, invPerm, NULL);
     if (gmres_iterations) *gmres_iterations = 0;
+    /* Process.c:16-17: the shock-capture state lives for the whole loop */
+    or_transport_problem pl = *prob;
+    double *state = calloc(2 * (size_t)(nel ? nel : 1), sizeof(double));
+    pl.Re_old = state;
+    pl.delta_old = state + (nel ? nel : 1);
+    prob = &pl;
     /* Process.c:37-86 */
     while (normdiff > nonlinear_tol * normu && it < max_nonlinear) {
         it++;
@@ -239,6 +306,6 @@ int or_transport_process(int nnodes, int nel, const double *x, const double *y,
         normu = sqrt(or_ddot(neq, U, U));
     }
     free(lm); free(Perm); free(invPerm); free(A); free(F);
-    free(Diag); free(invDiag); free(uold);
+    free(Diag); free(invDiag); free(uold); free(state);
     return it;
 }

@@ -365,6 +365,51 @@ int precond_apply_device(fg_system *s, const double *p, double *z, cudaStream_t 
 // h_shock_2sqrtArea.c, one thread per element (internal order).  Writes the
 // 3x3 block (ebe_assembly.c) into the SoA layout and the element load
 // vector Fe; the Dirichlet lifting is applied in k_transport_F.
+// YZBeta_ShockCapture.c:3-36: YZ-beta (beta = 1 and 2) relaxed against the
+// element's previous value; Re_old / delta_old (per element, internal
+// order) carry the state across the builds of one Process run.
+__device__ double yzbeta_eu(double *Re_old, double *delta_old, int e, double bx, double by, double gamma,
+                            double ue1, double ue2, double ue3, double ueb, double feb, double y23, double y31,
+                            double y12, double x32, double x13, double x21, double invArea, double h)
+{
+    double w = 0.5, Eu;
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = bgu + gamma*ueb - feb;
+    double nRu = fabs(Ru);
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    double nu = fabs(ueb);
+    if (nu >= 1e-12 && ng >= 1e-12) Eu = 0.25*h*nRu/ng + 0.125*h*h*nRu/nu;
+    else Eu = 0;
+    if (fabs(nRu - Re_old[e])/nRu < 0.2) w = 0.;
+    Eu = w*Eu + (1.0 - w)*delta_old[e];
+    Re_old[e] = nRu;
+    delta_old[e] = Eu;
+    return Eu;
+}
+
+// h_shock_calculation: 0 h_shock_2sqrtArea.c, 1 h_shock_Option1.c:3-19
+// (from grad u), 2 h_shock_Option2.c:3-16 (from the velocity)
+__device__ double h_shock_dev(int opt, double bx, double by, double u1, double u2, double u3, double y23, double y31,
+                              double y12, double x32, double x13, double x21, double Area)
+{
+    if (opt == 1) {
+        double P1 = fabs(u1*y23*y23 + u2*y31*y23 + u3*y12*y23 + u1*x32*x32 + u2*x13*x32 + u3*x21*x32);
+        double P2 = fabs(u1*y23*y31 + u2*y31*y31 + u3*y12*y31 + u1*x32*x13 + u2*x13*x13 + u3*x21*x13);
+        double P3 = fabs(u1*y23*y12 + u2*y31*y12 + u3*y12*y12 + u1*x32*x21 + u2*x13*x21 + u3*x21*x21);
+        double a1 = y23*u1 + y31*u2 + y12*u3, a2 = x32*u1 + x13*u2 + x21*u3;
+        double ng = sqrt(a1*a1 + a2*a2);
+        return P1 + P2 + P3 >= 1e-12 ? 4*Area*ng/(P1 + P2 + P3) : 0.0;
+    }
+    if (opt == 2) {
+        double P1 = fabs(bx*y23 + by*x32), P2 = fabs(bx*y31 + by*x13), P3 = fabs(bx*y12 + by*x21);
+        double nb = sqrt(bx*bx + by*by);
+        return P1 + P2 + P3 >= 1e-12 ? 4*Area*nb/(P1 + P2 + P3) : 0.0;
+    }
+    return sqrt(fabs(2*Area));
+}
+
 __device__ double cau_eu(double kx, double ky, double bx, double by, double gamma, double ue1, double ue2, double ue3,
                          double ueb, double feb, double y23, double y31, double y12, double x32, double x13,
                          double x21, double invArea, double h)
@@ -390,8 +435,8 @@ __device__ double cau_eu(double kx, double ky, double bx, double by, double gamm
 __global__ void k_transport_elem(int nel, int ld, const int *__restrict__ gien, const double *__restrict__ gx,
                                  const double *__restrict__ gy, const int *__restrict__ gtype,
                                  const int *__restrict__ node_dof, const double *__restrict__ up,
-                                 const double *__restrict__ u, fg_transport_coeffs cf,
-                                 double *__restrict__ A64, double *__restrict__ Fe)
+                                 const double *__restrict__ u, fg_transport_coeffs cf, double *Re_old,
+                                 double *delta_old, double *__restrict__ A64, double *__restrict__ Fe)
 {
     int pos = blockIdx.x * blockDim.x + threadIdx.x;
     if (pos >= nel) return;
@@ -429,8 +474,10 @@ __global__ void k_transport_elem(int nel, int ld, const int *__restrict__ gien, 
     double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
     double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
     double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
-    double hs = sqrt(fabs(2*Area));
-    double Eu = cf.cau ? cau_eu(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31, y12, x32, x13, x21,
+    double hs = h_shock_dev(cf.h_shock, bx, by, ue1, ue2, ue3, y23, y31, y12, x32, x13, x21, Area);
+    double Eu = cf.cau == 3 ? yzbeta_eu(Re_old, delta_old, pos, bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31,
+                                        y12, x32, x13, x21, invArea, hs)
+              : cf.cau ? cau_eu(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31, y12, x32, x13, x21,
                                 invArea, hs) : 0.0;
     double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
     double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
@@ -471,8 +518,8 @@ __device__ double cau_dd_eu(double bx, double by, double gamma, double ue1, doub
 __global__ void k_transport_dd_elem(int nel, int ld, const int *__restrict__ gien, const double *__restrict__ gx,
                                     const double *__restrict__ gy, const int *__restrict__ gtype,
                                     const int *__restrict__ node_dof, const double *__restrict__ up,
-                                    const double *__restrict__ u, fg_transport_coeffs cf,
-                                    double *__restrict__ A64, double *__restrict__ Fe)
+                                    const double *__restrict__ u, fg_transport_coeffs cf, double *Re_old,
+                                    double *delta_old, double *__restrict__ A64, double *__restrict__ Fe)
 {
     int pos = blockIdx.x * blockDim.x + threadIdx.x;
     if (pos >= nel) return;
@@ -499,9 +546,12 @@ __global__ void k_transport_dd_elem(int nel, int ld, const int *__restrict__ gie
     double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
     double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
     double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
-    double h = sqrt(fabs(2*Area));
+    double h = h_shock_dev(cf.h_shock, bx, by, ue1, ue2, ue3, y23, y31, y12, x32, x13, x21, Area);
     double Eu = 0.0;
-    if (cf.cau == 2)
+    if (cf.cau == 3)
+        Eu = yzbeta_eu(Re_old, delta_old, pos, bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31, y12, x32, x13, x21,
+                       invArea, h);
+    else if (cf.cau == 2)
         Eu = cau_dd_eu(bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
     else if (cf.cau == 1)
         Eu = cau_eu(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
@@ -698,8 +748,9 @@ int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev,
     const Topology &t = s->topo;
     if (t.ndof != 1) { set_error("transient transport assembly needs ndof == 1"); return FG_ERR_UNSUPPORTED; }
     if (!s->geometry_ok) { set_error("transient transport assembly before fg_set_geometry"); return FG_ERR_STATE; }
-    if (c->c.form != FG_TRANSPORT_SUPG || c->c.cau < FG_SHOCK_NONE || c->c.cau > FG_SHOCK_CAU) {
-        set_error("transient transport builds the SUPG form with CAU or no shock capture");
+    if (c->c.form != FG_TRANSPORT_SUPG || c->c.cau < FG_SHOCK_NONE || c->c.cau > FG_SHOCK_CAU ||
+        c->c.h_shock != FG_HSHOCK_2SQRTAREA) {
+        set_error("transient transport builds the SUPG form with CAU (h_shock 2sqrtArea) or no shock capture");
         return FG_ERR_UNSUPPORTED;
     }
     int r;
@@ -729,20 +780,32 @@ int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c, const 
         set_error("transport form must be FG_TRANSPORT_SUPG or FG_TRANSPORT_DD");
         return FG_ERR_ARG;
     }
-    if (c->cau < FG_SHOCK_NONE || c->cau > FG_SHOCK_CAUDD || (c->cau == FG_SHOCK_CAUDD && c->form != FG_TRANSPORT_DD)) {
-        set_error("shock capture must be NONE or CAU, or CAUDD with the DD form");
+    if (c->cau < FG_SHOCK_NONE || c->cau > FG_SHOCK_YZBETA || (c->cau == FG_SHOCK_CAUDD && c->form != FG_TRANSPORT_DD)) {
+        set_error("shock capture must be NONE, CAU or YZBETA, or CAUDD with the DD form");
         return FG_ERR_ARG;
+    }
+    if (c->h_shock < FG_HSHOCK_2SQRTAREA || c->h_shock > FG_HSHOCK_OPTION2) {
+        set_error("h_shock must be FG_HSHOCK_2SQRTAREA, _OPTION1 or _OPTION2");
+        return FG_ERR_ARG;
+    }
+    double *Re_old = nullptr, *delta_old = nullptr;
+    if (c->cau == FG_SHOCK_YZBETA) {       // Process.c:16-17: zero state, kept across builds
+        int r0;
+        if (s->shock_state.bytes < 16 * (size_t)s->nel_pad && (r0 = s->shock_state.alloc(16 * (size_t)s->nel_pad)))
+            return r0;
+        Re_old = s->shock_state.as<double>();
+        delta_old = Re_old + s->nel_pad;
     }
     if (t.nel > 0 && c->form == FG_TRANSPORT_DD)
         k_transport_dd_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(),
                                                                 s->gx.as<double>(), s->gy.as<double>(),
                                                                 s->gtype.as<int>(), s->node_dof.as<int>(),
-                                                                s->gup.as<double>(), u_dev, *c, s->A64.as<double>(),
-                                                                s->Fe.as<double>());
+                                                                s->gup.as<double>(), u_dev, *c, Re_old, delta_old,
+                                                                s->A64.as<double>(), s->Fe.as<double>());
     else if (t.nel > 0)
         k_transport_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(), s->gx.as<double>(),
                                                              s->gy.as<double>(), s->gtype.as<int>(), s->node_dof.as<int>(),
-                                                             s->gup.as<double>(), u_dev, *c, s->A64.as<double>(),
+                                                             s->gup.as<double>(), u_dev, *c, Re_old, delta_old, s->A64.as<double>(),
                                                              s->Fe.as<double>());
     FG_CUDA(cudaGetLastError());
     count_launches(1);

@@ -85,7 +85,7 @@ size_t fg_system::bytes() const
                            &dinv64, &dinv32, &ilu_flags, &ilu_ctr, &ilu_tmp, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
                            &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
-                           &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &state_u1, &state_u2, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
+                           &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &state_u1, &state_u2, &shock_state, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
                            &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
     size_t b = 0;
     for (auto *m : all) b += m->bytes;
@@ -598,7 +598,9 @@ int fg_transport_process(fg_system *s, const fg_transport_coeffs *c, const fg_so
     int it = 0, gmres = 0, r;
     double last_res = NAN;
     // a fresh run starts from a zero diagonal (Preprocess.c:292 callocs it)
+    // and zero YZBeta state (Process.c:16-17)
     FG_CUDA(cudaMemsetAsync(s->diag.p, 0, s->diag.bytes, s->stream));
+    if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
     // Process.c:37-86
     while (normdiff > nonlinear_tol * normu && it < max_nonlinear) {
         ++it;

@@ -48,6 +48,7 @@ struct fg_system {
     // state of the nonlinear and time loops (internal numbering) and norm scratch
     fg::DevMem gf1, gf2, state_u, state_a, state_old, norm_part;
     fg::DevMem state_u1, state_u2;     // u^{n-1}, u^n of the BDF2 steps
+    fg::DevMem shock_state;            // YZBeta Re_old, delta_old [2 * nel_pad]
     bool ns_geometry_ok = false, eu_geometry_ok = false;
     // resident right-hand side (internal numbering): F and M^-1 F
     fg::DevMem rhs_f, rhs_b;

@@ -23,7 +23,8 @@ FG_PREC_FP64, FG_PREC_MIXED = 64, 32
 FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 = 0, 1, 2
 FG_NS_SUPG_PSPG, FG_NS_VMS_DCDD = 0, 1
 FG_TRANSPORT_SUPG, FG_TRANSPORT_DD = 0, 1
-FG_SHOCK_NONE, FG_SHOCK_CAU, FG_SHOCK_CAUDD = 0, 1, 2
+FG_SHOCK_NONE, FG_SHOCK_CAU, FG_SHOCK_CAUDD, FG_SHOCK_YZBETA = 0, 1, 2, 3
+FG_HSHOCK_2SQRTAREA, FG_HSHOCK_OPTION1, FG_HSHOCK_OPTION2 = 0, 1, 2
 FG_REORDER_NONE, FG_REORDER_RCM = 0, 1
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE",
           5: "ERR_BREAKDOWN", 6: "ERR_NOTCONV", 7: "ERR_UNSUPPORTED", 8: "ERR_TIMEOUT"}
@@ -61,7 +62,7 @@ class SolveStats(ctypes.Structure):
 
 class TransportCoeffs(ctypes.Structure):
     _fields_ = [("k", _c_dbl), ("gamma", _c_dbl), ("beta", _c_dbl * 2), ("f", _c_dbl), ("cau", _c_int),
-                ("form", _c_int)]
+                ("form", _c_int), ("h_shock", _c_int)]
 
 
 class TTCoeffs(ctypes.Structure):
@@ -574,7 +575,7 @@ def ns_system(prob, reorder=False) -> System:
 
 def _coeffs(prob):
     return TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau),
-                           int(getattr(prob, "form", 0)))
+                           int(getattr(prob, "form", 0)), int(getattr(prob, "h_shock", 0)))
 
 
 def launch_count() -> int:

@@ -86,8 +86,9 @@ class TransportProblem:
     upresc: np.ndarray     # float64[nnodes], Dirichlet value (read where type == 0)
     upmode: int = 0        # 0: 1 on inflow edges x=xmin, y=ymin, else 0;  1: constant
     upval: float = 0.0
-    cau: int = 1           # ShockCapture: 0 none, 1 "CAU", 2 "CAUDD" (DD form only)
+    cau: int = 1           # ShockCapture: 0 none, 1 "CAU", 2 "CAUDD" (DD form only), 3 "YZBeta"
     form: int = 0          # StabilizationForm: 0 "SUPG", 1 "DD"
+    h_shock: int = 0       # h_Shock: 0 "2sqrtArea", 1 "Option1", 2 "Option2"
 
 
 def transport_problem(n_nodes_side: int, angle_deg=30.0, k=1e-6, gamma=0.0, f=0.0,

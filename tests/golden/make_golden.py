@@ -18,7 +18,9 @@ zero) on the Euler cases; and tests/golden/vms_ns.npz: Build_K_F_VMS_DCDD
 (blocks and residual at a state u) and its Picard Process loop on the NS
 cases; and tests/golden/dd_sst.npz: the steady transport driver's
 Build_K_F_DD with CAUDD and with CAU (blocks and F at a state u) and its
-Process loop on the transport cases.
+Process loop on the transport cases; and tests/golden/shock_sst.npz: the
+YZBeta shock capture and the h_shock Option1 / Option2 lengths with both
+forms (blocks and F at a state u, the Process loop).
 """
 import os
 import sys
@@ -163,9 +165,28 @@ def write_sst_dd():
     np.savez_compressed(os.path.join(HERE, "dd_sst.npz"), **out)
 
 
+SHOCK_CASES = [(0, 3, 0), (0, 3, 1), (0, 1, 2), (1, 3, 2), (1, 2, 1), (1, 3, 0)]   # (form, shock, h_shock)
+
+
+def write_sst_shock():
+    out = {}
+    for form, shock, hs in SHOCK_CASES:
+        p = G.transport_problem(13, angle_deg=110.0, k=1e-4, gamma=0.2, f=0.5, cau=shock)
+        p.form, p.h_shock = form, hs
+        u = np.random.Generator(np.random.PCG64(form * 100 + shock * 10 + hs)).random(p.mesh.neq)
+        A, F = O.ref_build(p, u)
+        U, its = O.ref_process(p, 1e-10, 1e-3, 30, 1000)
+        key = f"f{form}_c{shock}_h{hs}"
+        out[key + "_u"], out[key + "_A"], out[key + "_F"] = u, A, F[: p.mesh.neq]
+        out[key + "_U"], out[key + "_its"] = U, its
+        print(key, "process gmres", its)
+    np.savez_compressed(os.path.join(HERE, "shock_sst.npz"), **out)
+
+
 if __name__ == "__main__":
     main()
     write_euler()
     write_euler_schemes()
     write_ns_vms()
     write_sst_dd()
+    write_sst_shock()

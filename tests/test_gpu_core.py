@@ -194,3 +194,20 @@ def test_caudd_needs_dd_form(fg):
     s = fg.transport_system(p)
     with pytest.raises(Exception):
         s.transport_assemble(p)
+
+
+@pytest.mark.parametrize("form,shock,hs", [(0, 3, 0), (0, 1, 1), (0, 3, 2), (1, 3, 1), (1, 2, 2)])
+def test_shock_options_device(fg, form, shock, hs):
+    """YZBeta (state on the device) and the h_shock options: the first build
+    of a fresh system and the whole Process loop against the oracle."""
+    p = G.transport_problem(33, angle_deg=110.0, k=1e-4, gamma=0.2, f=0.5, cau=shock)
+    p.form, p.h_shock = form, hs
+    u = np.random.default_rng(11).random(p.mesh.neq)
+    A0, F0 = O.build_k_f_supg(p, u)
+    s = fg.transport_system(p)
+    F = s.transport_assemble(p, u)
+    assert np.array_equal(s.get_blocks(), A0) and np.array_equal(F[:-1], F0[:-1])
+    U0, nl0, it0 = O.transport_process(p, 1e-10, 1e-3, 30, 1000)
+    U, st = s.transport_process(p, 30, 1000, 1e-10, 1e-3)
+    assert st["nonlinear_iterations"] == nl0
+    assert rel(U, U0) <= 1e-9

@@ -149,3 +149,22 @@ def test_dd_against_reference_build(oracle_lib):
     A0, F0 = O.ref_build(p, u)
     A1, F1 = O.build_k_f_supg(p, u)
     assert np.array_equal(A0, A1) and np.array_equal(F0[:-1], F1[:-1])
+
+
+SHOCK = os.path.join(os.path.dirname(__file__), "golden", "shock_sst.npz")
+SHOCK_CASES = [(0, 3, 0), (0, 3, 1), (0, 1, 2), (1, 3, 2), (1, 2, 1), (1, 3, 0)]   # (form, shock, h_shock)
+
+
+@pytest.mark.parametrize("form,shock,hs", SHOCK_CASES)
+def test_shock_options_bit_exact(form, shock, hs, oracle_lib):
+    """ShockCapture "YZBeta" (with its per-element state across the Process
+    loop) and h_Shock "Option1" / "Option2", both forms, against the
+    reference's own runs."""
+    p = G.transport_problem(13, angle_deg=110.0, k=1e-4, gamma=0.2, f=0.5, cau=shock)
+    p.form, p.h_shock = form, hs
+    d = np.load(SHOCK)
+    key = f"f{form}_c{shock}_h{hs}"
+    A, F = O.build_k_f_supg(p, d[key + "_u"])
+    assert np.array_equal(A, d[key + "_A"]) and np.array_equal(F[: p.mesh.neq], d[key + "_F"])
+    U, nl, its = O.transport_process(p, 1e-10, 1e-3, 30, 1000)
+    assert its == int(d[key + "_its"]) and np.array_equal(U, d[key + "_U"])
