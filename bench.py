@@ -42,6 +42,12 @@ WORKLOAD = ("served steady SUPG/CAU transport: 256 requests, NxN nodes N~U[33,51
             "angle~U[0,360), k~logU[1e-8,1e-2]; device assembly + Diag + GMRES(30), FP32 inner + FP64 "
             "refinement to true rel. residual 1e-10, continuous batching")
 KMAX, TOL = 30, 1e-10
+BASIS = "fp32"          # storage of the Krylov basis in the mixed-precision solves (--basis)
+
+
+def served_precision(fg):
+    """Precision of the mixed solves: FP32 arithmetic, basis in FP32 or FP16."""
+    return fg.FG_PREC_MIXED16 if BASIS == "fp16" else fg.FG_PREC_MIXED
 # DRAM bytes / algorithmic bytes of one batched FP32 matvec, measured by ncu
 # (dram__bytes_read.sum + dram__bytes_write.sum of the two k_ebe_mv3
 # launches of one matvec of `bench.py --matvec-only --count 32 --steps 1`,
@@ -323,7 +329,7 @@ def c5_leg(fg, G, count=96, rates=(10, 30, 100, 300, 1000, 2000), seed=5):
     setup_s = time.perf_counter() - t0
 
     def one(rate):
-        sv = fg.Server(kmax=KMAX, lmax=10000, tol=TOL, precision=fg.FG_PREC_MIXED)
+        sv = fg.Server(kmax=KMAX, lmax=10000, tol=TOL, precision=served_precision(fg))
         gaps = rng.exponential(1.0 / rate, size=count) if rate else np.zeros(count)
         arrive = np.cumsum(gaps) - gaps[0]
         t_start = sv.now()
@@ -391,6 +397,8 @@ def main():
     ap.add_argument("--seed", type=int, default=4)
     ap.add_argument("--cpu-budget", type=int, default=400_000, help="elements in the CPU sample")
     ap.add_argument("--plain-count", type=int, default=0, help="instances in the plain FP64 leg (0 = all)")
+    ap.add_argument("--basis", choices=["fp32", "fp16"], default="fp32",
+                    help="storage of the Krylov basis in the mixed-precision solves (FP32 arithmetic either way)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-legs", action="store_true", help="skip the Euler and Navier-Stokes legs")
@@ -401,6 +409,8 @@ def main():
                     help="only the batched FP32 EBE matvec of --count instances (2 warm-up + --steps "
                          "matvecs); the small case the ncu traffic capture runs")
     args = ap.parse_args()
+    global BASIS
+    BASIS = args.basis
     rank, ws, dist = dist_setup()
     if args.impl == "reference":
         return run_reference(args, rank, ws, dist)
@@ -432,7 +442,7 @@ def main():
         """Serve every instance once through the request server (continuous
         batching); arrivals: submit times in seconds (None = all at once).
         Returns (makespan_s, list of per-request results)."""
-        sv = fg.Server(kmax=KMAX, lmax=10000, tol=TOL, precision=fg.FG_PREC_MIXED)
+        sv = fg.Server(kmax=KMAX, lmax=10000, tol=TOL, precision=served_precision(fg))
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -489,7 +499,7 @@ def main():
     def batch_step():
         for s, p in zip(systems, probs):
             s.transport_prepare(p)
-        return fg.solve_resident(systems, kmax=KMAX, lmax=10000, tol=TOL, precision=fg.FG_PREC_MIXED)
+        return fg.solve_resident(systems, kmax=KMAX, lmax=10000, tol=TOL, precision=served_precision(fg))
 
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -537,7 +547,7 @@ def main():
             for s, A, F in zip(systems, As, Fs):
                 s.set_blocks(A)
                 Bs.append(s.precond_setup(fg.FG_PRECOND_DIAG, 0, F))
-            return fg.solve_batch(systems, Bs, Fs, kmax=KMAX, lmax=10000, tol=TOL, precision=fg.FG_PREC_MIXED)
+            return fg.solve_batch(systems, Bs, Fs, kmax=KMAX, lmax=10000, tol=TOL, precision=served_precision(fg))
 
         e2e_step()
         et = []
@@ -571,7 +581,7 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * step_s, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 inner / f64 refinement", "data": "synthetic",
+            "vs_baseline": None, "dtype": "f32 inner (f16 basis) / f64 refinement" if BASIS == "fp16" else "f32 inner / f64 refinement", "data": "synthetic",
             "config": {"workload": WORKLOAD, "instances": args.count, "elements": nel_total, "dofs": n_total,
                        "kmax": KMAX, "tol": TOL, "l2": "inputs larger than L2 (per-step working set >1 GB)"},
             "latency_ms": {"p50": 1e3 * pct(lat, 50), "p99": 1e3 * pct(lat, 99),

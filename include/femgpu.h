@@ -197,7 +197,7 @@ int fg_get_diag(const fg_system *s, double *Diag);
 int fg_set_diag(fg_system *s, const double *Diag);
 
 /* ---- GMRES (Solvers_and_Preconditioners/pgmres.c:5-200) ---- */
-enum { FG_PREC_FP64 = 64, FG_PREC_MIXED = 32 };
+enum { FG_PREC_FP64 = 64, FG_PREC_MIXED = 32, FG_PREC_MIXED16 = 16 };
 typedef struct {
     int kmax;            /* KrylovBasisVectorsQuantity (k-1 Arnoldi steps/cycle) */
     int lmax;            /* LinearMaxIter: restart cycles                         */
@@ -206,7 +206,10 @@ typedef struct {
                             FG_PREC_MIXED: FP32 Arnoldi (blocks, basis, M^-1)
                             inside FP64 refinement: each cycle restarts from the
                             FP64 residual, stops when the true relative residual
-                            ||F - A X|| / ||F|| <= tol                            */
+                            ||F - A X|| / ||F|| <= tol;
+                            FG_PREC_MIXED16: the same with the Krylov basis
+                            stored in FP16 (scaled by a power of two near
+                            sqrt n; arithmetic stays FP32, kmax <= 32)            */
     double inner_tol;    /* mixed: relative decrease per FP32 cycle (0 = 1e-5)    */
 } fg_solver_opts;
 

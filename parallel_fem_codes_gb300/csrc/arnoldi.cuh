@@ -1,7 +1,8 @@
 // Arnoldi step and cycle-end kernels of the batched GMRES engine
 // (included by krylov.cu).
 //
-// Every dof kernel walks parts of kPartMin..n dofs.  Within a part the work
+// Every dof kernel walks parts of kPartMin..kPartMax dofs (the size is
+// chosen per batch from its total dofs).  Within a part the work
 // is split in two shapes so that loads are never serialised behind
 // reductions:
 //   * update passes are thread-per-dof: w[d] -= sum_j h_j V[j][d] with the
@@ -26,6 +27,67 @@ template <typename T> __device__ __forceinline__ typename Pk<T>::type ld_pk(cons
 template <typename T> __device__ __forceinline__ void st_pk(T *p, const typename Pk<T>::type &v)
 {
     *reinterpret_cast<typename Pk<T>::type *>(p) = v;
+}
+
+// The basis may be stored in a narrower type TV than the arithmetic type T
+// (FP16 under FP32 arithmetic): a basis pack is 16 bytes of TV, G dofs; the
+// work vectors are read and written G dofs at a time as G / Pk<T>::N packs.
+template <typename TV> struct VPk { static constexpr int G = 16 / sizeof(TV); };
+
+template <typename T, int G> __device__ __forceinline__ void ld_g(const T *p, T (&o)[G])
+{
+    constexpr int N = Pk<T>::N;
+#pragma unroll
+    for (int h = 0; h < G / N; ++h) {
+        const auto v = ld_pk(p + h * N);
+#pragma unroll
+        for (int c = 0; c < N; ++c) o[h * N + c] = v.v[c];
+    }
+}
+template <typename T, int G> __device__ __forceinline__ void st_g(T *p, const T (&o)[G])
+{
+    constexpr int N = Pk<T>::N;
+#pragma unroll
+    for (int h = 0; h < G / N; ++h) {
+        typename Pk<T>::type v;
+#pragma unroll
+        for (int c = 0; c < N; ++c) v.v[c] = o[h * N + c];
+        st_pk(p + h * N, v);
+    }
+}
+// one basis pack as T
+template <typename T, typename TV>
+__device__ __forceinline__ void ld_v(const TV *p, T (&o)[VPk<TV>::G])
+{
+    if constexpr (std::is_same<TV, __half>::value) {
+        const uint4 r = *reinterpret_cast<const uint4 *>(p);
+        const unsigned u[4] = {r.x, r.y, r.z, r.w};
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            __half2 hv;
+            memcpy(&hv, &u[h], 4);
+            const float2 f = __half22float2(hv);
+            o[2 * h] = (T)f.x;
+            o[2 * h + 1] = (T)f.y;
+        }
+    } else {
+        ld_g<T, VPk<TV>::G>(reinterpret_cast<const T *>(p), o);
+    }
+}
+template <typename T, typename TV>
+__device__ __forceinline__ void st_v(TV *p, const T (&o)[VPk<TV>::G])
+{
+    if constexpr (std::is_same<TV, __half>::value) {
+        unsigned u[4];
+#pragma unroll
+        for (int h = 0; h < 4; ++h) {
+            const __half2 hv = __floats2half2_rn((float)o[2 * h], (float)o[2 * h + 1]);
+            memcpy(&u[h], &hv, 4);
+        }
+        *reinterpret_cast<uint4 *>(p) = make_uint4(u[0], u[1], u[2], u[3]);
+    } else {
+        st_g<T, VPk<TV>::G>(reinterpret_cast<T *>(p), o);
+    }
 }
 
 // dots of V[0..i] with w over a part: warp-per-j, results to out[j]
@@ -63,95 +125,129 @@ __device__ __forceinline__ void part_dots(const SysDev &D, const DChunk &k, int 
 }
 
 // dots of V[0..i] with w and with v = V[i] over a part, in one sweep of the
-// basis: warp w takes j = w, w+8, w+16, w+24 (i < 32) together, so each pack
-// of w and v is loaded once per warp whatever the number of its vectors;
-// <V[j], w> to out[j], <V[j], v> to out[i + 1 + j]
-template <typename T>
+// basis.  With nv = i + 1 >= 8 vectors, warp w takes j = w, w+8, w+16, w+24
+// (i < 32) together over the whole part, so each pack of w and v is loaded
+// once per warp whatever the number of its vectors.  With fewer vectors
+// the idle warps split the dofs instead: S = 8 / nv warps per vector, each
+// on every S-th pack, their sums added in slice order (deterministic).
+// <V[j], w> to out[j], <V[j], v> to out[i + 1 + j].  Every thread of the
+// block must call it (it synchronises when the part is sliced).
+template <typename T, typename TV = T>
 __device__ __forceinline__ void part_dots2(const SysDev &D, const DChunk &k, int i, const T *__restrict__ w,
                                            double *out)
 {
-    constexpr int N = Pk<T>::N;
+    constexpr int G = VPk<TV>::G;
     constexpr int NW = kThreads / 32;
+    __shared__ double sl[2 * NW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const T *V = (const T *)D.V;
-    const T *vi = V + (size_t)i * D.n_pad;
-    const int nj = warp <= i ? (i - warp) / NW + 1 : 0;   // vectors of this warp (<= 4)
-    if (nj == 0) return;
-    const T *vj[4];
+    const int nv = i + 1;
+    const int S = nv >= NW ? 1 : NW / nv;                  // warps per vector
+    const int j0 = S == 1 ? warp : warp / S, sidx = S == 1 ? 0 : warp % S;
+    const int nj = S == 1 ? (warp <= i ? (i - warp) / NW + 1 : 0) : (j0 < nv ? 1 : 0);
+    const TV *V = (const TV *)D.V;
+    const TV *vi = V + (size_t)i * D.n_pad;
+    const TV *vj[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) vj[u] = V + (size_t)min(warp + NW * u, i) * D.n_pad;
+    for (int u = 0; u < 4; ++u) vj[u] = V + (size_t)min(j0 + NW * u, i) * D.n_pad;
     T a[4], b[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) a[u] = b[u] = (T)0;
-    for (int q = k.d0 + lane * N; q < k.d1; q += 32 * N) {
-        const auto w0 = ld_pk(w + q), u0 = ld_pk(vi + q);
-        typename Pk<T>::type v0[4];
+    if (nj > 0) {
+#pragma unroll 1
+        for (int q = k.d0 + (lane + 32 * sidx) * G; q < k.d1; q += 32 * G * S) {
+            T w0[G], u0[G], v0[4][G];
+            ld_g<T, G>(w + q, w0);
+            ld_v<T, TV>(vi + q, u0);
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (u < nj) v0[u] = ld_pk(vj[u] + q);
+            for (int u = 0; u < 4; ++u)
+                if (u < nj) ld_v<T, TV>(vj[u] + q, v0[u]);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            if (u >= nj) break;
+            for (int u = 0; u < 4; ++u) {
+                if (u >= nj) break;
 #pragma unroll
-            for (int c = 0; c < N; ++c) {
-                a[u] += v0[u].v[c] * w0.v[c];
-                b[u] += v0[u].v[c] * u0.v[c];
+                for (int c = 0; c < G; ++c) {
+                    a[u] += v0[u][c] * w0[c];
+                    b[u] += v0[u][c] * u0[c];
+                }
             }
         }
     }
+    if (S == 1) {
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        if (u >= nj) break;
-        const double sa = warp_sum((double)a[u]), sb = warp_sum((double)b[u]);
-        if (lane == 0) {
-            out[warp + NW * u] = sa;
-            out[i + 1 + warp + NW * u] = sb;
+        for (int u = 0; u < 4; ++u) {
+            if (u >= nj) break;
+            const double sa = warp_sum((double)a[u]), sb = warp_sum((double)b[u]);
+            if (lane == 0) {
+                out[j0 + NW * u] = sa;
+                out[i + 1 + j0 + NW * u] = sb;
+            }
         }
+        return;
+    }
+    const double sa = warp_sum((double)a[0]), sb = warp_sum((double)b[0]);
+    if (lane == 0 && nj > 0) {
+        sl[2 * warp] = sa;
+        sl[2 * warp + 1] = sb;
+    }
+    __syncthreads();
+    if (threadIdx.x < nv) {
+        const int j = threadIdx.x;
+        double ta = sl[2 * (j * S)], tb = sl[2 * (j * S) + 1];
+        for (int q = 1; q < S; ++q) {
+            ta += sl[2 * (j * S + q)];
+            tb += sl[2 * (j * S + q) + 1];
+        }
+        out[j] = ta;
+        out[i + 1 + j] = tb;
     }
 }
 
 // w[d] -= sum_{j<=i} h[j] V[j][d] for the dofs of the part (a pack per
 // thread, four basis vectors in flight); returns this thread's sum of the
 // new w^2 when want_norm.  Entries past n stay zero.
-template <typename T>
+template <typename T, typename TV = T>
 __device__ __forceinline__ double part_update(const SysDev &D, const DChunk &k, int i, const T *h, T *w,
                                               bool want_norm)
 {
-    constexpr int N = Pk<T>::N;
-    using P = typename Pk<T>::type;
-    const T *V = (const T *)D.V;
+    constexpr int G = VPk<TV>::G;
+    const TV *V = (const TV *)D.V;
     const size_t ld = (size_t)D.n_pad;
     double nrm = 0.0;
-    for (int q = k.d0 + threadIdx.x * N; q < k.d1; q += blockDim.x * N) {
-        P s0 = ld_pk(w + q), s1, s2, s3;
+    for (int q = k.d0 + threadIdx.x * G; q < k.d1; q += blockDim.x * G) {
+        T s0[G], s1[G], s2[G], s3[G];
+        ld_g<T, G>(w + q, s0);
 #pragma unroll
-        for (int c = 0; c < N; ++c) s1.v[c] = s2.v[c] = s3.v[c] = (T)0;
+        for (int c = 0; c < G; ++c) s1[c] = s2[c] = s3[c] = (T)0;
         int j = 0;
         for (; j + 3 <= i; j += 4) {
-            P v0 = ld_pk(V + j * ld + q), v1 = ld_pk(V + (j + 1) * ld + q);
-            P v2 = ld_pk(V + (j + 2) * ld + q), v3 = ld_pk(V + (j + 3) * ld + q);
+            T v0[G], v1[G], v2[G], v3[G];
+            ld_v<T, TV>(V + j * ld + q, v0);
+            ld_v<T, TV>(V + (j + 1) * ld + q, v1);
+            ld_v<T, TV>(V + (j + 2) * ld + q, v2);
+            ld_v<T, TV>(V + (j + 3) * ld + q, v3);
             const T h0 = h[j], h1 = h[j + 1], h2 = h[j + 2], h3 = h[j + 3];
 #pragma unroll
-            for (int c = 0; c < N; ++c) {
-                s0.v[c] -= h0 * v0.v[c];
-                s1.v[c] -= h1 * v1.v[c];
-                s2.v[c] -= h2 * v2.v[c];
-                s3.v[c] -= h3 * v3.v[c];
+            for (int c = 0; c < G; ++c) {
+                s0[c] -= h0 * v0[c];
+                s1[c] -= h1 * v1[c];
+                s2[c] -= h2 * v2[c];
+                s3[c] -= h3 * v3[c];
             }
         }
         for (; j <= i; ++j) {
-            P v0 = ld_pk(V + j * ld + q);
+            T v0[G];
+            ld_v<T, TV>(V + j * ld + q, v0);
             const T h0 = h[j];
 #pragma unroll
-            for (int c = 0; c < N; ++c) s0.v[c] -= h0 * v0.v[c];
+            for (int c = 0; c < G; ++c) s0[c] -= h0 * v0[c];
         }
 #pragma unroll
-        for (int c = 0; c < N; ++c) {
-            T v = (s0.v[c] + s1.v[c]) + (s2.v[c] + s3.v[c]);
-            s0.v[c] = v;
+        for (int c = 0; c < G; ++c) {
+            T v = (s0[c] + s1[c]) + (s2[c] + s3[c]);
+            s0[c] = v;
             if (want_norm) nrm += (double)(v * v);
         }
-        st_pk(w + q, s0);
+        st_g<T, G>(w + q, s0);
     }
     return nrm;
 }
@@ -204,7 +300,7 @@ k_dots1(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
 // (h1 = s, h2 = V^T (w - V s) = s - G s) with the second one taken from G
 // instead of a second sweep over the basis; c becomes column i of H and
 // the update that k_orth2 applies.  Used when kmax <= 32.
-template <typename T>
+template <typename T, typename TV = T>
 __global__ void __launch_bounds__(kThreads)
 k_dots1g(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
 {
@@ -234,21 +330,23 @@ k_dots1g(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const in
             st_pk(t + q, zero);
         }
         __syncthreads();
-        part_dots2<T>(D, k, i, w, red);
+        part_dots2<T, TV>(D, k, i, w, red);
         __syncthreads();
         for (int j = threadIdx.x; j < 2 * (i + 1); j += blockDim.x) D.part[k.part * kPartStride + j] = red[j];
         if (last_part(D, 1)) {
             reduce_parts(D, 2 * (i + 1), tot);
             const int km = D.kmax;
+            // the stored basis is sigma V: dots carry 1 / sigma, Gram entries 1 / sigma^2
+            const double s1 = D.vsci, s2 = (double)D.vsci * D.vsci;
             for (int j = threadIdx.x; j <= i; j += blockDim.x) {
-                D.G[j * km + i] = tot[i + 1 + j];
-                D.G[i * km + j] = tot[i + 1 + j];
+                D.G[j * km + i] = tot[i + 1 + j] * s2;
+                D.G[i * km + j] = tot[i + 1 + j] * s2;
             }
             __syncthreads();
             for (int j = threadIdx.x; j <= i; j += blockDim.x) {
                 double gs = 0.0;
-                for (int l = 0; l <= i; ++l) gs += D.G[j * km + l] * tot[l];
-                const double cj = tot[j] + (tot[j] - gs);
+                for (int l = 0; l <= i; ++l) gs += D.G[j * km + l] * (tot[l] * s1);
+                const double cj = tot[j] * s1 + (tot[j] * s1 - gs);
                 D.H[j * km + i] = cj;
                 D.hbuf[j] = cj;
             }
@@ -305,7 +403,7 @@ __device__ __forceinline__ void solve_y(const SysDev &D, int m)
 // pass 3: w -= sum_j h2_j v_j ; ||w||; then, in the last part, the Givens
 // rotations of column i and the residual estimate (pgmres.c:111-157), and
 // at the end of a cycle the solution of the triangular system.
-template <typename T>
+template <typename T, typename TV = T>
 __global__ void __launch_bounds__(kThreads)
 k_orth2(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
 {
@@ -319,9 +417,9 @@ k_orth2(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
         const SysDev &D = sys[k.sys];
         if (!D.st->in_cycle) continue;
         T *w = (T *)D.w;
-        for (int j = threadIdx.x; j <= i; j += blockDim.x) hs[j] = (T)D.hbuf[j];
+        for (int j = threadIdx.x; j <= i; j += blockDim.x) hs[j] = (T)(D.hbuf[j] * D.vsci);
         __syncthreads();
-        double acc = part_update<T>(D, k, i, hs, w, true);
+        double acc = part_update<T, TV>(D, k, i, hs, w, true);
         acc = warp_sum(acc);
         if (lane == 0) red[warp] = acc;
         __syncthreads();
@@ -370,7 +468,7 @@ k_orth2(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
 }
 
 // v_{i+1} = w * (1 / h_{i+1,i}) (pgmres.c:117)
-template <typename T>
+template <typename T, typename TV = T>
 __global__ void __launch_bounds__(kThreads)
 k_normalize(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
 {
@@ -379,15 +477,16 @@ k_normalize(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const
         const DChunk k = ch[c];
         const SysDev &D = sys[k.sys];
         if (!D.st->in_cycle) continue;
-        const T sc = (T)(1.0 / D.st->hn);
+        const T sc = (T)((double)D.vsc / D.st->hn);     // stored as sigma v
         const T *w = (const T *)D.w;
-        T *v = (T *)D.V + (size_t)(i + 1) * D.n_pad;
-        constexpr int N = Pk<T>::N;
-        for (int q = k.d0 + threadIdx.x * N; q < k.d1; q += blockDim.x * N) {
-            auto p = ld_pk(w + q);
+        TV *v = (TV *)D.V + (size_t)(i + 1) * D.n_pad;
+        constexpr int G = VPk<TV>::G;
+        for (int q = k.d0 + threadIdx.x * G; q < k.d1; q += blockDim.x * G) {
+            T p[G];
+            ld_g<T, G>(w + q, p);
 #pragma unroll
-            for (int c = 0; c < N; ++c) p.v[c] = q + c < D.n ? sc * p.v[c] : (T)0;
-            st_pk(v + q, p);
+            for (int c = 0; c < G; ++c) p[c] = q + c < D.n ? sc * p[c] : (T)0;
+            st_v<T, TV>(v + q, p);
         }
     }
 }
@@ -395,7 +494,7 @@ k_normalize(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const
 // ---------------------------------------------------------------- cycle end
 // x += V y (pgmres.c:173-175) with y from k_orth2; the last part does the
 // restart bookkeeping (:177-179).
-template <typename T>
+template <typename T, typename TV = T>
 __global__ void __launch_bounds__(kThreads)
 k_update(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch)
 {
@@ -407,23 +506,48 @@ k_update(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const in
         if (!D.st->live) continue;
         const int m = D.st->steps;
         __syncthreads();
-        for (int j = threadIdx.x; j < m; j += blockDim.x) y[j] = D.y[j];
+        for (int j = threadIdx.x; j < m; j += blockDim.x) y[j] = D.y[j] * D.vsci;
         __syncthreads();
-        const T *V = (const T *)D.V;
+        const TV *V = (const TV *)D.V;
         const size_t ld = (size_t)D.n_pad;
-        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) {
-            double xv = D.x[d];
+        // a 16-byte pack of the basis per thread and four vectors in flight;
+        // each dof still adds v_j y_j in j order (x and V are zero-padded to
+        // n_pad, so the pack past n adds zeros)
+        constexpr int N = VPk<TV>::G;
+        for (int q = k.d0 + threadIdx.x * N; q < k.d1; q += blockDim.x * N) {
+            double xv[N];
+#pragma unroll
+            for (int c = 0; c < N; c += 2) {
+                const double2 x2 = *reinterpret_cast<const double2 *>(D.x + q + c);
+                xv[c] = x2.x;
+                xv[c + 1] = x2.y;
+            }
             int j = 0;
             for (; j + 3 < m; j += 4) {
-                const double v0 = (double)V[j * ld + d], v1 = (double)V[(j + 1) * ld + d];
-                const double v2 = (double)V[(j + 2) * ld + d], v3 = (double)V[(j + 3) * ld + d];
-                xv = xv + v0 * y[j];
-                xv = xv + v1 * y[j + 1];
-                xv = xv + v2 * y[j + 2];
-                xv = xv + v3 * y[j + 3];
+                T v0[N], v1[N], v2[N], v3[N];
+                ld_v<T, TV>(V + j * ld + q, v0);
+                ld_v<T, TV>(V + (j + 1) * ld + q, v1);
+                ld_v<T, TV>(V + (j + 2) * ld + q, v2);
+                ld_v<T, TV>(V + (j + 3) * ld + q, v3);
+                const double y0 = y[j], y1 = y[j + 1], y2 = y[j + 2], y3 = y[j + 3];
+#pragma unroll
+                for (int c = 0; c < N; ++c) {
+                    xv[c] = xv[c] + (double)v0[c] * y0;
+                    xv[c] = xv[c] + (double)v1[c] * y1;
+                    xv[c] = xv[c] + (double)v2[c] * y2;
+                    xv[c] = xv[c] + (double)v3[c] * y3;
+                }
             }
-            for (; j < m; ++j) xv = xv + (double)V[j * ld + d] * y[j];
-            D.x[d] = xv;
+            for (; j < m; ++j) {
+                T v0[N];
+                ld_v<T, TV>(V + j * ld + q, v0);
+                const double y0 = y[j];
+#pragma unroll
+                for (int c = 0; c < N; ++c) xv[c] = xv[c] + (double)v0[c] * y0;
+            }
+#pragma unroll
+            for (int c = 0; c < N; c += 2)
+                *reinterpret_cast<double2 *>(D.x + q + c) = make_double2(xv[c], xv[c + 1]);
         }
         if (last_part(D, 4)) {
             if (threadIdx.x == 0) {

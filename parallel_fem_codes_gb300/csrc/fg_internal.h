@@ -133,7 +133,13 @@ int matrix_bandwidth(int n, const int *IA, const int *JA);
 constexpr int kMaxColours = 64;
 constexpr int kElemChunk = 1024;   // elements per matvec work item
 constexpr int kMaxParts = 1024;    // dof parts (reduction partials) per system
-constexpr int kPartMin = 2048;     // minimum dofs per part
+// Dofs per part of the Krylov dof kernels, chosen per batch: the batch's
+// dofs over kPartTarget parts, within [kPartMin, kPartMax].  A full batch
+// gets large parts (fixed per-part cost amortised; 8k-16k measured best on
+// GB300), a batch whose last few systems are still iterating gets small
+// ones so that it still spreads over the SMs.
+constexpr int kPartMin = 2048;
+constexpr int kPartMax = 12288;
 constexpr int kThreads = 256;
 
 struct SysState {
@@ -152,6 +158,8 @@ struct SysState {
 struct SysDev {
     int n, n_pad, nel, nel_pad, S, ndof, ncol, nparts, nnodes;
     int kmax, lmax, mixed, precond;
+    int vhalf;                 // basis stored in FP16, scaled by vsc (a power of two)
+    float vsc, vsci;           // sigma ~ sqrt(n) and 1 / sigma (1 without vhalf)
     double tol, inner_tol;
     const int *lm;             // [S][nel_pad] internal dofs
     const unsigned short *lm16;// [S][nel_pad] patch-local indices (0xFFFF = sink)

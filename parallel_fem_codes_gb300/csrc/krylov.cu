@@ -21,6 +21,8 @@
 #include <atomic>
 #include <chrono>
 #include <type_traits>
+
+#include <cuda_fp16.h>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -136,6 +138,7 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
                     : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+        const __half *Xh = in_sel == 1 && D.vhalf ? (const __half *)D.V + (size_t)step * D.n_pad : nullptr;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
@@ -170,13 +173,14 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
             for (int u = 0; u < DMAX; ++u) {
                 const int j = threadIdx.x + u * kThreads;
                 if (j < pnd) {
-                    xs[j] = (TA)X[dv[u] & 0x7fffffff];
+                    xs[j] = Xh ? (TA)(__half2float(Xh[dv[u] & 0x7fffffff]) * D.vsci) : (TA)X[dv[u] & 0x7fffffff];
                     ys[j] = (TA)0;
                 }
             }
         } else {
             for (int j = threadIdx.x; j < pnd; j += kThreads) {
-                xs[j] = (TA)X[D.dofs[pd0 + j] & 0x7fffffff];
+                xs[j] = Xh ? (TA)(__half2float(Xh[D.dofs[pd0 + j] & 0x7fffffff]) * D.vsci)
+                           : (TA)X[D.dofs[pd0 + j] & 0x7fffffff];
                 ys[j] = (TA)0;
             }
         }
@@ -294,6 +298,7 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
                     : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+        const __half *Xh = in_sel == 1 && D.vhalf ? (const __half *)D.V + (size_t)step * D.n_pad : nullptr;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
@@ -323,7 +328,8 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
 #pragma unroll
         for (int u = 0; u < DMAX; ++u) {
             const int j = threadIdx.x + u * kThreads;
-            if (j < pnd) xs[j] = (TA)X[dv[u] & 0x7fffffff];
+            if (j < pnd)
+                xs[j] = Xh ? (TA)(__half2float(Xh[dv[u] & 0x7fffffff]) * D.vsci) : (TA)X[dv[u] & 0x7fffffff];
         }
         __syncthreads();
 #pragma unroll
@@ -377,6 +383,7 @@ k_csr_mv(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const in
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
                     : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+        const __half *Xh = in_sel == 1 && D.vhalf ? (const __half *)D.V + (size_t)step * D.n_pad : nullptr;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *AA = sizeof(TA) == 8 ? (const TA *)D.AA64 : (const TA *)D.AA32;
         for (int base = k.d0; base < k.d1; base += ngrp) {
@@ -384,7 +391,8 @@ k_csr_mv(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const in
             TA s = 0;
             if (row < k.d1)
                 for (int q = D.csr_ia[row] + sub; q < D.csr_ia[row + 1]; q += W)
-                    s += ldst(AA + q) * (TA)X[__ldcs(D.csr_ja + q)];
+                    s += ldst(AA + q) * (Xh ? (TA)(__half2float(Xh[__ldcs(D.csr_ja + q)]) * D.vsci)
+                                             : (TA)X[__ldcs(D.csr_ja + q)]);
 #pragma unroll
             for (int o = W / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, W);
             if (row < k.d1 && sub == 0) Y[row] = (TY)s;
@@ -512,7 +520,15 @@ k_start(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
 }
 
 // v0 = r * (1 / ||r||) (pgmres.c:78-81)
-template <typename T>
+template <typename TV>
+__device__ __forceinline__ TV to_basis(double v)
+{
+    if constexpr (std::is_same<TV, __half>::value) return __float2half_rn((float)v);
+    else return (TV)v;
+}
+
+// v_0 = r / ||r||, stored as sigma v_0 (sigma = 1 unless the basis is FP16)
+template <typename T, typename TV = T>
 __global__ void __launch_bounds__(kThreads)
 k_scale_v0(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch)
 {
@@ -522,8 +538,11 @@ k_scale_v0(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const 
         const SysDev &D = sys[k.sys];
         if (!D.st->in_cycle) continue;
         const double sc = 1.0 / D.st->r0;
-        T *V0 = (T *)D.V;
-        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) V0[d] = (T)(sc * D.r64[d]);
+        TV *V0 = (TV *)D.V;
+        for (int d = k.d0 + threadIdx.x; d < k.d1; d += blockDim.x) {
+            const T v = (T)(sc * D.r64[d]);
+            V0[d] = to_basis<TV>((double)D.vsc * (double)v);
+        }
     }
 }
 
@@ -660,10 +679,20 @@ inline dim3 grid_for(int nchunks)
     return dim3((unsigned)std::max(1, std::min(nchunks, cap)));
 }
 
-int parts_for(int n)
+int parts_for(int n, int part_dofs = kPartMax)
 {
-    int p = (n + kPartMin - 1) / kPartMin;
+    int p = (n + part_dofs - 1) / part_dofs;
     return std::max(1, std::min(kMaxParts, p));
+}
+
+// part size of a batch (multiple of 8 dofs): its dofs over 8 CTAs per SM
+int part_dofs_for(const std::vector<BatchMember> &mem)
+{
+    long long tot = 0;
+    for (auto &m : mem) tot += m.s->topo.n;
+    const long long target = 8LL * sm_count();
+    const long long pd = std::max<long long>(kPartMin, std::min<long long>(kPartMax, tot / std::max(1LL, target)));
+    return (int)(pd & ~7LL);
 }
 
 }  // namespace
@@ -705,13 +734,15 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     }
     std::vector<DChunk> dch;
     std::vector<NChunk> nch;
+    const int pdofs = part_dofs_for(mem);
     for (int s = 0; s < P.nsys; ++s) {
         int n = mem[s].s->topo.n;
+        hs[s].nparts = parts_for(n, pdofs);
         int np = hs[s].nparts;
-        // part boundaries on multiples of 4 dofs (16-byte packs in FP32 and FP64)
+        // part boundaries on multiples of 8 dofs (16-byte packs in FP16, FP32 and FP64)
         for (int p = 0; p < np; ++p) {
-            int d0 = (int)((long long)n * p / np) & ~3;
-            int d1 = p + 1 == np ? n : (int)((long long)n * (p + 1) / np) & ~3;
+            int d0 = (int)((long long)n * p / np) & ~7;
+            int d1 = p + 1 == np ? n : (int)((long long)n * (p + 1) / np) & ~7;
             dch.push_back({s, p, d0, d1});
         }
         int nn = mem[s].s->topo.nnodes;
@@ -870,8 +901,9 @@ static int enqueue_precond(const Plan &P, int sel, cudaStream_t st)
     return 0;
 }
 
-// One restart cycle for every member; returns the number of kernels.
-template <typename T>
+// One restart cycle for every member; returns the number of kernels.  TV
+// is the basis' storage type (T, or FP16 under FP32 arithmetic).
+template <typename T, typename TV = T>
 static int enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
 {
     const SysDev *sys = P.sysdev.as<SysDev>();
@@ -884,37 +916,43 @@ static int enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
     int k = enqueue_matvec<T>(P, 0, 0, st);
     k += enqueue_precond<T>(P, 0, st);
     k_start<<<gd, kThreads, 0, st>>>(sys, dc, nd);
-    k_scale_v0<T><<<gd, kThreads, 0, st>>>(sys, dc, nd);
+    k_scale_v0<T, TV><<<gd, kThreads, 0, st>>>(sys, dc, nd);
     k += 2;
     for (int i = 0; i < cfg.kmax - 1; ++i) {
         k += enqueue_matvec<T>(P, 1, i, st);
         k += enqueue_precond<T>(P, 1, st);
-        if (gram) {
-            k_dots1g<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        if constexpr (std::is_same<T, TV>::value) {
+            if (gram) {
+                k_dots1g<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+            } else {
+                k_dots1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+                k_orth1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+                ++k;
+            }
         } else {
-            k_dots1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
-            k_orth1<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
-            ++k;
+            k_dots1g<T, TV><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);   // narrow basis: Gram path only
         }
-        k_orth2<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
-        k_normalize<T><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        k_orth2<T, TV><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
+        k_normalize<T, TV><<<gd, kThreads, 0, st>>>(sys, dc, nd, i);
         k += 3;
     }
-    k_update<T><<<gd, kThreads, 0, st>>>(sys, dc, nd);
+    k_update<T, TV><<<gd, kThreads, 0, st>>>(sys, dc, nd);
     k_live<<<(P.nsys + 255) / 256, 256, 0, st>>>(sys, P.nsys, P.live.as<int>());
     return k + 2;
 }
 
-static int ensure_workspace(fg_system *s, int kmax, int mixed)
+// mode: 0 FP64, 1 FP32 basis, 2 FP16 basis (mixed precision in both)
+static int ensure_workspace(fg_system *s, int kmax, int mode)
 {
     Workspace &w = s->ws;
-    if (w.kmax >= kmax && w.mixed == mixed) return FG_OK;
+    if (w.kmax >= kmax && w.mixed == mode) return FG_OK;
     w.kmax = 0;
     w.mixed = -1;
     size_t np = (size_t)s->n_pad;
-    size_t ts = mixed ? sizeof(float) : sizeof(double);
+    size_t ts = mode ? sizeof(float) : sizeof(double);
+    size_t vs = mode == 2 ? 2 : ts;
     int r;
-    if ((r = w.V.alloc(ts * np * kmax)) || (r = w.w.alloc(ts * np)) || (r = w.t.alloc(ts * np)) ||
+    if ((r = w.V.alloc(vs * np * kmax)) || (r = w.w.alloc(ts * np)) || (r = w.t.alloc(ts * np)) ||
         (r = w.x.alloc(8 * np)) || (r = w.b.alloc(8 * np)) || (r = w.ftrue.alloc(8 * np)) ||
         (r = w.r64.alloc(8 * np)) || (r = w.t64.alloc(8 * np)) || (r = w.u64.alloc(8 * np)) ||
         (r = w.small.alloc(8 * ((size_t)(kmax + 1) * kmax + 5 * (kmax + 1) + (size_t)kmax * kmax))) ||
@@ -922,7 +960,7 @@ static int ensure_workspace(fg_system *s, int kmax, int mixed)
         (r = w.counter.alloc(sizeof(unsigned) * 8)) || (r = w.state.alloc(sizeof(SysState))))
         return r;
     w.kmax = kmax;
-    w.mixed = mixed;
+    w.mixed = mode;
     return FG_OK;
 }
 
@@ -935,6 +973,13 @@ static SysDev make_desc(fg_system *s, const SolveConfig &cfg, bool has_f)
     D.ncol = t.ncol; D.nparts = parts_for(t.n); D.nnodes = t.nnodes;
     D.kmax = cfg.kmax; D.lmax = cfg.lmax; D.mixed = cfg.mixed; D.precond = cfg.precond;
     D.tol = cfg.tol; D.inner_tol = cfg.inner_tol;
+    D.vhalf = cfg.vhalf;
+    D.vsc = D.vsci = 1.0f;
+    if (cfg.vhalf) {   // unit vectors times 2^floor(log2 sqrt n): entries of order 1 in FP16
+        const int e = (int)std::floor(0.5 * std::log2((double)std::max(t.n, 1)));
+        D.vsc = std::ldexp(1.0f, e);
+        D.vsci = std::ldexp(1.0f, -e);
+    }
     D.lm = s->lm.as<int>(); D.A64 = s->A64.as<double>(); D.A32 = s->A32.as<float>();
     set_patch_fields(D, s);
     D.invd64 = s->invd64.as<double>(); D.invd32 = s->invd32.as<float>();
@@ -1000,14 +1045,14 @@ int BatchRun::stage(const BatchMember &m)
     fg_system *s = m.s;
     int r = validate_member(s, cfg);
     if (r) return r;
-    if ((r = ensure_workspace(s, cfg.kmax, cfg.mixed))) return r;
+    if ((r = ensure_workspace(s, cfg.kmax, cfg.mixed + cfg.vhalf))) return r;
     if (s->op == FG_OP_CSR && (r = csr_refresh(s, st))) return r;
     Workspace &w = s->ws;
     size_t vb = 8 * (size_t)s->n_pad;
     FG_CUDA(cudaMemsetAsync(w.x.p, 0, vb, st));
     FG_CUDA(cudaMemsetAsync(w.t64.p, 0, vb, st));
     FG_CUDA(cudaMemsetAsync(w.t.p, 0, (cfg.mixed ? 4 : 8) * (size_t)s->n_pad, st));
-    FG_CUDA(cudaMemsetAsync(w.V.p, 0, (cfg.mixed ? 4 : 8) * (size_t)s->n_pad * cfg.kmax, st));
+    FG_CUDA(cudaMemsetAsync(w.V.p, 0, (cfg.vhalf ? 2 : cfg.mixed ? 4 : 8) * (size_t)s->n_pad * cfg.kmax, st));
     FG_CUDA(cudaMemsetAsync(w.small.p, 0, w.small.bytes, st));
     if (cfg.device_io) {
         FG_CUDA(cudaMemcpyAsync(w.b.p, m.B, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToDevice, st));
@@ -1062,7 +1107,8 @@ int BatchRun::cycle(bool use_graph, std::vector<int> &live)
     if (use_graph && !exec) {
         cudaGraph_t graph = nullptr;
         FG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        graph_nodes = cfg.mixed ? enqueue_cycle<float>(Pl, cfg, st) : enqueue_cycle<double>(Pl, cfg, st);
+        graph_nodes = cfg.vhalf ? enqueue_cycle<float, __half>(Pl, cfg, st)
+                             : cfg.mixed ? enqueue_cycle<float>(Pl, cfg, st) : enqueue_cycle<double>(Pl, cfg, st);
         ce = cudaStreamEndCapture(st, &graph);
         if (ce != cudaSuccess) return cuda_fail(ce, "cudaStreamEndCapture");
         ce = cudaGraphInstantiate(&exec, graph, 0);
@@ -1073,7 +1119,8 @@ int BatchRun::cycle(bool use_graph, std::vector<int> &live)
         ce = cudaGraphLaunch(exec, st);
         count_launches(graph_nodes);
     } else {
-        count_launches(cfg.mixed ? enqueue_cycle<float>(Pl, cfg, st) : enqueue_cycle<double>(Pl, cfg, st));
+        count_launches(cfg.vhalf ? enqueue_cycle<float, __half>(Pl, cfg, st)
+                             : cfg.mixed ? enqueue_cycle<float>(Pl, cfg, st) : enqueue_cycle<double>(Pl, cfg, st));
         ce = cudaGetLastError();
     }
     if (ce == cudaSuccess) ce = cudaMemcpyAsync(h_live, Pl.live.p, sizeof(int) * mem.size(), cudaMemcpyDeviceToHost, st);

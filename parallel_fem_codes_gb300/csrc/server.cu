@@ -156,7 +156,7 @@ void fg_server::run()
 void fg_server::run_euler()
 {
     cudaSetDevice(device);
-    fg_solver_opts so{cfg.kmax, cfg.lmax, cfg.tol, cfg.mixed ? FG_PREC_MIXED : FG_PREC_FP64, o.inner_tol};
+    fg_solver_opts so{cfg.kmax, cfg.lmax, cfg.tol, o.precision, o.inner_tol};
     for (;;) {
         EulerRequest r;
         {
@@ -196,8 +196,11 @@ int fg_server_create(fg_server **out, const fg_server_opts *opts)
 {
     if (!out || !opts) { set_error("NULL argument"); return FG_ERR_ARG; }
     *out = nullptr;
-    if (opts->precision != FG_PREC_MIXED && opts->precision != FG_PREC_FP64) {
-        set_error("precision must be FG_PREC_FP64 or FG_PREC_MIXED"); return FG_ERR_ARG;
+    if (opts->precision != FG_PREC_MIXED && opts->precision != FG_PREC_FP64 && opts->precision != FG_PREC_MIXED16) {
+        set_error("precision must be FG_PREC_FP64, FG_PREC_MIXED or FG_PREC_MIXED16"); return FG_ERR_ARG;
+    }
+    if (opts->precision == FG_PREC_MIXED16 && opts->kmax > 32) {
+        set_error("FG_PREC_MIXED16 needs kmax <= 32"); return FG_ERR_ARG;
     }
     if (opts->kmax < 2 || opts->kmax > kPartStride - 4 || opts->lmax < 1) {
         set_error("kmax must be in [2, 60] and lmax >= 1"); return FG_ERR_ARG;
@@ -208,7 +211,8 @@ int fg_server_create(fg_server **out, const fg_server_opts *opts)
     sv->cfg.kmax = opts->kmax;
     sv->cfg.lmax = opts->lmax;
     sv->cfg.tol = opts->tol;
-    sv->cfg.mixed = opts->precision == FG_PREC_MIXED ? 1 : 0;
+    sv->cfg.mixed = opts->precision == FG_PREC_FP64 ? 0 : 1;
+    sv->cfg.vhalf = opts->precision == FG_PREC_MIXED16 ? 1 : 0;
     sv->cfg.inner_tol = opts->inner_tol > 0 ? opts->inner_tol : 1e-5;
     sv->cfg.precond = FG_PRECOND_DIAG;
     sv->cfg.device_io = 1;

@@ -401,18 +401,16 @@ int fg_set_diag(fg_system *s, const double *Diag)
     return FG_OK;
 }
 
+static int batch_config(fg_system *const *systems, int count, const fg_solver_opts *o, SolveConfig &cfg);
+
 int fg_solve(fg_system *s, const fg_solver_opts *o, const double *B, double *X, const double *F_true,
              fg_solve_stats *stats)
 {
     if (!s || !o || !B || !X) { set_error("NULL argument"); return FG_ERR_ARG; }
     SolveConfig cfg;
-    cfg.kmax = o->kmax; cfg.lmax = o->lmax; cfg.tol = o->tol;
-    cfg.mixed = o->precision == FG_PREC_MIXED ? 1 : 0;
-    if (o->precision != FG_PREC_MIXED && o->precision != FG_PREC_FP64) {
-        set_error("precision must be FG_PREC_FP64 or FG_PREC_MIXED"); return FG_ERR_ARG;
-    }
-    cfg.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
-    cfg.precond = s->precond;
+    fg_system *one[1] = {s};
+    int r0 = batch_config(one, 1, o, cfg);
+    if (r0) return r0;
     std::vector<BatchMember> mem{{s, B, F_true, X}};
     fg_solve_stats st{};
     int r = solve_batch(mem, cfg, &st, s->stream);
@@ -423,11 +421,15 @@ int fg_solve(fg_system *s, const fg_solver_opts *o, const double *B, double *X, 
 static int batch_config(fg_system *const *systems, int count, const fg_solver_opts *o, SolveConfig &cfg)
 {
     if (!systems || count < 1 || !o) { set_error("NULL argument or empty batch"); return FG_ERR_ARG; }
-    if (o->precision != FG_PREC_MIXED && o->precision != FG_PREC_FP64) {
-        set_error("precision must be FG_PREC_FP64 or FG_PREC_MIXED"); return FG_ERR_ARG;
+    if (o->precision != FG_PREC_MIXED && o->precision != FG_PREC_FP64 && o->precision != FG_PREC_MIXED16) {
+        set_error("precision must be FG_PREC_FP64, FG_PREC_MIXED or FG_PREC_MIXED16"); return FG_ERR_ARG;
+    }
+    if (o->precision == FG_PREC_MIXED16 && o->kmax > 32) {
+        set_error("FG_PREC_MIXED16 needs kmax <= 32 (Gram-corrected Arnoldi)"); return FG_ERR_ARG;
     }
     cfg.kmax = o->kmax; cfg.lmax = o->lmax; cfg.tol = o->tol;
-    cfg.mixed = o->precision == FG_PREC_MIXED ? 1 : 0;
+    cfg.mixed = o->precision == FG_PREC_FP64 ? 0 : 1;
+    cfg.vhalf = o->precision == FG_PREC_MIXED16 ? 1 : 0;
     cfg.inner_tol = o->inner_tol > 0 ? o->inner_tol : 1e-5;
     for (int i = 0; i < count; ++i) {
         if (!systems[i]) { set_error("NULL system in batch"); return FG_ERR_ARG; }

@@ -145,6 +145,7 @@ struct SolveConfig {
     int kmax = 30, lmax = 1000;
     double tol = 1e-10, inner_tol = 1e-5;
     int mixed = 0;         // 0: FP64 reference method; 1: FP32 Arnoldi in FP64 refinement
+    int vhalf = 0;         // mixed with the Krylov basis stored in FP16 (Gram path only)
     int precond = FG_PRECOND_DIAG;
     int device_io = 0;     // B/X/Ftrue are device pointers in internal numbering
     int use_graph = 1;

@@ -19,7 +19,7 @@ FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG, FG_PRECOND_ILU0, FG_PREC
 FG_SCALE_LEFT, FG_SCALE_LEFTRIGHT = 1, 2
 FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
-FG_PREC_FP64, FG_PREC_MIXED = 64, 32
+FG_PREC_FP64, FG_PREC_MIXED, FG_PREC_MIXED16 = 64, 32, 16
 FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 = 0, 1, 2
 FG_NS_SUPG_PSPG, FG_NS_VMS_DCDD = 0, 1
 FG_TRANSPORT_SUPG, FG_TRANSPORT_DD = 0, 1

@@ -62,3 +62,28 @@ def test_launch_count_grows(fg):
     s.transport_prepare(p)
     fg.solve_resident([s])
     assert fg.launch_count() > before
+
+
+def test_mixed16_basis_converges(fg):
+    """FP16 storage of the Krylov basis (FP32 arithmetic, FP64 refinement):
+    the batch reaches the same true relative residual and the FP64 solution."""
+    probs = G.batch_transport_problems(count=6, seed=7, nmin=17, nmax=97)
+    systems, Bs, Fs = [], [], []
+    for p in probs:
+        s = fg.transport_system(p)
+        F = s.transport_assemble(p)
+        Fp = s.precond_setup(fg.FG_PRECOND_DIAG, fg.FG_SETUP_ACCUMULATE, F)
+        systems.append(s); Bs.append(Fp); Fs.append(F)
+    X64, st64 = fg.solve_batch(systems, Bs, Fs, kmax=30, lmax=10000, tol=1e-10, precision=fg.FG_PREC_FP64)
+    X16, st16 = fg.solve_batch(systems, Bs, Fs, kmax=30, lmax=10000, tol=1e-10, precision=fg.FG_PREC_MIXED16)
+    for a, b, st in zip(X64, X16, st16):
+        assert st["converged"] == 1 and st["true_rel_residual"] <= 1e-10
+        assert np.linalg.norm(b[:-1] - a[:-1]) <= 1e-8 * np.linalg.norm(a[:-1])
+
+
+def test_mixed16_needs_gram_path(fg):
+    p = G.transport_problem(9)
+    s = fg.transport_system(p)
+    F = s.transport_assemble(p)
+    with pytest.raises(Exception):
+        fg.solve_batch([s], [F], [F], kmax=40, lmax=10, tol=1e-10, precision=fg.FG_PREC_MIXED16)
