@@ -88,6 +88,14 @@ __device__ __forceinline__ void reduce_parts(const SysDev &D, int nv, double *ou
     __syncthreads();
 }
 
+// A matvec input entry in the arithmetic type: an FP16 basis vector is
+// stored as sigma v, so it is scaled back (exactly: sigma is a power of two).
+template <typename TA, typename TX> __device__ __forceinline__ TA in_value(TX v, const SysDev &D)
+{
+    if constexpr (std::is_same<TX, __half>::value) return (TA)(__half2float(v) * D.vsci);
+    else return (TA)v;
+}
+
 // ---------------------------------------------------------------- EBE matvec
 // y[lm] += A_e x[lm] by patches.  A patch is up to patch_elems(S)
 // consecutive elements (internal order: sorted by their smallest dof, so a
@@ -138,7 +146,6 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
                     : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
-        const __half *Xh = in_sel == 1 && D.vhalf ? (const __half *)D.V + (size_t)step * D.n_pad : nullptr;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
@@ -173,14 +180,13 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
             for (int u = 0; u < DMAX; ++u) {
                 const int j = threadIdx.x + u * kThreads;
                 if (j < pnd) {
-                    xs[j] = Xh ? (TA)(__half2float(Xh[dv[u] & 0x7fffffff]) * D.vsci) : (TA)X[dv[u] & 0x7fffffff];
+                    xs[j] = in_value<TA>(X[dv[u] & 0x7fffffff], D);
                     ys[j] = (TA)0;
                 }
             }
         } else {
             for (int j = threadIdx.x; j < pnd; j += kThreads) {
-                xs[j] = Xh ? (TA)(__half2float(Xh[D.dofs[pd0 + j] & 0x7fffffff]) * D.vsci)
-                           : (TA)X[D.dofs[pd0 + j] & 0x7fffffff];
+                xs[j] = in_value<TA>(X[D.dofs[pd0 + j] & 0x7fffffff], D);
                 ys[j] = (TA)0;
             }
         }
@@ -298,7 +304,6 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
                     : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
-        const __half *Xh = in_sel == 1 && D.vhalf ? (const __half *)D.V + (size_t)step * D.n_pad : nullptr;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
@@ -328,8 +333,7 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
 #pragma unroll
         for (int u = 0; u < DMAX; ++u) {
             const int j = threadIdx.x + u * kThreads;
-            if (j < pnd)
-                xs[j] = Xh ? (TA)(__half2float(Xh[dv[u] & 0x7fffffff]) * D.vsci) : (TA)X[dv[u] & 0x7fffffff];
+            if (j < pnd) xs[j] = in_value<TA>(X[dv[u] & 0x7fffffff], D);
         }
         __syncthreads();
 #pragma unroll
@@ -383,7 +387,6 @@ k_csr_mv(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const in
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
                     : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
-        const __half *Xh = in_sel == 1 && D.vhalf ? (const __half *)D.V + (size_t)step * D.n_pad : nullptr;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *AA = sizeof(TA) == 8 ? (const TA *)D.AA64 : (const TA *)D.AA32;
         for (int base = k.d0; base < k.d1; base += ngrp) {
@@ -391,8 +394,7 @@ k_csr_mv(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const in
             TA s = 0;
             if (row < k.d1)
                 for (int q = D.csr_ia[row] + sub; q < D.csr_ia[row + 1]; q += W)
-                    s += ldst(AA + q) * (Xh ? (TA)(__half2float(Xh[__ldcs(D.csr_ja + q)]) * D.vsci)
-                                             : (TA)X[__ldcs(D.csr_ja + q)]);
+                    s += ldst(AA + q) * in_value<TA>(X[__ldcs(D.csr_ja + q)], D);
 #pragma unroll
             for (int o = W / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, W);
             if (row < k.d1 && sub == 0) Y[row] = (TY)s;
@@ -843,7 +845,8 @@ static void launch_csr_mv(const Plan &P, cudaStream_t st, int gate, int in_sel, 
 // Enqueue the matvec: mode 0 (x -> t64, FP64, gate live), mode 1 (V[step]
 // -> t, T, gate in_cycle), mode 2 (V[0] -> t, T, every member), mode 3
 // (x -> t64, FP64, every member).  Returns the number of kernels.
-template <typename T>
+// TV: storage type of the basis vector read in mode 1 (the Arnoldi step)
+template <typename T, typename TV = T>
 static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
 {
     const bool f64 = mode == 0 || mode == 3;
@@ -851,7 +854,7 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
     const int sel = f64 ? 0 : 1;
     if (P.op == FG_OP_CSR) {
         if (f64) launch_csr_mv<double, double, double>(P, st, gate, sel, sel, step);
-        else launch_csr_mv<T, T, T>(P, st, gate, sel, sel, step);
+        else launch_csr_mv<T, TV, T>(P, st, gate, sel, sel, step);
         return 1;
     }
     const SysDev *sys = P.sysdev.as<SysDev>();
@@ -865,7 +868,7 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
             MvLaunch::go<double, double, double>(P.S, cnt, st, sys, ch, nc, gate, 0, 0, 0, nullptr, nullptr,
                                                  P.maxdof);
         else
-            MvLaunch::go<T, T, T>(P.S, cnt, st, sys, ch, nc, gate, 1, 1, step, nullptr, nullptr, P.maxdof);
+            MvLaunch::go<T, TV, T>(P.S, cnt, st, sys, ch, nc, gate, 1, 1, step, nullptr, nullptr, P.maxdof);
         ++k;
     }
     return k;
@@ -919,7 +922,7 @@ static int enqueue_cycle(const Plan &P, const SolveConfig &cfg, cudaStream_t st)
     k_scale_v0<T, TV><<<gd, kThreads, 0, st>>>(sys, dc, nd);
     k += 2;
     for (int i = 0; i < cfg.kmax - 1; ++i) {
-        k += enqueue_matvec<T>(P, 1, i, st);
+        k += enqueue_matvec<T, TV>(P, 1, i, st);
         k += enqueue_precond<T>(P, 1, st);
         if constexpr (std::is_same<T, TV>::value) {
             if (gram) {
