@@ -168,6 +168,11 @@ enum { FG_PRECOND_NONE = 0, FG_PRECOND_DIAG = 1, FG_PRECOND_BLOCKDIAG = 2,
  * the next fg_precond_setup(FG_PRECOND_SPIKE); systems whose band factors
  * would exceed 8 GiB are rejected there with FG_ERR_UNSUPPORTED. */
 int fg_set_spike(fg_system *s, int k, int parts);
+/* Fill level p of the ILU preconditioner (Preconditioner "ILU<p>",
+ * CSR/ILUp_precond_setup.c:16 with the level-of-fill symbolic pass of
+ * ilup.c:164-301); 0 (the default) is ILU(0).  FG_PRECOND_ILU0 then sets up
+ * and applies ILU(p) on the factor pattern; p in [0, 16]. */
+int fg_set_ilu_fill(fg_system *s, int p);
 enum {
     FG_SETUP_ACCUMULATE = 1, /* Diag += new diagonal, as Diag_precond_EBE_setup
                                 does across nonlinear iterations              */

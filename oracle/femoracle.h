@@ -244,6 +244,14 @@ void or_csr_assemble(int nel, int S, const int *lm, const double *A, int NEQ,
                      const int *IA, const int *JA, double *AA);
 void or_csrmv(int n, const int *IA, const int *JA, const double *AA, const double *P, double *Q);
 int  or_ilu0_factor(int n, const int *IA, const int *JA, const double *AA, double *LU, double *D);
+/* ILU(p) (oracle/ilup.c): symbolic pass to a factor CSR (per row: L
+ * ascending, diagonal, U in the reference's order), numeric factorisation,
+ * substitutions. */
+int  or_ilup_symbolic(int n, const int *IA, const int *JA, int p, int **FIA, int **FJA, int **FDG);
+int  or_ilup_factor(int n, const int *IA, const int *JA, const double *AA, const int *FIA, const int *FJA,
+                    const int *FDG, double *LU, double *D);
+void or_ilup_apply(int n, const int *FIA, const int *FJA, const int *FDG, const double *LU, const double *D,
+                   const double *y, double *x);
 void or_ilu0_apply(int n, const int *IA, const int *JA, const double *LU, const double *D,
                    const double *y, double *x);
 

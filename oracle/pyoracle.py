@@ -664,9 +664,50 @@ def ilu0_apply(IA, JA, LU, D, y):
     return x
 
 
-def ref_csr(prob, A, P):
-    """The reference's csr_Initialization + csr_assembly + csrmv + ILU(0)."""
+def ilup(IA, JA, AA, p):
+    """ILU(p): returns (FIA, FJA, FDG, LU, D) on the factor CSR."""
+    L = lib()
+    n = len(IA) - 1
+    IA = np.ascontiguousarray(IA, dtype=np.int32)
+    JA = np.ascontiguousarray(JA, dtype=np.int32)
+    pi = ctypes.POINTER(_c_int)
+    fia, fja, fdg = pi(), pi(), pi()
+    L.or_ilup_symbolic.argtypes = [_c_int, _i32p, _i32p, _c_int, ctypes.POINTER(pi), ctypes.POINTER(pi),
+                                   ctypes.POINTER(pi)]
+    L.or_ilup_symbolic(n, IA, JA, int(p), ctypes.byref(fia), ctypes.byref(fja), ctypes.byref(fdg))
+    FIA = np.ctypeslib.as_array(fia, shape=(n + 1,)).copy()
+    FJA = np.ctypeslib.as_array(fja, shape=(max(int(FIA[-1]), 1),)).copy()[: int(FIA[-1])]
+    FDG = np.ctypeslib.as_array(fdg, shape=(max(n, 1),)).copy()[:n]
+    libc = ctypes.CDLL(None)
+    libc.free.argtypes = [ctypes.c_void_p]
+    for q in (fia, fja, fdg):
+        libc.free(ctypes.cast(q, ctypes.c_void_p))
+    LU = np.zeros(max(int(FIA[-1]), 1))
+    D = np.zeros(max(n, 1))
+    L.or_ilup_factor.argtypes = [_c_int, _i32p, _i32p, _f64p, _i32p, _i32p, _i32p, _f64p, _f64p]
+    rc = L.or_ilup_factor(n, IA, JA, np.ascontiguousarray(AA, dtype=np.float64), FIA, FJA, FDG, LU, D)
+    if rc:
+        raise ZeroDivisionError(f"ILU({p}): zero pivot in row {rc - 1}")
+    return FIA, FJA, FDG, LU, D
+
+
+def ilup_apply(FIA, FJA, FDG, LU, D, y):
+    L = lib()
+    n = len(FIA) - 1
+    L.or_ilup_apply.argtypes = [_c_int, _i32p, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p]
+    L.or_ilup_apply.restype = None
+    x = np.zeros(n)
+    L.or_ilup_apply(n, FIA, FJA, FDG, LU, D, np.ascontiguousarray(y[:n], dtype=np.float64), x)
+    return x
+
+
+def ref_csr(prob, A, P, ilu_p=0):
+    """The reference's csr_Initialization + csr_assembly + csrmv + ILU(p)
+    (Preconditioner "ILU<p>"): z = M^-1 P."""
     R = ref()
+    R.fr_sst_set_ilu.argtypes = [_c_int]
+    R.fr_sst_set_ilu.restype = None
+    R.fr_sst_set_ilu(int(ilu_p))
     R.fr_sst_csr.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _f64p, _c_int,
                              _i32p, _i32p, _f64p, _i32p, _f64p, _f64p, _f64p]
     m = prob.mesh

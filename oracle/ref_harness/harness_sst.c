@@ -59,6 +59,9 @@ typedef struct {
  * 3 "YZBeta"; h_Shock 0 "2sqrtArea" / 1 "Option1" / 2 "Option2" */
 static int g_form, g_shock = 1, g_hshock;
 
+static int g_ilu_p;   /* fill level of the ILU in fr_sst_csr ("ILU<p>") */
+void fr_sst_set_ilu(int p) { g_ilu_p = p; }
+
 /* Stabilisation of the following builds and Process runs. */
 void fr_sst_set_form(int form, int shock, int hshock)
 {
@@ -329,7 +332,7 @@ int fr_sst_csr(int nnodes, int nel, const double *x, const double *y, const int 
     int I;
     fr_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, 1e-10, 1e-3, 30, 10);
     strcpy(c.P.MatrixVectorProductScheme, "CSR");
-    strcpy(c.P.Preconditioner, "ILU0");
+    sprintf(c.P.Preconditioner, "ILU%d", g_ilu_p);
     csr_Initialization(&c.P, &c.M, &c.S);
     int nnz = c.P.nnzero;
     if (nnz > nnz_max) { fr_free(&c); return -1; }

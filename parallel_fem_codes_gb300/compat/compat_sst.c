@@ -194,21 +194,19 @@ int csrmv(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *Pv, d
     return rc ? fgc_fail(rc, "csrmv") : 0;
 }
 
-/* ILUp_precond_setup (CSR/ILUp_precond_setup.c:8-168) for "ILU0": ILU(0)
- * of the CSR operator, F preconditioned in place.  ILU(p > 0) is not on the
- * GPU and is refused. */
+/* ILUp_precond_setup (CSR/ILUp_precond_setup.c:8-168) for "ILU<p>": ILU(p)
+ * of the CSR operator (p = atoi(&Preconditioner[3]), capped at neq as the
+ * reference caps it), F preconditioned in place. */
 int ILUp_precond_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
 {
     (void)tag;
-    if (atoi(&P->Preconditioner[3]) != 0) {
-        fprintf(stderr, "femgpu: only ILU(0) runs on the GPU (Preconditioner \"%s\")\n", P->Preconditioner);
-        if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
-        return 1;
-    }
+    int p = atoi(&P->Preconditioner[3]);
+    if (p > P->neq) p = P->neq;
     fg_system *sys = fgc_system(P, M, S);
     if (!sys) return 1;
     if (fgc_upload_blocks(sys, M)) return 1;
-    int rc = fg_precond_setup(sys, FG_PRECOND_ILU0, 0, F);
+    int rc = fg_set_ilu_fill(sys, p > 16 ? 16 : p);
+    if (!rc) rc = fg_precond_setup(sys, FG_PRECOND_ILU0, 0, F);
     return rc ? fgc_fail(rc, "ILUp_precond_setup") : 0;
 }
 
@@ -261,7 +259,7 @@ int pgmres(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctions
                                            Fn->precond == NO_precond);
     if (Fn->precondR != NO_precond || !(ebe_ok || csr_ok)) {
         fprintf(stderr, "femgpu: pgmres supports mv = ebemv with Diag or no preconditioning, or mv = csrmv with "
-                        "ILU(0), SPIKE or no preconditioning, on the GPU\n");
+                        "ILU(p), SPIKE or no preconditioning, on the GPU\n");
         if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
         return 1;
     }

@@ -171,6 +171,7 @@ struct SysDev {
     // assembled CSR operator and ILU(0) (op == 1)
     int op, csr_w;
     const int *csr_ia, *csr_ja, *csr_diag;
+    const int *lu_ia, *lu_ja, *lu_dg;    // ILU(p) factor pattern
     const double *AA64, *LU64, *dinv64;
     const float *AA32, *LU32, *dinv32;
     void *ilu_tmp;             // forward-substitution output (T, n_pad)

@@ -4,9 +4,15 @@
 // * k_csr_assemble: CSR values from the element blocks, one thread per
 //   slot summing its element contributions in reference element order, as
 //   csr_assembly.c:3-54 adds them element by element.
-// * k_ilu0_factor: ILU(0) of Solvers_and_Preconditioners/CSR/
-//   ILUp_precond_setup.c:73-168 (IKJ elimination over the ascending L part
-//   of each row, inverse pivots kept).
+// * ilu_fill (host): the level-of-fill symbolic pass of ILU(p)
+//   (Solvers_and_Preconditioners/ilup.c:164-301, Preconditioner "ILU<p>"),
+//   giving the factor pattern: per row the L columns ascending, the
+//   diagonal, then the U columns in the order the pass admits them (the
+//   row's own, then the fill) -- the order the backward substitution sums
+//   them in.  For p = 0 it is the CSR pattern.
+// * k_ilu0_factor: ILU(p) of CSR/ILUp_precond_setup.c:73-168 on the factor
+//   pattern (IKJ elimination over the ascending L part of each row, inverse
+//   pivots kept; the matrix values are scattered into the pattern first).
 // * ilu_fwd / ilu_bwd: the forward and backward substitutions of
 //   CSR/ILUp_precond.c:4-47.
 //
@@ -189,14 +195,21 @@ struct FacSm {
     double uval[kFacPairs];
 };
 
-__device__ __forceinline__ int row_pos(const int *col, int len, int c)
+// slot of column c in a factor row (L part and diagonal ascending, ending at
+// nL; the U part after it in admission order)
+__device__ __forceinline__ int row_pos(const int *col, int len, int nL, int c)
 {
-    int lo = 0, hi = len - 1;
-    while (lo <= hi) {
-        int mid = (lo + hi) >> 1;
-        if (col[mid] == c) return mid;
-        if (col[mid] < c) lo = mid + 1; else hi = mid - 1;
+    if (c <= col[nL]) {
+        int lo = 0, hi = nL;
+        while (lo <= hi) {
+            int mid = (lo + hi) >> 1;
+            if (col[mid] == c) return mid;
+            if (col[mid] < c) lo = mid + 1; else hi = mid - 1;
+        }
+        return -1;
     }
+    for (int t = nL + 1; t < len; ++t)
+        if (col[t] == c) return t;
     return -1;
 }
 
@@ -214,13 +227,9 @@ __device__ void fac_row_seq(int i, const int *__restrict__ ia, const int *__rest
         const double lk = LU[k];
         for (int m = dg[jrow] + 1; m < ia[jrow + 1]; ++m) {
             const int col = ja[m];
-            int lo = b, hi = e - 1, pos = -1;
-            while (lo <= hi) {
-                int mid = (lo + hi) >> 1;
-                if (ja[mid] == col) { pos = mid; break; }
-                if (ja[mid] < col) lo = mid + 1; else hi = mid - 1;
-            }
-            if (pos < 0) continue;
+            const int rp = row_pos(ja + b, e - b, dg[i] - b, col);
+            if (rp < 0) continue;
+            const int pos = b + rp;
             if (col == i) piv = piv - lk * LU[m];
             else LU[pos] = LU[pos] - lk * LU[m];
         }
@@ -284,7 +293,7 @@ k_ilu0_factor(int n, const int *__restrict__ ord, const int *__restrict__ ia, co
                             if (S.ustart[mid] <= p) lo = mid; else hi = mid - 1;
                         }
                         const int m = S.u0[lo] + (p - S.ustart[lo]);
-                        S.pos[p] = (short)row_pos(S.col, len, ja[m]);
+                        S.pos[p] = (short)row_pos(S.col, len, nL, ja[m]);
                         S.uval[p] = __ldcg(LU + m);   // another lane waited for this row: read from L2
                     }
                 }
@@ -378,13 +387,13 @@ __global__ void k_ilu_solve(const SysDev *__restrict__ sys, const int2 *__restri
         if (!backward) {
             const T *in = sel == 0 ? (const T *)D.t64 : (const T *)D.t;
             for_pass_rows<G>(D.ilu_ford, D.ilu_fpass[it.y], [&](int i) {
-                fwd_row<T, G>(i, D.csr_ia, D.csr_ja, D.csr_diag, LU, in, tmp, err);
+                fwd_row<T, G>(i, D.lu_ia, D.lu_ja, D.lu_dg, LU, in, tmp, err);
             });
         } else {
             T *out = sel == 0 ? (T *)D.u64 : (T *)D.w;
             const T *dinv = sizeof(T) == 8 ? (const T *)D.dinv64 : (const T *)D.dinv32;
             for_pass_rows<G>(D.ilu_bord, D.ilu_bpass[it.y], [&](int i) {
-                bwd_row<T, G>(i, D.csr_ia, D.csr_ja, D.csr_diag, LU, dinv, tmp, out, err);
+                bwd_row<T, G>(i, D.lu_ia, D.lu_ja, D.lu_dg, LU, dinv, tmp, out, err);
             });
         }
     }
@@ -408,6 +417,13 @@ __global__ void k_ilu_pending(const SysDev *__restrict__ sys, const DChunk *__re
     }
 }
 
+// b[map[k]] = a[k]: the CSR values onto the ILU(p) factor pattern
+__global__ void k_scatter_map(int nnz, const int *__restrict__ map, const double *__restrict__ a, double *__restrict__ b)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nnz) b[map[k]] = a[k];
+}
+
 __global__ void k_f64_to_f32(const double *a, float *b, int n)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -426,17 +442,16 @@ static int warps_grid()
 
 // Level order of the rows for the forward (L) or backward (U) dependency
 // graph and its passes of at most `rows` rows, each inside one level.
-static void ilu_schedule(const CsrTopology &c, bool backward, int rows, std::vector<int> &order,
-                         std::vector<int2> &passes)
+static void ilu_schedule(int n, const std::vector<int> &ia, const std::vector<int> &ja, const std::vector<int> &dg,
+                         bool backward, int rows, std::vector<int> &order, std::vector<int2> &passes)
 {
-    const int n = c.n;
     std::vector<int> lev(n, 0);
     int top = 0;
     for (int t = 0; t < n; ++t) {
         const int i = backward ? n - 1 - t : t;
-        const int k0 = backward ? c.diag[i] + 1 : c.ia[i], k1 = backward ? c.ia[i + 1] : c.diag[i];
+        const int k0 = backward ? dg[i] + 1 : ia[i], k1 = backward ? ia[i + 1] : dg[i];
         int l = 0;
-        for (int k = k0; k < k1; ++k) l = std::max(l, lev[c.ja[k]] + 1);
+        for (int k = k0; k < k1; ++k) l = std::max(l, lev[ja[k]] + 1);
         lev[i] = l;
         top = std::max(top, l);
     }
@@ -456,7 +471,7 @@ static int sweep1(fg_system *s, bool backward, const double *in, double *out, cu
 {
     const int n = s->topo.n;
     int *ctr = s->ilu_ctr.as<int>(), *err = ctr + 4;
-    const int *ia = s->csr_ia.as<int>(), *ja = s->csr_ja.as<int>(), *dg = s->csr_diag.as<int>();
+    const int *ia = s->lu_ia.as<int>(), *ja = s->lu_ja.as<int>(), *dg = s->lu_dg.as<int>();
     const double *LU = s->LU64.as<double>(), *dinv = s->dinv64.as<double>();
     const int *ord = backward ? s->ilu_bord.as<int>() : s->ilu_ford.as<int>();
     const int2 *ps = backward ? s->ilu_bpass.as<int2>() : s->ilu_fpass.as<int2>();
@@ -479,6 +494,121 @@ static int sweep1(fg_system *s, bool backward, const double *in, double *out, cu
     return FG_OK;
 }
 
+// Symbolic ILU(p) (ilup.c:164-301): each row starts from its own entries
+// at level 0; its L part is eliminated leftmost pivot first, and an entry
+// of pivot row k's U part enters the row at level lev(i,k) + lev(k,c) + 1
+// when that is <= p (an entry already there keeps the smaller level).
+// Output rows: L ascending (the elimination order), diagonal, U in
+// admission order.
+static void ilu_fill(int n, const std::vector<int> &ia, const std::vector<int> &ja, int p, std::vector<int> &fia,
+                     std::vector<int> &fja, std::vector<int> &fdg)
+{
+    std::vector<int> slot(n, -1), lc, ll, uc, ul;
+    std::vector<std::vector<int>> urow(n), ulev(n), lrow(n);
+    for (int i = 0; i < n; ++i) {
+        lc.clear(); ll.clear(); uc.clear(); ul.clear();
+        for (int q = ia[i]; q < ia[i + 1]; ++q) {
+            const int c = ja[q];
+            if (c < i) { slot[c] = (int)lc.size(); lc.push_back(c); ll.push_back(0); }
+            else if (c > i) { slot[c] = n + (int)uc.size(); uc.push_back(c); ul.push_back(0); }
+        }
+        for (size_t jp = 0; jp < lc.size(); ++jp) {
+            size_t jm = jp;
+            for (size_t j = jp + 1; j < lc.size(); ++j)
+                if (lc[j] < lc[jm]) jm = j;
+            if (jm != jp) {
+                std::swap(lc[jp], lc[jm]);
+                std::swap(ll[jp], ll[jm]);
+                slot[lc[jp]] = (int)jp;
+                slot[lc[jm]] = (int)jm;
+            }
+            const int k = lc[jp], lk = ll[jp];
+            for (size_t j = 0; j < urow[k].size(); ++j) {
+                const int c = urow[k][j], it = ulev[k][j] + lk + 1;
+                if (it > p) continue;
+                const int sl = slot[c];
+                if (sl == -1) {
+                    if (c < i) { slot[c] = (int)lc.size(); lc.push_back(c); ll.push_back(it); }
+                    else if (c > i) { slot[c] = n + (int)uc.size(); uc.push_back(c); ul.push_back(it); }
+                } else if (sl < n) {
+                    ll[sl] = std::min(ll[sl], it);
+                } else {
+                    ul[sl - n] = std::min(ul[sl - n], it);
+                }
+            }
+        }
+        for (int c : lc) slot[c] = -1;
+        for (int c : uc) slot[c] = -1;
+        lrow[i] = lc;
+        urow[i] = uc;
+        ulev[i] = ul;
+    }
+    fia.assign(n + 1, 0);
+    for (int i = 0; i < n; ++i) fia[i + 1] = fia[i] + (int)(lrow[i].size() + 1 + urow[i].size());
+    fja.resize(fia[n]);
+    fdg.resize(n);
+    for (int i = 0; i < n; ++i) {
+        int b = fia[i];
+        for (int c : lrow[i]) fja[b++] = c;
+        fdg[i] = b;
+        fja[b++] = i;
+        for (int c : urow[i]) fja[b++] = c;
+    }
+}
+
+// The factor pattern of the system's fill level, the slot of every CSR
+// entry in it, the substitution schedules over it and the factor storage.
+int ilu_pattern_setup(fg_system *s)
+{
+    const int n = s->topo.n;
+    std::vector<int> ia(n + 1), ja, dg(n);
+    FG_CUDA(cudaMemcpy(ia.data(), s->csr_ia.p, sizeof(int) * (size_t)(n + 1), cudaMemcpyDeviceToHost));
+    ja.resize(std::max(ia[n], 0));
+    if (!ja.empty()) FG_CUDA(cudaMemcpy(ja.data(), s->csr_ja.p, sizeof(int) * ja.size(), cudaMemcpyDeviceToHost));
+    std::vector<int> fia, fja, fdg, map(ja.size());
+    ilu_fill(n, ia, ja, s->ilu_p, fia, fja, fdg);
+    {
+        std::vector<int> at(n, -1);
+        for (int i = 0; i < n; ++i) {
+            for (int t = fia[i]; t < fia[i + 1]; ++t) at[fja[t]] = t;
+            for (int q = ia[i]; q < ia[i + 1]; ++q) map[q] = at[ja[q]];
+            for (int t = fia[i]; t < fia[i + 1]; ++t) at[fja[t]] = -1;
+        }
+    }
+    auto up = [](DevMem &m, const std::vector<int> &v) -> int {
+        int rr = m.alloc(sizeof(int) * std::max<size_t>(v.size(), 1));
+        if (rr) return rr;
+        if (!v.empty()) return h2d(m.p, v.data(), sizeof(int) * v.size());
+        return FG_OK;
+    };
+    const size_t fnz = (size_t)std::max(fia[n], 1);
+    int r;
+    if ((r = up(s->lu_ia, fia)) || (r = up(s->lu_ja, fja)) || (r = up(s->lu_dg, fdg)) || (r = up(s->lu_map, map)) ||
+        (r = s->AAf64.alloc(8 * fnz)) || (r = s->LU64.alloc(8 * fnz)) || (r = s->LU32.alloc(4 * fnz)))
+        return r;
+    s->lu_nnz = fia[n];
+    // substitution schedule: lanes per row from the longest L or U part
+    int longest = 1;
+    for (int i = 0; i < n; ++i) longest = std::max({longest, fdg[i] - fia[i], fia[i + 1] - fdg[i] - 1});
+    s->ilu_g = longest <= 4 ? 4 : longest <= 8 ? 8 : longest <= 16 ? 16 : 32;
+    std::vector<int> fo, bo;
+    std::vector<int2> fp, bp;
+    ilu_schedule(n, fia, fja, fdg, false, 32 / s->ilu_g, fo, fp);
+    ilu_schedule(n, fia, fja, fdg, true, 32 / s->ilu_g, bo, bp);
+    auto up2 = [](DevMem &m, const std::vector<int2> &v) -> int {
+        int rr = m.alloc(sizeof(int2) * std::max<size_t>(v.size(), 1));
+        if (rr) return rr;
+        if (!v.empty()) return h2d(m.p, v.data(), sizeof(int2) * v.size());
+        return FG_OK;
+    };
+    if ((r = up(s->ilu_ford, fo)) || (r = up(s->ilu_bord, bo)) || (r = up2(s->ilu_fpass, fp)) ||
+        (r = up2(s->ilu_bpass, bp)))
+        return r;
+    s->ilu_nfpass = (int)fp.size();
+    s->ilu_nbpass = (int)bp.size();
+    return FG_OK;
+}
+
 int csr_setup(fg_system *s)
 {
     if (s->csr_ok) return FG_OK;
@@ -494,32 +624,11 @@ int csr_setup(fg_system *s)
     size_t nz = (size_t)std::max(c.nnz, 1), n1 = (size_t)c.n + 1;
     if ((r = up(s->csr_ia, c.ia)) || (r = up(s->csr_ja, c.ja)) || (r = up(s->csr_diag, c.diag)) ||
         (r = up(s->csr_inc_ptr, c.inc_ptr)) || (r = up(s->csr_inc, c.inc)) || (r = s->AA64.alloc(8 * nz)) ||
-        (r = s->AA32.alloc(4 * nz)) || (r = s->LU64.alloc(8 * nz)) || (r = s->LU32.alloc(4 * nz)) ||
-        (r = s->dinv64.alloc(8 * n1)) || (r = s->dinv32.alloc(4 * n1)) || (r = s->ilu_flags.alloc(4 * n1)) ||
+        (r = s->AA32.alloc(4 * nz)) || (r = s->dinv64.alloc(8 * n1)) || (r = s->dinv32.alloc(4 * n1)) || (r = s->ilu_flags.alloc(4 * n1)) ||
         (r = s->ilu_ctr.alloc(64)) || (r = s->ilu_tmp.alloc(8 * (size_t)std::max(s->n_pad, 1))))
         return r;
     s->csr_nnz = c.nnz;
-    // substitution schedule: lanes per row from the longest L or U part
-    int longest = 1;
-    for (int i = 0; i < c.n; ++i) longest = std::max({longest, c.diag[i] - c.ia[i], c.ia[i + 1] - c.diag[i] - 1});
-    s->ilu_g = longest <= 4 ? 4 : longest <= 8 ? 8 : longest <= 16 ? 16 : 32;
-    {
-        std::vector<int> fo, bo;
-        std::vector<int2> fp, bp;
-        ilu_schedule(c, false, 32 / s->ilu_g, fo, fp);
-        ilu_schedule(c, true, 32 / s->ilu_g, bo, bp);
-        auto up2 = [](DevMem &m, const std::vector<int2> &v) -> int {
-            int rr = m.alloc(sizeof(int2) * std::max<size_t>(v.size(), 1));
-            if (rr) return rr;
-            if (!v.empty()) return h2d(m.p, v.data(), sizeof(int2) * v.size());
-            return FG_OK;
-        };
-        if ((r = up(s->ilu_ford, fo)) || (r = up(s->ilu_bord, bo)) || (r = up2(s->ilu_fpass, fp)) ||
-            (r = up2(s->ilu_bpass, bp)))
-            return r;
-        s->ilu_nfpass = (int)fp.size();
-        s->ilu_nbpass = (int)bp.size();
-    }
+    if ((r = ilu_pattern_setup(s))) return r;
     double avg = c.n ? (double)c.nnz / c.n : 1.0;
     s->csr_w = avg <= 8 ? 4 : avg <= 16 ? 8 : 32;
     s->csr_ok = true;
@@ -553,17 +662,22 @@ int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st)
     int *flag = s->ilu_flags.as<int>(), *ctr = s->ilu_ctr.as<int>(), *err = ctr + 4;
     FG_CUDA(cudaMemsetAsync(s->ilu_ctr.p, 0, s->ilu_ctr.bytes, st));
     FG_CUDA(cudaMemsetAsync(flag, 0, 4 * (size_t)(n + 1), st));
+    // the matrix values on the factor pattern (fill slots start at 0)
+    FG_CUDA(cudaMemsetAsync(s->AAf64.p, 0, s->AAf64.bytes, st));
+    if (s->csr_nnz > 0)
+        k_scatter_map<<<(s->csr_nnz + 255) / 256, 256, 0, st>>>(s->csr_nnz, s->lu_map.as<int>(), s->AA64.as<double>(),
+                                                               s->AAf64.as<double>());
     if (n > 0)
-        k_ilu0_factor<<<8 * sm_count(), 32 * kFacWarps, 0, st>>>(n, s->ilu_ford.as<int>(), s->csr_ia.as<int>(),
-                                                                 s->csr_ja.as<int>(), s->csr_diag.as<int>(),
-                                                                 s->AA64.as<double>(), s->LU64.as<double>(),
+        k_ilu0_factor<<<8 * sm_count(), 32 * kFacWarps, 0, st>>>(n, s->ilu_ford.as<int>(), s->lu_ia.as<int>(),
+                                                                 s->lu_ja.as<int>(), s->lu_dg.as<int>(),
+                                                                 s->AAf64.as<double>(), s->LU64.as<double>(),
                                                                  s->dinv64.as<double>(), flag, ctr, err);
     FG_CUDA(cudaGetLastError());
-    k_f64_to_f32<<<(std::max(s->csr_nnz, 1) + 255) / 256, 256, 0, st>>>(s->LU64.as<double>(), s->LU32.as<float>(),
-                                                                       s->csr_nnz);
+    k_f64_to_f32<<<(std::max(s->lu_nnz, 1) + 255) / 256, 256, 0, st>>>(s->LU64.as<double>(), s->LU32.as<float>(),
+                                                                      s->lu_nnz);
     k_f64_to_f32<<<(n + 256) / 256, 256, 0, st>>>(s->dinv64.as<double>(), s->dinv32.as<float>(), n);
     FG_CUDA(cudaGetLastError());
-    count_launches(3);
+    count_launches(4);
     if (F_dev && n > 0) {
         double *tmp = s->ilu_tmp.as<double>();
         int r2;
@@ -572,8 +686,8 @@ int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st)
     int herr = 0;
     FG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
-    if (herr == FG_ERR_TIMEOUT) { set_error("ILU(0): a row dependency wait ran out"); return FG_ERR_TIMEOUT; }
-    if (herr == FG_ERR_BREAKDOWN) { set_error("ILU(0): zero pivot"); return FG_ERR_BREAKDOWN; }
+    if (herr == FG_ERR_TIMEOUT) { set_error("ILU(p): a row dependency wait ran out"); return FG_ERR_TIMEOUT; }
+    if (herr == FG_ERR_BREAKDOWN) { set_error("ILU(p): zero pivot"); return FG_ERR_BREAKDOWN; }
     s->precond = FG_PRECOND_ILU0;
     return FG_OK;
 }

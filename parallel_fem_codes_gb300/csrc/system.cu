@@ -82,7 +82,7 @@ size_t fg_system::bytes() const
     const DevMem *all[] = {&lm, &A64, &A32, &dinc_ptr, &dinc, &ninc_ptr, &ninc, &node_dof, &eorder, &perm,
                            &lm16, &pt_elem, &pt_dof, &pt_col, &pdofs, &pt_inc, &incl, &rhs_f, &rhs_b,
                            &csr_ia, &csr_ja, &csr_diag, &csr_inc_ptr, &csr_inc, &AA64, &AA32, &LU64, &LU32,
-                           &dinv64, &dinv32, &ilu_flags, &ilu_ctr, &ilu_tmp, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
+                           &dinv64, &dinv32, &lu_ia, &lu_ja, &lu_dg, &lu_map, &AAf64, &ilu_flags, &ilu_ctr, &ilu_tmp, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
                            &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
                            &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &state_u1, &state_u2, &shock_state, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
@@ -514,6 +514,16 @@ int fg_set_spike(fg_system *s, int k, int parts)
         if (s->precond == FG_PRECOND_SPIKE) s->precond = FG_PRECOND_NONE;   // set up again
     }
     return FG_OK;
+}
+
+int fg_set_ilu_fill(fg_system *s, int p)
+{
+    if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (p < 0 || p > 16) { set_error("ILU fill level must be in [0, 16]"); return FG_ERR_ARG; }
+    if (p == s->ilu_p) return FG_OK;
+    s->ilu_p = p;
+    if (s->precond == FG_PRECOND_ILU0) s->precond = FG_PRECOND_NONE;   // set up again
+    return s->csr_ok ? ilu_pattern_setup(s) : FG_OK;
 }
 
 int fg_get_csr(const fg_system *s, int *nnz, int *IA, int *JA, double *AA)

@@ -61,6 +61,10 @@ struct fg_system {
     // passes; ilu_g lanes per row
     int ilu_g = 32, ilu_nfpass = 0, ilu_nbpass = 0;
     fg::DevMem ilu_ford, ilu_bord, ilu_fpass, ilu_bpass;
+    // ILU(p) factor pattern (per row: L ascending, diagonal, U in the order
+    // the symbolic pass admits it) and the slot of every CSR entry in it
+    int ilu_p = 0, lu_nnz = 0;
+    fg::DevMem lu_ia, lu_ja, lu_dg, lu_map, AAf64;
     fg::DevMem csr_ia, csr_ja, csr_diag, csr_inc_ptr, csr_inc, AA64, AA32, LU64, LU32, dinv64, dinv32, ilu_flags,
         ilu_ctr, ilu_tmp;   // ilu_tmp: output of the forward substitution (n_pad doubles)
     // truncated SPIKE over row blocks of the CSR operator
@@ -83,6 +87,7 @@ int h2d(void *dst, const void *src, size_t bytes);
 
 // CSR / ILU(0) (ilu.cu)
 int csr_setup(fg_system *s);
+int ilu_pattern_setup(fg_system *s);   // ILU(p) factor pattern and schedules (after csr_setup)
 int csr_refresh(fg_system *s, cudaStream_t st);
 int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st);
 int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st);
@@ -114,6 +119,9 @@ inline void set_patch_fields(SysDev &D, const fg_system *s)
     D.AA32 = s->AA32.as<float>();
     D.LU64 = s->LU64.as<double>();
     D.LU32 = s->LU32.as<float>();
+    D.lu_ia = s->lu_ia.as<int>();
+    D.lu_ja = s->lu_ja.as<int>();
+    D.lu_dg = s->lu_dg.as<int>();
     D.dinv64 = s->dinv64.as<double>();
     D.dinv32 = s->dinv32.as<float>();
     D.ilu_tmp = s->ilu_tmp.p;

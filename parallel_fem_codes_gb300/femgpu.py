@@ -156,6 +156,7 @@ def lib(build_if_missing: bool = True):
     L.fg_launch_count.restype = ctypes.c_longlong
     L.fg_set_operator.argtypes = [_vp, _c_int]
     L.fg_set_spike.argtypes = [_vp, _c_int, _c_int]
+    L.fg_set_ilu_fill.argtypes = [_vp, _c_int]
     L.fg_get_csr.argtypes = [_vp, ctypes.POINTER(_c_int), _vp, _vp, _vp]
     L.fg_system_stream.argtypes = [_vp]
     L.fg_system_stream.restype = _vp
@@ -361,6 +362,10 @@ class System:
     def set_spike(self, k=16, parts=16):
         """Coupling size and block count of the SPIKE preconditioner."""
         check(lib().fg_set_spike(self._h, int(k), int(parts)))
+
+    def set_ilu_fill(self, p):
+        """Fill level of FG_PRECOND_ILU0 (Preconditioner "ILU<p>")."""
+        check(lib().fg_set_ilu_fill(self._h, int(p)))
 
     def csr(self):
         """(IA, JA, AA) of the assembled operator in the internal (RCM) numbering."""

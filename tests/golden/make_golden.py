@@ -20,7 +20,9 @@ cases; and tests/golden/dd_sst.npz: the steady transport driver's
 Build_K_F_DD with CAUDD and with CAU (blocks and F at a state u) and its
 Process loop on the transport cases; and tests/golden/shock_sst.npz: the
 YZBeta shock capture and the h_shock Option1 / Option2 lengths with both
-forms (blocks and F at a state u, the Process loop).
+forms (blocks and F at a state u, the Process loop); and
+tests/golden/ilup_sst.npz: the reference's ILU(p) ("ILU1", "ILU2", "ILU3")
+applied to a vector, with the CSR matrix it factorises.
 """
 import os
 import sys
@@ -183,6 +185,22 @@ def write_sst_shock():
     np.savez_compressed(os.path.join(HERE, "shock_sst.npz"), **out)
 
 
+def write_ilup():
+    out = {}
+    for n, ang, k in [(13, 30.0, 1e-3), (17, 200.0, 1e-2)]:
+        p = G.transport_problem(n, angle_deg=ang, k=k)
+        A, F = O.build_k_f_supg(p)
+        P = np.random.Generator(np.random.PCG64(n)).standard_normal(p.mesh.neq + 1)
+        P[-1] = 0.0
+        for lev in (1, 2, 3):
+            IA, JA, AA, invp, Q, z = O.ref_csr(p, A, P, ilu_p=lev)
+            key = f"n{n}_p{lev}"
+            out[key + "_IA"], out[key + "_JA"], out[key + "_AA"] = IA, JA, AA
+            out[key + "_P"], out[key + "_z"] = P, z[: p.mesh.neq]
+            print(key, "nnz", len(JA))
+    np.savez_compressed(os.path.join(HERE, "ilup_sst.npz"), **out)
+
+
 if __name__ == "__main__":
     main()
     write_euler()
@@ -190,3 +208,4 @@ if __name__ == "__main__":
     write_ns_vms()
     write_sst_dd()
     write_sst_shock()
+    write_ilup()

@@ -97,3 +97,33 @@ def test_gmres_ilu0(fg, precision):
     if precision == 32:
         assert res <= 1e-10
     assert rel(r.x[:-1], X0[:-1]) <= 1e-8
+
+
+@pytest.mark.parametrize("lev", [1, 2])
+def test_ilup_setup_bit_exact(fg, lev):
+    """ILU(p) (Preconditioner "ILU<p>"): the device factor pattern,
+    factorisation and substitutions against the oracle (pinned to the
+    reference's ILUp)."""
+    p, m, A, F, perm, inv, IA, JA, AA, lm, s = _setup(fg, 33)
+    FIA, FJA, FDG, LU, D = O.ilup(IA, JA, AA, lev)
+    s.set_ilu_fill(lev)
+    Fp = s.precond_setup(fg.FG_PRECOND_ILU0, 0, F)
+    Fi = np.append(F[:-1][perm[:-1]], 0.0)
+    zi = O.ilup_apply(FIA, FJA, FDG, LU, D, Fi)
+    z = np.zeros(m.neq + 1)
+    z[perm[:-1]] = zi
+    assert np.array_equal(Fp[:-1], z[:-1])
+
+
+def test_gmres_ilup_fewer_iterations(fg):
+    p, m, A, F, perm, inv, IA, JA, AA, lm, s = _setup(fg, 65, angle=30.0, k=1e-6)
+    its = []
+    for lev in (0, 2):
+        s.set_ilu_fill(lev)
+        Fp = s.precond_setup(fg.FG_PRECOND_ILU0, 0, F)
+        r = s.solve(Fp, tol=1e-10, F_true=F, precision=64)
+        assert r.stats["converged"] == 1
+        res = np.linalg.norm(F[:-1] - O.ebemv3_perm(lm, A, perm, inv, r.x)[:-1]) / np.linalg.norm(F[:-1])
+        assert res <= 1e-9
+        its.append(r.stats["iterations"])
+    assert its[1] <= its[0]

@@ -1,5 +1,6 @@
 """The oracle's CSR path and ILU(0) against the reference's own
 csr_Initialization, csr_assembly, csrmv and ILUp (bit-exact)."""
+import os
 import numpy as np
 import pytest
 
@@ -28,3 +29,28 @@ def test_csr_and_ilu0_match_reference(n, angle, k):
     rc, LU, D = O.ilu0(IA, JA, AA)
     assert rc == 0
     assert np.array_equal(O.ilu0_apply(IA, JA, LU, D, P)[:-1], z_r[:-1])
+
+
+ILUP = os.path.join(os.path.dirname(__file__), "golden", "ilup_sst.npz")
+
+
+@pytest.mark.parametrize("key", ["n13_p1", "n13_p2", "n13_p3", "n17_p1", "n17_p2", "n17_p3"])
+def test_ilup_bit_exact(key, oracle_lib):
+    """ILU(p) (level-of-fill symbolic pass, numeric factorisation and the
+    substitutions) against the reference's "ILU<p>" applied to a vector."""
+    d = np.load(ILUP)
+    p = int(key.split("_p")[1])
+    FIA, FJA, FDG, LU, D = O.ilup(d[key + "_IA"], d[key + "_JA"], d[key + "_AA"], p)
+    x = O.ilup_apply(FIA, FJA, FDG, LU, D, d[key + "_P"])
+    assert np.array_equal(x, d[key + "_z"])
+    assert FIA[-1] > len(d[key + "_JA"])          # fill entered
+
+
+def test_ilup_level0_is_ilu0(oracle_lib):
+    d = np.load(ILUP)
+    IA, JA, AA = d["n13_p1_IA"], d["n13_p1_JA"], d["n13_p1_AA"]
+    FIA, FJA, FDG, LU, D = O.ilup(IA, JA, AA, 0)
+    rc, LU0, D0 = O.ilu0(IA, JA, AA)
+    y = d["n13_p1_P"]
+    assert np.array_equal(FIA, IA) and np.array_equal(FJA, JA)
+    assert np.array_equal(O.ilup_apply(FIA, FJA, FDG, LU, D, y), O.ilu0_apply(IA, JA, LU0, D0, y)[: len(IA) - 1])
