@@ -431,7 +431,11 @@ int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_o
  * ndof = 1 and the geometry of fg_set_geometry: the blocks become
  * Ae = me + alpha dt ke (SUPG mass and the steady operator of
  * fg_transport_assemble), R = F - me du - ke u, accumulated in the
- * reference's element order (bit-identical). */
+ * reference's element order (bit-identical).  With c.form = FG_TRANSPORT_DD
+ * (StabilizationForm "DD", Predictor1) the build is Build_M_K_R_DD.c:5-190:
+ * the bubble condensed into me, ke and the load, and c.cau = FG_SHOCK_CAUDD
+ * the transient CAUDD relaxed against each element's previous value (state
+ * on the device, zeroed when fg_tt_predictor starts). */
 typedef struct {
     fg_transport_coeffs c;  /* conductivity, reaction, velocity, source, CAU */
     double alpha;           /* Alpha (Alpha_Build)                          */

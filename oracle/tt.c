@@ -12,6 +12,13 @@
  * element formulas are the reference's, term for term, so blocks and
  * residual agree to the last bit when both are compiled without
  * floating-point contraction.
+ *
+ * StabilizationForm "DD" with TimeIntegration "Predictor1"
+ * (setStabilizationForm.c:40-74): Build_M_K_R_DD.c:5-190 with the transient
+ * CAU_DD_ShockCapture.c (Ru includes du/dt) relaxed against the element's
+ * previous value, cb = (cbtil + cbtil_old) / 2 (the state, delta_old, lives
+ * for the whole time loop), the bubble condensed into the mass and
+ * stiffness blocks and the load as in the steady DD build.
  */
 #include "femoracle.h"
 #include <math.h>
@@ -41,6 +48,76 @@ static double tt_cau(double kx, double ky, double bx, double by, double gamma, d
     return 0;
 }
 
+/* Build_M_K_R_DD.c:61-180 for one element: Ae (row-major), the load term
+ * Fr[i] added to R[lm[i]] and the three terms sub[i][j] then subtracted. */
+static void tt_dd_element(double kx, double ky, double bx, double by, double gamma, double fv, const double X[3],
+                          const double Y[3], const double ue[3], const double due[3], double alpha, double dt,
+                          int shock, double *cbtilo, int e, double Ae[9], double Fr[3], double sub[3][3])
+{
+    const double third = 1.0/3.0, sixth = 1.0/6.0, seventh = 1.0/7.0, twelfth = 1.0/12.0;
+    const double t320 = 3./20.0, n920 = 9./20.0, n940 = 9./40.0, w = 0.5;
+    double y23 = Y[1] - Y[2], y31 = Y[2] - Y[0], y12 = Y[0] - Y[1];
+    double x32 = X[2] - X[1], x13 = X[0] - X[2], x21 = X[1] - X[0];
+    double TwoA = x21*y31 - x13*y12;
+    double Area = 0.5*TwoA;
+    double invArea = 1.0/Area;
+    double fe1 = fv, fe2 = fv, fe3 = fv;
+    double feb = third*(fe1 + fe2 + fe3);
+    double ueb = third*(ue[0] + ue[1] + ue[2]);
+    double dueb = third*(due[0] + due[1] + due[2]);
+    double Mhh = twelfth*Area, MBh = t320*Area;
+    double a1 = bx*y23 + by*x32, a2 = bx*y31 + by*x13, a3 = bx*y12 + by*x21;
+    double C12 = y23*y31 + x32*x13, C13 = y23*y12 + x32*x21, C23 = y31*y12 + x13*x21;
+    double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+    double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+    double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+    double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
+    double Eu = 0.0;
+    if (shock == 2) {           /* CAU_DD_ShockCapture with du/dt, h_shock_2sqrtArea, relaxed */
+        double h = sqrt(fabs(2*Area));
+        double bgu = 0.5*invArea*(ue[0]*(bx*y23 + by*x32) + ue[1]*(bx*y31 + by*x13) + ue[2]*(bx*y12 + by*x21));
+        double Ru = dueb + bgu + gamma*ueb - feb;
+        double gx = 0.5*invArea*(y23*ue[0] + y31*ue[1] + y12*ue[2]);
+        double gy = 0.5*invArea*(x32*ue[0] + x13*ue[1] + x21*ue[2]);
+        double ng = sqrt(gx*gx + gy*gy);
+        double cbtil = ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0;
+        double cb = w*cbtil + (1 - w)*cbtilo[e];
+        cbtilo[e] = cbtil;
+        Eu = cb;
+    }
+    double K12 = 0.25*Eu*invArea*C12, K13 = 0.25*Eu*invArea*C13, K23 = 0.25*Eu*invArea*C23;
+    double Khh[3][3];
+    Khh[0][0] = -(D12 + D13) + sixth*a1 + R11 -(K12 + K13);
+    Khh[0][1] =          D12 + sixth*a2 + R12 + K12;
+    Khh[0][2] =          D13 + sixth*a3 + R12 + K13;
+    Khh[1][0] =          D12 + sixth*a1 + R12 + K12;
+    Khh[1][1] = -(D12 + D23) + sixth*a2 + R11 -(K12 + K23);
+    Khh[1][2] =          D23 + sixth*a3 + R12 + K23;
+    Khh[2][0] =          D13 + sixth*a1 + R12 + K13;
+    Khh[2][1] =          D23 + sixth*a2 + R12 + K23;
+    Khh[2][2] = -(D13 + D23) + sixth*a3 + R11 -(K13 + K23);
+    double KhB[3] = { n920*(0.5*a1 + a2 + a3) + t320*gamma*Area, n920*(a1 + 0.5*a2 + a3) + t320*gamma*Area,
+                      n920*(a1 + a2 + 0.5*a3) + t320*gamma*Area };
+    double KBh[3] = { n940*a1 + t320*gamma*Area, n940*a2 + t320*gamma*Area, n940*a3 + t320*gamma*Area };
+    double KBB = -9*n940*(D12 + D13 + D23) + seventh*t320*(a1 + a2 + a3) + 9*seventh*n940*Area
+               - Eu*invArea*(C12 + C13 + C23)/360.;
+    double invKBB = 1.0/KBB;
+    double Fh[3] = { twelfth*Area*(2*fe1 + fe2 + fe3), twelfth*Area*(fe1 + 2*fe2 + fe3),
+                     twelfth*Area*(fe1 + fe2 + 2*fe3) };
+    double FB = t320*Area*(fe1 + fe2 + fe3);
+    for (int i = 0; i < 3; i++) {
+        double me[3];
+        for (int j = 0; j < 3; j++) me[j] = Mhh - invKBB*KhB[i]*MBh;
+        me[i] += Mhh;
+        Fr[i] = Fh[i] - invKBB*KhB[i]*FB;
+        for (int j = 0; j < 3; j++) {
+            double ke = Khh[i][j] - invKBB*KhB[i]*KBh[j];
+            Ae[3*i + j] = me[j] + alpha*dt*ke;
+            sub[i][j] = me[j]*due[j] + ke*ue[j];
+        }
+    }
+}
+
 void or_build_tt(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
                  const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
                  const double *u, const double *du, double *A, double *R)
@@ -55,8 +132,26 @@ void or_build_tt(int nnodes, int nel, const double *x, const double *y, const in
         U[J] = type[J] == 0 ? prob->upresc[J] : u[invp[J]];
         dU[J] = type[J] == 0 ? 0.0 : du[invp[J]];
     }
+    double *cbtilo = prob->delta_old, *own = NULL;    /* DD: the time loop's delta_old */
+    if (prob->form == 1 && !cbtilo) cbtilo = own = calloc((size_t)(nel ? nel : 1), sizeof(double));
     for (E = 0; E < nel; E++) {
         int J1 = ien[3*E], J2 = ien[3*E+1], J3 = ien[3*E+2];
+        if (prob->form == 1) {
+            const double Xv[3] = { x[J1], x[J2], x[J3] }, Yv[3] = { y[J1], y[J2], y[J3] };
+            const double uv[3] = { U[J1], U[J2], U[J3] }, dv[3] = { dU[J1], dU[J2], dU[J3] };
+            double Ae[9], Fr[3], sub[3][3];
+            tt_dd_element(kx, ky, prob->beta[0], prob->beta[1], gamma, prob->f, Xv, Yv, uv, dv, alpha, dt,
+                          prob->cau, cbtilo, E, Ae, Fr, sub);
+            const int lm[3] = { type[J1] == 0 ? neq : invp[J1], type[J2] == 0 ? neq : invp[J2],
+                                type[J3] == 0 ? neq : invp[J3] };
+            for (int i = 0; i < 3; i++) {            /* Build_M_K_R_DD.c:161-176 */
+                R[lm[i]] += Fr[i];
+                for (int j = 0; j < 3; j++) R[lm[i]] -= sub[i][j];
+            }
+            R[neq] = 0;
+            memcpy(A + 9L * E, Ae, sizeof Ae);
+            continue;
+        }
         double X0 = x[J1], X1 = x[J2], X2 = x[J3];
         double Y0 = y[J1], Y1 = y[J2], Y2 = y[J3];
         double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
@@ -129,6 +224,7 @@ void or_build_tt(int nnodes, int nel, const double *x, const double *y, const in
     }
     free(U);
     free(dU);
+    free(own);
 }
 
 typedef struct {
@@ -188,9 +284,13 @@ int or_tt_predictor(int nnodes, int nel, const double *x, const double *y, const
     double *Diag = calloc((size_t)NEQ + 1, sizeof(double)), *invDiag = calloc((size_t)NEQ + 1, sizeof(double));
     or_fill_lm(nel, 1, ien, type, invp, NEQ, lm);
     or_permutation_of_lm(nel, ien, type, invp, NEQ, Perm, invPerm, NULL);
-    tt_loop c = { { nel, NEQ, lm, Perm, invPerm, A, invDiag }, nnodes, nel, neq, x, y, type, invp, ien, prob, R,
+    /* the DD shock-capture state lives for the whole loop (Predictor_Old.c:30) */
+    or_transport_problem pl = *prob;
+    double *state = calloc((size_t)(nel ? nel : 1), sizeof(double));
+    pl.delta_old = state;
+    tt_loop c = { { nel, NEQ, lm, Perm, invPerm, A, invDiag }, nnodes, nel, neq, x, y, type, invp, ien, &pl, R,
                   Diag, solver_tol, kmax, lmax };
     int steps = or_time_integrate(neq, alpha, dt, to, tt_correct, &c, u, a, st);
-    free(lm); free(Perm); free(invPerm); free(A); free(R); free(Diag); free(invDiag);
+    free(lm); free(Perm); free(invPerm); free(A); free(R); free(Diag); free(invDiag); free(state);
     return steps;
 }

@@ -723,6 +723,102 @@ __global__ void k_tt_elem(int nel, int ld, const int *__restrict__ gien, const d
     }
 }
 
+// Build_M_K_R_DD.c:61-180 (StabilizationForm "DD", Predictor1): the steady
+// DD element (bubble condensed into the block and the load) with its mass
+// block me = Mhh - KhB MBh / KBB (+ Mhh on the diagonal), Ae = me + alpha dt
+// ke, and the transient CAUDD (Ru with du/dt) relaxed against the element's
+// previous value, cb = (cbtil + cbtil_old) / 2, cbtil_old in cbtilo (per
+// element, internal order, kept for the whole time loop).  Same residual
+// slots as k_tt_elem.
+__global__ void k_tt_dd_elem(int nel, int ld, const int *__restrict__ gien, const double *__restrict__ gx,
+                             const double *__restrict__ gy, const int *__restrict__ gtype,
+                             const int *__restrict__ node_dof, const double *__restrict__ up,
+                             const double *__restrict__ u, const double *__restrict__ du, fg_tt_coeffs tc,
+                             double *cbtilo, double *__restrict__ A64, double *__restrict__ Rt)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const fg_transport_coeffs &cf = tc.c;
+    const double third = 1.0/3.0, sixth = 1.0/6.0, seventh = 1.0/7.0, twelfth = 1.0/12.0;
+    const double t320 = 3./20.0, n920 = 9./20.0, n940 = 9./40.0, w = 0.5;
+    const double kx = cf.k, ky = cf.k, gamma = cf.gamma, bx = cf.beta[0], by = cf.beta[1];
+    int J1 = gien[pos], J2 = gien[ld + pos], J3 = gien[2 * (size_t)ld + pos];
+    double X0 = gx[J1], X1 = gx[J2], X2 = gx[J3];
+    double Y0 = gy[J1], Y1 = gy[J2], Y2 = gy[J3];
+    double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+    double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+    double TwoA = x21*y31 - x13*y12;
+    double Area = 0.5*TwoA;
+    double invArea = 1.0/Area;
+    double fe1 = cf.f, fe2 = cf.f, fe3 = cf.f;
+    double feb = third*(fe1 + fe2 + fe3);
+    const int J[3] = {J1, J2, J3};
+    double ue[3], due[3];
+    for (int a = 0; a < 3; ++a) {
+        const bool fixed = gtype[J[a]] == 0;
+        ue[a] = fixed ? up[J[a]] : u[node_dof[J[a]]];
+        due[a] = fixed ? 0.0 : du[node_dof[J[a]]];
+    }
+    double ueb = third*(ue[0] + ue[1] + ue[2]);
+    double dueb = third*(due[0] + due[1] + due[2]);
+    double Mhh = twelfth*Area, MBh = t320*Area;
+    double a1 = bx*y23 + by*x32, a2 = bx*y31 + by*x13, a3 = bx*y12 + by*x21;
+    double C12 = y23*y31 + x32*x13, C13 = y23*y12 + x32*x21, C23 = y31*y12 + x13*x21;
+    double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+    double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+    double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+    double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
+    double Eu = 0.0;
+    if (cf.cau == FG_SHOCK_CAUDD) {
+        double h = sqrt(fabs(2*Area));
+        double bgu = 0.5*invArea*(ue[0]*(bx*y23 + by*x32) + ue[1]*(bx*y31 + by*x13) + ue[2]*(bx*y12 + by*x21));
+        double Ru = dueb + bgu + gamma*ueb - feb;
+        double gxu = 0.5*invArea*(y23*ue[0] + y31*ue[1] + y12*ue[2]);
+        double gyu = 0.5*invArea*(x32*ue[0] + x13*ue[1] + x21*ue[2]);
+        double ng = sqrt(gxu*gxu + gyu*gyu);
+        double cbtil = ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0.0;
+        double cb = w*cbtil + (1 - w)*cbtilo[pos];
+        cbtilo[pos] = cbtil;
+        Eu = cb;
+    }
+    double K12 = 0.25*Eu*invArea*C12, K13 = 0.25*Eu*invArea*C13, K23 = 0.25*Eu*invArea*C23;
+    double Khh[9];
+    Khh[0] = -(D12 + D13) + sixth*a1 + R11 -(K12 + K13);
+    Khh[1] =          D12 + sixth*a2 + R12 + K12;
+    Khh[2] =          D13 + sixth*a3 + R12 + K13;
+    Khh[3] =          D12 + sixth*a1 + R12 + K12;
+    Khh[4] = -(D12 + D23) + sixth*a2 + R11 -(K12 + K23);
+    Khh[5] =          D23 + sixth*a3 + R12 + K23;
+    Khh[6] =          D13 + sixth*a1 + R12 + K13;
+    Khh[7] =          D23 + sixth*a2 + R12 + K23;
+    Khh[8] = -(D13 + D23) + sixth*a3 + R11 -(K13 + K23);
+    const double KhB[3] = {n920*(0.5*a1 + a2 + a3) + t320*gamma*Area, n920*(a1 + 0.5*a2 + a3) + t320*gamma*Area,
+                           n920*(a1 + a2 + 0.5*a3) + t320*gamma*Area};
+    const double KBh[3] = {n940*a1 + t320*gamma*Area, n940*a2 + t320*gamma*Area, n940*a3 + t320*gamma*Area};
+    double KBB = -9*n940*(D12 + D13 + D23) + seventh*t320*(a1 + a2 + a3) + 9*seventh*n940*Area
+               - Eu*invArea*(C12 + C13 + C23)/360.;
+    double invKBB = 1.0/KBB;
+    const double Fh[3] = {twelfth*Area*(2*fe1 + fe2 + fe3), twelfth*Area*(fe1 + 2*fe2 + fe3),
+                          twelfth*Area*(fe1 + fe2 + 2*fe3)};
+    double FB = t320*Area*(fe1 + fe2 + fe3);
+    const double adt = tc.alpha*tc.dt;
+    double *A = A64 + pos;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        double me[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) me[j] = Mhh - invKBB*KhB[i]*MBh;
+        me[i] += Mhh;
+        Rt[(size_t)(4 * i) * ld + pos] = Fh[i] - invKBB*KhB[i]*FB;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const double ke = Khh[3 * i + j] - invKBB*KhB[i]*KBh[j];
+            A[(size_t)(3 * i + j) * ld] = me[j] + adt*ke;
+            Rt[(size_t)(4 * i + 1 + j) * ld + pos] = me[j]*due[j] + ke*ue[j];
+        }
+    }
+}
+
 // R[d]: the element terms of dof d in reference element order, applied as
 // the reference applies them (R += Fe, then three subtractions); R[n] = 0.
 __global__ void k_tt_R(int n, int ld, const int *__restrict__ dptr, const int *__restrict__ dinc,
@@ -748,14 +844,28 @@ int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev,
     const Topology &t = s->topo;
     if (t.ndof != 1) { set_error("transient transport assembly needs ndof == 1"); return FG_ERR_UNSUPPORTED; }
     if (!s->geometry_ok) { set_error("transient transport assembly before fg_set_geometry"); return FG_ERR_STATE; }
-    if (c->c.form != FG_TRANSPORT_SUPG || c->c.cau < FG_SHOCK_NONE || c->c.cau > FG_SHOCK_CAU ||
-        c->c.h_shock != FG_HSHOCK_2SQRTAREA) {
-        set_error("transient transport builds the SUPG form with CAU (h_shock 2sqrtArea) or no shock capture");
+    const bool dd = c->c.form == FG_TRANSPORT_DD;
+    if (c->c.h_shock != FG_HSHOCK_2SQRTAREA ||
+        (dd ? (c->c.cau != FG_SHOCK_NONE && c->c.cau != FG_SHOCK_CAUDD)
+            : (c->c.form != FG_TRANSPORT_SUPG || c->c.cau < FG_SHOCK_NONE || c->c.cau > FG_SHOCK_CAU))) {
+        set_error("transient transport builds SUPG with CAU or none, or DD with CAUDD or none (h_shock 2sqrtArea)");
         return FG_ERR_UNSUPPORTED;
+    }
+    double *cbtilo = nullptr;
+    if (dd && c->c.cau == FG_SHOCK_CAUDD) {   // delta_old of the time loop, zero at its start
+        int r0;
+        if (s->shock_state.bytes < 16 * (size_t)s->nel_pad && (r0 = s->shock_state.alloc(16 * (size_t)s->nel_pad)))
+            return r0;
+        cbtilo = s->shock_state.as<double>() + s->nel_pad;
     }
     int r;
     if (s->Fe.bytes < 8 * (size_t)12 * s->nel_pad && (r = s->Fe.alloc(8 * (size_t)12 * s->nel_pad))) return r;
-    if (t.nel > 0)
+    if (t.nel > 0 && dd)
+        k_tt_dd_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(), s->gx.as<double>(),
+                                                         s->gy.as<double>(), s->gtype.as<int>(),
+                                                         s->node_dof.as<int>(), s->gup.as<double>(), u_dev, du_dev, *c,
+                                                         cbtilo, s->A64.as<double>(), s->Fe.as<double>());
+    else if (t.nel > 0)
         k_tt_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(), s->gx.as<double>(),
                                                       s->gy.as<double>(), s->gtype.as<int>(), s->node_dof.as<int>(),
                                                       s->gup.as<double>(), u_dev, du_dev, *c, s->A64.as<double>(),

@@ -984,6 +984,8 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
                     double *a, fg_time_stats *stats)
 {
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
+    // the DD shock-capture state starts at zero with the loop (Predictor_Old.c:30 callocs delta_old)
+    if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
     return time_loop(s, c->dt, c->alpha,
                      [&](double ab, double db, const double *du, const double *da, double *R) {
                          fg_tt_coeffs cc = *c;

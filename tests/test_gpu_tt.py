@@ -77,3 +77,34 @@ def test_tt_time_schemes(fg, scheme):
     assert st["steps"] == sto["steps"] and st["t"] == sto["t"]
     assert st["corrections"] == sto["corrections"]
     assert rel(ug, uo) < 1e-8
+
+
+@pytest.mark.parametrize("cau", [0, 2], ids=["none", "caudd"])
+def test_tt_dd_assembly_bit_exact(fg, cau):
+    """Build_M_K_R_DD on the device (first build of a fresh system: zero
+    shock-capture state) against the oracle."""
+    p = G.transport_problem(33, angle_deg=110.0, k=1e-3, gamma=0.2, f=0.5, cau=cau)
+    p.form = fg.FG_TRANSPORT_DD
+    rng = np.random.default_rng(4)
+    u = rng.random(p.mesh.neq)
+    du = rng.standard_normal(p.mesh.neq)
+    A0, R0 = O.build_tt(p, 0.5, 0.05, u=u, du=du)
+    s = fg.transport_system(p)
+    R = s.tt_assemble(p, 0.5, 0.05, u, du)
+    assert np.array_equal(R[:-1], R0[:-1]) and R[-1] == 0.0
+    assert np.array_equal(s.get_blocks(), A0)
+
+
+def test_tt_dd_predictor(fg):
+    """The Predictor_Old loop with the DD build and CAUDD (state kept on the
+    device across the corrections and steps) against the oracle."""
+    p = G.transport_problem(33, angle_deg=30.0, k=1e-3, f=0.0, cau=2)
+    p.form = fg.FG_TRANSPORT_DD
+    to_o = O.TimeOpts(0, 2, 1e-3, 0, 8 * 0.02, 1e-6, 0)
+    uo, ao, sto = O.tt_predictor(p, 0.5, 0.02, to_o, tol=1e-10, kmax=30)
+    s = fg.transport_system(p)
+    to = fg.time_opts(0, 2, 1e-3, 0, 8 * 0.02, 1e-6, precond=fg.FG_PRECOND_DIAG, setup_flags=0)
+    ug, ag, st = s.tt_predictor(p, 0.5, 0.02, to, kmax=30, tol=1e-10)
+    assert st["steps"] == sto["steps"] == 8
+    assert st["corrections"] == sto["corrections"]
+    assert rel(ug, uo) < 1e-8

@@ -68,3 +68,34 @@ def test_reaches_the_steady_solution():
     Us, nl, its = O.transport_process(p, 1e-12, 1e-3, 30, 1000)
     u, a, st = O.tt_predictor(p, 0.5, 0.05, O.TimeOpts(1, 5, 1e-6, 1, 1e3, 1e-9, 0), tol=1e-12)
     assert np.linalg.norm(u - Us[: p.mesh.neq]) / np.linalg.norm(Us[: p.mesh.neq]) < 1e-6
+
+
+def test_tt_dd_pinned_through_steady_dd(oracle_lib):
+    """The transient DD build (Build_M_K_R_DD) against the steady DD build
+    (pinned bit-exactly to the reference's Build_K_F_DD): at u = du = 0 with
+    zero boundary data the load is bit-identical; the stiffness part
+    (Ae(dt1) - Ae(dt2)) / (alpha (dt1 - dt2)) equals the steady block to
+    rounding; the mass part is Mhh (1 + delta_ij) - KhB MBh / KBB."""
+    p = G.transport_problem(13, angle_deg=110.0, k=1e-3, gamma=0.3, f=0.7, upmode=1, upval=0.0, cau=0)
+    p.form = 1
+    A_ss, F_ss = O.build_k_f_supg(p)
+    A1, R1 = O.build_tt(p, 0.5, 0.1)
+    A2, R2 = O.build_tt(p, 0.5, 0.05)
+    assert np.array_equal(R1[:-1], F_ss[:-1])
+    ke = (A1 - A2) / (0.5 * (0.1 - 0.05))
+    assert np.allclose(ke, A_ss, rtol=1e-9, atol=1e-12 * np.abs(A_ss).max())
+
+
+def test_tt_dd_caudd_state_and_loop(oracle_lib):
+    """CAUDD in the transient DD build: the relaxed coefficient depends on the
+    previous build (state), and the Predictor_Old loop converges to the
+    steady DD solution of the same problem."""
+    p = G.transport_problem(13, angle_deg=30.0, k=1e-2, cau=2)
+    p.form = 1
+    u = np.random.default_rng(3).random(p.mesh.neq)
+    A1, _ = O.build_tt(p, 0.5, 0.05, u=u)
+    A2, _ = O.build_tt(p, 0.5, 0.05, u=u)
+    assert np.array_equal(A1, A2)                    # fresh state each single build
+    uo, ao, st = O.tt_predictor(p, 0.5, 0.5, O.TimeOpts(1, 5, 1e-8, 1, 1e4, 1e-9, 0), tol=1e-12)
+    Us, nl, its = O.transport_process(p, 1e-12, 1e-8, 30, 1000)
+    assert np.linalg.norm(uo - Us) <= 1e-5 * np.linalg.norm(Us)
