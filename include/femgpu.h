@@ -365,7 +365,13 @@ typedef struct {
     double tolerance;  /* StabilizationTolerance: CAU is off below this |grad U|  */
     double alpha;      /* Alpha (time integration)                                */
     double dt;         /* DeltaT                                                  */
+    int form;          /* StabilizationForm: FG_EULER_SUPG (0), or FG_EULER_DD:
+                          Build_M_K_F_DD_Transiente.c with Delta_DD.c ("DD",
+                          "Predictor1", "CAUDD"); its per-element state (the
+                          bubble values and the relaxed delta) stays on the
+                          device and is zeroed when fg_euler_predictor starts */
 } fg_euler_coeffs;
+enum { FG_EULER_SUPG = 0, FG_EULER_DD = 1 };
 
 /* Node coordinates and the prescribed (rho, rho u, rho v, rho E) of every node
  * (upresc[4*node+k], read where dof k of the node is Dirichlet). */

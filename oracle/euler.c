@@ -236,6 +236,147 @@ static void eu_element(const or_euler_problem *pb, const double X[3], const doub
     }
 }
 
+/* Inverse Riemannian metric A0^-1 in entropy variables at Ub
+ * (Build_M_K_F_DD_Transiente.c:132-158, the same as the SUPG build's). */
+static void eu_a0inv(double gamma, const double Ub[4], double A0[4][4])
+{
+    double nU = (Ub[1] * Ub[1]) + (Ub[2] * Ub[2]);
+    double rho_i = Ub[3] - ((nU * 0.5) / Ub[0]);
+    double V2 = Ub[1] / rho_i, V3 = Ub[2] / rho_i, V4 = (-Ub[0]) / rho_i;
+    double re = -1.0 / (rho_i * V4);
+    double k1 = (V2 * V2 + V3 * V3) * 0.5 / V4;
+    A0[0][0] = re * (k1 * k1 + gamma);
+    A0[0][1] = re * (k1 * V2);
+    A0[0][2] = re * (k1 * V3);
+    A0[0][3] = re * ((k1 + 1.0) * V4);
+    A0[1][1] = re * (V2 * V2 - V4);
+    A0[1][2] = re * (V2 * V3);
+    A0[1][3] = re * (V2 * V4);
+    A0[2][2] = re * (V3 * V3 - V4);
+    A0[2][3] = re * (V3 * V4);
+    A0[3][3] = re * V4 * V4;
+    A0[1][0] = A0[0][1]; A0[2][0] = A0[0][2]; A0[3][0] = A0[0][3];
+    A0[2][1] = A0[1][2]; A0[3][1] = A0[1][3]; A0[3][2] = A0[2][3];
+}
+
+/* Delta_DD.c:4-89: the DD diffusion 0.5 |L U|_A0 / |grad_xi U|_A0 (0 below
+ * the tolerance on |grad U|_A0), relaxed against the element's previous
+ * value (w = 1/2, the relaxed value is kept), times sqrt(2 Area).  A_x grad
+ * and A_y grad use the reference's term lists (rows with a structural zero
+ * skip it). */
+static double eu_delta_dd(double tolerance, double *delta_old, const double gx[4], const double gy[4],
+                          double Ax[4][4], double Ay[4][4], double A0[4][4], const double dUb[4], const double b[3],
+                          const double c[3], double twoArea)
+{
+    double Agx[4], Agy[4], kx[4], ky[4], L[4];
+    Agx[0] = gx[1];
+    Agx[1] = Ax[1][0] * gx[0] + Ax[1][1] * gx[1] + Ax[1][2] * gx[2] + Ax[1][3] * gx[3];
+    Agx[2] = Ax[2][0] * gx[0] + Ax[2][1] * gx[1] + Ax[2][2] * gx[2];
+    Agx[3] = Ax[3][0] * gx[0] + Ax[3][1] * gx[1] + Ax[3][2] * gx[2] + Ax[3][3] * gx[3];
+    Agy[0] = gy[2];
+    Agy[1] = Ay[1][0] * gy[0] + Ay[1][1] * gy[1] + Ay[1][2] * gy[2];
+    Agy[2] = Ay[2][0] * gy[0] + Ay[2][1] * gy[1] + Ay[2][2] * gy[2] + Ay[2][3] * gy[3];
+    Agy[3] = Ay[3][0] * gy[0] + Ay[3][1] * gy[1] + Ay[3][2] * gy[2] + Ay[3][3] * gy[3];
+    for (int i = 0; i < 4; i++) {
+        kx[i] = (b[0] * gx[i] + c[0] * gy[i]) / twoArea;
+        ky[i] = (b[1] * gx[i] + c[1] * gy[i]) / twoArea;
+    }
+    double nk = sqrt(a0_norm2(A0, kx) + a0_norm2(A0, ky));
+    for (int i = 0; i < 4; i++) L[i] = dUb[i] + Agx[i] + Agy[i];
+    double nL = sqrt(a0_norm2(A0, L));
+    double ng = sqrt(a0_norm2(A0, gx) + a0_norm2(A0, gy));
+    double aux = ng >= tolerance ? 0.5 * nL / nk : 0.0;
+    double w = 0.5;
+    double delta = w * aux + (1 - w) * (*delta_old);
+    *delta_old = delta;
+    return delta * sqrt(twoArea);
+}
+
+/* Build_M_K_F_DD_Transiente.c:34-896 for one element: the Galerkin
+ * convection blocks K_j = b_j Ax + c_j Ay, the DD diffusion, and the bubble
+ * (4 unknowns) condensed with T = (MhB + dt KhB) (MBB + dt KBB)^-1:
+ * Me = Mhh - T MhB, Ke = Khh - T KBh, Ne = (MhB - T MBB) / dt; Ae = Me +
+ * alpha dt Ke, Re = -Me dUe - Ke Ue + Ne uB; the bubble state uB (4) and
+ * delta_old are updated. */
+static void eu_dd_element(const or_euler_problem *pb, const double X[3], const double Y[3], const double Ue[12],
+                          const double dUe[12], double *uB, double *delta_old, double Ae[144], double Re[12])
+{
+    const double third = 1.0 / 3.0, sixth = 1.0 / 6.0, nf = 9.0 / 40.0;
+    const double gamma = pb->gamma, alpha = pb->alpha, dt = pb->dt;
+    double b[3] = {Y[1] - Y[2], Y[2] - Y[0], Y[0] - Y[1]};
+    double c[3] = {X[2] - X[1], X[0] - X[2], X[1] - X[0]};
+    double twoArea = fabs(c[2] * b[1] - c[1] * b[2]);
+    double Area = 0.5 * twoArea;
+    double Ub[4], dUb[4], gx[4], gy[4], uBaux[4];
+    int i, j, r, q;
+    for (i = 0; i < 4; i++) {
+        Ub[i] = (Ue[i] + Ue[i + 4] + Ue[i + 8]) * third;
+        dUb[i] = (dUe[i] + dUe[i + 4] + dUe[i + 8]) * third;
+        uBaux[i] = uB[i];
+    }
+    for (i = 0; i < 4; i++) {
+        gx[i] = (Ue[i] * b[0] + Ue[i + 4] * b[1] + Ue[i + 8] * b[2]) / twoArea;
+        gy[i] = (Ue[i] * c[0] + Ue[i + 4] * c[1] + Ue[i + 8] * c[2]) / twoArea;
+    }
+    double Ax[4][4], Ay[4][4], A0[4][4];
+    eu_jacobians(gamma, pb->mach, pb->dimensionless, Ub, Ax, Ay);
+    eu_a0inv(gamma, Ub, A0);
+    double delta = eu_delta_dd(pb->tolerance, delta_old, gx, gy, Ax, Ay, A0, dUb, b, c, twoArea);
+
+    double K[3][4][4], KhB[12][4], T[12][4];
+    for (j = 0; j < 3; j++)
+        for (r = 0; r < 4; r++)
+            for (q = 0; q < 4; q++) K[j][r][q] = b[j] * Ax[r][q] + c[j] * Ay[r][q];
+    double Mhh1 = Area * sixth, Mhh2 = Area / 12.0, MhB = (3.0 * Area) / 20.0, MBB = (81.0 * Area) / 280.0;
+    double d4a = delta / (4.0 * Area);
+    /* KhB rows of node i: p_i Ax + q_i Ay */
+    double p[3] = {nf * (b[0] + 2.0 * b[1] + 2.0 * b[2]), nf * (2.0 * b[0] + b[1] + 2.0 * b[2]),
+                   nf * (2.0 * b[0] + 2.0 * b[1] + b[2])};
+    double pq[3] = {nf * (c[0] + 2.0 * c[1] + 2.0 * c[2]), nf * (2.0 * c[0] + c[1] + 2.0 * c[2]),
+                    nf * (2.0 * c[0] + 2.0 * c[1] + c[2])};
+    for (i = 0; i < 3; i++)
+        for (r = 0; r < 4; r++)
+            for (q = 0; q < 4; q++) KhB[4 * i + r][q] = p[i] * Ax[r][q] + pq[i] * Ay[r][q];
+    double S = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[0] * b[1] + b[0] * b[2] + b[1] * b[2] + c[0] * c[0] +
+               c[1] * c[1] + c[2] * c[2] + c[0] * c[1] + c[0] * c[2] + c[1] * c[2];
+    double KBB = (81.0 * delta * S) / (40.0 * Area);
+    double invBB = 1.0 / (MBB + dt * KBB);
+    for (r = 0; r < 12; r++)
+        for (q = 0; q < 4; q++)
+            T[r][q] = (r & 3) == q ? invBB * (MhB + dt * KhB[r][q]) : invBB * dt * KhB[r][q];
+    double invdt = 1.0 / dt, adt = alpha * dt;
+    for (i = 0; i < 3; i++)
+        for (r = 0; r < 4; r++) {
+            const int row = 4 * i + r;
+            double m = 0, k = 0;
+            for (j = 0; j < 3; j++) {
+                double dd = d4a * (b[i < j ? i : j] * b[i < j ? j : i] + c[i < j ? i : j] * c[i < j ? j : i]);
+                for (q = 0; q < 4; q++) {
+                    const int col = 4 * j + q;
+                    double me = r == q ? (i == j ? Mhh1 : Mhh2) - T[row][q] * MhB : -T[row][q] * MhB;
+                    double ke = K[j][r][q] * sixth;
+                    if (r == q) ke = ke + dd;
+                    for (int s = 0; s < 4; s++) ke = ke - T[row][s] * (nf * K[j][s][q]);
+                    m += me * dUe[col];
+                    k += ke * Ue[col];
+                    Ae[12 * row + col] = me + adt * ke;
+                }
+            }
+            double N = 0.0;
+            for (q = 0; q < 4; q++) {
+                double ne = r == q ? (MhB - T[row][q] * MBB) * invdt : (-T[row][q] * MBB) * invdt;
+                N = q == 0 ? ne * uBaux[0] : N + ne * uBaux[q];
+            }
+            Re[row] = N + (-m - k);
+        }
+    /* the new bubble values (:878-889) */
+    for (r = 0; r < 4; r++) {
+        double s = (nf * K[0][r][0]) * Ue[0];
+        for (int col = 1; col < 12; col++) s += (nf * K[col >> 2][r][col & 3]) * Ue[col];
+        uB[r] = invBB * (MBB * uBaux[r] - dt * MhB * (dUe[r] + dUe[r + 4] + dUe[r + 8]) - dt * s);
+    }
+}
+
 void or_build_euler(int nnodes, int nel, const double *x, const double *y, const int *type,
                     const int *invp, const int *ien, int neq, const or_euler_problem *prob,
                     const double *u, const double *du, double *A, double *R)
@@ -251,6 +392,12 @@ void or_build_euler(int nnodes, int nel, const double *x, const double *y, const
             else { U[d] = prob->upresc[d]; dU[d] = 0.0; }
         }
     memset(R, 0, sizeof(double) * ((size_t)NEQ + 1));
+    double *uB = prob->uB, *dold = prob->delta_old, *own = NULL;     /* DD state */
+    if (prob->form == 1 && (!uB || !dold)) {
+        own = calloc(5 * (size_t)(nel ? nel : 1), sizeof(double));
+        uB = own;
+        dold = own + 4 * (size_t)(nel ? nel : 1);
+    }
     for (E = 0; E < nel; E++) {
         double X[3], Y[3], Ue[12], dUe[12], Re[12];
         int lm[12];
@@ -264,11 +411,14 @@ void or_build_euler(int nnodes, int nel, const double *x, const double *y, const
                 lm[4 * v + k] = type[d] == 0 ? NEQ : invp[d];
             }
         }
-        eu_element(prob, X, Y, Ue, dUe, A + 144L * E, Re);
+        if (prob->form == 1)
+            eu_dd_element(prob, X, Y, Ue, dUe, uB + 4L * E, dold + E, A + 144L * E, Re);
+        else
+            eu_element(prob, X, Y, Ue, dUe, A + 144L * E, Re);
         for (k = 0; k < 12; k++) R[lm[k]] += Re[k];
         R[NEQ] = 0;
     }
-    free(U); free(dU);
+    free(U); free(dU); free(own);
 }
 
 /* ---- Predictor_Old with EBE 12x12 blocks and BlockDiag (4x4) ---- */
@@ -331,9 +481,14 @@ int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, co
     double *bd = malloc(sizeof(double) * 16 * nn), *inv = malloc(sizeof(double) * 16 * nn);
     or_fill_lm(nel, 4, ien, type, invp, NEQ, lm);
     for (i = 0; i < 4 * nnodes; i++) Id[i] = type[i] == 0 ? NEQ : invp[i];
-    eu_loop c = { { nel, nnodes, NEQ, lm, Id, A, inv }, nnodes, nel, neq, x, y, type, invp, ien, prob, R, bd,
+    /* the DD state (uB, delta_old) lives for the whole loop (Predictor_Old.c:20-30) */
+    or_euler_problem pl = *prob;
+    double *state = calloc(5 * (size_t)(nel ? nel : 1), sizeof(double));
+    pl.uB = state;
+    pl.delta_old = state + 4 * (size_t)(nel ? nel : 1);
+    eu_loop c = { { nel, nnodes, NEQ, lm, Id, A, inv }, nnodes, nel, neq, x, y, type, invp, ien, &pl, R, bd,
                   solver_tol, kmax, lmax };
     int steps = or_time_integrate(neq, prob->alpha, prob->dt, to, eu_correct, &c, u, a, st);
-    free(lm); free(Id); free(A); free(R); free(bd); free(inv);
+    free(lm); free(Id); free(A); free(R); free(bd); free(inv); free(state);
     return steps;
 }

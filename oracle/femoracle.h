@@ -175,6 +175,8 @@ typedef struct {
     double tolerance;      /* StabilizationTolerance (CAU switch on |grad U|)          */
     double alpha, dt;      /* Alpha_Build, DeltaT_Build                                */
     const double *upresc;  /* [4*nnodes] prescribed rho, rho u, rho v, rho E           */
+    int form;              /* 0: SUPG + CAU, 1: DD (Build_M_K_F_DD_Transiente + Delta_DD) */
+    double *uB, *delta_old;/* DD state: [4*nel] bubbles, [nel] delta (NULL: fresh zeros) */
 } or_euler_problem;
 
 /* Build_M_K_F_SUPG + Delta_CAU + eval_U_dU + ebe_assembly: A receives the

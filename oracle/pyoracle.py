@@ -164,6 +164,8 @@ def ref_euler():
         R.fr_eu_lm.restype = None
         R.fr_eu_build.argtypes = mesh + [_f64p, _f64p, _c_int, _f64p, _f64p, _f64p, _f64p]
         R.fr_eu_build.restype = None
+        R.fr_eu_set_form.argtypes = [_c_int]
+        R.fr_eu_set_form.restype = None
         R.fr_eu_blockdiag.argtypes = mesh + [_f64p, _f64p, _f64p]
         R.fr_eu_blockdiag.restype = None
         R.fr_eu_ebemv.argtypes = mesh + [_f64p, _f64p, _f64p]
@@ -179,7 +181,8 @@ def ref_euler():
 # ---------------------------------------------------------------- helpers
 class _EulerProblem(ctypes.Structure):
     _fields_ = [("gamma", _c_dbl), ("mach", _c_dbl), ("dimensionless", _c_int), ("tolerance", _c_dbl),
-                ("alpha", _c_dbl), ("dt", _c_dbl), ("upresc", ctypes.POINTER(_c_dbl))]
+                ("alpha", _c_dbl), ("dt", _c_dbl), ("upresc", ctypes.POINTER(_c_dbl)), ("form", _c_int),
+                ("uB", ctypes.c_void_p), ("delta_old", ctypes.c_void_p)]
 
 
 class TimeOpts(ctypes.Structure):
@@ -200,7 +203,7 @@ class _TimeStats(ctypes.Structure):
 def _eu_struct(p):
     up = np.ascontiguousarray(p.upresc, dtype=np.float64)
     s = _EulerProblem(p.gamma, p.mach, int(p.dimensionless), p.tolerance, p.alpha, p.dt,
-                      up.ctypes.data_as(ctypes.POINTER(_c_dbl)))
+                      up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(getattr(p, "form", 0)), None, None)
     return s, up
 
 
@@ -241,6 +244,7 @@ def ref_euler_build(prob, u=None, du=None):
     du = np.zeros(m.neq) if du is None else np.ascontiguousarray(du, dtype=np.float64)
     A = np.empty(m.nel * 144)
     R = np.empty(m.neq + 1)
+    ref_euler().fr_eu_set_form(int(getattr(prob, "form", 0)))
     ref_euler().fr_eu_build(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
                             int(prob.wall), u, du, A, R)
     return A.reshape(m.nel, 144), R
@@ -265,6 +269,7 @@ def ref_euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000):
     m = prob.mesh
     u = np.zeros(m.neq + 1)
     t = _c_dbl(0.0)
+    ref_euler().fr_eu_set_form(int(getattr(prob, "form", 0)))
     its = ref_euler().fr_eu_predictor(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
                                       int(prob.wall), np.ascontiguousarray(prob.init), topts.as_array(),
                                       kmax, lmax, tol, u, ctypes.byref(t))

@@ -72,6 +72,26 @@ typedef struct {
     AuxBuildStructuresType Aux;
 } fr_eu;
 
+static int g_eu_form;   /* 0: SUPG + CAU, 1: DD + CAUDD */
+void fr_eu_set_form(int form) { g_eu_form = form; }
+
+/* Ax_Ay_calculations.c:35-38 assigns Ay[0][0] twice and never Ay[0][3], and
+ * Build_M_K_F_DD_Transiente reads Ay[0][3] (through Ka14, Kb14, Kc14): the
+ * value is whatever the stack held.  The harness clears the stack before
+ * every DD build, so that the reference reads 0 there -- the Jacobian's
+ * value -- and its results are reproducible. */
+static __attribute__((noinline)) void fr_clear_stack(void)
+{
+    volatile char buf[1 << 16];
+    size_t i;
+    for (i = 0; i < sizeof buf; i++) buf[i] = 0;
+}
+static int fr_dd_build(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctionsType *F)
+{
+    fr_clear_stack();
+    return Build_M_K_F_DD_Transiente(P, M, S, F);
+}
+
 static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const double *y, const int *type,
                         const int *invp, const int *ien, int neq, const double *prm)
 {
@@ -81,8 +101,8 @@ static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const do
     strcpy(c->P.Solver, "GMRES");
     strcpy(c->P.TimeIntegration, "Predictor1");
     strcpy(c->P.MatrixVectorProductScheme, "EBE");
-    strcpy(c->P.StabilizationForm, "SUPG");
-    strcpy(c->P.ShockCapture, "CAU");
+    strcpy(c->P.StabilizationForm, g_eu_form ? "DD" : "SUPG");
+    strcpy(c->P.ShockCapture, g_eu_form ? "CAUDD" : "CAU");
     strcpy(c->P.Preconditioner, "BlockDiag");
     strcpy(c->P.Scaling, "NOT");
     strcpy(c->P.reordering, "NOT");
@@ -143,15 +163,21 @@ static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const do
     setSolver(&c->P, &c->O);
     setPreconditioner(&c->P, &c->F);
     setDimensionlessness(&c->P, &c->F);
-    c->O.Build = Build_M_K_F_SUPG;
-    c->F.ShockCapture = Delta_CAU;
+    if (g_eu_form) {       /* setStabilizationForm.c:31-34, 60-62: "DD", "Predictor1", "CAUDD" */
+        c->O.Build = fr_dd_build;
+        c->F.ShockCapture = Delta_DD;
+        c->S.uB = calloc(4 * (size_t)nel + 4, sizeof(double));
+    } else {
+        c->O.Build = Build_M_K_F_SUPG;
+        c->F.ShockCapture = Delta_CAU;
+    }
 }
 
 static void fr_eu_free(fr_eu *c)
 {
     free(c->S.Node); free(c->S.Element); free(c->S.F); free(c->S.U);
     free(c->S.lm); free(c->S.lmaux); free(c->M.A); free(c->M.Aaux);
-    free(c->M.Diag); free(c->M.invDiag); free(c->S.delta_old);
+    free(c->M.Diag); free(c->M.invDiag); free(c->S.delta_old); free(c->S.uB);
     if (c->M.Id) { free(c->M.Id[0]); free(c->M.Id); }
     if (c->M.BlockDiag) { free(c->M.BlockDiag[0]); free(c->M.BlockDiag); }
     if (c->M.invBlockDiag) { free(c->M.invBlockDiag[0]); free(c->M.invBlockDiag); }
@@ -186,7 +212,7 @@ void fr_eu_build(int nnodes, int nel, const double *x, const double *y, const in
     memcpy(c.S.u, u, sizeof(double) * (size_t)neq);
     memcpy(dus, du, sizeof(double) * (size_t)neq);
     c.S.du = dus;
-    Build_M_K_F_SUPG(&c.P, &c.M, &c.S, &c.F);
+    c.O.Build(&c.P, &c.M, &c.S, &c.F);
     memcpy(A_out, c.M.Aaux, sizeof(double) * 144 * (size_t)nel);
     memcpy(R_out, c.S.F, sizeof(double) * ((size_t)neq + 1));
     free(dus);
@@ -247,6 +273,8 @@ int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const
     /* the loops install and free their own du, uB, duB, delta_old and AuxBuild */
     free(c.S.delta_old);
     c.S.delta_old = NULL;
+    free(c.S.uB);
+    c.S.uB = NULL;
     if (topt[6] == 1.0)
         Predictor_Old_BDF(&c.P, &c.M, &c.S, &c.F, &c.O);
     else if (topt[6] == 2.0)

@@ -235,13 +235,180 @@ __global__ void __launch_bounds__(128) k_euler_elem(int nel, int ld, int n, cons
     }
 }
 
+// ---------------------------------------------------------------- DD form
+// Build_M_K_F_DD_Transiente.c:34-896 with Delta_DD.c:4-89.  Per element:
+// K_j = b_j Ax + c_j Ay (Galerkin convection, K_j / 6 in every row block),
+// the DD diffusion delta / (4 Area) (b_i b_j + c_i c_j) on the dof diagonal,
+// and the bubble condensed with T = (MhB + dt KhB) / (MBB + dt KBB) (KhB
+// rows of node i: p_i Ax + q_i Ay; KBh = 9/40 K_j): Me = Mhh - T MhB,
+// Ke = Khh - T KBh, Ne = (MhB - T MBB) / dt; Ae = Me + alpha dt Ke; the
+// residual row is Ne uB + (-Me dUe - Ke Ue); the bubble values uB and the
+// relaxed delta are element state (internal order) updated here.  K_j, KhB
+// and T are recomputed where used (same operands, same rounding) instead of
+// held in registers.  Ax_Ay_calculations.c leaves Ay[0][3] unassigned and the
+// reference reads it here; eu_jacobians gives it its value, 0.
+__device__ __forceinline__ double eu_kj(const double Ax[4][4], const double Ay[4][4], double bj, double cj, int r, int q)
+{
+    return bj * Ax[r][q] + cj * Ay[r][q];
+}
+
+__global__ void __launch_bounds__(128) k_euler_dd_elem(int nel, int ld, int n, const int *__restrict__ gien,
+                                                       const double *__restrict__ gx, const double *__restrict__ gy,
+                                                       const int *__restrict__ node_dof,
+                                                       const double *__restrict__ up, const double *__restrict__ u,
+                                                       const double *__restrict__ du, fg_euler_coeffs cf,
+                                                       double *delta_old, double *uB, double *__restrict__ A64,
+                                                       double *__restrict__ Fe)
+{
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const double third = 1.0 / 3.0, sixth = 1.0 / 6.0, nf = 9.0 / 40.0;
+    const double gamma = cf.gamma, dt = cf.dt;
+    double X[3], Y[3], Ue[12], dUe[12];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const int J = gien[(size_t)v * ld + pos];
+        X[v] = gx[J];
+        Y[v] = gy[J];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int d = node_dof[4 * J + k];
+            const bool dir = d == n;
+            Ue[4 * v + k] = dir ? up[4 * J + k] : u[d];
+            dUe[4 * v + k] = dir ? 0.0 : du[d];
+        }
+    }
+    const double b[3] = {Y[1] - Y[2], Y[2] - Y[0], Y[0] - Y[1]};
+    const double c[3] = {X[2] - X[1], X[0] - X[2], X[1] - X[0]};
+    const double twoArea = fabs(c[2] * b[1] - c[1] * b[2]);
+    const double Area = 0.5 * twoArea;
+    double Ub[4], dUb[4], gxu[4], gyu[4], uBaux[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        Ub[i] = (Ue[i] + Ue[i + 4] + Ue[i + 8]) * third;
+        dUb[i] = (dUe[i] + dUe[i + 4] + dUe[i + 8]) * third;
+        gxu[i] = (Ue[i] * b[0] + Ue[i + 4] * b[1] + Ue[i + 8] * b[2]) / twoArea;
+        gyu[i] = (Ue[i] * c[0] + Ue[i + 4] * c[1] + Ue[i + 8] * c[2]) / twoArea;
+        uBaux[i] = uB[(size_t)i * ld + pos];
+    }
+    const double nU = (Ub[1] * Ub[1]) + (Ub[2] * Ub[2]);
+    double Ax[4][4], Ay[4][4];
+    eu_jacobians(cf, Ub, Ax, Ay);
+    double delta;
+    {   // Delta_DD.c: A0^-1 norms, relaxed (w = 1/2), times sqrt(2 Area)
+        const double rho_i = Ub[3] - ((nU * 0.5) / Ub[0]);
+        const double V2 = Ub[1] / rho_i, V3 = Ub[2] / rho_i, V4 = (-Ub[0]) / rho_i;
+        const double re = -1.0 / (rho_i * V4);
+        const double k1 = (V2 * V2 + V3 * V3) * 0.5 / V4;
+        const double A0[10] = {re * (k1 * k1 + gamma), re * (k1 * V2),      re * (k1 * V3), re * ((k1 + 1.0) * V4),
+                               re * (V2 * V2 - V4),    re * (V2 * V3),      re * (V2 * V4), re * (V3 * V3 - V4),
+                               re * (V3 * V4),         re * V4 * V4};
+        double Agx[4], Agy[4], kx[4], ky[4], L[4];
+        Agx[0] = gxu[1];
+        Agx[1] = Ax[1][0] * gxu[0] + Ax[1][1] * gxu[1] + Ax[1][2] * gxu[2] + Ax[1][3] * gxu[3];
+        Agx[2] = Ax[2][0] * gxu[0] + Ax[2][1] * gxu[1] + Ax[2][2] * gxu[2];
+        Agx[3] = Ax[3][0] * gxu[0] + Ax[3][1] * gxu[1] + Ax[3][2] * gxu[2] + Ax[3][3] * gxu[3];
+        Agy[0] = gyu[2];
+        Agy[1] = Ay[1][0] * gyu[0] + Ay[1][1] * gyu[1] + Ay[1][2] * gyu[2];
+        Agy[2] = Ay[2][0] * gyu[0] + Ay[2][1] * gyu[1] + Ay[2][2] * gyu[2] + Ay[2][3] * gyu[3];
+        Agy[3] = Ay[3][0] * gyu[0] + Ay[3][1] * gyu[1] + Ay[3][2] * gyu[2] + Ay[3][3] * gyu[3];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            kx[i] = (b[0] * gxu[i] + c[0] * gyu[i]) / twoArea;
+            ky[i] = (b[1] * gxu[i] + c[1] * gyu[i]) / twoArea;
+            L[i] = dUb[i] + Agx[i] + Agy[i];
+        }
+        const double nk = sqrt(a0_norm2(A0, kx) + a0_norm2(A0, ky));
+        const double nL = sqrt(a0_norm2(A0, L));
+        const double ng = sqrt(a0_norm2(A0, gxu) + a0_norm2(A0, gyu));
+        const double aux = ng >= cf.tolerance ? 0.5 * nL / nk : 0.0;
+        const double w = 0.5;
+        double d = w * aux + (1 - w) * delta_old[pos];
+        delta_old[pos] = d;
+        delta = d * sqrt(twoArea);
+    }
+    const double Mhh1 = Area * sixth, Mhh2 = Area / 12.0, MhB = (3.0 * Area) / 20.0, MBB = (81.0 * Area) / 280.0;
+    const double d4a = delta / (4.0 * Area);
+    const double p[3] = {nf * (b[0] + 2.0 * b[1] + 2.0 * b[2]), nf * (2.0 * b[0] + b[1] + 2.0 * b[2]),
+                         nf * (2.0 * b[0] + 2.0 * b[1] + b[2])};
+    const double pq[3] = {nf * (c[0] + 2.0 * c[1] + 2.0 * c[2]), nf * (2.0 * c[0] + c[1] + 2.0 * c[2]),
+                          nf * (2.0 * c[0] + 2.0 * c[1] + c[2])};
+    const double S = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[0] * b[1] + b[0] * b[2] + b[1] * b[2] + c[0] * c[0] +
+                     c[1] * c[1] + c[2] * c[2] + c[0] * c[1] + c[0] * c[2] + c[1] * c[2];
+    const double KBB = (81.0 * delta * S) / (40.0 * Area);
+    const double invBB = 1.0 / (MBB + dt * KBB);
+    const double invdt = 1.0 / dt, adt = cf.alpha * dt;
+    double *a = A64 + pos;
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll 1
+        for (int r = 0; r < 4; ++r) {
+            const int row = 4 * i + r;
+            double T[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const double khb = p[i] * Ax[r][q] + pq[i] * Ay[r][q];
+                T[q] = r == q ? invBB * (MhB + dt * khb) : invBB * dt * khb;
+            }
+            double m = 0.0, k = 0.0;
+#pragma unroll 1
+            for (int j = 0; j < 3; ++j) {
+                const int lo = i < j ? i : j, hi = i < j ? j : i;
+                const double dd = d4a * (b[lo] * b[hi] + c[lo] * c[hi]);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int col = 4 * j + q;
+                    const double me = r == q ? (i == j ? Mhh1 : Mhh2) - T[q] * MhB : -T[q] * MhB;
+                    double ke = eu_kj(Ax, Ay, b[j], c[j], r, q) * sixth;
+                    if (r == q) ke = ke + dd;
+#pragma unroll
+                    for (int s2 = 0; s2 < 4; ++s2) ke = ke - T[s2] * (nf * eu_kj(Ax, Ay, b[j], c[j], s2, q));
+                    m += me * dUe[col];
+                    k += ke * Ue[col];
+                    a[(size_t)(12 * row + col) * ld] = me + adt * ke;
+                }
+            }
+            double N = 0.0;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const double ne = r == q ? (MhB - T[q] * MBB) * invdt : (-T[q] * MBB) * invdt;
+                N = q == 0 ? ne * uBaux[0] : N + ne * uBaux[q];
+            }
+            Fe[(size_t)row * ld + pos] = N + (-m - k);
+        }
+    }
+    // the new bubble values (:878-889)
+#pragma unroll 1
+    for (int r = 0; r < 4; ++r) {
+        double s = (nf * eu_kj(Ax, Ay, b[0], c[0], r, 0)) * Ue[0];
+#pragma unroll
+        for (int col = 1; col < 12; ++col) s += (nf * eu_kj(Ax, Ay, b[col >> 2], c[col >> 2], r, col & 3)) * Ue[col];
+        uB[(size_t)r * ld + pos] = invBB * (MBB * uBaux[r] - dt * MhB * (dUe[r] + dUe[r + 4] + dUe[r + 8]) - dt * s);
+    }
+}
+
 int euler_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
                           double *R_dev, cudaStream_t st)
 {
     const Topology &t = s->topo;
     if (t.ndof != 4) { set_error("Euler assembly needs ndof == 4"); return FG_ERR_UNSUPPORTED; }
     if (!s->eu_geometry_ok) { set_error("Euler assembly before fg_euler_set_geometry"); return FG_ERR_STATE; }
-    if (t.nel > 0)
+    if (c->form != FG_EULER_SUPG && c->form != FG_EULER_DD) {
+        set_error("Euler form must be FG_EULER_SUPG or FG_EULER_DD");
+        return FG_ERR_ARG;
+    }
+    if (c->form == FG_EULER_DD) {   // element state: delta_old [nel_pad], uB [4][nel_pad]
+        int r0;
+        if (s->shock_state.bytes < 40 * (size_t)s->nel_pad && (r0 = s->shock_state.alloc(40 * (size_t)s->nel_pad)))
+            return r0;
+        if (t.nel > 0)
+            k_euler_dd_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(),
+                                                                s->gx.as<double>(), s->gy.as<double>(),
+                                                                s->node_dof.as<int>(), s->gup.as<double>(), u_dev,
+                                                                du_dev, *c, s->shock_state.as<double>(),
+                                                                s->shock_state.as<double>() + s->nel_pad,
+                                                                s->A64.as<double>(), s->Fe.as<double>());
+    } else if (t.nel > 0)
         k_euler_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(),
                                                          s->gx.as<double>(), s->gy.as<double>(),
                                                          s->node_dof.as<int>(), s->gup.as<double>(), u_dev, du_dev,

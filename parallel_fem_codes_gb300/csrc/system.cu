@@ -952,6 +952,8 @@ int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_o
                        double *u, double *a, fg_time_stats *stats)
 {
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
+    // the DD element state starts at zero with the loop (Predictor_Old.c callocs uB and delta_old)
+    if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
     return time_loop(s, c->dt, c->alpha,
                      [&](double ab, double db, const double *du, const double *da, double *R) {
                          fg_euler_coeffs cc = *c;

@@ -23,6 +23,7 @@ FG_PREC_FP64, FG_PREC_MIXED, FG_PREC_MIXED16 = 64, 32, 16
 FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 = 0, 1, 2
 FG_NS_SUPG_PSPG, FG_NS_VMS_DCDD = 0, 1
 FG_TRANSPORT_SUPG, FG_TRANSPORT_DD = 0, 1
+FG_EULER_SUPG, FG_EULER_DD = 0, 1
 FG_SHOCK_NONE, FG_SHOCK_CAU, FG_SHOCK_CAUDD, FG_SHOCK_YZBETA = 0, 1, 2, 3
 FG_HSHOCK_2SQRTAREA, FG_HSHOCK_OPTION1, FG_HSHOCK_OPTION2 = 0, 1, 2
 FG_REORDER_NONE, FG_REORDER_RCM = 0, 1
@@ -85,7 +86,7 @@ class NSCoeffs(ctypes.Structure):
 
 class EulerCoeffs(ctypes.Structure):
     _fields_ = [("gamma", _c_dbl), ("mach", _c_dbl), ("dimensionless", _c_int), ("tolerance", _c_dbl),
-                ("alpha", _c_dbl), ("dt", _c_dbl)]
+                ("alpha", _c_dbl), ("dt", _c_dbl), ("form", _c_int)]
 
 
 class TimeOpts(ctypes.Structure):
@@ -546,7 +547,8 @@ def tt_coeffs(prob, alpha, dt) -> TTCoeffs:
 
 
 def euler_coeffs(prob) -> EulerCoeffs:
-    return EulerCoeffs(prob.gamma, prob.mach, int(prob.dimensionless), prob.tolerance, prob.alpha, prob.dt)
+    return EulerCoeffs(prob.gamma, prob.mach, int(prob.dimensionless), prob.tolerance, prob.alpha, prob.dt,
+                       int(getattr(prob, "form", 0)))
 
 
 def time_opts(stop_by_norm=0, max_corrections=2, correction_tol=1e-3, steady_state=0, final_time=0.0,

@@ -22,7 +22,11 @@ Process loop on the transport cases; and tests/golden/shock_sst.npz: the
 YZBeta shock capture and the h_shock Option1 / Option2 lengths with both
 forms (blocks and F at a state u, the Process loop); and
 tests/golden/ilup_sst.npz: the reference's ILU(p) ("ILU1", "ILU2", "ILU3")
-applied to a vector, with the CSR matrix it factorises.
+applied to a vector, with the CSR matrix it factorises; and
+tests/golden/dd_euler.npz: the Euler driver's Build_M_K_F_DD_Transiente (with
+Delta_DD) at a state (u, du) and its Predictor_Old loop, on the Euler cases
+(the harness clears the stack before each DD build: the reference reads an
+unassigned Jacobian entry there).
 """
 import os
 import sys
@@ -201,6 +205,23 @@ def write_ilup():
     np.savez_compressed(os.path.join(HERE, "ilup_sst.npz"), **out)
 
 
+def write_euler_dd():
+    out = {}
+    for name, (prob, seed, to) in euler_cases().items():
+        prob.form = 1
+        m = prob.mesh
+        rng = np.random.Generator(np.random.PCG64(seed + 20))
+        u = prob.initial_state() * (1.0 + 0.05 * rng.standard_normal(m.neq))
+        du = 0.01 * rng.standard_normal(m.neq)
+        A, R = O.ref_euler_build(prob, u, du)
+        to.scheme = 0
+        U, its, t = O.ref_euler_predictor(prob, to, 1e-10, 25, 1000)
+        out[name + "_u"], out[name + "_du"], out[name + "_A"], out[name + "_R"] = u, du, A, R
+        out[name + "_U"], out[name + "_its"], out[name + "_t"] = U, its, t
+        print(name, "DD gmres", its, "t", t)
+    np.savez_compressed(os.path.join(HERE, "dd_euler.npz"), **out)
+
+
 if __name__ == "__main__":
     main()
     write_euler()
@@ -209,3 +230,4 @@ if __name__ == "__main__":
     write_sst_dd()
     write_sst_shock()
     write_ilup()
+    write_euler_dd()

@@ -144,3 +144,32 @@ def test_euler_time_schemes(fg, scheme, steady):
     assert st["steps"] == sto["steps"]
     assert st["t"] == sto["t"]
     assert rel(ug, uo) < 1e-7
+
+
+@pytest.mark.parametrize("dimensionless", [True, False])
+def test_euler_dd_assembly_bit_exact(fg, dimensionless):
+    """Build_M_K_F_DD_Transiente on the device (first build of a fresh
+    system: zero element state) against the oracle, both Jacobian forms."""
+    p = G.obliquo_problem(17, dimensionless=dimensionless)
+    p.form = fg.FG_EULER_DD
+    rng = np.random.default_rng(5)
+    u = p.initial_state() * (1.0 + 0.05 * rng.standard_normal(p.mesh.neq))
+    du = 0.01 * rng.standard_normal(p.mesh.neq)
+    A0, R0 = O.build_euler(p, u, du)
+    s = fg.euler_system(p)
+    R = s.euler_assemble(p, u, du)
+    assert np.array_equal(R, R0)
+    assert np.array_equal(s.get_blocks(), A0)
+
+
+def test_euler_dd_predictor(fg):
+    """The DD loop (element state kept on the device across corrections and
+    steps) against the oracle."""
+    p = G.obliquo_problem(17)
+    p.form = fg.FG_EULER_DD
+    to_o = O.TimeOpts(0, 2, 1e-3, 0, 4 * p.dt, 1e-6, 0)
+    uo, ao, sto = O.euler_predictor(p, to_o, tol=1e-10, kmax=25)
+    s = fg.euler_system(p)
+    ug, ag, st = s.euler_predictor(p, fg.time_opts(0, 2, 1e-3, 0, 4 * p.dt, 1e-6), kmax=25, tol=1e-10)
+    assert st["steps"] == sto["steps"] == 4
+    assert rel(ug, uo) < 1e-7

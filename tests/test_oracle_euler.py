@@ -129,3 +129,35 @@ def test_against_reference_build(n, dimless):
     A, R = O.build_euler(p, u, du)
     Ar, Rr = O.ref_euler_build(p, u, du)
     assert np.array_equal(A, Ar) and np.array_equal(R, Rr)
+
+
+DDE = os.path.join(os.path.dirname(__file__), "golden", "dd_euler.npz")
+
+
+@pytest.mark.parametrize("name", ["eu_9_obliquo", "eu_7_dimensional"])
+def test_dd_bit_exact(name, oracle_lib):
+    """StabilizationForm "DD" (Build_M_K_F_DD_Transiente with Delta_DD):
+    blocks and residual at a state, and the Predictor_Old loop with its
+    element state (bubbles, relaxed delta), against the reference's own."""
+    g = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz")))
+    p = problem_from(g)
+    p.form = 1
+    d = np.load(DDE)
+    A, R = O.build_euler(p, d[name + "_u"], d[name + "_du"])
+    assert np.array_equal(A, d[name + "_A"]) and np.array_equal(R, d[name + "_R"])
+    u, a, st = O.euler_predictor(p, topts_from(g), tol=1e-10, kmax=25, lmax=1000)
+    assert st["gmres_iterations"] == int(d[name + "_its"]) and st["t"] == float(d[name + "_t"])
+    assert np.array_equal(u, d[name + "_U"])
+
+
+def test_dd_against_reference_build(oracle_lib):
+    if O.ref_euler() is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    p = G.obliquo_problem(11)
+    p.form = 1
+    rng = np.random.default_rng(11)
+    u = p.initial_state() * (1.0 + 0.05 * rng.standard_normal(p.mesh.neq))
+    du = 0.01 * rng.standard_normal(p.mesh.neq)
+    A0, R0 = O.ref_euler_build(p, u, du)
+    A1, R1 = O.build_euler(p, u, du)
+    assert np.array_equal(A0, A1) and np.array_equal(R0, R1)
