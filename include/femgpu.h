@@ -187,7 +187,13 @@ enum {
  * fg_unscale (Left_unscaling, :187-196: X *= sqrt(1/Diag)).  F: host n+1,
  * in place, may be NULL.  The system's preconditioner becomes
  * FG_PRECOND_NONE (set another one up afterwards if wanted). */
-enum { FG_SCALE_LEFT = 1, FG_SCALE_LEFTRIGHT = 2 };
+/* FG_SCALE_BLOCK: Block_scaling_EBE (Block_scaling.c:10-118, Scaling
+ * "BlockScaling" of the Euler driver, which installs it but never calls it):
+ * the block-diagonal set-up (F <- B^-1 F, the reference's 4x4 inverse), then
+ * in every element block the rows and columns of Dirichlet dofs cleared
+ * (diagonal 1) and each node's row block multiplied by its inverse block;
+ * fg_unscale is then the identity (NO_unscaling).  Systems with ndof 2-4. */
+enum { FG_SCALE_LEFT = 1, FG_SCALE_LEFTRIGHT = 2, FG_SCALE_BLOCK = 3 };
 int fg_scale(fg_system *s, int kind, double *F);
 int fg_unscale(fg_system *s, double *X);
 

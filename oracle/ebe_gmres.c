@@ -364,3 +364,36 @@ int or_ebe_block_solve(int nnodes, int nel, int B, const int *ien, const int *lm
     free(bd); free(inv);
     return it;
 }
+
+
+/* Block_scaling_EBE (Block_scaling.c:10-118), after the block-diagonal
+ * set-up has given inv (B*B per node, row-major): in every element block,
+ * the row and the column of each Dirichlet dof are cleared and its diagonal
+ * entry set to 1 (matrix_Bondary_Conditions), then every row block of node
+ * v is multiplied by inv[v] (matrix_Scaling, sums from 0 in j order). */
+void or_block_scale(int nel, int B, const int *ien, const int *Id, int NEQ, const double *inv, double *A)
+{
+    const int S = 3 * B;
+    double *m = malloc(sizeof(double) * (size_t)S * S);
+    for (int e = 0; e < nel; e++) {
+        double *Ae = A + (size_t)S * S * e;
+        memcpy(m, Ae, sizeof(double) * (size_t)S * S);
+        for (int I = 0; I < B; I++)
+            for (int v = 0; v < 3; v++) {
+                if (Id[B * ien[3 * e + v] + I] != NEQ) continue;
+                const int d = B * v + I;
+                for (int t = 0; t < S; t++) { m[d * S + t] = 0; m[t * S + d] = 0; }
+                m[d * S + d] = 1;
+            }
+        for (int v = 0; v < 3; v++) {
+            const double *iv = inv + (size_t)B * B * ien[3 * e + v];
+            for (int i = 0; i < B; i++)
+                for (int col = 0; col < S; col++) {
+                    double a = 0;
+                    for (int j = 0; j < B; j++) a += iv[i * B + j] * m[(B * v + j) * S + col];
+                    Ae[(B * v + i) * S + col] = a;
+                }
+        }
+    }
+    free(m);
+}

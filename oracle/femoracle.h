@@ -85,6 +85,9 @@ void or_blockdiag_setup(int nnodes, int nel, int B, const int *ien, const double
                         double *BlockDiag, double *invBlockDiag, double *F);
 void or_blockdiag_apply(int nnodes, int B, const int *Id, int NEQ,
                         const double *invBlockDiag, double *p, double *z);
+/* Block_scaling_EBE: Dirichlet rows/columns of the element blocks cleared
+ * (diagonal 1), each node's row block multiplied by its inverse block. */
+void or_block_scale(int nel, int B, const int *ien, const int *Id, int NEQ, const double *inv, double *A);
 
 /* ---- GMRES (Solvers_and_Preconditioners/pgmres.c:5-200) ---- */
 typedef int (*or_mv_fn)(void *ctx, double *P, double *Q);      /* Q = A P, vectors NEQ+1 */

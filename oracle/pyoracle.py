@@ -794,3 +794,29 @@ def unscale(invDiag, x):
     L.or_unscale(invDiag.shape[0] - 1, np.ascontiguousarray(invDiag, dtype=np.float64), x)
     return x
 
+
+
+
+def block_scale(mesh, A, inv, B=4):
+    """Block_scaling_EBE's element-block part (oracle/ebe_gmres.c) on copies:
+    returns the scaled blocks (nel, (3B)^2)."""
+    L = lib()
+    L.or_block_scale.argtypes = [_c_int, _c_int, _i32p, _i32p, _c_int, _f64p, _f64p]
+    L.or_block_scale.restype = None
+    Id = np.where(mesh.type == 0, mesh.neq, mesh.invp).astype(np.int32)
+    Ac = np.array(A, dtype=np.float64, copy=True).reshape(-1)
+    L.or_block_scale(mesh.nel, B, np.ascontiguousarray(mesh.ien, dtype=np.int32).reshape(-1), Id, mesh.neq,
+                     np.ascontiguousarray(inv, dtype=np.float64).reshape(-1), Ac)
+    return Ac.reshape(mesh.nel, -1)
+
+
+def ref_euler_block_scale(mesh, A, F):
+    """The reference's Block_scaling_EBE: returns (A, F, inverse blocks)."""
+    R = ref_euler()
+    R.fr_eu_block_scale.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _f64p, _f64p, _f64p]
+    R.fr_eu_block_scale.restype = None
+    Ac = np.array(A, dtype=np.float64, copy=True).reshape(-1)
+    Fc = np.array(F, dtype=np.float64, copy=True)
+    inv = np.empty(mesh.nnodes * 16)
+    R.fr_eu_block_scale(*_mesh_args(mesh), Ac, Fc, inv)
+    return Ac.reshape(mesh.nel, 144), Fc, inv

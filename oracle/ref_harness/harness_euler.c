@@ -291,6 +291,26 @@ int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const
     return its;
 }
 
+/* Block_scaling_EBE (its first block-diagonal set-up included) on caller
+ * blocks and F: A (144 per element) and F in place, inv_out the inverses. */
+int Block_scaling_EBE(ParametersType *, MatrixDataType *, FemStructsType *);
+void fr_eu_block_scale(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                       const int *ien, int neq, double *A, double *F, double *inv_out)
+{
+    fr_eu c;
+    static const double prm[6] = {1.4, 2.0, 1.0, 1e-8, 0.5, 1e-3};
+    int I;
+    fr_eu_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, prm);
+    memcpy(c.M.Aaux, A, sizeof(double) * 144 * (size_t)nel);
+    memcpy(c.S.F, F, sizeof(double) * ((size_t)neq + 1));
+    c.P.iterations = 0;
+    Block_scaling_EBE(&c.P, &c.M, &c.S);
+    memcpy(A, c.M.Aaux, sizeof(double) * 144 * (size_t)nel);
+    memcpy(F, c.S.F, sizeof(double) * ((size_t)neq + 1));
+    for (I = 0; I < nnodes; I++) memcpy(inv_out + 16L * I, c.M.invBlockDiag[I], 16 * sizeof(double));
+    fr_eu_free(&c);
+}
+
 /* Layout pin: the same sizes and offsets the drop-in shim reports for its
  * restated structs (parallel_fem_codes_gb300/compat/compat_block.c). */
 #include <stddef.h>

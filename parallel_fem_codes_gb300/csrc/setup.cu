@@ -297,12 +297,64 @@ __global__ void k_mul_sqrt(int n, const double *__restrict__ v, double *__restri
     if (i < n) x[i] *= sqrt(v[i]);
 }
 
+// Block_scaling_EBE's element part: Dirichlet rows and columns of the block
+// cleared with 1 on the diagonal (matrix_Bondary_Conditions), then each row
+// block of node v replaced by inv(v) times it (matrix_Scaling: sums from 0
+// in j order).  One thread per element; the block is read whole first.
+template <int B>
+__global__ void k_block_scale(int nel, int ld, int n, const int *__restrict__ gien, const int *__restrict__ node_dof,
+                              const double *__restrict__ ibd, double *__restrict__ A64)
+{
+    constexpr int S = 3 * B;
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    double m[S * S];
+    for (int q = 0; q < S * S; ++q) m[q] = A64[(size_t)q * ld + pos];
+    int J[3];
+    for (int v = 0; v < 3; ++v) J[v] = gien[(size_t)v * ld + pos];
+    for (int I = 0; I < B; ++I)
+        for (int v = 0; v < 3; ++v) {
+            if (node_dof[B * J[v] + I] != n) continue;
+            const int d = B * v + I;
+            for (int t = 0; t < S; ++t) { m[d * S + t] = 0.0; m[t * S + d] = 0.0; }
+            m[d * S + d] = 1.0;
+        }
+    for (int v = 0; v < 3; ++v) {
+        const double *iv = ibd + (size_t)B * B * J[v];
+        for (int i = 0; i < B; ++i)
+            for (int col = 0; col < S; ++col) {
+                double a = 0.0;
+                for (int j = 0; j < B; ++j) a += iv[i * B + j] * m[(B * v + j) * S + col];
+                A64[(size_t)((B * v + i) * S + col) * ld + pos] = a;
+            }
+    }
+}
+
 int scale_device(fg_system *s, int kind, double *F_dev, cudaStream_t st)
 {
     const Topology &t = s->topo;
     if (!s->blocks_ok) { set_error("scaling before element blocks were set"); return FG_ERR_STATE; }
-    if (kind != FG_SCALE_LEFT && kind != FG_SCALE_LEFTRIGHT) { set_error("unknown scaling"); return FG_ERR_ARG; }
+    if (kind != FG_SCALE_LEFT && kind != FG_SCALE_LEFTRIGHT && kind != FG_SCALE_BLOCK) {
+        set_error("unknown scaling"); return FG_ERR_ARG;
+    }
     int r;
+    if (kind == FG_SCALE_BLOCK) {
+        const int B = t.ndof;
+        if (B < 2 || B > 4) { set_error("block scaling needs ndof 2..4"); return FG_ERR_UNSUPPORTED; }
+        if ((r = precond_setup_device(s, FG_PRECOND_BLOCKDIAG, B == 4 ? FG_SETUP_REF_QUIRKS : 0, F_dev, st))) return r;
+        if (t.nel > 0) {
+            const dim3 g((t.nel + 63) / 64);
+            if (B == 2) k_block_scale<2><<<g, 64, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(), s->node_dof.as<int>(), s->ibd64.as<double>(), s->A64.as<double>());
+            else if (B == 3) k_block_scale<3><<<g, 64, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(), s->node_dof.as<int>(), s->ibd64.as<double>(), s->A64.as<double>());
+            else k_block_scale<4><<<g, 64, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(), s->node_dof.as<int>(), s->ibd64.as<double>(), s->A64.as<double>());
+            FG_CUDA(cudaGetLastError());
+            count_launches(1);
+        }
+        s->scale_kind = kind;
+        s->precond = FG_PRECOND_NONE;
+        s->csr_dirty = true;
+        return convert_blocks(s, st);
+    }
     if ((r = precond_setup_device(s, FG_PRECOND_DIAG, FG_SETUP_ACCUMULATE, F_dev, st))) return r;
     double *invd = s->invd64.as<double>();
     if (t.n > 0)                                      // invDiag[NEQ] = invDiag[NEQ - 1] (reference numbering)
@@ -317,6 +369,7 @@ int scale_device(fg_system *s, int kind, double *F_dev, cudaStream_t st)
         FG_CUDA(cudaGetLastError());
         count_launches(1);
     }
+    s->scale_kind = kind;
     s->precond = FG_PRECOND_NONE;                    // the scaled system is solved as it stands
     s->csr_dirty = true;
     return convert_blocks(s, st);
@@ -325,6 +378,7 @@ int scale_device(fg_system *s, int kind, double *F_dev, cudaStream_t st)
 int unscale_device(fg_system *s, double *x_dev, cudaStream_t st)
 {
     const int n = s->topo.n;
+    if (s->scale_kind == FG_SCALE_BLOCK) return FG_OK;   // NO_unscaling
     if (n > 0) k_mul_sqrt<<<(n + 255) / 256, 256, 0, st>>>(n, s->invd64.as<double>(), x_dev);
     FG_CUDA(cudaGetLastError());
     count_launches(1);

@@ -64,6 +64,7 @@ struct fg_system {
     // ILU(p) factor pattern (per row: L ascending, diagonal, U in the order
     // the symbolic pass admits it) and the slot of every CSR entry in it
     int ilu_p = 0, lu_nnz = 0;
+    int scale_kind = 0;                // last fg_scale kind (fg_unscale follows it)
     fg::DevMem lu_ia, lu_ja, lu_dg, lu_map, AAf64;
     fg::DevMem csr_ia, csr_ja, csr_diag, csr_inc_ptr, csr_inc, AA64, AA32, LU64, LU32, dinv64, dinv32, ilu_flags,
         ilu_ctr, ilu_tmp;   // ilu_tmp: output of the forward substitution (n_pad doubles)

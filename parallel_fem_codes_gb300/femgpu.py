@@ -16,7 +16,7 @@ from . import build as _build
 
 FG_OK = 0
 FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG, FG_PRECOND_ILU0, FG_PRECOND_SPIKE = 0, 1, 2, 3, 4
-FG_SCALE_LEFT, FG_SCALE_LEFTRIGHT = 1, 2
+FG_SCALE_LEFT, FG_SCALE_LEFTRIGHT, FG_SCALE_BLOCK = 1, 2, 3
 FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED, FG_PREC_MIXED16 = 64, 32, 16

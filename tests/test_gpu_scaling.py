@@ -52,3 +52,30 @@ def test_leftright_scaled_solve(fg):
     assert r.stats["converged"] == 1
     X = s.unscale(r.x)
     assert np.linalg.norm(X[:-1] - X0[:-1]) / np.linalg.norm(X0[:-1]) <= 1e-8
+
+
+def test_block_scaling_bit_exact_and_solve(fg):
+    """Block_scaling_EBE (Scaling "BlockScaling") on the device against the
+    oracle (pinned to the reference's Block_scaling_EBE): scaled blocks and
+    F bit-exact; the scaled system solves (no preconditioner) to the
+    solution of the BlockDiag-preconditioned one, and fg_unscale is the
+    identity."""
+    p = G.obliquo_problem(17)
+    m = p.mesh
+    u = p.initial_state() * (1.0 + 0.02 * np.random.default_rng(3).standard_normal(m.neq))
+    A, R = O.build_euler(p, u)
+    bd, ibd, Id, Fo = O.blockdiag_setup(m, A, R, ref_quirks=True)
+    As = O.block_scale(m, A, ibd)
+    s = fg.euler_system(p)
+    s.set_blocks(A)
+    Fg = s.scale(fg.FG_SCALE_BLOCK, R)
+    assert np.array_equal(s.get_blocks(), As.reshape(s.get_blocks().shape))
+    assert np.array_equal(Fg[:-1], Fo[:-1])
+    r = s.solve(Fg, tol=1e-12)
+    assert r.stats["converged"] == 1
+    assert np.array_equal(s.unscale(r.x)[:-1], r.x[:-1])
+    s2 = fg.euler_system(p)
+    s2.set_blocks(A)
+    F2 = s2.precond_setup(fg.FG_PRECOND_BLOCKDIAG, fg.FG_SETUP_REF_QUIRKS, R)
+    r2 = s2.solve(F2, tol=1e-12)
+    assert np.linalg.norm(r.x[:-1] - r2.x[:-1]) <= 1e-8 * np.linalg.norm(r2.x[:-1])

@@ -161,3 +161,18 @@ def test_dd_against_reference_build(oracle_lib):
     A0, R0 = O.ref_euler_build(p, u, du)
     A1, R1 = O.build_euler(p, u, du)
     assert np.array_equal(A0, A1) and np.array_equal(R0, R1)
+
+
+def test_block_scaling_against_reference(oracle_lib):
+    """Block_scaling_EBE restated (oracle/ebe_gmres.c) against the reference's
+    function called directly (the Euler driver installs it, never calls it)."""
+    if O.ref_euler() is None:
+        pytest.skip("reference build (oracle/_ref) not present")
+    for p in (G.obliquo_problem(9), G.obliquo_problem(7, dimensionless=False)):
+        m = p.mesh
+        u = p.initial_state() * (1.0 + 0.05 * np.random.default_rng(2).standard_normal(m.neq))
+        A, R = O.build_euler(p, u)
+        A1, F1, inv1 = O.ref_euler_block_scale(m, A, R)
+        bd, ibd, Id, Fo = O.blockdiag_setup(m, A, R, ref_quirks=True)
+        assert np.array_equal(inv1, ibd) and np.array_equal(F1, Fo)
+        assert np.array_equal(A1, O.block_scale(m, A, ibd))
