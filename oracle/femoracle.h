@@ -242,6 +242,11 @@ int or_tt_predictor(int nnodes, int nel, const double *x, const double *y, const
                     const or_time_opts *to, double solver_tol, int kmax, int lmax, double *u, double *a,
                     or_time_stats *st);
 
+/* h_shock_2sqrtArea (opt 0), h_shock_Option1 (1), h_shock_Option2 (2) of the
+ * transport drivers (oracle/sst.c). */
+double or_h_shock(int opt, double bx, double by, double u1, double u2, double u3, double y23, double y31,
+                  double y12, double x32, double x13, double x21, double Area);
+
 /* ---- assembled CSR path and ILU(0) (oracle/csr_ilu.c) ---- */
 int  or_csr_pattern(int nel, const int *ien, const int *type, const int *invp, int NEQ,
                     const int *Perm, const int *invPerm, int *IA, int *JA);

@@ -66,8 +66,8 @@ static double yzbeta(double *Re_old, double *delta_old, int e, double bx, double
 /* h_shock_calculation: 2sqrtArea (0, h_shock_2sqrtArea.c), Option1 (1,
  * h_shock_Option1.c:3-19, from grad u) or Option2 (2, h_shock_Option2.c:3-16,
  * from the velocity). */
-static double h_shock(int opt, double bx, double by, double u1, double u2, double u3, double y23, double y31,
-                      double y12, double x32, double x13, double x21, double Area)
+double or_h_shock(int opt, double bx, double by, double u1, double u2, double u3, double y23, double y31,
+                  double y12, double x32, double x13, double x21, double Area)
 {
     if (opt == 1) {
         double P1 = fabs(u1*y23*y23 + u2*y31*y23 + u3*y12*y23 + u1*x32*x32 + u2*x13*x32 + u3*x21*x32);
@@ -119,7 +119,7 @@ static void dd_element(double kx, double ky, double bx, double by, double gamma,
     double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
     double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
     double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
-    double h = h_shock(hopt, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+    double h = or_h_shock(hopt, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
     double Eu = 0.0;
     if (shock == 3)
         Eu = yzbeta(Re_old, delta_old, e, bx, by, gamma, ue[0], ue[1], ue[2], ueb, feb, y23, y31, y12, x32, x13,
@@ -227,7 +227,7 @@ void or_build_k_f_supg(int nnodes, int nel, const double *x, const double *y,
         double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
         double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
         double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
-        double hs = h_shock(prob->h_shock, bx, by, ue1, ue2, ue3, y23, y31, y12, x32, x13, x21, Area);
+        double hs = or_h_shock(prob->h_shock, bx, by, ue1, ue2, ue3, y23, y31, y12, x32, x13, x21, Area);
         double Eu = prob->cau == 3 ? yzbeta(Re_old, delta_old, E, bx, by, gamma, ue1, ue2, ue3, ueb, feb,
                                             y23, y31, y12, x32, x13, x21, invArea, hs)
                   : prob->cau ? cau(kx, ky, bx, by, gamma, ue1, ue2, ue3, ueb, feb,

@@ -48,11 +48,26 @@ static double tt_cau(double kx, double ky, double bx, double by, double gamma, d
     return 0;
 }
 
+/* YZBeta_ShockCapture of the transient driver (no state; Ru includes du/dt) */
+static double tt_yzbeta(double bx, double by, double gamma, double ue1, double ue2, double ue3, double ueb,
+                        double dueb, double feb, double y23, double y31, double y12, double x32, double x13,
+                        double x21, double invArea, double h)
+{
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = dueb + bgu + gamma*ueb - feb;
+    double nRu = fabs(Ru);
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    double nu = fabs(ueb);
+    return (nu >= 1e-12 && ng >= 1e-12) ? 0.25*h*nRu/ng + 0.125*h*h*nRu/nu : 0;
+}
+
 /* Build_M_K_R_DD.c:61-180 for one element: Ae (row-major), the load term
  * Fr[i] added to R[lm[i]] and the three terms sub[i][j] then subtracted. */
 static void tt_dd_element(double kx, double ky, double bx, double by, double gamma, double fv, const double X[3],
                           const double Y[3], const double ue[3], const double due[3], double alpha, double dt,
-                          int shock, double *cbtilo, int e, double Ae[9], double Fr[3], double sub[3][3])
+                          int shock, int hopt, double *cbtilo, int e, double Ae[9], double Fr[3], double sub[3][3])
 {
     const double third = 1.0/3.0, sixth = 1.0/6.0, seventh = 1.0/7.0, twelfth = 1.0/12.0;
     const double t320 = 3./20.0, n920 = 9./20.0, n940 = 9./40.0, w = 0.5;
@@ -73,14 +88,20 @@ static void tt_dd_element(double kx, double ky, double bx, double by, double gam
     double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
     double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
     double Eu = 0.0;
-    if (shock == 2) {           /* CAU_DD_ShockCapture with du/dt, h_shock_2sqrtArea, relaxed */
-        double h = sqrt(fabs(2*Area));
-        double bgu = 0.5*invArea*(ue[0]*(bx*y23 + by*x32) + ue[1]*(bx*y31 + by*x13) + ue[2]*(bx*y12 + by*x21));
-        double Ru = dueb + bgu + gamma*ueb - feb;
-        double gx = 0.5*invArea*(y23*ue[0] + y31*ue[1] + y12*ue[2]);
-        double gy = 0.5*invArea*(x32*ue[0] + x13*ue[1] + x21*ue[2]);
-        double ng = sqrt(gx*gx + gy*gy);
-        double cbtil = ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0;
+    if (shock == 2 || shock == 3) {   /* CAUDD or YZBeta (Ru with du/dt), relaxed */
+        double h = or_h_shock(hopt, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+        double cbtil;
+        if (shock == 3) {
+            cbtil = tt_yzbeta(bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb, y23, y31, y12, x32, x13, x21,
+                              invArea, h);
+        } else {
+            double bgu = 0.5*invArea*(ue[0]*(bx*y23 + by*x32) + ue[1]*(bx*y31 + by*x13) + ue[2]*(bx*y12 + by*x21));
+            double Ru = dueb + bgu + gamma*ueb - feb;
+            double gx = 0.5*invArea*(y23*ue[0] + y31*ue[1] + y12*ue[2]);
+            double gy = 0.5*invArea*(x32*ue[0] + x13*ue[1] + x21*ue[2]);
+            double ng = sqrt(gx*gx + gy*gy);
+            cbtil = ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0;
+        }
         double cb = w*cbtil + (1 - w)*cbtilo[e];
         cbtilo[e] = cbtil;
         Eu = cb;
@@ -141,7 +162,7 @@ void or_build_tt(int nnodes, int nel, const double *x, const double *y, const in
             const double uv[3] = { U[J1], U[J2], U[J3] }, dv[3] = { dU[J1], dU[J2], dU[J3] };
             double Ae[9], Fr[3], sub[3][3];
             tt_dd_element(kx, ky, prob->beta[0], prob->beta[1], gamma, prob->f, Xv, Yv, uv, dv, alpha, dt,
-                          prob->cau, cbtilo, E, Ae, Fr, sub);
+                          prob->cau, prob->h_shock, cbtilo, E, Ae, Fr, sub);
             const int lm[3] = { type[J1] == 0 ? neq : invp[J1], type[J2] == 0 ? neq : invp[J2],
                                 type[J3] == 0 ? neq : invp[J3] };
             for (int i = 0; i < 3; i++) {            /* Build_M_K_R_DD.c:161-176 */
@@ -182,8 +203,10 @@ void or_build_tt(int nnodes, int nel, const double *x, const double *y, const in
         double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
         double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
         double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
-        double hs = sqrt(fabs(2*Area));
-        double Eu = prob->cau ? tt_cau(kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb,
+        double hs = or_h_shock(prob->h_shock, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+        double Eu = prob->cau == 3 ? tt_yzbeta(bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb, y23, y31, y12,
+                                               x32, x13, x21, invArea, hs)
+                  : prob->cau ? tt_cau(kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb,
                                        y23, y31, y12, x32, x13, x21, invArea, hs) : 0.0;
         double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
         double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);

@@ -691,6 +691,21 @@ __device__ double tt_cau_eu(double kx, double ky, double bx, double by, double g
     return 0;
 }
 
+// YZBeta_ShockCapture of the transient driver: no state, Ru includes du/dt
+__device__ double tt_yz_eu(double bx, double by, double gamma, double ue1, double ue2, double ue3, double ueb,
+                           double dueb, double feb, double y23, double y31, double y12, double x32, double x13,
+                           double x21, double invArea, double h)
+{
+    double bgu = 0.5*invArea*(ue1*(bx*y23 + by*x32) + ue2*(bx*y31 + by*x13) + ue3*(bx*y12 + by*x21));
+    double Ru = dueb + bgu + gamma*ueb - feb;
+    double nRu = fabs(Ru);
+    double gx = 0.5*invArea*(y23*ue1 + y31*ue2 + y12*ue3);
+    double gy = 0.5*invArea*(x32*ue1 + x13*ue2 + x21*ue3);
+    double ng = sqrt(gx*gx + gy*gy);
+    double nu = fabs(ueb);
+    return (nu >= 1e-12 && ng >= 1e-12) ? 0.25*h*nRu/ng + 0.125*h*h*nRu/nu : 0.0;
+}
+
 __global__ void k_tt_elem(int nel, int ld, const int *__restrict__ gien, const double *__restrict__ gx,
                           const double *__restrict__ gy, const int *__restrict__ gtype,
                           const int *__restrict__ node_dof, const double *__restrict__ up,
@@ -739,8 +754,10 @@ __global__ void k_tt_elem(int nel, int ld, const int *__restrict__ gien, const d
     double Rpg11 = sixth*tau*gamma*(bx*y23 + by*x32);
     double Rpg21 = sixth*tau*gamma*(bx*y31 + by*x13);
     double Rpg31 = sixth*tau*gamma*(bx*y12 + by*x21);
-    double hs = sqrt(fabs(2*Area));
-    double Eu = cf.cau ? tt_cau_eu(kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb, y23, y31, y12, x32,
+    double hs = h_shock_dev(cf.h_shock, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+    double Eu = cf.cau == FG_SHOCK_YZBETA ? tt_yz_eu(bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb, y23, y31, y12,
+                                                    x32, x13, x21, invArea, hs)
+              : cf.cau ? tt_cau_eu(kx, ky, bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb, y23, y31, y12, x32,
                                    x13, x21, invArea, hs) : 0.0;
     double Csc12 = Eu*0.25*invArea*(y23*y31 + x32*x13);
     double Csc13 = Eu*0.25*invArea*(y23*y12 + x32*x21);
@@ -823,14 +840,19 @@ __global__ void k_tt_dd_elem(int nel, int ld, const int *__restrict__ gien, cons
     double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
     double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
     double Eu = 0.0;
-    if (cf.cau == FG_SHOCK_CAUDD) {
-        double h = sqrt(fabs(2*Area));
-        double bgu = 0.5*invArea*(ue[0]*(bx*y23 + by*x32) + ue[1]*(bx*y31 + by*x13) + ue[2]*(bx*y12 + by*x21));
-        double Ru = dueb + bgu + gamma*ueb - feb;
-        double gxu = 0.5*invArea*(y23*ue[0] + y31*ue[1] + y12*ue[2]);
-        double gyu = 0.5*invArea*(x32*ue[0] + x13*ue[1] + x21*ue[2]);
-        double ng = sqrt(gxu*gxu + gyu*gyu);
-        double cbtil = ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0.0;
+    if (cf.cau == FG_SHOCK_CAUDD || cf.cau == FG_SHOCK_YZBETA) {
+        double h = h_shock_dev(cf.h_shock, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+        double cbtil;
+        if (cf.cau == FG_SHOCK_YZBETA) {
+            cbtil = tt_yz_eu(bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
+        } else {
+            double bgu = 0.5*invArea*(ue[0]*(bx*y23 + by*x32) + ue[1]*(bx*y31 + by*x13) + ue[2]*(bx*y12 + by*x21));
+            double Ru = dueb + bgu + gamma*ueb - feb;
+            double gxu = 0.5*invArea*(y23*ue[0] + y31*ue[1] + y12*ue[2]);
+            double gyu = 0.5*invArea*(x32*ue[0] + x13*ue[1] + x21*ue[2]);
+            double ng = sqrt(gxu*gxu + gyu*gyu);
+            cbtil = ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0.0;
+        }
         double cb = w*cbtil + (1 - w)*cbtilo[pos];
         cbtilo[pos] = cbtil;
         Eu = cb;
@@ -899,14 +921,15 @@ int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev,
     if (t.ndof != 1) { set_error("transient transport assembly needs ndof == 1"); return FG_ERR_UNSUPPORTED; }
     if (!s->geometry_ok) { set_error("transient transport assembly before fg_set_geometry"); return FG_ERR_STATE; }
     const bool dd = c->c.form == FG_TRANSPORT_DD;
-    if (c->c.h_shock != FG_HSHOCK_2SQRTAREA ||
-        (dd ? (c->c.cau != FG_SHOCK_NONE && c->c.cau != FG_SHOCK_CAUDD)
-            : (c->c.form != FG_TRANSPORT_SUPG || c->c.cau < FG_SHOCK_NONE || c->c.cau > FG_SHOCK_CAU))) {
-        set_error("transient transport builds SUPG with CAU or none, or DD with CAUDD or none (h_shock 2sqrtArea)");
+    if (c->c.h_shock < FG_HSHOCK_2SQRTAREA || c->c.h_shock > FG_HSHOCK_OPTION2 ||
+        (dd ? (c->c.cau != FG_SHOCK_NONE && c->c.cau != FG_SHOCK_CAUDD && c->c.cau != FG_SHOCK_YZBETA)
+            : (c->c.form != FG_TRANSPORT_SUPG || c->c.cau == FG_SHOCK_CAUDD || c->c.cau < FG_SHOCK_NONE ||
+               c->c.cau > FG_SHOCK_YZBETA))) {
+        set_error("transient transport builds SUPG with CAU, YZBeta or none, or DD with CAUDD, YZBeta or none");
         return FG_ERR_UNSUPPORTED;
     }
     double *cbtilo = nullptr;
-    if (dd && c->c.cau == FG_SHOCK_CAUDD) {   // delta_old of the time loop, zero at its start
+    if (dd && (c->c.cau == FG_SHOCK_CAUDD || c->c.cau == FG_SHOCK_YZBETA)) {   // delta_old of the time loop, zero at its start
         int r0;
         if (s->shock_state.bytes < 16 * (size_t)s->nel_pad && (r0 = s->shock_state.alloc(16 * (size_t)s->nel_pad)))
             return r0;

@@ -108,3 +108,36 @@ def test_tt_dd_predictor(fg):
     assert st["steps"] == sto["steps"] == 8
     assert st["corrections"] == sto["corrections"]
     assert rel(ug, uo) < 1e-8
+
+
+@pytest.mark.parametrize("form,hs", [(0, 0), (0, 1), (0, 2), (1, 0), (1, 1), (1, 2)],
+                         ids=["supg-2sqrtA", "supg-opt1", "supg-opt2", "dd-2sqrtA", "dd-opt1", "dd-opt2"])
+def test_tt_yzbeta_h_shock_bit_exact(fg, form, hs):
+    """YZBeta_ShockCapture (Ru with du/dt) with each h_shock option, in the
+    SUPG and the DD transient builds (DD relaxed against the element's
+    previous coefficient: zero on a fresh system), against the oracle."""
+    p = G.transport_problem(33, angle_deg=50.0, k=1e-3, gamma=0.2, f=0.5, cau=fg.FG_SHOCK_YZBETA)
+    p.form, p.h_shock = form, hs
+    rng = np.random.default_rng(11 + hs)
+    u = rng.random(p.mesh.neq)
+    du = rng.standard_normal(p.mesh.neq)
+    A0, R0 = O.build_tt(p, 0.5, 0.05, u=u, du=du)
+    s = fg.transport_system(p)
+    R = s.tt_assemble(p, 0.5, 0.05, u, du)
+    assert np.array_equal(R[:-1], R0[:-1]) and R[-1] == 0.0
+    assert np.array_equal(s.get_blocks(), A0)
+
+
+def test_tt_yzbeta_dd_predictor(fg):
+    """The DD time loop with YZBeta (relaxed state on the device) against
+    the oracle's."""
+    p = G.transport_problem(33, angle_deg=30.0, k=1e-3, f=0.0, cau=fg.FG_SHOCK_YZBETA)
+    p.form, p.h_shock = fg.FG_TRANSPORT_DD, 2
+    to_o = O.TimeOpts(0, 2, 1e-3, 0, 6 * 0.02, 1e-6, 0)
+    uo, ao, sto = O.tt_predictor(p, 0.5, 0.02, to_o, tol=1e-10, kmax=30)
+    s = fg.transport_system(p)
+    to = fg.time_opts(0, 2, 1e-3, 0, 6 * 0.02, 1e-6, precond=fg.FG_PRECOND_DIAG, setup_flags=0)
+    ug, ag, st = s.tt_predictor(p, 0.5, 0.02, to, kmax=30, tol=1e-10)
+    assert st["steps"] == sto["steps"] == 6
+    assert st["corrections"] == sto["corrections"]
+    assert rel(ug, uo) < 1e-8

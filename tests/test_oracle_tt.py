@@ -99,3 +99,30 @@ def test_tt_dd_caudd_state_and_loop(oracle_lib):
     uo, ao, st = O.tt_predictor(p, 0.5, 0.5, O.TimeOpts(1, 5, 1e-8, 1, 1e4, 1e-9, 0), tol=1e-12)
     Us, nl, its = O.transport_process(p, 1e-12, 1e-8, 30, 1000)
     assert np.linalg.norm(uo - Us) <= 1e-5 * np.linalg.norm(Us)
+
+
+@pytest.mark.parametrize("hs", [0, 1, 2])
+def test_tt_yzbeta_pinned_through_steady_yzbeta(oracle_lib, hs):
+    """YZBeta_ShockCapture of the transient driver (no state, Ru with du/dt)
+    against the steady driver's (reference-pinned; relaxed with w = 1/2 on a
+    fresh state): at du = 0 the transient shock coefficient is twice the
+    steady first-build one, so the shock part of the stiffness doubles, for
+    each h_shock option.  Two transient builds at the same state agree
+    bit-for-bit (no state)."""
+    u = np.random.default_rng(7).random(G.transport_problem(13).mesh.neq)
+
+    def stiff(cau):
+        p = G.transport_problem(13, angle_deg=40.0, k=1e-3, gamma=0.2, f=0.5, cau=cau)
+        p.h_shock = hs
+        A1, _ = O.build_tt(p, 0.5, 0.1, u=u)
+        A2, _ = O.build_tt(p, 0.5, 0.05, u=u)
+        A1b, _ = O.build_tt(p, 0.5, 0.1, u=u)
+        assert np.array_equal(A1, A1b)
+        Ass, _ = O.build_k_f_supg(p, u=u)
+        return (A1 - A2) / (0.5 * (0.1 - 0.05)), Ass
+
+    ke3, ks3 = stiff(3)
+    ke0, ks0 = stiff(0)
+    shock_tt, shock_ss = ke3 - ke0, ks3 - ks0
+    assert np.abs(shock_ss).max() > 0
+    assert np.allclose(shock_tt, 2 * shock_ss, rtol=1e-7, atol=1e-9 * np.abs(ke0).max())
