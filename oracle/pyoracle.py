@@ -13,19 +13,29 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libfemoracle.so")
+# the same restatement built with the reference's -Ofast -march=native: the
+# timed CPU baseline only (never a checker)
+ORACLE_FAST_SO = os.path.join(HERE, "_build", "libfemoracle_fast.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_sst.so")
 REF_NS_SO = os.path.join(HERE, "_ref", "libref_ns.so")
 REF_EU_SO = os.path.join(HERE, "_ref", "libref_euler.so")
-REF_SRC = "/root/reference"
+# The reference's source tree (used only to build the checker): the
+# PFC_REFERENCE_DIR environment variable, else `reference` beside this
+# repository.
+REF_SRC = os.environ.get("PFC_REFERENCE_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
+_use_fast = False
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 _f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
 _c_int, _c_dbl = ctypes.c_int, ctypes.c_double
 
 
-def build(ref: bool | None = None) -> None:
-    """Compile the restatement, and the reference build when its sources exist."""
+def build(ref: bool | None = None, fast: bool = False) -> None:
+    """Compile the restatement, and the reference build when its sources exist.
+    fast: also the -Ofast -march=native timing build of the restatement."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if fast:
+        subprocess.run(["make", "-s", "-C", HERE, "fast"], check=True)
     if ref is None:
         ref = os.path.isdir(REF_SRC)
     if ref:
@@ -36,12 +46,23 @@ _lib = None
 _ref = None
 
 
+def use_fast_build() -> None:
+    """Load the -Ofast -march=native build of the restatement instead of the
+    checker build (timed CPU baseline only; call before the first oracle
+    call of the process)."""
+    global _use_fast
+    if _lib is not None:
+        raise RuntimeError("oracle library already loaded")
+    _use_fast = True
+
+
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(ORACLE_SO):
-            build(ref=False)
-        L = ctypes.CDLL(ORACLE_SO)
+        so = ORACLE_FAST_SO if _use_fast else ORACLE_SO
+        if not os.path.exists(so):
+            build(ref=False, fast=_use_fast)
+        L = ctypes.CDLL(so)
         L.or_mesh_structured.argtypes = [_c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _f64p, _f64p, _i32p]
         L.or_fill_lm.argtypes = [_c_int, _c_int, _i32p, _i32p, _i32p, _c_int, _i32p]
         L.or_fill_lm.restype = None

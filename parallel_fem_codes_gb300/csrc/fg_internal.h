@@ -50,6 +50,16 @@ struct Topology {
     std::vector<unsigned short> pt_col;  // npatch * kPatchColStride local colour offsets
     std::vector<int> dofs;       // patch-local dof -> internal dof, bit 31 = shared with another patch
     std::vector<unsigned short> lm16;    // nel*S local indices (internal order), 0xFFFF = sink
+    // x segment of each patch: its dofs lie in [xlo, xlo + xlen) (xlo and
+    // xlen multiples of 8, xlen <= kPatchXCap); lmx16: per element vertex
+    // its dof's position in that segment (0xFFFF = sink), for the matvec
+    // that copies the segment whole instead of gathering x dof by dof
+    std::vector<int> pt_xlo, pt_xlen;
+    std::vector<unsigned short> lmx16;
+    // 3x3: per patch one 16-byte aligned index blob (x-segment positions
+    // [3][W], dof list, incidence lists) at byte offset pt_boff[p]
+    std::vector<long long> pt_boff;
+    std::vector<unsigned char> blob;
     std::vector<int> pc_ptr, pc_list;    // patches grouped by patch colour
     // per-patch incidence lists: for patch p, at incl[pt_inc[p]] the list
     // starts (pnd + 1 entries) of each local dof, then the staged product
@@ -118,6 +128,7 @@ struct MvSmem {
     }
 };
 inline size_t mv_smem_bytes(int S, int maxdof, int w) { return MvSmem(S, maxdof, w).total; }
+constexpr int kPatchXCap = 1792;       // largest x segment of a 3x3 patch (entries)
 constexpr int kPatchMaxLocalColours = 16;
 constexpr int kPatchColStride = kPatchMaxLocalColours + 1;
 
@@ -167,6 +178,7 @@ struct SysDev {
     const unsigned short *pt_col;
     const int *pt_inc;                 // per-patch incidence lists (3x3 matvec)
     const unsigned short *incl;
+    const unsigned char *blob;         // per-patch index blobs (3x3 bulk-copy matvec)
     int maxdof;
     // assembled CSR operator and ILU(0) (op == 1)
     int op, csr_w;
@@ -210,6 +222,11 @@ constexpr int kPartStride = 64;    // doubles per part (>= kmax + 2, kmax <= 60)
 __host__ __device__ constexpr bool precond_separate(int p) { return p >= 2; }
 
 struct EChunk { int sys, e0, e1; };
+// One 3x3 patch of a batched matvec launch for the bulk-copy pipeline:
+// system, first element, index-blob offset (16-byte units) and size
+// (bytes), x segment start, and packed counts (elements | dofs << 16,
+// incidence entries | x segment length << 16).
+struct alignas(32) MvRec { int sys, pe0, boff16, bsize, xlo, pn, nx, pad; };
 struct DChunk { int sys, part, d0, d1; };
 struct NChunk { int sys, n0, n1; };
 

@@ -314,6 +314,11 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
         const int pd0 = D.pt_dof[p], pnd = D.pt_dof[p + 1] - pd0;
         const int i0 = D.pt_inc[p], ni = D.pt_inc[p + 1] - i0;
         const int head = (pnd + 1 + 7) & ~7;
+        const int W = (pne + 15) & ~15;       // staged product row (FP32 blocks: blocked row) length
+        // FP64 blocks are [entry][element]; FP32 blocks of a patch are one
+        // block [entry][W] at 9 pe0
+        const TA *Ap = sizeof(TA) == 8 ? A + pe0 : A + 9 * (size_t)pe0;
+        const size_t lda = sizeof(TA) == 8 ? ld : (size_t)W;
         int dv[DMAX];
 #pragma unroll
         for (int u = 0; u < DMAX; ++u) {
@@ -328,7 +333,7 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
 #pragma unroll
             for (int a = 0; a < 3; ++a) li[u][a] = __ldcs(D.lm16 + a * ld + pe0 + q);
 #pragma unroll
-            for (int m = 0; m < 9; ++m) av[u][m] = ldst(A + m * ld + pe0 + q);
+            for (int m = 0; m < 9; ++m) av[u][m] = ldst(Ap + m * lda + q);
         }
         __syncthreads();                      // the previous patch is done with shared memory
         for (int t = threadIdx.x; t < ni / 8; t += kThreads) cp_async16(ic + 8 * t, D.incl + i0 + 8 * t);
@@ -350,7 +355,7 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
                 TA acc = av[u][3 * r] * xv[0];
                 acc += av[u][3 * r + 1] * xv[1];
                 acc += av[u][3 * r + 2] * xv[2];
-                ye[r * PE + q] = acc;
+                ye[r * W + q] = acc;
             }
         }
         cp_async_wait_all();
@@ -367,6 +372,262 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
             if (dd < 0) atomicAdd(Y + d, (TY)v);          // shared dof: reduction store
             else Y[d] = (TY)v;
         }
+    }
+}
+
+// ---------------------------------------------------------------- 3x3 matvec, bulk-copy pipeline
+// The FP32-block 3x3 matvec of the batched engine as a warp-specialised
+// pipeline, one CTA of 1024 threads per SM.  Warp 0 is the producer: for
+// each patch of its CTA it waits until a stage of the three-stage
+// shared-memory ring is free, then one lane copies into it, with 1-D bulk
+// copies (cp.async.bulk, completion counted on the stage's "full"
+// mbarrier), everything the patch needs: its nine block rows, the three
+// rows of x-segment positions of its elements' vertices, its dof list and
+// incidence lists, and x itself -- the dofs of a patch lie in one short
+// segment of x (one contiguous band in the RCM numbering), so x arrives
+// as one copy instead of a dof-by-dof gather.  Warps 1..31 consume the
+// patches in order, with no global loads:
+//   products   each thread forms its elements' three row products from the
+//              staged blocks and x, and writes them over the first three
+//              block rows of its own elements (slots it alone reads);
+//   sums       the thread that owns a dof adds the products listed for it,
+//              in the fixed order of its incidence list, and writes it once
+//              (plain store, or red.add for a dof shared with patches of
+//              other colours, which run in other launches);
+// so each dof gets the same sum, in the same order, as in k_ebe_mv3.  The
+// consumers then release the stage on its "empty" mbarrier.
+// Every mbarrier wait is bounded (kMbarWaitCycles, ~2 s).  A consumer wait
+// that runs out marks the patch's system FG_ERR_TIMEOUT, stops the
+// producer, waits (bounded) for the copies in flight and ends the CTA; the
+// producer gives up on a free stage the same way.
+constexpr int kMv3pThreads = 1024;
+constexpr int kMv3pStages = 3;
+constexpr int kMv3pConsumers = kMv3pThreads - 32 * kMv3pStages;
+constexpr int kMv3pDofCap = 1536;                       // dofs per patch (the patch cap)
+constexpr int kMv3pIncCap = ((kMv3pDofCap + 1 + 7) / 8) * 8 + 3 * patch_elems(3);
+constexpr long long kMbarWaitCycles = 4000000000LL;     // ~2 s at 2 GHz
+// per-stage facts the producer leaves for the consumers (pne < 0: no patch)
+struct Mv3pMeta {
+    int pne, pnd, n, sys;
+    void *Y;
+    float vsci;
+    int W;             // block row / staged product row length (pne rounded up to 16)
+};
+template <typename TX>
+struct Mv3pSmem {
+    static constexpr int PE = patch_elems(3);
+    static constexpr size_t a = 0;                                   // [9][W] float, W <= PE
+    static constexpr size_t b = a + 9 * (size_t)PE * 4;              // index blob: [3][W] ushort, dofs, incidence
+    static constexpr size_t x = b + 6 * (size_t)PE + 4 * (size_t)kMv3pDofCap + 2 * (size_t)kMv3pIncCap;
+    static constexpr size_t meta = (x + (size_t)kPatchXCap * sizeof(TX) + 15) / 16 * 16;
+    static constexpr size_t stage = (meta + sizeof(Mv3pMeta) + 127) / 128 * 128;
+    static constexpr size_t full = kMv3pStages * stage;             // kMv3pStages mbarriers
+    static constexpr size_t empty = full + 8 * kMv3pStages;          // kMv3pStages mbarriers
+    static constexpr size_t abort = empty + 8 * kMv3pStages;         // consumers gave up
+    static constexpr size_t total = abort + 16;
+    static_assert(total <= 227 * 1024, "3x3 pipeline exceeds shared memory");
+    static_assert(x % 16 == 0, "x segment must stay 16-byte aligned");
+};
+static_assert(patch_elems(3) % 16 == 0, "patch rows must stay 16-byte aligned");
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(unsigned dst, const void *src, unsigned bytes, unsigned bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n"
+                 ::"r"(dst), "l"(src), "r"(bytes), "r"(bar) : "memory");
+}
+// true when the phase with this parity has completed; false after ~2 s
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    const long long t0 = clock64();
+    for (;;) {
+        unsigned ok;
+        asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+                     " selp.u32 %0, 1, 0, p;\n}\n" : "=r"(ok) : "r"(bar), "r"(parity) : "memory");
+        if (ok) return true;
+        if (clock64() - t0 > kMbarWaitCycles) return false;
+    }
+}
+// barrier 1 over the consumer warps only; returns true in every consumer
+// thread when any of them passed true
+__device__ __forceinline__ bool consumers_sync_or(bool v)
+{
+    unsigned r;
+    asm volatile("{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.or.pred q, 1, %2, p;\n"
+                 " selp.u32 %0, 1, 0, q;\n}\n" : "=r"(r) : "r"((unsigned)v), "n"(kMv3pConsumers) : "memory");
+    return r != 0;
+}
+__device__ __forceinline__ void consumers_sync()
+{
+    asm volatile("bar.sync 1, %0;\n" ::"n"(kMv3pConsumers) : "memory");
+}
+// a staged x entry in FP32 (an FP16 basis vector is stored as sigma v)
+template <typename TX> __device__ __forceinline__ float staged_x(TX v, float vsci)
+{
+    if constexpr (std::is_same<TX, __half>::value) return __half2float(v) * vsci;
+    else return (float)v;
+}
+
+template <typename TX, typename TY>
+__global__ void __launch_bounds__(kMv3pThreads, 1)
+k_ebe_mv3p(const SysDev *__restrict__ sys, const MvRec *__restrict__ rec, const int *__restrict__ nch,
+           int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out)
+{
+    extern __shared__ __align__(128) unsigned char mv3p_smem[];
+    using L = Mv3pSmem<TX>;
+    using TA = float;
+    constexpr int NC = kMv3pConsumers, ST = kMv3pStages;
+    constexpr unsigned short kSink = 0xFFFF;
+    volatile int *s_abort = reinterpret_cast<volatile int *>(mv3p_smem + L::abort);
+    const unsigned full0 = smem_u32(mv3p_smem + L::full), empty0 = smem_u32(mv3p_smem + L::empty);
+    const int total = *nch;
+    const int tid = threadIdx.x;
+
+    if (tid == 0) {
+        for (int s = 0; s < ST; ++s) {
+            mbar_init(full0 + 8u * s, 1);
+            mbar_init(empty0 + 8u * s, 1);
+            reinterpret_cast<Mv3pMeta *>(mv3p_smem + s * L::stage + L::meta)->sys = 0;
+        }
+        *s_abort = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+
+    // ------------------------------------------------ producers (warps 0..ST-1)
+    // Producer warp w fills stage w with the CTA's patches k = w, w + ST,
+    // ...: it waits until the consumers released the stage, then lane 0
+    // arms the stage's full barrier and issues the patch's three bulk
+    // copies (blocks, index blob, x segment).  The next patch's record and
+    // system fields are loaded before the wait, so they overlap it.  A
+    // patch whose system is gated off is passed as an empty stage; past the
+    // CTA's last patch the producer leaves an end marker and stops.
+    if (tid < 32 * ST) {
+        if (tid & 31) return;
+        const int w = tid >> 5, s = w;
+        unsigned char *stg = mv3p_smem + s * L::stage;
+        Mv3pMeta *meta = reinterpret_cast<Mv3pMeta *>(stg + L::meta);
+        const unsigned full = full0 + 8u * s;
+        for (int k = w;; k += ST) {
+            const long long c = blockIdx.x + (long long)k * gridDim.x;
+            const bool have = c < total;
+            MvRec r = have ? rec[c] : MvRec{};
+            const SysDev &D = sys[r.sys];
+            const bool live = have && gated(D, gate);
+            const int pne = r.pn & 0xFFFF, pnd = r.pn >> 16, xlen = r.nx >> 16;
+            const int W = (pne + 15) & ~15;
+            const TX *X = in_sel == 0 ? (const TX *)D.x
+                        : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+            void *Y = out_sel == 0 ? (void *)D.t64 : out_sel == 1 ? (void *)D.t : (void *)aux_out;
+            const int n = D.n;
+            const float vsci = D.vsci;
+            const TA *A = D.A32 + 9 * (size_t)r.pe0;
+            const unsigned char *blob = D.blob + 16 * (size_t)r.boff16;
+            if (k >= ST && !mbar_wait(empty0 + 8u * s, (unsigned)((k / ST - 1) & 1))) return;
+            if (*s_abort) return;
+            if (!have) {                                   // end of this CTA's patches
+                meta->pne = -1;
+                mbar_arrive(full);
+                return;
+            }
+            meta->sys = r.sys;
+            if (!live) {                                   // gated off: nothing to do
+                meta->pne = 0;
+                meta->pnd = 0;
+                mbar_arrive(full);
+                continue;
+            }
+            const unsigned ra = 9u * (unsigned)W * 4u, rb = (unsigned)r.bsize;
+            const unsigned rx = (unsigned)xlen * (unsigned)sizeof(TX);
+            meta->pne = pne;
+            meta->pnd = pnd;
+            meta->n = n;
+            meta->Y = Y;
+            meta->vsci = vsci;
+            meta->W = W;
+            mbar_expect_tx(full, ra + rb + rx);
+            bulk_g2s(smem_u32(stg + L::a), A, ra, full);
+            bulk_g2s(smem_u32(stg + L::b), blob, rb, full);
+            bulk_g2s(smem_u32(stg + L::x), X + r.xlo, rx, full);
+        }
+    }
+
+    // ------------------------------------------------ consumers (warps ST..31)
+    const int ct = tid - 32 * ST;
+    for (int j = 0;; ++j) {
+        const int s = j % ST;
+        unsigned char *stg = mv3p_smem + s * L::stage;
+        const Mv3pMeta *meta = reinterpret_cast<const Mv3pMeta *>(stg + L::meta);
+        const bool ok = mbar_wait(full0 + 8u * s, (unsigned)((j / ST) & 1));
+        const int pne = ok ? meta->pne : 0;
+        const int W = meta->W;
+        TA *sa = reinterpret_cast<TA *>(stg + L::a);
+        const unsigned short *sl = reinterpret_cast<const unsigned short *>(stg + L::b);
+        const TX *sx = reinterpret_cast<const TX *>(stg + L::x);
+        const float vsci = meta->vsci;
+        // products over the block rows 0..2 of the element's own slots
+        for (int q = ct; q < pne; q += NC) {
+            TA av[9], xv[3];
+#pragma unroll
+            for (int m = 0; m < 9; ++m) av[m] = sa[m * W + q];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const unsigned short li = sl[a * W + q];
+                xv[a] = li == kSink ? (TA)0 : staged_x(sx[li], vsci);
+            }
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+                TA acc = av[3 * r] * xv[0];
+                acc += av[3 * r + 1] * xv[1];
+                acc += av[3 * r + 2] * xv[2];
+                sa[r * W + q] = acc;
+            }
+        }
+        if (consumers_sync_or(!ok)) {
+            // give up: record the timeout, stop the producer, wait (bounded)
+            // for the copies that may be in flight into the stages
+            if (ct == 0) {
+                *s_abort = 1;
+                SysState *st = sys[meta->sys].st;         // 0 until the stage was first filled
+                st->status = FG_ERR_TIMEOUT;
+                st->live = 0;
+                for (int q = j; q < j + ST; ++q) mbar_wait(full0 + 8u * (q % ST), (unsigned)((q / ST) & 1));
+            }
+            return;
+        }
+        if (pne < 0) break;                               // no more patches
+        const int pnd = meta->pnd, n = meta->n;
+        TY *Y = reinterpret_cast<TY *>(meta->Y);
+        const int head = (pnd + 1 + 7) & ~7;
+        const int *dl = reinterpret_cast<const int *>(stg + L::b + 6 * (size_t)W);
+        const unsigned short *ic = reinterpret_cast<const unsigned short *>(stg + L::b + 6 * (size_t)W + 4 * (size_t)pnd);
+        for (int jj = ct; jj < pnd; jj += NC) {
+            const int dd = dl[jj];
+            const int d = dd & 0x7fffffff;
+            if (d == n) continue;                         // dof-list padding
+            const int e0 = ic[jj], e1 = ic[jj + 1];
+            TA v = (TA)0;
+            for (int e = e0; e < e1; ++e) v += sa[ic[head + e]];
+            if (dd < 0) atomicAdd(Y + d, (TY)v);          // shared dof: reduction store
+            else Y[d] = (TY)v;
+        }
+        // this thread's shared-memory writes (the products) before the next
+        // bulk copy into the stage
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        consumers_sync();                                 // stage s is free
+        if (ct == 0) mbar_arrive(empty0 + 8u * s);
     }
 }
 
@@ -621,6 +882,12 @@ int sm_count()
 
 namespace {
 
+// FP32 3x3 blocks: the bulk-copy pipeline (k_ebe_mv3p) instead of k_ebe_mv3
+#ifndef FG_MV3_PIPELINE
+#define FG_MV3_PIPELINE 1
+#endif
+constexpr bool kMv3Pipeline = FG_MV3_PIPELINE != 0;
+
 struct MvLaunch {
     // Persistent CTAs: as many as fit on the GPU (their dynamic shared memory,
     // mv_smem_bytes, decides how many per SM), at most one per patch.
@@ -663,6 +930,19 @@ struct MvLaunch {
         }
         const int g = std::max(1, std::min(nitems, occ * sm_count()));
         kern<<<g, kThreads, smem, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof);
+    }
+    // the 3x3 FP32 bulk-copy pipeline: one CTA per SM, at most one per patch
+    template <typename TX, typename TY>
+    static void pipeline(int nitems, cudaStream_t st, const SysDev *sys, const MvRec *rec, const int *nch, int gate,
+                         int in_sel, int out_sel, int step, const TX *ai, TY *ao)
+    {
+        using L = Mv3pSmem<TX>;
+        static std::once_flag once;
+        std::call_once(once, [] {
+            cudaFuncSetAttribute(k_ebe_mv3p<TX, TY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::total);
+        });
+        const int g = std::max(1, std::min(nitems, sm_count()));
+        k_ebe_mv3p<TX, TY><<<g, kMv3pThreads, L::total, st>>>(sys, rec, nch, gate, in_sel, out_sel, step, ai, ao);
     }
 };
 
@@ -708,6 +988,7 @@ struct Plan {
     std::vector<int> ech_off;      // ncol+1 offsets into echunks
     int n_dch = 0, n_nch = 0, n_ilu = 0, n_ilub = 0, n_spb = 0, n_spi = 0;
     DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
+    DevMem mvrec;                                  // 3x3: per matvec work item, for the bulk-copy pipeline
     DevMem ilu_fwd, ilu_bwd, ilu_ctr;              // sync-free ILU(0) substitutions
     DevMem sp_blocks, sp_ifaces;                   // SPIKE (system, block) and (system, interface) items
 };
@@ -792,9 +1073,22 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     P.n_spi = (int)spi.size();
     std::vector<int> ecounts(P.ncol);
     for (int c = 0; c < P.ncol; ++c) ecounts[c] = P.ech_off[c + 1] - P.ech_off[c];
+    std::vector<MvRec> recs;
+    if (P.S == 3) {
+        recs.reserve(ech.size());
+        for (const EChunk &k : ech) {
+            const Topology &t = mem[k.sys].s->topo;
+            const int p = k.e0;
+            const int pne = t.pt_elem[p + 1] - t.pt_elem[p], pnd = t.pt_dof[p + 1] - t.pt_dof[p];
+            const int ni = t.pt_inc[p + 1] - t.pt_inc[p];
+            recs.push_back({k.sys, t.pt_elem[p], (int)(t.pt_boff[p] / 16), (int)(t.pt_boff[p + 1] - t.pt_boff[p]),
+                            t.pt_xlo[p], pne | (pnd << 16), ni | (t.pt_xlen[p] << 16), 0});
+        }
+    }
     int r;
     if ((r = P.sysdev.alloc(sizeof(SysDev) * hs.size())) ||
         (r = P.echunks.alloc(sizeof(EChunk) * std::max<size_t>(1, ech.size()))) ||
+        (!recs.empty() && (r = P.mvrec.alloc(sizeof(MvRec) * recs.size()))) ||
         (r = P.ecount.alloc(sizeof(int) * std::max(1, P.ncol))) ||
         (r = P.dchunks.alloc(sizeof(DChunk) * std::max<size_t>(1, dch.size()))) ||
         (r = P.dcount.alloc(sizeof(int))) ||
@@ -806,6 +1100,8 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
         (r = P.sp_blocks.alloc(sizeof(int2) * std::max<size_t>(1, spb.size()))) ||
         (r = P.sp_ifaces.alloc(sizeof(int2) * std::max<size_t>(1, spi.size()))))
         return r;
+    if (!recs.empty())
+        FG_CUDA(cudaMemcpyAsync(P.mvrec.p, recs.data(), sizeof(MvRec) * recs.size(), cudaMemcpyHostToDevice, st));
     if (!spb.empty())
         FG_CUDA(cudaMemcpyAsync(P.sp_blocks.p, spb.data(), sizeof(int2) * spb.size(), cudaMemcpyHostToDevice, st));
     if (!spi.empty())
@@ -866,11 +1162,20 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
         if (!cnt) continue;
         const EChunk *ch = P.echunks.as<EChunk>() + P.ech_off[c];
         const int *nc = P.ecount.as<int>() + c;
-        if (f64)
+        bool done = false;
+        if (f64) {
             MvLaunch::go<double, double, double>(P.S, cnt, st, sys, ch, nc, gate, 0, 0, 0, nullptr, nullptr,
                                                  P.maxdof);
-        else
-            MvLaunch::go<T, TV, T>(P.S, cnt, st, sys, ch, nc, gate, 1, 1, step, nullptr, nullptr, P.maxdof);
+            done = true;
+        }
+        if constexpr (sizeof(T) == 4) {
+            if (!done && P.S == 3 && kMv3Pipeline && P.mvrec.p) {
+                MvLaunch::pipeline<TV, T>(cnt, st, sys, P.mvrec.as<MvRec>() + P.ech_off[c], nc, gate, 1, 1, step,
+                                          nullptr, nullptr);
+                done = true;
+            }
+        }
+        if (!done) MvLaunch::go<T, TV, T>(P.S, cnt, st, sys, ch, nc, gate, 1, 1, step, nullptr, nullptr, P.maxdof);
         ++k;
     }
     return k;

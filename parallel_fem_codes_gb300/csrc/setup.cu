@@ -49,16 +49,12 @@ int permute_out(fg_system *s, const double *int_dev, double *ref_dev, cudaStream
 // Host layout (reference element order, row-major S x S) -> SoA in the
 // internal element order: A64[k][pos] = raw[eorder[pos]][k].
 __global__ void k_blocks_in(const double *__restrict__ raw, const int *__restrict__ eorder, double *__restrict__ A64,
-                            float *__restrict__ A32, int nel, int ld, int SS)
+                            int nel, int ld, int SS)
 {
     int pos = blockIdx.x * blockDim.x + threadIdx.x;
     if (pos >= nel) return;
     const double *src = raw + (size_t)eorder[pos] * SS;
-    for (int k = 0; k < SS; ++k) {
-        double v = src[k];
-        A64[(size_t)k * ld + pos] = v;
-        A32[(size_t)k * ld + pos] = (float)v;
-    }
+    for (int k = 0; k < SS; ++k) A64[(size_t)k * ld + pos] = src[k];
 }
 
 __global__ void k_blocks_out(double *__restrict__ raw, const int *__restrict__ eorder, const double *__restrict__ A64,
@@ -76,11 +72,35 @@ __global__ void k_to_f32(const double *__restrict__ a, float *__restrict__ b, si
         b[i] = (float)a[i];
 }
 
+// 3x3 FP32 blocks, blocked per matvec patch: patch p (elements pe0 ..
+// pe0 + pne) is one [9][W] block at 9 pe0, W = pne rounded up to 16 (zero
+// padded), so the matvec moves a patch's blocks as one contiguous copy.
+// Elements without a free dof (after the last patch) have no FP32 copy.
+__global__ void k_to_f32_patches(const double *__restrict__ a, float *__restrict__ b, const int *__restrict__ pt_elem,
+                                 int npatch, int ld)
+{
+    for (int p = blockIdx.x; p < npatch; p += gridDim.x) {
+        const int pe0 = pt_elem[p], pne = pt_elem[p + 1] - pe0, W = (pne + 15) & ~15;
+        float *dst = b + 9 * (size_t)pe0;
+        for (int idx = threadIdx.x; idx < 9 * W; idx += blockDim.x) {
+            const int m = idx / W, i = idx - m * W;
+            dst[idx] = i < pne ? (float)a[(size_t)m * ld + pe0 + i] : 0.0f;
+        }
+    }
+}
+
 int convert_blocks(fg_system *s, cudaStream_t st)
 {
-    size_t n = (size_t)s->topo.S * s->topo.S * s->nel_pad;
-    k_to_f32<<<std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 8 * sm_count())), 256, 0, st>>>(
-        s->A64.as<double>(), s->A32.as<float>(), n);
+    if (s->topo.S == 3) {
+        const int np = s->topo.npatch;
+        if (np > 0)
+            k_to_f32_patches<<<std::max(1, std::min(np, 8 * sm_count())), 256, 0, st>>>(
+                s->A64.as<double>(), s->A32.as<float>(), s->pt_elem.as<int>(), np, s->nel_pad);
+    } else {
+        size_t n = (size_t)s->topo.S * s->topo.S * s->nel_pad;
+        k_to_f32<<<std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 8 * sm_count())), 256, 0, st>>>(
+            s->A64.as<double>(), s->A32.as<float>(), n);
+    }
     FG_CUDA(cudaGetLastError());
     count_launches(1);
     return FG_OK;
@@ -90,11 +110,11 @@ int upload_blocks_raw(fg_system *s, const double *raw_dev, cudaStream_t st)
 {
     int nel = s->topo.nel;
     if (nel > 0)
-        k_blocks_in<<<(nel + 255) / 256, 256, 0, st>>>(raw_dev, s->eorder.as<int>(), s->A64.as<double>(),
-                                                      s->A32.as<float>(), nel, s->nel_pad, s->topo.S * s->topo.S);
+        k_blocks_in<<<(nel + 255) / 256, 256, 0, st>>>(raw_dev, s->eorder.as<int>(), s->A64.as<double>(), nel,
+                                                      s->nel_pad, s->topo.S * s->topo.S);
     FG_CUDA(cudaGetLastError());
     count_launches(1);
-    return FG_OK;
+    return convert_blocks(s, st);
 }
 
 int download_blocks_raw(const fg_system *s, double *raw_dev, cudaStream_t st)

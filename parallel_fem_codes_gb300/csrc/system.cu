@@ -80,7 +80,7 @@ fg_system::~fg_system()
 size_t fg_system::bytes() const
 {
     const DevMem *all[] = {&lm, &A64, &A32, &dinc_ptr, &dinc, &ninc_ptr, &ninc, &node_dof, &eorder, &perm,
-                           &lm16, &pt_elem, &pt_dof, &pt_col, &pdofs, &pt_inc, &incl, &rhs_f, &rhs_b,
+                           &lm16, &blob, &pt_elem, &pt_dof, &pt_col, &pdofs, &pt_inc, &incl, &rhs_f, &rhs_b,
                            &csr_ia, &csr_ja, &csr_diag, &csr_inc_ptr, &csr_inc, &AA64, &AA32, &LU64, &LU32,
                            &dinv64, &dinv32, &lu_ia, &lu_ja, &lu_dg, &lu_map, &AAf64, &ilu_flags, &ilu_ctr, &ilu_tmp, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
                            &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
@@ -143,7 +143,7 @@ int fg_system_create(fg_system **out, int nnodes, int nel, int ndof, const int *
     std::vector<unsigned short> lm16((size_t)S * s->nel_pad, (unsigned short)0xFFFF);
     for (int p = 0; p < t.nel; ++p)
         for (int a = 0; a < S; ++a) lm16[(size_t)a * s->nel_pad + p] = t.lm16[(size_t)p * S + a];
-    if ((r = upload(s->lm16, lm16)) || (r = upload(s->pt_elem, t.pt_elem)) || (r = upload(s->pt_dof, t.pt_dof)) ||
+    if ((r = upload(s->lm16, lm16)) || (r = upload(s->blob, t.blob)) || (r = upload(s->pt_elem, t.pt_elem)) || (r = upload(s->pt_dof, t.pt_dof)) ||
         (r = upload(s->pt_col, t.pt_col)) || (r = upload(s->pdofs, t.dofs)) || (r = upload(s->pt_inc, t.pt_inc)) ||
         (r = upload(s->incl, t.incl))) {
         delete s;

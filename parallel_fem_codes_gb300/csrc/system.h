@@ -37,6 +37,7 @@ struct fg_system {
     fg::DevMem lm, A64, A32;
     fg::DevMem dinc_ptr, dinc, ninc_ptr, ninc, node_dof, eorder, perm;
     fg::DevMem lm16, pt_elem, pt_dof, pt_col, pdofs, pt_inc, incl;   // matvec patch layout
+    fg::DevMem blob;                   // 3x3: per-patch index blobs of the bulk-copy matvec
     // preconditioners
     fg::DevMem diag, invd64, invd32, bd, ibd64, ibd32;
     int precond = FG_PRECOND_NONE;
@@ -138,6 +139,7 @@ inline void set_patch_fields(SysDev &D, const fg_system *s)
     D.dofs = s->pdofs.as<int>();
     D.pt_inc = s->pt_inc.as<int>();
     D.incl = s->incl.as<unsigned short>();
+    D.blob = s->blob.as<unsigned char>();
     D.maxdof = std::max(1, s->topo.maxdof);
 }
 

@@ -311,27 +311,52 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
     t.eorder.resize(nel);
     t.pt_elem.clear();
     t.pt_dof.clear();
+    t.pt_xlo.clear();
+    t.pt_xlen.clear();
     t.pt_col.clear();
     t.dofs.clear();
     t.maxdof = 0;
     std::vector<int> local(n + 1, -1), owner_count(n + 1, 0);
     std::vector<uint32_t> lmask;   // per local dof: local colours used
     for (int b = 0, p = 0; b < nact; ++p) {
-        // local dofs of the patch, ascending internal index
+        // local dofs of the patch, ascending internal index; a 3x3 patch also
+        // keeps its dofs inside one x segment of at most kPatchXCap entries
+        // (8-aligned ends): past that it goes back to its last 16-element
+        // boundary
         std::vector<int> pd;
-        int e = b;
+        int e = b, lo = n, hi = -1;
+        size_t keep_pd = 0;
+        int keep_lo = n, keep_hi = -1;
         while (e < nact && e - b < PE) {
-            if ((e - b) % 16 == 0 && (int)pd.size() + 16 * S > dof_cap) break;
+            if ((e - b) % 16 == 0) {
+                if ((int)pd.size() + 16 * S > dof_cap) break;
+                keep_pd = pd.size(); keep_lo = lo; keep_hi = hi;
+            }
             for (int a = 0; a < S; ++a) {
                 int r = t.lm[(size_t)sorted[e] * S + a];
-                if (r != n && local[t.iperm[r]] < 0) { local[t.iperm[r]] = 0; pd.push_back(t.iperm[r]); }
+                if (r != n && local[t.iperm[r]] < 0) {
+                    local[t.iperm[r]] = 0;
+                    pd.push_back(t.iperm[r]);
+                    lo = std::min(lo, t.iperm[r]);
+                    hi = std::max(hi, t.iperm[r]);
+                }
             }
             ++e;
+            if (S == 3 && ((hi + 1 + 7) & ~7) - (lo & ~7) > kPatchXCap) {
+                if (keep_pd == 0) { set_error("a 16-element group spans more than the matvec's x segment"); return FG_ERR_UNSUPPORTED; }
+                for (size_t k = keep_pd; k < pd.size(); ++k) local[pd[k]] = -1;
+                pd.resize(keep_pd);
+                lo = keep_lo; hi = keep_hi;
+                e = b + (int)((e - 1 - b) / 16) * 16;
+                break;
+            }
         }
         t.pt_elem.push_back(b);
         t.pt_col.resize((size_t)(p + 1) * kPatchColStride, 0);
         t.pt_dof.push_back(0);
         std::sort(pd.begin(), pd.end());
+        t.pt_xlo.push_back(pd.front() & ~7);
+        t.pt_xlen.push_back(((pd.back() + 1 + 7) & ~7) - (pd.front() & ~7));
         for (size_t j = 0; j < pd.size(); ++j) { local[pd[j]] = (int)j; owner_count[pd[j]]++; }
         // greedy local colouring in patch order
         lmask.assign(pd.size(), 0u);
@@ -383,6 +408,7 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
     for (int p = 0; p < nel; ++p) t.epos[t.eorder[p]] = p;
     // patch-local element maps (internal element order)
     t.lm16.assign((size_t)nel * S, 0xFFFF);
+    t.lmx16.assign((size_t)nel * S, 0xFFFF);
     for (int p = 0; p < t.npatch; ++p) {
         const int b = t.pt_elem[p], e = t.pt_elem[p + 1];
         for (int j = t.pt_dof[p]; j < t.pt_dof[p + 1]; ++j) local[t.dofs[j] & 0x7fffffff] = j - t.pt_dof[p];
@@ -390,6 +416,7 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
             for (int a = 0; a < S; ++a) {
                 int r = t.lm[(size_t)t.eorder[q] * S + a];
                 t.lm16[(size_t)q * S + a] = r == n ? (unsigned short)0xFFFF : (unsigned short)local[t.iperm[r]];
+                t.lmx16[(size_t)q * S + a] = r == n ? (unsigned short)0xFFFF : (unsigned short)(t.iperm[r] - t.pt_xlo[p]);
             }
         for (int j = t.pt_dof[p]; j < t.pt_dof[p + 1]; ++j) local[t.dofs[j] & 0x7fffffff] = -1;
     }
@@ -401,6 +428,10 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
         std::vector<int> cnt;
         for (int p = 0; p < t.npatch; ++p) {
             const int b = t.pt_elem[p], e = t.pt_elem[p + 1], nd = t.pt_dof[p + 1] - t.pt_dof[p];
+            // staged products are rows of the patch width (3x3: its element
+            // count rounded up to 16, the row length of the blocked FP32
+            // blocks)
+            const int Wp = S == 3 ? (e - b + 15) / 16 * 16 : PEs;
             t.pt_inc[p] = (int)t.incl.size();
             cnt.assign(nd + 1, 0);
             for (int q = b; q < e; ++q)
@@ -417,10 +448,30 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
             for (int q = b; q < e; ++q)
                 for (int a = 0; a < S; ++a) {
                     const unsigned short l = t.lm16[(size_t)q * S + a];
-                    if (l != 0xFFFF) t.incl[base + head + fill[l]++] = (unsigned short)(a * PEs + (q - b));
+                    if (l != 0xFFFF) t.incl[base + head + fill[l]++] = (unsigned short)(a * Wp + (q - b));
                 }
         }
         t.pt_inc[t.npatch] = (int)t.incl.size();
+    }
+    // 3x3: one index blob per patch for the bulk-copy matvec, 16-byte
+    // aligned: x-segment positions [3][W] (W = element count rounded up to
+    // 16, padding 0xFFFF), the dof list, the incidence lists
+    if (S == 3) {
+        t.pt_boff.assign(t.npatch + 1, 0);
+        t.blob.clear();
+        for (int p = 0; p < t.npatch; ++p) {
+            const int b = t.pt_elem[p], e = t.pt_elem[p + 1], W = (e - b + 15) / 16 * 16;
+            t.pt_boff[p] = (long long)t.blob.size();
+            const size_t o = t.blob.size();
+            const size_t nd = t.pt_dof[p + 1] - t.pt_dof[p], ni = t.pt_inc[p + 1] - t.pt_inc[p];
+            t.blob.resize(o + 6 * (size_t)W + 4 * nd + 2 * ni);
+            unsigned short *lx = reinterpret_cast<unsigned short *>(t.blob.data() + o);
+            for (int a = 0; a < 3; ++a)
+                for (int i = 0; i < W; ++i) lx[a * W + i] = b + i < e ? t.lmx16[(size_t)(b + i) * 3 + a] : 0xFFFF;
+            std::memcpy(t.blob.data() + o + 6 * (size_t)W, t.dofs.data() + t.pt_dof[p], 4 * nd);
+            std::memcpy(t.blob.data() + o + 6 * (size_t)W + 4 * nd, t.incl.data() + t.pt_inc[p], 2 * ni);
+        }
+        t.pt_boff[t.npatch] = (long long)t.blob.size();
     }
     // patch colouring: patches that share a dof get different colours
     {
@@ -478,6 +529,28 @@ int build_topology(Topology &t, int nnodes, int nel, int ndof, const int *ien,
     t.node_dof.resize((size_t)nnodes * ndof);
     for (size_t d = 0; d < t.node_dof.size(); ++d)
         t.node_dof[d] = t.type[d] == 0 ? n : t.iperm[t.invp[d]];
+    // The matvec kernels copy a patch's rows in 16-byte units: every patch
+    // starts 16 elements aligned, its dof list and incidence lists start and
+    // end on 16-byte boundaries and fit the kernels' shared-memory caps.
+    {
+        const int PE = patch_elems(S), dcap = S == 3 ? 1536 : PE * S;
+        const int icap = (dcap + 1 + 7) / 8 * 8 + S * PE;
+        const int nel_pad = std::max(32, (nel + 31) / 32 * 32);
+        for (int p = 0; p < t.npatch; ++p) {
+            const int pe0 = t.pt_elem[p], pne = t.pt_elem[p + 1] - pe0;
+            const int pd0 = t.pt_dof[p], pnd = t.pt_dof[p + 1] - pd0;
+            const int i0 = S == 3 ? t.pt_inc[p] : 0, ni = S == 3 ? t.pt_inc[p + 1] - i0 : 0;
+            if (pe0 % 16 || pne < 1 || pne > PE || pe0 + (pne + 15) / 16 * 16 > nel_pad || pd0 % 4 || pnd % 4 ||
+                pnd < 1 || pnd > dcap || i0 % 8 || ni % 8 || ni > icap ||
+                (S == 3 && (t.pt_xlo[p] % 8 || t.pt_xlen[p] % 8 || t.pt_xlen[p] < 8 || t.pt_xlen[p] > kPatchXCap ||
+                            t.pt_xlo[p] + t.pt_xlen[p] > (n + 1 + 31) / 32 * 32 || t.pt_boff[p] % 16 ||
+                            t.pt_boff[p + 1] - t.pt_boff[p] > 6LL * PE + 4LL * dcap + 2LL * icap ||
+                            t.pt_boff[p + 1] / 16 > 0x7fffffffLL))) {
+                set_error("internal: matvec patch layout out of its bounds");
+                return FG_ERR_UNSUPPORTED;
+            }
+        }
+    }
     return FG_OK;
 }
 

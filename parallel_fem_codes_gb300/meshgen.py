@@ -114,16 +114,37 @@ def transport_problem(n_nodes_side: int, angle_deg=30.0, k=1e-6, gamma=0.0, f=0.
                             float(f), up.astype(np.float64), upmode, float(upval), cau)
 
 
-def batch_transport_problems(count=256, seed=4, nmin=33, nmax=513, cau=True):
-    """The batched transport workload: count independent steady SUPG problems,
-    mesh N x N nodes with N uniform in [nmin, nmax], velocity angle uniform in
-    [0, 360), conductivity log-uniform in [1e-8, 1e-2] (numpy PCG64, seeded)."""
+def batch_transport_params(count=256, seed=4, nmin=33, nmax=513):
+    """Per-instance parameters of the batched transport workload: lists of
+    nodes per side N (uniform in [nmin, nmax]), velocity angle in degrees
+    (uniform in [0, 360)) and conductivity (log-uniform in [1e-8, 1e-2]),
+    drawn from numpy PCG64 with the given seed."""
     rng = np.random.Generator(np.random.PCG64(seed))
     ns = rng.integers(nmin, nmax + 1, size=count)
     angles = rng.uniform(0.0, 360.0, size=count)
     ks = 10.0 ** rng.uniform(-8.0, -2.0, size=count)
-    return [transport_problem(int(n), float(a), float(kk), cau=cau)
-            for n, a, kk in zip(ns, angles, ks)]
+    return [int(n) for n in ns], [float(a) for a in angles], [float(k) for k in ks]
+
+
+def batch_transport_sizes(count=256, seed=4, nmin=33, nmax=513):
+    """(elements, free dofs) of every instance of the batched workload without
+    building its meshes: 2 (N-1)^2 triangles, (N-2)^2 interior nodes."""
+    ns, _, _ = batch_transport_params(count, seed, nmin, nmax)
+    return [2 * (n - 1) ** 2 for n in ns], [(n - 2) ** 2 for n in ns]
+
+
+def batch_transport_problem(i, count=256, seed=4, nmin=33, nmax=513, cau=True):
+    """Instance i of the batched transport workload (only its own mesh is built)."""
+    ns, angles, ks = batch_transport_params(count, seed, nmin, nmax)
+    return transport_problem(ns[i], angles[i], ks[i], cau=cau)
+
+
+def batch_transport_problems(count=256, seed=4, nmin=33, nmax=513, cau=True):
+    """The batched transport workload: count independent steady SUPG problems,
+    mesh N x N nodes with N uniform in [nmin, nmax], velocity angle uniform in
+    [0, 360), conductivity log-uniform in [1e-8, 1e-2] (numpy PCG64, seeded)."""
+    ns, angles, ks = batch_transport_params(count, seed, nmin, nmax)
+    return [transport_problem(n, a, kk, cau=cau) for n, a, kk in zip(ns, angles, ks)]
 
 
 def multi_dof_mesh(n_nodes_side: int, ndof: int, seed: int = 0, dirichlet=None, jitter: float = 0.0):

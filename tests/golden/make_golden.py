@@ -1,7 +1,9 @@
 """Generate the golden fixtures from the reference's own C (checker build).
 
 Run here, where the reference sources are present:
-    make -C oracle ref REF=/root/reference && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py
+(the reference tree: PFC_REFERENCE_DIR, default `reference` beside this
+repository)
 It writes tests/golden/sst_*.npz: mesh, connectivity (lm, Perm, invPerm,
 bandwidths), element blocks and right-hand side at u = 0, one Diag +
 GMRES(30) solve, and the full CAU Process loop (solution and GMRES
@@ -50,7 +52,7 @@ CASES = {
 
 def main():
     if not O.ref_available():
-        raise SystemExit("build the reference first: make -C oracle ref REF=/root/reference")
+        raise SystemExit("build the reference first: make -C oracle ref")
     for name, (n, ang, k, gm, f, upm, upv) in CASES.items():
         p = G.transport_problem(n, angle_deg=ang, k=k, gamma=gm, f=f, upmode=upm, upval=upv)
         if name == "sst_9_teste":

@@ -6,7 +6,8 @@ oracle/_ref/, runs it there on two inputs, and copies its outputs here:
   mesh_TESTE_8x8.dat    TESTE, "right" diagonal, 8 x 8 cells (NDOF = 1)
   mesh_OBLIQUO_6x6.dat  OBLIQUO, "right" diagonal, 6 x 6 cells (NDOF = 4)
 
-Needs the reference sources (REF, default /root/reference) and gcc; the
+Needs the reference sources (PFC_REFERENCE_DIR, default: the directory
+`reference` beside this repository) and gcc; the
 fixtures are committed, the tests only read them.
 """
 import os
@@ -16,7 +17,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("REF", "/root/reference")
+REF = os.environ.get("PFC_REFERENCE_DIR") or os.path.normpath(os.path.join(ROOT, "..", "reference"))
 OUT = os.path.join(ROOT, "oracle", "_ref")
 
 

@@ -14,7 +14,7 @@ import ctypes
 
 import numpy as np
 
-from . import build as _build
+from parallel_fem_codes_gb300 import build as _build
 
 c_int, c_dbl, c_char = ctypes.c_int, ctypes.c_double, ctypes.c_char
 P_dbl, P_int = ctypes.POINTER(c_dbl), ctypes.POINTER(c_int)

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from parallel_fem_codes_gb300 import refapi
+import refapi
 
 
 def test_shim_exports_reference_names():

@@ -9,7 +9,7 @@ import pytest
 
 import oracle as O
 from parallel_fem_codes_gb300 import meshgen as G
-from parallel_fem_codes_gb300 import refapi
+import refapi
 
 pytestmark = pytest.mark.gpu
 
