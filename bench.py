@@ -50,13 +50,14 @@ def served_precision(fg):
     """Precision of the mixed solves: FP32 arithmetic, basis in FP32 or FP16."""
     return fg.FG_PREC_MIXED16 if BASIS == "fp16" else fg.FG_PREC_MIXED
 # DRAM bytes / algorithmic bytes of one batched FP32 matvec, measured by ncu
-# (dram__bytes_read.sum + dram__bytes_write.sum of the two k_ebe_mv3
+# (dram__bytes_read.sum + dram__bytes_write.sum of the two k_ebe_mv3p
 # launches of one matvec of `bench.py --matvec-only --count 32 --steps 1`,
-# cold): 475.7 MB for 418.2 MB algorithmic; the difference is the patches'
-# incidence lists (16-bit index data, ~7 B per element), which the
-# algorithmic count leaves out.  The traffic scales with the instances (each
-# patch reads its own blocks once).
-MATVEC_TRAFFIC_RATIO = 475.7 / 418.19
+# cold): 481.6 MB for 418.19 MB algorithmic; the difference is the patches'
+# index blobs (16-bit x-segment positions, dof lists and incidence lists,
+# ~16.5 B per element where the algorithmic count charges 12 B of equation
+# numbers) and the x segments' 8-entry alignment.  The traffic scales with
+# the instances (each patch reads its own blocks and blob once).
+MATVEC_TRAFFIC_RATIO = 481.61 / 418.19
 
 
 # ------------------------------------------------------------------ CPU legs
@@ -633,7 +634,7 @@ def main():
                       "iterations_mean": float(np.mean(iters)),
                       "rel_err_vs_fp64_max": max(plain_err) if plain_err else None},
             "clocks": clocks, "gpu_launches": launches, "e2e": e2e,
-            "roofline": {"bound": "hbm", "kernel": "k_ebe_mv3<float> (all patch colours, batched)",
+            "roofline": {"bound": "hbm", "kernel": "k_ebe_mv3p<float,float> (all patch colours, batched)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind, "traffic": MATVEC_TRAFFIC_RATIO * bytes_mv,
                          "traffic_source": "ncu dram__bytes_read+write per matvec of a 32-instance capture "
