@@ -478,7 +478,10 @@ typedef struct {
     double tol;
     int precision;            /* FG_PREC_MIXED or FG_PREC_FP64          */
     double inner_tol;
-    size_t hbm_budget_bytes;  /* 0: 80% of the free device memory       */
+    size_t hbm_budget_bytes;  /* 0: 80% of the free device memory; a
+                                 request counts its system's arrays and the
+                                 workspace it will allocate; one request
+                                 runs alone even when it is larger      */
     int max_active;           /* 0: no limit                            */
 } fg_server_opts;
 typedef struct {
@@ -495,8 +498,11 @@ int fg_server_submit(fg_server *sv, fg_system *s, const fg_transport_coeffs *c, 
  * initial state and receives the final state; it and the system stay the
  * caller's but must not be touched until the result has been polled.  In
  * the result, stats.iterations counts the GMRES iterations of the loop,
- * stats.cycles its corrections.  Euler loops run one at a time, beside the
- * transport batch, on the system's own stream. */
+ * stats.cycles its corrections.  Up to 16 loops run at once (each on its
+ * system's stream, admitted against the same HBM budget as transport
+ * requests); their correction solves with the BlockDiag preconditioner
+ * share one continuously batched GMRES run (other preconditioners solve
+ * alone), so a loop's result equals its fg_euler_predictor run. */
 int fg_server_submit_euler(fg_server *sv, fg_system *s, const fg_euler_coeffs *c, const fg_time_opts *t,
                            double *u, unsigned long long tag);
 /* Move up to max finished results into out; *count receives how many. */

@@ -1340,6 +1340,22 @@ size_t workspace_bytes(const fg_system *s, int kmax, int mixed)
            8 * (size_t)kMaxParts * kPartStride + 256;
 }
 
+size_t request_bytes(const fg_system *s, int kmax, int mixed, bool time_loop)
+{
+    const Workspace &w = s->ws;
+    const DevMem *held[] = {&w.V, &w.w, &w.t, &w.x, &w.b, &w.ftrue, &w.r64, &w.t64, &w.u64, &w.small, &w.part,
+                            &w.counter, &w.state};
+    size_t have = 0;
+    for (auto *m : held) have += m->bytes;
+    size_t b = s->bytes() - std::min(have, s->bytes()) + workspace_bytes(s, kmax, mixed);
+    if (time_loop) {
+        const DevMem *loop[] = {&s->rhs_f, &s->rhs_b, &s->state_u, &s->state_a, &s->state_old};
+        for (auto *m : loop)
+            if (!m->p) b += 8 * (size_t)s->n_pad;
+    }
+    return b;
+}
+
 BatchRun::BatchRun(const SolveConfig &c, cudaStream_t s) : cfg(c), st(s) {}
 
 BatchRun::~BatchRun()

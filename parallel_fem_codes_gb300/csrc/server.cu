@@ -1,20 +1,25 @@
-// Request server: continuous batching of steady transport solves, and
-// Euler time loops beside them.
+// Request server: continuous batching of steady transport solves and of
+// the correction solves of Euler time loops.
 //
-// Transport: one worker thread owns a BatchRun.  Between restart cycles it admits
-// waiting requests (FIFO) while their Krylov workspace fits the HBM budget,
-// assembles each admitted system on the device, and runs one cycle for all
-// admitted solves; converged solves leave the batch immediately and their
-// results are published with submit / admit / done times.  Because every
-// system's reductions use only its own parts, a result does not depend on
-// which other requests shared its cycles.
+// Transport: one worker thread owns a BatchRun.  Between restart cycles it
+// admits waiting requests (FIFO) while their device footprint (the
+// system's arrays and its Krylov workspace) fits the HBM budget, assembles
+// each admitted system on the device, and runs one cycle for all admitted
+// solves; converged solves leave the batch immediately and their results
+// are published with submit / admit / done times.  Because every system's
+// reductions use only its own parts, a result does not depend on which
+// other requests shared its cycles.
 //
-// Euler: a second worker thread takes Euler requests (a system with Euler
-// geometry, coefficients, time-stepping controls and a host state) in FIFO
-// order and runs each request's Predictor_Old loop (fg_euler_predictor: the
-// loop's assembly, preconditioner set-up and solves stay on the device, on
-// the system's own stream), so Euler loops overlap with the transport
-// batch on the GPU.
+// Euler: a pool of request threads runs admitted Euler time loops
+// (Predictor_Old, 00_CommonFiles/Time_Integration/Predictor_Old.c:53-123:
+// assembly, preconditioner set-up and the update on each system's own
+// stream).  Each correction solve of a loop is handed to a second batch
+// thread, which keeps its own BatchRun of every Euler correction currently
+// waiting: corrections of different requests join and leave it between
+// restart cycles, exactly as transport solves do, so the Euler loops share
+// GMRES cycles instead of queueing behind one another.  A loop's result is
+// the same as its solo run (same kernels, per-system reductions).  Euler
+// requests are admitted against the same HBM budget.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -44,7 +49,18 @@ struct EulerRequest {
     double *u;
     unsigned long long tag;
     double t_submit;
+    size_t bytes;
 };
+
+// One correction solve waiting for the Euler batch.
+struct EulerSolve {
+    fg_system *s;
+    fg_solve_stats *stats;
+    bool done;
+    int rc;
+};
+
+constexpr int kEulerWorkers = 16;      // Euler time loops in flight at most
 
 }  // namespace fg
 
@@ -62,23 +78,40 @@ struct fg_server {
     std::deque<EulerRequest> queue_eu;
     std::condition_variable cv_work_eu;
     std::vector<fg_server_result> done;
-    std::vector<Request> active;   // parallel to the batch members
+    std::vector<Request> active;   // parallel to the batch members (transport thread only)
     std::set<fg_system *> busy;
-    size_t in_use = 0;
+    size_t in_use = 0;             // admitted bytes (transport + Euler)
+    int tr_active = 0, eu_active = 0;   // admitted requests
     bool stop = false;
     int error = FG_OK;
     std::string error_text;
-    std::thread worker, worker_eu;
+    std::thread worker, worker_eub;
+    std::vector<std::thread> workers_eu;
+    // Euler correction batch
+    SolveConfig cfg_eu;
+    cudaStream_t st_eu = nullptr;
+    std::deque<EulerSolve *> eu_pending;
+    std::condition_variable cv_eu_batch, cv_eu_solved;
+    bool stop_eub = false;
 
     double now() const { return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(); }
+    // a request of `bytes` may start: it fits the budget, or nothing else is
+    // admitted (one oversized request still runs alone)
+    bool fits(size_t bytes, int extra) const
+    {
+        return o.hbm_budget_bytes == 0 || in_use + bytes <= o.hbm_budget_bytes || tr_active + eu_active + extra == 0;
+    }
     void run();
     void run_euler();
+    void run_euler_batch();
+    int solve_correction(fg_system *s, const SolveConfig &c, fg_solve_stats *st);
     void fail(int code)
     {
         std::lock_guard<std::mutex> l(mu);
         error = code;
         error_text = fg_last_error();
         cv_done.notify_all();
+        cv_eu_solved.notify_all();
     }
 };
 
@@ -94,15 +127,19 @@ void fg_server::run()
             std::unique_lock<std::mutex> l(mu);
             if (active.empty() && queue.empty() && !stop)
                 cv_work.wait(l, [&] { return stop || !queue.empty(); });
+            if (active.empty() && !queue.empty() && !stop && !fits(queue.front().bytes, 0))
+                cv_work.wait_for(l, std::chrono::milliseconds(2),
+                                 [&] { return stop || queue.empty() || fits(queue.front().bytes, 0); });
             if (stop && queue.empty() && active.empty()) return;
             if (stop) { queue.clear(); }
             for (auto it = queue.begin(); it != queue.end();) {
-                bool fits = o.hbm_budget_bytes == 0 || in_use + it->bytes <= o.hbm_budget_bytes || active.empty();
-                bool slot = o.max_active <= 0 || (int)(active.size() + admit.size()) < o.max_active;
-                if (!fits || !slot) break;              // FIFO: the head waits for room
+                const bool room = fits(it->bytes, (int)admit.size());
+                const bool slot = o.max_active <= 0 || (int)(active.size() + admit.size()) < o.max_active;
+                if (!room || !slot) break;              // FIFO: the head waits for room
                 if (busy.count(it->s)) { ++it; continue; }
                 busy.insert(it->s);
                 in_use += it->bytes;
+                ++tr_active;
                 admit.push_back(*it);
                 it = queue.erase(it);
             }
@@ -142,9 +179,11 @@ void fg_server::run()
                 done.push_back(res);
                 busy.erase(r.s);
                 in_use -= r.bytes;
+                --tr_active;
             }
             cv_done.notify_all();
         }
+        cv_work_eu.notify_all();                      // room for waiting Euler loops
         batch.remove(fin);
         std::vector<int> sorted = fin;
         std::sort(sorted.rbegin(), sorted.rend());
@@ -153,40 +192,130 @@ void fg_server::run()
     }
 }
 
+// A correction solve of an Euler loop: joins the Euler batch when its
+// configuration is the batch's (the server's solver options with
+// BlockDiag), else runs alone on the system's stream.
+int fg_server::solve_correction(fg_system *s, const SolveConfig &c, fg_solve_stats *st)
+{
+    if (c.precond != cfg_eu.precond || c.kmax != cfg_eu.kmax || c.lmax != cfg_eu.lmax || c.tol != cfg_eu.tol ||
+        c.mixed != cfg_eu.mixed || c.vhalf != cfg_eu.vhalf || c.inner_tol != cfg_eu.inner_tol) {
+        std::vector<BatchMember> mem{{s, s->rhs_b.as<double>(), s->rhs_f.as<double>(), nullptr}};
+        return solve_batch(mem, c, st, s->stream);
+    }
+    FG_CUDA(cudaStreamSynchronize(s->stream));        // assembly and set-up finished before the batch reads them
+    EulerSolve job{s, st, false, FG_OK};
+    {
+        std::lock_guard<std::mutex> l(mu);
+        eu_pending.push_back(&job);
+    }
+    cv_eu_batch.notify_one();
+    std::unique_lock<std::mutex> l(mu);
+    cv_eu_solved.wait(l, [&] { return job.done; });    // the batch thread completes every job it takes
+    return job.rc;
+}
+
+void fg_server::run_euler_batch()
+{
+    cudaSetDevice(device);
+    BatchRun batch(cfg_eu, st_eu);
+    std::vector<EulerSolve *> act;                    // parallel to the batch members
+    std::vector<int> live;
+    auto give_up = [&](int rc) {
+        fail(rc);
+        std::lock_guard<std::mutex> l(mu);
+        for (auto *a : act) { a->rc = rc; a->done = true; }
+        for (auto *a : eu_pending) { a->rc = rc; a->done = true; }
+        eu_pending.clear();
+        cv_eu_solved.notify_all();
+    };
+    for (;;) {
+        std::deque<EulerSolve *> add;
+        {
+            std::unique_lock<std::mutex> l(mu);
+            if (act.empty()) cv_eu_batch.wait(l, [&] { return stop_eub || !eu_pending.empty(); });
+            if (stop_eub && act.empty() && eu_pending.empty()) return;
+            add.swap(eu_pending);
+        }
+        int rc = FG_OK;
+        for (auto *a : add) {
+            act.push_back(a);
+            if ((rc = batch.stage({a->s, a->s->rhs_b.as<double>(), a->s->rhs_f.as<double>(), nullptr}))) {
+                give_up(rc);
+                return;
+            }
+        }
+        if (!add.empty() && (rc = batch.commit())) { give_up(rc); return; }
+        if (act.empty()) continue;
+        if ((rc = batch.cycle(false, live))) { give_up(rc); return; }
+        std::vector<int> fin;
+        for (size_t i = 0; i < live.size(); ++i)
+            if (!live[i]) fin.push_back((int)i);
+        if (fin.empty()) continue;
+        std::vector<SysState> sts;
+        if ((rc = batch.finish(fin, sts))) { give_up(rc); return; }
+        {
+            std::lock_guard<std::mutex> l(mu);
+            for (size_t q = 0; q < fin.size(); ++q) {
+                EulerSolve *a = act[fin[q]];
+                fill_stats(sts[q], 0.0, *a->stats);
+                a->rc = FG_OK;
+                a->done = true;
+            }
+            cv_eu_solved.notify_all();
+        }
+        batch.remove(fin);
+        std::vector<int> sorted = fin;
+        std::sort(sorted.rbegin(), sorted.rend());
+        for (int i : sorted) act.erase(act.begin() + i);
+        if ((rc = batch.commit())) { give_up(rc); return; }
+    }
+}
+
 void fg_server::run_euler()
 {
     cudaSetDevice(device);
     fg_solver_opts so{cfg.kmax, cfg.lmax, cfg.tol, o.precision, o.inner_tol};
+    const CorrectionSolve hook = [this](fg_system *s, const SolveConfig &c, fg_solve_stats *st) {
+        return solve_correction(s, c, st);
+    };
     for (;;) {
         EulerRequest r;
         {
             std::unique_lock<std::mutex> l(mu);
-            cv_work_eu.wait(l, [&] { return stop || !queue_eu.empty(); });
+            cv_work_eu.wait(l, [&] { return stop || (!queue_eu.empty() && fits(queue_eu.front().bytes, 0)); });
             if (stop) { queue_eu.clear(); return; }
             r = queue_eu.front();
             queue_eu.pop_front();
+            in_use += r.bytes;
+            ++eu_active;
         }
         const double t_admit = now();
         fg_time_stats ts{};
-        int rc = fg_euler_predictor(r.s, &r.c, &so, &r.t, r.u, nullptr, &ts);
+        int rc = euler_predictor_hooked(r.s, &r.c, &so, &r.t, r.u, nullptr, &ts, &hook);
         if (rc != FG_OK) { fail(rc); return; }
         const double t = now();
-        std::lock_guard<std::mutex> l(mu);
-        fg_server_result res{};
-        res.tag = r.tag;
-        res.stats.iterations = ts.gmres_iterations;
-        res.stats.cycles = ts.corrections;
-        res.stats.converged = ts.true_rel_residual <= cfg.tol ? 1 : 0;
-        res.stats.status = FG_OK;
-        res.stats.eps = cfg.tol;
-        res.stats.true_rel_residual = ts.true_rel_residual;
-        res.stats.seconds = t - t_admit;
-        res.t_submit = r.t_submit;
-        res.t_admit = t_admit;
-        res.t_done = t;
-        done.push_back(res);
-        busy.erase(r.s);
-        cv_done.notify_all();
+        {
+            std::lock_guard<std::mutex> l(mu);
+            fg_server_result res{};
+            res.tag = r.tag;
+            res.stats.iterations = ts.gmres_iterations;
+            res.stats.cycles = ts.corrections;
+            res.stats.converged = ts.true_rel_residual <= cfg.tol ? 1 : 0;
+            res.stats.status = FG_OK;
+            res.stats.eps = cfg.tol;
+            res.stats.true_rel_residual = ts.true_rel_residual;
+            res.stats.seconds = t - t_admit;
+            res.t_submit = r.t_submit;
+            res.t_admit = t_admit;
+            res.t_done = t;
+            done.push_back(res);
+            busy.erase(r.s);
+            in_use -= r.bytes;
+            --eu_active;
+            cv_done.notify_all();
+        }
+        cv_work.notify_all();                         // room for waiting transport requests
+        cv_work_eu.notify_all();
     }
 }
 
@@ -217,8 +346,11 @@ int fg_server_create(fg_server **out, const fg_server_opts *opts)
     sv->cfg.precond = FG_PRECOND_DIAG;
     sv->cfg.device_io = 1;
     sv->cfg.use_graph = 0;
+    sv->cfg_eu = sv->cfg;
+    sv->cfg_eu.precond = FG_PRECOND_BLOCKDIAG;
     cudaError_t ce = cudaGetDevice(&sv->device);
     if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&sv->st, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaStreamCreateWithFlags(&sv->st_eu, cudaStreamNonBlocking);
     if (ce != cudaSuccess) { delete sv; return cuda_fail(ce, "fg_server_create"); }
     if (sv->o.hbm_budget_bytes == 0) {
         size_t fr = 0, tot = 0;
@@ -226,7 +358,8 @@ int fg_server_create(fg_server **out, const fg_server_opts *opts)
     }
     sv->t0 = std::chrono::steady_clock::now();
     sv->worker = std::thread([sv] { sv->run(); });
-    sv->worker_eu = std::thread([sv] { sv->run_euler(); });
+    sv->worker_eub = std::thread([sv] { sv->run_euler_batch(); });
+    for (int i = 0; i < kEulerWorkers; ++i) sv->workers_eu.emplace_back([sv] { sv->run_euler(); });
     *out = sv;
     return FG_OK;
 }
@@ -237,7 +370,7 @@ int fg_server_submit(fg_server *sv, fg_system *s, const fg_transport_coeffs *c, 
     if (!s->geometry_ok) { set_error("fg_server_submit: the system has no geometry (fg_set_geometry)"); return FG_ERR_STATE; }
     if (s->topo.ndof != 1) { set_error("fg_server_submit: transport systems have ndof == 1"); return FG_ERR_UNSUPPORTED; }
     if (s->device != sv->device) { set_error("fg_server_submit: system on another device"); return FG_ERR_ARG; }
-    Request r{s, *c, tag, sv->now(), 0.0, workspace_bytes(s, sv->cfg.kmax, sv->cfg.mixed)};
+    Request r{s, *c, tag, sv->now(), 0.0, request_bytes(s, sv->cfg.kmax, sv->cfg.mixed, false)};
     {
         std::lock_guard<std::mutex> l(sv->mu);
         if (sv->error) { set_error(sv->error_text); return sv->error; }
@@ -257,7 +390,7 @@ int fg_server_submit_euler(fg_server *sv, fg_system *s, const fg_euler_coeffs *c
         return FG_ERR_STATE;
     }
     if (s->device != sv->device) { set_error("fg_server_submit_euler: system on another device"); return FG_ERR_ARG; }
-    EulerRequest r{s, *c, *t, u, tag, sv->now()};
+    EulerRequest r{s, *c, *t, u, tag, sv->now(), request_bytes(s, sv->cfg.kmax, sv->cfg.mixed, true)};
     {
         std::lock_guard<std::mutex> l(sv->mu);
         if (sv->error) { set_error(sv->error_text); return sv->error; }
@@ -304,9 +437,18 @@ int fg_server_destroy(fg_server *sv)
     sv->cv_work.notify_all();
     sv->cv_work_eu.notify_all();
     if (sv->worker.joinable()) sv->worker.join();
-    if (sv->worker_eu.joinable()) sv->worker_eu.join();
+    for (auto &w : sv->workers_eu)
+        if (w.joinable()) w.join();                   // running loops finish first
+    {
+        std::lock_guard<std::mutex> l(sv->mu);
+        sv->stop_eub = true;
+    }
+    sv->cv_eu_batch.notify_all();
+    if (sv->worker_eub.joinable()) sv->worker_eub.join();
     cudaStreamSynchronize(sv->st);
     cudaStreamDestroy(sv->st);
+    cudaStreamSynchronize(sv->st_eu);
+    cudaStreamDestroy(sv->st_eu);
     delete sv;
     return FG_OK;
 }

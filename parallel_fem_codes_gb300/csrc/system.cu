@@ -793,7 +793,8 @@ namespace fg {
 //                      stage alpha 1/(2 - lambda) over (1 - lambda) dt)
 template <class Assemble>
 static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble, const fg_solver_opts *o,
-                     const fg_time_opts *to, double *u, double *a, fg_time_stats *stats)
+                     const fg_time_opts *to, double *u, double *a, fg_time_stats *stats,
+                     const CorrectionSolve *solve = nullptr)
 {
     if (to->precond < FG_PRECOND_NONE || to->precond > FG_PRECOND_SPIKE) {
         set_error("time-loop preconditioner must be NONE, DIAG, BLOCKDIAG, ILU0 or SPIKE");
@@ -839,9 +840,13 @@ static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble,
             if ((rr = precond_setup_device(s, to->precond, flags, s->rhs_b.as<double>(), s->stream))) return rr;
             s->rhs_ok = true;
             cfg.precond = s->precond;
-            std::vector<BatchMember> mem{{s, s->rhs_b.as<double>(), s->rhs_f.as<double>(), nullptr}};
             fg_solve_stats st{};
-            if ((rr = solve_batch(mem, cfg, &st, s->stream))) return rr;
+            if (solve) {
+                if ((rr = (*solve)(s, cfg, &st))) return rr;
+            } else {
+                std::vector<BatchMember> mem{{s, s->rhs_b.as<double>(), s->rhs_f.as<double>(), nullptr}};
+                if ((rr = solve_batch(mem, cfg, &st, s->stream))) return rr;
+            }
             gmres += st.iterations;
             last_res = st.true_rel_residual;
             const double *Da = s->ws.x.as<double>();
@@ -944,12 +949,8 @@ static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble,
 }
 
 
-}  // namespace fg
-
-extern "C" {
-
-int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *o, const fg_time_opts *to,
-                       double *u, double *a, fg_time_stats *stats)
+int euler_predictor_hooked(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *o, const fg_time_opts *to,
+                           double *u, double *a, fg_time_stats *stats, const CorrectionSolve *solve)
 {
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
     // the DD element state starts at zero with the loop (Predictor_Old.c callocs uB and delta_old)
@@ -961,7 +962,17 @@ int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_o
                          cc.dt = db;
                          return euler_assemble_device(s, &cc, du, da, R, s->stream);
                      },
-                     o, to, u, a, stats);
+                     o, to, u, a, stats, solve);
+}
+
+}  // namespace fg
+
+extern "C" {
+
+int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *o, const fg_time_opts *to,
+                       double *u, double *a, fg_time_stats *stats)
+{
+    return euler_predictor_hooked(s, c, o, to, u, a, stats, nullptr);
 }
 
 int fg_tt_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, const double *du, double *R)

@@ -1,5 +1,6 @@
 // The fg_system object and the batched Krylov engine (internal).
 #pragma once
+#include <functional>
 #include <memory>
 #include <vector>
 
@@ -219,6 +220,16 @@ size_t norm_scratch_bytes();
 // Transient transport (setup.cu)
 int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev, const double *du_dev, double *R_dev,
                        cudaStream_t st);
+// The correction solve of a time loop: the system's resident right-hand
+// side (B = rhs_b, Ftrue = rhs_f, device, internal numbering) solved into
+// ws.x with cfg; stats receives the result.  The time loops solve alone by
+// default; the request server passes one that joins its Euler batch.
+using CorrectionSolve = std::function<int(fg_system *, const SolveConfig &, fg_solve_stats *)>;
+int euler_predictor_hooked(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *o, const fg_time_opts *to,
+                           double *u, double *a, fg_time_stats *stats, const CorrectionSolve *solve);
+// Device bytes a request will hold once admitted: the system's arrays plus
+// the Krylov workspace and, for time loops, the loop's state vectors.
+size_t request_bytes(const fg_system *s, int kmax, int mixed, bool time_loop);
 // Euler (euler.cu)
 int euler_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
                           double *R_dev, cudaStream_t st);

@@ -114,3 +114,52 @@ def test_server_euler_rejects_transport_system(fg):
     with pytest.raises(fg.FemGpuError):
         sv.submit_euler(s, G.obliquo_problem(9), fg.time_opts(0, 1, 1e-3, 0, 1.0, 1e-6, max_steps=1), 7)
     sv.close()
+
+
+def test_server_budget_admits_one_at_a_time_from_idle(fg):
+    """A byte budget smaller than one request: four requests submitted to an
+    idle server are admitted one at a time (a request larger than the budget
+    still runs, alone), transport and Euler alike."""
+    probs = [G.transport_problem(33, angle_deg=40.0 * i, k=1e-4) for i in range(4)]
+    systems = [fg.transport_system(p) for p in probs]
+    ep = G.obliquo_problem(17)
+    es = fg.euler_system(ep)
+    to = fg.time_opts(0, 2, 1e-3, 0, 2 * ep.dt, 1e-6, max_steps=2)
+    sv = fg.Server(precision=fg.FG_PREC_MIXED, hbm_budget_bytes=1)
+    for i, (s, p) in enumerate(zip(systems, probs)):
+        sv.submit(s, p, i)
+    sv.submit_euler(es, ep, to, 10)
+    sv.wait(5, timeout=120)
+    res = sorted(sv.poll(), key=lambda r: r["t_admit"])
+    sv.close()
+    assert len(res) == 5 and all(r["converged"] == 1 for r in res)
+    for a, b in zip(res, res[1:]):
+        assert b["t_admit"] >= a["t_done"]      # never two admitted at once
+
+
+def test_served_euler_loops_share_cycles(fg):
+    """Several Euler loops submitted together run at the same time (their
+    correction solves share the Euler batch) and each ends in exactly the
+    state of its solo fg_euler_predictor run."""
+    eprobs = [G.obliquo_problem(n) for n in (17, 25, 33, 21)]
+    topts = [fg.time_opts(0, 2, 1e-3, 0, 3 * p.dt, 1e-6, max_steps=3) for p in eprobs]
+    solo = []
+    for p, to in zip(eprobs, topts):
+        s = fg.euler_system(p)
+        u, a, st = s.euler_predictor(p, to, kmax=30, lmax=10000, tol=1e-10, precision=fg.FG_PREC_MIXED)
+        solo.append((u, st))
+    esys = [fg.euler_system(p) for p in eprobs]
+    sv = fg.Server(precision=fg.FG_PREC_MIXED)
+    for i, (s, p, to) in enumerate(zip(esys, eprobs, topts)):
+        sv.submit_euler(s, p, to, i)
+    sv.wait(len(eprobs), timeout=120)
+    res = {r["tag"]: r for r in sv.poll()}
+    sv.close()
+    assert sorted(res) == list(range(len(eprobs)))
+    for i, (u0, st0) in enumerate(solo):
+        assert np.array_equal(res[i]["u"], u0)
+        assert res[i]["iterations"] == st0["gmres_iterations"]
+        assert res[i]["cycles"] == st0["corrections"]
+    overlaps = sum(res[i]["t_admit"] < res[j]["t_done"] and res[j]["t_admit"] < res[i]["t_done"]
+                   for i in res for j in res if i < j)
+    assert overlaps >= 3
