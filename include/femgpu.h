@@ -173,6 +173,23 @@ int fg_set_spike(fg_system *s, int k, int parts);
  * ilup.c:164-301); 0 (the default) is ILU(0).  FG_PRECOND_ILU0 then sets up
  * and applies ILU(p) on the factor pattern; p in [0, 16]. */
 int fg_set_ilu_fill(fg_system *s, int p);
+/* Block-Jacobi ILU(p): the CSR operator's rows (RCM numbering) cut into
+ * `blocks` equal row blocks, and only the couplings inside a block are
+ * factorised -- what `blocks` MPI ranks of the reference compute, each
+ * factorising its own rows' block (CSR/ILUp_precond_setup.c:20-29).  The
+ * substitutions' dependency depth drops about blocks-fold.  1 (the
+ * default) is the global ILU(p). */
+int fg_set_ilu_blocks(fg_system *s, int blocks);
+/* Polls (>= 1) a device-side dependency wait of the ILU kernels makes
+ * before it gives up and the call returns FG_ERR_TIMEOUT (default 2^24,
+ * about half a second); applies to the current device. */
+int fg_set_wait_limit(long long polls);
+/* Cap (bytes) on the device memory the library allocates in this process;
+ * an allocation that would pass it fails with FG_ERR_NOMEM and the call
+ * that needed it returns that code.  0 (the default) removes the cap.
+ * fg_memory_in_use gives the bytes currently allocated. */
+int fg_set_memory_limit(size_t bytes);
+size_t fg_memory_in_use(void);
 enum {
     FG_SETUP_ACCUMULATE = 1, /* Diag += new diagonal, as Diag_precond_EBE_setup
                                 does across nonlinear iterations              */

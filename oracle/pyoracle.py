@@ -717,6 +717,24 @@ def ilup(IA, JA, AA, p):
     return FIA, FJA, FDG, LU, D
 
 
+def block_diagonal_csr(IA, JA, AA, blocks):
+    """The couplings among the rows of each of `blocks` equal row blocks
+    (rows q n / P .. (q+1) n / P - 1): the CSR block each MPI rank of the
+    reference factorises by itself (CSR/ILUp_precond_setup.c:20-29, the
+    rank's own rows and columns).  Returns (IA, JA, AA) of that matrix."""
+    IA = np.asarray(IA)
+    JA = np.asarray(JA)
+    AA = np.asarray(AA)
+    n = len(IA) - 1
+    blk = np.empty(n, dtype=np.int64)
+    for q in range(blocks):
+        blk[q * n // blocks:(q + 1) * n // blocks] = q
+    rows = np.repeat(np.arange(n), np.diff(IA))
+    keep = blk[JA[:IA[-1]]] == blk[rows]
+    BIA = np.concatenate([[0], np.cumsum(np.bincount(rows[keep], minlength=n))]).astype(np.int32)
+    return BIA, JA[:IA[-1]][keep].astype(np.int32), AA[:IA[-1]][keep].astype(np.float64)
+
+
 def ilup_apply(FIA, FJA, FDG, LU, D, y):
     L = lib()
     n = len(FIA) - 1

@@ -25,8 +25,10 @@
 // waits for the row its entry reads.  The rows of one pass are of one level
 // and never read each other, so no lane waits for a row of its own warp,
 // and every row waited for belongs to a pass claimed earlier by a running
-// warp: the waits always end.  They are still bounded (kSpinLimit polls); a
-// wait that runs out records FG_ERR_TIMEOUT.  Level order keeps the
+// warp: the waits always end.  They are still bounded (g_spin_limit polls,
+// set by fg_set_wait_limit); a wait that runs out records FG_ERR_TIMEOUT
+// and the row goes on with 0 for the missing value, so no later wait
+// hangs on it.  Level order keeps the
 // critical path at the depth of the dependency graph: in plain row order a
 // warp that works through a run of rows turns the chain row i -> row i-1 of
 // a CSR matrix into a chain of the whole matrix.
@@ -49,12 +51,14 @@
 
 namespace fg {
 
-constexpr long kSpinLimit = 1L << 24;
+// Polls of a bounded dependency wait (fg_set_wait_limit; ~0.5 s at the
+// default, each poll after the first few sleeping 32 ns).
+__device__ long long g_spin_limit = 1LL << 24;
 
 __device__ __forceinline__ bool wait_ready(const int *flag, int *err)
 {
     cuda::atomic_ref<const int, cuda::thread_scope_device> a(*flag);
-    for (long it = 0; it < kSpinLimit; ++it) {
+    for (long long it = 0; it < g_spin_limit; ++it) {
         if (a.load(cuda::memory_order_acquire)) return true;
         __nanosleep(32);
     }
@@ -99,7 +103,7 @@ template <typename T>
 __device__ __forceinline__ T wait_value(const T *p, int *err)
 {
     cuda::atomic_ref<const T, cuda::thread_scope_device> a(*p);
-    for (long it = 0; it < kSpinLimit; ++it) {
+    for (long long it = 0; it < g_spin_limit; ++it) {
         const T v = a.load(cuda::memory_order_relaxed);
         if (!Pending<T>::is(v)) return v;
         if (it >= 4) __nanosleep(32);
@@ -421,7 +425,7 @@ __global__ void k_ilu_pending(const SysDev *__restrict__ sys, const DChunk *__re
 __global__ void k_scatter_map(int nnz, const int *__restrict__ map, const double *__restrict__ a, double *__restrict__ b)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k < nnz) b[map[k]] = a[k];
+    if (k < nnz && map[k] >= 0) b[map[k]] = a[k];     // -1: a coupling between ILU blocks
 }
 
 __global__ void k_f64_to_f32(const double *a, float *b, int n)
@@ -566,7 +570,27 @@ int ilu_pattern_setup(fg_system *s)
     ja.resize(std::max(ia[n], 0));
     if (!ja.empty()) FG_CUDA(cudaMemcpy(ja.data(), s->csr_ja.p, sizeof(int) * ja.size(), cudaMemcpyDeviceToHost));
     std::vector<int> fia, fja, fdg, map(ja.size());
-    ilu_fill(n, ia, ja, s->ilu_p, fia, fja, fdg);
+    // ilu_blocks > 1: block Jacobi, as the reference's ranks each factorise
+    // the couplings among their own rows (CSR/ILUp_precond_setup.c:20-29,
+    // A->n = neq, the rank's "own" CSR block): entries that couple two row
+    // blocks are left out of the factor pattern (their slots map to -1)
+    std::vector<int> bia, bja;
+    const std::vector<int> *pia = &ia, *pja = &ja;
+    if (s->ilu_blocks > 1 && n > 0) {
+        const int P = std::min(s->ilu_blocks, n);
+        std::vector<int> blk(n);
+        for (int q = 0; q < P; ++q)
+            for (int i = (int)((long long)q * n / P); i < (int)((long long)(q + 1) * n / P); ++i) blk[i] = q;
+        bia.assign(n + 1, 0);
+        for (int i = 0; i < n; ++i) {
+            for (int q = ia[i]; q < ia[i + 1]; ++q)
+                if (blk[ja[q]] == blk[i]) bja.push_back(ja[q]);
+            bia[i + 1] = (int)bja.size();
+        }
+        pia = &bia;
+        pja = &bja;
+    }
+    ilu_fill(n, *pia, *pja, s->ilu_p, fia, fja, fdg);
     {
         std::vector<int> at(n, -1);
         for (int i = 0; i < n; ++i) {
@@ -711,6 +735,12 @@ int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st)
 }
 
 // kPending into the outputs of the next substitutions of a batch.
+int set_wait_limit(long long polls)
+{
+    FG_CUDA(cudaMemcpyToSymbol(g_spin_limit, &polls, sizeof(polls)));
+    return FG_OK;
+}
+
 int launch_ilu_pending(const SysDev *sys, const DChunk *ch, const int *nch, int n_dch, int sel, int fp32,
                        cudaStream_t st)
 {

@@ -155,7 +155,7 @@ __global__ void k_diag_setup(const int *__restrict__ dptr, const int *__restrict
 // Nodal B x B diagonal blocks (EBE/BlockDiag_precond_EBE_setup.c:70-80,
 // EBE/BlockDiagDOF3_precond_EBE_setup.c:66-76) and their closed-form
 // inverses (matrix_Inverse :90-147, DOF3_matrix_Inverse :84-124).
-__device__ void inv4(const double *B, double *R, bool quirk)
+__device__ double inv4(const double *B, double *R, bool quirk)
 {
     double a=B[0],b=B[1],c=B[2],d=B[3],e=B[4],f=B[5],g=B[6],h=B[7];
     double i=B[8],j=B[9],k=B[10],l=B[11],m=B[12],n=B[13],o=B[14],p=B[15];
@@ -181,9 +181,10 @@ __device__ void inv4(const double *B, double *R, bool quirk)
     // the reference writes c*j*m in entry 14 where the cofactor has c*f*m
     R[14] = q*((quirk ? c*j*m : c*f*m) - b*g*m - c*e*n + a*g*n + b*e*o - a*f*o);
     R[15] = q*(-c*f*i + b*g*i + c*e*j - a*g*j - b*e*k + a*f*k);
+    return det;
 }
 
-__device__ void inv3(const double *B, double *R)
+__device__ double inv3(const double *B, double *R)
 {
     double a=B[0],b=B[1],c=B[2],d=B[3],e=B[4],f=B[5],g=B[6],h=B[7],i=B[8];
     double det = a*e*i - a*f*h - b*d*i + b*f*g + c*d*h - c*e*g;
@@ -191,19 +192,24 @@ __device__ void inv3(const double *B, double *R)
     R[0] = q*(e*i - f*h); R[1] = q*(c*h - b*i); R[2] = q*(b*f - c*e);
     R[3] = q*(f*g - d*i); R[4] = q*(a*i - c*g); R[5] = q*(c*d - a*f);
     R[6] = q*(d*h - e*g); R[7] = q*(b*g - a*h); R[8] = q*(a*e - b*d);
+    return det;
 }
 
-__device__ void inv2(const double *B, double *R)
+__device__ double inv2(const double *B, double *R)
 {
     double det = B[0] * B[3] - B[1] * B[2];
     double q = 1.0 / det;
     R[0] = q * B[3]; R[1] = -q * B[1]; R[2] = -q * B[2]; R[3] = q * B[0];
+    return det;
 }
 
+// A node with a free dof whose block is singular (zero or non-finite
+// determinant) sets *err to FG_ERR_BREAKDOWN; its inverse is still written
+// as the reference computes it.
 template <int B>
 __global__ void k_blockdiag_setup(const int *__restrict__ nptr, const int *__restrict__ ninc, const double *__restrict__ A64,
                                   int ld, int nnodes, int quirk, double *__restrict__ bd, double *__restrict__ ibd64,
-                                  float *__restrict__ ibd32)
+                                  float *__restrict__ ibd32, const int *__restrict__ node_dof, int n, int *err)
 {
     int nd = blockIdx.x * blockDim.x + threadIdx.x;
     if (nd >= nnodes) return;
@@ -215,9 +221,12 @@ __global__ void k_blockdiag_setup(const int *__restrict__ nptr, const int *__res
         for (int r = 0; r < B; ++r)
             for (int c = 0; c < B; ++c) blk[r * B + c] += A64[(size_t)((B * v + r) * S + B * v + c) * ld + pos];
     }
-    if (B == 4) inv4(blk, inv, quirk != 0);
-    else if (B == 3) inv3(blk, inv);
-    else inv2(blk, inv);
+    const double det = B == 4 ? inv4(blk, inv, quirk != 0) : B == 3 ? inv3(blk, inv) : inv2(blk, inv);
+    if (!(det != 0.0) || !isfinite(det)) {
+        bool free_dof = false;
+        for (int a = 0; a < B; ++a) free_dof |= node_dof[nd * B + a] != n;
+        if (free_dof) atomicExch(err, FG_ERR_BREAKDOWN);
+    }
     for (int q = 0; q < B * B; ++q) {
         bd[(size_t)nd * B * B + q] = blk[q];
         ibd64[(size_t)nd * B * B + q] = inv[q];
@@ -269,9 +278,18 @@ int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaS
         const int *np = s->ninc_ptr.as<int>(), *ni = s->ninc.as<int>();
         double *bd = s->bd.as<double>(), *i64 = s->ibd64.as<double>();
         float *i32 = s->ibd32.as<float>();
-        if (B == 4) k_blockdiag_setup<4><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32);
-        else if (B == 3) k_blockdiag_setup<3><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32);
-        else k_blockdiag_setup<2><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32);
+        const int *nd = s->node_dof.as<int>();
+        int *err = s->pc_err.as<int>();
+        FG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+        if (B == 4)
+            k_blockdiag_setup<4><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32,
+                                                    nd, t.n, err);
+        else if (B == 3)
+            k_blockdiag_setup<3><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32,
+                                                    nd, t.n, err);
+        else
+            k_blockdiag_setup<2><<<g, 128, 0, st>>>(np, ni, s->A64.as<double>(), s->nel_pad, t.nnodes, q, bd, i64, i32,
+                                                    nd, t.n, err);
         FG_CUDA(cudaGetLastError());
     count_launches(1);
         s->precond = kind;

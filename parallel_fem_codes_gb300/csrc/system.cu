@@ -1,3 +1,4 @@
+#include <atomic>
 // fg_system lifecycle and the public C ABI (include/femgpu.h).
 #include <algorithm>
 #include <chrono>
@@ -24,13 +25,34 @@ int cuda_fail(cudaError_t e, const char *what)
 // non-blocking streams are not ordered after, and cudaMemset returns before
 // it is done: wait for it, or a copy queued next on another stream could
 // land first and be zeroed.
+// Device bytes held by the library's allocations, and the optional cap on
+// them (fg_set_memory_limit; 0 = none).
+static std::atomic<size_t> g_dev_bytes{0}, g_dev_limit{0};
+
+void DevMem::release()
+{
+    if (p) {
+        cudaFree(p);
+        g_dev_bytes -= bytes;
+    }
+    p = nullptr;
+    bytes = 0;
+}
+
 int DevMem::alloc(size_t b)
 {
-    if (p) { cudaFree(p); p = nullptr; bytes = 0; }
+    release();
     if (b == 0) b = 16;
+    const size_t lim = g_dev_limit.load();
+    if (lim && g_dev_bytes.load() + b > lim) {
+        set_error("device allocation of " + std::to_string(b) + " bytes would pass the library's memory limit (" +
+                  std::to_string(lim) + " bytes)");
+        return FG_ERR_NOMEM;
+    }
     cudaError_t e = cudaMalloc(&p, b);
     if (e != cudaSuccess) { p = nullptr; return cuda_fail(e, "cudaMalloc"); }
     bytes = b;
+    g_dev_bytes += b;
     e = cudaMemset(p, 0, b);
     if (e == cudaSuccess) e = cudaStreamSynchronize(0);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemset");
@@ -155,7 +177,7 @@ int fg_system_create(fg_system **out, int nnodes, int nel, int ndof, const int *
         (r = upload(s->node_dof, t.node_dof)) || (r = upload(s->eorder, t.eorder)) || (r = upload(s->perm, perm)) ||
         (r = upload(s->gien, gien)) || (r = s->A64.alloc(8 * SS)) || (r = s->A32.alloc(4 * SS)) ||
         (r = s->diag.alloc(8 * (size_t)s->n_pad)) || (r = s->invd64.alloc(8 * (size_t)s->n_pad)) ||
-        (r = s->invd32.alloc(4 * (size_t)s->n_pad))) {
+        (r = s->invd32.alloc(4 * (size_t)s->n_pad)) || (r = s->pc_err.alloc(16))) {
         delete s;
         return r;
     }
@@ -328,9 +350,16 @@ int fg_precond_setup(fg_system *s, int kind, int flags, double *F)
     if (F) {
         if ((r = vec_out(s, fd, F, s->ws.r64.as<double>()))) return r;
     }
+    int perr = 0;
+    if (kind == FG_PRECOND_BLOCKDIAG)
+        FG_CUDA(cudaMemcpyAsync(&perr, s->pc_err.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     FG_CUDA(cudaStreamSynchronize(s->stream));
     FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
     FG_CUDA(cudaStreamSynchronize(s->stream));
+    if (perr) {
+        set_error("block-diagonal set-up: a node with a free dof has a singular diagonal block");
+        return FG_ERR_BREAKDOWN;
+    }
     return FG_OK;
 }
 
@@ -524,6 +553,32 @@ int fg_set_ilu_fill(fg_system *s, int p)
     s->ilu_p = p;
     if (s->precond == FG_PRECOND_ILU0) s->precond = FG_PRECOND_NONE;   // set up again
     return s->csr_ok ? ilu_pattern_setup(s) : FG_OK;
+}
+
+int fg_set_ilu_blocks(fg_system *s, int blocks)
+{
+    if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (blocks < 1 || blocks > std::max(1, s->topo.n)) {
+        set_error("ILU blocks must be in [1, number of equations]"); return FG_ERR_ARG;
+    }
+    if (blocks == s->ilu_blocks) return FG_OK;
+    s->ilu_blocks = blocks;
+    if (s->precond == FG_PRECOND_ILU0) s->precond = FG_PRECOND_NONE;   // set up again
+    return s->csr_ok ? ilu_pattern_setup(s) : FG_OK;
+}
+
+int fg_set_memory_limit(size_t bytes)
+{
+    g_dev_limit = bytes;
+    return FG_OK;
+}
+
+size_t fg_memory_in_use(void) { return g_dev_bytes.load(); }
+
+int fg_set_wait_limit(long long polls)
+{
+    if (polls < 1) { set_error("wait limit must be >= 1 poll"); return FG_ERR_ARG; }
+    return set_wait_limit(polls);
 }
 
 int fg_get_csr(const fg_system *s, int *nnz, int *IA, int *JA, double *AA)

@@ -16,8 +16,9 @@ struct DevMem {
     DevMem() = default;
     DevMem(const DevMem &) = delete;
     DevMem &operator=(const DevMem &) = delete;
-    ~DevMem() { if (p) cudaFree(p); }
+    ~DevMem() { release(); }
     int alloc(size_t b);     // zero-filled (the fill has completed on return)
+    void release();
     template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
@@ -41,6 +42,7 @@ struct fg_system {
     fg::DevMem blob;                   // 3x3: per-patch index blobs of the bulk-copy matvec
     // preconditioners
     fg::DevMem diag, invd64, invd32, bd, ibd64, ibd32;
+    fg::DevMem pc_err;                 // set-up status word (singular nodal block)
     int precond = FG_PRECOND_NONE;
     bool blocks_ok = false;
     // geometry (device assembly)
@@ -66,6 +68,7 @@ struct fg_system {
     // ILU(p) factor pattern (per row: L ascending, diagonal, U in the order
     // the symbolic pass admits it) and the slot of every CSR entry in it
     int ilu_p = 0, lu_nnz = 0;
+    int ilu_blocks = 1;                // block-Jacobi ILU over this many row blocks (1: global)
     int scale_kind = 0;                // last fg_scale kind (fg_unscale follows it)
     fg::DevMem lu_ia, lu_ja, lu_dg, lu_map, AAf64;
     fg::DevMem csr_ia, csr_ja, csr_diag, csr_inc_ptr, csr_inc, AA64, AA32, LU64, LU32, dinv64, dinv32, ilu_flags,
@@ -94,6 +97,7 @@ int ilu_pattern_setup(fg_system *s);   // ILU(p) factor pattern and schedules (a
 int csr_refresh(fg_system *s, cudaStream_t st);
 int ilu0_setup_device(fg_system *s, double *F_dev, cudaStream_t st);
 int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st);
+int set_wait_limit(long long polls);   // bounded dependency waits of the ILU kernels
 int launch_ilu_pending(const SysDev *sys, const DChunk *ch, const int *nch, int n_dch, int sel, int fp32,
                        cudaStream_t st);
 int launch_ilu_solve(const SysDev *sys, const int2 *items, int nitems, int *counter, int *err, int sel, int backward,

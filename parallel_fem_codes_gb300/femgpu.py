@@ -27,6 +27,8 @@ FG_EULER_SUPG, FG_EULER_DD = 0, 1
 FG_SHOCK_NONE, FG_SHOCK_CAU, FG_SHOCK_CAUDD, FG_SHOCK_YZBETA = 0, 1, 2, 3
 FG_HSHOCK_2SQRTAREA, FG_HSHOCK_OPTION1, FG_HSHOCK_OPTION2 = 0, 1, 2
 FG_REORDER_NONE, FG_REORDER_RCM = 0, 1
+FG_ERR_ARG, FG_ERR_CUDA, FG_ERR_NOMEM, FG_ERR_STATE = 1, 2, 3, 4
+FG_ERR_BREAKDOWN, FG_ERR_NOTCONV, FG_ERR_UNSUPPORTED, FG_ERR_TIMEOUT = 5, 6, 7, 8
 STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_NOMEM", 4: "ERR_STATE",
           5: "ERR_BREAKDOWN", 6: "ERR_NOTCONV", 7: "ERR_UNSUPPORTED", 8: "ERR_TIMEOUT"}
 
@@ -158,6 +160,10 @@ def lib(build_if_missing: bool = True):
     L.fg_set_operator.argtypes = [_vp, _c_int]
     L.fg_set_spike.argtypes = [_vp, _c_int, _c_int]
     L.fg_set_ilu_fill.argtypes = [_vp, _c_int]
+    L.fg_set_ilu_blocks.argtypes = [_vp, _c_int]
+    L.fg_set_wait_limit.argtypes = [ctypes.c_longlong]
+    L.fg_set_memory_limit.argtypes = [ctypes.c_size_t]
+    L.fg_memory_in_use.restype = ctypes.c_size_t
     L.fg_get_csr.argtypes = [_vp, ctypes.POINTER(_c_int), _vp, _vp, _vp]
     L.fg_system_stream.argtypes = [_vp]
     L.fg_system_stream.restype = _vp
@@ -363,6 +369,10 @@ class System:
     def set_spike(self, k=16, parts=16):
         """Coupling size and block count of the SPIKE preconditioner."""
         check(lib().fg_set_spike(self._h, int(k), int(parts)))
+
+    def set_ilu_blocks(self, blocks):
+        """Block-Jacobi ILU over `blocks` row blocks (1: global ILU)."""
+        check(lib().fg_set_ilu_blocks(self._h, int(blocks)))
 
     def set_ilu_fill(self, p):
         """Fill level of FG_PRECOND_ILU0 (Preconditioner "ILU<p>")."""
@@ -583,6 +593,20 @@ def ns_system(prob, reorder=False) -> System:
 def _coeffs(prob):
     return TransportCoeffs(prob.k, prob.gamma, (_c_dbl * 2)(*prob.beta), prob.f, int(prob.cau),
                            int(getattr(prob, "form", 0)), int(getattr(prob, "h_shock", 0)))
+
+
+def set_wait_limit(polls=1 << 24):
+    """Polls of the ILU kernels' bounded dependency waits (current device)."""
+    check(lib().fg_set_wait_limit(ctypes.c_longlong(int(polls))))
+
+
+def set_memory_limit(nbytes=0):
+    """Cap on the device bytes the library allocates (0: none)."""
+    check(lib().fg_set_memory_limit(int(nbytes)))
+
+
+def memory_in_use() -> int:
+    return int(lib().fg_memory_in_use())
 
 
 def launch_count() -> int:

@@ -127,3 +127,54 @@ def test_gmres_ilup_fewer_iterations(fg):
         assert res <= 1e-9
         its.append(r.stats["iterations"])
     assert its[1] <= its[0]
+
+
+@pytest.mark.parametrize("blocks,lev", [(1, 0), (4, 0), (16, 0), (8, 1)])
+def test_block_jacobi_ilu_bit_exact(fg, blocks, lev):
+    """Block-Jacobi ILU(p) over equal row blocks of the RCM-ordered CSR
+    operator (each block factorised by itself, as each MPI rank of the
+    reference does) against the oracle's ILU(p) of the block-diagonal
+    matrix; one block is the global ILU(p)."""
+    p, m, A, F, perm, inv, IA, JA, AA, lm, s = _setup(fg, 33)
+    BIA, BJA, BAA = O.block_diagonal_csr(IA, JA, AA, blocks)
+    FIA, FJA, FDG, LU, D = O.ilup(BIA, BJA, BAA, lev)
+    s.set_ilu_fill(lev)
+    s.set_ilu_blocks(blocks)
+    Fp = s.precond_setup(fg.FG_PRECOND_ILU0, 0, F)
+    Fi = np.append(F[:-1][perm[:-1]], 0.0)
+    zi = O.ilup_apply(FIA, FJA, FDG, LU, D, Fi)
+    z = np.zeros(m.neq + 1)
+    z[perm[:-1]] = zi[:m.neq]
+    assert np.array_equal(Fp[:-1], z[:-1])
+
+
+def test_block_jacobi_ilu_gmres(fg):
+    """GMRES with block-Jacobi ILU(0): converges to the FP64 solution, with
+    more iterations than the global ILU(0) and fewer than Diag."""
+    p, m, A, F, perm, inv, IA, JA, AA, lm, s = _setup(fg, 65, angle=30.0, k=1e-6)
+    X0, it0, *_ = O.ebe_diag_solve(lm, A, m.neq, F, perm, inv, kmax=30, lmax=1000, tol=1e-12)
+    its = []
+    for blocks in (1, 16):
+        s.set_ilu_blocks(blocks)
+        Fp = s.precond_setup(fg.FG_PRECOND_ILU0, 0, F)
+        r = s.solve(Fp, tol=1e-10, F_true=F, precision=64)
+        assert r.stats["converged"] == 1
+        assert rel(r.x[:-1], X0[:-1]) <= 1e-8
+        its.append(r.stats["iterations"])
+    assert its[0] <= its[1] < it0
+
+
+def test_ilu_wait_limit_times_out_and_recovers(fg):
+    """A one-poll limit on the ILU kernels' dependency waits: the set-up
+    returns FG_ERR_TIMEOUT instead of waiting (the waits end; nothing
+    hangs), and with the default limit back the same set-up succeeds."""
+    p, m, A, F, perm, inv, IA, JA, AA, lm, s = _setup(fg, 129)
+    try:
+        fg.set_wait_limit(1)
+        with pytest.raises(fg.FemGpuError) as e:
+            s.precond_setup(fg.FG_PRECOND_ILU0, 0, F)
+        assert e.value.code == fg.FG_ERR_TIMEOUT
+    finally:
+        fg.set_wait_limit()
+    Fp = s.precond_setup(fg.FG_PRECOND_ILU0, 0, F)
+    assert np.all(np.isfinite(Fp))
