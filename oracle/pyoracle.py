@@ -19,10 +19,17 @@ ORACLE_FAST_SO = os.path.join(HERE, "_build", "libfemoracle_fast.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_sst.so")
 REF_NS_SO = os.path.join(HERE, "_ref", "libref_ns.so")
 REF_EU_SO = os.path.join(HERE, "_ref", "libref_euler.so")
+# the reference's drivers compiled unchanged but linked against the
+# library's drop-in shims (oracle/Makefile `dropin`): same fr_* entry points
+DROPIN_SO = {"sst": os.path.join(HERE, "_ref", "libdropin_sst.so"),
+             "ns": os.path.join(HERE, "_ref", "libdropin_ns.so"),
+             "euler": os.path.join(HERE, "_ref", "libdropin_euler.so")}
 # The reference's source tree (used only to build the checker): the
 # PFC_REFERENCE_DIR environment variable, else `reference` beside this
 # repository.
 REF_SRC = os.environ.get("PFC_REFERENCE_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
+if not os.path.isdir(REF_SRC) and os.path.isdir(os.path.join(HERE, "_build", "refcopy", "00_CommonFiles")):
+    REF_SRC = os.path.join(HERE, "_build", "refcopy")     # a private copy made by `make -C oracle refcopy`
 _use_fast = False
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -40,6 +47,9 @@ def build(ref: bool | None = None, fast: bool = False) -> None:
         ref = os.path.isdir(REF_SRC)
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+        lib_dir = os.path.join(os.path.dirname(HERE), "parallel_fem_codes_gb300", "_lib")
+        if all(os.path.exists(os.path.join(lib_dir, f"libfemgpu_{k}.so")) for k in ("sst", "ns", "euler")):
+            subprocess.run(["make", "-s", "-C", HERE, "dropin", f"REF={REF_SRC}"], check=True)
 
 
 _lib = None
@@ -118,11 +128,28 @@ def ref_available() -> bool:
     return os.path.exists(REF_SO)
 
 
-def ref():
-    """The reference's own C (oracle/_ref), or None where it was not built."""
+_loaded = {}
+
+
+def dropin_available() -> bool:
+    return all(os.path.exists(p) for p in DROPIN_SO.values())
+
+
+def ref(path=None):
+    """The reference's own C (oracle/_ref), or None where it was not built;
+    path: another build of the same harness (the drop-in build)."""
     global _ref
+    if path is not None:
+        if path not in _loaded and os.path.exists(path):
+            _loaded[path] = _setup_sst(ctypes.CDLL(path))
+        return _loaded.get(path)
     if _ref is None and ref_available():
-        R = ctypes.CDLL(REF_SO)
+        _ref = _setup_sst(ctypes.CDLL(REF_SO))
+    return _ref
+
+
+def _setup_sst(R):
+    if True:
         R.fr_sst_connectivity.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
                                           _i32p, _i32p, _i32p, _i32p]
         R.fr_sst_build.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
@@ -141,18 +168,26 @@ def ref():
         R.fr_sst_layout.restype = None
         R.fr_sst_set_form.argtypes = [_c_int, _c_int, _c_int]
         R.fr_sst_set_form.restype = None
-        _ref = R
-    return _ref
+    return R
 
 
 _ref_ns = None
 
 
-def ref_ns():
+def ref_ns(path=None):
     """The reference's steady Navier-Stokes driver (oracle/_ref), or None."""
     global _ref_ns
+    if path is not None:
+        if path not in _loaded and os.path.exists(path):
+            _loaded[path] = _setup_ns(ctypes.CDLL(path))
+        return _loaded.get(path)
     if _ref_ns is None and os.path.exists(REF_NS_SO):
-        R = ctypes.CDLL(REF_NS_SO)
+        _ref_ns = _setup_ns(ctypes.CDLL(REF_NS_SO))
+    return _ref_ns
+
+
+def _setup_ns(R):
+    if True:
         mesh = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int]
         R.fr_ns_lm.argtypes = mesh + [_i32p]
         R.fr_ns_lm.restype = None
@@ -168,18 +203,26 @@ def ref_ns():
         R.fr_ns_set_form.restype = None
         R.fr_ns_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
         R.fr_ns_layout.restype = None
-        _ref_ns = R
-    return _ref_ns
+    return R
 
 
 _ref_eu = None
 
 
-def ref_euler():
+def ref_euler(path=None):
     """The reference's Euler driver (oracle/_ref), or None."""
     global _ref_eu
+    if path is not None:
+        if path not in _loaded and os.path.exists(path):
+            _loaded[path] = _setup_eu(ctypes.CDLL(path))
+        return _loaded.get(path)
     if _ref_eu is None and os.path.exists(REF_EU_SO):
-        R = ctypes.CDLL(REF_EU_SO)
+        _ref_eu = _setup_eu(ctypes.CDLL(REF_EU_SO))
+    return _ref_eu
+
+
+def _setup_eu(R):
+    if True:
         mesh = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int]
         R.fr_eu_lm.argtypes = mesh + [_i32p]
         R.fr_eu_lm.restype = None
@@ -195,8 +238,7 @@ def ref_euler():
                                              _f64p, ctypes.POINTER(_c_dbl)]
         R.fr_eu_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
         R.fr_eu_layout.restype = None
-        _ref_eu = R
-    return _ref_eu
+    return R
 
 
 # ---------------------------------------------------------------- helpers
@@ -285,13 +327,14 @@ def ref_euler_ebemv(mesh, A, P):
     return Q
 
 
-def ref_euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000):
+def ref_euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000, dropin=False):
     """The reference's Predictor_Old; returns (u[neq], GMRES iterations, final t)."""
     m = prob.mesh
     u = np.zeros(m.neq + 1)
     t = _c_dbl(0.0)
-    ref_euler().fr_eu_set_form(int(getattr(prob, "form", 0)))
-    its = ref_euler().fr_eu_predictor(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
+    R = ref_euler(DROPIN_SO["euler"]) if dropin else ref_euler()
+    R.fr_eu_set_form(int(getattr(prob, "form", 0)))
+    its = R.fr_eu_predictor(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
                                       int(prob.wall), np.ascontiguousarray(prob.init), topts.as_array(),
                                       kmax, lmax, tol, u, ctypes.byref(t))
     return u[:m.neq].copy(), its, t.value
@@ -364,12 +407,14 @@ def ref_ns_ebemv(mesh, A, P):
     return Q
 
 
-def ref_ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=100, form=0):
+def ref_ns_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, max_nonlinear=100, form=0,
+                   dropin=False):
     m = prob.mesh
-    ref_ns().fr_ns_set_form(form)
+    R = ref_ns(DROPIN_SO["ns"]) if dropin else ref_ns()
+    R.fr_ns_set_form(form)
     u = np.zeros(m.neq + 1)
     its = _c_int(0)
-    ref_ns().fr_ns_process(*_mesh_args(m), prob.reynolds, np.ascontiguousarray(prob.coef.reshape(-1)),
+    R.fr_ns_process(*_mesh_args(m), prob.reynolds, np.ascontiguousarray(prob.coef.reshape(-1)),
                            int(prob.lid), solver_tol, nonlinear_tol, kmax, lmax, max_nonlinear, u,
                            ctypes.byref(its))
     return u[:m.neq].copy(), its.value
@@ -570,10 +615,10 @@ def ref_connectivity(mesh):
     return lm.reshape(mesh.nel, 3), perm, inv, band, nnz
 
 
-def _ref_form(prob):
+def _ref_form(prob, R=None):
     """StabilizationForm / ShockCapture of the reference run: "SUPG" or "DD",
     "CAU" (cau 1, and the reference's stand-in for cau 0) or "CAUDD"."""
-    ref().fr_sst_set_form(int(getattr(prob, "form", 0)), int(prob.cau) if int(prob.cau) in (2, 3) else 1,
+    (R or ref()).fr_sst_set_form(int(getattr(prob, "form", 0)), int(prob.cau) if int(prob.cau) in (2, 3) else 1,
                           int(getattr(prob, "h_shock", 0)))
 
 
@@ -590,12 +635,15 @@ def ref_build(prob, u=None):
     return A.reshape(m.nel, 9), F
 
 
-def ref_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000):
+def ref_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, dropin=False):
+    """The reference's Process loop (dropin: its drop-in build, the same
+    driver on the library's GPU solve path)."""
     m = prob.mesh
     U = np.zeros(m.neq + 1)
     its = _c_int(0)
-    _ref_form(prob)
-    ref().fr_sst_process(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f,
+    R = ref(DROPIN_SO["sst"]) if dropin else ref()
+    _ref_form(prob, R)
+    R.fr_sst_process(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f,
                          prob.upmode, prob.upval, solver_tol, nonlinear_tol, kmax, lmax, U, ctypes.byref(its))
     return U[:m.neq].copy(), its.value
 

@@ -5,19 +5,30 @@
  * libfemgpu_euler.so for the Euler driver (ebemvNDOF4, BlockDiag_precond
  * and its EBE set-up).  Both also export pgmres, Diag_precond,
  * Diag_precond_EBE_setup, NO_precond and NO_precond_setup, with the
- * reference's names and signatures, running on the GPU through libfemgpu.
+ * reference's names and signatures, running on the GPU through libfemgpu,
+ * and for MatrixVectorProductScheme "CSR" csr_assembly, csrmv,
+ * ILUp_precond(_setup) ("ILU<p>") and SPIKE_precond(_setup) ("SPIKEk").
  * Linking one of them instead of the reference's pgmres.c,
- * MatrixVector_Operations/EBE/ebemvNDOF*.c and the preconditioner files
- * leaves every driver file (Process.c, Predictor_Old.c, the Build
- * functions) unchanged.  The BLAS-1 helpers the drivers call on host arrays
- * (ddot.c, daxpy.c, ...) stay the driver's own.
+ * MatrixVector_Operations/EBE/ebemvNDOF*.c, CSR/csrmv.c, the driver's
+ * csr_assembly.c and the preconditioner files leaves every driver file
+ * (Process.c, Predictor_Old.c, the Build functions) unchanged.  The BLAS-1
+ * helpers the drivers call on host arrays (ddot.c, daxpy.c, ...) stay the
+ * driver's own.
  *
  * One rank only (NPROC = 1): neq_bef = 0, NEQ = neq, vectors of NEQ + 1.
  * The GPU system of a MatrixDataType is created on first use from the
- * driver's Node/Element arrays (EBE storage: no reordering, as
- * setMatrixVectorProductType.c requires) and cached in a small table keyed
- * by the MatrixDataType pointer.  Errors print the library's message and
- * exit(1) as the reference does, unless FEMGPU_COMPAT_NO_EXIT is set.
+ * driver's Node/Element arrays and cached in a small table keyed by the
+ * MatrixDataType pointer: EBE storage keeps the node numbering (as
+ * setMatrixVectorProductType.c requires), CSR storage uses the reference's
+ * RCM renumbering unless Parameters->reordering is "NOT".  CSR storage:
+ * csr_assembly keeps each element's block (the library sums the blocks
+ * into its CSR values in element order), so MatrixData->AA is not filled;
+ * every consumer of AA on the solve path is in this shim.  SPIKE's
+ * row-block count (the reference's rank count) is FEMGPU_SPIKE_BLOCKS
+ * (default 16); FEMGPU_ILU_BLOCKS (default 1) gives block-Jacobi ILU over
+ * that many row blocks, as that many ranks would factorise.  Errors print
+ * the library's message and exit(1) as the reference does, unless
+ * FEMGPU_COMPAT_NO_EXIT is set.
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -50,7 +61,16 @@ static struct {
     const MatrixDataType *key;
     fg_system *sys;
     int nel, neq;
+    double *blocks;     /* CSR storage: element blocks captured by csr_assembly */
+    int csr;            /* the system runs on the CSR operator */
 } g_tab[FGC_MAX_SYSTEMS];
+
+static int fgc_slot(const MatrixDataType *M)
+{
+    for (int i = 0; i < FGC_MAX_SYSTEMS; i++)
+        if (g_tab[i].key == M) return i;
+    return -1;
+}
 
 static int fgc_fail(int rc, const char *where)
 {
@@ -87,20 +107,35 @@ static fg_system *fgc_system(ParametersType *P, MatrixDataType *M, FemStructsTyp
         ien[3 * i + 2] = S->Element[i].Vertex[2];
     }
     fg_system *sys = NULL;
-    int rc = fg_system_create(&sys, nn, ne, FGC_NDOF, ien, type, invp, P->neq, FG_REORDER_NONE);
+    const int csr = strcasecmp(P->MatrixVectorProductScheme, "CSR") == 0;
+    const int reorder = csr && strcasecmp(P->reordering, "NOT") != 0 ? FG_REORDER_RCM : FG_REORDER_NONE;
+    int rc = fg_system_create(&sys, nn, ne, FGC_NDOF, ien, type, invp, P->neq, reorder);
     free(type); free(invp); free(ien);
     if (rc) { fgc_fail(rc, "system set-up"); return NULL; }
     g_tab[free_slot].key = M;
     g_tab[free_slot].sys = sys;
     g_tab[free_slot].nel = ne;
     g_tab[free_slot].neq = P->neq;
+    g_tab[free_slot].blocks = NULL;
+    g_tab[free_slot].csr = 0;
+    if (csr) {
+        g_tab[free_slot].blocks = calloc((size_t)ne * FGC_S * FGC_S, sizeof(double));
+        if (!g_tab[free_slot].blocks) { fgc_fail(FG_ERR_NOMEM, "CSR block buffer"); return NULL; }
+    }
     return sys;
 }
 
-/* Element blocks as the Build function left them: nel rows of S*S in Aaux */
+/* Element blocks as the Build function left them: nel rows of S*S in Aaux
+ * (EBE), or as csr_assembly captured them (CSR). */
 static int fgc_upload_blocks(fg_system *sys, MatrixDataType *M)
 {
-    int rc = fg_set_blocks(sys, M->Aaux);
+    int i = fgc_slot(M);
+    const double *blk = i >= 0 && g_tab[i].blocks ? g_tab[i].blocks : M->Aaux;
+    int rc = fg_set_blocks(sys, blk);
+    if (!rc && i >= 0 && g_tab[i].blocks && !g_tab[i].csr) {
+        rc = fg_set_operator(sys, FG_OP_CSR);
+        if (!rc) g_tab[i].csr = 1;
+    }
     return rc ? fgc_fail(rc, "element blocks") : 0;
 }
 
@@ -176,17 +211,92 @@ int FGC_MV(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *Pv, 
     return rc ? fgc_fail(rc, "EBE matvec") : 0;
 }
 
-/* pgmres (pgmres.c:5-200) on the GPU when mv is this shim's matvec and the
- * preconditioner is one of this shim's; the blocks and the preconditioner
- * come from the *_setup call that precedes every solve (NS Process.c:37-38,
- * Predictor_Old.c:95-96).  Parameters->iterations grows by the Arnoldi steps. */
+/* csr_assembly (EU and NS csr_assembly.c): the element's S x S block is
+ * kept; the library sums the blocks into its CSR values in element order
+ * when a CSR consumer below runs. */
+void csr_assembly(ParametersType *P, MatrixDataType *M, FemStructsType *S, int E, double (*Me)[FGC_S])
+{
+    if (!fgc_system(P, M, S)) return;
+    int i = fgc_slot(M);
+    if (i < 0 || !g_tab[i].blocks || E < 0 || E >= g_tab[i].nel) return;
+    double *b = g_tab[i].blocks + (size_t)E * FGC_S * FGC_S;
+    for (int a = 0; a < FGC_S; a++)
+        for (int c = 0; c < FGC_S; c++) b[FGC_S * a + c] = Me[a][c];
+}
+
+/* csrmv (MatrixVector_Operations/CSR/csrmv.c:4-65): Q = A P, Q[NEQ] = 0. */
+int csrmv(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *Pv, double *Qv)
+{
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys || fgc_upload_blocks(sys, M)) return 1;
+    Pv[P->NEQ] = 0.0;
+    int rc = fg_matvec(sys, Pv, Qv, 64);
+    return rc ? fgc_fail(rc, "csrmv") : 0;
+}
+
+/* ILUp_precond_setup (CSR/ILUp_precond_setup.c:8-168) for "ILU<p>": ILU(p)
+ * of the CSR operator (p = atoi(&Preconditioner[3]), capped at neq as the
+ * reference caps it), F preconditioned in place. */
+int ILUp_precond_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
+{
+    (void)tag;
+    int p = atoi(&P->Preconditioner[3]);
+    if (p > P->neq) p = P->neq;
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys || fgc_upload_blocks(sys, M)) return 1;
+    const char *e = getenv("FEMGPU_ILU_BLOCKS");
+    int rc = fg_set_ilu_fill(sys, p > 16 ? 16 : p);
+    if (!rc) rc = fg_set_ilu_blocks(sys, e && atoi(e) > 0 ? atoi(e) : 1);
+    if (!rc) rc = fg_precond_setup(sys, FG_PRECOND_ILU0, 0, F);
+    return rc ? fgc_fail(rc, "ILUp_precond_setup") : 0;
+}
+
+/* ILUp_precond (CSR/ILUp_precond.c:4-47): z = (LU)^-1 p (p may be z). */
+int ILUp_precond(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    return fgc_apply(P, M, S, p, z, "ILUp_precond");
+}
+
+/* SPIKE_precond_setup (CSR/SPIKE_precond_setup.c:10-312): k from the
+ * "SPIKEk" string as the reference reads it (:54), the row blocks from
+ * FEMGPU_SPIKE_BLOCKS; F preconditioned in place. */
+int SPIKE_precond_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
+{
+    (void)tag;
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    int k = atoi(&P->Preconditioner[5]);
+    const char *e = getenv("FEMGPU_SPIKE_BLOCKS");
+    int rc = fg_set_spike(sys, k, e ? atoi(e) : 16);
+    if (rc) return fgc_fail(rc, "SPIKE_precond_setup");
+    if (fgc_upload_blocks(sys, M)) return 1;
+    rc = fg_precond_setup(sys, FG_PRECOND_SPIKE, 0, F);
+    if (rc) return fgc_fail(rc, "SPIKE_precond_setup");
+    P->k_SPIKE_block_size = k;
+    return 0;
+}
+
+/* SPIKE_precond (CSR/SPIKE_precond.c:8-158): z = M^-1 p (p may be z). */
+int SPIKE_precond(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    return fgc_apply(P, M, S, p, z, "SPIKE_precond");
+}
+
+/* pgmres (pgmres.c:5-200) on the GPU when mv is this shim's matvec (EBE or
+ * CSR) and the preconditioner is one of this shim's; the blocks and the
+ * preconditioner come from the *_setup call that precedes every solve (NS
+ * Process.c:37-38, Predictor_Old.c:95-96).  Parameters->iterations grows by
+ * the Arnoldi steps. */
 int pgmres(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctionsType *Fn, double *B, double *X)
 {
     fg_system *sys = fgc_system(P, M, S);
     if (!sys) return 1;
-    if (Fn->mv != FGC_MV || Fn->precondR != NO_precond ||
-        (Fn->precond != FGC_BD_APPLY && Fn->precond != Diag_precond && Fn->precond != NO_precond)) {
-        fprintf(stderr, "femgpu: pgmres supports this shim's EBE matvec and preconditioners on the GPU\n");
+    const int ebe_ok = Fn->mv == FGC_MV &&
+                       (Fn->precond == FGC_BD_APPLY || Fn->precond == Diag_precond || Fn->precond == NO_precond);
+    const int csr_ok = Fn->mv == csrmv && (Fn->precond == ILUp_precond || Fn->precond == SPIKE_precond ||
+                                           Fn->precond == NO_precond);
+    if ((Fn->precondR && Fn->precondR != NO_precond) || !(ebe_ok || csr_ok)) {
+        fprintf(stderr, "femgpu: pgmres supports this shim's EBE or CSR matvec and preconditioners on the GPU\n");
         if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
         return 1;
     }

@@ -257,7 +257,7 @@ int pgmres(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctions
     const int ebe_ok = Fn->mv == ebemv && (Fn->precond == Diag_precond || Fn->precond == NO_precond);
     const int csr_ok = Fn->mv == csrmv && (Fn->precond == ILUp_precond || Fn->precond == SPIKE_precond ||
                                            Fn->precond == NO_precond);
-    if (Fn->precondR != NO_precond || !(ebe_ok || csr_ok)) {
+    if ((Fn->precondR && Fn->precondR != NO_precond) || !(ebe_ok || csr_ok)) {
         fprintf(stderr, "femgpu: pgmres supports mv = ebemv with Diag or no preconditioning, or mv = csrmv with "
                         "ILU(p), SPIKE or no preconditioning, on the GPU\n");
         if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
