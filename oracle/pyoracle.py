@@ -47,6 +47,8 @@ def build(ref: bool | None = None, fast: bool = False) -> None:
         ref = os.path.isdir(REF_SRC)
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+        if os.path.isdir(os.path.join(REF_SRC, "02_Transport_Equation")):
+            subprocess.run(["make", "-s", "-C", HERE, "ref_tt", f"REF={REF_SRC}"], check=True)
         lib_dir = os.path.join(os.path.dirname(HERE), "parallel_fem_codes_gb300", "_lib")
         if all(os.path.exists(os.path.join(lib_dir, f"libfemgpu_{k}.so")) for k in ("sst", "ns", "euler")):
             subprocess.run(["make", "-s", "-C", HERE, "dropin", f"REF={REF_SRC}"], check=True)
@@ -484,6 +486,41 @@ def build_k_f_supg(prob, u=None):
     s, keep = _problem_struct(prob)
     lib().or_build_k_f_supg(*_mesh_args(m), ctypes.byref(s), np.ascontiguousarray(u, dtype=np.float64), A, F)
     F[m.neq] = 0.0
+    return A.reshape(m.nel, 9), F
+
+
+REF_TT_SO = os.path.join(HERE, "_ref", "libref_tt.so")
+_ref_tt = None
+
+
+def ref_tt():
+    """The reference's own transient-transport build (oracle/_ref, compiled
+    from a private copy of its sources by `make -C oracle ref_tt`), or None."""
+    global _ref_tt
+    if _ref_tt is None and os.path.exists(REF_TT_SO):
+        R = ctypes.CDLL(REF_TT_SO)
+        R.fr_tt_set_form.argtypes = [_c_int, _c_int, _c_int]
+        R.fr_tt_set_form.restype = None
+        R.fr_tt_build.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _c_dbl, _c_dbl,
+                                  _c_dbl, _c_dbl, _c_dbl, _c_int, _c_dbl, _c_dbl, _c_dbl, _f64p, _f64p, _c_int,
+                                  _f64p, _f64p]
+        _ref_tt = R
+    return _ref_tt
+
+
+def ref_tt_build(prob, alpha, dt, u=None, du=None, builds=1):
+    """Build_M_K_R_SUPG / Build_M_K_R_DD of the reference (by prob.form, with
+    prob.cau and prob.h_shock) at (u, du); returns (A[nel, 9], R[neq+1])."""
+    m = prob.mesh
+    R = ref_tt()
+    u = np.zeros(m.neq) if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    du = np.zeros(m.neq) if du is None else np.ascontiguousarray(du, dtype=np.float64)
+    cau = int(prob.cau)
+    R.fr_tt_set_form(int(getattr(prob, "form", 0)), cau if cau in (2, 3) else 1, int(getattr(prob, "h_shock", 0)))
+    A = np.empty(m.nel * 9)
+    F = np.zeros(m.neq + 1)
+    R.fr_tt_build(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f, prob.upmode, prob.upval,
+                  float(alpha), float(dt), u, du, int(builds), A, F)
     return A.reshape(m.nel, 9), F
 
 

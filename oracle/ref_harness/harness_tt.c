@@ -1,0 +1,145 @@
+/*
+ * Checker harness around the reference's own transient-transport build
+ * (02_Transport_Equation/2D/01_CommonFiles: Build_M_K_R_SUPG.c,
+ * Build_M_K_R_DD.c with their shock-capture and h_shock functions and
+ * eval_U_dU.c), compiled by oracle/Makefile (target "ref_tt") from a
+ * private copy of those sources whose TranspEquation.h includes the MPI
+ * stand-in instead of </usr/include/mpi/mpi.h> (its line 8; nothing else
+ * is changed).
+ *
+ * The structs are filled for one rank (neq_bef = 0, NEQ = neq, EBE
+ * storage) and the reference's own Fill_LM and Build function are called
+ * at the given state (u, du) with Alpha_Build and DeltaT_Build.  The
+ * function pointers are installed as setStabilizationForm.c installs them
+ * (the file is not linked: it pulls in the time-integration loops);
+ * setProblem is supplied here, the same synthetic problem as the steady
+ * harness.  Used only by tests.
+ */
+#include "TranspEquation.h"
+
+int Build_M_K_R_SUPG(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *);
+int Build_M_K_R_DD(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *);
+double CAU_ShockCapture(double, double, double, double, double, double, double, double, double, double, double,
+                        double, double, double, double, double, double, double, double);
+double CAU_DD_ShockCapture(double, double, double, double, double, double, double, double, double, double, double,
+                           double, double, double, double, double, double, double, double);
+double YZBeta_ShockCapture(double, double, double, double, double, double, double, double, double, double, double,
+                           double, double, double, double, double, double, double, double);
+double h_shock_2sqrtArea(double, double, double, double, double, double, double, double, double, double, double,
+                         double);
+double h_shock_Option1(double, double, double, double, double, double, double, double, double, double, double,
+                       double);
+double h_shock_Option2(double, double, double, double, double, double, double, double, double, double, double,
+                       double);
+void ebe_assembly(ParametersType *, MatrixDataType *, FemStructsType *, int, double (*)[3]);
+
+/* ---- synthetic problem (constant data, the steady harness's rule for the Dirichlet values) ---- */
+static double g_k, g_gamma, g_bx, g_by, g_f, g_upval, g_xmin, g_ymin;
+static int g_upmode;
+
+static double syn_k(void) { return g_k; }
+static double syn_gamma(void) { return g_gamma; }
+static double syn_font(double X, double Y, double k, double gm, double bx, double by)
+{ (void)X; (void)Y; (void)k; (void)gm; (void)bx; (void)by; return g_f; }
+static void syn_vel(double X, double Y, double B[2]) { (void)X; (void)Y; B[0] = g_bx; B[1] = g_by; }
+static double syn_upresc(double X, double Y)
+{
+    if (g_upmode == 1) return g_upval;
+    return (X <= g_xmin + 1e-12 || Y <= g_ymin + 1e-12) ? 1.0 : 0.0;
+}
+
+/* form 0 "SUPG" / 1 "DD"; shock 1 "CAU" / 2 "CAUDD" / 3 "YZBeta";
+ * h_shock 0 "2sqrtArea" / 1 "Option1" / 2 "Option2" */
+static int g_form, g_shock = 1, g_hshock;
+void fr_tt_set_form(int form, int shock, int hshock)
+{
+    g_form = form;
+    g_shock = shock;
+    g_hshock = hshock;
+}
+
+/* One build of the transient transport driver at (u, du): A (9 per
+ * element, row-major, Ae = me + alpha dt ke as ebe_assembly stores it) and
+ * R (neq).  delta_old (DD's relaxed CAUDD coefficient per element) starts
+ * at 0, as the time loop allocates it; `builds` builds run in a row at the
+ * same state (the DD state advances), the last one is returned. */
+int fr_tt_build(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                const int *ien, int neq, double k, double gamma, double bx, double by, double f, int upmode,
+                double upval, double alpha, double dt, const double *u, const double *du, int builds,
+                double *A_out, double *R_out)
+{
+    ParametersType P;
+    MatrixDataType M;
+    FemStructsType S;
+    FemFunctionsType F;
+    int I;
+    memset(&P, 0, sizeof P);
+    memset(&M, 0, sizeof M);
+    memset(&S, 0, sizeof S);
+    memset(&F, 0, sizeof F);
+    g_k = k; g_gamma = gamma; g_bx = bx; g_by = by; g_f = f; g_upmode = upmode; g_upval = upval;
+    g_xmin = x[0]; g_ymin = y[0];
+    for (I = 1; I < nnodes; I++) {
+        if (x[I] < g_xmin) g_xmin = x[I];
+        if (y[I] < g_ymin) g_ymin = y[I];
+    }
+    strcpy(P.MatrixVectorProductScheme, "EBE");
+    P.nnodes = P.nNodes = nnodes;
+    P.nel = P.nEl = nel;
+    P.neq = neq;
+    P.NEQ = neq;
+    P.NPROC = 1;
+    P.Alpha = P.Alpha_Build = alpha;
+    P.DeltaT = P.DeltaT_Build = dt;
+    F.Condutivity = syn_k;
+    F.Reaction = syn_gamma;
+    F.Font = syn_font;
+    F.Velocity = syn_vel;
+    F.upresc = syn_upresc;
+    F.assembly = ebe_assembly;
+    F.ShockCapture = g_shock == 3 ? YZBeta_ShockCapture : g_shock == 2 ? CAU_DD_ShockCapture : CAU_ShockCapture;
+    F.h_shock = g_hshock == 2 ? h_shock_Option2 : g_hshock == 1 ? h_shock_Option1 : h_shock_2sqrtArea;
+
+    NodeType *Node = calloc((size_t)nnodes, sizeof(NodeType));
+    ElementType *El = calloc((size_t)nel, sizeof(ElementType));
+    for (I = 0; I < nnodes; I++) {
+        Node[I].x = x[I];
+        Node[I].y = y[I];
+        Node[I].Type = type[I];
+        Node[I].Send = 1;
+        Node[I].invP_id = type[I] == 0 ? -1 : invp[I];
+    }
+    for (I = 0; I < nel; I++) {
+        El[I].Vertex[0] = ien[3 * I];
+        El[I].Vertex[1] = ien[3 * I + 1];
+        El[I].Vertex[2] = ien[3 * I + 2];
+    }
+    int **lm = calloc((size_t)nel, sizeof(int *));
+    int *lmaux = calloc((size_t)nel * 3, sizeof(int));
+    for (I = 0; I < nel; I++) lm[I] = &lmaux[3 * I];
+    double **A = calloc((size_t)nel, sizeof(double *));
+    double *Aaux = calloc((size_t)nel * 9, sizeof(double));
+    for (I = 0; I < nel; I++) A[I] = &Aaux[9 * I];
+    S.Node = Node;
+    S.Element = El;
+    S.lm = lm;
+    S.lmaux = lmaux;
+    S.F = calloc((size_t)neq + 1, sizeof(double));
+    S.u = calloc((size_t)neq + 1, sizeof(double));
+    S.du = calloc((size_t)neq + 1, sizeof(double));
+    S.delta_old = calloc((size_t)nel + 1, sizeof(double));
+    memcpy(S.u, u, sizeof(double) * (size_t)neq);
+    memcpy(S.du, du, sizeof(double) * (size_t)neq);
+    M.A = A;
+    M.Aaux = Aaux;
+    Fill_LM(&P, lm, Node, El);
+    for (I = 0; I < builds; I++) {
+        if (g_form == 1) Build_M_K_R_DD(&P, &M, &S, &F);
+        else Build_M_K_R_SUPG(&P, &M, &S, &F);
+    }
+    memcpy(A_out, Aaux, sizeof(double) * 9 * (size_t)nel);
+    memcpy(R_out, S.F, sizeof(double) * (size_t)neq);
+    free(Node); free(El); free(lm); free(lmaux); free(A); free(Aaux);
+    free(S.F); free(S.u); free(S.du); free(S.delta_old);
+    return 0;
+}

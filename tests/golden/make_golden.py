@@ -224,6 +224,26 @@ def write_euler_dd():
     np.savez_compressed(os.path.join(HERE, "dd_euler.npz"), **out)
 
 
+TT_CASES = [(0, 1, 0), (0, 3, 1), (0, 1, 2), (1, 2, 0), (1, 3, 2)]   # (form, shock, h_shock)
+
+
+def write_tt():
+    """The transient transport driver's own builds (Build_M_K_R_SUPG /
+    Build_M_K_R_DD, oracle/_ref/libref_tt.so) at random states (u, du)."""
+    out = {}
+    for form, cau, hs in TT_CASES:
+        p = G.transport_problem(17, angle_deg=35.0, k=1e-3, gamma=0.2, f=0.5, cau=cau)
+        p.form, p.h_shock = form, hs
+        rng = np.random.default_rng(100 + 10 * form + cau + 3 * hs)
+        u = rng.random(p.mesh.neq)
+        du = rng.standard_normal(p.mesh.neq)
+        A, R = O.ref_tt_build(p, 0.5, 0.01, u, du)
+        key = f"tt_{form}_{cau}_{hs}"
+        out[key + "_u"], out[key + "_du"], out[key + "_A"], out[key + "_R"] = u, du, A, R
+        print(key)
+    np.savez_compressed(os.path.join(HERE, "tt_ref.npz"), **out)
+
+
 if __name__ == "__main__":
     main()
     write_euler()
@@ -233,3 +253,4 @@ if __name__ == "__main__":
     write_sst_shock()
     write_ilup()
     write_euler_dd()
+    write_tt()

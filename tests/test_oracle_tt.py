@@ -1,12 +1,14 @@
-"""The transient transport restatement (oracle/tt.c: Build_M_K_R_SUPG.c and
-the Predictor_Old loop with Diag).  The reference's transient driver does
-not compile here (TranspEquation.h:8 includes an MPI header by absolute
-path), so the restatement is pinned through the steady build, which is
-pinned bit-exactly against the reference (tests/test_oracle_golden.py and
-the reference build): the stiffness part of the transient block equals the
-steady block, the load part of the transient residual equals the steady
-right-hand side, and the time loop keeps exact constant solutions and
-reaches the steady solution."""
+"""The transient transport restatement (oracle/tt.c: Build_M_K_R_SUPG.c,
+Build_M_K_R_DD.c and the Predictor_Old loop with Diag).
+
+Pinned to the reference itself: the transient driver's TranspEquation.h
+includes an MPI header by absolute path (line 8), so oracle/Makefile
+(`ref_tt`) compiles its build functions from a private copy with that line
+pointed at the MPI stand-in; tests/golden/tt_ref.npz holds that build's
+blocks and residuals (SUPG with CAU / YZBeta and each h_shock option, DD
+with CAUDD / YZBeta) at random states, and the restatement matches them
+bit for bit.  The checks through the steady build (pinned against the
+reference's steady driver) and the time-loop properties below stay."""
 import numpy as np
 import pytest
 
@@ -126,3 +128,35 @@ def test_tt_yzbeta_pinned_through_steady_yzbeta(oracle_lib, hs):
     shock_tt, shock_ss = ke3 - ke0, ks3 - ks0
     assert np.abs(shock_ss).max() > 0
     assert np.allclose(shock_tt, 2 * shock_ss, rtol=1e-7, atol=1e-9 * np.abs(ke0).max())
+
+
+TT_CASES = [(0, 1, 0), (0, 3, 1), (0, 1, 2), (1, 2, 0), (1, 3, 2)]   # (form, shock, h_shock)
+
+
+def _tt_problem(form, cau, hs):
+    p = G.transport_problem(17, angle_deg=35.0, k=1e-3, gamma=0.2, f=0.5, cau=cau)
+    p.form, p.h_shock = form, hs
+    return p
+
+
+@pytest.mark.parametrize("form,cau,hs", TT_CASES)
+def test_transient_build_matches_reference_golden(form, cau, hs):
+    """Blocks and residual bit-identical with the reference's own transient
+    build (tests/golden/tt_ref.npz, written by tests/golden/make_golden.py)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "tt_ref.npz"))
+    key = f"tt_{form}_{cau}_{hs}"
+    A, R = O.build_tt(_tt_problem(form, cau, hs), 0.5, 0.01, g[key + "_u"], g[key + "_du"])
+    assert np.array_equal(A, g[key + "_A"])
+    assert np.array_equal(R[:-1], g[key + "_R"][:-1])
+
+
+@pytest.mark.skipif(O.ref_tt() is None, reason="reference transient build absent")
+@pytest.mark.parametrize("form,cau,hs", TT_CASES)
+def test_transient_build_matches_reference(form, cau, hs):
+    p = _tt_problem(form, cau, hs)
+    rng = np.random.default_rng(7)
+    u, du = rng.random(p.mesh.neq), rng.standard_normal(p.mesh.neq)
+    A0, R0 = O.build_tt(p, 0.3, 0.05, u, du)
+    A1, R1 = O.ref_tt_build(p, 0.3, 0.05, u, du)
+    assert np.array_equal(A0, A1) and np.array_equal(R0[:-1], R1[:-1])
