@@ -667,6 +667,12 @@ def main():
         sv.close()
         return e0.elapsed_time(e1) / 1e3, res
 
+    # autotuner (set-up, untimed): launch shapes of the full batch, mixed and FP64
+    for s, p in zip(systems, probs):
+        s.transport_prepare(p)
+    tuned = {"mixed": fg.autotune(systems, kmax=KMAX, lmax=10000, tol=TOL, precision=served_precision(fg)),
+             "fp64": fg.autotune(systems, kmax=KMAX, lmax=100000, tol=TOL, precision=fg.FG_PREC_FP64)}
+
     for _ in range(args.warmup):
         served_pass()
     barrier(dist)
@@ -818,7 +824,7 @@ def main():
                                            "(bench.py --matvec-only --count 32), scaled by algorithmic bytes",
                          "ms_per_matvec": ms_mv,
                          "bytes_per_matvec": bytes_mv},
-            "cpu_baseline": cpu, "setup_s": setup_s, "legs": legs,
+            "cpu_baseline": cpu, "setup_s": setup_s, "legs": legs, "autotune": tuned,
         }
         print(json.dumps(line), flush=True)
     return 0

@@ -133,8 +133,11 @@ int fg_matvec(fg_system *s, const double *P, double *Q, int precision);
  * belongs to another allocator, or their loop must not pay cudaMalloc's
  * implicit synchronisation).  The scratch it needs comes from one fixed
  * array of about 33 MiB compiled into the library and held on every GPU
- * that loads it; systems with more than 2,097,151 equations or more than
- * 65,536 element patches of 1024 elements are rejected with FG_ERR_ARG.
+ * that loads it; systems with more than 2,097,151 equations, more than
+ * 65,536 element patches (a patch holds up to 1024 elements for 3x3
+ * blocks, 256 for larger blocks) or more than 64 patch colours are
+ * rejected with FG_ERR_ARG.  It always multiplies by the element blocks,
+ * also for a system switched to the CSR operator.
  * The first call on a device looks up the array's device address, so make
  * that first call before starting any stream capture.  The work is queued
  * on the system's stream (fg_system_stream) and the call returns without
@@ -291,6 +294,33 @@ void *fg_system_stream(const fg_system *s);
  * the systems.  Requires a previous solve (workspace) on every system. */
 int fg_bench_matvec(fg_system *const *systems, int count, int precision, int reps,
                     double *ms_per_matvec, double *bytes);
+
+/* Autotuner: times candidate launch shapes of a batch on the batch itself
+ * (one restart cycle each, CUDA events on the first system's stream) --
+ * the dof-part size of the Krylov kernels (2048 ... 16384 dofs) and, for
+ * 3x3 blocks in FP32, the matvec kernel (bulk-copy pipeline or register
+ * kernel) -- and keeps the fastest for the process, keyed by (block size,
+ * precision, batch-size class floor(log2(batch dofs))).  Every later batch
+ * of that key (fg_solve_batch, fg_solve_resident, the request server) uses
+ * it.  The systems need resident right-hand sides (fg_transport_prepare or
+ * a time-loop set-up).  remeasure 0 returns a cached choice when there is
+ * one (from_cache = 1).  The cycles run on the systems' workspaces, which
+ * the next solve reinitialises.  No counterpart in the reference (its
+ * launch shapes are fixed). */
+typedef struct {
+    int part_dofs;        /* dofs per part of the Krylov kernels            */
+    int mv3_pipeline;     /* 3x3 FP32 matvec: 1 bulk-copy pipeline, 0 the
+                             register kernel (other blocks: 1)              */
+    double ms_per_cycle;  /* one restart cycle of the batch with it         */
+    int from_cache;       /* taken from the cache, not measured now         */
+    int candidates;       /* launch shapes timed                            */
+} fg_tune_choice;
+int fg_autotune(fg_system *const *systems, int count, const fg_solver_opts *o, int remeasure,
+                fg_tune_choice *out);
+/* The cached choice for this batch's key; FG_ERR_STATE when none. */
+int fg_tune_lookup(fg_system *const *systems, int count, const fg_solver_opts *o, fg_tune_choice *out);
+/* Forget every cached choice (batches use the built-in rule again). */
+void fg_tune_clear(void);
 
 /* ---- steady SUPG/CAU transport assembly on the device ---- */
 typedef struct {

@@ -26,7 +26,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 
 #include "system.h"
 
@@ -969,11 +971,59 @@ int parts_for(int n, int part_dofs = kPartMax)
     return std::max(1, std::min(kMaxParts, p));
 }
 
-// part size of a batch (multiple of 8 dofs): its dofs over 8 CTAs per SM
-int part_dofs_for(const std::vector<BatchMember> &mem)
+}  // namespace
+
+// ---------------------------------------------------------------- autotuner
+// Measured launch shapes of a batch, chosen by fg_autotune and cached per
+// (block size, precision, batch-size class = floor(log2(batch dofs))) for
+// the process: the dof-part size of the Krylov kernels and, for 3x3
+// blocks in FP32, the matvec kernel (bulk-copy pipeline or the register
+// kernel).  A batch with no cached choice uses the built-in rule.
+struct TuneKey {
+    int S, mixed, vhalf, cls;
+    bool operator<(const TuneKey &o) const
+    {
+        return std::tie(S, mixed, vhalf, cls) < std::tie(o.S, o.mixed, o.vhalf, o.cls);
+    }
+};
+static std::mutex g_tune_mu;
+static std::map<TuneKey, fg_tune_choice> g_tune;
+// set by the autotuner while it times a candidate (this thread only)
+static thread_local const fg_tune_choice *t_tune_force = nullptr;
+
+static long long batch_dofs(const std::vector<BatchMember> &mem)
 {
     long long tot = 0;
     for (auto &m : mem) tot += m.s->topo.n;
+    return tot;
+}
+static TuneKey tune_key(int S, const SolveConfig &cfg, long long dofs)
+{
+    int cls = 0;
+    while ((2LL << cls) <= std::max(1LL, dofs)) ++cls;
+    return {S, cfg.mixed, cfg.vhalf, cls};
+}
+// the tuned choice of a batch, or nullptr
+static bool tuned_choice(const std::vector<BatchMember> &mem, const SolveConfig &cfg, fg_tune_choice &out)
+{
+    if (t_tune_force) { out = *t_tune_force; return true; }
+    if (mem.empty()) return false;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(mem[0].s->topo.S, cfg, batch_dofs(mem)));
+    if (it == g_tune.end()) return false;
+    out = it->second;
+    return true;
+}
+
+namespace {
+
+// part size of a batch (multiple of 8 dofs): the tuned one, else its dofs
+// over 8 CTAs per SM within [kPartMin, kPartMax]
+int part_dofs_for(const std::vector<BatchMember> &mem, const SolveConfig &cfg)
+{
+    fg_tune_choice tc;
+    if (tuned_choice(mem, cfg, tc) && tc.part_dofs > 0) return tc.part_dofs & ~7;
+    const long long tot = batch_dofs(mem);
     const long long target = 8LL * sm_count();
     const long long pd = std::max<long long>(kPartMin, std::min<long long>(kPartMax, tot / std::max(1LL, target)));
     return (int)(pd & ~7LL);
@@ -989,6 +1039,7 @@ struct Plan {
     int n_dch = 0, n_nch = 0, n_ilu = 0, n_ilub = 0, n_spb = 0, n_spi = 0;
     DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
     DevMem mvrec;                                  // 3x3: per matvec work item, for the bulk-copy pipeline
+    bool mv3p = true;                              // 3x3 FP32: the bulk-copy pipeline (else the register kernel)
     DevMem ilu_fwd, ilu_bwd, ilu_ctr;              // sync-free ILU(0) substitutions
     DevMem sp_blocks, sp_ifaces;                   // SPIKE (system, block) and (system, interface) items
 };
@@ -1019,7 +1070,11 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     }
     std::vector<DChunk> dch;
     std::vector<NChunk> nch;
-    const int pdofs = part_dofs_for(mem);
+    const int pdofs = part_dofs_for(mem, cfg);
+    {
+        fg_tune_choice tc;
+        P.mv3p = !(tuned_choice(mem, cfg, tc) && tc.mv3_pipeline == 0);
+    }
     for (int s = 0; s < P.nsys; ++s) {
         int n = mem[s].s->topo.n;
         hs[s].nparts = parts_for(n, pdofs);
@@ -1169,7 +1224,7 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
             done = true;
         }
         if constexpr (sizeof(T) == 4) {
-            if (!done && P.S == 3 && kMv3Pipeline && P.mvrec.p) {
+            if (!done && P.S == 3 && kMv3Pipeline && P.mv3p && P.mvrec.p) {
                 MvLaunch::pipeline<TV, T>(cnt, st, sys, P.mvrec.as<MvRec>() + P.ech_off[c], nc, gate, 1, 1, step,
                                           nullptr, nullptr);
                 done = true;
@@ -1338,6 +1393,91 @@ size_t workspace_bytes(const fg_system *s, int kmax, int mixed)
     return ts * np * (kmax + 2) + 8 * np * 6 +
            8 * ((size_t)(kmax + 1) * kmax + 5 * (kmax + 1) + (size_t)kmax * kmax) +
            8 * (size_t)kMaxParts * kPartStride + 256;
+}
+
+int autotune(std::vector<fg_system *> &sys, const SolveConfig &cfg0, bool remeasure, bool lookup_only,
+             fg_tune_choice *out)
+{
+    if (sys.empty()) { set_error("fg_autotune: empty batch"); return FG_ERR_ARG; }
+    std::vector<BatchMember> mem;
+    for (fg_system *s : sys) {
+        if (!s) { set_error("fg_autotune: NULL system"); return FG_ERR_ARG; }
+        if (s->topo.S != sys[0]->topo.S) { set_error("fg_autotune: a batch must hold one block size"); return FG_ERR_ARG; }
+        if (!s->rhs_ok) { set_error("fg_autotune: system without a resident right-hand side"); return FG_ERR_STATE; }
+        mem.push_back({s, s->rhs_b.as<double>(), s->rhs_f.as<double>(), nullptr});
+    }
+    SolveConfig cfg = cfg0;
+    cfg.device_io = 1;
+    cfg.use_graph = 0;
+    cfg.precond = sys[0]->precond;
+    const TuneKey key = tune_key(sys[0]->topo.S, cfg, batch_dofs(mem));
+    if (!remeasure || lookup_only) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            *out = it->second;
+            out->from_cache = 1;
+            return FG_OK;
+        }
+        if (lookup_only) { set_error("fg_tune_lookup: no cached choice for this batch"); return FG_ERR_STATE; }
+    }
+    cudaStream_t st = sys[0]->stream;
+    for (fg_system *s : sys) FG_CUDA(cudaStreamSynchronize(s->stream));
+    std::vector<fg_tune_choice> cand;
+    const int pds[] = {2048, 4096, 8192, 12288, 16384};
+    for (int pd : pds) {
+        cand.push_back({pd, 1, 0.0, 0, 0});
+        if (sys[0]->topo.S == 3 && cfg.mixed && !cfg.vhalf) cand.push_back({pd, 0, 0.0, 0, 0});
+    }
+    cudaEvent_t e0, e1;
+    FG_CUDA(cudaEventCreate(&e0));
+    FG_CUDA(cudaEventCreate(&e1));
+    fg_tune_choice best{};
+    best.ms_per_cycle = 1e300;
+    int r = FG_OK;
+    std::vector<int> live;
+    for (auto &c : cand) {
+        t_tune_force = &c;
+        {
+            BatchRun run(cfg, st);
+            for (auto &m : mem)
+                if ((r = run.stage(m))) break;
+            if (!r) r = run.commit();
+            if (!r) r = run.cycle(false, live);                     // warm-up (first launches)
+            if (!r) {
+                cudaEventRecord(e0, st);
+                r = run.cycle(false, live);
+                cudaEventRecord(e1, st);
+            }
+            if (!r) {
+                float ms = 0.f;
+                cudaError_t ce = cudaEventSynchronize(e1);
+                if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+                if (ce != cudaSuccess) r = cuda_fail(ce, "fg_autotune timing");
+                c.ms_per_cycle = ms;
+            }
+        }
+        t_tune_force = nullptr;
+        if (r) break;
+        if (c.ms_per_cycle < best.ms_per_cycle) best = c;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (r) return r;
+    best.candidates = (int)cand.size();
+    best.from_cache = 0;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[key] = best;
+    }
+    *out = best;
+    return FG_OK;
+}
+
+void tune_clear()
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
 }
 
 size_t request_bytes(const fg_system *s, int kmax, int mixed, bool time_loop)

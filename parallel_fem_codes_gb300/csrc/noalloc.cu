@@ -14,8 +14,15 @@
 // until the process exits.  It stores the system descriptor, the matvec
 // work-item table and two renumbering vectors of at most kNoAllocMaxEq entries,
 // so the entry point accepts systems with n + 1 <= kNoAllocMaxEq equations
-// (including the Dirichlet sink) and at most kNoAllocMaxChunks element
-// patches of kPatchElems elements, and rejects larger ones with FG_ERR_ARG.
+// (including the Dirichlet sink), at most kNoAllocMaxChunks element patches
+// (a patch holds up to 1024 elements for 3x3 blocks, 256 for larger blocks)
+// and at most kMaxColours patch colours, and rejects larger ones with
+// FG_ERR_ARG.  It always multiplies by the element blocks (the EBE
+// operator), also for a system switched to the assembled CSR operator
+// (fg_set_operator), whose fg_matvec sums the same products in another
+// order.  The host-side work-item table is one static array guarded by the
+// same lock as the address table (the library allocates no host memory in
+// this call either).
 //
 // Host code cannot use the array's name as a device address (in host code
 // it names a host-side stand-in): the device address is looked up once per
@@ -53,10 +60,10 @@ std::mutex g_scratch_mu;
 unsigned char *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of the scratch array on `dev` (which must be current).
+// (the caller holds g_scratch_mu)
 int scratch_on(int dev, unsigned char **out)
 {
     if (dev < 0 || dev >= kMaxDevices) { set_error("fg_matvec_noalloc: device index out of range"); return FG_ERR_ARG; }
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (!g_scratch_addr[dev]) {
         void *p = nullptr;
         cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -81,8 +88,9 @@ __global__ void k_na_scatter(const int *__restrict__ perm, const double *__restr
     if (i == n) dst[n] = 0.0;
 }
 
-// host-side chunk table of the call (per host thread, no heap)
-thread_local EChunk t_chunks[kNoAllocMaxChunks];
+// host-side work-item table of a call (guarded by g_scratch_mu, held until
+// its copy to the device has been staged)
+EChunk g_chunks[kNoAllocMaxChunks];
 
 }  // namespace
 }  // namespace fg
@@ -108,13 +116,19 @@ extern "C" int fg_matvec_noalloc(fg_system *s, const double *P_dev, double *Q_de
     int off[kMaxColours + 1] = {0};
     int counts[kMaxColours] = {0};
     int nch = 0;
-    if (t.npatch > kNoAllocMaxChunks || t.npcol > kMaxColours) {
-        set_error("fg_matvec_noalloc: system has more than " + std::to_string(kNoAllocMaxChunks) +
-                  " element patches, the fixed scratch holds no more");
+    if (t.npatch > kNoAllocMaxChunks) {
+        set_error("fg_matvec_noalloc: system has " + std::to_string(t.npatch) + " element patches, the fixed "
+                  "scratch holds at most " + std::to_string(kNoAllocMaxChunks));
         return FG_ERR_ARG;
     }
+    if (t.npcol > kMaxColours) {
+        set_error("fg_matvec_noalloc: system has " + std::to_string(t.npcol) + " patch colours, at most " +
+                  std::to_string(kMaxColours) + " are supported");
+        return FG_ERR_ARG;
+    }
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
     for (int c = 0; c < t.npcol; ++c) {
-        for (int q = t.pc_ptr[c]; q < t.pc_ptr[c + 1]; ++q) t_chunks[nch++] = {0, t.pc_list[q], 0};
+        for (int q = t.pc_ptr[c]; q < t.pc_ptr[c + 1]; ++q) g_chunks[nch++] = {0, t.pc_list[q], 0};
         off[c + 1] = nch;
         counts[c] = off[c + 1] - off[c];
     }
@@ -134,7 +148,8 @@ extern "C" int fg_matvec_noalloc(fg_system *s, const double *P_dev, double *Q_de
     cudaStream_t st = s->stream;
     FG_CUDA(cudaMemcpyAsync(d_desc, &D, sizeof(SysDev), cudaMemcpyHostToDevice, st));
     if (t.npcol) FG_CUDA(cudaMemcpyAsync(d_counts, counts, sizeof(int) * t.npcol, cudaMemcpyHostToDevice, st));
-    if (nch) FG_CUDA(cudaMemcpyAsync(d_chunks, t_chunks, sizeof(EChunk) * nch, cudaMemcpyHostToDevice, st));
+    // pageable source: staged before the call returns, while the lock is held
+    if (nch) FG_CUDA(cudaMemcpyAsync(d_chunks, g_chunks, sizeof(EChunk) * nch, cudaMemcpyHostToDevice, st));
     // x (reference numbering) -> internal numbering; y starts at zero
     k_na_gather<<<(t.n + 256) / 256, 256, 0, st>>>(s->perm.as<int>(), P_dev, d_x, t.n);
     FG_CUDA(cudaGetLastError());

@@ -606,6 +606,28 @@ int fg_bench_matvec(fg_system *const *systems, int count, int precision, int rep
     return bench_matvec(v, precision, reps, ms, bytes);
 }
 
+int fg_autotune(fg_system *const *systems, int count, const fg_solver_opts *o, int remeasure, fg_tune_choice *out)
+{
+    if (!systems || count < 1 || !o || !out) { set_error("NULL argument"); return FG_ERR_ARG; }
+    SolveConfig cfg;
+    int r = batch_config(systems, count, o, cfg);
+    if (r) return r;
+    std::vector<fg_system *> v(systems, systems + count);
+    return autotune(v, cfg, remeasure != 0, false, out);
+}
+
+int fg_tune_lookup(fg_system *const *systems, int count, const fg_solver_opts *o, fg_tune_choice *out)
+{
+    if (!systems || count < 1 || !o || !out) { set_error("NULL argument"); return FG_ERR_ARG; }
+    SolveConfig cfg;
+    int r = batch_config(systems, count, o, cfg);
+    if (r) return r;
+    std::vector<fg_system *> v(systems, systems + count);
+    return autotune(v, cfg, false, true, out);
+}
+
+void fg_tune_clear(void) { tune_clear(); }
+
 int fg_transport_prepare(fg_system *s, const fg_transport_coeffs *c, const double *u)
 {
     if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }

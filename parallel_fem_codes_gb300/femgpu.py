@@ -102,6 +102,14 @@ class TimeStats(ctypes.Structure):
                 ("seconds", _c_dbl), ("true_rel_residual", _c_dbl)]
 
 
+class TuneChoice(ctypes.Structure):
+    _fields_ = [("part_dofs", _c_int), ("mv3_pipeline", _c_int), ("ms_per_cycle", _c_dbl), ("from_cache", _c_int),
+                ("candidates", _c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class ServerOpts(ctypes.Structure):
     _fields_ = [("kmax", _c_int), ("lmax", _c_int), ("tol", _c_dbl), ("precision", _c_int),
                 ("inner_tol", _c_dbl), ("hbm_budget_bytes", ctypes.c_size_t), ("max_active", _c_int)]
@@ -163,6 +171,9 @@ def lib(build_if_missing: bool = True):
     L.fg_set_ilu_blocks.argtypes = [_vp, _c_int]
     L.fg_set_wait_limit.argtypes = [ctypes.c_longlong]
     L.fg_set_memory_limit.argtypes = [ctypes.c_size_t]
+    L.fg_autotune.argtypes = [_vp, _c_int, ctypes.POINTER(SolverOpts), _c_int, ctypes.POINTER(TuneChoice)]
+    L.fg_tune_lookup.argtypes = [_vp, _c_int, ctypes.POINTER(SolverOpts), ctypes.POINTER(TuneChoice)]
+    L.fg_tune_clear.restype = None
     L.fg_memory_in_use.restype = ctypes.c_size_t
     L.fg_get_csr.argtypes = [_vp, ctypes.POINTER(_c_int), _vp, _vp, _vp]
     L.fg_system_stream.argtypes = [_vp]
@@ -630,6 +641,30 @@ def solve_batch(systems, Bs, F_trues=None, kmax=30, lmax=1000, tol=1e-10, precis
     check(lib().fg_solve_batch(ctypes.cast(H, _vp), n, ctypes.byref(o), ctypes.cast(Bp, _vp), ctypes.cast(Xp, _vp),
                                None if Fp is None else ctypes.cast(Fp, _vp), ctypes.cast(st, _vp)))
     return Xs, [s.as_dict() for s in st]
+
+
+def autotune(systems, kmax=30, lmax=1000, tol=1e-10, precision=FG_PREC_MIXED, inner_tol=0.0, remeasure=False):
+    """Time candidate launch shapes on this batch (resident right-hand sides
+    required) and keep the fastest for its key; returns the choice."""
+    n = len(systems)
+    H = (_vp * n)(*[s.handle for s in systems])
+    o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+    c = TuneChoice()
+    check(lib().fg_autotune(ctypes.cast(H, _vp), n, ctypes.byref(o), int(bool(remeasure)), ctypes.byref(c)))
+    return c.as_dict()
+
+
+def tune_lookup(systems, kmax=30, lmax=1000, tol=1e-10, precision=FG_PREC_MIXED, inner_tol=0.0):
+    n = len(systems)
+    H = (_vp * n)(*[s.handle for s in systems])
+    o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+    c = TuneChoice()
+    check(lib().fg_tune_lookup(ctypes.cast(H, _vp), n, ctypes.byref(o), ctypes.byref(c)))
+    return c.as_dict()
+
+
+def tune_clear():
+    lib().fg_tune_clear()
 
 
 def solve_resident(systems, kmax=30, lmax=1000, tol=1e-10, precision=FG_PREC_FP64, inner_tol=0.0):

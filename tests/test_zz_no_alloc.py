@@ -43,6 +43,43 @@ def _noalloc(fg, s, P, precision):
     return Qd.cpu().numpy()
 
 
+def test_matvec_noalloc_matches_oracle(fg):
+    """Against the oracle's ebemv (oracle/ebe_gmres.c, a restatement of
+    00_CommonFiles/MatrixVector_Operations/EBE/ebemv.c:4-64), independently of
+    the library's own matvec."""
+    p = G.transport_problem(65, angle_deg=20.0, k=1e-4)
+    m = p.mesh
+    A, _ = O.build_k_f_supg(p)
+    lm = O.fill_lm(m)
+    perm, inv, _ = O.permutation_of_lm(m)
+    s = fg.System(m)
+    s.set_blocks(A)
+    rng = np.random.default_rng(5)
+    for call in range(2):
+        P = rng.standard_normal(m.neq + 1)
+        P[-1] = 0.0
+        ref = O.ebemv3_perm(lm, A, perm, inv, P)
+        for precision, tol in ((64, 1e-14), (32, 1e-5)):
+            got = _noalloc(fg, s, P, precision)
+            assert rel(got[:-1], ref[:-1]) <= tol, (call, precision)
+
+
+def test_matvec_noalloc_on_a_csr_system_uses_the_blocks(fg):
+    """A system switched to the assembled CSR operator: the allocation-free
+    matvec still multiplies by the element blocks, equal to the CSR product
+    up to summation order."""
+    p = G.transport_problem(33)
+    A, _ = O.build_k_f_supg(p)
+    s = fg.System(p.mesh)
+    s.set_blocks(A)
+    s.set_operator(fg.FG_OP_CSR)
+    P = np.random.default_rng(9).standard_normal(s.n + 1)
+    P[-1] = 0.0
+    ref = s.matvec(P, 64)
+    for _ in range(2):
+        assert rel(_noalloc(fg, s, P, 64)[:-1], ref[:-1]) <= 1e-14
+
+
 @pytest.mark.parametrize("kind", ["transport", "ndof4"])
 def test_matvec_noalloc_matches_matvec(fg, kind):
     if kind == "transport":
