@@ -297,7 +297,7 @@ int fg_bench_matvec(fg_system *const *systems, int count, int precision, int rep
 
 /* Autotuner: times candidate launch shapes of a batch on the batch itself
  * (one restart cycle each, CUDA events on the first system's stream) --
- * the dof-part size of the Krylov kernels (2048 ... 16384 dofs) and, for
+ * the dof-part size of the Krylov kernels (256 ... 16384 dofs) and, for
  * 3x3 blocks in FP32, the matvec kernel (bulk-copy pipeline or register
  * kernel) -- and keeps the fastest for the process, keyed by (block size,
  * precision, batch-size class floor(log2(batch dofs))).  Every later batch

@@ -144,13 +144,13 @@ int matrix_bandwidth(int n, const int *IA, const int *JA);
 constexpr int kMaxColours = 64;
 constexpr int kElemChunk = 1024;   // elements per matvec work item
 constexpr int kMaxParts = 1024;    // dof parts (reduction partials) per system
-// Dofs per part of the Krylov dof kernels, chosen per batch: the batch's
-// dofs over kPartTarget parts, within [kPartMin, kPartMax].  A full batch
-// gets large parts (fixed per-part cost amortised; 8k-16k measured best on
-// GB300), a batch whose last few systems are still iterating gets small
-// ones so that it still spreads over the SMs.
-constexpr int kPartMin = 2048;
-constexpr int kPartMax = 12288;
+// Dofs per part of the Krylov dof kernels, chosen per batch (unless the
+// autotuner cached a choice): the batch's dofs over one part per SM, within
+// [kPartMin, kPartMax].  Measured on GB300 (one restart cycle): a single
+// 16k-dof system is fastest at 256-dof parts, 65k at 512, 147k at 1024,
+// the 24.8M-dof served batch at 16384 (12288: +1.7%, 2048: +34%).
+constexpr int kPartMin = 256;
+constexpr int kPartMax = 16384;
 constexpr int kThreads = 256;
 
 struct SysState {

@@ -1018,13 +1018,13 @@ static bool tuned_choice(const std::vector<BatchMember> &mem, const SolveConfig 
 namespace {
 
 // part size of a batch (multiple of 8 dofs): the tuned one, else its dofs
-// over 8 CTAs per SM within [kPartMin, kPartMax]
+// over one part per SM within [kPartMin, kPartMax]
 int part_dofs_for(const std::vector<BatchMember> &mem, const SolveConfig &cfg)
 {
     fg_tune_choice tc;
     if (tuned_choice(mem, cfg, tc) && tc.part_dofs > 0) return tc.part_dofs & ~7;
     const long long tot = batch_dofs(mem);
-    const long long target = 8LL * sm_count();
+    const long long target = sm_count();
     const long long pd = std::max<long long>(kPartMin, std::min<long long>(kPartMax, tot / std::max(1LL, target)));
     return (int)(pd & ~7LL);
 }
@@ -1424,7 +1424,7 @@ int autotune(std::vector<fg_system *> &sys, const SolveConfig &cfg0, bool remeas
     cudaStream_t st = sys[0]->stream;
     for (fg_system *s : sys) FG_CUDA(cudaStreamSynchronize(s->stream));
     std::vector<fg_tune_choice> cand;
-    const int pds[] = {2048, 4096, 8192, 12288, 16384};
+    const int pds[] = {256, 512, 1024, 2048, 4096, 8192, 12288, 16384};
     for (int pd : pds) {
         cand.push_back({pd, 1, 0.0, 0, 0});
         if (sys[0]->topo.S == 3 && cfg.mixed && !cfg.vhalf) cand.push_back({pd, 0, 0.0, 0, 0});
