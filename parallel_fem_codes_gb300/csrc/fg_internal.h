@@ -145,10 +145,11 @@ constexpr int kMaxColours = 64;
 constexpr int kElemChunk = 1024;   // elements per matvec work item
 constexpr int kMaxParts = 1024;    // dof parts (reduction partials) per system
 // Dofs per part of the Krylov dof kernels, chosen per batch (unless the
-// autotuner cached a choice): the batch's dofs over one part per SM, within
-// [kPartMin, kPartMax].  Measured on GB300 (one restart cycle): a single
-// 16k-dof system is fastest at 256-dof parts, 65k at 512, 147k at 1024,
-// the 24.8M-dof served batch at 16384 (12288: +1.7%, 2048: +34%).
+// autotuner cached a choice): 2 sqrt(batch dofs), rounded to the nearest
+// power of two, within [kPartMin, kPartMax], so small systems spread over
+// many SMs and large batches keep the per-part overhead low.  Fitted to measured optima on GB300 (one
+// restart cycle): 16k dofs -> 256-dof parts, 65k -> 512, 147k -> 1024,
+// 3.1M (one NS system) -> ~3k, the 24.8M-dof served batch -> 8k-16k.
 constexpr int kPartMin = 256;
 constexpr int kPartMax = 16384;
 constexpr int kThreads = 256;

