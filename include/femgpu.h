@@ -319,6 +319,11 @@ int fg_autotune(fg_system *const *systems, int count, const fg_solver_opts *o, i
                 fg_tune_choice *out);
 /* The cached choice for this batch's key; FG_ERR_STATE when none. */
 int fg_tune_lookup(fg_system *const *systems, int count, const fg_solver_opts *o, fg_tune_choice *out);
+/* Install a choice for this batch's key without timing (a choice kept
+ * from an earlier run, or a pinned configuration); later batches of the key
+ * use it.  FG_ERR_ARG unless part_dofs is a multiple of 8 in
+ * [256, 16384] and mv3_pipeline is 0 or 1. */
+int fg_tune_set(fg_system *const *systems, int count, const fg_solver_opts *o, const fg_tune_choice *choice);
 /* Forget every cached choice (batches use the built-in rule again). */
 void fg_tune_clear(void);
 

@@ -400,9 +400,47 @@ __device__ __forceinline__ void solve_y(const SysDev &D, int m)
     }
 }
 
+// The last part's step after pass 3 (pgmres.c:111-157): h(i+1,i) = ||w||
+// from the summed squares, the earlier rotations applied to column i, the
+// new rotation, the residual estimate and the cycle's stop test; at the
+// end of a cycle the solution of the triangular system.  One thread.
+__device__ __forceinline__ void givens_step(const SysDev &D, int i, double sumsq)
+{
+    SysState *st = D.st;
+    const int km = D.kmax;
+    double *H = D.H, *cs = D.cs, *sn = D.sn, *g = D.g;
+    double hn = sqrt(sumsq);
+    st->hn = hn;
+    H[(i + 1) * km + i] = hn;
+    for (int j = 0; j <= i - 1; ++j) {
+        double h1 = cs[j] * H[j * km + i] + sn[j] * H[(j + 1) * km + i];
+        double h2 = -sn[j] * H[j * km + i] + cs[j] * H[(j + 1) * km + i];
+        H[j * km + i] = h1;
+        H[(j + 1) * km + i] = h2;
+    }
+    double r = sqrt(H[i * km + i] * H[i * km + i] + H[(i + 1) * km + i] * H[(i + 1) * km + i]);
+    cs[i] = H[i * km + i] / r;
+    sn[i] = H[(i + 1) * km + i] / r;
+    H[i * km + i] = r;
+    H[(i + 1) * km + i] = 0.0;
+    g[i + 1] = -sn[i] * g[i];
+    g[i] = cs[i] * g[i];
+    st->rho = fabs(g[i + 1]);
+    st->steps = i + 1;
+    st->iterations += 1;
+    double target = D.mixed ? st->target : st->eps;
+    if (!(r > 0.0) || !isfinite(st->rho)) {
+        st->status = FG_ERR_BREAKDOWN;
+        st->in_cycle = 0;
+        if (!(r > 0.0)) st->steps = i;     // column i unusable
+    } else if (!(st->rho > target) || i + 1 >= D.kmax - 1 || !(hn > 0.0)) {
+        st->in_cycle = 0;
+    }
+    if (!st->in_cycle) solve_y(D, st->steps);
+}
+
 // pass 3: w -= sum_j h2_j v_j ; ||w||; then, in the last part, the Givens
-// rotations of column i and the residual estimate (pgmres.c:111-157), and
-// at the end of a cycle the solution of the triangular system.
+// step (givens_step).
 template <typename T, typename TV = T>
 __global__ void __launch_bounds__(kThreads)
 k_orth2(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int *__restrict__ nch, int i)
@@ -430,39 +468,7 @@ k_orth2(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const int
         }
         if (last_part(D, 3)) {
             reduce_parts(D, 1, tot);
-            if (threadIdx.x == 0) {
-                SysState *st = D.st;
-                const int km = D.kmax;
-                double *H = D.H, *cs = D.cs, *sn = D.sn, *g = D.g;
-                double hn = sqrt(tot[0]);
-                st->hn = hn;
-                H[(i + 1) * km + i] = hn;
-                for (int j = 0; j <= i - 1; ++j) {
-                    double h1 = cs[j] * H[j * km + i] + sn[j] * H[(j + 1) * km + i];
-                    double h2 = -sn[j] * H[j * km + i] + cs[j] * H[(j + 1) * km + i];
-                    H[j * km + i] = h1;
-                    H[(j + 1) * km + i] = h2;
-                }
-                double r = sqrt(H[i * km + i] * H[i * km + i] + H[(i + 1) * km + i] * H[(i + 1) * km + i]);
-                cs[i] = H[i * km + i] / r;
-                sn[i] = H[(i + 1) * km + i] / r;
-                H[i * km + i] = r;
-                H[(i + 1) * km + i] = 0.0;
-                g[i + 1] = -sn[i] * g[i];
-                g[i] = cs[i] * g[i];
-                st->rho = fabs(g[i + 1]);
-                st->steps = i + 1;
-                st->iterations += 1;
-                double target = D.mixed ? st->target : st->eps;
-                if (!(r > 0.0) || !isfinite(st->rho)) {
-                    st->status = FG_ERR_BREAKDOWN;
-                    st->in_cycle = 0;
-                    if (!(r > 0.0)) st->steps = i;     // column i unusable
-                } else if (!(st->rho > target) || i + 1 >= D.kmax - 1 || !(hn > 0.0)) {
-                    st->in_cycle = 0;
-                }
-                if (!st->in_cycle) solve_y(D, st->steps);
-            }
+            if (threadIdx.x == 0) givens_step(D, i, tot[0]);
         }
     }
 }

@@ -889,7 +889,6 @@ namespace {
 #define FG_MV3_PIPELINE 1
 #endif
 constexpr bool kMv3Pipeline = FG_MV3_PIPELINE != 0;
-
 struct MvLaunch {
     // Persistent CTAs: as many as fit on the GPU (their dynamic shared memory,
     // mv_smem_bytes, decides how many per SM), at most one per patch.
@@ -1072,10 +1071,9 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     std::vector<DChunk> dch;
     std::vector<NChunk> nch;
     const int pdofs = part_dofs_for(mem, cfg);
-    {
-        fg_tune_choice tc;
-        P.mv3p = !(tuned_choice(mem, cfg, tc) && tc.mv3_pipeline == 0);
-    }
+    fg_tune_choice tc;
+    const bool tuned = tuned_choice(mem, cfg, tc);
+    P.mv3p = !(tuned && tc.mv3_pipeline == 0);
     for (int s = 0; s < P.nsys; ++s) {
         int n = mem[s].s->topo.n;
         hs[s].nparts = parts_for(n, pdofs);
@@ -1426,10 +1424,11 @@ int autotune(std::vector<fg_system *> &sys, const SolveConfig &cfg0, bool remeas
     for (fg_system *s : sys) FG_CUDA(cudaStreamSynchronize(s->stream));
     std::vector<fg_tune_choice> cand;
     const int pds[] = {256, 512, 1024, 2048, 4096, 8192, 12288, 16384};
-    for (int pd : pds) {
-        cand.push_back({pd, 1, 0.0, 0, 0});
-        if (sys[0]->topo.S == 3 && cfg.mixed && !cfg.vhalf) cand.push_back({pd, 0, 0.0, 0, 0});
-    }
+    const bool mv3_alt = sys[0]->topo.S == 3 && cfg.mixed && !cfg.vhalf;
+    for (int pd : pds)
+        for (int mv = 1; mv >= (mv3_alt ? 0 : 1); --mv) cand.push_back({pd, mv, 0.0, 0, 0});
+    const char *tlog = getenv("FEMGPU_TUNE_LOG");
+    const bool log = tlog && *tlog && *tlog != '0';
     cudaEvent_t e0, e1;
     FG_CUDA(cudaEventCreate(&e0));
     FG_CUDA(cudaEventCreate(&e1));
@@ -1460,6 +1459,9 @@ int autotune(std::vector<fg_system *> &sys, const SolveConfig &cfg0, bool remeas
         }
         t_tune_force = nullptr;
         if (r) break;
+        if (log)
+            fprintf(stderr, "fg_autotune: S=%d mixed=%d part_dofs=%d mv3_pipeline=%d: %.3f ms/cycle\n",
+                    sys[0]->topo.S, cfg.mixed, c.part_dofs, c.mv3_pipeline, c.ms_per_cycle);
         if (c.ms_per_cycle < best.ms_per_cycle) best = c;
     }
     cudaEventDestroy(e0);
@@ -1472,6 +1474,28 @@ int autotune(std::vector<fg_system *> &sys, const SolveConfig &cfg0, bool remeas
         g_tune[key] = best;
     }
     *out = best;
+    return FG_OK;
+}
+
+int tune_set(std::vector<fg_system *> &sys, const SolveConfig &cfg0, const fg_tune_choice &c)
+{
+    if (sys.empty()) { set_error("fg_tune_set: empty batch"); return FG_ERR_ARG; }
+    std::vector<BatchMember> mem;
+    for (fg_system *s : sys) {
+        if (!s) { set_error("fg_tune_set: NULL system"); return FG_ERR_ARG; }
+        if (s->topo.S != sys[0]->topo.S) { set_error("fg_tune_set: a batch must hold one block size"); return FG_ERR_ARG; }
+        mem.push_back({s, nullptr, nullptr, nullptr});
+    }
+    if (c.part_dofs < kPartMin || c.part_dofs > kPartMax || c.part_dofs % 8 || (c.mv3_pipeline & ~1)) {
+        set_error("fg_tune_set: part_dofs must be a multiple of 8 in [256, 16384], mv3_pipeline 0 or 1");
+        return FG_ERR_ARG;
+    }
+    SolveConfig cfg = cfg0;
+    cfg.precond = sys[0]->precond;
+    fg_tune_choice k = c;
+    k.from_cache = 0;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[tune_key(sys[0]->topo.S, cfg, batch_dofs(mem))] = k;
     return FG_OK;
 }
 

@@ -626,6 +626,16 @@ int fg_tune_lookup(fg_system *const *systems, int count, const fg_solver_opts *o
     return autotune(v, cfg, false, true, out);
 }
 
+int fg_tune_set(fg_system *const *systems, int count, const fg_solver_opts *o, const fg_tune_choice *choice)
+{
+    if (!systems || count < 1 || !o || !choice) { set_error("NULL argument"); return FG_ERR_ARG; }
+    SolveConfig cfg;
+    int r = batch_config(systems, count, o, cfg);
+    if (r) return r;
+    std::vector<fg_system *> v(systems, systems + count);
+    return tune_set(v, cfg, *choice);
+}
+
 void fg_tune_clear(void) { tune_clear(); }
 
 int fg_transport_prepare(fg_system *s, const fg_transport_coeffs *c, const double *u)

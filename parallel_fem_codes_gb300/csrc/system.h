@@ -208,6 +208,7 @@ int bench_matvec(std::vector<fg_system *> &systems, int precision, int reps, dou
 int autotune(std::vector<fg_system *> &sys, const SolveConfig &cfg, bool remeasure, bool lookup_only,
              fg_tune_choice *out);
 void tune_clear();
+int tune_set(std::vector<fg_system *> &sys, const SolveConfig &cfg, const fg_tune_choice &c);
 int launch_matvec_colours(int S, int precision, const SysDev *sys_dev, const EChunk *ch_dev, const int *counts_dev,
                           const int *off_host, int ncol, int maxdof, const double *x, double *y, cudaStream_t st);
 

@@ -103,8 +103,8 @@ class TimeStats(ctypes.Structure):
 
 
 class TuneChoice(ctypes.Structure):
-    _fields_ = [("part_dofs", _c_int), ("mv3_pipeline", _c_int), ("ms_per_cycle", _c_dbl), ("from_cache", _c_int),
-                ("candidates", _c_int)]
+    _fields_ = [("part_dofs", _c_int), ("mv3_pipeline", _c_int), ("ms_per_cycle", _c_dbl),
+                ("from_cache", _c_int), ("candidates", _c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -173,6 +173,7 @@ def lib(build_if_missing: bool = True):
     L.fg_set_memory_limit.argtypes = [ctypes.c_size_t]
     L.fg_autotune.argtypes = [_vp, _c_int, ctypes.POINTER(SolverOpts), _c_int, ctypes.POINTER(TuneChoice)]
     L.fg_tune_lookup.argtypes = [_vp, _c_int, ctypes.POINTER(SolverOpts), ctypes.POINTER(TuneChoice)]
+    L.fg_tune_set.argtypes = [_vp, _c_int, ctypes.POINTER(SolverOpts), ctypes.POINTER(TuneChoice)]
     L.fg_tune_clear.restype = None
     L.fg_memory_in_use.restype = ctypes.c_size_t
     L.fg_get_csr.argtypes = [_vp, ctypes.POINTER(_c_int), _vp, _vp, _vp]
@@ -661,6 +662,16 @@ def tune_lookup(systems, kmax=30, lmax=1000, tol=1e-10, precision=FG_PREC_MIXED,
     c = TuneChoice()
     check(lib().fg_tune_lookup(ctypes.cast(H, _vp), n, ctypes.byref(o), ctypes.byref(c)))
     return c.as_dict()
+
+
+def tune_set(systems, part_dofs, mv3_pipeline=1, kmax=30, lmax=1000, tol=1e-10, precision=FG_PREC_MIXED,
+             inner_tol=0.0):
+    """Install a launch-shape choice for this batch's key without timing."""
+    n = len(systems)
+    H = (_vp * n)(*[s.handle for s in systems])
+    o = SolverOpts(kmax, lmax, tol, precision, inner_tol)
+    c = TuneChoice(part_dofs, mv3_pipeline, 0.0, 0, 0)
+    check(lib().fg_tune_set(ctypes.cast(H, _vp), n, ctypes.byref(o), ctypes.byref(c)))
 
 
 def tune_clear():
