@@ -359,27 +359,30 @@ def euler_leg(fg, G, n=513, steps=20, corrections=2, kmax=25, cpu_job=None):
                      "last_true_rel_residual": st["true_rel_residual"],
                      "rel_diff_vs_blockdiag_fp64": float(np.linalg.norm(u - u_bd) / np.linalg.norm(u_bd))}
     out["csr_ilu0_rcm"] = ilu
-    # block-Jacobi ILU(0) over 1024 row blocks of the RCM numbering: what
-    # 1024 MPI ranks of the reference factorise (each its own rows)
-    bsteps = min(steps, 10)
-    blk = {"blocks": 1024, "steps_timed": bsteps}
-    sc.set_ilu_blocks(1024)
-    sc.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1, precond=fg.FG_PRECOND_ILU0,
-                                       setup_flags=0), kmax=kmax)                                  # warm-up
-    u_bd, _, _ = s.euler_predictor(p, fg.time_opts(0, corrections, 1e-3, 0, bsteps * p.dt, 1e-6, max_steps=bsteps),
+    # block-Jacobi ILU(0) over P row blocks of the RCM numbering: what P MPI
+    # ranks of the reference factorise (each its own rows); substitutions a
+    # warp per block.  Every step of the configuration.
+    u_bd, _, _ = s.euler_predictor(p, fg.time_opts(0, corrections, 1e-3, 0, steps * p.dt, 1e-6, max_steps=steps),
                                    kmax=kmax, tol=1e-10)
-    for name, prec in (("fp64", fg.FG_PREC_FP64), ("mixed", fg.FG_PREC_MIXED)):
-        to = fg.time_opts(0, corrections, 1e-3, 0, bsteps * p.dt, 1e-6, max_steps=bsteps, precond=fg.FG_PRECOND_ILU0,
-                          setup_flags=0)
-        t0 = time.perf_counter()
-        u, a, st = sc.euler_predictor(p, to, kmax=kmax, tol=1e-10, precision=prec)
-        wall = time.perf_counter() - t0
-        blk[name] = {"seconds": wall, "steps": st["steps"], "corrections": st["corrections"],
-                     "gmres_iterations": st["gmres_iterations"], "steps_per_s": st["steps"] / wall,
-                     "ms_per_correction": 1e3 * wall / st["corrections"],
-                     "last_true_rel_residual": st["true_rel_residual"],
-                     "rel_diff_vs_blockdiag_fp64": float(np.linalg.norm(u - u_bd) / np.linalg.norm(u_bd))}
-    out["csr_block_ilu0_rcm"] = blk
+    for nblk in (1024, 4096):
+        blk = {"blocks": nblk, "steps_timed": steps}
+        sc.set_ilu_blocks(nblk)
+        sc.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1, precond=fg.FG_PRECOND_ILU0,
+                                           setup_flags=0), kmax=kmax)                              # warm-up
+        for name, prec in (("fp64", fg.FG_PREC_FP64), ("mixed", fg.FG_PREC_MIXED)):
+            to = fg.time_opts(0, corrections, 1e-3, 0, steps * p.dt, 1e-6, max_steps=steps,
+                              precond=fg.FG_PRECOND_ILU0, setup_flags=0)
+            t0 = time.perf_counter()
+            u, a, st = sc.euler_predictor(p, to, kmax=kmax, tol=1e-10, precision=prec)
+            wall = time.perf_counter() - t0
+            blk[name] = {"seconds": wall, "steps": st["steps"], "corrections": st["corrections"],
+                         "gmres_iterations": st["gmres_iterations"], "steps_per_s": st["steps"] / wall,
+                         "ms_per_correction": 1e3 * wall / st["corrections"],
+                         "last_true_rel_residual": st["true_rel_residual"],
+                         "rel_diff_vs_blockdiag_fp64": float(np.linalg.norm(u - u_bd) / np.linalg.norm(u_bd))}
+        blk["ms_per_correction_vs_blockdiag"] = {
+            k: blk[k]["ms_per_correction"] / out[k]["ms_per_correction"] for k in ("fp64", "mixed")}
+        out[f"csr_block{nblk}_ilu0_rcm"] = blk
     return out
 
 

@@ -190,6 +190,7 @@ struct SysDev {
     void *ilu_tmp;             // forward-substitution output (T, n_pad)
     const int *ilu_ford, *ilu_bord;      // rows in forward / backward level order
     const int2 *ilu_fpass, *ilu_bpass;   // passes (start, rows) of those orders
+    int ilu_P;                           // block-Jacobi row blocks (1: global ILU)
     // truncated SPIKE (precond == FG_PRECOND_SPIKE): sp_P row blocks of the
     // CSR operator, coupling size sp_k; band LU factors, k x k corner
     // couplings, LU of the 2k x 2k reduced systems; FP64 apply scratch
@@ -216,6 +217,7 @@ struct SysDev {
     unsigned *counter;         // 4 counters (one per reduction kernel kind)
     SysState *st;
 };
+constexpr int kIluWsChunk = 8;      // rows per staged chunk of the warp-per-block ILU substitutions
 constexpr int kPartStride = 64;    // doubles per part (>= kmax + 2, kmax <= 60)
 
 // Preconditioners applied by kernels of their own between the matvec and

@@ -45,6 +45,8 @@
 // Compiled with -fmad=false: the factorisation and the FP64 substitutions
 // round exactly as the reference's C.
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <cuda/atomic>
 
 #include "system.h"
@@ -434,6 +436,180 @@ __global__ void k_f64_to_f32(const double *a, float *b, int n)
     if (i < n) b[i] = (float)a[i];
 }
 
+// ---------------------------------------------------------------- block-Jacobi substitutions
+// With block-Jacobi ILU(p) every row reads only rows of its own block, and
+// the dependency depth inside a block of an RCM-ordered FEM matrix is most
+// of its rows (a node's coupled dofs and its RCM neighbours chain): the
+// parallelism is across blocks.  So one warp (a CTA of its own) takes one
+// block and walks its rows in order (forward ascending, backward
+// descending); no row waits on another warp.  Everything a row reads sits
+// in shared memory: the block's values (loaded with the inputs, each
+// overwritten by its row's result: a row's own input is read only by that
+// row), its row pointers and inverse pivots (loaded once per block), and
+// the factor entries of the current chunk of kWsChunk rows, copied with
+// cp.async one chunk ahead into a double buffer.  Per row the G lanes take
+// its entries G at a time and form the products; lane 0 alone subtracts
+// them one by one in entry order (GB300's FP64 pipe is narrow: a chain run
+// by every lane of the warp costs 32 times its work), exactly as fwd_row /
+// bwd_row do, so the result is bit-identical to the level-scheduled sweep.
+constexpr int kWsChunk = kIluWsChunk;
+constexpr int kWsMaxBytes = 64 * 1024;           // shared memory of one block's warp
+
+// shared-memory layout of one warp: rows = block rows (even), ecap = entry capacity of a chunk
+template <typename T> struct WsSmem {
+    size_t prod, xs, ia, dg, dinv, ja, lu, total;
+    __host__ __device__ WsSmem(int rows, int ecap)
+    {
+        prod = 0;                                    // one row's products (32)
+        xs = prod + sizeof(T) * 32;
+        dinv = xs + sizeof(T) * (size_t)rows;
+        ia = dinv + sizeof(T) * (size_t)rows;
+        dg = ia + 4 * (size_t)(rows + 2);
+        lu = (dg + 4 * (size_t)rows + 15) / 16 * 16;
+        ja = lu + 2 * sizeof(T) * (size_t)ecap;
+        total = (ja + 2 * 4 * (size_t)ecap + 15) / 16 * 16;
+    }
+};
+
+__device__ __forceinline__ void cp_async4(void *smem, const void *g)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(g)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *g)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"((unsigned)__cvta_generic_to_shared(smem)), "l"(g)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <typename T, int G>
+__device__ void ws_block(int r0, int r1, const int *__restrict__ ia, const int *__restrict__ ja,
+                         const int *__restrict__ dg, const T *__restrict__ LU, const T *__restrict__ dinv,
+                         const T *__restrict__ in, T *__restrict__ out, bool backward, unsigned char *smem, int rows,
+                         int ecap)
+{
+    const int lane = threadIdx.x & 31;
+    const int m = r1 - r0, nch = (m + kWsChunk - 1) / kWsChunk;
+    const WsSmem<T> L(rows, ecap);
+    T *prod = reinterpret_cast<T *>(smem + L.prod);
+    T *xs = reinterpret_cast<T *>(smem + L.xs);
+    T *dv = reinterpret_cast<T *>(smem + L.dinv);
+    int *ias = reinterpret_cast<int *>(smem + L.ia);
+    int *dgs = reinterpret_cast<int *>(smem + L.dg);
+    T *lus = reinterpret_cast<T *>(smem + L.lu);
+    int *jas = reinterpret_cast<int *>(smem + L.ja);
+    // the block's inputs, row pointers and pivots
+    for (int t = lane; t < m; t += 32) {
+        xs[t] = in[r0 + t];
+        dgs[t] = dg[r0 + t];
+        if (backward) dv[t] = dinv[r0 + t];
+    }
+    for (int t = lane; t <= m; t += 32) ias[t] = ia[r0 + t];
+    __syncwarp();
+    auto rows_of = [&](int c, int &lo, int &hi) {     // block-local row range [lo, hi) of chunk c
+        const int t0 = c * kWsChunk, t1 = min(m, t0 + kWsChunk);
+        lo = backward ? m - t1 : t0;
+        hi = backward ? m - t0 : t1;
+    };
+    auto stage = [&](int c) {                         // the chunk's factor entries into buffer c & 1
+        if (c < nch) {
+            int lo, hi;
+            rows_of(c, lo, hi);
+            const int k0 = ias[lo], cnt = ias[hi] - k0;
+            T *lb = lus + (size_t)(c & 1) * ecap;
+            int *jb = jas + (size_t)(c & 1) * ecap;
+            for (int q = lane; q < cnt; q += 32) {
+                if (sizeof(T) == 8) cp_async8(lb + q, LU + k0 + q); else cp_async4(lb + q, LU + k0 + q);
+                cp_async4(jb + q, ja + k0 + q);
+            }
+        }
+        cp_commit();
+    };
+    stage(0);
+    for (int c = 0; c < nch; ++c) {
+        stage(c + 1);
+        cp_wait<1>();                                 // chunk c's entries have landed
+        __syncwarp();
+        int lo, hi;
+        rows_of(c, lo, hi);
+        const int kb = ias[lo];
+        const T *lb = lus + (size_t)(c & 1) * ecap;
+        const int *jb = jas + (size_t)(c & 1) * ecap;
+        for (int u = 0; u < hi - lo; ++u) {
+            const int t = backward ? hi - 1 - u : lo + u;
+            const int b = backward ? dgs[t] + 1 : ias[t];
+            const int e = backward ? ias[t + 1] : dgs[t];
+            T v = xs[t];
+            for (int base = b; base < e; base += G) {
+                const int k = base + lane;
+                if (lane < G && k < e) {
+                    const int jx = jb[k - kb] - r0;           // in the block by construction
+                    prod[lane] = (unsigned)jx < (unsigned)m ? xs[jx] * lb[k - kb] : (T)0;
+                }
+                __syncwarp();
+                if (lane == 0) {
+                    const int cnt = min(G, e - base);
+                    for (int q = 0; q < cnt; ++q) v = v - prod[q];
+                }
+                __syncwarp();
+            }
+            if (lane == 0) xs[t] = backward ? v * dv[t] : v;
+            __syncwarp();
+        }
+    }
+    cp_wait<0>();
+    for (int t = lane; t < m; t += 32) out[r0 + t] = xs[t];
+}
+
+// rows [r0, r1) of block q of P over n rows (the split of ilu_pattern_setup)
+__device__ __forceinline__ void ws_rows(int n, int P, int q, int &r0, int &r1)
+{
+    r0 = (int)((long long)q * n / P);
+    r1 = (int)((long long)(q + 1) * n / P);
+}
+
+// one system, FP64: in -> out over its P blocks, a warp (CTA) per block
+template <int G>
+__global__ void __launch_bounds__(32)
+k_ilu_ws1(int n, int P, const int *ia, const int *ja, const int *dg, const double *LU, const double *dinv,
+          const double *in, double *out, int backward, int rows, int ecap)
+{
+    extern __shared__ __align__(16) unsigned char ws_smem[];
+    for (int q = blockIdx.x; q < P; q += gridDim.x) {
+        int r0, r1;
+        ws_rows(n, P, q, r0, r1);
+        ws_block<double, G>(r0, r1, ia, ja, dg, LU, dinv, in, out, backward != 0, ws_smem, rows, ecap);
+        __syncwarp();
+    }
+}
+
+// Engine substitutions over a batch, items (system, block), a warp (CTA)
+// each: sel 0 (FP64, gate live) fwd t64 -> ilu_tmp, bwd ilu_tmp -> u64;
+// sel 1 (T, gate in cycle) fwd t -> ilu_tmp, bwd ilu_tmp -> w.
+template <typename T, int G>
+__global__ void __launch_bounds__(32)
+k_ilu_ws(const SysDev *__restrict__ sys, const int2 *__restrict__ items, int nitems, int sel, int backward, int rows,
+         int ecap)
+{
+    extern __shared__ __align__(16) unsigned char ws_smem[];
+    for (int c = blockIdx.x; c < nitems; c += gridDim.x) {
+        const int2 it = items[c];
+        const SysDev &D = sys[it.x];
+        if (sel == 0 ? !D.st->live : !D.st->in_cycle) continue;
+        const T *LU = sizeof(T) == 8 ? (const T *)D.LU64 : (const T *)D.LU32;
+        const T *dinv = sizeof(T) == 8 ? (const T *)D.dinv64 : (const T *)D.dinv32;
+        T *tmp = (T *)D.ilu_tmp;
+        const T *in = backward ? tmp : sel == 0 ? (const T *)D.t64 : (const T *)D.t;
+        T *out = !backward ? tmp : sel == 0 ? (T *)D.u64 : (T *)D.w;
+        int r0, r1;
+        ws_rows(D.n, D.ilu_P, it.y, r0, r1);
+        ws_block<T, G>(r0, r1, D.lu_ia, D.lu_ja, D.lu_dg, LU, dinv, in, out, backward != 0, ws_smem, rows, ecap);
+        __syncwarp();
+    }
+}
+
 // ---------------------------------------------------------------- host side
 // Substitution grid: one 256-thread CTA per SM.  The sweeps are bound by
 // the latency along the dependency levels, not by the number of warps in
@@ -442,6 +618,33 @@ __global__ void k_f64_to_f32(const double *a, float *b, int n)
 static int warps_grid()
 {
     return sm_count();
+}
+
+// Rows of the largest block (rounded up to even) when the warp-per-block
+// substitutions apply: block-Jacobi with at least two blocks whose values,
+// row pointers, pivots and two chunks of factor entries fit one warp's
+// shared memory in FP64; else 0.
+int ilu_ws_rows(const fg_system *s)
+{
+    const int n = s->topo.n;
+    if (s->ilu_blocks < 2 || n < 2) return 0;
+    const int P = std::min(s->ilu_blocks, n);
+    const int rows = (int)((((long long)n + P - 1) / P + 1) & ~1LL);
+    return WsSmem<double>(rows, kWsChunk * std::max(1, s->ilu_maxrow)).total <= (size_t)kWsMaxBytes ? rows : 0;
+}
+
+// dynamic shared memory above the default: raised per kernel when needed
+template <typename K> static void ws_attr(K kern, size_t smem)
+{
+    static std::mutex mu;
+    static std::map<const void *, size_t> set_bytes;
+    if (smem <= 48 * 1024) return;
+    std::lock_guard<std::mutex> lk(mu);
+    size_t &b = set_bytes[reinterpret_cast<const void *>(kern)];
+    if (smem > b) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        b = smem;
+    }
 }
 
 // Level order of the rows for the forward (L) or backward (U) dependency
@@ -474,6 +677,28 @@ static void ilu_schedule(int n, const std::vector<int> &ia, const std::vector<in
 static int sweep1(fg_system *s, bool backward, const double *in, double *out, cudaStream_t st)
 {
     const int n = s->topo.n;
+    if (ilu_ws_rows(s) > 0) {                         // block-Jacobi: a warp per block
+        const int P = std::min(s->ilu_blocks, n), rows = ilu_ws_rows(s), ecap = kWsChunk * s->ilu_maxrow;
+        const size_t smem = WsSmem<double>(rows, ecap).total;
+        const int g = std::max(1, std::min(P, 32 * sm_count()));
+        const int *ia = s->lu_ia.as<int>(), *ja = s->lu_ja.as<int>(), *dg = s->lu_dg.as<int>();
+        const double *LU = s->LU64.as<double>(), *dinv = s->dinv64.as<double>();
+#define FG_WS1(G)                                                                                        \
+    do {                                                                                                 \
+        ws_attr(k_ilu_ws1<G>, smem);                                                                     \
+        k_ilu_ws1<G><<<g, 32, smem, st>>>(n, P, ia, ja, dg, LU, dinv, in, out, backward, rows, ecap);    \
+    } while (0)
+        switch (s->ilu_g) {
+        case 4: FG_WS1(4); break;
+        case 8: FG_WS1(8); break;
+        case 16: FG_WS1(16); break;
+        default: FG_WS1(32); break;
+        }
+#undef FG_WS1
+        FG_CUDA(cudaGetLastError());
+        count_launches(1);
+        return FG_OK;
+    }
     int *ctr = s->ilu_ctr.as<int>(), *err = ctr + 4;
     const int *ia = s->lu_ia.as<int>(), *ja = s->lu_ja.as<int>(), *dg = s->lu_dg.as<int>();
     const double *LU = s->LU64.as<double>(), *dinv = s->dinv64.as<double>();
@@ -615,6 +840,8 @@ int ilu_pattern_setup(fg_system *s)
     int longest = 1;
     for (int i = 0; i < n; ++i) longest = std::max({longest, fdg[i] - fia[i], fia[i + 1] - fdg[i] - 1});
     s->ilu_g = longest <= 4 ? 4 : longest <= 8 ? 8 : longest <= 16 ? 16 : 32;
+    s->ilu_maxrow = 1;
+    for (int i = 0; i < n; ++i) s->ilu_maxrow = std::max(s->ilu_maxrow, fia[i + 1] - fia[i]);
     std::vector<int> fo, bo;
     std::vector<int2> fp, bp;
     ilu_schedule(n, fia, fja, fdg, false, 32 / s->ilu_g, fo, fp);
@@ -731,6 +958,39 @@ int ilu0_apply_device(fg_system *s, const double *p, double *z, cudaStream_t st)
     FG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     FG_CUDA(cudaStreamSynchronize(st));
     if (herr == FG_ERR_TIMEOUT) { set_error("ILU(0): a row dependency wait ran out"); return FG_ERR_TIMEOUT; }
+    return FG_OK;
+}
+
+// Warp-per-block substitution over a batch (engine): items (system, block),
+// rows of the largest block, ecap entries of the longest chunk.
+int launch_ilu_ws(const SysDev *sys, const int2 *items, int nitems, int sel, int backward, int fp32, int lanes,
+                  int rows, int ecap, cudaStream_t st)
+{
+    const size_t smem = fp32 ? WsSmem<float>(rows, ecap).total : WsSmem<double>(rows, ecap).total;
+    const int g = std::max(1, std::min(nitems, 32 * sm_count()));
+#define FG_WS(T, G)                                                                                 \
+    do {                                                                                            \
+        ws_attr(k_ilu_ws<T, G>, smem);                                                              \
+        k_ilu_ws<T, G><<<g, 32, smem, st>>>(sys, items, nitems, sel, backward, rows, ecap);          \
+    } while (0)
+    if (fp32) {
+        switch (lanes) {
+        case 4: FG_WS(float, 4); break;
+        case 8: FG_WS(float, 8); break;
+        case 16: FG_WS(float, 16); break;
+        default: FG_WS(float, 32); break;
+        }
+    } else {
+        switch (lanes) {
+        case 4: FG_WS(double, 4); break;
+        case 8: FG_WS(double, 8); break;
+        case 16: FG_WS(double, 16); break;
+        default: FG_WS(double, 32); break;
+        }
+    }
+#undef FG_WS
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
     return FG_OK;
 }
 

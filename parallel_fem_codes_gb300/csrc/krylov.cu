@@ -263,6 +263,97 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
     }
 }
 
+// The FP64 S x S matvec (S = 6, 9, 12) with a thread per (element, block
+// row) pair of the patch instead of a thread per element, in CTAs of 512
+// threads.  A patch colour of a mesh in natural node order holds only a
+// few hundred patches (7 colours of 256-element patches on a structured
+// mesh), so one launch has that many CTAs: per-element threads left 20% of
+// the warp slots filled, the FP64 pipe 40% busy and the loads of A waiting
+// on each other (ncu: long-scoreboard stalls); per-pair threads put S
+// times more independent rows in flight per CTA (12x12: 1.75 -> 2.07 TB/s
+// at 385x385).  In FP32 the S-fold x gathers from shared memory cost more
+// than that gains (9x9: 2.70 -> 1.97 TB/s), so FP32 keeps k_ebe_mv.  Per patch: x gathered and the patch's local
+// indices staged in shared memory; each pair forms its row product exactly
+// as the per-element kernel does (acc = A_r0 x_0, then acc += A_rm x_m in
+// m order) and stages it; the staged rows are added into the shared y
+// local colour by local colour; each dof is written once (plain store, or
+// red.add for a dof shared with patches of other colours).  Same sums in
+// the same order as k_ebe_mv, so the results are bit-identical.
+constexpr int kMvbThreads = 512;
+template <int S, typename TA, typename TX, typename TY>
+__global__ void __launch_bounds__(kMvbThreads, 2)
+k_ebe_mvb(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const int *__restrict__ nch,
+          int gate, int in_sel, int out_sel, int step, const TX *aux_in, TY *aux_out, int maxdof)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr unsigned short kSink = 0xFFFF;
+    constexpr int PE = patch_elems(S);
+    const MvSmem L(S, maxdof, (int)sizeof(TA));
+    TA *xs = reinterpret_cast<TA *>(smem_raw + L.xs);
+    TA *ys = reinterpret_cast<TA *>(smem_raw + L.ys);
+    TA *ye = reinterpret_cast<TA *>(smem_raw + L.ye);
+    unsigned short *ls = reinterpret_cast<unsigned short *>(smem_raw + L.ls);
+    const int total = *nch;
+    for (int c = blockIdx.x; c < total; c += gridDim.x) {
+        const EChunk k = ch[c];
+        const SysDev &D = sys[k.sys];
+        if (!gated(D, gate)) continue;
+        const TX *X = in_sel == 0 ? (const TX *)D.x
+                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+        TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
+        const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
+        const size_t ld = (size_t)D.nel_pad;
+        const int p = k.e0;
+        const int pe0 = D.pt_elem[p], pne = D.pt_elem[p + 1] - pe0;
+        const int pd0 = D.pt_dof[p], pnd = D.pt_dof[p + 1] - pd0;
+        const unsigned short *pc = D.pt_col + (size_t)p * kPatchColStride;
+        __syncthreads();                      // the previous patch is done with shared memory
+        for (int j = threadIdx.x; j < pnd; j += kMvbThreads) {
+            xs[j] = in_value<TA>(X[D.dofs[pd0 + j] & 0x7fffffff], D);
+            ys[j] = (TA)0;
+        }
+        for (int e = threadIdx.x; e < S * pne; e += kMvbThreads) {
+            const int a = e / pne, q = e - a * pne;
+            ls[a * PE + q] = __ldcs(D.lm16 + a * ld + pe0 + q);
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < S * pne; e += kMvbThreads) {
+            const int r = e / pne, q = e - r * pne;
+            TA xv[S];
+#pragma unroll
+            for (int a = 0; a < S; ++a) {
+                const unsigned short l = ls[a * PE + q];
+                xv[a] = l == kSink ? (TA)0 : xs[l];
+            }
+            const TA *Ar = A + (size_t)(r * S) * ld + pe0 + q;
+            TA acc = ldst(Ar) * xv[0];
+#pragma unroll
+            for (int m = 1; m < S; ++m) acc += ldst(Ar + (size_t)m * ld) * xv[m];
+            ye[r * PE + q] = acc;
+        }
+        __syncthreads();
+        for (int col = 0; col < kPatchMaxLocalColours; ++col) {
+            const int cs = pc[col], ce = pc[col + 1];
+            if (cs >= ce) break;
+            for (int q = cs + threadIdx.x; q < ce; q += kMvbThreads) {
+#pragma unroll
+                for (int r = 0; r < S; ++r) {
+                    const unsigned short l = ls[r * PE + q];
+                    if (l != kSink) ys[l] += ye[r * PE + q];
+                }
+            }
+            __syncthreads();
+        }
+        for (int j = threadIdx.x; j < pnd; j += kMvbThreads) {
+            const int dd = D.dofs[pd0 + j];
+            const int d = dd & 0x7fffffff;
+            if (d == D.n) continue;                       // dof-list padding
+            if (dd < 0) atomicAdd(Y + d, (TY)ys[j]);
+            else Y[d] = (TY)ys[j];
+        }
+    }
+}
+
 // 16-byte asynchronous copy global -> shared (cp.async, L2 only) and its wait.
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem)
 {
@@ -908,7 +999,17 @@ struct MvLaunch {
                     int in_sel, int out_sel, int step, const TX *ai, TY *ao, int maxdof)
     {
         const size_t smem = mv_smem_bytes(S, maxdof, sizeof(TA));
-        auto kern = S == 3 ? k_ebe_mv3<TA, TX, TY> : k_ebe_mv<S, TA, TX, TY>;
+        // FP64 S x S blocks: a thread per (element, row) (the FP64 pipe wants
+        // every warp slot); FP32: a thread per element (its x values
+        // gathered once, not once per row)
+        constexpr bool pairs = S > 3 && sizeof(TA) == 8;
+        auto pick = [] {
+            if constexpr (S == 3) return k_ebe_mv3<TA, TX, TY>;
+            else if constexpr (pairs) return k_ebe_mvb<S, TA, TX, TY>;
+            else return k_ebe_mv<S, TA, TX, TY>;
+        };
+        auto kern = pick();
+        const int nt = pairs ? kMvbThreads : kThreads;
         // the attribute and the occupancy are cached per instantiation
         // (last shared-memory size seen); they are host-side queries only
         static std::mutex mu;
@@ -923,14 +1024,14 @@ struct MvLaunch {
             }
             if (smem != occ_bytes) {
                 int o = 0;
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, kThreads, smem);
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, nt, smem);
                 occ_cached = std::max(o, 1);
                 occ_bytes = smem;
             }
             occ = occ_cached;
         }
         const int g = std::max(1, std::min(nitems, occ * sm_count()));
-        kern<<<g, kThreads, smem, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof);
+        kern<<<g, nt, smem, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof);
     }
     // the 3x3 FP32 bulk-copy pipeline: one CTA per SM, at most one per patch
     template <typename TX, typename TY>
@@ -1041,6 +1142,9 @@ struct Plan {
     DevMem mvrec;                                  // 3x3: per matvec work item, for the bulk-copy pipeline
     bool mv3p = true;                              // 3x3 FP32: the bulk-copy pipeline (else the register kernel)
     DevMem ilu_fwd, ilu_bwd, ilu_ctr;              // sync-free ILU(0) substitutions
+    DevMem ilu_ws;                                 // block-Jacobi: (system, block) items, a warp each
+    int n_ilw = 0, ilu_wx = 0, ilu_we = 0;         // items, rows of the largest block (0: level-scheduled
+                                                   // path), entries of the longest chunk
     DevMem sp_blocks, sp_ifaces;                   // SPIKE (system, block) and (system, interface) items
 };
 
@@ -1114,6 +1218,28 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
             }
         P.n_ilu = (int)fwd.size();
         P.n_ilub = (int)bwd.size();
+        // every member block-Jacobi with blocks small enough: a warp per block
+        int wx = 0, we = 1;
+        bool ws = true;
+        for (int s = 0; s < P.nsys && ws; ++s) {
+            const int rows = ilu_ws_rows(mem[s].s);
+            ws = rows > 0;
+            wx = std::max(wx, rows);
+            we = std::max(we, mem[s].s->ilu_maxrow);
+        }
+        we *= kIluWsChunk;
+        if (ws && P.nsys > 0) {
+            std::vector<int2> wit;
+            for (int s = 0; s < P.nsys; ++s) {
+                const int np = std::max(1, std::min(mem[s].s->ilu_blocks, mem[s].s->topo.n));
+                for (int q = 0; q < np; ++q) wit.push_back(make_int2(s, q));
+            }
+            if ((r0 = P.ilu_ws.alloc(sizeof(int2) * wit.size()))) return r0;
+            FG_CUDA(cudaMemcpyAsync(P.ilu_ws.p, wit.data(), sizeof(int2) * wit.size(), cudaMemcpyHostToDevice, st));
+            P.n_ilw = (int)wit.size();
+            P.ilu_wx = wx;
+            P.ilu_we = we;
+        }
     }
     // SPIKE: one CTA per block and per interface of every member
     std::vector<int2> spb, spi;
@@ -1248,6 +1374,12 @@ static int enqueue_precond(const Plan &P, int sel, cudaStream_t st)
             launch_blockdiag<T>(P.B, grid_for(P.n_nch), st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 1, 1,
                                 nullptr, nullptr);
         return 1;
+    }
+    if (P.precond == FG_PRECOND_ILU0 && P.n_ilw > 0) {
+        const int fp32 = sel == 1 && sizeof(T) == 4;
+        launch_ilu_ws(sys, P.ilu_ws.as<int2>(), P.n_ilw, sel, 0, fp32, P.ilu_g, P.ilu_wx, P.ilu_we, st);
+        launch_ilu_ws(sys, P.ilu_ws.as<int2>(), P.n_ilw, sel, 1, fp32, P.ilu_g, P.ilu_wx, P.ilu_we, st);
+        return 2;
     }
     if (P.precond == FG_PRECOND_ILU0) {
         int *ctr = P.ilu_ctr.as<int>(), *err = ctr + 4;
