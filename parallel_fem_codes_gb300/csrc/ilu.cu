@@ -449,9 +449,13 @@ __global__ void k_f64_to_f32(const double *a, float *b, int n)
 // the factor entries of the current chunk of kWsChunk rows, copied with
 // cp.async one chunk ahead into a double buffer.  Per row the G lanes take
 // its entries G at a time and form the products; lane 0 alone subtracts
-// them one by one in entry order (GB300's FP64 pipe is narrow: a chain run
-// by every lane of the warp costs 32 times its work), exactly as fwd_row /
-// bwd_row do, so the result is bit-identical to the level-scheduled sweep.
+// them one by one in entry order (GB300's FP64 pipe is narrow and takes a
+// whole warp instruction whatever the active lanes: a chain run by every
+// lane cost 20-35% more), exactly as fwd_row / bwd_row do, so the result
+// is bit-identical to the level-scheduled sweep.  Measured on Euler 513^2,
+// 1024 blocks, per correction: the level-scheduled sweep 443 ms (FP64) /
+// 346 ms (FP32 in the mixed solver), this kernel 86 / 71 ms; a lane per
+// block instead (32 blocks a warp, rows read through L1/L2) 303 / 285 ms.
 constexpr int kWsChunk = kIluWsChunk;
 constexpr int kWsMaxBytes = 64 * 1024;           // shared memory of one block's warp
 
