@@ -577,6 +577,77 @@ def run_kernel_tour(args):
     return 0
 
 
+def run_probe(args):
+    """Small single-kernel workloads for profiling (one JSON line each):
+    matvec:euler|ns:N:32|64   the S x S EBE matvec of Euler OBLIQUO / NS cavity N x N
+                              (assembled blocks), 2 warm-up + 2 timed matvecs;
+    ilu:N:P:steps             Euler OBLIQUO N x N, BlockDiag and block-Jacobi ILU(0)
+                              over P row blocks of the RCM CSR operator, FP64 and
+                              mixed, ms per correction;
+    ilusetup:N:P              the ILU(0) set-up (CSR values, factorisation, F <- M^-1 F)
+                              and one application through the host API."""
+    from parallel_fem_codes_gb300 import femgpu as fg, meshgen as G
+    fg.lib(build_if_missing=False)
+    kind, *rest = args.probe.split(":")
+    if kind == "matvec":
+        mesh, n, prec = rest[0], int(rest[1]), int(rest[2])
+        if mesh == "euler":
+            p = G.obliquo_problem(n)
+            s = fg.euler_system(p)
+            s.euler_assemble(p)
+        else:
+            p = G.cavity_problem(n, reynolds=1000.0, jitter=0.2)
+            s = fg.ns_system(p)
+            s.ns_assemble(p)
+        ms, b = fg.bench_matvec([s], precision=prec, reps=2)
+        peak, kindp = peaks()
+        print(json.dumps({"probe": args.probe, "ms": ms, "algorithmic_bytes": b, "GB_per_s": b / ms / 1e6,
+                          "frac": b / ms / 1e6 / peak, "peak_source": kindp, "patch_colours": s.info()["ncolours"]}),
+              flush=True)
+    elif kind == "ilu":
+        n, nb, steps = int(rest[0]), int(rest[1]), int(rest[2])
+        p = G.obliquo_problem(n)
+        s = fg.euler_system(p)
+        s.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1), kmax=25)
+        out = {"probe": args.probe}
+        t0 = time.perf_counter()
+        u_bd, _, st = s.euler_predictor(p, fg.time_opts(0, 2, 1e-3, 0, steps * p.dt, 1e-6, max_steps=steps), kmax=25,
+                                        tol=1e-10)
+        out["blockdiag_ms_per_correction"] = 1e3 * (time.perf_counter() - t0) / st["corrections"]
+        sc = fg.euler_system(p, reorder=True)
+        sc.set_operator(fg.FG_OP_CSR)
+        sc.set_ilu_blocks(nb)
+        sc.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1, precond=fg.FG_PRECOND_ILU0,
+                                           setup_flags=0), kmax=25)
+        for name, prec in (("fp64", fg.FG_PREC_FP64), ("mixed", fg.FG_PREC_MIXED)):
+            to = fg.time_opts(0, 2, 1e-3, 0, steps * p.dt, 1e-6, max_steps=steps, precond=fg.FG_PRECOND_ILU0,
+                              setup_flags=0)
+            t0 = time.perf_counter()
+            u, _, st = sc.euler_predictor(p, to, kmax=25, tol=1e-10, precision=prec)
+            out[name] = {"ms_per_correction": 1e3 * (time.perf_counter() - t0) / st["corrections"],
+                         "gmres_iterations": st["gmres_iterations"], "true_rel_residual": st["true_rel_residual"],
+                         "rel_diff_vs_blockdiag": float(np.linalg.norm(u - u_bd) / np.linalg.norm(u_bd))}
+        print(json.dumps(out), flush=True)
+    elif kind == "ilusetup":
+        n, nb = int(rest[0]), int(rest[1])
+        p = G.obliquo_problem(n)
+        sc = fg.euler_system(p, reorder=True)
+        sc.set_operator(fg.FG_OP_CSR)
+        sc.set_ilu_blocks(nb)
+        R = sc.euler_assemble(p)
+        sc.precond_setup(fg.FG_PRECOND_ILU0, 0, R.copy())
+        t0 = time.perf_counter()
+        sc.precond_setup(fg.FG_PRECOND_ILU0, 0, R.copy())
+        t1 = time.perf_counter()
+        sc.precond_apply(R.copy())
+        t2 = time.perf_counter()
+        print(json.dumps({"probe": args.probe, "setup_ms": 1e3 * (t1 - t0), "apply_ms_host_api": 1e3 * (t2 - t1)}),
+              flush=True)
+    else:
+        raise SystemExit(f"unknown probe {args.probe}")
+    return 0
+
+
 def run_matvec_only(args):
     from parallel_fem_codes_gb300 import femgpu as fg, meshgen as G
     fg.lib(build_if_missing=False)
@@ -611,6 +682,7 @@ def main():
     ap.add_argument("--c5-count", type=int, default=96, help="requests per rate of the mixed serving leg")
     ap.add_argument("--kernel-tour", action="store_true",
                     help="run every kernel family once at a moderate size (the per-kernel ncu table's workload)")
+    ap.add_argument("--probe", default="", help="a single-kernel workload for profiling (see run_probe)")
     ap.add_argument("--matvec-only", action="store_true",
                     help="only the batched FP32 EBE matvec of --count instances (2 warm-up + --steps "
                          "matvecs); the small case the ncu traffic capture runs")
@@ -621,6 +693,8 @@ def main():
     if args.impl == "reference":
         return run_reference(args, rank, ws, dist)
 
+    if args.probe:
+        return run_probe(args)
     if args.matvec_only:
         return run_matvec_only(args)
     if args.kernel_tour:

@@ -280,6 +280,18 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
 // red.add for a dof shared with patches of other colours).  Same sums in
 // the same order as k_ebe_mv, so the results are bit-identical.
 constexpr int kMvbThreads = 512;
+// rows per thread: FP64 one (every warp slot for the FP64 pipe); FP32 S /
+// FG_MVB_GROUPS32 row groups per element, 0 (the default) the per-element
+// k_ebe_mv: measured in FP32 (Euler 385^2 12x12 / NS 513^2 9x9, TB/s),
+// per element 1.82 / 2.70, one group of 512-thread CTAs 1.87 / 1.92, three
+// row groups 1.82 / 2.15.
+#ifndef FG_MVB_GROUPS32
+#define FG_MVB_GROUPS32 0
+#endif
+template <int S, typename TA> constexpr int mvb_rows()
+{
+    return sizeof(TA) == 8 ? 1 : (FG_MVB_GROUPS32 > 0 && S > 3 && S % FG_MVB_GROUPS32 == 0) ? S / FG_MVB_GROUPS32 : 0;
+}
 template <int S, typename TA, typename TX, typename TY>
 __global__ void __launch_bounds__(kMvbThreads, 2)
 k_ebe_mvb(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const int *__restrict__ nch,
@@ -317,19 +329,25 @@ k_ebe_mvb(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
             ls[a * PE + q] = __ldcs(D.lm16 + a * ld + pe0 + q);
         }
         __syncthreads();
-        for (int e = threadIdx.x; e < S * pne; e += kMvbThreads) {
-            const int r = e / pne, q = e - r * pne;
+        constexpr int R = mvb_rows<S, TA>() > 0 ? mvb_rows<S, TA>() : 1, NG = S / R;
+        static_assert(S % R == 0, "rows per thread must divide the block");
+        for (int e = threadIdx.x; e < NG * pne; e += kMvbThreads) {
+            const int g = e / pne, q = e - g * pne;
             TA xv[S];
 #pragma unroll
             for (int a = 0; a < S; ++a) {
                 const unsigned short l = ls[a * PE + q];
                 xv[a] = l == kSink ? (TA)0 : xs[l];
             }
-            const TA *Ar = A + (size_t)(r * S) * ld + pe0 + q;
-            TA acc = ldst(Ar) * xv[0];
 #pragma unroll
-            for (int m = 1; m < S; ++m) acc += ldst(Ar + (size_t)m * ld) * xv[m];
-            ye[r * PE + q] = acc;
+            for (int rr = 0; rr < R; ++rr) {
+                const int r = g * R + rr;
+                const TA *Ar = A + (size_t)(r * S) * ld + pe0 + q;
+                TA acc = ldst(Ar) * xv[0];
+#pragma unroll
+                for (int m = 1; m < S; ++m) acc += ldst(Ar + (size_t)m * ld) * xv[m];
+                ye[r * PE + q] = acc;
+            }
         }
         __syncthreads();
         for (int col = 0; col < kPatchMaxLocalColours; ++col) {
@@ -1002,7 +1020,7 @@ struct MvLaunch {
         // FP64 S x S blocks: a thread per (element, row) (the FP64 pipe wants
         // every warp slot); FP32: a thread per element (its x values
         // gathered once, not once per row)
-        constexpr bool pairs = S > 3 && sizeof(TA) == 8;
+        constexpr bool pairs = S > 3 && mvb_rows<S, TA>() > 0;
         auto pick = [] {
             if constexpr (S == 3) return k_ebe_mv3<TA, TX, TY>;
             else if constexpr (pairs) return k_ebe_mvb<S, TA, TX, TY>;
