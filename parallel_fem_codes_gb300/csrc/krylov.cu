@@ -998,6 +998,15 @@ namespace {
 #define FG_MV3_PIPELINE 1
 #endif
 constexpr bool kMv3Pipeline = FG_MV3_PIPELINE != 0;
+// the matvec kernel of an S x S launch: 3x3, the pair kernel, or per element
+template <int S, typename TA, typename TX, typename TY, bool PAIRS>
+static auto pick_mv()
+{
+    if constexpr (S == 3) return k_ebe_mv3<TA, TX, TY>;
+    else if constexpr (PAIRS && mvb_rows<S, TA>() > 0) return k_ebe_mvb<S, TA, TX, TY>;
+    else return k_ebe_mv<S, TA, TX, TY>;
+}
+
 struct MvLaunch {
     // Persistent CTAs: as many as fit on the GPU (their dynamic shared memory,
     // mv_smem_bytes, decides how many per SM), at most one per patch.
@@ -1020,33 +1029,34 @@ struct MvLaunch {
         // FP64 S x S blocks: a thread per (element, row) (the FP64 pipe wants
         // every warp slot); FP32: a thread per element (its x values
         // gathered once, not once per row)
-        constexpr bool pairs = S > 3 && mvb_rows<S, TA>() > 0;
-        auto pick = [] {
-            if constexpr (S == 3) return k_ebe_mv3<TA, TX, TY>;
-            else if constexpr (pairs) return k_ebe_mvb<S, TA, TX, TY>;
-            else return k_ebe_mv<S, TA, TX, TY>;
-        };
-        auto kern = pick();
+        // the pair kernel only where a colour launch leaves the per-element
+        // kernel's CTA slots (3 per SM) unfilled: FP64 12x12 Euler 513^2
+        // (~290 patches a launch) 2.02 -> 2.46 TB/s, but NS 1025^2 (~1170)
+        // 3.23 -> 2.83 TB/s; both give the same sums
+        constexpr bool can_pair = S > 3 && mvb_rows<S, TA>() > 0;
+        const bool pairs = can_pair && nitems < 3 * sm_count();
+        auto kern = pairs ? pick_mv<S, TA, TX, TY, true>() : pick_mv<S, TA, TX, TY, false>();
         const int nt = pairs ? kMvbThreads : kThreads;
-        // the attribute and the occupancy are cached per instantiation
-        // (last shared-memory size seen); they are host-side queries only
+        // the attribute and the occupancy are cached per kernel (last
+        // shared-memory size seen); they are host-side queries only
         static std::mutex mu;
-        static size_t set_bytes = 0, occ_bytes = 0;
-        static int occ_cached = 1;
+        static size_t set_bytes[2] = {0, 0}, occ_bytes[2] = {0, 0};
+        static int occ_cached[2] = {1, 1};
+        const int w = pairs ? 1 : 0;
         int occ;
         {
             std::lock_guard<std::mutex> lk(mu);
-            if (smem > set_bytes) {
+            if (smem > set_bytes[w]) {
                 cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-                set_bytes = smem;
+                set_bytes[w] = smem;
             }
-            if (smem != occ_bytes) {
+            if (smem != occ_bytes[w]) {
                 int o = 0;
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, nt, smem);
-                occ_cached = std::max(o, 1);
-                occ_bytes = smem;
+                occ_cached[w] = std::max(o, 1);
+                occ_bytes[w] = smem;
             }
-            occ = occ_cached;
+            occ = occ_cached[w];
         }
         const int g = std::max(1, std::min(nitems, occ * sm_count()));
         kern<<<g, nt, smem, st>>>(sys, ch, nch, gate, in_sel, out_sel, step, ai, ao, maxdof);
