@@ -756,6 +756,7 @@ def main():
     torch.cuda.synchronize()
     clk = ClockSampler(os.path.join(tempfile.gettempdir(), f"pfc_bench_clocks_{os.getpid()}_rank{rank}.csv"))
     l0 = fg.launch_count()
+    launches_before_timed = l0
     times, lat = [], []
     with clk:
         for _ in range(args.steps):
@@ -893,7 +894,7 @@ def main():
             "mixed": {"converged_all": conv, "worst_true_rel_residual": worst_res,
                       "iterations_mean": float(np.mean(iters)),
                       "rel_err_vs_fp64_max": max(plain_err) if plain_err else None},
-            "clocks": clocks, "gpu_launches": launches, "e2e": e2e,
+            "clocks": clocks, "gpu_launches": launches, "launches_before_timed": launches_before_timed, "e2e": e2e,
             "roofline": {"bound": "hbm", "kernel": "k_ebe_mv3p<float,float> (all patch colours, batched)",
                          "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_source": peak_kind, "traffic": MATVEC_TRAFFIC_RATIO * bytes_mv,

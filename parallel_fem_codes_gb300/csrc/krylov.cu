@@ -1029,12 +1029,12 @@ struct MvLaunch {
         // FP64 S x S blocks: a thread per (element, row) (the FP64 pipe wants
         // every warp slot); FP32: a thread per element (its x values
         // gathered once, not once per row)
-        // the pair kernel only where a colour launch leaves the per-element
-        // kernel's CTA slots (3 per SM) unfilled: FP64 12x12 Euler 513^2
-        // (~290 patches a launch) 2.02 -> 2.46 TB/s, but NS 1025^2 (~1170)
-        // 3.23 -> 2.83 TB/s; both give the same sums
+        // the pair kernel only for colour launches of up to two waves of the
+        // per-element kernel (3 CTAs per SM): FP64 12x12 Euler 513^2 (7
+        // launches of ~290-512 patches) 2.02 -> 2.46 TB/s, but NS 1025^2
+        // (~1170 a launch) 3.23 -> 2.83 TB/s; both give the same sums
         constexpr bool can_pair = S > 3 && mvb_rows<S, TA>() > 0;
-        const bool pairs = can_pair && nitems < 3 * sm_count();
+        const bool pairs = can_pair && nitems <= 6 * sm_count();
         auto kern = pairs ? pick_mv<S, TA, TX, TY, true>() : pick_mv<S, TA, TX, TY, false>();
         const int nt = pairs ? kMvbThreads : kThreads;
         // the attribute and the occupancy are cached per kernel (last
