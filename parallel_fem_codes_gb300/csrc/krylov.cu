@@ -290,7 +290,8 @@ constexpr int kMvbThreads = 512;
 #endif
 template <int S, typename TA> constexpr int mvb_rows()
 {
-    return sizeof(TA) == 8 ? 1 : (FG_MVB_GROUPS32 > 0 && S > 3 && S % FG_MVB_GROUPS32 == 0) ? S / FG_MVB_GROUPS32 : 0;
+    constexpr int g = FG_MVB_GROUPS32 > 0 ? FG_MVB_GROUPS32 : 1;
+    return sizeof(TA) == 8 ? 1 : (FG_MVB_GROUPS32 > 0 && S > 3 && S % g == 0) ? S / g : 0;
 }
 template <int S, typename TA, typename TX, typename TY>
 __global__ void __launch_bounds__(kMvbThreads, 2)
