@@ -218,9 +218,21 @@ void or_blockdiag_setup(int nnodes, int nel, int B, const int *ien, const double
  * NO_precond in every configuration of the reference's EBE drivers, so it
  * is omitted.  Returns 0; *iterations += Arnoldi steps taken.
  * ------------------------------------------------------------------- */
+static int or_pgmres_lr(int NEQ, int kmax, int lmax, double tol, or_mv_fn mv, or_pc_fn precond, or_pc_fn precondR,
+                        void *ctx, double *B, double *X, int *iterations);
+
 int or_pgmres(int NEQ, int kmax, int lmax, double tol,
               or_mv_fn mv, or_pc_fn precond, void *ctx,
               double *B, double *X, int *iterations)
+{
+    return or_pgmres_lr(NEQ, kmax, lmax, tol, mv, precond, NULL, ctx, B, X, iterations);
+}
+
+/* pgmres.c:5-200 with the right preconditioner precondR applied in place
+ * to v before every matvec (:61, :93) and to X at the end (:186); NULL is
+ * NO_precond. */
+static int or_pgmres_lr(int NEQ, int kmax, int lmax, double tol, or_mv_fn mv, or_pc_fn precond, or_pc_fn precondR,
+                        void *ctx, double *B, double *X, int *iterations)
 {
     int n = NEQ, i, j, k, l = 0, cont = 0;
     double *ubuf = calloc((size_t)kmax * (n + 1), sizeof(double));
@@ -240,6 +252,7 @@ int or_pgmres(int NEQ, int kmax, int lmax, double tol,
         i = 0;
         for (j = 0; j < kmax; j++) memset(U(j), 0, sizeof(double) * n);
         memcpy(v, X, sizeof(double) * n);
+        if (precondR) precondR(ctx, v, v);
         mv(ctx, v, U(0));
         precond(ctx, U(0), U(0));
         for (k = 0; k < n; k++) U(0)[k] += -1.0 * B[k];
@@ -250,6 +263,7 @@ int or_pgmres(int NEQ, int kmax, int lmax, double tol,
         do {
             cont++;
             memcpy(v, U(i), sizeof(double) * n);
+            if (precondR) precondR(ctx, v, v);
             mv(ctx, v, U(i+1));
             precond(ctx, U(i+1), U(i+1));
             for (j = 0; j <= i; j++) {
@@ -291,6 +305,7 @@ int or_pgmres(int NEQ, int kmax, int lmax, double tol,
     } while (rho > eps && l < lmax);
 #undef U
 #undef H
+    if (precondR) precondR(ctx, X, X);
     if (iterations) *iterations += cont;
     free(ubuf); free(h); free(e); free(c); free(s); free(y); free(v);
     return 0;
@@ -396,4 +411,132 @@ void or_block_scale(int nel, int B, const int *ien, const int *Id, int NEQ, cons
         }
     }
     free(m);
+}
+
+/* ---- element preconditioners of the EBE scheme (Preconditioner "LUe",
+ * "SGSe"; 3x3 blocks).  Both sweep the elements in order, in place on z
+ * (z[NEQ] is the sink, kept 0), each element reading the values the
+ * earlier ones wrote.  The expressions keep the reference's association:
+ * `a += -b*c - d*e` adds ((-(b*c)) - d*e) to a. ---- */
+
+/* LU_precond_EBE_setup.c:20-31: per element, the LU factors of its block
+ * with unit diagonal taken as 1 (A row-major, 9 per element). */
+void or_lue_setup(int nel, const double *A, double *LUe)
+{
+    for (int I = 0; I < nel; I++) {
+        const double *a = A + 9 * (long)I;
+        double *L = LUe + 9 * (long)I;
+        L[0] = 1.0;
+        L[1] = a[1];
+        L[2] = a[2];
+        L[3] = a[3];
+        L[4] = 1. / (1.0 - a[1] * a[3]);
+        L[5] = a[5] - a[2] * a[3];
+        L[6] = a[6];
+        L[7] = (a[7] - a[1] * a[6]) * L[4];
+        L[8] = 1. / (1.0 - a[2] * a[6] - L[7] * L[5]);
+    }
+}
+
+/* LU_precond_EBE.c:28-60: L then U of each element, in element order. */
+void or_lue_apply(int nel, const int *lm, int NEQ, const double *LUe, double *z)
+{
+    z[NEQ] = 0;
+    for (int I = 0; I < nel; I++) {
+        const int l0 = lm[3 * I], l1 = lm[3 * I + 1], l2 = lm[3 * I + 2];
+        const double *L = LUe + 9 * (long)I;
+        double z0 = z[l0], z1 = z[l1], z2 = z[l2];
+        z1 += -L[3] * z0;
+        z2 += -L[6] * z0 - L[7] * z1;
+        z2 *= L[8];
+        z1 = (z1 - L[5] * z2) * L[4];
+        z0 += -L[1] * z1 - L[2] * z2;
+        z[l0] = z0;
+        z[l1] = z1;
+        z[l2] = z2;
+        z[NEQ] = 0;
+    }
+}
+
+/* SGS_precond_EBE.c:4-40: the forward (lower) sweep, element order. */
+void or_sgs_fwd(int nel, const int *lm, int NEQ, const double *A, double *z)
+{
+    z[NEQ] = 0;
+    for (int I = 0; I < nel; I++) {
+        const int l0 = lm[3 * I], l1 = lm[3 * I + 1], l2 = lm[3 * I + 2];
+        const double *a = A + 9 * (long)I;
+        double z0 = z[l0], z1 = z[l1], z2 = z[l2];
+        z1 += -a[3] * z0;
+        z2 += -a[6] * z0 - a[7] * z1;
+        z[l1] = z1;
+        z[l2] = z2;
+        z[NEQ] = 0.0;
+    }
+}
+
+/* SGS_precond_EBE.c:42-76 (SGS_precondR_EBE): the backward (upper) sweep,
+ * elements in reverse order. */
+void or_sgs_bwd(int nel, const int *lm, int NEQ, const double *A, double *z)
+{
+    z[NEQ] = 0;
+    for (int I = nel - 1; I >= 0; I--) {
+        const int l0 = lm[3 * I], l1 = lm[3 * I + 1], l2 = lm[3 * I + 2];
+        const double *a = A + 9 * (long)I;
+        double z0 = z[l0], z1 = z[l1], z2 = z[l2];
+        z1 += -a[5] * z2;
+        z0 += -a[1] * z1 - a[2] * z2;
+        z[l0] = z0;
+        z[l1] = z1;
+        z[NEQ] = 0.0;
+    }
+}
+
+typedef struct {
+    ebe_ctx e;
+    const double *LUe;
+} elem_ctx;
+
+static int lue_pc_cb(void *p, double *x, double *z)
+{
+    elem_ctx *c = (elem_ctx *)p;
+    if (z != x) memcpy(z, x, sizeof(double) * (c->e.NEQ + 1));
+    or_lue_apply(c->e.nel, c->e.lm, c->e.NEQ, c->LUe, z);
+    return 0;
+}
+static int sgs_fwd_cb(void *p, double *x, double *z)
+{
+    elem_ctx *c = (elem_ctx *)p;
+    if (z != x) memcpy(z, x, sizeof(double) * (c->e.NEQ + 1));
+    or_sgs_fwd(c->e.nel, c->e.lm, c->e.NEQ, c->e.A, z);
+    return 0;
+}
+static int sgs_bwd_cb(void *p, double *x, double *z)
+{
+    elem_ctx *c = (elem_ctx *)p;
+    if (z != x) memcpy(z, x, sizeof(double) * (c->e.NEQ + 1));
+    or_sgs_bwd(c->e.nel, c->e.lm, c->e.NEQ, c->e.A, z);
+    return 0;
+}
+
+/* The element preconditioners' set-up (F <- M^-1 F) and pgmres, as
+ * Process.c:59-76 sequences them: kind 1 LUe (precond LU_precond_EBE,
+ * precondR NO_precond), kind 2 SGSe (precond SGS_precond_EBE, precondR
+ * SGS_precondR_EBE).  mv is ebemv (with the local RCM when Perm is given).
+ * Returns the GMRES iterations; F is preconditioned in place. */
+int or_ebe_elem_solve(int kind, int nel, const int *lm, const double *A, int NEQ, const int *Perm,
+                      const int *invPerm, double *F, int kmax, int lmax, double tol, double *X)
+{
+    double *LUe = kind == 1 ? calloc((size_t)9 * nel, sizeof(double)) : NULL;
+    elem_ctx c = { { nel, 3, NEQ, lm, Perm, invPerm, A, NULL }, LUe };
+    int it = 0;
+    if (kind == 1) {
+        or_lue_setup(nel, A, LUe);
+        or_lue_apply(nel, lm, NEQ, LUe, F);
+        or_pgmres_lr(NEQ, kmax, lmax, tol, ebe_mv_cb, lue_pc_cb, NULL, &c, F, X, &it);
+    } else {
+        or_sgs_fwd(nel, lm, NEQ, A, F);
+        or_pgmres_lr(NEQ, kmax, lmax, tol, ebe_mv_cb, sgs_fwd_cb, sgs_bwd_cb, &c, F, X, &it);
+    }
+    free(LUe);
+    return it;
 }

@@ -96,6 +96,17 @@ int or_pgmres(int NEQ, int kmax, int lmax, double tol,
               or_mv_fn mv, or_pc_fn precond, void *ctx,
               double *B, double *X, int *iterations);
 
+/* ---- element preconditioners "LUe" / "SGSe" (EBE/LU_precond_EBE*.c,
+ * EBE/SGS_precond_EBE*.c), 3x3 blocks, z (NEQ+1) in place ---- */
+void or_lue_setup(int nel, const double *A, double *LUe);
+void or_lue_apply(int nel, const int *lm, int NEQ, const double *LUe, double *z);
+void or_sgs_fwd(int nel, const int *lm, int NEQ, const double *A, double *z);
+void or_sgs_bwd(int nel, const int *lm, int NEQ, const double *A, double *z);
+/* set-up (F <- M^-1 F) + pgmres with the left / right pair: kind 1 LUe,
+ * kind 2 SGSe.  Returns GMRES iterations. */
+int or_ebe_elem_solve(int kind, int nel, const int *lm, const double *A, int NEQ, const int *Perm,
+                      const int *invPerm, double *F, int kmax, int lmax, double tol, double *X);
+
 /* One linear solve of an assembled EBE system (S = 3B) with the nodal
  * block-diagonal preconditioner: set-up (F preconditioned in place), then
  * pgmres.  Returns GMRES iterations. */

@@ -104,6 +104,16 @@ def lib():
                                         _f64p, _f64p, _f64p, _c_int, _c_int, _c_dbl, _f64p]
         L.or_ebe_block_solve.argtypes = [_c_int, _c_int, _c_int, _i32p, _i32p, _f64p, _i32p, _c_int, _c_int,
                                          _f64p, _c_int, _c_int, _c_dbl, _f64p]
+        L.or_lue_setup.argtypes = [_c_int, _f64p, _f64p]
+        L.or_lue_setup.restype = None
+        L.or_lue_apply.argtypes = [_c_int, _i32p, _c_int, _f64p, _f64p]
+        L.or_lue_apply.restype = None
+        L.or_sgs_fwd.argtypes = [_c_int, _i32p, _c_int, _f64p, _f64p]
+        L.or_sgs_fwd.restype = None
+        L.or_sgs_bwd.argtypes = [_c_int, _i32p, _c_int, _f64p, _f64p]
+        L.or_sgs_bwd.restype = None
+        L.or_ebe_elem_solve.argtypes = [_c_int, _c_int, _i32p, _f64p, _c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        _f64p, _c_int, _c_int, _c_dbl, _f64p]
         L.or_build_ns.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
                                   ctypes.c_void_p, _f64p, _f64p, _f64p]
         L.or_build_ns.restype = None
@@ -164,6 +174,10 @@ def _setup_sst(R):
         R.fr_ebemv.restype = None
         R.fr_diag_pgmres.argtypes = [_c_int, _c_int, _i32p, _f64p, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p,
                                      _c_int, _c_int, _c_dbl]
+        R.fr_ebe_prec_apply.argtypes = [_c_int, _c_int, _c_int, _i32p, _f64p, _f64p]
+        R.fr_ebe_prec_apply.restype = None
+        R.fr_ebe_prec_pgmres.argtypes = [_c_int, _c_int, _c_int, _i32p, _f64p, _i32p, _i32p, _f64p, _f64p,
+                                         _c_int, _c_int, _c_dbl]
         R.fr_symrcm.argtypes = [_c_int, _c_int, _i32p, _i32p, _i32p]
         R.fr_symrcm.restype = None
         R.fr_sst_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
@@ -613,6 +627,56 @@ def ebe_diag_solve(lm, A, NEQ, F, perm=None, inv=None, Diag=None, kmax=30, lmax=
                                  np.ascontiguousarray(A, dtype=np.float64).reshape(-1), NEQ,
                                  pp, ip, Diag, invDiag, F, kmax, lmax, tol, X)
     return X, it, Diag, invDiag, F
+
+
+# ---- element preconditioners "LUe" (kind 1) and "SGSe" (kind 2) ----
+def _lmA(lm, A):
+    return (np.ascontiguousarray(lm, dtype=np.int32).reshape(-1), np.ascontiguousarray(A, dtype=np.float64).reshape(-1))
+
+
+def elem_prec_apply(kind, lm, A, NEQ, z):
+    """kind 1: LUe set-up + LU_precond_EBE; 2: the SGS forward sweep; 3: the
+    SGS backward sweep (SGS_precondR_EBE); z (NEQ+1) not modified."""
+    l, a = _lmA(lm, A)
+    nel = lm.shape[0]
+    z = np.array(z, dtype=np.float64, copy=True)
+    if kind == 1:
+        LUe = np.zeros(9 * nel)
+        lib().or_lue_setup(nel, a, LUe)
+        lib().or_lue_apply(nel, l, NEQ, LUe, z)
+    elif kind == 2:
+        lib().or_sgs_fwd(nel, l, NEQ, a, z)
+    else:
+        lib().or_sgs_bwd(nel, l, NEQ, a, z)
+    return z
+
+
+def ebe_elem_solve(kind, lm, A, NEQ, F, perm=None, inv=None, kmax=30, lmax=1000, tol=1e-10):
+    """Element-preconditioner set-up + pgmres (kind 1 LUe, 2 SGSe);
+    returns (X, iterations, F')."""
+    l, a = _lmA(lm, A)
+    F = np.array(F, dtype=np.float64, copy=True)
+    X = np.zeros(NEQ + 1)
+    pp = perm.ctypes.data if perm is not None else None
+    ip = inv.ctypes.data if inv is not None else None
+    it = lib().or_ebe_elem_solve(kind, lm.shape[0], l, a, NEQ, pp, ip, F, kmax, lmax, tol, X)
+    return X, it, F
+
+
+def ref_elem_prec_apply(kind, lm, A, NEQ, z):
+    l, a = _lmA(lm, A)
+    z = np.array(z, dtype=np.float64, copy=True)
+    ref().fr_ebe_prec_apply(kind, lm.shape[0], NEQ, l, a, z)
+    return z
+
+
+def ref_ebe_elem_solve(kind, lm, A, perm, inv, F, kmax=30, lmax=1000, tol=1e-10):
+    l, a = _lmA(lm, A)
+    n = perm.shape[0] - 1
+    F = np.array(F, dtype=np.float64, copy=True)
+    X = np.zeros(n + 1)
+    it = ref().fr_ebe_prec_pgmres(kind, lm.shape[0], n, l, a, perm, inv, F, X, kmax, lmax, tol)
+    return X, it, F
 
 
 def ebe_block_solve(mesh, A, F, kmax=30, lmax=1000, tol=1e-10, ref_quirks=True):

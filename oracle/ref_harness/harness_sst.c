@@ -267,6 +267,63 @@ int fr_diag_pgmres(int nel, int NEQ, const int *lm, const double *A, const int *
     return Pm.iterations;
 }
 
+/* The element preconditioners of the reference on caller blocks (row-major
+ * 3x3 per element) and LM: kind 1 LU_precond_EBE_setup (which applies
+ * LU_precond_EBE to z), 2 SGS_precond_EBE, 3 SGS_precondR_EBE; z (NEQ+1)
+ * in place. */
+void fr_ebe_prec_apply(int kind, int nel, int NEQ, const int *lm, const double *A, double *z)
+{
+    ParametersType Pm; MatrixDataType M; FemStructsType S;
+    int I;
+    memset(&Pm, 0, sizeof Pm); memset(&M, 0, sizeof M); memset(&S, 0, sizeof S);
+    Pm.NEQ = NEQ; Pm.neq = NEQ; Pm.nel = nel; Pm.NPROC = 1;
+    int **l = calloc((size_t)nel, sizeof(int *));
+    double **a = calloc((size_t)nel, sizeof(double *));
+    for (I = 0; I < nel; I++) { l[I] = (int *)&lm[3*I]; a[I] = (double *)&A[9*I]; }
+    S.lm = l; M.A = a;
+    if (kind == 1) {
+        LU_precond_EBE_setup(&Pm, &M, &S, 1, z);
+        free(M.LUeaux); free(M.LUe);
+    } else if (kind == 2) {
+        SGS_precond_EBE(&Pm, &M, &S, z, z);
+    } else {
+        SGS_precondR_EBE(&Pm, &M, &S, z, z);
+    }
+    free(l); free(a);
+}
+
+/* LU_precond_EBE_setup / SGS_precond_EBE_setup followed by pgmres (mv =
+ * ebemv with the local RCM), with the precond / precondR pair that
+ * setPreconditioner.c:11-31 installs for "LUe" (kind 1) and "SGSe" (kind
+ * 2).  F is preconditioned in place; returns Parameters->iterations. */
+int fr_ebe_prec_pgmres(int kind, int nel, int NEQ, const int *lm, const double *A, const int *Perm,
+                       const int *invPerm, double *F, double *X, int kmax, int lmax, double tol)
+{
+    ParametersType Pm; MatrixDataType M; FemStructsType S; FemFunctionsType Fn;
+    int I;
+    memset(&Pm, 0, sizeof Pm); memset(&M, 0, sizeof M);
+    memset(&S, 0, sizeof S); memset(&Fn, 0, sizeof Fn);
+    Pm.NEQ = NEQ; Pm.neq = NEQ; Pm.nel = nel; Pm.NPROC = 1;
+    Pm.KrylovBasisVectorsQuantity = kmax; Pm.LinearMaxIter = lmax;
+    Pm.SolverTolerance = tol; Pm.iterations = 0;
+    int **l = calloc((size_t)nel, sizeof(int *));
+    double **a = calloc((size_t)nel, sizeof(double *));
+    for (I = 0; I < nel; I++) { l[I] = (int *)&lm[3*I]; a[I] = (double *)&A[9*I]; }
+    S.lm = l; M.A = a; M.Perm = (int *)Perm; M.invPerm = (int *)invPerm;
+    Fn.mv = ebemv;
+    if (kind == 1) {
+        Fn.precond = LU_precond_EBE; Fn.precondR = NO_precond;
+        LU_precond_EBE_setup(&Pm, &M, &S, 1, F);
+    } else {
+        Fn.precond = SGS_precond_EBE; Fn.precondR = SGS_precondR_EBE;
+        SGS_precond_EBE_setup(&Pm, &M, &S, 1, F);
+    }
+    pgmres(&Pm, &M, &S, &Fn, F, X);
+    if (kind == 1) { free(M.LUeaux); free(M.LUe); }
+    free(l); free(a);
+    return Pm.iterations;
+}
+
 /* REORDERING_SYMRCM on a caller CSR pattern (not modified). */
 void fr_symrcm(int n, int nnz, int *IA, int *JA, int *perm)
 {

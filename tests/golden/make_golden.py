@@ -244,6 +244,32 @@ def write_tt():
     np.savez_compressed(os.path.join(HERE, "tt_ref.npz"), **out)
 
 
+def write_elem_prec():
+    """The steady driver's element preconditioners (Preconditioner "LUe" and
+    "SGSe": LU_precond_EBE*.c, SGS_precond_EBE*.c and pgmres with their
+    precond / precondR pair, oracle/_ref/libref_sst.so) on the SUPG blocks
+    of a 17x17 and a 33x33 transport problem: one application of each sweep
+    to a random vector and the preconditioned right-hand side and solution
+    of each solve."""
+    out = {}
+    for n in (17, 33):
+        p = G.transport_problem(n, angle_deg=30.0, k=1e-3)
+        m = p.mesh
+        A, F = O.build_k_f_supg(p)
+        lm = O.fill_lm(m)
+        perm, inv, _ = O.permutation_of_lm(m)
+        z = np.append(np.random.default_rng(n).standard_normal(m.neq), 0.0)
+        key = f"ep_{n}"
+        out[key + "_z"] = z
+        for kind in (1, 2, 3):
+            out[key + f"_apply{kind}"] = O.ref_elem_prec_apply(kind, lm, A, m.neq, z)
+        for kind in (1, 2):
+            X, it, Fp = O.ref_ebe_elem_solve(kind, lm, A, perm, inv, F, kmax=30, lmax=200, tol=1e-10)
+            out[key + f"_X{kind}"], out[key + f"_F{kind}"], out[key + f"_it{kind}"] = X, Fp, np.array([it])
+        print(key)
+    np.savez_compressed(os.path.join(HERE, "elem_prec_sst.npz"), **out)
+
+
 if __name__ == "__main__":
     main()
     write_euler()
@@ -254,3 +280,4 @@ if __name__ == "__main__":
     write_ilup()
     write_euler_dd()
     write_tt()
+    write_elem_prec()
