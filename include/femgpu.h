@@ -160,7 +160,10 @@ int fg_get_csr(const fg_system *s, int *nnz, int *IA, int *JA, double *AA);
 /* ---- preconditioners (Solvers_and_Preconditioners/preconditioners.h) ---- */
 enum { FG_PRECOND_NONE = 0, FG_PRECOND_DIAG = 1, FG_PRECOND_BLOCKDIAG = 2,
        FG_PRECOND_ILU0 = 3, /* ILU(0) of the assembled CSR operator (fg_set_operator) */
-       FG_PRECOND_SPIKE = 4 /* truncated SPIKE of the CSR operator (fg_set_spike)   */ };
+       FG_PRECOND_SPIKE = 4, /* truncated SPIKE of the CSR operator (fg_set_spike)  */
+       FG_PRECOND_LUE = 5,  /* element LU sweep, Preconditioner "LUe" (3x3 EBE, FP64) */
+       FG_PRECOND_SGSE = 6  /* element symmetric Gauss-Seidel, "SGSe": forward sweep
+                               on the left, backward sweep on the right (3x3 EBE, FP64) */ };
 /* Truncated SPIKE ("SPIKEk", CSR/SPIKE_precond_setup.c:10-312 and
  * CSR/SPIKE_precond.c:8-158).  The reference's P MPI ranks become `parts`
  * row blocks of the CSR operator on one GPU (at most n / 2k, so every block
@@ -223,6 +226,11 @@ int fg_unscale(fg_system *s, double *X);
 int fg_precond_setup(fg_system *s, int kind, int flags, double *F);
 /* z = M^-1 p for host vectors of n+1 entries (p == z allowed). */
 int fg_precond_apply(fg_system *s, const double *p, double *z);
+/* The right preconditioner of the system's set-up applied to p (host
+ * vectors of NEQ + 1, reference numbering): the backward element sweep of
+ * FG_PRECOND_SGSE (SGS_precondR_EBE), the identity for every other kind
+ * (NO_precond).  p may equal z. */
+int fg_precond_apply_right(fg_system *s, const double *p, double *z);
 /* Diagonal used by the Diag preconditioner (n+1 entries, host). */
 int fg_get_diag(const fg_system *s, double *Diag);
 int fg_set_diag(fg_system *s, const double *Diag);

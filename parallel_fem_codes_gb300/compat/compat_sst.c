@@ -3,6 +3,7 @@
  * entry points, with the reference's names and signatures, running on the
  * GPU through libfemgpu.  Linking this library instead of
  * pgmres.c, ebemv.c, Diag_precond.c, EBE/Diag_precond_EBE_setup.c,
+ * EBE/LU_precond_EBE*.c, EBE/SGS_precond_EBE*.c ("LUe", "SGSe"),
  * NO_precond.c and NO_precond_setup.c (EBE storage) or csr_assembly.c,
  * csrmv.c, CSR/ILUp_precond*.c and CSR/SPIKE_precond*.c (MatrixVector-
  * ProductScheme "CSR" with "ILU0" or "SPIKEk") leaves every driver file
@@ -159,6 +160,59 @@ int Diag_precond(ParametersType *P, MatrixDataType *M, FemStructsType *S, double
     return rc ? fgc_fail(rc, "Diag_precond") : 0;
 }
 
+/* The element preconditioners (Preconditioner "LUe", "SGSe"; EBE
+ * storage): LU_precond_EBE_setup (EBE/LU_precond_EBE_setup.c:4-35) and
+ * SGS_precond_EBE_setup (EBE/SGS_precond_EBE_setup.c:4-12) build them from
+ * the current blocks and precondition F in place; LU_precond_EBE,
+ * SGS_precond_EBE and SGS_precondR_EBE apply them in place on the owned
+ * slice (p is not read, as in the reference: the drivers pass p == z). */
+static int fgc_elem_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int kind, double *F,
+                          const char *where)
+{
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    if (fgc_upload_blocks(sys, M)) return 1;
+    double keep = F[P->neq];
+    F[P->neq] = 0.0;
+    int rc = fg_precond_setup(sys, kind, 0, F);
+    F[P->neq] = keep;
+    return rc ? fgc_fail(rc, where) : 0;
+}
+static int fgc_elem_apply(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *z, int right,
+                          const char *where)
+{
+    fg_system *sys = fgc_system(P, M, S);
+    if (!sys) return 1;
+    z[P->neq] = 0.0;
+    int rc = right ? fg_precond_apply_right(sys, z, z) : fg_precond_apply(sys, z, z);
+    return rc ? fgc_fail(rc, where) : 0;
+}
+int LU_precond_EBE_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
+{
+    (void)tag;
+    return fgc_elem_setup(P, M, S, FG_PRECOND_LUE, F, "LU_precond_EBE_setup");
+}
+int LU_precond_EBE(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    (void)p;
+    return fgc_elem_apply(P, M, S, z, 0, "LU_precond_EBE");
+}
+int SGS_precond_EBE_setup(ParametersType *P, MatrixDataType *M, FemStructsType *S, int tag, double *F)
+{
+    (void)tag;
+    return fgc_elem_setup(P, M, S, FG_PRECOND_SGSE, F, "SGS_precond_EBE_setup");
+}
+int SGS_precond_EBE(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    (void)p;
+    return fgc_elem_apply(P, M, S, z, 0, "SGS_precond_EBE");
+}
+int SGS_precondR_EBE(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *p, double *z)
+{
+    (void)p;
+    return fgc_elem_apply(P, M, S, z, 1, "SGS_precondR_EBE");
+}
+
 /* ebemv (EBE/ebemv.c:4-64): Q = A P over NEQ + 1 entries; Q[NEQ] = 0. */
 int ebemv(ParametersType *P, MatrixDataType *M, FemStructsType *S, double *Pv, double *Qv)
 {
@@ -254,12 +308,16 @@ int pgmres(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctions
 {
     fg_system *sys = fgc_system(P, M, S);
     if (!sys) return 1;
-    const int ebe_ok = Fn->mv == ebemv && (Fn->precond == Diag_precond || Fn->precond == NO_precond);
-    const int csr_ok = Fn->mv == csrmv && (Fn->precond == ILUp_precond || Fn->precond == SPIKE_precond ||
-                                           Fn->precond == NO_precond);
-    if ((Fn->precondR && Fn->precondR != NO_precond) || !(ebe_ok || csr_ok)) {
-        fprintf(stderr, "femgpu: pgmres supports mv = ebemv with Diag or no preconditioning, or mv = csrmv with "
-                        "ILU(p), SPIKE or no preconditioning, on the GPU\n");
+    const int right_none = !Fn->precondR || Fn->precondR == NO_precond;
+    const int ebe_ok = Fn->mv == ebemv &&
+                       (((Fn->precond == Diag_precond || Fn->precond == NO_precond || Fn->precond == LU_precond_EBE) &&
+                         right_none) ||
+                        (Fn->precond == SGS_precond_EBE && Fn->precondR == SGS_precondR_EBE));
+    const int csr_ok = Fn->mv == csrmv && right_none &&
+                       (Fn->precond == ILUp_precond || Fn->precond == SPIKE_precond || Fn->precond == NO_precond);
+    if (!(ebe_ok || csr_ok)) {
+        fprintf(stderr, "femgpu: pgmres supports mv = ebemv with Diag, LUe, SGSe (with its right sweep) or no "
+                        "preconditioning, or mv = csrmv with ILU(p), SPIKE or no preconditioning, on the GPU\n");
         if (!getenv("FEMGPU_COMPAT_NO_EXIT")) exit(1);
         return 1;
     }

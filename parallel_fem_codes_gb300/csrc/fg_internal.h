@@ -191,6 +191,10 @@ struct SysDev {
     const int *ilu_ford, *ilu_bord;      // rows in forward / backward level order
     const int2 *ilu_fpass, *ilu_bpass;   // passes (start, rows) of those orders
     int ilu_P;                           // block-Jacobi row blocks (1: global ILU)
+    // element preconditioners (FG_PRECOND_LUE / SGSE): per element, in the
+    // reference element order, its internal dofs (sink n) and 9 coefficients
+    const int *ep_lmi;
+    const double *ep_coef;
     // truncated SPIKE (precond == FG_PRECOND_SPIKE): sp_P row blocks of the
     // CSR operator, coupling size sp_k; band LU factors, k x k corner
     // couplings, LU of the 2k x 2k reduced systems; FP64 apply scratch

@@ -147,7 +147,8 @@ k_ebe_mv(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const in
         const SysDev &D = sys[k.sys];
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
-                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad
+                    : in_sel == 3 ? (const TX *)D.r64 : aux_in;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
@@ -312,7 +313,8 @@ k_ebe_mvb(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
         const SysDev &D = sys[k.sys];
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
-                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad
+                    : in_sel == 3 ? (const TX *)D.r64 : aux_in;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
@@ -417,7 +419,8 @@ k_ebe_mv3(const SysDev *__restrict__ sys, const EChunk *__restrict__ ch, const i
         const SysDev &D = sys[k.sys];
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
-                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad
+                    : in_sel == 3 ? (const TX *)D.r64 : aux_in;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *A = sizeof(TA) == 8 ? (const TA *)D.A64 : (const TA *)D.A32;
         const size_t ld = (size_t)D.nel_pad;
@@ -641,7 +644,8 @@ k_ebe_mv3p(const SysDev *__restrict__ sys, const MvRec *__restrict__ rec, const 
             const int pne = r.pn & 0xFFFF, pnd = r.pn >> 16, xlen = r.nx >> 16;
             const int W = (pne + 15) & ~15;
             const TX *X = in_sel == 0 ? (const TX *)D.x
-                        : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+                        : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad
+                    : in_sel == 3 ? (const TX *)D.r64 : aux_in;
             void *Y = out_sel == 0 ? (void *)D.t64 : out_sel == 1 ? (void *)D.t : (void *)aux_out;
             const int n = D.n;
             const float vsci = D.vsci;
@@ -761,7 +765,8 @@ k_csr_mv(const SysDev *__restrict__ sys, const DChunk *__restrict__ ch, const in
         const SysDev &D = sys[k.sys];
         if (!gated(D, gate)) continue;
         const TX *X = in_sel == 0 ? (const TX *)D.x
-                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad : aux_in;
+                    : in_sel == 1 ? (const TX *)D.V + (size_t)step * D.n_pad
+                    : in_sel == 3 ? (const TX *)D.r64 : aux_in;
         TY *Y = out_sel == 0 ? (TY *)D.t64 : out_sel == 1 ? (TY *)D.t : aux_out;
         const TA *AA = sizeof(TA) == 8 ? (const TA *)D.AA64 : (const TA *)D.AA32;
         for (int base = k.d0; base < k.d1; base += ngrp) {
@@ -1170,6 +1175,7 @@ struct Plan {
     DevMem sysdev, echunks, ecount, dchunks, dcount, nchunks, ncount, live;
     DevMem mvrec;                                  // 3x3: per matvec work item, for the bulk-copy pipeline
     bool mv3p = true;                              // 3x3 FP32: the bulk-copy pipeline (else the register kernel)
+    bool rprec = false;                            // a right preconditioner (SGSe) before every matvec
     DevMem ilu_fwd, ilu_bwd, ilu_ctr;              // sync-free ILU(0) substitutions
     DevMem ilu_ws;                                 // block-Jacobi: (system, block) items, a warp each
     int n_ilw = 0, ilu_wx = 0, ilu_we = 0;         // items, rows of the largest block (0: level-scheduled
@@ -1207,6 +1213,7 @@ static int build_plan(Plan &P, std::vector<BatchMember> &mem, const SolveConfig 
     fg_tune_choice tc;
     const bool tuned = tuned_choice(mem, cfg, tc);
     P.mv3p = !(tuned && tc.mv3_pipeline == 0);
+    P.rprec = cfg.precond == FG_PRECOND_SGSE;
     for (int s = 0; s < P.nsys; ++s) {
         int n = mem[s].s->topo.n;
         hs[s].nparts = parts_for(n, pdofs);
@@ -1359,6 +1366,13 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
     const bool f64 = mode == 0 || mode == 3;
     const int gate = mode == 0 ? 0 : mode == 1 ? 1 : -1;
     const int sel = f64 ? 0 : 1;
+    // pgmres.c:61,93: v = precondR(x or u_i) before the matvec (SGSe), into r64
+    int in0 = 0, in1 = 1, kr = 0;
+    if (P.rprec && (mode == 0 || mode == 1)) {
+        launch_elem_prec(P.sysdev.as<SysDev>(), P.nsys, 3, mode == 0 ? 0 : 1, step, st);
+        in0 = in1 = 3;
+        kr = 1;
+    }
     if (P.op == FG_OP_CSR) {
         if (f64) launch_csr_mv<double, double, double>(P, st, gate, sel, sel, step);
         else launch_csr_mv<T, TV, T>(P, st, gate, sel, sel, step);
@@ -1373,7 +1387,7 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
         const int *nc = P.ecount.as<int>() + c;
         bool done = false;
         if (f64) {
-            MvLaunch::go<double, double, double>(P.S, cnt, st, sys, ch, nc, gate, 0, 0, 0, nullptr, nullptr,
+            MvLaunch::go<double, double, double>(P.S, cnt, st, sys, ch, nc, gate, in0, 0, 0, nullptr, nullptr,
                                                  P.maxdof);
             done = true;
         }
@@ -1384,10 +1398,10 @@ static int enqueue_matvec(const Plan &P, int mode, int step, cudaStream_t st)
                 done = true;
             }
         }
-        if (!done) MvLaunch::go<T, TV, T>(P.S, cnt, st, sys, ch, nc, gate, 1, 1, step, nullptr, nullptr, P.maxdof);
+        if (!done) MvLaunch::go<T, TV, T>(P.S, cnt, st, sys, ch, nc, gate, in1, 1, step, nullptr, nullptr, P.maxdof);
         ++k;
     }
-    return k;
+    return k + kr;
 }
 
 // M^-1 applied after a matvec: sel 0 (t64 -> u64, FP64) or 1 (t -> w, T).
@@ -1402,6 +1416,10 @@ static int enqueue_precond(const Plan &P, int sel, cudaStream_t st)
         else
             launch_blockdiag<T>(P.B, grid_for(P.n_nch), st, sys, P.nchunks.as<NChunk>(), P.ncount.as<int>(), 1, 1,
                                 nullptr, nullptr);
+        return 1;
+    }
+    if (P.precond == FG_PRECOND_LUE || P.precond == FG_PRECOND_SGSE) {   // FP64 only
+        launch_elem_prec(sys, P.nsys, P.precond == FG_PRECOND_LUE ? 1 : 2, sel, 0, st);
         return 1;
     }
     if (P.precond == FG_PRECOND_ILU0 && P.n_ilw > 0) {
@@ -1540,6 +1558,11 @@ int validate_member(fg_system *s, const SolveConfig &cfg)
     if (s->op == FG_OP_CSR && !s->csr_ok) { set_error("CSR operator selected but not set up"); return FG_ERR_STATE; }
     if (cfg.precond == FG_PRECOND_ILU0 && s->op != FG_OP_CSR) {
         set_error("ILU(0) needs the CSR operator (fg_set_operator(FG_OP_CSR))"); return FG_ERR_STATE;
+    }
+    if ((cfg.precond == FG_PRECOND_LUE || cfg.precond == FG_PRECOND_SGSE) &&
+        (cfg.mixed || s->topo.S != 3 || s->op != FG_OP_EBE)) {
+        set_error("the element preconditioners LUe / SGSe run in FP64 on 3x3 EBE systems");
+        return FG_ERR_UNSUPPORTED;
     }
     if (cfg.precond == FG_PRECOND_SPIKE && (s->op != FG_OP_CSR || !s->sp_ready)) {
         set_error("SPIKE needs the CSR operator and its set-up (fg_precond_setup)"); return FG_ERR_STATE;
@@ -1794,6 +1817,7 @@ int BatchRun::finish(const std::vector<int> &idx, std::vector<SysState> &out)
     int r = build_plan(F, sub, cfg, shs, st);
     if (r) return r;
     const SysDev *sys = F.sysdev.as<SysDev>();
+    if (F.rprec) launch_elem_prec(sys, F.nsys, 3, 2, 0, st);   // pgmres.c:186: X = precondR(X)
     count_launches(enqueue_matvec<double>(F, 3, 0, st));
     k_final<<<grid_for(F.n_dch), kThreads, 0, st>>>(sys, F.dchunks.as<DChunk>(), F.dcount.as<int>());
     FG_CUDA(cudaGetLastError());

@@ -252,6 +252,8 @@ __global__ void k_blockdiag_apply64(const int *__restrict__ node_dof, const doub
     }
 }
 
+static int elem_prec_setup(fg_system *s, int kind, cudaStream_t st);
+
 int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaStream_t st)
 {
     const Topology &t = s->topo;
@@ -268,6 +270,13 @@ int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaS
         FG_CUDA(cudaGetLastError());
     count_launches(1);
         s->precond = kind;
+        return FG_OK;
+    }
+    if (kind == FG_PRECOND_LUE || kind == FG_PRECOND_SGSE) {
+        int r;
+        if ((r = elem_prec_setup(s, kind, st))) return r;
+        s->precond = kind;
+        if (F_dev && (r = elem_prec_apply_device(s, false, F_dev, F_dev, st))) return r;
         return FG_OK;
     }
     if (kind == FG_PRECOND_BLOCKDIAG) {
@@ -304,6 +313,189 @@ int precond_setup_device(fg_system *s, int kind, int flags, double *F_dev, cudaS
     }
     set_error("unknown preconditioner kind");
     return FG_ERR_ARG;
+}
+
+// ---------------------------------------------------------------- element preconditioners
+// Preconditioner "LUe" (EBE/LU_precond_EBE_setup.c:20-31, LU_precond_EBE.c:
+// 28-60) and "SGSe" (EBE/SGS_precond_EBE.c: SGS_precond_EBE forward,
+// SGS_precondR_EBE backward).  Each sweeps the elements in order, in place,
+// every element reading the values the earlier ones wrote: a dependency
+// chain through the whole mesh, so one thread of one warp per system runs
+// it, in the reference's element order, while the other lanes stage the
+// next 32 element records (internal dofs, 9 coefficients) into shared
+// memory.  Expressions keep the reference's association (`a += -b*c -
+// d*e` adds ((-(b*c)) - d*e)); compiled without FMA contraction, so the
+// sweeps are bit-identical with the reference's.
+
+// per element, in reference element order: the LU factors of its block
+// (kind 1) or its entries (kind 2); thread per internal position
+__global__ void k_ep_coef(int kind, int nel, int ld, const int *__restrict__ eorder, const double *__restrict__ A64,
+                          double *__restrict__ coef)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= nel) return;
+    double a[9];
+    for (int m = 0; m < 9; ++m) a[m] = A64[(size_t)m * ld + p];
+    double *L = coef + 9 * (size_t)eorder[p];
+    if (kind == 1) {
+        L[0] = 1.0;
+        L[1] = a[1];
+        L[2] = a[2];
+        L[3] = a[3];
+        L[4] = 1. / (1.0 - a[1] * a[3]);
+        L[5] = a[5] - a[2] * a[3];
+        L[6] = a[6];
+        L[7] = (a[7] - a[1] * a[6]) * L[4];
+        L[8] = 1. / (1.0 - a[2] * a[6] - L[7] * L[5]);
+    } else {
+        for (int m = 0; m < 9; ++m) L[m] = a[m];
+    }
+}
+
+// out = in (n + 1 entries, the whole CTA), then the sweep on out by warp 0:
+// kind 1 LU, 2 SGS forward (elements ascending), 3 SGS backward (elements
+// descending).  Must be the CTA's last step (warp 0 alone goes on).
+__device__ void elem_sweep(int kind, int nel, int n, const int *__restrict__ lmi, const double *__restrict__ coef,
+                           const double *in, double *out)
+{
+    __shared__ int s_l[2][32][3];
+    __shared__ double s_c[2][32][9];
+    if (in != out)
+        for (int i = threadIdx.x; i <= n; i += blockDim.x) out[i] = in[i];
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x, nch = (nel + 31) / 32;
+    int rl[3] = {n, n, n};
+    double rc[9];
+    for (int m = 0; m < 9; ++m) rc[m] = 0.0;
+    auto load = [&](int c) {                          // element record of this lane in chunk c
+        const int t = c * 32 + lane;
+        if (c < nch && t < nel) {
+            const int I = kind == 3 ? nel - 1 - t : t;
+            for (int a = 0; a < 3; ++a) rl[a] = lmi[3 * (size_t)I + a];
+            for (int m = 0; m < 9; ++m) rc[m] = coef[9 * (size_t)I + m];
+        }
+    };
+    auto store = [&](int b) {
+        for (int a = 0; a < 3; ++a) s_l[b][lane][a] = rl[a];
+        for (int m = 0; m < 9; ++m) s_c[b][lane][m] = rc[m];
+    };
+    load(0);
+    store(0);
+    if (lane == 0) out[n] = 0.0;
+    __syncwarp();
+    for (int c = 0; c < nch; ++c) {
+        load(c + 1);                                  // in flight while lane 0 works
+        if (lane == 0) {
+            const int cnt = min(32, nel - c * 32), b = c & 1;
+            for (int e = 0; e < cnt; ++e) {
+                const int l0 = s_l[b][e][0], l1 = s_l[b][e][1], l2 = s_l[b][e][2];
+                const double *L = s_c[b][e];
+                double z0 = out[l0], z1 = out[l1], z2 = out[l2];
+                if (kind == 1) {
+                    z1 += -L[3] * z0;
+                    z2 += -L[6] * z0 - L[7] * z1;
+                    z2 *= L[8];
+                    z1 = (z1 - L[5] * z2) * L[4];
+                    z0 += -L[1] * z1 - L[2] * z2;
+                    out[l0] = z0;
+                    out[l1] = z1;
+                    out[l2] = z2;
+                } else if (kind == 2) {
+                    z1 += -L[3] * z0;
+                    z2 += -L[6] * z0 - L[7] * z1;
+                    out[l1] = z1;
+                    out[l2] = z2;
+                } else {
+                    z1 += -L[5] * z2;
+                    z0 += -L[1] * z1 - L[2] * z2;
+                    out[l0] = z0;
+                    out[l1] = z1;
+                }
+                out[n] = 0.0;
+            }
+        }
+        __syncwarp();
+        store((c + 1) & 1);
+        __syncwarp();
+    }
+}
+
+// one system: in -> out (device vectors, internal numbering)
+__global__ void k_elem_prec1(int kind, int nel, int n, const int *lmi, const double *coef, const double *in,
+                             double *out)
+{
+    elem_sweep(kind, nel, n, lmi, coef, in, out);
+}
+
+// a batch, a CTA per system (see launch_elem_prec)
+__global__ void k_elem_prec(const SysDev *__restrict__ sys, int kind, int sel, int step)
+{
+    const SysDev &D = sys[blockIdx.x];
+    if (sel == 0 ? !D.st->live : sel == 1 ? !D.st->in_cycle : false) return;
+    const double *in;
+    double *out;
+    if (kind == 3) {
+        in = sel == 0 || sel == 2 ? D.x : (const double *)D.V + (size_t)step * D.n_pad;
+        out = sel == 2 ? D.x : D.r64;
+    } else {
+        in = sel == 0 ? D.t64 : (const double *)D.t;
+        out = sel == 0 ? D.u64 : (double *)D.w;
+    }
+    elem_sweep(kind, D.nel, D.n, D.ep_lmi, D.ep_coef, in, out);
+}
+
+int launch_elem_prec(const SysDev *sys, int nsys, int kind, int sel, int step, cudaStream_t st)
+{
+    if (nsys > 0) k_elem_prec<<<nsys, 128, 0, st>>>(sys, kind, sel, step);
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    return FG_OK;
+}
+
+// the per-element records of a system (host connectivity, device blocks)
+static int elem_prec_setup(fg_system *s, int kind, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (t.S != 3 || s->op != FG_OP_EBE) {
+        set_error("the element preconditioners LUe / SGSe need 3x3 blocks on the EBE operator");
+        return FG_ERR_UNSUPPORTED;
+    }
+    int r;
+    if (!s->ep_lmi.p) {
+        std::vector<int> lmi(3 * (size_t)std::max(t.nel, 1), t.n);
+        for (int I = 0; I < t.nel; ++I)
+            for (int a = 0; a < 3; ++a) {
+                const int q = t.lm[3 * (size_t)I + a];
+                lmi[3 * (size_t)I + a] = q == t.n ? t.n : t.iperm[q];
+            }
+        if ((r = s->ep_lmi.alloc(sizeof(int) * lmi.size()))) return r;
+        FG_CUDA(cudaMemcpy(s->ep_lmi.p, lmi.data(), sizeof(int) * lmi.size(), cudaMemcpyHostToDevice));
+    }
+    if (!s->ep_coef.p && (r = s->ep_coef.alloc(sizeof(double) * 9 * (size_t)std::max(t.nel, 1)))) return r;
+    if (t.nel > 0)
+        k_ep_coef<<<(t.nel + 127) / 128, 128, 0, st>>>(kind == FG_PRECOND_LUE ? 1 : 2, t.nel, s->nel_pad,
+                                                       s->eorder.as<int>(), s->A64.as<double>(),
+                                                       s->ep_coef.as<double>());
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    return FG_OK;
+}
+
+// z = M^-1 p (left) or z = R p (right, SGSe only; the identity otherwise)
+int elem_prec_apply_device(fg_system *s, bool right, const double *p, double *z, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    const bool sgs = s->precond == FG_PRECOND_SGSE;
+    if (right && !sgs) {
+        if (p != z) FG_CUDA(cudaMemcpyAsync(z, p, 8 * (size_t)(t.n + 1), cudaMemcpyDeviceToDevice, st));
+        return FG_OK;
+    }
+    const int kind = right ? 3 : sgs ? 2 : 1;
+    k_elem_prec1<<<1, 128, 0, st>>>(kind, t.nel, t.n, s->ep_lmi.as<int>(), s->ep_coef.as<double>(), p, z);
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    return FG_OK;
 }
 
 // ---------------------------------------------------------------- diagonal scaling
@@ -435,6 +627,7 @@ int precond_apply_device(fg_system *s, const double *p, double *z, cudaStream_t 
     const Topology &t = s->topo;
     if (s->precond == FG_PRECOND_ILU0) return ilu0_apply_device(s, p, z, st);
     if (s->precond == FG_PRECOND_SPIKE) return spike_apply_device(s, p, z, st);
+    if (s->precond == FG_PRECOND_LUE || s->precond == FG_PRECOND_SGSE) return elem_prec_apply_device(s, false, p, z, st);
     if (s->precond == FG_PRECOND_DIAG) {
         k_diag_apply<<<(t.n + 256) / 256, 256, 0, st>>>(s->invd64.as<double>(), t.n, p, z);
     } else if (s->precond == FG_PRECOND_BLOCKDIAG) {

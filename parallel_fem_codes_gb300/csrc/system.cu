@@ -108,7 +108,7 @@ size_t fg_system::bytes() const
                            &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
                            &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &state_u1, &state_u2, &shock_state, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
-                           &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state};
+                           &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state, &ep_lmi, &ep_coef};
     size_t b = 0;
     for (auto *m : all) b += m->bytes;
     return b;
@@ -402,6 +402,20 @@ int fg_precond_apply(fg_system *s, const double *p, double *z)
     if (r) return r;
     if ((r = vec_in(s, p, s->ws.u64.as<double>(), s->ws.r64.as<double>()))) return r;
     if ((r = precond_apply_device(s, s->ws.u64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
+    if ((r = vec_out(s, s->ws.u64.as<double>(), z, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_precond_apply_right(fg_system *s, const double *p, double *z)
+{
+    if (!s || !p || !z) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = vec_in(s, p, s->ws.u64.as<double>(), s->ws.r64.as<double>()))) return r;
+    if ((r = elem_prec_apply_device(s, true, s->ws.u64.as<double>(), s->ws.u64.as<double>(), s->stream))) return r;
     if ((r = vec_out(s, s->ws.u64.as<double>(), z, s->ws.r64.as<double>()))) return r;
     FG_CUDA(cudaStreamSynchronize(s->stream));
     FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));

@@ -70,6 +70,7 @@ struct fg_system {
     int ilu_p = 0, lu_nnz = 0;
     int ilu_blocks = 1;                // block-Jacobi ILU over this many row blocks (1: global)
     int ilu_maxrow = 1;                // longest row of the factor pattern
+    fg::DevMem ep_lmi, ep_coef;        // element preconditioners: dofs and coefficients per element
     int scale_kind = 0;                // last fg_scale kind (fg_unscale follows it)
     fg::DevMem lu_ia, lu_ja, lu_dg, lu_map, AAf64;
     fg::DevMem csr_ia, csr_ja, csr_diag, csr_inc_ptr, csr_inc, AA64, AA32, LU64, LU32, dinv64, dinv32, ilu_flags,
@@ -103,7 +104,13 @@ int launch_ilu_pending(const SysDev *sys, const DChunk *ch, const int *nch, int 
                        cudaStream_t st);
 int launch_ilu_solve(const SysDev *sys, const int2 *items, int nitems, int *counter, int *err, int sel, int backward,
                      int fp32, int lanes, cudaStream_t st);
-int ilu_ws_rows(const fg_system *s);   // rows of the largest block-Jacobi block (warp-per-block path), or 0
+int ilu_ws_rows(const fg_system *s);
+// element preconditioner sweeps over a batch (setup.cu): kind 1 LU, 2 SGS
+// forward (left), 3 SGS backward (right); sel 0: t64 -> u64 (left) or
+// x -> r64 (right), gate live; 1: t -> w (left) or V[step] -> r64 (right),
+// gate in cycle; 2 (right): x in place, every member
+int launch_elem_prec(const SysDev *sys, int nsys, int kind, int sel, int step, cudaStream_t st);
+int elem_prec_apply_device(fg_system *s, bool right, const double *p, double *z, cudaStream_t st);   // rows of the largest block-Jacobi block (warp-per-block path), or 0
 int launch_ilu_ws(const SysDev *sys, const int2 *items, int nitems, int sel, int backward, int fp32, int lanes,
                   int rows, int ecap, cudaStream_t st);
 
@@ -141,6 +148,8 @@ inline void set_patch_fields(SysDev &D, const fg_system *s)
     D.ilu_fpass = s->ilu_fpass.as<int2>();
     D.ilu_bpass = s->ilu_bpass.as<int2>();
     D.ilu_P = std::max(1, std::min(s->ilu_blocks, s->topo.n));
+    D.ep_lmi = s->ep_lmi.as<int>();
+    D.ep_coef = s->ep_coef.as<double>();
     set_spike_fields(D, s);
     D.lm16 = s->lm16.as<unsigned short>();
     D.pt_elem = s->pt_elem.as<int>();

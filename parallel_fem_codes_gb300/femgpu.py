@@ -16,6 +16,7 @@ from . import build as _build
 
 FG_OK = 0
 FG_PRECOND_NONE, FG_PRECOND_DIAG, FG_PRECOND_BLOCKDIAG, FG_PRECOND_ILU0, FG_PRECOND_SPIKE = 0, 1, 2, 3, 4
+FG_PRECOND_LUE, FG_PRECOND_SGSE = 5, 6   # element LU sweep ("LUe"); element SGS ("SGSe", right sweep too)
 FG_SCALE_LEFT, FG_SCALE_LEFTRIGHT, FG_SCALE_BLOCK = 1, 2, 3
 FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
@@ -156,6 +157,7 @@ def lib(build_if_missing: bool = True):
     L.fg_matvec.argtypes = [_vp, _f64p, _f64p, _c_int]
     L.fg_precond_setup.argtypes = [_vp, _c_int, _c_int, _vp]
     L.fg_precond_apply.argtypes = [_vp, _f64p, _f64p]
+    L.fg_precond_apply_right.argtypes = [_vp, _f64p, _f64p]
     L.fg_get_diag.argtypes = [_vp, _f64p]
     L.fg_set_diag.argtypes = [_vp, _f64p]
     L.fg_solve.argtypes = [_vp, ctypes.POINTER(SolverOpts), _f64p, _f64p, _vp, ctypes.POINTER(SolveStats)]
@@ -434,6 +436,14 @@ class System:
         p = np.ascontiguousarray(p, dtype=np.float64)
         z = np.empty(self.n + 1)
         check(lib().fg_precond_apply(self._h, p, z))
+        return z
+
+    def precond_apply_right(self, p):
+        """The right preconditioner of the set-up (SGSe's backward sweep; the
+        identity for the other kinds)."""
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        z = np.empty(self.n + 1)
+        check(lib().fg_precond_apply_right(self._h, p, z))
         return z
 
     def diag(self):

@@ -20,7 +20,9 @@ import pytest
 import oracle as O
 
 LIBS = {"sst": ("libfemgpu_sst.so", ["pgmres", "ebemv", "csrmv", "Diag_precond", "Diag_precond_EBE_setup",
-                                     "ILUp_precond_setup", "SPIKE_precond_setup", "csr_assembly"]),
+                                     "ILUp_precond_setup", "SPIKE_precond_setup", "csr_assembly", "LU_precond_EBE",
+                                     "LU_precond_EBE_setup", "SGS_precond_EBE", "SGS_precondR_EBE",
+                                     "SGS_precond_EBE_setup"]),
         "ns": ("libfemgpu_ns.so", ["pgmres", "ebemvNDOF3", "BlockDiagDOF3_precond",
                                    "BlockDiagDOF3_precond_EBE_setup", "csrmv", "ILUp_precond_setup"]),
         "euler": ("libfemgpu_euler.so", ["pgmres", "ebemvNDOF4", "BlockDiag_precond", "BlockDiag_precond_EBE_setup",
