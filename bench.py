@@ -14,8 +14,10 @@ the same GPU.
 Output: one JSON line (rank 0).  `value` is served solves/s with every
 request submitted at t = 0, latency p50/p99 = done - submit;
 `served_poisson` repeats the pass with Poisson arrivals at 80% of that rate;
-`e2e` is the same metric through the host-buffer C ABI (element blocks and
-right-hand sides copied in, solutions copied out, every step).
+`e2e` is the same metric through the host-buffer C ABI: every step serves
+each request from host buffers (fg_server_submit_host: element blocks and
+right-hand side copied in, the solution copied out before the request is
+polled); `e2e.synchronous_batch` is the same through the synchronous calls.
 `--impl reference` times the reference's CPU implementation of the path (the
 oracle port where the reference's own build is absent) on the host cores,
 on a bounded sample of the same workload.
@@ -847,31 +849,53 @@ def main():
             out[...] = a
             return out
 
-        As, Fs = [], []
+        As, Fs, Xs = [], [], []
         for s, p in zip(systems, probs):
             Fs.append(pinned(s.transport_assemble(p)))
             As.append(pinned(s.get_blocks()))
-        h2d = sum(a.nbytes for a in As) + 2 * sum(f.nbytes for f in Fs)
-        d2h = 2 * sum(f.nbytes for f in Fs)
+            Xs.append(pinned(np.zeros(s.n + 1)))
+        h2d = sum(a.nbytes for a in As) + sum(f.nbytes for f in Fs)
+        d2h = sum(x.nbytes for x in Xs)
 
         def e2e_step():
+            """One served pass of host-buffer requests (fg_server_submit_host):
+            each request copies its blocks and F in, is admitted into the
+            running batch, and its X is copied out before it is polled."""
+            sv = fg.Server(kmax=KMAX, lmax=10000, tol=TOL, precision=served_precision(fg))
+            for i, (s, A, F, X) in enumerate(zip(systems, As, Fs, Xs)):
+                sv.submit_host(s, A, F, X, i)
+            sv.wait(len(systems), timeout=600)
+            out = sv.poll(len(systems) + 16)
+            sv.close()
+            return out
+
+        def e2e_sync_step():
             Bs = []
             for s, A, F in zip(systems, As, Fs):
                 s.set_blocks(A)
                 Bs.append(s.precond_setup(fg.FG_PRECOND_DIAG, 0, F))
             return fg.solve_batch(systems, Bs, Fs, kmax=KMAX, lmax=10000, tol=TOL, precision=served_precision(fg))
 
-        e2e_step()
-        et = []
-        for _ in range(max(1, args.steps)):
-            e0.record(stream)
-            xs, st2 = e2e_step()
-            e1.record(stream)
-            e1.synchronize()
-            et.append(e0.elapsed_time(e1) / 1e3)
-        e2e_s = reduce_max(dist, sum(et) / len(et))
+        def timed(fn):
+            fn()
+            et = []
+            for _ in range(max(1, args.steps)):
+                torch.cuda.synchronize()
+                e0.record(stream)
+                out = fn()
+                e1.record(stream)
+                e1.synchronize()
+                et.append(e0.elapsed_time(e1) / 1e3)
+            return reduce_max(dist, sum(et) / len(et)), out
+
+        e2e_s, res_h = timed(e2e_step)
+        sync_s, _ = timed(e2e_sync_step)
         e2e = {"value": ws * args.count / e2e_s, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+               "d2h_bytes_per_step": int(d2h), "path": "fg_server_submit_host",
+               "converged_all": all(r["converged"] == 1 for r in res_h),
+               "worst_true_rel_residual": max(r["true_rel_residual"] for r in res_h),
+               "synchronous_batch": {"value": ws * args.count / sync_s, "unit": "solves/s",
+                                     "path": "fg_set_blocks + fg_precond_setup + fg_solve_batch"}}
 
     legs = None
     if not args.no_legs and rank == 0:

@@ -553,6 +553,15 @@ int fg_server_create(fg_server **out, const fg_server_opts *opts);
 /* Queue a request; thread-safe.  The system must not be in use elsewhere
  * until its result has been polled. */
 int fg_server_submit(fg_server *sv, fg_system *s, const fg_transport_coeffs *c, unsigned long long tag);
+/* Queue a request with host buffers (the C ABI of fg_set_blocks +
+ * fg_precond_setup(FG_PRECOND_DIAG, 0, F) + fg_solve, served): A the
+ * element blocks (row-major S x S per element, reference element order),
+ * F the right-hand side (NEQ + 1); X (NEQ + 1) receives the solution
+ * before the result can be polled.  The buffers stay the caller's but must
+ * not be touched until then; pinned (page-locked) buffers copy fastest.
+ * 3x3 systems. */
+int fg_server_submit_host(fg_server *sv, fg_system *s, const double *A, const double *F, double *X,
+                          unsigned long long tag);
 /* Queue an Euler time loop (fg_euler_predictor with the server's kmax,
  * lmax, tol, precision and inner_tol); thread-safe.  u (host, n) is the
  * initial state and receives the final state; it and the system stay the

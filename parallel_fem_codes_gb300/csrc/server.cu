@@ -40,6 +40,8 @@ struct Request {
     unsigned long long tag;
     double t_submit, t_admit;
     size_t bytes;
+    const double *hA = nullptr, *hF = nullptr;   // host-buffer request: blocks and right-hand side
+    double *hX = nullptr;                         // and its solution
 };
 
 struct EulerRequest {
@@ -146,7 +148,7 @@ void fg_server::run()
         }
         if (!admit.empty()) {
             for (auto &r : admit) {
-                int rc = fg_transport_prepare(r.s, &r.c, nullptr);
+                int rc = r.hA ? prepare_host_request(r.s, r.hA, r.hF) : fg_transport_prepare(r.s, &r.c, nullptr);
                 if (rc == FG_OK && cudaStreamSynchronize(r.s->stream) != cudaSuccess) rc = cuda_fail(cudaGetLastError(), "prepare");
                 if (rc == FG_OK) rc = batch.stage({r.s, r.s->rhs_b.as<double>(), r.s->rhs_f.as<double>(), nullptr});
                 if (rc != FG_OK) { fail(rc); return; }
@@ -165,6 +167,8 @@ void fg_server::run()
         if (fin.empty()) continue;
         std::vector<SysState> sts;
         if ((rc = batch.finish(fin, sts)) != FG_OK) { fail(rc); return; }
+        for (int i : fin)                                // host-buffer requests: X before the result
+            if (active[i].hX && (rc = download_solution(active[i].s, active[i].hX, st)) != FG_OK) { fail(rc); return; }
         double t = now();
         {
             std::lock_guard<std::mutex> l(mu);
@@ -361,6 +365,26 @@ int fg_server_create(fg_server **out, const fg_server_opts *opts)
     sv->worker_eub = std::thread([sv] { sv->run_euler_batch(); });
     for (int i = 0; i < kEulerWorkers; ++i) sv->workers_eu.emplace_back([sv] { sv->run_euler(); });
     *out = sv;
+    return FG_OK;
+}
+
+int fg_server_submit_host(fg_server *sv, fg_system *s, const double *A, const double *F, double *X,
+                          unsigned long long tag)
+{
+    if (!sv || !s || !A || !F || !X) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (s->topo.S != 3) { set_error("fg_server_submit_host: 3x3 element blocks (ndof == 1)"); return FG_ERR_UNSUPPORTED; }
+    if (s->device != sv->device) { set_error("fg_server_submit_host: system on another device"); return FG_ERR_ARG; }
+    Request r{s, fg_transport_coeffs{}, tag, sv->now(), 0.0, request_bytes(s, sv->cfg.kmax, sv->cfg.mixed, false)};
+    r.hA = A;
+    r.hF = F;
+    r.hX = X;
+    {
+        std::lock_guard<std::mutex> l(sv->mu);
+        if (sv->error) { set_error(sv->error_text); return sv->error; }
+        if (sv->stop) { set_error("server is stopping"); return FG_ERR_STATE; }
+        sv->queue.push_back(r);
+    }
+    sv->cv_work.notify_one();
     return FG_OK;
 }
 

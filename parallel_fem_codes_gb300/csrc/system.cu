@@ -877,6 +877,38 @@ int fg_euler_assemble(fg_system *s, const fg_euler_coeffs *c, const double *u, c
 
 namespace fg {
 
+// A served request with host buffers: element blocks A (reference element
+// order) and right-hand side F (NEQ + 1, reference numbering) uploaded,
+// Diag set up afresh and applied: the resident right-hand sides of the
+// batch engine (rhs_b = M^-1 F, rhs_f = F for the true residual), as
+// fg_set_blocks + fg_precond_setup(FG_PRECOND_DIAG, 0, F) leave them.
+int prepare_host_request(fg_system *s, const double *A, const double *F)
+{
+    int r = fg_set_blocks(s, A);
+    if (r) return r;
+    if ((r = ensure_io(s))) return r;
+    if ((r = stage(s, s->rhs_f, 8 * (size_t)s->n_pad)) || (r = stage(s, s->rhs_b, 8 * (size_t)s->n_pad))) return r;
+    FG_CUDA(cudaMemsetAsync(s->rhs_f.p, 0, 8 * (size_t)s->n_pad, s->stream));
+    if ((r = vec_in(s, F, s->rhs_f.as<double>(), s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaMemcpyAsync(s->rhs_b.p, s->rhs_f.p, 8 * (size_t)s->n_pad, cudaMemcpyDeviceToDevice, s->stream));
+    if ((r = precond_setup_device(s, FG_PRECOND_DIAG, 0, s->rhs_b.as<double>(), s->stream))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    s->rhs_ok = true;
+    return FG_OK;
+}
+
+// the batch engine's solution of a system (internal numbering) to a host
+// vector (reference numbering, NEQ + 1), on stream st
+int download_solution(fg_system *s, double *X, cudaStream_t st)
+{
+    int r;
+    if ((r = permute_out(s, s->ws.x.as<double>(), s->ws.r64.as<double>(), st))) return r;
+    FG_CUDA(cudaMemcpyAsync(X, s->ws.r64.p, 8 * (size_t)(s->topo.n + 1), cudaMemcpyDeviceToHost, st));
+    FG_CUDA(cudaStreamSynchronize(st));
+    return FG_OK;
+}
+
+
 // The time loops of 00_CommonFiles/Time_Integration with the state (u, a,
 // u_old, and u^{n-1}, u^n for BDF2), the residual and the increment kept on
 // the device; per correction one assembly (`assemble(alpha_b, dt_b, u, a,

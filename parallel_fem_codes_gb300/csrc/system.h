@@ -268,6 +268,8 @@ int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c,
 // Gathers / scatters between reference and internal numbering (n+1 vectors)
 int permute_in(fg_system *s, const double *ref_dev, double *int_dev, cudaStream_t st);
 int permute_out(fg_system *s, const double *int_dev, double *ref_dev, cudaStream_t st);
+int prepare_host_request(fg_system *s, const double *A, const double *F);   // server: host blocks and F
+int download_solution(fg_system *s, double *X, cudaStream_t st);             // engine x -> host X
 
 int sm_count();
 

@@ -203,6 +203,7 @@ def lib(build_if_missing: bool = True):
                                   ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
     L.fg_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerOpts)]
     L.fg_server_submit.argtypes = [_vp, _vp, ctypes.POINTER(TransportCoeffs), ctypes.c_ulonglong]
+    L.fg_server_submit_host.argtypes = [_vp, _vp, _f64p, _f64p, _f64p, ctypes.c_ulonglong]
     L.fg_server_submit_euler.argtypes = [_vp, _vp, ctypes.POINTER(EulerCoeffs), ctypes.POINTER(TimeOpts), _f64p,
                                          ctypes.c_ulonglong]
     L.fg_server_poll.argtypes = [_vp, _vp, _c_int, ctypes.POINTER(_c_int)]
@@ -724,6 +725,17 @@ class Server:
         c = _coeffs(prob)
         self._keep[tag] = system
         check(lib().fg_server_submit(self._h, system.handle, ctypes.byref(c), tag))
+
+    def submit_host(self, system, A, F, X, tag):
+        """A request with host buffers: blocks A (nel x S*S), right-hand side
+        F (n+1); X (n+1, float64, C-contiguous) receives the solution before
+        the result is polled.  The arrays are kept alive until then."""
+        if not (isinstance(X, np.ndarray) and X.dtype == np.float64 and X.flags.c_contiguous):
+            raise ValueError("X must be a C-contiguous float64 array")
+        A = np.ascontiguousarray(A, dtype=np.float64)
+        F = np.ascontiguousarray(F, dtype=np.float64)
+        self._keep[tag] = (system, A, F, X)
+        check(lib().fg_server_submit_host(self._h, system.handle, A.reshape(-1), F, X, tag))
 
     def submit_euler(self, system, prob, topts, tag, u0=None):
         c = euler_coeffs(prob)

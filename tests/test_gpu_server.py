@@ -163,3 +163,36 @@ def test_served_euler_loops_share_cycles(fg):
     overlaps = sum(res[i]["t_admit"] < res[j]["t_done"] and res[j]["t_admit"] < res[i]["t_done"]
                    for i in res for j in res if i < j)
     assert overlaps >= 3
+
+
+def test_host_buffer_requests_equal_solo(fg):
+    """fg_server_submit_host: blocks and right-hand side from host buffers
+    (the C ABI of fg_set_blocks + fg_precond_setup(Diag) + fg_solve, served);
+    the solution lands in the caller's host array before the result is
+    polled and equals the device-assembled solve run alone, bit for bit."""
+    probs = [G.transport_problem(n, angle_deg=a, k=k) for n, a, k in
+             [(33, 30.0, 1e-6), (17, 200.0, 1e-3), (65, 95.0, 1e-8), (25, 315.0, 1e-5)]]
+    solo, bufs = [], []
+    for p in probs:
+        s = fg.transport_system(p)
+        F = s.transport_assemble(p)
+        A = s.get_blocks()
+        s.transport_prepare(p)
+        st = fg.solve_resident([s], precision=fg.FG_PREC_MIXED)[0]
+        solo.append((s.solution(), st))
+        bufs.append((A, F))
+    systems = [fg.transport_system(p) for p in probs]
+    Xs = [np.full(p.mesh.neq + 1, np.nan) for p in probs]
+    sv = fg.Server(precision=fg.FG_PREC_MIXED)
+    for i, (s, (A, F)) in enumerate(zip(systems, bufs)):
+        sv.submit_host(s, A, F, Xs[i], i)
+    sv.wait(len(probs), timeout=120)
+    res = {r["tag"]: r for r in sv.poll()}
+    sv.close()
+    assert sorted(res) == list(range(len(probs)))
+    for i in range(len(probs)):
+        X0, st0 = solo[i]
+        assert res[i]["converged"] == 1 and res[i]["status"] == 0
+        assert res[i]["iterations"] == st0["iterations"]
+        assert res[i]["true_rel_residual"] <= 1e-10
+        assert np.array_equal(Xs[i][:-1], X0[:-1])
