@@ -230,6 +230,12 @@ typedef int (*or_correction_fn)(void *ctx, double alpha_b, double dt_b, const do
  * the steps (a TR-BDF2 step is its TR and BDF2 stages), -1 on failure. */
 int or_time_integrate(int neq, double alpha, double dt, const or_time_opts *to, or_correction_fn correct,
                       void *ctx, double *u, double *a, or_time_stats *st);
+/* The same with a hook called once per OR_TIME_PREDICTOR step after the
+ * prediction of u and a (coef = (1 - alpha) dt): Predictor_New.c:78-83
+ * predicts its per-element bubble unknowns there. */
+typedef void (*or_predict_fn)(void *ctx, double coef);
+int or_time_integrate_ex(int neq, double alpha, double dt, const or_time_opts *to, or_correction_fn correct,
+                         or_predict_fn predict, void *ctx, double *u, double *a, or_time_stats *st);
 
 /* Predictor_Old.c:6-134 with EBE 12x12 blocks, BlockDiag (4x4, the
  * reference's inverse) and GMRES.  u: initial state on entry (the
@@ -252,6 +258,26 @@ int or_tt_predictor(int nnodes, int nel, const double *x, const double *y, const
                     const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
                     const or_time_opts *to, double solver_tol, int kmax, int lmax, double *u, double *a,
                     or_time_stats *st);
+
+/* Build_M_F_DD (TimeIntegration "Predictor2" with StabilizationForm "DD"):
+ * the bubble unknown of each element kept (uB, duB: nel values) and
+ * condensed out; A receives Me (9 per element), F the load (NEQ + 1, F[NEQ]
+ * = 0), cond (invN2, R2, M2[0..2]) 5 per element.  prob->delta_old (nel)
+ * holds the relaxed shock-capture state (NULL: fresh zeros). */
+void or_build_tt_mfdd(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                      const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
+                      const double *u, const double *du, const double *uB, const double *duB, double *A,
+                      double *F, double *cond);
+/* calculate_DaB: Da[NEQ] = 0, DaB[e] = invN2 (R2 - M2 . Da[lm[e]]) */
+void or_tt_dab(int nel, const int *lm, int NEQ, const double *cond, double *Da, double *DaB);
+/* Predictor_New with Build_M_F_DD, calculate_DaB, accumulating Diag and
+ * GMRES (the time-step stop tests of to; to->scheme is ignored).  u:
+ * initial state in, final out; a (neq), uB, aB (nel) receive the final
+ * du/dt and bubble unknowns. */
+int or_tt_predictor2(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                     const int *ien, int neq, const or_transport_problem *prob, double alpha, double dt,
+                     const or_time_opts *to, double solver_tol, int kmax, int lmax, double *u, double *a,
+                     double *uB, double *aB, or_time_stats *st);
 
 /* h_shock_2sqrtArea (opt 0), h_shock_Option1 (1), h_shock_Option2 (2) of the
  * transport drivers (oracle/sst.c). */

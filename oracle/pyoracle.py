@@ -132,6 +132,14 @@ def lib():
         L.or_tt_predictor.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
                                       ctypes.c_void_p, _c_dbl, _c_dbl, ctypes.c_void_p, _c_dbl, _c_int, _c_int,
                                       _f64p, _f64p, ctypes.c_void_p]
+        L.or_build_tt_mfdd.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, ctypes.c_void_p,
+                                       _c_dbl, _c_dbl, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p]
+        L.or_build_tt_mfdd.restype = None
+        L.or_tt_dab.argtypes = [_c_int, _i32p, _c_int, _f64p, _f64p, _f64p]
+        L.or_tt_dab.restype = None
+        L.or_tt_predictor2.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                       ctypes.c_void_p, _c_dbl, _c_dbl, ctypes.c_void_p, _c_dbl, _c_int, _c_int,
+                                       _f64p, _f64p, _f64p, _f64p, ctypes.c_void_p]
         _lib = L
     return _lib
 
@@ -518,6 +526,12 @@ def ref_tt():
         R.fr_tt_build.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _c_dbl, _c_dbl,
                                   _c_dbl, _c_dbl, _c_dbl, _c_int, _c_dbl, _c_dbl, _c_dbl, _f64p, _f64p, _c_int,
                                   _f64p, _f64p]
+        R.fr_tt_mfdd_build.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _c_dbl, _c_dbl,
+                                       _c_dbl, _c_dbl, _c_dbl, _c_int, _c_dbl, _c_dbl, _c_dbl, _f64p, _f64p,
+                                       _f64p, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p]
+        R.fr_tt_predictor2.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _c_dbl, _c_dbl,
+                                       _c_dbl, _c_dbl, _c_dbl, _c_int, _c_dbl, _c_dbl, _c_dbl, _i32p, _i32p,
+                                       _f64p, _f64p, _c_int, _c_int, _c_dbl, _f64p]
         _ref_tt = R
     return _ref_tt
 
@@ -536,6 +550,43 @@ def ref_tt_build(prob, alpha, dt, u=None, du=None, builds=1):
     R.fr_tt_build(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f, prob.upmode, prob.upval,
                   float(alpha), float(dt), u, du, int(builds), A, F)
     return A.reshape(m.nel, 9), F
+
+
+def _ref_tt_form(R, prob):
+    cau = int(prob.cau)
+    R.fr_tt_set_form(1, cau if cau in (2, 3) else 2, int(getattr(prob, "h_shock", 0)))
+
+
+def ref_tt_mfdd_build(prob, alpha, dt, u, du, uB, duB, Da):
+    """The reference's Build_M_F_DD (fresh delta_old) at (u, du, uB, duB),
+    then its calculate_DaB on Da; returns (A[nel, 9], F[neq+1], cond[nel,
+    5], DaB[nel])."""
+    m = prob.mesh
+    R = ref_tt()
+    _ref_tt_form(R, prob)
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    A = np.empty(m.nel * 9)
+    F = np.zeros(m.neq + 1)
+    cond = np.empty(m.nel * 5)
+    DaB = np.empty(m.nel)
+    R.fr_tt_mfdd_build(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f, prob.upmode,
+                       prob.upval, float(alpha), float(dt), f(u), f(du), f(uB), f(duB), f(Da), A, F, cond, DaB)
+    return A.reshape(m.nel, 9), F, cond.reshape(m.nel, 5), DaB
+
+
+def ref_tt_predictor2(prob, alpha, dt, topts: TimeOpts, tol=1e-10, kmax=30, lmax=1000, u0=None):
+    """The reference's Predictor_New with Build_M_F_DD, Diag and pgmres;
+    returns (u[neq], GMRES iterations)."""
+    m = prob.mesh
+    R = ref_tt()
+    _ref_tt_form(R, prob)
+    perm, inv, _ = permutation_of_lm(m)
+    init = np.zeros(m.neq + 1) if u0 is None else np.append(np.asarray(u0, dtype=np.float64), 0.0)
+    u = np.zeros(m.neq + 1)
+    its = R.fr_tt_predictor2(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f, prob.upmode,
+                             prob.upval, float(alpha), float(dt), perm, inv, init, topts.as_array(), int(kmax),
+                             int(lmax), float(tol), u)
+    return u[:m.neq].copy(), its
 
 
 def build_tt(prob, alpha, dt, u=None, du=None):
@@ -563,6 +614,55 @@ def tt_predictor(prob, alpha, dt, topts: TimeOpts, tol=1e-10, kmax=30, lmax=1000
     lib().or_tt_predictor(*_mesh_args(m), ctypes.byref(s), float(alpha), float(dt), ctypes.byref(topts), tol, kmax,
                           lmax, u, a, ctypes.byref(st))
     return u[:m.neq].copy(), a[:m.neq].copy(), {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def build_tt_mfdd(prob, alpha, dt, u=None, du=None, uB=None, duB=None, delta_old=None):
+    """Build_M_F_DD (TimeIntegration "Predictor2", form DD) at (u, du) with
+    the bubble unknowns (uB, duB: one per element); returns (A[nel, 9],
+    F[neq+1], cond[nel, 5] = invN2, R2, M2[0..2]).  delta_old (nel, updated
+    in place) is the relaxed shock-capture state, None = fresh zeros."""
+    m = prob.mesh
+    z = np.zeros
+    u = z(m.neq) if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    du = z(m.neq) if du is None else np.ascontiguousarray(du, dtype=np.float64)
+    uB = z(m.nel) if uB is None else np.ascontiguousarray(uB, dtype=np.float64)
+    duB = z(m.nel) if duB is None else np.ascontiguousarray(duB, dtype=np.float64)
+    A = np.empty(m.nel * 9)
+    F = np.empty(m.neq + 1)
+    cond = np.empty(m.nel * 5)
+    s, keep = _problem_struct(prob)
+    if delta_old is not None:
+        s.delta_old = delta_old.ctypes.data
+    lib().or_build_tt_mfdd(*_mesh_args(m), ctypes.byref(s), float(alpha), float(dt), u, du, uB, duB, A, F, cond)
+    return A.reshape(m.nel, 9), F, cond.reshape(m.nel, 5)
+
+
+def tt_dab(lm, cond, Da):
+    """calculate_DaB: the bubble increments (nel) from Da (neq + 1)."""
+    nel = lm.shape[0]
+    Da = np.array(Da, dtype=np.float64, copy=True)
+    DaB = np.empty(nel)
+    lib().or_tt_dab(nel, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1), Da.shape[0] - 1,
+                    np.ascontiguousarray(cond, dtype=np.float64).reshape(-1), Da, DaB)
+    return DaB
+
+
+def tt_predictor2(prob, alpha, dt, topts: TimeOpts, tol=1e-10, kmax=30, lmax=1000, u0=None):
+    """Predictor_New with Build_M_F_DD ("Predictor2", form DD); returns
+    (u, a, uB, aB, stats)."""
+    m = prob.mesh
+    u = np.zeros(m.neq + 1)
+    if u0 is not None:
+        u[:m.neq] = u0
+    a = np.zeros(m.neq + 1)
+    uB = np.zeros(max(m.nel, 1))
+    aB = np.zeros(max(m.nel, 1))
+    st = _TimeStats()
+    s, keep = _problem_struct(prob)
+    lib().or_tt_predictor2(*_mesh_args(m), ctypes.byref(s), float(alpha), float(dt), ctypes.byref(topts), tol, kmax,
+                           lmax, u, a, uB, aB, ctypes.byref(st))
+    return (u[:m.neq].copy(), a[:m.neq].copy(), uB[:m.nel].copy(), aB[:m.nel].copy(),
+            {k: getattr(st, k) for k, _ in st._fields_})
 
 
 def ebemv3_perm(lm, A, perm, inv, P):

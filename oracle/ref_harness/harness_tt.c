@@ -143,3 +143,189 @@ int fr_tt_build(int nnodes, int nel, const double *x, const double *y, const int
     free(S.F); free(S.u); free(S.du); free(S.delta_old);
     return 0;
 }
+
+/* ---- TimeIntegration "Predictor2" with StabilizationForm "DD" ----
+ * setStabilizationForm.c:51-54 installs Build_M_F_DD and Predictor_New.
+ * fr_tt_mfdd_build: one Build_M_F_DD at (u, du, uB, duB) with a fresh
+ * delta_old, then calculate_DaB on the caller's Da (NEQ + 1; its sink is
+ * set to 0 there).  A (9 per element), F (NEQ + 1), cond (invN2, R2,
+ * M2[0..2] per element) and DaB (nel) are returned. */
+int Build_M_F_DD(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *);
+int calculate_DaB(ParametersType *, FemStructsType *, double *, double *);
+int Predictor_New(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *, FemOtherFunctionsType *);
+void setStopCriteria(ParametersType *, FemFunctionsType *);
+int pgmres(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *, double *, double *);
+int ebemv(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
+int Diag_precond(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
+int NO_precond(ParametersType *, MatrixDataType *, FemStructsType *, double *, double *);
+int Diag_precond_EBE_setup(ParametersType *, MatrixDataType *, FemStructsType *, int, double *);
+
+typedef struct {
+    ParametersType P;
+    MatrixDataType M;
+    FemStructsType S;
+    FemFunctionsType F;
+    FemOtherFunctionsType O;
+} fr_tt;
+
+static const double *g_init;
+static int syn_init(ParametersType *P, NodeType *Node, double *u)
+{
+    (void)Node;
+    memcpy(u, g_init, sizeof(double) * (size_t)P->neq);
+    return 0;
+}
+
+static void fr_tt_setup(fr_tt *c, int nnodes, int nel, const double *x, const double *y, const int *type,
+                        const int *invp, const int *ien, int neq, double k, double gamma, double bx, double by,
+                        double f, int upmode, double upval, double alpha, double dt)
+{
+    int I;
+    memset(c, 0, sizeof(*c));
+    g_k = k; g_gamma = gamma; g_bx = bx; g_by = by; g_f = f; g_upmode = upmode; g_upval = upval;
+    g_xmin = x[0]; g_ymin = y[0];
+    for (I = 1; I < nnodes; I++) {
+        if (x[I] < g_xmin) g_xmin = x[I];
+        if (y[I] < g_ymin) g_ymin = y[I];
+    }
+    strcpy(c->P.MatrixVectorProductScheme, "EBE");
+    strcpy(c->P.StabilizationForm, "DD");
+    strcpy(c->P.TimeIntegration, "Predictor2");
+    strcpy(c->P.Preconditioner, "Diag");
+    c->P.nnodes = c->P.nNodes = nnodes;
+    c->P.nel = c->P.nEl = nel;
+    c->P.neq = neq;
+    c->P.NEQ = neq;
+    c->P.NPROC = 1;
+    c->P.Alpha = c->P.Alpha_Build = alpha;
+    c->P.DeltaT = c->P.DeltaT_Build = dt;
+    c->F.Condutivity = syn_k;
+    c->F.Reaction = syn_gamma;
+    c->F.Font = syn_font;
+    c->F.Velocity = syn_vel;
+    c->F.upresc = syn_upresc;
+    c->F.InitialSolution = syn_init;
+    c->F.assembly = ebe_assembly;
+    c->F.ShockCapture = g_shock == 3 ? YZBeta_ShockCapture : CAU_DD_ShockCapture;
+    c->F.h_shock = g_hshock == 2 ? h_shock_Option2 : g_hshock == 1 ? h_shock_Option1 : h_shock_2sqrtArea;
+    /* setPreconditioner.c:10-15 ("Diag", EBE); the transient driver never
+     * sets precondR, which pgmres.c:61,93,186 calls: the identity here, as
+     * the other drivers install it (NO_precond) */
+    c->F.mv = ebemv;
+    c->F.precond = Diag_precond;
+    c->F.precondR = NO_precond;
+    c->F.precond_setup = Diag_precond_EBE_setup;
+    c->O.Build = Build_M_F_DD;
+    c->O.solver = pgmres;
+    NodeType *Node = calloc((size_t)nnodes, sizeof(NodeType));
+    ElementType *El = calloc((size_t)nel, sizeof(ElementType));
+    for (I = 0; I < nnodes; I++) {
+        Node[I].x = x[I];
+        Node[I].y = y[I];
+        Node[I].Type = type[I];
+        Node[I].Send = 1;
+        Node[I].invP_id = type[I] == 0 ? -1 : invp[I];
+    }
+    for (I = 0; I < nel; I++) {
+        El[I].Vertex[0] = ien[3 * I];
+        El[I].Vertex[1] = ien[3 * I + 1];
+        El[I].Vertex[2] = ien[3 * I + 2];
+    }
+    c->S.Node = Node;
+    c->S.Element = El;
+    c->S.lm = calloc((size_t)nel, sizeof(int *));
+    c->S.lmaux = calloc((size_t)nel * 3, sizeof(int));
+    for (I = 0; I < nel; I++) c->S.lm[I] = &c->S.lmaux[3 * I];
+    c->M.A = calloc((size_t)nel, sizeof(double *));
+    c->M.Aaux = calloc((size_t)nel * 9, sizeof(double));
+    for (I = 0; I < nel; I++) c->M.A[I] = &c->M.Aaux[9 * I];
+    c->M.Diag = calloc((size_t)neq + 1, sizeof(double));
+    c->M.invDiag = calloc((size_t)neq + 1, sizeof(double));
+    c->S.F = calloc((size_t)neq + 1, sizeof(double));
+    c->S.u = calloc((size_t)neq + 1, sizeof(double));
+    Fill_LM(&c->P, c->S.lm, Node, El);
+}
+
+static void fr_tt_free(fr_tt *c)
+{
+    free(c->S.Node); free(c->S.Element); free(c->S.lm); free(c->S.lmaux); free(c->M.A); free(c->M.Aaux);
+    free(c->M.Diag); free(c->M.invDiag); free(c->S.F); free(c->S.u);
+}
+
+int fr_tt_mfdd_build(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                     const int *ien, int neq, double k, double gamma, double bx, double by, double f, int upmode,
+                     double upval, double alpha, double dt, const double *u, const double *du, const double *uB,
+                     const double *duB, const double *Da, double *A_out, double *F_out, double *cond_out,
+                     double *DaB_out)
+{
+    fr_tt c;
+    AuxBuildStructuresType Aux;
+    int I;
+    fr_tt_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, k, gamma, bx, by, f, upmode, upval, alpha, dt);
+    memset(&Aux, 0, sizeof Aux);
+    double *R2aux = calloc((size_t)nel, sizeof(double)), *M2aux = calloc((size_t)nel * 3, sizeof(double));
+    double **R2 = calloc((size_t)nel, sizeof(double *)), **M2 = calloc((size_t)nel, sizeof(double *));
+    for (I = 0; I < nel; I++) { R2[I] = &R2aux[I]; M2[I] = &M2aux[3 * I]; }
+    Aux.R2 = R2;
+    Aux.M2 = M2;
+    Aux.invN2 = calloc((size_t)nel, sizeof(double));
+    c.S.AuxBuild = &Aux;
+    c.S.du = calloc((size_t)neq + 1, sizeof(double));
+    c.S.uB = calloc((size_t)nel, sizeof(double));
+    c.S.duB = calloc((size_t)nel, sizeof(double));
+    c.S.delta_old = calloc((size_t)nel, sizeof(double));
+    memcpy(c.S.u, u, sizeof(double) * (size_t)neq);
+    memcpy(c.S.du, du, sizeof(double) * (size_t)neq);
+    memcpy(c.S.uB, uB, sizeof(double) * (size_t)nel);
+    memcpy(c.S.duB, duB, sizeof(double) * (size_t)nel);
+    Build_M_F_DD(&c.P, &c.M, &c.S, &c.F);
+    double *Dac = calloc((size_t)neq + 1, sizeof(double));
+    memcpy(Dac, Da, sizeof(double) * ((size_t)neq + 1));
+    calculate_DaB(&c.P, &c.S, Dac, DaB_out);
+    memcpy(A_out, c.M.Aaux, sizeof(double) * 9 * (size_t)nel);
+    memcpy(F_out, c.S.F, sizeof(double) * ((size_t)neq + 1));
+    for (I = 0; I < nel; I++) {
+        cond_out[5 * I] = Aux.invN2[I];
+        cond_out[5 * I + 1] = R2[I][0];
+        cond_out[5 * I + 2] = M2[I][0];
+        cond_out[5 * I + 3] = M2[I][1];
+        cond_out[5 * I + 4] = M2[I][2];
+    }
+    free(Dac); free(R2aux); free(M2aux); free(R2); free(M2); free(Aux.invN2);
+    free(c.S.du); free(c.S.uB); free(c.S.duB); free(c.S.delta_old);
+    fr_tt_free(&c);
+    return 0;
+}
+
+/* The reference's own Predictor_New loop with Build_M_F_DD, Diag and
+ * pgmres (EBE on the caller's local RCM permutation Perm / invPerm, NEQ + 1
+ * each).  topt: stop_by_norm, max_corrections, correction_tol,
+ * steady_state, final_time, time_tol; solver: kmax, lmax, tol.  u_out
+ * (neq) receives the final state; returns the GMRES iterations. */
+int fr_tt_predictor2(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                     const int *ien, int neq, double k, double gamma, double bx, double by, double f, int upmode,
+                     double upval, double alpha, double dt, const int *Perm, const int *invPerm,
+                     const double *init, const double *topt, int kmax, int lmax, double tol, double *u_out)
+{
+    fr_tt c;
+    fr_tt_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, k, gamma, bx, by, f, upmode, upval, alpha, dt);
+    c.M.Perm = (int *)Perm;
+    c.M.invPerm = (int *)invPerm;
+    g_init = init;
+    strcpy(c.P.StopMulticorrection, topt[0] != 0.0 ? "NORM" : "ITERATION");
+    c.P.NonLinearMaxIter = (int)topt[1];
+    c.P.NonLinearTolerance = topt[2];
+    strcpy(c.P.StopAtSteadyState, topt[3] != 0.0 ? "YES" : "NO");
+    c.P.FinalTime = topt[4];
+    c.P.TimeIntegrationTolerance = topt[5];
+    c.P.KrylovBasisVectorsQuantity = kmax;
+    c.P.LinearMaxIter = lmax;
+    c.P.SolverTolerance = tol;
+    c.P.iterations = 0;
+    setStopCriteria(&c.P, &c.F);
+    Predictor_New(&c.P, &c.M, &c.S, &c.F, &c.O);
+    memcpy(u_out, c.S.u, sizeof(double) * (size_t)neq);
+    int its = c.P.iterations;
+    fr_tt_free(&c);
+    return its;
+}

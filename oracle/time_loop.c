@@ -4,7 +4,9 @@
  * transient-transport restatements (test infrastructure: the checker the
  * device time loops are compared with, never a product path).
  *
- *   OR_TIME_PREDICTOR  Predictor_Old.c:53-126
+ *   OR_TIME_PREDICTOR  Predictor_Old.c:53-126; with a `predict` hook (the
+ *                      bubble unknowns of the DD builds, updated by the
+ *                      caller's correction) Predictor_New.c:67-159
  *   OR_TIME_BDF        Predictor_Old_BDF.c:44-150
  *   OR_TIME_TRBDF2     Predictor_New_TRBDF2.c:55-190 without the bubble
  *                      unknowns uB, aB (they feed only the DD builders)
@@ -74,6 +76,12 @@ static int stop_time(loop_state *L, const double *u, const double *u_old, double
 int or_time_integrate(int neq, double alpha, double dt, const or_time_opts *to, or_correction_fn correct,
                       void *ctx, double *u, double *a, or_time_stats *st)
 {
+    return or_time_integrate_ex(neq, alpha, dt, to, correct, NULL, ctx, u, a, st);
+}
+
+int or_time_integrate_ex(int neq, double alpha, double dt, const or_time_opts *to, or_correction_fn correct,
+                         or_predict_fn predict, void *ctx, double *u, double *a, or_time_stats *st)
+{
     size_t nb = sizeof(double) * ((size_t)neq + 1);
     double *u_old = calloc(1, nb), *u1 = calloc(1, nb), *u2 = calloc(1, nb);
     loop_state L = { neq, 0, 0, 0, to, correct, ctx, calloc(1, nb), calloc(1, nb) };
@@ -87,6 +95,7 @@ int or_time_integrate(int neq, double alpha, double dt, const or_time_opts *to, 
             memcpy(u_old, u, sizeof(double) * (size_t)neq);
             axpy(neq, (1.0 - alpha) * dt, a, u);                      /* prediction */
             memset(a, 0, sizeof(double) * (size_t)neq);
+            if (predict) predict(ctx, (1.0 - alpha) * dt);              /* Predictor_New.c:82-83 */
             if ((rc = multicorrect(&L, alpha, dt, alpha * dt, u, a))) break;
         } while (!stop_time(&L, u, u_old, t, dt));
     } else if (to->scheme == OR_TIME_BDF) {

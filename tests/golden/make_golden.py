@@ -244,6 +244,37 @@ def write_tt():
     np.savez_compressed(os.path.join(HERE, "tt_ref.npz"), **out)
 
 
+TT_P2_CASES = [(2, 0), (3, 2)]   # (shock, h_shock) of the DD form
+
+
+def write_tt_predictor2():
+    """TimeIntegration "Predictor2" of the transient transport driver
+    (oracle/_ref/libref_tt.so): one Build_M_F_DD + calculate_DaB at random
+    states, and the reference's own Predictor_New loop (Diag, pgmres) over
+    4 steps of 2 corrections."""
+    out = {}
+    for cau, hs in TT_P2_CASES:
+        p = G.transport_problem(17, angle_deg=35.0, k=1e-3, gamma=0.2, f=0.5, cau=cau)
+        p.form, p.h_shock = 1, hs
+        m = p.mesh
+        rng = np.random.default_rng(200 + 10 * cau + hs)
+        u = rng.random(m.neq)
+        du = rng.standard_normal(m.neq)
+        uB = rng.random(m.nel)
+        duB = rng.standard_normal(m.nel)
+        Da = np.append(rng.standard_normal(m.neq), 5.0)
+        A, F, cond, DaB = O.ref_tt_mfdd_build(p, 0.5, 0.01, u, du, uB, duB, Da)
+        key = f"p2_{cau}_{hs}"
+        for name, v in (("u", u), ("du", du), ("uB", uB), ("duB", duB), ("Da", Da), ("A", A), ("F", F),
+                        ("cond", cond), ("DaB", DaB)):
+            out[f"{key}_{name}"] = v
+        to = O.TimeOpts(0, 2, 1e-3, 0, 0.04 + 1e-12, 1e-6, 0, 0)
+        U, its = O.ref_tt_predictor2(p, 0.5, 0.01, to, tol=1e-10, kmax=30, lmax=1000)
+        out[key + "_U"], out[key + "_its"] = U, np.array([its])
+        print(key, "gmres", its)
+    np.savez_compressed(os.path.join(HERE, "tt_predictor2_ref.npz"), **out)
+
+
 def write_elem_prec():
     """The steady driver's element preconditioners (Preconditioner "LUe" and
     "SGSe": LU_precond_EBE*.c, SGS_precond_EBE*.c and pgmres with their
@@ -280,4 +311,5 @@ if __name__ == "__main__":
     write_ilup()
     write_euler_dd()
     write_tt()
+    write_tt_predictor2()
     write_elem_prec()

@@ -160,3 +160,98 @@ def test_transient_build_matches_reference(form, cau, hs):
     A0, R0 = O.build_tt(p, 0.3, 0.05, u, du)
     A1, R1 = O.ref_tt_build(p, 0.3, 0.05, u, du)
     assert np.array_equal(A0, A1) and np.array_equal(R0[:-1], R1[:-1])
+
+
+# ---- TimeIntegration "Predictor2" with the DD form: Build_M_F_DD.c,
+# calculate_DaB.c and Predictor_New.c (the bubble of each element kept as
+# an unknown and condensed out of the element system) ----
+
+P2_CASES = [(2, 0), (3, 2)]    # (shock CAUDD / YZBeta, h_shock)
+
+
+def _p2_problem(cau, hs, n=17):
+    p = G.transport_problem(n, angle_deg=35.0, k=1e-3, gamma=0.2, f=0.5, cau=cau)
+    p.form, p.h_shock = 1, hs
+    return p
+
+
+@pytest.fixture(scope="module")
+def p2gold():
+    import os
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "tt_predictor2_ref.npz"))
+
+
+@pytest.mark.parametrize("cau,hs", P2_CASES)
+def test_predictor2_build_matches_reference_golden(p2gold, cau, hs):
+    """Me, F, the condensation data (invN2, R2, M2) and calculate_DaB's
+    bubble increments bit-identical with the reference's own functions."""
+    g, key = p2gold, f"p2_{cau}_{hs}"
+    p = _p2_problem(cau, hs)
+    A, F, cond = O.build_tt_mfdd(p, 0.5, 0.01, g[key + "_u"], g[key + "_du"], g[key + "_uB"], g[key + "_duB"])
+    assert np.array_equal(A, g[key + "_A"])
+    assert np.array_equal(F, g[key + "_F"])
+    assert np.array_equal(cond, g[key + "_cond"])
+    DaB = O.tt_dab(O.fill_lm(p.mesh), cond, g[key + "_Da"])
+    assert np.array_equal(DaB, g[key + "_DaB"])
+
+
+@pytest.mark.parametrize("cau,hs", P2_CASES)
+def test_predictor2_loop_matches_reference_golden(p2gold, cau, hs):
+    """The whole Predictor_New loop (4 steps x 2 corrections, Diag, GMRES):
+    the final state and the GMRES iteration count equal the reference's."""
+    g, key = p2gold, f"p2_{cau}_{hs}"
+    to = O.TimeOpts(0, 2, 1e-3, 0, 0.04 + 1e-12, 1e-6, 0, 0)
+    u, a, uB, aB, st = O.tt_predictor2(_p2_problem(cau, hs), 0.5, 0.01, to, tol=1e-10, kmax=30, lmax=1000)
+    assert st["steps"] == 4 and st["corrections"] == 8
+    assert st["gmres_iterations"] == int(g[key + "_its"][0])
+    assert np.array_equal(u, g[key + "_U"])
+
+
+@pytest.mark.skipif(O.ref_tt() is None, reason="reference transient build absent")
+def test_predictor2_matches_reference_live():
+    p = _p2_problem(2, 1, n=13)
+    m = p.mesh
+    rng = np.random.default_rng(11)
+    u, du = rng.random(m.neq), rng.standard_normal(m.neq)
+    uB, duB = rng.random(m.nel), rng.standard_normal(m.nel)
+    Da = np.append(rng.standard_normal(m.neq), 1.0)
+    A0, F0, c0, D0 = O.ref_tt_mfdd_build(p, 0.3, 0.05, u, du, uB, duB, Da)
+    A1, F1, c1 = O.build_tt_mfdd(p, 0.3, 0.05, u, du, uB, duB)
+    assert np.array_equal(A0, A1) and np.array_equal(F0, F1) and np.array_equal(c0, c1)
+    assert np.array_equal(D0, O.tt_dab(O.fill_lm(m), c1, Da))
+    to = O.TimeOpts(1, 3, 1e-4, 0, 0.15 + 1e-12, 1e-6, 0, 0)
+    U0, its0 = O.ref_tt_predictor2(p, 0.5, 0.05, to, tol=1e-10)
+    U1, a1, uB1, aB1, st = O.tt_predictor2(p, 0.5, 0.05, to, tol=1e-10)
+    assert st["gmres_iterations"] == its0 and np.array_equal(U0, U1)
+
+
+def test_predictor2_bubble_condensation():
+    """Static condensation: the condensed element system is exact.  For
+    each element, solving the 4x4 system [M1 N1; M2 N2] (nodal rows and the
+    bubble row) for (Da_e, DaB) with the element's own residuals gives
+    DaB = invN2 (R2 - M2 . Da_e), and Me Da_e = R1 - N1 invN2 R2 on the
+    nodal rows -- checked by assembling the 4x4 blocks from the
+    condensation data and comparing with calculate_DaB's increments."""
+    p = _p2_problem(2, 0, n=9)
+    m = p.mesh
+    rng = np.random.default_rng(5)
+    A, F, cond = O.build_tt_mfdd(p, 0.5, 0.02, rng.random(m.neq), rng.standard_normal(m.neq),
+                                 rng.random(m.nel), rng.standard_normal(m.nel))
+    Da = np.append(rng.standard_normal(m.neq), 0.0)
+    DaB = O.tt_dab(O.fill_lm(m), cond, Da)
+    lm = O.fill_lm(m)
+    invN2, R2, M2 = cond[:, 0], cond[:, 1], cond[:, 2:5]
+    # bubble row of the 4x4 system: M2 . Da_e + N2 DaB = R2
+    resid = np.einsum("ej,ej->e", M2, Da[lm]) + DaB / invN2 - R2
+    assert np.abs(resid).max() <= 1e-12 * max(np.abs(R2).max(), 1.0)
+
+
+def test_predictor2_reaches_the_steady_dd_solution():
+    """With a large step the loop's state approaches the steady DD solution
+    of the same problem (the bubble equation is the steady DD's in the
+    limit du/dt -> 0)."""
+    p = _p2_problem(2, 0, n=13)
+    p.k = 1e-2
+    u, a, uB, aB, st = O.tt_predictor2(p, 0.5, 0.5, O.TimeOpts(1, 5, 1e-8, 1, 1e4, 1e-9, 0, 0), tol=1e-12)
+    Us, nl, its = O.transport_process(p, 1e-12, 1e-8, 30, 1000)
+    assert np.linalg.norm(u - Us[: p.mesh.neq]) <= 1e-4 * np.linalg.norm(Us[: p.mesh.neq])
