@@ -459,7 +459,8 @@ typedef struct {
     int precond;           /* FG_PRECOND_BLOCKDIAG, FG_PRECOND_DIAG or NONE; ILU0 or
                               SPIKE on a system switched to FG_OP_CSR            */
     int setup_flags;       /* FG_SETUP_REF_QUIRKS: the reference's 4x4 inverse     */
-    int scheme;            /* FG_TIME_PREDICTOR (0), FG_TIME_BDF, FG_TIME_TRBDF2    */
+    int scheme;            /* FG_TIME_PREDICTOR (0), FG_TIME_BDF, FG_TIME_TRBDF2,
+                              FG_TIME_PREDICTOR2 (transient transport DD only)   */
 } fg_time_opts;
 
 /* TimeIntegration of the drivers (setStabilizationForm.c):
@@ -475,8 +476,14 @@ typedef struct {
  *                      1/(2 - lambda) over (1 - lambda) dt, prediction
  *                      A u - B u_old).  "Predictor1_TRBDF2"
  *                      (Predictor_Old_TRBDF2.c) solves against a right-hand
- *                      side that nothing fills and is not restated. */
-enum { FG_TIME_PREDICTOR = 0, FG_TIME_BDF = 1, FG_TIME_TRBDF2 = 2 };
+ *                      side that nothing fills and is not restated.
+ *   FG_TIME_PREDICTOR2 "Predictor2"        Predictor_New.c:3-179 with the
+ *                      transient transport DD form (fg_tt_predictor only):
+ *                      Predictor_Old's steps plus one bubble unknown per
+ *                      element, predicted with u (uB += (1 - alpha) dt aB,
+ *                      aB = 0) and corrected after each solve from Da
+ *                      (calculate_DaB: aB += DaB, uB += alpha dt DaB). */
+enum { FG_TIME_PREDICTOR = 0, FG_TIME_BDF = 1, FG_TIME_TRBDF2 = 2, FG_TIME_PREDICTOR2 = 3 };
 
 typedef struct {
     int steps;
@@ -522,6 +529,27 @@ int fg_tt_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, const d
  * Diag_precond_EBE_setup) or any other kind this system supports. */
 int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *opts, const fg_time_opts *t,
                     double *u, double *a, fg_time_stats *stats);
+/* TimeIntegration "Predictor2" (t->scheme FG_TIME_PREDICTOR2, c.form
+ * FG_TRANSPORT_DD): each correction builds with Build_M_F_DD.c:6-263 -- the
+ * element's bubble kept as an unknown (uB, duB) and condensed out of the
+ * element system, N2 = MBB + alpha dt KBB -- and recovers the bubble
+ * increment from Da (calculate_DaB.c:3-30); bubble unknowns and condensation
+ * data stay on the device.  Blocks, load and DaB are bit-identical with the
+ * reference's functions.
+ *
+ * One build at (u, du, uB, duB) with a fresh shock-capture state (u, du:
+ * free dofs, reference numbering; uB, duB: nel values in reference element
+ * order; NULL = 0).  F (host, n+1, may be NULL) receives the load, cond
+ * (host, 5 per element, may be NULL) invN2, R2, M2[0..2]; the blocks stay on
+ * the device (fg_get_blocks). */
+int fg_tt_bubble_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, const double *du, const double *uB,
+                          const double *duB, double *F, double *cond);
+/* calculate_DaB after the last Predictor2 build: DaB (host, nel) from Da
+ * (host, n+1, reference numbering; its sink entry is read as 0). */
+int fg_tt_bubble_dab(fg_system *s, const double *Da, double *DaB);
+/* The bubble unknowns uB and aB (host, nel each, reference element order,
+ * either may be NULL) after fg_tt_predictor with FG_TIME_PREDICTOR2. */
+int fg_tt_bubble_state(fg_system *s, double *uB, double *aB);
 
 /* ---- request server: continuous batching of transport solves ----
  * A worker thread owns one batch.  Requests (a system whose geometry is set,

@@ -1126,8 +1126,165 @@ __global__ void k_tt_dd_elem(int nel, int ld, const int *__restrict__ gien, cons
     }
 }
 
+// Build_M_F_DD.c:52-244 (TimeIntegration "Predictor2", form DD), a thread
+// per element: the element's bubble kept as an unknown (uB, duB in the
+// bubble planes, internal element position) and condensed out with
+// N2 = MBB + alpha dt KBB.  Writes Me into the blocks, the load
+// R1 - invN2 N1 R2 of vertex i into Rt plane 4 i (one term per incidence),
+// and invN2, R2, M2[0..2] into the bubble planes for the correction
+// (calculate_DaB).  The shock capture is relaxed against cbtilo as in
+// k_tt_dd_elem.
+__global__ void k_tt_mfdd_elem(int nel, int ld, const int *__restrict__ gien, const double *__restrict__ gx,
+                               const double *__restrict__ gy, const int *__restrict__ gtype,
+                               const int *__restrict__ node_dof, const double *__restrict__ up,
+                               const double *__restrict__ u, const double *__restrict__ du, fg_tt_coeffs tc,
+                               double *cbtilo, double *__restrict__ bub, double *__restrict__ A64,
+                               double *__restrict__ Rt)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const fg_transport_coeffs &cf = tc.c;
+    const double third = 1.0/3.0, sixth = 1.0/6.0, seventh = 1.0/7.0, twelfth = 1.0/12.0;
+    const double t320 = 3./20.0, n920 = 9./20.0, n940 = 9./40.0, w = 0.5;
+    const double kx = cf.k, ky = cf.k, gamma = cf.gamma, bx = cf.beta[0], by = cf.beta[1];
+    int J1 = gien[pos], J2 = gien[ld + pos], J3 = gien[2 * (size_t)ld + pos];
+    double X0 = gx[J1], X1 = gx[J2], X2 = gx[J3];
+    double Y0 = gy[J1], Y1 = gy[J2], Y2 = gy[J3];
+    double y23 = Y1 - Y2, y31 = Y2 - Y0, y12 = Y0 - Y1;
+    double x32 = X2 - X1, x13 = X0 - X2, x21 = X1 - X0;
+    double TwoA = x21*y31 - x13*y12;
+    double Area = 0.5*TwoA;
+    double invArea = 1.0/Area;
+    double fe1 = cf.f, fe2 = cf.f, fe3 = cf.f;
+    double feb = third*(fe1 + fe2 + fe3);
+    const int J[3] = {J1, J2, J3};
+    double ue[3], due[3];
+    for (int a = 0; a < 3; ++a) {
+        const bool fixed = gtype[J[a]] == 0;
+        ue[a] = fixed ? up[J[a]] : u[node_dof[J[a]]];
+        due[a] = fixed ? 0.0 : du[node_dof[J[a]]];
+    }
+    const double uB = bub[pos], duB = bub[(size_t)ld + pos];
+    double ueb = third*(ue[0] + ue[1] + ue[2]);
+    double dueb = third*(due[0] + due[1] + due[2]);
+    double Mhh = twelfth*Area, MhB = t320*Area, MBh = MhB, MBB = (81.0/280.)*Area;
+    double a1 = bx*y23 + by*x32, a2 = bx*y31 + by*x13, a3 = bx*y12 + by*x21;
+    double C12 = y23*y31 + x32*x13, C13 = y23*y12 + x32*x21, C23 = y31*y12 + x13*x21;
+    double D12 = 0.25*invArea*((kx*y23*y31) + (ky*x32*x13));
+    double D13 = 0.25*invArea*((kx*y23*y12) + (ky*x32*x21));
+    double D23 = 0.25*invArea*((kx*y31*y12) + (ky*x13*x21));
+    double R11 = sixth*gamma*Area, R12 = twelfth*gamma*Area;
+    double Eu = 0.0;
+    if (cf.cau == FG_SHOCK_CAUDD || cf.cau == FG_SHOCK_YZBETA) {
+        double h = h_shock_dev(cf.h_shock, bx, by, ue[0], ue[1], ue[2], y23, y31, y12, x32, x13, x21, Area);
+        double cbtil;
+        if (cf.cau == FG_SHOCK_YZBETA) {
+            cbtil = tt_yz_eu(bx, by, gamma, ue[0], ue[1], ue[2], ueb, dueb, feb, y23, y31, y12, x32, x13, x21, invArea, h);
+        } else {
+            double bgu = 0.5*invArea*(ue[0]*(bx*y23 + by*x32) + ue[1]*(bx*y31 + by*x13) + ue[2]*(bx*y12 + by*x21));
+            double Ru = dueb + bgu + gamma*ueb - feb;
+            double gxu = 0.5*invArea*(y23*ue[0] + y31*ue[1] + y12*ue[2]);
+            double gyu = 0.5*invArea*(x32*ue[0] + x13*ue[1] + x21*ue[2]);
+            double ng = sqrt(gxu*gxu + gyu*gyu);
+            cbtil = ng > 1e-10 ? 0.5*h*fabs(Ru)/ng : 0.0;
+        }
+        double cb = w*cbtil + (1 - w)*cbtilo[pos];
+        cbtilo[pos] = cbtil;
+        Eu = cb;
+    }
+    double K12 = 0.25*Eu*invArea*C12, K13 = 0.25*Eu*invArea*C13, K23 = 0.25*Eu*invArea*C23;
+    double Khh[9];
+    Khh[0] = -(D12 + D13) + sixth*a1 + R11 -(K12 + K13);
+    Khh[1] =          D12 + sixth*a2 + R12 + K12;
+    Khh[2] =          D13 + sixth*a3 + R12 + K13;
+    Khh[3] =          D12 + sixth*a1 + R12 + K12;
+    Khh[4] = -(D12 + D23) + sixth*a2 + R11 -(K12 + K23);
+    Khh[5] =          D23 + sixth*a3 + R12 + K23;
+    Khh[6] =          D13 + sixth*a1 + R12 + K13;
+    Khh[7] =          D23 + sixth*a2 + R12 + K23;
+    Khh[8] = -(D13 + D23) + sixth*a3 + R11 -(K13 + K23);
+    const double KhB[3] = {n920*(0.5*a1 + a2 + a3) + t320*gamma*Area, n920*(a1 + 0.5*a2 + a3) + t320*gamma*Area,
+                           n920*(a1 + a2 + 0.5*a3) + t320*gamma*Area};
+    const double KBh[3] = {n940*a1 + t320*gamma*Area, n940*a2 + t320*gamma*Area, n940*a3 + t320*gamma*Area};
+    double KBB = -9*n940*(D12 + D13 + D23) + seventh*t320*(a1 + a2 + a3) + 9*seventh*n940*Area
+               - Eu*invArea*(C12 + C13 + C23)/360.;
+    const double Fh[3] = {twelfth*Area*(2*fe1 + fe2 + fe3), twelfth*Area*(fe1 + 2*fe2 + fe3),
+                          twelfth*Area*(fe1 + fe2 + 2*fe3)};
+    double FB = t320*Area*(fe1 + fe2 + fe3);
+    const double alpha = tc.alpha, dt = tc.dt;
+    double N2 = MBB + alpha*dt*KBB;
+    double invN2 = 1.0/N2;
+    double R2 = FB - MBB*duB - KBB*uB;
+    double M1[9], M2[3], N1[3], R1[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        M1[3 * i] = Mhh;
+        M1[3 * i + 1] = Mhh;
+        M1[3 * i + 2] = Mhh;
+        M1[3 * i + i] += Mhh;
+        M2[i] = MBh + alpha*dt*KBh[i];
+        N1[i] = MhB + alpha*dt*KhB[i];
+        R1[i] = Fh[i] - MhB*duB - KhB[i]*uB;
+        R1[i] -= Mhh*due[i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            M1[3 * i + j] += alpha*dt*Khh[3 * i + j];
+            R1[i] -= Mhh*due[j] + Khh[3 * i + j]*ue[j];
+        }
+        R2 -= MBh*due[i] + KBh[i]*ue[i];
+    }
+    double *A = A64 + pos;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) A[(size_t)(3 * i + j) * ld] = M1[3 * i + j] - invN2*N1[i]*M2[j];
+        Rt[(size_t)(4 * i) * ld + pos] = R1[i] - invN2*N1[i]*R2;
+    }
+    bub[2 * (size_t)ld + pos] = invN2;
+    bub[3 * (size_t)ld + pos] = R2;
+    bub[4 * (size_t)ld + pos] = M2[0];
+    bub[5 * (size_t)ld + pos] = M2[1];
+    bub[6 * (size_t)ld + pos] = M2[2];
+}
+
+// calculate_DaB.c:16-27 from the solve's Da (internal numbering; the sink,
+// a prescribed vertex, reads 0 as Da[NEQ] = 0 there), then Predictor_New.c:
+// 104-105: aB += DaB, uB += coef DaB (update), or DaB into out (!update).
+__global__ void k_tt_bubble_correct(int nel, int ld, const int *__restrict__ gien, const int *__restrict__ gtype,
+                                    const int *__restrict__ node_dof, const double *__restrict__ Da, double coef,
+                                    int update, double *__restrict__ bub, double *__restrict__ out)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    double d[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int J = gien[(size_t)a * ld + pos];
+        d[a] = gtype[J] == 0 ? 0.0 : Da[node_dof[J]];
+    }
+    const double M2Da = bub[4 * (size_t)ld + pos]*d[0] + bub[5 * (size_t)ld + pos]*d[1] + bub[6 * (size_t)ld + pos]*d[2];
+    const double DaB = bub[2 * (size_t)ld + pos]*(bub[3 * (size_t)ld + pos] - M2Da);
+    if (update) {
+        bub[(size_t)ld + pos] += DaB;
+        bub[pos] += coef*DaB;
+    } else {
+        out[pos] = DaB;
+    }
+}
+
+// Predictor_New.c:82-83: uB += coef aB, aB = 0
+__global__ void k_tt_bubble_predict(int nel, int ld, double coef, double *__restrict__ bub)
+{
+    int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    bub[pos] += coef*bub[(size_t)ld + pos];
+    bub[(size_t)ld + pos] = 0.0;
+}
+
 // R[d]: the element terms of dof d in reference element order, applied as
-// the reference applies them (R += Fe, then three subtractions); R[n] = 0.
+// the reference applies them (R += Fe, then three subtractions unless the
+// build has one term per incidence); R[n] = 0.
+template <bool SUB>
 __global__ void k_tt_R(int n, int ld, const int *__restrict__ dptr, const int *__restrict__ dinc,
                        const double *__restrict__ Rt, double *__restrict__ R)
 {
@@ -1138,9 +1295,11 @@ __global__ void k_tt_R(int n, int ld, const int *__restrict__ dptr, const int *_
     for (int q = dptr[d]; q < dptr[d + 1]; ++q) {
         const int pos = dinc[q] >> 4, a = dinc[q] & 15;
         s += Rt[(size_t)(4 * a) * ld + pos];
-        s -= Rt[(size_t)(4 * a + 1) * ld + pos];
-        s -= Rt[(size_t)(4 * a + 2) * ld + pos];
-        s -= Rt[(size_t)(4 * a + 3) * ld + pos];
+        if (SUB) {
+            s -= Rt[(size_t)(4 * a + 1) * ld + pos];
+            s -= Rt[(size_t)(4 * a + 2) * ld + pos];
+            s -= Rt[(size_t)(4 * a + 3) * ld + pos];
+        }
     }
     R[d] = s;
 }
@@ -1179,13 +1338,79 @@ int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev,
                                                       s->gup.as<double>(), u_dev, du_dev, *c, s->A64.as<double>(),
                                                       s->Fe.as<double>());
     FG_CUDA(cudaGetLastError());
-    k_tt_R<<<(t.n + 256) / 256, 256, 0, st>>>(t.n, s->nel_pad, s->dinc_ptr.as<int>(), s->dinc.as<int>(),
-                                             s->Fe.as<double>(), R_dev);
+    k_tt_R<true><<<(t.n + 256) / 256, 256, 0, st>>>(t.n, s->nel_pad, s->dinc_ptr.as<int>(), s->dinc.as<int>(),
+                                                   s->Fe.as<double>(), R_dev);
     FG_CUDA(cudaGetLastError());
     count_launches(2);
     s->blocks_ok = true;
     s->csr_dirty = true;
     return convert_blocks(s, st);
+}
+
+int tt_bubble_alloc(fg_system *s, cudaStream_t st)
+{
+    (void)st;
+    if (s->bubble.bytes >= 8 * (size_t)kBubblePlanes * s->nel_pad) return FG_OK;
+    return s->bubble.alloc(8 * (size_t)kBubblePlanes * s->nel_pad);   // zero-filled
+}
+
+int tt_mfdd_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev, const double *du_dev,
+                            double *F_dev, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (t.ndof != 1) { set_error("transient transport assembly needs ndof == 1"); return FG_ERR_UNSUPPORTED; }
+    if (!s->geometry_ok) { set_error("transient transport assembly before fg_set_geometry"); return FG_ERR_STATE; }
+    if (c->c.form != FG_TRANSPORT_DD || c->c.h_shock < FG_HSHOCK_2SQRTAREA || c->c.h_shock > FG_HSHOCK_OPTION2 ||
+        (c->c.cau != FG_SHOCK_NONE && c->c.cau != FG_SHOCK_CAUDD && c->c.cau != FG_SHOCK_YZBETA)) {
+        set_error("Predictor2 builds the DD form with CAUDD, YZBeta or no shock capture");
+        return FG_ERR_UNSUPPORTED;
+    }
+    int r;
+    if (s->shock_state.bytes < 16 * (size_t)s->nel_pad && (r = s->shock_state.alloc(16 * (size_t)s->nel_pad)))
+        return r;
+    if ((r = tt_bubble_alloc(s, st))) return r;
+    if (s->Fe.bytes < 8 * (size_t)12 * s->nel_pad && (r = s->Fe.alloc(8 * (size_t)12 * s->nel_pad))) return r;
+    double *cbtilo = s->shock_state.as<double>() + s->nel_pad;
+    if (t.nel > 0)
+        k_tt_mfdd_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(), s->gx.as<double>(),
+                                                           s->gy.as<double>(), s->gtype.as<int>(),
+                                                           s->node_dof.as<int>(), s->gup.as<double>(), u_dev, du_dev,
+                                                           *c, cbtilo, s->bubble.as<double>(), s->A64.as<double>(),
+                                                           s->Fe.as<double>());
+    FG_CUDA(cudaGetLastError());
+    k_tt_R<false><<<(t.n + 256) / 256, 256, 0, st>>>(t.n, s->nel_pad, s->dinc_ptr.as<int>(), s->dinc.as<int>(),
+                                                    s->Fe.as<double>(), F_dev);
+    FG_CUDA(cudaGetLastError());
+    count_launches(2);
+    s->blocks_ok = true;
+    s->csr_dirty = true;
+    return convert_blocks(s, st);
+}
+
+int tt_bubble_correct_device(fg_system *s, const double *Da_dev, double coef, double *DaB_dev, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (!s->bubble.p) { set_error("no Predictor2 build on this system"); return FG_ERR_STATE; }
+    if (t.nel > 0) {
+        k_tt_bubble_correct<<<(t.nel + 255) / 256, 256, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(),
+                                                                s->gtype.as<int>(), s->node_dof.as<int>(), Da_dev,
+                                                                coef, DaB_dev ? 0 : 1, s->bubble.as<double>(),
+                                                                DaB_dev);
+        FG_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
+    return FG_OK;
+}
+
+int tt_bubble_predict_device(fg_system *s, double coef, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (t.nel > 0) {
+        k_tt_bubble_predict<<<(t.nel + 255) / 256, 256, 0, st>>>(t.nel, s->nel_pad, coef, s->bubble.as<double>());
+        FG_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
+    return FG_OK;
 }
 
 int transport_assemble_device(fg_system *s, const fg_transport_coeffs *c, const double *u_dev, double *F_dev,

@@ -107,7 +107,7 @@ size_t fg_system::bytes() const
                            &dinv64, &dinv32, &lu_ia, &lu_ja, &lu_dg, &lu_map, &AAf64, &ilu_flags, &ilu_ctr, &ilu_tmp, &ilu_ford, &ilu_bord, &ilu_fpass, &ilu_bpass, &sp_bs, &sp_bl, &sp_bu, &sp_boff, &sp_band,
                            &sp_B, &sp_C, &sp_S, &sp_piv, &sp_g, &sp_h, &sp_x, &sp_tw, &sp_err, &sp_items, &sp_sysdev,
                            &diag, &invd64, &invd32, &bd, &ibd64, &ibd32, &gx, &gy, &gup, &gien, &gtype,
-                           &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &state_u1, &state_u2, &shock_state, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
+                           &ginvp, &Fe, &F64, &gf1, &gf2, &state_u, &state_a, &state_old, &state_u1, &state_u2, &shock_state, &bubble, &norm_part, &ws.V, &ws.w, &ws.t, &ws.x, &ws.b, &ws.ftrue, &ws.r64,
                            &ws.t64, &ws.u64, &ws.small, &ws.part, &ws.counter, &ws.state, &ep_lmi, &ep_coef};
     size_t b = 0;
     for (auto *m : all) b += m->bytes;
@@ -924,19 +924,35 @@ int download_solution(fg_system *s, double *X, cudaStream_t st)
 //   FG_TIME_TRBDF2     Predictor_New_TRBDF2.c:55-190 without the bubble
 //                      unknowns (TR stage alpha 1/2 over lambda dt, BDF2
 //                      stage alpha 1/(2 - lambda) over (1 - lambda) dt)
+//   FG_TIME_PREDICTOR2 Predictor_New.c:67-159: the Predictor_Old steps plus
+//                      the hooks of the per-element bubble unknowns
+//                      (predicted after u and a, corrected from each Da)
+// Per-step and per-correction hooks: predict(coef = (1 - alpha) dt) after
+// the prediction of u and a, corrected(Da, coef = alpha dt) after a += Da
+// and u += coef Da.
+struct LoopHooks {
+    std::function<int(double)> predict;
+    std::function<int(const double *, double)> corrected;
+};
+
 template <class Assemble>
 static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble, const fg_solver_opts *o,
                      const fg_time_opts *to, double *u, double *a, fg_time_stats *stats,
-                     const CorrectionSolve *solve = nullptr)
+                     const CorrectionSolve *solve = nullptr, const LoopHooks *hooks = nullptr)
 {
     if (to->precond < FG_PRECOND_NONE || to->precond > FG_PRECOND_SPIKE) {
         set_error("time-loop preconditioner must be NONE, DIAG, BLOCKDIAG, ILU0 or SPIKE");
         return FG_ERR_ARG;
     }
     if (to->max_corrections < 1 || !(dt > 0)) { set_error("max_corrections >= 1 and dt > 0 required"); return FG_ERR_ARG; }
-    if (to->scheme < FG_TIME_PREDICTOR || to->scheme > FG_TIME_TRBDF2) {
-        set_error("time scheme must be FG_TIME_PREDICTOR, FG_TIME_BDF or FG_TIME_TRBDF2");
+    if (to->scheme < FG_TIME_PREDICTOR || to->scheme > FG_TIME_PREDICTOR2) {
+        set_error("time scheme must be FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 or FG_TIME_PREDICTOR2");
         return FG_ERR_ARG;
+    }
+    const bool p2 = to->scheme == FG_TIME_PREDICTOR2;
+    if (p2 && !hooks) {
+        set_error("FG_TIME_PREDICTOR2 runs the transient transport DD build (fg_tt_predictor)");
+        return FG_ERR_UNSUPPORTED;
     }
     auto t0 = std::chrono::steady_clock::now();
     const int n = s->topo.n;
@@ -985,6 +1001,7 @@ static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble,
             const double *Da = s->ws.x.as<double>();
             if ((rr = axpy_norms_device(n, 1, Da, da, part, norms, s->stream))) return rr;   // a += Da
             if ((rr = axpy_device(n, coef, Da, du, s->stream))) return rr;                 // u += coef Da
+            if (hooks && hooks->corrected && (rr = hooks->corrected(Da, coef))) return rr;
             if (to->stop_by_norm) {
                 FG_CUDA(cudaMemcpyAsync(s->h_vec, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
                 FG_CUDA(cudaStreamSynchronize(s->stream));
@@ -1017,13 +1034,14 @@ static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble,
         return FG_OK;
     };
     bool stop_time = false;
-    if (to->scheme == FG_TIME_PREDICTOR) {
+    if (to->scheme == FG_TIME_PREDICTOR || p2) {
         do {
             ++steps;
             t += dt;
             if ((r = copy(dold, du))) return r;
             if ((r = axpy_device(n, (1.0 - alpha) * dt, da, du, s->stream))) return r;      // prediction
             FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+            if (p2 && hooks->predict && (r = hooks->predict((1.0 - alpha) * dt))) return r;
             if ((r = multicorrect(alpha, dt, alpha * dt)) || (r = time_stop(dt, stop_time))) return r;
         } while (!stop_time);
     } else if (to->scheme == FG_TIME_BDF) {
@@ -1132,6 +1150,30 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
     // the DD shock-capture state starts at zero with the loop (Predictor_Old.c:30 callocs delta_old)
     if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
+    if (to->scheme == FG_TIME_PREDICTOR2) {
+        // "Predictor2" exists for the DD form only (setStabilizationForm.c:51-54)
+        if (c->c.form != FG_TRANSPORT_DD) {
+            set_error("FG_TIME_PREDICTOR2 needs the DD form (FG_TRANSPORT_DD)");
+            return FG_ERR_UNSUPPORTED;
+        }
+        int r = tt_bubble_alloc(s, s->stream);
+        if (r) return r;
+        // uB and aB start at zero (Predictor_New.c:24,36 calloc them)
+        FG_CUDA(cudaMemsetAsync(s->bubble.p, 0, s->bubble.bytes, s->stream));
+        LoopHooks h;
+        h.predict = [&](double coef) { return tt_bubble_predict_device(s, coef, s->stream); };
+        h.corrected = [&](const double *Da, double coef) {
+            return tt_bubble_correct_device(s, Da, coef, nullptr, s->stream);
+        };
+        return time_loop(s, c->dt, c->alpha,
+                         [&](double ab, double db, const double *du, const double *da, double *R) {
+                             fg_tt_coeffs cc = *c;
+                             cc.alpha = ab;
+                             cc.dt = db;
+                             return tt_mfdd_assemble_device(s, &cc, du, da, R, s->stream);
+                         },
+                         o, to, u, a, stats, nullptr, &h);
+    }
     return time_loop(s, c->dt, c->alpha,
                      [&](double ab, double db, const double *du, const double *da, double *R) {
                          fg_tt_coeffs cc = *c;
@@ -1140,6 +1182,86 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
                          return tt_assemble_device(s, &cc, du, da, R, s->stream);
                      },
                      o, to, u, a, stats);
+}
+
+// host (reference element order) <-> bubble plane k (internal element position)
+static int bubble_plane_in(fg_system *s, int k, const double *h)
+{
+    const Topology &t = s->topo;
+    std::vector<double> v((size_t)s->nel_pad, 0.0);
+    for (int pos = 0; pos < t.nel; ++pos) v[pos] = h ? h[t.eorder[pos]] : 0.0;
+    FG_CUDA(cudaMemcpyAsync(s->bubble.as<double>() + (size_t)k * s->nel_pad, v.data(), 8 * (size_t)s->nel_pad,
+                            cudaMemcpyHostToDevice, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+static int bubble_planes_out(fg_system *s, int k0, int planes, double *h)
+{
+    const Topology &t = s->topo;
+    std::vector<double> v((size_t)planes * s->nel_pad);
+    FG_CUDA(cudaMemcpyAsync(v.data(), s->bubble.as<double>() + (size_t)k0 * s->nel_pad, 8 * v.size(),
+                            cudaMemcpyDeviceToHost, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    for (int pos = 0; pos < t.nel; ++pos)
+        for (int k = 0; k < planes; ++k) h[(size_t)planes * t.eorder[pos] + k] = v[(size_t)k * s->nel_pad + pos];
+    return FG_OK;
+}
+
+int fg_tt_bubble_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, const double *du, const double *uB,
+                          const double *duB, double *F, double *cond)
+{
+    if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = stage(s, s->state_a, 8 * (size_t)s->n_pad)) || (r = tt_bubble_alloc(s, s->stream))) return r;
+    if ((r = state_in(s, u, s->ws.t64.as<double>())) || (r = state_in(s, du, s->state_a.as<double>()))) return r;
+    if ((r = bubble_plane_in(s, 0, uB)) || (r = bubble_plane_in(s, 1, duB))) return r;
+    if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
+    if ((r = tt_mfdd_assemble_device(s, c, s->ws.t64.as<double>(), s->state_a.as<double>(), s->ws.u64.as<double>(),
+                                     s->stream)))
+        return r;
+    if (F && (r = vec_out(s, s->ws.u64.as<double>(), F, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    if (cond && (r = bubble_planes_out(s, 2, 5, cond))) return r;
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_tt_bubble_dab(fg_system *s, const double *Da, double *DaB)
+{
+    if (!s || !Da || !DaB) { set_error("NULL argument"); return FG_ERR_ARG; }
+    // the build's element scratch (Fe, 12 planes of nel_pad) receives DaB
+    if (!s->bubble.p || s->Fe.bytes < 8 * (size_t)s->nel_pad) {
+        set_error("no Predictor2 build on this system");
+        return FG_ERR_STATE;
+    }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = vec_in(s, Da, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
+    if ((r = tt_bubble_correct_device(s, s->ws.t64.as<double>(), 0.0, s->Fe.as<double>(), s->stream))) return r;
+    std::vector<double> v((size_t)s->nel_pad);
+    FG_CUDA(cudaMemcpyAsync(v.data(), s->Fe.p, 8 * v.size(), cudaMemcpyDeviceToHost, s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    for (int pos = 0; pos < s->topo.nel; ++pos) DaB[s->topo.eorder[pos]] = v[pos];
+    return FG_OK;
+}
+
+int fg_tt_bubble_state(fg_system *s, double *uB, double *aB)
+{
+    if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
+    if (!s->bubble.p) { set_error("no Predictor2 build on this system"); return FG_ERR_STATE; }
+    std::vector<double> v(2 * (size_t)s->topo.nel + 2);
+    int r = bubble_planes_out(s, 0, 2, v.data());
+    if (r) return r;
+    for (int e = 0; e < s->topo.nel; ++e) {
+        if (uB) uB[e] = v[2 * (size_t)e];
+        if (aB) aB[e] = v[2 * (size_t)e + 1];
+    }
+    return FG_OK;
 }
 
 }  // extern "C"

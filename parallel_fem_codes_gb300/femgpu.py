@@ -21,7 +21,7 @@ FG_SCALE_LEFT, FG_SCALE_LEFTRIGHT, FG_SCALE_BLOCK = 1, 2, 3
 FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED, FG_PREC_MIXED16 = 64, 32, 16
-FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 = 0, 1, 2
+FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2, FG_TIME_PREDICTOR2 = 0, 1, 2, 3
 FG_NS_SUPG_PSPG, FG_NS_VMS_DCDD = 0, 1
 FG_TRANSPORT_SUPG, FG_TRANSPORT_DD = 0, 1
 FG_EULER_SUPG, FG_EULER_DD = 0, 1
@@ -199,6 +199,9 @@ def lib(build_if_missing: bool = True):
     L.fg_scale.argtypes = [_vp, _c_int, _vp]
     L.fg_unscale.argtypes = [_vp, _vp]
     L.fg_tt_assemble.argtypes = [_vp, ctypes.POINTER(TTCoeffs), _vp, _vp, _vp]
+    L.fg_tt_bubble_assemble.argtypes = [_vp, ctypes.POINTER(TTCoeffs), _vp, _vp, _vp, _vp, _vp, _vp]
+    L.fg_tt_bubble_dab.argtypes = [_vp, _vp, _vp]
+    L.fg_tt_bubble_state.argtypes = [_vp, _vp, _vp]
     L.fg_tt_predictor.argtypes = [_vp, ctypes.POINTER(TTCoeffs), ctypes.POINTER(SolverOpts),
                                   ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
     L.fg_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerOpts)]
@@ -531,6 +534,36 @@ class System:
         dd = None if du is None else np.ascontiguousarray(du, dtype=np.float64)
         check(lib().fg_tt_assemble(self._h, ctypes.byref(c), _ptr(uu), _ptr(dd), R.ctypes.data))
         return R
+
+    def tt_bubble_assemble(self, prob, alpha, dt, u=None, du=None, uB=None, duB=None):
+        """Build_M_F_DD ("Predictor2", form DD) at (u, du) and the bubble
+        unknowns (uB, duB: one per element, reference order) with a fresh
+        shock-capture state; returns (F[n+1], cond[nel, 5] = invN2, R2,
+        M2[0..2]); the blocks stay on the device."""
+        c = tt_coeffs(prob, alpha, dt)
+        nel = self.mesh.nel
+        F = np.empty(self.n + 1)
+        cond = np.empty(5 * max(nel, 1))
+        arr = [None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in (u, du, uB, duB)]
+        check(lib().fg_tt_bubble_assemble(self._h, ctypes.byref(c), *[_ptr(v) for v in arr], F.ctypes.data,
+                                          cond.ctypes.data))
+        return F, cond[: 5 * nel].reshape(nel, 5)
+
+    def tt_bubble_dab(self, Da):
+        """calculate_DaB after the last Predictor2 build: DaB (nel) from Da (n+1)."""
+        Da = np.ascontiguousarray(Da, dtype=np.float64)
+        if Da.shape != (self.n + 1,):
+            raise ValueError("Da needs n + 1 entries")
+        DaB = np.empty(max(self.mesh.nel, 1))
+        check(lib().fg_tt_bubble_dab(self._h, Da.ctypes.data, DaB.ctypes.data))
+        return DaB[: self.mesh.nel]
+
+    def tt_bubble_state(self):
+        """(uB, aB) after tt_predictor with FG_TIME_PREDICTOR2."""
+        nel = self.mesh.nel
+        uB, aB = np.empty(max(nel, 1)), np.empty(max(nel, 1))
+        check(lib().fg_tt_bubble_state(self._h, uB.ctypes.data, aB.ctypes.data))
+        return uB[:nel], aB[:nel]
 
     def tt_predictor(self, prob, alpha, dt, topts, u0=None, kmax=30, lmax=1000, tol=1e-10,
                      precision=FG_PREC_FP64, inner_tol=0.0):

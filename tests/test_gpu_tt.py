@@ -3,7 +3,10 @@ fg_tt_predictor) against the CPU restatement (oracle/tt.c): blocks
 Ae = me + alpha dt ke and the residual R = F - me du - ke u are
 bit-identical (same terms, same element-order accumulation, no FMA
 contraction); the Predictor_Old loop with accumulating Diag reaches the
-oracle's states to rel-L2 1e-8 at tol 1e-10, in FP64 and mixed precision."""
+oracle's states to rel-L2 1e-8 at tol 1e-10, in FP64 and mixed precision.
+"Predictor2" (fg_tt_bubble_assemble, FG_TIME_PREDICTOR2): the bubble
+build, its condensation data and calculate_DaB bit-identical, the loop's
+u and bubble unknowns to 1e-8."""
 import numpy as np
 import pytest
 
@@ -141,3 +144,64 @@ def test_tt_yzbeta_dd_predictor(fg):
     assert st["steps"] == sto["steps"] == 6
     assert st["corrections"] == sto["corrections"]
     assert rel(ug, uo) < 1e-8
+
+
+# ---- TimeIntegration "Predictor2" with the DD form (Build_M_F_DD.c,
+# calculate_DaB.c, Predictor_New.c): one bubble unknown per element ----
+
+@pytest.mark.parametrize("n,cau,hs,reorder", [(17, 2, 0, True), (33, 3, 2, True), (33, 2, 1, False)])
+def test_tt_predictor2_build_bit_exact(fg, n, cau, hs, reorder):
+    """Me, the load, the condensation data and calculate_DaB's increments
+    bit-identical with the oracle (itself bit-identical with the
+    reference's own functions, tests/test_oracle_tt.py)."""
+    p = G.transport_problem(n, angle_deg=35.0, k=1e-3, gamma=0.2, f=0.5, cau=cau)
+    p.form, p.h_shock = fg.FG_TRANSPORT_DD, hs
+    m = p.mesh
+    rng = np.random.default_rng(n + cau)
+    u, du = rng.random(m.neq), rng.standard_normal(m.neq)
+    uB, duB = rng.random(m.nel), rng.standard_normal(m.nel)
+    A0, F0, c0 = O.build_tt_mfdd(p, 0.5, 0.05, u, du, uB, duB)
+    s = fg.transport_system(p, reorder=reorder)
+    F, cond = s.tt_bubble_assemble(p, 0.5, 0.05, u, du, uB, duB)
+    assert np.array_equal(F[:-1], F0[:-1]) and F[-1] == 0.0
+    assert np.array_equal(cond, c0)
+    assert np.array_equal(s.get_blocks(), A0)
+    Da = np.append(rng.standard_normal(m.neq), 0.0)
+    assert np.array_equal(s.tt_bubble_dab(Da), O.tt_dab(O.fill_lm(m), c0, Da))
+
+
+@pytest.mark.parametrize("cau", [2, 3], ids=["caudd", "yzbeta"])
+def test_tt_predictor2_loop(fg, cau):
+    """The Predictor_New loop on the device (state, bubble unknowns and
+    shock-capture state resident) against the oracle's loop: u and uB to
+    rel-L2 1e-8, a and aB to 1e-6, same steps and corrections."""
+    p = G.transport_problem(33, angle_deg=30.0, k=1e-3, f=0.0, cau=cau)
+    p.form = fg.FG_TRANSPORT_DD
+    to_o = O.TimeOpts(0, 2, 1e-3, 0, 6 * 0.02, 1e-6, 0, 0)
+    uo, ao, uBo, aBo, sto = O.tt_predictor2(p, 0.5, 0.02, to_o, tol=1e-10, kmax=30)
+    s = fg.transport_system(p)
+    to = fg.time_opts(0, 2, 1e-3, 0, 6 * 0.02, 1e-6, precond=fg.FG_PRECOND_DIAG, setup_flags=0,
+                      scheme=fg.FG_TIME_PREDICTOR2)
+    ug, ag, st = s.tt_predictor(p, 0.5, 0.02, to, kmax=30, tol=1e-10)
+    uB, aB = s.tt_bubble_state()
+    assert st["steps"] == sto["steps"] == 6
+    assert st["corrections"] == sto["corrections"]
+    assert rel(ug, uo) < 1e-8 and rel(uB, uBo) < 1e-8
+    assert rel(ag, ao) < 1e-6 and rel(aB, aBo) < 1e-6
+
+
+def test_tt_predictor2_needs_dd(fg):
+    """Predictor2 exists for the DD form only (setStabilizationForm.c:51-54);
+    the Euler loop has no bubble build here."""
+    p = G.transport_problem(9, angle_deg=30.0, k=1e-3)
+    s = fg.transport_system(p)
+    to = fg.time_opts(0, 1, 1e-3, 0, 0.02, 1e-6, precond=fg.FG_PRECOND_DIAG, setup_flags=0,
+                      scheme=fg.FG_TIME_PREDICTOR2)
+    with pytest.raises(fg.FemGpuError) as e:
+        s.tt_predictor(p, 0.5, 0.02, to)
+    assert e.value.code == fg.FG_ERR_UNSUPPORTED
+    ep = G.obliquo_problem(9)
+    se = fg.euler_system(ep)
+    with pytest.raises(fg.FemGpuError) as e:
+        se.euler_predictor(ep, fg.time_opts(0, 1, 1e-3, 0, ep.dt, 1e-6, max_steps=1, scheme=fg.FG_TIME_PREDICTOR2))
+    assert e.value.code == fg.FG_ERR_UNSUPPORTED
