@@ -14,6 +14,11 @@
  * (the file is not linked: it pulls in the time-integration loops);
  * setProblem is supplied here, the same synthetic problem as the steady
  * harness.  Used only by tests.
+ *
+ * "Predictor2" (fr_tt_mfdd_build, fr_tt_predictor2): Build_M_F_DD.c and
+ * calculate_DaB.c, and the reference's own Predictor_New loop with its
+ * Criteria, pgmres, ebemv and Diag preconditioner compiled from the same
+ * private copy.
  */
 #include "TranspEquation.h"
 
