@@ -436,6 +436,8 @@ typedef struct {
                           "Predictor1", "CAUDD"); its per-element state (the
                           bubble values and the relaxed delta) stays on the
                           device and is zeroed when fg_euler_predictor starts */
+    double invY[4];    /* Parameters->invY: the scaling of the YZBeta shock
+                          capture that "Predictor2" uses (FG_TIME_PREDICTOR2)   */
 } fg_euler_coeffs;
 enum { FG_EULER_SUPG = 0, FG_EULER_DD = 1 };
 
@@ -460,7 +462,8 @@ typedef struct {
                               SPIKE on a system switched to FG_OP_CSR            */
     int setup_flags;       /* FG_SETUP_REF_QUIRKS: the reference's 4x4 inverse     */
     int scheme;            /* FG_TIME_PREDICTOR (0), FG_TIME_BDF, FG_TIME_TRBDF2,
-                              FG_TIME_PREDICTOR2 (transient transport DD only)   */
+                              FG_TIME_PREDICTOR2 (the DD forms of the transient
+                              transport and Euler builds)                     */
 } fg_time_opts;
 
 /* TimeIntegration of the drivers (setStabilizationForm.c):
@@ -478,10 +481,11 @@ typedef struct {
  *                      (Predictor_Old_TRBDF2.c) solves against a right-hand
  *                      side that nothing fills and is not restated.
  *   FG_TIME_PREDICTOR2 "Predictor2"        Predictor_New.c:3-179 with the
- *                      transient transport DD form (fg_tt_predictor only):
- *                      Predictor_Old's steps plus one bubble unknown per
- *                      element, predicted with u (uB += (1 - alpha) dt aB,
- *                      aB = 0) and corrected after each solve from Da
+ *                      DD form (fg_tt_predictor: one bubble unknown per
+ *                      element; fg_euler_predictor: four, with YZBeta):
+ *                      Predictor_Old's steps plus the bubble unknowns,
+ *                      predicted with u (uB += (1 - alpha) dt aB, aB = 0)
+ *                      and corrected after each solve from Da
  *                      (calculate_DaB: aB += DaB, uB += alpha dt DaB). */
 enum { FG_TIME_PREDICTOR = 0, FG_TIME_BDF = 1, FG_TIME_TRBDF2 = 2, FG_TIME_PREDICTOR2 = 3 };
 
@@ -503,6 +507,23 @@ typedef struct {
  * receives du/dt.  The state stays on the device for the whole loop. */
 int fg_euler_predictor(fg_system *s, const fg_euler_coeffs *c, const fg_solver_opts *opts,
                        const fg_time_opts *t, double *u, double *a, fg_time_stats *stats);
+/* TimeIntegration "Predictor2" of the Euler driver (t->scheme
+ * FG_TIME_PREDICTOR2 with c.form FG_EULER_DD; ShockCapture "YZBeta" with
+ * c.invY): each correction builds with Build_M_F_DD_Transiente.c:6-821 --
+ * four bubble unknowns per element kept and condensed out of the element
+ * system, Delta_YZBeta for the DD diffusion and Delta_YZBetaNMV (relaxed,
+ * state on the device) for the bubble stiffness -- and recovers the bubble
+ * increments from Da (calculate_DaB.c:3-61).  With "CAUDD" the reference
+ * passes an A0 it never computes to Delta_DD (:137-138), an undefined
+ * result, so that combination is not offered.
+ *
+ * One build at (u, du, uB, duB) with fresh shock-capture states (u, du:
+ * free dofs, reference numbering; uB, duB: 4 per element, reference element
+ * order; NULL = 0).  F (host, n+1, may be NULL) receives the load, cond
+ * (host, 53 per element, may be NULL) invN2, R2[4], M2[4][12]; the blocks
+ * stay on the device (fg_get_blocks). */
+int fg_euler_bubble_assemble(fg_system *s, const fg_euler_coeffs *c, const double *u, const double *du,
+                             const double *uB, const double *duB, double *F, double *cond);
 
 /* ---- transient SUPG/CAU transport (02_Transport_Equation) ----
  * Replaces Build_M_K_R_SUPG.c:6-252 (with CAU_ShockCapture.c:3-33,
@@ -544,12 +565,14 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
  * the device (fg_get_blocks). */
 int fg_tt_bubble_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, const double *du, const double *uB,
                           const double *duB, double *F, double *cond);
-/* calculate_DaB after the last Predictor2 build: DaB (host, nel) from Da
- * (host, n+1, reference numbering; its sink entry is read as 0). */
-int fg_tt_bubble_dab(fg_system *s, const double *Da, double *DaB);
-/* The bubble unknowns uB and aB (host, nel each, reference element order,
- * either may be NULL) after fg_tt_predictor with FG_TIME_PREDICTOR2. */
-int fg_tt_bubble_state(fg_system *s, double *uB, double *aB);
+/* calculate_DaB after the last Predictor2 build (transient transport or
+ * Euler): DaB (host; nb = 1 or 4 values per element, element-major in
+ * reference element order) from Da (host, n+1, reference numbering; its
+ * sink entry is read as 0). */
+int fg_bubble_dab(fg_system *s, const double *Da, double *DaB);
+/* The bubble unknowns uB and aB (host, nb per element as above, either may
+ * be NULL) after a Predictor2 loop (FG_TIME_PREDICTOR2). */
+int fg_bubble_state(fg_system *s, double *uB, double *aB);
 
 /* ---- request server: continuous batching of transport solves ----
  * A worker thread owns one batch.  Requests (a system whose geometry is set,

@@ -492,3 +492,281 @@ int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, co
     free(lm); free(Id); free(A); free(R); free(bd); free(inv); free(state);
     return steps;
 }
+
+/* ---- TimeIntegration "Predictor2" with StabilizationForm "DD" and
+ * ShockCapture "YZBeta" (setStabilizationForm.c:51-53, 64-66):
+ * Build_M_F_DD_Transiente.c:6-821 keeps the four bubble unknowns of each
+ * element (uB, duB) and condenses them out of the element system,
+ * calculate_DaB.c:3-61 recovers their increments from Da, and
+ * Predictor_New.c predicts and corrects them with u and a.  The build
+ * passes an A0 it never computes to the shock capture (:137-138): with
+ * "CAUDD" (Delta_DD, which reads A0) the result is undefined, so only
+ * "YZBeta" (Delta_YZBeta, which does not) is restated.  The
+ * no-penetrability adjustment (BC_no_penetrability) is the identity for
+ * every problem but CYLINDER and NACA0012 (set_BC_no_penetrability.c). ---- */
+
+/* Delta_YZBeta.c:4-104 (nmv = 0: 0.5 (delta1 + delta2), no state) or
+ * Delta_YZBetaNMV.c:4-93 (nmv = 1: 0.5 delta1 relaxed against the element's
+ * previous value with w = 1/2, the relaxed value kept; its pow(x, 1) is x) */
+static double eu_delta_yz(const double invY[4], const double gx[4], const double gy[4], double Ax[4][4],
+                          double Ay[4][4], const double dUb[4], const double b[3], const double c[3], double twoArea,
+                          const double Ub[4], int nmv, double *old)
+{
+    double Agx[4], Agy[4], Z[4];
+    Agx[0] = gx[1];
+    Agx[1] = Ax[1][0] * gx[0] + Ax[1][1] * gx[1] + Ax[1][2] * gx[2] + Ax[1][3] * gx[3];
+    Agx[2] = Ax[2][0] * gx[0] + Ax[2][1] * gx[1] + Ax[2][2] * gx[2];
+    Agx[3] = Ax[3][0] * gx[0] + Ax[3][1] * gx[1] + Ax[3][2] * gx[2] + Ax[3][3] * gx[3];
+    Agy[0] = gy[2];
+    Agy[1] = Ay[1][0] * gy[0] + Ay[1][1] * gy[1] + Ay[1][2] * gy[2];
+    Agy[2] = Ay[2][0] * gy[0] + Ay[2][1] * gy[1] + Ay[2][2] * gy[2] + Ay[2][3] * gy[3];
+    Agy[3] = Ay[3][0] * gy[0] + Ay[3][1] * gy[1] + Ay[3][2] * gy[2] + Ay[3][3] * gy[3];
+    for (int i = 0; i < 4; i++) Z[i] = dUb[i] + Agx[i] + Agy[i];
+    double nYZ = sqrt(invY[0] * Z[0] * invY[0] * Z[0] + invY[1] * Z[1] * invY[1] * Z[1] +
+                      invY[2] * Z[2] * invY[2] * Z[2] + invY[3] * Z[3] * invY[3] * Z[3]);
+    double nx = invY[0] * gx[0] * invY[0] * gx[0] + invY[1] * gx[1] * invY[1] * gx[1] +
+                invY[2] * gx[2] * invY[2] * gx[2] + invY[3] * gx[3] * invY[3] * gx[3];
+    double ny = invY[0] * gy[0] * invY[0] * gy[0] + invY[1] * gy[1] * invY[1] * gy[1] +
+                invY[2] * gy[2] * invY[2] * gy[2] + invY[3] * gy[3] * invY[3] * gy[3];
+    double sum = nx + ny;
+    double nYU = sqrt(invY[0] * Ub[0] * invY[0] * Ub[0] + invY[1] * Ub[1] * invY[1] * Ub[1] +
+                      invY[2] * Ub[2] * invY[2] * Ub[2] + invY[3] * Ub[3] * invY[3] * Ub[3]);
+    double ngr = sqrt(gx[0] * gx[0] + gy[0] * gy[0]), J1, J2;
+    if (fabs(ngr) >= 1e-12) {
+        J1 = gx[0] / ngr;
+        J2 = gy[0] / ngr;
+    } else {
+        J1 = J2 = 0.0;
+    }
+    double H = (fabs(J1 * b[0] + J2 * c[0]) + fabs(J1 * b[1] + J2 * c[1]) + fabs(J1 * b[2] + J2 * c[2])) / twoArea;
+    H = fabs(H) >= 1e-12 ? 2.0 * (1.0 / H) : 0.0;
+    double as = fabs(sum) >= 1e-12 ? 1.0 / sqrt(sum) : 0.0;
+    double au = fabs(nYU) >= 1e-12 ? 1.0 : 0.0;
+    double d1 = nYZ * as * au * (H * 0.5);
+    if (nmv) {
+        double w = 0.5;
+        double d = w * (0.5 * d1) + (1 - w) * (*old);
+        *old = d;
+        return d;
+    }
+    double as2 = fabs(sum) >= 1e-12 ? 1.0 : 0.0;
+    double au2 = fabs(nYU) >= 1e-12 ? 1.0 / nYU : 0.0;
+    double d2 = nYZ * as2 * au2 * (H * 0.5 * H * 0.5);
+    return 0.5 * (d1 + d2);
+}
+
+/* Build_M_F_DD_Transiente.c:43-810 for one element.  Me is formed from the
+ * matrices before the (identity) no-penetrability adjustment, as there. */
+static void eu_mfdd_element(const or_euler_problem *pb, const double X[3], const double Y[3], const double Ue[12],
+                            const double dUe[12], const double uB[4], const double duB[4], double *old_nmv,
+                            double Me[144], double Fe[12], double cond[53])
+{
+    static const double ones[4] = {1.0, 1.0, 1.0, 1.0};
+    const double *invY = pb->invY ? pb->invY : ones;
+    const double third = 1.0 / 3.0, sixth = 1.0 / 6.0, nf = 9.0 / 40.0;
+    double b[3] = {Y[1] - Y[2], Y[2] - Y[0], Y[0] - Y[1]};
+    double c[3] = {X[2] - X[1], X[0] - X[2], X[1] - X[0]};
+    double twoArea = fabs(c[2] * b[1] - c[1] * b[2]);
+    double Area = 0.5 * twoArea;
+    double Ub[4], dUb[4], gx[4], gy[4];
+    int i, j, r, q, k;
+    for (i = 0; i < 4; i++) {
+        Ub[i] = (Ue[i] + Ue[i + 4] + Ue[i + 8]) * third;
+        dUb[i] = (dUe[i] + dUe[i + 4] + dUe[i + 8]) * third;
+    }
+    for (i = 0; i < 4; i++) {
+        gx[i] = (Ue[i] * b[0] + Ue[i + 4] * b[1] + Ue[i + 8] * b[2]) / twoArea;
+        gy[i] = (Ue[i] * c[0] + Ue[i + 4] * c[1] + Ue[i + 8] * c[2]) / twoArea;
+    }
+    double Ax[4][4], Ay[4][4];
+    eu_jacobians(pb->gamma, pb->mach, pb->dimensionless, Ub, Ax, Ay);
+    double delta = eu_delta_yz(invY, gx, gy, Ax, Ay, dUb, b, c, twoArea, Ub, 0, NULL);
+    double K[3][4][4];
+    for (j = 0; j < 3; j++)
+        for (r = 0; r < 4; r++)
+            for (q = 0; q < 4; q++) K[j][r][q] = b[j] * Ax[r][q] + c[j] * Ay[r][q];
+    double Mhh1 = Area * sixth, Mhh2 = Area / 12.0, MhB = (3.0 * Area) / 20.0, MBB = (81.0 * Area) / 280.0;
+    double d4a = delta / (4.0 * Area);
+    double p[3] = {nf * (b[0] + 2.0 * b[1] + 2.0 * b[2]), nf * (2.0 * b[0] + b[1] + 2.0 * b[2]),
+                   nf * (2.0 * b[0] + 2.0 * b[1] + b[2])};
+    double pq[3] = {nf * (c[0] + 2.0 * c[1] + 2.0 * c[2]), nf * (2.0 * c[0] + c[1] + 2.0 * c[2]),
+                    nf * (2.0 * c[0] + 2.0 * c[1] + c[2])};
+    double KhB[12][4], KBh[4][12], Khhg[4][12];
+    for (i = 0; i < 3; i++)
+        for (r = 0; r < 4; r++)
+            for (q = 0; q < 4; q++) {
+                KhB[4 * i + r][q] = p[i] * Ax[r][q] + pq[i] * Ay[r][q];
+                KBh[r][4 * i + q] = nf * K[i][r][q];
+                Khhg[r][4 * i + q] = K[i][r][q] * sixth;
+            }
+    double dnmv = eu_delta_yz(invY, gx, gy, Ax, Ay, dUb, b, c, twoArea, Ub, 1, old_nmv);
+    double S = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[0] * b[1] + b[0] * b[2] + b[1] * b[2] + c[0] * c[0] +
+               c[1] * c[1] + c[2] * c[2] + c[0] * c[1] + c[0] * c[2] + c[1] * c[2];
+    double KBB = (81.0 * dnmv * S) / (40.0 * Area);
+    double adt = pb->alpha * pb->dt;
+    double M1[12][12], N1[12][4], M2[4][12];
+    for (i = 0; i < 3; i++)
+        for (j = 0; j < 3; j++) {
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            double dd = d4a * (b[lo] * b[hi] + c[lo] * c[hi]);
+            double mhh = i == j ? Mhh1 : Mhh2;
+            for (r = 0; r < 4; r++)
+                for (q = 0; q < 4; q++) {
+                    double kg = Khhg[r][4 * j + q];
+                    M1[4 * i + r][4 * j + q] = r == q ? mhh + adt * (kg + dd) : adt * kg;
+                }
+        }
+    for (i = 0; i < 12; i++)
+        for (q = 0; q < 4; q++) N1[i][q] = (i & 3) == q ? MhB + adt * KhB[i][q] : adt * KhB[i][q];
+    for (r = 0; r < 4; r++)
+        for (j = 0; j < 12; j++) M2[r][j] = (j & 3) == r ? MhB + adt * KBh[r][j] : adt * KBh[r][j];
+    double invN2 = 1.0 / (MBB + adt * KBB);
+    for (i = 0; i < 12; i++)                  /* :692-701 */
+        for (j = 0; j < 12; j++) {
+            double soma = 0.0;
+            for (k = 0; k < 4; k++) soma += N1[i][k] * M2[k][j];
+            Me[12 * i + j] = M1[i][j] - invN2 * soma;
+        }
+    double R1[12], R2[4];
+    for (i = 0; i < 3; i++)                   /* :719-760 */
+        for (r = 0; r < 4; r++) {
+            const int row = 4 * i + r;
+            R1[row] = -MhB * duB[r] - (KhB[row][0] * uB[0] + KhB[row][1] * uB[1] + KhB[row][2] * uB[2] +
+                                       KhB[row][3] * uB[3]);
+            double kh = 0.0;
+            for (int col = 0; col < 12; col++) {
+                const int jb = col >> 2;
+                const int lo = i < jb ? i : jb, hi = i < jb ? jb : i;
+                double coef = Khhg[r][col];
+                if ((col & 3) == r) coef = d4a * (b[lo] * b[hi] + c[lo] * c[hi]) + coef;
+                kh = col == 0 ? coef * Ue[0] : kh + coef * Ue[col];
+            }
+            double m = (i == 0 ? Mhh1 : Mhh2) * dUe[r] + (i == 1 ? Mhh1 : Mhh2) * dUe[4 + r] +
+                       (i == 2 ? Mhh1 : Mhh2) * dUe[8 + r];
+            R1[row] += -m - kh;
+        }
+    for (r = 0; r < 4; r++) {                 /* :764-781 */
+        R2[r] = -MBB * duB[r] - KBB * uB[r];
+        double kb = KBh[r][0] * Ue[0];
+        for (int col = 1; col < 12; col++) kb += KBh[r][col] * Ue[col];
+        R2[r] += -(MhB * dUe[r] + MhB * dUe[4 + r] + MhB * dUe[8 + r]) - kb;
+    }
+    for (i = 0; i < 12; i++)                  /* :789-790 */
+        Fe[i] = R1[i] - invN2 * (N1[i][0] * R2[0] + N1[i][1] * R2[1] + N1[i][2] * R2[2] + N1[i][3] * R2[3]);
+    cond[0] = invN2;
+    for (r = 0; r < 4; r++) cond[1 + r] = R2[r];
+    for (r = 0; r < 4; r++)
+        for (j = 0; j < 12; j++) cond[5 + 12 * r + j] = M2[r][j];
+}
+
+void or_build_euler_mfdd(int nnodes, int nel, const double *x, const double *y, const int *type,
+                         const int *invp, const int *ien, int neq, const or_euler_problem *prob,
+                         const double *u, const double *du, const double *uB, const double *duB, double *dnmv,
+                         double *A, double *F, double *cond)
+{
+    int E, v, k, NEQ = neq;
+    size_t nn = (size_t)(nnodes ? nnodes : 1);
+    double *U = malloc(sizeof(double) * 4 * nn), *dU = malloc(sizeof(double) * 4 * nn), *own = NULL;
+    for (v = 0; v < nnodes; v++)              /* eval_U_dU.c:3-59 */
+        for (k = 0; k < 4; k++) {
+            long d = 4L * v + k;
+            if (type[d] > 0) { U[d] = u[invp[d]]; dU[d] = du[invp[d]]; }
+            else { U[d] = prob->upresc[d]; dU[d] = 0.0; }
+        }
+    if (!dnmv) dnmv = own = calloc((size_t)(nel ? nel : 1), sizeof(double));
+    memset(F, 0, sizeof(double) * ((size_t)NEQ + 1));
+    for (E = 0; E < nel; E++) {
+        double X[3], Y[3], Ue[12], dUe[12], Fe[12];
+        int lm[12];
+        for (v = 0; v < 3; v++) {
+            int J = ien[3 * E + v];
+            X[v] = x[J]; Y[v] = y[J];
+            for (k = 0; k < 4; k++) {
+                long d = 4L * J + k;
+                Ue[4 * v + k] = U[d];
+                dUe[4 * v + k] = dU[d];
+                lm[4 * v + k] = type[d] == 0 ? NEQ : invp[d];
+            }
+        }
+        eu_mfdd_element(prob, X, Y, Ue, dUe, uB + 4L * E, duB + 4L * E, dnmv + E, A + 144L * E, Fe, cond + 53L * E);
+        for (k = 0; k < 12; k++) F[lm[k]] += Fe[k];
+        F[NEQ] = 0;
+    }
+    free(U); free(dU); free(own);
+}
+
+void or_euler_dab(int nel, const int *lm, int NEQ, const double *cond, double *Da, double *DaB)
+{
+    Da[NEQ] = 0.0;                            /* calculate_DaB.c:18-57 */
+    for (int e = 0; e < nel; e++) {
+        const double *cd = cond + 53L * e;
+        const int *l = lm + 12L * e;
+        for (int r = 0; r < 4; r++) {
+            const double *m = cd + 5 + 12 * r;
+            double s = m[0] * Da[l[0]];
+            for (int j = 1; j < 12; j++) s += m[j] * Da[l[j]];
+            DaB[4L * e + r] = cd[0] * (cd[1 + r] - s);
+        }
+    }
+}
+
+typedef struct {
+    eu_loop base;
+    double *uB, *aB, *cond, *DaB, *dnmv;
+    int *lm12;
+} eu_loop2;
+
+static void eu_predict2(void *p, double coef)
+{
+    eu_loop2 *c = (eu_loop2 *)p;
+    size_t m = 4 * (size_t)c->base.nel;
+    for (size_t i = 0; i < m; i++) c->uB[i] += coef * c->aB[i];      /* Predictor_New.c:82-83 */
+    memset(c->aB, 0, sizeof(double) * m);
+}
+
+static int eu_correct2(void *p, double alpha_b, double dt_b, const double *u, const double *a, double *Da, int *gi)
+{
+    eu_loop2 *c = (eu_loop2 *)p;
+    eu_loop *b = &c->base;
+    or_euler_problem pb = *b->prob;
+    pb.alpha = alpha_b;
+    pb.dt = dt_b;
+    or_build_euler_mfdd(b->nnodes, b->nel, b->x, b->y, b->type, b->invp, b->ien, b->neq, &pb, u, a, c->uB, c->aB,
+                        c->dnmv, (double *)b->mv.A, b->R, c->cond);
+    or_blockdiag_setup(b->nnodes, b->nel, 4, b->ien, b->mv.A, b->mv.Id, b->neq, 1, b->bd, (double *)b->mv.inv, b->R);
+    or_pgmres(b->neq, b->kmax, b->lmax, b->solver_tol, eu_mv_cb, eu_pc_cb, &b->mv, b->R, Da, gi);
+    or_euler_dab(b->nel, c->lm12, b->neq, c->cond, Da, c->DaB);      /* :99 */
+    const double coef = alpha_b * dt_b;
+    size_t m = 4 * (size_t)b->nel;
+    for (size_t i = 0; i < m; i++) {                                  /* :104-105 */
+        c->aB[i] += c->DaB[i];
+        c->uB[i] += coef * c->DaB[i];
+    }
+    return 0;
+}
+
+int or_euler_predictor2(int nnodes, int nel, const double *x, const double *y, const int *type,
+                        const int *invp, const int *ien, int neq, const or_euler_problem *prob,
+                        const or_time_opts *to, double solver_tol, int kmax, int lmax,
+                        double *u, double *a, double *uB, double *aB, or_time_stats *st)
+{
+    int NEQ = neq, i;
+    size_t ne = (size_t)(nel ? nel : 1), nn = (size_t)(nnodes ? nnodes : 1);
+    int *lm = malloc(sizeof(int) * 12 * ne), *Id = malloc(sizeof(int) * 4 * nn);
+    double *A = malloc(sizeof(double) * 144 * ne);
+    double *R = calloc((size_t)NEQ + 1, sizeof(double));
+    double *bd = malloc(sizeof(double) * 16 * nn), *inv = malloc(sizeof(double) * 16 * nn);
+    double *cond = calloc(53 * ne, sizeof(double)), *DaB = calloc(4 * ne, sizeof(double));
+    double *dnmv = calloc(ne, sizeof(double));
+    or_fill_lm(nel, 4, ien, type, invp, NEQ, lm);
+    for (i = 0; i < 4 * nnodes; i++) Id[i] = type[i] == 0 ? NEQ : invp[i];
+    memset(uB, 0, sizeof(double) * 4 * ne);  /* Predictor_New.c:24,36 calloc uB and aB */
+    memset(aB, 0, sizeof(double) * 4 * ne);
+    or_time_opts t2 = *to;
+    t2.scheme = OR_TIME_PREDICTOR;
+    eu_loop2 c = { { { nel, nnodes, NEQ, lm, Id, A, inv }, nnodes, nel, neq, x, y, type, invp, ien, prob, R, bd,
+                     solver_tol, kmax, lmax }, uB, aB, cond, DaB, dnmv, lm };
+    int steps = or_time_integrate_ex(neq, prob->alpha, prob->dt, &t2, eu_correct2, eu_predict2, &c, u, a, st);
+    free(lm); free(Id); free(A); free(R); free(bd); free(inv); free(cond); free(DaB); free(dnmv);
+    return steps;
+}

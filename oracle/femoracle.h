@@ -191,6 +191,7 @@ typedef struct {
     const double *upresc;  /* [4*nnodes] prescribed rho, rho u, rho v, rho E           */
     int form;              /* 0: SUPG + CAU, 1: DD (Build_M_K_F_DD_Transiente + Delta_DD) */
     double *uB, *delta_old;/* DD state: [4*nel] bubbles, [nel] delta (NULL: fresh zeros) */
+    const double *invY;    /* [4] Parameters->invY of YZBeta (NULL: 1, 1, 1, 1)        */
 } or_euler_problem;
 
 /* Build_M_K_F_SUPG + Delta_CAU + eval_U_dU + ebe_assembly: A receives the
@@ -199,6 +200,19 @@ typedef struct {
 void or_build_euler(int nnodes, int nel, const double *x, const double *y, const int *type,
                     const int *invp, const int *ien, int neq, const or_euler_problem *prob,
                     const double *u, const double *du, double *A, double *R);
+
+/* TimeIntegration "Predictor2" with StabilizationForm "DD" and ShockCapture
+ * "YZBeta": Build_M_F_DD_Transiente (four bubble unknowns per element kept,
+ * uB and duB [4*nel], condensed out with N2 = MBB + alpha dt KBB), Me into
+ * A (144 per element), the load into F (NEQ + 1, sink 0), cond (invN2, R2[4],
+ * M2[4][12]: 53 per element).  dnmv [nel] is Delta_YZBetaNMV's relaxed
+ * state (NULL: fresh zeros). */
+void or_build_euler_mfdd(int nnodes, int nel, const double *x, const double *y, const int *type,
+                         const int *invp, const int *ien, int neq, const or_euler_problem *prob,
+                         const double *u, const double *du, const double *uB, const double *duB, double *dnmv,
+                         double *A, double *F, double *cond);
+/* calculate_DaB of the Euler driver: Da[NEQ] = 0, DaB (4 per element) */
+void or_euler_dab(int nel, const int *lm, int NEQ, const double *cond, double *Da, double *DaB);
 
 /* Stop tests of 00_CommonFiles/Time_Integration/Criteria.c */
 typedef struct {
@@ -244,6 +258,13 @@ int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, co
                        const int *invp, const int *ien, int neq, const or_euler_problem *prob,
                        const or_time_opts *to, double solver_tol, int kmax, int lmax,
                        double *u, double *a, or_time_stats *st);
+/* Predictor_New with Build_M_F_DD_Transiente, calculate_DaB, BlockDiag (the
+ * reference's 4x4 inverse) and GMRES.  u: initial state in, final out; a
+ * (neq), uB, aB (4 nel) receive the final du/dt and bubble unknowns. */
+int or_euler_predictor2(int nnodes, int nel, const double *x, const double *y, const int *type,
+                        const int *invp, const int *ien, int neq, const or_euler_problem *prob,
+                        const or_time_opts *to, double solver_tol, int kmax, int lmax,
+                        double *u, double *a, double *uB, double *aB, or_time_stats *st);
 
 /* ---- transient SUPG/CAU transport (02_Transport_Equation, oracle/tt.c) ----
  * Build_M_K_R_SUPG: A receives Ae = me + alpha dt ke (9 per element), R the

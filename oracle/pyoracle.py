@@ -123,6 +123,15 @@ def lib():
         L.or_build_euler.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
                                      ctypes.c_void_p, _f64p, _f64p, _f64p, _f64p]
         L.or_build_euler.restype = None
+        L.or_build_euler_mfdd.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                          ctypes.c_void_p, _f64p, _f64p, _f64p, _f64p, ctypes.c_void_p,
+                                          _f64p, _f64p, _f64p]
+        L.or_build_euler_mfdd.restype = None
+        L.or_euler_dab.argtypes = [_c_int, _i32p, _c_int, _f64p, _f64p, _f64p]
+        L.or_euler_dab.restype = None
+        L.or_euler_predictor2.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
+                                          ctypes.c_void_p, ctypes.c_void_p, _c_dbl, _c_int, _c_int,
+                                          _f64p, _f64p, _f64p, _f64p, ctypes.c_void_p]
         L.or_euler_predictor.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int,
                                          ctypes.c_void_p, ctypes.c_void_p, _c_dbl, _c_int, _c_int,
                                          _f64p, _f64p, ctypes.c_void_p]
@@ -260,6 +269,12 @@ def _setup_eu(R):
         R.fr_eu_ebemv.restype = None
         R.fr_eu_predictor.argtypes = mesh + [_f64p, _f64p, _c_int, _f64p, _f64p, _c_int, _c_int, _c_dbl,
                                              _f64p, ctypes.POINTER(_c_dbl)]
+        if hasattr(R, "fr_eu_mfdd_build"):
+            R.fr_eu_set_invY.argtypes = [_f64p]
+            R.fr_eu_set_invY.restype = None
+            R.fr_eu_mfdd_build.argtypes = mesh + [_f64p, _f64p, _c_int, _f64p, _f64p, _f64p, _f64p, _f64p, _f64p,
+                                                  _f64p, _f64p, _f64p]
+            R.fr_eu_mfdd_build.restype = None
         R.fr_eu_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
         R.fr_eu_layout.restype = None
     return R
@@ -269,7 +284,7 @@ def _setup_eu(R):
 class _EulerProblem(ctypes.Structure):
     _fields_ = [("gamma", _c_dbl), ("mach", _c_dbl), ("dimensionless", _c_int), ("tolerance", _c_dbl),
                 ("alpha", _c_dbl), ("dt", _c_dbl), ("upresc", ctypes.POINTER(_c_dbl)), ("form", _c_int),
-                ("uB", ctypes.c_void_p), ("delta_old", ctypes.c_void_p)]
+                ("uB", ctypes.c_void_p), ("delta_old", ctypes.c_void_p), ("invY", ctypes.POINTER(_c_dbl))]
 
 
 class TimeOpts(ctypes.Structure):
@@ -289,9 +304,11 @@ class _TimeStats(ctypes.Structure):
 
 def _eu_struct(p):
     up = np.ascontiguousarray(p.upresc, dtype=np.float64)
+    iy = np.ascontiguousarray(getattr(p, "invY", np.ones(4)), dtype=np.float64)
     s = _EulerProblem(p.gamma, p.mach, int(p.dimensionless), p.tolerance, p.alpha, p.dt,
-                      up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(getattr(p, "form", 0)), None, None)
-    return s, up
+                      up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(getattr(p, "form", 0)), None, None,
+                      iy.ctypes.data_as(ctypes.POINTER(_c_dbl)))
+    return s, (up, iy)
 
 
 def build_euler(prob, u=None, du=None):
@@ -317,6 +334,68 @@ def euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000, u0=Non
     lib().or_euler_predictor(*_mesh_args(m), ctypes.byref(s), ctypes.byref(topts), tol, kmax, lmax, u, a,
                              ctypes.byref(st))
     return u[:m.neq].copy(), a[:m.neq].copy(), {k: getattr(st, k) for k, _ in st._fields_}
+
+
+def build_euler_mfdd(prob, u=None, du=None, uB=None, duB=None, dnmv=None):
+    """Build_M_F_DD_Transiente ("Predictor2", DD, YZBeta) at (u, du) and the
+    bubble unknowns (uB, duB: 4 per element); returns (A[nel, 144],
+    F[neq+1], cond[nel, 53] = invN2, R2[4], M2[4][12]).  dnmv (nel, updated
+    in place) is Delta_YZBetaNMV's state, None = fresh zeros."""
+    m = prob.mesh
+    f = lambda a, n: np.zeros(n) if a is None else np.ascontiguousarray(a, dtype=np.float64)
+    u = prob.initial_state() if u is None else np.ascontiguousarray(u, dtype=np.float64)
+    du, uB, duB = f(du, m.neq), f(uB, 4 * m.nel), f(duB, 4 * m.nel)
+    A = np.empty(m.nel * 144)
+    F = np.empty(m.neq + 1)
+    cond = np.empty(m.nel * 53)
+    s, keep = _eu_struct(prob)
+    lib().or_build_euler_mfdd(*_mesh_args(m), ctypes.byref(s), u, du, uB, duB,
+                              None if dnmv is None else dnmv.ctypes.data, A, F, cond)
+    return A.reshape(m.nel, 144), F, cond.reshape(m.nel, 53)
+
+
+def euler_dab(lm, cond, Da):
+    """calculate_DaB of the Euler driver: DaB (4 per element) from Da (neq + 1)."""
+    nel = lm.shape[0]
+    Da = np.array(Da, dtype=np.float64, copy=True)
+    DaB = np.empty(4 * nel)
+    lib().or_euler_dab(nel, np.ascontiguousarray(lm, dtype=np.int32).reshape(-1), Da.shape[0] - 1,
+                       np.ascontiguousarray(cond, dtype=np.float64).reshape(-1), Da, DaB)
+    return DaB
+
+
+def euler_predictor2(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000, u0=None):
+    """Predictor_New with Build_M_F_DD_Transiente; returns (u, a, uB, aB, stats)."""
+    m = prob.mesh
+    u = np.zeros(m.neq + 1)
+    u[:m.neq] = prob.initial_state() if u0 is None else u0
+    a = np.zeros(m.neq + 1)
+    uB = np.zeros(4 * max(m.nel, 1))
+    aB = np.zeros(4 * max(m.nel, 1))
+    st = _TimeStats()
+    s, keep = _eu_struct(prob)
+    lib().or_euler_predictor2(*_mesh_args(m), ctypes.byref(s), ctypes.byref(topts), tol, kmax, lmax, u, a, uB, aB,
+                              ctypes.byref(st))
+    return (u[:m.neq].copy(), a[:m.neq].copy(), uB[:4 * m.nel].copy(), aB[:4 * m.nel].copy(),
+            {k: getattr(st, k) for k, _ in st._fields_})
+
+
+def ref_euler_mfdd_build(prob, u, du, uB, duB, Da):
+    """The reference's Build_M_F_DD_Transiente (fresh delta states) and its
+    calculate_DaB on Da; returns (A[nel, 144], F[neq+1], cond[nel, 53],
+    DaB[4 nel])."""
+    m = prob.mesh
+    R = ref_euler()
+    R.fr_eu_set_form(2)
+    R.fr_eu_set_invY(np.ascontiguousarray(getattr(prob, "invY", np.ones(4)), dtype=np.float64))
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    A = np.empty(m.nel * 144)
+    F = np.zeros(m.neq + 1)
+    cond = np.empty(m.nel * 53)
+    DaB = np.empty(4 * m.nel)
+    R.fr_eu_mfdd_build(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)), int(prob.wall),
+                       f(u), f(du), f(uB), f(duB), f(Da), A, F, cond, DaB)
+    return A.reshape(m.nel, 144), F, cond.reshape(m.nel, 53), DaB
 
 
 def ref_euler_lm(mesh):
@@ -357,7 +436,11 @@ def ref_euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000, dr
     u = np.zeros(m.neq + 1)
     t = _c_dbl(0.0)
     R = ref_euler(DROPIN_SO["euler"]) if dropin else ref_euler()
-    R.fr_eu_set_form(int(getattr(prob, "form", 0)))
+    if topts.scheme == 3:      # "Predictor2": DD + YZBeta with Build_M_F_DD_Transiente
+        R.fr_eu_set_form(2)
+        R.fr_eu_set_invY(np.ascontiguousarray(getattr(prob, "invY", np.ones(4)), dtype=np.float64))
+    else:
+        R.fr_eu_set_form(int(getattr(prob, "form", 0)))
     its = R.fr_eu_predictor(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
                                       int(prob.wall), np.ascontiguousarray(prob.init), topts.as_array(),
                                       kmax, lmax, tol, u, ctypes.byref(t))

@@ -72,8 +72,10 @@ typedef struct {
     AuxBuildStructuresType Aux;
 } fr_eu;
 
-static int g_eu_form;   /* 0: SUPG + CAU, 1: DD + CAUDD */
+static int g_eu_form;   /* 0: SUPG + CAU, 1: DD + CAUDD, 2: DD + YZBeta with Build_M_F_DD_Transiente */
 void fr_eu_set_form(int form) { g_eu_form = form; }
+static double g_invY[4] = {1.0, 1.0, 1.0, 1.0};
+void fr_eu_set_invY(const double *invY) { memcpy(g_invY, invY, sizeof g_invY); }
 
 /* Ax_Ay_calculations.c:35-38 assigns Ay[0][0] twice and never Ay[0][3], and
  * Build_M_K_F_DD_Transiente reads Ay[0][3] (through Ka14, Kb14, Kc14): the
@@ -91,6 +93,12 @@ static int fr_dd_build(ParametersType *P, MatrixDataType *M, FemStructsType *S, 
     fr_clear_stack();
     return Build_M_K_F_DD_Transiente(P, M, S, F);
 }
+/* Build_M_F_DD_Transiente ("Predictor2") reads the same Ay[0][3] */
+static int fr_mfdd_build(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctionsType *F)
+{
+    fr_clear_stack();
+    return Build_M_F_DD_Transiente(P, M, S, F);
+}
 
 static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const double *y, const int *type,
                         const int *invp, const int *ien, int neq, const double *prm)
@@ -102,7 +110,8 @@ static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const do
     strcpy(c->P.TimeIntegration, "Predictor1");
     strcpy(c->P.MatrixVectorProductScheme, "EBE");
     strcpy(c->P.StabilizationForm, g_eu_form ? "DD" : "SUPG");
-    strcpy(c->P.ShockCapture, g_eu_form ? "CAUDD" : "CAU");
+    strcpy(c->P.ShockCapture, g_eu_form == 2 ? "YZBeta" : g_eu_form ? "CAUDD" : "CAU");
+    memcpy(c->P.invY, g_invY, sizeof g_invY);
     strcpy(c->P.Preconditioner, "BlockDiag");
     strcpy(c->P.Scaling, "NOT");
     strcpy(c->P.reordering, "NOT");
@@ -163,7 +172,15 @@ static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const do
     setSolver(&c->P, &c->O);
     setPreconditioner(&c->P, &c->F);
     setDimensionlessness(&c->P, &c->F);
-    if (g_eu_form) {       /* setStabilizationForm.c:31-34, 60-62: "DD", "Predictor1", "CAUDD" */
+    if (g_eu_form == 2) {  /* setStabilizationForm.c:47-50, 64-66: "DD", "Predictor2", "YZBeta";
+                            * set_BC_no_penetrability.c:18-21 for other problems */
+        c->O.Build = fr_mfdd_build;
+        c->F.ShockCapture = Delta_YZBeta;
+        c->F.BC_General_theta = BC_theta_NO;
+        c->F.BC_theta = NULL;
+        c->F.BC_no_penetrability = NO_BC_no_penetrability;
+        c->S.uB = calloc(4 * (size_t)nel + 4, sizeof(double));
+    } else if (g_eu_form) {  /* setStabilizationForm.c:31-34, 60-62: "DD", "Predictor1", "CAUDD" */
         c->O.Build = fr_dd_build;
         c->F.ShockCapture = Delta_DD;
         c->S.uB = calloc(4 * (size_t)nel + 4, sizeof(double));
@@ -250,7 +267,7 @@ void fr_eu_ebemv(int nnodes, int nel, const double *x, const double *y, const in
 /* The predictor/multicorrector time loops of the reference.
  * topt: stop_by_norm, max_corrections, correction_tol, steady_state,
  *       final_time, time_tol, scheme (0 Predictor_Old, 1 Predictor_Old_BDF,
- *       2 Predictor_New_TRBDF2); solver: kmax, lmax, tol. */
+ *       2 Predictor_New_TRBDF2, 3 Predictor_New); solver: kmax, lmax, tol. */
 int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
                     const int *ien, int neq, const double *prm, const double *coef, int wall,
                     const double *init, const double *topt, int kmax, int lmax, double tol, double *u_out,
@@ -275,7 +292,9 @@ int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const
     c.S.delta_old = NULL;
     free(c.S.uB);
     c.S.uB = NULL;
-    if (topt[6] == 1.0)
+    if (topt[6] == 3.0)
+        Predictor_New(&c.P, &c.M, &c.S, &c.F, &c.O);
+    else if (topt[6] == 1.0)
         Predictor_Old_BDF(&c.P, &c.M, &c.S, &c.F, &c.O);
     else if (topt[6] == 2.0)
         Predictor_New_TRBDF2(&c.P, &c.M, &c.S, &c.F, &c.O);
@@ -348,4 +367,51 @@ void fr_eu_layout(long *out)
     out[i++] = (long)sizeof(NodeType);
     out[i++] = (long)offsetof(NodeType, invP_id);
     out[i++] = (long)sizeof(ElementType);
+}
+
+/* One Build_M_F_DD_Transiente ("Predictor2", form 2) at (u, du, uB, duB)
+ * with fresh delta states, then calculate_DaB on the caller's Da (NEQ + 1).
+ * A (144 per element), F (NEQ + 1), cond (invN2, R2[4], M2[4][12] per
+ * element) and DaB (4 per element) are returned. */
+int Build_M_F_DD_Transiente(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *);
+int calculate_DaB(ParametersType *, FemStructsType *, double *, double *);
+void fr_eu_mfdd_build(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                      const int *ien, int neq, const double *prm, const double *coef, int wall, const double *u,
+                      const double *du, const double *uB, const double *duB, const double *Da, double *A_out,
+                      double *F_out, double *cond_out, double *DaB_out)
+{
+    fr_eu c;
+    int I, r, j;
+    fr_eu_problem(coef, wall, NULL);
+    fr_eu_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, prm);
+    double *R2aux = calloc(4 * (size_t)nel, sizeof(double)), *M2aux = calloc(48 * (size_t)nel, sizeof(double));
+    double **R2 = calloc((size_t)nel, sizeof(double *)), **M2 = calloc((size_t)nel, sizeof(double *));
+    for (I = 0; I < nel; I++) { R2[I] = &R2aux[4 * I]; M2[I] = &M2aux[48 * I]; }
+    c.Aux.R2 = R2;
+    c.Aux.M2 = M2;
+    c.Aux.invN2 = calloc((size_t)nel, sizeof(double));
+    c.Aux.delta_old_NMV = calloc((size_t)nel, sizeof(double));
+    double *dus = calloc((size_t)neq + 1, sizeof(double)), *duBs = calloc(4 * (size_t)nel, sizeof(double));
+    memcpy(c.S.u, u, sizeof(double) * (size_t)neq);
+    memcpy(dus, du, sizeof(double) * (size_t)neq);
+    memcpy(c.S.uB, uB, sizeof(double) * 4 * (size_t)nel);
+    memcpy(duBs, duB, sizeof(double) * 4 * (size_t)nel);
+    c.S.du = dus;
+    c.S.duB = duBs;
+    c.O.Build(&c.P, &c.M, &c.S, &c.F);
+    double *Dac = calloc((size_t)neq + 1, sizeof(double));
+    memcpy(Dac, Da, sizeof(double) * ((size_t)neq + 1));
+    calculate_DaB(&c.P, &c.S, Dac, DaB_out);
+    memcpy(A_out, c.M.Aaux, sizeof(double) * 144 * (size_t)nel);
+    memcpy(F_out, c.S.F, sizeof(double) * ((size_t)neq + 1));
+    for (I = 0; I < nel; I++) {
+        cond_out[53 * I] = c.Aux.invN2[I];
+        for (r = 0; r < 4; r++) cond_out[53 * I + 1 + r] = R2[I][r];
+        for (r = 0; r < 4; r++)
+            for (j = 0; j < 12; j++) cond_out[53 * I + 5 + 12 * r + j] = M2[I][12 * r + j];
+    }
+    free(Dac); free(dus); free(duBs); free(R2aux); free(M2aux); free(R2); free(M2);
+    free(c.Aux.invN2); free(c.Aux.delta_old_NMV);
+    c.S.du = c.S.duB = NULL;
+    fr_eu_free(&c);
 }

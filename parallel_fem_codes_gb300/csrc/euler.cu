@@ -387,6 +387,287 @@ __global__ void __launch_bounds__(128) k_euler_dd_elem(int nel, int ld, int n, c
     }
 }
 
+// Delta_YZBeta.c:4-104 (nmv = 0: 0.5 (delta1 + delta2), no state) or
+// Delta_YZBetaNMV.c:4-93 (nmv = 1: 0.5 delta1 relaxed against *old with
+// w = 1/2, the relaxed value kept; its pow(x, 1) is x).  A_x grad and A_y
+// grad use the reference's term lists.
+__device__ double eu_delta_yz(const double invY[4], const double gx[4], const double gy[4], const double Ax[4][4],
+                              const double Ay[4][4], const double dUb[4], const double b[3], const double c[3],
+                              double twoArea, const double Ub[4], int nmv, double *old)
+{
+    double Agx[4], Agy[4], Z[4];
+    Agx[0] = gx[1];
+    Agx[1] = Ax[1][0] * gx[0] + Ax[1][1] * gx[1] + Ax[1][2] * gx[2] + Ax[1][3] * gx[3];
+    Agx[2] = Ax[2][0] * gx[0] + Ax[2][1] * gx[1] + Ax[2][2] * gx[2];
+    Agx[3] = Ax[3][0] * gx[0] + Ax[3][1] * gx[1] + Ax[3][2] * gx[2] + Ax[3][3] * gx[3];
+    Agy[0] = gy[2];
+    Agy[1] = Ay[1][0] * gy[0] + Ay[1][1] * gy[1] + Ay[1][2] * gy[2];
+    Agy[2] = Ay[2][0] * gy[0] + Ay[2][1] * gy[1] + Ay[2][2] * gy[2] + Ay[2][3] * gy[3];
+    Agy[3] = Ay[3][0] * gy[0] + Ay[3][1] * gy[1] + Ay[3][2] * gy[2] + Ay[3][3] * gy[3];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) Z[i] = dUb[i] + Agx[i] + Agy[i];
+    const double nYZ = sqrt(invY[0] * Z[0] * invY[0] * Z[0] + invY[1] * Z[1] * invY[1] * Z[1] +
+                            invY[2] * Z[2] * invY[2] * Z[2] + invY[3] * Z[3] * invY[3] * Z[3]);
+    const double nx = invY[0] * gx[0] * invY[0] * gx[0] + invY[1] * gx[1] * invY[1] * gx[1] +
+                      invY[2] * gx[2] * invY[2] * gx[2] + invY[3] * gx[3] * invY[3] * gx[3];
+    const double ny = invY[0] * gy[0] * invY[0] * gy[0] + invY[1] * gy[1] * invY[1] * gy[1] +
+                      invY[2] * gy[2] * invY[2] * gy[2] + invY[3] * gy[3] * invY[3] * gy[3];
+    const double sum = nx + ny;
+    const double nYU = sqrt(invY[0] * Ub[0] * invY[0] * Ub[0] + invY[1] * Ub[1] * invY[1] * Ub[1] +
+                            invY[2] * Ub[2] * invY[2] * Ub[2] + invY[3] * Ub[3] * invY[3] * Ub[3]);
+    const double ngr = sqrt(gx[0] * gx[0] + gy[0] * gy[0]);
+    double J1 = 0.0, J2 = 0.0;
+    if (fabs(ngr) >= 1e-12) {
+        J1 = gx[0] / ngr;
+        J2 = gy[0] / ngr;
+    }
+    double H = (fabs(J1 * b[0] + J2 * c[0]) + fabs(J1 * b[1] + J2 * c[1]) + fabs(J1 * b[2] + J2 * c[2])) / twoArea;
+    H = fabs(H) >= 1e-12 ? 2.0 * (1.0 / H) : 0.0;
+    const double as = fabs(sum) >= 1e-12 ? 1.0 / sqrt(sum) : 0.0;
+    const double au = fabs(nYU) >= 1e-12 ? 1.0 : 0.0;
+    const double d1 = nYZ * as * au * (H * 0.5);
+    if (nmv) {
+        const double w = 0.5;
+        const double d = w * (0.5 * d1) + (1 - w) * (*old);
+        *old = d;
+        return d;
+    }
+    const double as2 = fabs(sum) >= 1e-12 ? 1.0 : 0.0;
+    const double au2 = fabs(nYU) >= 1e-12 ? 1.0 / nYU : 0.0;
+    const double d2 = nYZ * as2 * au2 * (H * 0.5 * H * 0.5);
+    return 0.5 * (d1 + d2);
+}
+
+// Build_M_F_DD_Transiente.c:43-810 ("Predictor2", DD, YZBeta), a thread per
+// element (internal position pos).  The four bubble unknowns (uB, duB) are
+// condensed out of the element system with N2 = MBB + alpha dt KBB: the
+// block Me = M1 - N1 M2 / N2 (formed, as there, before the no-penetrability
+// adjustment, which is the identity here), the load R1 - N1 R2 / N2 into Fe
+// (12 planes), and invN2, R2, M2 into the bubble planes for the correction.
+// The entries of M1, N1 and M2 are formed on the fly from Ax, Ay and the
+// edge vectors, each with the reference's expression.  Bubble planes (stride
+// ld): 0-3 uB, 4-7 aB (duB), 8 invN2, 9-12 R2, 13-60 M2 (4 x 12), 61
+// Delta_YZBetaNMV's relaxed state.
+__global__ void __launch_bounds__(128) k_euler_mfdd_elem(int nel, int ld, int n, const int *__restrict__ gien,
+                                                         const double *__restrict__ gx, const double *__restrict__ gy,
+                                                         const int *__restrict__ node_dof,
+                                                         const double *__restrict__ up, const double *__restrict__ u,
+                                                         const double *__restrict__ du, fg_euler_coeffs cf,
+                                                         double *__restrict__ bub, double *__restrict__ A64,
+                                                         double *__restrict__ Fe)
+{
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    const double third = 1.0 / 3.0, sixth = 1.0 / 6.0, nf = 9.0 / 40.0;
+    double X[3], Y[3], Ue[12], dUe[12];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const int J = gien[(size_t)v * ld + pos];
+        X[v] = gx[J];
+        Y[v] = gy[J];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int d = node_dof[4 * J + k];
+            const bool dir = d == n;
+            Ue[4 * v + k] = dir ? up[4 * J + k] : u[d];
+            dUe[4 * v + k] = dir ? 0.0 : du[d];
+        }
+    }
+    const double b[3] = {Y[1] - Y[2], Y[2] - Y[0], Y[0] - Y[1]};
+    const double c[3] = {X[2] - X[1], X[0] - X[2], X[1] - X[0]};
+    const double twoArea = fabs(c[2] * b[1] - c[1] * b[2]);
+    const double Area = 0.5 * twoArea;
+    double Ub[4], dUb[4], gxu[4], gyu[4], uB[4], duB[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        Ub[i] = (Ue[i] + Ue[i + 4] + Ue[i + 8]) * third;
+        dUb[i] = (dUe[i] + dUe[i + 4] + dUe[i + 8]) * third;
+        gxu[i] = (Ue[i] * b[0] + Ue[i + 4] * b[1] + Ue[i + 8] * b[2]) / twoArea;
+        gyu[i] = (Ue[i] * c[0] + Ue[i + 4] * c[1] + Ue[i + 8] * c[2]) / twoArea;
+        uB[i] = bub[(size_t)i * ld + pos];
+        duB[i] = bub[(size_t)(4 + i) * ld + pos];
+    }
+    double Ax[4][4], Ay[4][4];
+    eu_jacobians(cf, Ub, Ax, Ay);
+    const double delta = eu_delta_yz(cf.invY, gxu, gyu, Ax, Ay, dUb, b, c, twoArea, Ub, 0, nullptr);
+    const double Mhh1 = Area * sixth, Mhh2 = Area / 12.0, MhB = (3.0 * Area) / 20.0, MBB = (81.0 * Area) / 280.0;
+    const double d4a = delta / (4.0 * Area);
+    const double p[3] = {nf * (b[0] + 2.0 * b[1] + 2.0 * b[2]), nf * (2.0 * b[0] + b[1] + 2.0 * b[2]),
+                         nf * (2.0 * b[0] + 2.0 * b[1] + b[2])};
+    const double pq[3] = {nf * (c[0] + 2.0 * c[1] + 2.0 * c[2]), nf * (2.0 * c[0] + c[1] + 2.0 * c[2]),
+                          nf * (2.0 * c[0] + 2.0 * c[1] + c[2])};
+    double *old = bub + (size_t)61 * ld + pos;
+    double onmv = *old;
+    const double dnmv = eu_delta_yz(cf.invY, gxu, gyu, Ax, Ay, dUb, b, c, twoArea, Ub, 1, &onmv);
+    *old = onmv;
+    const double S = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[0] * b[1] + b[0] * b[2] + b[1] * b[2] + c[0] * c[0] +
+                     c[1] * c[1] + c[2] * c[2] + c[0] * c[1] + c[0] * c[2] + c[1] * c[2];
+    const double KBB = (81.0 * dnmv * S) / (40.0 * Area);
+    const double adt = cf.alpha * cf.dt;
+    const double invN2 = 1.0 / (MBB + adt * KBB);
+    // M2[r][col] = (MhB +) adt nf (b_j Ax + c_j Ay)[r][q]; N1[row][q] = (MhB +) adt (p_i Ax + pq_i Ay)[r][q]
+    auto m2 = [&](int r, int col) {
+        const int j = col >> 2, q = col & 3;
+        const double kbh = nf * (b[j] * Ax[r][q] + c[j] * Ay[r][q]);
+        return q == r ? MhB + adt * kbh : adt * kbh;
+    };
+    auto khb = [&](int i, int r, int q) { return p[i] * Ax[r][q] + pq[i] * Ay[r][q]; };
+    auto n1 = [&](int i, int r, int q) { return r == q ? MhB + adt * khb(i, r, q) : adt * khb(i, r, q); };
+    // R2 (:764-781)
+    double R2[4];
+#pragma unroll 1
+    for (int r = 0; r < 4; ++r) {
+        R2[r] = -MBB * duB[r] - KBB * uB[r];
+        double kb = (nf * (b[0] * Ax[r][0] + c[0] * Ay[r][0])) * Ue[0];
+#pragma unroll
+        for (int col = 1; col < 12; ++col) {
+            const int j = col >> 2, q = col & 3;
+            kb += (nf * (b[j] * Ax[r][q] + c[j] * Ay[r][q])) * Ue[col];
+        }
+        R2[r] += -(MhB * dUe[r] + MhB * dUe[4 + r] + MhB * dUe[8 + r]) - kb;
+    }
+    double *a = A64 + pos;
+#pragma unroll 1
+    for (int i = 0; i < 3; ++i) {
+#pragma unroll 1
+        for (int r = 0; r < 4; ++r) {
+            const int row = 4 * i + r;
+            double N1r[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) N1r[q] = n1(i, r, q);
+            double kh = 0.0;
+#pragma unroll 1
+            for (int j = 0; j < 3; ++j) {
+                const int lo = i < j ? i : j, hi = i < j ? j : i;
+                const double dd = d4a * (b[lo] * b[hi] + c[lo] * c[hi]);
+                const double mhh = i == j ? Mhh1 : Mhh2;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int col = 4 * j + q;
+                    const double kg = (b[j] * Ax[r][q] + c[j] * Ay[r][q]) * sixth;
+                    const double m1 = r == q ? mhh + adt * (kg + dd) : adt * kg;
+                    double soma = 0.0;
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) soma += N1r[k] * m2(k, col);
+                    a[(size_t)(12 * row + col) * ld] = m1 - invN2 * soma;
+                    const double coef = r == q ? dd + kg : kg;
+                    kh = col == 0 ? coef * Ue[0] : kh + coef * Ue[col];
+                }
+            }
+            const double KhBr0 = khb(i, r, 0), KhBr1 = khb(i, r, 1), KhBr2 = khb(i, r, 2), KhBr3 = khb(i, r, 3);
+            double R1 = -MhB * duB[r] - (KhBr0 * uB[0] + KhBr1 * uB[1] + KhBr2 * uB[2] + KhBr3 * uB[3]);
+            const double m = (i == 0 ? Mhh1 : Mhh2) * dUe[r] + (i == 1 ? Mhh1 : Mhh2) * dUe[4 + r] +
+                             (i == 2 ? Mhh1 : Mhh2) * dUe[8 + r];
+            R1 += -m - kh;
+            Fe[(size_t)row * ld + pos] =
+                R1 - invN2 * (N1r[0] * R2[0] + N1r[1] * R2[1] + N1r[2] * R2[2] + N1r[3] * R2[3]);
+        }
+    }
+    bub[(size_t)8 * ld + pos] = invN2;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) bub[(size_t)(9 + r) * ld + pos] = R2[r];
+#pragma unroll 1
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int col = 0; col < 12; ++col) bub[(size_t)(13 + 12 * r + col) * ld + pos] = m2(r, col);
+}
+
+// calculate_DaB.c:18-57 from the solve's Da (internal numbering; Dirichlet
+// dofs read 0 as Da[NEQ] = 0 there), then Predictor_New.c:104-105 (update:
+// aB += DaB, uB += coef DaB) or DaB into out[r * ld + pos] (!update)
+__global__ void k_euler_bubble_correct(int nel, int ld, int n, const int *__restrict__ gien,
+                                       const int *__restrict__ node_dof, const double *__restrict__ Da, double coef,
+                                       int update, double *__restrict__ bub, double *__restrict__ out)
+{
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+    double d[12];
+#pragma unroll
+    for (int v = 0; v < 3; ++v) {
+        const int J = gien[(size_t)v * ld + pos];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int q = node_dof[4 * J + k];
+            d[4 * v + k] = q == n ? 0.0 : Da[q];
+        }
+    }
+    const double invN2 = bub[(size_t)8 * ld + pos];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const double *m = bub + (size_t)(13 + 12 * r) * ld + pos;
+        double s = m[0] * d[0];
+#pragma unroll
+        for (int j = 1; j < 12; ++j) s += m[(size_t)j * ld] * d[j];
+        const double DaB = invN2 * (bub[(size_t)(9 + r) * ld + pos] - s);
+        if (update) {
+            bub[(size_t)(4 + r) * ld + pos] += DaB;
+            bub[(size_t)r * ld + pos] += coef * DaB;
+        } else {
+            out[(size_t)r * ld + pos] = DaB;
+        }
+    }
+}
+
+// Predictor_New.c:82-83 for the four bubble unknowns: uB += coef aB, aB = 0
+__global__ void k_euler_bubble_predict(int nel, int ld, double coef, double *__restrict__ bub)
+{
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pos >= nel) return;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        bub[(size_t)r * ld + pos] += coef * bub[(size_t)(4 + r) * ld + pos];
+        bub[(size_t)(4 + r) * ld + pos] = 0.0;
+    }
+}
+
+int euler_mfdd_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
+                               double *F_dev, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (t.ndof != 4) { set_error("Euler assembly needs ndof == 4"); return FG_ERR_UNSUPPORTED; }
+    if (!s->eu_geometry_ok) { set_error("Euler assembly before fg_euler_set_geometry"); return FG_ERR_STATE; }
+    if (c->form != FG_EULER_DD) { set_error("Euler Predictor2 builds the DD form (FG_EULER_DD)"); return FG_ERR_ARG; }
+    int r = bubble_alloc(s, 4);
+    if (r) return r;
+    if (t.nel > 0)
+        k_euler_mfdd_elem<<<(t.nel + 127) / 128, 128, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(),
+                                                              s->gx.as<double>(), s->gy.as<double>(),
+                                                              s->node_dof.as<int>(), s->gup.as<double>(), u_dev,
+                                                              du_dev, *c, s->bubble.as<double>(), s->A64.as<double>(),
+                                                              s->Fe.as<double>());
+    FG_CUDA(cudaGetLastError());
+    count_launches(1);
+    if ((r = gather_residual(s, s->Fe.as<double>(), F_dev, st))) return r;
+    s->blocks_ok = true;
+    s->csr_dirty = true;
+    return convert_blocks(s, st);
+}
+
+int euler_bubble_correct_device(fg_system *s, const double *Da_dev, double coef, double *DaB_dev, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (s->bubble_nb != 4) { set_error("no Euler Predictor2 build on this system"); return FG_ERR_STATE; }
+    if (t.nel > 0) {
+        k_euler_bubble_correct<<<(t.nel + 255) / 256, 256, 0, st>>>(t.nel, s->nel_pad, t.n, s->gien.as<int>(),
+                                                                   s->node_dof.as<int>(), Da_dev, coef,
+                                                                   DaB_dev ? 0 : 1, s->bubble.as<double>(), DaB_dev);
+        FG_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
+    return FG_OK;
+}
+
+int euler_bubble_predict_device(fg_system *s, double coef, cudaStream_t st)
+{
+    const Topology &t = s->topo;
+    if (t.nel > 0) {
+        k_euler_bubble_predict<<<(t.nel + 255) / 256, 256, 0, st>>>(t.nel, s->nel_pad, coef, s->bubble.as<double>());
+        FG_CUDA(cudaGetLastError());
+        count_launches(1);
+    }
+    return FG_OK;
+}
+
 int euler_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
                           double *R_dev, cudaStream_t st)
 {

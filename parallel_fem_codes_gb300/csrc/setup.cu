@@ -1347,11 +1347,17 @@ int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev,
     return convert_blocks(s, st);
 }
 
-int tt_bubble_alloc(fg_system *s, cudaStream_t st)
+// the bubble planes of a Predictor2 build with nb unknowns per element
+// (1: transient transport, 4: Euler), zero-filled when (re)allocated
+int bubble_alloc(fg_system *s, int nb)
 {
-    (void)st;
-    if (s->bubble.bytes >= 8 * (size_t)kBubblePlanes * s->nel_pad) return FG_OK;
-    return s->bubble.alloc(8 * (size_t)kBubblePlanes * s->nel_pad);   // zero-filled
+    const size_t want = 8 * (size_t)(nb == 4 ? kBubblePlanesEuler : kBubblePlanes) * s->nel_pad;
+    if (s->bubble_nb != nb || s->bubble.bytes < want) {
+        int r = s->bubble.alloc(want);
+        if (r) { s->bubble_nb = 0; return r; }
+        s->bubble_nb = nb;
+    }
+    return FG_OK;
 }
 
 int tt_mfdd_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev, const double *du_dev,
@@ -1368,7 +1374,7 @@ int tt_mfdd_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u
     int r;
     if (s->shock_state.bytes < 16 * (size_t)s->nel_pad && (r = s->shock_state.alloc(16 * (size_t)s->nel_pad)))
         return r;
-    if ((r = tt_bubble_alloc(s, st))) return r;
+    if ((r = bubble_alloc(s, 1))) return r;
     if (s->Fe.bytes < 8 * (size_t)12 * s->nel_pad && (r = s->Fe.alloc(8 * (size_t)12 * s->nel_pad))) return r;
     double *cbtilo = s->shock_state.as<double>() + s->nel_pad;
     if (t.nel > 0)
@@ -1390,7 +1396,7 @@ int tt_mfdd_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u
 int tt_bubble_correct_device(fg_system *s, const double *Da_dev, double coef, double *DaB_dev, cudaStream_t st)
 {
     const Topology &t = s->topo;
-    if (!s->bubble.p) { set_error("no Predictor2 build on this system"); return FG_ERR_STATE; }
+    if (s->bubble_nb != 1) { set_error("no transient transport Predictor2 build on this system"); return FG_ERR_STATE; }
     if (t.nel > 0) {
         k_tt_bubble_correct<<<(t.nel + 255) / 256, 256, 0, st>>>(t.nel, s->nel_pad, s->gien.as<int>(),
                                                                 s->gtype.as<int>(), s->node_dof.as<int>(), Da_dev,

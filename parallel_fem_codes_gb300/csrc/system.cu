@@ -1106,6 +1106,30 @@ int euler_predictor_hooked(fg_system *s, const fg_euler_coeffs *c, const fg_solv
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
     // the DD element state starts at zero with the loop (Predictor_Old.c callocs uB and delta_old)
     if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
+    if (to->scheme == FG_TIME_PREDICTOR2) {
+        // "Predictor2" with "DD" (setStabilizationForm.c:47-50), ShockCapture "YZBeta"
+        if (c->form != FG_EULER_DD) {
+            set_error("FG_TIME_PREDICTOR2 needs the DD form (FG_EULER_DD)");
+            return FG_ERR_UNSUPPORTED;
+        }
+        int r = bubble_alloc(s, 4);
+        if (r) return r;
+        // uB, aB and Delta_YZBetaNMV's state start at zero (Predictor_New.c calloc)
+        FG_CUDA(cudaMemsetAsync(s->bubble.p, 0, s->bubble.bytes, s->stream));
+        LoopHooks h;
+        h.predict = [&](double coef) { return euler_bubble_predict_device(s, coef, s->stream); };
+        h.corrected = [&](const double *Da, double coef) {
+            return euler_bubble_correct_device(s, Da, coef, nullptr, s->stream);
+        };
+        return time_loop(s, c->dt, c->alpha,
+                         [&](double ab, double db, const double *du, const double *da, double *R) {
+                             fg_euler_coeffs cc = *c;
+                             cc.alpha = ab;
+                             cc.dt = db;
+                             return euler_mfdd_assemble_device(s, &cc, du, da, R, s->stream);
+                         },
+                         o, to, u, a, stats, solve, &h);
+    }
     return time_loop(s, c->dt, c->alpha,
                      [&](double ab, double db, const double *du, const double *da, double *R) {
                          fg_euler_coeffs cc = *c;
@@ -1156,7 +1180,7 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
             set_error("FG_TIME_PREDICTOR2 needs the DD form (FG_TRANSPORT_DD)");
             return FG_ERR_UNSUPPORTED;
         }
-        int r = tt_bubble_alloc(s, s->stream);
+        int r = bubble_alloc(s, 1);
         if (r) return r;
         // uB and aB start at zero (Predictor_New.c:24,36 calloc them)
         FG_CUDA(cudaMemsetAsync(s->bubble.p, 0, s->bubble.bytes, s->stream));
@@ -1184,24 +1208,27 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
                      o, to, u, a, stats);
 }
 
-// host (reference element order) <-> bubble plane k (internal element position)
-static int bubble_plane_in(fg_system *s, int k, const double *h)
+// host (planes values per element, element-major, reference element order;
+// NULL = 0) <-> planes k0.. of a plane array (internal element position)
+static int planes_in(fg_system *s, double *dev, int k0, int planes, const double *h)
 {
     const Topology &t = s->topo;
-    std::vector<double> v((size_t)s->nel_pad, 0.0);
-    for (int pos = 0; pos < t.nel; ++pos) v[pos] = h ? h[t.eorder[pos]] : 0.0;
-    FG_CUDA(cudaMemcpyAsync(s->bubble.as<double>() + (size_t)k * s->nel_pad, v.data(), 8 * (size_t)s->nel_pad,
-                            cudaMemcpyHostToDevice, s->stream));
+    std::vector<double> v((size_t)planes * s->nel_pad, 0.0);
+    for (int pos = 0; pos < t.nel; ++pos)
+        for (int k = 0; k < planes; ++k)
+            v[(size_t)k * s->nel_pad + pos] = h ? h[(size_t)planes * t.eorder[pos] + k] : 0.0;
+    FG_CUDA(cudaMemcpyAsync(dev + (size_t)k0 * s->nel_pad, v.data(), 8 * v.size(), cudaMemcpyHostToDevice,
+                            s->stream));
     FG_CUDA(cudaStreamSynchronize(s->stream));
     return FG_OK;
 }
 
-static int bubble_planes_out(fg_system *s, int k0, int planes, double *h)
+static int planes_out(fg_system *s, const double *dev, int k0, int planes, double *h)
 {
     const Topology &t = s->topo;
     std::vector<double> v((size_t)planes * s->nel_pad);
-    FG_CUDA(cudaMemcpyAsync(v.data(), s->bubble.as<double>() + (size_t)k0 * s->nel_pad, 8 * v.size(),
-                            cudaMemcpyDeviceToHost, s->stream));
+    FG_CUDA(cudaMemcpyAsync(v.data(), dev + (size_t)k0 * s->nel_pad, 8 * v.size(), cudaMemcpyDeviceToHost,
+                            s->stream));
     FG_CUDA(cudaStreamSynchronize(s->stream));
     for (int pos = 0; pos < t.nel; ++pos)
         for (int k = 0; k < planes; ++k) h[(size_t)planes * t.eorder[pos] + k] = v[(size_t)k * s->nel_pad + pos];
@@ -1214,53 +1241,76 @@ int fg_tt_bubble_assemble(fg_system *s, const fg_tt_coeffs *c, const double *u, 
     if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
     int r = ensure_io(s);
     if (r) return r;
-    if ((r = stage(s, s->state_a, 8 * (size_t)s->n_pad)) || (r = tt_bubble_alloc(s, s->stream))) return r;
+    if ((r = stage(s, s->state_a, 8 * (size_t)s->n_pad)) || (r = bubble_alloc(s, 1))) return r;
     if ((r = state_in(s, u, s->ws.t64.as<double>())) || (r = state_in(s, du, s->state_a.as<double>()))) return r;
-    if ((r = bubble_plane_in(s, 0, uB)) || (r = bubble_plane_in(s, 1, duB))) return r;
+    if ((r = planes_in(s, s->bubble.as<double>(), 0, 1, uB)) || (r = planes_in(s, s->bubble.as<double>(), 1, 1, duB)))
+        return r;
     if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
     if ((r = tt_mfdd_assemble_device(s, c, s->ws.t64.as<double>(), s->state_a.as<double>(), s->ws.u64.as<double>(),
                                      s->stream)))
         return r;
     if (F && (r = vec_out(s, s->ws.u64.as<double>(), F, s->ws.r64.as<double>()))) return r;
     FG_CUDA(cudaStreamSynchronize(s->stream));
-    if (cond && (r = bubble_planes_out(s, 2, 5, cond))) return r;
+    if (cond && (r = planes_out(s, s->bubble.as<double>(), 2, 5, cond))) return r;
     FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
     FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
     FG_CUDA(cudaStreamSynchronize(s->stream));
     return FG_OK;
 }
 
-int fg_tt_bubble_dab(fg_system *s, const double *Da, double *DaB)
+int fg_euler_bubble_assemble(fg_system *s, const fg_euler_coeffs *c, const double *u, const double *du,
+                             const double *uB, const double *duB, double *F, double *cond)
+{
+    if (!s || !c) { set_error("NULL argument"); return FG_ERR_ARG; }
+    int r = ensure_io(s);
+    if (r) return r;
+    if ((r = stage(s, s->state_a, 8 * (size_t)s->n_pad)) || (r = bubble_alloc(s, 4))) return r;
+    if ((r = state_in(s, u, s->ws.t64.as<double>())) || (r = state_in(s, du, s->state_a.as<double>()))) return r;
+    // fresh shock-capture state, then uB and duB
+    FG_CUDA(cudaMemsetAsync(s->bubble.p, 0, s->bubble.bytes, s->stream));
+    if ((r = planes_in(s, s->bubble.as<double>(), 0, 4, uB)) || (r = planes_in(s, s->bubble.as<double>(), 4, 4, duB)))
+        return r;
+    if ((r = euler_mfdd_assemble_device(s, c, s->ws.t64.as<double>(), s->state_a.as<double>(),
+                                        s->ws.u64.as<double>(), s->stream)))
+        return r;
+    if (F && (r = vec_out(s, s->ws.u64.as<double>(), F, s->ws.r64.as<double>()))) return r;
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    if (cond && (r = planes_out(s, s->bubble.as<double>(), 8, 53, cond))) return r;
+    FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
+    FG_CUDA(cudaMemsetAsync(s->ws.u64.p, 0, s->ws.u64.bytes, s->stream));
+    FG_CUDA(cudaStreamSynchronize(s->stream));
+    return FG_OK;
+}
+
+int fg_bubble_dab(fg_system *s, const double *Da, double *DaB)
 {
     if (!s || !Da || !DaB) { set_error("NULL argument"); return FG_ERR_ARG; }
+    const int nb = s->bubble_nb;
     // the build's element scratch (Fe, 12 planes of nel_pad) receives DaB
-    if (!s->bubble.p || s->Fe.bytes < 8 * (size_t)s->nel_pad) {
+    if (!nb || s->Fe.bytes < 8 * (size_t)nb * s->nel_pad) {
         set_error("no Predictor2 build on this system");
         return FG_ERR_STATE;
     }
     int r = ensure_io(s);
     if (r) return r;
     if ((r = vec_in(s, Da, s->ws.t64.as<double>(), s->ws.r64.as<double>()))) return r;
-    if ((r = tt_bubble_correct_device(s, s->ws.t64.as<double>(), 0.0, s->Fe.as<double>(), s->stream))) return r;
-    std::vector<double> v((size_t)s->nel_pad);
-    FG_CUDA(cudaMemcpyAsync(v.data(), s->Fe.p, 8 * v.size(), cudaMemcpyDeviceToHost, s->stream));
+    r = nb == 4 ? euler_bubble_correct_device(s, s->ws.t64.as<double>(), 0.0, s->Fe.as<double>(), s->stream)
+                : tt_bubble_correct_device(s, s->ws.t64.as<double>(), 0.0, s->Fe.as<double>(), s->stream);
+    if (r) return r;
+    r = planes_out(s, s->Fe.as<double>(), 0, nb, DaB);
     FG_CUDA(cudaMemsetAsync(s->ws.t64.p, 0, s->ws.t64.bytes, s->stream));
     FG_CUDA(cudaStreamSynchronize(s->stream));
-    for (int pos = 0; pos < s->topo.nel; ++pos) DaB[s->topo.eorder[pos]] = v[pos];
-    return FG_OK;
+    return r;
 }
 
-int fg_tt_bubble_state(fg_system *s, double *uB, double *aB)
+int fg_bubble_state(fg_system *s, double *uB, double *aB)
 {
     if (!s) { set_error("NULL argument"); return FG_ERR_ARG; }
-    if (!s->bubble.p) { set_error("no Predictor2 build on this system"); return FG_ERR_STATE; }
-    std::vector<double> v(2 * (size_t)s->topo.nel + 2);
-    int r = bubble_planes_out(s, 0, 2, v.data());
-    if (r) return r;
-    for (int e = 0; e < s->topo.nel; ++e) {
-        if (uB) uB[e] = v[2 * (size_t)e];
-        if (aB) aB[e] = v[2 * (size_t)e + 1];
-    }
+    const int nb = s->bubble_nb;
+    if (!nb) { set_error("no Predictor2 build on this system"); return FG_ERR_STATE; }
+    int r = FG_OK;
+    if (uB && (r = planes_out(s, s->bubble.as<double>(), 0, nb, uB))) return r;
+    if (aB && (r = planes_out(s, s->bubble.as<double>(), nb, nb, aB))) return r;
     return FG_OK;
 }
 

@@ -53,8 +53,11 @@ struct fg_system {
     fg::DevMem gf1, gf2, state_u, state_a, state_old, norm_part;
     fg::DevMem state_u1, state_u2;     // u^{n-1}, u^n of the BDF2 steps
     fg::DevMem shock_state;            // YZBeta Re_old, delta_old [2 * nel_pad]
-    // Predictor2 bubble planes [kBubblePlanes * nel_pad]: uB, aB, invN2, R2, M2[0..2]
+    // Predictor2 bubble planes of nel_pad doubles, nb = 1 (transient
+    // transport: uB, aB, invN2, R2, M2[3]) or 4 (Euler: uB[4], aB[4], invN2,
+    // R2[4], M2[4][12], Delta_YZBetaNMV's state)
     fg::DevMem bubble;
+    int bubble_nb = 0;
     bool ns_geometry_ok = false, eu_geometry_ok = false;
     // resident right-hand side (internal numbering): F and M^-1 F
     fg::DevMem rhs_f, rhs_b;
@@ -248,12 +251,18 @@ int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev,
 // the bubble planes (uB, aB as duB); F_dev the load.  The correction
 // (calculate_DaB from Da, internal numbering) updates aB and uB with coef =
 // alpha dt, or writes DaB into DaB_dev (element positions) when given.
-constexpr int kBubblePlanes = 7;
-int tt_bubble_alloc(fg_system *s, cudaStream_t st);
+constexpr int kBubblePlanes = 7, kBubblePlanesEuler = 62;
+int bubble_alloc(fg_system *s, int nb);
 int tt_mfdd_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev, const double *du_dev,
                             double *F_dev, cudaStream_t st);
 int tt_bubble_correct_device(fg_system *s, const double *Da_dev, double coef, double *DaB_dev, cudaStream_t st);
 int tt_bubble_predict_device(fg_system *s, double coef, cudaStream_t st);
+// Euler "Predictor2" (euler.cu): Build_M_F_DD_Transiente with YZBeta, and
+// the same correction / prediction of its four bubble unknowns per element
+int euler_mfdd_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
+                               double *F_dev, cudaStream_t st);
+int euler_bubble_correct_device(fg_system *s, const double *Da_dev, double coef, double *DaB_dev, cudaStream_t st);
+int euler_bubble_predict_device(fg_system *s, double coef, cudaStream_t st);
 // The correction solve of a time loop: the system's resident right-hand
 // side (B = rhs_b, Ftrue = rhs_f, device, internal numbering) solved into
 // ws.x with cfg; stats receives the result.  The time loops solve alone by

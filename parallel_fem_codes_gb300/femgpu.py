@@ -89,7 +89,7 @@ class NSCoeffs(ctypes.Structure):
 
 class EulerCoeffs(ctypes.Structure):
     _fields_ = [("gamma", _c_dbl), ("mach", _c_dbl), ("dimensionless", _c_int), ("tolerance", _c_dbl),
-                ("alpha", _c_dbl), ("dt", _c_dbl), ("form", _c_int)]
+                ("alpha", _c_dbl), ("dt", _c_dbl), ("form", _c_int), ("invY", _c_dbl * 4)]
 
 
 class TimeOpts(ctypes.Structure):
@@ -200,8 +200,9 @@ def lib(build_if_missing: bool = True):
     L.fg_unscale.argtypes = [_vp, _vp]
     L.fg_tt_assemble.argtypes = [_vp, ctypes.POINTER(TTCoeffs), _vp, _vp, _vp]
     L.fg_tt_bubble_assemble.argtypes = [_vp, ctypes.POINTER(TTCoeffs), _vp, _vp, _vp, _vp, _vp, _vp]
-    L.fg_tt_bubble_dab.argtypes = [_vp, _vp, _vp]
-    L.fg_tt_bubble_state.argtypes = [_vp, _vp, _vp]
+    L.fg_euler_bubble_assemble.argtypes = [_vp, ctypes.POINTER(EulerCoeffs), _vp, _vp, _vp, _vp, _vp, _vp]
+    L.fg_bubble_dab.argtypes = [_vp, _vp, _vp]
+    L.fg_bubble_state.argtypes = [_vp, _vp, _vp]
     L.fg_tt_predictor.argtypes = [_vp, ctypes.POINTER(TTCoeffs), ctypes.POINTER(SolverOpts),
                                   ctypes.POINTER(TimeOpts), _f64p, _vp, ctypes.POINTER(TimeStats)]
     L.fg_server_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(ServerOpts)]
@@ -549,21 +550,40 @@ class System:
                                           cond.ctypes.data))
         return F, cond[: 5 * nel].reshape(nel, 5)
 
-    def tt_bubble_dab(self, Da):
-        """calculate_DaB after the last Predictor2 build: DaB (nel) from Da (n+1)."""
+    def _bubble_nb(self):
+        return 4 if self.S == 12 else 1
+
+    def bubble_dab(self, Da):
+        """calculate_DaB after the last Predictor2 build: DaB (1 or 4 per
+        element, element-major) from Da (n+1)."""
         Da = np.ascontiguousarray(Da, dtype=np.float64)
         if Da.shape != (self.n + 1,):
             raise ValueError("Da needs n + 1 entries")
-        DaB = np.empty(max(self.mesh.nel, 1))
-        check(lib().fg_tt_bubble_dab(self._h, Da.ctypes.data, DaB.ctypes.data))
-        return DaB[: self.mesh.nel]
+        m = self._bubble_nb() * self.mesh.nel
+        DaB = np.empty(max(m, 1))
+        check(lib().fg_bubble_dab(self._h, Da.ctypes.data, DaB.ctypes.data))
+        return DaB[:m]
 
-    def tt_bubble_state(self):
-        """(uB, aB) after tt_predictor with FG_TIME_PREDICTOR2."""
+    def bubble_state(self):
+        """(uB, aB) after a Predictor2 loop (FG_TIME_PREDICTOR2)."""
+        m = self._bubble_nb() * self.mesh.nel
+        uB, aB = np.empty(max(m, 1)), np.empty(max(m, 1))
+        check(lib().fg_bubble_state(self._h, uB.ctypes.data, aB.ctypes.data))
+        return uB[:m], aB[:m]
+
+    def euler_bubble_assemble(self, prob, u=None, du=None, uB=None, duB=None):
+        """Build_M_F_DD_Transiente (Euler "Predictor2", DD, YZBeta) at (u, du)
+        and the bubble unknowns (4 per element) with fresh shock-capture
+        states; returns (F[n+1], cond[nel, 53] = invN2, R2[4], M2[4][12]);
+        the blocks stay on the device."""
+        c = euler_coeffs(prob)
         nel = self.mesh.nel
-        uB, aB = np.empty(max(nel, 1)), np.empty(max(nel, 1))
-        check(lib().fg_tt_bubble_state(self._h, uB.ctypes.data, aB.ctypes.data))
-        return uB[:nel], aB[:nel]
+        F = np.empty(self.n + 1)
+        cond = np.empty(53 * max(nel, 1))
+        arr = [None if v is None else np.ascontiguousarray(v, dtype=np.float64) for v in (u, du, uB, duB)]
+        check(lib().fg_euler_bubble_assemble(self._h, ctypes.byref(c), *[_ptr(v) for v in arr], F.ctypes.data,
+                                             cond.ctypes.data))
+        return F, cond[: 53 * nel].reshape(nel, 53)
 
     def tt_predictor(self, prob, alpha, dt, topts, u0=None, kmax=30, lmax=1000, tol=1e-10,
                      precision=FG_PREC_FP64, inner_tol=0.0):
@@ -613,8 +633,11 @@ def tt_coeffs(prob, alpha, dt) -> TTCoeffs:
 
 
 def euler_coeffs(prob) -> EulerCoeffs:
+    """Euler coefficients of a problem; invY (the YZBeta scaling of
+    "Predictor2") from prob.invY, default ones."""
+    iy = [float(v) for v in getattr(prob, "invY", (1.0, 1.0, 1.0, 1.0))]
     return EulerCoeffs(prob.gamma, prob.mach, int(prob.dimensionless), prob.tolerance, prob.alpha, prob.dt,
-                       int(getattr(prob, "form", 0)))
+                       int(getattr(prob, "form", 0)), (_c_dbl * 4)(*iy))
 
 
 def time_opts(stop_by_norm=0, max_corrections=2, correction_tol=1e-3, steady_state=0, final_time=0.0,

@@ -244,6 +244,32 @@ def write_tt():
     np.savez_compressed(os.path.join(HERE, "tt_ref.npz"), **out)
 
 
+EU_P2_INVY = (1.0, 0.5, 2.0, 0.25)
+
+
+def write_euler_predictor2():
+    """TimeIntegration "Predictor2" of the Euler driver with "DD" and
+    "YZBeta" (oracle/_ref/libref_euler.so): one Build_M_F_DD_Transiente +
+    calculate_DaB at a random state, and the reference's own Predictor_New
+    loop (BlockDiag, pgmres) over 3 steps of 2 corrections."""
+    p = G.obliquo_problem(9)
+    p.invY = np.array(EU_P2_INVY)
+    m = p.mesh
+    rng = np.random.default_rng(31)
+    u = p.initial_state() * (1 + 0.05 * rng.standard_normal(m.neq))
+    du = 0.1 * rng.standard_normal(m.neq)
+    uB = 0.01 * rng.standard_normal(4 * m.nel)
+    duB = 0.01 * rng.standard_normal(4 * m.nel)
+    Da = np.append(rng.standard_normal(m.neq), 3.0)
+    A, F, cond, DaB = O.ref_euler_mfdd_build(p, u, du, uB, duB, Da)
+    out = {"u": u, "du": du, "uB": uB, "duB": duB, "Da": Da, "A": A, "F": F, "cond": cond, "DaB": DaB}
+    to = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6, 0, 3)
+    U, its, t = O.ref_euler_predictor(p, to, 1e-10, 25, 1000)
+    out["U"], out["its"] = U, np.array([its])
+    print("euler predictor2 gmres", its)
+    np.savez_compressed(os.path.join(HERE, "euler_predictor2_ref.npz"), **out)
+
+
 TT_P2_CASES = [(2, 0), (3, 2)]   # (shock, h_shock) of the DD form
 
 
@@ -312,4 +338,5 @@ if __name__ == "__main__":
     write_euler_dd()
     write_tt()
     write_tt_predictor2()
+    write_euler_predictor2()
     write_elem_prec()

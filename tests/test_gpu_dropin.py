@@ -8,7 +8,9 @@ linked with the reference's CPU solve path (oracle/Makefile `ref`):
 * Navier-Stokes Process.c (04_SS_NavierStokes_Equations/2D/01_CommonFiles/
   Process.c:6-62: Picard, BlockDiagDOF3 + pgmres), cavity 17 x 17, Re 100;
 * Predictor_Old.c (00_CommonFiles/Time_Integration/Predictor_Old.c:6-134:
-  Euler OBLIQUO 17 x 17, 4 steps, 2 corrections, BlockDiag + pgmres).
+  Euler OBLIQUO 17 x 17, 4 steps, 2 corrections, BlockDiag + pgmres);
+* Predictor_New.c with Build_M_F_DD_Transiente.c ("Predictor2", DD,
+  YZBeta: the bubble unknowns, calculate_DaB), 3 steps.
 
 Solutions within rel-L2 1e-9, GMRES iterations (Parameters->iterations)
 within +-2 per linear solve.  Skipped where the drop-in builds are absent
@@ -59,3 +61,15 @@ def test_euler_predictor_old_dropin():
     assert t1 == t0
     assert rel(u1, u0) <= 1e-9
     assert abs(it1 - it0) <= 2 * 8
+
+
+def test_euler_predictor2_dropin():
+    """Predictor_New.c with Build_M_F_DD_Transiente.c ("Predictor2", DD,
+    YZBeta) linked unchanged against the shims."""
+    p = G.obliquo_problem(17)
+    p.invY = np.array([1.0, 0.5, 2.0, 0.25])
+    to = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6, 0, 3)
+    u0, it0, _ = O.ref_euler_predictor(p, to, tol=1e-10, kmax=25)
+    u1, it1, _ = O.ref_euler_predictor(p, to, tol=1e-10, kmax=25, dropin=True)
+    assert rel(u1, u0) <= 1e-9
+    assert abs(it1 - it0) <= 2 * 6

@@ -173,3 +173,59 @@ def test_euler_dd_predictor(fg):
     ug, ag, st = s.euler_predictor(p, fg.time_opts(0, 2, 1e-3, 0, 4 * p.dt, 1e-6), kmax=25, tol=1e-10)
     assert st["steps"] == sto["steps"] == 4
     assert rel(ug, uo) < 1e-7
+
+
+# ---- "Predictor2" (DD, YZBeta): Build_M_F_DD_Transiente, calculate_DaB and
+# Predictor_New with four bubble unknowns per element ----
+
+def _p2_problem(n, dimensionless=True):
+    p = G.obliquo_problem(n, dimensionless=dimensionless)
+    p.form = 1
+    p.invY = np.array([1.0, 0.5, 2.0, 0.25])
+    return p
+
+
+@pytest.mark.parametrize("n,dimless", [(9, True), (17, False), (33, True)])
+def test_euler_predictor2_build_bit_exact(fg, n, dimless):
+    """Me, the load, the condensation data (invN2, R2, M2) and
+    calculate_DaB's increments bit-identical with the oracle (itself
+    bit-identical with the reference's functions)."""
+    p = _p2_problem(n, dimless)
+    m = p.mesh
+    rng = np.random.default_rng(n)
+    u = p.initial_state() * (1 + 0.05 * rng.standard_normal(m.neq))
+    du = 0.1 * rng.standard_normal(m.neq)
+    uB, duB = 0.01 * rng.standard_normal(4 * m.nel), 0.01 * rng.standard_normal(4 * m.nel)
+    A0, F0, c0 = O.build_euler_mfdd(p, u, du, uB, duB)
+    s = fg.euler_system(p)
+    F, cond = s.euler_bubble_assemble(p, u, du, uB, duB)
+    assert np.array_equal(F[:-1], F0[:-1]) and F[-1] == 0.0
+    assert np.array_equal(cond, c0)
+    assert np.array_equal(s.get_blocks(), A0)
+    Da = np.append(rng.standard_normal(m.neq), 0.0)
+    assert np.array_equal(s.bubble_dab(Da), O.euler_dab(O.fill_lm(m), c0, Da))
+
+
+def test_euler_predictor2_loop(fg):
+    """The Predictor_New loop on the device (state, four bubble unknowns per
+    element and the relaxed YZBeta state resident) against the oracle's: u
+    and uB to rel-L2 1e-7, same steps and corrections."""
+    p = _p2_problem(17)
+    to_o = O.TimeOpts(0, 2, 1e-3, 0, 4 * p.dt + 1e-12, 1e-6, 0, 3)
+    uo, ao, uBo, aBo, sto = O.euler_predictor2(p, to_o, tol=1e-10, kmax=25)
+    s = fg.euler_system(p)
+    to = fg.time_opts(0, 2, 1e-3, 0, 4 * p.dt + 1e-12, 1e-6, scheme=fg.FG_TIME_PREDICTOR2)
+    ug, ag, st = s.euler_predictor(p, to, kmax=25, tol=1e-10)
+    uB, aB = s.bubble_state()
+    assert st["steps"] == sto["steps"] == 4
+    assert st["corrections"] == sto["corrections"]
+    assert rel(ug, uo) < 1e-7 and rel(uB, uBo) < 1e-7
+    assert rel(aB, aBo) < 1e-5
+
+
+def test_euler_predictor2_needs_dd(fg):
+    p = G.obliquo_problem(9)
+    s = fg.euler_system(p)
+    with pytest.raises(fg.FemGpuError) as e:
+        s.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1, scheme=fg.FG_TIME_PREDICTOR2))
+    assert e.value.code == fg.FG_ERR_UNSUPPORTED

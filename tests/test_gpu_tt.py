@@ -167,7 +167,7 @@ def test_tt_predictor2_build_bit_exact(fg, n, cau, hs, reorder):
     assert np.array_equal(cond, c0)
     assert np.array_equal(s.get_blocks(), A0)
     Da = np.append(rng.standard_normal(m.neq), 0.0)
-    assert np.array_equal(s.tt_bubble_dab(Da), O.tt_dab(O.fill_lm(m), c0, Da))
+    assert np.array_equal(s.bubble_dab(Da), O.tt_dab(O.fill_lm(m), c0, Da))
 
 
 @pytest.mark.parametrize("cau", [2, 3], ids=["caudd", "yzbeta"])
@@ -183,7 +183,7 @@ def test_tt_predictor2_loop(fg, cau):
     to = fg.time_opts(0, 2, 1e-3, 0, 6 * 0.02, 1e-6, precond=fg.FG_PRECOND_DIAG, setup_flags=0,
                       scheme=fg.FG_TIME_PREDICTOR2)
     ug, ag, st = s.tt_predictor(p, 0.5, 0.02, to, kmax=30, tol=1e-10)
-    uB, aB = s.tt_bubble_state()
+    uB, aB = s.bubble_state()
     assert st["steps"] == sto["steps"] == 6
     assert st["corrections"] == sto["corrections"]
     assert rel(ug, uo) < 1e-8 and rel(uB, uBo) < 1e-8
@@ -191,17 +191,11 @@ def test_tt_predictor2_loop(fg, cau):
 
 
 def test_tt_predictor2_needs_dd(fg):
-    """Predictor2 exists for the DD form only (setStabilizationForm.c:51-54);
-    the Euler loop has no bubble build here."""
+    """Predictor2 exists for the DD form only (setStabilizationForm.c:51-54)."""
     p = G.transport_problem(9, angle_deg=30.0, k=1e-3)
     s = fg.transport_system(p)
     to = fg.time_opts(0, 1, 1e-3, 0, 0.02, 1e-6, precond=fg.FG_PRECOND_DIAG, setup_flags=0,
                       scheme=fg.FG_TIME_PREDICTOR2)
     with pytest.raises(fg.FemGpuError) as e:
         s.tt_predictor(p, 0.5, 0.02, to)
-    assert e.value.code == fg.FG_ERR_UNSUPPORTED
-    ep = G.obliquo_problem(9)
-    se = fg.euler_system(ep)
-    with pytest.raises(fg.FemGpuError) as e:
-        se.euler_predictor(ep, fg.time_opts(0, 1, 1e-3, 0, ep.dt, 1e-6, max_steps=1, scheme=fg.FG_TIME_PREDICTOR2))
     assert e.value.code == fg.FG_ERR_UNSUPPORTED

@@ -176,3 +176,75 @@ def test_block_scaling_against_reference(oracle_lib):
         bd, ibd, Id, Fo = O.blockdiag_setup(m, A, R, ref_quirks=True)
         assert np.array_equal(inv1, ibd) and np.array_equal(F1, Fo)
         assert np.array_equal(A1, O.block_scale(m, A, ibd))
+
+
+# ---- TimeIntegration "Predictor2" with "DD" and "YZBeta": Build_M_F_DD_Transiente.c,
+# Delta_YZBeta.c, Delta_YZBetaNMV.c, calculate_DaB.c and Predictor_New.c ----
+
+def _p2_problem(n=9):
+    p = G.obliquo_problem(n)
+    p.invY = np.array([1.0, 0.5, 2.0, 0.25])
+    return p
+
+
+@pytest.fixture(scope="module")
+def p2gold():
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "euler_predictor2_ref.npz"))
+
+
+def test_predictor2_build_matches_reference_golden(p2gold):
+    """Me, F, the condensation data (invN2, R2, M2) and calculate_DaB's
+    bubble increments bit-identical with the reference's own functions."""
+    g = p2gold
+    p = _p2_problem()
+    A, F, cond = O.build_euler_mfdd(p, g["u"], g["du"], g["uB"], g["duB"])
+    assert np.array_equal(A, g["A"]) and np.array_equal(F, g["F"]) and np.array_equal(cond, g["cond"])
+    assert np.array_equal(O.euler_dab(O.fill_lm(p.mesh), cond, g["Da"]), g["DaB"])
+
+
+def test_predictor2_loop_matches_reference_golden(p2gold):
+    """The whole Predictor_New loop (3 steps x 2 corrections, BlockDiag,
+    GMRES): final state and GMRES iterations equal the reference's."""
+    p = _p2_problem()
+    to = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6, 0, 3)
+    u, a, uB, aB, st = O.euler_predictor2(p, to, 1e-10, 25, 1000)
+    assert st["steps"] == 3 and st["corrections"] == 6
+    assert st["gmres_iterations"] == int(p2gold["its"][0])
+    assert np.array_equal(u, p2gold["U"])
+    assert np.abs(uB).max() > 0                      # the bubbles move
+
+
+@pytest.mark.skipif(O.ref_euler() is None, reason="reference build (oracle/_ref) not present")
+def test_predictor2_against_reference_build():
+    p = _p2_problem(11)
+    p.invY = np.array([0.8, 1.5, 0.7, 0.3])
+    m = p.mesh
+    rng = np.random.default_rng(5)
+    u = p.initial_state() * (1 + 0.05 * rng.standard_normal(m.neq))
+    du = 0.1 * rng.standard_normal(m.neq)
+    uB, duB = 0.01 * rng.standard_normal(4 * m.nel), 0.01 * rng.standard_normal(4 * m.nel)
+    Da = np.append(rng.standard_normal(m.neq), 1.0)
+    A0, F0, c0, D0 = O.ref_euler_mfdd_build(p, u, du, uB, duB, Da)
+    A1, F1, c1 = O.build_euler_mfdd(p, u, du, uB, duB)
+    assert np.array_equal(A0, A1) and np.array_equal(F0, F1) and np.array_equal(c0, c1)
+    assert np.array_equal(D0, O.euler_dab(O.fill_lm(m), c1, Da))
+    to = O.TimeOpts(1, 3, 1e-4, 0, 2 * p.dt + 1e-12, 1e-6, 0, 3)
+    U0, its0, t0 = O.ref_euler_predictor(p, to, 1e-10, 25, 1000)
+    U1, a1, uB1, aB1, st = O.euler_predictor2(p, to, 1e-10, 25, 1000)
+    assert st["gmres_iterations"] == its0 and np.array_equal(U0, U1)
+
+
+def test_predictor2_bubble_rows_are_solved():
+    """The bubble rows of each element's system, M2 . Da_e + N2 DaB = R2,
+    hold for calculate_DaB's increments (static condensation is exact)."""
+    p = _p2_problem()
+    m = p.mesh
+    rng = np.random.default_rng(9)
+    A, F, cond = O.build_euler_mfdd(p, p.initial_state(), 0.1 * rng.standard_normal(m.neq),
+                                    0.01 * rng.standard_normal(4 * m.nel), 0.01 * rng.standard_normal(4 * m.nel))
+    lm = O.fill_lm(m)
+    Da = np.append(rng.standard_normal(m.neq), 0.0)
+    DaB = O.euler_dab(lm, cond, Da).reshape(m.nel, 4)
+    invN2, R2, M2 = cond[:, 0], cond[:, 1:5], cond[:, 5:].reshape(m.nel, 4, 12)
+    resid = np.einsum("erj,ej->er", M2, Da[lm]) + DaB / invN2[:, None] - R2
+    assert np.abs(resid).max() <= 1e-12 * max(np.abs(R2).max(), 1.0)
