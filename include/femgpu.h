@@ -437,7 +437,11 @@ typedef struct {
                           bubble values and the relaxed delta) stays on the
                           device and is zeroed when fg_euler_predictor starts */
     double invY[4];    /* Parameters->invY: the scaling of the YZBeta shock
-                          capture that "Predictor2" uses (FG_TIME_PREDICTOR2)   */
+                          capture (Delta_YZBeta.c)                             */
+    int shock;         /* ShockCapture: 0 = the form's own (Delta_CAU for SUPG,
+                          Delta_DD for DD), FG_SHOCK_YZBETA = Delta_YZBeta with
+                          invY (setStabilizationForm.c:24-26, 64-66);
+                          "Predictor2" always uses YZBeta                      */
 } fg_euler_coeffs;
 enum { FG_EULER_SUPG = 0, FG_EULER_DD = 1 };
 

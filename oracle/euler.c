@@ -115,6 +115,11 @@ static double eu_delta_cau(double tolerance, const double gx[4], const double gy
     return ng >= tolerance ? nL / nk : 0.0;
 }
 
+static double eu_delta_yz(const double invY[4], const double gx[4], const double gy[4], double Ax[4][4],
+                          double Ay[4][4], const double dUb[4], const double b[3], const double c[3], double twoArea,
+                          const double Ub[4], int nmv, double *old);
+static const double eu_ones[4] = {1.0, 1.0, 1.0, 1.0};
+
 /* One element: Ae = Me + alpha dt Ke (12x12, row-major) and Re = -Me dUe - Ke Ue. */
 static void eu_element(const or_euler_problem *pb, const double X[3], const double Y[3], const double Ue[12],
                        const double dUe[12], double Ae[144], double Re[12])
@@ -166,7 +171,10 @@ static void eu_element(const or_euler_problem *pb, const double X[3], const doub
     mul4(Ay, Ax, Ayx);
     mul4(Ay, Ay, Ayy);
 
-    double delta = eu_delta_cau(pb->tolerance, gx, gy, Ax, Ay, A0, dUb, b, c, twoArea);
+    /* ShockCapture "CAU" (Delta_CAU) or "YZBeta" (Delta_YZBeta, setStabilizationForm.c:24-26) */
+    double delta = pb->shock == 3
+                       ? eu_delta_yz(pb->invY ? pb->invY : eu_ones, gx, gy, Ax, Ay, dUb, b, c, twoArea, Ub, 0, NULL)
+                       : eu_delta_cau(pb->tolerance, gx, gy, Ax, Ay, A0, dUb, b, c, twoArea);
 
     /* SUPG tau (:240-269) */
     double betax = 2.0 * (gx[0] * Ub[0] + gx[1] * Ub[1] + gx[2] * Ub[2] + gx[3] * Ub[3]);
@@ -321,7 +329,10 @@ static void eu_dd_element(const or_euler_problem *pb, const double X[3], const d
     double Ax[4][4], Ay[4][4], A0[4][4];
     eu_jacobians(gamma, pb->mach, pb->dimensionless, Ub, Ax, Ay);
     eu_a0inv(gamma, Ub, A0);
-    double delta = eu_delta_dd(pb->tolerance, delta_old, gx, gy, Ax, Ay, A0, dUb, b, c, twoArea);
+    /* ShockCapture "CAUDD" (Delta_DD) or "YZBeta" (Delta_YZBeta, setStabilizationForm.c:64-66) */
+    double delta = pb->shock == 3
+                       ? eu_delta_yz(pb->invY ? pb->invY : eu_ones, gx, gy, Ax, Ay, dUb, b, c, twoArea, Ub, 0, NULL)
+                       : eu_delta_dd(pb->tolerance, delta_old, gx, gy, Ax, Ay, A0, dUb, b, c, twoArea);
 
     double K[3][4][4], KhB[12][4], T[12][4];
     for (j = 0; j < 3; j++)
@@ -561,8 +572,7 @@ static void eu_mfdd_element(const or_euler_problem *pb, const double X[3], const
                             const double dUe[12], const double uB[4], const double duB[4], double *old_nmv,
                             double Me[144], double Fe[12], double cond[53])
 {
-    static const double ones[4] = {1.0, 1.0, 1.0, 1.0};
-    const double *invY = pb->invY ? pb->invY : ones;
+    const double *invY = pb->invY ? pb->invY : eu_ones;
     const double third = 1.0 / 3.0, sixth = 1.0 / 6.0, nf = 9.0 / 40.0;
     double b[3] = {Y[1] - Y[2], Y[2] - Y[0], Y[0] - Y[1]};
     double c[3] = {X[2] - X[1], X[0] - X[2], X[1] - X[0]};

@@ -192,6 +192,7 @@ typedef struct {
     int form;              /* 0: SUPG + CAU, 1: DD (Build_M_K_F_DD_Transiente + Delta_DD) */
     double *uB, *delta_old;/* DD state: [4*nel] bubbles, [nel] delta (NULL: fresh zeros) */
     const double *invY;    /* [4] Parameters->invY of YZBeta (NULL: 1, 1, 1, 1)        */
+    int shock;             /* 0: the form's own (CAU / CAUDD); 3: YZBeta (Delta_YZBeta) */
 } or_euler_problem;
 
 /* Build_M_K_F_SUPG + Delta_CAU + eval_U_dU + ebe_assembly: A receives the

@@ -284,7 +284,8 @@ def _setup_eu(R):
 class _EulerProblem(ctypes.Structure):
     _fields_ = [("gamma", _c_dbl), ("mach", _c_dbl), ("dimensionless", _c_int), ("tolerance", _c_dbl),
                 ("alpha", _c_dbl), ("dt", _c_dbl), ("upresc", ctypes.POINTER(_c_dbl)), ("form", _c_int),
-                ("uB", ctypes.c_void_p), ("delta_old", ctypes.c_void_p), ("invY", ctypes.POINTER(_c_dbl))]
+                ("uB", ctypes.c_void_p), ("delta_old", ctypes.c_void_p), ("invY", ctypes.POINTER(_c_dbl)),
+                ("shock", _c_int)]
 
 
 class TimeOpts(ctypes.Structure):
@@ -307,7 +308,7 @@ def _eu_struct(p):
     iy = np.ascontiguousarray(getattr(p, "invY", np.ones(4)), dtype=np.float64)
     s = _EulerProblem(p.gamma, p.mach, int(p.dimensionless), p.tolerance, p.alpha, p.dt,
                       up.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(getattr(p, "form", 0)), None, None,
-                      iy.ctypes.data_as(ctypes.POINTER(_c_dbl)))
+                      iy.ctypes.data_as(ctypes.POINTER(_c_dbl)), int(getattr(p, "shock", 0)))
     return s, (up, iy)
 
 
@@ -404,13 +405,23 @@ def ref_euler_lm(mesh):
     return lm.reshape(mesh.nel, 12)
 
 
+def _ref_eu_form(R, prob):
+    """The harness's form code: 0 SUPG + CAU, 1 DD + CAUDD, 3 SUPG + YZBeta,
+    4 DD + YZBeta (invY from the problem)."""
+    form = int(getattr(prob, "form", 0))
+    if int(getattr(prob, "shock", 0)) == 3:
+        R.fr_eu_set_invY(np.ascontiguousarray(getattr(prob, "invY", np.ones(4)), dtype=np.float64))
+        form += 3
+    R.fr_eu_set_form(form)
+
+
 def ref_euler_build(prob, u=None, du=None):
     m = prob.mesh
     u = prob.initial_state() if u is None else np.ascontiguousarray(u, dtype=np.float64)
     du = np.zeros(m.neq) if du is None else np.ascontiguousarray(du, dtype=np.float64)
     A = np.empty(m.nel * 144)
     R = np.empty(m.neq + 1)
-    ref_euler().fr_eu_set_form(int(getattr(prob, "form", 0)))
+    _ref_eu_form(ref_euler(), prob)
     ref_euler().fr_eu_build(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
                             int(prob.wall), u, du, A, R)
     return A.reshape(m.nel, 144), R
@@ -440,7 +451,7 @@ def ref_euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000, dr
         R.fr_eu_set_form(2)
         R.fr_eu_set_invY(np.ascontiguousarray(getattr(prob, "invY", np.ones(4)), dtype=np.float64))
     else:
-        R.fr_eu_set_form(int(getattr(prob, "form", 0)))
+        _ref_eu_form(R, prob)
     its = R.fr_eu_predictor(*_mesh_args(m), prob.params(), np.ascontiguousarray(prob.coef.reshape(-1)),
                                       int(prob.wall), np.ascontiguousarray(prob.init), topts.as_array(),
                                       kmax, lmax, tol, u, ctypes.byref(t))

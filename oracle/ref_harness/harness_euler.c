@@ -72,7 +72,9 @@ typedef struct {
     AuxBuildStructuresType Aux;
 } fr_eu;
 
-static int g_eu_form;   /* 0: SUPG + CAU, 1: DD + CAUDD, 2: DD + YZBeta with Build_M_F_DD_Transiente */
+/* 0: SUPG + CAU, 1: DD + CAUDD, 2: DD + YZBeta with Build_M_F_DD_Transiente
+ * ("Predictor2"), 3: SUPG + YZBeta, 4: DD + YZBeta (Predictor1 build) */
+static int g_eu_form;
 void fr_eu_set_form(int form) { g_eu_form = form; }
 static double g_invY[4] = {1.0, 1.0, 1.0, 1.0};
 void fr_eu_set_invY(const double *invY) { memcpy(g_invY, invY, sizeof g_invY); }
@@ -109,8 +111,8 @@ static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const do
     strcpy(c->P.Solver, "GMRES");
     strcpy(c->P.TimeIntegration, "Predictor1");
     strcpy(c->P.MatrixVectorProductScheme, "EBE");
-    strcpy(c->P.StabilizationForm, g_eu_form ? "DD" : "SUPG");
-    strcpy(c->P.ShockCapture, g_eu_form == 2 ? "YZBeta" : g_eu_form ? "CAUDD" : "CAU");
+    strcpy(c->P.StabilizationForm, g_eu_form == 0 || g_eu_form == 3 ? "SUPG" : "DD");
+    strcpy(c->P.ShockCapture, g_eu_form >= 2 ? "YZBeta" : g_eu_form ? "CAUDD" : "CAU");
     memcpy(c->P.invY, g_invY, sizeof g_invY);
     strcpy(c->P.Preconditioner, "BlockDiag");
     strcpy(c->P.Scaling, "NOT");
@@ -180,13 +182,14 @@ static void fr_eu_setup(fr_eu *c, int nnodes, int nel, const double *x, const do
         c->F.BC_theta = NULL;
         c->F.BC_no_penetrability = NO_BC_no_penetrability;
         c->S.uB = calloc(4 * (size_t)nel + 4, sizeof(double));
-    } else if (g_eu_form) {  /* setStabilizationForm.c:31-34, 60-62: "DD", "Predictor1", "CAUDD" */
+    } else if (g_eu_form == 1 || g_eu_form == 4) {  /* setStabilizationForm.c:31-34, 60-66: "DD",
+                                                     * "Predictor1", "CAUDD" or "YZBeta" */
         c->O.Build = fr_dd_build;
-        c->F.ShockCapture = Delta_DD;
+        c->F.ShockCapture = g_eu_form == 4 ? Delta_YZBeta : Delta_DD;
         c->S.uB = calloc(4 * (size_t)nel + 4, sizeof(double));
-    } else {
+    } else {                 /* :7-27: "SUPG", "CAU" or "YZBeta" */
         c->O.Build = Build_M_K_F_SUPG;
-        c->F.ShockCapture = Delta_CAU;
+        c->F.ShockCapture = g_eu_form == 3 ? Delta_YZBeta : Delta_CAU;
     }
 }
 

@@ -72,6 +72,10 @@ __device__ __forceinline__ void eu_jacobians(const fg_euler_coeffs &cf, const do
     Ay[3][1] = Ax[3][2];
 }
 
+__device__ double eu_delta_yz(const double invY[4], const double gx[4], const double gy[4], const double Ax[4][4],
+                              const double Ay[4][4], const double dUb[4], const double b[3], const double c[3],
+                              double twoArea, const double Ub[4], int nmv, double *old);
+
 // w^T A0^-1 w, symmetric expansion of Delta_CAU.c:37-63 (A0 upper triangle)
 __device__ __forceinline__ double a0_norm2(const double A0[10], const double w[4])
 {
@@ -124,9 +128,12 @@ __global__ void __launch_bounds__(128) k_euler_elem(int nel, int ld, int n, cons
     double Ax[4][4], Ay[4][4];
     eu_jacobians(cf, Ub, Ax, Ay);
 
-    // A0^-1 (Build_M_K_F_SUPG.c:131-158), upper triangle
+    // A0^-1 (Build_M_K_F_SUPG.c:131-158), upper triangle; ShockCapture "CAU"
+    // or "YZBeta" (Delta_YZBeta with invY)
     double delta;
-    {
+    if (cf.shock == FG_SHOCK_YZBETA) {
+        delta = eu_delta_yz(cf.invY, gxu, gyu, Ax, Ay, dUb, b, c, twoArea, Ub, 0, nullptr);
+    } else {
         const double rho_i = Ub[3] - ((nU * 0.5) / Ub[0]);
         const double V2 = Ub[1] / rho_i, V3 = Ub[2] / rho_i, V4 = (-Ub[0]) / rho_i;
         const double re = -1.0 / (rho_i * V4);
@@ -295,7 +302,9 @@ __global__ void __launch_bounds__(128) k_euler_dd_elem(int nel, int ld, int n, c
     double Ax[4][4], Ay[4][4];
     eu_jacobians(cf, Ub, Ax, Ay);
     double delta;
-    {   // Delta_DD.c: A0^-1 norms, relaxed (w = 1/2), times sqrt(2 Area)
+    if (cf.shock == FG_SHOCK_YZBETA) {   // ShockCapture "YZBeta": Delta_YZBeta, no state
+        delta = eu_delta_yz(cf.invY, gxu, gyu, Ax, Ay, dUb, b, c, twoArea, Ub, 0, nullptr);
+    } else {   // Delta_DD.c: A0^-1 norms, relaxed (w = 1/2), times sqrt(2 Area)
         const double rho_i = Ub[3] - ((nU * 0.5) / Ub[0]);
         const double V2 = Ub[1] / rho_i, V3 = Ub[2] / rho_i, V4 = (-Ub[0]) / rho_i;
         const double re = -1.0 / (rho_i * V4);
@@ -676,6 +685,10 @@ int euler_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *
     if (!s->eu_geometry_ok) { set_error("Euler assembly before fg_euler_set_geometry"); return FG_ERR_STATE; }
     if (c->form != FG_EULER_SUPG && c->form != FG_EULER_DD) {
         set_error("Euler form must be FG_EULER_SUPG or FG_EULER_DD");
+        return FG_ERR_ARG;
+    }
+    if (c->shock != 0 && c->shock != FG_SHOCK_YZBETA) {
+        set_error("Euler shock capture must be 0 (the form's own) or FG_SHOCK_YZBETA");
         return FG_ERR_ARG;
     }
     if (c->form == FG_EULER_DD) {   // element state: delta_old [nel_pad], uB [4][nel_pad]

@@ -89,7 +89,7 @@ class NSCoeffs(ctypes.Structure):
 
 class EulerCoeffs(ctypes.Structure):
     _fields_ = [("gamma", _c_dbl), ("mach", _c_dbl), ("dimensionless", _c_int), ("tolerance", _c_dbl),
-                ("alpha", _c_dbl), ("dt", _c_dbl), ("form", _c_int), ("invY", _c_dbl * 4)]
+                ("alpha", _c_dbl), ("dt", _c_dbl), ("form", _c_int), ("invY", _c_dbl * 4), ("shock", _c_int)]
 
 
 class TimeOpts(ctypes.Structure):
@@ -637,7 +637,7 @@ def euler_coeffs(prob) -> EulerCoeffs:
     "Predictor2") from prob.invY, default ones."""
     iy = [float(v) for v in getattr(prob, "invY", (1.0, 1.0, 1.0, 1.0))]
     return EulerCoeffs(prob.gamma, prob.mach, int(prob.dimensionless), prob.tolerance, prob.alpha, prob.dt,
-                       int(getattr(prob, "form", 0)), (_c_dbl * 4)(*iy))
+                       int(getattr(prob, "form", 0)), (_c_dbl * 4)(*iy), int(getattr(prob, "shock", 0)))
 
 
 def time_opts(stop_by_norm=0, max_corrections=2, correction_tol=1e-3, steady_state=0, final_time=0.0,

@@ -247,6 +247,30 @@ def write_tt():
 EU_P2_INVY = (1.0, 0.5, 2.0, 0.25)
 
 
+def write_euler_yzbeta():
+    """ShockCapture "YZBeta" (Delta_YZBeta.c) in the Euler SUPG and
+    Predictor1 DD builds (oracle/_ref/libref_euler.so): one build at a
+    random state per form, and Predictor_Old / Predictor_Old_BDF over 3
+    steps of 2 corrections."""
+    out = {}
+    for form in (0, 1):
+        p = G.obliquo_problem(9)
+        p.form, p.shock, p.invY = form, 3, np.array(EU_P2_INVY)
+        m = p.mesh
+        rng = np.random.default_rng(40 + form)
+        u = p.initial_state() * (1 + 0.05 * rng.standard_normal(m.neq))
+        du = 0.05 * rng.standard_normal(m.neq)
+        A, R = O.ref_euler_build(p, u, du)
+        key = f"yz_{form}"
+        out[key + "_u"], out[key + "_du"], out[key + "_A"], out[key + "_R"] = u, du, A, R
+        for scheme in (0, 1):
+            to = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6, 0, scheme)
+            U, its, t = O.ref_euler_predictor(p, to, 1e-10, 25, 1000)
+            out[f"{key}_s{scheme}_U"], out[f"{key}_s{scheme}_its"] = U, np.array([its])
+            print(key, scheme, "gmres", its)
+    np.savez_compressed(os.path.join(HERE, "euler_yzbeta_ref.npz"), **out)
+
+
 def write_euler_predictor2():
     """TimeIntegration "Predictor2" of the Euler driver with "DD" and
     "YZBeta" (oracle/_ref/libref_euler.so): one Build_M_F_DD_Transiente +
@@ -339,4 +363,5 @@ if __name__ == "__main__":
     write_tt()
     write_tt_predictor2()
     write_euler_predictor2()
+    write_euler_yzbeta()
     write_elem_prec()

@@ -229,3 +229,31 @@ def test_euler_predictor2_needs_dd(fg):
     with pytest.raises(fg.FemGpuError) as e:
         s.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1, scheme=fg.FG_TIME_PREDICTOR2))
     assert e.value.code == fg.FG_ERR_UNSUPPORTED
+
+
+# ---- ShockCapture "YZBeta" (Delta_YZBeta with invY) in the SUPG and DD builds ----
+
+@pytest.mark.parametrize("form,dimless", [(0, True), (0, False), (1, True), (1, False)],
+                         ids=["supg", "supg-dimensional", "dd", "dd-dimensional"])
+def test_euler_yzbeta_assembly_bit_exact(fg, form, dimless):
+    p = G.obliquo_problem(17, dimensionless=dimless)
+    p.form, p.shock, p.invY = form, fg.FG_SHOCK_YZBETA, np.array([0.8, 1.5, 0.7, 0.3])
+    u, du = _perturbed(p, 21 + form)
+    A0, R0 = O.build_euler(p, u, du)
+    s = fg.euler_system(p)
+    R = s.euler_assemble(p, u, du)
+    assert np.array_equal(R, R0)
+    assert np.array_equal(s.get_blocks(), A0)
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["supg", "dd"])
+def test_euler_yzbeta_predictor(fg, form):
+    p = G.obliquo_problem(17)
+    p.form, p.shock, p.invY = form, fg.FG_SHOCK_YZBETA, np.array([1.0, 0.5, 2.0, 0.25])
+    to_o = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6, 0)
+    uo, ao, sto = O.euler_predictor(p, to_o, tol=1e-10, kmax=25)
+    s = fg.euler_system(p)
+    ug, ag, st = s.euler_predictor(p, fg.time_opts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6), kmax=25, tol=1e-10)
+    assert st["steps"] == sto["steps"] == 3
+    assert st["corrections"] == sto["corrections"]
+    assert rel(ug, uo) < 1e-7

@@ -248,3 +248,47 @@ def test_predictor2_bubble_rows_are_solved():
     invN2, R2, M2 = cond[:, 0], cond[:, 1:5], cond[:, 5:].reshape(m.nel, 4, 12)
     resid = np.einsum("erj,ej->er", M2, Da[lm]) + DaB / invN2[:, None] - R2
     assert np.abs(resid).max() <= 1e-12 * max(np.abs(R2).max(), 1.0)
+
+
+# ---- ShockCapture "YZBeta" (Delta_YZBeta.c) in the SUPG and Predictor1 DD builds ----
+
+@pytest.fixture(scope="module")
+def yzgold():
+    return np.load(os.path.join(os.path.dirname(__file__), "golden", "euler_yzbeta_ref.npz"))
+
+
+def _yz_problem(form, n=9):
+    p = G.obliquo_problem(n)
+    p.form, p.shock, p.invY = form, 3, np.array([1.0, 0.5, 2.0, 0.25])
+    return p
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["supg", "dd"])
+def test_yzbeta_build_matches_reference_golden(yzgold, form):
+    key = f"yz_{form}"
+    A, R = O.build_euler(_yz_problem(form), yzgold[key + "_u"], yzgold[key + "_du"])
+    assert np.array_equal(A, yzgold[key + "_A"]) and np.array_equal(R, yzgold[key + "_R"])
+
+
+@pytest.mark.parametrize("form", [0, 1], ids=["supg", "dd"])
+@pytest.mark.parametrize("scheme", [0, 1], ids=["predictor", "bdf"])
+def test_yzbeta_loops_match_reference_golden(yzgold, form, scheme):
+    p = _yz_problem(form)
+    to = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6, 0, scheme)
+    u, a, st = O.euler_predictor(p, to, 1e-10, 25, 1000)
+    key = f"yz_{form}_s{scheme}"
+    assert st["gmres_iterations"] == int(yzgold[key + "_its"][0])
+    assert np.array_equal(u, yzgold[key + "_U"])
+
+
+@pytest.mark.skipif(O.ref_euler() is None, reason="reference build (oracle/_ref) not present")
+@pytest.mark.parametrize("form,dimless", [(0, False), (1, False), (0, True)])
+def test_yzbeta_against_reference_build(form, dimless):
+    p = G.obliquo_problem(11, dimensionless=dimless)
+    p.form, p.shock, p.invY = form, 3, np.array([0.8, 1.5, 0.7, 0.3])
+    rng = np.random.default_rng(12 + form)
+    u = p.initial_state() * (1 + 0.05 * rng.standard_normal(p.mesh.neq))
+    du = 0.05 * rng.standard_normal(p.mesh.neq)
+    A0, R0 = O.ref_euler_build(p, u, du)
+    A1, R1 = O.build_euler(p, u, du)
+    assert np.array_equal(A0, A1) and np.array_equal(R0, R1)
