@@ -724,14 +724,67 @@ typedef struct {
     eu_loop base;
     double *uB, *aB, *cond, *DaB, *dnmv;
     int *lm12;
+    double *uB1, *uB2;         /* uB_old (TR-BDF2) or uB1 (BDF); uB2 (BDF) */
 } eu_loop2;
 
-static void eu_predict2(void *p, double coef)
+/* uB_InitialSolution.c:3-111: each element's four bubble values are the
+ * centroid averages of its nodal state.  The reference tests a prescribed
+ * dof by invP_id != NEQ, while Preprocess.c:173 marks them with -1, so it
+ * reads u[-1] there; the prescribed value its other branch names is used. */
+static void eu_ub_initial(const eu_loop *b, const double *u, double *uB)
+{
+    const double third = 1.0 / 3.0;
+    for (int e = 0; e < b->nel; e++) {
+        double Ue[12];
+        for (int v = 0; v < 3; v++) {
+            const int J = b->ien[3 * e + v];
+            for (int k = 0; k < 4; k++) {
+                const long d = 4L * J + k;
+                Ue[4 * v + k] = b->type[d] > 0 ? u[b->invp[d]] : b->prob->upresc[d];
+            }
+        }
+        for (int i = 0; i < 4; i++) uB[4L * e + i] = (Ue[i] + Ue[i + 4] + Ue[i + 8]) * third;
+    }
+}
+
+static void eu_bubble2(void *p, int op, double c1, double c2, const double *u)
 {
     eu_loop2 *c = (eu_loop2 *)p;
-    size_t m = 4 * (size_t)c->base.nel;
-    for (size_t i = 0; i < m; i++) c->uB[i] += coef * c->aB[i];      /* Predictor_New.c:82-83 */
-    memset(c->aB, 0, sizeof(double) * m);
+    const size_t m = 4 * (size_t)c->base.nel;
+    size_t i;
+    switch (op) {
+    case OR_B_PREDICT:                        /* Predictor_New.c:82-83, _TRBDF2.c:91-92 */
+        for (i = 0; i < m; i++) c->uB[i] += c1 * c->aB[i];
+        memset(c->aB, 0, sizeof(double) * m);
+        break;
+    case OR_B_TRBDF2_START:                   /* Predictor_New_TRBDF2.c:63 */
+        eu_ub_initial(&c->base, u, c->uB);
+        break;
+    case OR_B_TRBDF2_COMBINE:                 /* :151-154 */
+        for (i = 0; i < m; i++) {
+            c->uB[i] = c1 * c->uB[i] - c2 * c->uB1[i];
+            c->aB[i] = 0.0;
+        }
+        break;
+    case OR_B_TRBDF2_SAVE:                    /* :192 */
+    case OR_B_BDF_START:                      /* Predictor_New_BDF.c:77-78 */
+        memcpy(c->uB1, c->uB, sizeof(double) * m);
+        if (op == OR_B_BDF_START) memset(c->aB, 0, sizeof(double) * m);
+        break;
+    case OR_B_BDF_SAVE2:                      /* :111 */
+        memcpy(c->uB2, c->uB, sizeof(double) * m);
+        break;
+    case OR_B_BDF_COMBINE:                    /* :139-142 */
+        for (i = 0; i < m; i++) {
+            c->uB[i] = c1 * c->uB2[i] - c2 * c->uB1[i];
+            c->aB[i] = 0.0;
+        }
+        break;
+    case OR_B_BDF_SHIFT:                      /* :177-178 */
+        memcpy(c->uB1, c->uB2, sizeof(double) * m);
+        memcpy(c->uB2, c->uB, sizeof(double) * m);
+        break;
+    }
 }
 
 static int eu_correct2(void *p, double alpha_b, double dt_b, const double *u, const double *a, double *Da, int *gi)
@@ -768,15 +821,17 @@ int or_euler_predictor2(int nnodes, int nel, const double *x, const double *y, c
     double *bd = malloc(sizeof(double) * 16 * nn), *inv = malloc(sizeof(double) * 16 * nn);
     double *cond = calloc(53 * ne, sizeof(double)), *DaB = calloc(4 * ne, sizeof(double));
     double *dnmv = calloc(ne, sizeof(double));
+    double *uB1 = calloc(4 * ne, sizeof(double)), *uB2 = calloc(4 * ne, sizeof(double));
     or_fill_lm(nel, 4, ien, type, invp, NEQ, lm);
     for (i = 0; i < 4 * nnodes; i++) Id[i] = type[i] == 0 ? NEQ : invp[i];
     memset(uB, 0, sizeof(double) * 4 * ne);  /* Predictor_New.c:24,36 calloc uB and aB */
     memset(aB, 0, sizeof(double) * 4 * ne);
-    or_time_opts t2 = *to;
-    t2.scheme = OR_TIME_PREDICTOR;
+    or_time_opts t2 = *to;                   /* Predictor_New, _BDF or _TRBDF2 */
+    if (t2.scheme != OR_TIME_NEW_BDF && t2.scheme != OR_TIME_TRBDF2) t2.scheme = OR_TIME_PREDICTOR;
     eu_loop2 c = { { { nel, nnodes, NEQ, lm, Id, A, inv }, nnodes, nel, neq, x, y, type, invp, ien, prob, R, bd,
-                     solver_tol, kmax, lmax }, uB, aB, cond, DaB, dnmv, lm };
-    int steps = or_time_integrate_ex(neq, prob->alpha, prob->dt, &t2, eu_correct2, eu_predict2, &c, u, a, st);
+                     solver_tol, kmax, lmax }, uB, aB, cond, DaB, dnmv, lm, uB1, uB2 };
+    int steps = or_time_integrate_ex(neq, prob->alpha, prob->dt, &t2, eu_correct2, eu_bubble2, &c, u, a, st);
     free(lm); free(Id); free(A); free(R); free(bd); free(inv); free(cond); free(DaB); free(dnmv);
+    free(uB1); free(uB2);
     return steps;
 }

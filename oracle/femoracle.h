@@ -224,10 +224,11 @@ typedef struct {
     double final_time;     /* FinalTime                                                 */
     double time_tol;       /* TimeIntegrationTolerance                                  */
     int max_steps;         /* bound on the time steps (0: none; not in the reference)   */
-    int scheme;            /* OR_TIME_PREDICTOR, OR_TIME_BDF or OR_TIME_TRBDF2          */
+    int scheme;            /* OR_TIME_PREDICTOR, OR_TIME_BDF, OR_TIME_TRBDF2 or
+                              OR_TIME_NEW_BDF (Predictor_New_BDF's u loop)           */
 } or_time_opts;
 
-enum { OR_TIME_PREDICTOR = 0, OR_TIME_BDF = 1, OR_TIME_TRBDF2 = 2 };
+enum { OR_TIME_PREDICTOR = 0, OR_TIME_BDF = 1, OR_TIME_TRBDF2 = 2, OR_TIME_NEW_BDF = 4 };
 
 typedef struct {
     int steps, corrections, gmres_iterations;
@@ -245,12 +246,23 @@ typedef int (*or_correction_fn)(void *ctx, double alpha_b, double dt_b, const do
  * the steps (a TR-BDF2 step is its TR and BDF2 stages), -1 on failure. */
 int or_time_integrate(int neq, double alpha, double dt, const or_time_opts *to, or_correction_fn correct,
                       void *ctx, double *u, double *a, or_time_stats *st);
-/* The same with a hook called once per OR_TIME_PREDICTOR step after the
- * prediction of u and a (coef = (1 - alpha) dt): Predictor_New.c:78-83
- * predicts its per-element bubble unknowns there. */
-typedef void (*or_predict_fn)(void *ctx, double coef);
+/* The same with the bubble operations of the Predictor2 loops
+ * (Predictor_New.c, Predictor_New_BDF.c, Predictor_New_TRBDF2.c), called
+ * where those loops act on their per-element unknowns uB, aB (the
+ * correction of uB, aB from Da stays in `correct`):
+ *   OR_B_PREDICT        uB += c1 aB, aB = 0
+ *   OR_B_TRBDF2_START   uB = the element centroid of u (uB_InitialSolution)
+ *   OR_B_TRBDF2_COMBINE uB = c1 uB - c2 uB_old, aB = 0
+ *   OR_B_TRBDF2_SAVE    uB_old = uB
+ *   OR_B_BDF_START      uB1 = uB, aB = 0
+ *   OR_B_BDF_SAVE2      uB2 = uB
+ *   OR_B_BDF_COMBINE    uB = c1 uB2 - c2 uB1, aB = 0
+ *   OR_B_BDF_SHIFT      uB1 = uB2, uB2 = uB */
+enum { OR_B_PREDICT = 0, OR_B_TRBDF2_START, OR_B_TRBDF2_COMBINE, OR_B_TRBDF2_SAVE, OR_B_BDF_START,
+       OR_B_BDF_SAVE2, OR_B_BDF_COMBINE, OR_B_BDF_SHIFT };
+typedef void (*or_bubble_fn)(void *ctx, int op, double c1, double c2, const double *u);
 int or_time_integrate_ex(int neq, double alpha, double dt, const or_time_opts *to, or_correction_fn correct,
-                         or_predict_fn predict, void *ctx, double *u, double *a, or_time_stats *st);
+                         or_bubble_fn bubble, void *ctx, double *u, double *a, or_time_stats *st);
 
 /* Predictor_Old.c:6-134 with EBE 12x12 blocks, BlockDiag (4x4, the
  * reference's inverse) and GMRES.  u: initial state on entry (the
@@ -259,9 +271,11 @@ int or_euler_predictor(int nnodes, int nel, const double *x, const double *y, co
                        const int *invp, const int *ien, int neq, const or_euler_problem *prob,
                        const or_time_opts *to, double solver_tol, int kmax, int lmax,
                        double *u, double *a, or_time_stats *st);
-/* Predictor_New with Build_M_F_DD_Transiente, calculate_DaB, BlockDiag (the
- * reference's 4x4 inverse) and GMRES.  u: initial state in, final out; a
- * (neq), uB, aB (4 nel) receive the final du/dt and bubble unknowns. */
+/* Predictor_New (to->scheme OR_TIME_PREDICTOR), Predictor_New_BDF
+ * (OR_TIME_NEW_BDF) or Predictor_New_TRBDF2 (OR_TIME_TRBDF2) with
+ * Build_M_F_DD_Transiente, calculate_DaB, BlockDiag (the reference's 4x4
+ * inverse) and GMRES.  u: initial state in, final out; a (neq), uB, aB
+ * (4 nel) receive the final du/dt and bubble unknowns. */
 int or_euler_predictor2(int nnodes, int nel, const double *x, const double *y, const int *type,
                         const int *invp, const int *ien, int neq, const or_euler_problem *prob,
                         const or_time_opts *to, double solver_tol, int kmax, int lmax,

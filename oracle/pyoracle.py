@@ -447,7 +447,8 @@ def ref_euler_predictor(prob, topts: TimeOpts, tol=1e-10, kmax=25, lmax=1000, dr
     u = np.zeros(m.neq + 1)
     t = _c_dbl(0.0)
     R = ref_euler(DROPIN_SO["euler"]) if dropin else ref_euler()
-    if topts.scheme == 3:      # "Predictor2": DD + YZBeta with Build_M_F_DD_Transiente
+    if topts.scheme in (3, 4) or getattr(prob, "form", 0) == 2:
+        # "Predictor2" (Predictor_New, _BDF, or _TRBDF2 with form 2): DD + YZBeta, Build_M_F_DD_Transiente
         R.fr_eu_set_form(2)
         R.fr_eu_set_invY(np.ascontiguousarray(getattr(prob, "invY", np.ones(4)), dtype=np.float64))
     else:

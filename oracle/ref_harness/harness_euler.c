@@ -270,7 +270,8 @@ void fr_eu_ebemv(int nnodes, int nel, const double *x, const double *y, const in
 /* The predictor/multicorrector time loops of the reference.
  * topt: stop_by_norm, max_corrections, correction_tol, steady_state,
  *       final_time, time_tol, scheme (0 Predictor_Old, 1 Predictor_Old_BDF,
- *       2 Predictor_New_TRBDF2, 3 Predictor_New); solver: kmax, lmax, tol. */
+ *       2 Predictor_New_TRBDF2, 3 Predictor_New, 4 Predictor_New_BDF); solver:
+ *       kmax, lmax, tol. */
 int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
                     const int *ien, int neq, const double *prm, const double *coef, int wall,
                     const double *init, const double *topt, int kmax, int lmax, double tol, double *u_out,
@@ -297,6 +298,8 @@ int fr_eu_predictor(int nnodes, int nel, const double *x, const double *y, const
     c.S.uB = NULL;
     if (topt[6] == 3.0)
         Predictor_New(&c.P, &c.M, &c.S, &c.F, &c.O);
+    else if (topt[6] == 4.0)
+        Predictor_New_BDF(&c.P, &c.M, &c.S, &c.F, &c.O);
     else if (topt[6] == 1.0)
         Predictor_Old_BDF(&c.P, &c.M, &c.S, &c.F, &c.O);
     else if (topt[6] == 2.0)
@@ -417,4 +420,32 @@ void fr_eu_mfdd_build(int nnodes, int nel, const double *x, const double *y, con
     free(c.Aux.invN2); free(c.Aux.delta_old_NMV);
     c.S.du = c.S.duB = NULL;
     fr_eu_free(&c);
+}
+
+/* uB_InitialSolution.c:3-111 as its second branch intends: the reference
+ * tests a prescribed dof with invP_id != NEQ, but Preprocess.c:173 (and
+ * this harness) mark them with -1, so the reference file reads u[-1] there.
+ * This harness links this copy instead: prescribed dofs take their
+ * prescribed value. */
+int uB_InitialSolution(ParametersType *Parameters, FemStructsType *FemStructs, FemFunctionsType *FemFunctions,
+                       double *u, double *uB)
+{
+    const double third = 1.0 / 3.0;
+    NodeType *Node = FemStructs->Node;
+    ElementType *El = FemStructs->Element;
+    int e, v, k, i;
+    for (e = 0; e < Parameters->nel; e++) {
+        double Ue[12];
+        for (v = 0; v < 3; v++) {
+            const int J = El[e].Vertex[v];
+            const double X = Node[J].x, Y = Node[J].y;
+            for (k = 0; k < 4; k++) {
+                double pv = k == 0 ? FemFunctions->rhopresc(X, Y) : k == 1 ? FemFunctions->v1presc(X, Y)
+                          : k == 2 ? FemFunctions->v2presc(X, Y) : FemFunctions->epresc(X, Y);
+                Ue[4 * v + k] = Node[J].Type[k] != 0 ? u[Node[J].invP_id[k]] : pv;
+            }
+        }
+        for (i = 0; i < 4; i++) uB[4 * e + i] = (Ue[i] + Ue[i + 4] + Ue[i + 8]) * third;
+    }
+    return 0;
 }

@@ -80,7 +80,7 @@ int or_time_integrate(int neq, double alpha, double dt, const or_time_opts *to, 
 }
 
 int or_time_integrate_ex(int neq, double alpha, double dt, const or_time_opts *to, or_correction_fn correct,
-                         or_predict_fn predict, void *ctx, double *u, double *a, or_time_stats *st)
+                         or_bubble_fn bubble, void *ctx, double *u, double *a, or_time_stats *st)
 {
     size_t nb = sizeof(double) * ((size_t)neq + 1);
     double *u_old = calloc(1, nb), *u1 = calloc(1, nb), *u2 = calloc(1, nb);
@@ -95,7 +95,7 @@ int or_time_integrate_ex(int neq, double alpha, double dt, const or_time_opts *t
             memcpy(u_old, u, sizeof(double) * (size_t)neq);
             axpy(neq, (1.0 - alpha) * dt, a, u);                      /* prediction */
             memset(a, 0, sizeof(double) * (size_t)neq);
-            if (predict) predict(ctx, (1.0 - alpha) * dt);              /* Predictor_New.c:82-83 */
+            if (bubble) bubble(ctx, OR_B_PREDICT, (1.0 - alpha) * dt, 0.0, u);  /* Predictor_New.c:82-83 */
             if ((rc = multicorrect(&L, alpha, dt, alpha * dt, u, a))) break;
         } while (!stop_time(&L, u, u_old, t, dt));
     } else if (to->scheme == OR_TIME_BDF) {
@@ -127,21 +127,52 @@ int or_time_integrate_ex(int neq, double alpha, double dt, const or_time_opts *t
         const double B = (1.0 - lambda) * (1.0 - lambda) / (lambda * (2.0 - lambda));
         const double dtTR = lambda * dt, dtBDF2 = (1.0 - lambda) * dt;
         const double aTR = 0.5, aBDF2 = 1.0 / (2.0 - lambda);
+        if (bubble) bubble(ctx, OR_B_TRBDF2_START, 0.0, 0.0, u);     /* Predictor_New_TRBDF2.c:63 */
         memcpy(u_old, u, sizeof(double) * (size_t)neq);
         do {
             L.steps++;
             t += dtTR;                                                /* TR stage */
             axpy(neq, aTR * dtTR, a, u);
             memset(a, 0, sizeof(double) * (size_t)neq);
+            if (bubble) bubble(ctx, OR_B_PREDICT, aTR * dtTR, 0.0, u);
             if ((rc = multicorrect(&L, aTR, dtTR, aTR * dtTR, u, a))) break;
             t += dtBDF2;                                              /* BDF2 stage */
             for (i = 0; i < neq; i++) {
                 u[i] = A * u[i] - B * u_old[i];
                 a[i] = 0.0;
             }
+            if (bubble) bubble(ctx, OR_B_TRBDF2_COMBINE, A, B, u);
             if ((rc = multicorrect(&L, aBDF2, dtBDF2, aBDF2 * dtBDF2, u, a))) break;
             memcpy(u_old, u, sizeof(double) * (size_t)neq);
+            if (bubble) bubble(ctx, OR_B_TRBDF2_SAVE, 0.0, 0.0, u);
         } while (!stop_time(&L, u, u_old, t, dtBDF2));
+    } else if (to->scheme == OR_TIME_NEW_BDF) {
+        /* Predictor_New_BDF.c:54-184: a BDF1 step with Alpha_Build = 1
+         * (u += dt Da), then BDF2 steps with Alpha_Build = 2/3; each step
+         * keeps u_old = u before its prediction for the steady-state test */
+        const double four_thirds = 4.0 / 3.0, two_thirds = 2.0 / 3.0, one_third = 1.0 / 3.0;
+        L.steps++;
+        t += dt;
+        memcpy(u1, u, sizeof(double) * (size_t)neq);
+        memset(a, 0, sizeof(double) * (size_t)neq);
+        if (bubble) bubble(ctx, OR_B_BDF_START, 0.0, 0.0, u);
+        rc = multicorrect(&L, 1.0, dt, dt, u, a);
+        memcpy(u2, u, sizeof(double) * (size_t)neq);
+        if (bubble) bubble(ctx, OR_B_BDF_SAVE2, 0.0, 0.0, u);
+        if (!rc) do {
+            L.steps++;
+            t += dt;
+            memcpy(u_old, u, sizeof(double) * (size_t)neq);
+            for (i = 0; i < neq; i++) {
+                u[i] = four_thirds * u2[i] - one_third * u1[i];
+                a[i] = 0.0;
+            }
+            if (bubble) bubble(ctx, OR_B_BDF_COMBINE, four_thirds, one_third, u);
+            if ((rc = multicorrect(&L, 2.0 / 3.0, dt, two_thirds * dt, u, a))) break;
+            memcpy(u1, u2, sizeof(double) * (size_t)neq);
+            memcpy(u2, u, sizeof(double) * (size_t)neq);
+            if (bubble) bubble(ctx, OR_B_BDF_SHIFT, 0.0, 0.0, u);
+        } while (!stop_time(&L, u, u_old, t, dt));
     } else {
         rc = -1;
     }

@@ -470,9 +470,11 @@ typedef struct {
     double *uB, *aB, *cond, *DaB;
 } tt_loop2;
 
-static void tt_predict2(void *p, double coef)
+static void tt_predict2(void *p, int op, double coef, double c2, const double *u)
 {
     tt_loop2 *c = (tt_loop2 *)p;
+    (void)c2; (void)u;
+    if (op != OR_B_PREDICT) return;          /* Predictor_New has no other bubble step */
     for (int e = 0; e < c->base.nel; e++) c->uB[e] += coef * c->aB[e];   /* :82-83 */
     memset(c->aB, 0, sizeof(double) * (size_t)c->base.nel);
 }

@@ -291,6 +291,15 @@ def write_euler_predictor2():
     U, its, t = O.ref_euler_predictor(p, to, 1e-10, 25, 1000)
     out["U"], out["its"] = U, np.array([its])
     print("euler predictor2 gmres", its)
+    # "Predictor2_BDF" (Predictor_New_BDF) and "Predictor2_TRBDF2"
+    # (Predictor_New_TRBDF2 with the bubble build; the harness links a
+    # uB_InitialSolution that reads prescribed values, see harness_euler.c)
+    p.form = 2
+    for scheme in (4, 2):
+        to = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6, 0, scheme)
+        U, its, t = O.ref_euler_predictor(p, to, 1e-10, 25, 1000)
+        out[f"U_s{scheme}"], out[f"its_s{scheme}"] = U, np.array([its])
+        print("euler predictor2 scheme", scheme, "gmres", its)
     np.savez_compressed(os.path.join(HERE, "euler_predictor2_ref.npz"), **out)
 
 

@@ -214,6 +214,20 @@ def test_predictor2_loop_matches_reference_golden(p2gold):
     assert np.abs(uB).max() > 0                      # the bubbles move
 
 
+@pytest.mark.parametrize("scheme", [4, 2], ids=["predictor2_bdf", "predictor2_trbdf2"])
+def test_predictor2_bdf_trbdf2_match_reference_golden(p2gold, scheme):
+    """Predictor_New_BDF ("Predictor2_BDF": a BDF1 step with Alpha_Build 1,
+    then BDF2 with 2/3, u_old kept per step) and Predictor_New_TRBDF2
+    ("Predictor2_TRBDF2": uB from the initial state, TR and BDF2 stages on
+    uB too) with Build_M_F_DD_Transiente: final state and GMRES iterations
+    equal the reference's."""
+    p = _p2_problem()
+    to = O.TimeOpts(0, 2, 1e-3, 0, 3 * p.dt + 1e-12, 1e-6, 0, scheme)
+    u, a, uB, aB, st = O.euler_predictor2(p, to, 1e-10, 25, 1000)
+    assert st["gmres_iterations"] == int(p2gold[f"its_s{scheme}"][0])
+    assert np.array_equal(u, p2gold[f"U_s{scheme}"])
+
+
 @pytest.mark.skipif(O.ref_euler() is None, reason="reference build (oracle/_ref) not present")
 def test_predictor2_against_reference_build():
     p = _p2_problem(11)
