@@ -490,8 +490,26 @@ typedef struct {
  *                      Predictor_Old's steps plus the bubble unknowns,
  *                      predicted with u (uB += (1 - alpha) dt aB, aB = 0)
  *                      and corrected after each solve from Da
- *                      (calculate_DaB: aB += DaB, uB += alpha dt DaB). */
-enum { FG_TIME_PREDICTOR = 0, FG_TIME_BDF = 1, FG_TIME_TRBDF2 = 2, FG_TIME_PREDICTOR2 = 3 };
+ *                      (calculate_DaB: aB += DaB, uB += alpha dt DaB).
+ *   FG_TIME_PREDICTOR2_BDF    "Predictor2_BDF"  Predictor_New_BDF.c:54-184
+ *                      (fg_euler_predictor, DD): a BDF1 step with
+ *                      Alpha_Build = 1 (u += dt Da), then BDF2 steps with
+ *                      Alpha_Build = 2/3; u_old = u before each BDF2
+ *                      prediction (the steady-state test compares with the
+ *                      previous step); the bubble unknowns follow the same
+ *                      combinations.
+ *   FG_TIME_PREDICTOR2_TRBDF2 "Predictor2_TRBDF2"  Predictor_New_TRBDF2.c
+ *                      (fg_euler_predictor, DD): the TR-BDF2 stages of
+ *                      FG_TIME_TRBDF2 with the bubble unknowns, uB starting
+ *                      from the element centroids of the initial state
+ *                      (uB_InitialSolution; prescribed dofs take their
+ *                      prescribed value -- the reference reads u[-1] there,
+ *                      testing invP_id against NEQ where Preprocess.c:173
+ *                      stores -1).  The Predictor1 DD build is not offered
+ *                      with FG_TIME_TRBDF2 (the reference pairs it with
+ *                      Predictor_Old_TRBDF2, which is not restated). */
+enum { FG_TIME_PREDICTOR = 0, FG_TIME_BDF = 1, FG_TIME_TRBDF2 = 2, FG_TIME_PREDICTOR2 = 3,
+       FG_TIME_PREDICTOR2_BDF = 4, FG_TIME_PREDICTOR2_TRBDF2 = 5 };
 
 typedef struct {
     int steps;

@@ -617,15 +617,46 @@ __global__ void k_euler_bubble_correct(int nel, int ld, int n, const int *__rest
     }
 }
 
-// Predictor_New.c:82-83 for the four bubble unknowns: uB += coef aB, aB = 0
-__global__ void k_euler_bubble_predict(int nel, int ld, double coef, double *__restrict__ bub)
+// The bubble steps of Predictor_New.c, Predictor_New_BDF.c and
+// Predictor_New_TRBDF2.c on the four unknowns of each element (BubbleOp;
+// planes 0-3 uB, 4-7 aB, 62-65 uB_old / uB1, 66-69 uB2).  kBubbleTrStart
+// is uB_InitialSolution.c: the element centroids of the state, prescribed
+// dofs taking their prescribed values.
+__global__ void k_euler_bubble_op(int nel, int ld, int n, int op, double c1, double c2,
+                                  const int *__restrict__ gien, const int *__restrict__ node_dof,
+                                  const double *__restrict__ up, const double *__restrict__ u,
+                                  double *__restrict__ bub)
 {
     const int pos = blockIdx.x * blockDim.x + threadIdx.x;
     if (pos >= nel) return;
+    const double third = 1.0 / 3.0;
+    double Ue[12];
+    if (op == kBubbleTrStart) {
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+            const int J = gien[(size_t)v * ld + pos];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int d = node_dof[4 * J + k];
+                Ue[4 * v + k] = d == n ? up[4 * J + k] : u[d];
+            }
+        }
+    }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        bub[(size_t)r * ld + pos] += coef * bub[(size_t)(4 + r) * ld + pos];
-        bub[(size_t)(4 + r) * ld + pos] = 0.0;
+        double *uB = bub + (size_t)r * ld + pos, *aB = bub + (size_t)(4 + r) * ld + pos;
+        double *o1 = bub + (size_t)(62 + r) * ld + pos, *o2 = bub + (size_t)(66 + r) * ld + pos;
+        switch (op) {
+        case kBubblePredict: *uB += c1 * *aB; *aB = 0.0; break;
+        case kBubbleTrStart: *uB = (Ue[r] + Ue[r + 4] + Ue[r + 8]) * third; break;
+        case kBubbleTrCombine: *uB = c1 * *uB - c2 * *o1; *aB = 0.0; break;
+        case kBubbleTrSave: *o1 = *uB; break;
+        case kBubbleBdfStart: *o1 = *uB; *aB = 0.0; break;
+        case kBubbleBdfSave2: *o2 = *uB; break;
+        case kBubbleBdfCombine: *uB = c1 * *o2 - c2 * *o1; *aB = 0.0; break;
+        case kBubbleBdfShift: *o1 = *o2; *o2 = *uB; break;
+        default: break;
+        }
     }
 }
 
@@ -666,11 +697,15 @@ int euler_bubble_correct_device(fg_system *s, const double *Da_dev, double coef,
     return FG_OK;
 }
 
-int euler_bubble_predict_device(fg_system *s, double coef, cudaStream_t st)
+int euler_bubble_op_device(fg_system *s, int op, double c1, double c2, const double *u_dev, cudaStream_t st)
 {
     const Topology &t = s->topo;
+    if (s->bubble_nb != 4) { set_error("no Euler Predictor2 build on this system"); return FG_ERR_STATE; }
+    if (op < kBubblePredict || op > kBubbleBdfShift) { set_error("unknown bubble step"); return FG_ERR_ARG; }
     if (t.nel > 0) {
-        k_euler_bubble_predict<<<(t.nel + 255) / 256, 256, 0, st>>>(t.nel, s->nel_pad, coef, s->bubble.as<double>());
+        k_euler_bubble_op<<<(t.nel + 255) / 256, 256, 0, st>>>(t.nel, s->nel_pad, t.n, op, c1, c2, s->gien.as<int>(),
+                                                              s->node_dof.as<int>(), s->gup.as<double>(), u_dev,
+                                                              s->bubble.as<double>());
         FG_CUDA(cudaGetLastError());
         count_launches(1);
     }

@@ -925,13 +925,18 @@ int download_solution(fg_system *s, double *X, cudaStream_t st)
 //                      unknowns (TR stage alpha 1/2 over lambda dt, BDF2
 //                      stage alpha 1/(2 - lambda) over (1 - lambda) dt)
 //   FG_TIME_PREDICTOR2 Predictor_New.c:67-159: the Predictor_Old steps plus
-//                      the hooks of the per-element bubble unknowns
-//                      (predicted after u and a, corrected from each Da)
-// Per-step and per-correction hooks: predict(coef = (1 - alpha) dt) after
-// the prediction of u and a, corrected(Da, coef = alpha dt) after a += Da
-// and u += coef Da.
+//                      the per-element bubble unknowns (predicted after u
+//                      and a, corrected from each Da)
+//   FG_TIME_PREDICTOR2_BDF    Predictor_New_BDF.c:54-184 (BDF1 with
+//                      Alpha_Build 1 and u += dt Da, then BDF2 with 2/3;
+//                      u_old = u before each BDF2 prediction), with bubbles
+//   FG_TIME_PREDICTOR2_TRBDF2 Predictor_New_TRBDF2.c: FG_TIME_TRBDF2's stages
+//                      with bubbles, uB starting from the element centroids
+// The bubble hooks: bubble(op, c1, c2, u) at the points where those loops
+// act on uB and aB (BubbleOp), corrected(Da, coef = alpha dt) after
+// a += Da and u += coef Da.
 struct LoopHooks {
-    std::function<int(double)> predict;
+    std::function<int(int, double, double, const double *)> bubble;
     std::function<int(const double *, double)> corrected;
 };
 
@@ -945,15 +950,18 @@ static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble,
         return FG_ERR_ARG;
     }
     if (to->max_corrections < 1 || !(dt > 0)) { set_error("max_corrections >= 1 and dt > 0 required"); return FG_ERR_ARG; }
-    if (to->scheme < FG_TIME_PREDICTOR || to->scheme > FG_TIME_PREDICTOR2) {
-        set_error("time scheme must be FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2 or FG_TIME_PREDICTOR2");
+    if (to->scheme < FG_TIME_PREDICTOR || to->scheme > FG_TIME_PREDICTOR2_TRBDF2) {
+        set_error("time scheme must be one of FG_TIME_PREDICTOR .. FG_TIME_PREDICTOR2_TRBDF2");
         return FG_ERR_ARG;
     }
-    const bool p2 = to->scheme == FG_TIME_PREDICTOR2;
+    const bool p2 = to->scheme >= FG_TIME_PREDICTOR2;
     if (p2 && !hooks) {
-        set_error("FG_TIME_PREDICTOR2 runs the transient transport DD build (fg_tt_predictor)");
+        set_error("the Predictor2 schemes run the DD bubble builds (fg_tt_predictor, fg_euler_predictor)");
         return FG_ERR_UNSUPPORTED;
     }
+    auto bubble = [&](int op, double c1, double c2) -> int {
+        return p2 && hooks->bubble ? hooks->bubble(op, c1, c2, s->state_u.as<double>()) : FG_OK;
+    };
     auto t0 = std::chrono::steady_clock::now();
     const int n = s->topo.n;
     fg_system *one[1] = {s};
@@ -966,7 +974,9 @@ static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble,
         (r = stage(s, s->state_u, vb)) || (r = stage(s, s->state_a, vb)) || (r = stage(s, s->state_old, vb)) ||
         (r = stage(s, s->norm_part, norm_scratch_bytes())))
         return r;
-    if (to->scheme == FG_TIME_BDF && ((r = stage(s, s->state_u1, vb)) || (r = stage(s, s->state_u2, vb)))) return r;
+    if ((to->scheme == FG_TIME_BDF || to->scheme == FG_TIME_PREDICTOR2_BDF) &&
+        ((r = stage(s, s->state_u1, vb)) || (r = stage(s, s->state_u2, vb))))
+        return r;
     double *du = s->state_u.as<double>(), *da = s->state_a.as<double>(), *dold = s->state_old.as<double>();
     FG_CUDA(cudaMemsetAsync(s->state_u.p, 0, vb, s->stream));
     if ((r = state_in(s, u, du))) return r;
@@ -1034,15 +1044,36 @@ static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble,
         return FG_OK;
     };
     bool stop_time = false;
-    if (to->scheme == FG_TIME_PREDICTOR || p2) {
+    if (to->scheme == FG_TIME_PREDICTOR || to->scheme == FG_TIME_PREDICTOR2) {
         do {
             ++steps;
             t += dt;
             if ((r = copy(dold, du))) return r;
             if ((r = axpy_device(n, (1.0 - alpha) * dt, da, du, s->stream))) return r;      // prediction
             FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
-            if (p2 && hooks->predict && (r = hooks->predict((1.0 - alpha) * dt))) return r;
+            if ((r = bubble(kBubblePredict, (1.0 - alpha) * dt, 0.0))) return r;
             if ((r = multicorrect(alpha, dt, alpha * dt)) || (r = time_stop(dt, stop_time))) return r;
+        } while (!stop_time);
+    } else if (to->scheme == FG_TIME_PREDICTOR2_BDF) {
+        const double four_thirds = 4.0 / 3.0, two_thirds = 2.0 / 3.0, one_third = 1.0 / 3.0;
+        double *u1 = s->state_u1.as<double>(), *u2 = s->state_u2.as<double>();
+        ++steps;                                                                          // BDF1, Alpha_Build 1
+        t += dt;
+        if ((r = copy(u1, du))) return r;
+        FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+        if ((r = bubble(kBubbleBdfStart, 0.0, 0.0))) return r;
+        if ((r = multicorrect(1.0, dt, dt)) || (r = copy(u2, du)) || (r = bubble(kBubbleBdfSave2, 0.0, 0.0))) return r;
+        do {                                                                              // BDF2, Alpha_Build 2/3
+            ++steps;
+            t += dt;
+            if ((r = copy(dold, du))) return r;
+            if ((r = lincomb_device(n, four_thirds, u2, one_third, u1, du, s->stream))) return r;
+            FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+            if ((r = bubble(kBubbleBdfCombine, four_thirds, one_third))) return r;
+            if ((r = multicorrect(2.0 / 3.0, dt, two_thirds * dt))) return r;
+            if ((r = copy(u1, u2)) || (r = copy(u2, du)) || (r = bubble(kBubbleBdfShift, 0.0, 0.0)) ||
+                (r = time_stop(dt, stop_time)))
+                return r;
         } while (!stop_time);
     } else if (to->scheme == FG_TIME_BDF) {
         const double four_thirds = 4.0 / 3.0, two_thirds = 2.0 / 3.0, one_third = 1.0 / 3.0;
@@ -1066,18 +1097,21 @@ static int time_loop(fg_system *s, double dt, double alpha, Assemble &&assemble,
         const double B = (1.0 - lambda) * (1.0 - lambda) / (lambda * (2.0 - lambda));
         const double dtTR = lambda * dt, dtBDF2 = (1.0 - lambda) * dt;
         const double aTR = 0.5, aBDF2 = 1.0 / (2.0 - lambda);
-        if ((r = copy(dold, du))) return r;
+        if ((r = bubble(kBubbleTrStart, 0.0, 0.0)) || (r = copy(dold, du))) return r;
         do {
             ++steps;
             t += dtTR;                                                                    // TR stage
             if ((r = axpy_device(n, aTR * dtTR, da, du, s->stream))) return r;
             FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+            if ((r = bubble(kBubblePredict, aTR * dtTR, 0.0))) return r;
             if ((r = multicorrect(aTR, dtTR, aTR * dtTR))) return r;
             t += dtBDF2;                                                                  // BDF2 stage
             if ((r = lincomb_device(n, A, du, B, dold, du, s->stream))) return r;
             FG_CUDA(cudaMemsetAsync(da, 0, nb, s->stream));
+            if ((r = bubble(kBubbleTrCombine, A, B))) return r;
             if ((r = multicorrect(aBDF2, dtBDF2, aBDF2 * dtBDF2))) return r;
-            if ((r = copy(dold, du)) || (r = time_stop(dtBDF2, stop_time))) return r;
+            if ((r = copy(dold, du)) || (r = bubble(kBubbleTrSave, 0.0, 0.0)) || (r = time_stop(dtBDF2, stop_time)))
+                return r;
         } while (!stop_time);
     }
     if ((r = vec_out(s, du, s->h_vec, s->ws.r64.as<double>()))) return r;
@@ -1106,10 +1140,16 @@ int euler_predictor_hooked(fg_system *s, const fg_euler_coeffs *c, const fg_solv
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
     // the DD element state starts at zero with the loop (Predictor_Old.c callocs uB and delta_old)
     if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
-    if (to->scheme == FG_TIME_PREDICTOR2) {
-        // "Predictor2" with "DD" (setStabilizationForm.c:47-50), ShockCapture "YZBeta"
+    if (c->form == FG_EULER_DD && to->scheme == FG_TIME_TRBDF2) {
+        set_error("the DD build with TR-BDF2 is Predictor2_TRBDF2 (FG_TIME_PREDICTOR2_TRBDF2); the reference pairs "
+                  "the Predictor1 DD build with Predictor_Old_TRBDF2, which is not restated");
+        return FG_ERR_UNSUPPORTED;
+    }
+    if (to->scheme >= FG_TIME_PREDICTOR2) {
+        // "Predictor2", "Predictor2_BDF", "Predictor2_TRBDF2" with "DD" (setStabilizationForm.c:47-58),
+        // ShockCapture "YZBeta"
         if (c->form != FG_EULER_DD) {
-            set_error("FG_TIME_PREDICTOR2 needs the DD form (FG_EULER_DD)");
+            set_error("the Predictor2 schemes need the DD form (FG_EULER_DD)");
             return FG_ERR_UNSUPPORTED;
         }
         int r = bubble_alloc(s, 4);
@@ -1117,7 +1157,9 @@ int euler_predictor_hooked(fg_system *s, const fg_euler_coeffs *c, const fg_solv
         // uB, aB and Delta_YZBetaNMV's state start at zero (Predictor_New.c calloc)
         FG_CUDA(cudaMemsetAsync(s->bubble.p, 0, s->bubble.bytes, s->stream));
         LoopHooks h;
-        h.predict = [&](double coef) { return euler_bubble_predict_device(s, coef, s->stream); };
+        h.bubble = [&](int op, double c1, double c2, const double *u_dev) {
+            return euler_bubble_op_device(s, op, c1, c2, u_dev, s->stream);
+        };
         h.corrected = [&](const double *Da, double coef) {
             return euler_bubble_correct_device(s, Da, coef, nullptr, s->stream);
         };
@@ -1174,6 +1216,11 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
     if (!s || !c || !o || !to || !u) { set_error("NULL argument"); return FG_ERR_ARG; }
     // the DD shock-capture state starts at zero with the loop (Predictor_Old.c:30 callocs delta_old)
     if (s->shock_state.p) FG_CUDA(cudaMemsetAsync(s->shock_state.p, 0, s->shock_state.bytes, s->stream));
+    if (to->scheme == FG_TIME_PREDICTOR2_BDF || to->scheme == FG_TIME_PREDICTOR2_TRBDF2) {
+        set_error("the transient transport driver offers Predictor2 only (its _BDF and _TRBDF2 options are "
+                  "commented out, setStabilizationForm.c:55-62)");
+        return FG_ERR_UNSUPPORTED;
+    }
     if (to->scheme == FG_TIME_PREDICTOR2) {
         // "Predictor2" exists for the DD form only (setStabilizationForm.c:51-54)
         if (c->c.form != FG_TRANSPORT_DD) {
@@ -1185,7 +1232,9 @@ int fg_tt_predictor(fg_system *s, const fg_tt_coeffs *c, const fg_solver_opts *o
         // uB and aB start at zero (Predictor_New.c:24,36 calloc them)
         FG_CUDA(cudaMemsetAsync(s->bubble.p, 0, s->bubble.bytes, s->stream));
         LoopHooks h;
-        h.predict = [&](double coef) { return tt_bubble_predict_device(s, coef, s->stream); };
+        h.bubble = [&](int op, double c1, double, const double *) {
+            return op == kBubblePredict ? tt_bubble_predict_device(s, c1, s->stream) : FG_OK;
+        };
         h.corrected = [&](const double *Da, double coef) {
             return tt_bubble_correct_device(s, Da, coef, nullptr, s->stream);
         };

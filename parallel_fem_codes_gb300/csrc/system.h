@@ -55,7 +55,7 @@ struct fg_system {
     fg::DevMem shock_state;            // YZBeta Re_old, delta_old [2 * nel_pad]
     // Predictor2 bubble planes of nel_pad doubles, nb = 1 (transient
     // transport: uB, aB, invN2, R2, M2[3]) or 4 (Euler: uB[4], aB[4], invN2,
-    // R2[4], M2[4][12], Delta_YZBetaNMV's state)
+    // R2[4], M2[4][12], Delta_YZBetaNMV's state, uB_old / uB1 [4], uB2 [4])
     fg::DevMem bubble;
     int bubble_nb = 0;
     bool ns_geometry_ok = false, eu_geometry_ok = false;
@@ -251,7 +251,18 @@ int tt_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev,
 // the bubble planes (uB, aB as duB); F_dev the load.  The correction
 // (calculate_DaB from Da, internal numbering) updates aB and uB with coef =
 // alpha dt, or writes DaB into DaB_dev (element positions) when given.
-constexpr int kBubblePlanes = 7, kBubblePlanesEuler = 62;
+constexpr int kBubblePlanes = 7, kBubblePlanesEuler = 70;
+// the bubble steps of the Predictor2 loops (Predictor_New*.c)
+enum BubbleOp {
+    kBubblePredict = 0,     // uB += c1 aB, aB = 0
+    kBubbleTrStart,         // uB = element centroids of u (uB_InitialSolution)
+    kBubbleTrCombine,       // uB = c1 uB - c2 uB_old, aB = 0
+    kBubbleTrSave,          // uB_old = uB
+    kBubbleBdfStart,        // uB1 = uB, aB = 0
+    kBubbleBdfSave2,        // uB2 = uB
+    kBubbleBdfCombine,      // uB = c1 uB2 - c2 uB1, aB = 0
+    kBubbleBdfShift         // uB1 = uB2, uB2 = uB
+};
 int bubble_alloc(fg_system *s, int nb);
 int tt_mfdd_assemble_device(fg_system *s, const fg_tt_coeffs *c, const double *u_dev, const double *du_dev,
                             double *F_dev, cudaStream_t st);
@@ -262,7 +273,7 @@ int tt_bubble_predict_device(fg_system *s, double coef, cudaStream_t st);
 int euler_mfdd_assemble_device(fg_system *s, const fg_euler_coeffs *c, const double *u_dev, const double *du_dev,
                                double *F_dev, cudaStream_t st);
 int euler_bubble_correct_device(fg_system *s, const double *Da_dev, double coef, double *DaB_dev, cudaStream_t st);
-int euler_bubble_predict_device(fg_system *s, double coef, cudaStream_t st);
+int euler_bubble_op_device(fg_system *s, int op, double c1, double c2, const double *u_dev, cudaStream_t st);
 // The correction solve of a time loop: the system's resident right-hand
 // side (B = rhs_b, Ftrue = rhs_f, device, internal numbering) solved into
 // ws.x with cfg; stats receives the result.  The time loops solve alone by

@@ -22,6 +22,7 @@ FG_OP_EBE, FG_OP_CSR = 0, 1
 FG_SETUP_ACCUMULATE, FG_SETUP_REF_QUIRKS = 1, 2
 FG_PREC_FP64, FG_PREC_MIXED, FG_PREC_MIXED16 = 64, 32, 16
 FG_TIME_PREDICTOR, FG_TIME_BDF, FG_TIME_TRBDF2, FG_TIME_PREDICTOR2 = 0, 1, 2, 3
+FG_TIME_PREDICTOR2_BDF, FG_TIME_PREDICTOR2_TRBDF2 = 4, 5
 FG_NS_SUPG_PSPG, FG_NS_VMS_DCDD = 0, 1
 FG_TRANSPORT_SUPG, FG_TRANSPORT_DD = 0, 1
 FG_EULER_SUPG, FG_EULER_DD = 0, 1

@@ -257,3 +257,33 @@ def test_euler_yzbeta_predictor(fg, form):
     assert st["steps"] == sto["steps"] == 3
     assert st["corrections"] == sto["corrections"]
     assert rel(ug, uo) < 1e-7
+
+
+@pytest.mark.parametrize("scheme,steady", [(4, 0), (4, 1), (5, 0)], ids=["bdf", "bdf-steady", "trbdf2"])
+def test_euler_predictor2_bdf_trbdf2(fg, scheme, steady):
+    """"Predictor2_BDF" (Predictor_New_BDF) and "Predictor2_TRBDF2"
+    (Predictor_New_TRBDF2 with the bubble build: uB from the initial
+    state's element centroids) on the device against the oracle."""
+    p = _p2_problem(17)
+    p.form = 1
+    o_scheme = {4: 4, 5: 2}[scheme]
+    to_o = O.TimeOpts(0, 2, 1e-3, steady, 3 * p.dt + 1e-12, 1e-6, 0, o_scheme)
+    uo, ao, uBo, aBo, sto = O.euler_predictor2(p, to_o, tol=1e-10, kmax=25)
+    s = fg.euler_system(p)
+    to = fg.time_opts(0, 2, 1e-3, steady, 3 * p.dt + 1e-12, 1e-6, scheme=scheme)
+    ug, ag, st = s.euler_predictor(p, to, kmax=25, tol=1e-10)
+    uB, aB = s.bubble_state()
+    assert st["steps"] == sto["steps"] and st["t"] == sto["t"]
+    assert st["corrections"] == sto["corrections"]
+    assert rel(ug, uo) < 1e-7 and rel(uB, uBo) < 1e-7
+
+
+def test_euler_dd_trbdf2_is_predictor2(fg):
+    """The Predictor1 DD build with TR-BDF2 is refused (the reference pairs
+    it with Predictor_Old_TRBDF2, which is not restated)."""
+    p = G.obliquo_problem(9)
+    p.form = fg.FG_EULER_DD
+    s = fg.euler_system(p)
+    with pytest.raises(fg.FemGpuError) as e:
+        s.euler_predictor(p, fg.time_opts(0, 1, 1e-3, 0, p.dt, 1e-6, max_steps=1, scheme=fg.FG_TIME_TRBDF2))
+    assert e.value.code == fg.FG_ERR_UNSUPPORTED

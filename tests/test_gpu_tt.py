@@ -199,3 +199,9 @@ def test_tt_predictor2_needs_dd(fg):
     with pytest.raises(fg.FemGpuError) as e:
         s.tt_predictor(p, 0.5, 0.02, to)
     assert e.value.code == fg.FG_ERR_UNSUPPORTED
+    p.form = fg.FG_TRANSPORT_DD                     # _BDF / _TRBDF2: Euler driver only
+    for scheme in (fg.FG_TIME_PREDICTOR2_BDF, fg.FG_TIME_PREDICTOR2_TRBDF2):
+        to.scheme = scheme
+        with pytest.raises(fg.FemGpuError) as e:
+            s.tt_predictor(p, 0.5, 0.02, to)
+        assert e.value.code == fg.FG_ERR_UNSUPPORTED
