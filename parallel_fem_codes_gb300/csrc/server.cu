@@ -414,7 +414,12 @@ int fg_server_submit_euler(fg_server *sv, fg_system *s, const fg_euler_coeffs *c
         return FG_ERR_STATE;
     }
     if (s->device != sv->device) { set_error("fg_server_submit_euler: system on another device"); return FG_ERR_ARG; }
-    EulerRequest r{s, *c, *t, u, tag, sv->now(), request_bytes(s, sv->cfg.kmax, sv->cfg.mixed, true)};
+    size_t bytes = request_bytes(s, sv->cfg.kmax, sv->cfg.mixed, true);
+    // element state the loop allocates: the DD bubbles and delta, and the
+    // Predictor2 bubble planes
+    if (c->form == FG_EULER_DD && s->shock_state.bytes < 40 * (size_t)s->nel_pad) bytes += 40 * (size_t)s->nel_pad;
+    if (t->scheme >= FG_TIME_PREDICTOR2 && s->bubble_nb != 4) bytes += 8 * (size_t)kBubblePlanesEuler * s->nel_pad;
+    EulerRequest r{s, *c, *t, u, tag, sv->now(), bytes};
     {
         std::lock_guard<std::mutex> l(sv->mu);
         if (sv->error) { set_error(sv->error_text); return sv->error; }
