@@ -24,6 +24,7 @@ REF_EU_SO = os.path.join(HERE, "_ref", "libref_euler.so")
 DROPIN_SO = {"sst": os.path.join(HERE, "_ref", "libdropin_sst.so"),
              "ns": os.path.join(HERE, "_ref", "libdropin_ns.so"),
              "euler": os.path.join(HERE, "_ref", "libdropin_euler.so")}
+DROPIN_TT_SO = os.path.join(HERE, "_ref", "libdropin_tt.so")
 # The reference's source tree (used only to build the checker): the
 # PFC_REFERENCE_DIR environment variable, else `reference` beside this
 # repository.
@@ -47,11 +48,14 @@ def build(ref: bool | None = None, fast: bool = False) -> None:
         ref = os.path.isdir(REF_SRC)
     if ref:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
-        if os.path.isdir(os.path.join(REF_SRC, "02_Transport_Equation")):
+        tt = os.path.isdir(os.path.join(REF_SRC, "02_Transport_Equation"))
+        if tt:
             subprocess.run(["make", "-s", "-C", HERE, "ref_tt", f"REF={REF_SRC}"], check=True)
         lib_dir = os.path.join(os.path.dirname(HERE), "parallel_fem_codes_gb300", "_lib")
         if all(os.path.exists(os.path.join(lib_dir, f"libfemgpu_{k}.so")) for k in ("sst", "ns", "euler")):
             subprocess.run(["make", "-s", "-C", HERE, "dropin", f"REF={REF_SRC}"], check=True)
+        if tt and os.path.exists(os.path.join(lib_dir, "libfemgpu_tt.so")):
+            subprocess.run(["make", "-s", "-C", HERE, "dropin_tt", f"REF={REF_SRC}"], check=True)
 
 
 _lib = None
@@ -610,12 +614,30 @@ REF_TT_SO = os.path.join(HERE, "_ref", "libref_tt.so")
 _ref_tt = None
 
 
-def ref_tt():
+_dropin_tt = None
+
+
+def dropin_tt_available() -> bool:
+    return os.path.exists(DROPIN_TT_SO) and os.path.exists(REF_TT_SO)
+
+
+def ref_tt(dropin=False):
     """The reference's own transient-transport build (oracle/_ref, compiled
-    from a private copy of its sources by `make -C oracle ref_tt`), or None."""
-    global _ref_tt
+    from a private copy of its sources by `make -C oracle ref_tt`), or None;
+    dropin=True: the same driver files linked against the library's shim
+    (`make -C oracle dropin_tt`)."""
+    global _ref_tt, _dropin_tt
+    if dropin:
+        if _dropin_tt is None and os.path.exists(DROPIN_TT_SO):
+            _dropin_tt = _setup_tt(ctypes.CDLL(DROPIN_TT_SO))
+        return _dropin_tt
     if _ref_tt is None and os.path.exists(REF_TT_SO):
-        R = ctypes.CDLL(REF_TT_SO)
+        _ref_tt = _setup_tt(ctypes.CDLL(REF_TT_SO))
+    return _ref_tt
+
+
+def _setup_tt(R):
+    if True:
         R.fr_tt_set_form.argtypes = [_c_int, _c_int, _c_int]
         R.fr_tt_set_form.restype = None
         R.fr_tt_build.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _c_dbl, _c_dbl,
@@ -627,8 +649,10 @@ def ref_tt():
         R.fr_tt_predictor2.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _c_dbl, _c_dbl,
                                        _c_dbl, _c_dbl, _c_dbl, _c_int, _c_dbl, _c_dbl, _c_dbl, _i32p, _i32p,
                                        _f64p, _f64p, _c_int, _c_int, _c_dbl, _f64p]
-        _ref_tt = R
-    return _ref_tt
+        R.fr_tt_predictor1.argtypes = R.fr_tt_predictor2.argtypes
+        R.fr_tt_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
+        R.fr_tt_layout.restype = None
+    return R
 
 
 def ref_tt_build(prob, alpha, dt, u=None, du=None, builds=1):
@@ -669,11 +693,33 @@ def ref_tt_mfdd_build(prob, alpha, dt, u, du, uB, duB, Da):
     return A.reshape(m.nel, 9), F, cond.reshape(m.nel, 5), DaB
 
 
-def ref_tt_predictor2(prob, alpha, dt, topts: TimeOpts, tol=1e-10, kmax=30, lmax=1000, u0=None):
+def ref_tt_predictor1(prob, alpha, dt, topts: TimeOpts, tol=1e-10, kmax=30, lmax=1000, u0=None, dropin=False):
+    """The reference's Predictor_Old with Build_M_K_R_SUPG / Build_M_K_R_DD
+    (by prob.form), Diag and pgmres; returns (u[neq], GMRES iterations)."""
+    m = prob.mesh
+    R = ref_tt(dropin)
+    cau = int(prob.cau)
+    R.fr_tt_set_form(int(getattr(prob, "form", 0)), cau if cau in (2, 3) else 1, int(getattr(prob, "h_shock", 0)))
+    perm, inv, _ = permutation_of_lm(m)
+    init = np.zeros(m.neq + 1) if u0 is None else np.append(np.asarray(u0, dtype=np.float64), 0.0)
+    u = np.zeros(m.neq + 1)
+    its = R.fr_tt_predictor1(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f, prob.upmode,
+                             prob.upval, float(alpha), float(dt), perm, inv, init, topts.as_array(), int(kmax),
+                             int(lmax), float(tol), u)
+    return u[:m.neq].copy(), its
+
+
+def ref_tt_layout():
+    out = np.zeros(64, dtype=np.int64)
+    ref_tt().fr_tt_layout(out)
+    return out
+
+
+def ref_tt_predictor2(prob, alpha, dt, topts: TimeOpts, tol=1e-10, kmax=30, lmax=1000, u0=None, dropin=False):
     """The reference's Predictor_New with Build_M_F_DD, Diag and pgmres;
     returns (u[neq], GMRES iterations)."""
     m = prob.mesh
-    R = ref_tt()
+    R = ref_tt(dropin)
     _ref_tt_form(R, prob)
     perm, inv, _ = permutation_of_lm(m)
     init = np.zeros(m.neq + 1) if u0 is None else np.append(np.asarray(u0, dtype=np.float64), 0.0)

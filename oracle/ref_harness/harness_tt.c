@@ -334,3 +334,83 @@ int fr_tt_predictor2(int nnodes, int nel, const double *x, const double *y, cons
     fr_tt_free(&c);
     return its;
 }
+
+/* Predictor_Old (TimeIntegration "Predictor1") with the form's build
+ * (Build_M_K_R_SUPG or Build_M_K_R_DD, setStabilizationForm.c:8-45), Diag
+ * and pgmres; arguments as fr_tt_predictor2. */
+int Predictor_Old(ParametersType *, MatrixDataType *, FemStructsType *, FemFunctionsType *, FemOtherFunctionsType *);
+int fr_tt_predictor1(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                     const int *ien, int neq, double k, double gamma, double bx, double by, double f, int upmode,
+                     double upval, double alpha, double dt, const int *Perm, const int *invPerm,
+                     const double *init, const double *topt, int kmax, int lmax, double tol, double *u_out)
+{
+    fr_tt c;
+    fr_tt_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, k, gamma, bx, by, f, upmode, upval, alpha, dt);
+    strcpy(c.P.TimeIntegration, "Predictor1");
+    strcpy(c.P.StabilizationForm, g_form == 1 ? "DD" : "SUPG");
+    c.O.Build = g_form == 1 ? Build_M_K_R_DD : Build_M_K_R_SUPG;
+    if (g_form != 1) c.F.ShockCapture = g_shock == 3 ? YZBeta_ShockCapture : CAU_ShockCapture;
+    c.M.Perm = (int *)Perm;
+    c.M.invPerm = (int *)invPerm;
+    g_init = init;
+    strcpy(c.P.StopMulticorrection, topt[0] != 0.0 ? "NORM" : "ITERATION");
+    c.P.NonLinearMaxIter = (int)topt[1];
+    c.P.NonLinearTolerance = topt[2];
+    strcpy(c.P.StopAtSteadyState, topt[3] != 0.0 ? "YES" : "NO");
+    c.P.FinalTime = topt[4];
+    c.P.TimeIntegrationTolerance = topt[5];
+    c.P.KrylovBasisVectorsQuantity = kmax;
+    c.P.LinearMaxIter = lmax;
+    c.P.SolverTolerance = tol;
+    c.P.iterations = 0;
+    setStopCriteria(&c.P, &c.F);
+    Predictor_Old(&c.P, &c.M, &c.S, &c.F, &c.O);
+    memcpy(u_out, c.S.u, sizeof(double) * (size_t)neq);
+    int its = c.P.iterations;
+    fr_tt_free(&c);
+    return its;
+}
+
+/* Field offsets of the reference's transient-transport structs, the same
+ * list the drop-in shim reports (layout pin). */
+#include <stddef.h>
+void fr_tt_layout(long *out)
+{
+    out[0] = (long)sizeof(ParametersType);
+    out[1] = (long)offsetof(ParametersType, SolverTolerance);
+    out[2] = (long)offsetof(ParametersType, KrylovBasisVectorsQuantity);
+    out[3] = (long)offsetof(ParametersType, nnodes);
+    out[4] = (long)offsetof(ParametersType, nel);
+    out[5] = (long)offsetof(ParametersType, neq);
+    out[6] = (long)offsetof(ParametersType, neq_bef);
+    out[7] = (long)offsetof(ParametersType, NEQ);
+    out[8] = (long)offsetof(ParametersType, LinearMaxIter);
+    out[9] = (long)offsetof(ParametersType, iterations);
+    out[10] = (long)offsetof(ParametersType, RANK);
+    out[11] = (long)offsetof(ParametersType, NPROC);
+    out[12] = (long)sizeof(MatrixDataType);
+    out[13] = (long)offsetof(MatrixDataType, A);
+    out[14] = (long)offsetof(MatrixDataType, Aaux);
+    out[15] = (long)offsetof(MatrixDataType, Diag);
+    out[16] = (long)offsetof(MatrixDataType, invDiag);
+    out[17] = (long)offsetof(MatrixDataType, Perm);
+    out[18] = (long)offsetof(MatrixDataType, invPerm);
+    out[19] = (long)sizeof(FemStructsType);
+    out[20] = (long)offsetof(FemStructsType, lm);
+    out[21] = (long)offsetof(FemStructsType, lmaux);
+    out[22] = (long)offsetof(FemStructsType, Node);
+    out[23] = (long)offsetof(FemStructsType, Element);
+    out[24] = (long)sizeof(FemFunctionsType);
+    out[25] = (long)offsetof(FemFunctionsType, mv);
+    out[26] = (long)offsetof(FemFunctionsType, precond);
+    out[27] = (long)offsetof(FemFunctionsType, precondR);
+    out[28] = (long)offsetof(FemFunctionsType, precond_setup);
+    out[29] = (long)sizeof(NodeType);
+    out[30] = (long)sizeof(ElementType);
+    out[31] = (long)offsetof(MatrixDataType, AA);
+    out[32] = (long)offsetof(MatrixDataType, JA);
+    out[33] = (long)offsetof(MatrixDataType, IA);
+    out[34] = (long)offsetof(ParametersType, MatrixVectorProductScheme);
+    out[35] = (long)offsetof(ParametersType, Preconditioner);
+    out[36] = (long)offsetof(ParametersType, nnzero);
+}

@@ -16,7 +16,8 @@ LIB = os.path.join(OUT, "libfemgpu.so")
 COMPAT_SST = os.path.join(OUT, "libfemgpu_sst.so")
 COMPAT_NS = os.path.join(OUT, "libfemgpu_ns.so")
 COMPAT_EULER = os.path.join(OUT, "libfemgpu_euler.so")
-COMPAT = [COMPAT_SST, COMPAT_NS, COMPAT_EULER]
+COMPAT_TT = os.path.join(OUT, "libfemgpu_tt.so")
+COMPAT = [COMPAT_SST, COMPAT_NS, COMPAT_EULER, COMPAT_TT]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # (source, extra flags); setup.cu is rounded exactly as written (no FMA
@@ -68,10 +69,11 @@ def build(force: bool = False) -> str:
         objs = list(ex.map(lambda u: _compile(*u), UNITS))
     subprocess.run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"], check=True)
     # drop-in shims with the reference's entry-point names: steady transport,
-    # steady Navier-Stokes and Euler drivers (one per struct layout)
+    # steady Navier-Stokes, Euler and transient transport drivers (one per
+    # struct layout)
     cc = os.environ.get("CC", "gcc")
     shims = [(COMPAT_SST, "compat_sst.c", []), (COMPAT_NS, "compat_block.c", ["-DFGC_NS"]),
-             (COMPAT_EULER, "compat_block.c", ["-DFGC_EULER"])]
+             (COMPAT_EULER, "compat_block.c", ["-DFGC_EULER"]), (COMPAT_TT, "compat_sst.c", ["-DFGC_TT"])]
     for out, src, defs in shims:
         subprocess.run([cc, "-O2", "-fPIC", "-shared", "-std=gnu99", "-Wall", *defs, "-o", out,
                         os.path.join(PKG, "compat", src), "-L" + OUT, "-lfemgpu", "-Wl,-rpath,$ORIGIN"],

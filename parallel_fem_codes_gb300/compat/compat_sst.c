@@ -21,6 +21,11 @@
  * driver's Node/Element arrays and cached in a small table keyed by the
  * MatrixDataType pointer (the reference's structs have no room for it).
  *
+ * Built with -DFGC_TT the same shim serves the transient-transport driver
+ * (02_Transport_Equation: its structs, femgpu_ref_tt.h; its solve path is
+ * pgmres, ebemv, Diag and NO; that driver never sets precondR, which the
+ * reference's pgmres calls, and the shim reads a NULL precondR as none).
+ *
  * Errors: the reference prints and stops (mycalloc.c:10-13,
  * setPreconditioner.c:66-69).  The shim prints the library's message and
  * calls exit(1) the same way, unless FEMGPU_COMPAT_NO_EXIT is set in the
@@ -30,7 +35,13 @@
 #include <stdlib.h>
 #include <string.h>
 
+#ifdef FGC_TT
+#include "femgpu_ref_tt.h"
+#define FGC_LAYOUT fgc_tt_layout
+#else
 #include "femgpu_ref_sst.h"
+#define FGC_LAYOUT fgc_sst_layout
+#endif
 #include "../../include/femgpu.h"
 
 #define FGC_MAX_SYSTEMS 64
@@ -338,7 +349,7 @@ int pgmres(ParametersType *P, MatrixDataType *M, FemStructsType *S, FemFunctions
 /* Field offsets of the restated structs (layout pin, compared with the
  * reference's own header by the tests). */
 #include <stddef.h>
-void fgc_sst_layout(long *out)
+void FGC_LAYOUT(long *out)
 {
     out[0] = (long)sizeof(ParametersType);
     out[1] = (long)offsetof(ParametersType, SolverTolerance);

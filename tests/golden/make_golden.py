@@ -303,6 +303,21 @@ def write_euler_predictor2():
     np.savez_compressed(os.path.join(HERE, "euler_predictor2_ref.npz"), **out)
 
 
+def write_tt_predictor1():
+    """The transient transport driver's own Predictor_Old loop (Diag,
+    pgmres) with Build_M_K_R_SUPG (CAU) and Build_M_K_R_DD (CAUDD),
+    4 steps of 2 corrections (oracle/_ref/libref_tt.so)."""
+    out = {}
+    for form, cau in ((0, 1), (1, 2)):
+        p = G.transport_problem(17, angle_deg=30.0, k=1e-3, f=0.0, cau=cau)
+        p.form = form
+        to = O.TimeOpts(0, 2, 1e-3, 0, 4 * 0.02 + 1e-12, 1e-6, 0, 0)
+        U, its = O.ref_tt_predictor1(p, 0.5, 0.02, to)
+        out[f"p1_{form}_U"], out[f"p1_{form}_its"] = U, np.array([its])
+        print("tt predictor1 form", form, "gmres", its)
+    np.savez_compressed(os.path.join(HERE, "tt_predictor1_ref.npz"), **out)
+
+
 TT_P2_CASES = [(2, 0), (3, 2)]   # (shock, h_shock) of the DD form
 
 
@@ -370,6 +385,7 @@ if __name__ == "__main__":
     write_ilup()
     write_euler_dd()
     write_tt()
+    write_tt_predictor1()
     write_tt_predictor2()
     write_euler_predictor2()
     write_euler_yzbeta()

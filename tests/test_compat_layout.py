@@ -58,3 +58,26 @@ def test_block_shim_layout_matches_reference_header(kind):
     ours = np.zeros(64, dtype=np.int64)
     getattr(refapi.block_shim(kind), refapi._KINDS[kind]["layout"])(ours)
     assert np.array_equal(ours[:31], theirs[:31])
+
+
+def _tt_shim():
+    from parallel_fem_codes_gb300 import build as _b
+    _b.build()
+    L = ctypes.CDLL(_b.COMPAT_TT)
+    L.fgc_tt_layout.argtypes = [np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
+    L.fgc_tt_layout.restype = None
+    return L
+
+
+def test_tt_shim_exports_reference_names():
+    """The transient-transport driver's solve path (pgmres, ebemv, Diag, NO)."""
+    L = _tt_shim()
+    for name in ("pgmres", "ebemv", "Diag_precond", "Diag_precond_EBE_setup", "NO_precond", "NO_precond_setup"):
+        assert hasattr(L, name), name
+
+
+@pytest.mark.skipif(O.ref_tt() is None, reason="reference transient build (oracle/_ref) not present")
+def test_tt_shim_layout_matches_reference_header():
+    ours = np.zeros(64, dtype=np.int64)
+    _tt_shim().fgc_tt_layout(ours)
+    assert np.array_equal(ours[:37], O.ref_tt_layout()[:37])

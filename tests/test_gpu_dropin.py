@@ -10,7 +10,10 @@ linked with the reference's CPU solve path (oracle/Makefile `ref`):
 * Predictor_Old.c (00_CommonFiles/Time_Integration/Predictor_Old.c:6-134:
   Euler OBLIQUO 17 x 17, 4 steps, 2 corrections, BlockDiag + pgmres);
 * Predictor_New.c with Build_M_F_DD_Transiente.c ("Predictor2", DD,
-  YZBeta: the bubble unknowns, calculate_DaB), 3 steps.
+  YZBeta: the bubble unknowns, calculate_DaB), 3 steps;
+* the transient transport driver (02_Transport_Equation: Predictor_Old.c
+  with Build_M_K_R_SUPG / _DD, Predictor_New.c with Build_M_F_DD) against
+  libfemgpu_tt.so, 4 steps.
 
 Solutions within rel-L2 1e-9, GMRES iterations (Parameters->iterations)
 within +-2 per linear solve.  Skipped where the drop-in builds are absent
@@ -73,3 +76,20 @@ def test_euler_predictor2_dropin():
     u1, it1, _ = O.ref_euler_predictor(p, to, tol=1e-10, kmax=25, dropin=True)
     assert rel(u1, u0) <= 1e-9
     assert abs(it1 - it0) <= 2 * 6
+
+
+@pytest.mark.skipif(not O.dropin_tt_available(), reason="transient-transport drop-in build absent")
+@pytest.mark.parametrize("form,cau,scheme", [(0, 1, 0), (1, 2, 0), (1, 2, 3)],
+                         ids=["predictor1-supg", "predictor1-dd", "predictor2-dd"])
+def test_transient_transport_dropin(form, cau, scheme):
+    """The transient driver's Predictor_Old / Predictor_New with its builds,
+    linked unchanged against libfemgpu_tt.so, against the same files linked
+    with the reference's CPU solve path."""
+    p = G.transport_problem(17, angle_deg=30.0, k=1e-3, f=0.0, cau=cau)
+    p.form = form
+    to = O.TimeOpts(0, 2, 1e-3, 0, 4 * 0.02 + 1e-12, 1e-6, 0, 0)
+    run = O.ref_tt_predictor2 if scheme == 3 else O.ref_tt_predictor1
+    u0, it0 = run(p, 0.5, 0.02, to)
+    u1, it1 = run(p, 0.5, 0.02, to, dropin=True)
+    assert rel(u1, u0) <= 1e-9
+    assert abs(it1 - it0) <= 2 * 8

@@ -255,3 +255,18 @@ def test_predictor2_reaches_the_steady_dd_solution():
     u, a, uB, aB, st = O.tt_predictor2(p, 0.5, 0.5, O.TimeOpts(1, 5, 1e-8, 1, 1e4, 1e-9, 0, 0), tol=1e-12)
     Us, nl, its = O.transport_process(p, 1e-12, 1e-8, 30, 1000)
     assert np.linalg.norm(u - Us[: p.mesh.neq]) <= 1e-4 * np.linalg.norm(Us[: p.mesh.neq])
+
+
+@pytest.mark.parametrize("form,cau", [(0, 1), (1, 2)], ids=["supg-cau", "dd-caudd"])
+def test_predictor1_loop_matches_reference_golden(form, cau):
+    """The Predictor_Old loop of the transient driver (Diag, GMRES) with the
+    SUPG and DD builds: final state and GMRES iterations equal the
+    reference's own loop (tests/golden/tt_predictor1_ref.npz)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "tt_predictor1_ref.npz"))
+    p = G.transport_problem(17, angle_deg=30.0, k=1e-3, f=0.0, cau=cau)
+    p.form = form
+    to = O.TimeOpts(0, 2, 1e-3, 0, 4 * 0.02 + 1e-12, 1e-6, 0, 0)
+    u, a, st = O.tt_predictor(p, 0.5, 0.02, to)
+    assert st["gmres_iterations"] == int(g[f"p1_{form}_its"][0])
+    assert np.array_equal(u, g[f"p1_{form}_U"])
