@@ -52,3 +52,24 @@ def test_reference_drivers_link_against_the_shims(femgpu):
             assert sym in shim_defs, (kind, sym)                      # provided by the shim
         # the drivers themselves are the reference's
         assert ("Process" if kind != "euler" else "Predictor_Old") in defined
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(O.REF_SRC, "02_Transport_Equation")),
+                    reason="reference sources absent")
+@pytest.mark.skipif(shutil.which("nm") is None, reason="nm absent")
+def test_transient_driver_links_against_its_shim(femgpu):
+    """The transient-transport driver (Predictor_Old.c, Predictor_New.c, its
+    Build functions, from a private copy whose header points at the MPI
+    stand-in) links against libfemgpu_tt.so in place of its solve path."""
+    subprocess.run(["make", "-s", "-C", os.path.dirname(O.__file__), "dropin_tt", f"REF={O.REF_SRC}"], check=True)
+    lib_dir = os.path.dirname(femgpu.library_path())
+    so = O.DROPIN_TT_SO
+    needed = subprocess.run(["readelf", "-d", so], check=True, capture_output=True, text=True).stdout
+    assert "libfemgpu_tt.so" in needed
+    undef, defined = _symbols(so, True), _symbols(so, False)
+    shim_defs = _symbols(os.path.join(lib_dir, "libfemgpu_tt.so"), False)
+    for sym in ("pgmres", "ebemv", "Diag_precond", "Diag_precond_EBE_setup", "NO_precond"):
+        assert sym in undef and sym not in defined, sym
+        assert sym in shim_defs, sym
+    for sym in ("Predictor_Old", "Predictor_New", "Build_M_F_DD", "Build_M_K_R_SUPG", "calculate_DaB"):
+        assert sym in defined, sym
