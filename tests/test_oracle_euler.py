@@ -306,3 +306,30 @@ def test_yzbeta_against_reference_build(form, dimless):
     A0, R0 = O.ref_euler_build(p, u, du)
     A1, R1 = O.build_euler(p, u, du)
     assert np.array_equal(A0, A1) and np.array_equal(R0, R1)
+
+
+@pytest.mark.skipif(O.ref_euler() is None, reason="reference build (oracle/_ref) not present")
+@pytest.mark.parametrize("scheme", [3, 4, 2], ids=["predictor2", "predictor2_bdf", "predictor2_trbdf2"])
+@pytest.mark.parametrize("dimless,stop_norm", [(True, 1), (False, 0)])
+def test_predictor2_schemes_against_reference_build(scheme, dimless, stop_norm):
+    """Every Predictor2 loop in both Jacobian forms and both correction stop
+    tests: bit-identical with the reference's Predictor_New* loops."""
+    p = G.obliquo_problem(9, dimensionless=dimless)
+    p.form, p.invY = 2, np.array([0.9, 0.6, 1.7, 0.4])
+    to = O.TimeOpts(stop_norm, 3, 1e-4, 0, 3 * p.dt + 1e-12, 1e-6, 0, scheme)
+    U0, its0, _ = O.ref_euler_predictor(p, to, 1e-10, 25, 1000)
+    U1, a1, uB1, aB1, st = O.euler_predictor2(p, to, 1e-10, 25, 1000)
+    assert st["gmres_iterations"] == its0 and np.array_equal(U0, U1)
+
+
+@pytest.mark.skipif(O.ref_euler() is None, reason="reference build (oracle/_ref) not present")
+@pytest.mark.parametrize("form", [0, 1], ids=["supg", "dd"])
+def test_yzbeta_steady_stop_against_reference_build(form):
+    """YZBeta with the steady-state time stop (Predictor_Old)."""
+    p = G.obliquo_problem(9)
+    p.form, p.shock, p.invY = form, 3, np.array([1.0, 0.5, 2.0, 0.25])
+    to = O.TimeOpts(1, 4, 1e-3, 1, 20 * p.dt, 1e-3, 0, 0)
+    U0, its0, t0 = O.ref_euler_predictor(p, to, 1e-10, 25, 1000)
+    U1, a1, st = O.euler_predictor(p, to, 1e-10, 25, 1000)
+    assert np.all(np.isfinite(U0))
+    assert st["gmres_iterations"] == its0 and st["t"] == t0 and np.array_equal(U0, U1)

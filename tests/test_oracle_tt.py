@@ -270,3 +270,30 @@ def test_predictor1_loop_matches_reference_golden(form, cau):
     u, a, st = O.tt_predictor(p, 0.5, 0.02, to)
     assert st["gmres_iterations"] == int(g[f"p1_{form}_its"][0])
     assert np.array_equal(u, g[f"p1_{form}_U"])
+
+
+@pytest.mark.skipif(O.ref_tt() is None, reason="reference transient build absent")
+@pytest.mark.parametrize("cau,hs,angle", [(2, 0, 10.0), (2, 2, 135.0), (3, 0, 250.0), (3, 1, 320.0)])
+def test_predictor2_option_matrix_against_reference(cau, hs, angle):
+    """Predictor2 over the DD shock captures and h_shock options at several
+    flow angles: the whole Predictor_New loop bit-identical with the
+    reference's (final state, GMRES iterations)."""
+    p = G.transport_problem(13, angle_deg=angle, k=1e-3, gamma=0.1, f=0.3, cau=cau)
+    p.form, p.h_shock = 1, hs
+    to = O.TimeOpts(1, 3, 1e-4, 0, 3 * 0.03 + 1e-12, 1e-6, 0, 0)
+    U0, its0 = O.ref_tt_predictor2(p, 0.5, 0.03, to, tol=1e-10)
+    U1, a1, uB1, aB1, st = O.tt_predictor2(p, 0.5, 0.03, to, tol=1e-10)
+    assert st["gmres_iterations"] == its0 and np.array_equal(U0, U1)
+
+
+@pytest.mark.skipif(O.ref_tt() is None, reason="reference transient build absent")
+@pytest.mark.parametrize("form,cau,hs", [(0, 1, 1), (0, 3, 2), (1, 3, 0)])
+def test_predictor1_option_matrix_against_reference(form, cau, hs):
+    """Predictor_Old over the SUPG / DD forms with CAU, YZBeta and CAUDD and
+    the h_shock options: bit-identical with the reference's loop."""
+    p = G.transport_problem(13, angle_deg=75.0, k=1e-3, gamma=0.1, f=0.3, cau=cau)
+    p.form, p.h_shock = form, hs
+    to = O.TimeOpts(1, 3, 1e-4, 0, 3 * 0.03 + 1e-12, 1e-6, 0, 0)
+    U0, its0 = O.ref_tt_predictor1(p, 0.5, 0.03, to, tol=1e-10)
+    U1, a1, st = O.tt_predictor(p, 0.5, 0.03, to, tol=1e-10)
+    assert st["gmres_iterations"] == its0 and np.array_equal(U0, U1)
