@@ -17,6 +17,8 @@ ORACLE_SO = os.path.join(HERE, "_build", "libfemoracle.so")
 # timed CPU baseline only (never a checker)
 ORACLE_FAST_SO = os.path.join(HERE, "_build", "libfemoracle_fast.so")
 REF_SO = os.path.join(HERE, "_ref", "libref_sst.so")
+# the same driver compiled with the reference's -Ofast -march=native: timing only
+REF_FAST_SO = os.path.join(HERE, "_ref", "libref_sst_fast.so")
 REF_NS_SO = os.path.join(HERE, "_ref", "libref_ns.so")
 REF_EU_SO = os.path.join(HERE, "_ref", "libref_euler.so")
 # the reference's drivers compiled unchanged but linked against the
@@ -168,10 +170,48 @@ def dropin_available() -> bool:
     return all(os.path.exists(p) for p in DROPIN_SO.values())
 
 
+_use_ref_fast = False
+
+
+def ref_sources():
+    """The reference's source tree, else the private copy `make refcopy`
+    keeps under _build, else None."""
+    for d in (REF_SRC, os.path.join(HERE, "_build", "refcopy")):
+        if os.path.isdir(os.path.join(d, "01_SS_Transport_Equation")):
+            return d
+    return None
+
+
+def build_ref_fast() -> bool:
+    """Compile the steady-transport driver with the reference's own
+    optimisation flags (`make ref_fast`) where its sources are at hand;
+    False where they are not or the build fails."""
+    src = ref_sources()
+    if src is None:
+        return False
+    r = subprocess.run(["make", "-s", "-C", HERE, "ref_fast", f"REF={src}"], capture_output=True)
+    return r.returncode == 0 and os.path.exists(REF_FAST_SO)
+
+
+def use_ref_fast() -> None:
+    """Make ref() load the -Ofast build (timed CPU arm only; call before the
+    first ref() call of the process)."""
+    global _use_ref_fast
+    if _ref is not None:
+        raise RuntimeError("reference build already loaded")
+    _use_ref_fast = True
+
+
+def using_ref_fast() -> bool:
+    return _use_ref_fast
+
+
 def ref(path=None):
     """The reference's own C (oracle/_ref), or None where it was not built;
     path: another build of the same harness (the drop-in build)."""
     global _ref
+    if _use_ref_fast and path is None:
+        path = REF_FAST_SO
     if path is not None:
         if path not in _loaded and os.path.exists(path):
             _loaded[path] = _setup_sst(ctypes.CDLL(path))
@@ -195,6 +235,10 @@ def _setup_sst(R):
         R.fr_ebemv.restype = None
         R.fr_diag_pgmres.argtypes = [_c_int, _c_int, _i32p, _f64p, _i32p, _i32p, _f64p, _f64p, _f64p, _f64p,
                                      _c_int, _c_int, _c_dbl]
+        if hasattr(R, "fr_sst_timed_solve"):
+            R.fr_sst_timed_solve.argtypes = [_c_int, _c_int, _f64p, _f64p, _i32p, _i32p, _i32p, _c_int, _c_dbl,
+                                             _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_int, _c_dbl, _c_int, _c_int, _c_dbl,
+                                             ctypes.POINTER(_c_dbl)]
         R.fr_ebe_prec_apply.argtypes = [_c_int, _c_int, _c_int, _i32p, _f64p, _f64p]
         R.fr_ebe_prec_apply.restype = None
         R.fr_ebe_prec_pgmres.argtypes = [_c_int, _c_int, _c_int, _i32p, _f64p, _i32p, _i32p, _f64p, _f64p,
@@ -988,6 +1032,20 @@ def ref_process(prob, solver_tol=1e-10, nonlinear_tol=1e-3, kmax=30, lmax=1000, 
     R.fr_sst_process(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f,
                          prob.upmode, prob.upval, solver_tol, nonlinear_tol, kmax, lmax, U, ctypes.byref(its))
     return U[:m.neq].copy(), its.value
+
+
+def ref_timed_solve(prob, kmax=30, lmax=1000, tol=1e-10):
+    """One iteration of the reference's Process (Build_K_F at u = 0,
+    scaling, Diag set-up, pgmres, unscaling), timed inside the reference
+    build after its untimed Preprocess work; returns (seconds, GMRES
+    iterations)."""
+    m = prob.mesh
+    sec = _c_dbl(0.0)
+    R = ref()
+    _ref_form(prob, R)
+    its = R.fr_sst_timed_solve(*_mesh_args(m), prob.k, prob.gamma, prob.beta[0], prob.beta[1], prob.f,
+                               prob.upmode, prob.upval, int(kmax), int(lmax), float(tol), ctypes.byref(sec))
+    return sec.value, its
 
 
 def ref_ebemv(lm, A, perm, inv, P):

@@ -420,3 +420,38 @@ int fr_sst_csr(int nnodes, int nel, const double *x, const double *y, const int 
     fr_free(&c);
     return nnz;
 }
+
+/* One linear solve of the driver as one iteration of Process.c:40-79 runs
+ * it -- Build_K_F at u = 0, scaling, the Diag set-up, pgmres, unscaling --
+ * timed alone (CLOCK_MONOTONIC): the connectivity and its local reordering
+ * (Preprocess) are made first, untimed, as the driver makes them before
+ * Process.  *seconds receives the time; returns the GMRES iterations.  The
+ * timed CPU baseline of bench.py calls this from the -Ofast build. */
+#include <time.h>
+int fr_sst_timed_solve(int nnodes, int nel, const double *x, const double *y, const int *type, const int *invp,
+                       const int *ien, int neq, double k, double gamma, double bx, double by, double f, int upmode,
+                       double upval, int kmax, int lmax, double tol, double *seconds)
+{
+    fr_sst c;
+    struct timespec t0, t1;
+    fr_problem(k, gamma, bx, by, f, upmode, upval, x, y, nnodes);
+    fr_setup(&c, nnodes, nel, x, y, type, invp, ien, neq, tol, 1e-3, kmax, lmax);
+    setProblem(&c.P, &c.F);
+    setMatrixVectorProductType(&c.P, &c.F);
+    setSolver(&c.P, &c.O);
+    setScaling(&c.P, &c.F);
+    setPreconditioner(&c.P, &c.F);
+    setStabilizationForm(&c.P, &c.F, &c.O);
+    c.P.iterations = 0;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    c.O.Build_K_F(&c.P, &c.M, &c.S, &c.F);
+    c.F.scaling(&c.P, &c.M, &c.S);
+    c.F.precond_setup(&c.P, &c.M, &c.S, 1, c.S.F);
+    c.O.solver(&c.P, &c.M, &c.S, &c.F, c.S.F, c.S.U);
+    c.F.unscaling(&c.P, &c.M, &c.S, c.S.u);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    *seconds = (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+    int its = c.P.iterations;
+    fr_free(&c);
+    return its;
+}
