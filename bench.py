@@ -67,8 +67,9 @@ MATVEC_TRAFFIC_RATIO = 481.61 / 418.19
 # (Build_K_F_SUPG + CAU, Diag_precond_EBE_setup, FP64 pgmres GMRES(30), tol
 # 1e-10) built with the reference's own compiler flags (-Ofast
 # -march=native), one instance per host core, every core busy: the
-# reference's own functions (oracle/Makefile `ref_fast`) where its sources
-# are at hand, else the oracle's restatement of them (`fast`).  The timed
+# reference's own functions where oracle.build() compiled them
+# (oracle/Makefile `ref_fast`, only where the reference's sources are),
+# else the oracle's restatement of them (`fast`).  The timed
 # region of a solve is what the reference's Process_Time covers for one
 # linear solve: assembly, preconditioner set-up and GMRES; the mesh and its
 # connectivity (Preprocess) are made before it, as the GPU arm's meshes are
@@ -82,15 +83,12 @@ CPU_KINDS = {
 
 
 def cpu_kind():
-    """("reference" | "port") for the timed CPU arm, building the
-    reference's -Ofast copy where its sources are at hand (call before the
+    """("reference" | "port") for the timed CPU arm: the reference's -Ofast
+    build where oracle.build() made it, else the restatement (call before the
     CPU pool starts)."""
     import oracle as O
     O.build(ref=False, fast=True)
-    try:
-        return "reference" if O.build_ref_fast() else "port"
-    except Exception:                   # no compiler or sources: the restatement
-        return "port"
+    return "reference" if O.ref_fast_available() else "port"
 
 
 def _cpu_init(kind="port"):

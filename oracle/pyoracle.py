@@ -49,7 +49,7 @@ def build(ref: bool | None = None, fast: bool = False) -> None:
     if ref is None:
         ref = os.path.isdir(REF_SRC)
     if ref:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "ref_fast", f"REF={REF_SRC}"], check=True)
         tt = os.path.isdir(os.path.join(REF_SRC, "02_Transport_Equation"))
         if tt:
             subprocess.run(["make", "-s", "-C", HERE, "ref_tt", f"REF={REF_SRC}"], check=True)
@@ -173,24 +173,10 @@ def dropin_available() -> bool:
 _use_ref_fast = False
 
 
-def ref_sources():
-    """The reference's source tree, else the private copy `make refcopy`
-    keeps under _build, else None."""
-    for d in (REF_SRC, os.path.join(HERE, "_build", "refcopy")):
-        if os.path.isdir(os.path.join(d, "01_SS_Transport_Equation")):
-            return d
-    return None
-
-
-def build_ref_fast() -> bool:
-    """Compile the steady-transport driver with the reference's own
-    optimisation flags (`make ref_fast`) where its sources are at hand;
-    False where they are not or the build fails."""
-    src = ref_sources()
-    if src is None:
-        return False
-    r = subprocess.run(["make", "-s", "-C", HERE, "ref_fast", f"REF={src}"], capture_output=True)
-    return r.returncode == 0 and os.path.exists(REF_FAST_SO)
+def ref_fast_available() -> bool:
+    """The -Ofast build of the reference's steady-transport driver
+    (`make ref_fast`, made by build() where the reference's sources are)."""
+    return os.path.exists(REF_FAST_SO)
 
 
 def use_ref_fast() -> None:
